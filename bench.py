@@ -1,0 +1,382 @@
+#!/usr/bin/env python3
+"""Benchmark: NEMO's per-timestep stencil hot path on the GYRE nn_GYRE=25 basin.
+
+Workload (one "step"): nemo_gpu_stp_hotpath = dyn_spg_ts (phase 1, 37 barotropic
+sub-steps in one persistent kernel, phase 3), tsa = 0 + FCT 2nd-order advection of
+T and S with on-the-fly transports, rotated iso-neutral laplacian diffusion, and
+the implicit vertical diffusion with the salinity clamp, on a 752 x 502 x 31 grid
+(11.7 M cells), ln_bench spacing (106 km), rdt = 7200 s. Inputs are the seeded
+synthetic GYRE state (analytic T/S + noise, double-gyre flow); they are resident
+in HBM and larger than L2 (no L2 flush is needed between steps).
+
+metric: cell-steps/s of the mixed-precision form (FP32 bulk, FP64 barotropic
+accumulators); the FP64 plain form is measured on the same inputs and reported
+beside it with the SST difference between the two.
+
+--impl reference times the reference's algorithm on the host cores: NEMO cannot
+be built here (no Fortran compiler), so that arm runs the oracle (the C FP64
+restatement of the reference routines) on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "nemo-fmi-devel_gb300"))
+
+METRIC = "cell-steps/s, mixed-precision vs FP64 GPU at ≤1e-3 K SST error; % HBM peak"
+UNIT = "cell-steps/s"
+# algorithmic bytes per 3-D cell of each routine (FP64, FP32-bulk): every 3-D field
+# the routine reads or writes counted once; the barotropic sub-steps count 25 2-D
+# values per 2-D cell per sub-step (accumulators FP64 in both forms)
+ALG_BYTES = {
+    "tra_adv": (88, 44),
+    "tra_ldf": (88, 44),
+    "tra_zdf": (64, 32),
+    "dyn_spg_ts_3d": (80, 40),
+    "dyn_spg_ts_substep_2d": (200, 140),
+}
+KERNELS_PER_STEP = 10  # spg: 4, fct: 3, iso: 2, zdf: 1
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def start(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+
+    def stop(self):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 5 + i and "Active" in s[5 + i]
+                          and "Not" not in s[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def build_case(nn, nmem, seed):
+    from nemo_gpu import gyre
+    dom = gyre.domain(nn)
+    nam = gyre.namelist()
+    states = [gyre.state(dom, nam, seed=seed, member=m) for m in range(nmem)]
+    return dom, nam, states
+
+
+HOT_3D = ("un", "vn", "wn", "ua", "va", "avt", "uslp", "vslp", "wslpi", "wslpj")
+HOT_2D = ("sshn", "un_b", "vn_b", "ub_b", "vb_b", "utau", "vtau", "emp")
+ACC_2D = ("SSHA", "UA_B", "VA_B", "UN_ADV", "VN_ADV", "UB2_B", "VB2_B", "UN_BF", "VN_BF")
+
+
+def make_ctx(dom, nam, states, prec, stream):
+    """A context with every hot-path field bound to device tensors holding the state."""
+    import numpy as np
+    import torch
+    from nemo_gpu import api
+    ctx = api.Context(dom, nam, nmembers=len(states), prec=prec, stream=stream)
+    dev = {}
+
+    def put(name, arrays, fp64=False):
+        t = ctx.to_device(arrays, dtype=torch.float64 if fp64 else None)
+        dev[name] = t
+        ctx.bind(name, t)
+
+    put("TSB", [s["tsb"] for s in states])
+    put("TSN", [s["tsn"] for s in states])
+    put("TSA", [np.zeros_like(s["tsb"]) for s in states])
+    for n in HOT_3D:
+        put(n.upper(), [s[n] for s in states])
+    for n in ("ub", "vb", "sshb"):
+        put(n.upper(), [s[n] for s in states])
+    for n in HOT_2D:
+        put(n.upper(), [s[n] for s in states])
+    put("RCDU_BOT", [s["rcdu_bot"] for s in states])
+    z3 = [np.zeros_like(s["avt"]) for s in states]
+    put("AH_WSLP2", z3)
+    put("AKZ", z3)
+    z2 = [np.zeros_like(s["sshn"]) for s in states]
+    for n in ACC_2D:
+        put(n, z2, fp64=True)
+    return ctx, dev
+
+
+def time_steps(ctx, stream, steps, kt0, dev_index):
+    import torch
+    from nemo_gpu import dist
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist.barrier(dev_index)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for s in range(steps):
+            ctx.stp_hotpath(kt0 + s)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    dist.barrier(dev_index)
+    ctx.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+    from nemo_gpu import dist
+    rank, world = dist.init("nccl")
+    _, _, local = dist.env_rank()
+    torch.cuda.set_device(local)
+    dom, nam, states = build_case(args.nn, args.members, seed=100 + rank)
+    jpi, jpj, jpk = dom["jpi"], dom["jpj"], dom["jpk"]
+    cells = jpi * jpj * jpk * args.members
+    stream = torch.cuda.Stream()
+    out = {}
+    # ---------------------------------------------------------------- mixed (headline)
+    ctx, dev = make_ctx(dom, nam, states, args.prec, stream)
+    icycle, nn_baro, _ = ctx.spg_info()
+    kt0 = 5
+    for w in range(args.warmup):
+        ctx.stp_hotpath(kt0 + w)
+    ctx.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms = time_steps(ctx, stream, args.steps, kt0 + args.warmup, local)
+    ck = clocks.stop()
+    ms_max = dist.max_over_ranks(ms, device=f"cuda:{local}")
+    ms_step = ms_max / args.steps
+    value = cells * world * args.steps / (ms_max / 1e3)
+    # per-routine timing (the library's ln_timing) for the roofline
+    ctx.set_timing(True)
+    for s in range(max(3, min(args.steps, 10))):
+        ctx.stp_hotpath(kt0 + 1000 + s)
+    ctx.synchronize()
+    rt, ncalls = ctx.get_timing()
+    ctx.set_timing(False)
+    rt = {k: v / max(ncalls, 1) for k, v in rt.items()}
+    sst_mixed = ctx.to_host(dev["TSA"], (jpi, jpj, jpk, 2))
+    # ---------------------------------------------------------------- FP64 arm
+    fp64 = None
+    if not args.no_fp64 and args.prec == "mixed":
+        ctx64, dev64 = make_ctx(dom, nam, states, "fp64", stream)
+        for w in range(2):
+            ctx64.stp_hotpath(kt0 + w)
+        ctx64.synchronize()
+        k64 = max(2, args.steps // 4)
+        ms64 = dist.max_over_ranks(time_steps(ctx64, stream, k64, kt0 + 2, local), device=f"cuda:{local}")
+        ctx64.set_timing(True)
+        for s in range(3):
+            ctx64.stp_hotpath(kt0 + 1000 + s)
+        ctx64.synchronize()
+        rt64, n64 = ctx64.get_timing()
+        ctx64.set_timing(False)
+        # the same step on the same inputs in both forms: SST (T at level 1) difference
+        for c_, d_ in ((ctx, dev), (ctx64, dev64)):
+            for n in ("UA", "VA", "UN", "VN"):
+                d_[n].copy_(c_.to_device([s[n.lower()] for s in states]))
+            for n in ACC_2D:
+                d_[n].zero_()
+            c_.stp_hotpath(kt0 + 5000)
+            c_.synchronize()
+        a32 = ctx.to_host(dev["TSA"], (jpi, jpj, jpk, 2))
+        a64 = ctx64.to_host(dev64["TSA"], (jpi, jpj, jpk, 2))
+        if isinstance(a32, list):
+            a32, a64 = a32[0], a64[0]
+        tm = dom["k_bot"] > 0
+        sst_err = float(np.abs(a32[:, :, 0, 0] - a64[:, :, 0, 0])[tm].max())
+        sss_err = float(np.abs(a32[:, :, 0, 1] - a64[:, :, 0, 1])[tm].max())
+        fp64 = {"value": cells * world * k64 / (ms64 / 1e3), "ms_per_step": ms64 / k64,
+                "routine_ms": {k: v / max(n64, 1) for k, v in rt64.items()},
+                "sst_abs_err_1step_K": sst_err, "sss_abs_err_1step_psu": sss_err}
+        ctx64.close()
+        del dev64
+    # ---------------------------------------------------------------- e2e (host buffers, C ABI)
+    e2e = None
+    if not args.no_e2e:
+        ins = ["TSB", "TSN"] + [n.upper() for n in HOT_3D] + [n.upper() for n in HOT_2D] + ["RCDU_BOT"]
+        outs = ["TSA", "UA", "VA", "UN", "VN", "AH_WSLP2"] + list(ACC_2D)
+        host = {}
+        for n in set(ins + outs):
+            host[n] = torch.empty(dev[n].numel(), dtype=dev[n].dtype, pin_memory=True)
+            host[n].copy_(dev[n].cpu())
+        bi = sum(host[n].numel() * host[n].element_size() for n in ins)
+        bo = sum(host[n].numel() * host[n].element_size() for n in outs)
+        ke = max(2, args.steps // 2)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for s in range(ke):
+                for n in ins:
+                    ctx.upload(n, host[n])
+                ctx.stp_hotpath(kt0 + 9000 + s)
+                for n in outs:
+                    ctx.download(n, host[n])
+            e1.record(stream)
+        ctx.synchronize()
+        wall = time.perf_counter() - t0
+        ems = dist.max_over_ranks(e0.elapsed_time(e1), device=f"cuda:{local}")
+        e2e = {"value": cells * world * ke / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": bi,
+               "d2h_bytes_per_step": bo, "ms_per_step": ems / ke, "wall_ms_per_step": 1e3 * wall / ke,
+               "host_buffers": "pinned; nemo_gpu_field_upload/download through the C ABI"}
+    # ---------------------------------------------------------------- roofline
+    hbm, src = peaks()
+    b = 1 if args.prec == "mixed" else 0
+    per_cell = {"tra_adv": ALG_BYTES["tra_adv"][b], "tra_ldf": ALG_BYTES["tra_ldf"][b],
+                "tra_zdf": ALG_BYTES["tra_zdf"][b],
+                "dyn_spg_ts": ALG_BYTES["dyn_spg_ts_3d"][b]
+                + ALG_BYTES["dyn_spg_ts_substep_2d"][b] * icycle / jpk}
+    routine = max(rt, key=rt.get)
+    alg_bytes = per_cell[routine] * cells
+    achieved = alg_bytes / (rt[routine] / 1e3) / 1e9
+    routines = {k: {"ms": rt[k], "alg_GBps": per_cell[k] * cells / (rt[k] / 1e3) / 1e9,
+                    "frac": per_cell[k] * cells / (rt[k] / 1e3) / 1e9 / hbm} for k in rt}
+    step_bytes = sum(per_cell[k] for k in per_cell) * cells
+    res = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 bulk + f64 accumulators" if args.prec == "mixed" else "f64",
+        "data": "synthetic: seeded GYRE analytic state (no reference data files exist)",
+        "config": {"workload": f"GYRE nn_GYRE={args.nn} hot path step (dyn_spg_ts + FCT + iso ldf + zdf)",
+                   "grid": [jpi, jpj, jpk], "members": args.members, "cells": cells, "icycle": icycle,
+                   "nn_baro": nn_baro, "rdt": nam["rn_rdt"], "ln_bench": True,
+                   "l2": "inputs larger than L2 (%.2f GB resident), no flush" % (
+                       sum(t.numel() * t.element_size() for t in dev.values()) / 1e9),
+                   "parallelism": f"replicas x{world}"},
+        "clocks": ck, "gpu_launches": KERNELS_PER_STEP * args.steps,
+        "roofline": {"bound": "hbm", "kernel": routine, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "peak_source": src,
+                     "alg_bytes_per_launch": alg_bytes},
+        "routines": routines,
+        "step_alg_GBps": step_bytes / (ms_step / 1e3) / 1e9,
+        "e2e": e2e, "fp64": fp64,
+    }
+    if fp64:
+        res["speedup_vs_fp64"] = value / fp64["value"]
+    if rank == 0 and world == 1 and not args.no_cpu:
+        res["cpu_baseline"] = cpu_baseline(dom, nam, states[0], budget_s=args.cpu_budget)
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(res))
+
+
+def cpu_baseline(dom, nam, st, budget_s=20.0, threads=None):
+    """The oracle (C FP64 restatement of the reference routines) on the host cores."""
+    import numpy as np
+    from oracle import ora
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    o = ora.Oracle(dom, nam)
+    keep = {}
+    for n in ("tsb", "tsn") + HOT_3D + ("ub", "vb", "sshb") + HOT_2D:
+        keep[n] = np.array(st[n], order="F", copy=True)
+        o.bind(n.upper(), keep[n])
+    keep["rc"] = np.array(st["rcdu_bot"], order="F", copy=True)
+    o.bind("RCDU_BOT", keep["rc"])
+    keep["tsa"] = np.zeros_like(st["tsb"], order="F")
+    o.bind("TSA", keep["tsa"])
+    for n in ("AH_WSLP2", "AKZ"):
+        keep[n] = np.zeros_like(st["avt"], order="F")
+        o.bind(n, keep[n])
+    for n in ACC_2D:
+        keep[n] = np.zeros(st["sshn"].shape, order="F")
+        o.bind(n, keep[n])
+    cells = dom["jpi"] * dom["jpj"] * dom["jpk"]
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        o.stp_hotpath(5 + n)
+        n += 1
+        if time.perf_counter() - t0 > budget_s or n >= 50:
+            break
+    dt = time.perf_counter() - t0
+    nthr = int(os.environ.get("OMP_NUM_THREADS", "0") or 0) or os.cpu_count()
+    o.close()
+    return {"value": cells * n / dt, "unit": UNIT, "cores": nthr, "kind": "port",
+            "sample": f"{n} full hot-path steps of the same GYRE nn_GYRE=25 workload (FP64 oracle, OpenMP)"}
+
+
+def run_reference(args):
+    from nemo_gpu import dist
+    rank, world = dist.init("gloo")
+    if rank != 0:
+        return
+    dom, nam, states = build_case(args.nn, 1, seed=100)
+    cb = cpu_baseline(dom, nam, states[0], budget_s=max(5.0, min(60.0, 2.0 * args.steps)))
+    res = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dom["jpi"] * dom["jpj"] * dom["jpk"] / cb["value"],
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic: seeded GYRE analytic state",
+           "config": {"workload": f"GYRE nn_GYRE={args.nn} hot path step (dyn_spg_ts + FCT + iso ldf + zdf)",
+                      "grid": [dom["jpi"], dom["jpj"], dom["jpk"]], "members": 1},
+           "cpu_baseline": cb,
+           "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "note": "NEMO (Fortran) cannot be built in this environment; the reference arm runs the C FP64 "
+                   "restatement of the same routines (oracle/) on the host cores"}
+    print(json.dumps(res))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--prec", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--nn", type=int, default=25)
+    ap.add_argument("--members", type=int, default=1)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,278 @@
+/*
+ * nemo_gpu.h -- C ABI of the GB300 (sm_103a) implementation of NEMO's per-timestep
+ * ocean stencil path: FCT tracer advection, laplacian / rotated-isopycnal lateral
+ * diffusion, implicit vertical diffusion, the split-explicit barotropic sub-stepping
+ * and the lbc_lnk halo fill, plus the compensated global sum.
+ *
+ * Conventions (identical to the Fortran arrays the entry points replace):
+ *  - every field is a Fortran column-major array (jpi,jpj[,jpk][,kjpt]): i is the
+ *    contiguous index, then j, then k, then the tracer index;
+ *  - with an ensemble context (nmembers > 1) every field pointer addresses nmembers
+ *    such arrays stored one after the other (member index outermost);
+ *  - array arguments are DEVICE pointers (fields are resident on the GPU across
+ *    timesteps); they are double* for a NEMO_PREC_FP64 context and float* for a
+ *    NEMO_PREC_MIXED context, except the fields nemo_gpu_field_is_fp64() reports as
+ *    FP64 (barotropic time-filter accumulators), which stay double* in both modes;
+ *  - scalars (time steps, signs, land values) are always double;
+ *  - every entry point returns a status (NEMO_OK = 0); it never aborts, traps or
+ *    exits. The text of the last error is returned by nemo_gpu_last_error(). Errors
+ *    of asynchronous kernels surface at the next nemo_gpu_synchronize().
+ *  - one context = one CUDA stream; a context is not re-entrant.
+ *
+ * Each entry point cites the reference routine (file:line within NEMO 4.0 src/OCE)
+ * whose body it replaces; the Fortran caller keeps the reference's argument list.
+ */
+#ifndef NEMO_GPU_H
+#define NEMO_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+enum nemo_status {
+  NEMO_OK = 0,
+  NEMO_ERR_ARG = 1,          /* null pointer, bad size, unknown option value          */
+  NEMO_ERR_UNSUPPORTED = 2,  /* reference option this path does not implement         */
+  NEMO_ERR_UNBOUND = 3,      /* a module-global field the call reads is not bound     */
+  NEMO_ERR_CUDA = 4,         /* CUDA runtime error                                    */
+  NEMO_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up (barrier)          */
+  NEMO_ERR_NOMEM = 6,        /* device allocation failed at context creation          */
+  NEMO_ERR_STATE = 7         /* call order violated (e.g. iso before its first pass)  */
+};
+
+/* ------------------------------------------------------------ precision modes */
+enum nemo_prec {
+  NEMO_PREC_FP64 = 0,   /* plain form: every field and every operation in FP64       */
+  NEMO_PREC_MIXED = 1   /* FP32 bulk; FP64 barotropic accumulators and global sums    */
+};
+
+/* --------------------------------------------------------- vorticity schemes
+ * Same integer values as dynvor.F90:65-70 (np_ENS ... np_MIX). */
+enum nemo_vor { NEMO_VOR_ENS = 0, NEMO_VOR_ENE = 1, NEMO_VOR_ENT = 2,
+                NEMO_VOR_EET = 3, NEMO_VOR_EEN = 4, NEMO_VOR_MIX = 5 };
+
+/* --------------------------------------------------------- domain description
+ * Host pointers, read once by nemo_gpu_create. The masks (tmask, umask, vmask,
+ * wmask, ssmask, ssumask, ssvmask, tmask_i) and level indices (mikt, mbkt, mbku,
+ * mbkv) are derived from k_top/k_bot exactly as dommsk.F90:133-238 and
+ * domzgr.F90:292-314 derive them; the inverse/product metrics (e1e2t, r1_e1e2t,
+ * e2_e1u, ...) as domhgr.F90:133-151; ht_0/hu_0/hv_0 and r1_hu_0/r1_hv_0 as
+ * domain.F90:149-183. */
+typedef struct nemo_dom_desc {
+  int jpi, jpj, jpk;               /* par_oce.F90 domain sizes                           */
+  int jperio;                      /* lateral b.c. (0 = closed basin; only 0 supported)  */
+  const double *e1t, *e2t;         /* (jpi,jpj) horizontal scale factors [m]             */
+  const double *e1u, *e2u;
+  const double *e1v, *e2v;
+  const double *e1f, *e2f;
+  const double *ff_f, *ff_t;       /* (jpi,jpj) Coriolis parameter at f-/t-points [1/s]   */
+  const int *k_top, *k_bot;        /* (jpi,jpj) first / last wet T-level, 0 over land    */
+  const double *e3t_0, *e3u_0;     /* (jpi,jpj,jpk) rest-state vertical scale factors [m] */
+  const double *e3v_0, *e3w_0;
+  const double *e3f_0;
+} nemo_dom_desc;
+
+/* ------------------------------------------------------------ namelist subset
+ * The members of the reference namelists (cfgs/SHARED/namelist_ref) read by the
+ * routines on this path. Unsupported switches must be 0 (checked at creation). */
+typedef struct nemo_namelist {
+  double rn_rdt;          /* &namdom: baroclinic time step [s]                        */
+  double rn_atfp;         /* &namdom: Asselin filter parameter                        */
+  int nit000;             /* &namrun nn_it000: first time step                        */
+  int neuler;             /* 0: Euler first step (no restart), 1: leapfrog restart   */
+  int ln_linssh;          /* &namdom: linear free surface (fixed levels)              */
+  int ln_zps;             /* partial-step bottom gradients in lap/iso (domzgr)        */
+  int ln_isfcav;          /* ice-shelf cavities: must be 0                            */
+  int ln_traldf_lap;      /* &namtra_ldf operator: laplacian                          */
+  int ln_traldf_blp;      /*                       bilaplacian                        */
+  int ln_traldf_iso;      /* direction: iso-neutral (standard operator)               */
+  int ln_traldf_msc;      /* method of stabilizing correction                         */
+  double rn_aht_0;        /* constant eddy diffusivity aht0 = 1/2 Ud Ld used when the
+                             ahtu/ahtv fields are not bound (ldftra.F90:296-308) [m2/s] */
+  int ln_zdfddm;          /* &namzdf: double diffusion (separate avs for salinity)    */
+  int ln_zad_Aimp;        /* adaptive-implicit vertical advection: must be 0          */
+  int ln_bt_fw;           /* &namdyn_spg: forward barotropic integration              */
+  int ln_bt_av;           /*              time filtering of barotropic variables      */
+  int nn_bt_flt;          /*              filter: 0 none, 1 boxcar nn_baro, 2 boxcar 2 */
+  int ln_bt_auto;         /*              nn_baro from rn_bt_cmax                      */
+  int nn_baro;            /*              sub-steps per rn_rdt when ln_bt_auto = 0     */
+  double rn_bt_cmax;      /*              maximum barotropic Courant number            */
+  double rn_bt_alpha;     /*              temporal diffusion parameter                 */
+  int nvor_scheme;        /* &namdyn_vor: enum nemo_vor                                */
+  int nn_een_e3f;         /*              e3f averaging of the EEN scheme              */
+  int ln_dynadv_vec;      /* &namdyn_adv: vector-form momentum advection               */
+  int ln_sco;             /* s-coordinate (dom_oce)                                    */
+  int ln_apr_dyn;         /* &namsbc_apr: atmospheric pressure forcing in dyn          */
+  double rn_scal_load;    /* &namsbc_tide scalar loading factor                        */
+  double grav;            /* phycst.F90:38                                             */
+  double rau0;            /* reference density (eosbn2)                                */
+} nemo_namelist;
+
+/* ------------------------------------------------------- module-global fields
+ * Arrays the reference routines read from Fortran modules rather than from their
+ * argument lists (oce.F90, dom_oce.F90, zdf_oce.F90, ldfslp.F90, sbc_oce.F90,
+ * zdfdrg.F90, dynspg_ts.F90). The caller binds device arrays to them once; the
+ * dimension of each is given in brackets. T = 3-D (jpi,jpj,jpk), S = 2-D (jpi,jpj),
+ * TS = (jpi,jpj,jpk,2), G = (jpi,jpj,2). */
+enum nemo_field_id {
+  NEMO_F_TSB = 0,   /* [TS] before tracers tsb                         oce.F90        */
+  NEMO_F_TSN,       /* [TS] now tracers tsn                                           */
+  NEMO_F_TSA,       /* [TS] tracer trend / after tracers tsa                          */
+  NEMO_F_UN, NEMO_F_VN, NEMO_F_WN,     /* [T] now velocities                          */
+  NEMO_F_UB, NEMO_F_VB,                /* [T] before velocities                       */
+  NEMO_F_UA, NEMO_F_VA,                /* [T] momentum trends                         */
+  NEMO_F_AVT, NEMO_F_AVS,              /* [T] vertical diffusivities   zdf_oce.F90    */
+  NEMO_F_AHTU, NEMO_F_AHTV,            /* [T] lateral diffusivities    ldftra.F90     */
+  NEMO_F_USLP, NEMO_F_VSLP,            /* [T] iso-neutral slopes       ldfslp.F90     */
+  NEMO_F_WSLPI, NEMO_F_WSLPJ,
+  NEMO_F_AH_WSLP2, NEMO_F_AKZ,         /* [T] written by tra_ldf_iso, read by zdf     */
+  NEMO_F_E3T_B, NEMO_F_E3T_N, NEMO_F_E3T_A,   /* [T] time-varying scale factors       */
+  NEMO_F_E3U_N, NEMO_F_E3V_N, NEMO_F_E3W_N,
+  NEMO_F_GTSU, NEMO_F_GTSV,            /* [G] partial-step bottom gradients (zpshde)  */
+  NEMO_F_GTUI, NEMO_F_GTVI,            /* [G] partial-step top gradients              */
+  NEMO_F_SSHB, NEMO_F_SSHN, NEMO_F_SSHA,      /* [S] sea surface height (ssha: FP64)  */
+  NEMO_F_UB_B, NEMO_F_VB_B,            /* [S] before barotropic velocities            */
+  NEMO_F_UN_B, NEMO_F_VN_B,            /* [S] now barotropic velocities               */
+  NEMO_F_UA_B, NEMO_F_VA_B,            /* [S] after barotropic velocities (FP64)      */
+  NEMO_F_UN_ADV, NEMO_F_VN_ADV,        /* [S] time-filtered transports (FP64)         */
+  NEMO_F_UB2_B, NEMO_F_VB2_B,          /* [S] half-step fluxes, restart field (FP64)  */
+  NEMO_F_UN_BF, NEMO_F_VN_BF,          /* [S] filtered half-step fluxes (FP64)        */
+  NEMO_F_UTAU, NEMO_F_VTAU,            /* [S] wind stress                 sbc_oce.F90 */
+  NEMO_F_UTAU_B, NEMO_F_VTAU_B,
+  NEMO_F_EMP, NEMO_F_EMP_B,            /* [S] evaporation minus precipitation         */
+  NEMO_F_RNF, NEMO_F_RNF_B,            /* [S] runoff                                  */
+  NEMO_F_RCDU_BOT,                     /* [S] bottom drag coefficient x |U|  zdfdrg   */
+  NEMO_F_SSH_IB, NEMO_F_SSH_IBB,       /* [S] inverse-barometer ssh       sbcapr.F90  */
+  NEMO_F_COUNT
+};
+
+typedef struct nemo_ctx nemo_ctx;
+
+/* ------------------------------------------------------------- life cycle */
+
+/* Create a context: uploads the domain (nemo_dom_desc) and the namelist subset,
+ * derives masks and metrics, computes the barotropic sub-step count and weights
+ * (dyn_spg_ts_init, dynspg_ts.F90:1466-1493, and ts_wgt, :1313-1388), and
+ * allocates the library-owned work arrays (the reference's automatic arrays such
+ * as zwx, zwy, zwz, zwi at traadv_fct.F90:86). stream is a cudaStream_t, or NULL
+ * for a stream the context creates. Replaces the allocation/initialisation done
+ * in nemo_init (nemogcm.F90:249-472) for the fields of this path. */
+int nemo_gpu_create(const nemo_dom_desc *dom, const nemo_namelist *nam,
+                    int nmembers, int prec, void *stream, nemo_ctx **out);
+int nemo_gpu_destroy(nemo_ctx *ctx);
+
+/* Text of the last error of this context ("" if none). */
+const char *nemo_gpu_last_error(const nemo_ctx *ctx);
+
+/* Wait for all work of the context; reports asynchronous kernel errors. */
+int nemo_gpu_synchronize(nemo_ctx *ctx);
+
+/* Bind a device array to a module-global field (enum nemo_field_id).
+ * Passing NULL unbinds it (e.g. NEMO_F_AHTU = NULL selects the constant rn_aht_0,
+ * the e3 fields = NULL select the rest-state e3*_0 of the domain). */
+int nemo_gpu_bind(nemo_ctx *ctx, int field_id, void *dev_ptr);
+
+/* Number of elements (per member) and precision of a field (1 = FP64, 0 = FP32). */
+size_t nemo_gpu_field_numel(const nemo_ctx *ctx, int field_id);
+int nemo_gpu_field_is_fp64(const nemo_ctx *ctx, int field_id);
+
+/* Barotropic sub-step count icycle, and nn_baro after ln_bt_auto (dynspg_ts.F90:1491). */
+int nemo_gpu_spg_info(const nemo_ctx *ctx, int *icycle, int *nn_baro, double *rdtbt);
+
+/* Copy between a host buffer and a bound field (all members) on the context
+ * stream; host memory should be pinned for asynchronous copies. */
+int nemo_gpu_field_upload(nemo_ctx *ctx, int field_id, const void *host);
+int nemo_gpu_field_download(nemo_ctx *ctx, int field_id, void *host);
+
+/* -------------------------------------------------------------- hot path */
+
+/* Effective transports zun = e2u e3u_n un, zvn = e1v e3v_n vn, zwn = e1e2t wn with
+ * level jpk zeroed (traadv.F90:99-124, no Stokes drift / eiv / mle). */
+int nemo_gpu_tra_adv_trp(nemo_ctx *ctx, const void *un, const void *vn, const void *wn,
+                         void *zun, void *zvn, void *zwn);
+
+/* tra_adv_fct (traadv_fct.F90:54-327) with nonosc (:330-428) and interp_4th_cpt
+ * (:517-616). kn_fct_h in {2,4}, kn_fct_v in {2,4}. cdtype "TRA" or "TRC". */
+int nemo_gpu_tra_adv_fct(nemo_ctx *ctx, int kt, int kit000, const char *cdtype, double p2dt,
+                         const void *pun, const void *pvn, const void *pwn,
+                         const void *ptb, const void *ptn, void *pta,
+                         int kjpt, int kn_fct_h, int kn_fct_v);
+
+/* tra_ldf_lap (traldf_lap_blp.F90:47-158). pahu/pahv NULL = rn_aht_0 * umask/vmask.
+ * pgu..pgvi (jpi,jpj,kjpt) are read only when ln_zps (they may be NULL otherwise). */
+int nemo_gpu_tra_ldf_lap(nemo_ctx *ctx, int kt, int kit000, const char *cdtype,
+                         const void *pahu, const void *pahv,
+                         const void *pgu, const void *pgv, const void *pgui, const void *pgvi,
+                         const void *ptb, void *pta, int kjpt, int kpass);
+
+/* tra_ldf_iso (traldf_iso.F90:50-382): reads the bound slopes, writes the bound
+ * ah_wslp2 and akz on kpass = 1. */
+int nemo_gpu_tra_ldf_iso(nemo_ctx *ctx, int kt, int kit000, const char *cdtype,
+                         const void *pahu, const void *pahv,
+                         const void *pgu, const void *pgv, const void *pgui, const void *pgvi,
+                         const void *ptb, const void *ptbb, void *pta, int kjpt, int kpass);
+
+/* tra_zdf_imp (trazdf.F90:109-268): pta becomes the after tracer. Reads the bound
+ * avt (avs), and ah_wslp2/akz when ln_traldf_iso. */
+int nemo_gpu_tra_zdf_imp(nemo_ctx *ctx, int kt, int kit000, const char *cdtype, double p2dt,
+                         const void *ptb, void *pta, int kjpt);
+
+/* tra_zdf (trazdf.F90:46-106) on the bound tsb/tsa: r2dt choice (:66-68), the
+ * implicit solve, then WHERE( tsa(:,:,:,jp_sal) < 0 ) tsa = 0.1 (:83). */
+int nemo_gpu_tra_zdf(nemo_ctx *ctx, int kt);
+
+/* dyn_spg_ts (dynspg_ts.F90:121-1310) on the bound fields: phase 1 forcing,
+ * icycle barotropic sub-steps in one persistent kernel, phase 3 correction. */
+int nemo_gpu_dyn_spg_ts(nemo_ctx *ctx, int kt);
+
+/* lbc_lnk for one array of nk levels (nk = 1 for a 2-D array) and nl 4th-dim
+ * slices, closed-basin branch of lbc_lnk_generic.h90:80-105. cd_nat in
+ * T,U,V,W,F; psgn is only used across a north fold (not supported). The array
+ * is FP64 when is_fp64 != 0, else FP32. */
+int nemo_gpu_lbc_lnk(nemo_ctx *ctx, const char *cdname, void *ptab, int nk, int nl,
+                     const char *cd_nat, double psgn, double pval, int is_fp64);
+
+/* lbc_lnk_multi (lbc_lnk_multi_generic.h90:16-40): kfld arrays in one launch. */
+int nemo_gpu_lbc_lnk_multi(nemo_ctx *ctx, const char *cdname, int kfld, void *const *ptabs,
+                           const int *nk, const char *cd_nats, const double *psgns,
+                           double pval, int is_fp64);
+
+/* glob_sum (lib_fortran_generic.h90:32-65 with DDPDD, lib_fortran.F90:300-332):
+ * sum of ptab(:,:,k) * tmask_i over nk levels in double-double arithmetic, one
+ * result per member written to the host array out[nmembers]. ptab is FP64 when
+ * is_fp64 != 0. */
+int nemo_gpu_glob_sum(nemo_ctx *ctx, const char *cdname, const void *ptab, int nk,
+                      int is_fp64, double *out);
+
+/* The path of one timestep stp (step.F90:194-257) on the bound fields, in the
+ * reference's order: dyn_spg_ts, tsa = 0 (:234), tra_adv (transports + FCT),
+ * tra_ldf (lap or iso, per the namelist), tra_zdf (implicit + salinity clamp).
+ * The first call for a class of kt (Euler start, leapfrog) is captured in a CUDA
+ * graph that later calls replay. */
+int nemo_gpu_stp_hotpath(nemo_ctx *ctx, int kt);
+
+/* ------------------------------------------------------------ timing */
+
+/* Per-routine device timing of nemo_gpu_stp_hotpath, the counterpart of the
+ * reference's ln_timing (timing.F90:89-212, timing_start/stop around tra_adv,
+ * tra_ldf, tra_zdf, dyn_spg). While on, the hot path runs without graph replay and
+ * records CUDA events between routines. ms[0..3] = cumulative milliseconds in
+ * dyn_spg_ts, tra_adv, tra_ldf, tra_zdf since timing was switched on. */
+int nemo_gpu_set_timing(nemo_ctx *ctx, int on);
+int nemo_gpu_get_timing(nemo_ctx *ctx, double *ms, int *ncalls);
+
+/* ------------------------------------------------------------ test hook */
+
+/* Bound of the grid barriers of the persistent sub-step kernel: each wait gives up
+ * after max_spins polls and the next nemo_gpu_synchronize() returns
+ * NEMO_ERR_TIMEOUT. extra_arrivals > 0 makes every barrier wait for blocks that do
+ * not exist, so that the timeout path can be exercised without faulting the GPU. */
+int nemo_gpu_set_barrier_limit(nemo_ctx *ctx, long long max_spins, int extra_arrivals);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NEMO_GPU_H */

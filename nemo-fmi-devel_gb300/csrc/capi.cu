@@ -1,0 +1,1010 @@
+// capi.cu -- the C ABI of include/nemo_gpu.h: context life cycle, domain derivation,
+// module-field binding, and the entry points that replace the bodies of NEMO's
+// tra_adv_fct, tra_ldf_lap/iso, tra_zdf_imp, dyn_spg_ts, lbc_lnk and glob_sum.
+//
+// The host derives the masks, level indices and metric products from the domain
+// description with the formulas of dommsk.F90, domzgr.F90, domhgr.F90 and
+// domain.F90 in FP64, then uploads them once (rounded to FP32 for a mixed context).
+// All later work is asynchronous on the context's stream.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/nemo_gpu.h"
+#include "launch.h"
+
+using namespace nemo;
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+// Per-precision device copy of the derived domain.
+template <class T>
+struct DomStore {
+  Dom<T> d{};
+  std::vector<void*> owned;
+};
+
+}  // namespace
+
+struct nemo_ctx {
+  int jpi = 0, jpj = 0, jpk = 0, nmem = 1, prec = NEMO_PREC_FP64;
+  long n2 = 0, n3 = 0;
+  nemo_namelist nam{};
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  int nsm = 0;
+  // derived host domain (FP64)
+  std::vector<double> e1t, e2t, e1u, e2u, e1v, e2v, e1f, e2f, ff_f, ff_t;
+  std::vector<double> r1_e1t, r1_e2t, r1_e1u, r1_e2u, r1_e1v, r1_e2v, e1e2t, r1_e1e2t, e1e2u, e1e2v;
+  std::vector<double> r1_e1e2u, r1_e1e2v, e2_e1u, e1_e2v;
+  std::vector<double> ssmask, ssumask, ssvmask, tmask_i, ht_0, hu_0, hv_0, r1_hu_0, r1_hv_0;
+  std::vector<double> zwz, ftne, ftnw, ftse, ftsw;
+  std::vector<ColInfo> ci;
+  std::vector<uint8_t> mbkt;
+  std::vector<double> e3_0[5];  // t,u,v,w,f rest state (3-D)
+  bool e3_uniform[5] = {false, false, false, false, false};
+  // spg
+  int nn_baro = 0, icycle = 0;
+  double rdtbt = 0;
+  std::vector<double> wgt1, wgt2;
+  double* d_wgt1 = nullptr;
+  double* d_wgt2 = nullptr;
+  int ring0 = 0;
+  // device domain
+  DomStore<double> dd;
+  DomStore<float> df;
+  // bound fields
+  void* f[NEMO_F_COUNT] = {};
+  // work arrays
+  void* fct_w[6] = {};
+  void* fct_ztw = nullptr;
+  int fct_kjpt = 0;
+  void* spg_w[5] = {};
+  void* ring[3] = {};
+  unsigned int* bar_mem = nullptr;  // count, gen
+  int* err_flag = nullptr;
+  long long bar_spins = 4000000;
+  int bar_extra = 0;
+  int p2_blocks = 0;
+  double* gs_part = nullptr;
+  double* gs_out = nullptr;
+  int gs_nblk = 0;
+  double r2dt = 0;
+  std::map<int, cudaGraphExec_t> graphs;
+  bool graphs_ok = true;
+  // per-routine timing of the hot path (the ln_timing of timing.F90:89-212)
+  bool timing = false;
+  cudaEvent_t tev[5] = {};
+  double tms[4] = {0, 0, 0, 0};
+  int tcalls = 0;
+};
+
+namespace {
+
+int fail(nemo_ctx* c, int code, const char* fmt, ...) {
+  if (c) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    c->err = buf;
+  }
+  return code;
+}
+
+int cuda_fail(nemo_ctx* c, cudaError_t e, const char* what) {
+  return fail(c, NEMO_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(expr, what)                                  \
+  do {                                                  \
+    cudaError_t e_ = (expr);                            \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
+  } while (0)
+
+inline size_t I2(const nemo_ctx* c, int i, int j) { return (size_t)(i - 1) + (size_t)c->jpi * (j - 1); }
+inline size_t I3(const nemo_ctx* c, int i, int j, int k) { return I2(c, i, j) + (size_t)c->n2 * (k - 1); }
+
+bool is_fp64_field(int id) {
+  switch (id) {
+    case NEMO_F_SSHA: case NEMO_F_UA_B: case NEMO_F_VA_B: case NEMO_F_UN_ADV: case NEMO_F_VN_ADV:
+    case NEMO_F_UB2_B: case NEMO_F_VB2_B: case NEMO_F_UN_BF: case NEMO_F_VN_BF:
+      return true;
+    default:
+      return false;
+  }
+}
+
+size_t field_numel(const nemo_ctx* c, int id) {
+  switch (id) {
+    case NEMO_F_TSB: case NEMO_F_TSN: case NEMO_F_TSA: return 2 * (size_t)c->n3;
+    case NEMO_F_GTSU: case NEMO_F_GTSV: case NEMO_F_GTUI: case NEMO_F_GTVI: return 2 * (size_t)c->n2;
+    default: break;
+  }
+  if (id >= NEMO_F_SSHB) return (size_t)c->n2;
+  return (size_t)c->n3;
+}
+
+// ts_wgt (dynspg_ts.F90:1313-1388)
+void ts_wgt(nemo_ctx* c, int ll_av, int ll_fw, int* jpit) {
+  const int nb = c->nn_baro, n3b = 3 * nb;
+  c->wgt1.assign(n3b, 0.0);
+  c->wgt2.assign(n3b, 0.0);
+  int jic = ll_fw ? nb : 2 * nb;
+  if (ll_av) {
+    if (c->nam.nn_bt_flt == 0) {
+      c->wgt1[jic - 1] = 1.0;
+      *jpit = jic;
+    } else {
+      const double lim = c->nam.nn_bt_flt == 1 ? 0.5 : 1.0;
+      for (int jn = 1; jn <= n3b; ++jn) {
+        double za1 = std::fabs((double)(jn - jic)) / (double)nb;
+        if (za1 < lim) { c->wgt1[jn - 1] = 1.0; *jpit = jn; }
+      }
+    }
+  } else {
+    c->wgt1[jic - 1] = 1.0;
+    *jpit = jic;
+  }
+  for (int jn = 1; jn <= *jpit; ++jn)
+    for (int ji = jn; ji <= *jpit; ++ji) c->wgt2[jn - 1] = c->wgt2[jn - 1] + c->wgt1[ji - 1];
+  double s1 = 0, s2 = 0;
+  for (int jn = 1; jn <= *jpit; ++jn) { s1 += c->wgt1[jn - 1]; s2 += c->wgt2[jn - 1]; }
+  const double za1 = 1.0 / s1, za2 = 1.0 / s2;
+  for (int jn = 1; jn <= *jpit; ++jn) {
+    c->wgt1[jn - 1] = c->wgt1[jn - 1] * za1;
+    c->wgt2[jn - 1] = c->wgt2[jn - 1] * za2;
+  }
+}
+
+// Coriolis factors of dyn_spg_ts for a linear free surface (dynspg_ts.F90:241-342).
+void coriolis_factors(nemo_ctx* c, const std::vector<double>& tmask, const std::vector<double>& umask) {
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = c->n2;
+  c->zwz.assign(n2, 0.0);
+  c->ftne.assign(n2, 0.0); c->ftnw.assign(n2, 0.0); c->ftse.assign(n2, 0.0); c->ftsw.assign(n2, 0.0);
+  const int sc = c->nam.nvor_scheme;
+  const auto& ht = c->ht_0;
+  const auto& ssm = c->ssmask;
+  (void)tmask;
+  if (sc == NEMO_VOR_EEN) {
+    for (int jj = 1; jj <= jpj - 1; ++jj)
+      for (int ji = 1; ji <= jpi - 1; ++ji) {
+        double z;
+        double s = ht[I2(c, ji, jj + 1)] + ht[I2(c, ji + 1, jj + 1)] + ht[I2(c, ji, jj)] + ht[I2(c, ji + 1, jj)];
+        if (c->nam.nn_een_e3f == 0) z = s * 0.25;
+        else {
+          double m = ssm[I2(c, ji, jj + 1)] + ssm[I2(c, ji + 1, jj + 1)] + ssm[I2(c, ji, jj)] + ssm[I2(c, ji + 1, jj)];
+          z = s / (m > 1.0 ? m : 1.0);
+        }
+        if (z != 0.0) z = c->ff_f[I2(c, ji, jj)] / z;
+        c->zwz[I2(c, ji, jj)] = z;
+      }
+    for (int jj = 1; jj <= jpj; ++jj) c->zwz[I2(c, jpi, jj)] = 0.0;
+    for (int ji = 1; ji <= jpi; ++ji) c->zwz[I2(c, ji, jpj)] = 0.0;
+    const auto& w = c->zwz;
+    for (int jj = 2; jj <= jpj; ++jj)
+      for (int ji = 2; ji <= jpi; ++ji) {
+        c->ftne[I2(c, ji, jj)] = w[I2(c, ji - 1, jj)] + w[I2(c, ji, jj)] + w[I2(c, ji, jj - 1)];
+        c->ftnw[I2(c, ji, jj)] = w[I2(c, ji - 1, jj - 1)] + w[I2(c, ji - 1, jj)] + w[I2(c, ji, jj)];
+        c->ftse[I2(c, ji, jj)] = w[I2(c, ji, jj)] + w[I2(c, ji, jj - 1)] + w[I2(c, ji - 1, jj - 1)];
+        c->ftsw[I2(c, ji, jj)] = w[I2(c, ji, jj - 1)] + w[I2(c, ji - 1, jj - 1)] + w[I2(c, ji - 1, jj)];
+      }
+  } else if (sc == NEMO_VOR_EET) {
+    const auto& ff = c->ff_f;
+    for (int jj = 2; jj <= jpj; ++jj)
+      for (int ji = 2; ji <= jpi; ++ji) {
+        double z1_ht = ssm[I2(c, ji, jj)] / (ht[I2(c, ji, jj)] + 1.0 - ssm[I2(c, ji, jj)]);
+        c->ftne[I2(c, ji, jj)] = (ff[I2(c, ji - 1, jj)] + ff[I2(c, ji, jj)] + ff[I2(c, ji, jj - 1)]) * z1_ht;
+        c->ftnw[I2(c, ji, jj)] = (ff[I2(c, ji - 1, jj - 1)] + ff[I2(c, ji - 1, jj)] + ff[I2(c, ji, jj)]) * z1_ht;
+        c->ftse[I2(c, ji, jj)] = (ff[I2(c, ji, jj)] + ff[I2(c, ji, jj - 1)] + ff[I2(c, ji - 1, jj - 1)]) * z1_ht;
+        c->ftsw[I2(c, ji, jj)] = (ff[I2(c, ji, jj - 1)] + ff[I2(c, ji - 1, jj - 1)] + ff[I2(c, ji - 1, jj)]) * z1_ht;
+      }
+  } else if (sc == NEMO_VOR_ENE || sc == NEMO_VOR_ENS || sc == NEMO_VOR_MIX) {
+    std::vector<double> zhf(n2, 0.0);
+    if (c->nam.ln_sco)
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          double m = ssm[I2(c, ji, jj)] + ssm[I2(c, ji + 1, jj)] + ssm[I2(c, ji, jj + 1)] + ssm[I2(c, ji + 1, jj + 1)];
+          zhf[I2(c, ji, jj)] = (ht[I2(c, ji, jj)] + ht[I2(c, ji + 1, jj)] + ht[I2(c, ji, jj + 1)] + ht[I2(c, ji + 1, jj + 1)]) /
+                               (m > 1.0 ? m : 1.0);
+        }
+    for (int jj = 1; jj <= jpj - 1; ++jj)
+      for (int ji = 1; ji <= jpi; ++ji)
+        zhf[I2(c, ji, jj)] = zhf[I2(c, ji, jj)] * (1.0 - umask[I3(c, ji, jj, 1)] * umask[I3(c, ji, jj + 1, 1)]);
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi; ++ji)
+          zhf[I2(c, ji, jj)] =
+              zhf[I2(c, ji, jj)] + c->e3_0[4][I3(c, ji, jj, jk)] * umask[I3(c, ji, jj, jk)] * umask[I3(c, ji, jj + 1, jk)];
+    for (int jj = 1; jj <= jpj; ++jj) zhf[I2(c, jpi, jj)] = 0.0;
+    for (int ji = 1; ji <= jpi; ++ji) zhf[I2(c, ji, jpj)] = 0.0;
+    for (size_t p = 0; p < n2; ++p)
+      if (zhf[p] != 0.0) c->zwz[p] = 1.0 / zhf[p];
+    for (size_t p = 0; p < n2; ++p) c->zwz[p] = c->ff_f[p] * c->zwz[p];
+  }
+}
+
+template <class T>
+int upload(nemo_ctx* c, DomStore<T>& st, const std::vector<double>& src, const T** dst) {
+  std::vector<T> h(src.size());
+  for (size_t i = 0; i < src.size(); ++i) h[i] = (T)src[i];
+  void* p = nullptr;
+  CK(cudaMalloc(&p, h.size() * sizeof(T) + 16), "cudaMalloc(domain)");
+  st.owned.push_back(p);
+  CK(cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice), "upload(domain)");
+  *dst = (const T*)p;
+  return NEMO_OK;
+}
+
+// e3 field: a 1-D profile when horizontally uniform, else the full 3-D array.
+template <class T>
+int upload_e3(nemo_ctx* c, DomStore<T>& st, int which, E3<T>* e) {
+  const auto& a = c->e3_0[which];
+  if (c->e3_uniform[which]) {
+    std::vector<double> prof(c->jpk);
+    for (int k = 0; k < c->jpk; ++k) prof[k] = a[(size_t)k * c->n2];
+    const T* p;
+    int st_ = upload(c, st, prof, &p);
+    if (st_) return st_;
+    *e = E3<T>{p, 1, 0, 0};
+  } else {
+    const T* p;
+    int st_ = upload(c, st, a, &p);
+    if (st_) return st_;
+    *e = E3<T>{p, c->n2, 0, 1};
+  }
+  return NEMO_OK;
+}
+
+template <class T>
+int build_dom(nemo_ctx* c, DomStore<T>& st) {
+  Dom<T>& d = st.d;
+  d.jpi = c->jpi; d.jpj = c->jpj; d.jpk = c->jpk; d.nmem = c->nmem; d.n2 = c->n2; d.n3 = c->n3;
+  int s = 0;
+#define UP(name) if ((s = upload(c, st, c->name, &d.name))) return s
+  UP(e1t); UP(e2t); UP(e1u); UP(e2u); UP(e1v); UP(e2v);
+  UP(r1_e1u); UP(r1_e2u); UP(r1_e1v); UP(r1_e2v);
+  UP(e1e2t); UP(r1_e1e2t); UP(e2_e1u); UP(e1_e2v); UP(r1_e1e2u); UP(r1_e1e2v);
+  UP(ht_0); UP(hu_0); UP(hv_0); UP(r1_hu_0); UP(r1_hv_0);
+  UP(ssmask); UP(ssumask); UP(ssvmask);
+  UP(ff_t); UP(zwz); UP(ftne); UP(ftnw); UP(ftse); UP(ftsw);
+#undef UP
+  {
+    void* p = nullptr;
+    CK(cudaMalloc(&p, c->n2 * sizeof(double)), "cudaMalloc(tmask_i)");
+    st.owned.push_back(p);
+    CK(cudaMemcpy(p, c->tmask_i.data(), c->n2 * sizeof(double), cudaMemcpyHostToDevice), "upload(tmask_i)");
+    d.tmask_i = (const double*)p;
+    CK(cudaMalloc(&p, c->n2 * sizeof(ColInfo)), "cudaMalloc(colinfo)");
+    st.owned.push_back(p);
+    CK(cudaMemcpy(p, c->ci.data(), c->n2 * sizeof(ColInfo), cudaMemcpyHostToDevice), "upload(colinfo)");
+    d.ci = (const ColInfo*)p;
+    CK(cudaMalloc(&p, c->n2), "cudaMalloc(mbkt)");
+    st.owned.push_back(p);
+    CK(cudaMemcpy(p, c->mbkt.data(), c->n2, cudaMemcpyHostToDevice), "upload(mbkt)");
+    d.mbkt = (const uint8_t*)p;
+  }
+  if ((s = upload_e3(c, st, 0, &d.e3t_n))) return s;
+  d.e3t_b = d.e3t_n; d.e3t_a = d.e3t_n;
+  if ((s = upload_e3(c, st, 1, &d.e3u_n))) return s;
+  if ((s = upload_e3(c, st, 2, &d.e3v_n))) return s;
+  if ((s = upload_e3(c, st, 3, &d.e3w_n))) return s;
+  return NEMO_OK;
+}
+
+template <class T>
+void free_dom(DomStore<T>& st) {
+  for (void* p : st.owned) cudaFree(p);
+  st.owned.clear();
+}
+
+// Domain derivation (dommsk.F90:133-238, domzgr.F90:292-314, domhgr.F90:133-151,
+// domain.F90:149-183) and spg set-up (dynspg_ts.F90:1479-1493).
+int derive_domain(nemo_ctx* c, const nemo_dom_desc* dm) {
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = c->n2, n3 = c->n3;
+  auto cp2 = [&](std::vector<double>& v, const double* s) { v.assign(s, s + n2); };
+  cp2(c->e1t, dm->e1t); cp2(c->e2t, dm->e2t); cp2(c->e1u, dm->e1u); cp2(c->e2u, dm->e2u);
+  cp2(c->e1v, dm->e1v); cp2(c->e2v, dm->e2v); cp2(c->e1f, dm->e1f); cp2(c->e2f, dm->e2f);
+  cp2(c->ff_f, dm->ff_f); cp2(c->ff_t, dm->ff_t);
+  const double* e3s[5] = {dm->e3t_0, dm->e3u_0, dm->e3v_0, dm->e3w_0, dm->e3f_0};
+  for (int w = 0; w < 5; ++w) {
+    c->e3_0[w].assign(e3s[w], e3s[w] + n3);
+    bool uni = true;
+    for (int k = 0; k < jpk && uni; ++k) {
+      const double v0 = c->e3_0[w][(size_t)k * n2];
+      for (size_t p = 0; p < n2; ++p)
+        if (c->e3_0[w][(size_t)k * n2 + p] != v0) { uni = false; break; }
+    }
+    c->e3_uniform[w] = uni;
+  }
+  auto mk = [&](std::vector<double>& v) { v.assign(n2, 0.0); };
+  mk(c->r1_e1t); mk(c->r1_e2t); mk(c->r1_e1u); mk(c->r1_e2u); mk(c->r1_e1v); mk(c->r1_e2v); mk(c->e1e2t);
+  mk(c->r1_e1e2t); mk(c->e1e2u); mk(c->e1e2v); mk(c->r1_e1e2u); mk(c->r1_e1e2v); mk(c->e2_e1u); mk(c->e1_e2v);
+  for (size_t p = 0; p < n2; ++p) {
+    c->r1_e1t[p] = 1.0 / c->e1t[p]; c->r1_e2t[p] = 1.0 / c->e2t[p];
+    c->r1_e1u[p] = 1.0 / c->e1u[p]; c->r1_e2u[p] = 1.0 / c->e2u[p];
+    c->r1_e1v[p] = 1.0 / c->e1v[p]; c->r1_e2v[p] = 1.0 / c->e2v[p];
+    c->e1e2t[p] = c->e1t[p] * c->e2t[p]; c->r1_e1e2t[p] = 1.0 / c->e1e2t[p];
+    c->e1e2u[p] = c->e1u[p] * c->e2u[p]; c->e1e2v[p] = c->e1v[p] * c->e2v[p];
+    c->r1_e1e2u[p] = 1.0 / c->e1e2u[p]; c->r1_e1e2v[p] = 1.0 / c->e1e2v[p];
+    c->e2_e1u[p] = c->e2u[p] / c->e1u[p]; c->e1_e2v[p] = c->e1v[p] / c->e2v[p];
+  }
+  // masks
+  std::vector<double> tmask(n3, 0.0), umask(n3, 0.0), vmask(n3, 0.0);
+  for (int jj = 1; jj <= jpj; ++jj)
+    for (int ji = 1; ji <= jpi; ++ji) {
+      int kt = dm->k_top[I2(c, ji, jj)], kb = dm->k_bot[I2(c, ji, jj)];
+      if (kt < 0 || kt > 1) return fail(c, NEMO_ERR_UNSUPPORTED, "k_top(%d,%d)=%d: ice-shelf cavities are not supported", ji, jj, kt);
+      if (kb < 0 || kb > jpk) return fail(c, NEMO_ERR_ARG, "k_bot(%d,%d)=%d out of range", ji, jj, kb);
+      bool edge = ji == 1 || ji == jpi || jj == 1 || jj == jpj;
+      if (kt != 0 && !edge)
+        for (int jk = kt; jk <= kb; ++jk) tmask[I3(c, ji, jj, jk)] = 1.0;
+    }
+  for (int jk = 1; jk <= jpk; ++jk)
+    for (int jj = 1; jj <= jpj - 1; ++jj)
+      for (int ji = 1; ji <= jpi - 1; ++ji) {
+        umask[I3(c, ji, jj, jk)] = tmask[I3(c, ji, jj, jk)] * tmask[I3(c, ji + 1, jj, jk)];
+        vmask[I3(c, ji, jj, jk)] = tmask[I3(c, ji, jj, jk)] * tmask[I3(c, ji, jj + 1, jk)];
+      }
+  for (int jk = 1; jk <= jpk; ++jk) {
+    for (int jj = 1; jj <= jpj; ++jj) {
+      umask[I3(c, 1, jj, jk)] = 0; umask[I3(c, jpi, jj, jk)] = 0;
+      vmask[I3(c, 1, jj, jk)] = 0; vmask[I3(c, jpi, jj, jk)] = 0;
+    }
+    for (int ji = 1; ji <= jpi; ++ji) {
+      umask[I3(c, ji, 1, jk)] = 0; umask[I3(c, ji, jpj, jk)] = 0;
+      vmask[I3(c, ji, 1, jk)] = 0; vmask[I3(c, ji, jpj, jk)] = 0;
+    }
+  }
+  // column ranges; verify that each mask is one contiguous level range
+  c->ci.assign(n2, ColInfo{});
+  c->mbkt.assign(n2, 1);
+  auto range = [&](const std::vector<double>& m, size_t p, uint8_t& lo, uint8_t& hi) -> bool {
+    int l = 0, h = -1;
+    for (int k = 1; k <= jpk; ++k)
+      if (m[p + n2 * (k - 1)] != 0.0) { if (l == 0) l = k; h = k; }
+    if (l == 0) { lo = 1; hi = 0; return true; }
+    for (int k = l; k <= h; ++k)
+      if (m[p + n2 * (k - 1)] == 0.0) return false;
+    lo = (uint8_t)l; hi = (uint8_t)h;
+    return true;
+  };
+  for (size_t p = 0; p < n2; ++p) {
+    ColInfo& q = c->ci[p];
+    if (!range(tmask, p, q.tlo, q.thi) || !range(umask, p, q.ulo, q.uhi) || !range(vmask, p, q.vlo, q.vhi))
+      return fail(c, NEMO_ERR_UNSUPPORTED, "column %zu: wet levels are not contiguous", p);
+    int kb = dm->k_bot[p];
+    c->mbkt[p] = (uint8_t)(kb > 1 ? kb : 1);
+  }
+  for (int jj = 1; jj <= jpj; ++jj)
+    for (int ji = 1; ji <= jpi; ++ji) {
+      ColInfo& q = c->ci[I2(c, ji, jj)];
+      if (ji == jpi || jj == jpj || ji == 1 || jj == 1) { q.mbku = 1; q.mbkv = 1; continue; }
+      int a = c->mbkt[I2(c, ji + 1, jj)], b = c->mbkt[I2(c, ji, jj)], e = c->mbkt[I2(c, ji, jj + 1)];
+      q.mbku = (uint8_t)((a < b ? a : b) > 1 ? (a < b ? a : b) : 1);
+      q.mbkv = (uint8_t)((e < b ? e : b) > 1 ? (e < b ? e : b) : 1);
+    }
+  c->ssmask.assign(n2, 0.0); c->ssumask.assign(n2, 0.0); c->ssvmask.assign(n2, 0.0); c->tmask_i.assign(n2, 0.0);
+  for (size_t p = 0; p < n2; ++p) {
+    const ColInfo& q = c->ci[p];
+    c->ssmask[p] = q.tlo <= q.thi ? 1.0 : 0.0;
+    c->ssumask[p] = q.ulo <= q.uhi ? 1.0 : 0.0;
+    c->ssvmask[p] = q.vlo <= q.vhi ? 1.0 : 0.0;
+  }
+  for (int jj = 1; jj <= jpj; ++jj)
+    for (int ji = 1; ji <= jpi; ++ji) {
+      bool edge = ji == 1 || ji == jpi || jj == 1 || jj == jpj;
+      c->tmask_i[I2(c, ji, jj)] = c->ssmask[I2(c, ji, jj)] * (edge ? 0.0 : 1.0);
+    }
+  c->ht_0.assign(n2, 0.0); c->hu_0.assign(n2, 0.0); c->hv_0.assign(n2, 0.0);
+  c->r1_hu_0.assign(n2, 0.0); c->r1_hv_0.assign(n2, 0.0);
+  for (int jk = 0; jk < jpk; ++jk)
+    for (size_t p = 0; p < n2; ++p) {
+      c->ht_0[p] = c->ht_0[p] + c->e3_0[0][p + n2 * jk] * tmask[p + n2 * jk];
+      c->hu_0[p] = c->hu_0[p] + c->e3_0[1][p + n2 * jk] * umask[p + n2 * jk];
+      c->hv_0[p] = c->hv_0[p] + c->e3_0[2][p + n2 * jk] * vmask[p + n2 * jk];
+    }
+  for (size_t p = 0; p < n2; ++p) {
+    c->r1_hu_0[p] = c->ssumask[p] / (c->hu_0[p] + 1.0 - c->ssumask[p]);
+    c->r1_hv_0[p] = c->ssvmask[p] / (c->hv_0[p] + 1.0 - c->ssvmask[p]);
+  }
+  // dyn_spg_ts_init
+  double zcmax = -1e300;
+  for (size_t p = 0; p < n2; ++p) {
+    double zxr2 = c->r1_e1t[p] * c->r1_e1t[p], zyr2 = c->r1_e2t[p] * c->r1_e2t[p];
+    double h = c->ht_0[p] > 0.0 ? c->ht_0[p] : 0.0;
+    double zcu = std::sqrt(c->nam.grav * h * (zxr2 + zyr2));
+    if (zcu > zcmax) zcmax = zcu;
+  }
+  c->nn_baro = c->nam.ln_bt_auto ? (int)std::ceil(c->nam.rn_rdt / c->nam.rn_bt_cmax * zcmax) : c->nam.nn_baro;
+  if (c->nn_baro < 1) c->nn_baro = 1;
+  c->rdtbt = c->nam.rn_rdt / (double)c->nn_baro;
+  int jpit = 0;
+  ts_wgt(c, c->nam.ln_bt_av, c->nam.ln_bt_fw, &jpit);
+  c->icycle = jpit;
+  coriolis_factors(c, tmask, umask);
+  return NEMO_OK;
+}
+
+template <class T>
+const Dom<T>& dom(nemo_ctx* c);
+template <>
+const Dom<double>& dom<double>(nemo_ctx* c) { return c->dd.d; }
+template <>
+const Dom<float>& dom<float>(nemo_ctx* c) { return c->df.d; }
+
+// Dom with the bound time-varying e3 fields substituted for the rest state.
+template <class T>
+Dom<T> dom_now(nemo_ctx* c) {
+  Dom<T> d = dom<T>(c);
+  auto sub = [&](int id, E3<T>& e) {
+    if (c->f[id]) e = E3<T>{(const T*)c->f[id], c->n2, c->n3, 1};
+  };
+  sub(NEMO_F_E3T_B, d.e3t_b); sub(NEMO_F_E3T_N, d.e3t_n); sub(NEMO_F_E3T_A, d.e3t_a);
+  sub(NEMO_F_E3U_N, d.e3u_n); sub(NEMO_F_E3V_N, d.e3v_n); sub(NEMO_F_E3W_N, d.e3w_n);
+  return d;
+}
+
+int ensure_fct_work(nemo_ctx* c, int kjpt, int need_ztw) {
+  const size_t es = c->prec == NEMO_PREC_FP64 ? 8 : 4;
+  const size_t bytes = (size_t)kjpt * c->n3 * c->nmem * es;
+  if (kjpt > c->fct_kjpt) {
+    for (auto& p : c->fct_w) { cudaFree(p); p = nullptr; }
+    cudaFree(c->fct_ztw); c->fct_ztw = nullptr;
+    for (auto& p : c->fct_w) {
+      if (cudaMalloc(&p, bytes) != cudaSuccess) return fail(c, NEMO_ERR_NOMEM, "FCT work arrays (%zu bytes)", bytes);
+      cudaMemset(p, 0, bytes);
+    }
+    c->fct_kjpt = kjpt;
+  }
+  if (need_ztw && !c->fct_ztw) {
+    if (cudaMalloc(&c->fct_ztw, (size_t)c->fct_kjpt * c->n3 * c->nmem * es) != cudaSuccess)
+      return fail(c, NEMO_ERR_NOMEM, "FCT compact-interpolation array");
+    cudaMemset(c->fct_ztw, 0, (size_t)c->fct_kjpt * c->n3 * c->nmem * es);
+  }
+  return NEMO_OK;
+}
+
+int check_cdtype(nemo_ctx* c, const char* cdtype, int* is_trc) {
+  if (!cdtype) return fail(c, NEMO_ERR_ARG, "cdtype is NULL");
+  if (!strncmp(cdtype, "TRA", 3)) *is_trc = 0;
+  else if (!strncmp(cdtype, "TRC", 3)) *is_trc = 1;
+  else return fail(c, NEMO_ERR_ARG, "cdtype must be TRA or TRC");
+  return NEMO_OK;
+}
+
+template <class T>
+int run_fct(nemo_ctx* c, double p2dt, const void* pun, const void* pvn, const void* pwn, int trp, const void* ptb,
+            const void* ptn, const void* pta_in, void* pta, int kjpt, int kh, int kv) {
+  int s = ensure_fct_work(c, kjpt, kv == 4);
+  if (s) return s;
+  FctArgs<T> a{};
+  a.p2dt = (T)p2dt;
+  a.pun = (const T*)pun; a.pvn = (const T*)pvn; a.pwn = (const T*)pwn; a.trp = trp;
+  a.ptb = (const T*)ptb; a.ptn = (const T*)ptn; a.pta_in = (const T*)pta_in; a.pta = (T*)pta;
+  a.zwi = (T*)c->fct_w[0]; a.ax = (T*)c->fct_w[1]; a.ay = (T*)c->fct_w[2]; a.az = (T*)c->fct_w[3];
+  a.betup = (T*)c->fct_w[4]; a.betdo = (T*)c->fct_w[5];
+  a.ztw = (const T*)c->fct_ztw;
+  a.kjpt = kjpt; a.kn_fct_h = kh; a.kn_fct_v = kv; a.linssh = c->nam.ln_linssh;
+  cudaError_t e = launch_fct<T>(dom_now<T>(c), a, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "tra_adv_fct launch");
+  return NEMO_OK;
+}
+
+template <class T>
+LdfArgs<T> ldf_args(nemo_ctx* c, const void* pahu, const void* pahv, const void* pgu, const void* pgv, const void* ptb,
+                    const void* ptbb, void* pta, int kjpt, int kpass) {
+  LdfArgs<T> a{};
+  a.pahu = (const T*)pahu; a.pahv = (const T*)pahv;
+  a.aht_c = (T)(c->nam.ln_traldf_blp ? std::sqrt(c->nam.rn_aht_0) : c->nam.rn_aht_0);
+  a.pgu = (const T*)pgu; a.pgv = (const T*)pgv; a.zps = c->nam.ln_zps;
+  a.ptb = (const T*)ptb; a.ptbb = (const T*)ptbb; a.pta = (T*)pta;
+  a.kjpt = kjpt; a.kpass = kpass; a.zsign = kpass == 1 ? T(1) : T(-1);
+  return a;
+}
+
+template <class T>
+int run_ldf_lap(nemo_ctx* c, const void* pahu, const void* pahv, const void* pgu, const void* pgv, const void* ptb,
+                void* pta, int kjpt, int kpass) {
+  LdfArgs<T> a = ldf_args<T>(c, pahu, pahv, pgu, pgv, ptb, ptb, pta, kjpt, kpass);
+  cudaError_t e = launch_ldf_lap<T>(dom_now<T>(c), a, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "tra_ldf_lap launch");
+  return NEMO_OK;
+}
+
+template <class T>
+int run_ldf_iso(nemo_ctx* c, int kt, int kit000, const void* pahu, const void* pahv, const void* pgu, const void* pgv,
+                const void* ptb, const void* ptbb, void* pta, int kjpt, int kpass) {
+  const nemo_namelist& nm = c->nam;
+  if (!c->f[NEMO_F_USLP] || !c->f[NEMO_F_VSLP] || !c->f[NEMO_F_WSLPI] || !c->f[NEMO_F_WSLPJ] ||
+      !c->f[NEMO_F_AH_WSLP2] || !c->f[NEMO_F_AKZ])
+    return fail(c, NEMO_ERR_UNBOUND, "tra_ldf_iso: slopes, ah_wslp2 and akz must be bound");
+  LdfArgs<T> a = ldf_args<T>(c, pahu, pahv, pgu, pgv, ptb, ptbb, pta, kjpt, kpass);
+  a.uslp = (const T*)c->f[NEMO_F_USLP]; a.vslp = (const T*)c->f[NEMO_F_VSLP];
+  a.wslpi = (const T*)c->f[NEMO_F_WSLPI]; a.wslpj = (const T*)c->f[NEMO_F_WSLPJ];
+  a.ah_wslp2 = (T*)c->f[NEMO_F_AH_WSLP2]; a.akz = (T*)c->f[NEMO_F_AKZ];
+  a.lap = nm.ln_traldf_lap; a.blp = nm.ln_traldf_blp; a.msc = nm.ln_traldf_msc;
+  const double z2dt = (nm.neuler == 0 && kt == nm.nit000) ? nm.rn_rdt : 2.0 * nm.rn_rdt;
+  a.z2dt = (T)z2dt; a.z1_2dt = (T)(1.0 / z2dt);
+  if (kpass == 1 && kt == kit000) {
+    const size_t bytes = c->n3 * c->nmem * sizeof(T);
+    CK(cudaMemsetAsync(a.akz, 0, bytes, c->stream), "akz = 0");
+    CK(cudaMemsetAsync(a.ah_wslp2, 0, bytes, c->stream), "ah_wslp2 = 0");
+  }
+  cudaError_t e = launch_ldf_iso<T>(dom_now<T>(c), a, kpass == 1 && !nm.ln_traldf_msc,
+                                    kpass == 1 && nm.ln_traldf_msc, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "tra_ldf_iso launch");
+  return NEMO_OK;
+}
+
+template <class T>
+int run_zdf(nemo_ctx* c, double p2dt, const void* ptb, void* pta, int kjpt, int is_trc, int clamp) {
+  const nemo_namelist& nm = c->nam;
+  ZdfArgs<T> a{};
+  a.p2dt = (T)p2dt; a.ptb = (const T*)ptb; a.pta = (T*)pta; a.kjpt = kjpt;
+  a.avt = (const T*)c->f[NEMO_F_AVT]; a.avs = (const T*)c->f[NEMO_F_AVS];
+  a.ddm = nm.ln_zdfddm; a.is_trc = is_trc; a.clamp_sal = clamp;
+  if (!is_trc && !a.avt) return fail(c, NEMO_ERR_UNBOUND, "tra_zdf_imp: avt must be bound");
+  if ((is_trc || nm.ln_zdfddm) && !a.avs) return fail(c, NEMO_ERR_UNBOUND, "tra_zdf_imp: avs must be bound");
+  if (nm.ln_traldf_iso) {
+    a.add = (const T*)c->f[nm.ln_traldf_msc ? NEMO_F_AKZ : NEMO_F_AH_WSLP2];
+    if (!a.add) return fail(c, NEMO_ERR_UNBOUND, "tra_zdf_imp: ah_wslp2/akz must be bound with iso-neutral mixing");
+  }
+  cudaError_t e = launch_zdf<T>(dom_now<T>(c), a, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "tra_zdf_imp launch");
+  return NEMO_OK;
+}
+
+template <class T>
+int run_spg(nemo_ctx* c, int kt) {
+  const nemo_namelist& nm = c->nam;
+  void* const* F = c->f;
+  const int need[] = {NEMO_F_UA, NEMO_F_VA, NEMO_F_UN, NEMO_F_VN, NEMO_F_SSHN, NEMO_F_SSHA, NEMO_F_UN_B,
+                      NEMO_F_VN_B, NEMO_F_UB_B, NEMO_F_VB_B, NEMO_F_UA_B, NEMO_F_VA_B, NEMO_F_UN_ADV,
+                      NEMO_F_VN_ADV, NEMO_F_UB2_B, NEMO_F_VB2_B, NEMO_F_UN_BF, NEMO_F_VN_BF, NEMO_F_UTAU,
+                      NEMO_F_VTAU, NEMO_F_EMP, NEMO_F_RCDU_BOT};
+  for (int id : need)
+    if (!F[id]) return fail(c, NEMO_ERR_UNBOUND, "dyn_spg_ts: field %d must be bound", id);
+  if (!nm.ln_bt_fw)
+    for (int id : {NEMO_F_UB, NEMO_F_VB, NEMO_F_SSHB, NEMO_F_UTAU_B, NEMO_F_VTAU_B, NEMO_F_EMP_B})
+      if (!F[id]) return fail(c, NEMO_ERR_UNBOUND, "dyn_spg_ts (ln_bt_fw=F): field %d must be bound", id);
+  if (nm.ln_apr_dyn && (!F[NEMO_F_SSH_IB] || (!nm.ln_bt_fw && !F[NEMO_F_SSH_IBB])))
+    return fail(c, NEMO_ERR_UNBOUND, "dyn_spg_ts (ln_apr_dyn): ssh_ib must be bound");
+  // kt-dependent scalars (:185-216, :346-349)
+  const double z2dt_bf = (kt == nm.nit000 && nm.neuler == 0) ? nm.rn_rdt : 2.0 * nm.rn_rdt;
+  int ll_init = nm.ln_bt_av;
+  bool reweight = false;
+  int ll_fw_start = 0;
+  if (kt == nm.nit000) {
+    if (nm.neuler == 0) ll_init = 1;
+    ll_fw_start = (nm.ln_bt_fw || nm.neuler == 0) ? 1 : 0;
+    reweight = true;
+  }
+  if (!nm.ln_bt_fw && nm.neuler == 0 && kt == nm.nit000 + 1) { ll_fw_start = 0; reweight = true; }
+  if (reweight) {
+    int jpit = 0;
+    ts_wgt(c, nm.ln_bt_av, ll_fw_start, &jpit);
+    c->icycle = jpit;
+    CK(cudaMemcpyAsync(c->d_wgt1, c->wgt1.data(), c->wgt1.size() * 8, cudaMemcpyHostToDevice, c->stream), "weights");
+    CK(cudaMemcpyAsync(c->d_wgt2, c->wgt2.data(), c->wgt2.size() * 8, cudaMemcpyHostToDevice, c->stream), "weights");
+    CK(cudaStreamSynchronize(c->stream), "weights");
+  }
+  SpgArgs<T> a{};
+  a.ua = (T*)F[NEMO_F_UA]; a.va = (T*)F[NEMO_F_VA]; a.un = (T*)F[NEMO_F_UN]; a.vn = (T*)F[NEMO_F_VN];
+  a.ub = (const T*)F[NEMO_F_UB]; a.vb = (const T*)F[NEMO_F_VB];
+  a.sshn = (const T*)F[NEMO_F_SSHN]; a.sshb = (const T*)F[NEMO_F_SSHB];
+  a.un_b = (const T*)F[NEMO_F_UN_B]; a.vn_b = (const T*)F[NEMO_F_VN_B];
+  a.ub_b = (const T*)F[NEMO_F_UB_B]; a.vb_b = (const T*)F[NEMO_F_VB_B];
+  a.utau = (const T*)F[NEMO_F_UTAU]; a.vtau = (const T*)F[NEMO_F_VTAU];
+  a.utau_b = (const T*)F[NEMO_F_UTAU_B]; a.vtau_b = (const T*)F[NEMO_F_VTAU_B];
+  a.emp = (const T*)F[NEMO_F_EMP]; a.emp_b = (const T*)F[NEMO_F_EMP_B];
+  a.rnf = (const T*)F[NEMO_F_RNF]; a.rnf_b = (const T*)F[NEMO_F_RNF_B];
+  a.rCdU_bot = (const T*)F[NEMO_F_RCDU_BOT]; a.ssh_ib = (const T*)F[NEMO_F_SSH_IB]; a.ssh_ibb = (const T*)F[NEMO_F_SSH_IBB];
+  a.ssha = (double*)F[NEMO_F_SSHA]; a.ua_b = (double*)F[NEMO_F_UA_B]; a.va_b = (double*)F[NEMO_F_VA_B];
+  a.un_adv = (double*)F[NEMO_F_UN_ADV]; a.vn_adv = (double*)F[NEMO_F_VN_ADV];
+  a.ub2_b = (double*)F[NEMO_F_UB2_B]; a.vb2_b = (double*)F[NEMO_F_VB2_B];
+  a.un_bf = (double*)F[NEMO_F_UN_BF]; a.vn_bf = (double*)F[NEMO_F_VN_BF];
+  a.zu_frc = (T*)c->spg_w[0]; a.zv_frc = (T*)c->spg_w[1]; a.zssh_frc = (T*)c->spg_w[2];
+  a.zCdU_u = (T*)c->spg_w[3]; a.zCdU_v = (T*)c->spg_w[4];
+  a.ring_ssh = (T*)c->ring[0]; a.ring_u = (T*)c->ring[1]; a.ring_v = (T*)c->ring[2];
+  a.wgt1 = c->d_wgt1; a.wgt2 = c->d_wgt2;
+  a.ln_bt_fw = nm.ln_bt_fw; a.ln_apr_dyn = nm.ln_apr_dyn; a.nvor = nm.nvor_scheme; a.ll_init = ll_init;
+  a.icycle = c->icycle;
+  // With time averaging every call restarts the barotropic levels, so the ring can
+  // restart at slot 0; without it the levels carry over and the rotation continues.
+  if (ll_init) c->ring0 = 0;
+  a.ring0 = c->ring0;
+  a.phase3_filter = !(kt == nm.nit000 && nm.neuler == 0);
+  a.rdtbt = (T)c->rdtbt; a.grav = (T)nm.grav; a.r1_rau0 = (T)(1.0 / nm.rau0);
+  a.scal_load = (T)nm.rn_scal_load; a.rn_bt_alpha = (T)nm.rn_bt_alpha;
+  a.rn_atfp = nm.rn_atfp; a.r1_2dt_b = 1.0 / z2dt_bf;
+  GridBar bar{c->bar_mem, c->bar_mem + 1, c->err_flag, (unsigned)(c->p2_blocks + c->bar_extra), c->bar_spins};
+  cudaError_t e = launch_spg<T>(dom_now<T>(c), a, bar, c->p2_blocks, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "dyn_spg_ts launch");
+  c->ring0 = (c->ring0 + 3 * c->icycle) & 3;
+  return NEMO_OK;
+}
+
+template <class T>
+int run_hotpath(nemo_ctx* c, int kt) {
+  const nemo_namelist& nm = c->nam;
+  void* const* F = c->f;
+  if (!F[NEMO_F_TSB] || !F[NEMO_F_TSN] || !F[NEMO_F_TSA] || !F[NEMO_F_WN])
+    return fail(c, NEMO_ERR_UNBOUND, "stp_hotpath: tsb, tsn, tsa, un, vn, wn must be bound");
+  auto mark = [&](int i) { if (c->timing) cudaEventRecord(c->tev[i], c->stream); };
+  mark(0);
+  int s = run_spg<T>(c, kt);
+  if (s) return s;
+  mark(1);
+  const double r2dt = (nm.neuler == 0 && kt == nm.nit000) ? nm.rn_rdt : 2.0 * nm.rn_rdt;
+  // tsa = 0 (step.F90:234) folded into the first trend (pta_in = NULL)
+  s = run_fct<T>(c, r2dt, F[NEMO_F_UN], F[NEMO_F_VN], F[NEMO_F_WN], 1, F[NEMO_F_TSB], F[NEMO_F_TSN], nullptr,
+                 F[NEMO_F_TSA], 2, 2, 2);
+  if (s) return s;
+  mark(2);
+  if (nm.ln_traldf_iso)
+    s = run_ldf_iso<T>(c, kt, nm.nit000, F[NEMO_F_AHTU], F[NEMO_F_AHTV], F[NEMO_F_GTSU], F[NEMO_F_GTSV], F[NEMO_F_TSB],
+                       F[NEMO_F_TSB], F[NEMO_F_TSA], 2, 1);
+  else
+    s = run_ldf_lap<T>(c, F[NEMO_F_AHTU], F[NEMO_F_AHTV], F[NEMO_F_GTSU], F[NEMO_F_GTSV], F[NEMO_F_TSB], F[NEMO_F_TSA], 2, 1);
+  if (s) return s;
+  mark(3);
+  s = run_zdf<T>(c, r2dt, F[NEMO_F_TSB], F[NEMO_F_TSA], 2, 0, 1);
+  if (s) return s;
+  if (c->timing) {
+    mark(4);
+    CK(cudaEventSynchronize(c->tev[4]), "timing");
+    for (int i = 0; i < 4; ++i) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, c->tev[i], c->tev[i + 1]);
+      c->tms[i] += ms;
+    }
+    c->tcalls += 1;
+  }
+  return NEMO_OK;
+}
+
+}  // namespace
+
+// ================================================================== C ABI
+extern "C" {
+
+int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmembers, int prec, void* stream,
+                    nemo_ctx** out) {
+  if (!out) return NEMO_ERR_ARG;
+  *out = nullptr;
+  if (!dm || !nam) return NEMO_ERR_ARG;
+  if (nmembers < 1 || (prec != NEMO_PREC_FP64 && prec != NEMO_PREC_MIXED)) return NEMO_ERR_ARG;
+  if (!dm->e1t || !dm->e2t || !dm->e1u || !dm->e2u || !dm->e1v || !dm->e2v || !dm->e1f || !dm->e2f || !dm->ff_f ||
+      !dm->ff_t || !dm->k_top || !dm->k_bot || !dm->e3t_0 || !dm->e3u_0 || !dm->e3v_0 || !dm->e3w_0 || !dm->e3f_0)
+    return NEMO_ERR_ARG;
+  nemo_ctx* c = new nemo_ctx();
+  c->jpi = dm->jpi; c->jpj = dm->jpj; c->jpk = dm->jpk; c->nmem = nmembers; c->prec = prec;
+  c->n2 = (long)c->jpi * c->jpj; c->n3 = c->n2 * c->jpk;
+  c->nam = *nam;
+  auto bad = [&](int code) { nemo_gpu_destroy(c); return code; };
+  if (dm->jpi < 4 || dm->jpj < 4 || dm->jpk < 3 || dm->jpk > KMAX || dm->jpk > 255) return bad(NEMO_ERR_UNSUPPORTED);
+  if (dm->jperio != 0 || nam->ln_isfcav || nam->ln_zad_Aimp) return bad(NEMO_ERR_UNSUPPORTED);
+  if (nam->nvor_scheme < 0 || nam->nvor_scheme > 5) return bad(NEMO_ERR_ARG);
+  if (!nam->ln_linssh) return bad(NEMO_ERR_UNSUPPORTED);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return bad(NEMO_ERR_CUDA);
+  cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (stream) c->stream = (cudaStream_t)stream;
+  else {
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return bad(NEMO_ERR_CUDA);
+    c->own_stream = true;
+  }
+  int s = derive_domain(c, dm);
+  if (s) { fprintf(stderr, "nemo_gpu_create: %s\n", c->err.c_str()); return bad(s); }
+  s = prec == NEMO_PREC_FP64 ? build_dom<double>(c, c->dd) : build_dom<float>(c, c->df);
+  if (s) return bad(s);
+  const size_t es = prec == NEMO_PREC_FP64 ? 8 : 4;
+  const size_t b2 = (size_t)c->n2 * c->nmem * es;
+  for (auto& p : c->spg_w) {
+    if (cudaMalloc(&p, b2) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
+    cudaMemset(p, 0, b2);
+  }
+  for (auto& p : c->ring) {
+    if (cudaMalloc(&p, 4 * b2) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
+    cudaMemset(p, 0, 4 * b2);
+  }
+  if (cudaMalloc(&c->d_wgt1, 3 * (size_t)c->nn_baro * 8) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
+  if (cudaMalloc(&c->d_wgt2, 3 * (size_t)c->nn_baro * 8) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
+  cudaMemcpy(c->d_wgt1, c->wgt1.data(), c->wgt1.size() * 8, cudaMemcpyHostToDevice);
+  cudaMemcpy(c->d_wgt2, c->wgt2.data(), c->wgt2.size() * 8, cudaMemcpyHostToDevice);
+  if (cudaMalloc(&c->bar_mem, 2 * sizeof(unsigned int)) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
+  if (cudaMalloc(&c->err_flag, sizeof(int)) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
+  cudaMemset(c->bar_mem, 0, 2 * sizeof(unsigned int));
+  cudaMemset(c->err_flag, 0, sizeof(int));
+  const int bps = prec == NEMO_PREC_FP64 ? spg_p2_blocks_per_sm<double>() : spg_p2_blocks_per_sm<float>();
+  long need = (c->n2 * c->nmem + 255) / 256;
+  long maxb = (long)bps * c->nsm;
+  c->p2_blocks = (int)(need < maxb ? need : maxb);
+  if (c->p2_blocks < 1) return bad(NEMO_ERR_CUDA);
+  c->gs_nblk = c->nsm * 4;
+  if (cudaMalloc(&c->gs_part, 2 * (size_t)c->gs_nblk * c->nmem * 8) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
+  if (cudaMalloc(&c->gs_out, (size_t)c->nmem * 8) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
+  if (ensure_fct_work(c, 2, 0)) return bad(NEMO_ERR_NOMEM);
+  if (cudaDeviceSynchronize() != cudaSuccess) return bad(NEMO_ERR_CUDA);
+  *out = c;
+  return NEMO_OK;
+}
+
+int nemo_gpu_destroy(nemo_ctx* c) {
+  if (!c) return NEMO_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);
+  free_dom(c->dd);
+  free_dom(c->df);
+  for (auto p : c->fct_w) cudaFree(p);
+  cudaFree(c->fct_ztw);
+  for (auto p : c->spg_w) cudaFree(p);
+  for (auto p : c->ring) cudaFree(p);
+  cudaFree(c->d_wgt1); cudaFree(c->d_wgt2);
+  cudaFree(c->bar_mem); cudaFree(c->err_flag);
+  cudaFree(c->gs_part); cudaFree(c->gs_out);
+  for (auto e : c->tev)
+    if (e) cudaEventDestroy(e);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return NEMO_OK;
+}
+
+const char* nemo_gpu_last_error(const nemo_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int nemo_gpu_synchronize(nemo_ctx* c) {
+  if (!c) return NEMO_ERR_ARG;
+  CK(cudaStreamSynchronize(c->stream), "synchronize");
+  int flag = 0;
+  CK(cudaMemcpy(&flag, c->err_flag, sizeof(int), cudaMemcpyDeviceToHost), "read status");
+  if (flag) {
+    cudaMemset(c->err_flag, 0, sizeof(int));
+    cudaMemset(c->bar_mem, 0, 2 * sizeof(unsigned int));
+    return fail(c, NEMO_ERR_TIMEOUT, "a grid barrier of the barotropic sub-step kernel timed out");
+  }
+  return NEMO_OK;
+}
+
+int nemo_gpu_bind(nemo_ctx* c, int id, void* p) {
+  if (!c || id < 0 || id >= NEMO_F_COUNT) return fail(c, NEMO_ERR_ARG, "bad field id %d", id);
+  c->f[id] = p;
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);
+  c->graphs.clear();
+  return NEMO_OK;
+}
+
+size_t nemo_gpu_field_numel(const nemo_ctx* c, int id) {
+  if (!c || id < 0 || id >= NEMO_F_COUNT) return 0;
+  return field_numel(c, id);
+}
+
+int nemo_gpu_field_is_fp64(const nemo_ctx* c, int id) {
+  if (!c) return 0;
+  return c->prec == NEMO_PREC_FP64 || is_fp64_field(id);
+}
+
+int nemo_gpu_spg_info(const nemo_ctx* c, int* icycle, int* nn_baro, double* rdtbt) {
+  if (!c) return NEMO_ERR_ARG;
+  if (icycle) *icycle = c->icycle;
+  if (nn_baro) *nn_baro = c->nn_baro;
+  if (rdtbt) *rdtbt = c->rdtbt;
+  return NEMO_OK;
+}
+
+int nemo_gpu_field_upload(nemo_ctx* c, int id, const void* host) {
+  if (!c || id < 0 || id >= NEMO_F_COUNT || !host) return fail(c, NEMO_ERR_ARG, "field_upload: bad argument");
+  if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "field_upload: field %d is not bound", id);
+  size_t bytes = field_numel(c, id) * c->nmem * (nemo_gpu_field_is_fp64(c, id) ? 8 : 4);
+  CK(cudaMemcpyAsync(c->f[id], host, bytes, cudaMemcpyHostToDevice, c->stream), "field_upload");
+  return NEMO_OK;
+}
+
+int nemo_gpu_field_download(nemo_ctx* c, int id, void* host) {
+  if (!c || id < 0 || id >= NEMO_F_COUNT || !host) return fail(c, NEMO_ERR_ARG, "field_download: bad argument");
+  if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "field_download: field %d is not bound", id);
+  size_t bytes = field_numel(c, id) * c->nmem * (nemo_gpu_field_is_fp64(c, id) ? 8 : 4);
+  CK(cudaMemcpyAsync(host, c->f[id], bytes, cudaMemcpyDeviceToHost, c->stream), "field_download");
+  return NEMO_OK;
+}
+
+int nemo_gpu_tra_adv_trp(nemo_ctx* c, const void* un, const void* vn, const void* wn, void* zun, void* zvn, void* zwn) {
+  if (!c || !un || !vn || !wn || !zun || !zvn || !zwn) return fail(c, NEMO_ERR_ARG, "tra_adv_trp: null pointer");
+  cudaError_t e = c->prec == NEMO_PREC_FP64
+                      ? launch_adv_trp<double>(dom_now<double>(c), (const double*)un, (const double*)vn,
+                                               (const double*)wn, (double*)zun, (double*)zvn, (double*)zwn, c->stream)
+                      : launch_adv_trp<float>(dom_now<float>(c), (const float*)un, (const float*)vn, (const float*)wn,
+                                              (float*)zun, (float*)zvn, (float*)zwn, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "tra_adv_trp launch");
+  return NEMO_OK;
+}
+
+int nemo_gpu_tra_adv_fct(nemo_ctx* c, int kt, int kit000, const char* cdtype, double p2dt, const void* pun,
+                         const void* pvn, const void* pwn, const void* ptb, const void* ptn, void* pta, int kjpt,
+                         int kn_fct_h, int kn_fct_v) {
+  (void)kt; (void)kit000;
+  if (!c) return NEMO_ERR_ARG;
+  int is_trc = 0;
+  if (int s = check_cdtype(c, cdtype, &is_trc)) return s;
+  if (!pun || !pvn || !pwn || !ptb || !ptn || !pta || kjpt < 1) return fail(c, NEMO_ERR_ARG, "tra_adv_fct: bad argument");
+  if ((kn_fct_h != 2 && kn_fct_h != 4) || (kn_fct_v != 2 && kn_fct_v != 4))
+    return fail(c, NEMO_ERR_ARG, "tra_adv_fct: kn_fct_h/kn_fct_v must be 2 or 4");
+  return c->prec == NEMO_PREC_FP64
+             ? run_fct<double>(c, p2dt, pun, pvn, pwn, 0, ptb, ptn, pta, pta, kjpt, kn_fct_h, kn_fct_v)
+             : run_fct<float>(c, p2dt, pun, pvn, pwn, 0, ptb, ptn, pta, pta, kjpt, kn_fct_h, kn_fct_v);
+}
+
+int nemo_gpu_tra_ldf_lap(nemo_ctx* c, int kt, int kit000, const char* cdtype, const void* pahu, const void* pahv,
+                         const void* pgu, const void* pgv, const void* pgui, const void* pgvi, const void* ptb,
+                         void* pta, int kjpt, int kpass) {
+  (void)kt; (void)kit000; (void)pgui; (void)pgvi;
+  if (!c) return NEMO_ERR_ARG;
+  int is_trc = 0;
+  if (int s = check_cdtype(c, cdtype, &is_trc)) return s;
+  if (!ptb || !pta || kjpt < 1 || (kpass != 1 && kpass != 2)) return fail(c, NEMO_ERR_ARG, "tra_ldf_lap: bad argument");
+  if (c->nam.ln_zps && (!pgu || !pgv)) return fail(c, NEMO_ERR_ARG, "tra_ldf_lap: pgu/pgv required with ln_zps");
+  return c->prec == NEMO_PREC_FP64 ? run_ldf_lap<double>(c, pahu, pahv, pgu, pgv, ptb, pta, kjpt, kpass)
+                                   : run_ldf_lap<float>(c, pahu, pahv, pgu, pgv, ptb, pta, kjpt, kpass);
+}
+
+int nemo_gpu_tra_ldf_iso(nemo_ctx* c, int kt, int kit000, const char* cdtype, const void* pahu, const void* pahv,
+                         const void* pgu, const void* pgv, const void* pgui, const void* pgvi, const void* ptb,
+                         const void* ptbb, void* pta, int kjpt, int kpass) {
+  (void)pgui; (void)pgvi;
+  if (!c) return NEMO_ERR_ARG;
+  int is_trc = 0;
+  if (int s = check_cdtype(c, cdtype, &is_trc)) return s;
+  if (!ptb || !ptbb || !pta || kjpt < 1 || (kpass != 1 && kpass != 2))
+    return fail(c, NEMO_ERR_ARG, "tra_ldf_iso: bad argument");
+  if (c->nam.ln_zps && (!pgu || !pgv)) return fail(c, NEMO_ERR_ARG, "tra_ldf_iso: pgu/pgv required with ln_zps");
+  return c->prec == NEMO_PREC_FP64
+             ? run_ldf_iso<double>(c, kt, kit000, pahu, pahv, pgu, pgv, ptb, ptbb, pta, kjpt, kpass)
+             : run_ldf_iso<float>(c, kt, kit000, pahu, pahv, pgu, pgv, ptb, ptbb, pta, kjpt, kpass);
+}
+
+int nemo_gpu_tra_zdf_imp(nemo_ctx* c, int kt, int kit000, const char* cdtype, double p2dt, const void* ptb, void* pta,
+                         int kjpt) {
+  (void)kt; (void)kit000;
+  if (!c) return NEMO_ERR_ARG;
+  int is_trc = 0;
+  if (int s = check_cdtype(c, cdtype, &is_trc)) return s;
+  if (!ptb || !pta || kjpt < 1) return fail(c, NEMO_ERR_ARG, "tra_zdf_imp: bad argument");
+  return c->prec == NEMO_PREC_FP64 ? run_zdf<double>(c, p2dt, ptb, pta, kjpt, is_trc, 0)
+                                   : run_zdf<float>(c, p2dt, ptb, pta, kjpt, is_trc, 0);
+}
+
+int nemo_gpu_tra_zdf(nemo_ctx* c, int kt) {
+  if (!c) return NEMO_ERR_ARG;
+  const nemo_namelist& nm = c->nam;
+  if (!c->f[NEMO_F_TSB] || !c->f[NEMO_F_TSA]) return fail(c, NEMO_ERR_UNBOUND, "tra_zdf: tsb and tsa must be bound");
+  if (nm.neuler == 0 && kt == nm.nit000) c->r2dt = nm.rn_rdt;
+  else if (kt <= nm.nit000 + 1 || c->r2dt == 0.0) c->r2dt = 2.0 * nm.rn_rdt;
+  int s = c->prec == NEMO_PREC_FP64 ? run_zdf<double>(c, c->r2dt, c->f[NEMO_F_TSB], c->f[NEMO_F_TSA], 2, 0, 0)
+                                    : run_zdf<float>(c, c->r2dt, c->f[NEMO_F_TSB], c->f[NEMO_F_TSA], 2, 0, 0);
+  if (s) return s;
+  // WHERE( tsa(:,:,:,jp_sal) < 0 ) tsa = 0.1 on every member's salinity slice
+  for (int m = 0; m < c->nmem; ++m) {
+    cudaError_t e = c->prec == NEMO_PREC_FP64
+                        ? launch_clamp<double>((double*)c->f[NEMO_F_TSA] + (2L * m + 1) * c->n3, c->n3, c->stream)
+                        : launch_clamp<float>((float*)c->f[NEMO_F_TSA] + (2L * m + 1) * c->n3, c->n3, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "tra_zdf clamp");
+  }
+  return NEMO_OK;
+}
+
+int nemo_gpu_dyn_spg_ts(nemo_ctx* c, int kt) {
+  if (!c) return NEMO_ERR_ARG;
+  return c->prec == NEMO_PREC_FP64 ? run_spg<double>(c, kt) : run_spg<float>(c, kt);
+}
+
+int nemo_gpu_lbc_lnk(nemo_ctx* c, const char* cdname, void* ptab, int nk, int nl, const char* cd_nat, double psgn,
+                     double pval, int is_fp64) {
+  (void)cdname; (void)psgn;
+  if (!c || !ptab || nk < 1 || nl < 1 || !cd_nat) return fail(c, NEMO_ERR_ARG, "lbc_lnk: bad argument");
+  const char n = cd_nat[0];
+  if (n != 'T' && n != 'U' && n != 'V' && n != 'W' && n != 'F') return fail(c, NEMO_ERR_ARG, "lbc_lnk: bad grid nature");
+  const long nslab = (long)nk * nl * c->nmem;
+  cudaError_t e = is_fp64 ? launch_lbc<double>((double*)ptab, c->jpi, c->jpj, nslab, n == 'F', pval, c->stream)
+                          : launch_lbc<float>((float*)ptab, c->jpi, c->jpj, nslab, n == 'F', (float)pval, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "lbc_lnk launch");
+  return NEMO_OK;
+}
+
+int nemo_gpu_lbc_lnk_multi(nemo_ctx* c, const char* cdname, int kfld, void* const* ptabs, const int* nk,
+                           const char* cd_nats, const double* psgns, double pval, int is_fp64) {
+  if (!c || kfld < 1 || kfld > 9 || !ptabs || !nk || !cd_nats || !psgns) return fail(c, NEMO_ERR_ARG, "lbc_lnk_multi: bad argument");
+  for (int f = 0; f < kfld; ++f) {
+    char nat[2] = {cd_nats[f], 0};
+    int s = nemo_gpu_lbc_lnk(c, cdname, ptabs[f], nk[f], 1, nat, psgns[f], pval, is_fp64);
+    if (s) return s;
+  }
+  return NEMO_OK;
+}
+
+int nemo_gpu_glob_sum(nemo_ctx* c, const char* cdname, const void* ptab, int nk, int is_fp64, double* out) {
+  (void)cdname;
+  if (!c || !ptab || nk < 1 || !out) return fail(c, NEMO_ERR_ARG, "glob_sum: bad argument");
+  const double* tmi = c->prec == NEMO_PREC_FP64 ? c->dd.d.tmask_i : c->df.d.tmask_i;
+  cudaError_t e = is_fp64 ? launch_globsum<double>((const double*)ptab, tmi, c->n2, nk, c->nmem, c->gs_part, c->gs_nblk,
+                                                   c->gs_out, c->stream)
+                          : launch_globsum<float>((const float*)ptab, tmi, c->n2, nk, c->nmem, c->gs_part, c->gs_nblk,
+                                                  c->gs_out, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "glob_sum launch");
+  CK(cudaMemcpyAsync(out, c->gs_out, (size_t)c->nmem * 8, cudaMemcpyDeviceToHost, c->stream), "glob_sum result");
+  CK(cudaStreamSynchronize(c->stream), "glob_sum");
+  return NEMO_OK;
+}
+
+int nemo_gpu_stp_hotpath(nemo_ctx* c, int kt) {
+  if (!c) return NEMO_ERR_ARG;
+  const nemo_namelist& nm = c->nam;
+  // class of kt: the Euler/leapfrog start steps differ in scalars and weights
+  const int cls = kt == nm.nit000 ? 0 : (kt == nm.nit000 + 1 ? 1 : 2);
+  const bool carry = !nm.ln_bt_av;  // ring rotation carries across calls: no replay
+  if (cls == 2 && c->graphs_ok && !carry && !c->timing) {
+    auto it = c->graphs.find(cls);
+    if (it != c->graphs.end()) {
+      CK(cudaGraphLaunch(it->second, c->stream), "graph launch");
+      return NEMO_OK;
+    }
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      int s = c->prec == NEMO_PREC_FP64 ? run_hotpath<double>(c, kt) : run_hotpath<float>(c, kt);
+      cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
+      cudaGraphExec_t ex = nullptr;
+      if (s == NEMO_OK && ee == cudaSuccess && g && cudaGraphInstantiate(&ex, g, 0) == cudaSuccess) {
+        cudaGraphDestroy(g);
+        c->graphs[cls] = ex;
+        CK(cudaGraphLaunch(ex, c->stream), "graph launch");
+        return NEMO_OK;
+      }
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      if (s != NEMO_OK) return s;
+    }
+    c->graphs_ok = false;  // capture unavailable: direct launches from now on
+    cudaGetLastError();
+  }
+  return c->prec == NEMO_PREC_FP64 ? run_hotpath<double>(c, kt) : run_hotpath<float>(c, kt);
+}
+
+int nemo_gpu_set_timing(nemo_ctx* c, int on) {
+  if (!c) return NEMO_ERR_ARG;
+  if (on && !c->tev[0])
+    for (auto& e : c->tev) CK(cudaEventCreate(&e), "timing events");
+  c->timing = on != 0;
+  for (double& t : c->tms) t = 0.0;
+  c->tcalls = 0;
+  return NEMO_OK;
+}
+
+int nemo_gpu_get_timing(nemo_ctx* c, double* ms, int* ncalls) {
+  if (!c || !ms) return NEMO_ERR_ARG;
+  for (int i = 0; i < 4; ++i) ms[i] = c->tms[i];
+  if (ncalls) *ncalls = c->tcalls;
+  return NEMO_OK;
+}
+
+int nemo_gpu_set_barrier_limit(nemo_ctx* c, long long max_spins, int extra_arrivals) {
+  if (!c || max_spins < 1 || extra_arrivals < 0) return fail(c, NEMO_ERR_ARG, "set_barrier_limit: bad argument");
+  c->bar_spins = max_spins;
+  c->bar_extra = extra_arrivals;
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);
+  c->graphs.clear();
+  return NEMO_OK;
+}
+
+}  // extern "C"

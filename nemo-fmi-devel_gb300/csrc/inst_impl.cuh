@@ -1,0 +1,118 @@
+// inst_impl.cuh -- definitions of the launchers declared in launch.h; included by
+// inst_fp64.cu and inst_fp32.cu, each of which instantiates one precision.
+#pragma once
+#include "launch.h"
+
+namespace nemo {
+
+constexpr int BX = 32, BY = 4;
+
+template <class T>
+static dim3 col_grid(const Dom<T>& d) {
+  return dim3((d.jpi + BX - 1) / BX, (d.jpj + BY - 1) / BY, d.nmem);
+}
+
+template <class T>
+cudaError_t launch_adv_trp(const Dom<T>& d, const T* un, const T* vn, const T* wn, T* zun, T* zvn, T* zwn,
+                           cudaStream_t s) {
+  k_adv_trp<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, un, vn, wn, zun, zvn, zwn);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_fct(const Dom<T>& d, const FctArgs<T>& a, cudaStream_t s) {
+  if (a.kn_fct_v == 4) {
+    k_interp4<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a.ptn, const_cast<T*>(a.ztw), a.kjpt);
+  }
+  k_fct_a<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  k_fct_b<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  k_fct_c<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_ldf_lap(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s) {
+  k_ldf_lap<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_ldf_iso(const Dom<T>& d, const LdfArgs<T>& a, int copy_akz_edges, int msc_edges, cudaStream_t s) {
+  k_ldf_iso<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  if (copy_akz_edges) k_iso_akz_copy_edges<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  if (msc_edges) k_iso_msc_edges<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_zdf(const Dom<T>& d, const ZdfArgs<T>& a, cudaStream_t s) {
+  k_zdf_imp<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_clamp(T* x, long n, cudaStream_t s) {
+  long nb = (n + 255) / 256;
+  if (nb > 152L * 16) nb = 152L * 16;
+  if (nb < 1) nb = 1;
+  k_clamp_neg<T><<<(unsigned)nb, 256, 0, s>>>(x, n);
+  return cudaGetLastError();
+}
+
+template <class T>
+int spg_p2_blocks_per_sm() {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_spg_p2<T>, 256, 0) != cudaSuccess) return 0;
+  return nb;
+}
+
+template <class T>
+cudaError_t launch_spg(const Dom<T>& d, const SpgArgs<T>& a, const GridBar& bar, int p2_blocks, cudaStream_t s) {
+  k_spg_p1a<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  k_spg_p1b<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(p2_blocks);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaError_t e = cudaLaunchKernelEx(&cfg, k_spg_p2<T>, d, a, bar);
+  if (e != cudaSuccess) return e;
+  k_spg_p3<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_lbc(T* p, int jpi, int jpj, long nslab, int is_f, T pval, cudaStream_t s) {
+  long per = 2L * jpi + 2L * jpj;
+  unsigned gx = (unsigned)((per + 255) / 256);
+  unsigned gy = (unsigned)(nslab < 65535 ? nslab : 65535);
+  k_lbc_closed<T><<<dim3(gx, gy), 256, 0, s>>>(p, jpi, jpj, nslab, is_f, pval);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_globsum(const T* x, const double* tmask_i, long n2, int nk, int nmem, double* part, int nblk,
+                           double* out, cudaStream_t s) {
+  k_globsum_partial<T><<<dim3(nblk, nmem), 256, 0, s>>>(x, tmask_i, n2, nk, part);
+  k_globsum_final<<<nmem, 256, 0, s>>>(part, nblk, out);
+  return cudaGetLastError();
+}
+
+#define NEMO_INSTANTIATE(T)                                                                                   \
+  template cudaError_t launch_adv_trp<T>(const Dom<T>&, const T*, const T*, const T*, T*, T*, T*, cudaStream_t); \
+  template cudaError_t launch_fct<T>(const Dom<T>&, const FctArgs<T>&, cudaStream_t);                        \
+  template cudaError_t launch_ldf_lap<T>(const Dom<T>&, const LdfArgs<T>&, cudaStream_t);                    \
+  template cudaError_t launch_ldf_iso<T>(const Dom<T>&, const LdfArgs<T>&, int, int, cudaStream_t);          \
+  template cudaError_t launch_zdf<T>(const Dom<T>&, const ZdfArgs<T>&, cudaStream_t);                        \
+  template cudaError_t launch_clamp<T>(T*, long, cudaStream_t);                                              \
+  template cudaError_t launch_spg<T>(const Dom<T>&, const SpgArgs<T>&, const GridBar&, int, cudaStream_t);   \
+  template int spg_p2_blocks_per_sm<T>();                                                                    \
+  template cudaError_t launch_lbc<T>(T*, int, int, long, int, T, cudaStream_t);                              \
+  template cudaError_t launch_globsum<T>(const T*, const double*, long, int, int, double*, int, double*, cudaStream_t);
+
+}  // namespace nemo

@@ -1,0 +1,427 @@
+// k_dyn.cuh -- split-explicit free surface (dyn_spg_ts, dynspg_ts.F90:121-1310) for a
+// linear free surface, plus lbc_lnk and the compensated global sum.
+//
+// Phase 1 (forcing of the 2-D system) and phase 3 (correction of the 3-D fields)
+// are column kernels. Phase 2, the icycle barotropic sub-steps, is ONE persistent
+// cooperative kernel: each sub-step is two grid-wide stages separated by a bounded
+// grid barrier (after ssha_e, after ua_e/va_e). The three time levels of ssh, u, v
+// and the new level live in a ring of 4 slots, so the reference's swap
+// (:1176-1186) is an index rotation and no stage overwrites a level a neighbouring
+// point still reads. T is the bulk type; the time-filter accumulators ssha, ua_b,
+// va_b, un_adv, vn_adv (and the restart fields ub2_b, vb2_b, un_bf, vn_bf) are FP64
+// in both precision modes.
+#pragma once
+#include "nemo_common.cuh"
+
+namespace nemo {
+
+template <class T>
+struct SpgArgs {
+  // 3-D
+  T *ua, *va, *un, *vn;
+  const T *ub, *vb;
+  // 2-D inputs
+  const T *sshn, *sshb, *un_b, *vn_b, *ub_b, *vb_b;
+  const T *utau, *vtau, *utau_b, *vtau_b, *emp, *emp_b, *rnf, *rnf_b;
+  const T *rCdU_bot, *ssh_ib, *ssh_ibb;
+  // FP64 accumulators / restart fields
+  double *ssha, *ua_b, *va_b, *un_adv, *vn_adv, *ub2_b, *vb2_b, *un_bf, *vn_bf;
+  // library work arrays (2-D, per member)
+  T *zu_frc, *zv_frc, *zssh_frc, *zCdU_u, *zCdU_v;
+  T *ring_ssh, *ring_u, *ring_v;  // 4 slots each
+  const double *wgt1, *wgt2;
+  int ln_bt_fw, ln_apr_dyn, nvor, ll_init, icycle, ring0, phase3_filter;
+  T rdtbt, grav, r1_rau0, scal_load, rn_bt_alpha;
+  double rn_atfp, r1_2dt_b;
+};
+
+template <class T>
+__device__ __forceinline__ long pt_ij(const Dom<T>& d, int i, int j) { return (long)(i - 1) + (long)(j - 1) * d.jpi; }
+
+// ---------------------------------------------------------------------------------
+// Phase 1a (:358-378): zu_frc = SUM_k e3u*ua*umask * r1_hu_n, then ua -= zu_frc*umask
+// on the interior. One thread per column, all columns.
+template <class T>
+__global__ void k_spg_p1a(Dom<T> d, SpgArgs<T> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int m = blockIdx.z;
+  if (i > d.jpi || j > d.jpj) return;
+  const long ij = pt_ij(d, i, j), n2 = d.n2, m3 = (long)m * d.n3, m2 = (long)m * n2;
+  const ColInfo ci = d.ci[ij];
+  T su = T(0), sv = T(0);
+  for (int k = 1; k <= d.jpk - 1; ++k) {
+    const long q = m3 + ij + (long)(k - 1) * n2;
+    su = su + d.e3u_n(ij, k, m) * a.ua[q] * umsk<T>(ci, k);
+    sv = sv + d.e3v_n(ij, k, m) * a.va[q] * vmsk<T>(ci, k);
+  }
+  su = su * d.r1_hu_0[ij];
+  sv = sv * d.r1_hv_0[ij];
+  a.zu_frc[m2 + ij] = su;
+  a.zv_frc[m2 + ij] = sv;
+  if (i >= 2 && i <= d.jpi - 1 && j >= 2 && j <= d.jpj - 1)
+    for (int k = 1; k <= d.jpk - 1; ++k) {
+      const long q = m3 + ij + (long)(k - 1) * n2;
+      a.ua[q] = a.ua[q] - su * umsk<T>(ci, k);
+      a.va[q] = a.va[q] - sv * vmsk<T>(ci, k);
+    }
+}
+
+// Barotropic Coriolis trend of a flux field (ENE/MIX, ENS, EET/EEN, ENT) at an
+// interior point (:390-443 and :1000-1056). fx/fy return the fluxes zwx/zwy at a
+// point; for ENT fu/fv return the velocities and hu/hv the inverse depths.
+template <class T, class FX, class FY, class FU, class FV>
+__device__ __forceinline__ void coriolis(const Dom<T>& d, int nvor, long p, FX fx, FY fy, FU fu, FV fv, T z1_hu,
+                                         T z1_hv, T& zu_trd, T& zv_trd) {
+  const int jpi = d.jpi;
+  const T r1_4 = T(0.25), r1_8 = T(0.125), r1_12 = T(1) / T(12);
+  if (nvor == 2) {  // ENT
+    const T* e = d.e1e2t;
+    const T* h = d.ht_0;
+    const T* ft = d.ff_t;
+    zu_trd = +r1_4 * d.r1_e1e2u[p] * z1_hu *
+             (e[p + 1] * h[p + 1] * ft[p + 1] * (fv(p + 1) + fv(p + 1 - jpi)) + e[p] * h[p] * ft[p] * (fv(p) + fv(p - jpi)));
+    zv_trd = -r1_4 * d.r1_e1e2v[p] * z1_hv *
+             (e[p + jpi] * h[p + jpi] * ft[p + jpi] * (fu(p + jpi) + fu(p - 1 + jpi)) + e[p] * h[p] * ft[p] * (fu(p) + fu(p - 1)));
+  } else if (nvor == 1 || nvor == 5) {  // ENE, MIX
+    const T zy1 = (fy(p - jpi) + fy(p + 1 - jpi)) * d.r1_e1u[p];
+    const T zy2 = (fy(p) + fy(p + 1)) * d.r1_e1u[p];
+    const T zx1 = (fx(p - 1) + fx(p - 1 + jpi)) * d.r1_e2v[p];
+    const T zx2 = (fx(p) + fx(p + jpi)) * d.r1_e2v[p];
+    zu_trd = r1_4 * (d.zwz[p - jpi] * zy1 + d.zwz[p] * zy2);
+    zv_trd = -r1_4 * (d.zwz[p - 1] * zx1 + d.zwz[p] * zx2);
+  } else if (nvor == 0) {  // ENS
+    const T zy1 = r1_8 * (fy(p - jpi) + fy(p + 1 - jpi) + fy(p) + fy(p + 1)) * d.r1_e1u[p];
+    const T zx1 = -r1_8 * (fx(p - 1) + fx(p - 1 + jpi) + fx(p) + fx(p + jpi)) * d.r1_e2v[p];
+    zu_trd = zy1 * (d.zwz[p - jpi] + d.zwz[p]);
+    zv_trd = zx1 * (d.zwz[p - 1] + d.zwz[p]);
+  } else {  // EET, EEN
+    zu_trd = +r1_12 * d.r1_e1u[p] *
+             (d.ftne[p] * fy(p) + d.ftnw[p + 1] * fy(p + 1) + d.ftse[p] * fy(p - jpi) + d.ftsw[p + 1] * fy(p + 1 - jpi));
+    zv_trd = -r1_12 * d.r1_e2v[p] *
+             (d.ftsw[p + jpi] * fx(p - 1 + jpi) + d.ftse[p + jpi] * fx(p + jpi) + d.ftnw[p] * fx(p - 1) + d.ftne[p] * fx(p));
+  }
+}
+
+// Phase 1b (:387-702): Coriolis of the now barotropic flow, bottom stress, wind,
+// atmospheric pressure, ssh forcing, initial barotropic levels, zeroed sums.
+template <class T>
+__global__ void k_spg_p1b(Dom<T> d, SpgArgs<T> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int m = blockIdx.z;
+  if (i > d.jpi || j > d.jpj) return;
+  const long p = pt_ij(d, i, j), n2 = d.n2, m2 = (long)m * n2, m3 = (long)m * d.n3;
+  const T r1_2 = T(0.5);
+  const bool interior = i >= 2 && i <= d.jpi - 1 && j >= 2 && j <= d.jpj - 1;
+  if (interior) {
+    const T* unb = a.un_b + m2;
+    const T* vnb = a.vn_b + m2;
+    auto fx = [&](long q) -> T { return unb[q] * d.hu_0[q] * d.e2u[q]; };
+    auto fy = [&](long q) -> T { return vnb[q] * d.hv_0[q] * d.e1v[q]; };
+    auto fu = [&](long q) -> T { return unb[q]; };
+    auto fv = [&](long q) -> T { return vnb[q]; };
+    T zu_trd, zv_trd;
+    coriolis(d, a.nvor, p, fx, fy, fu, fv, d.r1_hu_0[p], d.r1_hv_0[p], zu_trd, zv_trd);
+    T zu = a.zu_frc[m2 + p] - zu_trd * d.ssumask[p];
+    T zv = a.zv_frc[m2 + p] - zv_trd * d.ssvmask[p];
+    // bottom stress from the baroclinic bottom velocity (:519-557)
+    const ColInfo ci = d.ci[p];
+    const long qu = m3 + p + (long)(ci.mbku - 1) * n2, qv = m3 + p + (long)(ci.mbkv - 1) * n2;
+    T zwx, zwy;
+    if (a.ln_bt_fw) { zwx = a.un[qu] - unb[p]; zwy = a.vn[qv] - vnb[p]; }
+    else { zwx = a.ub[qu] - a.ub_b[m2 + p]; zwy = a.vb[qv] - a.vb_b[m2 + p]; }
+    const T* cdu = a.rCdU_bot + m2;
+    zu = zu + d.r1_hu_0[p] * r1_2 * (cdu[p + 1] + cdu[p]) * zwx;
+    zv = zv + d.r1_hv_0[p] * r1_2 * (cdu[p + d.jpi] + cdu[p]) * zwy;
+    // wind (:589-604)
+    if (a.ln_bt_fw) {
+      zu = zu + a.r1_rau0 * a.utau[m2 + p] * d.r1_hu_0[p];
+      zv = zv + a.r1_rau0 * a.vtau[m2 + p] * d.r1_hv_0[p];
+    } else {
+      const T zztmp = a.r1_rau0 * r1_2;
+      zu = zu + zztmp * (a.utau_b[m2 + p] + a.utau[m2 + p]) * d.r1_hu_0[p];
+      zv = zv + zztmp * (a.vtau_b[m2 + p] + a.vtau[m2 + p]) * d.r1_hv_0[p];
+    }
+    // atmospheric pressure (:606-629)
+    if (a.ln_apr_dyn) {
+      const T* ib = a.ssh_ib + m2;
+      T zu_spg, zv_spg;
+      if (a.ln_bt_fw) {
+        zu_spg = a.grav * (ib[p + 1] - ib[p]) * d.r1_e1u[p];
+        zv_spg = a.grav * (ib[p + d.jpi] - ib[p]) * d.r1_e2v[p];
+      } else {
+        const T* ibb = a.ssh_ibb + m2;
+        const T zztmp = a.grav * r1_2;
+        zu_spg = zztmp * (ib[p + 1] - ib[p] + ibb[p + 1] - ibb[p]) * d.r1_e1u[p];
+        zv_spg = zztmp * (ib[p + d.jpi] - ib[p] + ibb[p + d.jpi] - ibb[p]) * d.r1_e2v[p];
+      }
+      zu = zu + zu_spg;
+      zv = zv + zv_spg;
+    }
+    a.zu_frc[m2 + p] = zu;
+    a.zv_frc[m2 + p] = zv;
+    a.zCdU_u[m2 + p] = r1_2 * (cdu[p + 1] + cdu[p]);
+    a.zCdU_v[m2 + p] = r1_2 * (cdu[p + d.jpi] + cdu[p]);
+  }
+  // ssh forcing (:633-639); rnf / fwfisf are 0 when absent
+  {
+    const T r = a.rnf ? a.rnf[m2 + p] : T(0);
+    T f;
+    if (a.ln_bt_fw) f = a.r1_rau0 * (a.emp[m2 + p] - r + T(0));
+    else {
+      const T rb = a.rnf_b ? a.rnf_b[m2 + p] : T(0);
+      f = a.r1_rau0 * r1_2 * (a.emp[m2 + p] + a.emp_b[m2 + p] - r - rb + T(0) + T(0));
+    }
+    a.zssh_frc[m2 + p] = f;
+  }
+  // initial barotropic levels (:665-693) in ring slots n = ring0, b, bb
+  const long nmem2 = (long)d.nmem * n2;
+  const int sn = a.ring0 & 3, sb = (a.ring0 + 1) & 3, sbb = (a.ring0 + 2) & 3;
+  if (a.ll_init) {
+    a.ring_ssh[sbb * nmem2 + m2 + p] = T(0); a.ring_u[sbb * nmem2 + m2 + p] = T(0); a.ring_v[sbb * nmem2 + m2 + p] = T(0);
+    a.ring_ssh[sb * nmem2 + m2 + p] = T(0); a.ring_u[sb * nmem2 + m2 + p] = T(0); a.ring_v[sb * nmem2 + m2 + p] = T(0);
+  }
+  if (a.ln_bt_fw) {
+    a.ring_ssh[sn * nmem2 + m2 + p] = a.sshn[m2 + p];
+    a.ring_u[sn * nmem2 + m2 + p] = a.un_b[m2 + p];
+    a.ring_v[sn * nmem2 + m2 + p] = a.vn_b[m2 + p];
+  } else {
+    a.ring_ssh[sn * nmem2 + m2 + p] = a.sshb[m2 + p];
+    a.ring_u[sn * nmem2 + m2 + p] = a.ub_b[m2 + p];
+    a.ring_v[sn * nmem2 + m2 + p] = a.vb_b[m2 + p];
+  }
+  a.ua_b[m2 + p] = 0.0; a.va_b[m2 + p] = 0.0; a.ssha[m2 + p] = 0.0;
+  a.un_adv[m2 + p] = 0.0; a.vn_adv[m2 + p] = 0.0;
+}
+
+// Predictor (AB3) and AM4 coefficients of sub-step jn (:724-732, :904-928).
+template <class T>
+__device__ __forceinline__ void ab3(int jn, int ll_init, T& za1, T& za2, T& za3) {
+  if (jn < 3 && ll_init) { za1 = T(1); za2 = T(0); za3 = T(0); }
+  else { za1 = T(1.781105); za2 = T(-1.06221); za3 = T(0.281105); }
+}
+template <class T>
+__device__ __forceinline__ void am4(int jn, int ll_init, T alpha, T& za0, T& za1, T& za2, T& za3) {
+  if (jn == 1 && ll_init) { za0 = T(1); za1 = T(0); za2 = T(0); za3 = T(0); }
+  else if (jn == 2 && ll_init) { za0 = T(1.0833333333333); za1 = T(-0.1666666666666); za2 = T(0.0833333333333); za3 = T(0); }
+  else if (alpha == T(0)) { za0 = T(0.614); za1 = T(0.285); za2 = T(0.088); za3 = T(0.013); }
+  else {
+    const T zepsilon = T(0.00976186) - T(0.13451357) * alpha;
+    const T zgamma = T(0.08344500) - T(0.51358400) * alpha;
+    za0 = T(0.5) + zgamma + T(2) * alpha + T(2) * zepsilon;
+    za1 = T(1) - za0 - zgamma - zepsilon;
+    za2 = zgamma;
+    za3 = zepsilon;
+  }
+}
+
+// Phase 2: the icycle sub-steps (:712-1207) in one persistent kernel.
+template <class T>
+__global__ void __launch_bounds__(256) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar bar) {
+  const long n2 = d.n2, nmem2 = (long)d.nmem * n2;
+  const int jpi = d.jpi, jpj = d.jpj;
+  const long tid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long nth = (long)gridDim.x * blockDim.x;
+  const T grav = a.grav, rdtbt = a.rdtbt;
+  int r = a.ring0;
+  for (int jn = 1; jn <= a.icycle; ++jn) {
+    const int sn = r & 3, sb = (r + 1) & 3, sbb = (r + 2) & 3, sa = (r + 3) & 3;
+    T za1, za2, za3;
+    ab3(jn, a.ll_init, za1, za2, za3);
+    const double w2 = a.wgt2[jn - 1], w1 = a.wgt1[jn - 1];
+    // ---- stage 1: fluxes, un_adv sums, ssha_e (:735-879)
+    for (long g = tid; g < nmem2; g += nth) {
+      const long m2 = (g / n2) * n2, p = g - m2;
+      const int i = (int)(p % jpi) + 1, j = (int)(p / jpi) + 1;
+      const T* un_e = a.ring_u + sn * nmem2 + m2;
+      const T* ub_e = a.ring_u + sb * nmem2 + m2;
+      const T* ubb_e = a.ring_u + sbb * nmem2 + m2;
+      const T* vn_e = a.ring_v + sn * nmem2 + m2;
+      const T* vb_e = a.ring_v + sb * nmem2 + m2;
+      const T* vbb_e = a.ring_v + sbb * nmem2 + m2;
+      auto zwx = [&](long q) -> T { return d.e2u[q] * (za1 * un_e[q] + za2 * ub_e[q] + za3 * ubb_e[q]) * d.hu_0[q]; };
+      auto zwy = [&](long q) -> T { return d.e1v[q] * (za1 * vn_e[q] + za2 * vb_e[q] + za3 * vbb_e[q]) * d.hv_0[q]; };
+      const T wx = zwx(p), wy = zwy(p);
+      a.un_adv[m2 + p] = a.un_adv[m2 + p] + (double)(T(w2) * wx * d.r1_e2u[p]);
+      a.vn_adv[m2 + p] = a.vn_adv[m2 + p] + (double)(T(w2) * wy * d.r1_e1v[p]);
+      T ssha_e = T(0);
+      if (i >= 2 && i <= jpi - 1 && j >= 2 && j <= jpj - 1) {
+        const T zhdiv = (wx - zwx(p - 1) + wy - zwy(p - jpi)) * d.r1_e1e2t[p];
+        ssha_e = (a.ring_ssh[sn * nmem2 + m2 + p] - rdtbt * (a.zssh_frc[m2 + p] + zhdiv)) * d.ssmask[p];
+      }
+      a.ring_ssh[sa * nmem2 + m2 + p] = ssha_e;
+    }
+    if (!grid_barrier(bar)) return;
+    // ---- stage 2: AM4 ssh, Coriolis, drag, pressure gradient, ua_e, sums (:904-1204)
+    T zb0, zb1, zb2, zb3;
+    am4(jn, a.ll_init, a.rn_bt_alpha, zb0, zb1, zb2, zb3);
+    for (long g = tid; g < nmem2; g += nth) {
+      const long m2 = (g / n2) * n2, p = g - m2;
+      const int i = (int)(p % jpi) + 1, j = (int)(p / jpi) + 1;
+      T ua_e = T(0), va_e = T(0);
+      if (i >= 2 && i <= jpi - 1 && j >= 2 && j <= jpj - 1) {
+        const T* un_e = a.ring_u + sn * nmem2 + m2;
+        const T* ub_e = a.ring_u + sb * nmem2 + m2;
+        const T* ubb_e = a.ring_u + sbb * nmem2 + m2;
+        const T* vn_e = a.ring_v + sn * nmem2 + m2;
+        const T* vb_e = a.ring_v + sb * nmem2 + m2;
+        const T* vbb_e = a.ring_v + sbb * nmem2 + m2;
+        const T* sa_ = a.ring_ssh + sa * nmem2 + m2;
+        const T* sn_ = a.ring_ssh + sn * nmem2 + m2;
+        const T* sb_ = a.ring_ssh + sb * nmem2 + m2;
+        const T* sbb_ = a.ring_ssh + sbb * nmem2 + m2;
+        auto uext = [&](long q) -> T { return za1 * un_e[q] + za2 * ub_e[q] + za3 * ubb_e[q]; };
+        auto vext = [&](long q) -> T { return za1 * vn_e[q] + za2 * vb_e[q] + za3 * vbb_e[q]; };
+        auto zwx = [&](long q) -> T { return d.e2u[q] * uext(q) * d.hu_0[q]; };
+        auto zwy = [&](long q) -> T { return d.e1v[q] * vext(q) * d.hv_0[q]; };
+        auto sp2 = [&](long q) -> T { return zb0 * sa_[q] + zb1 * sn_[q] + zb2 * sb_[q] + zb3 * sbb_[q]; };
+        const T z1_hu = d.ssumask[p] / (d.hu_0[p] + T(1) - d.ssumask[p]);
+        const T z1_hv = d.ssvmask[p] / (d.hv_0[p] + T(1) - d.ssvmask[p]);
+        T zu_trd, zv_trd;
+        coriolis(d, a.nvor, p, zwx, zwy, uext, vext, z1_hu, z1_hv, zu_trd, zv_trd);
+        zu_trd = zu_trd + a.zCdU_u[m2 + p] * un_e[p] * d.r1_hu_0[p];
+        zv_trd = zv_trd + a.zCdU_v[m2 + p] * vn_e[p] * d.r1_hv_0[p];
+        const T s0 = sp2(p);
+        const T zu_spg = -grav * (sp2(p + 1) - s0) * d.r1_e1u[p];
+        const T zv_spg = -grav * (sp2(p + jpi) - s0) * d.r1_e2v[p];
+        const T wxs = (T(1) - a.scal_load) * zu_spg;
+        const T wys = (T(1) - a.scal_load) * zv_spg;
+        ua_e = (un_e[p] + rdtbt * (wxs + zu_trd + a.zu_frc[m2 + p])) * d.ssumask[p];
+        va_e = (vn_e[p] + rdtbt * (wys + zv_trd + a.zv_frc[m2 + p])) * d.ssvmask[p];
+      }
+      a.ring_u[sa * nmem2 + m2 + p] = ua_e;
+      a.ring_v[sa * nmem2 + m2 + p] = va_e;
+      a.ua_b[m2 + p] = a.ua_b[m2 + p] + w1 * (double)ua_e;
+      a.va_b[m2 + p] = a.va_b[m2 + p] + w1 * (double)va_e;
+      a.ssha[m2 + p] = a.ssha[m2 + p] + w1 * (double)a.ring_ssh[sa * nmem2 + m2 + p];
+    }
+    r = (r + 3) & 3;
+    if (!grid_barrier(bar)) return;
+  }
+}
+
+// Phase 3 (:1214-1269): time-filtered transports, baroclinic trend update and the
+// correction of the now velocities. One thread per column, all columns.
+template <class T>
+__global__ void k_spg_p3(Dom<T> d, SpgArgs<T> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int m = blockIdx.z;
+  if (i > d.jpi || j > d.jpj) return;
+  const long p = pt_ij(d, i, j), n2 = d.n2, m2 = (long)m * n2, m3 = (long)m * d.n3;
+  double uadv = a.un_adv[m2 + p], vadv = a.vn_adv[m2 + p];
+  if (a.ln_bt_fw) {
+    const double zwx = uadv, zwy = vadv;
+    if (a.phase3_filter) {
+      uadv = 0.5 * (a.ub2_b[m2 + p] + zwx - a.rn_atfp * a.un_bf[m2 + p]);
+      vadv = 0.5 * (a.vb2_b[m2 + p] + zwy - a.rn_atfp * a.vn_bf[m2 + p]);
+      a.un_bf[m2 + p] = a.rn_atfp * a.un_bf[m2 + p] + (zwx - a.ub2_b[m2 + p]);
+      a.vn_bf[m2 + p] = a.rn_atfp * a.vn_bf[m2 + p] + (zwy - a.vb2_b[m2 + p]);
+    } else {
+      a.un_bf[m2 + p] = 0.0;
+      a.vn_bf[m2 + p] = 0.0;
+    }
+    a.ub2_b[m2 + p] = zwx;
+    a.vb2_b[m2 + p] = zwy;
+    a.un_adv[m2 + p] = uadv;
+    a.vn_adv[m2 + p] = vadv;
+  }
+  const T du = (T)((a.ua_b[m2 + p] - (double)a.ub_b[m2 + p]) * a.r1_2dt_b);
+  const T dv = (T)((a.va_b[m2 + p] - (double)a.vb_b[m2 + p]) * a.r1_2dt_b);
+  const T cu = (T)(uadv * (double)d.r1_hu_0[p]);
+  const T cv = (T)(vadv * (double)d.r1_hv_0[p]);
+  const T unb = a.un_b[m2 + p], vnb = a.vn_b[m2 + p];
+  const ColInfo ci = d.ci[p];
+  for (int k = 1; k <= d.jpk - 1; ++k) {
+    const long q = m3 + p + (long)(k - 1) * n2;
+    a.ua[q] = a.ua[q] + du;
+    a.va[q] = a.va[q] + dv;
+    a.un[q] = (a.un[q] + cu - unb) * umsk<T>(ci, k);
+    a.vn[q] = (a.vn[q] + cv - vnb) * vmsk<T>(ci, k);
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// lbc_lnk closed branch (lbc_lnk_generic.h90:88-101) on nslab (i,j) slices: columns
+// 1 and jpi, rows 1 and jpj take pval; F-point arrays keep column and row 1.
+template <class T>
+__global__ void k_lbc_closed(T* p, int jpi, int jpj, long nslab, int is_f, T pval) {
+  const long per = 2L * jpi + 2L * jpj;
+  const long s = blockIdx.y;
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < per; e += (long)gridDim.x * blockDim.x) {
+    for (long sl = s; sl < nslab; sl += gridDim.y) {
+      T* a = p + sl * (long)jpi * jpj;
+      long i, j;
+      bool first;  // on column 1 or row 1
+      if (e < jpj) { i = 1; j = e + 1; first = true; }
+      else if (e < 2L * jpj) { i = jpi; j = e - jpj + 1; first = false; }
+      else if (e < 2L * jpj + jpi) { i = e - 2L * jpj + 1; j = 1; first = true; }
+      else { i = e - 2L * jpj - jpi + 1; j = jpj; first = false; }
+      if (first && is_f) continue;
+      a[(i - 1) + (j - 1) * (long)jpi] = pval;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// glob_sum (lib_fortran_generic.h90:32-65): sum of x*tmask_i in double-double
+// arithmetic (the compensated pair (sum, err) of DDPDD, lib_fortran.F90:300-332),
+// combined across threads with the same two-sum, one result per member.
+__device__ __forceinline__ void dd_add(double& hi, double& lo, double a_hi, double a_lo) {
+  const double zt1 = a_hi + hi;
+  const double zerr = zt1 - a_hi;
+  const double zt2 = ((hi - zerr) + (a_hi - (zt1 - zerr))) + a_lo + lo;
+  hi = zt1 + zt2;
+  lo = zt2 - ((zt1 + zt2) - zt1);
+}
+
+template <class T>
+__global__ void k_globsum_partial(const T* __restrict__ x, const double* __restrict__ tmask_i, long n2, int nk,
+                                  double* __restrict__ part) {
+  const int m = blockIdx.y;
+  const long n = n2 * nk;
+  const T* xm = x + (long)m * n;
+  double hi = 0.0, lo = 0.0;
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+    dd_add(hi, lo, (double)xm[e] * tmask_i[e % n2], 0.0);
+  __shared__ double sh[2][256];
+  sh[0][threadIdx.x] = hi;
+  sh[1][threadIdx.x] = lo;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) {
+      double h = sh[0][threadIdx.x], l = sh[1][threadIdx.x];
+      dd_add(h, l, sh[0][threadIdx.x + s], sh[1][threadIdx.x + s]);
+      sh[0][threadIdx.x] = h;
+      sh[1][threadIdx.x] = l;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * ((long)m * gridDim.x + blockIdx.x)] = sh[0][0];
+    part[2 * ((long)m * gridDim.x + blockIdx.x) + 1] = sh[1][0];
+  }
+}
+
+static __global__ void k_globsum_final(const double* __restrict__ part, int nblk, double* __restrict__ out) {
+  const int m = blockIdx.x;
+  double hi = 0.0, lo = 0.0;
+  __shared__ double sh[2][256];
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) dd_add(hi, lo, part[2 * ((long)m * nblk + b)], part[2 * ((long)m * nblk + b) + 1]);
+  sh[0][threadIdx.x] = hi;
+  sh[1][threadIdx.x] = lo;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) {
+      double h = sh[0][threadIdx.x], l = sh[1][threadIdx.x];
+      dd_add(h, l, sh[0][threadIdx.x + s], sh[1][threadIdx.x + s]);
+      sh[0][threadIdx.x] = h;
+      sh[1][threadIdx.x] = l;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[m] = sh[0][0];
+}
+
+}  // namespace nemo

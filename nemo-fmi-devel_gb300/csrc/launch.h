@@ -1,0 +1,32 @@
+// launch.h -- host launchers of the kernels, explicitly instantiated for double (in
+// inst_fp64.cu, compiled without FMA contraction) and float (inst_fp32.cu).
+#pragma once
+#include "k_dyn.cuh"
+#include "k_tra.cuh"
+
+namespace nemo {
+
+template <class T>
+cudaError_t launch_adv_trp(const Dom<T>& d, const T* un, const T* vn, const T* wn, T* zun, T* zvn, T* zwn,
+                           cudaStream_t s);
+template <class T>
+cudaError_t launch_fct(const Dom<T>& d, const FctArgs<T>& a, cudaStream_t s);
+template <class T>
+cudaError_t launch_ldf_lap(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s);
+template <class T>
+cudaError_t launch_ldf_iso(const Dom<T>& d, const LdfArgs<T>& a, int copy_akz_edges, int msc_edges, cudaStream_t s);
+template <class T>
+cudaError_t launch_zdf(const Dom<T>& d, const ZdfArgs<T>& a, cudaStream_t s);
+template <class T>
+cudaError_t launch_clamp(T* x, long n, cudaStream_t s);
+template <class T>
+cudaError_t launch_spg(const Dom<T>& d, const SpgArgs<T>& a, const GridBar& bar, int p2_blocks, cudaStream_t s);
+template <class T>
+int spg_p2_blocks_per_sm();
+template <class T>
+cudaError_t launch_lbc(T* p, int jpi, int jpj, long nslab, int is_f, T pval, cudaStream_t s);
+template <class T>
+cudaError_t launch_globsum(const T* x, const double* tmask_i, long n2, int nk, int nmem, double* part, int nblk,
+                           double* out, cudaStream_t s);
+
+}  // namespace nemo

@@ -1,0 +1,124 @@
+"""ctypes binding of the C ABI declared in include/nemo_gpu.h.
+
+The structures mirror ``nemo_dom_desc`` and ``nemo_namelist`` member for member;
+the field ids are read from the header's ``enum nemo_field_id`` so the two cannot
+drift apart.
+"""
+import ctypes as C
+import os
+import re
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))),
+                      "include", "nemo_gpu.h")
+
+NEMO_OK, NEMO_ERR_ARG, NEMO_ERR_UNSUPPORTED, NEMO_ERR_UNBOUND = 0, 1, 2, 3
+NEMO_ERR_CUDA, NEMO_ERR_TIMEOUT, NEMO_ERR_NOMEM, NEMO_ERR_STATE = 4, 5, 6, 7
+PREC_FP64, PREC_MIXED = 0, 1
+VOR = {"ENS": 0, "ENE": 1, "ENT": 2, "EET": 3, "EEN": 4, "MIX": 5}
+
+
+def _field_ids():
+    txt = open(HEADER).read()
+    body = re.search(r"enum nemo_field_id \{(.*?)\};", txt, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    names = [n.split("=")[0].strip() for n in body.split(",")]
+    names = [n for n in names if n]
+    return {n[len("NEMO_F_"):]: i for i, n in enumerate(names)}
+
+
+F = _field_ids()  # e.g. F["TSB"] == 0, F["COUNT"] == number of fields
+FP64_FIELDS = {"SSHA", "UA_B", "VA_B", "UN_ADV", "VN_ADV", "UB2_B", "VB2_B", "UN_BF", "VN_BF"}
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class DomDesc(C.Structure):
+    _fields_ = [("jpi", C.c_int), ("jpj", C.c_int), ("jpk", C.c_int), ("jperio", C.c_int),
+                ("e1t", _dp), ("e2t", _dp), ("e1u", _dp), ("e2u", _dp), ("e1v", _dp), ("e2v", _dp),
+                ("e1f", _dp), ("e2f", _dp), ("ff_f", _dp), ("ff_t", _dp), ("k_top", _ip), ("k_bot", _ip),
+                ("e3t_0", _dp), ("e3u_0", _dp), ("e3v_0", _dp), ("e3w_0", _dp), ("e3f_0", _dp)]
+
+
+class Namelist(C.Structure):
+    _fields_ = [("rn_rdt", C.c_double), ("rn_atfp", C.c_double), ("nit000", C.c_int), ("neuler", C.c_int),
+                ("ln_linssh", C.c_int), ("ln_zps", C.c_int), ("ln_isfcav", C.c_int),
+                ("ln_traldf_lap", C.c_int), ("ln_traldf_blp", C.c_int), ("ln_traldf_iso", C.c_int),
+                ("ln_traldf_msc", C.c_int), ("rn_aht_0", C.c_double), ("ln_zdfddm", C.c_int),
+                ("ln_zad_Aimp", C.c_int), ("ln_bt_fw", C.c_int), ("ln_bt_av", C.c_int), ("nn_bt_flt", C.c_int),
+                ("ln_bt_auto", C.c_int), ("nn_baro", C.c_int), ("rn_bt_cmax", C.c_double),
+                ("rn_bt_alpha", C.c_double), ("nvor_scheme", C.c_int), ("nn_een_e3f", C.c_int),
+                ("ln_dynadv_vec", C.c_int), ("ln_sco", C.c_int), ("ln_apr_dyn", C.c_int),
+                ("rn_scal_load", C.c_double), ("grav", C.c_double), ("rau0", C.c_double)]
+
+
+def make_desc(dom):
+    """DomDesc for a domain dict of Fortran-ordered float64/int32 numpy arrays.
+
+    The numpy arrays must stay alive while the descriptor is used (creation only)."""
+    import numpy as np
+    d = DomDesc()
+    d.jpi, d.jpj, d.jpk, d.jperio = dom["jpi"], dom["jpj"], dom["jpk"], dom.get("jperio", 0)
+    keep = []
+    for name in ("e1t", "e2t", "e1u", "e2u", "e1v", "e2v", "e1f", "e2f", "ff_f", "ff_t",
+                 "e3t_0", "e3u_0", "e3v_0", "e3w_0", "e3f_0"):
+        a = np.asfortranarray(dom[name], dtype=np.float64)
+        keep.append(a)
+        setattr(d, name, a.ctypes.data_as(_dp))
+    for name in ("k_top", "k_bot"):
+        a = np.asfortranarray(dom[name], dtype=np.int32)
+        keep.append(a)
+        setattr(d, name, a.ctypes.data_as(_ip))
+    d._keep = keep
+    return d
+
+
+def make_namelist(nam):
+    n = Namelist()
+    for k, _ in Namelist._fields_:
+        setattr(n, k, nam[k])
+    return n
+
+
+def _proto(lib, name, restype, argtypes):
+    f = getattr(lib, name)
+    f.restype = restype
+    f.argtypes = argtypes
+    return f
+
+
+def load(path):
+    """Load the CUDA library and declare the prototypes of every C ABI symbol."""
+    lib = C.CDLL(path)
+    vp, i, d, cp = C.c_void_p, C.c_int, C.c_double, C.c_char_p
+    _proto(lib, "nemo_gpu_create", i, [C.POINTER(DomDesc), C.POINTER(Namelist), i, i, vp, C.POINTER(vp)])
+    _proto(lib, "nemo_gpu_destroy", i, [vp])
+    _proto(lib, "nemo_gpu_last_error", cp, [vp])
+    _proto(lib, "nemo_gpu_synchronize", i, [vp])
+    _proto(lib, "nemo_gpu_bind", i, [vp, i, vp])
+    _proto(lib, "nemo_gpu_field_numel", C.c_size_t, [vp, i])
+    _proto(lib, "nemo_gpu_field_is_fp64", i, [vp, i])
+    _proto(lib, "nemo_gpu_spg_info", i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(d)])
+    _proto(lib, "nemo_gpu_field_upload", i, [vp, i, vp])
+    _proto(lib, "nemo_gpu_field_download", i, [vp, i, vp])
+    _proto(lib, "nemo_gpu_tra_adv_trp", i, [vp, vp, vp, vp, vp, vp, vp])
+    _proto(lib, "nemo_gpu_tra_adv_fct", i, [vp, i, i, cp, d, vp, vp, vp, vp, vp, vp, i, i, i])
+    _proto(lib, "nemo_gpu_tra_ldf_lap", i, [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
+    _proto(lib, "nemo_gpu_tra_ldf_iso", i, [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
+    _proto(lib, "nemo_gpu_tra_zdf_imp", i, [vp, i, i, cp, d, vp, vp, i])
+    _proto(lib, "nemo_gpu_tra_zdf", i, [vp, i])
+    _proto(lib, "nemo_gpu_dyn_spg_ts", i, [vp, i])
+    _proto(lib, "nemo_gpu_lbc_lnk", i, [vp, cp, vp, i, i, cp, d, d, i])
+    _proto(lib, "nemo_gpu_lbc_lnk_multi", i, [vp, cp, i, C.POINTER(vp), C.POINTER(i), cp, C.POINTER(d), d, i])
+    _proto(lib, "nemo_gpu_glob_sum", i, [vp, cp, vp, i, i, C.POINTER(d)])
+    _proto(lib, "nemo_gpu_stp_hotpath", i, [vp, i])
+    _proto(lib, "nemo_gpu_set_barrier_limit", i, [vp, C.c_longlong, i])
+    _proto(lib, "nemo_gpu_set_timing", i, [vp, i])
+    _proto(lib, "nemo_gpu_get_timing", i, [vp, C.POINTER(d), C.POINTER(i)])
+    return lib
+
+
+def header_symbols():
+    """Names of every function the header declares."""
+    txt = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    return sorted(set(re.findall(r"\b(nemo_gpu_\w+)\s*\(", txt)))

@@ -1,0 +1,178 @@
+"""Host mirror of the reference's Fortran interfaces over the CUDA library.
+
+Every method forwards to the C ABI (include/nemo_gpu.h) with device pointers; the
+argument lists are the Fortran ones (traadv_fct.F90:54-80, traldf_lap_blp.F90:47-76,
+traldf_iso.F90:50-103, trazdf.F90:109-135, dynspg_ts.F90:121, lbclnk.F90:81-102,
+lib_fortran_generic.h90:32). Errors raise ``NemoError`` with the library's message,
+as the reference's ctl_stop would stop the model. There is no CPU path: without the
+compiled library or a GPU the constructor fails.
+
+Tensors are torch tensors on the CUDA device whose memory is the Fortran array:
+a (jpi,jpj,jpk[,kjpt]) field of m members is a C-contiguous tensor of shape
+(m, [kjpt,] jpk, jpj, jpi) (or any contiguous tensor with that many elements).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _ffi
+from . import build as _build
+
+
+class NemoError(RuntimeError):
+    pass
+
+
+_LIB = None
+
+
+def library():
+    """The loaded CUDA library (built in-tree on first use)."""
+    global _LIB
+    if _LIB is None:
+        _LIB = _ffi.load(_build.build())
+    return _LIB
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    if not t.is_cuda or not t.is_contiguous():
+        raise NemoError("fields must be contiguous CUDA tensors")
+    return t.data_ptr()
+
+
+class Context:
+    """A nemo_gpu context: one domain, one namelist, nmembers ensemble members."""
+
+    def __init__(self, dom, nam, nmembers=1, prec="fp64", stream=None):
+        import torch
+        if not torch.cuda.is_available():
+            raise NemoError("a CUDA device is required (the library has no CPU path)")
+        self.torch = torch
+        self.lib = library()
+        self.dom, self.nam = dom, dict(nam)
+        self.nmem = nmembers
+        self.prec = _ffi.PREC_FP64 if prec == "fp64" else _ffi.PREC_MIXED
+        self.dtype = torch.float64 if self.prec == _ffi.PREC_FP64 else torch.float32
+        self.jpi, self.jpj, self.jpk = dom["jpi"], dom["jpj"], dom["jpk"]
+        desc = _ffi.make_desc(dom)
+        nl = _ffi.make_namelist(self.nam)
+        h = C.c_void_p()
+        s = stream.cuda_stream if stream is not None else None
+        st = self.lib.nemo_gpu_create(C.byref(desc), C.byref(nl), nmembers, self.prec, s, C.byref(h))
+        if st != 0:
+            raise NemoError(f"nemo_gpu_create failed with status {st}")
+        self.h = h
+        self.bound = {}
+
+    # ------------------------------------------------------------------ life cycle
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.nemo_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, st, what):
+        if st != 0:
+            msg = self.lib.nemo_gpu_last_error(self.h).decode()
+            raise NemoError(f"{what}: status {st}: {msg}")
+
+    def synchronize(self):
+        self._ck(self.lib.nemo_gpu_synchronize(self.h), "synchronize")
+
+    # ------------------------------------------------------------------ fields
+    def field_dtype(self, name):
+        return self.torch.float64 if self.lib.nemo_gpu_field_is_fp64(self.h, _ffi.F[name]) else self.torch.float32
+
+    def field_numel(self, name):
+        return int(self.lib.nemo_gpu_field_numel(self.h, _ffi.F[name]))
+
+    def to_device(self, arr, dtype=None):
+        """Device tensor holding a Fortran-order numpy array (or a list of members)."""
+        torch = self.torch
+        arrs = arr if isinstance(arr, (list, tuple)) else [arr]
+        flat = np.concatenate([np.asarray(a).ravel(order="F") for a in arrs])
+        return torch.from_numpy(flat).to(device="cuda", dtype=dtype or self.dtype).contiguous()
+
+    def to_host(self, t, shape):
+        """Fortran-order numpy array(s) (one per member) from a device tensor."""
+        a = t.detach().to("cpu", self.torch.float64).numpy()
+        n = int(np.prod(shape))
+        if a.size == n:
+            return a.reshape(shape, order="F")
+        return [a[m * n:(m + 1) * n].reshape(shape, order="F") for m in range(a.size // n)]
+
+    def bind(self, name, tensor):
+        self.bound[name] = tensor
+        self._ck(self.lib.nemo_gpu_bind(self.h, _ffi.F[name], _ptr(tensor)), f"bind {name}")
+
+    def spg_info(self):
+        ic, nb, dt = C.c_int(), C.c_int(), C.c_double()
+        self._ck(self.lib.nemo_gpu_spg_info(self.h, C.byref(ic), C.byref(nb), C.byref(dt)), "spg_info")
+        return ic.value, nb.value, dt.value
+
+    def set_barrier_limit(self, max_spins, extra_arrivals=0):
+        self._ck(self.lib.nemo_gpu_set_barrier_limit(self.h, max_spins, extra_arrivals), "set_barrier_limit")
+
+    def set_timing(self, on):
+        self._ck(self.lib.nemo_gpu_set_timing(self.h, int(on)), "set_timing")
+
+    def get_timing(self):
+        ms = (C.c_double * 4)()
+        n = C.c_int()
+        self._ck(self.lib.nemo_gpu_get_timing(self.h, ms, C.byref(n)), "get_timing")
+        return dict(zip(("dyn_spg_ts", "tra_adv", "tra_ldf", "tra_zdf"), list(ms))), n.value
+
+    def upload(self, name, host):
+        """nemo_gpu_field_upload from a (pinned) host torch tensor."""
+        self._ck(self.lib.nemo_gpu_field_upload(self.h, _ffi.F[name], host.data_ptr()), f"upload {name}")
+
+    def download(self, name, host):
+        self._ck(self.lib.nemo_gpu_field_download(self.h, _ffi.F[name], host.data_ptr()), f"download {name}")
+
+    # ------------------------------------------------------------------ routines
+    def tra_adv_trp(self, un, vn, wn, zun, zvn, zwn):
+        self._ck(self.lib.nemo_gpu_tra_adv_trp(self.h, *map(_ptr, (un, vn, wn, zun, zvn, zwn))), "tra_adv_trp")
+
+    def tra_adv_fct(self, kt, kit000, cdtype, p2dt, pun, pvn, pwn, ptb, ptn, pta, kjpt, kn_fct_h, kn_fct_v):
+        self._ck(self.lib.nemo_gpu_tra_adv_fct(self.h, kt, kit000, cdtype.encode(), p2dt, _ptr(pun), _ptr(pvn),
+                                               _ptr(pwn), _ptr(ptb), _ptr(ptn), _ptr(pta), kjpt, kn_fct_h, kn_fct_v),
+                 "tra_adv_fct")
+
+    def tra_ldf_lap(self, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb, pta, kjpt, kpass):
+        self._ck(self.lib.nemo_gpu_tra_ldf_lap(self.h, kt, kit000, cdtype.encode(), *map(_ptr, (
+            pahu, pahv, pgu, pgv, pgui, pgvi, ptb, pta)), kjpt, kpass), "tra_ldf_lap")
+
+    def tra_ldf_iso(self, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb, ptbb, pta, kjpt, kpass):
+        self._ck(self.lib.nemo_gpu_tra_ldf_iso(self.h, kt, kit000, cdtype.encode(), *map(_ptr, (
+            pahu, pahv, pgu, pgv, pgui, pgvi, ptb, ptbb, pta)), kjpt, kpass), "tra_ldf_iso")
+
+    def tra_zdf_imp(self, kt, kit000, cdtype, p2dt, ptb, pta, kjpt):
+        self._ck(self.lib.nemo_gpu_tra_zdf_imp(self.h, kt, kit000, cdtype.encode(), p2dt, _ptr(ptb), _ptr(pta), kjpt),
+                 "tra_zdf_imp")
+
+    def tra_zdf(self, kt):
+        self._ck(self.lib.nemo_gpu_tra_zdf(self.h, kt), "tra_zdf")
+
+    def dyn_spg_ts(self, kt):
+        self._ck(self.lib.nemo_gpu_dyn_spg_ts(self.h, kt), "dyn_spg_ts")
+
+    def lbc_lnk(self, t, nk, cd_nat, psgn=1.0, pval=0.0, nl=1):
+        is64 = int(t.dtype == self.torch.float64)
+        self._ck(self.lib.nemo_gpu_lbc_lnk(self.h, b"lbc", _ptr(t), nk, nl, cd_nat.encode(), psgn, pval, is64),
+                 "lbc_lnk")
+
+    def glob_sum(self, t, nk):
+        out = (C.c_double * self.nmem)()
+        is64 = int(t.dtype == self.torch.float64)
+        self._ck(self.lib.nemo_gpu_glob_sum(self.h, b"glob_sum", _ptr(t), nk, is64, out), "glob_sum")
+        return list(out)
+
+    def stp_hotpath(self, kt):
+        self._ck(self.lib.nemo_gpu_stp_hotpath(self.h, kt), "stp_hotpath")

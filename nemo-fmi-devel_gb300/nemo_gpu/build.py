@@ -1,0 +1,76 @@
+"""Build recipe of the CUDA library (sm_103a only).
+
+Three translation units are compiled in parallel and linked into
+``nemo_gpu/_lib/libnemo_gpu.so``:
+
+* ``inst_fp64.cu`` -- FP64 kernels, ``--fmad=false`` so that every double operation
+  rounds exactly like the reference's FP64 CPU build (no fused multiply-add);
+* ``inst_fp32.cu`` -- FP32-bulk kernels of the mixed-precision mode;
+* ``capi.cu``      -- the C ABI (host code).
+"""
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG_DIR)
+CSRC = os.path.join(ROOT, "csrc")
+OBJ_DIR = os.path.join(ROOT, "_build")
+LIB_DIR = os.path.join(PKG_DIR, "_lib")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-std=c++17", "--extended-lambda", "-lineinfo", "-Xcompiler", "-fPIC"]
+UNITS = {
+    "inst_fp64.cu": ["--fmad=false"],
+    "inst_fp32.cu": [],
+    "capi.cu": [],
+}
+
+
+def library_path():
+    return os.path.join(LIB_DIR, "libnemo_gpu.so")
+
+
+def _nvcc():
+    nv = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nv):
+        raise RuntimeError("nvcc not found")
+    return nv
+
+
+def _sources_newer(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(force=False, verbose=False):
+    """Compile the CUDA library if any source is newer than it; return its path."""
+    os.makedirs(OBJ_DIR, exist_ok=True)
+    os.makedirs(LIB_DIR, exist_ok=True)
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    headers.append(os.path.join(os.path.dirname(ROOT), "include", "nemo_gpu.h"))
+    nvcc = _nvcc()
+    jobs = []
+    for unit, extra in UNITS.items():
+        src = os.path.join(CSRC, unit)
+        obj = os.path.join(OBJ_DIR, unit.replace(".cu", ".o"))
+        if force or _sources_newer(obj, [src] + headers):
+            jobs.append([nvcc] + ARCH + COMMON + extra + ["-c", src, "-o", obj])
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+        if verbose:
+            print(" ".join(cmd))
+        return r
+
+    with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        list(ex.map(run, jobs))
+    objs = [os.path.join(OBJ_DIR, u.replace(".cu", ".o")) for u in UNITS]
+    lib = library_path()
+    if force or jobs or _sources_newer(lib, objs):
+        run([nvcc] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"])
+    return lib

@@ -1,0 +1,227 @@
+"""Synthetic GYRE inputs: the analytic GYRE configuration of the reference plus
+seeded noise, standing in for a model state (the reference ships no data files).
+
+Formulas restated from the reference's user-defined GYRE configuration:
+grid and Coriolis parameter from src/OCE/USR/usrdef_hgr.F90:85-165, vertical levels
+from usrdef_zgr.F90:94-176 with DOM/depth_e3.F90 (depth_to_e3 / e3_to_depth), the
+closed flat-bottom basin from usrdef_zgr.F90:179-210, initial T/S from
+usrdef_istate.F90:64-78, wind stress and E-P from usrdef_sbc.F90:90-188, the
+constant eddy diffusivity aht0 = 1/2 Ud Ld from LDF/ldftra.F90:296-299 and the
+non-linear bottom drag from ZDF/zdfdrg.F90:126-136. Namelist values follow
+cfgs/GYRE_PISCES/EXPREF/namelist_cfg on top of cfgs/SHARED/namelist_ref.
+
+Velocities, slopes, vertical diffusivity and the momentum trend are synthetic:
+a surface-intensified double-gyre from a streamfunction plus seeded noise, with w
+from continuity, so that the flow is realistic in size and structure.
+
+All arrays are numpy float64 in Fortran order (jpi,jpj[,jpk][,2]); an ensemble
+stacks members along a trailing axis (member outermost in memory).
+"""
+import math
+
+import numpy as np
+
+RA, RAD, OMEGA, GRAV, RAU0 = 6371229.0, math.pi / 180.0, 7.292116e-05, 9.80665, 1026.0
+
+
+def namelist(**over):
+    """Namelist subset for GYRE (namelist_cfg over namelist_ref)."""
+    nam = dict(
+        rn_rdt=7200.0, rn_atfp=0.1, nit000=1, neuler=1, ln_linssh=1, ln_zps=0, ln_isfcav=0,
+        ln_traldf_lap=1, ln_traldf_blp=0, ln_traldf_iso=1, ln_traldf_msc=0,
+        rn_aht_0=(0.5 * 0.02) * 100.0e3, ln_zdfddm=0, ln_zad_Aimp=0,
+        ln_bt_fw=1, ln_bt_av=1, nn_bt_flt=1, ln_bt_auto=1, nn_baro=30, rn_bt_cmax=0.8, rn_bt_alpha=0.0,
+        nvor_scheme=1, nn_een_e3f=0, ln_dynadv_vec=1, ln_sco=0, ln_apr_dyn=0, rn_scal_load=0.0,
+        grav=GRAV, rau0=RAU0)
+    nam.update(over)
+    return nam
+
+
+def zgr_z(jpk):
+    """1-D GYRE levels (usrdef_zgr.F90:134-165 and depth_e3.F90)."""
+    zsur, za0, za1, zkth, zacr = -2033.194295283385, 155.8325369664153, 146.3615918601890, 17.28520372419791, 5.0
+    k = np.arange(1, jpk + 1, dtype=np.float64)
+    depw = zsur + za0 * k + za1 * zacr * np.log(np.cosh((k - zkth) / zacr))
+    dept = zsur + za0 * (k + 0.5) + za1 * zacr * np.log(np.cosh((k + 0.5 - zkth) / zacr))
+    e3w = np.empty(jpk)
+    e3t = np.empty(jpk)
+    e3w[0] = 2.0 * (dept[0] - depw[0])
+    e3w[1:] = dept[1:] - dept[:-1]
+    e3t[:-1] = depw[1:] - depw[:-1]
+    e3t[-1] = 2.0 * (dept[-1] - depw[-1])
+    depw2 = np.empty(jpk)
+    dept2 = np.empty(jpk)
+    depw2[0] = 0.0
+    dept2[0] = 0.5 * e3w[0]
+    for j in range(1, jpk):
+        depw2[j] = depw2[j - 1] + e3t[j - 1]
+        dept2[j] = dept2[j - 1] + e3w[j]
+    return dept2, depw2, e3t, e3w
+
+
+def domain(nn_gyre, jpk=31, ln_bench=True):
+    """GYRE domain: jpi = 30 nn_GYRE + 2, jpj = 20 nn_GYRE + 2 (usrdef_nam.F90:76-77)."""
+    jpi, jpj = 30 * nn_gyre + 2, 20 * nn_gyre + 2
+    ze1 = 106000.0 / nn_gyre
+    zsin, zcos = -math.sqrt(2.0) * 0.5, math.sqrt(2.0) * 0.5
+    ze1deg = ze1 / (RA * RAD)
+    zlam1, zphi1 = -85.0, 29.0
+    zphi0 = zphi1 + zsin * ze1deg * (jpj - 2)
+    if ln_bench:
+        ze1 = 106000.0
+    ii = np.arange(1, jpi + 1, dtype=np.float64)[:, None]
+    jj = np.arange(1, jpj + 1, dtype=np.float64)[None, :]
+    gphit = zphi0 - (ii - 1.5) * ze1deg * zsin + (jj - 1.5) * ze1deg * zcos
+    gphiu = zphi0 - (ii - 1.0) * ze1deg * zsin + (jj - 1.5) * ze1deg * zcos
+    gphiv = zphi0 - (ii - 1.5) * ze1deg * zsin + (jj - 1.0) * ze1deg * zcos
+    gphif = zphi0 - (ii - 1.0) * ze1deg * zsin + (jj - 1.0) * ze1deg * zcos
+    zbeta = 2.0 * OMEGA * math.cos(RAD * zphi1) / RA
+    zf0 = 2.0 * OMEGA * math.sin(RAD * 15.0)
+    ff_f = zf0 + zbeta * np.abs(gphif - 15.0) * RAD * RA
+    ff_t = zf0 + zbeta * np.abs(gphit - 15.0) * RAD * RA
+    e1 = np.full((jpi, jpj), ze1, order="F")
+    dept, depw, e3t1, e3w1 = zgr_z(jpk)
+    def lev(p):
+        return np.asfortranarray(np.broadcast_to(p[None, None, :], (jpi, jpj, jpk)).copy())
+    kb = np.full((jpi, jpj), jpk - 1, dtype=np.int32)
+    kb[0, :] = kb[-1, :] = 0
+    kb[:, 0] = kb[:, -1] = 0
+    kt = np.minimum(1, kb).astype(np.int32)
+    dom = dict(jpi=jpi, jpj=jpj, jpk=jpk, jperio=0,
+               e1t=e1, e2t=e1.copy(order="F"), e1u=e1.copy(order="F"), e2u=e1.copy(order="F"),
+               e1v=e1.copy(order="F"), e2v=e1.copy(order="F"), e1f=e1.copy(order="F"), e2f=e1.copy(order="F"),
+               ff_f=np.asfortranarray(ff_f), ff_t=np.asfortranarray(ff_t),
+               k_top=np.asfortranarray(kt), k_bot=np.asfortranarray(kb),
+               e3t_0=lev(e3t1), e3u_0=lev(e3t1), e3v_0=lev(e3t1), e3w_0=lev(e3w1), e3f_0=lev(e3t1),
+               gdept_1d=dept, gphit=gphit, gphiu=gphiu, gphiv=gphiv)
+    return dom
+
+
+def masks(dom):
+    """tmask, umask, vmask, wmask (float64, Fortran order) as dommsk.F90 builds them."""
+    jpi, jpj, jpk = dom["jpi"], dom["jpj"], dom["jpk"]
+    k = np.arange(1, jpk + 1)[None, None, :]
+    kt, kb = dom["k_top"][:, :, None], dom["k_bot"][:, :, None]
+    t = ((kt != 0) & (k >= kt) & (k <= kb)).astype(np.float64)
+    t[0], t[-1], t[:, 0], t[:, -1] = 0, 0, 0, 0
+    u = np.zeros_like(t)
+    v = np.zeros_like(t)
+    u[:-1, :-1] = t[:-1, :-1] * t[1:, :-1]
+    v[:-1, :-1] = t[:-1, :-1] * t[:-1, 1:]
+    u[0], u[:, 0], v[0], v[:, 0] = 0, 0, 0, 0
+    w = t.copy()
+    w[:, :, 1:] = t[:, :, 1:] * t[:, :, :-1]
+    f = lambda a: np.asfortranarray(a)
+    return f(t), f(u), f(v), f(w)
+
+
+def _istate(dept):
+    """Analytic T and S profiles (usrdef_istate.F90:64-78)."""
+    d = dept
+    t = ((16. - 12. * np.tanh((d - 400) / 700)) * (-np.tanh((500. - d) / 150.) + 1.) / 2.
+         + (15. * (1. - np.tanh((d - 50.) / 1500.)) - 1.4 * np.tanh((d - 100.) / 100.)
+            + 7. * (1500. - d) / 1500.) * (-np.tanh((d - 500.) / 150.) + 1.) / 2.)
+    s = ((36.25 - 1.13 * np.tanh((d - 305) / 460)) * (-np.tanh((500. - d) / 150.) + 1.) / 2
+         + (35.55 + 1.25 * (5000. - d) / 5000. - 1.62 * np.tanh((d - 60.) / 650.)
+            + 0.2 * np.tanh((d - 35.) / 100.) + 0.2 * np.tanh((d - 1000.) / 5000.))
+         * (-np.tanh((d - 500.) / 150.) + 1.) / 2)
+    return t, s
+
+
+def _smooth(rng, shape, passes=2):
+    a = rng.standard_normal(shape)
+    for _ in range(passes):
+        a[1:-1, 1:-1] = 0.25 * (a[2:, 1:-1] + a[:-2, 1:-1] + a[1:-1, 2:] + a[1:-1, :-2])
+    return a
+
+
+def state(dom, nam, seed=0, noise_t=0.05, noise_s=0.01, u0=0.5, member=0):
+    """Seeded synthetic state (one member) on a GYRE domain."""
+    rng = np.random.default_rng([seed, member])
+    jpi, jpj, jpk = dom["jpi"], dom["jpj"], dom["jpk"]
+    tm, um, vm, wm = masks(dom)
+    e3t = dom["e3t_0"]
+    e1, e2 = dom["e1u"], dom["e2v"]
+    t1, s1 = _istate(dom["gdept_1d"])
+    ts = np.zeros((jpi, jpj, jpk, 2), order="F")
+    ts[..., 0] = (t1[None, None, :] + noise_t * rng.standard_normal((jpi, jpj, jpk))) * tm
+    ts[..., 1] = (s1[None, None, :] + noise_s * rng.standard_normal((jpi, jpj, jpk))) * tm
+    tsn = ts.copy(order="F")
+    tsn[..., 0] += 0.01 * rng.standard_normal((jpi, jpj, jpk)) * tm
+    tsn[..., 1] += 0.002 * rng.standard_normal((jpi, jpj, jpk)) * tm
+    # double gyre streamfunction at f-points, zero on the closed boundary
+    x = (np.arange(1, jpi + 1) - 1.0) / (jpi - 2)
+    y = (np.arange(1, jpj + 1) - 1.0) / (jpj - 2)
+    psi = np.sin(np.pi * np.clip(x, 0, 1))[:, None] * np.sin(2 * np.pi * np.clip(y, 0, 1))[None, :]
+    psi[-1, :] = 0
+    psi[:, -1] = 0
+    psi = psi * u0 * e1.mean() * (jpj - 2) / (2 * np.pi)
+    ubt = np.zeros((jpi, jpj))
+    vbt = np.zeros((jpi, jpj))
+    ubt[:, 1:] = -(psi[:, 1:] - psi[:, :-1]) / e2[:, 1:]
+    vbt[1:, :] = (psi[1:, :] - psi[:-1, :]) / e1[1:, :]
+    prof = np.exp(-dom["gdept_1d"] / 600.0)
+    un = ubt[:, :, None] * prof[None, None, :] + 0.03 * rng.standard_normal((jpi, jpj, jpk))
+    vn = vbt[:, :, None] * prof[None, None, :] + 0.03 * rng.standard_normal((jpi, jpj, jpk))
+    un, vn = np.asfortranarray(un * um), np.asfortranarray(vn * vm)
+    # w from continuity (sshwzv.F90 wzv, linear free surface)
+    e2u, e1v, e1e2t = dom["e2u"], dom["e1v"], dom["e1t"] * dom["e2t"]
+    fu = e2u[:, :, None] * dom["e3u_0"] * un
+    fv = e1v[:, :, None] * dom["e3v_0"] * vn
+    hdiv = np.zeros((jpi, jpj, jpk))
+    hdiv[1:-1, 1:-1, :] = (fu[1:-1, 1:-1] - fu[:-2, 1:-1] + fv[1:-1, 1:-1] - fv[1:-1, :-2]) / (
+        e1e2t[1:-1, 1:-1, None] * e3t[1:-1, 1:-1])
+    wn = np.zeros((jpi, jpj, jpk), order="F")
+    for k in range(jpk - 2, -1, -1):
+        wn[:, :, k] = wn[:, :, k + 1] - e3t[:, :, k] * hdiv[:, :, k] * tm[:, :, k]
+    ub = np.asfortranarray((un + 0.01 * rng.standard_normal(un.shape)) * um)
+    vb = np.asfortranarray((vn + 0.01 * rng.standard_normal(vn.shape)) * vm)
+    ua = np.asfortranarray(1.0e-6 * rng.standard_normal(un.shape) * um)
+    va = np.asfortranarray(1.0e-6 * rng.standard_normal(vn.shape) * vm)
+    hu = (dom["e3u_0"] * um).sum(axis=2)
+    hv = (dom["e3v_0"] * vm).sum(axis=2)
+    r1hu = np.where(hu > 0, 1.0 / np.where(hu > 0, hu, 1.0), 0.0)
+    r1hv = np.where(hv > 0, 1.0 / np.where(hv > 0, hv, 1.0), 0.0)
+    def bt(u, e3, m, r1h):
+        return np.asfortranarray((e3 * u * m).sum(axis=2) * r1h)
+    un_b, vn_b = bt(un, dom["e3u_0"], um, r1hu), bt(vn, dom["e3v_0"], vm, r1hv)
+    ub_b, vb_b = bt(ub, dom["e3u_0"], um, r1hu), bt(vb, dom["e3v_0"], vm, r1hv)
+    sshn = np.asfortranarray(0.3 * _smooth(rng, (jpi, jpj), 4) * tm[:, :, 0])
+    sshb = np.asfortranarray((sshn + 0.01 * rng.standard_normal((jpi, jpj))) * tm[:, :, 0])
+    # wind stress (usrdef_sbc.F90:160-172 at the first day) and E-P (:107-139)
+    ztau = 0.105 / math.sqrt(2.0)
+    ztaun = ztau - 0.015 * math.cos((1.0 * nam["rn_rdt"] / 3600.0 - 171 * 24) / (180 * 24) * math.pi)
+    utau = np.asfortranarray(-ztaun * np.sin(math.pi * (dom["gphiu"] - 15.) / (29. - 15.)))
+    vtau = np.asfortranarray(ztaun * np.sin(math.pi * (dom["gphiv"] - 15.) / (29. - 15.)))
+    g = dom["gphit"]
+    emp = np.where((g >= 14.845) & (g <= 37.2),
+                   0.7 * 3.16e-5 * np.sin(math.pi / 2 * (g - 37.2) / (24.6 - 37.2)),
+                   -0.8 * 3.16e-5 * np.sin(math.pi / 2 * (g - 37.2) / (46.8 - 37.2))) * tm[:, :, 0]
+    wet = tm[:, :, 0] > 0
+    emp = np.asfortranarray(emp - emp[wet].mean() * tm[:, :, 0])
+    # bottom drag coefficient * |U| at t-points, negative (zdfdrg.F90:126-136)
+    kbot = np.maximum(dom["k_bot"], 1) - 1
+    ubot = np.take_along_axis(ub, kbot[:, :, None], axis=2)[:, :, 0]
+    vbot = np.take_along_axis(vb, kbot[:, :, None], axis=2)[:, :, 0]
+    zut = ubot + np.roll(ubot, 1, axis=0)
+    zvt = vbot + np.roll(vbot, 1, axis=1)
+    rcdu = np.asfortranarray(-1.e-3 * np.sqrt(0.25 * (zut * zut + zvt * zvt) + 2.5e-3) * tm[:, :, 0])
+    # vertical diffusivity: background 1.2e-5 + mixed layer + a few convective columns
+    avt = 1.2e-5 + 1e-3 * np.exp(-dom["gdept_1d"] / 50.0)[None, None, :] * (1 + rng.random((jpi, jpj, jpk)))
+    conv = rng.random((jpi, jpj)) < 0.02
+    avt = avt + np.where(conv[:, :, None], 10.0, 0.0) * (dom["gdept_1d"] < 300)[None, None, :]
+    avt = avt * wm
+    avt[:, :, 0] = 0.0
+    avt[:, :, -1] = 0.0
+    avt = np.asfortranarray(avt)
+    # iso-neutral slopes, |slope| <= rn_slpmax = 0.01
+    def slope(m):
+        a = 0.004 * rng.standard_normal((jpi, jpj, jpk))
+        return np.asfortranarray(np.clip(a, -0.01, 0.01) * m)
+    uslp, vslp, wslpi, wslpj = slope(um), slope(vm), slope(wm), slope(wm)
+    wslpi[:, :, 0] = 0.0
+    wslpj[:, :, 0] = 0.0
+    return dict(tsb=ts, tsn=tsn, un=un, vn=vn, wn=wn, ub=ub, vb=vb, ua=ua, va=va,
+                un_b=un_b, vn_b=vn_b, ub_b=ub_b, vb_b=vb_b, sshn=sshn, sshb=sshb,
+                utau=utau, vtau=vtau, emp=emp, rcdu_bot=rcdu, avt=avt,
+                uslp=uslp, vslp=vslp, wslpi=wslpi, wslpj=wslpj)

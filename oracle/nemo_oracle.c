@@ -1,0 +1,1375 @@
+/*
+ * nemo_oracle.c -- CPU FP64 restatement of NEMO 4.0's stencil hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker; see nemo_oracle.h). Parity is UNPINNED
+ * against the reference's own outputs (NEMO cannot be built here and ships no
+ * golden vectors); it is pinned by analytic known-answer tests.
+ *
+ * Every routine restates the cited Fortran loop nest with the same loop bounds and
+ * the same left-to-right association of + - * /. Arrays are Fortran column-major
+ * with 1-based index helpers I2/I3/I4. Automatic Fortran work arrays that the
+ * reference leaves undefined outside the loop ranges are zero-filled here; the
+ * routines never read those points (this is checked by the NaN-poisoning test).
+ * Compile with -O2 -ffp-contract=off so that no multiply-add is fused.
+ */
+#include "nemo_oracle.h"
+
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define I2(i, j) ((size_t)((i)-1) + (size_t)jpi * (size_t)((j)-1))
+#define I3(i, j, k) (I2(i, j) + (size_t)jpi * (size_t)jpj * (size_t)((k)-1))
+#define I4(i, j, k, n) (I3(i, j, k) + (size_t)jpi * (size_t)jpj * (size_t)jpk * (size_t)((n)-1))
+
+struct ora_ctx {
+  int jpi, jpj, jpk;
+  nemo_namelist nam;
+  double *e1t, *e2t, *e1u, *e2u, *e1v, *e2v, *e1f, *e2f, *ff_f, *ff_t;
+  double *r1_e1t, *r1_e2t, *r1_e1u, *r1_e2u, *r1_e1v, *r1_e2v;
+  double *e1e2t, *r1_e1e2t, *e1e2u, *e1e2v, *r1_e1e2u, *r1_e1e2v, *e2_e1u, *e1_e2v;
+  int *mikt, *mbkt, *mbku, *mbkv;
+  double *tmask, *umask, *vmask, *wmask;
+  double *ssmask, *ssumask, *ssvmask, *tmask_h, *tmask_i;
+  double *e3t_0, *e3u_0, *e3v_0, *e3w_0, *e3f_0;
+  double *ht_0, *hu_0, *hv_0, *r1_hu_0, *r1_hv_0;
+  double *ahtu_c, *ahtv_c; /* constant masked diffusivity (ldftra.F90:292-372) */
+  /* dyn_spg_ts module state */
+  int nn_baro, icycle;
+  double rdtbt;
+  double *wgtbtp1, *wgtbtp2, *zwz, *ftne, *ftnw, *ftse, *ftsw;
+  double *sshn_e, *sshb_e, *sshbb_e, *un_e, *ub_e, *ubb_e, *vn_e, *vb_e, *vbb_e;
+  double *ssha_e, *ua_e, *va_e, *hu_e, *hv_e, *hur_e, *hvr_e;
+  double r2dt;
+  double *f[NEMO_F_COUNT];
+};
+
+static void spg_coriolis_factors(ora_ctx *c);
+static double *zalloc(size_t n) { return (double *)calloc(n ? n : 1, sizeof(double)); }
+
+/* Work arrays that stand for the reference's automatic arrays (undefined until
+ * written). With ora_set_poison(1) they start as NaN instead of 0, so a test can
+ * show that no routine reads a point the reference leaves undefined. */
+static int g_poison = 0;
+void ora_set_poison(int on) { g_poison = on; }
+static double *walloc(size_t n) {
+  double *p = zalloc(n);
+  if (g_poison)
+    for (size_t i = 0; i < n; ++i) p[i] = NAN;
+  return p;
+}
+
+/* SIGN(a,b) of lib_fortran.F90:339-351 (key_nosignedzero): b >= 0 gives |a|. */
+static inline double sign_nsz(double a, double b) { return b >= 0.0 ? fabs(a) : -fabs(a); }
+static inline double dmax(double a, double b) { return a > b ? a : b; }
+static inline double dmin(double a, double b) { return a < b ? a : b; }
+
+/* ------------------------------------------------------------------ lbc_lnk */
+/* Closed-basin branch of lbc_lnk_generic.h90:80-105 (jperio = 0): columns 1 and
+ * jpi, rows 1 and jpj take pval, except that F-point arrays keep column/row 1. */
+static void lbc_closed(int jpi, int jpj, double *a, int nslices, char nat, double pval) {
+  for (int s = 0; s < nslices; ++s) {
+    double *p = a + (size_t)s * jpi * jpj;
+    for (int jj = 1; jj <= jpj; ++jj) {
+      if (nat != 'F') p[I2(1, jj)] = pval;
+      p[I2(jpi, jj)] = pval;
+    }
+    for (int ji = 1; ji <= jpi; ++ji) {
+      if (nat != 'F') p[I2(ji, 1)] = pval;
+      p[I2(ji, jpj)] = pval;
+    }
+  }
+}
+
+int ora_lbc_lnk(ora_ctx *c, double *ptab, int nk, int nl, char cd_nat, double psgn, double pval) {
+  (void)psgn;
+  if (!c || !ptab || nk < 1 || nl < 1) return NEMO_ERR_ARG;
+  lbc_closed(c->jpi, c->jpj, ptab, nk * nl, cd_nat, pval);
+  return NEMO_OK;
+}
+
+/* ------------------------------------------------------------------ ts_wgt */
+/* dynspg_ts.F90:1313-1388 */
+static void ts_wgt(ora_ctx *c, int ll_av, int ll_fw, int *jpit, double *zwgt1, double *zwgt2) {
+  int nn_baro = c->nn_baro, jic, n3 = 3 * nn_baro;
+  for (int i = 0; i < n3; ++i) { zwgt1[i] = 0.0; zwgt2[i] = 0.0; }
+  jic = ll_fw ? nn_baro : 2 * nn_baro;
+  if (ll_av) {
+    switch (c->nam.nn_bt_flt) {
+      case 0: zwgt1[jic - 1] = 1.0; *jpit = jic; break;
+      case 1:
+        for (int jn = 1; jn <= n3; ++jn) {
+          double za1 = fabs((double)(jn - jic)) / (double)nn_baro;
+          if (za1 < 0.5) { zwgt1[jn - 1] = 1.0; *jpit = jn; }
+        }
+        break;
+      default:
+        for (int jn = 1; jn <= n3; ++jn) {
+          double za1 = fabs((double)(jn - jic)) / (double)nn_baro;
+          if (za1 < 1.0) { zwgt1[jn - 1] = 1.0; *jpit = jn; }
+        }
+        break;
+    }
+  } else {
+    zwgt1[jic - 1] = 1.0;
+    *jpit = jic;
+  }
+  for (int jn = 1; jn <= *jpit; ++jn)
+    for (int ji = jn; ji <= *jpit; ++ji) zwgt2[jn - 1] = zwgt2[jn - 1] + zwgt1[ji - 1];
+  double s1 = 0.0, s2 = 0.0;
+  for (int jn = 1; jn <= *jpit; ++jn) { s1 += zwgt1[jn - 1]; s2 += zwgt2[jn - 1]; }
+  double za1 = 1.0 / s1, za2 = 1.0 / s2;
+  for (int jn = 1; jn <= *jpit; ++jn) {
+    zwgt1[jn - 1] = zwgt1[jn - 1] * za1;
+    zwgt2[jn - 1] = zwgt2[jn - 1] * za2;
+  }
+}
+
+/* ------------------------------------------------------------------ create */
+int ora_create(const nemo_dom_desc *d, const nemo_namelist *nam, ora_ctx **out) {
+  if (!d || !nam || !out) return NEMO_ERR_ARG;
+  if (d->jpi < 4 || d->jpj < 4 || d->jpk < 3 || d->jperio != 0) return NEMO_ERR_UNSUPPORTED;
+  ora_ctx *c = (ora_ctx *)calloc(1, sizeof(ora_ctx));
+  const int jpi = d->jpi, jpj = d->jpj, jpk = d->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  c->jpi = jpi; c->jpj = jpj; c->jpk = jpk; c->nam = *nam;
+#define CP2(dst, src) do { c->dst = zalloc(n2); memcpy(c->dst, d->src, n2 * sizeof(double)); } while (0)
+#define CP3(dst, src) do { c->dst = zalloc(n3); memcpy(c->dst, d->src, n3 * sizeof(double)); } while (0)
+  CP2(e1t, e1t); CP2(e2t, e2t); CP2(e1u, e1u); CP2(e2u, e2u); CP2(e1v, e1v); CP2(e2v, e2v);
+  CP2(e1f, e1f); CP2(e2f, e2f); CP2(ff_f, ff_f); CP2(ff_t, ff_t);
+  CP3(e3t_0, e3t_0); CP3(e3u_0, e3u_0); CP3(e3v_0, e3v_0); CP3(e3w_0, e3w_0); CP3(e3f_0, e3f_0);
+#undef CP2
+#undef CP3
+  /* domhgr.F90:133-151 */
+  c->r1_e1t = zalloc(n2); c->r1_e2t = zalloc(n2); c->r1_e1u = zalloc(n2); c->r1_e2u = zalloc(n2);
+  c->r1_e1v = zalloc(n2); c->r1_e2v = zalloc(n2); c->e1e2t = zalloc(n2); c->r1_e1e2t = zalloc(n2);
+  c->e1e2u = zalloc(n2); c->e1e2v = zalloc(n2); c->r1_e1e2u = zalloc(n2); c->r1_e1e2v = zalloc(n2);
+  c->e2_e1u = zalloc(n2); c->e1_e2v = zalloc(n2);
+  for (size_t p = 0; p < n2; ++p) {
+    c->r1_e1t[p] = 1.0 / c->e1t[p]; c->r1_e2t[p] = 1.0 / c->e2t[p];
+    c->r1_e1u[p] = 1.0 / c->e1u[p]; c->r1_e2u[p] = 1.0 / c->e2u[p];
+    c->r1_e1v[p] = 1.0 / c->e1v[p]; c->r1_e2v[p] = 1.0 / c->e2v[p];
+    c->e1e2t[p] = c->e1t[p] * c->e2t[p]; c->r1_e1e2t[p] = 1.0 / c->e1e2t[p];
+    c->e1e2u[p] = c->e1u[p] * c->e2u[p]; c->e1e2v[p] = c->e1v[p] * c->e2v[p];
+    c->r1_e1e2u[p] = 1.0 / c->e1e2u[p]; c->r1_e1e2v[p] = 1.0 / c->e1e2v[p];
+    c->e2_e1u[p] = c->e2u[p] / c->e1u[p]; c->e1_e2v[p] = c->e1v[p] / c->e2v[p];
+  }
+  /* dommsk.F90:133-145 tmask from k_top/k_bot, then lbc_lnk 'T' */
+  c->tmask = zalloc(n3); c->umask = zalloc(n3); c->vmask = zalloc(n3); c->wmask = zalloc(n3);
+  for (int jj = 1; jj <= jpj; ++jj)
+    for (int ji = 1; ji <= jpi; ++ji) {
+      int kt = d->k_top[I2(ji, jj)], kb = d->k_bot[I2(ji, jj)];
+      if (kt != 0)
+        for (int jk = kt; jk <= kb; ++jk) c->tmask[I3(ji, jj, jk)] = 1.0;
+    }
+  lbc_closed(jpi, jpj, c->tmask, jpk, 'T', 0.0);
+  /* dommsk.F90:172-183 umask/vmask (fmask not used on this path), lbc 'U'/'V' */
+  for (int jk = 1; jk <= jpk; ++jk)
+    for (int jj = 1; jj <= jpj - 1; ++jj)
+      for (int ji = 1; ji <= jpi - 1; ++ji) {
+        c->umask[I3(ji, jj, jk)] = c->tmask[I3(ji, jj, jk)] * c->tmask[I3(ji + 1, jj, jk)];
+        c->vmask[I3(ji, jj, jk)] = c->tmask[I3(ji, jj, jk)] * c->tmask[I3(ji, jj + 1, jk)];
+      }
+  lbc_closed(jpi, jpj, c->umask, jpk, 'U', 0.0);
+  lbc_closed(jpi, jpj, c->vmask, jpk, 'V', 0.0);
+  /* dommsk.F90:189-194 */
+  for (size_t p = 0; p < n2; ++p) c->wmask[p] = c->tmask[p];
+  for (int jk = 2; jk <= jpk; ++jk)
+    for (size_t p = 0; p < n2; ++p) c->wmask[p + n2 * (jk - 1)] = c->tmask[p + n2 * (jk - 1)] * c->tmask[p + n2 * (jk - 2)];
+  /* dommsk.F90:201-238 */
+  c->ssmask = zalloc(n2); c->ssumask = zalloc(n2); c->ssvmask = zalloc(n2);
+  c->tmask_h = zalloc(n2); c->tmask_i = zalloc(n2);
+  for (size_t p = 0; p < n2; ++p) {
+    double a = 0, b = 0, e = 0;
+    for (int jk = 0; jk < jpk; ++jk) {
+      a = dmax(a, c->tmask[p + n2 * jk]); b = dmax(b, c->umask[p + n2 * jk]); e = dmax(e, c->vmask[p + n2 * jk]);
+    }
+    c->ssmask[p] = a; c->ssumask[p] = b; c->ssvmask[p] = e;
+  }
+  for (int jj = 1; jj <= jpj; ++jj)
+    for (int ji = 1; ji <= jpi; ++ji)
+      c->tmask_h[I2(ji, jj)] = (ji == 1 || ji == jpi || jj == 1 || jj == jpj) ? 0.0 : 1.0;
+  for (size_t p = 0; p < n2; ++p) c->tmask_i[p] = c->ssmask[p] * c->tmask_h[p];
+  /* domzgr.F90:292-314 */
+  c->mikt = (int *)calloc(n2, sizeof(int)); c->mbkt = (int *)calloc(n2, sizeof(int));
+  c->mbku = (int *)calloc(n2, sizeof(int)); c->mbkv = (int *)calloc(n2, sizeof(int));
+  for (size_t p = 0; p < n2; ++p) {
+    c->mikt[p] = d->k_top[p] > 1 ? d->k_top[p] : 1;
+    c->mbkt[p] = d->k_bot[p] > 1 ? d->k_bot[p] : 1;
+  }
+  for (int jj = 1; jj <= jpj - 1; ++jj)
+    for (int ji = 1; ji <= jpi - 1; ++ji) {
+      int a = c->mbkt[I2(ji + 1, jj)], b = c->mbkt[I2(ji, jj)], e = c->mbkt[I2(ji, jj + 1)];
+      c->mbku[I2(ji, jj)] = a < b ? a : b;
+      c->mbkv[I2(ji, jj)] = e < b ? e : b;
+    }
+  for (int jj = 1; jj <= jpj; ++jj)
+    for (int ji = 1; ji <= jpi; ++ji)
+      if (ji == 1 || ji == jpi || jj == 1 || jj == jpj) { c->mbku[I2(ji, jj)] = 1; c->mbkv[I2(ji, jj)] = 1; }
+      else {
+        if (c->mbku[I2(ji, jj)] < 1) c->mbku[I2(ji, jj)] = 1;
+        if (c->mbkv[I2(ji, jj)] < 1) c->mbkv[I2(ji, jj)] = 1;
+      }
+  /* domain.F90:149-183 */
+  c->ht_0 = zalloc(n2); c->hu_0 = zalloc(n2); c->hv_0 = zalloc(n2);
+  c->r1_hu_0 = zalloc(n2); c->r1_hv_0 = zalloc(n2);
+  for (int jk = 0; jk < jpk; ++jk)
+    for (size_t p = 0; p < n2; ++p) {
+      c->ht_0[p] = c->ht_0[p] + c->e3t_0[p + n2 * jk] * c->tmask[p + n2 * jk];
+      c->hu_0[p] = c->hu_0[p] + c->e3u_0[p + n2 * jk] * c->umask[p + n2 * jk];
+      c->hv_0[p] = c->hv_0[p] + c->e3v_0[p + n2 * jk] * c->vmask[p + n2 * jk];
+    }
+  for (size_t p = 0; p < n2; ++p) {
+    c->r1_hu_0[p] = c->ssumask[p] / (c->hu_0[p] + 1.0 - c->ssumask[p]);
+    c->r1_hv_0[p] = c->ssvmask[p] / (c->hv_0[p] + 1.0 - c->ssvmask[p]);
+  }
+  /* ldftra.F90:292-372 constant masked diffusivity */
+  c->ahtu_c = zalloc(n3); c->ahtv_c = zalloc(n3);
+  {
+    double a0 = nam->ln_traldf_blp ? sqrt(nam->rn_aht_0) : nam->rn_aht_0;
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (size_t p = 0; p < n2; ++p) {
+        c->ahtu_c[p + n2 * (jk - 1)] = a0 * c->umask[p + n2 * (jk - 1)];
+        c->ahtv_c[p + n2 * (jk - 1)] = a0 * c->vmask[p + n2 * (jk - 1)];
+      }
+  }
+  /* dyn_spg_ts_init, dynspg_ts.F90:1479-1493 */
+  {
+    double zcmax = -1.0e300;
+    for (size_t p = 0; p < n2; ++p) {
+      double zxr2 = c->r1_e1t[p] * c->r1_e1t[p];
+      double zyr2 = c->r1_e2t[p] * c->r1_e2t[p];
+      double zcu = sqrt(nam->grav * dmax(c->ht_0[p], 0.0) * (zxr2 + zyr2));
+      zcmax = dmax(zcmax, zcu);
+    }
+    c->nn_baro = nam->ln_bt_auto ? (int)ceil(nam->rn_rdt / nam->rn_bt_cmax * zcmax) : nam->nn_baro;
+    if (c->nn_baro < 1) c->nn_baro = 1;
+    c->rdtbt = nam->rn_rdt / (double)c->nn_baro;
+  }
+  c->wgtbtp1 = zalloc(3 * (size_t)c->nn_baro); c->wgtbtp2 = zalloc(3 * (size_t)c->nn_baro);
+  c->zwz = zalloc(n2); c->ftne = zalloc(n2); c->ftnw = zalloc(n2); c->ftse = zalloc(n2); c->ftsw = zalloc(n2);
+  c->sshn_e = zalloc(n2); c->sshb_e = zalloc(n2); c->sshbb_e = zalloc(n2);
+  c->un_e = zalloc(n2); c->ub_e = zalloc(n2); c->ubb_e = zalloc(n2);
+  c->vn_e = zalloc(n2); c->vb_e = zalloc(n2); c->vbb_e = zalloc(n2);
+  c->ssha_e = zalloc(n2); c->ua_e = zalloc(n2); c->va_e = zalloc(n2);
+  c->hu_e = zalloc(n2); c->hv_e = zalloc(n2); c->hur_e = zalloc(n2); c->hvr_e = zalloc(n2);
+  {
+    /* icycle for the steady leapfrog case; dyn_spg_ts recomputes it at nit000 */
+    int jpit = 0;
+    ts_wgt(c, nam->ln_bt_av, nam->ln_bt_fw, &jpit, c->wgtbtp1, c->wgtbtp2);
+    c->icycle = jpit;
+  }
+  c->r2dt = 2.0 * nam->rn_rdt;
+  spg_coriolis_factors(c);
+  *out = c;
+  return NEMO_OK;
+}
+
+int ora_destroy(ora_ctx *c) {
+  if (!c) return NEMO_OK;
+  double **dp[] = {&c->e1t, &c->e2t, &c->e1u, &c->e2u, &c->e1v, &c->e2v, &c->e1f, &c->e2f, &c->ff_f, &c->ff_t,
+                   &c->r1_e1t, &c->r1_e2t, &c->r1_e1u, &c->r1_e2u, &c->r1_e1v, &c->r1_e2v, &c->e1e2t,
+                   &c->r1_e1e2t, &c->e1e2u, &c->e1e2v, &c->r1_e1e2u, &c->r1_e1e2v, &c->e2_e1u, &c->e1_e2v,
+                   &c->tmask, &c->umask, &c->vmask, &c->wmask, &c->ssmask, &c->ssumask, &c->ssvmask,
+                   &c->tmask_h, &c->tmask_i, &c->e3t_0, &c->e3u_0, &c->e3v_0, &c->e3w_0, &c->e3f_0,
+                   &c->ht_0, &c->hu_0, &c->hv_0, &c->r1_hu_0, &c->r1_hv_0, &c->ahtu_c, &c->ahtv_c,
+                   &c->wgtbtp1, &c->wgtbtp2, &c->zwz, &c->ftne, &c->ftnw, &c->ftse, &c->ftsw,
+                   &c->sshn_e, &c->sshb_e, &c->sshbb_e, &c->un_e, &c->ub_e, &c->ubb_e, &c->vn_e, &c->vb_e,
+                   &c->vbb_e, &c->ssha_e, &c->ua_e, &c->va_e, &c->hu_e, &c->hv_e, &c->hur_e, &c->hvr_e};
+  for (size_t i = 0; i < sizeof(dp) / sizeof(dp[0]); ++i) free(*dp[i]);
+  free(c->mikt); free(c->mbkt); free(c->mbku); free(c->mbkv);
+  free(c);
+  return NEMO_OK;
+}
+
+int ora_bind(ora_ctx *c, int id, double *p) {
+  if (!c || id < 0 || id >= NEMO_F_COUNT) return NEMO_ERR_ARG;
+  c->f[id] = p;
+  return NEMO_OK;
+}
+
+int ora_spg_info(const ora_ctx *c, int *icycle, int *nn_baro, double *rdtbt) {
+  if (!c) return NEMO_ERR_ARG;
+  if (icycle) *icycle = c->icycle;
+  if (nn_baro) *nn_baro = c->nn_baro;
+  if (rdtbt) *rdtbt = c->rdtbt;
+  return NEMO_OK;
+}
+
+const double *ora_array(const ora_ctx *c, const char *name) {
+#define R(n) if (!strcmp(name, #n)) return c->n
+  R(tmask); R(umask); R(vmask); R(wmask); R(ssmask); R(ssumask); R(ssvmask); R(tmask_i); R(tmask_h);
+  R(ht_0); R(hu_0); R(hv_0); R(r1_hu_0); R(r1_hv_0); R(e1e2t); R(r1_e1e2t); R(wgtbtp1); R(wgtbtp2);
+  R(zwz); R(e2_e1u); R(e1_e2v); R(r1_e1u); R(r1_e2v);
+#undef R
+  return NULL;
+}
+
+const int *ora_iarray(const ora_ctx *c, const char *name) {
+  if (!strcmp(name, "mikt")) return c->mikt;
+  if (!strcmp(name, "mbkt")) return c->mbkt;
+  if (!strcmp(name, "mbku")) return c->mbku;
+  if (!strcmp(name, "mbkv")) return c->mbkv;
+  return NULL;
+}
+
+/* Field accessors with the rest-state default of the e3 fields (ln_linssh). */
+static const double *fld(const ora_ctx *c, int id) {
+  if (c->f[id]) return c->f[id];
+  switch (id) {
+    case NEMO_F_E3T_B: case NEMO_F_E3T_N: case NEMO_F_E3T_A: return c->e3t_0;
+    case NEMO_F_E3U_N: return c->e3u_0;
+    case NEMO_F_E3V_N: return c->e3v_0;
+    case NEMO_F_E3W_N: return c->e3w_0;
+    default: return NULL;
+  }
+}
+
+/* ----------------------------------------------------------- tra_adv transports */
+/* traadv.F90:99-124 (no Stokes drift, no vvl z-tilde, no eiv/mle) */
+int ora_tra_adv_trp(ora_ctx *c, const double *un, const double *vn, const double *wn,
+                    double *zun, double *zvn, double *zwn) {
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj;
+  const double *e3u = fld(c, NEMO_F_E3U_N), *e3v = fld(c, NEMO_F_E3V_N);
+  for (size_t p = 0; p < n2; ++p) { zun[p + n2 * (jpk - 1)] = 0; zvn[p + n2 * (jpk - 1)] = 0; zwn[p + n2 * (jpk - 1)] = 0; }
+  for (int jk = 1; jk <= jpk - 1; ++jk)
+    for (size_t p = 0; p < n2; ++p) {
+      size_t q = p + n2 * (jk - 1);
+      zun[q] = c->e2u[p] * e3u[q] * un[q];
+      zvn[q] = c->e1v[p] * e3v[q] * vn[q];
+      zwn[q] = c->e1e2t[p] * wn[q];
+    }
+  return NEMO_OK;
+}
+
+/* ------------------------------------------------------------ interp_4th_cpt */
+/* traadv_fct.F90:517-616 (ln_isfcav = F). pt_out is defined on the interior
+ * columns, levels 2..jpkm1, exactly where the reference defines it. */
+int ora_interp_4th_cpt(ora_ctx *c, const double *pt_in, double *pt_out) {
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n3 = (size_t)jpi * jpj * jpk;
+  double *zwd = walloc(n3), *zwi = walloc(n3), *zws = walloc(n3), *zwrm = walloc(n3), *zwt = walloc(n3);
+  const double *wmask = c->wmask;
+  for (int jk = 3; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t q = I3(ji, jj, jk);
+        zwd[q] = 3.0 * wmask[q] + 1.0;
+        zwi[q] = wmask[q];
+        zws[q] = wmask[q];
+        zwrm[q] = 3.0 * wmask[q] * (pt_in[q] + pt_in[I3(ji, jj, jk - 1)]);
+      }
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      int ikt = c->mikt[I2(ji, jj)] + 1;
+      int ikb = c->mbkt[I2(ji, jj)];
+      size_t q = I3(ji, jj, ikt);
+      zwd[q] = 1.0; zwi[q] = 0.0; zws[q] = 0.0;
+      zwrm[q] = 0.5 * (pt_in[I3(ji, jj, ikt - 1)] + pt_in[I3(ji, jj, ikt)]);
+      q = I3(ji, jj, ikb);
+      zwd[q] = 1.0; zwi[q] = 0.0; zws[q] = 0.0;
+      /* over land ikb = 1 and the reference reads pt_in(:,:,0) into an unused
+       * zwrm(:,:,1); 0 stands in for that value here */
+      zwrm[q] = ikb >= 2 ? 0.5 * (pt_in[I3(ji, jj, ikb - 1)] + pt_in[I3(ji, jj, ikb)]) : 0.0;
+    }
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) zwt[I3(ji, jj, 2)] = zwd[I3(ji, jj, 2)];
+  for (int jk = 3; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji)
+        zwt[I3(ji, jj, jk)] = zwd[I3(ji, jj, jk)] - zwi[I3(ji, jj, jk)] * zws[I3(ji, jj, jk - 1)] / zwt[I3(ji, jj, jk - 1)];
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) pt_out[I3(ji, jj, 2)] = zwrm[I3(ji, jj, 2)];
+  for (int jk = 3; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji)
+        pt_out[I3(ji, jj, jk)] = zwrm[I3(ji, jj, jk)] - zwi[I3(ji, jj, jk)] / zwt[I3(ji, jj, jk - 1)] * pt_out[I3(ji, jj, jk - 1)];
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji)
+      pt_out[I3(ji, jj, jpk - 1)] = pt_out[I3(ji, jj, jpk - 1)] / zwt[I3(ji, jj, jpk - 1)];
+  for (int jk = jpk - 2; jk >= 2; --jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji)
+        pt_out[I3(ji, jj, jk)] = (pt_out[I3(ji, jj, jk)] - zws[I3(ji, jj, jk)] * pt_out[I3(ji, jj, jk + 1)]) / zwt[I3(ji, jj, jk)];
+  free(zwd); free(zwi); free(zws); free(zwrm); free(zwt);
+  return NEMO_OK;
+}
+
+/* -------------------------------------------------------------------- nonosc */
+/* traadv_fct.F90:330-428 */
+static void nonosc(ora_ctx *c, const double *pbef, double *paa, double *pbb, double *pcc,
+                   const double *paft, double p2dt) {
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n3 = (size_t)jpi * jpj * jpk;
+  const double *tmask = c->tmask, *e3t_n = fld(c, NEMO_F_E3T_N);
+  const double zbig = 1.e+40, zrtrn = 1.e-15;
+  double *zbetup = zalloc(n3), *zbetdo = zalloc(n3), *zbup = walloc(n3), *zbdo = walloc(n3);
+  for (size_t q = 0; q < n3; ++q) {
+    zbup[q] = dmax(pbef[q] * tmask[q] - zbig * (1.0 - tmask[q]), paft[q] * tmask[q] - zbig * (1.0 - tmask[q]));
+    zbdo[q] = dmin(pbef[q] * tmask[q] + zbig * (1.0 - tmask[q]), paft[q] * tmask[q] + zbig * (1.0 - tmask[q]));
+  }
+  for (int jk = 1; jk <= jpk - 1; ++jk) {
+    int ikm1 = jk - 1 > 1 ? jk - 1 : 1;
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        double zup = zbup[I3(ji, jj, jk)];
+        zup = dmax(zup, zbup[I3(ji - 1, jj, jk)]); zup = dmax(zup, zbup[I3(ji + 1, jj, jk)]);
+        zup = dmax(zup, zbup[I3(ji, jj - 1, jk)]); zup = dmax(zup, zbup[I3(ji, jj + 1, jk)]);
+        zup = dmax(zup, zbup[I3(ji, jj, ikm1)]); zup = dmax(zup, zbup[I3(ji, jj, jk + 1)]);
+        double zdo = zbdo[I3(ji, jj, jk)];
+        zdo = dmin(zdo, zbdo[I3(ji - 1, jj, jk)]); zdo = dmin(zdo, zbdo[I3(ji + 1, jj, jk)]);
+        zdo = dmin(zdo, zbdo[I3(ji, jj - 1, jk)]); zdo = dmin(zdo, zbdo[I3(ji, jj + 1, jk)]);
+        zdo = dmin(zdo, zbdo[I3(ji, jj, ikm1)]); zdo = dmin(zdo, zbdo[I3(ji, jj, jk + 1)]);
+        double zpos = dmax(0., paa[I3(ji - 1, jj, jk)]) - dmin(0., paa[I3(ji, jj, jk)])
+                    + dmax(0., pbb[I3(ji, jj - 1, jk)]) - dmin(0., pbb[I3(ji, jj, jk)])
+                    + dmax(0., pcc[I3(ji, jj, jk + 1)]) - dmin(0., pcc[I3(ji, jj, jk)]);
+        double zneg = dmax(0., paa[I3(ji, jj, jk)]) - dmin(0., paa[I3(ji - 1, jj, jk)])
+                    + dmax(0., pbb[I3(ji, jj, jk)]) - dmin(0., pbb[I3(ji, jj - 1, jk)])
+                    + dmax(0., pcc[I3(ji, jj, jk)]) - dmin(0., pcc[I3(ji, jj, jk + 1)]);
+        double zbt = c->e1e2t[I2(ji, jj)] * e3t_n[I3(ji, jj, jk)] / p2dt;
+        zbetup[I3(ji, jj, jk)] = (zup - paft[I3(ji, jj, jk)]) / (zpos + zrtrn) * zbt;
+        zbetdo[I3(ji, jj, jk)] = (paft[I3(ji, jj, jk)] - zdo) / (zneg + zrtrn) * zbt;
+      }
+  }
+  lbc_closed(jpi, jpj, zbetup, jpk, 'T', 0.0);
+  lbc_closed(jpi, jpj, zbetdo, jpk, 'T', 0.0);
+  for (int jk = 1; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        double zau = dmin(1.0, dmin(zbetdo[I3(ji, jj, jk)], zbetup[I3(ji + 1, jj, jk)]));
+        double zbu = dmin(1.0, dmin(zbetup[I3(ji, jj, jk)], zbetdo[I3(ji + 1, jj, jk)]));
+        double zcu = (0.5 + sign_nsz(0.5, paa[I3(ji, jj, jk)]));
+        paa[I3(ji, jj, jk)] = paa[I3(ji, jj, jk)] * (zcu * zau + (1.0 - zcu) * zbu);
+        double zav = dmin(1.0, dmin(zbetdo[I3(ji, jj, jk)], zbetup[I3(ji, jj + 1, jk)]));
+        double zbv = dmin(1.0, dmin(zbetup[I3(ji, jj, jk)], zbetdo[I3(ji, jj + 1, jk)]));
+        double zcv = (0.5 + sign_nsz(0.5, pbb[I3(ji, jj, jk)]));
+        pbb[I3(ji, jj, jk)] = pbb[I3(ji, jj, jk)] * (zcv * zav + (1.0 - zcv) * zbv);
+        double za = dmin(1., dmin(zbetdo[I3(ji, jj, jk + 1)], zbetup[I3(ji, jj, jk)]));
+        double zb = dmin(1., dmin(zbetup[I3(ji, jj, jk + 1)], zbetdo[I3(ji, jj, jk)]));
+        double zc = (0.5 + sign_nsz(0.5, pcc[I3(ji, jj, jk + 1)]));
+        pcc[I3(ji, jj, jk + 1)] = pcc[I3(ji, jj, jk + 1)] * (zc * za + (1.0 - zc) * zb);
+      }
+  lbc_closed(jpi, jpj, paa, jpk, 'U', 0.0);
+  lbc_closed(jpi, jpj, pbb, jpk, 'V', 0.0);
+  free(zbetup); free(zbetdo); free(zbup); free(zbdo);
+}
+
+/* --------------------------------------------------------------- tra_adv_fct */
+/* traadv_fct.F90:54-327 (no trend / ptr / hst diagnostics, ln_isfcav = F) */
+int ora_tra_adv_fct(ora_ctx *c, int kt, int kit000, const char *cdtype, double p2dt,
+                    const double *pun, const double *pvn, const double *pwn,
+                    const double *ptb, const double *ptn, double *pta,
+                    int kjpt, int kn_fct_h, int kn_fct_v) {
+  (void)kt; (void)kit000; (void)cdtype;
+  if ((kn_fct_h != 2 && kn_fct_h != 4) || (kn_fct_v != 2 && kn_fct_v != 4) || kjpt < 1) return NEMO_ERR_ARG;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  const double *tmask = c->tmask, *umask = c->umask, *vmask = c->vmask, *wmask = c->wmask;
+  const double *e3t_b = fld(c, NEMO_F_E3T_B), *e3t_n = fld(c, NEMO_F_E3T_N), *e3t_a = fld(c, NEMO_F_E3T_A);
+  const double r1_6 = 1.0 / 6.0;
+  double *zwi = zalloc(n3), *zwx = walloc(n3), *zwy = walloc(n3), *zwz = walloc(n3);
+  double *ztu = walloc(n3), *ztv = walloc(n3), *zltu = walloc(n3), *zltv = walloc(n3), *ztw = walloc(n3);
+  for (size_t p = 0; p < n2; ++p) {
+    zwz[p] = 0.0;
+    zwx[p + n2 * (jpk - 1)] = 0.0; zwy[p + n2 * (jpk - 1)] = 0.0; zwz[p + n2 * (jpk - 1)] = 0.0;
+  }
+  memset(zwi, 0, n3 * sizeof(double));
+  for (int jn = 1; jn <= kjpt; ++jn) {
+    const double *tb = ptb + n3 * (jn - 1), *tn = ptn + n3 * (jn - 1);
+    double *ta = pta + n3 * (jn - 1);
+    /* upstream fluxes (:123-135) */
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double zfp_ui = pun[q] + fabs(pun[q]);
+          double zfm_ui = pun[q] - fabs(pun[q]);
+          double zfp_vj = pvn[q] + fabs(pvn[q]);
+          double zfm_vj = pvn[q] - fabs(pvn[q]);
+          zwx[q] = 0.5 * (zfp_ui * tb[q] + zfm_ui * tb[I3(ji + 1, jj, jk)]);
+          zwy[q] = 0.5 * (zfp_vj * tb[q] + zfm_vj * tb[I3(ji, jj + 1, jk)]);
+        }
+    /* (:137-145) */
+    for (int jk = 2; jk <= jpk - 1; ++jk)
+      for (int jj = 1; jj <= jpj; ++jj)
+        for (int ji = 1; ji <= jpi; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double zfp_wk = pwn[q] + fabs(pwn[q]);
+          double zfm_wk = pwn[q] - fabs(pwn[q]);
+          zwz[q] = 0.5 * (zfp_wk * tb[q] + zfm_wk * tb[I3(ji, jj, jk - 1)]) * wmask[q];
+        }
+    /* (:146-156) linear free surface, no cavities */
+    if (c->nam.ln_linssh)
+      for (size_t p = 0; p < n2; ++p) zwz[p] = pwn[p] * tb[p];
+    /* (:158-170) */
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double ztra = -(zwx[q] - zwx[I3(ji - 1, jj, jk)] + zwy[q] - zwy[I3(ji, jj - 1, jk)]
+                          + zwz[q] - zwz[I3(ji, jj, jk + 1)]) * c->r1_e1e2t[I2(ji, jj)];
+          ta[q] = ta[q] + ztra / e3t_n[q] * tmask[q];
+          zwi[q] = (e3t_b[q] * tb[q] + p2dt * ztra) / e3t_a[q] * tmask[q];
+        }
+    /* horizontal antidiffusive fluxes (:180-251) */
+    if (kn_fct_h == 2) {
+      for (int jk = 1; jk <= jpk - 1; ++jk)
+        for (int jj = 1; jj <= jpj - 1; ++jj)
+          for (int ji = 1; ji <= jpi - 1; ++ji) {
+            size_t q = I3(ji, jj, jk);
+            zwx[q] = 0.5 * pun[q] * (tn[q] + tn[I3(ji + 1, jj, jk)]) - zwx[q];
+            zwy[q] = 0.5 * pvn[q] * (tn[q] + tn[I3(ji, jj + 1, jk)]) - zwy[q];
+          }
+    } else {
+      for (size_t p = 0; p < n2; ++p) { zltu[p + n2 * (jpk - 1)] = 0.0; zltv[p + n2 * (jpk - 1)] = 0.0; }
+      for (int jk = 1; jk <= jpk - 1; ++jk) {
+        for (int jj = 1; jj <= jpj - 1; ++jj)
+          for (int ji = 1; ji <= jpi - 1; ++ji) {
+            size_t q = I3(ji, jj, jk);
+            ztu[q] = (tn[I3(ji + 1, jj, jk)] - tn[q]) * umask[q];
+            ztv[q] = (tn[I3(ji, jj + 1, jk)] - tn[q]) * vmask[q];
+          }
+        for (int jj = 2; jj <= jpj - 1; ++jj)
+          for (int ji = 2; ji <= jpi - 1; ++ji) {
+            size_t q = I3(ji, jj, jk);
+            zltu[q] = (ztu[q] + ztu[I3(ji - 1, jj, jk)]) * r1_6;
+            zltv[q] = (ztv[q] + ztv[I3(ji, jj - 1, jk)]) * r1_6;
+          }
+      }
+      lbc_closed(jpi, jpj, zltu, jpk, 'T', 0.0);
+      lbc_closed(jpi, jpj, zltv, jpk, 'T', 0.0);
+      for (int jk = 1; jk <= jpk - 1; ++jk)
+        for (int jj = 1; jj <= jpj - 1; ++jj)
+          for (int ji = 1; ji <= jpi - 1; ++ji) {
+            size_t q = I3(ji, jj, jk);
+            double zC2t_u = tn[q] + tn[I3(ji + 1, jj, jk)];
+            double zC2t_v = tn[q] + tn[I3(ji, jj + 1, jk)];
+            zwx[q] = 0.5 * pun[q] * (zC2t_u + zltu[q] - zltu[I3(ji + 1, jj, jk)]) - zwx[q];
+            zwy[q] = 0.5 * pvn[q] * (zC2t_v + zltv[q] - zltv[I3(ji, jj + 1, jk)]) - zwy[q];
+          }
+    }
+    /* vertical antidiffusive fluxes (:253-275) */
+    if (kn_fct_v == 2) {
+      for (int jk = 2; jk <= jpk - 1; ++jk)
+        for (int jj = 2; jj <= jpj - 1; ++jj)
+          for (int ji = 2; ji <= jpi - 1; ++ji) {
+            size_t q = I3(ji, jj, jk);
+            zwz[q] = (pwn[q] * 0.5 * (tn[q] + tn[I3(ji, jj, jk - 1)]) - zwz[q]) * wmask[q];
+          }
+    } else {
+      ora_interp_4th_cpt(c, tn, ztw);
+      for (int jk = 2; jk <= jpk - 1; ++jk)
+        for (int jj = 2; jj <= jpj - 1; ++jj)
+          for (int ji = 2; ji <= jpi - 1; ++ji) {
+            size_t q = I3(ji, jj, jk);
+            zwz[q] = (pwn[q] * ztw[q] - zwz[q]) * wmask[q];
+          }
+    }
+    if (c->nam.ln_linssh)
+      for (size_t p = 0; p < n2; ++p) zwz[p] = 0.0;
+    /* (:280) */
+    lbc_closed(jpi, jpj, zwi, jpk, 'T', 0.0);
+    lbc_closed(jpi, jpj, zwx, jpk, 'U', 0.0);
+    lbc_closed(jpi, jpj, zwy, jpk, 'V', 0.0);
+    lbc_closed(jpi, jpj, zwz, jpk, 'W', 0.0);
+    /* (:284) */
+    nonosc(c, tb, zwx, zwy, zwz, zwi, p2dt);
+    /* (:288-297) */
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          ta[q] = ta[q] - (zwx[q] - zwx[I3(ji - 1, jj, jk)] + zwy[q] - zwy[I3(ji, jj - 1, jk)]
+                           + zwz[q] - zwz[I3(ji, jj, jk + 1)]) * c->r1_e1e2t[I2(ji, jj)] / e3t_n[q];
+        }
+  }
+  free(zwi); free(zwx); free(zwy); free(zwz); free(ztu); free(ztv); free(zltu); free(zltv); free(ztw);
+  return NEMO_OK;
+}
+
+/* --------------------------------------------------------------- tra_ldf_lap */
+/* traldf_lap_blp.F90:47-158 (ln_isfcav = F; no ptr/hst diagnostics) */
+int ora_tra_ldf_lap(ora_ctx *c, int kt, int kit000, const char *cdtype,
+                    const double *pahu, const double *pahv,
+                    const double *pgu, const double *pgv, const double *pgui, const double *pgvi,
+                    const double *ptb, double *pta, int kjpt, int kpass) {
+  (void)kt; (void)kit000; (void)cdtype; (void)pgui; (void)pgvi;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  if (!pahu) pahu = c->ahtu_c;
+  if (!pahv) pahv = c->ahtv_c;
+  const double *e3u = fld(c, NEMO_F_E3U_N), *e3v = fld(c, NEMO_F_E3V_N), *e3t_n = fld(c, NEMO_F_E3T_N);
+  double zsign = kpass == 1 ? 1.0 : -1.0;
+  double *ztu = walloc(n3), *ztv = walloc(n3), *zaheeu = walloc(n3), *zaheev = walloc(n3);
+  for (int jk = 1; jk <= jpk - 1; ++jk)
+    for (int jj = 1; jj <= jpj - 1; ++jj)
+      for (int ji = 1; ji <= jpi - 1; ++ji) {
+        size_t q = I3(ji, jj, jk);
+        zaheeu[q] = zsign * pahu[q] * c->e2_e1u[I2(ji, jj)] * e3u[q];
+        zaheev[q] = zsign * pahv[q] * c->e1_e2v[I2(ji, jj)] * e3v[q];
+      }
+  for (int jn = 1; jn <= kjpt; ++jn) {
+    const double *tb = ptb + n3 * (jn - 1);
+    double *ta = pta + n3 * (jn - 1);
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          ztu[q] = zaheeu[q] * (tb[I3(ji + 1, jj, jk)] - tb[q]);
+          ztv[q] = zaheev[q] * (tb[I3(ji, jj + 1, jk)] - tb[q]);
+        }
+    if (c->nam.ln_zps)
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          int ku = c->mbku[I2(ji, jj)], kv = c->mbkv[I2(ji, jj)];
+          ztu[I3(ji, jj, ku)] = zaheeu[I3(ji, jj, ku)] * pgu[I2(ji, jj) + n2 * (jn - 1)];
+          ztv[I3(ji, jj, kv)] = zaheev[I3(ji, jj, kv)] * pgv[I2(ji, jj) + n2 * (jn - 1)];
+        }
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          ta[q] = ta[q] + (ztu[q] - ztu[I3(ji - 1, jj, jk)] + ztv[q] - ztv[I3(ji, jj - 1, jk)])
+                              / (c->e1e2t[I2(ji, jj)] * e3t_n[q]);
+        }
+  }
+  free(ztu); free(ztv); free(zaheeu); free(zaheev);
+  return NEMO_OK;
+}
+
+/* --------------------------------------------------------------- tra_ldf_iso */
+/* traldf_iso.F90:50-382 (ln_isfcav = F; no ptr/hst diagnostics) */
+int ora_tra_ldf_iso(ora_ctx *c, int kt, int kit000, const char *cdtype,
+                    const double *pahu, const double *pahv,
+                    const double *pgu, const double *pgv, const double *pgui, const double *pgvi,
+                    const double *ptb, const double *ptbb, double *pta, int kjpt, int kpass) {
+  (void)cdtype; (void)pgui; (void)pgvi;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  const nemo_namelist *nm = &c->nam;
+  double *ah_wslp2 = c->f[NEMO_F_AH_WSLP2], *akz = c->f[NEMO_F_AKZ];
+  const double *uslp = c->f[NEMO_F_USLP], *vslp = c->f[NEMO_F_VSLP];
+  const double *wslpi = c->f[NEMO_F_WSLPI], *wslpj = c->f[NEMO_F_WSLPJ];
+  if (!ah_wslp2 || !akz || !uslp || !vslp || !wslpi || !wslpj) return NEMO_ERR_UNBOUND;
+  if (!pahu) pahu = c->ahtu_c;
+  if (!pahv) pahv = c->ahtv_c;
+  const double *tmask = c->tmask, *umask = c->umask, *vmask = c->vmask, *wmask = c->wmask;
+  const double *e3u = fld(c, NEMO_F_E3U_N), *e3v = fld(c, NEMO_F_E3V_N), *e3t_n = fld(c, NEMO_F_E3T_N);
+  const double *e3w = fld(c, NEMO_F_E3W_N);
+  (void)tmask;
+  if (kpass == 1 && kt == kit000) {
+    memset(akz, 0, n3 * sizeof(double));
+    memset(ah_wslp2, 0, n3 * sizeof(double));
+  }
+  double z2dt = (nm->neuler == 0 && kt == nm->nit000) ? nm->rn_rdt : 2. * nm->rn_rdt;
+  double z1_2dt = 1.0 / z2dt;
+  double zsign = kpass == 1 ? 1.0 : -1.0;
+  if (kpass == 1) {
+    for (int jk = 2; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double zmsku = wmask[q] / dmax(umask[I3(ji, jj, jk - 1)] + umask[I3(ji - 1, jj, jk)]
+                                         + umask[I3(ji - 1, jj, jk - 1)] + umask[q], 1.0);
+          double zmskv = wmask[q] / dmax(vmask[I3(ji, jj, jk - 1)] + vmask[I3(ji, jj - 1, jk)]
+                                         + vmask[I3(ji, jj - 1, jk - 1)] + vmask[q], 1.0);
+          double zahu_w = (pahu[I3(ji, jj, jk - 1)] + pahu[I3(ji - 1, jj, jk)]
+                           + pahu[I3(ji - 1, jj, jk - 1)] + pahu[q]) * zmsku;
+          double zahv_w = (pahv[I3(ji, jj, jk - 1)] + pahv[I3(ji, jj - 1, jk)]
+                           + pahv[I3(ji, jj - 1, jk - 1)] + pahv[q]) * zmskv;
+          ah_wslp2[q] = zahu_w * wslpi[q] * wslpi[q] + zahv_w * wslpj[q] * wslpj[q];
+        }
+    if (nm->ln_traldf_msc) {
+      for (int jk = 2; jk <= jpk - 1; ++jk)
+        for (int jj = 2; jj <= jpj - 1; ++jj)
+          for (int ji = 2; ji <= jpi - 1; ++ji) {
+            size_t q = I3(ji, jj, jk);
+            double e1u0 = c->e1u[I2(ji, jj)], e1um = c->e1u[I2(ji - 1, jj)];
+            double e2v0 = c->e2v[I2(ji, jj)], e2vm = c->e2v[I2(ji, jj - 1)];
+            akz[q] = 0.25 * ((pahu[q] + pahu[I3(ji, jj, jk - 1)]) / (e1u0 * e1u0)
+                             + (pahu[I3(ji - 1, jj, jk)] + pahu[I3(ji - 1, jj, jk - 1)]) / (e1um * e1um)
+                             + (pahv[q] + pahv[I3(ji, jj, jk - 1)]) / (e2v0 * e2v0)
+                             + (pahv[I3(ji, jj - 1, jk)] + pahv[I3(ji, jj - 1, jk - 1)]) / (e2vm * e2vm));
+          }
+      if (nm->ln_traldf_blp) {
+        for (int jk = 2; jk <= jpk - 1; ++jk)
+          for (int jj = 1; jj <= jpj - 1; ++jj)
+            for (int ji = 1; ji <= jpi - 1; ++ji) {
+              size_t q = I3(ji, jj, jk);
+              akz[q] = 16.0 * ah_wslp2[q] * (akz[q] + ah_wslp2[q] / (e3w[q] * e3w[q]));
+            }
+      } else if (nm->ln_traldf_lap) {
+        for (int jk = 2; jk <= jpk - 1; ++jk)
+          for (int jj = 1; jj <= jpj - 1; ++jj)
+            for (int ji = 1; ji <= jpi - 1; ++ji) {
+              size_t q = I3(ji, jj, jk);
+              double ze3w_2 = e3w[q] * e3w[q];
+              double zcoef0 = z2dt * (akz[q] + ah_wslp2[q] / ze3w_2);
+              akz[q] = dmax(zcoef0 - 0.5, 0.0) * ze3w_2 * z1_2dt;
+            }
+      }
+    } else {
+      memcpy(akz, ah_wslp2, n3 * sizeof(double));
+    }
+  }
+  double *zdit = walloc(n3), *zdjt = walloc(n3), *zftu = walloc(n3), *zftv = walloc(n3), *ztfw = walloc(n3);
+  double *zdkt = walloc(n2), *zdk1t = walloc(n2);
+  for (int jn = 1; jn <= kjpt; ++jn) {
+    const double *tb = ptb + n3 * (jn - 1), *tbb = ptbb + n3 * (jn - 1);
+    double *ta = pta + n3 * (jn - 1);
+    for (int jk = 1; jk <= jpk; ++jk)
+      for (int jj = 1; jj <= jpj; ++jj) {
+        zdit[I3(1, jj, jk)] = 0.0; zdit[I3(jpi, jj, jk)] = 0.0;
+        zdjt[I3(1, jj, jk)] = 0.0; zdjt[I3(jpi, jj, jk)] = 0.0;
+      }
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          zdit[q] = (tb[I3(ji + 1, jj, jk)] - tb[q]) * umask[q];
+          zdjt[q] = (tb[I3(ji, jj + 1, jk)] - tb[q]) * vmask[q];
+        }
+    if (nm->ln_zps)
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          zdit[I3(ji, jj, c->mbku[I2(ji, jj)])] = pgu[I2(ji, jj) + n2 * (jn - 1)];
+          zdjt[I3(ji, jj, c->mbkv[I2(ji, jj)])] = pgv[I2(ji, jj) + n2 * (jn - 1)];
+        }
+    for (int jk = 1; jk <= jpk - 1; ++jk) {
+      for (size_t p = 0; p < n2; ++p)
+        zdk1t[p] = (tb[p + n2 * (jk - 1)] - tb[p + n2 * jk]) * wmask[p + n2 * jk];
+      if (jk == 1) memcpy(zdkt, zdk1t, n2 * sizeof(double));
+      else
+        for (size_t p = 0; p < n2; ++p)
+          zdkt[p] = (tb[p + n2 * (jk - 2)] - tb[p + n2 * (jk - 1)]) * wmask[p + n2 * (jk - 1)];
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double zabe1 = pahu[q] * c->e2_e1u[I2(ji, jj)] * e3u[q];
+          double zabe2 = pahv[q] * c->e1_e2v[I2(ji, jj)] * e3v[q];
+          double zmsku = 1. / dmax(wmask[I3(ji + 1, jj, jk)] + wmask[I3(ji, jj, jk + 1)]
+                                   + wmask[I3(ji + 1, jj, jk + 1)] + wmask[q], 1.);
+          double zmskv = 1. / dmax(wmask[I3(ji, jj + 1, jk)] + wmask[I3(ji, jj, jk + 1)]
+                                   + wmask[I3(ji, jj + 1, jk + 1)] + wmask[q], 1.);
+          double zcof1 = -pahu[q] * c->e2u[I2(ji, jj)] * uslp[q] * zmsku;
+          double zcof2 = -pahv[q] * c->e1v[I2(ji, jj)] * vslp[q] * zmskv;
+          zftu[q] = (zabe1 * zdit[q] + zcof1 * (zdkt[I2(ji + 1, jj)] + zdk1t[I2(ji, jj)]
+                                                + zdk1t[I2(ji + 1, jj)] + zdkt[I2(ji, jj)])) * umask[q];
+          zftv[q] = (zabe2 * zdjt[q] + zcof2 * (zdkt[I2(ji, jj + 1)] + zdk1t[I2(ji, jj)]
+                                                + zdk1t[I2(ji, jj + 1)] + zdkt[I2(ji, jj)])) * vmask[q];
+        }
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          ta[q] = ta[q] + zsign * (zftu[q] - zftu[I3(ji - 1, jj, jk)] + zftv[q] - zftv[I3(ji, jj - 1, jk)])
+                              * c->r1_e1e2t[I2(ji, jj)] / e3t_n[q];
+        }
+    }
+    for (int jk = 1; jk <= jpk; ++jk)
+      for (int jj = 1; jj <= jpj; ++jj) { ztfw[I3(1, jj, jk)] = 0.0; ztfw[I3(jpi, jj, jk)] = 0.0; }
+    for (size_t p = 0; p < n2; ++p) { ztfw[p] = 0.0; ztfw[p + n2 * (jpk - 1)] = 0.0; }
+    for (int jk = 2; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double zmsku = wmask[q] / dmax(umask[I3(ji, jj, jk - 1)] + umask[I3(ji - 1, jj, jk)]
+                                         + umask[I3(ji - 1, jj, jk - 1)] + umask[q], 1.0);
+          double zmskv = wmask[q] / dmax(vmask[I3(ji, jj, jk - 1)] + vmask[I3(ji, jj - 1, jk)]
+                                         + vmask[I3(ji, jj - 1, jk - 1)] + vmask[q], 1.0);
+          double zahu_w = (pahu[I3(ji, jj, jk - 1)] + pahu[I3(ji - 1, jj, jk)]
+                           + pahu[I3(ji - 1, jj, jk - 1)] + pahu[q]) * zmsku;
+          double zahv_w = (pahv[I3(ji, jj, jk - 1)] + pahv[I3(ji, jj - 1, jk)]
+                           + pahv[I3(ji, jj - 1, jk - 1)] + pahv[q]) * zmskv;
+          double zcoef3 = -zahu_w * c->e2t[I2(ji, jj)] * zmsku * wslpi[q];
+          double zcoef4 = -zahv_w * c->e1t[I2(ji, jj)] * zmskv * wslpj[q];
+          ztfw[q] = zcoef3 * (zdit[I3(ji, jj, jk - 1)] + zdit[I3(ji - 1, jj, jk)]
+                              + zdit[I3(ji - 1, jj, jk - 1)] + zdit[q])
+                  + zcoef4 * (zdjt[I3(ji, jj, jk - 1)] + zdjt[I3(ji, jj - 1, jk)]
+                              + zdjt[I3(ji, jj - 1, jk - 1)] + zdjt[q]);
+        }
+    if (nm->ln_traldf_lap) {
+      for (int jk = 2; jk <= jpk - 1; ++jk)
+        for (int jj = 1; jj <= jpj - 1; ++jj)
+          for (int ji = 2; ji <= jpi - 1; ++ji) {
+            size_t q = I3(ji, jj, jk);
+            ztfw[q] = ztfw[q] + c->e1e2t[I2(ji, jj)] / e3w[q] * wmask[q]
+                                    * (ah_wslp2[q] - akz[q]) * (tb[I3(ji, jj, jk - 1)] - tb[q]);
+          }
+    } else if (kpass == 1) {
+      for (int jk = 2; jk <= jpk - 1; ++jk)
+        for (int jj = 1; jj <= jpj - 1; ++jj)
+          for (int ji = 2; ji <= jpi - 1; ++ji) {
+            size_t q = I3(ji, jj, jk);
+            ztfw[q] = ztfw[q] + ah_wslp2[q] * c->e1e2t[I2(ji, jj)] * (tb[I3(ji, jj, jk - 1)] - tb[q]) / e3w[q] * wmask[q];
+          }
+    } else {
+      for (int jk = 2; jk <= jpk - 1; ++jk)
+        for (int jj = 1; jj <= jpj - 1; ++jj)
+          for (int ji = 2; ji <= jpi - 1; ++ji) {
+            size_t q = I3(ji, jj, jk);
+            ztfw[q] = ztfw[q] + c->e1e2t[I2(ji, jj)] / e3w[q] * wmask[q]
+                                    * (ah_wslp2[q] * (tb[I3(ji, jj, jk - 1)] - tb[q])
+                                       + akz[q] * (tbb[I3(ji, jj, jk - 1)] - tbb[q]));
+          }
+    }
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          ta[q] = ta[q] + zsign * (ztfw[q] - ztfw[I3(ji, jj, jk + 1)]) * c->r1_e1e2t[I2(ji, jj)] / e3t_n[q];
+        }
+  }
+  free(zdit); free(zdjt); free(zftu); free(zftv); free(ztfw); free(zdkt); free(zdk1t);
+  return NEMO_OK;
+}
+
+/* --------------------------------------------------------------- tra_zdf_imp */
+/* trazdf.F90:109-268 (ln_zad_Aimp = F) */
+int ora_tra_zdf_imp(ora_ctx *c, int kt, int kit000, const char *cdtype, double p2dt,
+                    const double *ptb, double *pta, int kjpt) {
+  (void)kt; (void)kit000;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n3 = (size_t)jpi * jpj * jpk;
+  const nemo_namelist *nm = &c->nam;
+  const int is_trc = cdtype && cdtype[0] == 'T' && cdtype[1] == 'R' && cdtype[2] == 'C';
+  const double *avt = c->f[NEMO_F_AVT], *avs = c->f[NEMO_F_AVS];
+  const double *akz = c->f[NEMO_F_AKZ], *ah_wslp2 = c->f[NEMO_F_AH_WSLP2];
+  const double *e3t_b = fld(c, NEMO_F_E3T_B), *e3t_n = fld(c, NEMO_F_E3T_N), *e3t_a = fld(c, NEMO_F_E3T_A);
+  const double *e3w = fld(c, NEMO_F_E3W_N), *tmask = c->tmask;
+  const int l_ldfslp = nm->ln_traldf_iso;
+  if (!avt && !is_trc) return NEMO_ERR_UNBOUND;
+  if (l_ldfslp && ((nm->ln_traldf_msc && !akz) || (!nm->ln_traldf_msc && !ah_wslp2))) return NEMO_ERR_UNBOUND;
+  double *zwi = walloc(n3), *zwt = walloc(n3), *zwd = walloc(n3), *zws = walloc(n3);
+  for (int jn = 1; jn <= kjpt; ++jn) {
+    const double *tb = ptb + n3 * (jn - 1);
+    double *ta = pta + n3 * (jn - 1);
+    if ((!is_trc && (jn == 1 || (jn == 2 && nm->ln_zdfddm))) || (is_trc && jn == 1)) {
+      const double *coef = (!is_trc && jn == 1) ? avt : avs;
+      if (!coef) { free(zwi); free(zwt); free(zwd); free(zws); return NEMO_ERR_UNBOUND; }
+      for (int jk = 2; jk <= jpk; ++jk)
+        for (int jj = 1; jj <= jpj; ++jj)
+          for (int ji = 1; ji <= jpi; ++ji) zwt[I3(ji, jj, jk)] = coef[I3(ji, jj, jk)];
+      for (int jj = 1; jj <= jpj; ++jj)
+        for (int ji = 1; ji <= jpi; ++ji) zwt[I3(ji, jj, 1)] = 0.0;
+      if (l_ldfslp) {
+        const double *add = nm->ln_traldf_msc ? akz : ah_wslp2;
+        for (int jk = 2; jk <= jpk - 1; ++jk)
+          for (int jj = 2; jj <= jpj - 1; ++jj)
+            for (int ji = 2; ji <= jpi - 1; ++ji) zwt[I3(ji, jj, jk)] = zwt[I3(ji, jj, jk)] + add[I3(ji, jj, jk)];
+      }
+      for (int jk = 1; jk <= jpk - 1; ++jk)
+        for (int jj = 2; jj <= jpj - 1; ++jj)
+          for (int ji = 2; ji <= jpi - 1; ++ji) {
+            size_t q = I3(ji, jj, jk);
+            zwi[q] = -p2dt * zwt[q] / e3w[q];
+            zws[q] = -p2dt * zwt[I3(ji, jj, jk + 1)] / e3w[I3(ji, jj, jk + 1)];
+            zwd[q] = e3t_a[q] - zwi[q] - zws[q];
+          }
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) zwt[I3(ji, jj, 1)] = zwd[I3(ji, jj, 1)];
+      for (int jk = 2; jk <= jpk - 1; ++jk)
+        for (int jj = 2; jj <= jpj - 1; ++jj)
+          for (int ji = 2; ji <= jpi - 1; ++ji)
+            zwt[I3(ji, jj, jk)] = zwd[I3(ji, jj, jk)] - zwi[I3(ji, jj, jk)] * zws[I3(ji, jj, jk - 1)] / zwt[I3(ji, jj, jk - 1)];
+    }
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t q = I3(ji, jj, 1);
+        ta[q] = e3t_b[q] * tb[q] + p2dt * e3t_n[q] * ta[q];
+      }
+    for (int jk = 2; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double zrhs = e3t_b[q] * tb[q] + p2dt * e3t_n[q] * ta[q];
+          ta[q] = zrhs - zwi[q] / zwt[I3(ji, jj, jk - 1)] * ta[I3(ji, jj, jk - 1)];
+        }
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t q = I3(ji, jj, jpk - 1);
+        ta[q] = ta[q] / zwt[q] * tmask[q];
+      }
+    for (int jk = jpk - 2; jk >= 1; --jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          ta[q] = (ta[q] - zws[q] * ta[I3(ji, jj, jk + 1)]) / zwt[q] * tmask[q];
+        }
+  }
+  free(zwi); free(zwt); free(zwd); free(zws);
+  return NEMO_OK;
+}
+
+/* trazdf.F90:46-106 on the bound tsb / tsa (no trend diagnostics) */
+int ora_tra_zdf(ora_ctx *c, int kt) {
+  const nemo_namelist *nm = &c->nam;
+  double *tsb = c->f[NEMO_F_TSB], *tsa = c->f[NEMO_F_TSA];
+  if (!tsb || !tsa) return NEMO_ERR_UNBOUND;
+  if (nm->neuler == 0 && kt == nm->nit000) c->r2dt = nm->rn_rdt;
+  else if (kt <= nm->nit000 + 1) c->r2dt = 2. * nm->rn_rdt;
+  int st = ora_tra_zdf_imp(c, kt, nm->nit000, "TRA", c->r2dt, tsb, tsa, 2);
+  if (st) return st;
+  const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk;
+  double *sa = tsa + n3;
+  for (size_t q = 0; q < n3; ++q)
+    if (sa[q] < 0.0) sa[q] = 0.1;
+  return NEMO_OK;
+}
+
+/* Coriolis factors of dyn_spg_ts (dynspg_ts.F90:241-342) for a linear free
+ * surface: zwz = ff_f / hf (ENE/ENS/MIX) or the EEN/EET triads. The reference
+ * computes them at kt = nit000; they depend only on the domain, so they are also
+ * computed at context creation to give calls that start later the same values. */
+static void spg_coriolis_factors(ora_ctx *c) {
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj;
+  const nemo_namelist *nm = &c->nam;
+  const double *umask = c->umask, *ssmask = c->ssmask;
+  double *zhf = zalloc(n2);
+  const int sc = nm->nvor_scheme;
+  if (sc == NEMO_VOR_EEN) {
+    const double *ht_n = c->ht_0;
+    for (int jj = 1; jj <= jpj - 1; ++jj)
+      for (int ji = 1; ji <= jpi - 1; ++ji) {
+        double z;
+        if (nm->nn_een_e3f == 0)
+          z = (ht_n[I2(ji, jj + 1)] + ht_n[I2(ji + 1, jj + 1)] + ht_n[I2(ji, jj)] + ht_n[I2(ji + 1, jj)]) * 0.25;
+        else
+          z = (ht_n[I2(ji, jj + 1)] + ht_n[I2(ji + 1, jj + 1)] + ht_n[I2(ji, jj)] + ht_n[I2(ji + 1, jj)])
+              / dmax(1.0, ssmask[I2(ji, jj + 1)] + ssmask[I2(ji + 1, jj + 1)] + ssmask[I2(ji, jj)] + ssmask[I2(ji + 1, jj)]);
+        if (z != 0.0) z = c->ff_f[I2(ji, jj)] / z;
+        c->zwz[I2(ji, jj)] = z;
+      }
+    lbc_closed(jpi, jpj, c->zwz, 1, 'F', 0.0);
+    for (int jj = 1; jj <= jpj; ++jj) {
+      c->ftne[I2(1, jj)] = 0; c->ftnw[I2(1, jj)] = 0; c->ftse[I2(1, jj)] = 0; c->ftsw[I2(1, jj)] = 0;
+    }
+    for (int jj = 2; jj <= jpj; ++jj)
+      for (int ji = 2; ji <= jpi; ++ji) {
+        const double *w = c->zwz;
+        c->ftne[I2(ji, jj)] = w[I2(ji - 1, jj)] + w[I2(ji, jj)] + w[I2(ji, jj - 1)];
+        c->ftnw[I2(ji, jj)] = w[I2(ji - 1, jj - 1)] + w[I2(ji - 1, jj)] + w[I2(ji, jj)];
+        c->ftse[I2(ji, jj)] = w[I2(ji, jj)] + w[I2(ji, jj - 1)] + w[I2(ji - 1, jj - 1)];
+        c->ftsw[I2(ji, jj)] = w[I2(ji, jj - 1)] + w[I2(ji - 1, jj - 1)] + w[I2(ji - 1, jj)];
+      }
+  } else if (sc == NEMO_VOR_EET) {
+    const double *ht_n = c->ht_0, *ff = c->ff_f;
+    for (int jj = 1; jj <= jpj; ++jj) {
+      c->ftne[I2(1, jj)] = 0; c->ftnw[I2(1, jj)] = 0; c->ftse[I2(1, jj)] = 0; c->ftsw[I2(1, jj)] = 0;
+    }
+    for (int jj = 2; jj <= jpj; ++jj)
+      for (int ji = 2; ji <= jpi; ++ji) {
+        double z1_ht = ssmask[I2(ji, jj)] / (ht_n[I2(ji, jj)] + 1.0 - ssmask[I2(ji, jj)]);
+        c->ftne[I2(ji, jj)] = (ff[I2(ji - 1, jj)] + ff[I2(ji, jj)] + ff[I2(ji, jj - 1)]) * z1_ht;
+        c->ftnw[I2(ji, jj)] = (ff[I2(ji - 1, jj - 1)] + ff[I2(ji - 1, jj)] + ff[I2(ji, jj)]) * z1_ht;
+        c->ftse[I2(ji, jj)] = (ff[I2(ji, jj)] + ff[I2(ji, jj - 1)] + ff[I2(ji - 1, jj - 1)]) * z1_ht;
+        c->ftsw[I2(ji, jj)] = (ff[I2(ji, jj - 1)] + ff[I2(ji - 1, jj - 1)] + ff[I2(ji - 1, jj)]) * z1_ht;
+      }
+  } else if (sc == NEMO_VOR_ENE || sc == NEMO_VOR_ENS || sc == NEMO_VOR_MIX) {
+    for (size_t p = 0; p < n2; ++p) { c->zwz[p] = 0.0; zhf[p] = 0.0; }
+    if (nm->ln_sco) {
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji)
+          zhf[I2(ji, jj)] = (c->ht_0[I2(ji, jj)] + c->ht_0[I2(ji + 1, jj)] + c->ht_0[I2(ji, jj + 1)] + c->ht_0[I2(ji + 1, jj + 1)])
+                            / dmax(ssmask[I2(ji, jj)] + ssmask[I2(ji + 1, jj)] + ssmask[I2(ji, jj + 1)] + ssmask[I2(ji + 1, jj + 1)], 1.0);
+    }
+    for (int jj = 1; jj <= jpj - 1; ++jj)
+      for (int ji = 1; ji <= jpi; ++ji)
+        zhf[I2(ji, jj)] = zhf[I2(ji, jj)] * (1.0 - umask[I3(ji, jj, 1)] * umask[I3(ji, jj + 1, 1)]);
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi; ++ji)
+          zhf[I2(ji, jj)] = zhf[I2(ji, jj)] + c->e3f_0[I3(ji, jj, jk)] * umask[I3(ji, jj, jk)] * umask[I3(ji, jj + 1, jk)];
+    lbc_closed(jpi, jpj, zhf, 1, 'F', 0.0);
+    for (size_t p = 0; p < n2; ++p)
+      if (zhf[p] != 0.0) c->zwz[p] = 1.0 / zhf[p];
+    for (size_t p = 0; p < n2; ++p) c->zwz[p] = c->ff_f[p] * c->zwz[p];
+  }
+  free(zhf);
+}
+
+/* ---------------------------------------------------------------- dyn_spg_ts */
+/* dynspg_ts.F90:121-1310 for ln_linssh = T without isf, wetting/drying, tides,
+ * bdy, agrif, Stokes drift or assimilation increments. */
+int ora_dyn_spg_ts(ora_ctx *c, int kt) {
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj;
+  const nemo_namelist *nm = &c->nam;
+  if (!nm->ln_linssh) return NEMO_ERR_UNSUPPORTED;
+  double *const *F = c->f;
+  double *ua = F[NEMO_F_UA], *va = F[NEMO_F_VA], *un = F[NEMO_F_UN], *vn = F[NEMO_F_VN];
+  double *ub = F[NEMO_F_UB], *vb = F[NEMO_F_VB];
+  double *sshn = F[NEMO_F_SSHN], *sshb = F[NEMO_F_SSHB], *ssha = F[NEMO_F_SSHA];
+  double *un_b = F[NEMO_F_UN_B], *vn_b = F[NEMO_F_VN_B], *ub_b = F[NEMO_F_UB_B], *vb_b = F[NEMO_F_VB_B];
+  double *ua_b = F[NEMO_F_UA_B], *va_b = F[NEMO_F_VA_B];
+  double *un_adv = F[NEMO_F_UN_ADV], *vn_adv = F[NEMO_F_VN_ADV];
+  double *ub2_b = F[NEMO_F_UB2_B], *vb2_b = F[NEMO_F_VB2_B], *un_bf = F[NEMO_F_UN_BF], *vn_bf = F[NEMO_F_VN_BF];
+  double *utau = F[NEMO_F_UTAU], *vtau = F[NEMO_F_VTAU], *utau_b = F[NEMO_F_UTAU_B], *vtau_b = F[NEMO_F_VTAU_B];
+  double *emp = F[NEMO_F_EMP], *emp_b = F[NEMO_F_EMP_B], *rnf = F[NEMO_F_RNF], *rnf_b = F[NEMO_F_RNF_B];
+  double *rCdU_bot = F[NEMO_F_RCDU_BOT], *ssh_ib = F[NEMO_F_SSH_IB], *ssh_ibb = F[NEMO_F_SSH_IBB];
+  if (!ua || !va || !un || !vn || !sshn || !ssha || !un_b || !vn_b || !ub_b || !vb_b || !ua_b || !va_b ||
+      !un_adv || !vn_adv || !ub2_b || !vb2_b || !un_bf || !vn_bf || !utau || !vtau || !emp || !rCdU_bot)
+    return NEMO_ERR_UNBOUND;
+  if (!nm->ln_bt_fw && (!ub || !vb || !sshb || !utau_b || !vtau_b || !emp_b)) return NEMO_ERR_UNBOUND;
+  if (nm->ln_apr_dyn && (!ssh_ib || (!nm->ln_bt_fw && !ssh_ibb))) return NEMO_ERR_UNBOUND;
+  const double *umask = c->umask, *vmask = c->vmask, *e3u = fld(c, NEMO_F_E3U_N), *e3v = fld(c, NEMO_F_E3V_N);
+  const double *hu_n = c->hu_0, *hv_n = c->hv_0, *r1_hu_n = c->r1_hu_0, *r1_hv_n = c->r1_hv_0;
+  const double *ssumask = c->ssumask, *ssvmask = c->ssvmask, *ssmask = c->ssmask;
+  const double r1_2 = 0.5, r1_4 = 0.25, r1_8 = 0.125, r1_12 = 1.0 / 12.0;
+  const double grav = nm->grav, r1_rau0 = 1.0 / nm->rau0, rdtbt = c->rdtbt;
+  const int ln_bt_fw = nm->ln_bt_fw, ln_dynadv_vec = nm->ln_dynadv_vec;
+  double *zu_frc = walloc(n2), *zv_frc = walloc(n2), *zu_trd = walloc(n2), *zv_trd = walloc(n2);
+  double *zwx = walloc(n2), *zwy = walloc(n2), *zssh_frc = walloc(n2), *zhdiv = walloc(n2);
+  double *zsshp2_e = walloc(n2), *zCdU_u = walloc(n2), *zCdU_v = walloc(n2);
+  double z2dt_bf = (kt == nm->nit000 && nm->neuler == 0) ? nm->rn_rdt : 2.0 * nm->rn_rdt;
+  double r1_2dt_b = 1.0 / z2dt_bf;
+  int ll_init = nm->ln_bt_av, ll_fw_start = 0;
+  if (kt == nm->nit000) {
+    if (nm->neuler == 0) ll_init = 1;
+    ll_fw_start = (nm->ln_bt_fw || nm->neuler == 0) ? 1 : 0;
+    ts_wgt(c, nm->ln_bt_av, ll_fw_start, &c->icycle, c->wgtbtp1, c->wgtbtp2);
+  }
+  /* (:225-231) bottom friction only */
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      zCdU_u[I2(ji, jj)] = r1_2 * (rCdU_bot[I2(ji + 1, jj)] + rCdU_bot[I2(ji, jj)]);
+      zCdU_v[I2(ji, jj)] = r1_2 * (rCdU_bot[I2(ji, jj + 1)] + rCdU_bot[I2(ji, jj)]);
+    }
+  if (kt == nm->nit000) spg_coriolis_factors(c);
+  if (!nm->ln_bt_fw && (nm->neuler == 0 && kt == nm->nit000 + 1)) {
+    ll_fw_start = 0;
+    ts_wgt(c, nm->ln_bt_av, ll_fw_start, &c->icycle, c->wgtbtp1, c->wgtbtp2);
+  }
+  /* Phase 1 (:358-378) */
+  for (size_t p = 0; p < n2; ++p) { zu_frc[p] = 0.0; zv_frc[p] = 0.0; }
+  for (int jk = 1; jk <= jpk - 1; ++jk)
+    for (size_t p = 0; p < n2; ++p) {
+      size_t q = p + n2 * (jk - 1);
+      zu_frc[p] = zu_frc[p] + e3u[q] * ua[q] * umask[q];
+      zv_frc[p] = zv_frc[p] + e3v[q] * va[q] * vmask[q];
+    }
+  for (size_t p = 0; p < n2; ++p) { zu_frc[p] = zu_frc[p] * r1_hu_n[p]; zv_frc[p] = zv_frc[p] * r1_hv_n[p]; }
+  for (int jk = 1; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t q = I3(ji, jj, jk);
+        ua[q] = ua[q] - zu_frc[I2(ji, jj)] * umask[q];
+        va[q] = va[q] - zv_frc[I2(ji, jj)] * vmask[q];
+      }
+  /* barotropic Coriolis (:387-443) */
+  for (size_t p = 0; p < n2; ++p) {
+    zwx[p] = un_b[p] * hu_n[p] * c->e2u[p];
+    zwy[p] = vn_b[p] * hv_n[p] * c->e1v[p];
+  }
+  const int sc = nm->nvor_scheme;
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      size_t p = I2(ji, jj);
+      if (sc == NEMO_VOR_ENT) {
+        const double *e = c->e1e2t, *h = c->ht_0, *ft = c->ff_t;
+        zu_trd[p] = +r1_4 * c->r1_e1e2u[p] * r1_hu_n[p]
+                    * (e[I2(ji + 1, jj)] * h[I2(ji + 1, jj)] * ft[I2(ji + 1, jj)] * (vn_b[I2(ji + 1, jj)] + vn_b[I2(ji + 1, jj - 1)])
+                       + e[p] * h[p] * ft[p] * (vn_b[p] + vn_b[I2(ji, jj - 1)]));
+        zv_trd[p] = -r1_4 * c->r1_e1e2v[p] * r1_hv_n[p]
+                    * (e[I2(ji, jj + 1)] * h[I2(ji, jj + 1)] * ft[I2(ji, jj + 1)] * (un_b[I2(ji, jj + 1)] + un_b[I2(ji - 1, jj + 1)])
+                       + e[p] * h[p] * ft[p] * (un_b[p] + un_b[I2(ji - 1, jj)]));
+      } else if (sc == NEMO_VOR_ENE || sc == NEMO_VOR_MIX) {
+        double zy1 = (zwy[I2(ji, jj - 1)] + zwy[I2(ji + 1, jj - 1)]) * c->r1_e1u[p];
+        double zy2 = (zwy[p] + zwy[I2(ji + 1, jj)]) * c->r1_e1u[p];
+        double zx1 = (zwx[I2(ji - 1, jj)] + zwx[I2(ji - 1, jj + 1)]) * c->r1_e2v[p];
+        double zx2 = (zwx[p] + zwx[I2(ji, jj + 1)]) * c->r1_e2v[p];
+        zu_trd[p] = r1_4 * (c->zwz[I2(ji, jj - 1)] * zy1 + c->zwz[p] * zy2);
+        zv_trd[p] = -r1_4 * (c->zwz[I2(ji - 1, jj)] * zx1 + c->zwz[p] * zx2);
+      } else if (sc == NEMO_VOR_ENS) {
+        double zy1 = r1_8 * (zwy[I2(ji, jj - 1)] + zwy[I2(ji + 1, jj - 1)] + zwy[p] + zwy[I2(ji + 1, jj)]) * c->r1_e1u[p];
+        double zx1 = -r1_8 * (zwx[I2(ji - 1, jj)] + zwx[I2(ji - 1, jj + 1)] + zwx[p] + zwx[I2(ji, jj + 1)]) * c->r1_e2v[p];
+        zu_trd[p] = zy1 * (c->zwz[I2(ji, jj - 1)] + c->zwz[p]);
+        zv_trd[p] = zx1 * (c->zwz[I2(ji - 1, jj)] + c->zwz[p]);
+      } else {
+        zu_trd[p] = +r1_12 * c->r1_e1u[p] * (c->ftne[p] * zwy[p] + c->ftnw[I2(ji + 1, jj)] * zwy[I2(ji + 1, jj)]
+                                              + c->ftse[p] * zwy[I2(ji, jj - 1)] + c->ftsw[I2(ji + 1, jj)] * zwy[I2(ji + 1, jj - 1)]);
+        zv_trd[p] = -r1_12 * c->r1_e2v[p] * (c->ftsw[I2(ji, jj + 1)] * zwx[I2(ji - 1, jj + 1)] + c->ftse[I2(ji, jj + 1)] * zwx[I2(ji, jj + 1)]
+                                              + c->ftnw[p] * zwx[I2(ji - 1, jj)] + c->ftne[p] * zwx[p]);
+      }
+    }
+  /* (:511-516) */
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      size_t p = I2(ji, jj);
+      zu_frc[p] = zu_frc[p] - zu_trd[p] * ssumask[p];
+      zv_frc[p] = zv_frc[p] - zv_trd[p] * ssvmask[p];
+    }
+  /* bottom stress from baroclinic velocities (:519-557) */
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      size_t p = I2(ji, jj);
+      int ikbu = c->mbku[p], ikbv = c->mbkv[p];
+      if (ln_bt_fw) {
+        zwx[p] = un[I3(ji, jj, ikbu)] - un_b[p];
+        zwy[p] = vn[I3(ji, jj, ikbv)] - vn_b[p];
+      } else {
+        zwx[p] = ub[I3(ji, jj, ikbu)] - ub_b[p];
+        zwy[p] = vb[I3(ji, jj, ikbv)] - vb_b[p];
+      }
+    }
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      size_t p = I2(ji, jj);
+      zu_frc[p] = zu_frc[p] + r1_hu_n[p] * r1_2 * (rCdU_bot[I2(ji + 1, jj)] + rCdU_bot[p]) * zwx[p];
+      zv_frc[p] = zv_frc[p] + r1_hv_n[p] * r1_2 * (rCdU_bot[I2(ji, jj + 1)] + rCdU_bot[p]) * zwy[p];
+    }
+  /* wind (:589-604) */
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      size_t p = I2(ji, jj);
+      if (ln_bt_fw) {
+        zu_frc[p] = zu_frc[p] + r1_rau0 * utau[p] * r1_hu_n[p];
+        zv_frc[p] = zv_frc[p] + r1_rau0 * vtau[p] * r1_hv_n[p];
+      } else {
+        double zztmp = r1_rau0 * r1_2;
+        zu_frc[p] = zu_frc[p] + zztmp * (utau_b[p] + utau[p]) * r1_hu_n[p];
+        zv_frc[p] = zv_frc[p] + zztmp * (vtau_b[p] + vtau[p]) * r1_hv_n[p];
+      }
+    }
+  /* atmospheric pressure (:606-629) */
+  if (nm->ln_apr_dyn)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t p = I2(ji, jj);
+        double zu_spg, zv_spg;
+        if (ln_bt_fw) {
+          zu_spg = grav * (ssh_ib[I2(ji + 1, jj)] - ssh_ib[p]) * c->r1_e1u[p];
+          zv_spg = grav * (ssh_ib[I2(ji, jj + 1)] - ssh_ib[p]) * c->r1_e2v[p];
+        } else {
+          double zztmp = grav * r1_2;
+          zu_spg = zztmp * (ssh_ib[I2(ji + 1, jj)] - ssh_ib[p] + ssh_ibb[I2(ji + 1, jj)] - ssh_ibb[p]) * c->r1_e1u[p];
+          zv_spg = zztmp * (ssh_ib[I2(ji, jj + 1)] - ssh_ib[p] + ssh_ibb[I2(ji, jj + 1)] - ssh_ibb[p]) * c->r1_e2v[p];
+        }
+        zu_frc[p] = zu_frc[p] + zu_spg;
+        zv_frc[p] = zv_frc[p] + zv_spg;
+      }
+  /* ssh forcing (:633-639), rnf / fwfisf absent when not bound */
+  for (size_t p = 0; p < n2; ++p) {
+    double r = rnf ? rnf[p] : 0.0;
+    if (ln_bt_fw) zssh_frc[p] = r1_rau0 * (emp[p] - r + 0.0);
+    else {
+      double rb = rnf_b ? rnf_b[p] : 0.0;
+      zssh_frc[p] = r1_rau0 * r1_2 * (emp[p] + emp_b[p] - r - rb + 0.0 + 0.0);
+    }
+  }
+  /* Phase 2 initialisation (:665-702) */
+  if (ll_init)
+    for (size_t p = 0; p < n2; ++p) {
+      c->sshbb_e[p] = 0; c->ubb_e[p] = 0; c->vbb_e[p] = 0; c->sshb_e[p] = 0; c->ub_e[p] = 0; c->vb_e[p] = 0;
+    }
+  for (size_t p = 0; p < n2; ++p) {
+    if (ln_bt_fw) {
+      c->sshn_e[p] = sshn[p]; c->un_e[p] = un_b[p]; c->vn_e[p] = vn_b[p];
+    } else {
+      c->sshn_e[p] = sshb[p]; c->un_e[p] = ub_b[p]; c->vn_e[p] = vb_b[p];
+    }
+    c->hu_e[p] = hu_n[p]; c->hv_e[p] = hv_n[p]; c->hur_e[p] = r1_hu_n[p]; c->hvr_e[p] = r1_hv_n[p];
+    ua_b[p] = 0; va_b[p] = 0; ssha[p] = 0; un_adv[p] = 0; vn_adv[p] = 0;
+  }
+  /* sub-step loop (:712-1207) */
+  for (int jn = 1; jn <= c->icycle; ++jn) {
+    double za0, za1, za2, za3;
+    if (jn < 3 && ll_init) { za1 = 1.0; za2 = 0.0; za3 = 0.0; }
+    else { za1 = 1.781105; za2 = -1.06221; za3 = 0.281105; }
+    for (size_t p = 0; p < n2; ++p) {
+      c->ua_e[p] = za1 * c->un_e[p] + za2 * c->ub_e[p] + za3 * c->ubb_e[p];
+      c->va_e[p] = za1 * c->vn_e[p] + za2 * c->vb_e[p] + za3 * c->vbb_e[p];
+    }
+    /* linssh: zhup2_e = hu_n, zhvp2_e = hv_n (:788-792) */
+    for (size_t p = 0; p < n2; ++p) {
+      zwx[p] = c->e2u[p] * c->ua_e[p] * hu_n[p];
+      zwy[p] = c->e1v[p] * c->va_e[p] * hv_n[p];
+    }
+    za2 = c->wgtbtp2[jn - 1];
+    for (size_t p = 0; p < n2; ++p) {
+      un_adv[p] = un_adv[p] + za2 * zwx[p] * c->r1_e2u[p];
+      vn_adv[p] = vn_adv[p] + za2 * zwy[p] * c->r1_e1v[p];
+    }
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t p = I2(ji, jj);
+        zhdiv[p] = (zwx[p] - zwx[I2(ji - 1, jj)] + zwy[p] - zwy[I2(ji, jj - 1)]) * c->r1_e1e2t[p];
+      }
+    for (size_t p = 0; p < n2; ++p) c->ssha_e[p] = (c->sshn_e[p] - rdtbt * (zssh_frc[p] + zhdiv[p])) * ssmask[p];
+    lbc_closed(jpi, jpj, c->ssha_e, 1, 'T', 0.0);
+    if (jn == 1 && ll_init) { za0 = 1.0; za1 = 0.0; za2 = 0.0; za3 = 0.0; }
+    else if (jn == 2 && ll_init) { za0 = 1.0833333333333; za1 = -0.1666666666666; za2 = 0.0833333333333; za3 = 0.0; }
+    else if (nm->rn_bt_alpha == 0.0) { za0 = 0.614; za1 = 0.285; za2 = 0.088; za3 = 0.013; }
+    else {
+      double zepsilon = 0.00976186 - 0.13451357 * nm->rn_bt_alpha;
+      double zgamma = 0.08344500 - 0.51358400 * nm->rn_bt_alpha;
+      za0 = 0.5 + zgamma + 2.0 * nm->rn_bt_alpha + 2.0 * zepsilon;
+      za1 = 1.0 - za0 - zgamma - zepsilon;
+      za2 = zgamma;
+      za3 = zepsilon;
+    }
+    for (size_t p = 0; p < n2; ++p)
+      zsshp2_e[p] = za0 * c->ssha_e[p] + za1 * c->sshn_e[p] + za2 * c->sshb_e[p] + za3 * c->sshbb_e[p];
+    /* Coriolis (:1000-1056) with zhup2_e = hu_n (linssh) */
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t p = I2(ji, jj);
+        if (sc == NEMO_VOR_ENT) {
+          const double *e = c->e1e2t, *h = c->ht_0, *ft = c->ff_t;
+          double z1_hu = ssumask[p] / (hu_n[p] + 1.0 - ssumask[p]);
+          double z1_hv = ssvmask[p] / (hv_n[p] + 1.0 - ssvmask[p]);
+          zu_trd[p] = +r1_4 * c->r1_e1e2u[p] * z1_hu
+                      * (e[I2(ji + 1, jj)] * h[I2(ji + 1, jj)] * ft[I2(ji + 1, jj)] * (c->va_e[I2(ji + 1, jj)] + c->va_e[I2(ji + 1, jj - 1)])
+                         + e[p] * h[p] * ft[p] * (c->va_e[p] + c->va_e[I2(ji, jj - 1)]));
+          zv_trd[p] = -r1_4 * c->r1_e1e2v[p] * z1_hv
+                      * (e[I2(ji, jj + 1)] * h[I2(ji, jj + 1)] * ft[I2(ji, jj + 1)] * (c->ua_e[I2(ji, jj + 1)] + c->ua_e[I2(ji - 1, jj + 1)])
+                         + e[p] * h[p] * ft[p] * (c->ua_e[p] + c->ua_e[I2(ji - 1, jj)]));
+        } else if (sc == NEMO_VOR_ENE || sc == NEMO_VOR_MIX) {
+          double zy1 = (zwy[I2(ji, jj - 1)] + zwy[I2(ji + 1, jj - 1)]) * c->r1_e1u[p];
+          double zy2 = (zwy[p] + zwy[I2(ji + 1, jj)]) * c->r1_e1u[p];
+          double zx1 = (zwx[I2(ji - 1, jj)] + zwx[I2(ji - 1, jj + 1)]) * c->r1_e2v[p];
+          double zx2 = (zwx[p] + zwx[I2(ji, jj + 1)]) * c->r1_e2v[p];
+          zu_trd[p] = r1_4 * (c->zwz[I2(ji, jj - 1)] * zy1 + c->zwz[p] * zy2);
+          zv_trd[p] = -r1_4 * (c->zwz[I2(ji - 1, jj)] * zx1 + c->zwz[p] * zx2);
+        } else if (sc == NEMO_VOR_ENS) {
+          double zy1 = r1_8 * (zwy[I2(ji, jj - 1)] + zwy[I2(ji + 1, jj - 1)] + zwy[p] + zwy[I2(ji + 1, jj)]) * c->r1_e1u[p];
+          double zx1 = -r1_8 * (zwx[I2(ji - 1, jj)] + zwx[I2(ji - 1, jj + 1)] + zwx[p] + zwx[I2(ji, jj + 1)]) * c->r1_e2v[p];
+          zu_trd[p] = zy1 * (c->zwz[I2(ji, jj - 1)] + c->zwz[p]);
+          zv_trd[p] = zx1 * (c->zwz[I2(ji - 1, jj)] + c->zwz[p]);
+        } else {
+          zu_trd[p] = +r1_12 * c->r1_e1u[p] * (c->ftne[p] * zwy[p] + c->ftnw[I2(ji + 1, jj)] * zwy[I2(ji + 1, jj)]
+                                                + c->ftse[p] * zwy[I2(ji, jj - 1)] + c->ftsw[I2(ji + 1, jj)] * zwy[I2(ji + 1, jj - 1)]);
+          zv_trd[p] = -r1_12 * c->r1_e2v[p] * (c->ftsw[I2(ji, jj + 1)] * zwx[I2(ji - 1, jj + 1)] + c->ftse[I2(ji, jj + 1)] * zwx[I2(ji, jj + 1)]
+                                                + c->ftnw[p] * zwx[I2(ji - 1, jj)] + c->ftne[p] * zwx[p]);
+        }
+      }
+    /* bottom stress (:1072-1079) */
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t p = I2(ji, jj);
+        zu_trd[p] = zu_trd[p] + zCdU_u[p] * c->un_e[p] * c->hur_e[p];
+        zv_trd[p] = zv_trd[p] + zCdU_v[p] * c->vn_e[p] * c->hvr_e[p];
+      }
+    /* surface pressure gradient (:1093-1101) */
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t p = I2(ji, jj);
+        double zu_spg = -grav * (zsshp2_e[I2(ji + 1, jj)] - zsshp2_e[p]) * c->r1_e1u[p];
+        double zv_spg = -grav * (zsshp2_e[I2(ji, jj + 1)] - zsshp2_e[p]) * c->r1_e2v[p];
+        zwx[p] = (1.0 - nm->rn_scal_load) * zu_spg;
+        zwy[p] = (1.0 - nm->rn_scal_load) * zv_spg;
+      }
+    /* next velocities, vector form (:1106-1122) */
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t p = I2(ji, jj);
+        c->ua_e[p] = (c->un_e[p] + rdtbt * (zwx[p] + zu_trd[p] + zu_frc[p])) * ssumask[p];
+        c->va_e[p] = (c->vn_e[p] + rdtbt * (zwy[p] + zv_trd[p] + zv_frc[p])) * ssvmask[p];
+      }
+    lbc_closed(jpi, jpj, c->ua_e, 1, 'U', 0.0);
+    lbc_closed(jpi, jpj, c->va_e, 1, 'V', 0.0);
+    /* swap (:1176-1186) */
+    for (size_t p = 0; p < n2; ++p) {
+      c->ubb_e[p] = c->ub_e[p]; c->ub_e[p] = c->un_e[p]; c->un_e[p] = c->ua_e[p];
+      c->vbb_e[p] = c->vb_e[p]; c->vb_e[p] = c->vn_e[p]; c->vn_e[p] = c->va_e[p];
+      c->sshbb_e[p] = c->sshb_e[p]; c->sshb_e[p] = c->sshn_e[p]; c->sshn_e[p] = c->ssha_e[p];
+    }
+    /* sums (:1190-1204) */
+    za1 = c->wgtbtp1[jn - 1];
+    for (size_t p = 0; p < n2; ++p) {
+      ua_b[p] = ua_b[p] + za1 * c->ua_e[p];
+      va_b[p] = va_b[p] + za1 * c->va_e[p];
+      ssha[p] = ssha[p] + za1 * c->ssha_e[p];
+    }
+  }
+  (void)ln_dynadv_vec;
+  /* Phase 3 (:1214-1269) */
+  if (ln_bt_fw) {
+    for (size_t p = 0; p < n2; ++p) {
+      zwx[p] = un_adv[p];
+      zwy[p] = vn_adv[p];
+      if (!(kt == nm->nit000 && nm->neuler == 0)) {
+        un_adv[p] = r1_2 * (ub2_b[p] + zwx[p] - nm->rn_atfp * un_bf[p]);
+        vn_adv[p] = r1_2 * (vb2_b[p] + zwy[p] - nm->rn_atfp * vn_bf[p]);
+        un_bf[p] = nm->rn_atfp * un_bf[p] + (zwx[p] - ub2_b[p]);
+        vn_bf[p] = nm->rn_atfp * vn_bf[p] + (zwy[p] - vb2_b[p]);
+      } else {
+        un_bf[p] = 0.0;
+        vn_bf[p] = 0.0;
+      }
+      ub2_b[p] = zwx[p];
+      vb2_b[p] = zwy[p];
+    }
+  }
+  for (int jk = 1; jk <= jpk - 1; ++jk)
+    for (size_t p = 0; p < n2; ++p) {
+      size_t q = p + n2 * (jk - 1);
+      ua[q] = ua[q] + (ua_b[p] - ub_b[p]) * r1_2dt_b;
+      va[q] = va[q] + (va_b[p] - vb_b[p]) * r1_2dt_b;
+    }
+  for (int jk = 1; jk <= jpk - 1; ++jk)
+    for (size_t p = 0; p < n2; ++p) {
+      size_t q = p + n2 * (jk - 1);
+      un[q] = (un[q] + un_adv[p] * r1_hu_n[p] - un_b[p]) * umask[q];
+      vn[q] = (vn[q] + vn_adv[p] * r1_hv_n[p] - vn_b[p]) * vmask[q];
+    }
+  free(zu_frc); free(zv_frc); free(zu_trd); free(zv_trd); free(zwx); free(zwy); free(zssh_frc); free(zhdiv);
+  free(zsshp2_e); free(zCdU_u); free(zCdU_v);
+  return NEMO_OK;
+}
+
+/* ---------------------------------------------------------------- glob_sum */
+/* DDPDD, lib_fortran.F90:300-332 */
+static void ddpdd(double a_re, double *b_re, double *b_im) {
+  double zt1 = a_re + *b_re;
+  double zerr = zt1 - a_re;
+  double zt2 = ((*b_re - zerr) + (a_re - (zt1 - zerr))) + 0.0 + *b_im;
+  double s = zt1 + zt2;
+  *b_im = zt2 - ((zt1 + zt2) - zt1);
+  *b_re = s;
+}
+
+/* lib_fortran_generic.h90:32-65 (OPERATION_GLOBSUM: mask tmask_i) */
+int ora_glob_sum(ora_ctx *c, const double *ptab, int nk, double *out) {
+  const int jpi = c->jpi, jpj = c->jpj;
+  double re = 0.0, im = 0.0;
+  for (int jk = 1; jk <= nk; ++jk)
+    for (int jj = 1; jj <= jpj; ++jj)
+      for (int ji = 1; ji <= jpi; ++ji) {
+        double ztmp = ptab[I2(ji, jj) + (size_t)jpi * jpj * (jk - 1)] * c->tmask_i[I2(ji, jj)];
+        ddpdd(ztmp, &re, &im);
+      }
+  *out = re;
+  return NEMO_OK;
+}
+
+/* ---------------------------------------------------------- one hot-path step */
+/* step.F90:194-257 on the bound fields: dyn_spg_ts, tsa = 0, tra_adv (transports
+ * + FCT), tra_ldf (iso or lap), tra_zdf. FCT orders come from kn_fct_h/v = 2. */
+int ora_stp_hotpath(ora_ctx *c, int kt) {
+  const nemo_namelist *nm = &c->nam;
+  const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk;
+  double *tsb = c->f[NEMO_F_TSB], *tsn = c->f[NEMO_F_TSN], *tsa = c->f[NEMO_F_TSA];
+  if (!tsb || !tsn || !tsa || !c->f[NEMO_F_UN] || !c->f[NEMO_F_VN] || !c->f[NEMO_F_WN]) return NEMO_ERR_UNBOUND;
+  int st = ora_dyn_spg_ts(c, kt);
+  if (st) return st;
+  memset(tsa, 0, 2 * n3 * sizeof(double));
+  double r2dt = (nm->neuler == 0 && kt == nm->nit000) ? nm->rn_rdt : 2.0 * nm->rn_rdt;
+  double *zun = zalloc(n3), *zvn = zalloc(n3), *zwn = zalloc(n3);
+  ora_tra_adv_trp(c, c->f[NEMO_F_UN], c->f[NEMO_F_VN], c->f[NEMO_F_WN], zun, zvn, zwn);
+  st = ora_tra_adv_fct(c, kt, nm->nit000, "TRA", r2dt, zun, zvn, zwn, tsb, tsn, tsa, 2, 2, 2);
+  free(zun); free(zvn); free(zwn);
+  if (st) return st;
+  const double *ahtu = c->f[NEMO_F_AHTU], *ahtv = c->f[NEMO_F_AHTV];
+  if (nm->ln_traldf_iso)
+    st = ora_tra_ldf_iso(c, kt, nm->nit000, "TRA", ahtu, ahtv, c->f[NEMO_F_GTSU], c->f[NEMO_F_GTSV],
+                         c->f[NEMO_F_GTUI], c->f[NEMO_F_GTVI], tsb, tsb, tsa, 2, 1);
+  else
+    st = ora_tra_ldf_lap(c, kt, nm->nit000, "TRA", ahtu, ahtv, c->f[NEMO_F_GTSU], c->f[NEMO_F_GTSV],
+                         c->f[NEMO_F_GTUI], c->f[NEMO_F_GTVI], tsb, tsa, 2, 1);
+  if (st) return st;
+  return ora_tra_zdf(c, kt);
+}

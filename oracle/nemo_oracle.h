@@ -1,0 +1,68 @@
+/*
+ * nemo_oracle.h -- CPU FP64 restatement of NEMO 4.0's per-timestep stencil path.
+ *
+ * TEST INFRASTRUCTURE ONLY. This is the checker the parity tests, the smoke test
+ * and the CPU-baseline leg of the benchmark compare the CUDA library against; it is
+ * never linked into, loaded by or called from the product path.
+ *
+ * Parity status: UNPINNED against the reference's own outputs. NEMO cannot be built
+ * in this environment (no Fortran compiler, MPI or NetCDF) and its tree ships no
+ * golden vectors or known-answer tests for these routines. Each function below
+ * restates the cited Fortran line for line (same loop bounds, same expression
+ * association, no FMA contraction: build with -ffp-contract=off) and is pinned by
+ * the analytic known-answer properties in tests/test_oracle_kat.py.
+ *
+ * The functions mirror the C ABI of include/nemo_gpu.h with host pointers and an
+ * ora_ prefix, for one ensemble member; the module-global fields are bound with
+ * ora_bind() using the same enum nemo_field_id.
+ */
+#ifndef NEMO_ORACLE_H
+#define NEMO_ORACLE_H
+
+#include "../include/nemo_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ora_ctx ora_ctx;
+
+int ora_create(const nemo_dom_desc *dom, const nemo_namelist *nam, ora_ctx **out);
+int ora_destroy(ora_ctx *c);
+int ora_bind(ora_ctx *c, int field_id, double *host_ptr);
+int ora_spg_info(const ora_ctx *c, int *icycle, int *nn_baro, double *rdtbt);
+/* Derived domain arrays for inspection: name in tmask, umask, vmask, wmask (3-D),
+ * ssmask, ssumask, ssvmask, tmask_i, ht_0, hu_0, hv_0, r1_hu_0, r1_hv_0, e1e2t,
+ * r1_e1e2t (2-D), wgtbtp1, wgtbtp2 (3*nn_baro). Returns NULL for an unknown name. */
+const double *ora_array(const ora_ctx *c, const char *name);
+const int *ora_iarray(const ora_ctx *c, const char *name); /* mikt mbkt mbku mbkv */
+
+int ora_tra_adv_trp(ora_ctx *c, const double *un, const double *vn, const double *wn,
+                    double *zun, double *zvn, double *zwn);
+int ora_tra_adv_fct(ora_ctx *c, int kt, int kit000, const char *cdtype, double p2dt,
+                    const double *pun, const double *pvn, const double *pwn,
+                    const double *ptb, const double *ptn, double *pta,
+                    int kjpt, int kn_fct_h, int kn_fct_v);
+int ora_interp_4th_cpt(ora_ctx *c, const double *pt_in, double *pt_out);
+int ora_tra_ldf_lap(ora_ctx *c, int kt, int kit000, const char *cdtype,
+                    const double *pahu, const double *pahv,
+                    const double *pgu, const double *pgv, const double *pgui, const double *pgvi,
+                    const double *ptb, double *pta, int kjpt, int kpass);
+int ora_tra_ldf_iso(ora_ctx *c, int kt, int kit000, const char *cdtype,
+                    const double *pahu, const double *pahv,
+                    const double *pgu, const double *pgv, const double *pgui, const double *pgvi,
+                    const double *ptb, const double *ptbb, double *pta, int kjpt, int kpass);
+int ora_tra_zdf_imp(ora_ctx *c, int kt, int kit000, const char *cdtype, double p2dt,
+                    const double *ptb, double *pta, int kjpt);
+int ora_tra_zdf(ora_ctx *c, int kt);
+int ora_dyn_spg_ts(ora_ctx *c, int kt);
+int ora_lbc_lnk(ora_ctx *c, double *ptab, int nk, int nl, char cd_nat, double psgn, double pval);
+int ora_glob_sum(ora_ctx *c, const double *ptab, int nk, double *out);
+int ora_stp_hotpath(ora_ctx *c, int kt);
+/* 1: start the work arrays standing for Fortran automatic arrays as NaN */
+void ora_set_poison(int on);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,158 @@
+"""ctypes wrapper of the oracle library (test infrastructure only).
+
+Mirrors the C ABI of include/nemo_gpu.h on host numpy arrays (one member).
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(os.path.dirname(HERE), "nemo-fmi-devel_gb300"))
+from nemo_gpu import _ffi  # noqa: E402
+
+from . import build as _build  # noqa: E402
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = C.CDLL(_build.build())
+        vp, i, d, cp = C.c_void_p, C.c_int, C.c_double, C.c_char_p
+        def P(name, argtypes, restype=C.c_int):
+            f = getattr(L, name)
+            f.argtypes, f.restype = argtypes, restype
+        P("ora_create", [C.POINTER(_ffi.DomDesc), C.POINTER(_ffi.Namelist), C.POINTER(vp)])
+        P("ora_destroy", [vp])
+        P("ora_bind", [vp, i, vp])
+        P("ora_spg_info", [vp, C.POINTER(i), C.POINTER(i), C.POINTER(d)])
+        P("ora_array", [vp, cp], C.POINTER(C.c_double))
+        P("ora_iarray", [vp, cp], C.POINTER(C.c_int))
+        P("ora_tra_adv_trp", [vp, vp, vp, vp, vp, vp, vp])
+        P("ora_tra_adv_fct", [vp, i, i, cp, d, vp, vp, vp, vp, vp, vp, i, i, i])
+        P("ora_interp_4th_cpt", [vp, vp, vp])
+        P("ora_tra_ldf_lap", [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
+        P("ora_tra_ldf_iso", [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
+        P("ora_tra_zdf_imp", [vp, i, i, cp, d, vp, vp, i])
+        P("ora_tra_zdf", [vp, i])
+        P("ora_dyn_spg_ts", [vp, i])
+        P("ora_lbc_lnk", [vp, vp, i, i, C.c_char, d, d])
+        P("ora_glob_sum", [vp, vp, i, C.POINTER(d)])
+        P("ora_stp_hotpath", [vp, i])
+        P("ora_set_poison", [i], None)
+        _lib = L
+    return _lib
+
+
+def set_poison(on):
+    """Start the oracle's automatic-array work buffers as NaN (1) or 0 (0)."""
+    lib().ora_set_poison(int(on))
+
+
+def _p(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and (a.flags.f_contiguous or a.ndim == 1), "oracle arrays: float64 Fortran order"
+    return a.ctypes.data
+
+
+class Oracle:
+    """One oracle context (one member)."""
+
+    def __init__(self, dom, nam):
+        self.dom, self.nam = dom, nam
+        self._desc = _ffi.make_desc(dom)
+        self._nl = _ffi.make_namelist(nam)
+        h = C.c_void_p()
+        st = lib().ora_create(C.byref(self._desc), C.byref(self._nl), C.byref(h))
+        if st:
+            raise RuntimeError(f"ora_create failed ({st})")
+        self.h = h
+        self.bound = {}
+        self.jpi, self.jpj, self.jpk = dom["jpi"], dom["jpj"], dom["jpk"]
+
+    def close(self):
+        if self.h:
+            lib().ora_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def bind(self, name, arr):
+        """Bind a float64 Fortran-order array to a module-global field (kept alive here)."""
+        self.bound[name] = arr
+        st = lib().ora_bind(self.h, _ffi.F[name], _p(arr))
+        assert st == 0
+
+    def spg_info(self):
+        ic, nb, dt = C.c_int(), C.c_int(), C.c_double()
+        lib().ora_spg_info(self.h, C.byref(ic), C.byref(nb), C.byref(dt))
+        return ic.value, nb.value, dt.value
+
+    def array(self, name, ndim=2):
+        p = lib().ora_array(self.h, name.encode())
+        if not p:
+            raise KeyError(name)
+        if name.startswith("wgtbtp"):
+            n = 3 * self.spg_info()[1]
+            return np.ctypeslib.as_array(p, shape=(n,)).copy()
+        shape = (self.jpi, self.jpj, self.jpk) if ndim == 3 else (self.jpi, self.jpj)
+        n = int(np.prod(shape))
+        return np.ctypeslib.as_array(p, shape=(n,)).copy().reshape(shape, order="F")
+
+    def iarray(self, name):
+        p = lib().ora_iarray(self.h, name.encode())
+        return np.ctypeslib.as_array(p, shape=(self.jpi * self.jpj,)).copy().reshape((self.jpi, self.jpj), order="F")
+
+    def _ck(self, st, what):
+        if st != 0:
+            raise RuntimeError(f"{what} failed with status {st}")
+
+    def tra_adv_trp(self, un, vn, wn):
+        out = [np.zeros_like(un, order="F") for _ in range(3)]
+        self._ck(lib().ora_tra_adv_trp(self.h, _p(un), _p(vn), _p(wn), *[_p(o) for o in out]), "tra_adv_trp")
+        return out
+
+    def tra_adv_fct(self, kt, kit000, cdtype, p2dt, pun, pvn, pwn, ptb, ptn, pta, kjpt, kh, kv):
+        self._ck(lib().ora_tra_adv_fct(self.h, kt, kit000, cdtype.encode(), p2dt, _p(pun), _p(pvn), _p(pwn),
+                                       _p(ptb), _p(ptn), _p(pta), kjpt, kh, kv), "tra_adv_fct")
+
+    def interp_4th_cpt(self, pt_in):
+        out = np.zeros_like(pt_in, order="F")
+        self._ck(lib().ora_interp_4th_cpt(self.h, _p(pt_in), _p(out)), "interp_4th_cpt")
+        return out
+
+    def tra_ldf_lap(self, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb, pta, kjpt, kpass):
+        self._ck(lib().ora_tra_ldf_lap(self.h, kt, kit000, cdtype.encode(), _p(pahu), _p(pahv), _p(pgu), _p(pgv),
+                                       _p(pgui), _p(pgvi), _p(ptb), _p(pta), kjpt, kpass), "tra_ldf_lap")
+
+    def tra_ldf_iso(self, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb, ptbb, pta, kjpt, kpass):
+        self._ck(lib().ora_tra_ldf_iso(self.h, kt, kit000, cdtype.encode(), _p(pahu), _p(pahv), _p(pgu), _p(pgv),
+                                       _p(pgui), _p(pgvi), _p(ptb), _p(ptbb), _p(pta), kjpt, kpass), "tra_ldf_iso")
+
+    def tra_zdf_imp(self, kt, kit000, cdtype, p2dt, ptb, pta, kjpt):
+        self._ck(lib().ora_tra_zdf_imp(self.h, kt, kit000, cdtype.encode(), p2dt, _p(ptb), _p(pta), kjpt),
+                 "tra_zdf_imp")
+
+    def tra_zdf(self, kt):
+        self._ck(lib().ora_tra_zdf(self.h, kt), "tra_zdf")
+
+    def dyn_spg_ts(self, kt):
+        self._ck(lib().ora_dyn_spg_ts(self.h, kt), "dyn_spg_ts")
+
+    def lbc_lnk(self, a, nat, pval=0.0):
+        nk = 1 if a.ndim == 2 else int(np.prod(a.shape[2:]))
+        self._ck(lib().ora_lbc_lnk(self.h, _p(a), nk, 1, nat.encode(), 1.0, pval), "lbc_lnk")
+
+    def glob_sum(self, a):
+        nk = 1 if a.ndim == 2 else a.shape[2]
+        out = C.c_double()
+        self._ck(lib().ora_glob_sum(self.h, _p(a), nk, C.byref(out)), "glob_sum")
+        return out.value
+
+    def stp_hotpath(self, kt):
+        self._ck(lib().ora_stp_hotpath(self.h, kt), "stp_hotpath")

@@ -1,0 +1,108 @@
+"""Shared set-up of the parity tests: one oracle per member and one GPU context
+over the same seeded GYRE state, with the module-global fields bound on both."""
+import numpy as np
+
+from nemo_gpu import _ffi, gyre
+
+FIELDS_3D = ("un", "vn", "wn", "ub", "vb", "ua", "va", "avt", "uslp", "vslp", "wslpi", "wslpj")
+FIELDS_2D = ("sshn", "sshb", "un_b", "vn_b", "ub_b", "vb_b", "utau", "vtau", "emp")
+ACC_2D = ("SSHA", "UA_B", "VA_B", "UN_ADV", "VN_ADV", "UB2_B", "VB2_B", "UN_BF", "VN_BF")
+
+
+def relerr(ref, got):
+    """Normwise relative error max|got - ref| / max|ref| (0 when both are 0)."""
+    ref = np.asarray(ref, dtype=np.float64)
+    got = np.asarray(got, dtype=np.float64)
+    d = np.abs(got - ref).max() if ref.size else 0.0
+    s = np.abs(ref).max() if ref.size else 0.0
+    return 0.0 if d == 0 else d / (s if s > 0 else 1.0)
+
+
+class Pair:
+    """Oracle(s) and a GPU context holding identical inputs."""
+
+    def __init__(self, nn=1, prec="fp64", nmem=1, seed=0, states=None, **nam_over):
+        from nemo_gpu import api
+        from oracle import ora
+        self.dom = gyre.domain(nn)
+        self.nam = gyre.namelist(**nam_over)
+        self.nmem = nmem
+        self.states = states or [gyre.state(self.dom, self.nam, seed=seed, member=m) for m in range(nmem)]
+        self.ora = [ora.Oracle(self.dom, self.nam) for _ in range(nmem)]
+        self.ctx = api.Context(self.dom, self.nam, nmembers=nmem, prec=prec)
+        self.torch = self.ctx.torch
+        self.host = [dict() for _ in range(nmem)]   # arrays bound to each oracle
+        self.dev = {}                                # tensors bound to the GPU context
+        jpi, jpj, jpk = self.dom["jpi"], self.dom["jpj"], self.dom["jpk"]
+        self.s2, self.s3, self.s4 = (jpi, jpj), (jpi, jpj, jpk), (jpi, jpj, jpk, 2)
+
+    # -- helpers
+    def to_dev(self, arrays, fp64=False):
+        return self.ctx.to_device(arrays, dtype=self.torch.float64 if fp64 else None)
+
+    def per_member(self, t, shape):
+        out = self.ctx.to_host(t, shape)
+        return out if isinstance(out, list) else [out]
+
+    def bind(self, name, key=None, zero=False, shape=None, fp64=None):
+        """Bind state[key] (or zeros) as field NAME on every oracle and on the GPU."""
+        key = key or name.lower()
+        arrs = []
+        for m in range(self.nmem):
+            if zero:
+                a = np.zeros(shape, order="F")
+            else:
+                a = np.array(self.states[m][key], dtype=np.float64, order="F", copy=True)
+            self.host[m][name] = a
+            self.ora[m].bind(name, a)
+            arrs.append(a)
+        if fp64 is None:
+            fp64 = name in _ffi.FP64_FIELDS
+        t = self.to_dev(arrs, fp64=fp64)
+        self.dev[name] = t
+        self.ctx.bind(name, t)
+        return t
+
+    def bind_iso(self):
+        for n in ("USLP", "VSLP", "WSLPI", "WSLPJ"):
+            self.bind(n)
+        self.bind("AH_WSLP2", zero=True, shape=self.s3)
+        self.bind("AKZ", zero=True, shape=self.s3)
+
+    def bind_spg(self):
+        for n in ("UA", "VA", "UN", "VN", "UB", "VB"):
+            self.bind(n)
+        for n in FIELDS_2D:
+            self.bind(n.upper())
+        self.bind("RCDU_BOT", key="rcdu_bot")
+        for n in ACC_2D:
+            self.bind(n, zero=True, shape=self.s2)
+
+    def bind_hotpath(self):
+        self.bind("TSB", key="tsb")
+        self.bind("TSN", key="tsn")
+        self.bind("TSA", zero=True, shape=self.s4)
+        self.bind("WN")
+        self.bind("AVT")
+        self.bind_iso()
+        self.bind_spg()
+
+    def compare(self, name, shape, tol, mask=None, report=None):
+        """Check the GPU field NAME against every oracle member; return the worst error."""
+        got = self.per_member(self.dev[name], shape)
+        worst = 0.0
+        exact = 0
+        total = 0
+        for m in range(self.nmem):
+            ref = self.host[m][name]
+            g = got[m]
+            if mask is not None:
+                ref, g = ref[mask], g[mask]
+            e = relerr(ref, g)
+            worst = max(worst, e)
+            exact += int((np.asarray(ref) == np.asarray(g)).sum())
+            total += np.asarray(ref).size
+        if report is not None:
+            report[name] = (worst, exact / max(total, 1))
+        assert worst <= tol, f"{name}: relative error {worst:.3e} > {tol:.1e}"
+        return worst
