@@ -264,6 +264,14 @@ int nemo_gpu_stp_hotpath(nemo_ctx *ctx, int kt);
 int nemo_gpu_set_timing(nemo_ctx *ctx, int on);
 int nemo_gpu_get_timing(nemo_ctx *ctx, double *ms, int *ncalls);
 
+/* ------------------------------------------------------------ kernel choice */
+
+/* on = 1 (default): in a mixed-precision context whose configuration allows it
+ * (FCT 2/2, linear free surface, z-coordinate, constant eddy diffusivity,
+ * iso-neutral laplacian) nemo_gpu_stp_hotpath runs FCT advection and iso-neutral
+ * diffusion as one fused kernel; on = 0 forces the per-routine kernels. */
+int nemo_gpu_set_fusion(nemo_ctx *ctx, int on);
+
 /* ------------------------------------------------------------ test hook */
 
 /* Bound of the grid barriers of the persistent sub-step kernel: each wait gives up

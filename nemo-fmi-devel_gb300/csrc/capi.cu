@@ -84,6 +84,7 @@ struct nemo_ctx {
   bool graphs_ok = true;
   // per-routine timing of the hot path (the ln_timing of timing.F90:89-212)
   bool timing = false;
+  bool no_fusion = false;  // force the per-routine kernels (tests compare both)
   cudaEvent_t tev[5] = {};
   double tms[4] = {0, 0, 0, 0};
   int tcalls = 0;
@@ -638,6 +639,57 @@ int run_spg(nemo_ctx* c, int kt) {
   return NEMO_OK;
 }
 
+// The fused FCT + iso-neutral kernel covers the GYRE configuration of the mixed
+// form; anything else runs the per-routine kernels.
+bool fused_ok(nemo_ctx* c) {
+  const nemo_namelist& nm = c->nam;
+  if (c->prec != NEMO_PREC_MIXED || c->no_fusion) return false;
+  if (!nm.ln_linssh || nm.ln_zps || !nm.ln_traldf_iso || nm.ln_traldf_blp) return false;
+  if (c->f[NEMO_F_AHTU] || c->f[NEMO_F_AHTV]) return false;
+  for (int id : {NEMO_F_E3T_B, NEMO_F_E3T_N, NEMO_F_E3T_A, NEMO_F_E3U_N, NEMO_F_E3V_N, NEMO_F_E3W_N})
+    if (c->f[id]) return false;
+  for (int w = 0; w < 4; ++w)
+    if (!c->e3_uniform[w]) return false;
+  return true;
+}
+
+int run_tra_fused(nemo_ctx* c, int kt, double r2dt) {
+  const nemo_namelist& nm = c->nam;
+  void* const* F = c->f;
+  if (!F[NEMO_F_USLP] || !F[NEMO_F_VSLP] || !F[NEMO_F_WSLPI] || !F[NEMO_F_WSLPJ] || !F[NEMO_F_AH_WSLP2] ||
+      !F[NEMO_F_AKZ])
+    return fail(c, NEMO_ERR_UNBOUND, "tra_ldf_iso: slopes, ah_wslp2 and akz must be bound");
+  FusedArgs<float> a{};
+  a.p2dt = (float)r2dt;
+  a.un = (const float*)F[NEMO_F_UN]; a.vn = (const float*)F[NEMO_F_VN]; a.wn = (const float*)F[NEMO_F_WN];
+  a.tb = (const float*)F[NEMO_F_TSB]; a.tn = (const float*)F[NEMO_F_TSN]; a.ta = (float*)F[NEMO_F_TSA];
+  a.uslp = (const float*)F[NEMO_F_USLP]; a.vslp = (const float*)F[NEMO_F_VSLP];
+  a.wslpi = (const float*)F[NEMO_F_WSLPI]; a.wslpj = (const float*)F[NEMO_F_WSLPJ];
+  a.ah_wslp2 = (float*)F[NEMO_F_AH_WSLP2]; a.akz = (float*)F[NEMO_F_AKZ];
+  a.aht_c = (float)nm.rn_aht_0;
+  a.lap = nm.ln_traldf_lap; a.msc = nm.ln_traldf_msc; a.linssh = nm.ln_linssh;
+  const double z2dt = (nm.neuler == 0 && kt == nm.nit000) ? nm.rn_rdt : 2.0 * nm.rn_rdt;
+  a.z2dt = (float)z2dt; a.z1_2dt = (float)(1.0 / z2dt);
+  const Dom<float> d = dom_now<float>(c);
+  if (kt == nm.nit000) {
+    const size_t bytes = c->n3 * c->nmem * sizeof(float);
+    CK(cudaMemsetAsync(a.akz, 0, bytes, c->stream), "akz = 0");
+    CK(cudaMemsetAsync(a.ah_wslp2, 0, bytes, c->stream), "ah_wslp2 = 0");
+  }
+  cudaError_t e = launch_tra_fused(d, a, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "fused tracer kernel launch");
+  // tsa = 0 on the edge columns (the fused kernel writes the interior columns)
+  e = launch_lbc<float>((float*)F[NEMO_F_TSA], c->jpi, c->jpj, 2L * c->jpk * c->nmem, 0, 0.0f, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "tsa edges");
+  if (!nm.ln_traldf_msc) {
+    LdfArgs<float> la{};
+    la.ah_wslp2 = a.ah_wslp2; la.akz = a.akz;
+    e = launch_iso_akz_edges<float>(d, la, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "akz edges");
+  }
+  return NEMO_OK;
+}
+
 template <class T>
 int run_hotpath(nemo_ctx* c, int kt) {
   const nemo_namelist& nm = c->nam;
@@ -650,6 +702,25 @@ int run_hotpath(nemo_ctx* c, int kt) {
   if (s) return s;
   mark(1);
   const double r2dt = (nm.neuler == 0 && kt == nm.nit000) ? nm.rn_rdt : 2.0 * nm.rn_rdt;
+  if (fused_ok(c)) {
+    s = run_tra_fused(c, kt, r2dt);
+    if (s) return s;
+    mark(2);
+    mark(3);
+    s = run_zdf<T>(c, r2dt, F[NEMO_F_TSB], F[NEMO_F_TSA], 2, 0, 1);
+    if (s) return s;
+    if (c->timing) {
+      mark(4);
+      CK(cudaEventSynchronize(c->tev[4]), "timing");
+      for (int i = 0; i < 4; ++i) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c->tev[i], c->tev[i + 1]);
+        c->tms[i] += ms;
+      }
+      c->tcalls += 1;
+    }
+    return NEMO_OK;
+  }
   // tsa = 0 (step.F90:234) folded into the first trend (pta_in = NULL)
   s = run_fct<T>(c, r2dt, F[NEMO_F_UN], F[NEMO_F_VN], F[NEMO_F_WN], 1, F[NEMO_F_TSB], F[NEMO_F_TSN], nullptr,
                  F[NEMO_F_TSA], 2, 2, 2);
@@ -995,6 +1066,14 @@ int nemo_gpu_get_timing(nemo_ctx* c, double* ms, int* ncalls) {
   if (!c || !ms) return NEMO_ERR_ARG;
   for (int i = 0; i < 4; ++i) ms[i] = c->tms[i];
   if (ncalls) *ncalls = c->tcalls;
+  return NEMO_OK;
+}
+
+int nemo_gpu_set_fusion(nemo_ctx* c, int on) {
+  if (!c) return NEMO_ERR_ARG;
+  c->no_fusion = !on;
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);
+  c->graphs.clear();
   return NEMO_OK;
 }
 

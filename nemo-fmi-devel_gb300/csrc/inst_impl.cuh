@@ -45,6 +45,12 @@ cudaError_t launch_ldf_iso(const Dom<T>& d, const LdfArgs<T>& a, int copy_akz_ed
 }
 
 template <class T>
+cudaError_t launch_iso_akz_edges(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s) {
+  k_iso_akz_copy_edges<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  return cudaGetLastError();
+}
+
+template <class T>
 cudaError_t launch_zdf(const Dom<T>& d, const ZdfArgs<T>& a, cudaStream_t s) {
   k_zdf_imp<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
   return cudaGetLastError();
@@ -109,6 +115,7 @@ cudaError_t launch_globsum(const T* x, const double* tmask_i, long n2, int nk, i
   template cudaError_t launch_ldf_lap<T>(const Dom<T>&, const LdfArgs<T>&, cudaStream_t);                    \
   template cudaError_t launch_ldf_iso<T>(const Dom<T>&, const LdfArgs<T>&, int, int, cudaStream_t);          \
   template cudaError_t launch_zdf<T>(const Dom<T>&, const ZdfArgs<T>&, cudaStream_t);                        \
+  template cudaError_t launch_iso_akz_edges<T>(const Dom<T>&, const LdfArgs<T>&, cudaStream_t);              \
   template cudaError_t launch_clamp<T>(T*, long, cudaStream_t);                                              \
   template cudaError_t launch_spg<T>(const Dom<T>&, const SpgArgs<T>&, const GridBar&, int, cudaStream_t);   \
   template int spg_p2_blocks_per_sm<T>();                                                                    \

@@ -631,12 +631,25 @@ __global__ void k_zdf_imp(Dom<T> d, ZdfArgs<T> a) {
         return v;
       };
       T wtk = wt(1);
+      T g = T(0);
       for (int k = 1; k <= jpk - 1; ++k) {
         const T wtk1 = wt(k + 1);
         zwi[k] = -a.p2dt * wtk / d.e3w_n(c.ij, k, c.m);
         zws[k] = -a.p2dt * wtk1 / d.e3w_n(c.ij, k + 1, c.m);
-        const T zwd = d.e3t_a(c.ij, k, c.m) - zwi[k] - zws[k];
-        zwt[k] = (k == 1) ? zwd : zwd - zwi[k] * zws[k - 1] / zwt[k - 1];
+        const T e3a = d.e3t_a(c.ij, k, c.m);
+        if constexpr (sizeof(T) == 8) {
+          // 1st recurrence as written in the reference (trazdf.F90:223-234)
+          const T zwd = e3a - zwi[k] - zws[k];
+          zwt[k] = (k == 1) ? zwd : zwd - zwi[k] * zws[k - 1] / zwt[k - 1];
+        } else {
+          // FP32: the same pivots without cancellation. With g(k) = zwt(k) + zws(k),
+          // zwt(k) = zwd(k) - zwi(k) zws(k-1)/zwt(k-1) is g(k) - zws(k) where
+          // g(k) = e3t_a(k) - zwi(k) g(k-1)/zwt(k-1): a sum of non-negative terms
+          // (zwi, zws <= 0), whereas zwd - zwi zws/zwt cancels to O(e3t) from
+          // O(p2dt avt/e3w) when the vertical diffusivity is large.
+          g = (k == 1) ? e3a - zwi[k] : e3a - zwi[k] * (g / zwt[k - 1]);
+          zwt[k] = g - zws[k];
+        }
         wtk = wtk1;
       }
     }

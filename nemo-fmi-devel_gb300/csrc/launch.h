@@ -3,6 +3,7 @@
 #pragma once
 #include "k_dyn.cuh"
 #include "k_tra.cuh"
+#include "k_fused.cuh"
 
 namespace nemo {
 
@@ -16,6 +17,8 @@ cudaError_t launch_ldf_lap(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s)
 template <class T>
 cudaError_t launch_ldf_iso(const Dom<T>& d, const LdfArgs<T>& a, int copy_akz_edges, int msc_edges, cudaStream_t s);
 template <class T>
+cudaError_t launch_iso_akz_edges(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s);
+template <class T>
 cudaError_t launch_zdf(const Dom<T>& d, const ZdfArgs<T>& a, cudaStream_t s);
 template <class T>
 cudaError_t launch_clamp(T* x, long n, cudaStream_t s);
@@ -28,5 +31,8 @@ cudaError_t launch_lbc(T* p, int jpi, int jpj, long nslab, int is_f, T pval, cud
 template <class T>
 cudaError_t launch_globsum(const T* x, const double* tmask_i, long n2, int nk, int nmem, double* part, int nblk,
                            double* out, cudaStream_t s);
+
+// fused FCT + iso-neutral tracer kernel (float only)
+cudaError_t launch_tra_fused(const Dom<float>& d, const FusedArgs<float>& a, cudaStream_t s);
 
 }  // namespace nemo

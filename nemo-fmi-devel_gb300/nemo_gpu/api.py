@@ -120,6 +120,9 @@ class Context:
     def set_barrier_limit(self, max_spins, extra_arrivals=0):
         self._ck(self.lib.nemo_gpu_set_barrier_limit(self.h, max_spins, extra_arrivals), "set_barrier_limit")
 
+    def set_fusion(self, on):
+        self._ck(self.lib.nemo_gpu_set_fusion(self.h, int(on)), "set_fusion")
+
     def set_timing(self, on):
         self._ck(self.lib.nemo_gpu_set_timing(self.h, int(on)), "set_timing")
 

@@ -20,6 +20,14 @@
 #include <stdlib.h>
 #include <string.h>
 
+/* Loops whose iterations write disjoint points run in parallel for the CPU
+ * baseline; every point is computed by the same operations in the same order. */
+#ifdef _OPENMP
+#define OMP_FOR _Pragma("omp parallel for schedule(static)")
+#else
+#define OMP_FOR
+#endif
+
 #define I2(i, j) ((size_t)((i)-1) + (size_t)jpi * (size_t)((j)-1))
 #define I3(i, j, k) (I2(i, j) + (size_t)jpi * (size_t)jpj * (size_t)((k)-1))
 #define I4(i, j, k, n) (I3(i, j, k) + (size_t)jpi * (size_t)jpj * (size_t)jpk * (size_t)((n)-1))
@@ -335,6 +343,7 @@ int ora_tra_adv_trp(ora_ctx *c, const double *un, const double *vn, const double
   const size_t n2 = (size_t)jpi * jpj;
   const double *e3u = fld(c, NEMO_F_E3U_N), *e3v = fld(c, NEMO_F_E3V_N);
   for (size_t p = 0; p < n2; ++p) { zun[p + n2 * (jpk - 1)] = 0; zvn[p + n2 * (jpk - 1)] = 0; zwn[p + n2 * (jpk - 1)] = 0; }
+  OMP_FOR
   for (int jk = 1; jk <= jpk - 1; ++jk)
     for (size_t p = 0; p < n2; ++p) {
       size_t q = p + n2 * (jk - 1);
@@ -378,12 +387,14 @@ int ora_interp_4th_cpt(ora_ctx *c, const double *pt_in, double *pt_out) {
   for (int jj = 2; jj <= jpj - 1; ++jj)
     for (int ji = 2; ji <= jpi - 1; ++ji) zwt[I3(ji, jj, 2)] = zwd[I3(ji, jj, 2)];
   for (int jk = 3; jk <= jpk - 1; ++jk)
+    OMP_FOR
     for (int jj = 2; jj <= jpj - 1; ++jj)
       for (int ji = 2; ji <= jpi - 1; ++ji)
         zwt[I3(ji, jj, jk)] = zwd[I3(ji, jj, jk)] - zwi[I3(ji, jj, jk)] * zws[I3(ji, jj, jk - 1)] / zwt[I3(ji, jj, jk - 1)];
   for (int jj = 2; jj <= jpj - 1; ++jj)
     for (int ji = 2; ji <= jpi - 1; ++ji) pt_out[I3(ji, jj, 2)] = zwrm[I3(ji, jj, 2)];
   for (int jk = 3; jk <= jpk - 1; ++jk)
+    OMP_FOR
     for (int jj = 2; jj <= jpj - 1; ++jj)
       for (int ji = 2; ji <= jpi - 1; ++ji)
         pt_out[I3(ji, jj, jk)] = zwrm[I3(ji, jj, jk)] - zwi[I3(ji, jj, jk)] / zwt[I3(ji, jj, jk - 1)] * pt_out[I3(ji, jj, jk - 1)];
@@ -391,6 +402,7 @@ int ora_interp_4th_cpt(ora_ctx *c, const double *pt_in, double *pt_out) {
     for (int ji = 2; ji <= jpi - 1; ++ji)
       pt_out[I3(ji, jj, jpk - 1)] = pt_out[I3(ji, jj, jpk - 1)] / zwt[I3(ji, jj, jpk - 1)];
   for (int jk = jpk - 2; jk >= 2; --jk)
+    OMP_FOR
     for (int jj = 2; jj <= jpj - 1; ++jj)
       for (int ji = 2; ji <= jpi - 1; ++ji)
         pt_out[I3(ji, jj, jk)] = (pt_out[I3(ji, jj, jk)] - zws[I3(ji, jj, jk)] * pt_out[I3(ji, jj, jk + 1)]) / zwt[I3(ji, jj, jk)];
@@ -411,6 +423,7 @@ static void nonosc(ora_ctx *c, const double *pbef, double *paa, double *pbb, dou
     zbup[q] = dmax(pbef[q] * tmask[q] - zbig * (1.0 - tmask[q]), paft[q] * tmask[q] - zbig * (1.0 - tmask[q]));
     zbdo[q] = dmin(pbef[q] * tmask[q] + zbig * (1.0 - tmask[q]), paft[q] * tmask[q] + zbig * (1.0 - tmask[q]));
   }
+  OMP_FOR
   for (int jk = 1; jk <= jpk - 1; ++jk) {
     int ikm1 = jk - 1 > 1 ? jk - 1 : 1;
     for (int jj = 2; jj <= jpj - 1; ++jj)
@@ -436,6 +449,7 @@ static void nonosc(ora_ctx *c, const double *pbef, double *paa, double *pbb, dou
   }
   lbc_closed(jpi, jpj, zbetup, jpk, 'T', 0.0);
   lbc_closed(jpi, jpj, zbetdo, jpk, 'T', 0.0);
+  OMP_FOR
   for (int jk = 1; jk <= jpk - 1; ++jk)
     for (int jj = 2; jj <= jpj - 1; ++jj)
       for (int ji = 2; ji <= jpi - 1; ++ji) {
@@ -481,6 +495,7 @@ int ora_tra_adv_fct(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
     const double *tb = ptb + n3 * (jn - 1), *tn = ptn + n3 * (jn - 1);
     double *ta = pta + n3 * (jn - 1);
     /* upstream fluxes (:123-135) */
+    OMP_FOR
     for (int jk = 1; jk <= jpk - 1; ++jk)
       for (int jj = 1; jj <= jpj - 1; ++jj)
         for (int ji = 1; ji <= jpi - 1; ++ji) {
@@ -493,6 +508,7 @@ int ora_tra_adv_fct(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
           zwy[q] = 0.5 * (zfp_vj * tb[q] + zfm_vj * tb[I3(ji, jj + 1, jk)]);
         }
     /* (:137-145) */
+    OMP_FOR
     for (int jk = 2; jk <= jpk - 1; ++jk)
       for (int jj = 1; jj <= jpj; ++jj)
         for (int ji = 1; ji <= jpi; ++ji) {
@@ -505,6 +521,7 @@ int ora_tra_adv_fct(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
     if (c->nam.ln_linssh)
       for (size_t p = 0; p < n2; ++p) zwz[p] = pwn[p] * tb[p];
     /* (:158-170) */
+    OMP_FOR
     for (int jk = 1; jk <= jpk - 1; ++jk)
       for (int jj = 2; jj <= jpj - 1; ++jj)
         for (int ji = 2; ji <= jpi - 1; ++ji) {
@@ -516,6 +533,7 @@ int ora_tra_adv_fct(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
         }
     /* horizontal antidiffusive fluxes (:180-251) */
     if (kn_fct_h == 2) {
+      OMP_FOR
       for (int jk = 1; jk <= jpk - 1; ++jk)
         for (int jj = 1; jj <= jpj - 1; ++jj)
           for (int ji = 1; ji <= jpi - 1; ++ji) {
@@ -525,6 +543,7 @@ int ora_tra_adv_fct(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
           }
     } else {
       for (size_t p = 0; p < n2; ++p) { zltu[p + n2 * (jpk - 1)] = 0.0; zltv[p + n2 * (jpk - 1)] = 0.0; }
+      OMP_FOR
       for (int jk = 1; jk <= jpk - 1; ++jk) {
         for (int jj = 1; jj <= jpj - 1; ++jj)
           for (int ji = 1; ji <= jpi - 1; ++ji) {
@@ -541,6 +560,7 @@ int ora_tra_adv_fct(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
       }
       lbc_closed(jpi, jpj, zltu, jpk, 'T', 0.0);
       lbc_closed(jpi, jpj, zltv, jpk, 'T', 0.0);
+      OMP_FOR
       for (int jk = 1; jk <= jpk - 1; ++jk)
         for (int jj = 1; jj <= jpj - 1; ++jj)
           for (int ji = 1; ji <= jpi - 1; ++ji) {
@@ -553,6 +573,7 @@ int ora_tra_adv_fct(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
     }
     /* vertical antidiffusive fluxes (:253-275) */
     if (kn_fct_v == 2) {
+      OMP_FOR
       for (int jk = 2; jk <= jpk - 1; ++jk)
         for (int jj = 2; jj <= jpj - 1; ++jj)
           for (int ji = 2; ji <= jpi - 1; ++ji) {
@@ -561,6 +582,7 @@ int ora_tra_adv_fct(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
           }
     } else {
       ora_interp_4th_cpt(c, tn, ztw);
+      OMP_FOR
       for (int jk = 2; jk <= jpk - 1; ++jk)
         for (int jj = 2; jj <= jpj - 1; ++jj)
           for (int ji = 2; ji <= jpi - 1; ++ji) {
@@ -578,6 +600,7 @@ int ora_tra_adv_fct(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
     /* (:284) */
     nonosc(c, tb, zwx, zwy, zwz, zwi, p2dt);
     /* (:288-297) */
+    OMP_FOR
     for (int jk = 1; jk <= jpk - 1; ++jk)
       for (int jj = 2; jj <= jpj - 1; ++jj)
         for (int ji = 2; ji <= jpi - 1; ++ji) {
@@ -604,6 +627,7 @@ int ora_tra_ldf_lap(ora_ctx *c, int kt, int kit000, const char *cdtype,
   const double *e3u = fld(c, NEMO_F_E3U_N), *e3v = fld(c, NEMO_F_E3V_N), *e3t_n = fld(c, NEMO_F_E3T_N);
   double zsign = kpass == 1 ? 1.0 : -1.0;
   double *ztu = walloc(n3), *ztv = walloc(n3), *zaheeu = walloc(n3), *zaheev = walloc(n3);
+  OMP_FOR
   for (int jk = 1; jk <= jpk - 1; ++jk)
     for (int jj = 1; jj <= jpj - 1; ++jj)
       for (int ji = 1; ji <= jpi - 1; ++ji) {
@@ -614,6 +638,7 @@ int ora_tra_ldf_lap(ora_ctx *c, int kt, int kit000, const char *cdtype,
   for (int jn = 1; jn <= kjpt; ++jn) {
     const double *tb = ptb + n3 * (jn - 1);
     double *ta = pta + n3 * (jn - 1);
+    OMP_FOR
     for (int jk = 1; jk <= jpk - 1; ++jk)
       for (int jj = 1; jj <= jpj - 1; ++jj)
         for (int ji = 1; ji <= jpi - 1; ++ji) {
@@ -628,6 +653,7 @@ int ora_tra_ldf_lap(ora_ctx *c, int kt, int kit000, const char *cdtype,
           ztu[I3(ji, jj, ku)] = zaheeu[I3(ji, jj, ku)] * pgu[I2(ji, jj) + n2 * (jn - 1)];
           ztv[I3(ji, jj, kv)] = zaheev[I3(ji, jj, kv)] * pgv[I2(ji, jj) + n2 * (jn - 1)];
         }
+    OMP_FOR
     for (int jk = 1; jk <= jpk - 1; ++jk)
       for (int jj = 2; jj <= jpj - 1; ++jj)
         for (int ji = 2; ji <= jpi - 1; ++ji) {
@@ -668,6 +694,7 @@ int ora_tra_ldf_iso(ora_ctx *c, int kt, int kit000, const char *cdtype,
   double z1_2dt = 1.0 / z2dt;
   double zsign = kpass == 1 ? 1.0 : -1.0;
   if (kpass == 1) {
+    OMP_FOR
     for (int jk = 2; jk <= jpk - 1; ++jk)
       for (int jj = 2; jj <= jpj - 1; ++jj)
         for (int ji = 2; ji <= jpi - 1; ++ji) {
@@ -683,6 +710,7 @@ int ora_tra_ldf_iso(ora_ctx *c, int kt, int kit000, const char *cdtype,
           ah_wslp2[q] = zahu_w * wslpi[q] * wslpi[q] + zahv_w * wslpj[q] * wslpj[q];
         }
     if (nm->ln_traldf_msc) {
+      OMP_FOR
       for (int jk = 2; jk <= jpk - 1; ++jk)
         for (int jj = 2; jj <= jpj - 1; ++jj)
           for (int ji = 2; ji <= jpi - 1; ++ji) {
@@ -695,6 +723,7 @@ int ora_tra_ldf_iso(ora_ctx *c, int kt, int kit000, const char *cdtype,
                              + (pahv[I3(ji, jj - 1, jk)] + pahv[I3(ji, jj - 1, jk - 1)]) / (e2vm * e2vm));
           }
       if (nm->ln_traldf_blp) {
+        OMP_FOR
         for (int jk = 2; jk <= jpk - 1; ++jk)
           for (int jj = 1; jj <= jpj - 1; ++jj)
             for (int ji = 1; ji <= jpi - 1; ++ji) {
@@ -702,6 +731,7 @@ int ora_tra_ldf_iso(ora_ctx *c, int kt, int kit000, const char *cdtype,
               akz[q] = 16.0 * ah_wslp2[q] * (akz[q] + ah_wslp2[q] / (e3w[q] * e3w[q]));
             }
       } else if (nm->ln_traldf_lap) {
+        OMP_FOR
         for (int jk = 2; jk <= jpk - 1; ++jk)
           for (int jj = 1; jj <= jpj - 1; ++jj)
             for (int ji = 1; ji <= jpi - 1; ++ji) {
@@ -725,6 +755,7 @@ int ora_tra_ldf_iso(ora_ctx *c, int kt, int kit000, const char *cdtype,
         zdit[I3(1, jj, jk)] = 0.0; zdit[I3(jpi, jj, jk)] = 0.0;
         zdjt[I3(1, jj, jk)] = 0.0; zdjt[I3(jpi, jj, jk)] = 0.0;
       }
+    OMP_FOR
     for (int jk = 1; jk <= jpk - 1; ++jk)
       for (int jj = 1; jj <= jpj - 1; ++jj)
         for (int ji = 1; ji <= jpi - 1; ++ji) {
@@ -745,6 +776,7 @@ int ora_tra_ldf_iso(ora_ctx *c, int kt, int kit000, const char *cdtype,
       else
         for (size_t p = 0; p < n2; ++p)
           zdkt[p] = (tb[p + n2 * (jk - 2)] - tb[p + n2 * (jk - 1)]) * wmask[p + n2 * (jk - 1)];
+      OMP_FOR
       for (int jj = 1; jj <= jpj - 1; ++jj)
         for (int ji = 1; ji <= jpi - 1; ++ji) {
           size_t q = I3(ji, jj, jk);
@@ -761,6 +793,7 @@ int ora_tra_ldf_iso(ora_ctx *c, int kt, int kit000, const char *cdtype,
           zftv[q] = (zabe2 * zdjt[q] + zcof2 * (zdkt[I2(ji, jj + 1)] + zdk1t[I2(ji, jj)]
                                                 + zdk1t[I2(ji, jj + 1)] + zdkt[I2(ji, jj)])) * vmask[q];
         }
+      OMP_FOR
       for (int jj = 2; jj <= jpj - 1; ++jj)
         for (int ji = 2; ji <= jpi - 1; ++ji) {
           size_t q = I3(ji, jj, jk);
@@ -771,6 +804,7 @@ int ora_tra_ldf_iso(ora_ctx *c, int kt, int kit000, const char *cdtype,
     for (int jk = 1; jk <= jpk; ++jk)
       for (int jj = 1; jj <= jpj; ++jj) { ztfw[I3(1, jj, jk)] = 0.0; ztfw[I3(jpi, jj, jk)] = 0.0; }
     for (size_t p = 0; p < n2; ++p) { ztfw[p] = 0.0; ztfw[p + n2 * (jpk - 1)] = 0.0; }
+    OMP_FOR
     for (int jk = 2; jk <= jpk - 1; ++jk)
       for (int jj = 2; jj <= jpj - 1; ++jj)
         for (int ji = 2; ji <= jpi - 1; ++ji) {
@@ -791,6 +825,7 @@ int ora_tra_ldf_iso(ora_ctx *c, int kt, int kit000, const char *cdtype,
                               + zdjt[I3(ji, jj - 1, jk - 1)] + zdjt[q]);
         }
     if (nm->ln_traldf_lap) {
+      OMP_FOR
       for (int jk = 2; jk <= jpk - 1; ++jk)
         for (int jj = 1; jj <= jpj - 1; ++jj)
           for (int ji = 2; ji <= jpi - 1; ++ji) {
@@ -799,6 +834,7 @@ int ora_tra_ldf_iso(ora_ctx *c, int kt, int kit000, const char *cdtype,
                                     * (ah_wslp2[q] - akz[q]) * (tb[I3(ji, jj, jk - 1)] - tb[q]);
           }
     } else if (kpass == 1) {
+      OMP_FOR
       for (int jk = 2; jk <= jpk - 1; ++jk)
         for (int jj = 1; jj <= jpj - 1; ++jj)
           for (int ji = 2; ji <= jpi - 1; ++ji) {
@@ -806,6 +842,7 @@ int ora_tra_ldf_iso(ora_ctx *c, int kt, int kit000, const char *cdtype,
             ztfw[q] = ztfw[q] + ah_wslp2[q] * c->e1e2t[I2(ji, jj)] * (tb[I3(ji, jj, jk - 1)] - tb[q]) / e3w[q] * wmask[q];
           }
     } else {
+      OMP_FOR
       for (int jk = 2; jk <= jpk - 1; ++jk)
         for (int jj = 1; jj <= jpj - 1; ++jj)
           for (int ji = 2; ji <= jpi - 1; ++ji) {
@@ -815,6 +852,7 @@ int ora_tra_ldf_iso(ora_ctx *c, int kt, int kit000, const char *cdtype,
                                        + akz[q] * (tbb[I3(ji, jj, jk - 1)] - tbb[q]));
           }
     }
+    OMP_FOR
     for (int jk = 1; jk <= jpk - 1; ++jk)
       for (int jj = 2; jj <= jpj - 1; ++jj)
         for (int ji = 2; ji <= jpi - 1; ++ji) {
@@ -860,6 +898,7 @@ int ora_tra_zdf_imp(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
           for (int jj = 2; jj <= jpj - 1; ++jj)
             for (int ji = 2; ji <= jpi - 1; ++ji) zwt[I3(ji, jj, jk)] = zwt[I3(ji, jj, jk)] + add[I3(ji, jj, jk)];
       }
+      OMP_FOR
       for (int jk = 1; jk <= jpk - 1; ++jk)
         for (int jj = 2; jj <= jpj - 1; ++jj)
           for (int ji = 2; ji <= jpi - 1; ++ji) {
@@ -871,6 +910,7 @@ int ora_tra_zdf_imp(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
       for (int jj = 2; jj <= jpj - 1; ++jj)
         for (int ji = 2; ji <= jpi - 1; ++ji) zwt[I3(ji, jj, 1)] = zwd[I3(ji, jj, 1)];
       for (int jk = 2; jk <= jpk - 1; ++jk)
+        OMP_FOR
         for (int jj = 2; jj <= jpj - 1; ++jj)
           for (int ji = 2; ji <= jpi - 1; ++ji)
             zwt[I3(ji, jj, jk)] = zwd[I3(ji, jj, jk)] - zwi[I3(ji, jj, jk)] * zws[I3(ji, jj, jk - 1)] / zwt[I3(ji, jj, jk - 1)];
@@ -881,6 +921,7 @@ int ora_tra_zdf_imp(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
         ta[q] = e3t_b[q] * tb[q] + p2dt * e3t_n[q] * ta[q];
       }
     for (int jk = 2; jk <= jpk - 1; ++jk)
+      OMP_FOR
       for (int jj = 2; jj <= jpj - 1; ++jj)
         for (int ji = 2; ji <= jpi - 1; ++ji) {
           size_t q = I3(ji, jj, jk);
@@ -893,6 +934,7 @@ int ora_tra_zdf_imp(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
         ta[q] = ta[q] / zwt[q] * tmask[q];
       }
     for (int jk = jpk - 2; jk >= 1; --jk)
+      OMP_FOR
       for (int jj = 2; jj <= jpj - 1; ++jj)
         for (int ji = 2; ji <= jpi - 1; ++ji) {
           size_t q = I3(ji, jj, jk);
@@ -1052,6 +1094,7 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
       zv_frc[p] = zv_frc[p] + e3v[q] * va[q] * vmask[q];
     }
   for (size_t p = 0; p < n2; ++p) { zu_frc[p] = zu_frc[p] * r1_hu_n[p]; zv_frc[p] = zv_frc[p] * r1_hv_n[p]; }
+  OMP_FOR
   for (int jk = 1; jk <= jpk - 1; ++jk)
     for (int jj = 2; jj <= jpj - 1; ++jj)
       for (int ji = 2; ji <= jpi - 1; ++ji) {
@@ -1065,6 +1108,7 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
     zwy[p] = vn_b[p] * hv_n[p] * c->e1v[p];
   }
   const int sc = nm->nvor_scheme;
+  OMP_FOR
   for (int jj = 2; jj <= jpj - 1; ++jj)
     for (int ji = 2; ji <= jpi - 1; ++ji) {
       size_t p = I2(ji, jj);
@@ -1096,6 +1140,7 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
       }
     }
   /* (:511-516) */
+  OMP_FOR
   for (int jj = 2; jj <= jpj - 1; ++jj)
     for (int ji = 2; ji <= jpi - 1; ++ji) {
       size_t p = I2(ji, jj);
@@ -1103,6 +1148,7 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
       zv_frc[p] = zv_frc[p] - zv_trd[p] * ssvmask[p];
     }
   /* bottom stress from baroclinic velocities (:519-557) */
+  OMP_FOR
   for (int jj = 2; jj <= jpj - 1; ++jj)
     for (int ji = 2; ji <= jpi - 1; ++ji) {
       size_t p = I2(ji, jj);
@@ -1115,6 +1161,7 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
         zwy[p] = vb[I3(ji, jj, ikbv)] - vb_b[p];
       }
     }
+  OMP_FOR
   for (int jj = 2; jj <= jpj - 1; ++jj)
     for (int ji = 2; ji <= jpi - 1; ++ji) {
       size_t p = I2(ji, jj);
@@ -1122,6 +1169,7 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
       zv_frc[p] = zv_frc[p] + r1_hv_n[p] * r1_2 * (rCdU_bot[I2(ji, jj + 1)] + rCdU_bot[p]) * zwy[p];
     }
   /* wind (:589-604) */
+  OMP_FOR
   for (int jj = 2; jj <= jpj - 1; ++jj)
     for (int ji = 2; ji <= jpi - 1; ++ji) {
       size_t p = I2(ji, jj);
@@ -1136,6 +1184,7 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
     }
   /* atmospheric pressure (:606-629) */
   if (nm->ln_apr_dyn)
+    OMP_FOR
     for (int jj = 2; jj <= jpj - 1; ++jj)
       for (int ji = 2; ji <= jpi - 1; ++ji) {
         size_t p = I2(ji, jj);
@@ -1179,25 +1228,30 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
     double za0, za1, za2, za3;
     if (jn < 3 && ll_init) { za1 = 1.0; za2 = 0.0; za3 = 0.0; }
     else { za1 = 1.781105; za2 = -1.06221; za3 = 0.281105; }
+    OMP_FOR
     for (size_t p = 0; p < n2; ++p) {
       c->ua_e[p] = za1 * c->un_e[p] + za2 * c->ub_e[p] + za3 * c->ubb_e[p];
       c->va_e[p] = za1 * c->vn_e[p] + za2 * c->vb_e[p] + za3 * c->vbb_e[p];
     }
     /* linssh: zhup2_e = hu_n, zhvp2_e = hv_n (:788-792) */
+    OMP_FOR
     for (size_t p = 0; p < n2; ++p) {
       zwx[p] = c->e2u[p] * c->ua_e[p] * hu_n[p];
       zwy[p] = c->e1v[p] * c->va_e[p] * hv_n[p];
     }
     za2 = c->wgtbtp2[jn - 1];
+    OMP_FOR
     for (size_t p = 0; p < n2; ++p) {
       un_adv[p] = un_adv[p] + za2 * zwx[p] * c->r1_e2u[p];
       vn_adv[p] = vn_adv[p] + za2 * zwy[p] * c->r1_e1v[p];
     }
+    OMP_FOR
     for (int jj = 2; jj <= jpj - 1; ++jj)
       for (int ji = 2; ji <= jpi - 1; ++ji) {
         size_t p = I2(ji, jj);
         zhdiv[p] = (zwx[p] - zwx[I2(ji - 1, jj)] + zwy[p] - zwy[I2(ji, jj - 1)]) * c->r1_e1e2t[p];
       }
+    OMP_FOR
     for (size_t p = 0; p < n2; ++p) c->ssha_e[p] = (c->sshn_e[p] - rdtbt * (zssh_frc[p] + zhdiv[p])) * ssmask[p];
     lbc_closed(jpi, jpj, c->ssha_e, 1, 'T', 0.0);
     if (jn == 1 && ll_init) { za0 = 1.0; za1 = 0.0; za2 = 0.0; za3 = 0.0; }
@@ -1211,9 +1265,11 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
       za2 = zgamma;
       za3 = zepsilon;
     }
+    OMP_FOR
     for (size_t p = 0; p < n2; ++p)
       zsshp2_e[p] = za0 * c->ssha_e[p] + za1 * c->sshn_e[p] + za2 * c->sshb_e[p] + za3 * c->sshbb_e[p];
     /* Coriolis (:1000-1056) with zhup2_e = hu_n (linssh) */
+    OMP_FOR
     for (int jj = 2; jj <= jpj - 1; ++jj)
       for (int ji = 2; ji <= jpi - 1; ++ji) {
         size_t p = I2(ji, jj);
@@ -1247,6 +1303,7 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
         }
       }
     /* bottom stress (:1072-1079) */
+    OMP_FOR
     for (int jj = 2; jj <= jpj - 1; ++jj)
       for (int ji = 2; ji <= jpi - 1; ++ji) {
         size_t p = I2(ji, jj);
@@ -1254,6 +1311,7 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
         zv_trd[p] = zv_trd[p] + zCdU_v[p] * c->vn_e[p] * c->hvr_e[p];
       }
     /* surface pressure gradient (:1093-1101) */
+    OMP_FOR
     for (int jj = 2; jj <= jpj - 1; ++jj)
       for (int ji = 2; ji <= jpi - 1; ++ji) {
         size_t p = I2(ji, jj);
@@ -1263,6 +1321,7 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
         zwy[p] = (1.0 - nm->rn_scal_load) * zv_spg;
       }
     /* next velocities, vector form (:1106-1122) */
+    OMP_FOR
     for (int jj = 2; jj <= jpj - 1; ++jj)
       for (int ji = 2; ji <= jpi - 1; ++ji) {
         size_t p = I2(ji, jj);
@@ -1272,6 +1331,7 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
     lbc_closed(jpi, jpj, c->ua_e, 1, 'U', 0.0);
     lbc_closed(jpi, jpj, c->va_e, 1, 'V', 0.0);
     /* swap (:1176-1186) */
+    OMP_FOR
     for (size_t p = 0; p < n2; ++p) {
       c->ubb_e[p] = c->ub_e[p]; c->ub_e[p] = c->un_e[p]; c->un_e[p] = c->ua_e[p];
       c->vbb_e[p] = c->vb_e[p]; c->vb_e[p] = c->vn_e[p]; c->vn_e[p] = c->va_e[p];
@@ -1279,6 +1339,7 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
     }
     /* sums (:1190-1204) */
     za1 = c->wgtbtp1[jn - 1];
+    OMP_FOR
     for (size_t p = 0; p < n2; ++p) {
       ua_b[p] = ua_b[p] + za1 * c->ua_e[p];
       va_b[p] = va_b[p] + za1 * c->va_e[p];
@@ -1288,6 +1349,7 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
   (void)ln_dynadv_vec;
   /* Phase 3 (:1214-1269) */
   if (ln_bt_fw) {
+    OMP_FOR
     for (size_t p = 0; p < n2; ++p) {
       zwx[p] = un_adv[p];
       zwy[p] = vn_adv[p];
@@ -1304,12 +1366,14 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
       vb2_b[p] = zwy[p];
     }
   }
+  OMP_FOR
   for (int jk = 1; jk <= jpk - 1; ++jk)
     for (size_t p = 0; p < n2; ++p) {
       size_t q = p + n2 * (jk - 1);
       ua[q] = ua[q] + (ua_b[p] - ub_b[p]) * r1_2dt_b;
       va[q] = va[q] + (va_b[p] - vb_b[p]) * r1_2dt_b;
     }
+  OMP_FOR
   for (int jk = 1; jk <= jpk - 1; ++jk)
     for (size_t p = 0; p < n2; ++p) {
       size_t q = p + n2 * (jk - 1);
