@@ -247,6 +247,25 @@ int nemo_gpu_lbc_lnk_multi(nemo_ctx *ctx, const char *cdname, int kfld, void *co
 int nemo_gpu_glob_sum(nemo_ctx *ctx, const char *cdname, const void *ptab, int nk,
                       int is_fp64, double *out);
 
+/* glob_sum without any device allocation, for callers that cannot allocate at
+ * the point of the call: code running inside an open CUDA stream capture, hosts
+ * whose device memory belongs to another runtime (OpenACC / CUDA Fortran data
+ * regions, a coupler's caching allocator), or set-ups that fix their device
+ * footprint at start-up. This entry point has no counterpart in the reference
+ * (whose glob_sum is lib_fortran_generic.h90:32-65); it computes the same masked
+ * double-double sum as nemo_gpu_glob_sum but needs no context: ptab holds nmembers
+ * consecutive (jpi,jpj,nk) fields (FP64 when is_fp64 != 0, else FP32), tmask_i is
+ * the (jpi,jpj) FP64 interior mask, and out receives nmembers sums -- all three are
+ * DEVICE pointers; stream is a cudaStream_t or NULL. The block partial sums live
+ * in a static device array of the library (about 1 MB, held by every GPU that
+ * loads it until the process exits), so at most 64 members per call; larger
+ * requests return NEMO_ERR_ARG. The first call on each device looks up that
+ * array's device address (cudaGetSymbolAddress); make it before any stream
+ * capture. Calls that overlap on the GPU (other streams, other host threads)
+ * share the array and race: serialise them. */
+int nemo_gpu_glob_sum_noalloc(const void *ptab, const double *tmask_i, int jpi, int jpj, int nk,
+                              int nmembers, int is_fp64, void *stream, double *out);
+
 /* The path of one timestep stp (step.F90:194-257) on the bound fields, in the
  * reference's order: dyn_spg_ts, tsa = 0 (:234), tra_adv (transports + FCT),
  * tra_ldf (lap or iso, per the namelist), tra_zdf (implicit + salinity clamp).

@@ -111,6 +111,7 @@ def load(path):
     _proto(lib, "nemo_gpu_lbc_lnk", i, [vp, cp, vp, i, i, cp, d, d, i])
     _proto(lib, "nemo_gpu_lbc_lnk_multi", i, [vp, cp, i, C.POINTER(vp), C.POINTER(i), cp, C.POINTER(d), d, i])
     _proto(lib, "nemo_gpu_glob_sum", i, [vp, cp, vp, i, i, C.POINTER(d)])
+    _proto(lib, "nemo_gpu_glob_sum_noalloc", i, [vp, vp, i, i, i, i, i, vp, vp])
     _proto(lib, "nemo_gpu_stp_hotpath", i, [vp, i])
     _proto(lib, "nemo_gpu_set_barrier_limit", i, [vp, C.c_longlong, i])
     _proto(lib, "nemo_gpu_set_timing", i, [vp, i])

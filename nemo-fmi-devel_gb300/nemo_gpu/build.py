@@ -6,7 +6,8 @@ Three translation units are compiled in parallel and linked into
 * ``inst_fp64.cu`` -- FP64 kernels, ``--fmad=false`` so that every double operation
   rounds exactly like the reference's FP64 CPU build (no fused multiply-add);
 * ``inst_fp32.cu`` -- FP32-bulk kernels of the mixed-precision mode;
-* ``capi.cu``      -- the C ABI (host code).
+* ``capi.cu``      -- the C ABI (host code);
+* ``noalloc.cu``   -- the allocation-free global sum (static device scratch).
 """
 import concurrent.futures as cf
 import os
@@ -24,6 +25,7 @@ UNITS = {
     "inst_fp64.cu": ["--fmad=false"],
     "inst_fp32.cu": [],
     "capi.cu": [],
+    "noalloc.cu": ["--fmad=false"],
 }
 
 
