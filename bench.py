@@ -42,7 +42,28 @@ ALG_BYTES = {
     "dyn_spg_ts_3d": (80, 40),
     "dyn_spg_ts_substep_2d": (200, 140),
 }
-KERNELS_PER_STEP = 10  # spg: 4, fct: 3, iso: 2, zdf: 1
+# algorithmic 3-D fields per cell of each kernel of the hot path (T and S, transports
+# computed on the fly, 1-D e3 profile, eddy diffusivity from the masks): every 3-D
+# array the kernel reads or writes, counted once; times the element size
+KERNEL_FIELDS = {
+    "fct_a": 17,     # read un vn wn, tb(2) tn(2); write ta(2) zwi(2) ax(2) ay(2) az(2)
+    "fct_b": 14,     # read tb(2) zwi(2) ax(2) ay(2) az(2); write betup(2) betdo(2)
+    "fct_c": 20,     # read ax ay az betup betdo (x2), zftu zftv ztfw (x2); ta(2) read+write
+    "iso_flux": 14,  # read tb(2) uslp vslp wslpi wslpj; write ah_wslp2 akz, zftu zftv ztfw (x2)
+    "zdf_imp": 8,    # read avt ah_wslp2 tb(2); ta(2) read+write
+    "spg_p1a": 2,    # read ua va (column sums)
+    "spg_p3": 8,     # ua va un vn read+write
+}
+# per 2-D cell, bytes (FP64, FP32-bulk) of the 2-D kernels
+KERNEL_BYTES_2D = {
+    "spg_p1b": (232, 152),  # ~20 bulk 2-D values + 5 FP64 sums zeroed + 3 ring levels written
+}
+
+
+# DRAM bytes (read + write) per launch from one ncu capture of the kernel on this
+# workload: (kernel, precision, nn_GYRE) -> bytes; filled in from the committed
+# ncu summaries
+TRAFFIC = {}
 
 
 def peaks():
@@ -189,14 +210,17 @@ def run_gpu(args):
     ms_max = dist.max_over_ranks(ms, device=f"cuda:{local}")
     ms_step = ms_max / args.steps
     value = cells * world * args.steps / (ms_max / 1e3)
-    # per-routine timing (the library's ln_timing) for the roofline
+    # per-routine and per-kernel timing (CUDA events on the context's stream)
     ctx.set_timing(True)
-    for s in range(max(3, min(args.steps, 10))):
+    ntime = max(3, min(args.steps, 10))
+    for s in range(ntime):
         ctx.stp_hotpath(kt0 + 1000 + s)
     ctx.synchronize()
     rt, ncalls = ctx.get_timing()
+    kt_ = ctx.get_kernel_timing()
     ctx.set_timing(False)
     rt = {k: v / max(ncalls, 1) for k, v in rt.items()}
+    launches_per_step = sum(n for _, n in kt_.values()) / ntime
     sst_mixed = ctx.to_host(dev["TSA"], (jpi, jpj, jpk, 2))
     # ---------------------------------------------------------------- FP64 arm
     fp64 = None
@@ -270,11 +294,30 @@ def run_gpu(args):
                 "tra_zdf": ALG_BYTES["tra_zdf"][b],
                 "dyn_spg_ts": ALG_BYTES["dyn_spg_ts_3d"][b]
                 + ALG_BYTES["dyn_spg_ts_substep_2d"][b] * icycle / jpk}
-    routine = max(rt, key=rt.get)
-    alg_bytes = per_cell[routine] * cells
-    achieved = alg_bytes / (rt[routine] / 1e3) / 1e9
+    es = 4 if args.prec == "mixed" else 8
+    n2 = jpi * jpj * args.members
+
+    def kernel_bytes(name):
+        if name == "spg_p2":  # every 2-D value of every sub-step (L2-resident working set)
+            return ALG_BYTES["dyn_spg_ts_substep_2d"][b] * icycle * n2
+        if name in KERNEL_BYTES_2D:
+            return KERNEL_BYTES_2D[name][b] * n2
+        if name in ("iso_akz_edges", "iso_msc_edges"):  # edge columns only: ah_wslp2, akz
+            return 2 * es * (2 * jpi + 2 * jpj) * jpk * args.members
+        return KERNEL_FIELDS.get(name, 0) * es * cells
+
+    kernels = {}
+    for name, (kms, nl) in kt_.items():
+        us = 1e3 * kms / max(nl, 1)
+        kb = kernel_bytes(name)
+        kernels[name] = {"us": us, "launches_per_step": nl / ntime, "alg_bytes": kb,
+                         "alg_GBps": kb / (us / 1e6) / 1e9 if kb and us > 0 else None,
+                         "frac": kb / (us / 1e6) / 1e9 / hbm if kb and us > 0 else None}
+    top = max(kernels, key=lambda k: kernels[k]["us"])
+    achieved = kernels[top]["alg_GBps"]
+    alg_bytes = kernels[top]["alg_bytes"]
     routines = {k: {"ms": rt[k], "alg_GBps": per_cell[k] * cells / (rt[k] / 1e3) / 1e9,
-                    "frac": per_cell[k] * cells / (rt[k] / 1e3) / 1e9 / hbm} for k in rt}
+                    "frac": per_cell[k] * cells / (rt[k] / 1e3) / 1e9 / hbm} for k in rt if rt[k] > 0.01}
     step_bytes = sum(per_cell[k] for k in per_cell) * cells
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -287,10 +330,12 @@ def run_gpu(args):
                    "l2": "inputs larger than L2 (%.2f GB resident), no flush" % (
                        sum(t.numel() * t.element_size() for t in dev.values()) / 1e9),
                    "parallelism": f"replicas x{world}"},
-        "clocks": ck, "gpu_launches": KERNELS_PER_STEP * args.steps,
-        "roofline": {"bound": "hbm", "kernel": routine, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None, "peak_source": src,
-                     "alg_bytes_per_launch": alg_bytes},
+        "clocks": ck, "gpu_launches": int(round(launches_per_step * args.steps)),
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm if achieved else None, "traffic": TRAFFIC.get((top, args.prec, args.nn)),
+                     "peak_source": src, "alg_bytes_per_launch": alg_bytes,
+                     "duration_us": kernels[top]["us"]},
+        "kernels": kernels,
         "routines": routines,
         "step_alg_GBps": step_bytes / (ms_step / 1e3) / 1e9,
         "e2e": e2e, "fp64": fp64,

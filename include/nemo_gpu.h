@@ -283,6 +283,22 @@ int nemo_gpu_stp_hotpath(nemo_ctx *ctx, int kt);
 int nemo_gpu_set_timing(nemo_ctx *ctx, int on);
 int nemo_gpu_get_timing(nemo_ctx *ctx, double *ms, int *ncalls);
 
+/* The kernels of the library, for per-kernel timing. */
+enum nemo_kernel_id {
+  NEMO_K_ADV_TRP, NEMO_K_INTERP4, NEMO_K_FCT_A, NEMO_K_FCT_B, NEMO_K_FCT_C, NEMO_K_LDF_LAP,
+  NEMO_K_ISO_FLUX, NEMO_K_ISO_DIV, NEMO_K_ISO_AKZ_EDGES, NEMO_K_ISO_MSC_EDGES, NEMO_K_ZDF_IMP,
+  NEMO_K_CLAMP, NEMO_K_SPG_P1A, NEMO_K_SPG_P1B, NEMO_K_SPG_P2, NEMO_K_SPG_P3,
+  NEMO_K_COUNT
+};
+
+/* Per-kernel device timing of nemo_gpu_stp_hotpath while timing is on (no
+ * counterpart in the reference, whose timing stops at routines): a CUDA event is
+ * recorded on the context's stream after every kernel launch, so
+ * ms[id] = cumulative milliseconds between the end of the previous kernel and the
+ * end of kernel id, launches[id] = how many launches of it were timed. Both arrays
+ * hold NEMO_K_COUNT entries; n is their length (entries past NEMO_K_COUNT are 0). */
+int nemo_gpu_get_kernel_timing(nemo_ctx *ctx, double *ms, int *launches, int n);
+
 /* ------------------------------------------------------------ kernel choice */
 
 /* on = 1 (default): in a mixed-precision context whose configuration allows it

@@ -68,9 +68,12 @@ struct nemo_ctx {
   // work arrays
   void* fct_w[6] = {};
   void* fct_ztw = nullptr;
+  void* iso_w[3] = {};         // iso-neutral fluxes zftu, zftv, ztfw
+  int iso_kjpt = 0;
   int fct_kjpt = 0;
   void* spg_w[5] = {};
   void* ring[3] = {};
+  void* spg_x[7] = {};  // fx (2 slots), fy (2 slots), zs, du|dv|cu|cv
   unsigned int* bar_mem = nullptr;  // count, gen
   int* err_flag = nullptr;
   long long bar_spins = 4000000;
@@ -88,7 +91,15 @@ struct nemo_ctx {
   cudaEvent_t tev[5] = {};
   double tms[4] = {0, 0, 0, 0};
   int tcalls = 0;
+  // per-kernel timing (events after every launch while timing is on)
+  KernelClock kc;
+  double kms[NEMO_K_COUNT] = {};
+  int kcnt[NEMO_K_COUNT] = {};
 };
+
+namespace nemo {
+thread_local KernelClock* t_kclock = nullptr;
+}
 
 namespace {
 
@@ -479,6 +490,19 @@ int ensure_fct_work(nemo_ctx* c, int kjpt, int need_ztw) {
   return NEMO_OK;
 }
 
+int ensure_iso_work(nemo_ctx* c, int kjpt) {
+  if (kjpt <= c->iso_kjpt) return NEMO_OK;
+  const size_t bytes = (size_t)kjpt * c->n3 * c->nmem * (c->prec == NEMO_PREC_FP64 ? 8 : 4);
+  for (auto& p : c->iso_w) {
+    cudaFree(p);
+    p = nullptr;
+  }
+  for (auto& p : c->iso_w)
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return fail(c, NEMO_ERR_NOMEM, "iso-neutral flux arrays (%zu bytes)", bytes);
+  c->iso_kjpt = kjpt;
+  return NEMO_OK;
+}
+
 int check_cdtype(nemo_ctx* c, const char* cdtype, int* is_trc) {
   if (!cdtype) return fail(c, NEMO_ERR_ARG, "cdtype is NULL");
   if (!strncmp(cdtype, "TRA", 3)) *is_trc = 0;
@@ -489,7 +513,8 @@ int check_cdtype(nemo_ctx* c, const char* cdtype, int* is_trc) {
 
 template <class T>
 int run_fct(nemo_ctx* c, double p2dt, const void* pun, const void* pvn, const void* pwn, int trp, const void* ptb,
-            const void* ptn, const void* pta_in, void* pta, int kjpt, int kh, int kv) {
+            const void* ptn, const void* pta_in, void* pta, int kjpt, int kh, int kv,
+            const LdfArgs<T>* iso = nullptr) {
   int s = ensure_fct_work(c, kjpt, kv == 4);
   if (s) return s;
   FctArgs<T> a{};
@@ -500,6 +525,10 @@ int run_fct(nemo_ctx* c, double p2dt, const void* pun, const void* pvn, const vo
   a.betup = (T*)c->fct_w[4]; a.betdo = (T*)c->fct_w[5];
   a.ztw = (const T*)c->fct_ztw;
   a.kjpt = kjpt; a.kn_fct_h = kh; a.kn_fct_v = kv; a.linssh = c->nam.ln_linssh;
+  if (iso) {
+    a.with_iso = 1;
+    a.iso = *iso;
+  }
   cudaError_t e = launch_fct<T>(dom_now<T>(c), a, c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "tra_adv_fct launch");
   return NEMO_OK;
@@ -526,18 +555,24 @@ int run_ldf_lap(nemo_ctx* c, const void* pahu, const void* pahv, const void* pgu
   return NEMO_OK;
 }
 
+// Iso-neutral arguments for one call (traldf_iso.F90:130-203): bound slopes and
+// coefficient arrays, time step, and on the first pass of kit000 the zeroing of
+// ah_wslp2 / akz.
 template <class T>
-int run_ldf_iso(nemo_ctx* c, int kt, int kit000, const void* pahu, const void* pahv, const void* pgu, const void* pgv,
-                const void* ptb, const void* ptbb, void* pta, int kjpt, int kpass) {
+int iso_args(nemo_ctx* c, int kt, int kit000, const void* pahu, const void* pahv, const void* pgu, const void* pgv,
+             const void* ptb, const void* ptbb, void* pta, int kjpt, int kpass, LdfArgs<T>* out) {
   const nemo_namelist& nm = c->nam;
   if (!c->f[NEMO_F_USLP] || !c->f[NEMO_F_VSLP] || !c->f[NEMO_F_WSLPI] || !c->f[NEMO_F_WSLPJ] ||
       !c->f[NEMO_F_AH_WSLP2] || !c->f[NEMO_F_AKZ])
     return fail(c, NEMO_ERR_UNBOUND, "tra_ldf_iso: slopes, ah_wslp2 and akz must be bound");
+  int s = ensure_iso_work(c, kjpt);
+  if (s) return s;
   LdfArgs<T> a = ldf_args<T>(c, pahu, pahv, pgu, pgv, ptb, ptbb, pta, kjpt, kpass);
   a.uslp = (const T*)c->f[NEMO_F_USLP]; a.vslp = (const T*)c->f[NEMO_F_VSLP];
   a.wslpi = (const T*)c->f[NEMO_F_WSLPI]; a.wslpj = (const T*)c->f[NEMO_F_WSLPJ];
   a.ah_wslp2 = (T*)c->f[NEMO_F_AH_WSLP2]; a.akz = (T*)c->f[NEMO_F_AKZ];
   a.lap = nm.ln_traldf_lap; a.blp = nm.ln_traldf_blp; a.msc = nm.ln_traldf_msc;
+  a.zftu = (T*)c->iso_w[0]; a.zftv = (T*)c->iso_w[1]; a.ztfw = (T*)c->iso_w[2];
   const double z2dt = (nm.neuler == 0 && kt == nm.nit000) ? nm.rn_rdt : 2.0 * nm.rn_rdt;
   a.z2dt = (T)z2dt; a.z1_2dt = (T)(1.0 / z2dt);
   if (kpass == 1 && kt == kit000) {
@@ -545,6 +580,17 @@ int run_ldf_iso(nemo_ctx* c, int kt, int kit000, const void* pahu, const void* p
     CK(cudaMemsetAsync(a.akz, 0, bytes, c->stream), "akz = 0");
     CK(cudaMemsetAsync(a.ah_wslp2, 0, bytes, c->stream), "ah_wslp2 = 0");
   }
+  *out = a;
+  return NEMO_OK;
+}
+
+template <class T>
+int run_ldf_iso(nemo_ctx* c, int kt, int kit000, const void* pahu, const void* pahv, const void* pgu, const void* pgv,
+                const void* ptb, const void* ptbb, void* pta, int kjpt, int kpass) {
+  LdfArgs<T> a{};
+  int s = iso_args<T>(c, kt, kit000, pahu, pahv, pgu, pgv, ptb, ptbb, pta, kjpt, kpass, &a);
+  if (s) return s;
+  const nemo_namelist& nm = c->nam;
   cudaError_t e = launch_ldf_iso<T>(dom_now<T>(c), a, kpass == 1 && !nm.ln_traldf_msc,
                                     kpass == 1 && nm.ln_traldf_msc, c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "tra_ldf_iso launch");
@@ -621,6 +667,8 @@ int run_spg(nemo_ctx* c, int kt) {
   a.zu_frc = (T*)c->spg_w[0]; a.zv_frc = (T*)c->spg_w[1]; a.zssh_frc = (T*)c->spg_w[2];
   a.zCdU_u = (T*)c->spg_w[3]; a.zCdU_v = (T*)c->spg_w[4];
   a.ring_ssh = (T*)c->ring[0]; a.ring_u = (T*)c->ring[1]; a.ring_v = (T*)c->ring[2];
+  a.fx = (T*)c->spg_x[0]; a.fy = (T*)c->spg_x[1]; a.zs = (T*)c->spg_x[2];
+  a.du = (T*)c->spg_x[3]; a.dv = (T*)c->spg_x[4]; a.cu = (T*)c->spg_x[5]; a.cv = (T*)c->spg_x[6];
   a.wgt1 = c->d_wgt1; a.wgt2 = c->d_wgt2;
   a.ln_bt_fw = nm.ln_bt_fw; a.ln_apr_dyn = nm.ln_apr_dyn; a.nvor = nm.nvor_scheme; a.ll_init = ll_init;
   a.icycle = c->icycle;
@@ -639,57 +687,6 @@ int run_spg(nemo_ctx* c, int kt) {
   return NEMO_OK;
 }
 
-// The fused FCT + iso-neutral kernel covers the GYRE configuration of the mixed
-// form; anything else runs the per-routine kernels.
-bool fused_ok(nemo_ctx* c) {
-  const nemo_namelist& nm = c->nam;
-  if (c->prec != NEMO_PREC_MIXED || c->no_fusion) return false;
-  if (!nm.ln_linssh || nm.ln_zps || !nm.ln_traldf_iso || nm.ln_traldf_blp) return false;
-  if (c->f[NEMO_F_AHTU] || c->f[NEMO_F_AHTV]) return false;
-  for (int id : {NEMO_F_E3T_B, NEMO_F_E3T_N, NEMO_F_E3T_A, NEMO_F_E3U_N, NEMO_F_E3V_N, NEMO_F_E3W_N})
-    if (c->f[id]) return false;
-  for (int w = 0; w < 4; ++w)
-    if (!c->e3_uniform[w]) return false;
-  return true;
-}
-
-int run_tra_fused(nemo_ctx* c, int kt, double r2dt) {
-  const nemo_namelist& nm = c->nam;
-  void* const* F = c->f;
-  if (!F[NEMO_F_USLP] || !F[NEMO_F_VSLP] || !F[NEMO_F_WSLPI] || !F[NEMO_F_WSLPJ] || !F[NEMO_F_AH_WSLP2] ||
-      !F[NEMO_F_AKZ])
-    return fail(c, NEMO_ERR_UNBOUND, "tra_ldf_iso: slopes, ah_wslp2 and akz must be bound");
-  FusedArgs<float> a{};
-  a.p2dt = (float)r2dt;
-  a.un = (const float*)F[NEMO_F_UN]; a.vn = (const float*)F[NEMO_F_VN]; a.wn = (const float*)F[NEMO_F_WN];
-  a.tb = (const float*)F[NEMO_F_TSB]; a.tn = (const float*)F[NEMO_F_TSN]; a.ta = (float*)F[NEMO_F_TSA];
-  a.uslp = (const float*)F[NEMO_F_USLP]; a.vslp = (const float*)F[NEMO_F_VSLP];
-  a.wslpi = (const float*)F[NEMO_F_WSLPI]; a.wslpj = (const float*)F[NEMO_F_WSLPJ];
-  a.ah_wslp2 = (float*)F[NEMO_F_AH_WSLP2]; a.akz = (float*)F[NEMO_F_AKZ];
-  a.aht_c = (float)nm.rn_aht_0;
-  a.lap = nm.ln_traldf_lap; a.msc = nm.ln_traldf_msc; a.linssh = nm.ln_linssh;
-  const double z2dt = (nm.neuler == 0 && kt == nm.nit000) ? nm.rn_rdt : 2.0 * nm.rn_rdt;
-  a.z2dt = (float)z2dt; a.z1_2dt = (float)(1.0 / z2dt);
-  const Dom<float> d = dom_now<float>(c);
-  if (kt == nm.nit000) {
-    const size_t bytes = c->n3 * c->nmem * sizeof(float);
-    CK(cudaMemsetAsync(a.akz, 0, bytes, c->stream), "akz = 0");
-    CK(cudaMemsetAsync(a.ah_wslp2, 0, bytes, c->stream), "ah_wslp2 = 0");
-  }
-  cudaError_t e = launch_tra_fused(d, a, c->stream);
-  if (e != cudaSuccess) return cuda_fail(c, e, "fused tracer kernel launch");
-  // tsa = 0 on the edge columns (the fused kernel writes the interior columns)
-  e = launch_lbc<float>((float*)F[NEMO_F_TSA], c->jpi, c->jpj, 2L * c->jpk * c->nmem, 0, 0.0f, c->stream);
-  if (e != cudaSuccess) return cuda_fail(c, e, "tsa edges");
-  if (!nm.ln_traldf_msc) {
-    LdfArgs<float> la{};
-    la.ah_wslp2 = a.ah_wslp2; la.akz = a.akz;
-    e = launch_iso_akz_edges<float>(d, la, c->stream);
-    if (e != cudaSuccess) return cuda_fail(c, e, "akz edges");
-  }
-  return NEMO_OK;
-}
-
 template <class T>
 int run_hotpath(nemo_ctx* c, int kt) {
   const nemo_namelist& nm = c->nam;
@@ -697,30 +694,37 @@ int run_hotpath(nemo_ctx* c, int kt) {
   if (!F[NEMO_F_TSB] || !F[NEMO_F_TSN] || !F[NEMO_F_TSA] || !F[NEMO_F_WN])
     return fail(c, NEMO_ERR_UNBOUND, "stp_hotpath: tsb, tsn, tsa, un, vn, wn must be bound");
   auto mark = [&](int i) { if (c->timing) cudaEventRecord(c->tev[i], c->stream); };
+  // the kernel clock is installed for this thread until the function returns
+  struct ClockGuard {
+    explicit ClockGuard(KernelClock* k) { t_kclock = k; }
+    ~ClockGuard() { t_kclock = nullptr; }
+  } guard(c->timing ? &c->kc : nullptr);
+  if (c->timing) {
+    c->kc.n = 0;
+    cudaEventRecord(c->kc.ev[0], c->stream);
+  }
   mark(0);
   int s = run_spg<T>(c, kt);
   if (s) return s;
   mark(1);
   const double r2dt = (nm.neuler == 0 && kt == nm.nit000) ? nm.rn_rdt : 2.0 * nm.rn_rdt;
-  if (fused_ok(c)) {
-    s = run_tra_fused(c, kt, r2dt);
+  if (nm.ln_traldf_iso && !c->no_fusion) {
+    // tsa = 0, tra_adv and tra_ldf (iso-neutral, first pass): the iso-neutral
+    // fluxes first, then the three FCT stages; the last adds both the corrected
+    // advective trend and the iso-neutral divergence of each point, in the
+    // reference's order
+    LdfArgs<T> la{};
+    s = iso_args<T>(c, kt, nm.nit000, F[NEMO_F_AHTU], F[NEMO_F_AHTV], F[NEMO_F_GTSU], F[NEMO_F_GTSV],
+                    F[NEMO_F_TSB], F[NEMO_F_TSB], F[NEMO_F_TSA], 2, 1, &la);
     if (s) return s;
+    CK(launch_iso_flux<T>(dom_now<T>(c), la, c->stream), "iso fluxes");
+    s = run_fct<T>(c, r2dt, F[NEMO_F_UN], F[NEMO_F_VN], F[NEMO_F_WN], 1, F[NEMO_F_TSB], F[NEMO_F_TSN], nullptr,
+                   F[NEMO_F_TSA], 2, 2, 2, &la);
+    if (s) return s;
+    cudaError_t e = launch_iso_edges<T>(dom_now<T>(c), la, !nm.ln_traldf_msc, nm.ln_traldf_msc, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "iso edges");
     mark(2);
-    mark(3);
-    s = run_zdf<T>(c, r2dt, F[NEMO_F_TSB], F[NEMO_F_TSA], 2, 0, 1);
-    if (s) return s;
-    if (c->timing) {
-      mark(4);
-      CK(cudaEventSynchronize(c->tev[4]), "timing");
-      for (int i = 0; i < 4; ++i) {
-        float ms = 0;
-        cudaEventElapsedTime(&ms, c->tev[i], c->tev[i + 1]);
-        c->tms[i] += ms;
-      }
-      c->tcalls += 1;
-    }
-    return NEMO_OK;
-  }
+  } else {
   // tsa = 0 (step.F90:234) folded into the first trend (pta_in = NULL)
   s = run_fct<T>(c, r2dt, F[NEMO_F_UN], F[NEMO_F_VN], F[NEMO_F_WN], 1, F[NEMO_F_TSB], F[NEMO_F_TSN], nullptr,
                  F[NEMO_F_TSA], 2, 2, 2);
@@ -732,6 +736,7 @@ int run_hotpath(nemo_ctx* c, int kt) {
   else
     s = run_ldf_lap<T>(c, F[NEMO_F_AHTU], F[NEMO_F_AHTV], F[NEMO_F_GTSU], F[NEMO_F_GTSV], F[NEMO_F_TSB], F[NEMO_F_TSA], 2, 1);
   if (s) return s;
+  }
   mark(3);
   s = run_zdf<T>(c, r2dt, F[NEMO_F_TSB], F[NEMO_F_TSA], 2, 0, 1);
   if (s) return s;
@@ -744,6 +749,12 @@ int run_hotpath(nemo_ctx* c, int kt) {
       c->tms[i] += ms;
     }
     c->tcalls += 1;
+    for (int i = 0; i < c->kc.n; ++i) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, c->kc.ev[i], c->kc.ev[i + 1]);
+      c->kms[c->kc.id[i]] += ms;
+      c->kcnt[c->kc.id[i]] += 1;
+    }
   }
   return NEMO_OK;
 }
@@ -793,6 +804,11 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
     if (cudaMalloc(&p, 4 * b2) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
     cudaMemset(p, 0, 4 * b2);
   }
+  for (int w = 0; w < 7; ++w) {
+    const size_t bytes = w < 2 ? 2 * b2 : b2;
+    if (cudaMalloc(&c->spg_x[w], bytes) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
+    cudaMemset(c->spg_x[w], 0, bytes);
+  }
   if (cudaMalloc(&c->d_wgt1, 3 * (size_t)c->nn_baro * 8) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
   if (cudaMalloc(&c->d_wgt2, 3 * (size_t)c->nn_baro * 8) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
   cudaMemcpy(c->d_wgt1, c->wgt1.data(), c->wgt1.size() * 8, cudaMemcpyHostToDevice);
@@ -810,6 +826,7 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
   if (cudaMalloc(&c->gs_part, 2 * (size_t)c->gs_nblk * c->nmem * 8) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
   if (cudaMalloc(&c->gs_out, (size_t)c->nmem * 8) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
   if (ensure_fct_work(c, 2, 0)) return bad(NEMO_ERR_NOMEM);
+  if (c->nam.ln_traldf_iso && ensure_iso_work(c, 2)) return bad(NEMO_ERR_NOMEM);
   if (cudaDeviceSynchronize() != cudaSuccess) return bad(NEMO_ERR_CUDA);
   *out = c;
   return NEMO_OK;
@@ -823,12 +840,16 @@ int nemo_gpu_destroy(nemo_ctx* c) {
   free_dom(c->df);
   for (auto p : c->fct_w) cudaFree(p);
   cudaFree(c->fct_ztw);
+  for (auto p : c->iso_w) cudaFree(p);
   for (auto p : c->spg_w) cudaFree(p);
   for (auto p : c->ring) cudaFree(p);
+  for (auto p : c->spg_x) cudaFree(p);
   cudaFree(c->d_wgt1); cudaFree(c->d_wgt2);
   cudaFree(c->bar_mem); cudaFree(c->err_flag);
   cudaFree(c->gs_part); cudaFree(c->gs_out);
   for (auto e : c->tev)
+    if (e) cudaEventDestroy(e);
+  for (auto e : c->kc.ev)
     if (e) cudaEventDestroy(e);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -1054,11 +1075,24 @@ int nemo_gpu_stp_hotpath(nemo_ctx* c, int kt) {
 
 int nemo_gpu_set_timing(nemo_ctx* c, int on) {
   if (!c) return NEMO_ERR_ARG;
-  if (on && !c->tev[0])
+  if (on && !c->tev[0]) {
     for (auto& e : c->tev) CK(cudaEventCreate(&e), "timing events");
+    for (auto& e : c->kc.ev) CK(cudaEventCreate(&e), "timing events");
+  }
   c->timing = on != 0;
   for (double& t : c->tms) t = 0.0;
   c->tcalls = 0;
+  for (double& t : c->kms) t = 0.0;
+  for (int& n : c->kcnt) n = 0;
+  return NEMO_OK;
+}
+
+int nemo_gpu_get_kernel_timing(nemo_ctx* c, double* ms, int* launches, int n) {
+  if (!c || n < 0 || (n > 0 && (!ms || !launches))) return NEMO_ERR_ARG;
+  for (int i = 0; i < n; ++i) {
+    ms[i] = i < NEMO_K_COUNT ? c->kms[i] : 0.0;
+    launches[i] = i < NEMO_K_COUNT ? c->kcnt[i] : 0;
+  }
   return NEMO_OK;
 }
 

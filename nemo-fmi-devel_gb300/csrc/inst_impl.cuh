@@ -7,15 +7,23 @@ namespace nemo {
 
 constexpr int BX = 32, BY = 4;
 
+// one thread per water column (recurrences along k)
 template <class T>
 static dim3 col_grid(const Dom<T>& d) {
   return dim3((d.jpi + BX - 1) / BX, (d.jpj + BY - 1) / BY, d.nmem);
 }
 
+// one thread per (i,j,k) point: z = member * jpk + (k - 1)
+template <class T>
+static dim3 pt_grid(const Dom<T>& d) {
+  return dim3((d.jpi + BX - 1) / BX, (d.jpj + BY - 1) / BY, d.nmem * d.jpk);
+}
+
 template <class T>
 cudaError_t launch_adv_trp(const Dom<T>& d, const T* un, const T* vn, const T* wn, T* zun, T* zvn, T* zwn,
                            cudaStream_t s) {
-  k_adv_trp<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, un, vn, wn, zun, zvn, zwn);
+  k_adv_trp<T><<<pt_grid(d), dim3(BX, BY), 0, s>>>(d, un, vn, wn, zun, zvn, zwn);
+  ktick(NEMO_K_ADV_TRP, s);
   return cudaGetLastError();
 }
 
@@ -23,36 +31,66 @@ template <class T>
 cudaError_t launch_fct(const Dom<T>& d, const FctArgs<T>& a, cudaStream_t s) {
   if (a.kn_fct_v == 4) {
     k_interp4<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a.ptn, const_cast<T*>(a.ztw), a.kjpt);
+    ktick(NEMO_K_INTERP4, s);
   }
-  k_fct_a<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
-  k_fct_b<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
-  k_fct_c<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  k_fct_a<T><<<pt_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  ktick(NEMO_K_FCT_A, s);
+  k_fct_b<T><<<pt_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  ktick(NEMO_K_FCT_B, s);
+  k_fct_c<T><<<pt_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  ktick(NEMO_K_FCT_C, s);
   return cudaGetLastError();
 }
 
 template <class T>
 cudaError_t launch_ldf_lap(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s) {
-  k_ldf_lap<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  k_ldf_lap<T><<<pt_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  ktick(NEMO_K_LDF_LAP, s);
   return cudaGetLastError();
 }
 
 template <class T>
 cudaError_t launch_ldf_iso(const Dom<T>& d, const LdfArgs<T>& a, int copy_akz_edges, int msc_edges, cudaStream_t s) {
-  k_ldf_iso<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
-  if (copy_akz_edges) k_iso_akz_copy_edges<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
-  if (msc_edges) k_iso_msc_edges<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
-  return cudaGetLastError();
+  k_iso_flux<T><<<pt_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  ktick(NEMO_K_ISO_FLUX, s);
+  k_iso_div<T><<<pt_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  ktick(NEMO_K_ISO_DIV, s);
+  return launch_iso_edges<T>(d, a, copy_akz_edges, msc_edges, s);
 }
 
 template <class T>
-cudaError_t launch_iso_akz_edges(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s) {
-  k_iso_akz_copy_edges<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+cudaError_t launch_iso_flux(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s) {
+  k_iso_flux<T><<<pt_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  ktick(NEMO_K_ISO_FLUX, s);
+  return cudaGetLastError();
+}
+
+// the points of ah_wslp2 / akz the interior sweep does not write (edge columns,
+// levels 1 and jpk; row and column 1 of the MSC correction)
+template <class T>
+cudaError_t launch_iso_edges(const Dom<T>& d, const LdfArgs<T>& a, int copy_akz_edges, int msc_edges, cudaStream_t s) {
+  if (copy_akz_edges) {
+    k_iso_akz_copy_edges<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+    ktick(NEMO_K_ISO_AKZ_EDGES, s);
+  }
+  if (msc_edges) {
+    k_iso_msc_edges<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+    ktick(NEMO_K_ISO_MSC_EDGES, s);
+  }
   return cudaGetLastError();
 }
 
 template <class T>
 cudaError_t launch_zdf(const Dom<T>& d, const ZdfArgs<T>& a, cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    if (d.jpk == 31) {  // the GYRE levels: columns in registers
+      k_zdf_imp_reg<31><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+      ktick(NEMO_K_ZDF_IMP, s);
+      return cudaGetLastError();
+    }
+  }
   k_zdf_imp<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  ktick(NEMO_K_ZDF_IMP, s);
   return cudaGetLastError();
 }
 
@@ -62,6 +100,7 @@ cudaError_t launch_clamp(T* x, long n, cudaStream_t s) {
   if (nb > 152L * 16) nb = 152L * 16;
   if (nb < 1) nb = 1;
   k_clamp_neg<T><<<(unsigned)nb, 256, 0, s>>>(x, n);
+  ktick(NEMO_K_CLAMP, s);
   return cudaGetLastError();
 }
 
@@ -75,7 +114,9 @@ int spg_p2_blocks_per_sm() {
 template <class T>
 cudaError_t launch_spg(const Dom<T>& d, const SpgArgs<T>& a, const GridBar& bar, int p2_blocks, cudaStream_t s) {
   k_spg_p1a<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  ktick(NEMO_K_SPG_P1A, s);
   k_spg_p1b<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  ktick(NEMO_K_SPG_P1B, s);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(p2_blocks);
   cfg.blockDim = dim3(256);
@@ -88,7 +129,9 @@ cudaError_t launch_spg(const Dom<T>& d, const SpgArgs<T>& a, const GridBar& bar,
   cfg.numAttrs = 1;
   cudaError_t e = cudaLaunchKernelEx(&cfg, k_spg_p2<T>, d, a, bar);
   if (e != cudaSuccess) return e;
-  k_spg_p3<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  ktick(NEMO_K_SPG_P2, s);
+  k_spg_p3<T><<<pt_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  ktick(NEMO_K_SPG_P3, s);
   return cudaGetLastError();
 }
 
@@ -115,7 +158,8 @@ cudaError_t launch_globsum(const T* x, const double* tmask_i, long n2, int nk, i
   template cudaError_t launch_ldf_lap<T>(const Dom<T>&, const LdfArgs<T>&, cudaStream_t);                    \
   template cudaError_t launch_ldf_iso<T>(const Dom<T>&, const LdfArgs<T>&, int, int, cudaStream_t);          \
   template cudaError_t launch_zdf<T>(const Dom<T>&, const ZdfArgs<T>&, cudaStream_t);                        \
-  template cudaError_t launch_iso_akz_edges<T>(const Dom<T>&, const LdfArgs<T>&, cudaStream_t);              \
+  template cudaError_t launch_iso_edges<T>(const Dom<T>&, const LdfArgs<T>&, int, int, cudaStream_t);        \
+  template cudaError_t launch_iso_flux<T>(const Dom<T>&, const LdfArgs<T>&, cudaStream_t);                   \
   template cudaError_t launch_clamp<T>(T*, long, cudaStream_t);                                              \
   template cudaError_t launch_spg<T>(const Dom<T>&, const SpgArgs<T>&, const GridBar&, int, cudaStream_t);   \
   template int spg_p2_blocks_per_sm<T>();                                                                    \

@@ -29,6 +29,9 @@ struct SpgArgs {
   // library work arrays (2-D, per member)
   T *zu_frc, *zv_frc, *zssh_frc, *zCdU_u, *zCdU_v;
   T *ring_ssh, *ring_u, *ring_v;  // 4 slots each
+  T *fx, *fy;                     // 2 slots each: predictor fluxes zwx, zwy of a sub-step
+  T* zs;                          // zsshp2_e of the current sub-step
+  T *du, *dv, *cu, *cv;           // phase-3 column terms, computed at the end of phase 2
   const double *wgt1, *wgt2;
   int ln_bt_fw, ln_apr_dyn, nvor, ll_init, icycle, ring0, phase3_filter;
   T rdtbt, grav, r1_rau0, scal_load, rn_bt_alpha;
@@ -216,130 +219,159 @@ __device__ __forceinline__ void am4(int jn, int ll_init, T alpha, T& za0, T& za1
   }
 }
 
-// Phase 2: the icycle sub-steps (:712-1207) in one persistent kernel.
+// Phase 2: the icycle sub-steps (:712-1207) in one persistent kernel, followed by
+// the per-column part of phase 3.
+//
+// Every 2-D point is owned by one thread for the whole kernel. A sub-step is two
+// stages separated by grid barriers:
+//  A: ssha_e from the divergence of the published predictor fluxes, its sum into
+//     ssha, and the AM4 surface height zsshp2_e, published in zs;
+//  B: Coriolis from the neighbours' published fluxes, bottom drag, pressure
+//     gradient from zs, the new ua_e/va_e and their sums -- then, from the owner's
+//     own levels only, the predictor fluxes of the next sub-step (published in the
+//     other fx/fy slot) and their un_adv/vn_adv sums.
+// Each published value is computed once, by its owner, with the reference's
+// expression, so neighbours read exactly the value they would have recomputed.
 template <class T>
 __global__ void __launch_bounds__(256) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar bar) {
-  const long n2 = d.n2, nmem2 = (long)d.nmem * n2;
+  const int n2 = (int)d.n2;
+  const int nmem2 = d.nmem * n2;
   const int jpi = d.jpi, jpj = d.jpj;
-  const long tid = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long nth = (long)gridDim.x * blockDim.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nth = gridDim.x * blockDim.x;
   const T grav = a.grav, rdtbt = a.rdtbt;
   int r = a.ring0;
-  for (int jn = 1; jn <= a.icycle; ++jn) {
-    const int sn = r & 3, sb = (r + 1) & 3, sbb = (r + 2) & 3, sa = (r + 3) & 3;
+  auto interior = [&](int p) -> bool {
+    const int i = p % jpi + 1, j = p / jpi + 1;
+    return i >= 2 && i <= jpi - 1 && j >= 2 && j <= jpj - 1;
+  };
+  // predictor fluxes of sub-step jn from the owner's levels (:724-800) and their
+  // un_adv / vn_adv sums (:860-862)
+  auto predictor = [&](int jn, int rr, int g) {
+    const int m2 = (g / n2) * n2, p = g - m2;
     T za1, za2, za3;
     ab3(jn, a.ll_init, za1, za2, za3);
-    const double w2 = a.wgt2[jn - 1], w1 = a.wgt1[jn - 1];
-    // ---- stage 1: fluxes, un_adv sums, ssha_e (:735-879)
-    for (long g = tid; g < nmem2; g += nth) {
-      const long m2 = (g / n2) * n2, p = g - m2;
-      const int i = (int)(p % jpi) + 1, j = (int)(p / jpi) + 1;
-      const T* un_e = a.ring_u + sn * nmem2 + m2;
-      const T* ub_e = a.ring_u + sb * nmem2 + m2;
-      const T* ubb_e = a.ring_u + sbb * nmem2 + m2;
-      const T* vn_e = a.ring_v + sn * nmem2 + m2;
-      const T* vb_e = a.ring_v + sb * nmem2 + m2;
-      const T* vbb_e = a.ring_v + sbb * nmem2 + m2;
-      auto zwx = [&](long q) -> T { return d.e2u[q] * (za1 * un_e[q] + za2 * ub_e[q] + za3 * ubb_e[q]) * d.hu_0[q]; };
-      auto zwy = [&](long q) -> T { return d.e1v[q] * (za1 * vn_e[q] + za2 * vb_e[q] + za3 * vbb_e[q]) * d.hv_0[q]; };
-      const T wx = zwx(p), wy = zwy(p);
-      a.un_adv[m2 + p] = a.un_adv[m2 + p] + (double)(T(w2) * wx * d.r1_e2u[p]);
-      a.vn_adv[m2 + p] = a.vn_adv[m2 + p] + (double)(T(w2) * wy * d.r1_e1v[p]);
-      T ssha_e = T(0);
-      if (i >= 2 && i <= jpi - 1 && j >= 2 && j <= jpj - 1) {
-        const T zhdiv = (wx - zwx(p - 1) + wy - zwy(p - jpi)) * d.r1_e1e2t[p];
-        ssha_e = (a.ring_ssh[sn * nmem2 + m2 + p] - rdtbt * (a.zssh_frc[m2 + p] + zhdiv)) * d.ssmask[p];
-      }
-      a.ring_ssh[sa * nmem2 + m2 + p] = ssha_e;
-    }
-    if (!grid_barrier(bar)) return;
-    // ---- stage 2: AM4 ssh, Coriolis, drag, pressure gradient, ua_e, sums (:904-1204)
+    const int sn = rr & 3, sb = (rr + 1) & 3, sbb = (rr + 2) & 3;
+    const T ua_e = za1 * a.ring_u[sn * nmem2 + g] + za2 * a.ring_u[sb * nmem2 + g] + za3 * a.ring_u[sbb * nmem2 + g];
+    const T va_e = za1 * a.ring_v[sn * nmem2 + g] + za2 * a.ring_v[sb * nmem2 + g] + za3 * a.ring_v[sbb * nmem2 + g];
+    const T zwx = d.e2u[p] * ua_e * d.hu_0[p];
+    const T zwy = d.e1v[p] * va_e * d.hv_0[p];
+    a.fx[(jn & 1) * nmem2 + g] = zwx;
+    a.fy[(jn & 1) * nmem2 + g] = zwy;
+    const T w2 = (T)a.wgt2[jn - 1];
+    a.un_adv[g] = a.un_adv[g] + (double)(w2 * zwx * d.r1_e2u[p]);
+    a.vn_adv[g] = a.vn_adv[g] + (double)(w2 * zwy * d.r1_e1v[p]);
+  };
+  if (a.icycle >= 1)
+    for (int g = tid; g < nmem2; g += nth) predictor(1, r, g);
+  if (!grid_barrier(bar)) return;
+  for (int jn = 1; jn <= a.icycle; ++jn) {
+    const int sn = r & 3, sb = (r + 1) & 3, sbb = (r + 2) & 3, sa = (r + 3) & 3;
+    const T* fx = a.fx + (jn & 1) * nmem2;
+    const T* fy = a.fy + (jn & 1) * nmem2;
+    const double w1 = a.wgt1[jn - 1];
     T zb0, zb1, zb2, zb3;
     am4(jn, a.ll_init, a.rn_bt_alpha, zb0, zb1, zb2, zb3);
-    for (long g = tid; g < nmem2; g += nth) {
-      const long m2 = (g / n2) * n2, p = g - m2;
-      const int i = (int)(p % jpi) + 1, j = (int)(p / jpi) + 1;
+    // ---- stage A: ssha_e (:871-879), its sum (:1204), AM4 ssh (:930-931)
+    for (int g = tid; g < nmem2; g += nth) {
+      const int m2 = (g / n2) * n2, p = g - m2;
+      T ssha_e = T(0);
+      const T sshn = a.ring_ssh[sn * nmem2 + g];
+      if (interior(p)) {
+        const T zhdiv = (fx[g] - fx[g - 1] + fy[g] - fy[g - jpi]) * d.r1_e1e2t[p];
+        ssha_e = (sshn - rdtbt * (a.zssh_frc[g] + zhdiv)) * d.ssmask[p];
+      }
+      a.ring_ssh[sa * nmem2 + g] = ssha_e;
+      a.ssha[g] = a.ssha[g] + w1 * (double)ssha_e;
+      a.zs[g] = zb0 * ssha_e + zb1 * sshn + zb2 * a.ring_ssh[sb * nmem2 + g] + zb3 * a.ring_ssh[sbb * nmem2 + g];
+    }
+    if (!grid_barrier(bar)) return;
+    // ---- stage B: Coriolis, drag, pressure gradient, ua_e/va_e, sums (:1000-1204)
+    for (int g = tid; g < nmem2; g += nth) {
+      const int m2 = (g / n2) * n2, p = g - m2;
       T ua_e = T(0), va_e = T(0);
-      if (i >= 2 && i <= jpi - 1 && j >= 2 && j <= jpj - 1) {
-        const T* un_e = a.ring_u + sn * nmem2 + m2;
-        const T* ub_e = a.ring_u + sb * nmem2 + m2;
-        const T* ubb_e = a.ring_u + sbb * nmem2 + m2;
-        const T* vn_e = a.ring_v + sn * nmem2 + m2;
-        const T* vb_e = a.ring_v + sb * nmem2 + m2;
-        const T* vbb_e = a.ring_v + sbb * nmem2 + m2;
-        const T* sa_ = a.ring_ssh + sa * nmem2 + m2;
-        const T* sn_ = a.ring_ssh + sn * nmem2 + m2;
-        const T* sb_ = a.ring_ssh + sb * nmem2 + m2;
-        const T* sbb_ = a.ring_ssh + sbb * nmem2 + m2;
-        auto uext = [&](long q) -> T { return za1 * un_e[q] + za2 * ub_e[q] + za3 * ubb_e[q]; };
-        auto vext = [&](long q) -> T { return za1 * vn_e[q] + za2 * vb_e[q] + za3 * vbb_e[q]; };
-        auto zwx = [&](long q) -> T { return d.e2u[q] * uext(q) * d.hu_0[q]; };
-        auto zwy = [&](long q) -> T { return d.e1v[q] * vext(q) * d.hv_0[q]; };
-        auto sp2 = [&](long q) -> T { return zb0 * sa_[q] + zb1 * sn_[q] + zb2 * sb_[q] + zb3 * sbb_[q]; };
+      const T un_e = a.ring_u[sn * nmem2 + g], vn_e = a.ring_v[sn * nmem2 + g];
+      if (interior(p)) {
+        T za1, za2, za3;
+        ab3(jn, a.ll_init, za1, za2, za3);
+        auto fxq = [&](int q) -> T { return fx[m2 + q]; };
+        auto fyq = [&](int q) -> T { return fy[m2 + q]; };
+        // the ENT scheme needs the extrapolated velocities themselves
+        auto uext = [&](int q) -> T {
+          return za1 * a.ring_u[sn * nmem2 + m2 + q] + za2 * a.ring_u[sb * nmem2 + m2 + q] +
+                 za3 * a.ring_u[sbb * nmem2 + m2 + q];
+        };
+        auto vext = [&](int q) -> T {
+          return za1 * a.ring_v[sn * nmem2 + m2 + q] + za2 * a.ring_v[sb * nmem2 + m2 + q] +
+                 za3 * a.ring_v[sbb * nmem2 + m2 + q];
+        };
         const T z1_hu = d.ssumask[p] / (d.hu_0[p] + T(1) - d.ssumask[p]);
         const T z1_hv = d.ssvmask[p] / (d.hv_0[p] + T(1) - d.ssvmask[p]);
         T zu_trd, zv_trd;
-        coriolis(d, a.nvor, p, zwx, zwy, uext, vext, z1_hu, z1_hv, zu_trd, zv_trd);
-        zu_trd = zu_trd + a.zCdU_u[m2 + p] * un_e[p] * d.r1_hu_0[p];
-        zv_trd = zv_trd + a.zCdU_v[m2 + p] * vn_e[p] * d.r1_hv_0[p];
-        const T s0 = sp2(p);
-        const T zu_spg = -grav * (sp2(p + 1) - s0) * d.r1_e1u[p];
-        const T zv_spg = -grav * (sp2(p + jpi) - s0) * d.r1_e2v[p];
+        coriolis(d, a.nvor, (long)p, fxq, fyq, uext, vext, z1_hu, z1_hv, zu_trd, zv_trd);
+        zu_trd = zu_trd + a.zCdU_u[g] * un_e * d.r1_hu_0[p];
+        zv_trd = zv_trd + a.zCdU_v[g] * vn_e * d.r1_hv_0[p];
+        const T s0 = a.zs[g];
+        const T zu_spg = -grav * (a.zs[g + 1] - s0) * d.r1_e1u[p];
+        const T zv_spg = -grav * (a.zs[g + jpi] - s0) * d.r1_e2v[p];
         const T wxs = (T(1) - a.scal_load) * zu_spg;
         const T wys = (T(1) - a.scal_load) * zv_spg;
-        ua_e = (un_e[p] + rdtbt * (wxs + zu_trd + a.zu_frc[m2 + p])) * d.ssumask[p];
-        va_e = (vn_e[p] + rdtbt * (wys + zv_trd + a.zv_frc[m2 + p])) * d.ssvmask[p];
+        ua_e = (un_e + rdtbt * (wxs + zu_trd + a.zu_frc[g])) * d.ssumask[p];
+        va_e = (vn_e + rdtbt * (wys + zv_trd + a.zv_frc[g])) * d.ssvmask[p];
       }
-      a.ring_u[sa * nmem2 + m2 + p] = ua_e;
-      a.ring_v[sa * nmem2 + m2 + p] = va_e;
-      a.ua_b[m2 + p] = a.ua_b[m2 + p] + w1 * (double)ua_e;
-      a.va_b[m2 + p] = a.va_b[m2 + p] + w1 * (double)va_e;
-      a.ssha[m2 + p] = a.ssha[m2 + p] + w1 * (double)a.ring_ssh[sa * nmem2 + m2 + p];
+      a.ring_u[sa * nmem2 + g] = ua_e;
+      a.ring_v[sa * nmem2 + g] = va_e;
+      a.ua_b[g] = a.ua_b[g] + w1 * (double)ua_e;
+      a.va_b[g] = a.va_b[g] + w1 * (double)va_e;
+      if (jn < a.icycle) predictor(jn + 1, (r + 3) & 3, g);
     }
     r = (r + 3) & 3;
     if (!grid_barrier(bar)) return;
   }
+  // ---- phase 3, per column (:1214-1240, :1266-1269): time-filtered transports
+  // and the two depth-independent terms each level adds
+  for (int g = tid; g < nmem2; g += nth) {
+    const int m2 = (g / n2) * n2, p = g - m2;
+    double uadv = a.un_adv[g], vadv = a.vn_adv[g];
+    if (a.ln_bt_fw) {
+      const double zwx = uadv, zwy = vadv;
+      if (a.phase3_filter) {
+        uadv = 0.5 * (a.ub2_b[g] + zwx - a.rn_atfp * a.un_bf[g]);
+        vadv = 0.5 * (a.vb2_b[g] + zwy - a.rn_atfp * a.vn_bf[g]);
+        a.un_bf[g] = a.rn_atfp * a.un_bf[g] + (zwx - a.ub2_b[g]);
+        a.vn_bf[g] = a.rn_atfp * a.vn_bf[g] + (zwy - a.vb2_b[g]);
+      } else {
+        a.un_bf[g] = 0.0;
+        a.vn_bf[g] = 0.0;
+      }
+      a.ub2_b[g] = zwx;
+      a.vb2_b[g] = zwy;
+      a.un_adv[g] = uadv;
+      a.vn_adv[g] = vadv;
+    }
+    a.du[g] = (T)((a.ua_b[g] - (double)a.ub_b[g]) * a.r1_2dt_b);
+    a.dv[g] = (T)((a.va_b[g] - (double)a.vb_b[g]) * a.r1_2dt_b);
+    a.cu[g] = (T)(uadv * (double)d.r1_hu_0[p]);
+    a.cv[g] = (T)(vadv * (double)d.r1_hv_0[p]);
+  }
 }
 
-// Phase 3 (:1214-1269): time-filtered transports, baroclinic trend update and the
-// correction of the now velocities. One thread per column, all columns.
+// Phase 3, per point (:1236-1240, :1266-1269): the barotropic trend added to ua, va
+// and the now velocities corrected to the time-filtered transports.
 template <class T>
 __global__ void k_spg_p3(Dom<T> d, SpgArgs<T> a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int m = blockIdx.z;
-  if (i > d.jpi || j > d.jpj) return;
-  const long p = pt_ij(d, i, j), n2 = d.n2, m2 = (long)m * n2, m3 = (long)m * d.n3;
-  double uadv = a.un_adv[m2 + p], vadv = a.vn_adv[m2 + p];
-  if (a.ln_bt_fw) {
-    const double zwx = uadv, zwy = vadv;
-    if (a.phase3_filter) {
-      uadv = 0.5 * (a.ub2_b[m2 + p] + zwx - a.rn_atfp * a.un_bf[m2 + p]);
-      vadv = 0.5 * (a.vb2_b[m2 + p] + zwy - a.rn_atfp * a.vn_bf[m2 + p]);
-      a.un_bf[m2 + p] = a.rn_atfp * a.un_bf[m2 + p] + (zwx - a.ub2_b[m2 + p]);
-      a.vn_bf[m2 + p] = a.rn_atfp * a.vn_bf[m2 + p] + (zwy - a.vb2_b[m2 + p]);
-    } else {
-      a.un_bf[m2 + p] = 0.0;
-      a.vn_bf[m2 + p] = 0.0;
-    }
-    a.ub2_b[m2 + p] = zwx;
-    a.vb2_b[m2 + p] = zwy;
-    a.un_adv[m2 + p] = uadv;
-    a.vn_adv[m2 + p] = vadv;
-  }
-  const T du = (T)((a.ua_b[m2 + p] - (double)a.ub_b[m2 + p]) * a.r1_2dt_b);
-  const T dv = (T)((a.va_b[m2 + p] - (double)a.vb_b[m2 + p]) * a.r1_2dt_b);
-  const T cu = (T)(uadv * (double)d.r1_hu_0[p]);
-  const T cv = (T)(vadv * (double)d.r1_hv_0[p]);
-  const T unb = a.un_b[m2 + p], vnb = a.vn_b[m2 + p];
+  const int k = (int)(blockIdx.z % (unsigned)d.jpk) + 1;
+  const int m = (int)(blockIdx.z / (unsigned)d.jpk);
+  if (i > d.jpi || j > d.jpj || k > d.jpk - 1) return;
+  const long p = pt_ij(d, i, j), m2 = (long)m * d.n2;
+  const long q = (long)m * d.n3 + p + (long)(k - 1) * d.n2;
   const ColInfo ci = d.ci[p];
-  for (int k = 1; k <= d.jpk - 1; ++k) {
-    const long q = m3 + p + (long)(k - 1) * n2;
-    a.ua[q] = a.ua[q] + du;
-    a.va[q] = a.va[q] + dv;
-    a.un[q] = (a.un[q] + cu - unb) * umsk<T>(ci, k);
-    a.vn[q] = (a.vn[q] + cv - vnb) * vmsk<T>(ci, k);
-  }
+  a.ua[q] = a.ua[q] + a.du[m2 + p];
+  a.va[q] = a.va[q] + a.dv[m2 + p];
+  a.un[q] = (a.un[q] + a.cu[m2 + p] - a.un_b[m2 + p]) * umsk<T>(ci, k);
+  a.vn[q] = (a.vn[q] + a.cv[m2 + p] - a.vn_b[m2 + p]) * vmsk<T>(ci, k);
 }
 
 // ---------------------------------------------------------------------------------

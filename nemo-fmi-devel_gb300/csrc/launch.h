@@ -3,9 +3,27 @@
 #pragma once
 #include "k_dyn.cuh"
 #include "k_tra.cuh"
-#include "k_fused.cuh"
+#include "../../include/nemo_gpu.h"
 
 namespace nemo {
+
+// Per-kernel timing: while a context times the hot path it installs its clock for
+// the calling thread, and every launcher below records an event on the launch
+// stream after each kernel it enqueues (ids: enum nemo_kernel_id).
+struct KernelClock {
+  static constexpr int CAP = 96;
+  cudaEvent_t ev[CAP + 1] = {};  // ev[0]: before the first kernel
+  int id[CAP] = {};
+  int n = 0;
+};
+extern thread_local KernelClock* t_kclock;
+inline void ktick(int id, cudaStream_t s) {
+  KernelClock* k = t_kclock;
+  if (k && k->n < KernelClock::CAP) {
+    cudaEventRecord(k->ev[k->n + 1], s);
+    k->id[k->n++] = id;
+  }
+}
 
 template <class T>
 cudaError_t launch_adv_trp(const Dom<T>& d, const T* un, const T* vn, const T* wn, T* zun, T* zvn, T* zwn,
@@ -17,7 +35,9 @@ cudaError_t launch_ldf_lap(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s)
 template <class T>
 cudaError_t launch_ldf_iso(const Dom<T>& d, const LdfArgs<T>& a, int copy_akz_edges, int msc_edges, cudaStream_t s);
 template <class T>
-cudaError_t launch_iso_akz_edges(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s);
+cudaError_t launch_iso_flux(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s);
+template <class T>
+cudaError_t launch_iso_edges(const Dom<T>& d, const LdfArgs<T>& a, int copy_akz_edges, int msc_edges, cudaStream_t s);
 template <class T>
 cudaError_t launch_zdf(const Dom<T>& d, const ZdfArgs<T>& a, cudaStream_t s);
 template <class T>
@@ -31,8 +51,5 @@ cudaError_t launch_lbc(T* p, int jpi, int jpj, long nslab, int is_f, T pval, cud
 template <class T>
 cudaError_t launch_globsum(const T* x, const double* tmask_i, long n2, int nk, int nmem, double* part, int nblk,
                            double* out, cudaStream_t s);
-
-// fused FCT + iso-neutral tracer kernel (float only)
-cudaError_t launch_tra_fused(const Dom<float>& d, const FusedArgs<float>& a, cudaStream_t s);
 
 }  // namespace nemo

@@ -17,16 +17,17 @@ PREC_FP64, PREC_MIXED = 0, 1
 VOR = {"ENS": 0, "ENE": 1, "ENT": 2, "EET": 3, "EEN": 4, "MIX": 5}
 
 
-def _field_ids():
+def _enum(name, prefix):
     txt = open(HEADER).read()
-    body = re.search(r"enum nemo_field_id \{(.*?)\};", txt, re.S).group(1)
+    body = re.search(r"enum %s \{(.*?)\};" % name, txt, re.S).group(1)
     body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
     names = [n.split("=")[0].strip() for n in body.split(",")]
     names = [n for n in names if n]
-    return {n[len("NEMO_F_"):]: i for i, n in enumerate(names)}
+    return {n[len(prefix):]: i for i, n in enumerate(names)}
 
 
-F = _field_ids()  # e.g. F["TSB"] == 0, F["COUNT"] == number of fields
+F = _enum("nemo_field_id", "NEMO_F_")  # e.g. F["TSB"] == 0, F["COUNT"] == number of fields
+K = _enum("nemo_kernel_id", "NEMO_K_")  # kernel ids of nemo_gpu_get_kernel_timing
 FP64_FIELDS = {"SSHA", "UA_B", "VA_B", "UN_ADV", "VN_ADV", "UB2_B", "VB2_B", "UN_BF", "VN_BF"}
 
 _dp = C.POINTER(C.c_double)
@@ -117,6 +118,7 @@ def load(path):
     _proto(lib, "nemo_gpu_set_timing", i, [vp, i])
     _proto(lib, "nemo_gpu_set_fusion", i, [vp, i])
     _proto(lib, "nemo_gpu_get_timing", i, [vp, C.POINTER(d), C.POINTER(i)])
+    _proto(lib, "nemo_gpu_get_kernel_timing", i, [vp, C.POINTER(d), C.POINTER(i), i])
     return lib
 
 

@@ -132,6 +132,15 @@ class Context:
         self._ck(self.lib.nemo_gpu_get_timing(self.h, ms, C.byref(n)), "get_timing")
         return dict(zip(("dyn_spg_ts", "tra_adv", "tra_ldf", "tra_zdf"), list(ms))), n.value
 
+    def get_kernel_timing(self):
+        """{kernel name: (cumulative ms, launches)} of the kernels timed since set_timing(True)."""
+        nk = _ffi.K["COUNT"]
+        ms = (C.c_double * nk)()
+        cnt = (C.c_int * nk)()
+        self._ck(self.lib.nemo_gpu_get_kernel_timing(self.h, ms, cnt, nk), "get_kernel_timing")
+        names = {v: k.lower() for k, v in _ffi.K.items() if k != "COUNT"}
+        return {names[i]: (ms[i], cnt[i]) for i in range(nk) if cnt[i] > 0}
+
     def upload(self, name, host):
         """nemo_gpu_field_upload from a (pinned) host torch tensor."""
         self._ck(self.lib.nemo_gpu_field_upload(self.h, _ffi.F[name], host.data_ptr()), f"upload {name}")
