@@ -73,7 +73,7 @@ struct nemo_ctx {
   int fct_kjpt = 0;
   void* spg_w[5] = {};
   void* ring[3] = {};
-  void* spg_x[7] = {};  // fx (2 slots), fy (2 slots), zs, du|dv|cu|cv
+  void* spg_x[6] = {};  // fx (2 slots), fy (2 slots), du, dv, cu, cv
   unsigned int* bar_mem = nullptr;  // count, gen
   int* err_flag = nullptr;
   long long bar_spins = 4000000;
@@ -249,7 +249,7 @@ void coriolis_factors(nemo_ctx* c, const std::vector<double>& tmask, const std::
 }
 
 template <class T>
-int upload(nemo_ctx* c, DomStore<T>& st, const std::vector<double>& src, const T** dst) {
+int upload(nemo_ctx* c, DomStore<T>& st, const std::vector<double>& src, RO<T>* dst) {
   std::vector<T> h(src.size());
   for (size_t i = 0; i < src.size(); ++i) h[i] = (T)src[i];
   void* p = nullptr;
@@ -267,12 +267,12 @@ int upload_e3(nemo_ctx* c, DomStore<T>& st, int which, E3<T>* e) {
   if (c->e3_uniform[which]) {
     std::vector<double> prof(c->jpk);
     for (int k = 0; k < c->jpk; ++k) prof[k] = a[(size_t)k * c->n2];
-    const T* p;
+    RO<T> p;
     int st_ = upload(c, st, prof, &p);
     if (st_) return st_;
     *e = E3<T>{p, 1, 0, 0};
   } else {
-    const T* p;
+    RO<T> p;
     int st_ = upload(c, st, a, &p);
     if (st_) return st_;
     *e = E3<T>{p, c->n2, 0, 1};
@@ -667,8 +667,8 @@ int run_spg(nemo_ctx* c, int kt) {
   a.zu_frc = (T*)c->spg_w[0]; a.zv_frc = (T*)c->spg_w[1]; a.zssh_frc = (T*)c->spg_w[2];
   a.zCdU_u = (T*)c->spg_w[3]; a.zCdU_v = (T*)c->spg_w[4];
   a.ring_ssh = (T*)c->ring[0]; a.ring_u = (T*)c->ring[1]; a.ring_v = (T*)c->ring[2];
-  a.fx = (T*)c->spg_x[0]; a.fy = (T*)c->spg_x[1]; a.zs = (T*)c->spg_x[2];
-  a.du = (T*)c->spg_x[3]; a.dv = (T*)c->spg_x[4]; a.cu = (T*)c->spg_x[5]; a.cv = (T*)c->spg_x[6];
+  a.fx = (T*)c->spg_x[0]; a.fy = (T*)c->spg_x[1];
+  a.du = (T*)c->spg_x[2]; a.dv = (T*)c->spg_x[3]; a.cu = (T*)c->spg_x[4]; a.cv = (T*)c->spg_x[5];
   a.wgt1 = c->d_wgt1; a.wgt2 = c->d_wgt2;
   a.ln_bt_fw = nm.ln_bt_fw; a.ln_apr_dyn = nm.ln_apr_dyn; a.nvor = nm.nvor_scheme; a.ll_init = ll_init;
   a.icycle = c->icycle;
@@ -804,7 +804,7 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
     if (cudaMalloc(&p, 4 * b2) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
     cudaMemset(p, 0, 4 * b2);
   }
-  for (int w = 0; w < 7; ++w) {
+  for (int w = 0; w < 6; ++w) {
     const size_t bytes = w < 2 ? 2 * b2 : b2;
     if (cudaMalloc(&c->spg_x[w], bytes) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
     cudaMemset(c->spg_x[w], 0, bytes);
@@ -818,7 +818,8 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
   cudaMemset(c->bar_mem, 0, 2 * sizeof(unsigned int));
   cudaMemset(c->err_flag, 0, sizeof(int));
   const int bps = prec == NEMO_PREC_FP64 ? spg_p2_blocks_per_sm<double>() : spg_p2_blocks_per_sm<float>();
-  long need = (c->n2 * c->nmem + 255) / 256;
+  // one block per 32 x 8 tile of the sub-step kernel, at most all co-resident
+  long need = (long)((c->jpi + 31) / 32) * ((c->jpj + 7) / 8) * c->nmem;
   long maxb = (long)bps * c->nsm;
   c->p2_blocks = (int)(need < maxb ? need : maxb);
   if (c->p2_blocks < 1) return bad(NEMO_ERR_CUDA);
@@ -1029,7 +1030,7 @@ int nemo_gpu_lbc_lnk_multi(nemo_ctx* c, const char* cdname, int kfld, void* cons
 int nemo_gpu_glob_sum(nemo_ctx* c, const char* cdname, const void* ptab, int nk, int is_fp64, double* out) {
   (void)cdname;
   if (!c || !ptab || nk < 1 || !out) return fail(c, NEMO_ERR_ARG, "glob_sum: bad argument");
-  const double* tmi = c->prec == NEMO_PREC_FP64 ? c->dd.d.tmask_i : c->df.d.tmask_i;
+  const double* tmi = c->prec == NEMO_PREC_FP64 ? c->dd.d.tmask_i.p : c->df.d.tmask_i.p;
   cudaError_t e = is_fp64 ? launch_globsum<double>((const double*)ptab, tmi, c->n2, nk, c->nmem, c->gs_part, c->gs_nblk,
                                                    c->gs_out, c->stream)
                           : launch_globsum<float>((const float*)ptab, tmi, c->n2, nk, c->nmem, c->gs_part, c->gs_nblk,

@@ -13,6 +13,12 @@ static dim3 col_grid(const Dom<T>& d) {
   return dim3((d.jpi + BX - 1) / BX, (d.jpj + BY - 1) / BY, d.nmem);
 }
 
+// one thread per KCH-level chunk of a column: z = member * nchunk + chunk
+template <class T>
+static dim3 kc_grid(const Dom<T>& d) {
+  return dim3((d.jpi + BX - 1) / BX, (d.jpj + BY - 1) / BY, d.nmem * ((d.jpk + KCH - 1) / KCH));
+}
+
 // one thread per (i,j,k) point: z = member * jpk + (k - 1)
 template <class T>
 static dim3 pt_grid(const Dom<T>& d) {
@@ -30,14 +36,14 @@ cudaError_t launch_adv_trp(const Dom<T>& d, const T* un, const T* vn, const T* w
 template <class T>
 cudaError_t launch_fct(const Dom<T>& d, const FctArgs<T>& a, cudaStream_t s) {
   if (a.kn_fct_v == 4) {
-    k_interp4<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a.ptn, const_cast<T*>(a.ztw), a.kjpt);
+    k_interp4<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a.ptn, const_cast<T*>(a.ztw.p), a.kjpt);
     ktick(NEMO_K_INTERP4, s);
   }
-  k_fct_a<T><<<pt_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  k_fct_a<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
   ktick(NEMO_K_FCT_A, s);
-  k_fct_b<T><<<pt_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  k_fct_b<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
   ktick(NEMO_K_FCT_B, s);
-  k_fct_c<T><<<pt_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  k_fct_c<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
   ktick(NEMO_K_FCT_C, s);
   return cudaGetLastError();
 }
@@ -51,7 +57,7 @@ cudaError_t launch_ldf_lap(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s)
 
 template <class T>
 cudaError_t launch_ldf_iso(const Dom<T>& d, const LdfArgs<T>& a, int copy_akz_edges, int msc_edges, cudaStream_t s) {
-  k_iso_flux<T><<<pt_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  k_iso_flux<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
   ktick(NEMO_K_ISO_FLUX, s);
   k_iso_div<T><<<pt_grid(d), dim3(BX, BY), 0, s>>>(d, a);
   ktick(NEMO_K_ISO_DIV, s);
@@ -60,7 +66,7 @@ cudaError_t launch_ldf_iso(const Dom<T>& d, const LdfArgs<T>& a, int copy_akz_ed
 
 template <class T>
 cudaError_t launch_iso_flux(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s) {
-  k_iso_flux<T><<<pt_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  k_iso_flux<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
   ktick(NEMO_K_ISO_FLUX, s);
   return cudaGetLastError();
 }

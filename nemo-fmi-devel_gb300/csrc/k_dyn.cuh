@@ -3,8 +3,9 @@
 //
 // Phase 1 (forcing of the 2-D system) and phase 3 (correction of the 3-D fields)
 // are column kernels. Phase 2, the icycle barotropic sub-steps, is ONE persistent
-// cooperative kernel: each sub-step is two grid-wide stages separated by a bounded
-// grid barrier (after ssha_e, after ua_e/va_e). The three time levels of ssh, u, v
+// cooperative kernel with one bounded grid barrier per sub-step (each block
+// recomputes the new ssh of a one-point halo instead of waiting for its owner). The
+// three time levels of ssh, u, v
 // and the new level live in a ring of 4 slots, so the reference's swap
 // (:1176-1186) is an index rotation and no stage overwrites a level a neighbouring
 // point still reads. T is the bulk type; the time-filter accumulators ssha, ua_b,
@@ -19,20 +20,19 @@ template <class T>
 struct SpgArgs {
   // 3-D
   T *ua, *va, *un, *vn;
-  const T *ub, *vb;
+  RO<T> ub, vb;
   // 2-D inputs
-  const T *sshn, *sshb, *un_b, *vn_b, *ub_b, *vb_b;
-  const T *utau, *vtau, *utau_b, *vtau_b, *emp, *emp_b, *rnf, *rnf_b;
-  const T *rCdU_bot, *ssh_ib, *ssh_ibb;
+  RO<T> sshn, sshb, un_b, vn_b, ub_b, vb_b;
+  RO<T> utau, vtau, utau_b, vtau_b, emp, emp_b, rnf, rnf_b;
+  RO<T> rCdU_bot, ssh_ib, ssh_ibb;
   // FP64 accumulators / restart fields
   double *ssha, *ua_b, *va_b, *un_adv, *vn_adv, *ub2_b, *vb2_b, *un_bf, *vn_bf;
   // library work arrays (2-D, per member)
   T *zu_frc, *zv_frc, *zssh_frc, *zCdU_u, *zCdU_v;
   T *ring_ssh, *ring_u, *ring_v;  // 4 slots each
   T *fx, *fy;                     // 2 slots each: predictor fluxes zwx, zwy of a sub-step
-  T* zs;                          // zsshp2_e of the current sub-step
   T *du, *dv, *cu, *cv;           // phase-3 column terms, computed at the end of phase 2
-  const double *wgt1, *wgt2;
+  RO<double> wgt1, wgt2;
   int ln_bt_fw, ln_apr_dyn, nvor, ll_init, icycle, ring0, phase3_filter;
   T rdtbt, grav, r1_rau0, scal_load, rn_bt_alpha;
   double rn_atfp, r1_2dt_b;
@@ -71,39 +71,52 @@ __global__ void k_spg_p1a(Dom<T> d, SpgArgs<T> a) {
 }
 
 // Barotropic Coriolis trend of a flux field (ENE/MIX, ENS, EET/EEN, ENT) at an
-// interior point (:390-443 and :1000-1056). fx/fy return the fluxes zwx/zwy at a
-// point; for ENT fu/fv return the velocities and hu/hv the inverse depths.
-template <class T, class FX, class FY, class FU, class FV>
-__device__ __forceinline__ void coriolis(const Dom<T>& d, int nvor, long p, FX fx, FY fy, FU fu, FV fv, T z1_hu,
-                                         T z1_hv, T& zu_trd, T& zv_trd) {
+// interior point (:390-443 and :1000-1056). Every scheme reads the same eight
+// neighbours, passed preloaded: x[0..3] = zwx at p-1, p, p-1+jpi, p+jpi and
+// y[0..3] = zwy at p-jpi, p+1-jpi, p, p+1; for ENT xu / yv are the velocities at
+// the same points and z1_hu / z1_hv the inverse depths.
+template <class T>
+__device__ __forceinline__ void coriolis(const Dom<T>& d, int nvor, long p, const T (&x)[4], const T (&y)[4],
+                                         const T (&xu)[4], const T (&yv)[4], T z1_hu, T z1_hv, T& zu_trd,
+                                         T& zv_trd) {
   const int jpi = d.jpi;
   const T r1_4 = T(0.25), r1_8 = T(0.125), r1_12 = T(1) / T(12);
   if (nvor == 2) {  // ENT
-    const T* e = d.e1e2t;
-    const T* h = d.ht_0;
-    const T* ft = d.ff_t;
+    const RO<T> e = d.e1e2t;
+    const RO<T> h = d.ht_0;
+    const RO<T> ft = d.ff_t;
     zu_trd = +r1_4 * d.r1_e1e2u[p] * z1_hu *
-             (e[p + 1] * h[p + 1] * ft[p + 1] * (fv(p + 1) + fv(p + 1 - jpi)) + e[p] * h[p] * ft[p] * (fv(p) + fv(p - jpi)));
+             (e[p + 1] * h[p + 1] * ft[p + 1] * (yv[3] + yv[1]) + e[p] * h[p] * ft[p] * (yv[2] + yv[0]));
     zv_trd = -r1_4 * d.r1_e1e2v[p] * z1_hv *
-             (e[p + jpi] * h[p + jpi] * ft[p + jpi] * (fu(p + jpi) + fu(p - 1 + jpi)) + e[p] * h[p] * ft[p] * (fu(p) + fu(p - 1)));
+             (e[p + jpi] * h[p + jpi] * ft[p + jpi] * (xu[3] + xu[2]) + e[p] * h[p] * ft[p] * (xu[1] + xu[0]));
   } else if (nvor == 1 || nvor == 5) {  // ENE, MIX
-    const T zy1 = (fy(p - jpi) + fy(p + 1 - jpi)) * d.r1_e1u[p];
-    const T zy2 = (fy(p) + fy(p + 1)) * d.r1_e1u[p];
-    const T zx1 = (fx(p - 1) + fx(p - 1 + jpi)) * d.r1_e2v[p];
-    const T zx2 = (fx(p) + fx(p + jpi)) * d.r1_e2v[p];
+    const T zy1 = (y[0] + y[1]) * d.r1_e1u[p];
+    const T zy2 = (y[2] + y[3]) * d.r1_e1u[p];
+    const T zx1 = (x[0] + x[2]) * d.r1_e2v[p];
+    const T zx2 = (x[1] + x[3]) * d.r1_e2v[p];
     zu_trd = r1_4 * (d.zwz[p - jpi] * zy1 + d.zwz[p] * zy2);
     zv_trd = -r1_4 * (d.zwz[p - 1] * zx1 + d.zwz[p] * zx2);
   } else if (nvor == 0) {  // ENS
-    const T zy1 = r1_8 * (fy(p - jpi) + fy(p + 1 - jpi) + fy(p) + fy(p + 1)) * d.r1_e1u[p];
-    const T zx1 = -r1_8 * (fx(p - 1) + fx(p - 1 + jpi) + fx(p) + fx(p + jpi)) * d.r1_e2v[p];
+    const T zy1 = r1_8 * (y[0] + y[1] + y[2] + y[3]) * d.r1_e1u[p];
+    const T zx1 = -r1_8 * (x[0] + x[2] + x[1] + x[3]) * d.r1_e2v[p];
     zu_trd = zy1 * (d.zwz[p - jpi] + d.zwz[p]);
     zv_trd = zx1 * (d.zwz[p - 1] + d.zwz[p]);
   } else {  // EET, EEN
     zu_trd = +r1_12 * d.r1_e1u[p] *
-             (d.ftne[p] * fy(p) + d.ftnw[p + 1] * fy(p + 1) + d.ftse[p] * fy(p - jpi) + d.ftsw[p + 1] * fy(p + 1 - jpi));
+             (d.ftne[p] * y[2] + d.ftnw[p + 1] * y[3] + d.ftse[p] * y[0] + d.ftsw[p + 1] * y[1]);
     zv_trd = -r1_12 * d.r1_e2v[p] *
-             (d.ftsw[p + jpi] * fx(p - 1 + jpi) + d.ftse[p + jpi] * fx(p + jpi) + d.ftnw[p] * fx(p - 1) + d.ftne[p] * fx(p));
+             (d.ftsw[p + jpi] * x[2] + d.ftse[p + jpi] * x[3] + d.ftnw[p] * x[0] + d.ftne[p] * x[1]);
   }
+}
+
+// the eight neighbours of p that coriolis() reads, of a point function f
+template <class T, class F>
+__device__ __forceinline__ void nbx(F f, long p, int jpi, T (&x)[4]) {
+  x[0] = f(p - 1); x[1] = f(p); x[2] = f(p - 1 + jpi); x[3] = f(p + jpi);
+}
+template <class T, class F>
+__device__ __forceinline__ void nby(F f, long p, int jpi, T (&y)[4]) {
+  y[0] = f(p - jpi); y[1] = f(p + 1 - jpi); y[2] = f(p); y[3] = f(p + 1);
 }
 
 // Phase 1b (:387-702): Coriolis of the now barotropic flow, bottom stress, wind,
@@ -118,14 +131,21 @@ __global__ void k_spg_p1b(Dom<T> d, SpgArgs<T> a) {
   const T r1_2 = T(0.5);
   const bool interior = i >= 2 && i <= d.jpi - 1 && j >= 2 && j <= d.jpj - 1;
   if (interior) {
-    const T* unb = a.un_b + m2;
-    const T* vnb = a.vn_b + m2;
+    const RO<T> unb = a.un_b + m2;
+    const RO<T> vnb = a.vn_b + m2;
     auto fx = [&](long q) -> T { return unb[q] * d.hu_0[q] * d.e2u[q]; };
     auto fy = [&](long q) -> T { return vnb[q] * d.hv_0[q] * d.e1v[q]; };
     auto fu = [&](long q) -> T { return unb[q]; };
     auto fv = [&](long q) -> T { return vnb[q]; };
+    T x[4], y[4], xu[4] = {}, yv[4] = {};
+    nbx(fx, p, d.jpi, x);
+    nby(fy, p, d.jpi, y);
+    if (a.nvor == 2) {
+      nbx(fu, p, d.jpi, xu);
+      nby(fv, p, d.jpi, yv);
+    }
     T zu_trd, zv_trd;
-    coriolis(d, a.nvor, p, fx, fy, fu, fv, d.r1_hu_0[p], d.r1_hv_0[p], zu_trd, zv_trd);
+    coriolis(d, a.nvor, p, x, y, xu, yv, d.r1_hu_0[p], d.r1_hv_0[p], zu_trd, zv_trd);
     T zu = a.zu_frc[m2 + p] - zu_trd * d.ssumask[p];
     T zv = a.zv_frc[m2 + p] - zv_trd * d.ssvmask[p];
     // bottom stress from the baroclinic bottom velocity (:519-557)
@@ -134,7 +154,7 @@ __global__ void k_spg_p1b(Dom<T> d, SpgArgs<T> a) {
     T zwx, zwy;
     if (a.ln_bt_fw) { zwx = a.un[qu] - unb[p]; zwy = a.vn[qv] - vnb[p]; }
     else { zwx = a.ub[qu] - a.ub_b[m2 + p]; zwy = a.vb[qv] - a.vb_b[m2 + p]; }
-    const T* cdu = a.rCdU_bot + m2;
+    const RO<T> cdu = a.rCdU_bot + m2;
     zu = zu + d.r1_hu_0[p] * r1_2 * (cdu[p + 1] + cdu[p]) * zwx;
     zv = zv + d.r1_hv_0[p] * r1_2 * (cdu[p + d.jpi] + cdu[p]) * zwy;
     // wind (:589-604)
@@ -148,13 +168,13 @@ __global__ void k_spg_p1b(Dom<T> d, SpgArgs<T> a) {
     }
     // atmospheric pressure (:606-629)
     if (a.ln_apr_dyn) {
-      const T* ib = a.ssh_ib + m2;
+      const RO<T> ib = a.ssh_ib + m2;
       T zu_spg, zv_spg;
       if (a.ln_bt_fw) {
         zu_spg = a.grav * (ib[p + 1] - ib[p]) * d.r1_e1u[p];
         zv_spg = a.grav * (ib[p + d.jpi] - ib[p]) * d.r1_e2v[p];
       } else {
-        const T* ibb = a.ssh_ibb + m2;
+        const RO<T> ibb = a.ssh_ibb + m2;
         const T zztmp = a.grav * r1_2;
         zu_spg = zztmp * (ib[p + 1] - ib[p] + ibb[p + 1] - ibb[p]) * d.r1_e1u[p];
         zv_spg = zztmp * (ib[p + d.jpi] - ib[p] + ibb[p + d.jpi] - ibb[p]) * d.r1_e2v[p];
@@ -219,36 +239,47 @@ __device__ __forceinline__ void am4(int jn, int ll_init, T alpha, T& za0, T& za1
   }
 }
 
-// Phase 2: the icycle sub-steps (:712-1207) in one persistent kernel, followed by
-// the per-column part of phase 3.
-//
-// Every 2-D point is owned by one thread for the whole kernel. A sub-step is two
-// stages separated by grid barriers:
-//  A: ssha_e from the divergence of the published predictor fluxes, its sum into
-//     ssha, and the AM4 surface height zsshp2_e, published in zs;
-//  B: Coriolis from the neighbours' published fluxes, bottom drag, pressure
-//     gradient from zs, the new ua_e/va_e and their sums -- then, from the owner's
-//     own levels only, the predictor fluxes of the next sub-step (published in the
-//     other fx/fy slot) and their un_adv/vn_adv sums.
-// Each published value is computed once, by its owner, with the reference's
-// expression, so neighbours read exactly the value they would have recomputed.
+// Phase 2 (:664-1207): the icycle sub-steps in one persistent cooperative kernel,
+// ONE grid barrier per sub-step. Blocks own 32 x 8 tiles of points. In sub-step jn
+// a block first computes, for its tile and a one-point halo to the east and north,
+// the new ssh (ssha_e, :871-879) and the AM4 ssh zsshp2_e (:930-931) into shared
+// memory -- from the predictor fluxes and ssh levels published before the last
+// barrier -- and keeps ssha_e and the ssha sum (:1204) of the points it owns; then,
+// per owned point, the Coriolis, drag and pressure-gradient trends, ua_e / va_e and
+// their sums (:1000-1204), and the predictor fluxes of sub-step jn+1 (:724-800) with
+// their un_adv / vn_adv sums (:860-862). Reads and writes of one sub-step never
+// touch the same ring slot or flux buffer, so one barrier separates sub-steps.
+constexpr int P2_TX = 32, P2_TY = 8;
+
+template <class T>
+__device__ __forceinline__ int p2_tiles(const Dom<T>& d) {
+  return ((d.jpi + P2_TX - 1) / P2_TX) * ((d.jpj + P2_TY - 1) / P2_TY) * d.nmem;
+}
+
 template <class T>
 __global__ void __launch_bounds__(256) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar bar) {
+  __shared__ T zs_s[P2_TY + 1][P2_TX + 1];
   const int n2 = (int)d.n2;
   const int nmem2 = d.nmem * n2;
   const int jpi = d.jpi, jpj = d.jpj;
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nth = gridDim.x * blockDim.x;
+  const int ntx = (jpi + P2_TX - 1) / P2_TX, nty = (jpj + P2_TY - 1) / P2_TY;
+  const int ntile = ntx * nty * d.nmem;
+  const int tx = threadIdx.x % P2_TX, ty = threadIdx.x / P2_TX;
   const T grav = a.grav, rdtbt = a.rdtbt;
+  // forcing of the sub-steps, written by phase 1 and only read here
+  const RO<T> zssh_frc = a.zssh_frc, zu_frc = a.zu_frc, zv_frc = a.zv_frc, zCdU_u = a.zCdU_u, zCdU_v = a.zCdU_v;
   int r = a.ring0;
-  auto interior = [&](int p) -> bool {
-    const int i = p % jpi + 1, j = p / jpi + 1;
-    return i >= 2 && i <= jpi - 1 && j >= 2 && j <= jpj - 1;
+  auto interior = [&](int i, int j) -> bool { return i >= 2 && i <= jpi - 1 && j >= 2 && j <= jpj - 1; };
+  // tile t -> member offset m2 and the 1-based indices of its first point
+  auto tile = [&](int t, int& m2, int& i0, int& j0) {
+    const int m = t / (ntx * nty), tt = t - m * (ntx * nty);
+    m2 = m * n2;
+    i0 = (tt % ntx) * P2_TX + 1;
+    j0 = (tt / ntx) * P2_TY + 1;
   };
   // predictor fluxes of sub-step jn from the owner's levels (:724-800) and their
   // un_adv / vn_adv sums (:860-862)
-  auto predictor = [&](int jn, int rr, int g) {
-    const int m2 = (g / n2) * n2, p = g - m2;
+  auto predictor = [&](int jn, int rr, int g, int p) {
     T za1, za2, za3;
     ab3(jn, a.ll_init, za1, za2, za3);
     const int sn = rr & 3, sb = (rr + 1) & 3, sbb = (rr + 2) & 3;
@@ -263,7 +294,15 @@ __global__ void __launch_bounds__(256) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar 
     a.vn_adv[g] = a.vn_adv[g] + (double)(w2 * zwy * d.r1_e1v[p]);
   };
   if (a.icycle >= 1)
-    for (int g = tid; g < nmem2; g += nth) predictor(1, r, g);
+    for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
+      int m2, i0, j0;
+      tile(t, m2, i0, j0);
+      const int i = i0 + tx, j = j0 + ty;
+      if (i <= jpi && j <= jpj) {
+        const int p = (i - 1) + (j - 1) * jpi;
+        predictor(1, r, m2 + p, p);
+      }
+    }
   if (!grid_barrier(bar)) return;
   for (int jn = 1; jn <= a.icycle; ++jn) {
     const int sn = r & 3, sb = (r + 1) & 3, sbb = (r + 2) & 3, sa = (r + 3) & 3;
@@ -272,64 +311,132 @@ __global__ void __launch_bounds__(256) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar 
     const double w1 = a.wgt1[jn - 1];
     T zb0, zb1, zb2, zb3;
     am4(jn, a.ll_init, a.rn_bt_alpha, zb0, zb1, zb2, zb3);
-    // ---- stage A: ssha_e (:871-879), its sum (:1204), AM4 ssh (:930-931)
-    for (int g = tid; g < nmem2; g += nth) {
-      const int m2 = (g / n2) * n2, p = g - m2;
-      T ssha_e = T(0);
-      const T sshn = a.ring_ssh[sn * nmem2 + g];
-      if (interior(p)) {
-        const T zhdiv = (fx[g] - fx[g - 1] + fy[g] - fy[g - jpi]) * d.r1_e1e2t[p];
-        ssha_e = (sshn - rdtbt * (a.zssh_frc[g] + zhdiv)) * d.ssmask[p];
+    for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
+      int m2, i0, j0;
+      tile(t, m2, i0, j0);
+      // Every value this tile reads that the sub-step does not produce is loaded
+      // first, so the loads of both stages are in flight together.
+      const int i = i0 + tx, j = j0 + ty;
+      const bool own = i <= jpi && j <= jpj;
+      const bool inner = own && interior(i, j);
+      const int p = own ? (i - 1) + (j - 1) * jpi : 0, g = m2 + p;
+      T x[4] = {}, y[4] = {}, xu[4] = {}, yv[4] = {};
+      T sn0 = T(0), sb0 = T(0), sbb0 = T(0), un_e = T(0), vn_e = T(0), ub_e = T(0), vb_e = T(0);
+      double acc_s = 0.0, acc_u = 0.0, acc_v = 0.0, acc_au = 0.0, acc_av = 0.0;
+      if (own) {
+        sn0 = a.ring_ssh[sn * nmem2 + g];
+        sb0 = a.ring_ssh[sb * nmem2 + g];
+        sbb0 = a.ring_ssh[sbb * nmem2 + g];
+        un_e = a.ring_u[sn * nmem2 + g];
+        vn_e = a.ring_v[sn * nmem2 + g];
+        ub_e = a.ring_u[sb * nmem2 + g];
+        vb_e = a.ring_v[sb * nmem2 + g];
+        acc_s = a.ssha[g]; acc_u = a.ua_b[g]; acc_v = a.va_b[g];
+        acc_au = a.un_adv[g]; acc_av = a.vn_adv[g];
+        if (inner) {
+          nbx([&](long q) { return fx[m2 + q]; }, (long)p, jpi, x);
+          nby([&](long q) { return fy[m2 + q]; }, (long)p, jpi, y);
+          if (a.nvor == 2) {  // the ENT scheme uses the extrapolated velocities
+            T za1, za2, za3;
+            ab3(jn, a.ll_init, za1, za2, za3);
+            auto uext = [&](long q) -> T {
+              return za1 * a.ring_u[sn * nmem2 + m2 + q] + za2 * a.ring_u[sb * nmem2 + m2 + q] +
+                     za3 * a.ring_u[sbb * nmem2 + m2 + q];
+            };
+            auto vext = [&](long q) -> T {
+              return za1 * a.ring_v[sn * nmem2 + m2 + q] + za2 * a.ring_v[sb * nmem2 + m2 + q] +
+                     za3 * a.ring_v[sbb * nmem2 + m2 + q];
+            };
+            nbx(uext, (long)p, jpi, xu);
+            nby(vext, (long)p, jpi, yv);
+          }
+        }
       }
-      a.ring_ssh[sa * nmem2 + g] = ssha_e;
-      a.ssha[g] = a.ssha[g] + w1 * (double)ssha_e;
-      a.zs[g] = zb0 * ssha_e + zb1 * sshn + zb2 * a.ring_ssh[sb * nmem2 + g] + zb3 * a.ring_ssh[sbb * nmem2 + g];
-    }
-    if (!grid_barrier(bar)) return;
-    // ---- stage B: Coriolis, drag, pressure gradient, ua_e/va_e, sums (:1000-1204)
-    for (int g = tid; g < nmem2; g += nth) {
-      const int m2 = (g / n2) * n2, p = g - m2;
-      T ua_e = T(0), va_e = T(0);
-      const T un_e = a.ring_u[sn * nmem2 + g], vn_e = a.ring_v[sn * nmem2 + g];
-      if (interior(p)) {
-        T za1, za2, za3;
-        ab3(jn, a.ll_init, za1, za2, za3);
-        auto fxq = [&](int q) -> T { return fx[m2 + q]; };
-        auto fyq = [&](int q) -> T { return fy[m2 + q]; };
-        // the ENT scheme needs the extrapolated velocities themselves
-        auto uext = [&](int q) -> T {
-          return za1 * a.ring_u[sn * nmem2 + m2 + q] + za2 * a.ring_u[sb * nmem2 + m2 + q] +
-                 za3 * a.ring_u[sbb * nmem2 + m2 + q];
-        };
-        auto vext = [&](int q) -> T {
-          return za1 * a.ring_v[sn * nmem2 + m2 + q] + za2 * a.ring_v[sb * nmem2 + m2 + q] +
-                 za3 * a.ring_v[sbb * nmem2 + m2 + q];
-        };
-        const T z1_hu = d.ssumask[p] / (d.hu_0[p] + T(1) - d.ssumask[p]);
-        const T z1_hv = d.ssvmask[p] / (d.hv_0[p] + T(1) - d.ssvmask[p]);
-        T zu_trd, zv_trd;
-        coriolis(d, a.nvor, (long)p, fxq, fyq, uext, vext, z1_hu, z1_hv, zu_trd, zv_trd);
-        zu_trd = zu_trd + a.zCdU_u[g] * un_e * d.r1_hu_0[p];
-        zv_trd = zv_trd + a.zCdU_v[g] * vn_e * d.r1_hv_0[p];
-        const T s0 = a.zs[g];
-        const T zu_spg = -grav * (a.zs[g + 1] - s0) * d.r1_e1u[p];
-        const T zv_spg = -grav * (a.zs[g + jpi] - s0) * d.r1_e2v[p];
-        const T wxs = (T(1) - a.scal_load) * zu_spg;
-        const T wys = (T(1) - a.scal_load) * zv_spg;
-        ua_e = (un_e + rdtbt * (wxs + zu_trd + a.zu_frc[g])) * d.ssumask[p];
-        va_e = (vn_e + rdtbt * (wys + zv_trd + a.zv_frc[g])) * d.ssvmask[p];
+      // the halo position of this thread, if any: the east column (9) and the
+      // north row (32) of the tile
+      int hti = -1, htj = -1;
+      if (threadIdx.x < P2_TY + 1) { hti = P2_TX; htj = threadIdx.x; }
+      else if (threadIdx.x < P2_TY + 1 + P2_TX) { hti = threadIdx.x - (P2_TY + 1); htj = P2_TY; }
+      const int hi_ = i0 + hti, hj_ = j0 + htj;
+      const bool halo = hti >= 0 && hi_ <= jpi && hj_ <= jpj;
+      const int hp = halo ? (hi_ - 1) + (hj_ - 1) * jpi : 0, hg = m2 + hp;
+      T h_fx0 = T(0), h_fxw = T(0), h_fy0 = T(0), h_fys = T(0), h_sn = T(0), h_sb = T(0), h_sbb = T(0);
+      if (halo) {
+        h_sn = a.ring_ssh[sn * nmem2 + hg];
+        h_sb = a.ring_ssh[sb * nmem2 + hg];
+        h_sbb = a.ring_ssh[sbb * nmem2 + hg];
+        if (interior(hi_, hj_)) {
+          h_fx0 = fx[hg]; h_fxw = fx[hg - 1]; h_fy0 = fy[hg]; h_fys = fy[hg - jpi];
+        }
       }
-      a.ring_u[sa * nmem2 + g] = ua_e;
-      a.ring_v[sa * nmem2 + g] = va_e;
-      a.ua_b[g] = a.ua_b[g] + w1 * (double)ua_e;
-      a.va_b[g] = a.va_b[g] + w1 * (double)va_e;
-      if (jn < a.icycle) predictor(jn + 1, (r + 3) & 3, g);
+      // ---- ssha_e (:871-879) and zsshp2_e (:930-931) of the owned point and the halo
+      // position; the owned point's new level and ssha sum (:1204)
+      if (own) {
+        T ssha_e = T(0);
+        if (inner) {
+          const T zhdiv = (x[1] - x[0] + y[2] - y[0]) * d.r1_e1e2t[p];
+          ssha_e = (sn0 - rdtbt * (zssh_frc[g] + zhdiv)) * d.ssmask[p];
+        }
+        zs_s[ty][tx] = zb0 * ssha_e + zb1 * sn0 + zb2 * sb0 + zb3 * sbb0;
+        a.ring_ssh[sa * nmem2 + g] = ssha_e;
+        a.ssha[g] = acc_s + w1 * (double)ssha_e;
+      }
+      if (halo) {
+        T ssha_e = T(0);
+        if (interior(hi_, hj_)) {
+          const T zhdiv = (h_fx0 - h_fxw + h_fy0 - h_fys) * d.r1_e1e2t[hp];
+          ssha_e = (h_sn - rdtbt * (zssh_frc[hg] + zhdiv)) * d.ssmask[hp];
+        }
+        zs_s[htj][hti] = zb0 * ssha_e + zb1 * h_sn + zb2 * h_sb + zb3 * h_sbb;
+      }
+      __syncthreads();
+      // ---- Coriolis, drag, pressure gradient, ua_e/va_e and their sums (:1000-1204),
+      // then the predictor of sub-step jn+1 (:724-800) and its sums (:860-862)
+      if (own) {
+        T ua_e = T(0), va_e = T(0);
+        if (inner) {
+          const T z1_hu = d.ssumask[p] / (d.hu_0[p] + T(1) - d.ssumask[p]);
+          const T z1_hv = d.ssvmask[p] / (d.hv_0[p] + T(1) - d.ssvmask[p]);
+          T zu_trd, zv_trd;
+          coriolis(d, a.nvor, (long)p, x, y, xu, yv, z1_hu, z1_hv, zu_trd, zv_trd);
+          zu_trd = zu_trd + zCdU_u[g] * un_e * d.r1_hu_0[p];
+          zv_trd = zv_trd + zCdU_v[g] * vn_e * d.r1_hv_0[p];
+          const T s0 = zs_s[ty][tx];
+          const T zu_spg = -grav * (zs_s[ty][tx + 1] - s0) * d.r1_e1u[p];
+          const T zv_spg = -grav * (zs_s[ty + 1][tx] - s0) * d.r1_e2v[p];
+          const T wxs = (T(1) - a.scal_load) * zu_spg;
+          const T wys = (T(1) - a.scal_load) * zv_spg;
+          ua_e = (un_e + rdtbt * (wxs + zu_trd + zu_frc[g])) * d.ssumask[p];
+          va_e = (vn_e + rdtbt * (wys + zv_trd + zv_frc[g])) * d.ssvmask[p];
+        }
+        a.ring_u[sa * nmem2 + g] = ua_e;
+        a.ring_v[sa * nmem2 + g] = va_e;
+        a.ua_b[g] = acc_u + w1 * (double)ua_e;
+        a.va_b[g] = acc_v + w1 * (double)va_e;
+        if (jn < a.icycle) {
+          // levels of sub-step jn+1: n = ua_e (new), b = un_e, bb = ub_e
+          T za1, za2, za3;
+          ab3(jn + 1, a.ll_init, za1, za2, za3);
+          const T uex = za1 * ua_e + za2 * un_e + za3 * ub_e;
+          const T vex = za1 * va_e + za2 * vn_e + za3 * vb_e;
+          const T zwx = d.e2u[p] * uex * d.hu_0[p];
+          const T zwy = d.e1v[p] * vex * d.hv_0[p];
+          a.fx[((jn + 1) & 1) * nmem2 + g] = zwx;
+          a.fy[((jn + 1) & 1) * nmem2 + g] = zwy;
+          const T w2 = (T)a.wgt2[jn];
+          a.un_adv[g] = acc_au + (double)(w2 * zwx * d.r1_e2u[p]);
+          a.vn_adv[g] = acc_av + (double)(w2 * zwy * d.r1_e1v[p]);
+        }
+      }
+      __syncthreads();  // zs_s is rewritten by the next tile
     }
     r = (r + 3) & 3;
     if (!grid_barrier(bar)) return;
   }
   // ---- phase 3, per column (:1214-1240, :1266-1269): time-filtered transports
   // and the two depth-independent terms each level adds
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nth = gridDim.x * blockDim.x;
   for (int g = tid; g < nmem2; g += nth) {
     const int m2 = (g / n2) * n2, p = g - m2;
     double uadv = a.un_adv[g], vadv = a.vn_adv[g];
@@ -368,10 +475,11 @@ __global__ void k_spg_p3(Dom<T> d, SpgArgs<T> a) {
   const long p = pt_ij(d, i, j), m2 = (long)m * d.n2;
   const long q = (long)m * d.n3 + p + (long)(k - 1) * d.n2;
   const ColInfo ci = d.ci[p];
-  a.ua[q] = a.ua[q] + a.du[m2 + p];
-  a.va[q] = a.va[q] + a.dv[m2 + p];
-  a.un[q] = (a.un[q] + a.cu[m2 + p] - a.un_b[m2 + p]) * umsk<T>(ci, k);
-  a.vn[q] = (a.vn[q] + a.cv[m2 + p] - a.vn_b[m2 + p]) * vmsk<T>(ci, k);
+  const RO<T> du = a.du, dv = a.dv, cu = a.cu, cv = a.cv;  // written by phase 2
+  a.ua[q] = a.ua[q] + du[m2 + p];
+  a.va[q] = a.va[q] + dv[m2 + p];
+  a.un[q] = (a.un[q] + cu[m2 + p] - a.un_b[m2 + p]) * umsk<T>(ci, k);
+  a.vn[q] = (a.vn[q] + cv[m2 + p] - a.vn_b[m2 + p]) * vmsk<T>(ci, k);
 }
 
 // ---------------------------------------------------------------------------------

@@ -63,6 +63,31 @@ __device__ __forceinline__ PtIdx pt_index(const Dom<T>& d) {
   return c;
 }
 
+// k-march kernels: grid x = i, y = j, z = member * nchunk + chunk. A thread walks
+// the levels k0..k1 of one column (KCH levels per chunk), keeping in registers what
+// level k+1 shares with level k, so the vertical neighbours are loaded once.
+constexpr int KCH = 8;
+struct KIdx {
+  int i, j, m, k0, k1;
+  long ij;
+  bool valid, interior;
+};
+template <class T>
+__device__ __forceinline__ KIdx k_index(const Dom<T>& d) {
+  const int nch = (d.jpk + KCH - 1) / KCH;
+  KIdx c;
+  c.i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  c.j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  c.m = (int)(blockIdx.z / (unsigned)nch);
+  const int ch = (int)blockIdx.z - c.m * nch;
+  c.k0 = ch * KCH + 1;
+  c.k1 = c.k0 + KCH - 1 < d.jpk ? c.k0 + KCH - 1 : d.jpk;
+  c.valid = c.i <= d.jpi && c.j <= d.jpj;
+  c.interior = c.i >= 2 && c.i <= d.jpi - 1 && c.j >= 2 && c.j <= d.jpj - 1;
+  c.ij = (long)(c.i - 1) + (long)(c.j - 1) * d.jpi;
+  return c;
+}
+
 // --------------------------------------------------------------------------------
 // traadv.F90:99-124: zun = e2u*e3u_n*un, zvn = e1v*e3v_n*vn, zwn = e1e2t*wn, 0 at jpk.
 template <class T>
@@ -85,16 +110,16 @@ __global__ void k_adv_trp(Dom<T> d, const T* __restrict__ un, const T* __restric
 // advection + iso-neutral trend of the hot path).
 template <class T>
 struct LdfArgs {
-  const T *pahu, *pahv;      // NULL: aht_c * umask/vmask above jpk (ldftra.F90:292-372)
+  RO<T> pahu, pahv;          // NULL: aht_c * umask/vmask above jpk (ldftra.F90:292-372)
   T aht_c;
-  const T *pgu, *pgv;        // partial-step gradients (jpi,jpj,kjpt) when zps
+  RO<T> pgu, pgv;            // partial-step gradients (jpi,jpj,kjpt) when zps
   int zps;
-  const T *ptb, *ptbb;
+  RO<T> ptb, ptbb;
   T* pta;
   int kjpt, kpass;
   T zsign;
   // iso-neutral
-  const T *uslp, *vslp, *wslpi, *wslpj;
+  RO<T> uslp, vslp, wslpi, wslpj;
   T *ah_wslp2, *akz;
   int lap, blp, msc;
   T z2dt, z1_2dt;
@@ -105,14 +130,14 @@ struct LdfArgs {
 template <class T>
 struct FctArgs {
   T p2dt;
-  const T *pun, *pvn, *pwn;  // transports, or velocities when trp != 0
+  RO<T> pun, pvn, pwn;       // transports, or velocities when trp != 0
   int trp;                   // 1: scale velocities to transports on the fly (traadv.F90:110-114)
-  const T *ptb, *ptn;        // (jpi,jpj,jpk,kjpt)
+  RO<T> ptb, ptn;            // (jpi,jpj,jpk,kjpt)
   const T* pta_in;           // NULL: the trend starts from tsa = 0 (step.F90:234)
   T* pta;                    // (jpi,jpj,jpk,kjpt)
   T *zwi, *ax, *ay, *az;     // work: monotone guess and antidiffusive fluxes (jpi,jpj,jpk,kjpt)
   T *betup, *betdo;          // work: limiter coefficients (jpi,jpj,jpk,kjpt)
-  const T* ztw;              // compact 4th-order tn at w-points (kn_fct_v = 4), or NULL
+  RO<T> ztw;                 // compact 4th-order tn at w-points (kn_fct_v = 4), or NULL
   int kjpt, kn_fct_h, kn_fct_v, linssh;
   int with_iso;              // stage c also adds the iso-neutral trend (kpass 1) of `iso`
   LdfArgs<T> iso;
@@ -143,139 +168,214 @@ __device__ __forceinline__ T ups(T u, T tl, T tr) {
 
 // FCT stage a: upstream trend into pta, monotone guess zwi, antidiffusive fluxes
 // (traadv_fct.F90:119-278) with the lbc_lnk of :280 folded in (edge values 0).
+// k-march: the upstream flux through the w-face between levels k and k+1 is
+// computed once (the bottom flux of k is the top flux of k+1), and tb, tn of
+// level k and the transport through that face are carried to level k+1.
 template <class T>
-__global__ void k_fct_a(Dom<T> d, FctArgs<T> a) {
-  const PtIdx c = pt_index(d);
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 3) k_fct_a(Dom<T> d, FctArgs<T> a) {
+  const KIdx c = k_index(d);
   if (!c.valid) return;
-  const int jpi = d.jpi, jpk = d.jpk, k = c.k;
-  const long n2 = d.n2, n3 = d.n3, q = c.q;
-  const long mv = (long)c.m * n3;
-  const T r1_6 = T(1) / T(6);
-  const bool work = c.interior && k <= jpk - 1;
-  ColInfo ci{}, ciw{}, cie{}, cis{}, cin{};
-  T ue = T(0), uw = T(0), vn_ = T(0), vs = T(0), wt = T(0), wb = T(0), r1_e1e2t = T(0);
-  T e3n = T(1), e3b = T(1), e3a = T(1);
-  if (work) {
-    ci = d.ci[c.ij]; ciw = d.ci[c.ij - 1]; cie = d.ci[c.ij + 1]; cis = d.ci[c.ij - jpi]; cin = d.ci[c.ij + jpi];
-    ue = trp_u(d, a, c.ij, mv + q, k, c.m);
-    uw = trp_u(d, a, c.ij - 1, mv + q - 1, k, c.m);
-    vn_ = trp_v(d, a, c.ij, mv + q, k, c.m);
-    vs = trp_v(d, a, c.ij - jpi, mv + q - jpi, k, c.m);
-    wt = trp_w(d, a, c.ij, mv + q);
-    if (k + 1 <= jpk - 1) wb = trp_w(d, a, c.ij, mv + q + n2);
-    r1_e1e2t = d.r1_e1e2t[c.ij];
-    e3n = d.e3t_n(c.ij, k, c.m); e3b = d.e3t_b(c.ij, k, c.m); e3a = d.e3t_a(c.ij, k, c.m);
+  const int jpi = d.jpi, jpk = d.jpk;
+  const long n2 = d.n2, n3 = d.n3, ij = c.ij;
+  if (!c.interior) {  // edge columns: every level 0 (pta: its input)
+    for (int k = c.k0; k <= c.k1; ++k) {
+      const long q = ij + (long)(k - 1) * n2;
+      for (int n = 0; n < a.kjpt; ++n) {
+        const long mo = ((long)c.m * a.kjpt + n) * n3;
+        a.zwi[mo + q] = T(0); a.ax[mo + q] = T(0); a.ay[mo + q] = T(0); a.az[mo + q] = T(0);
+        T* ta = a.pta + mo;
+        const T* tai = a.pta_in ? a.pta_in + mo : nullptr;
+        if (!tai) ta[q] = T(0);
+        else if (tai != ta) ta[q] = tai[q];
+      }
+    }
+    return;
   }
-  for (int n = 0; n < a.kjpt; ++n) {
-    const long mo = ((long)c.m * a.kjpt + n) * n3;
-    const T* tb = a.ptb + mo;
-    const T* tn = a.ptn + mo;
-    T* ta = a.pta + mo;
-    const T* tai = a.pta_in ? a.pta_in + mo : nullptr;
-    if (!work) {
-      a.zwi[mo + q] = T(0); a.ax[mo + q] = T(0); a.ay[mo + q] = T(0); a.az[mo + q] = T(0);
-      if (!tai) ta[q] = T(0);
-      else if (tai != ta) ta[q] = tai[q];
-      continue;
+  const long mv = (long)c.m * n3;
+  const ColInfo ci = d.ci[ij], ciw = d.ci[ij - 1], cie = d.ci[ij + 1], cis = d.ci[ij - jpi], cin = d.ci[ij + jpi];
+  const T r1_e1e2t = d.r1_e1e2t[ij];
+  const T r1_6 = T(1) / T(6);
+  constexpr int NT = 2;  // tracers per pass over the levels
+  for (int n0 = 0; n0 < a.kjpt; n0 += NT) {
+    const int nt = a.kjpt - n0 < NT ? a.kjpt - n0 : NT;
+    // carried from level k-1: tb(k-1), tn(k-1), the bottom upstream flux of k-1
+    T tbp[NT] = {}, tnp[NT] = {}, zwzb[NT] = {};
+    T wt = T(0);  // transport through the top face of level k
+    for (int k = c.k0; k <= c.k1; ++k) {
+      const long q = ij + (long)(k - 1) * n2;
+      if (k == jpk) {  // level jpk: no work, edge values
+        for (int nn = 0; nn < nt; ++nn) {
+          const long mo = ((long)c.m * a.kjpt + n0 + nn) * n3;
+          a.zwi[mo + q] = T(0); a.ax[mo + q] = T(0); a.ay[mo + q] = T(0); a.az[mo + q] = T(0);
+          T* ta = a.pta + mo;
+          const T* tai = a.pta_in ? a.pta_in + mo : nullptr;
+          if (!tai) ta[q] = T(0);
+          else if (tai != ta) ta[q] = tai[q];
+        }
+        continue;
+      }
+      const bool first = k == c.k0;
+      const T ue = trp_u(d, a, ij, mv + q, k, c.m);
+      const T uw = trp_u(d, a, ij - 1, mv + q - 1, k, c.m);
+      const T vn_ = trp_v(d, a, ij, mv + q, k, c.m);
+      const T vs = trp_v(d, a, ij - jpi, mv + q - jpi, k, c.m);
+      if (first) wt = trp_w(d, a, ij, mv + q);
+      const T wb = (k + 1 <= jpk - 1) ? trp_w(d, a, ij, mv + q + n2) : T(0);
+      const T e3n = d.e3t_n(ij, k, c.m), e3b = d.e3t_b(ij, k, c.m), e3a = d.e3t_a(ij, k, c.m);
+      const T tm = tmsk<T>(ci, k), wk = wmsk<T>(ci, k), wk1 = wmsk<T>(ci, k + 1);
+#pragma unroll
+      for (int nn = 0; nn < NT; ++nn) {
+        if (nn >= nt) break;
+        const long mo = ((long)c.m * a.kjpt + n0 + nn) * n3;
+        const RO<T> tb = a.ptb + mo;
+        const RO<T> tn = a.ptn + mo;
+        T* ta = a.pta + mo;
+        const T* tai = a.pta_in ? a.pta_in + mo : nullptr;
+        const T tb0 = tb[q];
+        if (first && k > 1) {  // the carried values of level k-1
+          tbp[nn] = tb[q - n2];
+          tnp[nn] = tn[q - n2];
+          zwzb[nn] = ups(wt, tb0, tbp[nn]) * wk;
+        }
+        const T zwx_e = ups(ue, tb0, tb[q + 1]), zwx_w = ups(uw, tb[q - 1], tb0);
+        const T zwy_n = ups(vn_, tb0, tb[q + jpi]), zwy_s = ups(vs, tb[q - jpi], tb0);
+        // upstream vertical fluxes at the top (k) and bottom (k+1) faces (:137-156)
+        const T zwz_t = (k == 1) ? (a.linssh ? wt * tb0 : T(0)) : zwzb[nn];
+        const T zwz_b = (k + 1 <= jpk - 1) ? ups(wb, tb[q + n2], tb0) * wk1 : T(0);
+        const T ztra = -(zwx_e - zwx_w + zwy_n - zwy_s + zwz_t - zwz_b) * r1_e1e2t;
+        const T tin = tai ? tai[q] : T(0);
+        ta[q] = tin + ztra / e3n * tm;
+        a.zwi[mo + q] = (e3b * tb0 + a.p2dt * ztra) / e3a * tm;
+        // horizontal antidiffusive fluxes (:180-251)
+        const T tn0 = tn[q], tne = tn[q + 1], tnn = tn[q + jpi];
+        T axv, ayv;
+        if (a.kn_fct_h == 2) {
+          axv = T(0.5) * ue * (tn0 + tne) - zwx_e;
+          ayv = T(0.5) * vn_ * (tn0 + tnn) - zwy_n;
+        } else {
+          const T tnw = tn[q - 1], tns = tn[q - jpi];
+          const T ztu_w = (tn0 - tnw) * umsk<T>(ciw, k);
+          const T ztu_0 = (tne - tn0) * umsk<T>(ci, k);
+          const T zltu0 = (ztu_0 + ztu_w) * r1_6;
+          T zltue = T(0);
+          if (c.i + 1 <= jpi - 1) zltue = ((tn[q + 2] - tne) * umsk<T>(cie, k) + ztu_0) * r1_6;
+          const T ztv_s = (tn0 - tns) * vmsk<T>(cis, k);
+          const T ztv_0 = (tnn - tn0) * vmsk<T>(ci, k);
+          const T zltv0 = (ztv_0 + ztv_s) * r1_6;
+          T zltvn = T(0);
+          if (c.j + 1 <= d.jpj - 1) zltvn = ((tn[q + 2 * jpi] - tnn) * vmsk<T>(cin, k) + ztv_0) * r1_6;
+          const T zC2t_u = tn0 + tne;
+          const T zC2t_v = tn0 + tnn;
+          axv = T(0.5) * ue * (zC2t_u + zltu0 - zltue) - zwx_e;
+          ayv = T(0.5) * vn_ * (zC2t_v + zltv0 - zltvn) - zwy_n;
+        }
+        a.ax[mo + q] = axv;
+        a.ay[mo + q] = ayv;
+        // vertical antidiffusive flux at the top face of level k (:253-278)
+        T azv = T(0);
+        if (k >= 2) {
+          if (a.kn_fct_v == 2) azv = (wt * T(0.5) * (tn0 + tnp[nn]) - zwz_t) * wk;
+          else azv = (wt * a.ztw[mo + q] - zwz_t) * wk;
+        }
+        a.az[mo + q] = azv;
+        tbp[nn] = tb0;
+        tnp[nn] = tn0;
+        zwzb[nn] = zwz_b;
+      }
+      wt = wb;
     }
-    const T tb0 = tb[q];
-    const T zwx_e = ups(ue, tb0, tb[q + 1]), zwx_w = ups(uw, tb[q - 1], tb0);
-    const T zwy_n = ups(vn_, tb0, tb[q + jpi]), zwy_s = ups(vs, tb[q - jpi], tb0);
-    // upstream vertical fluxes at the top (k) and bottom (k+1) faces (:137-156)
-    T zwz_t;
-    if (k == 1) zwz_t = a.linssh ? wt * tb0 : T(0);
-    else zwz_t = ups(wt, tb0, tb[q - n2]) * wmsk<T>(ci, k);
-    const T zwz_b = (k + 1 <= jpk - 1) ? ups(wb, tb[q + n2], tb0) * wmsk<T>(ci, k + 1) : T(0);
-    const T ztra = -(zwx_e - zwx_w + zwy_n - zwy_s + zwz_t - zwz_b) * r1_e1e2t;
-    const T tm = tmsk<T>(ci, k);
-    const T tin = tai ? tai[q] : T(0);
-    ta[q] = tin + ztra / e3n * tm;
-    a.zwi[mo + q] = (e3b * tb0 + a.p2dt * ztra) / e3a * tm;
-    // horizontal antidiffusive fluxes (:180-251)
-    const T tn0 = tn[q], tne = tn[q + 1], tnn = tn[q + jpi];
-    T axv, ayv;
-    if (a.kn_fct_h == 2) {
-      axv = T(0.5) * ue * (tn0 + tne) - zwx_e;
-      ayv = T(0.5) * vn_ * (tn0 + tnn) - zwy_n;
-    } else {
-      const T tnw = tn[q - 1], tns = tn[q - jpi];
-      const T ztu_w = (tn0 - tnw) * umsk<T>(ciw, k);
-      const T ztu_0 = (tne - tn0) * umsk<T>(ci, k);
-      const T zltu0 = (ztu_0 + ztu_w) * r1_6;
-      T zltue = T(0);
-      if (c.i + 1 <= jpi - 1) zltue = ((tn[q + 2] - tne) * umsk<T>(cie, k) + ztu_0) * r1_6;
-      const T ztv_s = (tn0 - tns) * vmsk<T>(cis, k);
-      const T ztv_0 = (tnn - tn0) * vmsk<T>(ci, k);
-      const T zltv0 = (ztv_0 + ztv_s) * r1_6;
-      T zltvn = T(0);
-      if (c.j + 1 <= d.jpj - 1) zltvn = ((tn[q + 2 * jpi] - tnn) * vmsk<T>(cin, k) + ztv_0) * r1_6;
-      const T zC2t_u = tn0 + tne;
-      const T zC2t_v = tn0 + tnn;
-      axv = T(0.5) * ue * (zC2t_u + zltu0 - zltue) - zwx_e;
-      ayv = T(0.5) * vn_ * (zC2t_v + zltv0 - zltvn) - zwy_n;
-    }
-    a.ax[mo + q] = axv;
-    a.ay[mo + q] = ayv;
-    // vertical antidiffusive flux at the top face of level k (:253-278)
-    T azv = T(0);
-    if (k >= 2) {
-      if (a.kn_fct_v == 2) azv = (wt * T(0.5) * (tn0 + tn[q - n2]) - zwz_t) * wmsk<T>(ci, k);
-      else azv = (wt * a.ztw[mo + q] - zwz_t) * wmsk<T>(ci, k);
-    }
-    a.az[mo + q] = azv;
   }
 }
 
 // zbup / zbdo of nonosc (traadv_fct.F90:361-364) at one point.
+// With tm = 1 the reference's pbef*tm - zbig*(1-tm) is pbef exactly, with tm = 0 it is
+// -zbig (pbef, paft finite), so the masked extrema reduce to a select.
 template <class T>
 __device__ __forceinline__ void bupdo(T pbef, T paft, T tm, T& up, T& dn) {
   const T zbig = Big<T>::v;
-  up = fmx(pbef * tm - zbig * (T(1) - tm), paft * tm - zbig * (T(1) - tm));
-  dn = fmn(pbef * tm + zbig * (T(1) - tm), paft * tm + zbig * (T(1) - tm));
+  up = tm != T(0) ? fmx(pbef, paft) : -zbig;
+  dn = tm != T(0) ? fmn(pbef, paft) : zbig;
 }
-
 // FCT stage b: nonosc extrema and limiter coefficients zbetup / zbetdo
-// (traadv_fct.F90:366-400), edge values 0 (lbc_lnk of :400).
+// (traadv_fct.F90:366-400), edge values 0 (lbc_lnk of :400). k-march: tb, zwi and
+// their masked extrema of levels k and k+1 and az(k+1) are carried down.
 template <class T>
-__global__ void k_fct_b(Dom<T> d, FctArgs<T> a) {
-  const PtIdx c = pt_index(d);
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 4) k_fct_b(Dom<T> d, FctArgs<T> a) {
+  const KIdx c = k_index(d);
   if (!c.valid) return;
-  const int jpi = d.jpi, jpk = d.jpk, k = c.k;
-  const long n2 = d.n2, n3 = d.n3, q = c.q;
-  const bool work = c.interior && k <= jpk - 1;
+  const int jpi = d.jpi, jpk = d.jpk;
+  const long n2 = d.n2, n3 = d.n3, ij = c.ij;
   const T zrtrn = T(1.e-15);
-  ColInfo ci{}, ciw{}, cie{}, cis{}, cin{};
-  T zbt = T(0);
-  if (work) {
-    ci = d.ci[c.ij]; ciw = d.ci[c.ij - 1]; cie = d.ci[c.ij + 1]; cis = d.ci[c.ij - jpi]; cin = d.ci[c.ij + jpi];
-    zbt = d.e1e2t[c.ij] * d.e3t_n(c.ij, k, c.m) / a.p2dt;
-  }
-  const int km1 = k - 1 > 1 ? k - 1 : 1;
-  const long qm = c.ij + (long)(km1 - 1) * n2, qp = q + n2;
-  for (int n = 0; n < a.kjpt; ++n) {
-    const long mo = ((long)c.m * a.kjpt + n) * n3;
-    if (!work) {
-      a.betup[mo + q] = T(0); a.betdo[mo + q] = T(0);
-      continue;
+  auto zero = [&](int k) {
+    const long q = ij + (long)(k - 1) * n2;
+    for (int n = 0; n < a.kjpt; ++n) {
+      const long mo = ((long)c.m * a.kjpt + n) * n3;
+      a.betup[mo + q] = T(0);
+      a.betdo[mo + q] = T(0);
     }
-    const T* tb = a.ptb + mo;
-    const T* zwi = a.zwi + mo;
-    const T* ax = a.ax + mo;
-    const T* ay = a.ay + mo;
-    const T* az = a.az + mo;
-    T up, dn, u2, d2;
-    bupdo(tb[q], zwi[q], tmsk<T>(ci, k), up, dn);
-    bupdo(tb[q - 1], zwi[q - 1], tmsk<T>(ciw, k), u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-    bupdo(tb[q + 1], zwi[q + 1], tmsk<T>(cie, k), u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-    bupdo(tb[q - jpi], zwi[q - jpi], tmsk<T>(cis, k), u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-    bupdo(tb[q + jpi], zwi[q + jpi], tmsk<T>(cin, k), u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-    bupdo(tb[qm], zwi[qm], tmsk<T>(ci, km1), u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-    bupdo(tb[qp], zwi[qp], tmsk<T>(ci, k + 1), u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-    const T axw = ax[q - 1], ax0 = ax[q], ays = ay[q - jpi], ay0 = ay[q], az0 = az[q], azb = az[qp];
-    const T zpos = fmx(T(0), axw) - fmn(T(0), ax0) + fmx(T(0), ays) - fmn(T(0), ay0) + fmx(T(0), azb) - fmn(T(0), az0);
-    const T zneg = fmx(T(0), ax0) - fmn(T(0), axw) + fmx(T(0), ay0) - fmn(T(0), ays) + fmx(T(0), az0) - fmn(T(0), azb);
-    a.betup[mo + q] = (up - zwi[q]) / (zpos + zrtrn) * zbt;
-    a.betdo[mo + q] = (zwi[q] - dn) / (zneg + zrtrn) * zbt;
+  };
+  if (!c.interior) {
+    for (int k = c.k0; k <= c.k1; ++k) zero(k);
+    return;
+  }
+  const ColInfo ci = d.ci[ij], ciw = d.ci[ij - 1], cie = d.ci[ij + 1], cis = d.ci[ij - jpi], cin = d.ci[ij + jpi];
+  const T e1e2t = d.e1e2t[ij];
+  constexpr int NT = 2;
+  for (int n0 = 0; n0 < a.kjpt; n0 += NT) {
+    const int nt = a.kjpt - n0 < NT ? a.kjpt - n0 : NT;
+    // carried: masked extrema (up, dn) of the column at level k-1 and k, az(k)
+    T upm[NT] = {}, dnm[NT] = {}, up0[NT] = {}, dn0[NT] = {}, azk[NT] = {}, zwik[NT] = {};
+    for (int k = c.k0; k <= c.k1; ++k) {
+      if (k == jpk) {
+        const long q = ij + (long)(k - 1) * n2;
+        for (int nn = 0; nn < nt; ++nn) {
+          const long mo = ((long)c.m * a.kjpt + n0 + nn) * n3;
+          a.betup[mo + q] = T(0);
+          a.betdo[mo + q] = T(0);
+        }
+        continue;
+      }
+      const bool first = k == c.k0;
+      const long q = ij + (long)(k - 1) * n2, qp = q + n2;
+      const T zbt = e1e2t * d.e3t_n(ij, k, c.m) / a.p2dt;
+#pragma unroll
+      for (int nn = 0; nn < NT; ++nn) {
+        if (nn >= nt) break;
+        const long mo = ((long)c.m * a.kjpt + n0 + nn) * n3;
+        const RO<T> tb = a.ptb + mo;
+        const RO<T> zwi = a.zwi + mo;
+        const RO<T> ax = a.ax + mo;
+        const RO<T> ay = a.ay + mo;
+        const RO<T> az = a.az + mo;
+        if (first) {  // extrema of the column at levels k and k-1, az(k)
+          zwik[nn] = zwi[q];
+          bupdo(tb[q], zwik[nn], tmsk<T>(ci, k), up0[nn], dn0[nn]);
+          if (k > 1) bupdo(tb[q - n2], zwi[q - n2], tmsk<T>(ci, k - 1), upm[nn], dnm[nn]);
+          else { upm[nn] = up0[nn]; dnm[nn] = dn0[nn]; }
+          azk[nn] = az[q];
+        }
+        T upp, dnp;  // level k+1 of the column
+        bupdo(tb[qp], zwi[qp], tmsk<T>(ci, k + 1), upp, dnp);
+        // the reference's order: centre, west, east, south, north, above, below
+        T up = up0[nn], dn = dn0[nn], u2, d2;
+        bupdo(tb[q - 1], zwi[q - 1], tmsk<T>(ciw, k), u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
+        bupdo(tb[q + 1], zwi[q + 1], tmsk<T>(cie, k), u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
+        bupdo(tb[q - jpi], zwi[q - jpi], tmsk<T>(cis, k), u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
+        bupdo(tb[q + jpi], zwi[q + jpi], tmsk<T>(cin, k), u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
+        up = fmx(up, upm[nn]); dn = fmn(dn, dnm[nn]);
+        up = fmx(up, upp); dn = fmn(dn, dnp);
+        const T axw = ax[q - 1], ax0 = ax[q], ays = ay[q - jpi], ay0 = ay[q], az0 = azk[nn], azb = az[qp];
+        const T zpos = fmx(T(0), axw) - fmn(T(0), ax0) + fmx(T(0), ays) - fmn(T(0), ay0) + fmx(T(0), azb) - fmn(T(0), az0);
+        const T zneg = fmx(T(0), ax0) - fmn(T(0), axw) + fmx(T(0), ay0) - fmn(T(0), ays) + fmx(T(0), az0) - fmn(T(0), azb);
+        const T zw = zwik[nn];
+        a.betup[mo + q] = (up - zw) / (zpos + zrtrn) * zbt;
+        a.betdo[mo + q] = (zw - dn) / (zneg + zrtrn) * zbt;
+        upm[nn] = up0[nn]; dnm[nn] = dn0[nn];
+        up0[nn] = upp; dn0[nn] = dnp;
+        azk[nn] = azb;
+        zwik[nn] = zwi[qp];
+      }
+    }
   }
 }
 
@@ -291,7 +391,7 @@ __device__ __forceinline__ T limit(T f, T bdo0, T bup1, T bup0, T bdo1) {
 // interp_4th_cpt (traadv_fct.F90:517-616): compact 4th-order tn at w-points for the
 // interior columns, levels 2..jpkm1, one tridiagonal solve per column.
 template <class T>
-__global__ void k_interp4(Dom<T> d, const T* __restrict__ ptn, T* __restrict__ ztw, int kjpt) {
+__global__ void k_interp4(Dom<T> d, RO<T> ptn, T* __restrict__ ztw, int kjpt) {
   ColIdx<T> c = col_index(d);
   if (!c.valid || !c.interior) return;
   const int jpk = d.jpk;
@@ -302,7 +402,7 @@ __global__ void k_interp4(Dom<T> d, const T* __restrict__ ptn, T* __restrict__ z
   T zwt[KMAX], zws[KMAX], out[KMAX];
   for (int n = 0; n < kjpt; ++n) {
     const long mo = ((long)c.m * kjpt + n) * n3;
-    const T* t = ptn + mo;
+    const RO<T> t = ptn + mo;
     auto coef = [&](int k, T& zwd, T& zwi, T& zwsk, T& zwrm) {
       const T tk = t[c.ij + (long)(k - 1) * n2], tkm = t[c.ij + (long)(k - 2) * n2];
       if (k == ikt || k == ikb) {
@@ -331,15 +431,19 @@ __global__ void k_interp4(Dom<T> d, const T* __restrict__ ptn, T* __restrict__ z
 
 
 // --------------------------------------------------------------------------------
-template <class T>
+// Eddy diffusivity at a u (v) point: the bound array, else aht_c * umask (vmask)
+// above level jpk. W: the caller guarantees k < jpk and a wet point.
+template <bool W = false, class T>
 __device__ __forceinline__ T ahu(const Dom<T>& d, const LdfArgs<T>& a, const ColInfo& c, long ij, int k, int m) {
   if (a.pahu) return a.pahu[(long)m * d.n3 + ij + (long)(k - 1) * d.n2];
-  return k < d.jpk ? a.aht_c * umsk<T>(c, k) : T(0);
+  if constexpr (W) return a.aht_c * T(1);
+  else return k < d.jpk ? a.aht_c * umsk<T>(c, k) : T(0);
 }
-template <class T>
+template <bool W = false, class T>
 __device__ __forceinline__ T ahv(const Dom<T>& d, const LdfArgs<T>& a, const ColInfo& c, long ij, int k, int m) {
   if (a.pahv) return a.pahv[(long)m * d.n3 + ij + (long)(k - 1) * d.n2];
-  return k < d.jpk ? a.aht_c * vmsk<T>(c, k) : T(0);
+  if constexpr (W) return a.aht_c * T(1);
+  else return k < d.jpk ? a.aht_c * vmsk<T>(c, k) : T(0);
 }
 
 // tra_ldf_lap (traldf_lap_blp.F90:95-145) at one interior point.
@@ -359,7 +463,7 @@ __global__ void k_ldf_lap(Dom<T> d, LdfArgs<T> a) {
   for (int n = 0; n < a.kjpt; ++n) {
     const long mo = ((long)c.m * a.kjpt + n) * n3;
     const long go = ((long)c.m * a.kjpt + n) * n2;
-    const T* tb = a.ptb + mo;
+    const RO<T> tb = a.ptb + mo;
     T* ta = a.pta + mo;
     const T tb0 = tb[q];
     T ztu0 = zu0 * (tb[q + 1] - tb0);
@@ -377,39 +481,59 @@ __global__ void k_ldf_lap(Dom<T> d, LdfArgs<T> a) {
 }
 
 // Masked horizontal gradient zdit / zdjt of tra_ldf_iso (traldf_iso.F90:218-241).
-template <class T>
-__device__ __forceinline__ T dit(const LdfArgs<T>& a, const ColInfo& c, const T* tb, long q, int k, long g) {
+template <bool W = false, class T>
+__device__ __forceinline__ T dit(const LdfArgs<T>& a, const ColInfo& c, const RO<T>& tb, long q, int k, long g) {
   if (a.zps && k == c.mbku) return a.pgu[g];
-  return (tb[q + 1] - tb[q]) * umsk<T>(c, k);
+  return (tb[q + 1] - tb[q]) * umk<W, T>(c, k);
 }
-template <class T>
-__device__ __forceinline__ T djt(const LdfArgs<T>& a, const ColInfo& c, const T* tb, long q, int k, long g, int jpi) {
+template <bool W = false, class T>
+__device__ __forceinline__ T djt(const LdfArgs<T>& a, const ColInfo& c, const RO<T>& tb, long q, int k, long g, int jpi) {
   if (a.zps && k == c.mbkv) return a.pgv[g];
-  return (tb[q + jpi] - tb[q]) * vmsk<T>(c, k);
+  return (tb[q + jpi] - tb[q]) * vmk<W, T>(c, k);
+}
+
+// w-point mask weights and averaged eddy diffusivities of an interior point, level
+// 2 <= k <= jpkm1 (traldf_iso.F90:150-157 and :297-304: the same expressions)
+template <class T>
+struct IsoW {
+  T zmsku, zmskv, zahu_w, zahv_w;
+};
+template <bool W = false, class T>
+__device__ __forceinline__ IsoW<T> iso_w(const Dom<T>& d, const LdfArgs<T>& a, long ij, int k, int m,
+                                         const ColInfo& ci, const ColInfo& ciw, const ColInfo& cis) {
+  const int jpi = d.jpi;
+  const T wm = wmk<W, T>(ci, k);
+  IsoW<T> w;
+  w.zmsku = wm * rcount(umk<W, T>(ci, k - 1) + umk<W, T>(ciw, k) + umk<W, T>(ciw, k - 1) + umk<W, T>(ci, k));
+  w.zmskv = wm * rcount(vmk<W, T>(ci, k - 1) + vmk<W, T>(cis, k) + vmk<W, T>(cis, k - 1) + vmk<W, T>(ci, k));
+  w.zahu_w = (ahu<W>(d, a, ci, ij, k - 1, m) + ahu<W>(d, a, ciw, ij - 1, k, m) + ahu<W>(d, a, ciw, ij - 1, k - 1, m) +
+              ahu<W>(d, a, ci, ij, k, m)) * w.zmsku;
+  w.zahv_w = (ahv<W>(d, a, ci, ij, k - 1, m) + ahv<W>(d, a, cis, ij - jpi, k, m) + ahv<W>(d, a, cis, ij - jpi, k - 1, m) +
+              ahv<W>(d, a, ci, ij, k, m)) * w.zmskv;
+  return w;
 }
 
 // ah_wslp2 (traldf_iso.F90:146-164) and akz (:166-202) at one interior point, level
-// 2 <= k <= jpkm1, first pass.
-template <class T>
-__device__ __forceinline__ void iso_coefs(const Dom<T>& d, const LdfArgs<T>& a, long ij, int k, int m,
-                                          const ColInfo& ci, const ColInfo& ciw, const ColInfo& cis, T& ahw, T& akz) {
-  const int jpi = d.jpi;
+// 2 <= k <= jpkm1: computed on the first pass, read back on the second.
+template <bool W = false, class T>
+__device__ __forceinline__ void iso_coefs_at(const Dom<T>& d, const LdfArgs<T>& a, long ij, int k, int m,
+                                             const ColInfo& ci, const ColInfo& ciw, const ColInfo& cis,
+                                             const IsoW<T>& w, T& ahw, T& akz) {
   const long q = (long)m * d.n3 + ij + (long)(k - 1) * d.n2;
-  const T wm = wmsk<T>(ci, k);
-  const T zmsku = wm / fmx(umsk<T>(ci, k - 1) + umsk<T>(ciw, k) + umsk<T>(ciw, k - 1) + umsk<T>(ci, k), T(1));
-  const T zmskv = wm / fmx(vmsk<T>(ci, k - 1) + vmsk<T>(cis, k) + vmsk<T>(cis, k - 1) + vmsk<T>(ci, k), T(1));
-  const T zahu_w = (ahu(d, a, ci, ij, k - 1, m) + ahu(d, a, ciw, ij - 1, k, m) + ahu(d, a, ciw, ij - 1, k - 1, m) +
-                    ahu(d, a, ci, ij, k, m)) * zmsku;
-  const T zahv_w = (ahv(d, a, ci, ij, k - 1, m) + ahv(d, a, cis, ij - jpi, k, m) + ahv(d, a, cis, ij - jpi, k - 1, m) +
-                    ahv(d, a, ci, ij, k, m)) * zmskv;
+  if (a.kpass != 1) {
+    ahw = a.ah_wslp2[q];
+    akz = a.akz[q];
+    return;
+  }
+  const int jpi = d.jpi;
   const T wi = a.wslpi[q], wj = a.wslpj[q];
-  ahw = zahu_w * wi * wi + zahv_w * wj * wj;
+  ahw = w.zahu_w * wi * wi + w.zahv_w * wj * wj;
   if (a.msc) {
     const T e1u0 = d.e1u[ij], e1uw = d.e1u[ij - 1], e2v0 = d.e2v[ij], e2vs = d.e2v[ij - jpi];
-    T akzv = T(0.25) * ((ahu(d, a, ci, ij, k, m) + ahu(d, a, ci, ij, k - 1, m)) / (e1u0 * e1u0) +
-                        (ahu(d, a, ciw, ij - 1, k, m) + ahu(d, a, ciw, ij - 1, k - 1, m)) / (e1uw * e1uw) +
-                        (ahv(d, a, ci, ij, k, m) + ahv(d, a, ci, ij, k - 1, m)) / (e2v0 * e2v0) +
-                        (ahv(d, a, cis, ij - jpi, k, m) + ahv(d, a, cis, ij - jpi, k - 1, m)) / (e2vs * e2vs));
+    T akzv = T(0.25) * ((ahu<W>(d, a, ci, ij, k, m) + ahu<W>(d, a, ci, ij, k - 1, m)) / (e1u0 * e1u0) +
+                        (ahu<W>(d, a, ciw, ij - 1, k, m) + ahu<W>(d, a, ciw, ij - 1, k - 1, m)) / (e1uw * e1uw) +
+                        (ahv<W>(d, a, ci, ij, k, m) + ahv<W>(d, a, ci, ij, k - 1, m)) / (e2v0 * e2v0) +
+                        (ahv<W>(d, a, cis, ij - jpi, k, m) + ahv<W>(d, a, cis, ij - jpi, k - 1, m)) / (e2vs * e2vs));
     const T e3w = d.e3w_n(ij, k, m);
     if (a.blp) {
       akzv = T(16) * ahw * (akzv + ahw / (e3w * e3w));
@@ -424,124 +548,142 @@ __device__ __forceinline__ void iso_coefs(const Dom<T>& d, const LdfArgs<T>& a, 
   }
 }
 
-// Iso-neutral coefficients of interior point (ij, k) for one call: computed on the
-// first pass (the point of level k writes them), read on the second.
+// Iso-neutral fluxes (traldf_iso.F90:146-357) of one column, k-march: on the first
+// pass the coefficients ah_wslp2 / akz (levels 2..jpkm1, interior); the horizontal
+// fluxes zftu / zftv of the east and north faces (i <= jpim1, j <= jpjm1,
+// k <= jpkm1, :255-276); the vertical flux ztfw of the top face of each level
+// (interior; 0 at levels 1 and jpk, :291-357). Each flux is computed once, by the
+// column that owns its face. Carried from level k to k+1: tb of the three columns
+// whose differences the fluxes take, the vertical gradients zdk1t(k) (= zdkt(k+1))
+// and the four horizontal gradients zdit / zdjt that the w-face flux averages.
 template <class T>
-__device__ __forceinline__ void iso_coefs_at(const Dom<T>& d, const LdfArgs<T>& a, long ij, int k, int m,
-                                             const ColInfo& ci, const ColInfo& ciw, const ColInfo& cis, T& ahw,
-                                             T& akz) {
-  if (a.kpass == 1) {
-    iso_coefs(d, a, ij, k, m, ci, ciw, cis, ahw, akz);
-  } else {
-    const long q = (long)m * d.n3 + ij + (long)(k - 1) * d.n2;
-    ahw = a.ah_wslp2[q];
-    akz = a.akz[q];
-  }
-}
-
-// Iso-neutral fluxes of one point (traldf_iso.F90:146-357): on the first pass the
-// coefficients ah_wslp2 / akz of the point (levels 2..jpkm1, interior); the
-// horizontal fluxes zftu / zftv of the east and north faces (i <= jpim1,
-// j <= jpjm1, k <= jpkm1, :255-276); the vertical flux ztfw of the top face
-// (interior, levels 2..jpkm1; 0 at levels 1 and jpk, :291-357). Each flux is
-// computed once, by the point that owns its face.
-template <class T>
-__global__ void k_iso_flux(Dom<T> d, LdfArgs<T> a) {
-  const PtIdx c = pt_index(d);
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 3) k_iso_flux(Dom<T> d, LdfArgs<T> a) {
+  const KIdx c = k_index(d);
   if (!c.valid) return;
-  const int jpi = d.jpi, jpj = d.jpj, jpk = d.jpk, k = c.k;
-  const long n2 = d.n2, n3 = d.n3;
-  const long ij = c.ij, ijw = ij - 1, ijs = ij - jpi;
+  const int jpi = d.jpi, jpj = d.jpj, jpk = d.jpk;
+  const long n2 = d.n2, n3 = d.n3, ij = c.ij, ijw = ij - 1, ijs = ij - jpi;
   const long m3 = (long)c.m * n3;
-  const bool hface = c.i <= jpi - 1 && c.j <= jpj - 1 && k <= jpk - 1;
-  const bool vface = c.interior && k >= 2 && k <= jpk - 1;
-  if (!hface && !(c.interior && (k == 1 || k == jpk))) return;
-  const ColInfo ci = d.ci[ij];
-  const ColInfo cie = d.ci[ij + (c.i <= jpi - 1 ? 1 : 0)];
-  const ColInfo cin = d.ci[ij + (c.j <= jpj - 1 ? jpi : 0)];
-  // tracer-independent coefficients, computed once (the flux stores below could
-  // alias the metric arrays, so nothing is reloaded between tracers)
-  T zabe1 = T(0), zcof1 = T(0), zabe2 = T(0), zcof2 = T(0);
-  T umk = T(0), vmk = T(0), wk = T(0), wk1 = T(0), wke = T(0), wk1e = T(0), wkn = T(0), wk1n = T(0);
-  if (hface) {
-    T pah = ahu(d, a, ci, ij, k, c.m);
-    zabe1 = pah * d.e2_e1u[ij] * d.e3u_n(ij, k, c.m);
-    const T zmsku = T(1) / fmx(wmsk<T>(cie, k) + wmsk<T>(ci, k + 1) + wmsk<T>(cie, k + 1) + wmsk<T>(ci, k), T(1));
-    zcof1 = -pah * d.e2u[ij] * a.uslp[m3 + c.q] * zmsku;
-    pah = ahv(d, a, ci, ij, k, c.m);
-    zabe2 = pah * d.e1_e2v[ij] * d.e3v_n(ij, k, c.m);
-    const T zmskv = T(1) / fmx(wmsk<T>(cin, k) + wmsk<T>(ci, k + 1) + wmsk<T>(cin, k + 1) + wmsk<T>(ci, k), T(1));
-    zcof2 = -pah * d.e1v[ij] * a.vslp[m3 + c.q] * zmskv;
-    umk = umsk<T>(ci, k); vmk = vmsk<T>(ci, k);
-    wk = wmsk<T>(ci, k); wk1 = wmsk<T>(ci, k + 1);
-    wke = wmsk<T>(cie, k); wk1e = wmsk<T>(cie, k + 1);
-    wkn = wmsk<T>(cin, k); wk1n = wmsk<T>(cin, k + 1);
-  }
-  T zcoef3 = T(0), zcoef4 = T(0), zvert = T(0), wm = T(0), ahw = T(0), akz = T(0);
+  if (!(c.i <= jpi - 1 && c.j <= jpj - 1)) return;  // no face owned (interior columns are inside)
+  const bool icol = c.interior;
+  const ColInfo ci = d.ci[ij], cie = d.ci[ij + 1], cin = d.ci[ij + jpi];
   ColInfo ciw{}, cis{};
-  if (vface) {
-    ciw = d.ci[ijw]; cis = d.ci[ijs];
-    iso_coefs_at(d, a, ij, k, c.m, ci, ciw, cis, ahw, akz);
-    if (a.kpass == 1) {
-      a.ah_wslp2[m3 + c.q] = ahw;
-      a.akz[m3 + c.q] = akz;
-    }
-    wm = wmsk<T>(ci, k);
-    const T zmsku = wm / fmx(umsk<T>(ci, k - 1) + umsk<T>(ciw, k) + umsk<T>(ciw, k - 1) + umsk<T>(ci, k), T(1));
-    const T zmskv = wm / fmx(vmsk<T>(ci, k - 1) + vmsk<T>(cis, k) + vmsk<T>(cis, k - 1) + vmsk<T>(ci, k), T(1));
-    const T zahu_w = (ahu(d, a, ci, ij, k - 1, c.m) + ahu(d, a, ciw, ijw, k, c.m) + ahu(d, a, ciw, ijw, k - 1, c.m) +
-                      ahu(d, a, ci, ij, k, c.m)) * zmsku;
-    const T zahv_w = (ahv(d, a, ci, ij, k - 1, c.m) + ahv(d, a, cis, ijs, k, c.m) + ahv(d, a, cis, ijs, k - 1, c.m) +
-                      ahv(d, a, ci, ij, k, c.m)) * zmskv;
-    zcoef3 = -zahu_w * d.e2t[ij] * zmsku * a.wslpi[m3 + c.q];
-    zcoef4 = -zahv_w * d.e1t[ij] * zmskv * a.wslpj[m3 + c.q];
-    // the laplacian diagonal term of :359-366 without its tracer difference
-    if (a.lap) zvert = d.e1e2t[ij] / d.e3w_n(ij, k, c.m) * wm * (ahw - akz);
+  if (icol) {
+    ciw = d.ci[ijw];
+    cis = d.ci[ijs];
   }
-  for (int n = 0; n < a.kjpt; ++n) {
-    const long mo = ((long)c.m * a.kjpt + n) * n3;
-    const long go = ((long)c.m * a.kjpt + n) * n2;
-    const T* tb = a.ptb + mo;
-    const T* tbb = a.ptbb + mo;
-    const long qq = c.q;
-    if (hface) {
-      // vertical gradients (:250-254): zdk1t(k) = (tb(k)-tb(k+1))*wmask(k+1),
-      // zdkt(k) = (tb(k-1)-tb(k))*wmask(k), zdkt(1) = zdk1t(1)
-      const T t0 = tb[qq], t1 = tb[qq + n2], te = tb[qq + 1], te1 = tb[qq + 1 + n2];
-      const T tn = tb[qq + jpi], tn1 = tb[qq + jpi + n2];
-      const T dk1_0 = (t0 - t1) * wk1, dk1_e = (te - te1) * wk1e, dk1_n = (tn - tn1) * wk1n;
-      T dk0_0, dk0_e, dk0_n;
-      if (k == 1) {
-        dk0_0 = dk1_0; dk0_e = dk1_e; dk0_n = dk1_n;
-      } else {
-        dk0_0 = (tb[qq - n2] - t0) * wk;
-        dk0_e = (tb[qq + 1 - n2] - te) * wke;
-        dk0_n = (tb[qq + jpi - n2] - tn) * wkn;
+  constexpr int NT = 2;
+  for (int n0 = 0; n0 < a.kjpt; n0 += NT) {
+    const int nt = a.kjpt - n0 < NT ? a.kjpt - n0 : NT;
+    // carried, per tracer: tb(k) at (i,j), (i+1,j), (i,j+1); zdk1t(k-1) there; zdit at
+    // (i,j) and (i-1,j) and zdjt at (i,j) and (i,j-1) of level k-1; tb(k-1) at (i,j)
+    T t0c[NT] = {}, tec[NT] = {}, tnc[NT] = {}, k10[NT] = {}, k1e[NT] = {}, k1n[NT] = {};
+    T di0[NT] = {}, diw[NT] = {}, dj0[NT] = {}, djs[NT] = {}, tup[NT] = {};
+    for (int k = c.k0; k <= c.k1; ++k) {
+      const long q = ij + (long)(k - 1) * n2;
+      if (k == jpk) {  // interior: ztfw = 0 at jpk
+        if (icol)
+          for (int nn = 0; nn < nt; ++nn) a.ztfw[((long)c.m * a.kjpt + n0 + nn) * n3 + q] = T(0);
+        continue;
       }
-      const T zdi = (a.zps && k == ci.mbku) ? a.pgu[go + ij] : (te - t0) * umk;
-      const T zdj = (a.zps && k == ci.mbkv) ? a.pgv[go + ij] : (tn - t0) * vmk;
-      a.zftu[mo + qq] = (zabe1 * zdi + zcof1 * (dk0_e + dk1_0 + dk1_e + dk0_0)) * umk;
-      a.zftv[mo + qq] = (zabe2 * zdj + zcof2 * (dk0_n + dk1_0 + dk1_n + dk0_0)) * vmk;
-    }
-    if (c.interior) {
-      T z = T(0);
+      const bool first = k == c.k0;
+      const bool vface = icol && k >= 2;
+      // tracer-independent coefficients of the faces of (i,j,k)
+      T pah = ahu(d, a, ci, ij, k, c.m);
+      const T zabe1 = pah * d.e2_e1u[ij] * d.e3u_n(ij, k, c.m);
+      const T zmsku_h = rcount(wmsk<T>(cie, k) + wmsk<T>(ci, k + 1) + wmsk<T>(cie, k + 1) + wmsk<T>(ci, k));
+      const T zcof1 = -pah * d.e2u[ij] * a.uslp[m3 + q] * zmsku_h;
+      pah = ahv(d, a, ci, ij, k, c.m);
+      const T zabe2 = pah * d.e1_e2v[ij] * d.e3v_n(ij, k, c.m);
+      const T zmskv_h = rcount(wmsk<T>(cin, k) + wmsk<T>(ci, k + 1) + wmsk<T>(cin, k + 1) + wmsk<T>(ci, k));
+      const T zcof2 = -pah * d.e1v[ij] * a.vslp[m3 + q] * zmskv_h;
+      const T um = umsk<T>(ci, k), vm = vmsk<T>(ci, k);
+      const T wk = wmsk<T>(ci, k), wk1 = wmsk<T>(ci, k + 1), wke = wmsk<T>(cie, k), wk1e = wmsk<T>(cie, k + 1);
+      const T wkn = wmsk<T>(cin, k), wk1n = wmsk<T>(cin, k + 1);
+      T zcoef3 = T(0), zcoef4 = T(0), zvert = T(0), ahw = T(0), akz = T(0);
       if (vface) {
-        const long qm = qq - n2;
-        const T sdi = dit(a, ci, tb, qm, k - 1, go + ij) + dit(a, ciw, tb, qq - 1, k, go + ijw) +
-                      dit(a, ciw, tb, qm - 1, k - 1, go + ijw) + dit(a, ci, tb, qq, k, go + ij);
-        const T sdj = djt(a, ci, tb, qm, k - 1, go + ij, jpi) + djt(a, cis, tb, qq - jpi, k, go + ijs, jpi) +
-                      djt(a, cis, tb, qm - jpi, k - 1, go + ijs, jpi) + djt(a, ci, tb, qq, k, go + ij, jpi);
-        z = zcoef3 * sdi + zcoef4 * sdj;
-        if (a.lap) {
-          z = z + zvert * (tb[qm] - tb[qq]);
-        } else {
-          const T e1e2t = d.e1e2t[ij];
-          const T e3w = d.e3w_n(ij, k, c.m);
-          if (a.kpass == 1) z = z + ahw * e1e2t * (tb[qm] - tb[qq]) / e3w * wm;
-          else z = z + e1e2t / e3w * wm * (ahw * (tb[qm] - tb[qq]) + akz * (tbb[qm] - tbb[qq]));
+        const IsoW<T> w = iso_w(d, a, ij, k, c.m, ci, ciw, cis);
+        iso_coefs_at(d, a, ij, k, c.m, ci, ciw, cis, w, ahw, akz);
+        if (a.kpass == 1) {
+          a.ah_wslp2[m3 + q] = ahw;
+          a.akz[m3 + q] = akz;
         }
+        zcoef3 = -w.zahu_w * d.e2t[ij] * w.zmsku * a.wslpi[m3 + q];
+        zcoef4 = -w.zahv_w * d.e1t[ij] * w.zmskv * a.wslpj[m3 + q];
+        // the laplacian diagonal term of :359-366 without its tracer difference
+        if (a.lap) zvert = d.e1e2t[ij] / d.e3w_n(ij, k, c.m) * wk * (ahw - akz);
       }
-      a.ztfw[mo + qq] = z;
+#pragma unroll
+      for (int nn = 0; nn < NT; ++nn) {
+        if (nn >= nt) break;
+        const int n = n0 + nn;
+        const long mo = ((long)c.m * a.kjpt + n) * n3;
+        const long go = ((long)c.m * a.kjpt + n) * n2;
+        const RO<T> tb = a.ptb + mo;
+        // masked horizontal gradients zdit / zdjt (:218-241) at column offset o, level kk
+        auto zdit = [&](const ColInfo& cc, long o, int kk, T tl, T tr) -> T {
+          if (a.zps && kk == cc.mbku) return a.pgu[go + ij + o];
+          return (tr - tl) * umsk<T>(cc, kk);
+        };
+        auto zdjt = [&](const ColInfo& cc, long o, int kk, T tl, T tr) -> T {
+          if (a.zps && kk == cc.mbkv) return a.pgv[go + ij + o];
+          return (tr - tl) * vmsk<T>(cc, kk);
+        };
+        if (first) {
+          t0c[nn] = tb[q]; tec[nn] = tb[q + 1]; tnc[nn] = tb[q + jpi];
+          if (k > 1) {
+            const long qm = q - n2;
+            const T u0 = tb[qm], ue = tb[qm + 1], un = tb[qm + jpi];
+            k10[nn] = (u0 - t0c[nn]) * wk;
+            k1e[nn] = (ue - tec[nn]) * wke;
+            k1n[nn] = (un - tnc[nn]) * wkn;
+            tup[nn] = u0;
+            if (icol) {
+              const T uw = tb[qm - 1], us = tb[qm - jpi];
+              di0[nn] = zdit(ci, 0, k - 1, u0, ue);
+              diw[nn] = zdit(ciw, -1, k - 1, uw, u0);
+              dj0[nn] = zdjt(ci, 0, k - 1, u0, un);
+              djs[nn] = zdjt(cis, -jpi, k - 1, us, u0);
+            }
+          }
+        }
+        const T t0 = t0c[nn], te = tec[nn], tn = tnc[nn];
+        const T t1 = tb[q + n2], te1 = tb[q + 1 + n2], tn1 = tb[q + jpi + n2];
+        // vertical gradients (:250-254): zdk1t(k) = (tb(k)-tb(k+1))*wmask(k+1),
+        // zdkt(k) = zdk1t(k-1), zdkt(1) = zdk1t(1)
+        const T dk1_0 = (t0 - t1) * wk1, dk1_e = (te - te1) * wk1e, dk1_n = (tn - tn1) * wk1n;
+        const T dk0_0 = k == 1 ? dk1_0 : k10[nn];
+        const T dk0_e = k == 1 ? dk1_e : k1e[nn];
+        const T dk0_n = k == 1 ? dk1_n : k1n[nn];
+        const T zdi = zdit(ci, 0, k, t0, te);
+        const T zdj = zdjt(ci, 0, k, t0, tn);
+        a.zftu[mo + q] = (zabe1 * zdi + zcof1 * (dk0_e + dk1_0 + dk1_e + dk0_0)) * um;
+        a.zftv[mo + q] = (zabe2 * zdj + zcof2 * (dk0_n + dk1_0 + dk1_n + dk0_0)) * vm;
+        if (icol) {
+          const T tw = tb[q - 1], ts = tb[q - jpi];
+          const T zdiw = zdit(ciw, -1, k, tw, t0);
+          const T zdjs = zdjt(cis, -jpi, k, ts, t0);
+          T z = T(0);
+          if (vface) {
+            const T sdi = di0[nn] + zdiw + diw[nn] + zdi;
+            const T sdj = dj0[nn] + zdjs + djs[nn] + zdj;
+            z = zcoef3 * sdi + zcoef4 * sdj;
+            if (a.lap) {
+              z = z + zvert * (tup[nn] - t0);
+            } else {
+              const RO<T> tbb = a.ptbb + mo;
+              const T e1e2t = d.e1e2t[ij];
+              const T e3w = d.e3w_n(ij, k, c.m);
+              if (a.kpass == 1) z = z + ahw * e1e2t * (tup[nn] - t0) / e3w * wk;
+              else z = z + e1e2t / e3w * wk * (ahw * (tup[nn] - t0) + akz * (tbb[q - n2] - tbb[q]));
+            }
+          }
+          a.ztfw[mo + q] = z;
+          di0[nn] = zdi; diw[nn] = zdiw; dj0[nn] = zdj; djs[nn] = zdjs;
+        }
+        k10[nn] = dk1_0; k1e[nn] = dk1_e; k1n[nn] = dk1_n;
+        tup[nn] = t0;
+        t0c[nn] = t1; tec[nn] = te1; tnc[nn] = tn1;
+      }
     }
   }
 }
@@ -552,9 +694,9 @@ template <class T>
 __device__ __forceinline__ T iso_div(const Dom<T>& d, const LdfArgs<T>& a, const PtIdx& c, int n, T tav) {
   const long mo = ((long)c.m * a.kjpt + n) * d.n3, q = c.q;
   const T r1 = d.r1_e1e2t[c.ij], e3tn = d.e3t_n(c.ij, c.k, c.m);
-  const T* fu = a.zftu + mo;
-  const T* fv = a.zftv + mo;
-  const T* fw = a.ztfw + mo;
+  const RO<T> fu = a.zftu + mo;
+  const RO<T> fv = a.zftv + mo;
+  const RO<T> fw = a.ztfw + mo;
   tav = tav + a.zsign * (fu[q] - fu[q - 1] + fv[q] - fv[q - d.jpi]) * r1 / e3tn;
   tav = tav + a.zsign * (fw[q] - fw[q + d.n2]) * r1 / e3tn;
   return tav;
@@ -573,37 +715,74 @@ __global__ void k_iso_div(Dom<T> d, LdfArgs<T> a) {
 
 // FCT stage c: limit the fluxes (traadv_fct.F90:404-426) and add the divergence of
 // the corrected fluxes to pta (:288-297); with_iso also adds the iso-neutral trend
-// divergence of the same point from fluxes k_iso_flux computed (the tra_ldf call
-// that follows tra_adv in step.F90:248-252).
+// divergence of the same point from the fluxes k_iso_flux computed (the tra_ldf
+// call that follows tra_adv in step.F90:248-252). k-march: the limited flux through
+// the w-face between k and k+1, the coefficients of level k+1 and the iso-neutral
+// vertical flux of that face are carried down.
 template <class T>
-__global__ void k_fct_c(Dom<T> d, FctArgs<T> a) {
-  const PtIdx c = pt_index(d);
-  if (!c.valid || !c.interior || c.k > d.jpk - 1) return;
-  const int jpi = d.jpi, k = c.k;
-  const long n2 = d.n2, n3 = d.n3, q = c.q;
-  const T r1_e1e2t = d.r1_e1e2t[c.ij];
-  const T e3n = d.e3t_n(c.ij, k, c.m);
+__global__ void __launch_bounds__(128) k_fct_c(Dom<T> d, FctArgs<T> a) {
+  const KIdx c = k_index(d);
+  if (!c.valid || !c.interior) return;
+  const int jpi = d.jpi, jpk = d.jpk;
+  const long n2 = d.n2, n3 = d.n3, ij = c.ij;
+  const T r1_e1e2t = d.r1_e1e2t[ij];
   const bool w_lim = c.i - 1 >= 2;  // the face i-1 is limited only for i-1 >= 2 (then lbc: 0)
   const bool s_lim = c.j - 1 >= 2;
-  for (int n = 0; n < a.kjpt; ++n) {
-    const long mo = ((long)c.m * a.kjpt + n) * n3;
-    const T* ax = a.ax + mo;
-    const T* ay = a.ay + mo;
-    const T* az = a.az + mo;
-    const T* bu = a.betup + mo;
-    const T* bd = a.betdo + mo;
-    T* ta = a.pta + mo;
-    const T bu0 = bu[q], bd0 = bd[q];
-    const T axl = limit(ax[q], bd0, bu[q + 1], bu0, bd[q + 1]);
-    const T axlw = w_lim ? limit(ax[q - 1], bd[q - 1], bu0, bu[q - 1], bd0) : T(0);
-    const T ayl = limit(ay[q], bd0, bu[q + jpi], bu0, bd[q + jpi]);
-    const T ayls = s_lim ? limit(ay[q - jpi], bd[q - jpi], bu0, bu[q - jpi], bd0) : T(0);
-    // pcc(k) (not limited at k = 1) and pcc(k+1)
-    const T azl_t = k >= 2 ? limit(az[q], bd0, bu[q - n2], bu0, bd[q - n2]) : az[q];
-    const T azl_b = limit(az[q + n2], bd[q + n2], bu0, bu[q + n2], bd0);
-    T tav = ta[q] - (axl - axlw + ayl - ayls + azl_t - azl_b) * r1_e1e2t / e3n;
-    if (a.with_iso) tav = iso_div(d, a.iso, c, n, tav);
-    ta[q] = tav;
+  const int k1 = c.k1 < jpk - 1 ? c.k1 : jpk - 1;
+  constexpr int NT = 2;
+  for (int n0 = 0; n0 < a.kjpt; n0 += NT) {
+    const int nt = a.kjpt - n0 < NT ? a.kjpt - n0 : NT;
+    // carried: limiter coefficients of the column at level k, the limited flux
+    // through the top face of level k, the iso-neutral vertical flux of that face
+    T bu0[NT] = {}, bd0[NT] = {}, azt[NT] = {}, fwt[NT] = {};
+    for (int k = c.k0; k <= k1; ++k) {
+      const bool first = k == c.k0;
+      const long q = ij + (long)(k - 1) * n2, qp = q + n2;
+      const T e3n = d.e3t_n(ij, k, c.m);
+#pragma unroll
+      for (int nn = 0; nn < NT; ++nn) {
+        if (nn >= nt) break;
+        const int n = n0 + nn;
+        const long mo = ((long)c.m * a.kjpt + n) * n3;
+        const RO<T> ax = a.ax + mo;
+        const RO<T> ay = a.ay + mo;
+        const RO<T> az = a.az + mo;
+        const RO<T> bu = a.betup + mo;
+        const RO<T> bd = a.betdo + mo;
+        T* ta = a.pta + mo;
+        if (first) {
+          bu0[nn] = bu[q];
+          bd0[nn] = bd[q];
+          // pcc(k), not limited at k = 1
+          azt[nn] = k >= 2 ? limit(az[q], bd0[nn], bu[q - n2], bu0[nn], bd[q - n2]) : az[q];
+          if (a.with_iso) fwt[nn] = RO<T>(a.iso.ztfw + mo)[q];
+        }
+        const T b_u = bu0[nn], b_d = bd0[nn];
+        const T bup = bu[qp], bdp = bd[qp];
+        const T axl = limit(ax[q], b_d, bu[q + 1], b_u, bd[q + 1]);
+        const T axlw = w_lim ? limit(ax[q - 1], bd[q - 1], b_u, bu[q - 1], b_d) : T(0);
+        const T ayl = limit(ay[q], b_d, bu[q + jpi], b_u, bd[q + jpi]);
+        const T ayls = s_lim ? limit(ay[q - jpi], bd[q - jpi], b_u, bu[q - jpi], b_d) : T(0);
+        // pcc(k+1): the limited flux through the bottom face
+        const T azl_b = limit(az[qp], bdp, b_u, bup, b_d);
+        T tav = ta[q] - (axl - axlw + ayl - ayls + azt[nn] - azl_b) * r1_e1e2t / e3n;
+        if (a.with_iso) {
+          // iso-neutral divergence: horizontal (traldf_iso.F90:278-284), then
+          // vertical (:359-366)
+          const RO<T> fu = a.iso.zftu + mo;
+          const RO<T> fv = a.iso.zftv + mo;
+          const RO<T> fw = a.iso.ztfw + mo;
+          const T fwb = fw[qp];
+          tav = tav + a.iso.zsign * (fu[q] - fu[q - 1] + fv[q] - fv[q - jpi]) * r1_e1e2t / e3n;
+          tav = tav + a.iso.zsign * (fwt[nn] - fwb) * r1_e1e2t / e3n;
+          fwt[nn] = fwb;
+        }
+        ta[q] = tav;
+        bu0[nn] = bup;
+        bd0[nn] = bdp;
+        azt[nn] = azl_b;
+      }
+    }
   }
 }
 
@@ -650,10 +829,10 @@ __global__ void k_iso_akz_copy_edges(Dom<T> d, LdfArgs<T> a) {
 template <class T>
 struct ZdfArgs {
   T p2dt;
-  const T* ptb;
+  RO<T> ptb;
   T* pta;
   int kjpt;
-  const T *avt, *avs, *add;  // add: ah_wslp2 (standard iso), akz (msc) or NULL
+  RO<T> avt, avs, add;       // add: ah_wslp2 (standard iso), akz (msc) or NULL
   int ddm, is_trc, clamp_sal;
 };
 
@@ -672,7 +851,7 @@ __global__ void k_zdf_imp(Dom<T> d, ZdfArgs<T> a) {
   for (int n = 0; n < a.kjpt; ++n) {
     const bool build = (!a.is_trc && (n == 0 || (n == 1 && a.ddm))) || (a.is_trc && n == 0);
     if (build) {
-      const T* coef = (!a.is_trc && n == 0) ? a.avt : a.avs;
+      const RO<T> coef = (!a.is_trc && n == 0) ? a.avt : a.avs;
       // zwt(k) = avt(k) (+ iso-neutral coefficient), zwt(1) = 0 (:153-176)
       auto wt = [&](int k) -> T {
         if (k == 1) return T(0);
@@ -706,7 +885,7 @@ __global__ void k_zdf_imp(Dom<T> d, ZdfArgs<T> a) {
       }
     }
     const long mo = ((long)c.m * a.kjpt + n) * n3;
-    const T* tb = a.ptb + mo;
+    const RO<T> tb = a.ptb + mo;
     T* ta = a.pta + mo;
     const bool clamp = a.clamp_sal && !a.is_trc && n == 1;
     // 2nd recurrence (:238-250), the forward values kept in pta as in the reference
@@ -751,7 +930,7 @@ __global__ void __launch_bounds__(128) k_zdf_imp_reg(Dom<float> d, ZdfArgs<float
   for (int n = 0; n < a.kjpt; ++n) {
     const bool build = (!a.is_trc && (n == 0 || (n == 1 && a.ddm))) || (a.is_trc && n == 0);
     if (build) {
-      const float* coef = (!a.is_trc && n == 0) ? a.avt : a.avs;
+      const RO<float> coef = (!a.is_trc && n == 0) ? a.avt : a.avs;
       float wt[NK + 1];
 #pragma unroll
       for (int k = 2; k <= NK; ++k) {
@@ -771,7 +950,7 @@ __global__ void __launch_bounds__(128) k_zdf_imp_reg(Dom<float> d, ZdfArgs<float
       }
     }
     const long mo = ((long)c.m * a.kjpt + n) * n3 + c.ij;
-    const float* tb = a.ptb + mo;
+    const RO<float> tb = a.ptb + mo;
     float* ta = a.pta + mo;
     const bool clamp = a.clamp_sal && !a.is_trc && n == 1;
     float x[NK];

@@ -11,6 +11,7 @@
 // T range (dommsk.F90:189-194).
 #pragma once
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 namespace nemo {
@@ -19,12 +20,36 @@ struct __align__(8) ColInfo {
   uint8_t tlo, thi, ulo, uhi, vlo, vhi, mbku, mbkv;
 };
 
+// Loads through the read-only data path (ld.global.nc). The compiler may move them
+// ahead of the kernel's stores, so they are used only for arrays that no thread
+// writes while the kernel runs.
+template <class T>
+__device__ __forceinline__ T ldro(const T* p) { return __ldg(p); }
+template <>
+__device__ __forceinline__ ColInfo ldro<ColInfo>(const ColInfo* p) {
+  const unsigned long long v = __ldg(reinterpret_cast<const unsigned long long*>(p));
+  ColInfo c;
+  memcpy(&c, &v, sizeof(c));
+  return c;
+}
+
+// A device array read only through ldro.
+template <class T>
+struct RO {
+  const T* p;
+  __host__ __device__ RO(const T* q = nullptr) : p(q) {}
+  __device__ __forceinline__ T operator[](long i) const { return ldro(p + i); }
+  __host__ __device__ RO operator+(long o) const { return RO(p + o); }
+  __host__ __device__ RO operator-(long o) const { return RO(p - o); }
+  __host__ __device__ explicit operator bool() const { return p != nullptr; }
+};
+
 // A scale-factor field e3(i,j,k[,member]) = p[m*sm + (k-1)*sk + ij*s]. A horizontally
 // uniform field (z-coordinate with full steps) is stored as a 1-D profile with
 // s = 0, sk = 1, so no 3-D metric traffic is spent on it.
 template <class T>
 struct E3 {
-  const T* p;
+  RO<T> p;
   long sk;
   long sm;
   int s;
@@ -37,15 +62,15 @@ template <class T>
 struct Dom {
   int jpi, jpj, jpk, nmem;
   long n2, n3;  // points per member of a 2-D / 3-D field
-  const T *e1t, *e2t, *e1u, *e2u, *e1v, *e2v;
-  const T *r1_e1u, *r1_e2u, *r1_e1v, *r1_e2v;
-  const T *e1e2t, *r1_e1e2t, *e2_e1u, *e1_e2v, *r1_e1e2u, *r1_e1e2v;
-  const T *ht_0, *hu_0, *hv_0, *r1_hu_0, *r1_hv_0;
-  const T *ssmask, *ssumask, *ssvmask;
-  const T *ff_t, *zwz, *ftne, *ftnw, *ftse, *ftsw;
-  const double* tmask_i;
-  const ColInfo* ci;
-  const uint8_t* mbkt;
+  RO<T> e1t, e2t, e1u, e2u, e1v, e2v;
+  RO<T> r1_e1u, r1_e2u, r1_e1v, r1_e2v;
+  RO<T> e1e2t, r1_e1e2t, e2_e1u, e1_e2v, r1_e1e2u, r1_e1e2v;
+  RO<T> ht_0, hu_0, hv_0, r1_hu_0, r1_hv_0;
+  RO<T> ssmask, ssumask, ssvmask;
+  RO<T> ff_t, zwz, ftne, ftnw, ftse, ftsw;
+  RO<double> tmask_i;
+  RO<ColInfo> ci;
+  RO<uint8_t> mbkt;
   E3<T> e3t_b, e3t_n, e3t_a, e3u_n, e3v_n, e3w_n;
 };
 
@@ -66,10 +91,45 @@ __device__ __forceinline__ T wmsk(const ColInfo& c, int k) {
 // SIGN(a,b) with key_nosignedzero (lib_fortran.F90:339-351): b >= 0 gives |a|.
 template <class T>
 __device__ __forceinline__ T sign_nsz(T a, T b) { return b >= T(0) ? fabs(a) : -fabs(a); }
+// Mask lookups of a kernel body compiled twice: W = true where the caller has
+// checked that every mask the body reads is 1 (the wet interior, most points), so
+// every multiplication by a mask folds away (x * 1 is exact); W = false reads the
+// column's level ranges.
+template <bool W, class T>
+__device__ __forceinline__ T tmk(const ColInfo& c, int k) {
+  if constexpr (W) return T(1); else return tmsk<T>(c, k);
+}
+template <bool W, class T>
+__device__ __forceinline__ T umk(const ColInfo& c, int k) {
+  if constexpr (W) return T(1); else return umsk<T>(c, k);
+}
+template <bool W, class T>
+__device__ __forceinline__ T vmk(const ColInfo& c, int k) {
+  if constexpr (W) return T(1); else return vmsk<T>(c, k);
+}
+template <bool W, class T>
+__device__ __forceinline__ T wmk(const ColInfo& c, int k) {
+  if constexpr (W) return T(1); else return wmsk<T>(c, k);
+}
+// the T (U, V) range of column c covers levels lo..hi
+__device__ __forceinline__ bool t_wet(const ColInfo& c, int lo, int hi) { return c.tlo <= lo && hi <= c.thi; }
+__device__ __forceinline__ bool u_wet(const ColInfo& c, int lo, int hi) { return c.ulo <= lo && hi <= c.uhi; }
+__device__ __forceinline__ bool v_wet(const ColInfo& c, int lo, int hi) { return c.vlo <= lo && hi <= c.vhi; }
+
 template <class T>
 __device__ __forceinline__ T fmx(T a, T b) { return a > b ? a : b; }
 template <class T>
 __device__ __forceinline__ T fmn(T a, T b) { return a < b ? a : b; }
+
+// 1 / MAX(n, 1) for a sum n of four 0/1 masks (n = 0..4), as the correctly rounded
+// quotient the division gives, without dividing: 1, 1, 1/2, 1/3, 1/4.
+template <class T> struct Third;
+template <> struct Third<double> { static constexpr double v = 0x1.5555555555555p-2; };
+template <> struct Third<float> { static constexpr float v = 0x1.555556p-2f; };
+template <class T>
+__device__ __forceinline__ T rcount(T n) {
+  return n <= T(1) ? T(1) : (n == T(2) ? T(0.5) : (n == T(3) ? Third<T>::v : T(0.25)));
+}
 
 // Land sentinel of nonosc (traadv_fct.F90:354). 1e40 overflows FP32; 1e30 keeps the
 // same role (far beyond any tracer value) without overflow.
@@ -78,10 +138,13 @@ template <> struct Big<double> { static constexpr double v = 1.e+40; };
 template <> struct Big<float> { static constexpr float v = 1.e+30f; };
 
 // Grid barrier for persistent kernels launched cooperatively (all blocks resident).
-// Each wait is bounded: after max_spins polls the block records NEMO_ERR_TIMEOUT in
-// *err and returns false; every block checks the flag after each barrier and leaves
-// its loop, so the kernel always ends. gen is read before arriving (sense reversal
-// by generation counter); the last block to arrive resets the count and bumps gen.
+// Thread 0 of each block reads the generation (acquire), arrives on the counter
+// with an acquire-release atomic, and the last block to arrive resets the counter
+// and publishes the next generation with a release store; the others poll the
+// generation with acquire loads, which makes every write before the barrier
+// visible after it. Each wait is bounded: after max_spins polls the block records
+// NEMO_ERR_TIMEOUT in *err and returns false; every block checks the flag after
+// each barrier and leaves its loop, so the kernel always ends.
 struct GridBar {
   unsigned int* count;
   unsigned int* gen;
@@ -90,33 +153,44 @@ struct GridBar {
   long long max_spins;
 };
 
+__device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned int atom_add_acq_rel_gpu(unsigned int* p, unsigned int v) {
+  unsigned int old;
+  asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+__device__ __forceinline__ void st_release_gpu(unsigned int* p, unsigned int v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 __device__ __forceinline__ bool grid_barrier(const GridBar& b) {
+  __shared__ int s_err;  // the error flag as thread 0 saw it, for the whole block
   __syncthreads();
   if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) {
-    volatile unsigned int* vgen = b.gen;
     volatile int* verr = b.err;
-    unsigned int g = *vgen;
-    __threadfence();
-    unsigned int arrived = atomicAdd(b.count, 1u);
+    const unsigned int g = ld_acquire_gpu(b.gen);
+    const unsigned int arrived = atom_add_acq_rel_gpu(b.count, 1u);
     if (arrived == b.nblocks - 1) {
-      atomicExch(b.count, 0u);
-      __threadfence();
-      atomicAdd(b.gen, 1u);
+      *b.count = 0u;  // ordered before the release below
+      st_release_gpu(b.gen, g + 1u);
     } else {
       long long s = 0;
-      while (*vgen == g) {
-        if (*verr != 0) break;
-        if (++s > b.max_spins) {
+      while (ld_acquire_gpu(b.gen) == g) {
+        if ((++s & 63) == 0 && *verr != 0) break;
+        if (s > b.max_spins) {
           atomicExch(b.err, 5);
           break;
         }
-        __nanosleep(64);
       }
     }
-    __threadfence();
+    s_err = *verr;
   }
   __syncthreads();
-  return *((volatile int*)b.err) == 0;
+  return s_err == 0;
 }
 
 }  // namespace nemo

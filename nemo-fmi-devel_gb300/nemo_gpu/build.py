@@ -1,11 +1,14 @@
 """Build recipe of the CUDA library (sm_103a only).
 
-Three translation units are compiled in parallel and linked into
+Four translation units are compiled in parallel and linked into
 ``nemo_gpu/_lib/libnemo_gpu.so``:
 
 * ``inst_fp64.cu`` -- FP64 kernels, ``--fmad=false`` so that every double operation
   rounds exactly like the reference's FP64 CPU build (no fused multiply-add);
-* ``inst_fp32.cu`` -- FP32-bulk kernels of the mixed-precision mode;
+* ``inst_fp32.cu`` -- FP32-bulk kernels of the mixed-precision mode, with
+  ``--prec-div=false`` (single-precision quotients within 2 ulp instead of
+  correctly rounded: the mixed form's tolerance is set by FP32 storage, and the
+  correctly rounded quotient costs a multi-instruction sequence per division);
 * ``capi.cu``      -- the C ABI (host code);
 * ``noalloc.cu``   -- the allocation-free global sum (static device scratch).
 """
@@ -23,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "--extended-lambda", "-lineinfo", "-Xcompiler", "-fPIC"]
 UNITS = {
     "inst_fp64.cu": ["--fmad=false"],
-    "inst_fp32.cu": [],
+    "inst_fp32.cu": ["--prec-div=false"],
     "capi.cu": [],
     "noalloc.cu": ["--fmad=false"],
 }
