@@ -74,6 +74,7 @@ struct nemo_ctx {
   void* spg_w[5] = {};
   void* ring[3] = {};
   void* spg_x[6] = {};  // fx (2 slots), fy (2 slots), du, dv, cu, cv
+  float* spg_ff = nullptr;  // mixed form: compensated sub-step sums, 10 x nmem x n2
   unsigned int* bar_mem = nullptr;  // count, gen
   int* err_flag = nullptr;
   long long bar_spins = 4000000;
@@ -669,6 +670,7 @@ int run_spg(nemo_ctx* c, int kt) {
   a.ring_ssh = (T*)c->ring[0]; a.ring_u = (T*)c->ring[1]; a.ring_v = (T*)c->ring[2];
   a.fx = (T*)c->spg_x[0]; a.fy = (T*)c->spg_x[1];
   a.du = (T*)c->spg_x[2]; a.dv = (T*)c->spg_x[3]; a.cu = (T*)c->spg_x[4]; a.cv = (T*)c->spg_x[5];
+  a.ff = c->spg_ff;
   a.wgt1 = c->d_wgt1; a.wgt2 = c->d_wgt2;
   a.ln_bt_fw = nm.ln_bt_fw; a.ln_apr_dyn = nm.ln_apr_dyn; a.nvor = nm.nvor_scheme; a.ll_init = ll_init;
   a.icycle = c->icycle;
@@ -809,6 +811,11 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
     if (cudaMalloc(&c->spg_x[w], bytes) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
     cudaMemset(c->spg_x[w], 0, bytes);
   }
+  if (prec != NEMO_PREC_FP64) {
+    const size_t bytes = 10 * (size_t)c->nmem * c->n2 * sizeof(float);
+    if (cudaMalloc(&c->spg_ff, bytes) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
+    cudaMemset(c->spg_ff, 0, bytes);
+  }
   if (cudaMalloc(&c->d_wgt1, 3 * (size_t)c->nn_baro * 8) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
   if (cudaMalloc(&c->d_wgt2, 3 * (size_t)c->nn_baro * 8) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
   cudaMemcpy(c->d_wgt1, c->wgt1.data(), c->wgt1.size() * 8, cudaMemcpyHostToDevice);
@@ -845,6 +852,7 @@ int nemo_gpu_destroy(nemo_ctx* c) {
   for (auto p : c->spg_w) cudaFree(p);
   for (auto p : c->ring) cudaFree(p);
   for (auto p : c->spg_x) cudaFree(p);
+  cudaFree(c->spg_ff);
   cudaFree(c->d_wgt1); cudaFree(c->d_wgt2);
   cudaFree(c->bar_mem); cudaFree(c->err_flag);
   cudaFree(c->gs_part); cudaFree(c->gs_out);

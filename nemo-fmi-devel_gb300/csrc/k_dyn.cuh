@@ -32,6 +32,7 @@ struct SpgArgs {
   T *ring_ssh, *ring_u, *ring_v;  // 4 slots each
   T *fx, *fy;                     // 2 slots each: predictor fluxes zwx, zwy of a sub-step
   T *du, *dv, *cu, *cv;           // phase-3 column terms, computed at the end of phase 2
+  float* ff;                      // mixed form: the five sums as (hi, lo) float pairs, 10 x nmem2
   RO<double> wgt1, wgt2;
   int ln_bt_fw, ln_apr_dyn, nvor, ll_init, icycle, ring0, phase3_filter;
   T rdtbt, grav, r1_rau0, scal_load, rn_bt_alpha;
@@ -251,13 +252,44 @@ __device__ __forceinline__ void am4(int jn, int ll_init, T alpha, T& za0, T& za1
 // touch the same ring slot or flux buffer, so one barrier separates sub-steps.
 constexpr int P2_TX = 32, P2_TY = 8;
 
+// The time-filter sums of the sub-steps (ssha, ua_b, va_b :1202-1204; un_adv,
+// vn_adv :860-862). FP64 form: the reference's FP64 accumulation. Mixed form: each
+// sum is a float pair hi + lo, updated with an exact product (the FMA residual) and
+// a two-sum on the FP32 pipe -- error ~2^-46 of the sum, far below the FP32 storage
+// of the summed values -- and converted to the FP64 fields once, at the end of the
+// kernel. (FP64 arithmetic runs at 1/64 of the FP32 rate on this GPU, and five FP64
+// sums per point per sub-step would occupy its FP64 pipe.) The intrinsics keep the
+// compiler from contracting the compensated steps.
+struct FF {
+  float h, l;
+};
+// s += p + e, with |e| small against p
+__device__ __forceinline__ void ff_add(FF& s, float p, float e) {
+  const float t = __fadd_rn(s.h, p);
+  const float bp = __fadd_rn(t, -s.h);
+  const float err = __fadd_rn(__fadd_rn(s.h, -__fadd_rn(t, -bp)), __fadd_rn(p, -bp));
+  s.l = __fadd_rn(s.l, __fadd_rn(err, e));
+  s.h = t;
+}
+// s += w * x with the FP64 weight w split as wh + wl
+__device__ __forceinline__ void ff_add_w(FF& s, float wh, float wl, float x) {
+  const float p = __fmul_rn(wh, x);
+  const float e = __fadd_rn(__fmaf_rn(wh, x, -p), __fmul_rn(wl, x));
+  ff_add(s, p, e);
+}
+// index of the hi / lo float of sum `which` (0 ssha, 1 ua_b, 2 va_b, 3 un_adv,
+// 4 vn_adv) at point g
+__device__ __forceinline__ long ffi(int which, int part, int nmem2, int g) {
+  return (long)(2 * which + part) * nmem2 + g;
+}
+
 template <class T>
 __device__ __forceinline__ int p2_tiles(const Dom<T>& d) {
   return ((d.jpi + P2_TX - 1) / P2_TX) * ((d.jpj + P2_TY - 1) / P2_TY) * d.nmem;
 }
 
 template <class T>
-__global__ void __launch_bounds__(256) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar bar) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar bar) {
   __shared__ T zs_s[P2_TY + 1][P2_TX + 1];
   const int n2 = (int)d.n2;
   const int nmem2 = d.nmem * n2;
@@ -290,8 +322,14 @@ __global__ void __launch_bounds__(256) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar 
     a.fx[(jn & 1) * nmem2 + g] = zwx;
     a.fy[(jn & 1) * nmem2 + g] = zwy;
     const T w2 = (T)a.wgt2[jn - 1];
-    a.un_adv[g] = a.un_adv[g] + (double)(w2 * zwx * d.r1_e2u[p]);
-    a.vn_adv[g] = a.vn_adv[g] + (double)(w2 * zwy * d.r1_e1v[p]);
+    if constexpr (sizeof(T) == 8) {
+      a.un_adv[g] = a.un_adv[g] + (double)(w2 * zwx * d.r1_e2u[p]);
+      a.vn_adv[g] = a.vn_adv[g] + (double)(w2 * zwy * d.r1_e1v[p]);
+    } else {  // first predictor of the kernel: the sums start here
+      for (int w = 0; w < 10; ++w) a.ff[(long)w * nmem2 + g] = 0.0f;
+      a.ff[ffi(3, 0, nmem2, g)] = w2 * zwx * d.r1_e2u[p];
+      a.ff[ffi(4, 0, nmem2, g)] = w2 * zwy * d.r1_e1v[p];
+    }
   };
   if (a.icycle >= 1)
     for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
@@ -309,6 +347,7 @@ __global__ void __launch_bounds__(256) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar 
     const T* fx = a.fx + (jn & 1) * nmem2;
     const T* fy = a.fy + (jn & 1) * nmem2;
     const double w1 = a.wgt1[jn - 1];
+    const float w1h = (float)w1, w1l = (float)(w1 - (double)w1h);  // mixed form: w1 = w1h + w1l
     T zb0, zb1, zb2, zb3;
     am4(jn, a.ll_init, a.rn_bt_alpha, zb0, zb1, zb2, zb3);
     for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
@@ -322,7 +361,8 @@ __global__ void __launch_bounds__(256) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar 
       const int p = own ? (i - 1) + (j - 1) * jpi : 0, g = m2 + p;
       T x[4] = {}, y[4] = {}, xu[4] = {}, yv[4] = {};
       T sn0 = T(0), sb0 = T(0), sbb0 = T(0), un_e = T(0), vn_e = T(0), ub_e = T(0), vb_e = T(0);
-      double acc_s = 0.0, acc_u = 0.0, acc_v = 0.0, acc_au = 0.0, acc_av = 0.0;
+      double acc_s = 0.0, acc_u = 0.0, acc_v = 0.0, acc_au = 0.0, acc_av = 0.0;  // FP64 form
+      FF f_s{}, f_u{}, f_v{}, f_au{}, f_av{};                                    // mixed form
       if (own) {
         sn0 = a.ring_ssh[sn * nmem2 + g];
         sb0 = a.ring_ssh[sb * nmem2 + g];
@@ -331,8 +371,16 @@ __global__ void __launch_bounds__(256) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar 
         vn_e = a.ring_v[sn * nmem2 + g];
         ub_e = a.ring_u[sb * nmem2 + g];
         vb_e = a.ring_v[sb * nmem2 + g];
-        acc_s = a.ssha[g]; acc_u = a.ua_b[g]; acc_v = a.va_b[g];
-        acc_au = a.un_adv[g]; acc_av = a.vn_adv[g];
+        if constexpr (sizeof(T) == 8) {
+          acc_s = a.ssha[g]; acc_u = a.ua_b[g]; acc_v = a.va_b[g];
+          acc_au = a.un_adv[g]; acc_av = a.vn_adv[g];
+        } else {
+          f_s = FF{a.ff[ffi(0, 0, nmem2, g)], a.ff[ffi(0, 1, nmem2, g)]};
+          f_u = FF{a.ff[ffi(1, 0, nmem2, g)], a.ff[ffi(1, 1, nmem2, g)]};
+          f_v = FF{a.ff[ffi(2, 0, nmem2, g)], a.ff[ffi(2, 1, nmem2, g)]};
+          f_au = FF{a.ff[ffi(3, 0, nmem2, g)], a.ff[ffi(3, 1, nmem2, g)]};
+          f_av = FF{a.ff[ffi(4, 0, nmem2, g)], a.ff[ffi(4, 1, nmem2, g)]};
+        }
         if (inner) {
           nbx([&](long q) { return fx[m2 + q]; }, (long)p, jpi, x);
           nby([&](long q) { return fy[m2 + q]; }, (long)p, jpi, y);
@@ -379,7 +427,13 @@ __global__ void __launch_bounds__(256) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar 
         }
         zs_s[ty][tx] = zb0 * ssha_e + zb1 * sn0 + zb2 * sb0 + zb3 * sbb0;
         a.ring_ssh[sa * nmem2 + g] = ssha_e;
-        a.ssha[g] = acc_s + w1 * (double)ssha_e;
+        if constexpr (sizeof(T) == 8) {
+          a.ssha[g] = acc_s + w1 * (double)ssha_e;
+        } else {
+          ff_add_w(f_s, w1h, w1l, ssha_e);
+          a.ff[ffi(0, 0, nmem2, g)] = f_s.h;
+          a.ff[ffi(0, 1, nmem2, g)] = f_s.l;
+        }
       }
       if (halo) {
         T ssha_e = T(0);
@@ -411,8 +465,17 @@ __global__ void __launch_bounds__(256) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar 
         }
         a.ring_u[sa * nmem2 + g] = ua_e;
         a.ring_v[sa * nmem2 + g] = va_e;
-        a.ua_b[g] = acc_u + w1 * (double)ua_e;
-        a.va_b[g] = acc_v + w1 * (double)va_e;
+        if constexpr (sizeof(T) == 8) {
+          a.ua_b[g] = acc_u + w1 * (double)ua_e;
+          a.va_b[g] = acc_v + w1 * (double)va_e;
+        } else {
+          ff_add_w(f_u, w1h, w1l, ua_e);
+          ff_add_w(f_v, w1h, w1l, va_e);
+          a.ff[ffi(1, 0, nmem2, g)] = f_u.h;
+          a.ff[ffi(1, 1, nmem2, g)] = f_u.l;
+          a.ff[ffi(2, 0, nmem2, g)] = f_v.h;
+          a.ff[ffi(2, 1, nmem2, g)] = f_v.l;
+        }
         if (jn < a.icycle) {
           // levels of sub-step jn+1: n = ua_e (new), b = un_e, bb = ub_e
           T za1, za2, za3;
@@ -424,8 +487,17 @@ __global__ void __launch_bounds__(256) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar 
           a.fx[((jn + 1) & 1) * nmem2 + g] = zwx;
           a.fy[((jn + 1) & 1) * nmem2 + g] = zwy;
           const T w2 = (T)a.wgt2[jn];
-          a.un_adv[g] = acc_au + (double)(w2 * zwx * d.r1_e2u[p]);
-          a.vn_adv[g] = acc_av + (double)(w2 * zwy * d.r1_e1v[p]);
+          if constexpr (sizeof(T) == 8) {
+            a.un_adv[g] = acc_au + (double)(w2 * zwx * d.r1_e2u[p]);
+            a.vn_adv[g] = acc_av + (double)(w2 * zwy * d.r1_e1v[p]);
+          } else {
+            ff_add(f_au, w2 * zwx * d.r1_e2u[p], 0.0f);
+            ff_add(f_av, w2 * zwy * d.r1_e1v[p], 0.0f);
+            a.ff[ffi(3, 0, nmem2, g)] = f_au.h;
+            a.ff[ffi(3, 1, nmem2, g)] = f_au.l;
+            a.ff[ffi(4, 0, nmem2, g)] = f_av.h;
+            a.ff[ffi(4, 1, nmem2, g)] = f_av.l;
+          }
         }
       }
       __syncthreads();  // zs_s is rewritten by the next tile
@@ -439,6 +511,14 @@ __global__ void __launch_bounds__(256) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar 
   const int nth = gridDim.x * blockDim.x;
   for (int g = tid; g < nmem2; g += nth) {
     const int m2 = (g / n2) * n2, p = g - m2;
+    if constexpr (sizeof(T) == 4) {  // the compensated sums into the FP64 fields
+      auto sum = [&](int w) { return (double)a.ff[ffi(w, 0, nmem2, g)] + (double)a.ff[ffi(w, 1, nmem2, g)]; };
+      a.ssha[g] = sum(0);
+      a.ua_b[g] = sum(1);
+      a.va_b[g] = sum(2);
+      a.un_adv[g] = sum(3);
+      a.vn_adv[g] = sum(4);
+    }
     double uadv = a.un_adv[g], vadv = a.vn_adv[g];
     if (a.ln_bt_fw) {
       const double zwx = uadv, zwy = vadv;
