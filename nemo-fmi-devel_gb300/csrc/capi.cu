@@ -59,6 +59,8 @@ struct nemo_ctx {
   std::vector<double> wgt1, wgt2;
   double* d_wgt1 = nullptr;
   double* d_wgt2 = nullptr;
+  float* d_wgtf = nullptr;  // mixed form: wgt1 split as hi | lo, and wgt2, as floats
+  std::vector<float> wgtf;
   int ring0 = 0;
   // device domain
   DomStore<double> dd;
@@ -321,6 +323,20 @@ template <class T>
 void free_dom(DomStore<T>& st) {
   for (void* p : st.owned) cudaFree(p);
   st.owned.clear();
+}
+
+// The sub-step weights as the mixed form's sub-step kernel uses them: wgt1 = hi + lo
+// (two floats, for the compensated sums) and wgt2 rounded to float, in three blocks
+// of wgt1.size() entries.
+void float_weights(nemo_ctx* c) {
+  const size_t n = c->wgt1.size();
+  c->wgtf.assign(3 * n, 0.0f);
+  for (size_t i = 0; i < n; ++i) {
+    const float h = (float)c->wgt1[i];
+    c->wgtf[i] = h;
+    c->wgtf[n + i] = (float)(c->wgt1[i] - (double)h);
+    c->wgtf[2 * n + i] = (float)c->wgt2[i];
+  }
 }
 
 // Domain derivation (dommsk.F90:133-238, domzgr.F90:292-314, domhgr.F90:133-151,
@@ -648,6 +664,8 @@ int run_spg(nemo_ctx* c, int kt) {
     c->icycle = jpit;
     CK(cudaMemcpyAsync(c->d_wgt1, c->wgt1.data(), c->wgt1.size() * 8, cudaMemcpyHostToDevice, c->stream), "weights");
     CK(cudaMemcpyAsync(c->d_wgt2, c->wgt2.data(), c->wgt2.size() * 8, cudaMemcpyHostToDevice, c->stream), "weights");
+    float_weights(c);
+    CK(cudaMemcpyAsync(c->d_wgtf, c->wgtf.data(), c->wgtf.size() * 4, cudaMemcpyHostToDevice, c->stream), "weights");
     CK(cudaStreamSynchronize(c->stream), "weights");
   }
   SpgArgs<T> a{};
@@ -671,7 +689,7 @@ int run_spg(nemo_ctx* c, int kt) {
   a.fx = (T*)c->spg_x[0]; a.fy = (T*)c->spg_x[1];
   a.du = (T*)c->spg_x[2]; a.dv = (T*)c->spg_x[3]; a.cu = (T*)c->spg_x[4]; a.cv = (T*)c->spg_x[5];
   a.ff = c->spg_ff;
-  a.wgt1 = c->d_wgt1; a.wgt2 = c->d_wgt2;
+  a.wgt1 = c->d_wgt1; a.wgt2 = c->d_wgt2; a.wgtf = c->d_wgtf; a.nwgt = (int)c->wgt1.size();
   a.ln_bt_fw = nm.ln_bt_fw; a.ln_apr_dyn = nm.ln_apr_dyn; a.nvor = nm.nvor_scheme; a.ll_init = ll_init;
   a.icycle = c->icycle;
   // With time averaging every call restarts the barotropic levels, so the ring can
@@ -820,6 +838,9 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
   if (cudaMalloc(&c->d_wgt2, 3 * (size_t)c->nn_baro * 8) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
   cudaMemcpy(c->d_wgt1, c->wgt1.data(), c->wgt1.size() * 8, cudaMemcpyHostToDevice);
   cudaMemcpy(c->d_wgt2, c->wgt2.data(), c->wgt2.size() * 8, cudaMemcpyHostToDevice);
+  if (cudaMalloc(&c->d_wgtf, 3 * 3 * (size_t)c->nn_baro * 4) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
+  float_weights(c);
+  cudaMemcpy(c->d_wgtf, c->wgtf.data(), c->wgtf.size() * 4, cudaMemcpyHostToDevice);
   if (cudaMalloc(&c->bar_mem, 2 * sizeof(unsigned int)) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
   if (cudaMalloc(&c->err_flag, sizeof(int)) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
   cudaMemset(c->bar_mem, 0, 2 * sizeof(unsigned int));
@@ -853,7 +874,7 @@ int nemo_gpu_destroy(nemo_ctx* c) {
   for (auto p : c->ring) cudaFree(p);
   for (auto p : c->spg_x) cudaFree(p);
   cudaFree(c->spg_ff);
-  cudaFree(c->d_wgt1); cudaFree(c->d_wgt2);
+  cudaFree(c->d_wgt1); cudaFree(c->d_wgt2); cudaFree(c->d_wgtf);
   cudaFree(c->bar_mem); cudaFree(c->err_flag);
   cudaFree(c->gs_part); cudaFree(c->gs_out);
   for (auto e : c->tev)

@@ -2,6 +2,7 @@
 // inst_fp64.cu and inst_fp32.cu, each of which instantiates one precision.
 #pragma once
 #include "launch.h"
+#include "k_hot.cuh"
 
 namespace nemo {
 
@@ -35,6 +36,15 @@ cudaError_t launch_adv_trp(const Dom<T>& d, const T* un, const T* vn, const T* w
 
 template <class T>
 cudaError_t launch_fct(const Dom<T>& d, const FctArgs<T>& a, cudaStream_t s) {
+  if (hot_fct_ok(d, a)) {
+    k_fct_a_hot<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+    ktick(NEMO_K_FCT_A, s);
+    k_fct_b_hot<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+    ktick(NEMO_K_FCT_B, s);
+    k_fct_c_hot<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+    ktick(NEMO_K_FCT_C, s);
+    return cudaGetLastError();
+  }
   if (a.kn_fct_v == 4) {
     k_interp4<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a.ptn, const_cast<T*>(a.ztw.p), a.kjpt);
     ktick(NEMO_K_INTERP4, s);
@@ -57,8 +67,7 @@ cudaError_t launch_ldf_lap(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s)
 
 template <class T>
 cudaError_t launch_ldf_iso(const Dom<T>& d, const LdfArgs<T>& a, int copy_akz_edges, int msc_edges, cudaStream_t s) {
-  k_iso_flux<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
-  ktick(NEMO_K_ISO_FLUX, s);
+  launch_iso_flux<T>(d, a, s);
   k_iso_div<T><<<pt_grid(d), dim3(BX, BY), 0, s>>>(d, a);
   ktick(NEMO_K_ISO_DIV, s);
   return launch_iso_edges<T>(d, a, copy_akz_edges, msc_edges, s);
@@ -66,7 +75,8 @@ cudaError_t launch_ldf_iso(const Dom<T>& d, const LdfArgs<T>& a, int copy_akz_ed
 
 template <class T>
 cudaError_t launch_iso_flux(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s) {
-  k_iso_flux<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  if (hot_iso_ok(d, a)) k_iso_flux_hot<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  else k_iso_flux<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
   ktick(NEMO_K_ISO_FLUX, s);
   return cudaGetLastError();
 }
@@ -119,7 +129,14 @@ int spg_p2_blocks_per_sm() {
 
 template <class T>
 cudaError_t launch_spg(const Dom<T>& d, const SpgArgs<T>& a, const GridBar& bar, int p2_blocks, cudaStream_t s) {
-  k_spg_p1a<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  bool p1a_reg = false;
+  if constexpr (sizeof(T) == 4) {
+    if (d.jpk == 31) {  // the GYRE levels: columns in registers
+      k_spg_p1a_reg<31><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+      p1a_reg = true;
+    }
+  }
+  if (!p1a_reg) k_spg_p1a<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
   ktick(NEMO_K_SPG_P1A, s);
   k_spg_p1b<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
   ktick(NEMO_K_SPG_P1B, s);
@@ -136,7 +153,8 @@ cudaError_t launch_spg(const Dom<T>& d, const SpgArgs<T>& a, const GridBar& bar,
   cudaError_t e = cudaLaunchKernelEx(&cfg, k_spg_p2<T>, d, a, bar);
   if (e != cudaSuccess) return e;
   ktick(NEMO_K_SPG_P2, s);
-  k_spg_p3<T><<<pt_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  k_spg_p3<T><<<dim3((d.jpi + BX - 1) / BX, (d.jpj + BY - 1) / BY, d.nmem * ((d.jpk + KCH3 - 1) / KCH3)),
+                 dim3(BX, BY), 0, s>>>(d, a);
   ktick(NEMO_K_SPG_P3, s);
   return cudaGetLastError();
 }

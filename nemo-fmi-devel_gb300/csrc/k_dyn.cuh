@@ -16,6 +16,8 @@
 
 namespace nemo {
 
+constexpr int KCH3 = 8;  // levels per thread of the phase-3 kernel
+
 template <class T>
 struct SpgArgs {
   // 3-D
@@ -34,6 +36,8 @@ struct SpgArgs {
   T *du, *dv, *cu, *cv;           // phase-3 column terms, computed at the end of phase 2
   float* ff;                      // mixed form: the five sums as (hi, lo) float pairs, 10 x nmem2
   RO<double> wgt1, wgt2;
+  RO<float> wgtf;                 // mixed form: wgt1 hi | wgt1 lo | wgt2, nwgt entries each
+  int nwgt;
   int ln_bt_fw, ln_apr_dyn, nvor, ll_init, icycle, ring0, phase3_filter;
   T rdtbt, grav, r1_rau0, scal_load, rn_bt_alpha;
   double rn_atfp, r1_2dt_b;
@@ -68,6 +72,43 @@ __global__ void k_spg_p1a(Dom<T> d, SpgArgs<T> a) {
       const long q = m3 + ij + (long)(k - 1) * n2;
       a.ua[q] = a.ua[q] - su * umsk<T>(ci, k);
       a.va[q] = a.va[q] - sv * vmsk<T>(ci, k);
+    }
+}
+
+// Phase 1a for FP32 and jpk = NK known at compile time: the column of ua / va is
+// loaded whole into registers, summed in the reference's order, then corrected and
+// stored, so each value is read once and all loads are in flight together.
+template <int NK>
+__global__ void __launch_bounds__(128) k_spg_p1a_reg(Dom<float> d, SpgArgs<float> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int m = blockIdx.z;
+  if (i > d.jpi || j > d.jpj) return;
+  const long ij = pt_ij(d, i, j), n2 = d.n2, m2 = (long)m * n2;
+  const ColInfo ci = d.ci[ij];
+  float* ua = a.ua + (long)m * d.n3 + ij;
+  float* va = a.va + (long)m * d.n3 + ij;
+  float u[NK - 1], v[NK - 1];
+#pragma unroll
+  for (int k = 1; k <= NK - 1; ++k) {
+    u[k - 1] = ua[(k - 1) * n2];
+    v[k - 1] = va[(k - 1) * n2];
+  }
+  float su = 0.f, sv = 0.f;
+#pragma unroll
+  for (int k = 1; k <= NK - 1; ++k) {
+    su = su + d.e3u_n(ij, k, m) * u[k - 1] * umsk<float>(ci, k);
+    sv = sv + d.e3v_n(ij, k, m) * v[k - 1] * vmsk<float>(ci, k);
+  }
+  su = su * d.r1_hu_0[ij];
+  sv = sv * d.r1_hv_0[ij];
+  a.zu_frc[m2 + ij] = su;
+  a.zv_frc[m2 + ij] = sv;
+  if (i >= 2 && i <= d.jpi - 1 && j >= 2 && j <= d.jpj - 1)
+#pragma unroll
+    for (int k = 1; k <= NK - 1; ++k) {
+      ua[(k - 1) * n2] = u[k - 1] - su * umsk<float>(ci, k);
+      va[(k - 1) * n2] = v[k - 1] - sv * vmsk<float>(ci, k);
     }
 }
 
@@ -321,7 +362,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
     const T zwy = d.e1v[p] * va_e * d.hv_0[p];
     a.fx[(jn & 1) * nmem2 + g] = zwx;
     a.fy[(jn & 1) * nmem2 + g] = zwy;
-    const T w2 = (T)a.wgt2[jn - 1];
+    T w2;
+    if constexpr (sizeof(T) == 8) w2 = a.wgt2[jn - 1];
+    else w2 = a.wgtf[2 * a.nwgt + jn - 1];
     if constexpr (sizeof(T) == 8) {
       a.un_adv[g] = a.un_adv[g] + (double)(w2 * zwx * d.r1_e2u[p]);
       a.vn_adv[g] = a.vn_adv[g] + (double)(w2 * zwy * d.r1_e1v[p]);
@@ -346,8 +389,14 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
     const int sn = r & 3, sb = (r + 1) & 3, sbb = (r + 2) & 3, sa = (r + 3) & 3;
     const T* fx = a.fx + (jn & 1) * nmem2;
     const T* fy = a.fy + (jn & 1) * nmem2;
-    const double w1 = a.wgt1[jn - 1];
-    const float w1h = (float)w1, w1l = (float)(w1 - (double)w1h);  // mixed form: w1 = w1h + w1l
+    double w1 = 0.0;         // FP64 form
+    float w1h = 0.f, w1l = 0.f;  // mixed form: w1 = w1h + w1l
+    if constexpr (sizeof(T) == 8) {
+      w1 = a.wgt1[jn - 1];
+    } else {
+      w1h = a.wgtf[jn - 1];
+      w1l = a.wgtf[a.nwgt + jn - 1];
+    }
     T zb0, zb1, zb2, zb3;
     am4(jn, a.ll_init, a.rn_bt_alpha, zb0, zb1, zb2, zb3);
     for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
@@ -486,7 +535,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
           const T zwy = d.e1v[p] * vex * d.hv_0[p];
           a.fx[((jn + 1) & 1) * nmem2 + g] = zwx;
           a.fy[((jn + 1) & 1) * nmem2 + g] = zwy;
-          const T w2 = (T)a.wgt2[jn];
+          T w2;
+          if constexpr (sizeof(T) == 8) w2 = a.wgt2[jn];
+          else w2 = a.wgtf[2 * a.nwgt + jn];
           if constexpr (sizeof(T) == 8) {
             a.un_adv[g] = acc_au + (double)(w2 * zwx * d.r1_e2u[p]);
             a.vn_adv[g] = acc_av + (double)(w2 * zwy * d.r1_e1v[p]);
@@ -543,23 +594,32 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
   }
 }
 
-// Phase 3, per point (:1236-1240, :1266-1269): the barotropic trend added to ua, va
-// and the now velocities corrected to the time-filtered transports.
+// Phase 3 (:1236-1240, :1266-1269): the barotropic trend added to ua, va and the now
+// velocities corrected to the time-filtered transports; one thread walks a chunk of
+// levels of one column, the column terms loaded once.
 template <class T>
-__global__ void k_spg_p3(Dom<T> d, SpgArgs<T> a) {
+__global__ void __launch_bounds__(128) k_spg_p3(Dom<T> d, SpgArgs<T> a) {
+  const int nch = (d.jpk + KCH3 - 1) / KCH3;
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int k = (int)(blockIdx.z % (unsigned)d.jpk) + 1;
-  const int m = (int)(blockIdx.z / (unsigned)d.jpk);
-  if (i > d.jpi || j > d.jpj || k > d.jpk - 1) return;
+  const int m = (int)(blockIdx.z / (unsigned)nch);
+  const int k0 = ((int)blockIdx.z - m * nch) * KCH3 + 1;
+  if (i > d.jpi || j > d.jpj) return;
+  const int k1 = k0 + KCH3 - 1 < d.jpk - 1 ? k0 + KCH3 - 1 : d.jpk - 1;
   const long p = pt_ij(d, i, j), m2 = (long)m * d.n2;
-  const long q = (long)m * d.n3 + p + (long)(k - 1) * d.n2;
   const ColInfo ci = d.ci[p];
   const RO<T> du = a.du, dv = a.dv, cu = a.cu, cv = a.cv;  // written by phase 2
-  a.ua[q] = a.ua[q] + du[m2 + p];
-  a.va[q] = a.va[q] + dv[m2 + p];
-  a.un[q] = (a.un[q] + cu[m2 + p] - a.un_b[m2 + p]) * umsk<T>(ci, k);
-  a.vn[q] = (a.vn[q] + cv[m2 + p] - a.vn_b[m2 + p]) * vmsk<T>(ci, k);
+  const T du0 = du[m2 + p], dv0 = dv[m2 + p], cu0 = cu[m2 + p], cv0 = cv[m2 + p];
+  const T unb = a.un_b[m2 + p], vnb = a.vn_b[m2 + p];
+  const long base = (long)m * d.n3 + p;
+  for (int k = k0; k <= k1; ++k) {
+    const long q = base + (long)(k - 1) * d.n2;
+    const T ua = a.ua[q], va = a.va[q], un = a.un[q], vn = a.vn[q];
+    a.ua[q] = ua + du0;
+    a.va[q] = va + dv0;
+    a.un[q] = (un + cu0 - unb) * umsk<T>(ci, k);
+    a.vn[q] = (vn + cv0 - vnb) * vmsk<T>(ci, k);
+  }
 }
 
 // ---------------------------------------------------------------------------------

@@ -810,14 +810,21 @@ __global__ void k_iso_msc_edges(Dom<T> d, LdfArgs<T> a) {
 }
 
 // akz = ah_wslp2 on the whole array (traldf_iso.F90:200-201) for the points the
-// interior sweep does not write (edge columns, levels 1 and jpk).
+// interior sweep does not write: levels 1 and jpk of interior columns, every level
+// of the edge columns.
 template <class T>
 __global__ void k_iso_akz_copy_edges(Dom<T> d, LdfArgs<T> a) {
   ColIdx<T> c = col_index(d);
   if (!c.valid) return;
+  const long base = (long)c.m * d.n3 + c.ij;
+  if (c.interior) {
+    const long qt = base + (long)(d.jpk - 1) * d.n2;
+    a.akz[base] = a.ah_wslp2[base];
+    a.akz[qt] = a.ah_wslp2[qt];
+    return;
+  }
   for (int k = 1; k <= d.jpk; ++k) {
-    if (c.interior && k >= 2 && k <= d.jpk - 1) continue;
-    const long q = (long)c.m * d.n3 + c.ij + (long)(k - 1) * d.n2;
+    const long q = base + (long)(k - 1) * d.n2;
     a.akz[q] = a.ah_wslp2[q];
   }
 }
