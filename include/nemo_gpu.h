@@ -182,8 +182,14 @@ int nemo_gpu_field_is_fp64(const nemo_ctx *ctx, int field_id);
 /* Barotropic sub-step count icycle, and nn_baro after ln_bt_auto (dynspg_ts.F90:1491). */
 int nemo_gpu_spg_info(const nemo_ctx *ctx, int *icycle, int *nn_baro, double *rdtbt);
 
-/* Copy between a host buffer and a bound field (all members) on the context
- * stream; host memory should be pinned for asynchronous copies. */
+/* Copy between a host buffer and a bound field (all members). Both are
+ * asynchronous and ordered with the context's work: an upload runs after the work
+ * already queued on the context stream (and after a pending download of the same
+ * field), a download after the work already queued and the pending uploads, and the
+ * next routine called on the context waits for both. Uploads and downloads use two
+ * copy streams of the context, so one step's downloads overlap the next step's
+ * uploads. Host memory should be pinned; read a downloaded buffer, or upload it
+ * into another field, only after nemo_gpu_synchronize. */
 int nemo_gpu_field_upload(nemo_ctx *ctx, int field_id, const void *host);
 int nemo_gpu_field_download(nemo_ctx *ctx, int field_id, void *host);
 

@@ -96,6 +96,15 @@ struct nemo_ctx {
   int tcalls = 0;
   // per-kernel timing (events after every launch while timing is on)
   KernelClock kc;
+  // host copies: uploads and downloads run on their own streams so that the
+  // downloads of one step overlap the uploads of the next
+  cudaStream_t h2d = nullptr, d2h = nullptr;
+  cudaEvent_t ev_main = nullptr;   // the context stream's work so far
+  cudaEvent_t ev_up = nullptr;     // the last upload
+  cudaEvent_t ev_down = nullptr;   // the last download
+  cudaEvent_t ev_field[NEMO_F_COUNT] = {};  // the last download of each field
+  bool up_pending = false, down_pending = false;
+  bool field_pending[NEMO_F_COUNT] = {};
   double kms[NEMO_K_COUNT] = {};
   int kcnt[NEMO_K_COUNT] = {};
 };
@@ -127,6 +136,21 @@ int cuda_fail(nemo_ctx* c, cudaError_t e, const char* what) {
     cudaError_t e_ = (expr);                            \
     if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
   } while (0)
+
+// Before the context stream runs work: wait for the pending host copies (the work
+// reads uploaded fields and may overwrite fields being downloaded).
+int join_copies(nemo_ctx* c) {
+  if (c->up_pending) {
+    CK(cudaStreamWaitEvent(c->stream, c->ev_up, 0), "wait for uploads");
+    c->up_pending = false;
+  }
+  if (c->down_pending) {
+    CK(cudaStreamWaitEvent(c->stream, c->ev_down, 0), "wait for downloads");
+    c->down_pending = false;
+    for (bool& b : c->field_pending) b = false;
+  }
+  return NEMO_OK;
+}
 
 inline size_t I2(const nemo_ctx* c, int i, int j) { return (size_t)(i - 1) + (size_t)c->jpi * (j - 1); }
 inline size_t I3(const nemo_ctx* c, int i, int j, int k) { return I2(c, i, j) + (size_t)c->n2 * (k - 1); }
@@ -810,6 +834,13 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return bad(NEMO_ERR_CUDA);
     c->own_stream = true;
   }
+  if (cudaStreamCreateWithFlags(&c->h2d, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->d2h, cudaStreamNonBlocking) != cudaSuccess)
+    return bad(NEMO_ERR_CUDA);
+  for (cudaEvent_t* e : {&c->ev_main, &c->ev_up, &c->ev_down})
+    if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return bad(NEMO_ERR_CUDA);
+  for (auto& e : c->ev_field)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return bad(NEMO_ERR_CUDA);
   int s = derive_domain(c, dm);
   if (s) { fprintf(stderr, "nemo_gpu_create: %s\n", c->err.c_str()); return bad(s); }
   s = prec == NEMO_PREC_FP64 ? build_dom<double>(c, c->dd) : build_dom<float>(c, c->df);
@@ -881,6 +912,12 @@ int nemo_gpu_destroy(nemo_ctx* c) {
     if (e) cudaEventDestroy(e);
   for (auto e : c->kc.ev)
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : {c->ev_main, c->ev_up, c->ev_down})
+    if (e) cudaEventDestroy(e);
+  for (auto e : c->ev_field)
+    if (e) cudaEventDestroy(e);
+  if (c->h2d) cudaStreamDestroy(c->h2d);
+  if (c->d2h) cudaStreamDestroy(c->d2h);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return NEMO_OK;
@@ -890,6 +927,10 @@ const char* nemo_gpu_last_error(const nemo_ctx* c) { return c ? c->err.c_str() :
 
 int nemo_gpu_synchronize(nemo_ctx* c) {
   if (!c) return NEMO_ERR_ARG;
+  CK(cudaStreamSynchronize(c->h2d), "synchronize");
+  CK(cudaStreamSynchronize(c->d2h), "synchronize");
+  c->up_pending = c->down_pending = false;
+  for (bool& b : c->field_pending) b = false;
   CK(cudaStreamSynchronize(c->stream), "synchronize");
   int flag = 0;
   CK(cudaMemcpy(&flag, c->err_flag, sizeof(int), cudaMemcpyDeviceToHost), "read status");
@@ -931,7 +972,13 @@ int nemo_gpu_field_upload(nemo_ctx* c, int id, const void* host) {
   if (!c || id < 0 || id >= NEMO_F_COUNT || !host) return fail(c, NEMO_ERR_ARG, "field_upload: bad argument");
   if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "field_upload: field %d is not bound", id);
   size_t bytes = field_numel(c, id) * c->nmem * (nemo_gpu_field_is_fp64(c, id) ? 8 : 4);
-  CK(cudaMemcpyAsync(c->f[id], host, bytes, cudaMemcpyHostToDevice, c->stream), "field_upload");
+  // after the work already queued (it may read the field) and the field's download
+  CK(cudaEventRecord(c->ev_main, c->stream), "field_upload");
+  CK(cudaStreamWaitEvent(c->h2d, c->ev_main, 0), "field_upload");
+  if (c->field_pending[id]) CK(cudaStreamWaitEvent(c->h2d, c->ev_field[id], 0), "field_upload");
+  CK(cudaMemcpyAsync(c->f[id], host, bytes, cudaMemcpyHostToDevice, c->h2d), "field_upload");
+  CK(cudaEventRecord(c->ev_up, c->h2d), "field_upload");
+  c->up_pending = true;
   return NEMO_OK;
 }
 
@@ -939,12 +986,21 @@ int nemo_gpu_field_download(nemo_ctx* c, int id, void* host) {
   if (!c || id < 0 || id >= NEMO_F_COUNT || !host) return fail(c, NEMO_ERR_ARG, "field_download: bad argument");
   if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "field_download: field %d is not bound", id);
   size_t bytes = field_numel(c, id) * c->nmem * (nemo_gpu_field_is_fp64(c, id) ? 8 : 4);
-  CK(cudaMemcpyAsync(host, c->f[id], bytes, cudaMemcpyDeviceToHost, c->stream), "field_download");
+  // after the work already queued and any pending upload
+  CK(cudaEventRecord(c->ev_main, c->stream), "field_download");
+  CK(cudaStreamWaitEvent(c->d2h, c->ev_main, 0), "field_download");
+  if (c->up_pending) CK(cudaStreamWaitEvent(c->d2h, c->ev_up, 0), "field_download");
+  CK(cudaMemcpyAsync(host, c->f[id], bytes, cudaMemcpyDeviceToHost, c->d2h), "field_download");
+  CK(cudaEventRecord(c->ev_field[id], c->d2h), "field_download");
+  CK(cudaEventRecord(c->ev_down, c->d2h), "field_download");
+  c->field_pending[id] = true;
+  c->down_pending = true;
   return NEMO_OK;
 }
 
 int nemo_gpu_tra_adv_trp(nemo_ctx* c, const void* un, const void* vn, const void* wn, void* zun, void* zvn, void* zwn) {
   if (!c || !un || !vn || !wn || !zun || !zvn || !zwn) return fail(c, NEMO_ERR_ARG, "tra_adv_trp: null pointer");
+  if (join_copies(c)) return NEMO_ERR_CUDA;
   cudaError_t e = c->prec == NEMO_PREC_FP64
                       ? launch_adv_trp<double>(dom_now<double>(c), (const double*)un, (const double*)vn,
                                                (const double*)wn, (double*)zun, (double*)zvn, (double*)zwn, c->stream)
@@ -959,6 +1015,7 @@ int nemo_gpu_tra_adv_fct(nemo_ctx* c, int kt, int kit000, const char* cdtype, do
                          int kn_fct_h, int kn_fct_v) {
   (void)kt; (void)kit000;
   if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
   int is_trc = 0;
   if (int s = check_cdtype(c, cdtype, &is_trc)) return s;
   if (!pun || !pvn || !pwn || !ptb || !ptn || !pta || kjpt < 1) return fail(c, NEMO_ERR_ARG, "tra_adv_fct: bad argument");
@@ -974,6 +1031,7 @@ int nemo_gpu_tra_ldf_lap(nemo_ctx* c, int kt, int kit000, const char* cdtype, co
                          void* pta, int kjpt, int kpass) {
   (void)kt; (void)kit000; (void)pgui; (void)pgvi;
   if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
   int is_trc = 0;
   if (int s = check_cdtype(c, cdtype, &is_trc)) return s;
   if (!ptb || !pta || kjpt < 1 || (kpass != 1 && kpass != 2)) return fail(c, NEMO_ERR_ARG, "tra_ldf_lap: bad argument");
@@ -987,6 +1045,7 @@ int nemo_gpu_tra_ldf_iso(nemo_ctx* c, int kt, int kit000, const char* cdtype, co
                          const void* ptbb, void* pta, int kjpt, int kpass) {
   (void)pgui; (void)pgvi;
   if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
   int is_trc = 0;
   if (int s = check_cdtype(c, cdtype, &is_trc)) return s;
   if (!ptb || !ptbb || !pta || kjpt < 1 || (kpass != 1 && kpass != 2))
@@ -1001,6 +1060,7 @@ int nemo_gpu_tra_zdf_imp(nemo_ctx* c, int kt, int kit000, const char* cdtype, do
                          int kjpt) {
   (void)kt; (void)kit000;
   if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
   int is_trc = 0;
   if (int s = check_cdtype(c, cdtype, &is_trc)) return s;
   if (!ptb || !pta || kjpt < 1) return fail(c, NEMO_ERR_ARG, "tra_zdf_imp: bad argument");
@@ -1010,6 +1070,7 @@ int nemo_gpu_tra_zdf_imp(nemo_ctx* c, int kt, int kit000, const char* cdtype, do
 
 int nemo_gpu_tra_zdf(nemo_ctx* c, int kt) {
   if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
   const nemo_namelist& nm = c->nam;
   if (!c->f[NEMO_F_TSB] || !c->f[NEMO_F_TSA]) return fail(c, NEMO_ERR_UNBOUND, "tra_zdf: tsb and tsa must be bound");
   if (nm.neuler == 0 && kt == nm.nit000) c->r2dt = nm.rn_rdt;
@@ -1029,6 +1090,7 @@ int nemo_gpu_tra_zdf(nemo_ctx* c, int kt) {
 
 int nemo_gpu_dyn_spg_ts(nemo_ctx* c, int kt) {
   if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
   return c->prec == NEMO_PREC_FP64 ? run_spg<double>(c, kt) : run_spg<float>(c, kt);
 }
 
@@ -1036,6 +1098,7 @@ int nemo_gpu_lbc_lnk(nemo_ctx* c, const char* cdname, void* ptab, int nk, int nl
                      double pval, int is_fp64) {
   (void)cdname; (void)psgn;
   if (!c || !ptab || nk < 1 || nl < 1 || !cd_nat) return fail(c, NEMO_ERR_ARG, "lbc_lnk: bad argument");
+  if (join_copies(c)) return NEMO_ERR_CUDA;
   const char n = cd_nat[0];
   if (n != 'T' && n != 'U' && n != 'V' && n != 'W' && n != 'F') return fail(c, NEMO_ERR_ARG, "lbc_lnk: bad grid nature");
   const long nslab = (long)nk * nl * c->nmem;
@@ -1048,6 +1111,7 @@ int nemo_gpu_lbc_lnk(nemo_ctx* c, const char* cdname, void* ptab, int nk, int nl
 int nemo_gpu_lbc_lnk_multi(nemo_ctx* c, const char* cdname, int kfld, void* const* ptabs, const int* nk,
                            const char* cd_nats, const double* psgns, double pval, int is_fp64) {
   if (!c || kfld < 1 || kfld > 9 || !ptabs || !nk || !cd_nats || !psgns) return fail(c, NEMO_ERR_ARG, "lbc_lnk_multi: bad argument");
+  if (join_copies(c)) return NEMO_ERR_CUDA;
   for (int f = 0; f < kfld; ++f) {
     char nat[2] = {cd_nats[f], 0};
     int s = nemo_gpu_lbc_lnk(c, cdname, ptabs[f], nk[f], 1, nat, psgns[f], pval, is_fp64);
@@ -1059,6 +1123,7 @@ int nemo_gpu_lbc_lnk_multi(nemo_ctx* c, const char* cdname, int kfld, void* cons
 int nemo_gpu_glob_sum(nemo_ctx* c, const char* cdname, const void* ptab, int nk, int is_fp64, double* out) {
   (void)cdname;
   if (!c || !ptab || nk < 1 || !out) return fail(c, NEMO_ERR_ARG, "glob_sum: bad argument");
+  if (join_copies(c)) return NEMO_ERR_CUDA;
   const double* tmi = c->prec == NEMO_PREC_FP64 ? c->dd.d.tmask_i.p : c->df.d.tmask_i.p;
   cudaError_t e = is_fp64 ? launch_globsum<double>((const double*)ptab, tmi, c->n2, nk, c->nmem, c->gs_part, c->gs_nblk,
                                                    c->gs_out, c->stream)
@@ -1072,6 +1137,7 @@ int nemo_gpu_glob_sum(nemo_ctx* c, const char* cdname, const void* ptab, int nk,
 
 int nemo_gpu_stp_hotpath(nemo_ctx* c, int kt) {
   if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
   const nemo_namelist& nm = c->nam;
   // class of kt: the Euler/leapfrog start steps differ in scalars and weights
   const int cls = kt == nm.nit000 ? 0 : (kt == nm.nit000 + 1 ? 1 : 2);

@@ -1,0 +1,59 @@
+"""Host copies through the C ABI (nemo_gpu_field_upload / nemo_gpu_field_download)
+overlapped on the context's copy streams give the same results as fully serialised
+copies: each step uploads new inputs, runs the hot path and downloads its outputs,
+once with no synchronisation until the end and once synchronising after every call.
+"""
+import pytest
+
+from harness import Pair
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+INS = ("TSB", "TSN", "UN", "VN", "UA", "VA")
+OUTS = ("TSA", "UA", "VA", "UN", "VN")
+
+
+@pytest.fixture(autouse=True)
+def _gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _run(prec, serialise, nsteps=3):
+    p = Pair(nn=2, prec=prec, seed=21, neuler=0)
+    p.bind_hotpath()
+    gen = torch.Generator().manual_seed(5)
+    ins = {}
+    for n in INS:
+        base = p.dev[n].detach().cpu()
+        ins[n] = []
+        for s in range(nsteps):  # a different input every step
+            h = torch.empty(base.numel(), dtype=base.dtype, pin_memory=True)
+            h.copy_(base.reshape(-1) * (1.0 + 0.01 * s) + 1e-3 * torch.randn(base.numel(), generator=gen).to(base.dtype))
+            ins[n].append(h)
+    outs = {n: [torch.empty(p.dev[n].numel(), dtype=p.dev[n].dtype, pin_memory=True) for _ in range(nsteps)]
+            for n in OUTS}
+    for s in range(nsteps):
+        for n in INS:
+            p.ctx.upload(n, ins[n][s])
+            if serialise:
+                p.ctx.synchronize()
+        p.ctx.stp_hotpath(3 + s)
+        if serialise:
+            p.ctx.synchronize()
+        for n in OUTS:
+            p.ctx.download(n, outs[n][s])
+            if serialise:
+                p.ctx.synchronize()
+    p.ctx.synchronize()
+    return outs
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_overlapped_copies_match_serialised(prec):
+    a = _run(prec, serialise=False)
+    b = _run(prec, serialise=True)
+    for n in OUTS:
+        for s, (x, y) in enumerate(zip(a[n], b[n])):
+            assert torch.equal(x, y), f"{n} step {s}: overlapped copies differ from serialised ones"
