@@ -186,9 +186,10 @@ int nemo_gpu_spg_info(const nemo_ctx *ctx, int *icycle, int *nn_baro, double *rd
  * asynchronous and ordered with the context's work: an upload runs after the work
  * already queued on the context stream (and after a pending download of the same
  * field), a download after the work already queued and the pending uploads, and the
- * next routine called on the context waits for both. Uploads and downloads use two
- * copy streams of the context, so one step's downloads overlap the next step's
- * uploads. Host memory should be pinned; read a downloaded buffer, or upload it
+ * next routine called on the context waits for both. Uploads and downloads use
+ * copy streams of the context (field id modulo four upload and two download
+ * streams), so copies of different fields run on several copy engines at once and
+ * one step's downloads overlap the next step's uploads. Host memory should be pinned; read a downloaded buffer, or upload it
  * into another field, only after nemo_gpu_synchronize. */
 int nemo_gpu_field_upload(nemo_ctx *ctx, int field_id, const void *host);
 int nemo_gpu_field_download(nemo_ctx *ctx, int field_id, void *host);

@@ -98,13 +98,18 @@ struct nemo_ctx {
   KernelClock kc;
   // host copies: uploads and downloads run on their own streams so that the
   // downloads of one step overlap the uploads of the next
-  cudaStream_t h2d = nullptr, d2h = nullptr;
-  cudaEvent_t ev_main = nullptr;   // the context stream's work so far
-  cudaEvent_t ev_up = nullptr;     // the last upload
-  cudaEvent_t ev_down = nullptr;   // the last download
+  // (fields spread over several streams by id, to keep several copy engines busy)
+  static constexpr int NUP = 4, NDOWN = 2;
+  cudaStream_t h2d[NUP] = {}, d2h[NDOWN] = {};
+  cudaEvent_t ev_main = nullptr;          // the context stream's work so far
+  cudaEvent_t ev_up[NUP] = {};            // the last upload of each upload stream
+  cudaEvent_t ev_down[NDOWN] = {};        // the last download of each download stream
   cudaEvent_t ev_field[NEMO_F_COUNT] = {};  // the last download of each field
-  bool up_pending = false, down_pending = false;
+  bool up_pending[NUP] = {}, down_pending[NDOWN] = {};
   bool field_pending[NEMO_F_COUNT] = {};
+  // hot path: the iso-neutral fluxes run on a side stream beside dyn_spg_ts
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   double kms[NEMO_K_COUNT] = {};
   int kcnt[NEMO_K_COUNT] = {};
 };
@@ -140,15 +145,20 @@ int cuda_fail(nemo_ctx* c, cudaError_t e, const char* what) {
 // Before the context stream runs work: wait for the pending host copies (the work
 // reads uploaded fields and may overwrite fields being downloaded).
 int join_copies(nemo_ctx* c) {
-  if (c->up_pending) {
-    CK(cudaStreamWaitEvent(c->stream, c->ev_up, 0), "wait for uploads");
-    c->up_pending = false;
-  }
-  if (c->down_pending) {
-    CK(cudaStreamWaitEvent(c->stream, c->ev_down, 0), "wait for downloads");
-    c->down_pending = false;
+  for (int k = 0; k < nemo_ctx::NUP; ++k)
+    if (c->up_pending[k]) {
+      CK(cudaStreamWaitEvent(c->stream, c->ev_up[k], 0), "wait for uploads");
+      c->up_pending[k] = false;
+    }
+  bool any = false;
+  for (int k = 0; k < nemo_ctx::NDOWN; ++k)
+    if (c->down_pending[k]) {
+      CK(cudaStreamWaitEvent(c->stream, c->ev_down[k], 0), "wait for downloads");
+      c->down_pending[k] = false;
+      any = true;
+    }
+  if (any)
     for (bool& b : c->field_pending) b = false;
-  }
   return NEMO_OK;
 }
 
@@ -748,20 +758,34 @@ int run_hotpath(nemo_ctx* c, int kt) {
     cudaEventRecord(c->kc.ev[0], c->stream);
   }
   mark(0);
+  const bool fused = nm.ln_traldf_iso && !c->no_fusion;
+  LdfArgs<T> la{};
+  // The iso-neutral fluxes read tsb and the slopes only, and dyn_spg_ts touches
+  // neither them nor their outputs: outside per-kernel timing they run on the side
+  // stream beside dyn_spg_ts and join before FCT stage c adds their divergence.
+  const bool overlap = fused && !c->timing;
+  if (fused) {
+    int s = iso_args<T>(c, kt, nm.nit000, F[NEMO_F_AHTU], F[NEMO_F_AHTV], F[NEMO_F_GTSU], F[NEMO_F_GTSV],
+                        F[NEMO_F_TSB], F[NEMO_F_TSB], F[NEMO_F_TSA], 2, 1, &la);
+    if (s) return s;
+    if (overlap) {
+      CK(cudaEventRecord(c->ev_fork, c->stream), "fork");
+      CK(cudaStreamWaitEvent(c->side, c->ev_fork, 0), "fork");
+      CK(launch_iso_flux<T>(dom_now<T>(c), la, c->side), "iso fluxes");
+      CK(cudaEventRecord(c->ev_join, c->side), "join");
+    }
+  }
   int s = run_spg<T>(c, kt);
   if (s) return s;
   mark(1);
   const double r2dt = (nm.neuler == 0 && kt == nm.nit000) ? nm.rn_rdt : 2.0 * nm.rn_rdt;
-  if (nm.ln_traldf_iso && !c->no_fusion) {
+  if (fused) {
     // tsa = 0, tra_adv and tra_ldf (iso-neutral, first pass): the iso-neutral
-    // fluxes first, then the three FCT stages; the last adds both the corrected
+    // fluxes, then the three FCT stages; the last adds both the corrected
     // advective trend and the iso-neutral divergence of each point, in the
     // reference's order
-    LdfArgs<T> la{};
-    s = iso_args<T>(c, kt, nm.nit000, F[NEMO_F_AHTU], F[NEMO_F_AHTV], F[NEMO_F_GTSU], F[NEMO_F_GTSV],
-                    F[NEMO_F_TSB], F[NEMO_F_TSB], F[NEMO_F_TSA], 2, 1, &la);
-    if (s) return s;
-    CK(launch_iso_flux<T>(dom_now<T>(c), la, c->stream), "iso fluxes");
+    if (overlap) CK(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "join");
+    else CK(launch_iso_flux<T>(dom_now<T>(c), la, c->stream), "iso fluxes");
     s = run_fct<T>(c, r2dt, F[NEMO_F_UN], F[NEMO_F_VN], F[NEMO_F_WN], 1, F[NEMO_F_TSB], F[NEMO_F_TSN], nullptr,
                    F[NEMO_F_TSA], 2, 2, 2, &la);
     if (s) return s;
@@ -834,11 +858,17 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return bad(NEMO_ERR_CUDA);
     c->own_stream = true;
   }
-  if (cudaStreamCreateWithFlags(&c->h2d, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&c->d2h, cudaStreamNonBlocking) != cudaSuccess)
-    return bad(NEMO_ERR_CUDA);
-  for (cudaEvent_t* e : {&c->ev_main, &c->ev_up, &c->ev_down})
+  for (auto& st : c->h2d)
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return bad(NEMO_ERR_CUDA);
+  for (auto& st : c->d2h)
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return bad(NEMO_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess) return bad(NEMO_ERR_CUDA);
+  for (cudaEvent_t* e : {&c->ev_main, &c->ev_fork, &c->ev_join})
     if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return bad(NEMO_ERR_CUDA);
+  for (auto& e : c->ev_up)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return bad(NEMO_ERR_CUDA);
+  for (auto& e : c->ev_down)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return bad(NEMO_ERR_CUDA);
   for (auto& e : c->ev_field)
     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return bad(NEMO_ERR_CUDA);
   int s = derive_domain(c, dm);
@@ -912,12 +942,19 @@ int nemo_gpu_destroy(nemo_ctx* c) {
     if (e) cudaEventDestroy(e);
   for (auto e : c->kc.ev)
     if (e) cudaEventDestroy(e);
-  for (cudaEvent_t e : {c->ev_main, c->ev_up, c->ev_down})
+  for (cudaEvent_t e : {c->ev_main, c->ev_fork, c->ev_join})
     if (e) cudaEventDestroy(e);
+  for (auto e : c->ev_up)
+    if (e) cudaEventDestroy(e);
+  for (auto e : c->ev_down)
+    if (e) cudaEventDestroy(e);
+  if (c->side) cudaStreamDestroy(c->side);
   for (auto e : c->ev_field)
     if (e) cudaEventDestroy(e);
-  if (c->h2d) cudaStreamDestroy(c->h2d);
-  if (c->d2h) cudaStreamDestroy(c->d2h);
+  for (auto st : c->h2d)
+    if (st) cudaStreamDestroy(st);
+  for (auto st : c->d2h)
+    if (st) cudaStreamDestroy(st);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return NEMO_OK;
@@ -927,9 +964,10 @@ const char* nemo_gpu_last_error(const nemo_ctx* c) { return c ? c->err.c_str() :
 
 int nemo_gpu_synchronize(nemo_ctx* c) {
   if (!c) return NEMO_ERR_ARG;
-  CK(cudaStreamSynchronize(c->h2d), "synchronize");
-  CK(cudaStreamSynchronize(c->d2h), "synchronize");
-  c->up_pending = c->down_pending = false;
+  for (auto st : c->h2d) CK(cudaStreamSynchronize(st), "synchronize");
+  for (auto st : c->d2h) CK(cudaStreamSynchronize(st), "synchronize");
+  for (bool& b : c->up_pending) b = false;
+  for (bool& b : c->down_pending) b = false;
   for (bool& b : c->field_pending) b = false;
   CK(cudaStreamSynchronize(c->stream), "synchronize");
   int flag = 0;
@@ -973,12 +1011,14 @@ int nemo_gpu_field_upload(nemo_ctx* c, int id, const void* host) {
   if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "field_upload: field %d is not bound", id);
   size_t bytes = field_numel(c, id) * c->nmem * (nemo_gpu_field_is_fp64(c, id) ? 8 : 4);
   // after the work already queued (it may read the field) and the field's download
+  const int k = id % nemo_ctx::NUP;  // a field always on the same stream: uploads of it stay ordered
+  cudaStream_t st = c->h2d[k];
   CK(cudaEventRecord(c->ev_main, c->stream), "field_upload");
-  CK(cudaStreamWaitEvent(c->h2d, c->ev_main, 0), "field_upload");
-  if (c->field_pending[id]) CK(cudaStreamWaitEvent(c->h2d, c->ev_field[id], 0), "field_upload");
-  CK(cudaMemcpyAsync(c->f[id], host, bytes, cudaMemcpyHostToDevice, c->h2d), "field_upload");
-  CK(cudaEventRecord(c->ev_up, c->h2d), "field_upload");
-  c->up_pending = true;
+  CK(cudaStreamWaitEvent(st, c->ev_main, 0), "field_upload");
+  if (c->field_pending[id]) CK(cudaStreamWaitEvent(st, c->ev_field[id], 0), "field_upload");
+  CK(cudaMemcpyAsync(c->f[id], host, bytes, cudaMemcpyHostToDevice, st), "field_upload");
+  CK(cudaEventRecord(c->ev_up[k], st), "field_upload");
+  c->up_pending[k] = true;
   return NEMO_OK;
 }
 
@@ -987,14 +1027,17 @@ int nemo_gpu_field_download(nemo_ctx* c, int id, void* host) {
   if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "field_download: field %d is not bound", id);
   size_t bytes = field_numel(c, id) * c->nmem * (nemo_gpu_field_is_fp64(c, id) ? 8 : 4);
   // after the work already queued and any pending upload
+  const int k = id % nemo_ctx::NDOWN;
+  cudaStream_t st = c->d2h[k];
   CK(cudaEventRecord(c->ev_main, c->stream), "field_download");
-  CK(cudaStreamWaitEvent(c->d2h, c->ev_main, 0), "field_download");
-  if (c->up_pending) CK(cudaStreamWaitEvent(c->d2h, c->ev_up, 0), "field_download");
-  CK(cudaMemcpyAsync(host, c->f[id], bytes, cudaMemcpyDeviceToHost, c->d2h), "field_download");
-  CK(cudaEventRecord(c->ev_field[id], c->d2h), "field_download");
-  CK(cudaEventRecord(c->ev_down, c->d2h), "field_download");
+  CK(cudaStreamWaitEvent(st, c->ev_main, 0), "field_download");
+  for (int u = 0; u < nemo_ctx::NUP; ++u)
+    if (c->up_pending[u]) CK(cudaStreamWaitEvent(st, c->ev_up[u], 0), "field_download");
+  CK(cudaMemcpyAsync(host, c->f[id], bytes, cudaMemcpyDeviceToHost, st), "field_download");
+  CK(cudaEventRecord(c->ev_field[id], st), "field_download");
+  CK(cudaEventRecord(c->ev_down[k], st), "field_download");
   c->field_pending[id] = true;
-  c->down_pending = true;
+  c->down_pending[k] = true;
   return NEMO_OK;
 }
 
