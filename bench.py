@@ -60,10 +60,14 @@ KERNEL_BYTES_2D = {
 }
 
 
-# DRAM bytes (read + write) per launch from one ncu capture of the kernel on this
-# workload: (kernel, precision, nn_GYRE) -> bytes; filled in from the committed
-# ncu summaries
-TRAFFIC = {}
+# DRAM bytes (read + write) per launch from one ncu capture of the DRAM counters of
+# this workload's nn_GYRE=15 case, scaled to nn_GYRE=25 by the cell ratio (every
+# kernel's traffic is proportional to its cells).
+# (kernel, precision, nn_GYRE) -> bytes
+TRAFFIC = {(k, "mixed", 25): v * 1e6 for k, v in {
+    "spg_p2": 59.2, "iso_flux": 541.1, "fct_c": 895.2, "fct_a": 675.9, "fct_b": 590.5, "zdf_imp": 279.7,
+    "spg_p3": 219.8, "spg_p1a": 96.7, "spg_p1b": 36.2, "iso_akz_edges": 6.8}.items()}
+TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, nn_GYRE=15 capture scaled by cells"
 
 
 def peaks():
@@ -330,6 +334,7 @@ def run_gpu(args):
         "clocks": ck, "gpu_launches": int(round(launches_per_step * args.steps)),
         "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm if achieved else None, "traffic": TRAFFIC.get((top, args.prec, args.nn)),
+                     "traffic_source": TRAFFIC_SOURCE if (top, args.prec, args.nn) in TRAFFIC else None,
                      "peak_source": src, "alg_bytes_per_launch": alg_bytes,
                      "duration_us": kernels[top]["us"]},
         "kernels": kernels,
