@@ -66,7 +66,7 @@ __device__ __forceinline__ PtIdx pt_index(const Dom<T>& d) {
 // k-march kernels: grid x = i, y = j, z = member * nchunk + chunk. A thread walks
 // the levels k0..k1 of one column (KCH levels per chunk), keeping in registers what
 // level k+1 shares with level k, so the vertical neighbours are loaded once.
-constexpr int KCH = 8;
+constexpr int KCH = 16;
 struct KIdx {
   int i, j, m, k0, k1;
   long ij;
