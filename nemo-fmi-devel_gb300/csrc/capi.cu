@@ -82,6 +82,7 @@ struct nemo_ctx {
   long long bar_spins = 4000000;
   int bar_extra = 0;
   int p2_blocks = 0;
+  int p2_cache = 0;  // the sub-step kernel keeps its constants in shared memory
   double* gs_part = nullptr;
   double* gs_out = nullptr;
   int gs_nblk = 0;
@@ -722,6 +723,7 @@ int run_spg(nemo_ctx* c, int kt) {
   a.ring_ssh = (T*)c->ring[0]; a.ring_u = (T*)c->ring[1]; a.ring_v = (T*)c->ring[2];
   a.fx = (T*)c->spg_x[0]; a.fy = (T*)c->spg_x[1];
   a.du = (T*)c->spg_x[2]; a.dv = (T*)c->spg_x[3]; a.cu = (T*)c->spg_x[4]; a.cv = (T*)c->spg_x[5];
+  a.cache = c->p2_cache;
   a.ff = c->spg_ff;
   a.wgt1 = c->d_wgt1; a.wgt2 = c->d_wgt2; a.wgtf = c->d_wgtf; a.nwgt = (int)c->wgt1.size();
   a.ln_bt_fw = nm.ln_bt_fw; a.ln_apr_dyn = nm.ln_apr_dyn; a.nvor = nm.nvor_scheme; a.ll_init = ll_init;
@@ -906,11 +908,19 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
   if (cudaMalloc(&c->err_flag, sizeof(int)) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
   cudaMemset(c->bar_mem, 0, 2 * sizeof(unsigned int));
   cudaMemset(c->err_flag, 0, sizeof(int));
-  const int bps = prec == NEMO_PREC_FP64 ? spg_p2_blocks_per_sm<double>() : spg_p2_blocks_per_sm<float>();
-  // one block per 32 x 8 tile of the sub-step kernel, at most all co-resident
-  long need = (long)((c->jpi + 31) / 32) * ((c->jpj + 7) / 8) * c->nmem;
-  long maxb = (long)bps * c->nsm;
-  c->p2_blocks = (int)(need < maxb ? need : maxb);
+  // one block per 32 x 8 tile of the sub-step kernel, at most all co-resident; the
+  // mixed form with the ENE/MIX scheme keeps its constants in shared memory when no
+  // block owns more than P2_MAXT tiles
+  const long need = (long)((c->jpi + 31) / 32) * ((c->jpj + 7) / 8) * c->nmem;
+  auto p2_grid = [&](int cache) {
+    const int bps = prec == NEMO_PREC_FP64 ? spg_p2_blocks_per_sm<double>(0) : spg_p2_blocks_per_sm<float>(cache);
+    const long maxb = (long)bps * c->nsm;
+    c->p2_blocks = (int)(need < maxb ? need : maxb);
+    c->p2_cache = cache;
+  };
+  const int nv = c->nam.nvor_scheme;
+  p2_grid(prec != NEMO_PREC_FP64 && (nv == 1 || nv == 5) ? 1 : 0);
+  if (c->p2_cache && (c->p2_blocks < 1 || need > (long)c->p2_blocks * P2_MAXT)) p2_grid(0);
   if (c->p2_blocks < 1) return bad(NEMO_ERR_CUDA);
   c->gs_nblk = c->nsm * 4;
   if (cudaMalloc(&c->gs_part, 2 * (size_t)c->gs_nblk * c->nmem * 8) != cudaSuccess) return bad(NEMO_ERR_NOMEM);

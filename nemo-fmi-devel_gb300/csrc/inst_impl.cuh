@@ -120,10 +120,16 @@ cudaError_t launch_clamp(T* x, long n, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// co-resident blocks per SM of the sub-step kernel, with or without the constant
+// cache (dynamic shared memory beyond the 48 KB default needs the opt-in)
 template <class T>
-int spg_p2_blocks_per_sm() {
+int spg_p2_blocks_per_sm(int cache) {
+  const size_t dyn = cache ? P2_CACHE_BYTES : 0;
+  if (cache &&
+      cudaFuncSetAttribute(k_spg_p2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess)
+    return 0;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_spg_p2<T>, 256, 0) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_spg_p2<T>, 256, dyn) != cudaSuccess) return 0;
   return nb;
 }
 
@@ -143,7 +149,7 @@ cudaError_t launch_spg(const Dom<T>& d, const SpgArgs<T>& a, const GridBar& bar,
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(p2_blocks);
   cfg.blockDim = dim3(256);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = a.cache ? P2_CACHE_BYTES : 0;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
@@ -186,7 +192,7 @@ cudaError_t launch_globsum(const T* x, const double* tmask_i, long n2, int nk, i
   template cudaError_t launch_iso_flux<T>(const Dom<T>&, const LdfArgs<T>&, cudaStream_t);                   \
   template cudaError_t launch_clamp<T>(T*, long, cudaStream_t);                                              \
   template cudaError_t launch_spg<T>(const Dom<T>&, const SpgArgs<T>&, const GridBar&, int, cudaStream_t);   \
-  template int spg_p2_blocks_per_sm<T>();                                                                    \
+  template int spg_p2_blocks_per_sm<T>(int);                                                                 \
   template cudaError_t launch_lbc<T>(T*, int, int, long, int, T, cudaStream_t);                              \
   template cudaError_t launch_globsum<T>(const T*, const double*, long, int, int, double*, int, double*, cudaStream_t);
 

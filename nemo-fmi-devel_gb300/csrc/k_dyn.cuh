@@ -39,6 +39,7 @@ struct SpgArgs {
   RO<float> wgtf;                 // mixed form: wgt1 hi | wgt1 lo | wgt2, nwgt entries each
   int nwgt;
   int ln_bt_fw, ln_apr_dyn, nvor, ll_init, icycle, ring0, phase3_filter;
+  int cache;  // mixed form, ENE/MIX: the sub-step constants cached in shared memory
   T rdtbt, grav, r1_rau0, scal_load, rn_bt_alpha;
   double rn_atfp, r1_2dt_b;
 };
@@ -292,6 +293,10 @@ __device__ __forceinline__ void am4(int jn, int ll_init, T alpha, T& za0, T& za1
 // their un_adv / vn_adv sums (:860-862). Reads and writes of one sub-step never
 // touch the same ring slot or flux buffer, so one barrier separates sub-steps.
 constexpr int P2_TX = 32, P2_TY = 8;
+// Constant cache of the mixed form (ENE/MIX vorticity): P2_NC floats per point of
+// each of up to P2_MAXT tiles a block owns, in dynamic shared memory.
+constexpr int P2_NC = 16, P2_MAXT = 3;
+constexpr size_t P2_CACHE_BYTES = (size_t)P2_NC * P2_MAXT * 256 * sizeof(float);
 
 // The time-filter sums of the sub-steps (ssha, ua_b, va_b :1202-1204; un_adv,
 // vn_adv :860-862). FP64 form: the reference's FP64 accumulation. Mixed form: each
@@ -384,6 +389,47 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
         predictor(1, r, m2 + p, p);
       }
     }
+  // Mixed form with the ENE/MIX scheme: the per-point constants of the Coriolis,
+  // drag, pressure-gradient and predictor terms, combined once and kept in shared
+  // memory for the whole kernel (the barrier's acquire empties L1 every sub-step, so
+  // they would otherwise come from L2 after each tile's __syncthreads). Each thread
+  // writes and reads only its own entries. FP32 products in another association than
+  // the general path below: within the mixed form's tolerance.
+  extern __shared__ float p2c[];
+  const bool cache = sizeof(T) == 4 && a.cache;
+  if (cache) {
+    int slot = 0;
+    for (int t = blockIdx.x; t < ntile && slot < P2_MAXT; t += gridDim.x, ++slot) {
+      int m2, i0, j0;
+      tile(t, m2, i0, j0);
+      const int i = i0 + tx, j = j0 + ty;
+      float cv[P2_NC] = {};
+      if (i <= jpi && j <= jpj) {
+        const int p = (i - 1) + (j - 1) * jpi, g = m2 + p;
+        if (interior(i, j)) {
+          const float su = (float)(T(1) - a.scal_load) * (float)(-grav);
+          cv[0] = 0.25f * (float)d.zwz[p - jpi] * (float)d.r1_e1u[p];  // times fy(p-jpi) + fy(p+1-jpi)
+          cv[1] = 0.25f * (float)d.zwz[p] * (float)d.r1_e1u[p];        // times fy(p) + fy(p+1)
+          cv[2] = -0.25f * (float)d.zwz[p - 1] * (float)d.r1_e2v[p];   // times fx(p-1) + fx(p-1+jpi)
+          cv[3] = -0.25f * (float)d.zwz[p] * (float)d.r1_e2v[p];       // times fx(p) + fx(p+jpi)
+          cv[4] = (float)zCdU_u[g] * (float)d.r1_hu_0[p];
+          cv[5] = (float)zCdU_v[g] * (float)d.r1_hv_0[p];
+          cv[6] = su * (float)d.r1_e1u[p];
+          cv[7] = su * (float)d.r1_e2v[p];
+          cv[8] = (float)zu_frc[g];
+          cv[9] = (float)zv_frc[g];
+          cv[10] = (float)d.ssumask[p];
+          cv[11] = (float)d.ssvmask[p];
+        }
+        cv[12] = (float)d.e2u[p] * (float)d.hu_0[p];
+        cv[13] = (float)d.e1v[p] * (float)d.hv_0[p];
+        cv[14] = (float)d.r1_e2u[p];
+        cv[15] = (float)d.r1_e1v[p];
+      }
+#pragma unroll
+      for (int cc = 0; cc < P2_NC; ++cc) p2c[(cc * P2_MAXT + slot) * 256 + threadIdx.x] = cv[cc];
+    }
+  }
   if (!grid_barrier(bar)) return;
   for (int jn = 1; jn <= a.icycle; ++jn) {
     const int sn = r & 3, sb = (r + 1) & 3, sbb = (r + 2) & 3, sa = (r + 3) & 3;
@@ -399,7 +445,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
     }
     T zb0, zb1, zb2, zb3;
     am4(jn, a.ll_init, a.rn_bt_alpha, zb0, zb1, zb2, zb3);
-    for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
+    int slot = 0;  // the tile's place in the constant cache
+    for (int t = blockIdx.x; t < ntile; t += gridDim.x, ++slot) {
       int m2, i0, j0;
       tile(t, m2, i0, j0);
       // Every value this tile reads that the sub-step does not produce is loaded
@@ -497,7 +544,18 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
       // then the predictor of sub-step jn+1 (:724-800) and its sums (:860-862)
       if (own) {
         T ua_e = T(0), va_e = T(0);
-        if (inner) {
+        // the cached constants of this point: C[c * P2_MAXT * 256]
+        const float* C = p2c + slot * 256 + threadIdx.x;
+        constexpr int CS = P2_MAXT * 256;
+        if (inner && cache) {
+          const T s0 = zs_s[ty][tx];
+          const T zu_trd = C[0] * (y[0] + y[1]) + C[CS] * (y[2] + y[3]) + C[4 * CS] * un_e;
+          const T zv_trd = C[2 * CS] * (x[0] + x[2]) + C[3 * CS] * (x[1] + x[3]) + C[5 * CS] * vn_e;
+          const T wxs = C[6 * CS] * (zs_s[ty][tx + 1] - s0);
+          const T wys = C[7 * CS] * (zs_s[ty + 1][tx] - s0);
+          ua_e = (un_e + rdtbt * (wxs + zu_trd + C[8 * CS])) * C[10 * CS];
+          va_e = (vn_e + rdtbt * (wys + zv_trd + C[9 * CS])) * C[11 * CS];
+        } else if (inner) {
           const T z1_hu = d.ssumask[p] / (d.hu_0[p] + T(1) - d.ssumask[p]);
           const T z1_hv = d.ssvmask[p] / (d.hv_0[p] + T(1) - d.ssvmask[p]);
           T zu_trd, zv_trd;
@@ -531,8 +589,10 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
           ab3(jn + 1, a.ll_init, za1, za2, za3);
           const T uex = za1 * ua_e + za2 * un_e + za3 * ub_e;
           const T vex = za1 * va_e + za2 * vn_e + za3 * vb_e;
-          const T zwx = d.e2u[p] * uex * d.hu_0[p];
-          const T zwy = d.e1v[p] * vex * d.hv_0[p];
+          const T zwx = cache ? (T)C[12 * CS] * uex : d.e2u[p] * uex * d.hu_0[p];
+          const T zwy = cache ? (T)C[13 * CS] * vex : d.e1v[p] * vex * d.hv_0[p];
+          const T r1e2u = cache ? (T)C[14 * CS] : d.r1_e2u[p];
+          const T r1e1v = cache ? (T)C[15 * CS] : d.r1_e1v[p];
           a.fx[((jn + 1) & 1) * nmem2 + g] = zwx;
           a.fy[((jn + 1) & 1) * nmem2 + g] = zwy;
           T w2;
@@ -542,8 +602,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
             a.un_adv[g] = acc_au + (double)(w2 * zwx * d.r1_e2u[p]);
             a.vn_adv[g] = acc_av + (double)(w2 * zwy * d.r1_e1v[p]);
           } else {
-            ff_add(f_au, w2 * zwx * d.r1_e2u[p], 0.0f);
-            ff_add(f_av, w2 * zwy * d.r1_e1v[p], 0.0f);
+            ff_add(f_au, w2 * zwx * r1e2u, 0.0f);
+            ff_add(f_av, w2 * zwy * r1e1v, 0.0f);
             a.ff[ffi(3, 0, nmem2, g)] = f_au.h;
             a.ff[ffi(3, 1, nmem2, g)] = f_au.l;
             a.ff[ffi(4, 0, nmem2, g)] = f_av.h;
