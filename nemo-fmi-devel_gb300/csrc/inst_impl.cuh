@@ -85,7 +85,7 @@ cudaError_t launch_iso_flux(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s
 // levels 1 and jpk; row and column 1 of the MSC correction)
 template <class T>
 cudaError_t launch_iso_edges(const Dom<T>& d, const LdfArgs<T>& a, int copy_akz_edges, int msc_edges, cudaStream_t s) {
-  if (copy_akz_edges) {
+  if (copy_akz_edges && !hot_iso_ok(d, a)) {  // the specialised flux kernel copies them itself
     k_iso_akz_copy_edges<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
     ktick(NEMO_K_ISO_AKZ_EDGES, s);
   }

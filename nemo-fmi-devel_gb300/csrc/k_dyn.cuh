@@ -76,43 +76,6 @@ __global__ void k_spg_p1a(Dom<T> d, SpgArgs<T> a) {
     }
 }
 
-// Phase 1a for FP32 and jpk = NK known at compile time: the column of ua / va is
-// loaded whole into registers, summed in the reference's order, then corrected and
-// stored, so each value is read once and all loads are in flight together.
-template <int NK>
-__global__ void __launch_bounds__(128) k_spg_p1a_reg(Dom<float> d, SpgArgs<float> a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int m = blockIdx.z;
-  if (i > d.jpi || j > d.jpj) return;
-  const long ij = pt_ij(d, i, j), n2 = d.n2, m2 = (long)m * n2;
-  const ColInfo ci = d.ci[ij];
-  float* ua = a.ua + (long)m * d.n3 + ij;
-  float* va = a.va + (long)m * d.n3 + ij;
-  float u[NK - 1], v[NK - 1];
-#pragma unroll
-  for (int k = 1; k <= NK - 1; ++k) {
-    u[k - 1] = ua[(k - 1) * n2];
-    v[k - 1] = va[(k - 1) * n2];
-  }
-  float su = 0.f, sv = 0.f;
-#pragma unroll
-  for (int k = 1; k <= NK - 1; ++k) {
-    su = su + d.e3u_n(ij, k, m) * u[k - 1] * umsk<float>(ci, k);
-    sv = sv + d.e3v_n(ij, k, m) * v[k - 1] * vmsk<float>(ci, k);
-  }
-  su = su * d.r1_hu_0[ij];
-  sv = sv * d.r1_hv_0[ij];
-  a.zu_frc[m2 + ij] = su;
-  a.zv_frc[m2 + ij] = sv;
-  if (i >= 2 && i <= d.jpi - 1 && j >= 2 && j <= d.jpj - 1)
-#pragma unroll
-    for (int k = 1; k <= NK - 1; ++k) {
-      ua[(k - 1) * n2] = u[k - 1] - su * umsk<float>(ci, k);
-      va[(k - 1) * n2] = v[k - 1] - sv * vmsk<float>(ci, k);
-    }
-}
-
 // Barotropic Coriolis trend of a flux field (ENE/MIX, ENS, EET/EEN, ENT) at an
 // interior point (:390-443 and :1000-1056). Every scheme reads the same eight
 // neighbours, passed preloaded: x[0..3] = zwx at p-1, p, p-1+jpi, p+jpi and
@@ -165,11 +128,7 @@ __device__ __forceinline__ void nby(F f, long p, int jpi, T (&y)[4]) {
 // Phase 1b (:387-702): Coriolis of the now barotropic flow, bottom stress, wind,
 // atmospheric pressure, ssh forcing, initial barotropic levels, zeroed sums.
 template <class T>
-__global__ void k_spg_p1b(Dom<T> d, SpgArgs<T> a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int m = blockIdx.z;
-  if (i > d.jpi || j > d.jpj) return;
+__device__ __forceinline__ void spg_p1b_point(const Dom<T>& d, const SpgArgs<T>& a, int i, int j, int m) {
   const long p = pt_ij(d, i, j), n2 = d.n2, m2 = (long)m * n2, m3 = (long)m * d.n3;
   const T r1_2 = T(0.5);
   const bool interior = i >= 2 && i <= d.jpi - 1 && j >= 2 && j <= d.jpj - 1;
@@ -260,6 +219,52 @@ __global__ void k_spg_p1b(Dom<T> d, SpgArgs<T> a) {
   a.ua_b[m2 + p] = 0.0; a.va_b[m2 + p] = 0.0; a.ssha[m2 + p] = 0.0;
   a.un_adv[m2 + p] = 0.0; a.vn_adv[m2 + p] = 0.0;
 }
+
+template <class T>
+__global__ void k_spg_p1b(Dom<T> d, SpgArgs<T> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i > d.jpi || j > d.jpj) return;
+  spg_p1b_point(d, a, i, j, (int)blockIdx.z);
+}
+
+// Phase 1a for FP32 and jpk = NK known at compile time: the column of ua / va is
+// loaded whole into registers, summed in the reference's order, then corrected and
+// stored, so each value is read once and all loads are in flight together.
+template <int NK>
+__global__ void __launch_bounds__(128) k_spg_p1a_reg(Dom<float> d, SpgArgs<float> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int m = blockIdx.z;
+  if (i > d.jpi || j > d.jpj) return;
+  const long ij = pt_ij(d, i, j), n2 = d.n2, m2 = (long)m * n2;
+  const ColInfo ci = d.ci[ij];
+  float* ua = a.ua + (long)m * d.n3 + ij;
+  float* va = a.va + (long)m * d.n3 + ij;
+  float u[NK - 1], v[NK - 1];
+#pragma unroll
+  for (int k = 1; k <= NK - 1; ++k) {
+    u[k - 1] = ua[(k - 1) * n2];
+    v[k - 1] = va[(k - 1) * n2];
+  }
+  float su = 0.f, sv = 0.f;
+#pragma unroll
+  for (int k = 1; k <= NK - 1; ++k) {
+    su = su + d.e3u_n(ij, k, m) * u[k - 1] * umsk<float>(ci, k);
+    sv = sv + d.e3v_n(ij, k, m) * v[k - 1] * vmsk<float>(ci, k);
+  }
+  su = su * d.r1_hu_0[ij];
+  sv = sv * d.r1_hv_0[ij];
+  a.zu_frc[m2 + ij] = su;
+  a.zv_frc[m2 + ij] = sv;
+  if (i >= 2 && i <= d.jpi - 1 && j >= 2 && j <= d.jpj - 1)
+#pragma unroll
+    for (int k = 1; k <= NK - 1; ++k) {
+      ua[(k - 1) * n2] = u[k - 1] - su * umsk<float>(ci, k);
+      va[(k - 1) * n2] = v[k - 1] - sv * vmsk<float>(ci, k);
+    }
+}
+
 
 // Predictor (AB3) and AM4 coefficients of sub-step jn (:724-732, :904-928).
 template <class T>

@@ -32,11 +32,26 @@ template <class T>
 __device__ __forceinline__ T v_in(const ColInfo& c, int k) { return (k >= c.vlo && k <= c.vhi) ? T(1) : T(0); }
 
 // Iso-neutral fluxes (traldf_iso.F90:146-357) of one column chunk; see k_iso_flux.
+// It also sets akz = ah_wslp2 on the points k_iso_akz_copy_edges covers in general.
 template <class T>
 __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 3) k_iso_flux_hot(Dom<T> d, LdfArgs<T> a) {
   const KIdx c = k_index(d);
   if (!c.valid) return;
   const int jpi = d.jpi, jpj = d.jpj, jpk = d.jpk;
+  {  // akz = ah_wslp2 where the interior sweep writes neither (traldf_iso.F90:200-201):
+     // every level of the edge columns, levels 1 and jpk of the interior columns
+    const long base = (long)c.m * d.n3 + c.ij;
+    auto copy = [&](int k) {
+      const long q = base + (long)(k - 1) * d.n2;
+      a.akz[q] = a.ah_wslp2[q];
+    };
+    if (!c.interior) {
+      for (int k = c.k0; k <= c.k1; ++k) copy(k);
+    } else {
+      if (c.k0 == 1) copy(1);
+      if (c.k1 == jpk) copy(jpk);
+    }
+  }
   if (!(c.i <= jpi - 1 && c.j <= jpj - 1)) return;  // no face owned
   const int n2 = (int)d.n2, ij = (int)c.ij;
   const bool icol = c.interior;
