@@ -99,8 +99,14 @@ cudaError_t launch_iso_edges(const Dom<T>& d, const LdfArgs<T>& a, int copy_akz_
 template <class T>
 cudaError_t launch_zdf(const Dom<T>& d, const ZdfArgs<T>& a, cudaStream_t s) {
   if constexpr (sizeof(T) == 4) {
-    if (d.jpk == 31) {  // the GYRE levels: columns in registers
-      k_zdf_imp_reg<31><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+    if (d.jpk == 31) {  // the GYRE levels: columns staged in shared memory
+      static bool attr = false;  // dynamic shared memory beyond 48 KB needs the opt-in
+      constexpr int smem = 4 * 31 * BX * BY * sizeof(float);
+      if (!attr) {
+        cudaFuncSetAttribute(k_zdf_imp_async<31>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        attr = true;
+      }
+      k_zdf_imp_async<31><<<col_grid(d), dim3(BX, BY), smem, s>>>(d, a);
       ktick(NEMO_K_ZDF_IMP, s);
       return cudaGetLastError();
     }

@@ -919,61 +919,90 @@ __global__ void k_zdf_imp(Dom<T> d, ZdfArgs<T> a) {
   }
 }
 
-// FP32, jpk = NK known at compile time: each column is loaded whole into registers
-// before it is solved (all its loads in flight at once, no load waiting on a store),
-// then stored whole. The same elimination as k_zdf_imp with two register arrays:
-// zw(k) = zwi(k) (zws(k) is zwi(k+1): both are -p2dt zwt(k+1) / e3w(k+1)) and the
-// reciprocal pivots 1 / zwt(k).
+// Asynchronous 4-byte copy global -> shared (the thread waits for its own copies).
+__device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
+// FP32, jpk = NK known at compile time: the elimination of k_zdf_imp with two
+// arrays, zw(k) = zwi(k) (zws(k) is zwi(k+1): both are -p2dt zwt(k+1) / e3w(k+1))
+// and the reciprocal pivots 1 / zwt(k), and everything per column in shared memory: each thread copies the levels of its own column
+// (diffusivities, then ta and tb of each tracer) with asynchronous copies, all in
+// flight together and without registers, then solves from shared memory (pivots zw
+// and 1/zwt there too; the forward values overwrite ta). No block synchronisation:
+// a thread reads only what it wrote or copied. Dynamic shared memory:
+// 4 * NK * (threads per block) floats.
 template <int NK>
-__global__ void __launch_bounds__(128) k_zdf_imp_reg(Dom<float> d, ZdfArgs<float> a) {
+__global__ void __launch_bounds__(128, 3) k_zdf_imp_async(Dom<float> d, ZdfArgs<float> a) {
+  extern __shared__ float zsm[];
+  const int nt = blockDim.x * blockDim.y, t = threadIdx.y * blockDim.x + threadIdx.x;
+  float* sx = zsm + t;                // sx[(k-1) * nt]: ta, then the forward values
+  float* sb = zsm + NK * nt + t;      // sb[(k-1) * nt]: tb (first: the added coefficient)
+  float* zw = zsm + 2 * NK * nt + t;  // zw[(k-1) * nt] = zwi(k), k = 1..NK
+  float* rz = zsm + 3 * NK * nt + t;  // rz[(k-1) * nt] = 1 / zwt(k), k = 1..NK-1
   ColIdx<float> c = col_index(d);
   if (!c.valid || !c.interior) return;
-  constexpr int K1 = NK - 1;  // levels solved: 1..jpk-1
+  constexpr int K1 = NK - 1;
   const long n2 = d.n2, n3 = d.n3;
   const ColInfo ci = d.ci[c.ij];
   const long m3 = (long)c.m * n3;
   const float p2dt = a.p2dt;
-  float zw[NK + 1], rzwt[NK];
+  bool built = false, built_avt = false;
   for (int n = 0; n < a.kjpt; ++n) {
-    const bool build = (!a.is_trc && (n == 0 || (n == 1 && a.ddm))) || (a.is_trc && n == 0);
-    if (build) {
-      const RO<float> coef = (!a.is_trc && n == 0) ? a.avt : a.avs;
-      float wt[NK + 1];
-#pragma unroll
+    // zwt = avt (T; S without double diffusion) or avs (S with it, passive tracers)
+    const bool use_avt = !a.is_trc && (n == 0 || !a.ddm);
+    if (!built || use_avt != built_avt) {
+      const float* coef = (use_avt ? a.avt : a.avs).p + m3 + c.ij;
+      const float* add = a.add ? a.add.p + m3 + c.ij : nullptr;
       for (int k = 2; k <= NK; ++k) {
-        const long q = m3 + c.ij + (long)(k - 1) * n2;
-        wt[k] = coef[q];
-        if (a.add && k <= NK - 1) wt[k] = wt[k] + a.add[q];
+        cp_async4(sx + (k - 1) * nt, coef + (long)(k - 1) * n2);
+        if (add && k <= NK - 1) cp_async4(sb + (k - 1) * nt, add + (long)(k - 1) * n2);
       }
-      zw[1] = -p2dt * 0.0f / d.e3w_n(c.ij, 1, c.m);
-#pragma unroll
-      for (int k = 2; k <= NK; ++k) zw[k] = -p2dt * wt[k] / d.e3w_n(c.ij, k, c.m);
-      float g = 0.0f;
-#pragma unroll
+      cp_async_wait_all();
+      zw[0] = -p2dt * 0.0f / d.e3w_n(c.ij, 1, c.m);
+#pragma unroll 4
+      for (int k = 2; k <= NK; ++k) {
+        float wt = sx[(k - 1) * nt];
+        if (add && k <= NK - 1) wt = wt + sb[(k - 1) * nt];
+        zw[(k - 1) * nt] = -p2dt * wt / d.e3w_n(c.ij, k, c.m);
+      }
+      float g = 0.0f, rprev = 0.0f;
+#pragma unroll 4
       for (int k = 1; k <= K1; ++k) {
         const float e3a = d.e3t_a(c.ij, k, c.m);
-        g = (k == 1) ? e3a - zw[1] : e3a - zw[k] * (g * rzwt[k - 1]);
-        rzwt[k] = 1.0f / (g - zw[k + 1]);
+        const float zk = zw[(k - 1) * nt];
+        g = (k == 1) ? e3a - zk : e3a - zk * (g * rprev);
+        rprev = 1.0f / (g - zw[k * nt]);
+        rz[(k - 1) * nt] = rprev;
       }
+      built = true;
+      built_avt = use_avt;
     }
     const long mo = ((long)c.m * a.kjpt + n) * n3 + c.ij;
-    const RO<float> tb = a.ptb + mo;
+    const float* tb = a.ptb.p + mo;
     float* ta = a.pta + mo;
     const bool clamp = a.clamp_sal && !a.is_trc && n == 1;
-    float x[NK];
-#pragma unroll
-    for (int k = 1; k <= K1; ++k) x[k] = ta[(long)(k - 1) * n2];
-    float prev = 0.0f;
-#pragma unroll
     for (int k = 1; k <= K1; ++k) {
-      const float zrhs = d.e3t_b(c.ij, k, c.m) * tb[(long)(k - 1) * n2] + p2dt * d.e3t_n(c.ij, k, c.m) * x[k];
-      prev = (k == 1) ? zrhs : zrhs - zw[k] * rzwt[k - 1] * prev;
-      x[k] = prev;
+      cp_async4(sx + (k - 1) * nt, ta + (long)(k - 1) * n2);
+      cp_async4(sb + (k - 1) * nt, tb + (long)(k - 1) * n2);
+    }
+    cp_async_wait_all();
+    float prev = 0.0f;
+#pragma unroll 4
+    for (int k = 1; k <= K1; ++k) {
+      const float zrhs = d.e3t_b(c.ij, k, c.m) * sb[(k - 1) * nt] + p2dt * d.e3t_n(c.ij, k, c.m) * sx[(k - 1) * nt];
+      prev = (k == 1) ? zrhs : zrhs - zw[(k - 1) * nt] * rz[(k - 2) * nt] * prev;
+      sx[(k - 1) * nt] = prev;
     }
     float nxt = 0.0f;
-#pragma unroll
+#pragma unroll 4
     for (int k = K1; k >= 1; --k) {
-      nxt = (k == K1 ? x[k] : x[k] - zw[k + 1] * nxt) * rzwt[k] * tmsk<float>(ci, k);
+      const float xk = sx[(k - 1) * nt];
+      nxt = (k == K1 ? xk : xk - zw[k * nt] * nxt) * rz[(k - 1) * nt] * tmsk<float>(ci, k);
       ta[(long)(k - 1) * n2] = (clamp && nxt < 0.0f) ? 0.1f : nxt;
     }
   }

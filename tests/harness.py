@@ -21,10 +21,10 @@ def relerr(ref, got):
 class Pair:
     """Oracle(s) and a GPU context holding identical inputs."""
 
-    def __init__(self, nn=1, prec="fp64", nmem=1, seed=0, states=None, **nam_over):
+    def __init__(self, nn=1, prec="fp64", nmem=1, seed=0, states=None, jpk=31, **nam_over):
         from nemo_gpu import api
         from oracle import ora
-        self.dom = gyre.domain(nn)
+        self.dom = gyre.domain(nn, jpk=jpk)
         self.nam = gyre.namelist(**nam_over)
         self.nmem = nmem
         self.states = states or [gyre.state(self.dom, self.nam, seed=seed, member=m) for m in range(nmem)]

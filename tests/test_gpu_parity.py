@@ -276,6 +276,23 @@ def test_stp_hotpath(prec):
 
 
 @pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("jpk", [20, 46])
+def test_stp_hotpath_other_level_counts(prec, jpk):
+    """The hot path with jpk other than GYRE's 31: the general FP32 column kernels (the
+    register ones are compiled for 31 levels) and level chunks that split unevenly."""
+    p = Pair(nn=1, prec=prec, seed=14, jpk=jpk)
+    p.bind_hotpath()
+    for kt in (5, 6, 7):
+        for o in p.ora:
+            o.stp_hotpath(kt)
+        p.ctx.stp_hotpath(kt)
+        p.ctx.synchronize()
+    p.compare("TSA", p.s4, tol(prec, "field"))
+    p.compare("AH_WSLP2", p.s3, tol(prec, "field"))
+    _spg_compare(p, prec)
+
+
+@pytest.mark.parametrize("prec", PRECS)
 def test_ensemble_members(prec):
     """Three members in one context, member index outermost; each against its own oracle."""
     p = Pair(nn=1, prec=prec, seed=13, nmem=3)
