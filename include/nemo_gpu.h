@@ -146,6 +146,16 @@ enum nemo_field_id {
   NEMO_F_RNF, NEMO_F_RNF_B,            /* [S] runoff                                  */
   NEMO_F_RCDU_BOT,                     /* [S] bottom drag coefficient x |U|  zdfdrg   */
   NEMO_F_SSH_IB, NEMO_F_SSH_IBB,       /* [S] inverse-barometer ssh       sbcapr.F90  */
+  /* Variable volume (ln_linssh = 0) only, maintained by domvvl.F90 (:183-196,
+   * :631-661); with ln_linssh = 1 the rest-state ht_0, hu_0, ... and e3f_0 are used
+   * whether bound or not. */
+  NEMO_F_HT_N,                         /* [S] now ocean depth at T-points             */
+  NEMO_F_HU_N, NEMO_F_HV_N,            /* [S] now ocean depth at U-/V-points          */
+  NEMO_F_R1_HU_N, NEMO_F_R1_HV_N,      /* [S] their masked inverses                   */
+  NEMO_F_HU_B, NEMO_F_HV_B,            /* [S] before depths (centred integration or
+                                              flux-form momentum, ln_dynadv_vec = 0)   */
+  NEMO_F_R1_HU_B, NEMO_F_R1_HV_B,      /* [S] (centred integration)                   */
+  NEMO_F_E3F_N,                        /* [T] now e3 at F-points (ENE/ENS/MIX schemes) */
   NEMO_F_COUNT
 };
 
@@ -295,6 +305,7 @@ enum nemo_kernel_id {
   NEMO_K_ADV_TRP, NEMO_K_INTERP4, NEMO_K_FCT_A, NEMO_K_FCT_B, NEMO_K_FCT_C, NEMO_K_LDF_LAP,
   NEMO_K_ISO_FLUX, NEMO_K_ISO_DIV, NEMO_K_ISO_AKZ_EDGES, NEMO_K_ISO_MSC_EDGES, NEMO_K_ZDF_IMP,
   NEMO_K_CLAMP, NEMO_K_SPG_P1A, NEMO_K_SPG_P1B, NEMO_K_SPG_P2, NEMO_K_SPG_P3,
+  NEMO_K_SPG_COR,   /* variable volume: Coriolis factors of the step */
   NEMO_K_COUNT
 };
 

@@ -74,6 +74,7 @@ struct nemo_ctx {
   int iso_kjpt = 0;
   int fct_kjpt = 0;
   void* spg_w[5] = {};
+  void* spg_cor[5] = {};  // variable volume: Coriolis factors of each member
   void* ring[3] = {};
   void* spg_x[6] = {};  // fx (2 slots), fy (2 slots), du, dv, cu, cv
   float* spg_ff = nullptr;  // mixed form: compensated sub-step sums, 10 x nmem x n2
@@ -180,6 +181,7 @@ size_t field_numel(const nemo_ctx* c, int id) {
   switch (id) {
     case NEMO_F_TSB: case NEMO_F_TSN: case NEMO_F_TSA: return 2 * (size_t)c->n3;
     case NEMO_F_GTSU: case NEMO_F_GTSV: case NEMO_F_GTUI: case NEMO_F_GTVI: return 2 * (size_t)c->n2;
+    case NEMO_F_E3F_N: return (size_t)c->n3;
     default: break;
   }
   if (id >= NEMO_F_SSHB) return (size_t)c->n2;
@@ -329,7 +331,7 @@ int build_dom(nemo_ctx* c, DomStore<T>& st) {
   UP(e1e2t); UP(r1_e1e2t); UP(e2_e1u); UP(e1_e2v); UP(r1_e1e2u); UP(r1_e1e2v);
   UP(ht_0); UP(hu_0); UP(hv_0); UP(r1_hu_0); UP(r1_hv_0);
   UP(ssmask); UP(ssumask); UP(ssvmask);
-  UP(ff_t); UP(zwz); UP(ftne); UP(ftnw); UP(ftse); UP(ftsw);
+  UP(ff_t); UP(ff_f); UP(zwz); UP(ftne); UP(ftnw); UP(ftse); UP(ftsw);
 #undef UP
   {
     void* p = nullptr;
@@ -682,6 +684,18 @@ int run_spg(nemo_ctx* c, int kt) {
       if (!F[id]) return fail(c, NEMO_ERR_UNBOUND, "dyn_spg_ts (ln_bt_fw=F): field %d must be bound", id);
   if (nm.ln_apr_dyn && (!F[NEMO_F_SSH_IB] || (!nm.ln_bt_fw && !F[NEMO_F_SSH_IBB])))
     return fail(c, NEMO_ERR_UNBOUND, "dyn_spg_ts (ln_apr_dyn): ssh_ib must be bound");
+  const int vvl = !nm.ln_linssh, flux = vvl && !nm.ln_dynadv_vec;
+  const int sc = nm.nvor_scheme;
+  if (vvl) {
+    for (int id : {NEMO_F_HT_N, NEMO_F_HU_N, NEMO_F_HV_N, NEMO_F_R1_HU_N, NEMO_F_R1_HV_N})
+      if (!F[id]) return fail(c, NEMO_ERR_UNBOUND, "dyn_spg_ts (ln_linssh=F): depth field %d must be bound", id);
+    if ((sc == NEMO_VOR_ENE || sc == NEMO_VOR_ENS || sc == NEMO_VOR_MIX) && !F[NEMO_F_E3F_N])
+      return fail(c, NEMO_ERR_UNBOUND, "dyn_spg_ts (ln_linssh=F): e3f_n must be bound");
+    if ((!nm.ln_bt_fw || flux) && (!F[NEMO_F_HU_B] || !F[NEMO_F_HV_B]))
+      return fail(c, NEMO_ERR_UNBOUND, "dyn_spg_ts (ln_linssh=F): hu_b, hv_b must be bound");
+    if (!nm.ln_bt_fw && (!F[NEMO_F_R1_HU_B] || !F[NEMO_F_R1_HV_B]))
+      return fail(c, NEMO_ERR_UNBOUND, "dyn_spg_ts (ln_linssh=F, ln_bt_fw=F): r1_hu_b, r1_hv_b must be bound");
+  }
   // kt-dependent scalars (:185-216, :346-349)
   const double z2dt_bf = (kt == nm.nit000 && nm.neuler == 0) ? nm.rn_rdt : 2.0 * nm.rn_rdt;
   int ll_init = nm.ln_bt_av;
@@ -736,8 +750,26 @@ int run_spg(nemo_ctx* c, int kt) {
   a.rdtbt = (T)c->rdtbt; a.grav = (T)nm.grav; a.r1_rau0 = (T)(1.0 / nm.rau0);
   a.scal_load = (T)nm.rn_scal_load; a.rn_bt_alpha = (T)nm.rn_bt_alpha;
   a.rn_atfp = nm.rn_atfp; a.r1_2dt_b = 1.0 / z2dt_bf;
+  // depths and Coriolis factors: the domain's rest state, or the bound fields and
+  // the per-member factors of this step with a variable volume
+  const Dom<T> dn = dom_now<T>(c);
+  a.vvl = vvl; a.flux = flux; a.een_e3f = nm.nn_een_e3f; a.sco = nm.ln_sco;
+  a.hs = vvl ? c->n2 : 0;
+  a.ht_n = dn.ht_0; a.hu_n = dn.hu_0; a.hv_n = dn.hv_0; a.r1_hu_n = dn.r1_hu_0; a.r1_hv_n = dn.r1_hv_0;
+  a.hu_b = dn.hu_0; a.hv_b = dn.hv_0; a.r1_hu_b = dn.r1_hu_0; a.r1_hv_b = dn.r1_hv_0;
+  a.zwz = dn.zwz; a.ftne = dn.ftne; a.ftnw = dn.ftnw; a.ftse = dn.ftse; a.ftsw = dn.ftsw;
+  if (vvl) {
+    auto ro = [&](int id) { return RO<T>((const T*)F[id]); };
+    a.ht_n = ro(NEMO_F_HT_N); a.hu_n = ro(NEMO_F_HU_N); a.hv_n = ro(NEMO_F_HV_N);
+    a.r1_hu_n = ro(NEMO_F_R1_HU_N); a.r1_hv_n = ro(NEMO_F_R1_HV_N);
+    a.hu_b = ro(NEMO_F_HU_B); a.hv_b = ro(NEMO_F_HV_B); a.r1_hu_b = ro(NEMO_F_R1_HU_B); a.r1_hv_b = ro(NEMO_F_R1_HV_B);
+    a.e3f_n = ro(NEMO_F_E3F_N);
+    for (int w = 0; w < 5; ++w) a.cor_w[w] = (T*)c->spg_cor[w];
+    a.zwz = (const T*)c->spg_cor[0]; a.ftne = (const T*)c->spg_cor[1]; a.ftnw = (const T*)c->spg_cor[2];
+    a.ftse = (const T*)c->spg_cor[3]; a.ftsw = (const T*)c->spg_cor[4];
+  }
   GridBar bar{c->bar_mem, c->bar_mem + 1, c->err_flag, (unsigned)(c->p2_blocks + c->bar_extra), c->bar_spins};
-  cudaError_t e = launch_spg<T>(dom_now<T>(c), a, bar, c->p2_blocks, c->stream);
+  cudaError_t e = launch_spg<T>(dn, a, bar, c->p2_blocks, c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "dyn_spg_ts launch");
   c->ring0 = (c->ring0 + 3 * c->icycle) & 3;
   return NEMO_OK;
@@ -851,7 +883,6 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
   if (dm->jpi < 4 || dm->jpj < 4 || dm->jpk < 3 || dm->jpk > KMAX || dm->jpk > 255) return bad(NEMO_ERR_UNSUPPORTED);
   if (dm->jperio != 0 || nam->ln_isfcav || nam->ln_zad_Aimp) return bad(NEMO_ERR_UNSUPPORTED);
   if (nam->nvor_scheme < 0 || nam->nvor_scheme > 5) return bad(NEMO_ERR_ARG);
-  if (!nam->ln_linssh) return bad(NEMO_ERR_UNSUPPORTED);
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return bad(NEMO_ERR_CUDA);
   cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -883,6 +914,11 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
     if (cudaMalloc(&p, b2) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
     cudaMemset(p, 0, b2);
   }
+  if (!nam->ln_linssh)
+    for (auto& p : c->spg_cor) {
+      if (cudaMalloc(&p, b2) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
+      cudaMemset(p, 0, b2);
+    }
   for (auto& p : c->ring) {
     if (cudaMalloc(&p, 4 * b2) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
     cudaMemset(p, 0, 4 * b2);
@@ -912,14 +948,16 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
   // mixed form with the ENE/MIX scheme keeps its constants in shared memory when no
   // block owns more than P2_MAXT tiles
   const long need = (long)((c->jpi + 31) / 32) * ((c->jpj + 7) / 8) * c->nmem;
+  const int vvl = !nam->ln_linssh;
   auto p2_grid = [&](int cache) {
-    const int bps = prec == NEMO_PREC_FP64 ? spg_p2_blocks_per_sm<double>(0) : spg_p2_blocks_per_sm<float>(cache);
+    const int bps =
+        prec == NEMO_PREC_FP64 ? spg_p2_blocks_per_sm<double>(0, vvl) : spg_p2_blocks_per_sm<float>(cache, vvl);
     const long maxb = (long)bps * c->nsm;
     c->p2_blocks = (int)(need < maxb ? need : maxb);
     c->p2_cache = cache;
   };
   const int nv = c->nam.nvor_scheme;
-  p2_grid(prec != NEMO_PREC_FP64 && (nv == 1 || nv == 5) ? 1 : 0);
+  p2_grid(prec != NEMO_PREC_FP64 && !vvl && (nv == 1 || nv == 5) ? 1 : 0);
   if (c->p2_cache && (c->p2_blocks < 1 || need > (long)c->p2_blocks * P2_MAXT)) p2_grid(0);
   if (c->p2_blocks < 1) return bad(NEMO_ERR_CUDA);
   c->gs_nblk = c->nsm * 4;
@@ -942,6 +980,7 @@ int nemo_gpu_destroy(nemo_ctx* c) {
   cudaFree(c->fct_ztw);
   for (auto p : c->iso_w) cudaFree(p);
   for (auto p : c->spg_w) cudaFree(p);
+  for (auto p : c->spg_cor) cudaFree(p);
   for (auto p : c->ring) cudaFree(p);
   for (auto p : c->spg_x) cudaFree(p);
   cudaFree(c->spg_ff);

@@ -129,18 +129,22 @@ cudaError_t launch_clamp(T* x, long n, cudaStream_t s) {
 // co-resident blocks per SM of the sub-step kernel, with or without the constant
 // cache (dynamic shared memory beyond the 48 KB default needs the opt-in)
 template <class T>
-int spg_p2_blocks_per_sm(int cache) {
+int spg_p2_blocks_per_sm(int cache, int vvl) {
   const size_t dyn = cache ? P2_CACHE_BYTES : 0;
-  if (cache &&
-      cudaFuncSetAttribute(k_spg_p2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess)
+  auto kern = vvl ? k_spg_p2<T, true> : k_spg_p2<T, false>;
+  if (cache && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess)
     return 0;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_spg_p2<T>, 256, dyn) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 256, dyn) != cudaSuccess) return 0;
   return nb;
 }
 
 template <class T>
 cudaError_t launch_spg(const Dom<T>& d, const SpgArgs<T>& a, const GridBar& bar, int p2_blocks, cudaStream_t s) {
+  if (a.vvl) {  // Coriolis factors from the now depths (:241-343)
+    k_spg_cor<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+    ktick(NEMO_K_SPG_COR, s);
+  }
   bool p1a_reg = false;
   if constexpr (sizeof(T) == 4) {
     if (d.jpk == 31) {  // the GYRE levels: columns in registers
@@ -162,7 +166,8 @@ cudaError_t launch_spg(const Dom<T>& d, const SpgArgs<T>& a, const GridBar& bar,
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaError_t e = cudaLaunchKernelEx(&cfg, k_spg_p2<T>, d, a, bar);
+  cudaError_t e = a.vvl ? cudaLaunchKernelEx(&cfg, k_spg_p2<T, true>, d, a, bar)
+                        : cudaLaunchKernelEx(&cfg, k_spg_p2<T, false>, d, a, bar);
   if (e != cudaSuccess) return e;
   ktick(NEMO_K_SPG_P2, s);
   k_spg_p3<T><<<dim3((d.jpi + BX - 1) / BX, (d.jpj + BY - 1) / BY, d.nmem * ((d.jpk + KCH3 - 1) / KCH3)),
@@ -198,7 +203,7 @@ cudaError_t launch_globsum(const T* x, const double* tmask_i, long n2, int nk, i
   template cudaError_t launch_iso_flux<T>(const Dom<T>&, const LdfArgs<T>&, cudaStream_t);                   \
   template cudaError_t launch_clamp<T>(T*, long, cudaStream_t);                                              \
   template cudaError_t launch_spg<T>(const Dom<T>&, const SpgArgs<T>&, const GridBar&, int, cudaStream_t);   \
-  template int spg_p2_blocks_per_sm<T>(int);                                                                 \
+  template int spg_p2_blocks_per_sm<T>(int, int);                                                                 \
   template cudaError_t launch_lbc<T>(T*, int, int, long, int, T, cudaStream_t);                              \
   template cudaError_t launch_globsum<T>(const T*, const double*, long, int, int, double*, int, double*, cudaStream_t);
 

@@ -1,5 +1,5 @@
 // k_dyn.cuh -- split-explicit free surface (dyn_spg_ts, dynspg_ts.F90:121-1310) for a
-// linear free surface, plus lbc_lnk and the compensated global sum.
+// linear or a variable-volume free surface, plus lbc_lnk and the compensated global sum.
 //
 // Phase 1 (forcing of the 2-D system) and phase 3 (correction of the 3-D fields)
 // are column kernels. Phase 2, the icycle barotropic sub-steps, is ONE persistent
@@ -40,6 +40,18 @@ struct SpgArgs {
   int nwgt;
   int ln_bt_fw, ln_apr_dyn, nvor, ll_init, icycle, ring0, phase3_filter;
   int cache;  // mixed form, ENE/MIX: the sub-step constants cached in shared memory
+  // Column depths (2-D): for a linear free surface the rest-state ht_0, hu_0, ...
+  // shared by all members (member stride hs = 0); with a variable volume the bound
+  // now / before depths of each member (hs = points per member). The Coriolis
+  // factors (:241-343) follow the same rule: the domain's, or those k_spg_cor
+  // computes from the now depths at every step.
+  RO<T> ht_n, hu_n, hv_n, r1_hu_n, r1_hv_n, hu_b, hv_b, r1_hu_b, r1_hv_b;
+  RO<T> zwz, ftne, ftnw, ftse, ftsw;
+  RO<T> e3f_n;   // (jpi,jpj,jpk) per member: variable volume, ENE/ENS/MIX schemes
+  T* cor_w[5];   // k_spg_cor output: zwz, ftne, ftnw, ftse, ftsw per member
+  long hs;
+  int vvl, flux;  // variable volume; flux-form momentum (variable volume, !ln_dynadv_vec)
+  int een_e3f, sco;
   T rdtbt, grav, r1_rau0, scal_load, rn_bt_alpha;
   double rn_atfp, r1_2dt_b;
 };
@@ -64,8 +76,8 @@ __global__ void k_spg_p1a(Dom<T> d, SpgArgs<T> a) {
     su = su + d.e3u_n(ij, k, m) * a.ua[q] * umsk<T>(ci, k);
     sv = sv + d.e3v_n(ij, k, m) * a.va[q] * vmsk<T>(ci, k);
   }
-  su = su * d.r1_hu_0[ij];
-  sv = sv * d.r1_hv_0[ij];
+  su = su * a.r1_hu_n[m * a.hs + ij];
+  sv = sv * a.r1_hv_n[m * a.hs + ij];
   a.zu_frc[m2 + ij] = su;
   a.zv_frc[m2 + ij] = sv;
   if (i >= 2 && i <= d.jpi - 1 && j >= 2 && j <= d.jpj - 1)
@@ -76,43 +88,117 @@ __global__ void k_spg_p1a(Dom<T> d, SpgArgs<T> a) {
     }
 }
 
+// Coriolis factors of one member (:241-343).
+template <class T>
+struct CorF {
+  RO<T> zwz, ftne, ftnw, ftse, ftsw;
+};
+// hm: member offset of the 2-D depth and factor arrays (m * hs)
+template <class T>
+__device__ __forceinline__ CorF<T> cor_of(const SpgArgs<T>& a, long hm) {
+  return CorF<T>{a.zwz + hm, a.ftne + hm, a.ftnw + hm, a.ftse + hm, a.ftsw + hm};
+}
+
 // Barotropic Coriolis trend of a flux field (ENE/MIX, ENS, EET/EEN, ENT) at an
 // interior point (:390-443 and :1000-1056). Every scheme reads the same eight
 // neighbours, passed preloaded: x[0..3] = zwx at p-1, p, p-1+jpi, p+jpi and
 // y[0..3] = zwy at p-jpi, p+1-jpi, p, p+1; for ENT xu / yv are the velocities at
-// the same points and z1_hu / z1_hv the inverse depths.
+// the same points, h[0..2] the depths at p, p+1, p+jpi and z1_hu / z1_hv the
+// inverse depths at the u- / v-point.
 template <class T>
-__device__ __forceinline__ void coriolis(const Dom<T>& d, int nvor, long p, const T (&x)[4], const T (&y)[4],
-                                         const T (&xu)[4], const T (&yv)[4], T z1_hu, T z1_hv, T& zu_trd,
-                                         T& zv_trd) {
+__device__ __forceinline__ void coriolis(const Dom<T>& d, const CorF<T>& f, int nvor, long p, const T (&x)[4],
+                                         const T (&y)[4], const T (&xu)[4], const T (&yv)[4], const T (&h)[3],
+                                         T z1_hu, T z1_hv, T& zu_trd, T& zv_trd) {
   const int jpi = d.jpi;
   const T r1_4 = T(0.25), r1_8 = T(0.125), r1_12 = T(1) / T(12);
   if (nvor == 2) {  // ENT
     const RO<T> e = d.e1e2t;
-    const RO<T> h = d.ht_0;
     const RO<T> ft = d.ff_t;
     zu_trd = +r1_4 * d.r1_e1e2u[p] * z1_hu *
-             (e[p + 1] * h[p + 1] * ft[p + 1] * (yv[3] + yv[1]) + e[p] * h[p] * ft[p] * (yv[2] + yv[0]));
+             (e[p + 1] * h[1] * ft[p + 1] * (yv[3] + yv[1]) + e[p] * h[0] * ft[p] * (yv[2] + yv[0]));
     zv_trd = -r1_4 * d.r1_e1e2v[p] * z1_hv *
-             (e[p + jpi] * h[p + jpi] * ft[p + jpi] * (xu[3] + xu[2]) + e[p] * h[p] * ft[p] * (xu[1] + xu[0]));
+             (e[p + jpi] * h[2] * ft[p + jpi] * (xu[3] + xu[2]) + e[p] * h[0] * ft[p] * (xu[1] + xu[0]));
   } else if (nvor == 1 || nvor == 5) {  // ENE, MIX
     const T zy1 = (y[0] + y[1]) * d.r1_e1u[p];
     const T zy2 = (y[2] + y[3]) * d.r1_e1u[p];
     const T zx1 = (x[0] + x[2]) * d.r1_e2v[p];
     const T zx2 = (x[1] + x[3]) * d.r1_e2v[p];
-    zu_trd = r1_4 * (d.zwz[p - jpi] * zy1 + d.zwz[p] * zy2);
-    zv_trd = -r1_4 * (d.zwz[p - 1] * zx1 + d.zwz[p] * zx2);
+    zu_trd = r1_4 * (f.zwz[p - jpi] * zy1 + f.zwz[p] * zy2);
+    zv_trd = -r1_4 * (f.zwz[p - 1] * zx1 + f.zwz[p] * zx2);
   } else if (nvor == 0) {  // ENS
     const T zy1 = r1_8 * (y[0] + y[1] + y[2] + y[3]) * d.r1_e1u[p];
     const T zx1 = -r1_8 * (x[0] + x[2] + x[1] + x[3]) * d.r1_e2v[p];
-    zu_trd = zy1 * (d.zwz[p - jpi] + d.zwz[p]);
-    zv_trd = zx1 * (d.zwz[p - 1] + d.zwz[p]);
+    zu_trd = zy1 * (f.zwz[p - jpi] + f.zwz[p]);
+    zv_trd = zx1 * (f.zwz[p - 1] + f.zwz[p]);
   } else {  // EET, EEN
     zu_trd = +r1_12 * d.r1_e1u[p] *
-             (d.ftne[p] * y[2] + d.ftnw[p + 1] * y[3] + d.ftse[p] * y[0] + d.ftsw[p + 1] * y[1]);
+             (f.ftne[p] * y[2] + f.ftnw[p + 1] * y[3] + f.ftse[p] * y[0] + f.ftsw[p + 1] * y[1]);
     zv_trd = -r1_12 * d.r1_e2v[p] *
-             (d.ftsw[p + jpi] * x[2] + d.ftse[p + jpi] * x[3] + d.ftnw[p] * x[0] + d.ftne[p] * x[1]);
+             (f.ftsw[p + jpi] * x[2] + f.ftse[p + jpi] * x[3] + f.ftnw[p] * x[0] + f.ftne[p] * x[1]);
   }
+}
+
+// Coriolis factors of a variable-volume step (:241-343, recomputed at every step
+// when ln_linssh = .false.) from the now depths: ht_n for EEN and EET, e3f_n for
+// ENE, ENS and MIX. One thread per point and member; the F-point lbc (:265) is
+// folded in (column jpi and row jpj are 0).
+template <class T>
+__global__ void k_spg_cor(Dom<T> d, SpgArgs<T> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int m = blockIdx.z;
+  const int jpi = d.jpi, jpj = d.jpj;
+  if (i > jpi || j > jpj) return;
+  const long p = pt_ij(d, i, j), m2 = (long)m * d.n2;
+  const RO<T> ht = a.ht_n + m2;
+  const RO<T> ff = d.ff_f;
+  const int sc = a.nvor;
+  T zwz = T(0), ne = T(0), nw = T(0), se = T(0), sw = T(0);
+  if (sc == 4) {  // EEN: ff_f over the averaged depth at F-points (:249-263)
+    auto zw = [&](long q, int ii, int jj) -> T {
+      if (ii > jpi - 1 || jj > jpj - 1) return T(0);
+      T z = ht[q + jpi] + ht[q + jpi + 1] + ht[q] + ht[q + 1];
+      if (a.een_e3f == 0) z = z * T(0.25);
+      else z = z / fmx(T(1), d.ssmask[q + jpi] + d.ssmask[q + jpi + 1] + d.ssmask[q] + d.ssmask[q + 1]);
+      if (z != T(0)) z = ff[q] / z;
+      return z;
+    };
+    zwz = zw(p, i, j);
+    if (i >= 2 && j >= 2) {  // (:267-275)
+      const T w_ij = zwz, w_wj = zw(p - 1, i - 1, j), w_is = zw(p - jpi, i, j - 1), w_ws = zw(p - 1 - jpi, i - 1, j - 1);
+      ne = w_wj + w_ij + w_is;
+      nw = w_ws + w_wj + w_ij;
+      se = w_ij + w_is + w_ws;
+      sw = w_is + w_ws + w_wj;
+    }
+  } else if (sc == 3) {  // EET (:278-287)
+    if (i >= 2 && j >= 2) {
+      const T z1_ht = d.ssmask[p] / (ht[p] + T(1) - d.ssmask[p]);
+      ne = (ff[p - 1] + ff[p] + ff[p - jpi]) * z1_ht;
+      nw = (ff[p - 1 - jpi] + ff[p - 1] + ff[p]) * z1_ht;
+      se = (ff[p] + ff[p - jpi] + ff[p - 1 - jpi]) * z1_ht;
+      sw = (ff[p - jpi] + ff[p - 1 - jpi] + ff[p - 1]) * z1_ht;
+    }
+  } else {  // ENE, ENS, MIX: ff_f / hf with hf the wet e3f_n column (:289-341)
+    T zhf = T(0);
+    if (i <= jpi - 1 && j <= jpj - 1) {
+      if (a.sco)
+        zhf = (d.ht_0[p] + d.ht_0[p + 1] + d.ht_0[p + jpi] + d.ht_0[p + jpi + 1]) /
+              fmx(d.ssmask[p] + d.ssmask[p + 1] + d.ssmask[p + jpi] + d.ssmask[p + jpi + 1], T(1));
+      const ColInfo c0 = d.ci[p], c1 = d.ci[p + jpi];
+      zhf = zhf * (T(1) - umsk<T>(c0, 1) * umsk<T>(c1, 1));
+      const RO<T> e3f = a.e3f_n + (long)m * d.n3 + p;
+      for (int k = 1; k <= d.jpk - 1; ++k) zhf = zhf + e3f[(long)(k - 1) * d.n2] * umsk<T>(c0, k) * umsk<T>(c1, k);
+    }
+    T r = T(0);
+    if (zhf != T(0)) r = T(1) / zhf;
+    zwz = ff[p] * r;
+  }
+  a.cor_w[0][m2 + p] = zwz;
+  a.cor_w[1][m2 + p] = ne;
+  a.cor_w[2][m2 + p] = nw;
+  a.cor_w[3][m2 + p] = se;
+  a.cor_w[4][m2 + p] = sw;
 }
 
 // the eight neighbours of p that coriolis() reads, of a point function f
@@ -129,14 +215,15 @@ __device__ __forceinline__ void nby(F f, long p, int jpi, T (&y)[4]) {
 // atmospheric pressure, ssh forcing, initial barotropic levels, zeroed sums.
 template <class T>
 __device__ __forceinline__ void spg_p1b_point(const Dom<T>& d, const SpgArgs<T>& a, int i, int j, int m) {
-  const long p = pt_ij(d, i, j), n2 = d.n2, m2 = (long)m * n2, m3 = (long)m * d.n3;
+  const long p = pt_ij(d, i, j), n2 = d.n2, m2 = (long)m * n2, m3 = (long)m * d.n3, hm = (long)m * a.hs;
   const T r1_2 = T(0.5);
   const bool interior = i >= 2 && i <= d.jpi - 1 && j >= 2 && j <= d.jpj - 1;
   if (interior) {
     const RO<T> unb = a.un_b + m2;
     const RO<T> vnb = a.vn_b + m2;
-    auto fx = [&](long q) -> T { return unb[q] * d.hu_0[q] * d.e2u[q]; };
-    auto fy = [&](long q) -> T { return vnb[q] * d.hv_0[q] * d.e1v[q]; };
+    const RO<T> hun = a.hu_n + hm, hvn = a.hv_n + hm, r1hu = a.r1_hu_n + hm, r1hv = a.r1_hv_n + hm;
+    auto fx = [&](long q) -> T { return unb[q] * hun[q] * d.e2u[q]; };
+    auto fy = [&](long q) -> T { return vnb[q] * hvn[q] * d.e1v[q]; };
     auto fu = [&](long q) -> T { return unb[q]; };
     auto fv = [&](long q) -> T { return vnb[q]; };
     T x[4], y[4], xu[4] = {}, yv[4] = {};
@@ -146,8 +233,18 @@ __device__ __forceinline__ void spg_p1b_point(const Dom<T>& d, const SpgArgs<T>&
       nbx(fu, p, d.jpi, xu);
       nby(fv, p, d.jpi, yv);
     }
+    T h[3] = {};
+    if (a.nvor == 2) {
+      const RO<T> ht = a.ht_n + hm;
+      h[0] = ht[p]; h[1] = ht[p + 1]; h[2] = ht[p + d.jpi];
+    }
     T zu_trd, zv_trd;
-    coriolis(d, a.nvor, p, x, y, xu, yv, d.r1_hu_0[p], d.r1_hv_0[p], zu_trd, zv_trd);
+    coriolis(d, cor_of(a, hm), a.nvor, p, x, y, xu, yv, h, r1hu[p], r1hv[p], zu_trd, zv_trd);
+    if (a.vvl) {  // variable volume: remove the surface pressure gradient (:447-509)
+      const RO<T> sn = a.sshn + m2;
+      zu_trd = zu_trd - a.grav * (sn[p + 1] - sn[p]) * d.r1_e1u[p];
+      zv_trd = zv_trd - a.grav * (sn[p + d.jpi] - sn[p]) * d.r1_e2v[p];
+    }
     T zu = a.zu_frc[m2 + p] - zu_trd * d.ssumask[p];
     T zv = a.zv_frc[m2 + p] - zv_trd * d.ssvmask[p];
     // bottom stress from the baroclinic bottom velocity (:519-557)
@@ -157,16 +254,16 @@ __device__ __forceinline__ void spg_p1b_point(const Dom<T>& d, const SpgArgs<T>&
     if (a.ln_bt_fw) { zwx = a.un[qu] - unb[p]; zwy = a.vn[qv] - vnb[p]; }
     else { zwx = a.ub[qu] - a.ub_b[m2 + p]; zwy = a.vb[qv] - a.vb_b[m2 + p]; }
     const RO<T> cdu = a.rCdU_bot + m2;
-    zu = zu + d.r1_hu_0[p] * r1_2 * (cdu[p + 1] + cdu[p]) * zwx;
-    zv = zv + d.r1_hv_0[p] * r1_2 * (cdu[p + d.jpi] + cdu[p]) * zwy;
+    zu = zu + r1hu[p] * r1_2 * (cdu[p + 1] + cdu[p]) * zwx;
+    zv = zv + r1hv[p] * r1_2 * (cdu[p + d.jpi] + cdu[p]) * zwy;
     // wind (:589-604)
     if (a.ln_bt_fw) {
-      zu = zu + a.r1_rau0 * a.utau[m2 + p] * d.r1_hu_0[p];
-      zv = zv + a.r1_rau0 * a.vtau[m2 + p] * d.r1_hv_0[p];
+      zu = zu + a.r1_rau0 * a.utau[m2 + p] * r1hu[p];
+      zv = zv + a.r1_rau0 * a.vtau[m2 + p] * r1hv[p];
     } else {
       const T zztmp = a.r1_rau0 * r1_2;
-      zu = zu + zztmp * (a.utau_b[m2 + p] + a.utau[m2 + p]) * d.r1_hu_0[p];
-      zv = zv + zztmp * (a.vtau_b[m2 + p] + a.vtau[m2 + p]) * d.r1_hv_0[p];
+      zu = zu + zztmp * (a.utau_b[m2 + p] + a.utau[m2 + p]) * r1hu[p];
+      zv = zv + zztmp * (a.vtau_b[m2 + p] + a.vtau[m2 + p]) * r1hv[p];
     }
     // atmospheric pressure (:606-629)
     if (a.ln_apr_dyn) {
@@ -253,8 +350,8 @@ __global__ void __launch_bounds__(128) k_spg_p1a_reg(Dom<float> d, SpgArgs<float
     su = su + d.e3u_n(ij, k, m) * u[k - 1] * umsk<float>(ci, k);
     sv = sv + d.e3v_n(ij, k, m) * v[k - 1] * vmsk<float>(ci, k);
   }
-  su = su * d.r1_hu_0[ij];
-  sv = sv * d.r1_hv_0[ij];
+  su = su * a.r1_hu_n[m * a.hs + ij];
+  sv = sv * a.r1_hv_n[m * a.hs + ij];
   a.zu_frc[m2 + ij] = su;
   a.zv_frc[m2 + ij] = sv;
   if (i >= 2 && i <= d.jpi - 1 && j >= 2 && j <= d.jpj - 1)
@@ -339,9 +436,13 @@ __device__ __forceinline__ int p2_tiles(const Dom<T>& d) {
   return ((d.jpi + P2_TX - 1) / P2_TX) * ((d.jpj + P2_TY - 1) / P2_TY) * d.nmem;
 }
 
-template <class T>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar bar) {
+template <class T, bool VVL>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? (VVL ? 3 : 4) : 2) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar bar) {
   __shared__ T zs_s[P2_TY + 1][P2_TX + 1];
+  // Variable volume: the new ssh ssha_e [0], the predictor ssh of the next sub-step
+  // [1] and the now ssh [2] of the tile and its halo, for the depths at u- and
+  // v-points that average two neighbouring T-points.
+  __shared__ T vv_s[VVL ? 3 : 1][P2_TY + 1][P2_TX + 1];
   const int n2 = (int)d.n2;
   const int nmem2 = d.nmem * n2;
   const int jpi = d.jpi, jpj = d.jpj;
@@ -360,16 +461,38 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
     i0 = (tt % ntx) * P2_TX + 1;
     j0 = (tt / ntx) * P2_TY + 1;
   };
+  // ssh averaged to the u- / v-point of interior point p from its values at p and
+  // at the east / north neighbour (:766-773, :888-895, :976-983)
+  const T r1_2 = T(0.5);
+  auto ssh_u = [&](int p, T s0, T se) -> T {
+    return r1_2 * d.ssumask[p] * d.r1_e1e2u[p] * (d.e1e2t[p] * s0 + d.e1e2t[p + 1] * se);
+  };
+  auto ssh_v = [&](int p, T s0, T sn) -> T {
+    return r1_2 * d.ssvmask[p] * d.r1_e1e2v[p] * (d.e1e2t[p] * s0 + d.e1e2t[p + jpi] * sn);
+  };
   // predictor fluxes of sub-step jn from the owner's levels (:724-800) and their
   // un_adv / vn_adv sums (:860-862)
-  auto predictor = [&](int jn, int rr, int g, int p) {
+  auto predictor = [&](int jn, int rr, int m2, int p, bool inner) {
+    const int g = m2 + p;
     T za1, za2, za3;
     ab3(jn, a.ll_init, za1, za2, za3);
     const int sn = rr & 3, sb = (rr + 1) & 3, sbb = (rr + 2) & 3;
     const T ua_e = za1 * a.ring_u[sn * nmem2 + g] + za2 * a.ring_u[sb * nmem2 + g] + za3 * a.ring_u[sbb * nmem2 + g];
     const T va_e = za1 * a.ring_v[sn * nmem2 + g] + za2 * a.ring_v[sb * nmem2 + g] + za3 * a.ring_v[sbb * nmem2 + g];
-    const T zwx = d.e2u[p] * ua_e * d.hu_0[p];
-    const T zwy = d.e1v[p] * va_e * d.hv_0[p];
+    T hu = d.hu_0[p], hv = d.hv_0[p];
+    if constexpr (VVL) {  // depth from the extrapolated ssh (:738-792)
+      if (inner) {
+        auto s_at = [&](int q) -> T {
+          return za1 * a.ring_ssh[sn * nmem2 + m2 + q] + za2 * a.ring_ssh[sb * nmem2 + m2 + q] +
+                 za3 * a.ring_ssh[sbb * nmem2 + m2 + q];
+        };
+        const T s0 = s_at(p);
+        hu = hu + ssh_u(p, s0, s_at(p + 1));
+        hv = hv + ssh_v(p, s0, s_at(p + jpi));
+      }
+    }
+    const T zwx = d.e2u[p] * ua_e * hu;
+    const T zwy = d.e1v[p] * va_e * hv;
     a.fx[(jn & 1) * nmem2 + g] = zwx;
     a.fy[(jn & 1) * nmem2 + g] = zwy;
     T w2;
@@ -391,17 +514,18 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
       const int i = i0 + tx, j = j0 + ty;
       if (i <= jpi && j <= jpj) {
         const int p = (i - 1) + (j - 1) * jpi;
-        predictor(1, r, m2 + p, p);
+        predictor(1, r, m2, p, interior(i, j));
       }
     }
-  // Mixed form with the ENE/MIX scheme: the per-point constants of the Coriolis,
-  // drag, pressure-gradient and predictor terms, combined once and kept in shared
-  // memory for the whole kernel (the barrier's acquire empties L1 every sub-step, so
-  // they would otherwise come from L2 after each tile's __syncthreads). Each thread
-  // writes and reads only its own entries. FP32 products in another association than
-  // the general path below: within the mixed form's tolerance.
+  // Mixed form with the ENE/MIX scheme and a linear free surface: the per-point
+  // constants of the Coriolis, drag, pressure-gradient and predictor terms, combined
+  // once and kept in shared memory for the whole kernel (the barrier's acquire
+  // empties L1 every sub-step, so they would otherwise come from L2 after each
+  // tile's __syncthreads). Each thread writes and reads only its own entries. FP32
+  // products in another association than the general path below: within the mixed
+  // form's tolerance.
   extern __shared__ float p2c[];
-  const bool cache = sizeof(T) == 4 && a.cache;
+  const bool cache = !VVL && sizeof(T) == 4 && a.cache;
   if (cache) {
     int slot = 0;
     for (int t = blockIdx.x; t < ntile && slot < P2_MAXT; t += gridDim.x, ++slot) {
@@ -450,10 +574,13 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
     }
     T zb0, zb1, zb2, zb3;
     am4(jn, a.ll_init, a.rn_bt_alpha, zb0, zb1, zb2, zb3);
+    T zc1 = T(0), zc2 = T(0), zc3 = T(0);  // predictor coefficients of sub-step jn+1
+    if constexpr (VVL) ab3(jn + 1, a.ll_init, zc1, zc2, zc3);
     int slot = 0;  // the tile's place in the constant cache
     for (int t = blockIdx.x; t < ntile; t += gridDim.x, ++slot) {
       int m2, i0, j0;
       tile(t, m2, i0, j0);
+      const long hm = VVL ? m2 : 0;  // member offset of the depths and Coriolis factors
       // Every value this tile reads that the sub-step does not produce is loaded
       // first, so the loads of both stages are in flight together.
       const int i = i0 + tx, j = j0 + ty;
@@ -462,6 +589,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
       const int p = own ? (i - 1) + (j - 1) * jpi : 0, g = m2 + p;
       T x[4] = {}, y[4] = {}, xu[4] = {}, yv[4] = {};
       T sn0 = T(0), sb0 = T(0), sbb0 = T(0), un_e = T(0), vn_e = T(0), ub_e = T(0), vb_e = T(0);
+      // ENT / flux form: the predictor depths of sub-step jn at the u- and v-point
+      // and at p, p+1, p+jpi (:738-792)
+      T hup = T(0), hvp = T(0), hq[3] = {};
       double acc_s = 0.0, acc_u = 0.0, acc_v = 0.0, acc_au = 0.0, acc_av = 0.0;  // FP64 form
       FF f_s{}, f_u{}, f_v{}, f_au{}, f_av{};                                    // mixed form
       if (own) {
@@ -485,9 +615,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
         if (inner) {
           nbx([&](long q) { return fx[m2 + q]; }, (long)p, jpi, x);
           nby([&](long q) { return fy[m2 + q]; }, (long)p, jpi, y);
+          T za1, za2, za3;
+          ab3(jn, a.ll_init, za1, za2, za3);
           if (a.nvor == 2) {  // the ENT scheme uses the extrapolated velocities
-            T za1, za2, za3;
-            ab3(jn, a.ll_init, za1, za2, za3);
             auto uext = [&](long q) -> T {
               return za1 * a.ring_u[sn * nmem2 + m2 + q] + za2 * a.ring_u[sb * nmem2 + m2 + q] +
                      za3 * a.ring_u[sbb * nmem2 + m2 + q];
@@ -498,6 +628,20 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
             };
             nbx(uext, (long)p, jpi, xu);
             nby(vext, (long)p, jpi, yv);
+          }
+          if constexpr (VVL) {
+            if (a.nvor == 2 || a.flux) {
+              auto s_at = [&](int q) -> T {
+                return za1 * a.ring_ssh[sn * nmem2 + m2 + q] + za2 * a.ring_ssh[sb * nmem2 + m2 + q] +
+                       za3 * a.ring_ssh[sbb * nmem2 + m2 + q];
+              };
+              const T s0 = za1 * sn0 + za2 * sb0 + za3 * sbb0, se = s_at(p + 1), so = s_at(p + jpi);
+              hup = d.hu_0[p] + ssh_u(p, s0, se);
+              hvp = d.hv_0[p] + ssh_v(p, s0, so);
+              hq[0] = d.ht_0[p] + s0;
+              hq[1] = d.ht_0[p + 1] + se;
+              hq[2] = d.ht_0[p + jpi] + so;
+            }
           }
         }
       }
@@ -527,6 +671,11 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
           ssha_e = (sn0 - rdtbt * (zssh_frc[g] + zhdiv)) * d.ssmask[p];
         }
         zs_s[ty][tx] = zb0 * ssha_e + zb1 * sn0 + zb2 * sb0 + zb3 * sbb0;
+        if constexpr (VVL) {
+          vv_s[0][ty][tx] = ssha_e;
+          vv_s[1][ty][tx] = zc1 * ssha_e + zc2 * sn0 + zc3 * sb0;
+          vv_s[2][ty][tx] = sn0;
+        }
         a.ring_ssh[sa * nmem2 + g] = ssha_e;
         if constexpr (sizeof(T) == 8) {
           a.ssha[g] = acc_s + w1 * (double)ssha_e;
@@ -543,12 +692,25 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
           ssha_e = (h_sn - rdtbt * (zssh_frc[hg] + zhdiv)) * d.ssmask[hp];
         }
         zs_s[htj][hti] = zb0 * ssha_e + zb1 * h_sn + zb2 * h_sb + zb3 * h_sbb;
+        if constexpr (VVL) {
+          vv_s[0][htj][hti] = ssha_e;
+          vv_s[1][htj][hti] = zc1 * ssha_e + zc2 * h_sn + zc3 * h_sb;
+          vv_s[2][htj][hti] = h_sn;
+        }
       }
       __syncthreads();
       // ---- Coriolis, drag, pressure gradient, ua_e/va_e and their sums (:1000-1204),
       // then the predictor of sub-step jn+1 (:724-800) and its sums (:860-862)
       if (own) {
         T ua_e = T(0), va_e = T(0);
+        // variable volume: depth of the new level, hu_0 + zsshu_a (:888-900, :1159-1165)
+        T hu_a = d.hu_0[p], hv_a = d.hv_0[p];
+        if constexpr (VVL) {
+          if (inner) {
+            hu_a = d.hu_0[p] + ssh_u(p, vv_s[0][ty][tx], vv_s[0][ty][tx + 1]);
+            hv_a = d.hv_0[p] + ssh_v(p, vv_s[0][ty][tx], vv_s[0][ty + 1][tx]);
+          }
+        }
         // the cached constants of this point: C[c * P2_MAXT * 256]
         const float* C = p2c + slot * 256 + threadIdx.x;
         constexpr int CS = P2_MAXT * 256;
@@ -561,28 +723,66 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
           ua_e = (un_e + rdtbt * (wxs + zu_trd + C[8 * CS])) * C[10 * CS];
           va_e = (vn_e + rdtbt * (wys + zv_trd + C[9 * CS])) * C[11 * CS];
         } else if (inner) {
-          const T z1_hu = d.ssumask[p] / (d.hu_0[p] + T(1) - d.ssumask[p]);
-          const T z1_hv = d.ssvmask[p] / (d.hv_0[p] + T(1) - d.ssvmask[p]);
+          T z1_hu = T(0), z1_hv = T(0);
+          if constexpr (!VVL) {  // rest-state depths, loaded here to keep them out of stage A
+            if (a.nvor == 2) {
+              hup = d.hu_0[p];
+              hvp = d.hv_0[p];
+              hq[0] = d.ht_0[p];
+              hq[1] = d.ht_0[p + 1];
+              hq[2] = d.ht_0[p + jpi];
+            }
+          }
+          if (a.nvor == 2) {
+            z1_hu = d.ssumask[p] / (hup + T(1) - d.ssumask[p]);
+            z1_hv = d.ssvmask[p] / (hvp + T(1) - d.ssvmask[p]);
+          }
           T zu_trd, zv_trd;
-          coriolis(d, a.nvor, (long)p, x, y, xu, yv, z1_hu, z1_hv, zu_trd, zv_trd);
-          zu_trd = zu_trd + zCdU_u[g] * un_e * d.r1_hu_0[p];
-          zv_trd = zv_trd + zCdU_v[g] * vn_e * d.r1_hv_0[p];
+          coriolis(d, cor_of(a, hm), a.nvor, (long)p, x, y, xu, yv, hq, z1_hu, z1_hv, zu_trd, zv_trd);
+          // depth of the current level hu_e and its inverse hur_e (:689-693, :1159-1165)
+          T hue = d.hu_0[p], hve = d.hv_0[p], hur = d.r1_hu_0[p], hvr = d.r1_hv_0[p];
+          if constexpr (VVL) {
+            if (jn == 1) {
+              hue = (a.ln_bt_fw ? a.hu_n : a.hu_b)[hm + p];
+              hve = (a.ln_bt_fw ? a.hv_n : a.hv_b)[hm + p];
+              hur = (a.ln_bt_fw ? a.r1_hu_n : a.r1_hu_b)[hm + p];
+              hvr = (a.ln_bt_fw ? a.r1_hv_n : a.r1_hv_b)[hm + p];
+            } else {  // from ssha_e of sub-step jn-1 = the now ssh
+              hue = d.hu_0[p] + ssh_u(p, vv_s[2][ty][tx], vv_s[2][ty][tx + 1]);
+              hve = d.hv_0[p] + ssh_v(p, vv_s[2][ty][tx], vv_s[2][ty + 1][tx]);
+              hur = d.ssumask[p] / (hue + T(1) - d.ssumask[p]);
+              hvr = d.ssvmask[p] / (hve + T(1) - d.ssvmask[p]);
+            }
+          }
+          zu_trd = zu_trd + zCdU_u[g] * un_e * hur;
+          zv_trd = zv_trd + zCdU_v[g] * vn_e * hvr;
           const T s0 = zs_s[ty][tx];
           const T zu_spg = -grav * (zs_s[ty][tx + 1] - s0) * d.r1_e1u[p];
           const T zv_spg = -grav * (zs_s[ty + 1][tx] - s0) * d.r1_e2v[p];
           const T wxs = (T(1) - a.scal_load) * zu_spg;
           const T wys = (T(1) - a.scal_load) * zv_spg;
-          ua_e = (un_e + rdtbt * (wxs + zu_trd + zu_frc[g])) * d.ssumask[p];
-          va_e = (vn_e + rdtbt * (wys + zv_trd + zv_frc[g])) * d.ssvmask[p];
+          if (!VVL || !a.flux) {  // vector form (:1106-1123)
+            ua_e = (un_e + rdtbt * (wxs + zu_trd + zu_frc[g])) * d.ssumask[p];
+            va_e = (vn_e + rdtbt * (wys + zv_trd + zv_frc[g])) * d.ssvmask[p];
+          } else {  // flux form (:973-991, :1124-1147)
+            const T zhust = d.hu_0[p] + ssh_u(p, s0, zs_s[ty][tx + 1]);
+            const T zhvst = d.hv_0[p] + ssh_v(p, s0, zs_s[ty + 1][tx]);
+            const T zhura = d.ssumask[p] / (hu_a + T(1) - d.ssumask[p]);
+            const T zhvra = d.ssvmask[p] / (hv_a + T(1) - d.ssvmask[p]);
+            ua_e = (hue * un_e + rdtbt * (zhust * wxs + hup * zu_trd + a.hu_n[hm + p] * zu_frc[g])) * zhura;
+            va_e = (hve * vn_e + rdtbt * (zhvst * wys + hvp * zv_trd + a.hv_n[hm + p] * zv_frc[g])) * zhvra;
+          }
         }
         a.ring_u[sa * nmem2 + g] = ua_e;
         a.ring_v[sa * nmem2 + g] = va_e;
+        // velocities, or transports with the new depth in flux form (:1190-1201)
+        const bool tr = VVL && a.flux;
         if constexpr (sizeof(T) == 8) {
-          a.ua_b[g] = acc_u + w1 * (double)ua_e;
-          a.va_b[g] = acc_v + w1 * (double)va_e;
+          a.ua_b[g] = tr ? acc_u + w1 * (double)ua_e * (double)hu_a : acc_u + w1 * (double)ua_e;
+          a.va_b[g] = tr ? acc_v + w1 * (double)va_e * (double)hv_a : acc_v + w1 * (double)va_e;
         } else {
-          ff_add_w(f_u, w1h, w1l, ua_e);
-          ff_add_w(f_v, w1h, w1l, va_e);
+          ff_add_w(f_u, w1h, w1l, tr ? ua_e * hu_a : ua_e);
+          ff_add_w(f_v, w1h, w1l, tr ? va_e * hv_a : va_e);
           a.ff[ffi(1, 0, nmem2, g)] = f_u.h;
           a.ff[ffi(1, 1, nmem2, g)] = f_u.l;
           a.ff[ffi(2, 0, nmem2, g)] = f_v.h;
@@ -594,8 +794,15 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
           ab3(jn + 1, a.ll_init, za1, za2, za3);
           const T uex = za1 * ua_e + za2 * un_e + za3 * ub_e;
           const T vex = za1 * va_e + za2 * vn_e + za3 * vb_e;
-          const T zwx = cache ? (T)C[12 * CS] * uex : d.e2u[p] * uex * d.hu_0[p];
-          const T zwy = cache ? (T)C[13 * CS] * vex : d.e1v[p] * vex * d.hv_0[p];
+          T hu = d.hu_0[p], hv = d.hv_0[p];
+          if constexpr (VVL) {  // depth from the extrapolated ssh (:738-792)
+            if (inner) {
+              hu = hu + ssh_u(p, vv_s[1][ty][tx], vv_s[1][ty][tx + 1]);
+              hv = hv + ssh_v(p, vv_s[1][ty][tx], vv_s[1][ty + 1][tx]);
+            }
+          }
+          const T zwx = cache ? (T)C[12 * CS] * uex : d.e2u[p] * uex * hu;
+          const T zwy = cache ? (T)C[13 * CS] * vex : d.e1v[p] * vex * hv;
           const T r1e2u = cache ? (T)C[14 * CS] : d.r1_e2u[p];
           const T r1e1v = cache ? (T)C[15 * CS] : d.r1_e1v[p];
           a.fx[((jn + 1) & 1) * nmem2 + g] = zwx;
@@ -621,12 +828,20 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
     r = (r + 3) & 3;
     if (!grid_barrier(bar)) return;
   }
-  // ---- phase 3, per column (:1214-1240, :1266-1269): time-filtered transports
+  // ---- phase 3, per column (:1214-1262, :1266-1269): time-filtered transports
   // and the two depth-independent terms each level adds
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nth = gridDim.x * blockDim.x;
+  // the time-averaged ssh at point g (final after the last barrier)
+  auto ssha_at = [&](int gg) -> double {
+    if constexpr (sizeof(T) == 4)
+      return (double)a.ff[ffi(0, 0, nmem2, gg)] + (double)a.ff[ffi(0, 1, nmem2, gg)];
+    else
+      return a.ssha[gg];
+  };
   for (int g = tid; g < nmem2; g += nth) {
     const int m2 = (g / n2) * n2, p = g - m2;
+    const long hm = VVL ? m2 : 0;
     if constexpr (sizeof(T) == 4) {  // the compensated sums into the FP64 fields
       auto sum = [&](int w) { return (double)a.ff[ffi(w, 0, nmem2, g)] + (double)a.ff[ffi(w, 1, nmem2, g)]; };
       a.ssha[g] = sum(0);
@@ -652,10 +867,31 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
       a.un_adv[g] = uadv;
       a.vn_adv[g] = vadv;
     }
-    a.du[g] = (T)((a.ua_b[g] - (double)a.ub_b[g]) * a.r1_2dt_b);
-    a.dv[g] = (T)((a.va_b[g] - (double)a.vb_b[g]) * a.r1_2dt_b);
-    a.cu[g] = (T)(uadv * (double)d.r1_hu_0[p]);
-    a.cv[g] = (T)(vadv * (double)d.r1_hv_0[p]);
+    double r1hu = (double)d.r1_hu_0[p], r1hv = (double)d.r1_hv_0[p];
+    if constexpr (VVL) {
+      r1hu = (double)a.r1_hu_n[hm + p];
+      r1hv = (double)a.r1_hv_n[hm + p];
+    }
+    if (!VVL || !a.flux) {
+      a.du[g] = (T)((a.ua_b[g] - (double)a.ub_b[g]) * a.r1_2dt_b);
+      a.dv[g] = (T)((a.va_b[g] - (double)a.vb_b[g]) * a.r1_2dt_b);
+    } else {  // flux form: summed transports to velocities (:1241-1262)
+      a.du[g] = (T)(r1hu * (a.ua_b[g] - (double)a.ub_b[g] * (double)a.hu_b[hm + p]) * a.r1_2dt_b);
+      a.dv[g] = (T)(r1hv * (a.va_b[g] - (double)a.vb_b[g] * (double)a.hv_b[hm + p]) * a.r1_2dt_b);
+      const int i = p % jpi + 1, j = p / jpi + 1;
+      double zsu = 0.0, zsv = 0.0;
+      if (interior(i, j)) {
+        const double s0 = ssha_at(g);
+        zsu = 0.5 * (double)d.ssumask[p] * (double)d.r1_e1e2u[p] *
+              ((double)d.e1e2t[p] * s0 + (double)d.e1e2t[p + 1] * ssha_at(g + 1));
+        zsv = 0.5 * (double)d.ssvmask[p] * (double)d.r1_e1e2v[p] *
+              ((double)d.e1e2t[p] * s0 + (double)d.e1e2t[p + jpi] * ssha_at(g + jpi));
+      }
+      a.ua_b[g] = a.ua_b[g] / ((double)d.hu_0[p] + zsu + 1.0 - (double)d.ssumask[p]);
+      a.va_b[g] = a.va_b[g] / ((double)d.hv_0[p] + zsv + 1.0 - (double)d.ssvmask[p]);
+    }
+    a.cu[g] = (T)(uadv * r1hu);
+    a.cv[g] = (T)(vadv * r1hv);
   }
 }
 

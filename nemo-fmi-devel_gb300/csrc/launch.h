@@ -45,7 +45,7 @@ cudaError_t launch_clamp(T* x, long n, cudaStream_t s);
 template <class T>
 cudaError_t launch_spg(const Dom<T>& d, const SpgArgs<T>& a, const GridBar& bar, int p2_blocks, cudaStream_t s);
 template <class T>
-int spg_p2_blocks_per_sm(int cache);
+int spg_p2_blocks_per_sm(int cache, int vvl);
 template <class T>
 cudaError_t launch_lbc(T* p, int jpi, int jpj, long nslab, int is_f, T pval, cudaStream_t s);
 template <class T>

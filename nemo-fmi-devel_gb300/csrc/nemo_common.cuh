@@ -67,7 +67,7 @@ struct Dom {
   RO<T> e1e2t, r1_e1e2t, e2_e1u, e1_e2v, r1_e1e2u, r1_e1e2v;
   RO<T> ht_0, hu_0, hv_0, r1_hu_0, r1_hv_0;
   RO<T> ssmask, ssumask, ssvmask;
-  RO<T> ff_t, zwz, ftne, ftnw, ftse, ftsw;
+  RO<T> ff_t, ff_f, zwz, ftne, ftnw, ftse, ftsw;
   RO<double> tmask_i;
   RO<ColInfo> ci;
   RO<uint8_t> mbkt;

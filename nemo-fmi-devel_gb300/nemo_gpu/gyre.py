@@ -225,3 +225,64 @@ def state(dom, nam, seed=0, noise_t=0.05, noise_s=0.01, u0=0.5, member=0):
                 un_b=un_b, vn_b=vn_b, ub_b=ub_b, vb_b=vb_b, sshn=sshn, sshb=sshb,
                 utau=utau, vtau=vtau, emp=emp, rcdu_bot=rcdu, avt=avt,
                 uslp=uslp, vslp=vslp, wslpi=wslpi, wslpj=wslpj)
+
+
+def zstar(dom, st):
+    """Variable-volume (z*) scale factors and depths of a state: the fields
+    domvvl.F90 maintains when ln_linssh = .false. -- e3t = e3t_0 (ht_0 + ssh) /
+    (ht_0 + 1 - ssmask) on wet levels (:849-851), e3u/e3v/e3f/e3w interpolated from
+    the e3t changes as dom_vvl_interpol does, column depths and their masked
+    inverses (:183-196). Before / now / after levels use sshb, sshn and a linear
+    extrapolation sshn + (sshn - sshb)."""
+    tm, um, vm, wm = masks(dom)
+    e1e2t = dom["e1t"] * dom["e2t"]
+    e1e2u = dom["e1u"] * dom["e2u"]
+    e1e2f = dom["e1f"] * dom["e2f"]
+    ssmask = tm.max(axis=2)
+    ssumask = um.max(axis=2)
+    ssvmask = vm.max(axis=2)
+    ht_0 = (dom["e3t_0"] * tm).sum(axis=2)
+    f = np.asfortranarray
+
+    def e3t_of(ssh):
+        s = (ht_0 + ssh) / (ht_0 + 1.0 - ssmask)
+        return f(dom["e3t_0"] * s[:, :, None] * tm + dom["e3t_0"] * (1.0 - tm))
+
+    def to_u(e3t):
+        d = e1e2t[:, :, None] * (e3t - dom["e3t_0"])
+        out = dom["e3u_0"].copy()
+        out[:-1] += um[:-1] * 0.5 * (d[:-1] + d[1:]) / e1e2u[:-1, :, None]
+        return f(out)
+
+    def to_v(e3t):
+        d = e1e2t[:, :, None] * (e3t - dom["e3t_0"])
+        e1e2v = dom["e1v"] * dom["e2v"]
+        out = dom["e3v_0"].copy()
+        out[:, :-1] += vm[:, :-1] * 0.5 * (d[:, :-1] + d[:, 1:]) / e1e2v[:, :-1, None]
+        return f(out)
+
+    def to_f(e3u):
+        d = e1e2u[:, :, None] * (e3u - dom["e3u_0"])
+        out = dom["e3f_0"].copy()
+        out[:, :-1] += um[:, :-1] * um[:, 1:] * 0.5 * (d[:, :-1] + d[:, 1:]) / e1e2f[:, :-1, None]
+        return f(out)
+
+    def to_w(e3t):
+        d = e3t - dom["e3t_0"]
+        out = dom["e3w_0"].copy()
+        out[:, :, 0] += d[:, :, 0]
+        out[:, :, 1:] += (1.0 - 0.5 * tm[:, :, 1:]) * d[:, :, :-1] + 0.5 * tm[:, :, 1:] * d[:, :, 1:]
+        return f(out)
+
+    def inv(h, m):
+        return f(m / (h + 1.0 - m))
+
+    ssha = (st["sshn"] + (st["sshn"] - st["sshb"])) * ssmask
+    e3t_b, e3t_n, e3t_a = e3t_of(st["sshb"]), e3t_of(st["sshn"]), e3t_of(ssha)
+    e3u_b, e3u_n, e3v_b, e3v_n = to_u(e3t_b), to_u(e3t_n), to_v(e3t_b), to_v(e3t_n)
+    hu_b, hu_n = f((e3u_b * um)[:, :, :-1].sum(axis=2)), f((e3u_n * um)[:, :, :-1].sum(axis=2))
+    hv_b, hv_n = f((e3v_b * vm)[:, :, :-1].sum(axis=2)), f((e3v_n * vm)[:, :, :-1].sum(axis=2))
+    return dict(e3t_b=e3t_b, e3t_n=e3t_n, e3t_a=e3t_a, e3u_n=e3u_n, e3v_n=e3v_n, e3w_n=to_w(e3t_n),
+                e3f_n=to_f(e3u_n), ht_n=f((e3t_n * tm)[:, :, :-1].sum(axis=2)),
+                hu_n=hu_n, hv_n=hv_n, r1_hu_n=inv(hu_n, ssumask), r1_hv_n=inv(hv_n, ssvmask),
+                hu_b=hu_b, hv_b=hv_b, r1_hu_b=inv(hu_b, ssumask), r1_hv_b=inv(hv_b, ssvmask))

@@ -54,7 +54,7 @@ struct ora_ctx {
   double *f[NEMO_F_COUNT];
 };
 
-static void spg_coriolis_factors(ora_ctx *c);
+static void spg_coriolis_factors(ora_ctx *c, const double *ht_n, const double *e3f_n);
 static double *zalloc(size_t n) { return (double *)calloc(n ? n : 1, sizeof(double)); }
 
 /* Work arrays that stand for the reference's automatic arrays (undefined until
@@ -270,7 +270,7 @@ int ora_create(const nemo_dom_desc *d, const nemo_namelist *nam, ora_ctx **out) 
     c->icycle = jpit;
   }
   c->r2dt = 2.0 * nam->rn_rdt;
-  spg_coriolis_factors(c);
+  spg_coriolis_factors(c, c->ht_0, c->e3f_0);
   *out = c;
   return NEMO_OK;
 }
@@ -323,7 +323,7 @@ const int *ora_iarray(const ora_ctx *c, const char *name) {
   return NULL;
 }
 
-/* Field accessors with the rest-state default of the e3 fields (ln_linssh). */
+/* Field accessors with the rest-state default of the e3 fields and depths (ln_linssh). */
 static const double *fld(const ora_ctx *c, int id) {
   if (c->f[id]) return c->f[id];
   switch (id) {
@@ -331,6 +331,12 @@ static const double *fld(const ora_ctx *c, int id) {
     case NEMO_F_E3U_N: return c->e3u_0;
     case NEMO_F_E3V_N: return c->e3v_0;
     case NEMO_F_E3W_N: return c->e3w_0;
+    case NEMO_F_E3F_N: return c->e3f_0;
+    case NEMO_F_HT_N: return c->ht_0;
+    case NEMO_F_HU_N: case NEMO_F_HU_B: return c->hu_0;
+    case NEMO_F_HV_N: case NEMO_F_HV_B: return c->hv_0;
+    case NEMO_F_R1_HU_N: case NEMO_F_R1_HU_B: return c->r1_hu_0;
+    case NEMO_F_R1_HV_N: case NEMO_F_R1_HV_B: return c->r1_hv_0;
     default: return NULL;
   }
 }
@@ -961,11 +967,13 @@ int ora_tra_zdf(ora_ctx *c, int kt) {
   return NEMO_OK;
 }
 
-/* Coriolis factors of dyn_spg_ts (dynspg_ts.F90:241-342) for a linear free
- * surface: zwz = ff_f / hf (ENE/ENS/MIX) or the EEN/EET triads. The reference
- * computes them at kt = nit000; they depend only on the domain, so they are also
- * computed at context creation to give calls that start later the same values. */
-static void spg_coriolis_factors(ora_ctx *c) {
+/* Coriolis factors of dyn_spg_ts (dynspg_ts.F90:241-342): zwz = ff_f / hf
+ * (ENE/ENS/MIX) or the EEN/EET triads, from the now depths ht_n and e3f_n. The
+ * reference computes them at kt = nit000 for a linear free surface (rest-state
+ * depths; they depend only on the domain, so they are also computed at context
+ * creation to give calls that start later the same values) and at every step
+ * otherwise. */
+static void spg_coriolis_factors(ora_ctx *c, const double *ht_n, const double *e3f_n) {
   const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
   const size_t n2 = (size_t)jpi * jpj;
   const nemo_namelist *nm = &c->nam;
@@ -973,7 +981,6 @@ static void spg_coriolis_factors(ora_ctx *c) {
   double *zhf = zalloc(n2);
   const int sc = nm->nvor_scheme;
   if (sc == NEMO_VOR_EEN) {
-    const double *ht_n = c->ht_0;
     for (int jj = 1; jj <= jpj - 1; ++jj)
       for (int ji = 1; ji <= jpi - 1; ++ji) {
         double z;
@@ -998,7 +1005,7 @@ static void spg_coriolis_factors(ora_ctx *c) {
         c->ftsw[I2(ji, jj)] = w[I2(ji, jj - 1)] + w[I2(ji - 1, jj - 1)] + w[I2(ji - 1, jj)];
       }
   } else if (sc == NEMO_VOR_EET) {
-    const double *ht_n = c->ht_0, *ff = c->ff_f;
+    const double *ff = c->ff_f;
     for (int jj = 1; jj <= jpj; ++jj) {
       c->ftne[I2(1, jj)] = 0; c->ftnw[I2(1, jj)] = 0; c->ftse[I2(1, jj)] = 0; c->ftsw[I2(1, jj)] = 0;
     }
@@ -1024,7 +1031,7 @@ static void spg_coriolis_factors(ora_ctx *c) {
     for (int jk = 1; jk <= jpk - 1; ++jk)
       for (int jj = 1; jj <= jpj - 1; ++jj)
         for (int ji = 1; ji <= jpi; ++ji)
-          zhf[I2(ji, jj)] = zhf[I2(ji, jj)] + c->e3f_0[I3(ji, jj, jk)] * umask[I3(ji, jj, jk)] * umask[I3(ji, jj + 1, jk)];
+          zhf[I2(ji, jj)] = zhf[I2(ji, jj)] + e3f_n[I3(ji, jj, jk)] * umask[I3(ji, jj, jk)] * umask[I3(ji, jj + 1, jk)];
     lbc_closed(jpi, jpj, zhf, 1, 'F', 0.0);
     for (size_t p = 0; p < n2; ++p)
       if (zhf[p] != 0.0) c->zwz[p] = 1.0 / zhf[p];
@@ -1034,13 +1041,14 @@ static void spg_coriolis_factors(ora_ctx *c) {
 }
 
 /* ---------------------------------------------------------------- dyn_spg_ts */
-/* dynspg_ts.F90:121-1310 for ln_linssh = T without isf, wetting/drying, tides,
- * bdy, agrif, Stokes drift or assimilation increments. */
+/* dynspg_ts.F90:121-1310 without isf, wetting/drying, tides, bdy, agrif, Stokes
+ * drift or assimilation increments. Linear (ln_linssh) or variable-volume free
+ * surface; with a variable volume, vector-form (ln_dynadv_vec) or flux-form
+ * momentum. */
 int ora_dyn_spg_ts(ora_ctx *c, int kt) {
   const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
   const size_t n2 = (size_t)jpi * jpj;
   const nemo_namelist *nm = &c->nam;
-  if (!nm->ln_linssh) return NEMO_ERR_UNSUPPORTED;
   double *const *F = c->f;
   double *ua = F[NEMO_F_UA], *va = F[NEMO_F_VA], *un = F[NEMO_F_UN], *vn = F[NEMO_F_VN];
   double *ub = F[NEMO_F_UB], *vb = F[NEMO_F_VB];
@@ -1058,7 +1066,30 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
   if (!nm->ln_bt_fw && (!ub || !vb || !sshb || !utau_b || !vtau_b || !emp_b)) return NEMO_ERR_UNBOUND;
   if (nm->ln_apr_dyn && (!ssh_ib || (!nm->ln_bt_fw && !ssh_ibb))) return NEMO_ERR_UNBOUND;
   const double *umask = c->umask, *vmask = c->vmask, *e3u = fld(c, NEMO_F_E3U_N), *e3v = fld(c, NEMO_F_E3V_N);
-  const double *hu_n = c->hu_0, *hv_n = c->hv_0, *r1_hu_n = c->r1_hu_0, *r1_hv_n = c->r1_hv_0;
+  /* depths: the rest state for a linear free surface (domain.F90:149-183), the
+   * bound now / before depths of domvvl.F90 otherwise */
+  const int vvl = !nm->ln_linssh, flux = vvl && !nm->ln_dynadv_vec;
+  const double *hu_n = c->hu_0, *hv_n = c->hv_0, *r1_hu_n = c->r1_hu_0, *r1_hv_n = c->r1_hv_0, *ht_n = c->ht_0;
+  const double *hu_b = c->hu_0, *hv_b = c->hv_0, *r1_hu_b = c->r1_hu_0, *r1_hv_b = c->r1_hv_0;
+  const double *e3f_n = c->e3f_0;
+  const int sc = nm->nvor_scheme;
+  if (vvl) {
+    hu_n = F[NEMO_F_HU_N]; hv_n = F[NEMO_F_HV_N]; r1_hu_n = F[NEMO_F_R1_HU_N]; r1_hv_n = F[NEMO_F_R1_HV_N];
+    ht_n = F[NEMO_F_HT_N];
+    if (!hu_n || !hv_n || !r1_hu_n || !r1_hv_n || !ht_n) return NEMO_ERR_UNBOUND;
+    if (sc == NEMO_VOR_ENE || sc == NEMO_VOR_ENS || sc == NEMO_VOR_MIX) {
+      e3f_n = F[NEMO_F_E3F_N];
+      if (!e3f_n) return NEMO_ERR_UNBOUND;
+    }
+    if (!nm->ln_bt_fw || flux) {
+      hu_b = F[NEMO_F_HU_B]; hv_b = F[NEMO_F_HV_B];
+      if (!hu_b || !hv_b) return NEMO_ERR_UNBOUND;
+    }
+    if (!nm->ln_bt_fw) {
+      r1_hu_b = F[NEMO_F_R1_HU_B]; r1_hv_b = F[NEMO_F_R1_HV_B];
+      if (!r1_hu_b || !r1_hv_b) return NEMO_ERR_UNBOUND;
+    }
+  }
   const double *ssumask = c->ssumask, *ssvmask = c->ssvmask, *ssmask = c->ssmask;
   const double r1_2 = 0.5, r1_4 = 0.25, r1_8 = 0.125, r1_12 = 1.0 / 12.0;
   const double grav = nm->grav, r1_rau0 = 1.0 / nm->rau0, rdtbt = c->rdtbt;
@@ -1066,6 +1097,8 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
   double *zu_frc = walloc(n2), *zv_frc = walloc(n2), *zu_trd = walloc(n2), *zv_trd = walloc(n2);
   double *zwx = walloc(n2), *zwy = walloc(n2), *zssh_frc = walloc(n2), *zhdiv = walloc(n2);
   double *zsshp2_e = walloc(n2), *zCdU_u = walloc(n2), *zCdU_v = walloc(n2);
+  double *zhup2_e = walloc(n2), *zhvp2_e = walloc(n2), *zhtp2_e = walloc(n2);
+  double *zsshu_a = walloc(n2), *zsshv_a = walloc(n2), *zhust_e = walloc(n2), *zhvst_e = walloc(n2);
   double z2dt_bf = (kt == nm->nit000 && nm->neuler == 0) ? nm->rn_rdt : 2.0 * nm->rn_rdt;
   double r1_2dt_b = 1.0 / z2dt_bf;
   int ll_init = nm->ln_bt_av, ll_fw_start = 0;
@@ -1080,7 +1113,8 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
       zCdU_u[I2(ji, jj)] = r1_2 * (rCdU_bot[I2(ji + 1, jj)] + rCdU_bot[I2(ji, jj)]);
       zCdU_v[I2(ji, jj)] = r1_2 * (rCdU_bot[I2(ji, jj + 1)] + rCdU_bot[I2(ji, jj)]);
     }
-  if (kt == nm->nit000) spg_coriolis_factors(c);
+  /* (:241-343) at nit000, and at every step with a variable volume */
+  if (kt == nm->nit000 || vvl) spg_coriolis_factors(c, ht_n, e3f_n);
   if (!nm->ln_bt_fw && (nm->neuler == 0 && kt == nm->nit000 + 1)) {
     ll_fw_start = 0;
     ts_wgt(c, nm->ln_bt_av, ll_fw_start, &c->icycle, c->wgtbtp1, c->wgtbtp2);
@@ -1107,13 +1141,12 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
     zwx[p] = un_b[p] * hu_n[p] * c->e2u[p];
     zwy[p] = vn_b[p] * hv_n[p] * c->e1v[p];
   }
-  const int sc = nm->nvor_scheme;
   OMP_FOR
   for (int jj = 2; jj <= jpj - 1; ++jj)
     for (int ji = 2; ji <= jpi - 1; ++ji) {
       size_t p = I2(ji, jj);
       if (sc == NEMO_VOR_ENT) {
-        const double *e = c->e1e2t, *h = c->ht_0, *ft = c->ff_t;
+        const double *e = c->e1e2t, *h = ht_n, *ft = c->ff_t;
         zu_trd[p] = +r1_4 * c->r1_e1e2u[p] * r1_hu_n[p]
                     * (e[I2(ji + 1, jj)] * h[I2(ji + 1, jj)] * ft[I2(ji + 1, jj)] * (vn_b[I2(ji + 1, jj)] + vn_b[I2(ji + 1, jj - 1)])
                        + e[p] * h[p] * ft[p] * (vn_b[p] + vn_b[I2(ji, jj - 1)]));
@@ -1139,6 +1172,15 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
                                               + c->ftnw[p] * zwx[I2(ji - 1, jj)] + c->ftne[p] * zwx[p]);
       }
     }
+  /* variable volume: remove the surface pressure gradient (:447-509) */
+  if (vvl)
+    OMP_FOR
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t p = I2(ji, jj);
+        zu_trd[p] = zu_trd[p] - grav * (sshn[I2(ji + 1, jj)] - sshn[p]) * c->r1_e1u[p];
+        zv_trd[p] = zv_trd[p] - grav * (sshn[I2(ji, jj + 1)] - sshn[p]) * c->r1_e2v[p];
+      }
   /* (:511-516) */
   OMP_FOR
   for (int jj = 2; jj <= jpj - 1; ++jj)
@@ -1217,10 +1259,11 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
   for (size_t p = 0; p < n2; ++p) {
     if (ln_bt_fw) {
       c->sshn_e[p] = sshn[p]; c->un_e[p] = un_b[p]; c->vn_e[p] = vn_b[p];
+      c->hu_e[p] = hu_n[p]; c->hv_e[p] = hv_n[p]; c->hur_e[p] = r1_hu_n[p]; c->hvr_e[p] = r1_hv_n[p];
     } else {
       c->sshn_e[p] = sshb[p]; c->un_e[p] = ub_b[p]; c->vn_e[p] = vb_b[p];
+      c->hu_e[p] = hu_b[p]; c->hv_e[p] = hv_b[p]; c->hur_e[p] = r1_hu_b[p]; c->hvr_e[p] = r1_hv_b[p];
     }
-    c->hu_e[p] = hu_n[p]; c->hv_e[p] = hv_n[p]; c->hur_e[p] = r1_hu_n[p]; c->hvr_e[p] = r1_hv_n[p];
     ua_b[p] = 0; va_b[p] = 0; ssha[p] = 0; un_adv[p] = 0; vn_adv[p] = 0;
   }
   /* sub-step loop (:712-1207) */
@@ -1233,11 +1276,35 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
       c->ua_e[p] = za1 * c->un_e[p] + za2 * c->ub_e[p] + za3 * c->ubb_e[p];
       c->va_e[p] = za1 * c->vn_e[p] + za2 * c->vb_e[p] + za3 * c->vbb_e[p];
     }
-    /* linssh: zhup2_e = hu_n, zhvp2_e = hv_n (:788-792) */
+    /* ocean depth of the predictor (:738-792): from the extrapolated ssh with a
+     * variable volume, the now depth otherwise */
+    if (vvl) {
+      OMP_FOR
+      for (size_t p = 0; p < n2; ++p)
+        zsshp2_e[p] = za1 * c->sshn_e[p] + za2 * c->sshb_e[p] + za3 * c->sshbb_e[p];
+      OMP_FOR
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t p = I2(ji, jj);
+          zwx[p] = r1_2 * ssumask[p] * c->r1_e1e2u[p]
+                   * (c->e1e2t[p] * zsshp2_e[p] + c->e1e2t[I2(ji + 1, jj)] * zsshp2_e[I2(ji + 1, jj)]);
+          zwy[p] = r1_2 * ssvmask[p] * c->r1_e1e2v[p]
+                   * (c->e1e2t[p] * zsshp2_e[p] + c->e1e2t[I2(ji, jj + 1)] * zsshp2_e[I2(ji, jj + 1)]);
+        }
+      lbc_closed(jpi, jpj, zwx, 1, 'U', 0.0);
+      lbc_closed(jpi, jpj, zwy, 1, 'V', 0.0);
+      for (size_t p = 0; p < n2; ++p) {
+        zhup2_e[p] = c->hu_0[p] + zwx[p];
+        zhvp2_e[p] = c->hv_0[p] + zwy[p];
+        zhtp2_e[p] = c->ht_0[p] + zsshp2_e[p];
+      }
+    } else
+      for (size_t p = 0; p < n2; ++p) { zhup2_e[p] = hu_n[p]; zhvp2_e[p] = hv_n[p]; zhtp2_e[p] = ht_n[p]; }
+    /* fluxes at jn + 1/2 (:799-800) */
     OMP_FOR
     for (size_t p = 0; p < n2; ++p) {
-      zwx[p] = c->e2u[p] * c->ua_e[p] * hu_n[p];
-      zwy[p] = c->e1v[p] * c->va_e[p] * hv_n[p];
+      zwx[p] = c->e2u[p] * c->ua_e[p] * zhup2_e[p];
+      zwy[p] = c->e1v[p] * c->va_e[p] * zhvp2_e[p];
     }
     za2 = c->wgtbtp2[jn - 1];
     OMP_FOR
@@ -1254,6 +1321,20 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
     OMP_FOR
     for (size_t p = 0; p < n2; ++p) c->ssha_e[p] = (c->sshn_e[p] - rdtbt * (zssh_frc[p] + zhdiv[p])) * ssmask[p];
     lbc_closed(jpi, jpj, c->ssha_e, 1, 'T', 0.0);
+    /* ssh at u- and v-points of the new level (:888-900) */
+    if (vvl) {
+      OMP_FOR
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t p = I2(ji, jj);
+          zsshu_a[p] = r1_2 * ssumask[p] * c->r1_e1e2u[p]
+                       * (c->e1e2t[p] * c->ssha_e[p] + c->e1e2t[I2(ji + 1, jj)] * c->ssha_e[I2(ji + 1, jj)]);
+          zsshv_a[p] = r1_2 * ssvmask[p] * c->r1_e1e2v[p]
+                       * (c->e1e2t[p] * c->ssha_e[p] + c->e1e2t[I2(ji, jj + 1)] * c->ssha_e[I2(ji, jj + 1)]);
+        }
+      lbc_closed(jpi, jpj, zsshu_a, 1, 'U', 0.0);
+      lbc_closed(jpi, jpj, zsshv_a, 1, 'V', 0.0);
+    }
     if (jn == 1 && ll_init) { za0 = 1.0; za1 = 0.0; za2 = 0.0; za3 = 0.0; }
     else if (jn == 2 && ll_init) { za0 = 1.0833333333333; za1 = -0.1666666666666; za2 = 0.0833333333333; za3 = 0.0; }
     else if (nm->rn_bt_alpha == 0.0) { za0 = 0.614; za1 = 0.285; za2 = 0.088; za3 = 0.013; }
@@ -1268,15 +1349,28 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
     OMP_FOR
     for (size_t p = 0; p < n2; ++p)
       zsshp2_e[p] = za0 * c->ssha_e[p] + za1 * c->sshn_e[p] + za2 * c->sshb_e[p] + za3 * c->sshbb_e[p];
-    /* Coriolis (:1000-1056) with zhup2_e = hu_n (linssh) */
+    /* flux form: depth at u- and v-points of the AM4 ssh (:973-991) */
+    if (flux)
+      OMP_FOR
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t p = I2(ji, jj);
+          double zx1 = r1_2 * ssumask[p] * c->r1_e1e2u[p]
+                       * (c->e1e2t[p] * zsshp2_e[p] + c->e1e2t[I2(ji + 1, jj)] * zsshp2_e[I2(ji + 1, jj)]);
+          double zy1 = r1_2 * ssvmask[p] * c->r1_e1e2v[p]
+                       * (c->e1e2t[p] * zsshp2_e[p] + c->e1e2t[I2(ji, jj + 1)] * zsshp2_e[I2(ji, jj + 1)]);
+          zhust_e[p] = c->hu_0[p] + zx1;
+          zhvst_e[p] = c->hv_0[p] + zy1;
+        }
+    /* Coriolis (:1000-1056) */
     OMP_FOR
     for (int jj = 2; jj <= jpj - 1; ++jj)
       for (int ji = 2; ji <= jpi - 1; ++ji) {
         size_t p = I2(ji, jj);
         if (sc == NEMO_VOR_ENT) {
-          const double *e = c->e1e2t, *h = c->ht_0, *ft = c->ff_t;
-          double z1_hu = ssumask[p] / (hu_n[p] + 1.0 - ssumask[p]);
-          double z1_hv = ssvmask[p] / (hv_n[p] + 1.0 - ssvmask[p]);
+          const double *e = c->e1e2t, *h = zhtp2_e, *ft = c->ff_t;
+          double z1_hu = ssumask[p] / (zhup2_e[p] + 1.0 - ssumask[p]);
+          double z1_hv = ssvmask[p] / (zhvp2_e[p] + 1.0 - ssvmask[p]);
           zu_trd[p] = +r1_4 * c->r1_e1e2u[p] * z1_hu
                       * (e[I2(ji + 1, jj)] * h[I2(ji + 1, jj)] * ft[I2(ji + 1, jj)] * (c->va_e[I2(ji + 1, jj)] + c->va_e[I2(ji + 1, jj - 1)])
                          + e[p] * h[p] * ft[p] * (c->va_e[p] + c->va_e[I2(ji, jj - 1)]));
@@ -1320,13 +1414,33 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
         zwx[p] = (1.0 - nm->rn_scal_load) * zu_spg;
         zwy[p] = (1.0 - nm->rn_scal_load) * zv_spg;
       }
-    /* next velocities, vector form (:1106-1122) */
+    /* next velocities, vector form (:1106-1122) or flux form (:1124-1147) */
     OMP_FOR
     for (int jj = 2; jj <= jpj - 1; ++jj)
       for (int ji = 2; ji <= jpi - 1; ++ji) {
         size_t p = I2(ji, jj);
-        c->ua_e[p] = (c->un_e[p] + rdtbt * (zwx[p] + zu_trd[p] + zu_frc[p])) * ssumask[p];
-        c->va_e[p] = (c->vn_e[p] + rdtbt * (zwy[p] + zv_trd[p] + zv_frc[p])) * ssvmask[p];
+        if (!flux) {
+          c->ua_e[p] = (c->un_e[p] + rdtbt * (zwx[p] + zu_trd[p] + zu_frc[p])) * ssumask[p];
+          c->va_e[p] = (c->vn_e[p] + rdtbt * (zwy[p] + zv_trd[p] + zv_frc[p])) * ssvmask[p];
+        } else {
+          double zhura = c->hu_0[p] + zsshu_a[p];
+          double zhvra = c->hv_0[p] + zsshv_a[p];
+          zhura = ssumask[p] / (zhura + 1.0 - ssumask[p]);
+          zhvra = ssvmask[p] / (zhvra + 1.0 - ssvmask[p]);
+          c->ua_e[p] = (c->hu_e[p] * c->un_e[p]
+                        + rdtbt * (zhust_e[p] * zwx[p] + zhup2_e[p] * zu_trd[p] + hu_n[p] * zu_frc[p])) * zhura;
+          c->va_e[p] = (c->hv_e[p] * c->vn_e[p]
+                        + rdtbt * (zhvst_e[p] * zwy[p] + zhvp2_e[p] * zv_trd[p] + hv_n[p] * zv_frc[p])) * zhvra;
+        }
+      }
+    /* depth of the new level (:1159-1165) */
+    if (vvl)
+      OMP_FOR
+      for (size_t p = 0; p < n2; ++p) {
+        c->hu_e[p] = c->hu_0[p] + zsshu_a[p];
+        c->hv_e[p] = c->hv_0[p] + zsshv_a[p];
+        c->hur_e[p] = ssumask[p] / (c->hu_e[p] + 1.0 - ssumask[p]);
+        c->hvr_e[p] = ssvmask[p] / (c->hv_e[p] + 1.0 - ssvmask[p]);
       }
     lbc_closed(jpi, jpj, c->ua_e, 1, 'U', 0.0);
     lbc_closed(jpi, jpj, c->va_e, 1, 'V', 0.0);
@@ -1337,12 +1451,17 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
       c->vbb_e[p] = c->vb_e[p]; c->vb_e[p] = c->vn_e[p]; c->vn_e[p] = c->va_e[p];
       c->sshbb_e[p] = c->sshb_e[p]; c->sshb_e[p] = c->sshn_e[p]; c->sshn_e[p] = c->ssha_e[p];
     }
-    /* sums (:1190-1204) */
+    /* sums of velocities or transports (:1190-1204) */
     za1 = c->wgtbtp1[jn - 1];
     OMP_FOR
     for (size_t p = 0; p < n2; ++p) {
-      ua_b[p] = ua_b[p] + za1 * c->ua_e[p];
-      va_b[p] = va_b[p] + za1 * c->va_e[p];
+      if (!flux) {
+        ua_b[p] = ua_b[p] + za1 * c->ua_e[p];
+        va_b[p] = va_b[p] + za1 * c->va_e[p];
+      } else {
+        ua_b[p] = ua_b[p] + za1 * c->ua_e[p] * c->hu_e[p];
+        va_b[p] = va_b[p] + za1 * c->va_e[p] * c->hv_e[p];
+      }
       ssha[p] = ssha[p] + za1 * c->ssha_e[p];
     }
   }
@@ -1366,13 +1485,35 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
       vb2_b[p] = zwy[p];
     }
   }
-  OMP_FOR
-  for (int jk = 1; jk <= jpk - 1; ++jk)
+  if (!flux) {  /* (:1233-1240) */
+    OMP_FOR
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (size_t p = 0; p < n2; ++p) {
+        size_t q = p + n2 * (jk - 1);
+        ua[q] = ua[q] + (ua_b[p] - ub_b[p]) * r1_2dt_b;
+        va[q] = va[q] + (va_b[p] - vb_b[p]) * r1_2dt_b;
+      }
+  } else {     /* (:1241-1262) */
+    for (int jj = 1; jj <= jpj - 1; ++jj)
+      for (int ji = 1; ji <= jpi - 1; ++ji) {
+        size_t p = I2(ji, jj);
+        zsshu_a[p] = r1_2 * ssumask[p] * c->r1_e1e2u[p] * (c->e1e2t[p] * ssha[p] + c->e1e2t[I2(ji + 1, jj)] * ssha[I2(ji + 1, jj)]);
+        zsshv_a[p] = r1_2 * ssvmask[p] * c->r1_e1e2v[p] * (c->e1e2t[p] * ssha[p] + c->e1e2t[I2(ji, jj + 1)] * ssha[I2(ji, jj + 1)]);
+      }
+    lbc_closed(jpi, jpj, zsshu_a, 1, 'U', 0.0);
+    lbc_closed(jpi, jpj, zsshv_a, 1, 'V', 0.0);
+    OMP_FOR
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (size_t p = 0; p < n2; ++p) {
+        size_t q = p + n2 * (jk - 1);
+        ua[q] = ua[q] + r1_hu_n[p] * (ua_b[p] - ub_b[p] * hu_b[p]) * r1_2dt_b;
+        va[q] = va[q] + r1_hv_n[p] * (va_b[p] - vb_b[p] * hv_b[p]) * r1_2dt_b;
+      }
     for (size_t p = 0; p < n2; ++p) {
-      size_t q = p + n2 * (jk - 1);
-      ua[q] = ua[q] + (ua_b[p] - ub_b[p]) * r1_2dt_b;
-      va[q] = va[q] + (va_b[p] - vb_b[p]) * r1_2dt_b;
+      ua_b[p] = ua_b[p] / (c->hu_0[p] + zsshu_a[p] + 1.0 - ssumask[p]);
+      va_b[p] = va_b[p] / (c->hv_0[p] + zsshv_a[p] + 1.0 - ssvmask[p]);
     }
+  }
   OMP_FOR
   for (int jk = 1; jk <= jpk - 1; ++jk)
     for (size_t p = 0; p < n2; ++p) {
@@ -1382,6 +1523,7 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
     }
   free(zu_frc); free(zv_frc); free(zu_trd); free(zv_trd); free(zwx); free(zwy); free(zssh_frc); free(zhdiv);
   free(zsshp2_e); free(zCdU_u); free(zCdU_v);
+  free(zhup2_e); free(zhvp2_e); free(zhtp2_e); free(zsshu_a); free(zsshv_a); free(zhust_e); free(zhvst_e);
   return NEMO_OK;
 }
 

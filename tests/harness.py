@@ -7,6 +7,9 @@ from nemo_gpu import _ffi, gyre
 FIELDS_3D = ("un", "vn", "wn", "ub", "vb", "ua", "va", "avt", "uslp", "vslp", "wslpi", "wslpj")
 FIELDS_2D = ("sshn", "sshb", "un_b", "vn_b", "ub_b", "vb_b", "utau", "vtau", "emp")
 ACC_2D = ("SSHA", "UA_B", "VA_B", "UN_ADV", "VN_ADV", "UB2_B", "VB2_B", "UN_BF", "VN_BF")
+# variable volume (ln_linssh = 0): z* scale factors and depths of each state
+ZSTAR = ("E3T_B", "E3T_N", "E3T_A", "E3U_N", "E3V_N", "E3W_N", "E3F_N", "HT_N", "HU_N", "HV_N",
+         "R1_HU_N", "R1_HV_N", "HU_B", "HV_B", "R1_HU_B", "R1_HV_B")
 
 
 def relerr(ref, got):
@@ -28,6 +31,10 @@ class Pair:
         self.nam = gyre.namelist(**nam_over)
         self.nmem = nmem
         self.states = states or [gyre.state(self.dom, self.nam, seed=seed, member=m) for m in range(nmem)]
+        self.vvl = not self.nam["ln_linssh"]
+        if self.vvl:
+            for st in self.states:
+                st.update(gyre.zstar(self.dom, st))
         self.ora = [ora.Oracle(self.dom, self.nam) for _ in range(nmem)]
         self.ctx = api.Context(self.dom, self.nam, nmembers=nmem, prec=prec)
         self.torch = self.ctx.torch
@@ -77,6 +84,12 @@ class Pair:
         self.bind("RCDU_BOT", key="rcdu_bot")
         for n in ACC_2D:
             self.bind(n, zero=True, shape=self.s2)
+        if self.vvl:
+            self.bind_zstar()
+
+    def bind_zstar(self):
+        for n in ZSTAR:
+            self.bind(n)
 
     def bind_hotpath(self):
         self.bind("TSB", key="tsb")

@@ -220,6 +220,59 @@ def test_dyn_spg_ts(prec, case):
     _spg_compare(p, prec)
 
 
+# variable-volume free surface (ln_linssh = 0): vector- and flux-form momentum,
+# forward and centred integration, every vorticity scheme
+VVL_CASES = [
+    dict(),
+    dict(ln_dynadv_vec=0),
+    dict(ln_dynadv_vec=0, ln_bt_fw=0),
+    dict(ln_bt_fw=0, nvor_scheme=0),
+    dict(nvor_scheme=2),
+    dict(ln_dynadv_vec=0, nvor_scheme=2),
+    dict(nvor_scheme=3),
+    dict(ln_dynadv_vec=0, nvor_scheme=4, nn_een_e3f=1),
+    dict(nvor_scheme=4),
+    dict(nvor_scheme=5, ln_apr_dyn=1),
+    dict(ln_dynadv_vec=0, ln_bt_av=0, rn_bt_alpha=0.1),
+]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("case", range(len(VVL_CASES)))
+def test_dyn_spg_ts_variable_volume(prec, case):
+    p = _spg_pair(prec, dict(ln_linssh=0, **VVL_CASES[case]))
+    for kt in (5, 6):
+        for o in p.ora:
+            o.dyn_spg_ts(kt)
+        p.ctx.dyn_spg_ts(kt)
+        p.ctx.synchronize()
+    _spg_compare(p, prec)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("flux", [0, 1])
+def test_stp_hotpath_variable_volume(prec, flux):
+    """The full path with z* scale factors and depths, two members, from nit000."""
+    p = Pair(nn=2, prec=prec, seed=15, neuler=0, nmem=2, ln_linssh=0, ln_dynadv_vec=1 - flux)
+    p.bind_hotpath()
+    for kt in (1, 2, 3):
+        for o in p.ora:
+            o.stp_hotpath(kt)
+        p.ctx.stp_hotpath(kt)
+        p.ctx.synchronize()
+    p.compare("TSA", p.s4, tol(prec, "field"))
+    p.compare("AH_WSLP2", p.s3, tol(prec, "field"))
+    _spg_compare(p, prec)
+
+
+def test_variable_volume_requires_depths():
+    p = Pair(nn=1, prec="fp64", seed=16, ln_linssh=0)
+    p.bind_spg()
+    p.ctx.bind("HU_N", None)
+    with pytest.raises(RuntimeError):
+        p.ctx.dyn_spg_ts(5)
+
+
 @pytest.mark.parametrize("neuler", [0, 1])
 def test_dyn_spg_ts_first_steps(neuler):
     """kt = nit000 (Euler start or restart), then nit000 + 1."""

@@ -201,6 +201,66 @@ def test_spg_conserves_volume():
     assert np.abs(f["SSHA"]).max() > 0
 
 
+ZSTAR_FIELDS = ("HT_N", "HU_N", "HV_N", "R1_HU_N", "R1_HV_N", "HU_B", "HV_B", "R1_HU_B", "R1_HV_B", "E3F_N",
+                "E3T_B", "E3T_N", "E3T_A", "E3U_N", "E3V_N", "E3W_N")
+
+
+def _bind_zstar(o, dom, st, keep):
+    """Bind the z* scale factors and depths of the state (variable volume)."""
+    z = gyre.zstar(dom, st)
+    for n in ZSTAR_FIELDS:
+        keep[n] = z[n.lower()]
+        o.bind(n, keep[n])
+    return keep
+
+
+VVL_CASES = [dict(ln_dynadv_vec=1, ln_bt_fw=1), dict(ln_dynadv_vec=0, ln_bt_fw=1),
+             dict(ln_dynadv_vec=0, ln_bt_fw=0, nvor_scheme=4), dict(ln_dynadv_vec=1, ln_bt_fw=1, nvor_scheme=2)]
+
+
+@pytest.mark.parametrize("case", VVL_CASES, ids=["vec", "flux", "flux-centred-een", "vec-ent"])
+def test_spg_vvl_rest_stays_at_rest(case):
+    dom, nam, st, o = make(ln_linssh=0, **case)
+    f = _bind_spg(o, dom, st, zero_flow=True)
+    _bind_zstar(o, dom, {k: np.zeros_like(v) if k.startswith("ssh") else v for k, v in st.items()}, f)
+    for n in ("UTAU_B", "VTAU_B", "EMP_B"):
+        f[n] = np.zeros((dom["jpi"], dom["jpj"]), order="F")
+        o.bind(n, f[n])
+    o.dyn_spg_ts(5)
+    for n in ("SSHA", "UA_B", "VA_B", "UN_ADV", "VN_ADV"):
+        assert np.abs(f[n]).max() == 0.0, n
+    assert np.abs(f["ua"]).max() == 0.0 and np.abs(f["un"]).max() == 0.0
+
+
+@pytest.mark.parametrize("case", VVL_CASES, ids=["vec", "flux", "flux-centred-een", "vec-ent"])
+def test_spg_vvl_conserves_volume(case):
+    """The time-averaged ssh of the sub-steps keeps the volume of the now ssh when
+    there is no surface water flux (flux-form divergence, closed basin)."""
+    dom, nam, st, o = make(seed=9, ln_linssh=0, **case)
+    f = _bind_spg(o, dom, st)
+    _bind_zstar(o, dom, st, f)
+    for n, k in (("UTAU_B", "utau"), ("VTAU_B", "vtau"), ("EMP_B", "emp")):
+        f[n] = st[k].copy(order="F")
+        o.bind(n, f[n])
+    f["emp"][:] = 0.0
+    f["EMP_B"][:] = 0.0
+    o.dyn_spg_ts(5)
+    e1e2t = dom["e1t"] * dom["e2t"]
+    ssh0 = st["sshn"] if case["ln_bt_fw"] else st["sshb"]
+    v0 = math.fsum((e1e2t * ssh0).ravel())
+    v1 = math.fsum((e1e2t * f["SSHA"]).ravel())
+    assert abs(v1 - v0) <= 1e-12 * math.fsum(np.abs(e1e2t * ssh0).ravel())
+    assert np.abs(f["SSHA"]).max() > 0
+    assert np.isfinite(f["ua"]).all() and np.isfinite(f["UA_B"]).all()
+
+
+def test_spg_vvl_requires_depths():
+    dom, nam, st, o = make(ln_linssh=0)
+    _bind_spg(o, dom, st)
+    with pytest.raises(RuntimeError):
+        o.dyn_spg_ts(5)
+
+
 def test_lbc_closed():
     dom, nam, st, o = make()
     a = np.asfortranarray(np.random.default_rng(1).standard_normal((dom["jpi"], dom["jpj"], 3)))
@@ -253,6 +313,13 @@ def test_no_undefined_reads():
             o.dyn_spg_ts(5)
             for n in ("SSHA", "UA_B", "UN_ADV", "ua", "un"):
                 out[n] = f[n].copy()
+            for vec in (1, 0):  # variable volume, vector and flux form
+                dom, nam, st, o = make(seed=13, ln_linssh=0, ln_dynadv_vec=vec)
+                f = _bind_spg(o, dom, st)
+                _bind_zstar(o, dom, st, f)
+                o.dyn_spg_ts(5)
+                for n in ("SSHA", "UA_B", "UN_ADV", "ua", "un"):
+                    out[f"vvl{vec}_{n}"] = f[n].copy()
             return out
         finally:
             ora.set_poison(0)
