@@ -42,6 +42,19 @@ ALG_BYTES = {
     "dyn_spg_ts_3d": (80, 40),
     "dyn_spg_ts_substep_2d": (200, 140),
 }
+# the shelf workload (z* variable volume, partial steps) adds the 3-D scale factors
+# each routine reads: tra_adv e3u_n e3v_n e3t_b e3t_n e3t_a (5), tra_ldf e3u_n e3v_n
+# e3w_n e3t_n (4), tra_zdf e3t_b e3t_n e3t_a e3w_n (4), dyn_spg_ts e3u_n e3v_n e3f_n (3)
+ALG_BYTES_SHELF = {
+    "tra_adv": (128, 64),
+    "tra_ldf": (120, 60),
+    "tra_zdf": (96, 48),
+    "dyn_spg_ts_3d": (104, 52),
+    "dyn_spg_ts_substep_2d": (200, 140),
+}
+# fields of the shelf state bound on top of the GYRE hot-path set
+SHELF_FIELDS = ("gtsu", "gtsv", "ssh_ib", "e3t_b", "e3t_n", "e3t_a", "e3u_n", "e3v_n", "e3w_n", "e3f_n",
+                "ht_n", "hu_n", "hv_n", "r1_hu_n", "r1_hv_n", "hu_b", "hv_b", "r1_hu_b", "r1_hv_b")
 # algorithmic 3-D fields per cell of each kernel of the hot path (T and S, transports
 # computed on the fly, 1-D e3 profile, eddy diffusivity from the masks): every 3-D
 # array the kernel reads or writes, counted once; times the element size
@@ -125,12 +138,25 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def build_case(nn, nmem, seed):
+def build_case(nn, nmem, seed, workload="gyre"):
+    if workload == "shelf":  # 1000 x 1200 x 56 synthetic shelf, z* levels
+        from nemo_gpu import shelf
+        dom = shelf.domain(1000, 1200, 56, seed=seed)
+        nam = shelf.namelist()
+        states = [shelf.state(dom, nam, seed=seed, member=m) for m in range(nmem)]
+        return dom, nam, states
     from nemo_gpu import gyre
     dom = gyre.domain(nn)
     nam = gyre.namelist()
     states = [gyre.state(dom, nam, seed=seed, member=m) for m in range(nmem)]
     return dom, nam, states
+
+
+def workload_name(args):
+    if args.workload == "shelf":
+        return ("synthetic shelf 1000x1200x56 hot path step (dyn_spg_ts z* flux form + FCT 4/4 + iso ldf "
+                "with partial steps + zdf)")
+    return f"GYRE nn_GYRE={args.nn} hot path step (dyn_spg_ts + FCT + iso ldf + zdf)"
 
 
 HOT_3D = ("un", "vn", "wn", "ua", "va", "avt", "uslp", "vslp", "wslpi", "wslpj")
@@ -165,8 +191,11 @@ def make_ctx(dom, nam, states, prec, stream):
     put("AH_WSLP2", z3)
     put("AKZ", z3)
     z2 = [np.zeros_like(s["sshn"]) for s in states]
-    for n in ACC_2D:
-        put(n, z2, fp64=True)
+    for n in ACC_2D:  # the restart fields of a run in progress where the state has them
+        put(n, [s[n.lower()] for s in states] if n.lower() in states[0] else z2, fp64=True)
+    for n in SHELF_FIELDS:
+        if n in states[0]:
+            put(n.upper(), [s[n] for s in states])
     return ctx, dev
 
 
@@ -194,7 +223,7 @@ def run_gpu(args):
     rank, world = dist.init("nccl")
     _, _, local = dist.env_rank()
     torch.cuda.set_device(local)
-    dom, nam, states = build_case(args.nn, args.members, seed=100 + rank)
+    dom, nam, states = build_case(args.nn, args.members, seed=100 + rank, workload=args.workload)
     jpi, jpj, jpk = dom["jpi"], dom["jpj"], dom["jpk"]
     cells = jpi * jpj * jpk * args.members
     stream = torch.cuda.Stream()
@@ -246,7 +275,10 @@ def run_gpu(args):
             for n in ("UA", "VA", "UN", "VN"):
                 d_[n].copy_(c_.to_device([s[n.lower()] for s in states]))
             for n in ACC_2D:
-                d_[n].zero_()
+                if n.lower() in states[0]:
+                    d_[n].copy_(c_.to_device([s[n.lower()] for s in states], dtype=torch.float64))
+                else:
+                    d_[n].zero_()
             c_.stp_hotpath(kt0 + 5000)
             c_.synchronize()
         a32 = ctx.to_host(dev["TSA"], (jpi, jpj, jpk, 2))
@@ -265,6 +297,7 @@ def run_gpu(args):
     e2e = None
     if not args.no_e2e:
         ins = ["TSB", "TSN"] + [n.upper() for n in HOT_3D] + [n.upper() for n in HOT_2D] + ["RCDU_BOT"]
+        ins += [n.upper() for n in SHELF_FIELDS if n in states[0]]
         outs = ["TSA", "UA", "VA", "UN", "VN", "AH_WSLP2"] + list(ACC_2D)
         host = {}
         for n in set(ins + outs):
@@ -291,10 +324,11 @@ def run_gpu(args):
     # ---------------------------------------------------------------- roofline
     hbm, src = peaks()
     b = 1 if args.prec == "mixed" else 0
-    per_cell = {"tra_adv": ALG_BYTES["tra_adv"][b], "tra_ldf": ALG_BYTES["tra_ldf"][b],
-                "tra_zdf": ALG_BYTES["tra_zdf"][b],
-                "dyn_spg_ts": ALG_BYTES["dyn_spg_ts_3d"][b]
-                + ALG_BYTES["dyn_spg_ts_substep_2d"][b] * icycle / jpk}
+    AB = ALG_BYTES_SHELF if args.workload == "shelf" else ALG_BYTES
+    per_cell = {"tra_adv": AB["tra_adv"][b], "tra_ldf": AB["tra_ldf"][b],
+                "tra_zdf": AB["tra_zdf"][b],
+                "dyn_spg_ts": AB["dyn_spg_ts_3d"][b]
+                + AB["dyn_spg_ts_substep_2d"][b] * icycle / jpk}
     es = 4 if args.prec == "mixed" else 8
     n2 = jpi * jpj * args.members
 
@@ -305,6 +339,8 @@ def run_gpu(args):
             return KERNEL_BYTES_2D[name][b] * n2
         if name in ("iso_akz_edges", "iso_msc_edges"):  # edge columns only: ah_wslp2, akz
             return 2 * es * (2 * jpi + 2 * jpj) * jpk * args.members
+        if args.workload == "shelf":  # per-kernel models are for the GYRE kernels (1-D e3)
+            return 0
         return KERNEL_FIELDS.get(name, 0) * es * cells
 
     kernels = {}
@@ -314,7 +350,8 @@ def run_gpu(args):
         kernels[name] = {"us": us, "launches_per_step": nl / ntime, "alg_bytes": kb,
                          "alg_GBps": kb / (us / 1e6) / 1e9 if kb and us > 0 else None,
                          "frac": kb / (us / 1e6) / 1e9 / hbm if kb and us > 0 else None}
-    top = max(kernels, key=lambda k: kernels[k]["us"])
+    modelled = [k for k in kernels if kernels[k]["alg_bytes"]]
+    top = max(modelled or kernels, key=lambda k: kernels[k]["us"])
     achieved = kernels[top]["alg_GBps"]
     alg_bytes = kernels[top]["alg_bytes"]
     routines = {k: {"ms": rt[k], "alg_GBps": per_cell[k] * cells / (rt[k] / 1e3) / 1e9,
@@ -324,10 +361,11 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 bulk + f64 accumulators" if args.prec == "mixed" else "f64",
-        "data": "synthetic: seeded GYRE analytic state (no reference data files exist)",
-        "config": {"workload": f"GYRE nn_GYRE={args.nn} hot path step (dyn_spg_ts + FCT + iso ldf + zdf)",
+        "data": "synthetic: seeded GYRE analytic state (no reference data files exist)" if args.workload == "gyre"
+        else "synthetic: seeded shelf (lognormal bathymetry, z*, partial steps); no reference data files exist",
+        "config": {"workload": workload_name(args),
                    "grid": [jpi, jpj, jpk], "members": args.members, "cells": cells, "icycle": icycle,
-                   "nn_baro": nn_baro, "rdt": nam["rn_rdt"], "ln_bench": True,
+                   "nn_baro": nn_baro, "rdt": nam["rn_rdt"], "ln_bench": args.workload == "gyre",
                    "l2": "inputs larger than L2 (%.2f GB resident), no flush" % (
                        sum(t.numel() * t.element_size() for t in dev.values()) / 1e9),
                    "parallelism": f"replicas x{world}"},
@@ -345,13 +383,13 @@ def run_gpu(args):
     if fp64:
         res["speedup_vs_fp64"] = value / fp64["value"]
     if rank == 0 and world == 1 and not args.no_cpu:
-        res["cpu_baseline"] = cpu_baseline(dom, nam, states[0], budget_s=args.cpu_budget)
+        res["cpu_baseline"] = cpu_baseline(dom, nam, states[0], budget_s=args.cpu_budget, what=workload_name(args))
     ctx.close()
     if rank == 0:
         print(json.dumps(res))
 
 
-def cpu_baseline(dom, nam, st, budget_s=20.0, threads=None):
+def cpu_baseline(dom, nam, st, budget_s=20.0, threads=None, what="GYRE nn_GYRE=25 workload"):
     """The oracle (C FP64 restatement of the reference routines) on the host cores."""
     import numpy as np
     from oracle import ora
@@ -364,13 +402,17 @@ def cpu_baseline(dom, nam, st, budget_s=20.0, threads=None):
         o.bind(n.upper(), keep[n])
     keep["rc"] = np.array(st["rcdu_bot"], order="F", copy=True)
     o.bind("RCDU_BOT", keep["rc"])
+    for n in SHELF_FIELDS:
+        if n in st:
+            keep[n] = np.array(st[n], order="F", copy=True)
+            o.bind(n.upper(), keep[n])
     keep["tsa"] = np.zeros_like(st["tsb"], order="F")
     o.bind("TSA", keep["tsa"])
     for n in ("AH_WSLP2", "AKZ"):
         keep[n] = np.zeros_like(st["avt"], order="F")
         o.bind(n, keep[n])
     for n in ACC_2D:
-        keep[n] = np.zeros(st["sshn"].shape, order="F")
+        keep[n] = np.array(st[n.lower()], order="F", copy=True) if n.lower() in st else np.zeros(st["sshn"].shape, order="F")
         o.bind(n, keep[n])
     cells = dom["jpi"] * dom["jpj"] * dom["jpk"]
     t0 = time.perf_counter()
@@ -384,7 +426,7 @@ def cpu_baseline(dom, nam, st, budget_s=20.0, threads=None):
     nthr = int(os.environ.get("OMP_NUM_THREADS", "0") or 0) or os.cpu_count()
     o.close()
     return {"value": cells * n / dt, "unit": UNIT, "cores": nthr, "kind": "port",
-            "sample": f"{n} full hot-path steps of the same GYRE nn_GYRE=25 workload (FP64 oracle, OpenMP)"}
+            "sample": f"{n} full hot-path steps of the same {what} (FP64 oracle, OpenMP)"}
 
 
 def run_reference(args):
@@ -392,13 +434,13 @@ def run_reference(args):
     rank, world = dist.init("gloo")
     if rank != 0:
         return
-    dom, nam, states = build_case(args.nn, 1, seed=100)
-    cb = cpu_baseline(dom, nam, states[0], budget_s=max(5.0, min(60.0, 2.0 * args.steps)))
+    dom, nam, states = build_case(args.nn, 1, seed=100, workload=args.workload)
+    cb = cpu_baseline(dom, nam, states[0], budget_s=max(5.0, min(60.0, 2.0 * args.steps)), what=workload_name(args))
     res = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dom["jpi"] * dom["jpj"] * dom["jpk"] / cb["value"],
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-           "data": "synthetic: seeded GYRE analytic state",
-           "config": {"workload": f"GYRE nn_GYRE={args.nn} hot path step (dyn_spg_ts + FCT + iso ldf + zdf)",
+           "data": "synthetic: seeded GYRE analytic state" if args.workload == "gyre" else "synthetic: seeded shelf",
+           "config": {"workload": workload_name(args),
                       "grid": [dom["jpi"], dom["jpj"], dom["jpk"]], "members": 1},
            "cpu_baseline": cb,
            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -415,6 +457,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--prec", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--nn", type=int, default=25)
+    ap.add_argument("--workload", default="gyre", choices=["gyre", "shelf"],
+                    help="gyre: GYRE nn_GYRE=--nn (the headline); shelf: the 1000x1200x56 z* shelf")
     ap.add_argument("--members", type=int, default=1)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

@@ -109,6 +109,9 @@ typedef struct nemo_namelist {
   double rn_scal_load;    /* &namsbc_tide scalar loading factor                        */
   double grav;            /* phycst.F90:38                                             */
   double rau0;            /* reference density (eosbn2)                                */
+  int nn_fct_h;           /* &namtra_adv: FCT order in the horizontal (2 or 4; 0 = 2)  */
+  int nn_fct_v;           /*              and the vertical (2 or 4; 0 = 2), used by
+                             nemo_gpu_stp_hotpath                                       */
 } nemo_namelist;
 
 /* ------------------------------------------------------- module-global fields

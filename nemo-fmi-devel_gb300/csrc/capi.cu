@@ -813,6 +813,7 @@ int run_hotpath(nemo_ctx* c, int kt) {
   if (s) return s;
   mark(1);
   const double r2dt = (nm.neuler == 0 && kt == nm.nit000) ? nm.rn_rdt : 2.0 * nm.rn_rdt;
+  const int fct_h = nm.nn_fct_h ? nm.nn_fct_h : 2, fct_v = nm.nn_fct_v ? nm.nn_fct_v : 2;  // &namtra_adv
   if (fused) {
     // tsa = 0, tra_adv and tra_ldf (iso-neutral, first pass): the iso-neutral
     // fluxes, then the three FCT stages; the last adds both the corrected
@@ -821,7 +822,7 @@ int run_hotpath(nemo_ctx* c, int kt) {
     if (overlap) CK(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "join");
     else CK(launch_iso_flux<T>(dom_now<T>(c), la, c->stream), "iso fluxes");
     s = run_fct<T>(c, r2dt, F[NEMO_F_UN], F[NEMO_F_VN], F[NEMO_F_WN], 1, F[NEMO_F_TSB], F[NEMO_F_TSN], nullptr,
-                   F[NEMO_F_TSA], 2, 2, 2, &la);
+                   F[NEMO_F_TSA], 2, fct_h, fct_v, &la);
     if (s) return s;
     cudaError_t e = launch_iso_edges<T>(dom_now<T>(c), la, !nm.ln_traldf_msc, nm.ln_traldf_msc, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "iso edges");
@@ -829,7 +830,7 @@ int run_hotpath(nemo_ctx* c, int kt) {
   } else {
   // tsa = 0 (step.F90:234) folded into the first trend (pta_in = NULL)
   s = run_fct<T>(c, r2dt, F[NEMO_F_UN], F[NEMO_F_VN], F[NEMO_F_WN], 1, F[NEMO_F_TSB], F[NEMO_F_TSN], nullptr,
-                 F[NEMO_F_TSA], 2, 2, 2);
+                 F[NEMO_F_TSA], 2, fct_h, fct_v);
   if (s) return s;
   mark(2);
   if (nm.ln_traldf_iso)
@@ -883,6 +884,8 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
   if (dm->jpi < 4 || dm->jpj < 4 || dm->jpk < 3 || dm->jpk > KMAX || dm->jpk > 255) return bad(NEMO_ERR_UNSUPPORTED);
   if (dm->jperio != 0 || nam->ln_isfcav || nam->ln_zad_Aimp) return bad(NEMO_ERR_UNSUPPORTED);
   if (nam->nvor_scheme < 0 || nam->nvor_scheme > 5) return bad(NEMO_ERR_ARG);
+  for (int o : {nam->nn_fct_h, nam->nn_fct_v})
+    if (o != 0 && o != 2 && o != 4) return bad(NEMO_ERR_ARG);
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return bad(NEMO_ERR_CUDA);
   cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -963,7 +966,8 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
   c->gs_nblk = c->nsm * 4;
   if (cudaMalloc(&c->gs_part, 2 * (size_t)c->gs_nblk * c->nmem * 8) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
   if (cudaMalloc(&c->gs_out, (size_t)c->nmem * 8) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
-  if (ensure_fct_work(c, 2, 0)) return bad(NEMO_ERR_NOMEM);
+  // work arrays of the hot path allocated here, so graph capture never allocates
+  if (ensure_fct_work(c, 2, c->nam.nn_fct_v == 4)) return bad(NEMO_ERR_NOMEM);
   if (c->nam.ln_traldf_iso && ensure_iso_work(c, 2)) return bad(NEMO_ERR_NOMEM);
   if (cudaDeviceSynchronize() != cudaSuccess) return bad(NEMO_ERR_CUDA);
   *out = c;

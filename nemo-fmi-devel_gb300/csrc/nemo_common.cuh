@@ -135,7 +135,12 @@ __device__ __forceinline__ T rcount(T n) {
 // same role (far beyond any tracer value) without overflow.
 template <class T> struct Big;
 template <> struct Big<double> { static constexpr double v = 1.e+40; };
-template <> struct Big<float> { static constexpr float v = 1.e+30f; };
+// FP32: the masked extrema of a cell whose whole stencil is land are +-zbig, and
+// nonosc divides them by zrtrn = 1e-15 and scales by e1e2t e3t / p2dt (up to ~1e11):
+// 1e10 keeps that product finite in FP32 (1e30 overflowed to inf, and the limiter's
+// 0 * inf gave NaN) while staying far above any tracer value, so wet points are
+// limited exactly as with the reference's 1e40.
+template <> struct Big<float> { static constexpr float v = 1.e+10f; };
 
 // Grid barrier for persistent kernels launched cooperatively (all blocks resident).
 // Thread 0 of each block reads the generation (acquire), arrives on the counter

@@ -50,7 +50,8 @@ class Namelist(C.Structure):
                 ("ln_bt_auto", C.c_int), ("nn_baro", C.c_int), ("rn_bt_cmax", C.c_double),
                 ("rn_bt_alpha", C.c_double), ("nvor_scheme", C.c_int), ("nn_een_e3f", C.c_int),
                 ("ln_dynadv_vec", C.c_int), ("ln_sco", C.c_int), ("ln_apr_dyn", C.c_int),
-                ("rn_scal_load", C.c_double), ("grav", C.c_double), ("rau0", C.c_double)]
+                ("rn_scal_load", C.c_double), ("grav", C.c_double), ("rau0", C.c_double),
+                ("nn_fct_h", C.c_int), ("nn_fct_v", C.c_int)]
 
 
 def make_desc(dom):

@@ -32,7 +32,7 @@ def namelist(**over):
         rn_aht_0=(0.5 * 0.02) * 100.0e3, ln_zdfddm=0, ln_zad_Aimp=0,
         ln_bt_fw=1, ln_bt_av=1, nn_bt_flt=1, ln_bt_auto=1, nn_baro=30, rn_bt_cmax=0.8, rn_bt_alpha=0.0,
         nvor_scheme=1, nn_een_e3f=0, ln_dynadv_vec=1, ln_sco=0, ln_apr_dyn=0, rn_scal_load=0.0,
-        grav=GRAV, rau0=RAU0)
+        grav=GRAV, rau0=RAU0, nn_fct_h=2, nn_fct_v=2)
     nam.update(over)
     return nam
 
@@ -135,7 +135,7 @@ def _smooth(rng, shape, passes=2):
     return a
 
 
-def state(dom, nam, seed=0, noise_t=0.05, noise_s=0.01, u0=0.5, member=0):
+def state(dom, nam, seed=0, noise_t=0.05, noise_s=0.01, u0=0.5, member=0, noise_u=0.03):
     """Seeded synthetic state (one member) on a GYRE domain."""
     rng = np.random.default_rng([seed, member])
     jpi, jpj, jpk = dom["jpi"], dom["jpj"], dom["jpk"]
@@ -161,8 +161,8 @@ def state(dom, nam, seed=0, noise_t=0.05, noise_s=0.01, u0=0.5, member=0):
     ubt[:, 1:] = -(psi[:, 1:] - psi[:, :-1]) / e2[:, 1:]
     vbt[1:, :] = (psi[1:, :] - psi[:-1, :]) / e1[1:, :]
     prof = np.exp(-dom["gdept_1d"] / 600.0)
-    un = ubt[:, :, None] * prof[None, None, :] + 0.03 * rng.standard_normal((jpi, jpj, jpk))
-    vn = vbt[:, :, None] * prof[None, None, :] + 0.03 * rng.standard_normal((jpi, jpj, jpk))
+    un = ubt[:, :, None] * prof[None, None, :] + noise_u * rng.standard_normal((jpi, jpj, jpk))
+    vn = vbt[:, :, None] * prof[None, None, :] + noise_u * rng.standard_normal((jpi, jpj, jpk))
     un, vn = np.asfortranarray(un * um), np.asfortranarray(vn * vm)
     # w from continuity (sshwzv.F90 wzv, linear free surface)
     e2u, e1v, e1e2t = dom["e2u"], dom["e1v"], dom["e1t"] * dom["e2t"]
@@ -221,19 +221,22 @@ def state(dom, nam, seed=0, noise_t=0.05, noise_s=0.01, u0=0.5, member=0):
     uslp, vslp, wslpi, wslpj = slope(um), slope(vm), slope(wm), slope(wm)
     wslpi[:, :, 0] = 0.0
     wslpj[:, :, 0] = 0.0
+    # restart fields of a run in progress (dynspg_ts.F90:1214-1227): the half-step
+    # transports of the previous step, close to the now barotropic transports
+    ub2_b, vb2_b = np.asfortranarray(un_b * hu), np.asfortranarray(vn_b * hv)
     return dict(tsb=ts, tsn=tsn, un=un, vn=vn, wn=wn, ub=ub, vb=vb, ua=ua, va=va,
-                un_b=un_b, vn_b=vn_b, ub_b=ub_b, vb_b=vb_b, sshn=sshn, sshb=sshb,
+                un_b=un_b, vn_b=vn_b, ub_b=ub_b, vb_b=vb_b, sshn=sshn, sshb=sshb, ub2_b=ub2_b, vb2_b=vb2_b,
                 utau=utau, vtau=vtau, emp=emp, rcdu_bot=rcdu, avt=avt,
                 uslp=uslp, vslp=vslp, wslpi=wslpi, wslpj=wslpj)
 
 
-def zstar(dom, st):
+def zstar(dom, st, ssha=None):
     """Variable-volume (z*) scale factors and depths of a state: the fields
     domvvl.F90 maintains when ln_linssh = .false. -- e3t = e3t_0 (ht_0 + ssh) /
     (ht_0 + 1 - ssmask) on wet levels (:849-851), e3u/e3v/e3f/e3w interpolated from
     the e3t changes as dom_vvl_interpol does, column depths and their masked
-    inverses (:183-196). Before / now / after levels use sshb, sshn and a linear
-    extrapolation sshn + (sshn - sshb)."""
+    inverses (:183-196). Before / now / after levels use sshb, sshn and ssha (by
+    default the linear extrapolation sshn + (sshn - sshb))."""
     tm, um, vm, wm = masks(dom)
     e1e2t = dom["e1t"] * dom["e2t"]
     e1e2u = dom["e1u"] * dom["e2u"]
@@ -277,7 +280,8 @@ def zstar(dom, st):
     def inv(h, m):
         return f(m / (h + 1.0 - m))
 
-    ssha = (st["sshn"] + (st["sshn"] - st["sshb"])) * ssmask
+    if ssha is None:
+        ssha = (st["sshn"] + (st["sshn"] - st["sshb"])) * ssmask
     e3t_b, e3t_n, e3t_a = e3t_of(st["sshb"]), e3t_of(st["sshn"]), e3t_of(ssha)
     e3u_b, e3u_n, e3v_b, e3v_n = to_u(e3t_b), to_u(e3t_n), to_v(e3t_b), to_v(e3t_n)
     hu_b, hu_n = f((e3u_b * um)[:, :, :-1].sum(axis=2)), f((e3u_n * um)[:, :, :-1].sum(axis=2))

@@ -1554,7 +1554,7 @@ int ora_glob_sum(ora_ctx *c, const double *ptab, int nk, double *out) {
 
 /* ---------------------------------------------------------- one hot-path step */
 /* step.F90:194-257 on the bound fields: dyn_spg_ts, tsa = 0, tra_adv (transports
- * + FCT), tra_ldf (iso or lap), tra_zdf. FCT orders come from kn_fct_h/v = 2. */
+ * + FCT), tra_ldf (iso or lap), tra_zdf. FCT orders from nn_fct_h/v (0 = 2). */
 int ora_stp_hotpath(ora_ctx *c, int kt) {
   const nemo_namelist *nm = &c->nam;
   const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk;
@@ -1566,7 +1566,8 @@ int ora_stp_hotpath(ora_ctx *c, int kt) {
   double r2dt = (nm->neuler == 0 && kt == nm->nit000) ? nm->rn_rdt : 2.0 * nm->rn_rdt;
   double *zun = zalloc(n3), *zvn = zalloc(n3), *zwn = zalloc(n3);
   ora_tra_adv_trp(c, c->f[NEMO_F_UN], c->f[NEMO_F_VN], c->f[NEMO_F_WN], zun, zvn, zwn);
-  st = ora_tra_adv_fct(c, kt, nm->nit000, "TRA", r2dt, zun, zvn, zwn, tsb, tsn, tsa, 2, 2, 2);
+  st = ora_tra_adv_fct(c, kt, nm->nit000, "TRA", r2dt, zun, zvn, zwn, tsb, tsn, tsa, 2, nm->nn_fct_h ? nm->nn_fct_h : 2,
+                       nm->nn_fct_v ? nm->nn_fct_v : 2);
   free(zun); free(zvn); free(zwn);
   if (st) return st;
   const double *ahtu = c->f[NEMO_F_AHTU], *ahtv = c->f[NEMO_F_AHTV];

@@ -18,23 +18,26 @@ def relerr(ref, got):
     got = np.asarray(got, dtype=np.float64)
     d = np.abs(got - ref).max() if ref.size else 0.0
     s = np.abs(ref).max() if ref.size else 0.0
+    if not (np.isfinite(d) and np.isfinite(s)):  # a NaN or inf anywhere fails
+        return float("inf")
     return 0.0 if d == 0 else d / (s if s > 0 else 1.0)
 
 
 class Pair:
     """Oracle(s) and a GPU context holding identical inputs."""
 
-    def __init__(self, nn=1, prec="fp64", nmem=1, seed=0, states=None, jpk=31, **nam_over):
+    def __init__(self, nn=1, prec="fp64", nmem=1, seed=0, states=None, jpk=31, dom=None, nam=None, **nam_over):
         from nemo_gpu import api
         from oracle import ora
-        self.dom = gyre.domain(nn, jpk=jpk)
-        self.nam = gyre.namelist(**nam_over)
+        self.dom = dom or gyre.domain(nn, jpk=jpk)
+        self.nam = nam or gyre.namelist(**nam_over)
         self.nmem = nmem
         self.states = states or [gyre.state(self.dom, self.nam, seed=seed, member=m) for m in range(nmem)]
         self.vvl = not self.nam["ln_linssh"]
         if self.vvl:
             for st in self.states:
-                st.update(gyre.zstar(self.dom, st))
+                if "ht_n" not in st:
+                    st.update(gyre.zstar(self.dom, st))
         self.ora = [ora.Oracle(self.dom, self.nam) for _ in range(nmem)]
         self.ctx = api.Context(self.dom, self.nam, nmembers=nmem, prec=prec)
         self.torch = self.ctx.torch

@@ -64,6 +64,28 @@ def test_tra_adv_fct(prec, kh, kv):
     assert relerr(ta, p.ctx.to_host(ta_dev, p.s4)) <= tol(prec, "trend")
 
 
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("kh,kv", [(2, 2), (4, 4)])
+def test_tra_adv_fct_shelf(prec, kh, kv):
+    """FCT over a bathymetry: interior columns with land below their bottom cell, where
+    the limiter's masked extrema (+-zbig) are all the stencil holds; z* scale factors."""
+    from nemo_gpu import shelf
+    dom = shelf.domain(40, 36, 56, seed=5)
+    nam = shelf.namelist()
+    st = shelf.state(dom, nam, seed=6)
+    p = Pair(prec=prec, dom=dom, nam=nam, states=[st])
+    for n in ("E3T_B", "E3T_N", "E3T_A", "E3U_N", "E3V_N", "E3W_N"):
+        p.bind(n)
+    zun, zvn, zwn = p.ora[0].tra_adv_trp(st["un"], st["vn"], st["wn"])
+    ta = np.zeros(p.s4, order="F")
+    ta_dev = p.to_dev([ta])
+    p.ora[0].tra_adv_fct(5, 1, "TRA", 600.0, zun, zvn, zwn, st["tsb"], st["tsn"], ta, 2, kh, kv)
+    p.ctx.tra_adv_fct(5, 1, "TRA", 600.0, p.to_dev([zun]), p.to_dev([zvn]), p.to_dev([zwn]),
+                      p.to_dev([st["tsb"]]), p.to_dev([st["tsn"]]), ta_dev, 2, kh, kv)
+    p.ctx.synchronize()
+    assert relerr(ta, p.ctx.to_host(ta_dev, p.s4)) <= tol(prec, "trend")
+
+
 def test_tra_adv_fct_passive_tracers():
     """cdtype = TRC with kjpt = 3 (trcadv.F90:127 calls the same routine)."""
     p = Pair(nn=1, prec="fp64", seed=3)
@@ -255,6 +277,30 @@ def test_stp_hotpath_variable_volume(prec, flux):
     """The full path with z* scale factors and depths, two members, from nit000."""
     p = Pair(nn=2, prec=prec, seed=15, neuler=0, nmem=2, ln_linssh=0, ln_dynadv_vec=1 - flux)
     p.bind_hotpath()
+    for kt in (1, 2, 3):
+        for o in p.ora:
+            o.stp_hotpath(kt)
+        p.ctx.stp_hotpath(kt)
+        p.ctx.synchronize()
+    p.compare("TSA", p.s4, tol(prec, "field"))
+    p.compare("AH_WSLP2", p.s3, tol(prec, "field"))
+    _spg_compare(p, prec)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_stp_hotpath_shelf(prec):
+    """The shelf configuration at reduced horizontal size (56 levels): z* variable
+    volume, partial bottom cells with their bottom gradients, FCT 4/4 through the
+    compact vertical interpolation, iso-neutral diffusion, EEN vorticity, flux-form
+    momentum and atmospheric pressure, nn_baro = 30, two members."""
+    from nemo_gpu import shelf
+    dom = shelf.domain(72, 56, 56, seed=3)
+    nam = shelf.namelist(neuler=0)
+    states = [shelf.state(dom, nam, seed=4, member=m) for m in range(2)]
+    p = Pair(prec=prec, nmem=2, dom=dom, nam=nam, states=states)
+    p.bind_hotpath()
+    for n in ("GTSU", "GTSV", "SSH_IB"):
+        p.bind(n)
     for kt in (1, 2, 3):
         for o in p.ora:
             o.stp_hotpath(kt)

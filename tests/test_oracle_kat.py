@@ -327,3 +327,40 @@ def test_no_undefined_reads():
     for k in a:
         assert np.isfinite(b[k]).all(), k
         np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+
+
+def test_shelf_domain_partial_cells():
+    """The synthetic shelf: partial bottom cells no thicker than their level, u/v
+    thicknesses the minima of their T-neighbours, column depths equal to the
+    bathymetry within the partial-cell rule, and a finite oracle hot-path step."""
+    from nemo_gpu import shelf
+    dom = shelf.domain(28, 24, 56, seed=1)
+    tm, um, vm, _ = gyre.masks(dom)
+    e3t1 = dom["e3t_0"][0, 0, :]
+    kb = dom["k_bot"]
+    wet = kb > 0
+    assert wet.sum() > 0.3 * wet.size
+    ii, jj = np.nonzero(wet)
+    ik = kb[ii, jj] - 1
+    part = dom["e3t_0"][ii, jj, ik]
+    assert (part > 0).all() and (part <= e3t1[ik] + 1e-12).all()
+    e3t = dom["e3t_0"]
+    np.testing.assert_array_equal(dom["e3u_0"][:-1, :-1], np.minimum(e3t[:-1, :-1], e3t[1:, :-1]))
+    np.testing.assert_array_equal(dom["e3v_0"][:-1, :-1], np.minimum(e3t[:-1, :-1], e3t[:-1, 1:]))
+    assert (np.diff(tm, axis=2) <= 0).all()          # wet levels are contiguous from the top
+    nam = shelf.namelist(neuler=0)
+    st = shelf.state(dom, nam, seed=2)
+    o = ora.Oracle(dom, nam)
+    keep = _bind_spg(o, dom, st)
+    for n in ("TSB", "TSN", "WN", "AVT", "USLP", "VSLP", "WSLPI", "WSLPJ", "GTSU", "GTSV", "SSH_IB"):
+        keep[n] = st[n.lower()].copy(order="F")
+        o.bind(n, keep[n])
+    _bind_zstar(o, dom, st, keep)
+    for n, shape in (("TSA", st["tsb"].shape), ("AH_WSLP2", st["avt"].shape), ("AKZ", st["avt"].shape)):
+        keep[n] = np.zeros(shape, order="F")
+        o.bind(n, keep[n])
+    for kt in (1, 2):
+        o.stp_hotpath(kt)
+    assert np.isfinite(keep["TSA"]).all() and np.isfinite(keep["ua"]).all() and np.abs(keep["SSHA"]).max() > 0
+    icycle, nn_baro, _ = o.spg_info()
+    assert nn_baro == 30 and icycle == 44
