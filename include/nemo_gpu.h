@@ -309,6 +309,7 @@ enum nemo_kernel_id {
   NEMO_K_ISO_FLUX, NEMO_K_ISO_DIV, NEMO_K_ISO_AKZ_EDGES, NEMO_K_ISO_MSC_EDGES, NEMO_K_ZDF_IMP,
   NEMO_K_CLAMP, NEMO_K_SPG_P1A, NEMO_K_SPG_P1B, NEMO_K_SPG_P2, NEMO_K_SPG_P3,
   NEMO_K_SPG_COR,   /* variable volume: Coriolis factors of the step */
+  NEMO_K_ISO_FLUX_TMA, /* iso-neutral fluxes with TMA-staged tracer planes */
   NEMO_K_COUNT
 };
 
@@ -327,6 +328,11 @@ int nemo_gpu_get_kernel_timing(nemo_ctx *ctx, double *ms, int *launches, int n);
  * iso-neutral laplacian) nemo_gpu_stp_hotpath runs FCT advection and iso-neutral
  * diffusion as one fused kernel; on = 0 forces the per-routine kernels. */
 int nemo_gpu_set_fusion(nemo_ctx *ctx, int on);
+
+/* on = 1 (default): in a mixed-precision context, the iso-neutral flux kernel of that
+ * configuration stages the tracer planes in shared memory with tensor copies (TMA)
+ * when jpi is a multiple of 4; on = 0 forces the kernel without TMA. Same results. */
+int nemo_gpu_set_tma(nemo_ctx *ctx, int on);
 
 /* ------------------------------------------------------------ test hook */
 

@@ -93,6 +93,7 @@ struct nemo_ctx {
   // per-routine timing of the hot path (the ln_timing of timing.F90:89-212)
   bool timing = false;
   bool no_fusion = false;  // force the per-routine kernels (tests compare both)
+  bool no_tma = false;     // force the kernels without TMA staging (tests compare both)
   cudaEvent_t tev[5] = {};
   double tms[4] = {0, 0, 0, 0};
   int tcalls = 0;
@@ -627,6 +628,7 @@ int iso_args(nemo_ctx* c, int kt, int kit000, const void* pahu, const void* pahv
   a.ah_wslp2 = (T*)c->f[NEMO_F_AH_WSLP2]; a.akz = (T*)c->f[NEMO_F_AKZ];
   a.lap = nm.ln_traldf_lap; a.blp = nm.ln_traldf_blp; a.msc = nm.ln_traldf_msc;
   a.zftu = (T*)c->iso_w[0]; a.zftv = (T*)c->iso_w[1]; a.ztfw = (T*)c->iso_w[2];
+  a.tma = !c->no_tma; a.err = c->err_flag;
   const double z2dt = (nm.neuler == 0 && kt == nm.nit000) ? nm.rn_rdt : 2.0 * nm.rn_rdt;
   a.z2dt = (T)z2dt; a.z1_2dt = (T)(1.0 / z2dt);
   if (kpass == 1 && kt == kit000) {
@@ -1028,6 +1030,7 @@ int nemo_gpu_synchronize(nemo_ctx* c) {
   if (flag) {
     cudaMemset(c->err_flag, 0, sizeof(int));
     cudaMemset(c->bar_mem, 0, 2 * sizeof(unsigned int));
+    if (flag == TM_ERR) return fail(c, NEMO_ERR_TIMEOUT, "a tensor copy of the iso-neutral flux kernel did not arrive");
     return fail(c, NEMO_ERR_TIMEOUT, "a grid barrier of the barotropic sub-step kernel timed out");
   }
   return NEMO_OK;
@@ -1298,6 +1301,14 @@ int nemo_gpu_get_timing(nemo_ctx* c, double* ms, int* ncalls) {
 int nemo_gpu_set_fusion(nemo_ctx* c, int on) {
   if (!c) return NEMO_ERR_ARG;
   c->no_fusion = !on;
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);
+  c->graphs.clear();
+  return NEMO_OK;
+}
+
+int nemo_gpu_set_tma(nemo_ctx* c, int on) {
+  if (!c) return NEMO_ERR_ARG;
+  c->no_tma = !on;
   for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);
   c->graphs.clear();
   return NEMO_OK;

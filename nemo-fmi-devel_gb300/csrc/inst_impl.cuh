@@ -1,8 +1,13 @@
 // inst_impl.cuh -- definitions of the launchers declared in launch.h; included by
 // inst_fp64.cu and inst_fp32.cu, each of which instantiates one precision.
 #pragma once
+#include <cudaTypedefs.h>
+
+#include <cstdint>
+
 #include "launch.h"
 #include "k_hot.cuh"
+#include "k_tma.cuh"
 
 namespace nemo {
 
@@ -73,10 +78,55 @@ cudaError_t launch_ldf_iso(const Dom<T>& d, const LdfArgs<T>& a, int copy_akz_ed
   return launch_iso_edges<T>(d, a, copy_akz_edges, msc_edges, s);
 }
 
+// cuTensorMapEncodeTiled from the driver, through the runtime (no libcuda link)
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    return (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }();
+  return fn;
+}
+
+// Tensor map of nf 3-D fields of floats stored one after the other per member, as a
+// 3-D tensor (jpi, jpj, jpk * nf * nmem), with a box of bx x by points of one level.
+// False (no TMA) when the rows are not a multiple of 16 bytes (jpi % 4 != 0) or the
+// base is not 16-byte aligned.
+template <class T>
+static bool field_tensor_map(const Dom<T>& d, const T* base, int nf, unsigned bx, unsigned by, CUtensorMap* map) {
+  const auto fn = tensor_map_encoder();
+  if (!fn || sizeof(T) != 4 || d.jpi % 4 != 0 || ((uintptr_t)base & 15) != 0) return false;
+  cuuint64_t dims[3] = {(cuuint64_t)d.jpi, (cuuint64_t)d.jpj, (cuuint64_t)d.jpk * nf * d.nmem};
+  cuuint64_t strides[2] = {(cuuint64_t)d.jpi * sizeof(T), (cuuint64_t)d.n2 * sizeof(T)};
+  cuuint32_t box[3] = {bx, by, 1}, es[3] = {1, 1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)base, dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template <class T>
 cudaError_t launch_iso_flux(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s) {
-  if (hot_iso_ok(d, a)) k_iso_flux_hot<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
-  else k_iso_flux<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  if (hot_iso_ok(d, a)) {
+    if constexpr (sizeof(T) == 4) {
+      IsoMaps maps;
+      if (a.tma && a.err && field_tensor_map(d, a.ptb.p, a.kjpt, TM_W, TM_H, &maps.tb) &&
+          field_tensor_map(d, a.uslp.p, 1, TM_X, TM_Y, &maps.uslp) &&
+          field_tensor_map(d, a.vslp.p, 1, TM_X, TM_Y, &maps.vslp) &&
+          field_tensor_map(d, a.wslpi.p, 1, TM_X, TM_Y, &maps.wslpi) &&
+          field_tensor_map(d, a.wslpj.p, 1, TM_X, TM_Y, &maps.wslpj)) {
+        const dim3 grid((d.jpi + TM_X - 1) / TM_X, (d.jpj + TM_Y - 1) / TM_Y, d.nmem * ((d.jpk + KCH - 1) / KCH));
+        k_iso_flux_tma<T><<<grid, dim3(TM_X, TM_Y), 0, s>>>(d, a, maps, a.err, 1 << 16);
+        ktick(NEMO_K_ISO_FLUX_TMA, s);
+        return cudaGetLastError();
+      }
+    }
+    k_iso_flux_hot<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  } else {
+    k_iso_flux<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  }
   ktick(NEMO_K_ISO_FLUX, s);
   return cudaGetLastError();
 }

@@ -124,6 +124,8 @@ struct LdfArgs {
   int lap, blp, msc;
   T z2dt, z1_2dt;
   T *zftu, *zftv, *ztfw;     // work: iso-neutral fluxes (jpi,jpj,jpk,kjpt)
+  int tma;                   // FP32 hot configuration: stage the tracer planes by TMA
+  int* err;                  // device error flag (a timed-out wait of the TMA kernel)
 };
 
 // Arguments shared by the three FCT kernels.

@@ -133,6 +133,10 @@ __device__ __forceinline__ T rcount(T n) {
 
 // Land sentinel of nonosc (traadv_fct.F90:354). 1e40 overflows FP32; 1e30 keeps the
 // same role (far beyond any tracer value) without overflow.
+// value of the device error flag after a timed-out wait on a tensor copy (a timed-out
+// grid barrier of the sub-step kernel writes NEMO_ERR_TIMEOUT)
+constexpr int TM_ERR = 2;
+
 template <class T> struct Big;
 template <> struct Big<double> { static constexpr double v = 1.e+40; };
 // FP32: the masked extrema of a cell whose whole stencil is land are +-zbig, and

@@ -118,6 +118,7 @@ def load(path):
     _proto(lib, "nemo_gpu_set_barrier_limit", i, [vp, C.c_longlong, i])
     _proto(lib, "nemo_gpu_set_timing", i, [vp, i])
     _proto(lib, "nemo_gpu_set_fusion", i, [vp, i])
+    _proto(lib, "nemo_gpu_set_tma", i, [vp, i])
     _proto(lib, "nemo_gpu_get_timing", i, [vp, C.POINTER(d), C.POINTER(i)])
     _proto(lib, "nemo_gpu_get_kernel_timing", i, [vp, C.POINTER(d), C.POINTER(i), i])
     return lib

@@ -123,6 +123,9 @@ class Context:
     def set_fusion(self, on):
         self._ck(self.lib.nemo_gpu_set_fusion(self.h, int(on)), "set_fusion")
 
+    def set_tma(self, on):
+        self._ck(self.lib.nemo_gpu_set_tma(self.h, int(on)), "set_tma")
+
     def set_timing(self, on):
         self._ck(self.lib.nemo_gpu_set_timing(self.h, int(on)), "set_timing")
 

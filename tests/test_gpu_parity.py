@@ -457,3 +457,31 @@ def test_fused_tracer_kernel_matches_per_routine_kernels(msc):
         res[fusion] = {n: p.ctx.to_host(p.dev[n], s) for n, s in (("TSA", p.s4), ("AH_WSLP2", p.s3), ("AKZ", p.s3))}
     for n in res[1]:
         assert relerr(res[0][n], res[1][n]) <= TOL32_FIELD, n
+
+
+@pytest.mark.parametrize("nmem", [1, 2])
+def test_iso_flux_tma_matches_plain_kernel(nmem):
+    """The FP32 iso-neutral flux kernel with TMA-staged tracer planes (jpi = 92, a
+    multiple of 4) against the same kernel reading global memory: identical results
+    (same arithmetic; the vertical term it leaves out is exactly 0), and both against
+    the oracle, over three steps with two level chunks per column."""
+    res = {}
+    for tma in (1, 0):
+        p = Pair(nn=3, prec="mixed", seed=17, nmem=nmem)
+        p.ctx.set_tma(tma)
+        p.bind_hotpath()
+        p.ctx.set_timing(True)  # per-kernel launch counts show which kernel ran
+        for kt in (5, 6, 7):
+            for o in p.ora:
+                o.stp_hotpath(kt)
+            p.ctx.stp_hotpath(kt)
+            p.ctx.synchronize()
+        ran = p.ctx.get_kernel_timing()
+        assert ("iso_flux_tma" in ran) == bool(tma) and ("iso_flux" in ran) != bool(tma), ran
+        p.compare("TSA", p.s4, TOL32_FIELD)
+        p.compare("AH_WSLP2", p.s3, TOL32_FIELD)
+        p.compare("AKZ", p.s3, TOL32_FIELD)
+        res[tma] = {n: p.ctx.to_host(p.dev[n], s) for n, s in (("TSA", p.s4), ("AH_WSLP2", p.s3), ("AKZ", p.s3))}
+    for n in res[1]:
+        a, b = np.asarray(res[0][n]), np.asarray(res[1][n])
+        assert np.array_equal(a, b), f"{n}: TMA and plain kernels differ (max {np.abs(a - b).max():.3e})"
