@@ -64,6 +64,9 @@ KERNEL_FIELDS = {
     "fct_c": 20,     # read ax ay az betup betdo (x2), zftu zftv ztfw (x2); ta(2) read+write
     "iso_flux": 14,  # read tb(2) uslp vslp wslpi wslpj; write ah_wslp2 akz, zftu zftv ztfw (x2)
     "iso_flux_tma": 14,  # the same kernel with TMA-staged tracer planes
+    "fct_fused": 15,     # read un vn wn tb(2) tn(2), zftu zftv ztfw (x2); write ta(2)
+    "fct_a_tma": 17,     # the stage-a / stage-b kernels with TMA-staged planes
+    "fct_b_tma": 14,
     "zdf_imp": 8,    # read avt ah_wslp2 tb(2); ta(2) read+write
     "spg_p1a": 2,    # read ua va (column sums)
     "spg_p3": 8,     # ua va un vn read+write

@@ -310,6 +310,8 @@ enum nemo_kernel_id {
   NEMO_K_CLAMP, NEMO_K_SPG_P1A, NEMO_K_SPG_P1B, NEMO_K_SPG_P2, NEMO_K_SPG_P3,
   NEMO_K_SPG_COR,   /* variable volume: Coriolis factors of the step */
   NEMO_K_ISO_FLUX_TMA, /* iso-neutral fluxes with TMA-staged tracer planes */
+  NEMO_K_FCT_FUSED,    /* FCT stages a, b, c in one kernel, TMA-staged inputs */
+  NEMO_K_FCT_A_TMA, NEMO_K_FCT_B_TMA, /* FCT stages a, b with TMA-staged planes */
   NEMO_K_COUNT
 };
 
@@ -333,6 +335,12 @@ int nemo_gpu_set_fusion(nemo_ctx *ctx, int on);
  * configuration stages the tracer planes in shared memory with tensor copies (TMA)
  * when jpi is a multiple of 4; on = 0 forces the kernel without TMA. Same results. */
 int nemo_gpu_set_tma(nemo_ctx *ctx, int on);
+
+/* on = 1: with TMA on (nemo_gpu_set_tma), the three FCT stages of that configuration
+ * run as ONE kernel that keeps the intermediates (monotone guess, antidiffusive
+ * fluxes, limiter coefficients) in shared memory and recomputes them on the tile
+ * halos instead of storing them; on = 0 (default): three kernels. Same results. */
+int nemo_gpu_set_fct_fused(nemo_ctx *ctx, int on);
 
 /* ------------------------------------------------------------ test hook */
 

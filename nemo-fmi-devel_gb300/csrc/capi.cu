@@ -94,6 +94,7 @@ struct nemo_ctx {
   bool timing = false;
   bool no_fusion = false;  // force the per-routine kernels (tests compare both)
   bool no_tma = false;     // force the kernels without TMA staging (tests compare both)
+  bool fct_fused = false;  // the three FCT stages as one kernel (with TMA)
   cudaEvent_t tev[5] = {};
   double tms[4] = {0, 0, 0, 0};
   int tcalls = 0;
@@ -580,6 +581,7 @@ int run_fct(nemo_ctx* c, double p2dt, const void* pun, const void* pvn, const vo
   a.betup = (T*)c->fct_w[4]; a.betdo = (T*)c->fct_w[5];
   a.ztw = (const T*)c->fct_ztw;
   a.kjpt = kjpt; a.kn_fct_h = kh; a.kn_fct_v = kv; a.linssh = c->nam.ln_linssh;
+  a.tma = !c->no_tma; a.fused = c->fct_fused; a.err = c->err_flag;
   if (iso) {
     a.with_iso = 1;
     a.iso = *iso;
@@ -1030,7 +1032,7 @@ int nemo_gpu_synchronize(nemo_ctx* c) {
   if (flag) {
     cudaMemset(c->err_flag, 0, sizeof(int));
     cudaMemset(c->bar_mem, 0, 2 * sizeof(unsigned int));
-    if (flag == TM_ERR) return fail(c, NEMO_ERR_TIMEOUT, "a tensor copy of the iso-neutral flux kernel did not arrive");
+    if (flag == TM_ERR) return fail(c, NEMO_ERR_TIMEOUT, "a tensor copy of a TMA-staged tracer kernel did not arrive");
     return fail(c, NEMO_ERR_TIMEOUT, "a grid barrier of the barotropic sub-step kernel timed out");
   }
   return NEMO_OK;
@@ -1301,6 +1303,14 @@ int nemo_gpu_get_timing(nemo_ctx* c, double* ms, int* ncalls) {
 int nemo_gpu_set_fusion(nemo_ctx* c, int on) {
   if (!c) return NEMO_ERR_ARG;
   c->no_fusion = !on;
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);
+  c->graphs.clear();
+  return NEMO_OK;
+}
+
+int nemo_gpu_set_fct_fused(nemo_ctx* c, int on) {
+  if (!c) return NEMO_ERR_ARG;
+  c->fct_fused = on != 0;
   for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);
   c->graphs.clear();
   return NEMO_OK;

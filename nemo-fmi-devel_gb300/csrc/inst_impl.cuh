@@ -39,9 +39,90 @@ cudaError_t launch_adv_trp(const Dom<T>& d, const T* un, const T* vn, const T* w
   return cudaGetLastError();
 }
 
+// cuTensorMapEncodeTiled from the driver, through the runtime (no libcuda link)
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    return (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }();
+  return fn;
+}
+
+// Tensor map of nf 3-D fields of floats stored one after the other per member, as a
+// 3-D tensor (jpi, jpj, jpk * nf * nmem), with a box of bx x by points of one level.
+// False (no TMA) when the rows are not a multiple of 16 bytes (jpi % 4 != 0) or the
+// base is not 16-byte aligned.
+template <class T>
+static bool field_tensor_map(const Dom<T>& d, const T* base, int nf, unsigned bx, unsigned by, CUtensorMap* map) {
+  const auto fn = tensor_map_encoder();
+  if (!fn || sizeof(T) != 4 || d.jpi % 4 != 0 || ((uintptr_t)base & 15) != 0) return false;
+  cuuint64_t dims[3] = {(cuuint64_t)d.jpi, (cuuint64_t)d.jpj, (cuuint64_t)d.jpk * nf * d.nmem};
+  cuuint64_t strides[2] = {(cuuint64_t)d.jpi * sizeof(T), (cuuint64_t)d.n2 * sizeof(T)};
+  cuuint32_t box[3] = {bx, by, 1}, es[3] = {1, 1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)base, dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template <class T>
 cudaError_t launch_fct(const Dom<T>& d, const FctArgs<T>& a, cudaStream_t s) {
   if (hot_fct_ok(d, a)) {
+    if constexpr (sizeof(T) == 4) {
+      if (a.tma && a.err && a.kjpt == 2) {  // planes staged by TMA
+        if (a.fused) {  // the three stages in one kernel
+          PlaneMaps<FF_NIN> maps;
+          const bool ok = field_tensor_map(d, a.pun.p, 1, FF_BW, FF_BH, &maps.m[0]) &&
+                          field_tensor_map(d, a.pvn.p, 1, FF_BW, FF_BH, &maps.m[1]) &&
+                          field_tensor_map(d, a.pwn.p, 1, FF_BW, FF_BH, &maps.m[2]) &&
+                          field_tensor_map(d, a.ptb.p, a.kjpt, FF_BW, FF_BH, &maps.m[3]) &&
+                          field_tensor_map(d, a.ptn.p, a.kjpt, FF_BW, FF_BH, &maps.m[4]);
+          if (ok) {
+            static const cudaError_t attr =
+                cudaFuncSetAttribute(k_fct_fused_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, FF_SMEM);
+            if (attr != cudaSuccess) return attr;
+            const dim3 grid((d.jpi + TM_X - 1) / TM_X, (d.jpj + TM_Y - 1) / TM_Y, d.nmem);
+            k_fct_fused_tma<T><<<grid, dim3(TM_X, TM_Y), FF_SMEM, s>>>(d, a, maps, a.err, 1 << 16);
+            ktick(NEMO_K_FCT_FUSED, s);
+            return cudaGetLastError();
+          }
+        } else {  // stages a and b with TMA-staged planes, then stage c
+          PlaneMaps<FA_NF> ma;
+          PlaneMaps<FB_NF> mb;
+          bool ok = field_tensor_map(d, a.pun.p, 1, TM_W, TM_H, &ma.m[0]) &&
+                    field_tensor_map(d, a.pvn.p, 1, TM_W, TM_H, &ma.m[1]) &&
+                    field_tensor_map(d, a.pwn.p, 1, TM_W, TM_H, &ma.m[2]) &&
+                    field_tensor_map(d, a.ptb.p, 2, TM_W, TM_H, &ma.m[3]) &&
+                    field_tensor_map(d, a.ptn.p, 2, TM_W, TM_H, &ma.m[5]);
+          ma.m[4] = ma.m[3];  // tb, tn: one map each, read at the two tracers' levels
+          ma.m[6] = ma.m[5];
+          const T* fb[5] = {a.ptb.p, a.zwi, a.ax, a.ay, a.az};
+          for (int f = 0; f < 5 && ok; ++f) {
+            ok = field_tensor_map(d, fb[f], 2, TM_W, TM_H, &mb.m[2 * f]);
+            mb.m[2 * f + 1] = mb.m[2 * f];
+          }
+          if (ok) {
+            static const cudaError_t attr_a =
+                cudaFuncSetAttribute(k_fct_a_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, FA_SMEM);
+            static const cudaError_t attr_b =
+                cudaFuncSetAttribute(k_fct_b_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, FB_SMEM);
+            if (attr_a != cudaSuccess) return attr_a;
+            if (attr_b != cudaSuccess) return attr_b;
+            const dim3 grid((d.jpi + TM_X - 1) / TM_X, (d.jpj + TM_Y - 1) / TM_Y, d.nmem * ((d.jpk + KCH - 1) / KCH));
+            k_fct_a_tma<T><<<grid, dim3(TM_X, TM_Y), FA_SMEM, s>>>(d, a, ma, a.err, 1 << 16);
+            ktick(NEMO_K_FCT_A_TMA, s);
+            k_fct_b_tma<T><<<grid, dim3(TM_X, TM_Y), FB_SMEM, s>>>(d, a, mb, a.err, 1 << 16);
+            ktick(NEMO_K_FCT_B_TMA, s);
+            k_fct_c_hot<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+            ktick(NEMO_K_FCT_C, s);
+            return cudaGetLastError();
+          }
+        }
+      }
+    }
     k_fct_a_hot<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
     ktick(NEMO_K_FCT_A, s);
     k_fct_b_hot<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
@@ -76,35 +157,6 @@ cudaError_t launch_ldf_iso(const Dom<T>& d, const LdfArgs<T>& a, int copy_akz_ed
   k_iso_div<T><<<pt_grid(d), dim3(BX, BY), 0, s>>>(d, a);
   ktick(NEMO_K_ISO_DIV, s);
   return launch_iso_edges<T>(d, a, copy_akz_edges, msc_edges, s);
-}
-
-// cuTensorMapEncodeTiled from the driver, through the runtime (no libcuda link)
-static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
-  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-        q != cudaDriverEntryPointSuccess)
-      return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
-    return (PFN_cuTensorMapEncodeTiled_v12000)p;
-  }();
-  return fn;
-}
-
-// Tensor map of nf 3-D fields of floats stored one after the other per member, as a
-// 3-D tensor (jpi, jpj, jpk * nf * nmem), with a box of bx x by points of one level.
-// False (no TMA) when the rows are not a multiple of 16 bytes (jpi % 4 != 0) or the
-// base is not 16-byte aligned.
-template <class T>
-static bool field_tensor_map(const Dom<T>& d, const T* base, int nf, unsigned bx, unsigned by, CUtensorMap* map) {
-  const auto fn = tensor_map_encoder();
-  if (!fn || sizeof(T) != 4 || d.jpi % 4 != 0 || ((uintptr_t)base & 15) != 0) return false;
-  cuuint64_t dims[3] = {(cuuint64_t)d.jpi, (cuuint64_t)d.jpj, (cuuint64_t)d.jpk * nf * d.nmem};
-  cuuint64_t strides[2] = {(cuuint64_t)d.jpi * sizeof(T), (cuuint64_t)d.n2 * sizeof(T)};
-  cuuint32_t box[3] = {bx, by, 1}, es[3] = {1, 1, 1};
-  return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)base, dims, strides, box, es,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 template <class T>

@@ -143,6 +143,9 @@ struct FctArgs {
   int kjpt, kn_fct_h, kn_fct_v, linssh;
   int with_iso;              // stage c also adds the iso-neutral trend (kpass 1) of `iso`
   LdfArgs<T> iso;
+  int tma;                   // FP32 hot configuration: stage the planes by TMA
+  int fused;                 // with tma: the three stages as one kernel (k_fct_fused_tma)
+  int* err;                  // device error flag (a timed-out wait of a TMA kernel)
 };
 
 // Upstream transports at the faces of column (i,j) (traadv_fct.F90:123-145).

@@ -126,6 +126,9 @@ class Context:
     def set_tma(self, on):
         self._ck(self.lib.nemo_gpu_set_tma(self.h, int(on)), "set_tma")
 
+    def set_fct_fused(self, on):
+        self._ck(self.lib.nemo_gpu_set_fct_fused(self.h, int(on)), "set_fct_fused")
+
     def set_timing(self, on):
         self._ck(self.lib.nemo_gpu_set_timing(self.h, int(on)), "set_timing")
 

@@ -459,11 +459,15 @@ def test_fused_tracer_kernel_matches_per_routine_kernels(msc):
         assert relerr(res[0][n], res[1][n]) <= TOL32_FIELD, n
 
 
+# kernel with TMA -> the kernels it replaces
+TMA_KERNELS = {"iso_flux_tma": ("iso_flux",), "fct_a_tma": ("fct_a",), "fct_b_tma": ("fct_b",)}
+
+
 @pytest.mark.parametrize("nmem", [1, 2])
-def test_iso_flux_tma_matches_plain_kernel(nmem):
-    """The FP32 iso-neutral flux kernel with TMA-staged tracer planes (jpi = 92, a
-    multiple of 4) against the same kernel reading global memory: identical results
-    (same arithmetic; the vertical term it leaves out is exactly 0), and both against
+def test_tma_kernels_match_plain_kernels(nmem):
+    """The FP32 hot-path kernels with TMA-staged planes (jpi = 92, a multiple of 4)
+    against the same kernels reading global memory: identical results (same
+    arithmetic; the iso-neutral vertical term left out is exactly 0), and both against
     the oracle, over three steps with two level chunks per column."""
     res = {}
     for tma in (1, 0):
@@ -477,7 +481,9 @@ def test_iso_flux_tma_matches_plain_kernel(nmem):
             p.ctx.stp_hotpath(kt)
             p.ctx.synchronize()
         ran = p.ctx.get_kernel_timing()
-        assert ("iso_flux_tma" in ran) == bool(tma) and ("iso_flux" in ran) != bool(tma), ran
+        for k, plain in TMA_KERNELS.items():
+            assert (k in ran) == bool(tma), ran
+            assert all((x in ran) != bool(tma) for x in plain), ran
         p.compare("TSA", p.s4, TOL32_FIELD)
         p.compare("AH_WSLP2", p.s3, TOL32_FIELD)
         p.compare("AKZ", p.s3, TOL32_FIELD)
@@ -485,3 +491,26 @@ def test_iso_flux_tma_matches_plain_kernel(nmem):
     for n in res[1]:
         a, b = np.asarray(res[0][n]), np.asarray(res[1][n])
         assert np.array_equal(a, b), f"{n}: TMA and plain kernels differ (max {np.abs(a - b).max():.3e})"
+
+
+def test_fct_fused_kernel_matches_three_kernels():
+    """The one-kernel FCT (intermediates in shared memory, halos recomputed) against
+    the three-kernel FCT: identical results, and against the oracle, with jpk = 20
+    (level chunks of the three-kernel form split unevenly) and two members."""
+    res = {}
+    for fused in (1, 0):
+        p = Pair(nn=1, prec="mixed", seed=19, nmem=2, jpk=20)
+        p.ctx.set_fct_fused(fused)
+        p.bind_hotpath()
+        p.ctx.set_timing(True)
+        for kt in (5, 6, 7):
+            for o in p.ora:
+                o.stp_hotpath(kt)
+            p.ctx.stp_hotpath(kt)
+            p.ctx.synchronize()
+        ran = p.ctx.get_kernel_timing()
+        assert ("fct_fused" in ran) == bool(fused), ran
+        p.compare("TSA", p.s4, TOL32_FIELD)
+        res[fused] = p.ctx.to_host(p.dev["TSA"], p.s4)
+    for a, b in zip(res[0], res[1]):
+        assert np.array_equal(np.asarray(a), np.asarray(b))
