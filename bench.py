@@ -300,9 +300,18 @@ def run_gpu(args):
     # ---------------------------------------------------------------- e2e (host buffers, C ABI)
     e2e = None
     if not args.no_e2e:
-        ins = ["TSB", "TSN"] + [n.upper() for n in HOT_3D] + [n.upper() for n in HOT_2D] + ["RCDU_BOT"]
-        ins += [n.upper() for n in SHELF_FIELDS if n in states[0]]
-        outs = ["TSA", "UA", "VA", "UN", "VN", "AH_WSLP2"] + list(ACC_2D)
+        # in the order the previous step releases them (the upload of a field waits for
+        # the last part of the previous step that reads it): dyn_spg_ts's own fields,
+        # the slopes (iso-neutral fluxes), the velocities and tn (FCT), then the rest;
+        # downloads of what dyn_spg_ts writes first (they start when it ends)
+        shelf = [n.upper() for n in SHELF_FIELDS if n in states[0]]
+        late = ("GTSU", "GTSV", "E3T_B", "E3T_N", "E3T_A", "E3U_N", "E3V_N", "E3W_N", "E3F_N")
+        ins = (["UA", "VA"] + [n.upper() for n in HOT_2D if n not in ("un_b", "vn_b")] + ["UN_B", "VN_B", "RCDU_BOT"]
+               + [n for n in shelf if n not in late]
+               + ["USLP", "VSLP", "WSLPI", "WSLPJ"] + [n for n in shelf if n in ("GTSU", "GTSV")]
+               + ["UN", "VN", "WN", "TSN", "TSB", "AVT"] + [n for n in shelf if n in late[2:]])
+        assert sorted(ins) == sorted(set(ins))
+        outs = ["UA", "VA", "UN", "VN"] + list(ACC_2D) + ["TSA", "AH_WSLP2"]
         host = {}
         for n in set(ins + outs):
             host[n] = torch.empty(dev[n].numel(), dtype=dev[n].dtype, pin_memory=True)

@@ -100,17 +100,24 @@ struct nemo_ctx {
   int tcalls = 0;
   // per-kernel timing (events after every launch while timing is on)
   KernelClock kc;
-  // host copies: uploads and downloads run on their own streams so that the
-  // downloads of one step overlap the uploads of the next
-  // (fields spread over several streams by id, to keep several copy engines busy)
-  static constexpr int NUP = 4, NDOWN = 2;
+  // host copies: uploads and downloads run on their own streams, each in call order
+  // (one stream already saturates the host link each way), so the downloads of one
+  // step overlap the uploads of the next; every field has the events of its last
+  // upload and last download, so work waits only for the copies of the fields it
+  // reads or writes
+  static constexpr int NUP = 1, NDOWN = 1;
   cudaStream_t h2d[NUP] = {}, d2h[NDOWN] = {};
-  cudaEvent_t ev_main = nullptr;          // the context stream's work so far
-  cudaEvent_t ev_up[NUP] = {};            // the last upload of each upload stream
-  cudaEvent_t ev_down[NDOWN] = {};        // the last download of each download stream
+  cudaEvent_t ev_main = nullptr;            // the context stream's work so far
+  cudaEvent_t ev_upf[NEMO_F_COUNT] = {};    // the last upload of each field
   cudaEvent_t ev_field[NEMO_F_COUNT] = {};  // the last download of each field
-  bool up_pending[NUP] = {}, down_pending[NDOWN] = {};
+  bool upf_pending[NEMO_F_COUNT] = {};
   bool field_pending[NEMO_F_COUNT] = {};
+  // the ends of dyn_spg_ts, the iso-neutral fluxes, FCT and the whole step in the
+  // last (staged) hot-path step: downloads of what dyn_spg_ts writes wait only for
+  // it, and the upload of a field waits only for the last part that reads it
+  cudaEvent_t ev_spg_done = nullptr, ev_fct_done = nullptr, ev_step_done = nullptr;
+  cudaEvent_t ev_iso_done = nullptr;  // ev_join when the iso-neutral fluxes ran on the side stream, else ev_fct_done
+  bool spg_done_valid = false;
   // hot path: the iso-neutral fluxes run on a side stream beside dyn_spg_ts
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -146,24 +153,66 @@ int cuda_fail(nemo_ctx* c, cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
   } while (0)
 
-// Before the context stream runs work: wait for the pending host copies (the work
+// Make stream st wait for the pending upload of field id (its device data) and, when
+// `writes`, for its pending download (the work overwrites it).
+int wait_field(nemo_ctx* c, cudaStream_t st, int id, bool writes) {
+  if (c->upf_pending[id]) CK(cudaStreamWaitEvent(st, c->ev_upf[id], 0), "wait for an upload");
+  if (writes && c->field_pending[id]) CK(cudaStreamWaitEvent(st, c->ev_field[id], 0), "wait for a download");
+  return NEMO_OK;
+}
+
+// Before the context stream runs work: wait for every pending host copy (the work
 // reads uploaded fields and may overwrite fields being downloaded).
 int join_copies(nemo_ctx* c) {
-  for (int k = 0; k < nemo_ctx::NUP; ++k)
-    if (c->up_pending[k]) {
-      CK(cudaStreamWaitEvent(c->stream, c->ev_up[k], 0), "wait for uploads");
-      c->up_pending[k] = false;
-    }
-  bool any = false;
-  for (int k = 0; k < nemo_ctx::NDOWN; ++k)
-    if (c->down_pending[k]) {
-      CK(cudaStreamWaitEvent(c->stream, c->ev_down[k], 0), "wait for downloads");
-      c->down_pending[k] = false;
-      any = true;
-    }
-  if (any)
-    for (bool& b : c->field_pending) b = false;
+  c->spg_done_valid = false;
+  for (int id = 0; id < NEMO_F_COUNT; ++id) {
+    if (wait_field(c, c->stream, id, true)) return NEMO_ERR_CUDA;
+    c->upf_pending[id] = false;
+    c->field_pending[id] = false;
+  }
   return NEMO_OK;
+}
+
+// the event after the last part of the last staged hot-path step that reads field id
+cudaEvent_t last_reader(const nemo_ctx* c, int id) {
+  switch (id) {
+    case NEMO_F_UA: case NEMO_F_VA: case NEMO_F_UB: case NEMO_F_VB:
+      return c->ev_spg_done;
+    case NEMO_F_USLP: case NEMO_F_VSLP: case NEMO_F_WSLPI: case NEMO_F_WSLPJ:
+    case NEMO_F_AHTU: case NEMO_F_AHTV: case NEMO_F_GTSU: case NEMO_F_GTSV:
+      return c->ev_iso_done;
+    case NEMO_F_UN: case NEMO_F_VN: case NEMO_F_WN: case NEMO_F_TSN:
+      return c->ev_fct_done;
+    default:
+      break;
+  }
+  if (id >= NEMO_F_SSHB && id != NEMO_F_E3F_N) return c->ev_spg_done;  // the 2-D fields: dyn_spg_ts only
+  return c->ev_step_done;
+}
+
+bool copies_pending(const nemo_ctx* c) {
+  for (int id = 0; id < NEMO_F_COUNT; ++id)
+    if (c->upf_pending[id] || c->field_pending[id]) return true;
+  return false;
+}
+
+// the fields dyn_spg_ts writes (the 3-D velocities and trends, the time-filter sums and
+// restart fields)
+bool spg_writes(int id) {
+  switch (id) {
+    case NEMO_F_UA: case NEMO_F_VA: case NEMO_F_UN: case NEMO_F_VN:
+    case NEMO_F_SSHA: case NEMO_F_UA_B: case NEMO_F_VA_B: case NEMO_F_UN_ADV: case NEMO_F_VN_ADV:
+    case NEMO_F_UB2_B: case NEMO_F_VB2_B: case NEMO_F_UN_BF: case NEMO_F_VN_BF:
+      return true;
+    default:
+      return false;
+  }
+}
+// the fields dyn_spg_ts reads besides those it writes: the before velocities, the
+// scale factors at u- and v-points, every 2-D field (and e3f_n)
+bool spg_reads(int id) {
+  if (spg_writes(id) || id == NEMO_F_UB || id == NEMO_F_VB || id == NEMO_F_E3U_N || id == NEMO_F_E3V_N) return true;
+  return id >= NEMO_F_SSHB;
 }
 
 inline size_t I2(const nemo_ctx* c, int i, int j) { return (size_t)(i - 1) + (size_t)c->jpi * (j - 1); }
@@ -780,7 +829,7 @@ int run_spg(nemo_ctx* c, int kt) {
 }
 
 template <class T>
-int run_hotpath(nemo_ctx* c, int kt) {
+int run_hotpath(nemo_ctx* c, int kt, bool staged) {
   const nemo_namelist& nm = c->nam;
   void* const* F = c->f;
   if (!F[NEMO_F_TSB] || !F[NEMO_F_TSN] || !F[NEMO_F_TSA] || !F[NEMO_F_WN])
@@ -796,6 +845,13 @@ int run_hotpath(nemo_ctx* c, int kt) {
     cudaEventRecord(c->kc.ev[0], c->stream);
   }
   mark(0);
+  // Staged (host copies pending): each part waits only for the copies of the fields it
+  // reads or writes -- dyn_spg_ts starts while the tracers and slopes still upload,
+  // and the downloads of what it writes start when it ends (ev_spg_done).
+  c->spg_done_valid = false;
+  if (staged)  // the iso-neutral coefficients the first pass may zero on this stream
+    if (wait_field(c, c->stream, NEMO_F_AH_WSLP2, true) || wait_field(c, c->stream, NEMO_F_AKZ, true))
+      return NEMO_ERR_CUDA;
   const bool fused = nm.ln_traldf_iso && !c->no_fusion;
   LdfArgs<T> la{};
   // The iso-neutral fluxes read tsb and the slopes only, and dyn_spg_ts touches
@@ -809,12 +865,23 @@ int run_hotpath(nemo_ctx* c, int kt) {
     if (overlap) {
       CK(cudaEventRecord(c->ev_fork, c->stream), "fork");
       CK(cudaStreamWaitEvent(c->side, c->ev_fork, 0), "fork");
+      if (staged)
+        for (int id : {NEMO_F_TSB, NEMO_F_USLP, NEMO_F_VSLP, NEMO_F_WSLPI, NEMO_F_WSLPJ, NEMO_F_AHTU, NEMO_F_AHTV,
+                       NEMO_F_GTSU, NEMO_F_GTSV, NEMO_F_E3U_N, NEMO_F_E3V_N, NEMO_F_E3W_N})
+          if (wait_field(c, c->side, id, false)) return NEMO_ERR_CUDA;
       CK(launch_iso_flux<T>(dom_now<T>(c), la, c->side), "iso fluxes");
       CK(cudaEventRecord(c->ev_join, c->side), "join");
     }
   }
+  if (staged)
+    for (int id = 0; id < NEMO_F_COUNT; ++id)
+      if (spg_reads(id) && wait_field(c, c->stream, id, spg_writes(id))) return NEMO_ERR_CUDA;
   int s = run_spg<T>(c, kt);
   if (s) return s;
+  if (staged) {
+    CK(cudaEventRecord(c->ev_spg_done, c->stream), "end of dyn_spg_ts");
+    if (join_copies(c)) return NEMO_ERR_CUDA;  // the tracer part: every remaining copy
+  }
   mark(1);
   const double r2dt = (nm.neuler == 0 && kt == nm.nit000) ? nm.rn_rdt : 2.0 * nm.rn_rdt;
   const int fct_h = nm.nn_fct_h ? nm.nn_fct_h : 2, fct_v = nm.nn_fct_v ? nm.nn_fct_v : 2;  // &namtra_adv
@@ -845,8 +912,13 @@ int run_hotpath(nemo_ctx* c, int kt) {
   if (s) return s;
   }
   mark(3);
+  if (staged) {
+    CK(cudaEventRecord(c->ev_fct_done, c->stream), "end of tra_adv / tra_ldf");
+    c->ev_iso_done = overlap ? c->ev_join : c->ev_fct_done;
+  }
   s = run_zdf<T>(c, r2dt, F[NEMO_F_TSB], F[NEMO_F_TSA], 2, 0, 1);
   if (s) return s;
+  if (staged) CK(cudaEventRecord(c->ev_step_done, c->stream), "end of the step");
   if (c->timing) {
     mark(4);
     CK(cudaEventSynchronize(c->tev[4]), "timing");
@@ -863,6 +935,7 @@ int run_hotpath(nemo_ctx* c, int kt) {
       c->kcnt[c->kc.id[i]] += 1;
     }
   }
+  if (staged) c->spg_done_valid = true;
   return NEMO_OK;
 }
 
@@ -905,10 +978,10 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
   if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess) return bad(NEMO_ERR_CUDA);
   for (cudaEvent_t* e : {&c->ev_main, &c->ev_fork, &c->ev_join})
     if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return bad(NEMO_ERR_CUDA);
-  for (auto& e : c->ev_up)
+  for (auto& e : c->ev_upf)
     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return bad(NEMO_ERR_CUDA);
-  for (auto& e : c->ev_down)
-    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return bad(NEMO_ERR_CUDA);
+  for (cudaEvent_t* e : {&c->ev_spg_done, &c->ev_fct_done, &c->ev_step_done})
+    if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return bad(NEMO_ERR_CUDA);
   for (auto& e : c->ev_field)
     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return bad(NEMO_ERR_CUDA);
   int s = derive_domain(c, dm);
@@ -1001,9 +1074,9 @@ int nemo_gpu_destroy(nemo_ctx* c) {
     if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : {c->ev_main, c->ev_fork, c->ev_join})
     if (e) cudaEventDestroy(e);
-  for (auto e : c->ev_up)
+  for (auto e : c->ev_upf)
     if (e) cudaEventDestroy(e);
-  for (auto e : c->ev_down)
+  for (cudaEvent_t e : {c->ev_spg_done, c->ev_fct_done, c->ev_step_done})
     if (e) cudaEventDestroy(e);
   if (c->side) cudaStreamDestroy(c->side);
   for (auto e : c->ev_field)
@@ -1023,8 +1096,7 @@ int nemo_gpu_synchronize(nemo_ctx* c) {
   if (!c) return NEMO_ERR_ARG;
   for (auto st : c->h2d) CK(cudaStreamSynchronize(st), "synchronize");
   for (auto st : c->d2h) CK(cudaStreamSynchronize(st), "synchronize");
-  for (bool& b : c->up_pending) b = false;
-  for (bool& b : c->down_pending) b = false;
+  for (bool& b : c->upf_pending) b = false;
   for (bool& b : c->field_pending) b = false;
   CK(cudaStreamSynchronize(c->stream), "synchronize");
   int flag = 0;
@@ -1068,15 +1140,19 @@ int nemo_gpu_field_upload(nemo_ctx* c, int id, const void* host) {
   if (!c || id < 0 || id >= NEMO_F_COUNT || !host) return fail(c, NEMO_ERR_ARG, "field_upload: bad argument");
   if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "field_upload: field %d is not bound", id);
   size_t bytes = field_numel(c, id) * c->nmem * (nemo_gpu_field_is_fp64(c, id) ? 8 : 4);
-  // after the work already queued (it may read the field) and the field's download
-  const int k = id % nemo_ctx::NUP;  // a field always on the same stream: uploads of it stay ordered
-  cudaStream_t st = c->h2d[k];
-  CK(cudaEventRecord(c->ev_main, c->stream), "field_upload");
-  CK(cudaStreamWaitEvent(st, c->ev_main, 0), "field_upload");
+  // after the work that reads the field (its last reader in the last staged hot-path
+  // step, else all the work already queued) and the field's download
+  cudaStream_t st = c->h2d[0];
+  if (c->spg_done_valid) {
+    CK(cudaStreamWaitEvent(st, last_reader(c, id), 0), "field_upload");
+  } else {
+    CK(cudaEventRecord(c->ev_main, c->stream), "field_upload");
+    CK(cudaStreamWaitEvent(st, c->ev_main, 0), "field_upload");
+  }
   if (c->field_pending[id]) CK(cudaStreamWaitEvent(st, c->ev_field[id], 0), "field_upload");
   CK(cudaMemcpyAsync(c->f[id], host, bytes, cudaMemcpyHostToDevice, st), "field_upload");
-  CK(cudaEventRecord(c->ev_up[k], st), "field_upload");
-  c->up_pending[k] = true;
+  CK(cudaEventRecord(c->ev_upf[id], st), "field_upload");
+  c->upf_pending[id] = true;
   return NEMO_OK;
 }
 
@@ -1084,18 +1160,19 @@ int nemo_gpu_field_download(nemo_ctx* c, int id, void* host) {
   if (!c || id < 0 || id >= NEMO_F_COUNT || !host) return fail(c, NEMO_ERR_ARG, "field_download: bad argument");
   if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "field_download: field %d is not bound", id);
   size_t bytes = field_numel(c, id) * c->nmem * (nemo_gpu_field_is_fp64(c, id) ? 8 : 4);
-  // after the work already queued and any pending upload
-  const int k = id % nemo_ctx::NDOWN;
-  cudaStream_t st = c->d2h[k];
-  CK(cudaEventRecord(c->ev_main, c->stream), "field_download");
-  CK(cudaStreamWaitEvent(st, c->ev_main, 0), "field_download");
-  for (int u = 0; u < nemo_ctx::NUP; ++u)
-    if (c->up_pending[u]) CK(cudaStreamWaitEvent(st, c->ev_up[u], 0), "field_download");
+  // after the work that writes the field (dyn_spg_ts of the last hot-path step for
+  // the fields it writes, else all the work already queued) and the field's upload
+  cudaStream_t st = c->d2h[0];
+  if (c->spg_done_valid && spg_writes(id)) {
+    CK(cudaStreamWaitEvent(st, c->ev_spg_done, 0), "field_download");
+  } else {
+    CK(cudaEventRecord(c->ev_main, c->stream), "field_download");
+    CK(cudaStreamWaitEvent(st, c->ev_main, 0), "field_download");
+  }
+  if (c->upf_pending[id]) CK(cudaStreamWaitEvent(st, c->ev_upf[id], 0), "field_download");
   CK(cudaMemcpyAsync(host, c->f[id], bytes, cudaMemcpyDeviceToHost, st), "field_download");
   CK(cudaEventRecord(c->ev_field[id], st), "field_download");
-  CK(cudaEventRecord(c->ev_down[k], st), "field_download");
   c->field_pending[id] = true;
-  c->down_pending[k] = true;
   return NEMO_OK;
 }
 
@@ -1238,6 +1315,10 @@ int nemo_gpu_glob_sum(nemo_ctx* c, const char* cdname, const void* ptab, int nk,
 
 int nemo_gpu_stp_hotpath(nemo_ctx* c, int kt) {
   if (!c) return NEMO_ERR_ARG;
+  // host copies in flight: direct launches that wait per field (see run_hotpath);
+  // otherwise the captured graph of the steady-state step
+  if (copies_pending(c) && !c->timing)
+    return c->prec == NEMO_PREC_FP64 ? run_hotpath<double>(c, kt, true) : run_hotpath<float>(c, kt, true);
   if (join_copies(c)) return NEMO_ERR_CUDA;
   const nemo_namelist& nm = c->nam;
   // class of kt: the Euler/leapfrog start steps differ in scalars and weights
@@ -1251,7 +1332,7 @@ int nemo_gpu_stp_hotpath(nemo_ctx* c, int kt) {
     }
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-      int s = c->prec == NEMO_PREC_FP64 ? run_hotpath<double>(c, kt) : run_hotpath<float>(c, kt);
+      int s = c->prec == NEMO_PREC_FP64 ? run_hotpath<double>(c, kt, false) : run_hotpath<float>(c, kt, false);
       cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
       cudaGraphExec_t ex = nullptr;
       if (s == NEMO_OK && ee == cudaSuccess && g && cudaGraphInstantiate(&ex, g, 0) == cudaSuccess) {
@@ -1267,7 +1348,7 @@ int nemo_gpu_stp_hotpath(nemo_ctx* c, int kt) {
     c->graphs_ok = false;  // capture unavailable: direct launches from now on
     cudaGetLastError();
   }
-  return c->prec == NEMO_PREC_FP64 ? run_hotpath<double>(c, kt) : run_hotpath<float>(c, kt);
+  return c->prec == NEMO_PREC_FP64 ? run_hotpath<double>(c, kt, false) : run_hotpath<float>(c, kt, false);
 }
 
 int nemo_gpu_set_timing(nemo_ctx* c, int on) {
