@@ -196,14 +196,21 @@ int nemo_gpu_field_is_fp64(const nemo_ctx *ctx, int field_id);
 int nemo_gpu_spg_info(const nemo_ctx *ctx, int *icycle, int *nn_baro, double *rdtbt);
 
 /* Copy between a host buffer and a bound field (all members). Both are
- * asynchronous and ordered with the context's work: an upload runs after the work
- * already queued on the context stream (and after a pending download of the same
- * field), a download after the work already queued and the pending uploads, and the
- * next routine called on the context waits for both. Uploads and downloads use
- * copy streams of the context (field id modulo four upload and two download
- * streams), so copies of different fields run on several copy engines at once and
- * one step's downloads overlap the next step's uploads. Host memory should be pinned; read a downloaded buffer, or upload it
- * into another field, only after nemo_gpu_synchronize. */
+ * asynchronous and ordered with the context's work per field. An upload runs after
+ * the work already queued that reads the field and after a pending download of the
+ * field; a download runs after the work already queued that writes the field and
+ * after a pending upload of it. Uploads run in call order on one copy stream and
+ * downloads on another, so one step's downloads overlap the next step's uploads.
+ * After nemo_gpu_stp_hotpath "the work that reads / writes the field" is the part of
+ * the step that last reads / writes it: the upload of a field the next step needs
+ * early (dyn_spg_ts's) starts while this step's tracer kernels run, and a download of
+ * what dyn_spg_ts writes starts when dyn_spg_ts ends. A routine waits only for the
+ * copies of the fields it reads or writes when nemo_gpu_stp_hotpath is called with
+ * copies in flight (dyn_spg_ts starts while the tracers still upload), for all
+ * pending copies otherwise. Upload fields in the order the step releases them:
+ * dyn_spg_ts's (ua, va, the 2-D fields), the slopes, un vn wn tsn, then the rest.
+ * Host memory should be pinned; read a downloaded buffer, or upload it into another
+ * field, only after nemo_gpu_synchronize. */
 int nemo_gpu_field_upload(nemo_ctx *ctx, int field_id, const void *host);
 int nemo_gpu_field_download(nemo_ctx *ctx, int field_id, void *host);
 
