@@ -82,8 +82,8 @@ KERNEL_BYTES_2D = {
 # kernel's traffic is proportional to its cells).
 # (kernel, precision, nn_GYRE) -> bytes
 TRAFFIC = {(k, "mixed", 25): v * 1e6 for k, v in {
-    "spg_p2": 59.2, "iso_flux": 541.1, "fct_c": 895.2, "fct_a": 675.9, "fct_b": 590.5, "zdf_imp": 279.7,
-    "spg_p3": 219.8, "spg_p1a": 96.7, "spg_p1b": 36.2, "iso_akz_edges": 6.8}.items()}
+    "spg_p2": 59.1, "iso_flux_tma": 548.6, "fct_c": 901.6, "fct_a_tma": 680.1, "fct_b_tma": 592.6, "zdf_imp": 277.5,
+    "spg_p3": 219.6, "spg_p1a": 96.7, "spg_p1b": 36.2}.items()}
 TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, nn_GYRE=15 capture scaled by cells"
 
 
