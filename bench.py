@@ -68,7 +68,7 @@ KERNEL_FIELDS = {
     "fct_a_tma": 17,     # the stage-a / stage-b kernels with TMA-staged planes
     "fct_b_tma": 14,
     "zdf_imp": 8,    # read avt ah_wslp2 tb(2); ta(2) read+write
-    "spg_p1a": 2,    # read ua va (column sums)
+    "spg_p1a": 2,    # read ua va (column sums; their removal from ua, va is done by phase 3)
     "spg_p3": 8,     # ua va un vn read+write
 }
 # per 2-D cell, bytes (FP64, FP32-bulk) of the 2-D kernels

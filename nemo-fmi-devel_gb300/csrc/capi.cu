@@ -76,7 +76,7 @@ struct nemo_ctx {
   void* spg_w[5] = {};
   void* spg_cor[5] = {};  // variable volume: Coriolis factors of each member
   void* ring[3] = {};
-  void* spg_x[6] = {};  // fx (2 slots), fy (2 slots), du, dv, cu, cv
+  void* spg_x[8] = {};  // fx (2 slots), fy (2 slots), du, dv, cu, cv, zmu, zmv
   float* spg_ff = nullptr;  // mixed form: compensated sub-step sums, 10 x nmem x n2
   unsigned int* bar_mem = nullptr;  // count, gen
   int* err_flag = nullptr;
@@ -790,6 +790,7 @@ int run_spg(nemo_ctx* c, int kt) {
   a.ring_ssh = (T*)c->ring[0]; a.ring_u = (T*)c->ring[1]; a.ring_v = (T*)c->ring[2];
   a.fx = (T*)c->spg_x[0]; a.fy = (T*)c->spg_x[1];
   a.du = (T*)c->spg_x[2]; a.dv = (T*)c->spg_x[3]; a.cu = (T*)c->spg_x[4]; a.cv = (T*)c->spg_x[5];
+  a.zmu = (T*)c->spg_x[6]; a.zmv = (T*)c->spg_x[7];
   a.cache = c->p2_cache;
   a.ff = c->spg_ff;
   a.wgt1 = c->d_wgt1; a.wgt2 = c->d_wgt2; a.wgtf = c->d_wgtf; a.nwgt = (int)c->wgt1.size();
@@ -1003,7 +1004,7 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
     if (cudaMalloc(&p, 4 * b2) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
     cudaMemset(p, 0, 4 * b2);
   }
-  for (int w = 0; w < 6; ++w) {
+  for (int w = 0; w < 8; ++w) {
     const size_t bytes = w < 2 ? 2 * b2 : b2;
     if (cudaMalloc(&c->spg_x[w], bytes) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
     cudaMemset(c->spg_x[w], 0, bytes);

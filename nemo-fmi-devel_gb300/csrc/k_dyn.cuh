@@ -34,6 +34,7 @@ struct SpgArgs {
   T *ring_ssh, *ring_u, *ring_v;  // 4 slots each
   T *fx, *fy;                     // 2 slots each: predictor fluxes zwx, zwy of a sub-step
   T *du, *dv, *cu, *cv;           // phase-3 column terms, computed at the end of phase 2
+  T *zmu, *zmv;                   // phase-1 column means, subtracted from ua, va by phase 3
   float* ff;                      // mixed form: the five sums as (hi, lo) float pairs, 10 x nmem2
   RO<double> wgt1, wgt2;
   RO<float> wgtf;                 // mixed form: wgt1 hi | wgt1 lo | wgt2, nwgt entries each
@@ -60,8 +61,10 @@ template <class T>
 __device__ __forceinline__ long pt_ij(const Dom<T>& d, int i, int j) { return (long)(i - 1) + (long)(j - 1) * d.jpi; }
 
 // ---------------------------------------------------------------------------------
-// Phase 1a (:358-378): zu_frc = SUM_k e3u*ua*umask * r1_hu_n, then ua -= zu_frc*umask
-// on the interior. One thread per column, all columns.
+// Phase 1a (:358-367): zu_frc = SUM_k e3u*ua*umask * r1_hu_n. One thread per column,
+// all columns. The removal of the mean from ua (:371-378) is left to phase 3, the next
+// kernel that touches ua (nothing between reads the 3-D trend): it applies
+// (ua - zu_frc*umask) + (ua_b - ub_b)/2dt, the reference's two roundings, in one pass.
 template <class T>
 __global__ void k_spg_p1a(Dom<T> d, SpgArgs<T> a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -80,12 +83,8 @@ __global__ void k_spg_p1a(Dom<T> d, SpgArgs<T> a) {
   sv = sv * a.r1_hv_n[m * a.hs + ij];
   a.zu_frc[m2 + ij] = su;
   a.zv_frc[m2 + ij] = sv;
-  if (i >= 2 && i <= d.jpi - 1 && j >= 2 && j <= d.jpj - 1)
-    for (int k = 1; k <= d.jpk - 1; ++k) {
-      const long q = m3 + ij + (long)(k - 1) * n2;
-      a.ua[q] = a.ua[q] - su * umsk<T>(ci, k);
-      a.va[q] = a.va[q] - sv * vmsk<T>(ci, k);
-    }
+  a.zmu[m2 + ij] = su;
+  a.zmv[m2 + ij] = sv;
 }
 
 // Coriolis factors of one member (:241-343).
@@ -326,8 +325,8 @@ __global__ void k_spg_p1b(Dom<T> d, SpgArgs<T> a) {
 }
 
 // Phase 1a for FP32 and jpk = NK known at compile time: the column of ua / va is
-// loaded whole into registers, summed in the reference's order, then corrected and
-// stored, so each value is read once and all loads are in flight together.
+// loaded whole into registers and summed in the reference's order, so all loads are
+// in flight together.
 template <int NK>
 __global__ void __launch_bounds__(128) k_spg_p1a_reg(Dom<float> d, SpgArgs<float> a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -354,12 +353,8 @@ __global__ void __launch_bounds__(128) k_spg_p1a_reg(Dom<float> d, SpgArgs<float
   sv = sv * a.r1_hv_n[m * a.hs + ij];
   a.zu_frc[m2 + ij] = su;
   a.zv_frc[m2 + ij] = sv;
-  if (i >= 2 && i <= d.jpi - 1 && j >= 2 && j <= d.jpj - 1)
-#pragma unroll
-    for (int k = 1; k <= NK - 1; ++k) {
-      ua[(k - 1) * n2] = u[k - 1] - su * umsk<float>(ci, k);
-      va[(k - 1) * n2] = v[k - 1] - sv * vmsk<float>(ci, k);
-    }
+  a.zmu[m2 + ij] = su;
+  a.zmv[m2 + ij] = sv;
 }
 
 
@@ -895,7 +890,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (VVL ? 3 : 4) : 2) k_spg
   }
 }
 
-// Phase 3 (:1236-1240, :1266-1269): the barotropic trend added to ua, va and the now
+// Phase 3 (:1236-1240, :1266-1269), with phase 1's removal of the column mean from
+// ua, va on the interior (:371-378): the barotropic trend added to ua, va and the now
 // velocities corrected to the time-filtered transports; one thread walks a chunk of
 // levels of one column, the column terms loaded once.
 template <class T>
@@ -912,10 +908,17 @@ __global__ void __launch_bounds__(128) k_spg_p3(Dom<T> d, SpgArgs<T> a) {
   const RO<T> du = a.du, dv = a.dv, cu = a.cu, cv = a.cv;  // written by phase 2
   const T du0 = du[m2 + p], dv0 = dv[m2 + p], cu0 = cu[m2 + p], cv0 = cv[m2 + p];
   const T unb = a.un_b[m2 + p], vnb = a.vn_b[m2 + p];
+  const bool interior = i >= 2 && i <= d.jpi - 1 && j >= 2 && j <= d.jpj - 1;
+  const T zm_u = interior ? a.zmu[m2 + p] : T(0), zm_v = interior ? a.zmv[m2 + p] : T(0);
   const long base = (long)m * d.n3 + p;
   for (int k = k0; k <= k1; ++k) {
     const long q = base + (long)(k - 1) * d.n2;
-    const T ua = a.ua[q], va = a.va[q], un = a.un[q], vn = a.vn[q];
+    T ua = a.ua[q], va = a.va[q];
+    const T un = a.un[q], vn = a.vn[q];
+    if (interior) {
+      ua = ua - zm_u * umsk<T>(ci, k);
+      va = va - zm_v * vmsk<T>(ci, k);
+    }
     a.ua[q] = ua + du0;
     a.va[q] = va + dv0;
     a.un[q] = (un + cu0 - unb) * umsk<T>(ci, k);
