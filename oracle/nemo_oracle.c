@@ -52,6 +52,9 @@ struct ora_ctx {
   double *ssha_e, *ua_e, *va_e, *hu_e, *hv_e, *hur_e, *hvr_e;
   double r2dt;
   double *f[NEMO_F_COUNT];
+  /* FCT limiter multipliers (3 faces x kjpt fields): 1 = record, 2 = replay */
+  double *fct_tape;
+  int fct_tape_mode;
 };
 
 static void spg_coriolis_factors(ora_ctx *c, const double *ht_n, const double *e3f_n);
@@ -419,7 +422,7 @@ int ora_interp_4th_cpt(ora_ctx *c, const double *pt_in, double *pt_out) {
 /* -------------------------------------------------------------------- nonosc */
 /* traadv_fct.F90:330-428 */
 static void nonosc(ora_ctx *c, const double *pbef, double *paa, double *pbb, double *pcc,
-                   const double *paft, double p2dt) {
+                   const double *paft, double p2dt, double *tape) {
   const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
   const size_t n3 = (size_t)jpi * jpj * jpk;
   const double *tmask = c->tmask, *e3t_n = fld(c, NEMO_F_E3T_N);
@@ -455,6 +458,7 @@ static void nonosc(ora_ctx *c, const double *pbef, double *paa, double *pbb, dou
   }
   lbc_closed(jpi, jpj, zbetup, jpk, 'T', 0.0);
   lbc_closed(jpi, jpj, zbetdo, jpk, 'T', 0.0);
+  if (tape) memset(tape, 0, 3 * n3 * sizeof(double));
   OMP_FOR
   for (int jk = 1; jk <= jpk - 1; ++jk)
     for (int jj = 2; jj <= jpj - 1; ++jj)
@@ -463,14 +467,17 @@ static void nonosc(ora_ctx *c, const double *pbef, double *paa, double *pbb, dou
         double zbu = dmin(1.0, dmin(zbetup[I3(ji, jj, jk)], zbetdo[I3(ji + 1, jj, jk)]));
         double zcu = (0.5 + sign_nsz(0.5, paa[I3(ji, jj, jk)]));
         paa[I3(ji, jj, jk)] = paa[I3(ji, jj, jk)] * (zcu * zau + (1.0 - zcu) * zbu);
+        if (tape) tape[I3(ji, jj, jk)] = zcu * zau + (1.0 - zcu) * zbu;
         double zav = dmin(1.0, dmin(zbetdo[I3(ji, jj, jk)], zbetup[I3(ji, jj + 1, jk)]));
         double zbv = dmin(1.0, dmin(zbetup[I3(ji, jj, jk)], zbetdo[I3(ji, jj + 1, jk)]));
         double zcv = (0.5 + sign_nsz(0.5, pbb[I3(ji, jj, jk)]));
         pbb[I3(ji, jj, jk)] = pbb[I3(ji, jj, jk)] * (zcv * zav + (1.0 - zcv) * zbv);
+        if (tape) tape[n3 + I3(ji, jj, jk)] = zcv * zav + (1.0 - zcv) * zbv;
         double za = dmin(1., dmin(zbetdo[I3(ji, jj, jk + 1)], zbetup[I3(ji, jj, jk)]));
         double zb = dmin(1., dmin(zbetup[I3(ji, jj, jk + 1)], zbetdo[I3(ji, jj, jk)]));
         double zc = (0.5 + sign_nsz(0.5, pcc[I3(ji, jj, jk + 1)]));
         pcc[I3(ji, jj, jk + 1)] = pcc[I3(ji, jj, jk + 1)] * (zc * za + (1.0 - zc) * zb);
+        if (tape) tape[2 * n3 + I3(ji, jj, jk + 1)] = zc * za + (1.0 - zc) * zb;
       }
   lbc_closed(jpi, jpj, paa, jpk, 'U', 0.0);
   lbc_closed(jpi, jpj, pbb, jpk, 'V', 0.0);
@@ -603,8 +610,18 @@ int ora_tra_adv_fct(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
     lbc_closed(jpi, jpj, zwx, jpk, 'U', 0.0);
     lbc_closed(jpi, jpj, zwy, jpk, 'V', 0.0);
     lbc_closed(jpi, jpj, zwz, jpk, 'W', 0.0);
-    /* (:284) */
-    nonosc(c, tb, zwx, zwy, zwz, zwi, p2dt);
+    /* (:284) the limiter; with a tape in replay mode the recorded multipliers
+     * instead (the tangent-linear with the limiter frozen) */
+    double *tp = c->fct_tape ? c->fct_tape + 3 * n3 * (size_t)(jn - 1) : NULL;
+    if (c->fct_tape_mode == 2) {
+      for (size_t q = 0; q < n3; ++q) {
+        zwx[q] = zwx[q] * tp[q];
+        zwy[q] = zwy[q] * tp[n3 + q];
+        zwz[q] = zwz[q] * tp[2 * n3 + q];
+      }
+    } else {
+      nonosc(c, tb, zwx, zwy, zwz, zwi, p2dt, c->fct_tape_mode == 1 ? tp : NULL);
+    }
     /* (:288-297) */
     OMP_FOR
     for (int jk = 1; jk <= jpk - 1; ++jk)
@@ -870,6 +887,44 @@ int ora_tra_ldf_iso(ora_ctx *c, int kt, int kit000, const char *cdtype,
   return NEMO_OK;
 }
 
+/* Matrix of the implicit vertical diffusion and its LU pivots (trazdf.F90:153-234,
+ * ln_zad_Aimp = F): zwi, zws the sub- and super-diagonals, zwt the pivots. */
+static void zdf_lu(ora_ctx *c, const double *coef, double p2dt, double *zwi, double *zwt, double *zwd,
+                   double *zws) {
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const nemo_namelist *nm = &c->nam;
+  const double *akz = c->f[NEMO_F_AKZ], *ah_wslp2 = c->f[NEMO_F_AH_WSLP2];
+  const double *e3t_a = fld(c, NEMO_F_E3T_A), *e3w = fld(c, NEMO_F_E3W_N);
+  const int l_ldfslp = nm->ln_traldf_iso;
+  for (int jk = 2; jk <= jpk; ++jk)
+    for (int jj = 1; jj <= jpj; ++jj)
+      for (int ji = 1; ji <= jpi; ++ji) zwt[I3(ji, jj, jk)] = coef[I3(ji, jj, jk)];
+  for (int jj = 1; jj <= jpj; ++jj)
+    for (int ji = 1; ji <= jpi; ++ji) zwt[I3(ji, jj, 1)] = 0.0;
+  if (l_ldfslp) {
+    const double *add = nm->ln_traldf_msc ? akz : ah_wslp2;
+    for (int jk = 2; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) zwt[I3(ji, jj, jk)] = zwt[I3(ji, jj, jk)] + add[I3(ji, jj, jk)];
+  }
+  OMP_FOR
+  for (int jk = 1; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t q = I3(ji, jj, jk);
+        zwi[q] = -p2dt * zwt[q] / e3w[q];
+        zws[q] = -p2dt * zwt[I3(ji, jj, jk + 1)] / e3w[I3(ji, jj, jk + 1)];
+        zwd[q] = e3t_a[q] - zwi[q] - zws[q];
+      }
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) zwt[I3(ji, jj, 1)] = zwd[I3(ji, jj, 1)];
+  for (int jk = 2; jk <= jpk - 1; ++jk)
+    OMP_FOR
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji)
+        zwt[I3(ji, jj, jk)] = zwd[I3(ji, jj, jk)] - zwi[I3(ji, jj, jk)] * zws[I3(ji, jj, jk - 1)] / zwt[I3(ji, jj, jk - 1)];
+}
+
 /* --------------------------------------------------------------- tra_zdf_imp */
 /* trazdf.F90:109-268 (ln_zad_Aimp = F) */
 int ora_tra_zdf_imp(ora_ctx *c, int kt, int kit000, const char *cdtype, double p2dt,
@@ -881,8 +936,7 @@ int ora_tra_zdf_imp(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
   const int is_trc = cdtype && cdtype[0] == 'T' && cdtype[1] == 'R' && cdtype[2] == 'C';
   const double *avt = c->f[NEMO_F_AVT], *avs = c->f[NEMO_F_AVS];
   const double *akz = c->f[NEMO_F_AKZ], *ah_wslp2 = c->f[NEMO_F_AH_WSLP2];
-  const double *e3t_b = fld(c, NEMO_F_E3T_B), *e3t_n = fld(c, NEMO_F_E3T_N), *e3t_a = fld(c, NEMO_F_E3T_A);
-  const double *e3w = fld(c, NEMO_F_E3W_N), *tmask = c->tmask;
+  const double *e3t_b = fld(c, NEMO_F_E3T_B), *e3t_n = fld(c, NEMO_F_E3T_N), *tmask = c->tmask;
   const int l_ldfslp = nm->ln_traldf_iso;
   if (!avt && !is_trc) return NEMO_ERR_UNBOUND;
   if (l_ldfslp && ((nm->ln_traldf_msc && !akz) || (!nm->ln_traldf_msc && !ah_wslp2))) return NEMO_ERR_UNBOUND;
@@ -893,33 +947,7 @@ int ora_tra_zdf_imp(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
     if ((!is_trc && (jn == 1 || (jn == 2 && nm->ln_zdfddm))) || (is_trc && jn == 1)) {
       const double *coef = (!is_trc && jn == 1) ? avt : avs;
       if (!coef) { free(zwi); free(zwt); free(zwd); free(zws); return NEMO_ERR_UNBOUND; }
-      for (int jk = 2; jk <= jpk; ++jk)
-        for (int jj = 1; jj <= jpj; ++jj)
-          for (int ji = 1; ji <= jpi; ++ji) zwt[I3(ji, jj, jk)] = coef[I3(ji, jj, jk)];
-      for (int jj = 1; jj <= jpj; ++jj)
-        for (int ji = 1; ji <= jpi; ++ji) zwt[I3(ji, jj, 1)] = 0.0;
-      if (l_ldfslp) {
-        const double *add = nm->ln_traldf_msc ? akz : ah_wslp2;
-        for (int jk = 2; jk <= jpk - 1; ++jk)
-          for (int jj = 2; jj <= jpj - 1; ++jj)
-            for (int ji = 2; ji <= jpi - 1; ++ji) zwt[I3(ji, jj, jk)] = zwt[I3(ji, jj, jk)] + add[I3(ji, jj, jk)];
-      }
-      OMP_FOR
-      for (int jk = 1; jk <= jpk - 1; ++jk)
-        for (int jj = 2; jj <= jpj - 1; ++jj)
-          for (int ji = 2; ji <= jpi - 1; ++ji) {
-            size_t q = I3(ji, jj, jk);
-            zwi[q] = -p2dt * zwt[q] / e3w[q];
-            zws[q] = -p2dt * zwt[I3(ji, jj, jk + 1)] / e3w[I3(ji, jj, jk + 1)];
-            zwd[q] = e3t_a[q] - zwi[q] - zws[q];
-          }
-      for (int jj = 2; jj <= jpj - 1; ++jj)
-        for (int ji = 2; ji <= jpi - 1; ++ji) zwt[I3(ji, jj, 1)] = zwd[I3(ji, jj, 1)];
-      for (int jk = 2; jk <= jpk - 1; ++jk)
-        OMP_FOR
-        for (int jj = 2; jj <= jpj - 1; ++jj)
-          for (int ji = 2; ji <= jpi - 1; ++ji)
-            zwt[I3(ji, jj, jk)] = zwd[I3(ji, jj, jk)] - zwi[I3(ji, jj, jk)] * zws[I3(ji, jj, jk - 1)] / zwt[I3(ji, jj, jk - 1)];
+      zdf_lu(c, coef, p2dt, zwi, zwt, zwd, zws);
     }
     for (int jj = 2; jj <= jpj - 1; ++jj)
       for (int ji = 2; ji <= jpi - 1; ++ji) {
@@ -1579,4 +1607,431 @@ int ora_stp_hotpath(ora_ctx *c, int kt) {
                          c->f[NEMO_F_GTUI], c->f[NEMO_F_GTVI], tsb, tsa, 2, 1);
   if (st) return st;
   return ora_tra_zdf(c, kt);
+}
+
+/* =================================================================== adjoint */
+/* Adjoints of the tracer routines with respect to their tracer arguments. NEMO
+ * itself has none (its tangent-linear and adjoint, NEMOTAM, is a separate
+ * project), so these follow the forward routines above: each is the transpose of
+ * the forward's tangent-linear, written as the forward loops run backwards with
+ * every assignment's partial derivatives scattered onto its operands. The
+ * coefficients (transports, diffusivities, slopes, scale factors, avt, the
+ * partial-step bottom gradients pgu/pgv) are held fixed, and so are the FCT
+ * limiter multipliers, which the forward records (ora_set_fct_tape mode 1).
+ * Replaying them (mode 2) turns ora_tra_adv_fct into the tangent-linear with the
+ * limiter frozen; lap, iso, zdf and nxt are linear in the tracers, so their
+ * forward routines are their own tangent-linears. Conventions: an adjoint
+ * accumulates into the adjoints of the inputs (ptb_ad += ...), and the adjoint
+ * of a trend array pta that the forward only adds to is left unchanged. */
+
+int ora_set_fct_tape(ora_ctx *c, double *tape, int mode) {
+  if (!c || mode < 0 || mode > 2 || (mode && !tape)) return NEMO_ERR_ARG;
+  c->fct_tape = mode ? tape : NULL;
+  c->fct_tape_mode = mode;
+  return NEMO_OK;
+}
+
+/* Adjoint of ora_tra_adv_fct (kn_fct_h = kn_fct_v = 2) with the recorded limiter. */
+int ora_tra_adv_fct_adj(ora_ctx *c, int kt, int kit000, const char *cdtype, double p2dt,
+                        const double *pun, const double *pvn, const double *pwn,
+                        double *ptb_ad, double *ptn_ad, const double *pta_ad,
+                        int kjpt, int kn_fct_h, int kn_fct_v) {
+  (void)kt; (void)kit000; (void)cdtype; (void)p2dt;
+  if (kn_fct_h != 2 || kn_fct_v != 2 || kjpt < 1) return NEMO_ERR_ARG;
+  if (!c->fct_tape) return NEMO_ERR_UNBOUND;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  const double *tmask = c->tmask, *wmask = c->wmask, *e3t_n = fld(c, NEMO_F_E3T_N);
+  double *ax = zalloc(n3), *ay = zalloc(n3), *az = zalloc(n3);
+  double *fx = zalloc(n3), *fy = zalloc(n3), *fz = zalloc(n3);
+  for (int jn = 1; jn <= kjpt; ++jn) {
+    const double *lam = pta_ad + n3 * (jn - 1), *tp = c->fct_tape + 3 * n3 * (size_t)(jn - 1);
+    double *tb_ad = ptb_ad + n3 * (jn - 1), *tn_ad = ptn_ad + n3 * (jn - 1);
+    memset(ax, 0, n3 * sizeof(double)); memset(ay, 0, n3 * sizeof(double)); memset(az, 0, n3 * sizeof(double));
+    /* (:288-297) trend of the limited fluxes */
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double g = lam[q] * c->r1_e1e2t[I2(ji, jj)] / e3t_n[q];
+          ax[q] -= g; ax[I3(ji - 1, jj, jk)] += g;
+          ay[q] -= g; ay[I3(ji, jj - 1, jk)] += g;
+          az[q] -= g; az[I3(ji, jj, jk + 1)] += g;
+        }
+    /* (:284 nonosc, :280 lbc) the recorded multipliers, 0 where the flux was zeroed */
+    for (size_t q = 0; q < n3; ++q) { ax[q] *= tp[q]; ay[q] *= tp[n3 + q]; az[q] *= tp[2 * n3 + q]; }
+    /* (:276-278) linear free surface: no antidiffusive flux through the surface */
+    if (c->nam.ln_linssh)
+      for (size_t p = 0; p < n2; ++p) az[p] = 0.0;
+    /* (:255-263) vertical antidiffusive flux = centred - upstream, interior columns */
+    memcpy(fz, az, n3 * sizeof(double));
+    for (int jk = 2; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double a = az[q] * wmask[q];
+          tn_ad[q] += pwn[q] * 0.5 * a;
+          tn_ad[I3(ji, jj, jk - 1)] += pwn[q] * 0.5 * a;
+          fz[q] = -a;
+        }
+    /* (:182-190) horizontal antidiffusive fluxes */
+    memcpy(fx, ax, n3 * sizeof(double));
+    memcpy(fy, ay, n3 * sizeof(double));
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          tn_ad[q] += 0.5 * pun[q] * ax[q];
+          tn_ad[I3(ji + 1, jj, jk)] += 0.5 * pun[q] * ax[q];
+          tn_ad[q] += 0.5 * pvn[q] * ay[q];
+          tn_ad[I3(ji, jj + 1, jk)] += 0.5 * pvn[q] * ay[q];
+          fx[q] = -ax[q];
+          fy[q] = -ay[q];
+        }
+    /* (:158-170) upstream trend (zwi, used only by the frozen limiter, drops out) */
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double h = lam[q] * tmask[q] / e3t_n[q] * c->r1_e1e2t[I2(ji, jj)];
+          fx[q] -= h; fx[I3(ji - 1, jj, jk)] += h;
+          fy[q] -= h; fy[I3(ji, jj - 1, jk)] += h;
+          fz[q] -= h; fz[I3(ji, jj, jk + 1)] += h;
+        }
+    /* (:146-156) surface flux of the linear free surface */
+    if (c->nam.ln_linssh)
+      for (size_t p = 0; p < n2; ++p) tb_ad[p] += pwn[p] * fz[p];
+    /* (:137-145) vertical upstream flux */
+    for (int jk = 2; jk <= jpk - 1; ++jk)
+      for (int jj = 1; jj <= jpj; ++jj)
+        for (int ji = 1; ji <= jpi; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double a = 0.5 * fz[q] * wmask[q];
+          tb_ad[q] += (pwn[q] + fabs(pwn[q])) * a;
+          tb_ad[I3(ji, jj, jk - 1)] += (pwn[q] - fabs(pwn[q])) * a;
+        }
+    /* (:123-135) horizontal upstream fluxes */
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          tb_ad[q] += 0.5 * (pun[q] + fabs(pun[q])) * fx[q];
+          tb_ad[I3(ji + 1, jj, jk)] += 0.5 * (pun[q] - fabs(pun[q])) * fx[q];
+          tb_ad[q] += 0.5 * (pvn[q] + fabs(pvn[q])) * fy[q];
+          tb_ad[I3(ji, jj + 1, jk)] += 0.5 * (pvn[q] - fabs(pvn[q])) * fy[q];
+        }
+  }
+  free(ax); free(ay); free(az); free(fx); free(fy); free(fz);
+  return NEMO_OK;
+}
+
+/* Adjoint of ora_tra_ldf_lap. The partial-step bottom faces (ln_zps) take the
+ * fixed pgu/pgv, so nothing flows from them to tb. */
+int ora_tra_ldf_lap_adj(ora_ctx *c, int kt, int kit000, const char *cdtype,
+                        const double *pahu, const double *pahv,
+                        const double *pgu, const double *pgv, const double *pgui, const double *pgvi,
+                        double *ptb_ad, const double *pta_ad, int kjpt, int kpass) {
+  (void)kt; (void)kit000; (void)cdtype; (void)pgu; (void)pgv; (void)pgui; (void)pgvi;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n3 = (size_t)jpi * jpj * jpk;
+  if (!pahu) pahu = c->ahtu_c;
+  if (!pahv) pahv = c->ahtv_c;
+  const double *e3u = fld(c, NEMO_F_E3U_N), *e3v = fld(c, NEMO_F_E3V_N), *e3t_n = fld(c, NEMO_F_E3T_N);
+  const double zsign = kpass == 1 ? 1.0 : -1.0;
+  double *ztu = zalloc(n3), *ztv = zalloc(n3);
+  for (int jn = 1; jn <= kjpt; ++jn) {
+    const double *lam = pta_ad + n3 * (jn - 1);
+    double *tb_ad = ptb_ad + n3 * (jn - 1);
+    memset(ztu, 0, n3 * sizeof(double)); memset(ztv, 0, n3 * sizeof(double));
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double g = lam[q] / (c->e1e2t[I2(ji, jj)] * e3t_n[q]);
+          ztu[q] += g; ztu[I3(ji - 1, jj, jk)] -= g;
+          ztv[q] += g; ztv[I3(ji, jj - 1, jk)] -= g;
+        }
+    if (c->nam.ln_zps)
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          ztu[I3(ji, jj, c->mbku[I2(ji, jj)])] = 0.0;
+          ztv[I3(ji, jj, c->mbkv[I2(ji, jj)])] = 0.0;
+        }
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double au = zsign * pahu[q] * c->e2_e1u[I2(ji, jj)] * e3u[q] * ztu[q];
+          double av = zsign * pahv[q] * c->e1_e2v[I2(ji, jj)] * e3v[q] * ztv[q];
+          tb_ad[I3(ji + 1, jj, jk)] += au; tb_ad[q] -= au;
+          tb_ad[I3(ji, jj + 1, jk)] += av; tb_ad[q] -= av;
+        }
+  }
+  free(ztu); free(ztv);
+  return NEMO_OK;
+}
+
+/* Adjoint of ora_tra_ldf_iso with respect to ptb (and ptbb, which only kpass = 2
+ * without ln_traldf_lap reads). ah_wslp2 and akz are read as the forward left
+ * them; the adjoint does not modify them. */
+int ora_tra_ldf_iso_adj(ora_ctx *c, int kt, int kit000, const char *cdtype,
+                        const double *pahu, const double *pahv,
+                        const double *pgu, const double *pgv, const double *pgui, const double *pgvi,
+                        double *ptb_ad, double *ptbb_ad, const double *pta_ad, int kjpt, int kpass) {
+  (void)kt; (void)kit000; (void)cdtype; (void)pgu; (void)pgv; (void)pgui; (void)pgvi;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  const nemo_namelist *nm = &c->nam;
+  const double *ah_wslp2 = c->f[NEMO_F_AH_WSLP2], *akz = c->f[NEMO_F_AKZ];
+  const double *uslp = c->f[NEMO_F_USLP], *vslp = c->f[NEMO_F_VSLP];
+  const double *wslpi = c->f[NEMO_F_WSLPI], *wslpj = c->f[NEMO_F_WSLPJ];
+  if (!ah_wslp2 || !akz || !uslp || !vslp || !wslpi || !wslpj) return NEMO_ERR_UNBOUND;
+  const int use_tbb = !nm->ln_traldf_lap && kpass != 1;
+  if (use_tbb && !ptbb_ad) return NEMO_ERR_ARG;
+  if (!pahu) pahu = c->ahtu_c;
+  if (!pahv) pahv = c->ahtv_c;
+  const double *umask = c->umask, *vmask = c->vmask, *wmask = c->wmask;
+  const double *e3u = fld(c, NEMO_F_E3U_N), *e3v = fld(c, NEMO_F_E3V_N), *e3t_n = fld(c, NEMO_F_E3T_N);
+  const double *e3w = fld(c, NEMO_F_E3W_N);
+  const double zsign = kpass == 1 ? 1.0 : -1.0;
+  double *dit = zalloc(n3), *djt = zalloc(n3), *tfw = zalloc(n3);
+  double *dkt = zalloc(n2), *dk1t = zalloc(n2), *ftu = zalloc(n2), *ftv = zalloc(n2);
+  for (int jn = 1; jn <= kjpt; ++jn) {
+    const double *lam = pta_ad + n3 * (jn - 1);
+    double *tb_ad = ptb_ad + n3 * (jn - 1);
+    double *tbb_ad = use_tbb ? ptbb_ad + n3 * (jn - 1) : NULL;
+    memset(dit, 0, n3 * sizeof(double)); memset(djt, 0, n3 * sizeof(double)); memset(tfw, 0, n3 * sizeof(double));
+    /* (:359-366) divergence of the vertical fluxes */
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double g = zsign * lam[q] * c->r1_e1e2t[I2(ji, jj)] / e3t_n[q];
+          tfw[q] += g; tfw[I3(ji, jj, jk + 1)] -= g;
+        }
+    /* the flux zeroed at the surface, the bottom and the edge columns (:294-296) */
+    for (int jk = 1; jk <= jpk; ++jk)
+      for (int jj = 1; jj <= jpj; ++jj) { tfw[I3(1, jj, jk)] = 0.0; tfw[I3(jpi, jj, jk)] = 0.0; }
+    for (size_t p = 0; p < n2; ++p) { tfw[p] = 0.0; tfw[p + n2 * (jpk - 1)] = 0.0; }
+    /* (:323-357) vertical laplacian part, jj from 1 */
+    for (int jk = 2; jk <= jpk - 1; ++jk)
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk), qu = I3(ji, jj, jk - 1);
+          double f = c->e1e2t[I2(ji, jj)] / e3w[q] * wmask[q] * tfw[q];
+          if (nm->ln_traldf_lap) {
+            double a = (ah_wslp2[q] - akz[q]) * f;
+            tb_ad[qu] += a; tb_ad[q] -= a;
+          } else if (kpass == 1) {
+            double a = ah_wslp2[q] * f;
+            tb_ad[qu] += a; tb_ad[q] -= a;
+          } else {
+            double a = ah_wslp2[q] * f, b = akz[q] * f;
+            tb_ad[qu] += a; tb_ad[q] -= a;
+            tbb_ad[qu] += b; tbb_ad[q] -= b;
+          }
+        }
+    /* (:298-321) rotated vertical flux from the four surrounding horizontal gradients */
+    for (int jk = 2; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double zmsku = wmask[q] / dmax(umask[I3(ji, jj, jk - 1)] + umask[I3(ji - 1, jj, jk)]
+                                         + umask[I3(ji - 1, jj, jk - 1)] + umask[q], 1.0);
+          double zmskv = wmask[q] / dmax(vmask[I3(ji, jj, jk - 1)] + vmask[I3(ji, jj - 1, jk)]
+                                         + vmask[I3(ji, jj - 1, jk - 1)] + vmask[q], 1.0);
+          double zahu_w = (pahu[I3(ji, jj, jk - 1)] + pahu[I3(ji - 1, jj, jk)]
+                           + pahu[I3(ji - 1, jj, jk - 1)] + pahu[q]) * zmsku;
+          double zahv_w = (pahv[I3(ji, jj, jk - 1)] + pahv[I3(ji, jj - 1, jk)]
+                           + pahv[I3(ji, jj - 1, jk - 1)] + pahv[q]) * zmskv;
+          double a3 = -zahu_w * c->e2t[I2(ji, jj)] * zmsku * wslpi[q] * tfw[q];
+          double a4 = -zahv_w * c->e1t[I2(ji, jj)] * zmskv * wslpj[q] * tfw[q];
+          dit[I3(ji, jj, jk - 1)] += a3; dit[I3(ji - 1, jj, jk)] += a3;
+          dit[I3(ji - 1, jj, jk - 1)] += a3; dit[q] += a3;
+          djt[I3(ji, jj, jk - 1)] += a4; djt[I3(ji, jj - 1, jk)] += a4;
+          djt[I3(ji, jj - 1, jk - 1)] += a4; djt[q] += a4;
+        }
+    /* (:243-285) level by level: horizontal rotated fluxes and their divergence */
+    for (int jk = jpk - 1; jk >= 1; --jk) {
+      memset(ftu, 0, n2 * sizeof(double)); memset(ftv, 0, n2 * sizeof(double));
+      memset(dkt, 0, n2 * sizeof(double)); memset(dk1t, 0, n2 * sizeof(double));
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double g = zsign * lam[q] * c->r1_e1e2t[I2(ji, jj)] / e3t_n[q];
+          ftu[I2(ji, jj)] += g; ftu[I2(ji - 1, jj)] -= g;
+          ftv[I2(ji, jj)] += g; ftv[I2(ji, jj - 1)] -= g;
+        }
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double zabe1 = pahu[q] * c->e2_e1u[I2(ji, jj)] * e3u[q];
+          double zabe2 = pahv[q] * c->e1_e2v[I2(ji, jj)] * e3v[q];
+          double zmsku = 1. / dmax(wmask[I3(ji + 1, jj, jk)] + wmask[I3(ji, jj, jk + 1)]
+                                   + wmask[I3(ji + 1, jj, jk + 1)] + wmask[q], 1.);
+          double zmskv = 1. / dmax(wmask[I3(ji, jj + 1, jk)] + wmask[I3(ji, jj, jk + 1)]
+                                   + wmask[I3(ji, jj + 1, jk + 1)] + wmask[q], 1.);
+          double zcof1 = -pahu[q] * c->e2u[I2(ji, jj)] * uslp[q] * zmsku;
+          double zcof2 = -pahv[q] * c->e1v[I2(ji, jj)] * vslp[q] * zmskv;
+          double fu = ftu[I2(ji, jj)] * umask[q], fv = ftv[I2(ji, jj)] * vmask[q];
+          dit[q] += zabe1 * fu;
+          djt[q] += zabe2 * fv;
+          double u1 = zcof1 * fu, v1 = zcof2 * fv;
+          dkt[I2(ji + 1, jj)] += u1; dk1t[I2(ji, jj)] += u1; dk1t[I2(ji + 1, jj)] += u1; dkt[I2(ji, jj)] += u1;
+          dkt[I2(ji, jj + 1)] += v1; dk1t[I2(ji, jj)] += v1; dk1t[I2(ji, jj + 1)] += v1; dkt[I2(ji, jj)] += v1;
+        }
+      /* zdkt: (tb(k-1) - tb(k)) * wmask(k), or zdk1t at the surface (:246-251) */
+      if (jk == 1) {
+        for (size_t p = 0; p < n2; ++p) dk1t[p] += dkt[p];
+      } else {
+        for (size_t p = 0; p < n2; ++p) {
+          double a = dkt[p] * wmask[p + n2 * (jk - 1)];
+          tb_ad[p + n2 * (jk - 2)] += a; tb_ad[p + n2 * (jk - 1)] -= a;
+        }
+      }
+      /* zdk1t: (tb(k) - tb(k+1)) * wmask(k+1) */
+      for (size_t p = 0; p < n2; ++p) {
+        double a = dk1t[p] * wmask[p + n2 * jk];
+        tb_ad[p + n2 * (jk - 1)] += a; tb_ad[p + n2 * jk] -= a;
+      }
+    }
+    /* (:228-241) the partial-step bottom gradients are fixed inputs */
+    if (nm->ln_zps)
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          dit[I3(ji, jj, c->mbku[I2(ji, jj)])] = 0.0;
+          djt[I3(ji, jj, c->mbkv[I2(ji, jj)])] = 0.0;
+        }
+    /* (:218-227) masked horizontal gradients */
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double a = dit[q] * umask[q], b = djt[q] * vmask[q];
+          tb_ad[I3(ji + 1, jj, jk)] += a; tb_ad[q] -= a;
+          tb_ad[I3(ji, jj + 1, jk)] += b; tb_ad[q] -= b;
+        }
+  }
+  free(dit); free(djt); free(tfw); free(dkt); free(dk1t); free(ftu); free(ftv);
+  return NEMO_OK;
+}
+
+/* Adjoint of ora_tra_zdf_imp: pta_ad (adjoint of the after tracer) becomes the
+ * adjoint of the trend that entered, ptb_ad accumulates the before tracer's. */
+int ora_tra_zdf_imp_adj(ora_ctx *c, int kt, int kit000, const char *cdtype, double p2dt,
+                        double *ptb_ad, double *pta_ad, int kjpt) {
+  (void)kt; (void)kit000;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n3 = (size_t)jpi * jpj * jpk;
+  const nemo_namelist *nm = &c->nam;
+  const int is_trc = cdtype && cdtype[0] == 'T' && cdtype[1] == 'R' && cdtype[2] == 'C';
+  const double *avt = c->f[NEMO_F_AVT], *avs = c->f[NEMO_F_AVS];
+  const double *e3t_b = fld(c, NEMO_F_E3T_B), *e3t_n = fld(c, NEMO_F_E3T_N), *tmask = c->tmask;
+  if (!avt && !is_trc) return NEMO_ERR_UNBOUND;
+  if (nm->ln_traldf_iso && ((nm->ln_traldf_msc && !c->f[NEMO_F_AKZ]) || (!nm->ln_traldf_msc && !c->f[NEMO_F_AH_WSLP2])))
+    return NEMO_ERR_UNBOUND;
+  double *zwi = zalloc(n3), *zwt = zalloc(n3), *zwd = zalloc(n3), *zws = zalloc(n3);
+  for (int jn = 1; jn <= kjpt; ++jn) {
+    double *tb_ad = ptb_ad + n3 * (jn - 1), *lam = pta_ad + n3 * (jn - 1);
+    if ((!is_trc && (jn == 1 || (jn == 2 && nm->ln_zdfddm))) || (is_trc && jn == 1)) {
+      const double *coef = (!is_trc && jn == 1) ? avt : avs;
+      if (!coef) { free(zwi); free(zwt); free(zwd); free(zws); return NEMO_ERR_UNBOUND; }
+      zdf_lu(c, coef, p2dt, zwi, zwt, zwd, zws);
+    }
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        /* back-substitution (:252-264), run forwards */
+        for (int jk = 1; jk <= jpk - 2; ++jk) {
+          size_t q = I3(ji, jj, jk);
+          double a = lam[q] * tmask[q] / zwt[q];
+          lam[I3(ji, jj, jk + 1)] -= zws[q] * a;
+          lam[q] = a;
+        }
+        size_t qb = I3(ji, jj, jpk - 1);
+        lam[qb] = lam[qb] * tmask[qb] / zwt[qb];
+        /* forward elimination with the right-hand side (:238-250), run backwards */
+        for (int jk = jpk - 1; jk >= 2; --jk) {
+          size_t q = I3(ji, jj, jk);
+          lam[I3(ji, jj, jk - 1)] -= zwi[q] / zwt[I3(ji, jj, jk - 1)] * lam[q];
+          tb_ad[q] += e3t_b[q] * lam[q];
+          lam[q] = p2dt * e3t_n[q] * lam[q];
+        }
+        size_t q1 = I3(ji, jj, 1);
+        tb_ad[q1] += e3t_b[q1] * lam[q1];
+        lam[q1] = p2dt * e3t_n[q1] * lam[q1];
+      }
+  }
+  free(zwi); free(zwt); free(zwd); free(zws);
+  return NEMO_OK;
+}
+
+/* ---------------------------------------------------------------- tra_nxt */
+/* tranxt.F90:66-188 with tra_nxt_fix (:191-237) on the bound tsb, tsn, tsa
+ * (linear free surface; no trend diagnostics, bdy or agrif). */
+int ora_tra_nxt(ora_ctx *c, int kt) {
+  const nemo_namelist *nm = &c->nam;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n3 = (size_t)jpi * jpj * jpk;
+  double *tsb = c->f[NEMO_F_TSB], *tsn = c->f[NEMO_F_TSN], *tsa = c->f[NEMO_F_TSA];
+  if (!tsb || !tsn || !tsa) return NEMO_ERR_UNBOUND;
+  if (!nm->ln_linssh) return NEMO_ERR_ARG;
+  lbc_closed(jpi, jpj, tsa, 2 * jpk, 'T', 0.0);          /* :109 */
+  if (nm->neuler == 0 && kt == nm->nit000) {               /* :144-149 Euler: swap only */
+    for (int jn = 0; jn < 2; ++jn)
+      memcpy(tsn + n3 * jn, tsa + n3 * jn, (n3 - (size_t)jpi * jpj) * sizeof(double));
+    return NEMO_OK;
+  }
+  const double atfp = nm->rn_atfp;
+  for (int jn = 0; jn < 2; ++jn) {                          /* :221-234 */
+    double *tb = tsb + n3 * jn, *tn = tsn + n3 * jn, *ta = tsa + n3 * jn;
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double ztn = tn[q];
+          double ztd = ta[q] - 2.0 * ztn + tb[q];
+          tb[q] = ztn + atfp * ztd;
+          tn[q] = ta[q];
+        }
+  }
+  lbc_closed(jpi, jpj, tsb, 2 * jpk, 'T', 0.0);          /* :165-167 */
+  lbc_closed(jpi, jpj, tsn, 2 * jpk, 'T', 0.0);
+  return NEMO_OK;
+}
+
+/* Adjoint of ora_tra_nxt on three adjoint arrays (jpi,jpj,jpk,2): on entry the
+ * adjoints of the after-swap tsb, tsn, tsa; on exit those of the before-swap ones. */
+int ora_tra_nxt_adj(ora_ctx *c, int kt, double *tsb_ad, double *tsn_ad, double *tsa_ad) {
+  const nemo_namelist *nm = &c->nam;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  if (!tsb_ad || !tsn_ad || !tsa_ad) return NEMO_ERR_ARG;
+  if (!nm->ln_linssh) return NEMO_ERR_ARG;
+  if (nm->neuler == 0 && kt == nm->nit000) {
+    for (int jn = 0; jn < 2; ++jn)
+      for (size_t q = 0; q < n3 - n2; ++q) {
+        tsa_ad[n3 * jn + q] += tsn_ad[n3 * jn + q];
+        tsn_ad[n3 * jn + q] = 0.0;
+      }
+    lbc_closed(jpi, jpj, tsa_ad, 2 * jpk, 'T', 0.0);
+    return NEMO_OK;
+  }
+  const double atfp = nm->rn_atfp;
+  lbc_closed(jpi, jpj, tsb_ad, 2 * jpk, 'T', 0.0);
+  lbc_closed(jpi, jpj, tsn_ad, 2 * jpk, 'T', 0.0);
+  lbc_closed(jpi, jpj, tsa_ad, 2 * jpk, 'T', 0.0);
+  for (int jn = 0; jn < 2; ++jn) {
+    double *bb = tsb_ad + n3 * jn, *nn = tsn_ad + n3 * jn, *aa = tsa_ad + n3 * jn;
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          size_t q = I3(ji, jj, jk);
+          double b = bb[q], n = nn[q];
+          aa[q] += n + atfp * b;
+          nn[q] = b - 2.0 * atfp * b;
+          bb[q] = atfp * b;
+        }
+  }
+  lbc_closed(jpi, jpj, tsa_ad, 2 * jpk, 'T', 0.0);
+  return NEMO_OK;
 }

@@ -59,6 +59,26 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt);
 int ora_lbc_lnk(ora_ctx *c, double *ptab, int nk, int nl, char cd_nat, double psgn, double pval);
 int ora_glob_sum(ora_ctx *c, const double *ptab, int nk, double *out);
 int ora_stp_hotpath(ora_ctx *c, int kt);
+/* Adjoints with respect to the tracer arguments (the coefficients held fixed).
+ * tape: 3 * kjpt * jpi*jpj*jpk doubles of FCT limiter multipliers; mode 1 makes
+ * ora_tra_adv_fct record them, mode 2 replay them (tangent-linear), 0 neither. */
+int ora_set_fct_tape(ora_ctx *c, double *tape, int mode);
+int ora_tra_adv_fct_adj(ora_ctx *c, int kt, int kit000, const char *cdtype, double p2dt,
+                        const double *pun, const double *pvn, const double *pwn,
+                        double *ptb_ad, double *ptn_ad, const double *pta_ad,
+                        int kjpt, int kn_fct_h, int kn_fct_v);
+int ora_tra_ldf_lap_adj(ora_ctx *c, int kt, int kit000, const char *cdtype,
+                        const double *pahu, const double *pahv,
+                        const double *pgu, const double *pgv, const double *pgui, const double *pgvi,
+                        double *ptb_ad, const double *pta_ad, int kjpt, int kpass);
+int ora_tra_ldf_iso_adj(ora_ctx *c, int kt, int kit000, const char *cdtype,
+                        const double *pahu, const double *pahv,
+                        const double *pgu, const double *pgv, const double *pgui, const double *pgvi,
+                        double *ptb_ad, double *ptbb_ad, const double *pta_ad, int kjpt, int kpass);
+int ora_tra_zdf_imp_adj(ora_ctx *c, int kt, int kit000, const char *cdtype, double p2dt,
+                        double *ptb_ad, double *pta_ad, int kjpt);
+int ora_tra_nxt(ora_ctx *c, int kt);
+int ora_tra_nxt_adj(ora_ctx *c, int kt, double *tsb_ad, double *tsn_ad, double *tsa_ad);
 /* 1: start the work arrays standing for Fortran automatic arrays as NaN */
 void ora_set_poison(int on);
 

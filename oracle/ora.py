@@ -43,6 +43,13 @@ def lib():
         P("ora_glob_sum", [vp, vp, i, C.POINTER(d)])
         P("ora_stp_hotpath", [vp, i])
         P("ora_set_poison", [i], None)
+        P("ora_set_fct_tape", [vp, vp, i])
+        P("ora_tra_adv_fct_adj", [vp, i, i, cp, d, vp, vp, vp, vp, vp, vp, i, i, i])
+        P("ora_tra_ldf_lap_adj", [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
+        P("ora_tra_ldf_iso_adj", [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
+        P("ora_tra_zdf_imp_adj", [vp, i, i, cp, d, vp, vp, i])
+        P("ora_tra_nxt", [vp, i])
+        P("ora_tra_nxt_adj", [vp, i, vp, vp, vp])
         _lib = L
     return _lib
 
@@ -156,3 +163,35 @@ class Oracle:
 
     def stp_hotpath(self, kt):
         self._ck(lib().ora_stp_hotpath(self.h, kt), "stp_hotpath")
+
+    # ---------------------------------------------------------------- adjoint
+    def set_fct_tape(self, tape, mode):
+        """mode 1: tra_adv_fct records its limiter multipliers into tape; 2: replays
+        them (the tangent-linear with the limiter frozen); 0: neither."""
+        self._fct_tape = tape
+        self._ck(lib().ora_set_fct_tape(self.h, _p(tape) if tape is not None else None, mode), "set_fct_tape")
+
+    def tra_adv_fct_adj(self, kt, kit000, cdtype, p2dt, pun, pvn, pwn, ptb_ad, ptn_ad, pta_ad, kjpt, kh, kv):
+        self._ck(lib().ora_tra_adv_fct_adj(self.h, kt, kit000, cdtype.encode(), p2dt, _p(pun), _p(pvn), _p(pwn),
+                                           _p(ptb_ad), _p(ptn_ad), _p(pta_ad), kjpt, kh, kv), "tra_adv_fct_adj")
+
+    def tra_ldf_lap_adj(self, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb_ad, pta_ad, kjpt, kpass):
+        self._ck(lib().ora_tra_ldf_lap_adj(self.h, kt, kit000, cdtype.encode(), _p(pahu), _p(pahv), _p(pgu),
+                                           _p(pgv), _p(pgui), _p(pgvi), _p(ptb_ad), _p(pta_ad), kjpt, kpass),
+                 "tra_ldf_lap_adj")
+
+    def tra_ldf_iso_adj(self, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb_ad, ptbb_ad, pta_ad, kjpt,
+                        kpass):
+        self._ck(lib().ora_tra_ldf_iso_adj(self.h, kt, kit000, cdtype.encode(), _p(pahu), _p(pahv), _p(pgu),
+                                           _p(pgv), _p(pgui), _p(pgvi), _p(ptb_ad), _p(ptbb_ad), _p(pta_ad), kjpt,
+                                           kpass), "tra_ldf_iso_adj")
+
+    def tra_zdf_imp_adj(self, kt, kit000, cdtype, p2dt, ptb_ad, pta_ad, kjpt):
+        self._ck(lib().ora_tra_zdf_imp_adj(self.h, kt, kit000, cdtype.encode(), p2dt, _p(ptb_ad), _p(pta_ad), kjpt),
+                 "tra_zdf_imp_adj")
+
+    def tra_nxt(self, kt):
+        self._ck(lib().ora_tra_nxt(self.h, kt), "tra_nxt")
+
+    def tra_nxt_adj(self, kt, tsb_ad, tsn_ad, tsa_ad):
+        self._ck(lib().ora_tra_nxt_adj(self.h, kt, _p(tsb_ad), _p(tsn_ad), _p(tsa_ad)), "tra_nxt_adj")
