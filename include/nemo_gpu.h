@@ -159,6 +159,12 @@ enum nemo_field_id {
                                               flux-form momentum, ln_dynadv_vec = 0)   */
   NEMO_F_R1_HU_B, NEMO_F_R1_HV_B,      /* [S] (centred integration)                   */
   NEMO_F_E3F_N,                        /* [T] now e3 at F-points (ENE/ENS/MIX schemes) */
+  /* Adjoint support (FP64 contexts; no counterpart in the reference): while bound,
+   * nemo_gpu_tra_adv_fct records its limiter multipliers here and
+   * nemo_gpu_tra_adv_fct_adj reads them. 3 * kjpt * jpi*jpj*jpk doubles per
+   * member, ordered (member, tracer, face x/y/z, k, j, i); 0 where the forward
+   * zeroed the antidiffusive flux. */
+  NEMO_F_FCT_TAPE,
   NEMO_F_COUNT
 };
 
@@ -251,6 +257,50 @@ int nemo_gpu_tra_zdf_imp(nemo_ctx *ctx, int kt, int kit000, const char *cdtype, 
  * implicit solve, then WHERE( tsa(:,:,:,jp_sal) < 0 ) tsa = 0.1 (:83). */
 int nemo_gpu_tra_zdf(nemo_ctx *ctx, int kt);
 
+/* tra_nxt (tranxt.F90:66-188 with tra_nxt_fix :191-237) on the bound tsb, tsn,
+ * tsa: lbc_lnk of tsa, then at the first step of an Euler start (neuler = 0,
+ * kt = nit000) tsn = tsa, otherwise the leapfrog swap with the Asselin filter
+ * tsb = tsn + rn_atfp (tsa - 2 tsn + tsb), tsn = tsa on the interior, and lbc_lnk
+ * of tsb and tsn. Linear free surface only (tra_nxt_vvl is not on the path). */
+int nemo_gpu_tra_nxt(nemo_ctx *ctx, int kt);
+
+/* ------------------------------------------------------------ adjoint
+ * Adjoints of the tracer routines with respect to their tracer arguments, in an
+ * FP64 context (NEMO_ERR_ARG otherwise). NEMO has no adjoint of these routines in
+ * its tree (its tangent-linear/adjoint, NEMOTAM, is a separate project), so these
+ * entry points have no reference counterpart; each keeps the argument list of its
+ * forward routine with the tracer arrays replaced by their adjoints, and is the
+ * transpose of the forward's tangent-linear with the coefficients (transports,
+ * diffusivities, slopes, scale factors, avt, ah_wslp2/akz as the forward left them)
+ * held fixed. An adjoint accumulates into the adjoints of the inputs
+ * (ptb_ad += ...); the adjoint of a trend array that the forward only adds to
+ * (pta_ad of tra_adv_fct and tra_ldf_*) is read and left unchanged. */
+
+/* FCT (kn_fct_h = kn_fct_v = 2) with the limiter multipliers the forward call
+ * recorded in NEMO_F_FCT_TAPE held fixed: ptb_ad += A_b^T pta_ad,
+ * ptn_ad += A_n^T pta_ad. pun, pvn, pwn are the forward call's transports. */
+int nemo_gpu_tra_adv_fct_adj(nemo_ctx *ctx, int kt, int kit000, const char *cdtype, double p2dt,
+                             const void *pun, const void *pvn, const void *pwn, void *ptb_ad,
+                             void *ptn_ad, const void *pta_ad, int kjpt, int kn_fct_h, int kn_fct_v);
+/* tra_ldf_lap: ptb_ad += L^T pta_ad. With ln_zps the bottom faces take the fixed
+ * pgu/pgv, so nothing flows through them. */
+int nemo_gpu_tra_ldf_lap_adj(nemo_ctx *ctx, int kt, int kit000, const char *cdtype, const void *pahu,
+                             const void *pahv, const void *pgu, const void *pgv, const void *pgui,
+                             const void *pgvi, void *ptb_ad, const void *pta_ad, int kjpt, int kpass);
+/* tra_ldf_iso: ptb_ad += ..., and ptbb_ad += ... for kpass = 2 without
+ * ln_traldf_lap (ptbb_ad may be NULL otherwise). Reads the bound ah_wslp2/akz. */
+int nemo_gpu_tra_ldf_iso_adj(nemo_ctx *ctx, int kt, int kit000, const char *cdtype, const void *pahu,
+                             const void *pahv, const void *pgu, const void *pgv, const void *pgui,
+                             const void *pgvi, void *ptb_ad, void *ptbb_ad, const void *pta_ad, int kjpt,
+                             int kpass);
+/* tra_zdf_imp: on entry pta_ad is the adjoint of the after tracer, on exit that
+ * of the trend the forward read; ptb_ad += e3t_b M^-T pta_ad. */
+int nemo_gpu_tra_zdf_imp_adj(nemo_ctx *ctx, int kt, int kit000, const char *cdtype, double p2dt,
+                             void *ptb_ad, void *pta_ad, int kjpt);
+/* tra_nxt on three (jpi,jpj,jpk,2) adjoint arrays: on entry the adjoints of the
+ * swapped tsb, tsn, tsa, on exit those of the fields before the swap. */
+int nemo_gpu_tra_nxt_adj(nemo_ctx *ctx, int kt, void *tsb_ad, void *tsn_ad, void *tsa_ad);
+
 /* dyn_spg_ts (dynspg_ts.F90:121-1310) on the bound fields: phase 1 forcing,
  * icycle barotropic sub-steps in one persistent kernel, phase 3 correction. */
 int nemo_gpu_dyn_spg_ts(nemo_ctx *ctx, int kt);
@@ -319,6 +369,8 @@ enum nemo_kernel_id {
   NEMO_K_ISO_FLUX_TMA, /* iso-neutral fluxes with TMA-staged tracer planes */
   NEMO_K_FCT_FUSED,    /* FCT stages a, b, c in one kernel, TMA-staged inputs */
   NEMO_K_FCT_A_TMA, NEMO_K_FCT_B_TMA, /* FCT stages a, b with TMA-staged planes */
+  NEMO_K_FCT_ADJ, NEMO_K_LAP_ADJ, NEMO_K_ISO_ADJ, NEMO_K_ZDF_ADJ, /* adjoints */
+  NEMO_K_TRA_NXT, NEMO_K_TRA_NXT_ADJ,
   NEMO_K_COUNT
 };
 

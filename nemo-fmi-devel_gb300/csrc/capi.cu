@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/nemo_gpu.h"
+#include "adj.h"
 #include "launch.h"
 
 using namespace nemo;
@@ -71,6 +72,8 @@ struct nemo_ctx {
   void* fct_w[6] = {};
   void* fct_ztw = nullptr;
   void* iso_w[3] = {};         // iso-neutral fluxes zftu, zftv, ztfw
+  void* adj_w[4] = {};         // iso-neutral adjoint: G and the gradient adjoints
+  int adj_kjpt = 0;
   int iso_kjpt = 0;
   int fct_kjpt = 0;
   void* spg_w[5] = {};
@@ -212,7 +215,7 @@ bool spg_writes(int id) {
 // scale factors at u- and v-points, every 2-D field (and e3f_n)
 bool spg_reads(int id) {
   if (spg_writes(id) || id == NEMO_F_UB || id == NEMO_F_VB || id == NEMO_F_E3U_N || id == NEMO_F_E3V_N) return true;
-  return id >= NEMO_F_SSHB;
+  return id >= NEMO_F_SSHB && id != NEMO_F_FCT_TAPE;
 }
 
 inline size_t I2(const nemo_ctx* c, int i, int j) { return (size_t)(i - 1) + (size_t)c->jpi * (j - 1); }
@@ -233,6 +236,7 @@ size_t field_numel(const nemo_ctx* c, int id) {
     case NEMO_F_TSB: case NEMO_F_TSN: case NEMO_F_TSA: return 2 * (size_t)c->n3;
     case NEMO_F_GTSU: case NEMO_F_GTSV: case NEMO_F_GTUI: case NEMO_F_GTVI: return 2 * (size_t)c->n2;
     case NEMO_F_E3F_N: return (size_t)c->n3;
+    case NEMO_F_FCT_TAPE: return 6 * (size_t)c->n3;  // 3 faces x 2 tracers
     default: break;
   }
   if (id >= NEMO_F_SSHB) return (size_t)c->n2;
@@ -619,10 +623,14 @@ int check_cdtype(nemo_ctx* c, const char* cdtype, int* is_trc) {
 template <class T>
 int run_fct(nemo_ctx* c, double p2dt, const void* pun, const void* pvn, const void* pwn, int trp, const void* ptb,
             const void* ptn, const void* pta_in, void* pta, int kjpt, int kh, int kv,
-            const LdfArgs<T>* iso = nullptr) {
+            const LdfArgs<T>* iso = nullptr, void* lim = nullptr) {
   int s = ensure_fct_work(c, kjpt, kv == 4);
   if (s) return s;
   FctArgs<T> a{};
+  if (lim) {  // record the limiter multipliers (0 on the faces the forward zeroes)
+    a.lim = (T*)lim;
+    CK(cudaMemsetAsync(lim, 0, 3 * (size_t)kjpt * c->n3 * c->nmem * sizeof(T), c->stream), "FCT tape = 0");
+  }
   a.p2dt = (T)p2dt;
   a.pun = (const T*)pun; a.pvn = (const T*)pvn; a.pwn = (const T*)pwn; a.trp = trp;
   a.ptb = (const T*)ptb; a.ptn = (const T*)ptn; a.pta_in = (const T*)pta_in; a.pta = (T*)pta;
@@ -1061,6 +1069,7 @@ int nemo_gpu_destroy(nemo_ctx* c) {
   for (auto p : c->fct_w) cudaFree(p);
   cudaFree(c->fct_ztw);
   for (auto p : c->iso_w) cudaFree(p);
+  for (auto p : c->adj_w) cudaFree(p);
   for (auto p : c->spg_w) cudaFree(p);
   for (auto p : c->spg_cor) cudaFree(p);
   for (auto p : c->ring) cudaFree(p);
@@ -1200,8 +1209,11 @@ int nemo_gpu_tra_adv_fct(nemo_ctx* c, int kt, int kit000, const char* cdtype, do
   if (!pun || !pvn || !pwn || !ptb || !ptn || !pta || kjpt < 1) return fail(c, NEMO_ERR_ARG, "tra_adv_fct: bad argument");
   if ((kn_fct_h != 2 && kn_fct_h != 4) || (kn_fct_v != 2 && kn_fct_v != 4))
     return fail(c, NEMO_ERR_ARG, "tra_adv_fct: kn_fct_h/kn_fct_v must be 2 or 4");
+  void* tape = c->f[NEMO_F_FCT_TAPE];
+  if (tape && c->prec != NEMO_PREC_FP64)
+    return fail(c, NEMO_ERR_ARG, "tra_adv_fct: the limiter tape needs an FP64 context");
   return c->prec == NEMO_PREC_FP64
-             ? run_fct<double>(c, p2dt, pun, pvn, pwn, 0, ptb, ptn, pta, pta, kjpt, kn_fct_h, kn_fct_v)
+             ? run_fct<double>(c, p2dt, pun, pvn, pwn, 0, ptb, ptn, pta, pta, kjpt, kn_fct_h, kn_fct_v, nullptr, tape)
              : run_fct<float>(c, p2dt, pun, pvn, pwn, 0, ptb, ptn, pta, pta, kjpt, kn_fct_h, kn_fct_v);
 }
 
@@ -1264,6 +1276,149 @@ int nemo_gpu_tra_zdf(nemo_ctx* c, int kt) {
                         : launch_clamp<float>((float*)c->f[NEMO_F_TSA] + (2L * m + 1) * c->n3, c->n3, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "tra_zdf clamp");
   }
+  return NEMO_OK;
+}
+
+int nemo_gpu_tra_nxt(nemo_ctx* c, int kt) {
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  const nemo_namelist& nm = c->nam;
+  void* const* F = c->f;
+  if (!F[NEMO_F_TSB] || !F[NEMO_F_TSN] || !F[NEMO_F_TSA])
+    return fail(c, NEMO_ERR_UNBOUND, "tra_nxt: tsb, tsn and tsa must be bound");
+  if (!nm.ln_linssh) return fail(c, NEMO_ERR_ARG, "tra_nxt: linear free surface only (ln_linssh)");
+  const int euler = nm.neuler == 0 && kt == nm.nit000;
+  cudaError_t e =
+      c->prec == NEMO_PREC_FP64
+          ? launch_tra_nxt<double>(dom<double>(c), (double*)F[NEMO_F_TSB], (double*)F[NEMO_F_TSN],
+                                   (double*)F[NEMO_F_TSA], nm.rn_atfp, euler, c->stream)
+          : launch_tra_nxt<float>(dom<float>(c), (float*)F[NEMO_F_TSB], (float*)F[NEMO_F_TSN], (float*)F[NEMO_F_TSA],
+                                  (float)nm.rn_atfp, euler, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "tra_nxt launch");
+  return NEMO_OK;
+}
+
+// ---------------------------------------------------------------------- adjoint
+static int adj_check(nemo_ctx* c, const char* cdtype, int* is_trc, const char* what) {
+  if (c->prec != NEMO_PREC_FP64) return fail(c, NEMO_ERR_ARG, "%s: adjoints need an FP64 context", what);
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (cdtype) return check_cdtype(c, cdtype, is_trc);
+  return NEMO_OK;
+}
+
+static int ensure_adj_work(nemo_ctx* c, int kjpt) {
+  if (kjpt <= c->adj_kjpt) return NEMO_OK;
+  const size_t bytes = (size_t)kjpt * c->n3 * c->nmem * sizeof(double);
+  for (auto& p : c->adj_w) {
+    cudaFree(p);
+    p = nullptr;
+  }
+  for (auto& p : c->adj_w)
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return fail(c, NEMO_ERR_NOMEM, "adjoint work arrays (%zu bytes)", bytes);
+  c->adj_kjpt = kjpt;
+  return NEMO_OK;
+}
+
+int nemo_gpu_tra_adv_fct_adj(nemo_ctx* c, int kt, int kit000, const char* cdtype, double p2dt, const void* pun,
+                             const void* pvn, const void* pwn, void* ptb_ad, void* ptn_ad, const void* pta_ad,
+                             int kjpt, int kn_fct_h, int kn_fct_v) {
+  (void)kt; (void)kit000; (void)p2dt;
+  if (!c) return NEMO_ERR_ARG;
+  int is_trc = 0;
+  if (int s = adj_check(c, cdtype, &is_trc, "tra_adv_fct_adj")) return s;
+  if (!pun || !pvn || !pwn || !ptb_ad || !ptn_ad || !pta_ad || kjpt < 1)
+    return fail(c, NEMO_ERR_ARG, "tra_adv_fct_adj: bad argument");
+  if (kn_fct_h != 2 || kn_fct_v != 2) return fail(c, NEMO_ERR_ARG, "tra_adv_fct_adj: kn_fct_h = kn_fct_v = 2 only");
+  if (!c->f[NEMO_F_FCT_TAPE])
+    return fail(c, NEMO_ERR_UNBOUND, "tra_adv_fct_adj: the limiter tape NEMO_F_FCT_TAPE must be bound");
+  FctAdj a{};
+  a.pun = (const double*)pun; a.pvn = (const double*)pvn; a.pwn = (const double*)pwn;
+  a.lam = (const double*)pta_ad; a.tape = (const double*)c->f[NEMO_F_FCT_TAPE];
+  a.tb_ad = (double*)ptb_ad; a.tn_ad = (double*)ptn_ad;
+  a.kjpt = kjpt; a.linssh = c->nam.ln_linssh;
+  cudaError_t e = launch_fct_adj(dom_now<double>(c), a, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "tra_adv_fct_adj launch");
+  return NEMO_OK;
+}
+
+int nemo_gpu_tra_ldf_lap_adj(nemo_ctx* c, int kt, int kit000, const char* cdtype, const void* pahu, const void* pahv,
+                             const void* pgu, const void* pgv, const void* pgui, const void* pgvi, void* ptb_ad,
+                             const void* pta_ad, int kjpt, int kpass) {
+  (void)kt; (void)kit000; (void)pgui; (void)pgvi;
+  if (!c) return NEMO_ERR_ARG;
+  int is_trc = 0;
+  if (int s = adj_check(c, cdtype, &is_trc, "tra_ldf_lap_adj")) return s;
+  if (!ptb_ad || !pta_ad || kjpt < 1 || (kpass != 1 && kpass != 2))
+    return fail(c, NEMO_ERR_ARG, "tra_ldf_lap_adj: bad argument");
+  LdfArgs<double> a = ldf_args<double>(c, pahu, pahv, pgu, pgv, nullptr, nullptr, nullptr, kjpt, kpass);
+  LdfAdj b{};
+  b.lam = (const double*)pta_ad; b.tb_ad = (double*)ptb_ad;
+  cudaError_t e = launch_lap_adj(dom_now<double>(c), a, b, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "tra_ldf_lap_adj launch");
+  return NEMO_OK;
+}
+
+int nemo_gpu_tra_ldf_iso_adj(nemo_ctx* c, int kt, int kit000, const char* cdtype, const void* pahu, const void* pahv,
+                             const void* pgu, const void* pgv, const void* pgui, const void* pgvi, void* ptb_ad,
+                             void* ptbb_ad, const void* pta_ad, int kjpt, int kpass) {
+  (void)kt; (void)kit000; (void)pgui; (void)pgvi;
+  if (!c) return NEMO_ERR_ARG;
+  int is_trc = 0;
+  if (int s = adj_check(c, cdtype, &is_trc, "tra_ldf_iso_adj")) return s;
+  const nemo_namelist& nm = c->nam;
+  if (!ptb_ad || !pta_ad || kjpt < 1 || (kpass != 1 && kpass != 2) || (kpass == 2 && !nm.ln_traldf_lap && !ptbb_ad))
+    return fail(c, NEMO_ERR_ARG, "tra_ldf_iso_adj: bad argument");
+  if (!c->f[NEMO_F_USLP] || !c->f[NEMO_F_VSLP] || !c->f[NEMO_F_WSLPI] || !c->f[NEMO_F_WSLPJ] ||
+      !c->f[NEMO_F_AH_WSLP2] || !c->f[NEMO_F_AKZ])
+    return fail(c, NEMO_ERR_UNBOUND, "tra_ldf_iso_adj: slopes, ah_wslp2 and akz must be bound");
+  if (int s = ensure_adj_work(c, kjpt)) return s;
+  LdfArgs<double> a = ldf_args<double>(c, pahu, pahv, pgu, pgv, nullptr, nullptr, nullptr, kjpt, kpass);
+  a.uslp = (const double*)c->f[NEMO_F_USLP]; a.vslp = (const double*)c->f[NEMO_F_VSLP];
+  a.wslpi = (const double*)c->f[NEMO_F_WSLPI]; a.wslpj = (const double*)c->f[NEMO_F_WSLPJ];
+  a.ah_wslp2 = (double*)c->f[NEMO_F_AH_WSLP2]; a.akz = (double*)c->f[NEMO_F_AKZ];
+  a.lap = nm.ln_traldf_lap; a.blp = nm.ln_traldf_blp; a.msc = nm.ln_traldf_msc;
+  LdfAdj b{};
+  b.lam = (const double*)pta_ad; b.tb_ad = (double*)ptb_ad; b.tbb_ad = (double*)ptbb_ad;
+  b.G = (double*)c->adj_w[0]; b.dit = (double*)c->adj_w[1]; b.djt = (double*)c->adj_w[2]; b.dk = (double*)c->adj_w[3];
+  cudaError_t e = launch_iso_adj(dom_now<double>(c), a, b, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "tra_ldf_iso_adj launch");
+  return NEMO_OK;
+}
+
+int nemo_gpu_tra_zdf_imp_adj(nemo_ctx* c, int kt, int kit000, const char* cdtype, double p2dt, void* ptb_ad,
+                             void* pta_ad, int kjpt) {
+  (void)kt; (void)kit000;
+  if (!c) return NEMO_ERR_ARG;
+  int is_trc = 0;
+  if (int s = adj_check(c, cdtype, &is_trc, "tra_zdf_imp_adj")) return s;
+  if (!ptb_ad || !pta_ad || kjpt < 1) return fail(c, NEMO_ERR_ARG, "tra_zdf_imp_adj: bad argument");
+  const nemo_namelist& nm = c->nam;
+  ZdfArgs<double> a{};
+  a.p2dt = p2dt; a.kjpt = kjpt;
+  a.avt = (const double*)c->f[NEMO_F_AVT]; a.avs = (const double*)c->f[NEMO_F_AVS];
+  a.ddm = nm.ln_zdfddm; a.is_trc = is_trc;
+  if (!is_trc && !a.avt) return fail(c, NEMO_ERR_UNBOUND, "tra_zdf_imp_adj: avt must be bound");
+  if ((is_trc || nm.ln_zdfddm) && !a.avs) return fail(c, NEMO_ERR_UNBOUND, "tra_zdf_imp_adj: avs must be bound");
+  if (nm.ln_traldf_iso) {
+    a.add = (const double*)c->f[nm.ln_traldf_msc ? NEMO_F_AKZ : NEMO_F_AH_WSLP2];
+    if (!a.add) return fail(c, NEMO_ERR_UNBOUND, "tra_zdf_imp_adj: ah_wslp2/akz must be bound");
+  }
+  ZdfAdj b{(double*)pta_ad, (double*)ptb_ad};
+  cudaError_t e = launch_zdf_adj(dom_now<double>(c), a, b, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "tra_zdf_imp_adj launch");
+  return NEMO_OK;
+}
+
+int nemo_gpu_tra_nxt_adj(nemo_ctx* c, int kt, void* tsb_ad, void* tsn_ad, void* tsa_ad) {
+  if (!c) return NEMO_ERR_ARG;
+  if (int s = adj_check(c, nullptr, nullptr, "tra_nxt_adj")) return s;
+  if (!tsb_ad || !tsn_ad || !tsa_ad) return fail(c, NEMO_ERR_ARG, "tra_nxt_adj: null pointer");
+  const nemo_namelist& nm = c->nam;
+  if (!nm.ln_linssh) return fail(c, NEMO_ERR_ARG, "tra_nxt_adj: linear free surface only (ln_linssh)");
+  const int euler = nm.neuler == 0 && kt == nm.nit000;
+  cudaError_t e = launch_tra_nxt_adj(dom<double>(c), (double*)tsb_ad, (double*)tsn_ad, (double*)tsa_ad, nm.rn_atfp,
+                                     euler, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "tra_nxt_adj launch");
   return NEMO_OK;
 }
 

@@ -70,7 +70,7 @@ static bool field_tensor_map(const Dom<T>& d, const T* base, int nf, unsigned bx
 
 template <class T>
 cudaError_t launch_fct(const Dom<T>& d, const FctArgs<T>& a, cudaStream_t s) {
-  if (hot_fct_ok(d, a)) {
+  if (hot_fct_ok(d, a) && !a.lim) {  // the limiter is recorded by k_fct_c only
     if constexpr (sizeof(T) == 4) {
       if (a.tma && a.err && a.kjpt == 2) {  // planes staged by TMA
         if (a.fused) {  // the three stages in one kernel

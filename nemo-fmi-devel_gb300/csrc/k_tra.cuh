@@ -146,6 +146,8 @@ struct FctArgs {
   int tma;                   // FP32 hot configuration: stage the planes by TMA
   int fused;                 // with tma: the three stages as one kernel (k_fct_fused_tma)
   int* err;                  // device error flag (a timed-out wait of a TMA kernel)
+  T* lim;                    // NULL, or where k_fct_c records the limiter multipliers
+                             // ((member*kjpt + n)*3 + face)*n3, for the adjoint
 };
 
 // Upstream transports at the faces of column (i,j) (traadv_fct.F90:123-145).
@@ -384,13 +386,18 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 4) k_fct_b(Dom<T> d,
   }
 }
 
-// Limited antidiffusive flux (traadv_fct.F90:407-422): f * ( c*a + (1-c)*b ).
+// Limiter multiplier of an antidiffusive flux f (traadv_fct.F90:407-422): c*a + (1-c)*b.
 template <class T>
-__device__ __forceinline__ T limit(T f, T bdo0, T bup1, T bup0, T bdo1) {
+__device__ __forceinline__ T limit_mult(T f, T bdo0, T bup1, T bup0, T bdo1) {
   const T za = fmn(T(1), fmn(bdo0, bup1));
   const T zb = fmn(T(1), fmn(bup0, bdo1));
   const T zc = (T(0.5) + sign_nsz(T(0.5), f));
-  return f * (zc * za + (T(1) - zc) * zb);
+  return zc * za + (T(1) - zc) * zb;
+}
+// Limited antidiffusive flux: f * ( c*a + (1-c)*b ).
+template <class T>
+__device__ __forceinline__ T limit(T f, T bdo0, T bup1, T bup0, T bdo1) {
+  return f * limit_mult(f, bdo0, bup1, bup0, bdo1);
 }
 
 // interp_4th_cpt (traadv_fct.F90:517-616): compact 4th-order tn at w-points for the
@@ -770,6 +777,12 @@ __global__ void __launch_bounds__(128) k_fct_c(Dom<T> d, FctArgs<T> a) {
         const T ayls = s_lim ? limit(ay[q - jpi], bd[q - jpi], b_u, bu[q - jpi], b_d) : T(0);
         // pcc(k+1): the limited flux through the bottom face
         const T azl_b = limit(az[qp], bdp, b_u, bup, b_d);
+        if (a.lim) {  // the multipliers of the faces this point owns
+          T* L = a.lim + ((long)c.m * a.kjpt + n) * 3 * n3;
+          L[q] = limit_mult(ax[q], b_d, bu[q + 1], b_u, bd[q + 1]);
+          L[n3 + q] = limit_mult(ay[q], b_d, bu[q + jpi], b_u, bd[q + jpi]);
+          L[2 * n3 + qp] = limit_mult(az[qp], bdp, b_u, bup, b_d);
+        }
         T tav = ta[q] - (axl - axlw + ayl - ayls + azt[nn] - azl_b) * r1_e1e2t / e3n;
         if (a.with_iso) {
           // iso-neutral divergence: horizontal (traldf_iso.F90:278-284), then

@@ -108,6 +108,12 @@ def load(path):
     _proto(lib, "nemo_gpu_tra_ldf_lap", i, [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
     _proto(lib, "nemo_gpu_tra_ldf_iso", i, [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
     _proto(lib, "nemo_gpu_tra_zdf_imp", i, [vp, i, i, cp, d, vp, vp, i])
+    _proto(lib, "nemo_gpu_tra_nxt", i, [vp, i])
+    _proto(lib, "nemo_gpu_tra_adv_fct_adj", i, [vp, i, i, cp, d, vp, vp, vp, vp, vp, vp, i, i, i])
+    _proto(lib, "nemo_gpu_tra_ldf_lap_adj", i, [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
+    _proto(lib, "nemo_gpu_tra_ldf_iso_adj", i, [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
+    _proto(lib, "nemo_gpu_tra_zdf_imp_adj", i, [vp, i, i, cp, d, vp, vp, i])
+    _proto(lib, "nemo_gpu_tra_nxt_adj", i, [vp, i, vp, vp, vp])
     _proto(lib, "nemo_gpu_tra_zdf", i, [vp, i])
     _proto(lib, "nemo_gpu_dyn_spg_ts", i, [vp, i])
     _proto(lib, "nemo_gpu_lbc_lnk", i, [vp, cp, vp, i, i, cp, d, d, i])

@@ -178,6 +178,34 @@ class Context:
     def tra_zdf(self, kt):
         self._ck(self.lib.nemo_gpu_tra_zdf(self.h, kt), "tra_zdf")
 
+    def tra_nxt(self, kt):
+        self._ck(self.lib.nemo_gpu_tra_nxt(self.h, kt), "tra_nxt")
+
+    # ------------------------------------------------------------------ adjoints
+    # The adjoint twins of the tracer routines (FP64 contexts): the tracer arrays of
+    # the forward's argument list are replaced by their adjoints; see nemo_gpu.h.
+    def tra_adv_fct_adj(self, kt, kit000, cdtype, p2dt, pun, pvn, pwn, ptb_ad, ptn_ad, pta_ad, kjpt, kn_fct_h,
+                        kn_fct_v):
+        self._ck(self.lib.nemo_gpu_tra_adv_fct_adj(self.h, kt, kit000, cdtype.encode(), p2dt, _ptr(pun), _ptr(pvn),
+                                                   _ptr(pwn), _ptr(ptb_ad), _ptr(ptn_ad), _ptr(pta_ad), kjpt,
+                                                   kn_fct_h, kn_fct_v), "tra_adv_fct_adj")
+
+    def tra_ldf_lap_adj(self, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb_ad, pta_ad, kjpt, kpass):
+        self._ck(self.lib.nemo_gpu_tra_ldf_lap_adj(self.h, kt, kit000, cdtype.encode(), *map(_ptr, (
+            pahu, pahv, pgu, pgv, pgui, pgvi, ptb_ad, pta_ad)), kjpt, kpass), "tra_ldf_lap_adj")
+
+    def tra_ldf_iso_adj(self, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb_ad, ptbb_ad, pta_ad, kjpt,
+                        kpass):
+        self._ck(self.lib.nemo_gpu_tra_ldf_iso_adj(self.h, kt, kit000, cdtype.encode(), *map(_ptr, (
+            pahu, pahv, pgu, pgv, pgui, pgvi, ptb_ad, ptbb_ad, pta_ad)), kjpt, kpass), "tra_ldf_iso_adj")
+
+    def tra_zdf_imp_adj(self, kt, kit000, cdtype, p2dt, ptb_ad, pta_ad, kjpt):
+        self._ck(self.lib.nemo_gpu_tra_zdf_imp_adj(self.h, kt, kit000, cdtype.encode(), p2dt, _ptr(ptb_ad),
+                                                   _ptr(pta_ad), kjpt), "tra_zdf_imp_adj")
+
+    def tra_nxt_adj(self, kt, tsb_ad, tsn_ad, tsa_ad):
+        self._ck(self.lib.nemo_gpu_tra_nxt_adj(self.h, kt, _ptr(tsb_ad), _ptr(tsn_ad), _ptr(tsa_ad)), "tra_nxt_adj")
+
     def dyn_spg_ts(self, kt):
         self._ck(self.lib.nemo_gpu_dyn_spg_ts(self.h, kt), "dyn_spg_ts")
 

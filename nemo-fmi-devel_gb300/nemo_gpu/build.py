@@ -1,6 +1,6 @@
 """Build recipe of the CUDA library (sm_103a only).
 
-Four translation units are compiled in parallel and linked into
+Five translation units are compiled in parallel and linked into
 ``nemo_gpu/_lib/libnemo_gpu.so``:
 
 * ``inst_fp64.cu`` -- FP64 kernels, ``--fmad=false`` so that every double operation
@@ -10,7 +10,9 @@ Four translation units are compiled in parallel and linked into
   correctly rounded: the mixed form's tolerance is set by FP32 storage, and the
   correctly rounded quotient costs a multi-instruction sequence per division);
 * ``capi.cu``      -- the C ABI (host code);
-* ``noalloc.cu``   -- the allocation-free global sum (static device scratch).
+* ``noalloc.cu``   -- the allocation-free global sum (static device scratch);
+* ``adj_fp64.cu``  -- the adjoint kernels of the tracer routines and tra_nxt
+  (``--fmad=false``).
 """
 import concurrent.futures as cf
 import os
@@ -29,6 +31,7 @@ UNITS = {
     "inst_fp32.cu": ["--prec-div=false"],
     "capi.cu": [],
     "noalloc.cu": ["--fmad=false"],
+    "adj_fp64.cu": ["--fmad=false"],
 }
 
 

@@ -104,3 +104,45 @@ class Case:
         ta = np.zeros(self.s4, order="F")
         tb = self.tsb()
         self.o.tra_ldf_iso(self.kit, self.kit, "TRA", None, None, self.gtsu, self.gtsv, None, None, tb, tb, ta, 2, 1)
+
+
+class GpuCase:
+    """A GPU context (FP64) over the fields of a Case, for nmem copies of it."""
+
+    def __init__(self, case, nmem=1):
+        from nemo_gpu import api
+        self.c = case
+        self.nmem = nmem
+        self.ctx = api.Context(case.dom, case.nam, nmembers=nmem, prec="fp64")
+        self.torch = self.ctx.torch
+        self.keep = {}
+        for n in ("USLP", "VSLP", "WSLPI", "WSLPJ", "AVT"):
+            self.bind(n, case.keep[n])
+        for n in ("AH_WSLP2", "AKZ"):
+            self.bind(n, np.zeros(case.s3, order="F"))
+        if not case.nam["ln_linssh"]:
+            for n in ("E3T_B", "E3T_N", "E3T_A", "E3U_N", "E3V_N", "E3W_N"):
+                self.bind(n, case.keep[n])
+        self.zun, self.zvn, self.zwn = (self.dev(a) for a in (case.zun, case.zvn, case.zwn))
+        self.gtsu, self.gtsv = self.dev(case.gtsu), self.dev(case.gtsv)
+
+    def dev(self, a, members=None):
+        """Device tensor of nmem copies of a (or of the given list of members)."""
+        return self.ctx.to_device(members if members is not None else [a] * self.nmem)
+
+    def host(self, t, shape):
+        self.ctx.synchronize()   # the context's kernels run on its own stream
+        out = self.ctx.to_host(t, shape)
+        return out if isinstance(out, list) else [out]
+
+    def bind(self, name, a):
+        t = self.dev(a)
+        self.keep[name] = t
+        self.ctx.bind(name, t)
+        return t
+
+    def iso_coefficients(self):
+        tb = self.dev(self.c.tsb())
+        ta = self.dev(np.zeros(self.c.s4, order="F"))
+        k = self.c.kit
+        self.ctx.tra_ldf_iso(k, k, "TRA", None, None, self.gtsu, self.gtsv, None, None, tb, tb, ta, 2, 1)
