@@ -64,6 +64,7 @@ class Context:
         if st != 0:
             raise NemoError(f"nemo_gpu_create failed with status {st}")
         self.h = h
+        self.stream = stream
         self.bound = {}
 
     # ------------------------------------------------------------------ life cycle
