@@ -462,6 +462,71 @@ def run_reference(args):
     print(json.dumps(res))
 
 
+def run_window(args):
+    """C4: gradient of the SST cost of a 48-step FP64 tracer window on GYRE
+    nn_GYRE=10 (forward sweep + checkpointed reverse sweep, checkpoints every 8)."""
+    import numpy as np
+    import torch
+    from nemo_gpu import adjoint, api, gyre
+    nn, nwin, every = args.nn if args.nn != 25 else 10, 48, 8
+    dom = gyre.domain(nn)
+    nam = gyre.namelist(neuler=0)
+    st = gyre.state(dom, nam, seed=100)
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        ctx = api.Context(dom, nam, nmembers=1, prec="fp64", stream=stream)
+        put = lambda n, a: (ctx.bind(n, ctx.to_device(a)), ctx.bound[n])[1]
+        for n in ("avt", "uslp", "vslp", "wslpi", "wslpj"):
+            put(n.upper(), st[n])
+        z3 = np.zeros_like(st["avt"])
+        put("AH_WSLP2", z3)
+        put("AKZ", z3)
+        for n in ("TSB", "TSN", "TSA"):
+            put(n, np.zeros_like(st["tsb"]))
+        un, vn, wn = (ctx.to_device(st[k]) for k in ("un", "vn", "wn"))
+        zun, zvn, zwn = (torch.empty_like(un) for _ in range(3))
+        ctx.tra_adv_trp(un, vn, wn, zun, zvn, zwn)
+        win = adjoint.TracerWindow(ctx, zun, zvn, zwn, nwin, every=every)
+        t0 = ctx.to_device(st["tsn"])
+        jpi, jpj, jpk = dom["jpi"], dom["jpj"], dom["jpk"]
+        tm = torch.from_numpy(np.ascontiguousarray((st["tsn"][:, :, 0, 0] != 0).T.astype(np.float64))).cuda()
+        target = ctx.to_device(st["tsn"]).view(2, jpk, jpj, jpi)[0, 0][None] + 0.1
+
+        def gradient():
+            _, tsn = win.forward(t0, t0)
+            _, g = adjoint.sst_cost(tsn, target, tm, (jpi, jpj, jpk))
+            return win.adjoint(torch.zeros_like(g), g)
+
+        for _ in range(args.warmup):
+            gradient()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        torch.cuda.synchronize()
+        e[0].record(stream)
+        for _ in range(args.steps):
+            win.forward(t0, t0)
+        e[1].record(stream)
+        torch.cuda.synchronize()
+        e[2].record(stream)
+        for _ in range(args.steps):
+            ab, an = gradient()
+        e[3].record(stream)
+        torch.cuda.synchronize()
+    fwd_ms, grad_ms = e[0].elapsed_time(e[1]) / args.steps, e[2].elapsed_time(e[3]) / args.steps
+    cells = jpi * jpj * jpk
+    # launches per gradient: forward and recomputed steps (FCT a, b, c; iso flux, div,
+    # edges; zdf; nxt = 8 each), adjoint steps (nxt, zdf, iso x3, fct = 6)
+    launches = args.steps * (nwin * 8 * 2 + nwin * 6)
+    res = {"metric": "cell-steps/s of the adjoint window gradient (forward + checkpointed reverse sweep)",
+           "value": cells * nwin / (grad_ms * 1e-3), "unit": "cell-steps/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": grad_ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic: seeded GYRE analytic state",
+           "config": {"workload": f"GYRE nn_GYRE={nn} FP64 tracer window, {nwin} steps, checkpoints every {every}, "
+                                  "J = sum (SST - target)^2", "cells": cells, "window_steps": nwin,
+                      "l2": "inputs (2 x 31 MB per state) below L2; no flush"},
+           "forward_sweep_ms": fwd_ms, "gradient_over_forward": grad_ms / fwd_ms, "gpu_launches": launches}
+    print(json.dumps(res))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -470,8 +535,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--prec", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--nn", type=int, default=25)
-    ap.add_argument("--workload", default="gyre", choices=["gyre", "shelf"],
-                    help="gyre: GYRE nn_GYRE=--nn (the headline); shelf: the 1000x1200x56 z* shelf")
+    ap.add_argument("--workload", default="gyre", choices=["gyre", "shelf", "window"],
+                    help="gyre: GYRE nn_GYRE=--nn (the headline); shelf: the 1000x1200x56 z* shelf; "
+                         "window: the gradient of a 48-step FP64 tracer window (nn_GYRE=10)")
     ap.add_argument("--members", type=int, default=1)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -482,6 +548,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "window":
+        run_window(args)
     else:
         run_gpu(args)
 
