@@ -203,6 +203,42 @@ def make_ctx(dom, nam, states, prec, stream):
     return ctx, dev
 
 
+def ten_days(dom, nam, states, stream, nsteps=120):
+    """The mixed form against FP64 after ten model days (120 steps of rdt = 7200 s) of
+    nemo_gpu_stp_model from an Euler start on the same state: RMS over wet points
+    and max of |mixed - FP64| for T, S, SST, SSS, SSH, U, V."""
+    import numpy as np
+    nam = dict(nam, neuler=0)
+    jpi, jpj, jpk = dom["jpi"], dom["jpj"], dom["jpk"]
+    out = {}
+    for prec in ("fp64", "mixed"):
+        ctx, dev = make_ctx(dom, nam, states, prec, stream)
+        for kt in range(1, nsteps + 1):
+            ctx.stp_model(kt)
+        ctx.synchronize()
+        get = lambda n, sh: np.asarray(ctx.to_host(dev[n], sh))
+        out[prec] = {"T": get("TSN", (jpi, jpj, jpk, 2))[..., 0], "S": get("TSN", (jpi, jpj, jpk, 2))[..., 1],
+                     "U": get("UN", (jpi, jpj, jpk)), "V": get("VN", (jpi, jpj, jpk)), "SSH": get("SSHN", (jpi, jpj))}
+        ctx.close()
+        del dev
+    tm = np.arange(1, jpk + 1)[None, None, :] <= dom["k_bot"][:, :, None]
+    res = {"steps": nsteps, "model_days": nsteps * nam["rn_rdt"] / 86400.0,
+           "step": "nemo_gpu_stp_model: the hot path + wzv, dyn_zdf time step, tra_nxt, dyn_nxt, ssh_swp; "
+                   "momentum trends outside the path held at 0"}
+    for n, sel in (("T", None), ("S", None), ("SST", "T"), ("SSS", "S"), ("U", None), ("V", None), ("SSH", None)):
+        a, b = out["mixed"][sel or n], out["fp64"][sel or n]
+        if n in ("SST", "SSS"):
+            a, b, m = a[:, :, 0], b[:, :, 0], tm[:, :, 0]
+        elif n == "SSH":
+            m = tm[:, :, 0]
+        else:
+            m = tm
+        d = (a - b)[m]
+        res[n] = {"rms": float(np.sqrt(np.mean(d * d))), "max": float(np.abs(d).max()),
+                  "range": float(np.abs(b[m]).max())}
+    return res
+
+
 def time_steps(ctx, stream, steps, kt0, dev_index):
     import torch
     from nemo_gpu import dist
@@ -297,6 +333,8 @@ def run_gpu(args):
                 "sst_abs_err_1step_K": sst_err, "sss_abs_err_1step_psu": sss_err}
         ctx64.close()
         del dev64
+        if not args.no_ten_days and args.workload == "gyre" and rank == 0:
+            fp64["ten_days"] = ten_days(dom, nam, states[:1], stream)
     # ---------------------------------------------------------------- e2e (host buffers, C ABI)
     e2e = None
     if not args.no_e2e:
@@ -541,6 +579,7 @@ def main():
     ap.add_argument("--members", type=int, default=1)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-ten-days", action="store_true", help="skip the ten-day mixed-vs-FP64 divergence")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     args = ap.parse_args()

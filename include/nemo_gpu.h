@@ -264,6 +264,33 @@ int nemo_gpu_tra_zdf(nemo_ctx *ctx, int kt);
  * of tsb and tsn. Linear free surface only (tra_nxt_vvl is not on the path). */
 int nemo_gpu_tra_nxt(nemo_ctx *ctx, int kt);
 
+/* ------------------------------------------------- the rest of a model step
+ * The routines that close the path into a time step with the linear free surface
+ * (step.F90:160-282), for a model run on the device. None is on the path itself. */
+
+/* div_hor (divhor.F90:62-110) and wzv (sshwzv.F90:129-213) on the bound un, vn:
+ * the horizontal divergence (0 on the closed edges), then wn integrated up from
+ * wn(jpk) = 0, with the e3t_a - e3t_b term of z*. */
+int nemo_gpu_wzv(nemo_ctx *ctx, int kt);
+/* The time step of dyn_zdf (dynzdf.F90:112) without vertical viscosity or drag:
+ * ua = (ub + r2dt ua) umask, va likewise. The implicit viscosity solve of
+ * dynzdf.F90:160-330 is not implemented. */
+int nemo_gpu_dyn_zdf_step(nemo_ctx *ctx, int kt);
+/* dyn_nxt (dynnxt.F90:66-377) for ln_linssh with ln_dynspg_ts and ln_bt_fw: the
+ * barotropic part of ua replaced by ua_b, lbc_lnk, the Euler swap or the Asselin
+ * filter and swap with ub returned to the time-split estimate, then un_b, ub_b.
+ * NEMO_ERR_UNSUPPORTED for other settings. */
+int nemo_gpu_dyn_nxt(nemo_ctx *ctx, int kt);
+/* ssh_swp (sshwzv.F90:216-267), linear free surface. */
+int nemo_gpu_ssh_swp(nemo_ctx *ctx, int kt);
+/* One model step on the bound fields, in step.F90's order: ua = va = 0, dyn_spg_ts,
+ * div_hor + wzv, the dyn_zdf time step, tsa = 0, tra_adv, tra_ldf, tra_zdf (with
+ * the salinity clamp), tra_nxt, dyn_nxt, ssh_swp -- the hot path closed by the
+ * routines above, with the momentum trends of dyn_adv, dyn_vor, dyn_ldf, dyn_hpg and
+ * the vertical viscosity held at 0 (they are not on the path). Captured into a CUDA
+ * graph like nemo_gpu_stp_hotpath. Linear free surface with ln_bt_fw. */
+int nemo_gpu_stp_model(nemo_ctx *ctx, int kt);
+
 /* ------------------------------------------------------------ adjoint
  * Adjoints of the tracer routines with respect to their tracer arguments, in an
  * FP64 context (NEMO_ERR_ARG otherwise). NEMO has no adjoint of these routines in
@@ -371,6 +398,7 @@ enum nemo_kernel_id {
   NEMO_K_FCT_A_TMA, NEMO_K_FCT_B_TMA, /* FCT stages a, b with TMA-staged planes */
   NEMO_K_FCT_ADJ, NEMO_K_LAP_ADJ, NEMO_K_ISO_ADJ, NEMO_K_ZDF_ADJ, /* adjoints */
   NEMO_K_TRA_NXT, NEMO_K_TRA_NXT_ADJ,
+  NEMO_K_WZV, NEMO_K_DYN_ZDF_STEP, NEMO_K_DYN_NXT, NEMO_K_SSH_SWP, /* rest of the model step */
   NEMO_K_COUNT
 };
 

@@ -16,6 +16,7 @@
 
 #include "../../include/nemo_gpu.h"
 #include "adj.h"
+#include "step.h"
 #include "launch.h"
 
 using namespace nemo;
@@ -837,8 +838,75 @@ int run_spg(nemo_ctx* c, int kt) {
   return NEMO_OK;
 }
 
+// ------------------------------------------------- the rest of a model step
+int model_fields(nemo_ctx* c, const char* what) {
+  const nemo_namelist& nm = c->nam;
+  for (int id : {NEMO_F_UN, NEMO_F_VN, NEMO_F_WN, NEMO_F_UA, NEMO_F_VA, NEMO_F_UB, NEMO_F_VB, NEMO_F_UN_B,
+                 NEMO_F_VN_B, NEMO_F_UB_B, NEMO_F_VB_B, NEMO_F_UA_B, NEMO_F_VA_B, NEMO_F_SSHB, NEMO_F_SSHN,
+                 NEMO_F_SSHA, NEMO_F_TSB, NEMO_F_TSN, NEMO_F_TSA})
+    if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "%s: field %d must be bound", what, id);
+  if (!nm.ln_linssh || !nm.ln_bt_fw)
+    return fail(c, NEMO_ERR_UNSUPPORTED, "%s: the linear free surface with ln_bt_fw only", what);
+  return NEMO_OK;
+}
+
 template <class T>
-int run_hotpath(nemo_ctx* c, int kt, bool staged) {
+int run_wzv(nemo_ctx* c, int kt) {
+  const nemo_namelist& nm = c->nam;
+  const double z1_2dt = (nm.neuler == 0 && kt == nm.nit000) ? 1.0 / nm.rn_rdt : 1.0 / (2.0 * nm.rn_rdt);
+  cudaError_t e = launch_wzv<T>(dom_now<T>(c), (const T*)c->f[NEMO_F_UN], (const T*)c->f[NEMO_F_VN],
+                                (T*)c->f[NEMO_F_WN], (T)z1_2dt, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "wzv launch");
+  return NEMO_OK;
+}
+
+template <class T>
+int run_dyn_zdf_step(nemo_ctx* c, int kt) {
+  const nemo_namelist& nm = c->nam;
+  const double r2dt = (nm.neuler == 0 && kt == nm.nit000) ? nm.rn_rdt : 2.0 * nm.rn_rdt;
+  cudaError_t e = launch_dyn_zdf_step<T>(dom_now<T>(c), (const T*)c->f[NEMO_F_UB], (const T*)c->f[NEMO_F_VB],
+                                         (T*)c->f[NEMO_F_UA], (T*)c->f[NEMO_F_VA], (T)r2dt, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "dyn_zdf step launch");
+  return NEMO_OK;
+}
+
+template <class T>
+int run_tra_nxt(nemo_ctx* c, int kt) {
+  const nemo_namelist& nm = c->nam;
+  cudaError_t e = launch_tra_nxt<T>(dom<T>(c), (T*)c->f[NEMO_F_TSB], (T*)c->f[NEMO_F_TSN], (T*)c->f[NEMO_F_TSA],
+                                    (T)nm.rn_atfp, nm.neuler == 0 && kt == nm.nit000, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "tra_nxt launch");
+  return NEMO_OK;
+}
+
+template <class T>
+int run_dyn_nxt(nemo_ctx* c, int kt) {
+  const nemo_namelist& nm = c->nam;
+  void* const* F = c->f;
+  NxtArgs<T, double> a{};
+  a.ua = (T*)F[NEMO_F_UA]; a.va = (T*)F[NEMO_F_VA]; a.un = (T*)F[NEMO_F_UN]; a.vn = (T*)F[NEMO_F_VN];
+  a.ub = (T*)F[NEMO_F_UB]; a.vb = (T*)F[NEMO_F_VB];
+  a.un_b = (T*)F[NEMO_F_UN_B]; a.vn_b = (T*)F[NEMO_F_VN_B]; a.ub_b = (T*)F[NEMO_F_UB_B]; a.vb_b = (T*)F[NEMO_F_VB_B];
+  a.ua_b = (const double*)F[NEMO_F_UA_B]; a.va_b = (const double*)F[NEMO_F_VA_B];
+  a.atfp = (T)nm.rn_atfp;
+  a.euler = nm.neuler == 0 && kt == nm.nit000;
+  cudaError_t e = launch_dyn_nxt<T>(dom<T>(c), a, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "dyn_nxt launch");
+  return NEMO_OK;
+}
+
+template <class T>
+int run_ssh_swp(nemo_ctx* c, int kt) {
+  const nemo_namelist& nm = c->nam;
+  cudaError_t e = launch_ssh_swp<T>(dom<T>(c), (T*)c->f[NEMO_F_SSHB], (T*)c->f[NEMO_F_SSHN],
+                                    (const double*)c->f[NEMO_F_SSHA], (T)nm.rn_atfp,
+                                    nm.neuler == 0 && kt == nm.nit000, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "ssh_swp launch");
+  return NEMO_OK;
+}
+
+template <class T>
+int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
   const nemo_namelist& nm = c->nam;
   void* const* F = c->f;
   if (!F[NEMO_F_TSB] || !F[NEMO_F_TSN] || !F[NEMO_F_TSA] || !F[NEMO_F_WN])
@@ -854,6 +922,11 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged) {
     cudaEventRecord(c->kc.ev[0], c->stream);
   }
   mark(0);
+  if (model) {  // ua = va = 0 (step.F90:183-184): no momentum trend outside the path
+    const size_t bytes = (size_t)c->n3 * c->nmem * sizeof(T);
+    CK(cudaMemsetAsync(F[NEMO_F_UA], 0, bytes, c->stream), "ua = 0");
+    CK(cudaMemsetAsync(F[NEMO_F_VA], 0, bytes, c->stream), "va = 0");
+  }
   // Staged (host copies pending): each part waits only for the copies of the fields it
   // reads or writes -- dyn_spg_ts starts while the tracers and slopes still upload,
   // and the downloads of what it writes start when it ends (ev_spg_done).
@@ -887,6 +960,10 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged) {
       if (spg_reads(id) && wait_field(c, c->stream, id, spg_writes(id))) return NEMO_ERR_CUDA;
   int s = run_spg<T>(c, kt);
   if (s) return s;
+  if (model) {  // div_hor + wzv after dyn_spg_ts (step.F90:206-211), the dyn_zdf time step
+    if ((s = run_wzv<T>(c, kt))) return s;
+    if ((s = run_dyn_zdf_step<T>(c, kt))) return s;
+  }
   if (staged) {
     CK(cudaEventRecord(c->ev_spg_done, c->stream), "end of dyn_spg_ts");
     if (join_copies(c)) return NEMO_ERR_CUDA;  // the tracer part: every remaining copy
@@ -927,6 +1004,11 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged) {
   }
   s = run_zdf<T>(c, r2dt, F[NEMO_F_TSB], F[NEMO_F_TSA], 2, 0, 1);
   if (s) return s;
+  if (model) {  // tra_nxt, dyn_nxt, ssh_swp (step.F90:280-282)
+    if ((s = run_tra_nxt<T>(c, kt))) return s;
+    if ((s = run_dyn_nxt<T>(c, kt))) return s;
+    if ((s = run_ssh_swp<T>(c, kt))) return s;
+  }
   if (staged) CK(cudaEventRecord(c->ev_step_done, c->stream), "end of the step");
   if (c->timing) {
     mark(4);
@@ -1287,15 +1369,39 @@ int nemo_gpu_tra_nxt(nemo_ctx* c, int kt) {
   if (!F[NEMO_F_TSB] || !F[NEMO_F_TSN] || !F[NEMO_F_TSA])
     return fail(c, NEMO_ERR_UNBOUND, "tra_nxt: tsb, tsn and tsa must be bound");
   if (!nm.ln_linssh) return fail(c, NEMO_ERR_ARG, "tra_nxt: linear free surface only (ln_linssh)");
-  const int euler = nm.neuler == 0 && kt == nm.nit000;
-  cudaError_t e =
-      c->prec == NEMO_PREC_FP64
-          ? launch_tra_nxt<double>(dom<double>(c), (double*)F[NEMO_F_TSB], (double*)F[NEMO_F_TSN],
-                                   (double*)F[NEMO_F_TSA], nm.rn_atfp, euler, c->stream)
-          : launch_tra_nxt<float>(dom<float>(c), (float*)F[NEMO_F_TSB], (float*)F[NEMO_F_TSN], (float*)F[NEMO_F_TSA],
-                                  (float)nm.rn_atfp, euler, c->stream);
-  if (e != cudaSuccess) return cuda_fail(c, e, "tra_nxt launch");
-  return NEMO_OK;
+  return c->prec == NEMO_PREC_FP64 ? run_tra_nxt<double>(c, kt) : run_tra_nxt<float>(c, kt);
+}
+
+int nemo_gpu_wzv(nemo_ctx* c, int kt) {
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (!c->f[NEMO_F_UN] || !c->f[NEMO_F_VN] || !c->f[NEMO_F_WN])
+    return fail(c, NEMO_ERR_UNBOUND, "wzv: un, vn and wn must be bound");
+  return c->prec == NEMO_PREC_FP64 ? run_wzv<double>(c, kt) : run_wzv<float>(c, kt);
+}
+
+int nemo_gpu_dyn_zdf_step(nemo_ctx* c, int kt) {
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  for (int id : {NEMO_F_UA, NEMO_F_VA, NEMO_F_UB, NEMO_F_VB})
+    if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "dyn_zdf_step: ua, va, ub and vb must be bound");
+  return c->prec == NEMO_PREC_FP64 ? run_dyn_zdf_step<double>(c, kt) : run_dyn_zdf_step<float>(c, kt);
+}
+
+int nemo_gpu_dyn_nxt(nemo_ctx* c, int kt) {
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (int s = model_fields(c, "dyn_nxt")) return s;
+  return c->prec == NEMO_PREC_FP64 ? run_dyn_nxt<double>(c, kt) : run_dyn_nxt<float>(c, kt);
+}
+
+int nemo_gpu_ssh_swp(nemo_ctx* c, int kt) {
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (!c->f[NEMO_F_SSHB] || !c->f[NEMO_F_SSHN] || !c->f[NEMO_F_SSHA])
+    return fail(c, NEMO_ERR_UNBOUND, "ssh_swp: sshb, sshn and ssha must be bound");
+  if (!c->nam.ln_linssh) return fail(c, NEMO_ERR_UNSUPPORTED, "ssh_swp: linear free surface only");
+  return c->prec == NEMO_PREC_FP64 ? run_ssh_swp<double>(c, kt) : run_ssh_swp<float>(c, kt);
 }
 
 // ---------------------------------------------------------------------- adjoint
@@ -1469,31 +1575,35 @@ int nemo_gpu_glob_sum(nemo_ctx* c, const char* cdname, const void* ptab, int nk,
   return NEMO_OK;
 }
 
-int nemo_gpu_stp_hotpath(nemo_ctx* c, int kt) {
+static int stp_common(nemo_ctx* c, int kt, bool model) {
   if (!c) return NEMO_ERR_ARG;
+  if (model)
+    if (int s = model_fields(c, "stp_model")) return s;
   // host copies in flight: direct launches that wait per field (see run_hotpath);
   // otherwise the captured graph of the steady-state step
-  if (copies_pending(c) && !c->timing)
+  if (!model && copies_pending(c) && !c->timing)
     return c->prec == NEMO_PREC_FP64 ? run_hotpath<double>(c, kt, true) : run_hotpath<float>(c, kt, true);
   if (join_copies(c)) return NEMO_ERR_CUDA;
   const nemo_namelist& nm = c->nam;
   // class of kt: the Euler/leapfrog start steps differ in scalars and weights
   const int cls = kt == nm.nit000 ? 0 : (kt == nm.nit000 + 1 ? 1 : 2);
   const bool carry = !nm.ln_bt_av;  // ring rotation carries across calls: no replay
+  const int key = cls + (model ? 10 : 0);
   if (cls == 2 && c->graphs_ok && !carry && !c->timing) {
-    auto it = c->graphs.find(cls);
+    auto it = c->graphs.find(key);
     if (it != c->graphs.end()) {
       CK(cudaGraphLaunch(it->second, c->stream), "graph launch");
       return NEMO_OK;
     }
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-      int s = c->prec == NEMO_PREC_FP64 ? run_hotpath<double>(c, kt, false) : run_hotpath<float>(c, kt, false);
+      int s = c->prec == NEMO_PREC_FP64 ? run_hotpath<double>(c, kt, false, model)
+                                        : run_hotpath<float>(c, kt, false, model);
       cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
       cudaGraphExec_t ex = nullptr;
       if (s == NEMO_OK && ee == cudaSuccess && g && cudaGraphInstantiate(&ex, g, 0) == cudaSuccess) {
         cudaGraphDestroy(g);
-        c->graphs[cls] = ex;
+        c->graphs[key] = ex;
         CK(cudaGraphLaunch(ex, c->stream), "graph launch");
         return NEMO_OK;
       }
@@ -1504,8 +1614,13 @@ int nemo_gpu_stp_hotpath(nemo_ctx* c, int kt) {
     c->graphs_ok = false;  // capture unavailable: direct launches from now on
     cudaGetLastError();
   }
-  return c->prec == NEMO_PREC_FP64 ? run_hotpath<double>(c, kt, false) : run_hotpath<float>(c, kt, false);
+  return c->prec == NEMO_PREC_FP64 ? run_hotpath<double>(c, kt, false, model)
+                                   : run_hotpath<float>(c, kt, false, model);
 }
+
+int nemo_gpu_stp_hotpath(nemo_ctx* c, int kt) { return stp_common(c, kt, false); }
+
+int nemo_gpu_stp_model(nemo_ctx* c, int kt) { return stp_common(c, kt, true); }
 
 int nemo_gpu_set_timing(nemo_ctx* c, int on) {
   if (!c) return NEMO_ERR_ARG;

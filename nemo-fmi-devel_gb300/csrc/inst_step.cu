@@ -1,0 +1,49 @@
+// inst_step.cu -- launchers of the rest-of-step kernels, both precisions; compiled
+// with --fmad=false so the FP64 form rounds as the reference's FP64 CPU build.
+#include "k_step.cuh"
+#include "launch.h"
+
+namespace nemo {
+
+namespace {
+constexpr int SX = 32, SY = 4;
+template <class T>
+dim3 s_col(const Dom<T>& d) { return dim3((d.jpi + SX - 1) / SX, (d.jpj + SY - 1) / SY, d.nmem); }
+template <class T>
+dim3 s_pt(const Dom<T>& d) { return dim3((d.jpi + SX - 1) / SX, (d.jpj + SY - 1) / SY, d.nmem * d.jpk); }
+}  // namespace
+
+template <class T>
+cudaError_t launch_wzv(const Dom<T>& d, const T* un, const T* vn, T* wn, T z1_2dt, cudaStream_t s) {
+  k_wzv<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, un, vn, wn, z1_2dt);
+  ktick(NEMO_K_WZV, s);
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_dyn_zdf_step(const Dom<T>& d, const T* ub, const T* vb, T* ua, T* va, T r2dt, cudaStream_t s) {
+  k_dyn_zdf_step<T><<<s_pt(d), dim3(SX, SY), 0, s>>>(d, ub, vb, ua, va, r2dt);
+  ktick(NEMO_K_DYN_ZDF_STEP, s);
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_dyn_nxt(const Dom<T>& d, const NxtArgs<T, double>& a, cudaStream_t s) {
+  k_dyn_nxt<T, double><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a);
+  ktick(NEMO_K_DYN_NXT, s);
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_ssh_swp(const Dom<T>& d, T* sshb, T* sshn, const double* ssha, T atfp, int euler, cudaStream_t s) {
+  k_ssh_swp<T, double><<<s_col(d), dim3(SX, SY), 0, s>>>(d, sshb, sshn, ssha, atfp, euler);
+  ktick(NEMO_K_SSH_SWP, s);
+  return cudaGetLastError();
+}
+
+#define NEMO_STEP_INST(T)                                                                                      \
+  template cudaError_t launch_wzv<T>(const Dom<T>&, const T*, const T*, T*, T, cudaStream_t);                  \
+  template cudaError_t launch_dyn_zdf_step<T>(const Dom<T>&, const T*, const T*, T*, T*, T, cudaStream_t);     \
+  template cudaError_t launch_dyn_nxt<T>(const Dom<T>&, const NxtArgs<T, double>&, cudaStream_t);              \
+  template cudaError_t launch_ssh_swp<T>(const Dom<T>&, T*, T*, const double*, T, int, cudaStream_t);
+NEMO_STEP_INST(double)
+NEMO_STEP_INST(float)
+
+}  // namespace nemo

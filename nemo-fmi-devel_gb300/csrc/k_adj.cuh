@@ -420,7 +420,9 @@ __global__ void k_tra_nxt(Dom<T> d, T* tsb, T* tsn, T* tsa, T atfp, int euler) {
       tsn[o] = T(0);
     } else if (c.k <= d.jpk - 1) {
       const T ztn = tsn[o];
-      const T ztd = tsa[o] - T(2) * ztn + tsb[o];
+      // FP32: the time laplacian from the two differences, which round to small
+      // values, instead of from the O(1) values (the same sum in exact arithmetic)
+      const T ztd = sizeof(T) == 4 ? (tsa[o] - ztn) - (ztn - tsb[o]) : tsa[o] - T(2) * ztn + tsb[o];
       tsb[o] = ztn + atfp * ztd;
       tsn[o] = tsa[o];
     }

@@ -873,6 +873,7 @@ __global__ void k_zdf_imp(Dom<T> d, ZdfArgs<T> a) {
   const long m3 = (long)c.m * n3;
   // rat(k) = zwi(k) / zwt(k-1): the tracer-independent factor of the 2nd recurrence
   T rat[KMAX], zws[KMAX], zwt[KMAX];
+  T zwi_k[sizeof(T) == 4 ? KMAX : 1];  // FP32: the sub-diagonal, for the increment form
   for (int n = 0; n < a.kjpt; ++n) {
     const bool build = (!a.is_trc && (n == 0 || (n == 1 && a.ddm))) || (a.is_trc && n == 0);
     if (build) {
@@ -893,6 +894,7 @@ __global__ void k_zdf_imp(Dom<T> d, ZdfArgs<T> a) {
         zws[k] = -a.p2dt * wtk1 / d.e3w_n(c.ij, k + 1, c.m);
         const T e3a = d.e3t_a(c.ij, k, c.m);
         if (k >= 2) rat[k] = zwi / zwt[k - 1];
+        if constexpr (sizeof(T) == 4) zwi_k[k] = zwi;
         if constexpr (sizeof(T) == 8) {
           // 1st recurrence as written in the reference (trazdf.F90:223-234)
           const T zwd = e3a - zwi - zws[k];
@@ -913,6 +915,31 @@ __global__ void k_zdf_imp(Dom<T> d, ZdfArgs<T> a) {
     const RO<T> tb = a.ptb + mo;
     T* ta = a.pta + mo;
     const bool clamp = a.clamp_sal && !a.is_trc && n == 1;
+    if constexpr (sizeof(T) == 4) {
+      // FP32: the increment form of k_zdf_imp_async (d = x - tb, one rounding of the
+      // O(1) values in x = tb + d)
+      const int K1 = jpk - 1;
+      T prev = T(0);
+      for (int k = 1; k <= K1; ++k) {
+        const long q = c.ij + (long)(k - 1) * n2;
+        const T tbk = tb[q];
+        T r = a.p2dt * d.e3t_n(c.ij, k, c.m) * ta[q] + (d.e3t_b(c.ij, k, c.m) - d.e3t_a(c.ij, k, c.m)) * tbk;
+        if (k > 1) r = r - zwi_k[k] * (tb[q - n2] - tbk);
+        if (k < K1) r = r - zws[k] * (tb[q + n2] - tbk);
+        else r = r + zws[k] * tbk;
+        prev = (k == 1) ? r : r - rat[k] * prev;
+        ta[q] = prev;
+      }
+      T dnx = T(0);
+      for (int k = K1; k >= 1; --k) {
+        const long q = c.ij + (long)(k - 1) * n2;
+        const T tbk = tb[q];
+        const T dk = (k == K1 ? ta[q] : ta[q] - zws[k] * dnx) / zwt[k];
+        const T x = (tbk + dk) * tmsk<T>(ci, k);
+        dnx = x - tbk;
+        ta[q] = (clamp && x < T(0)) ? T(0.1) : x;
+      }
+    } else {
     // 2nd recurrence (:238-250), the forward values kept in pta as in the reference
     T prev = T(0);
     for (int k = 1; k <= jpk - 1; ++k) {
@@ -933,6 +960,7 @@ __global__ void k_zdf_imp(Dom<T> d, ZdfArgs<T> a) {
       const long q = c.ij + (long)(k - 1) * n2;
       nxt = (ta[q] - zws[k] * nxt) / zwt[k] * tmsk<T>(ci, k);
       ta[q] = (clamp && nxt < T(0)) ? T(0.1) : nxt;
+    }
     }
   }
 }
@@ -1009,19 +1037,31 @@ __global__ void __launch_bounds__(128, 3) k_zdf_imp_async(Dom<float> d, ZdfArgs<
       cp_async4(sb + (k - 1) * nt, tb + (long)(k - 1) * n2);
     }
     cp_async_wait_all();
-    float prev = 0.0f;
+    // Increment form: the system is solved for d = x - tb, M d = rhs - M tb, whose
+    // right-hand side holds only the trend and differences of tb, so the O(1)
+    // tracer values are rounded once, in x = tb + d (the reference's form rounds
+    // the full values in both recurrences: ~10 ulps of salinity per step).
+    float prev = 0.0f, tbm = 0.0f;
 #pragma unroll 4
     for (int k = 1; k <= K1; ++k) {
-      const float zrhs = d.e3t_b(c.ij, k, c.m) * sb[(k - 1) * nt] + p2dt * d.e3t_n(c.ij, k, c.m) * sx[(k - 1) * nt];
-      prev = (k == 1) ? zrhs : zrhs - zw[(k - 1) * nt] * rz[(k - 2) * nt] * prev;
+      const float tbk = sb[(k - 1) * nt];
+      float r = p2dt * d.e3t_n(c.ij, k, c.m) * sx[(k - 1) * nt] +
+                (d.e3t_b(c.ij, k, c.m) - d.e3t_a(c.ij, k, c.m)) * tbk;
+      if (k > 1) r = r - zw[(k - 1) * nt] * (tbm - tbk);    // zwi(k) (tb(k-1) - tb(k))
+      if (k < K1) r = r - zw[k * nt] * (sb[k * nt] - tbk);  // zws(k) (tb(k+1) - tb(k))
+      else r = r + zw[k * nt] * tbk;                        // last row: no x(k+1)
+      prev = (k == 1) ? r : r - zw[(k - 1) * nt] * rz[(k - 2) * nt] * prev;
       sx[(k - 1) * nt] = prev;
+      tbm = tbk;
     }
-    float nxt = 0.0f;
+    float dnx = 0.0f;  // x(k+1) - tb(k+1) of the stored (masked) x(k+1)
 #pragma unroll 4
     for (int k = K1; k >= 1; --k) {
-      const float xk = sx[(k - 1) * nt];
-      nxt = (k == K1 ? xk : xk - zw[k * nt] * nxt) * rz[(k - 1) * nt] * tmsk<float>(ci, k);
-      ta[(long)(k - 1) * n2] = (clamp && nxt < 0.0f) ? 0.1f : nxt;
+      const float yk = sx[(k - 1) * nt], tbk = sb[(k - 1) * nt];
+      const float dk = (k == K1 ? yk : yk - zw[k * nt] * dnx) * rz[(k - 1) * nt];
+      const float x = (tbk + dk) * tmsk<float>(ci, k);
+      dnx = x - tbk;
+      ta[(long)(k - 1) * n2] = (clamp && x < 0.0f) ? 0.1f : x;
     }
   }
 }

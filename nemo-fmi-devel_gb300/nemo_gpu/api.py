@@ -182,6 +182,23 @@ class Context:
     def tra_nxt(self, kt):
         self._ck(self.lib.nemo_gpu_tra_nxt(self.h, kt), "tra_nxt")
 
+    def wzv(self, kt):
+        self._ck(self.lib.nemo_gpu_wzv(self.h, kt), "wzv")
+
+    def dyn_zdf_step(self, kt):
+        self._ck(self.lib.nemo_gpu_dyn_zdf_step(self.h, kt), "dyn_zdf_step")
+
+    def dyn_nxt(self, kt):
+        self._ck(self.lib.nemo_gpu_dyn_nxt(self.h, kt), "dyn_nxt")
+
+    def ssh_swp(self, kt):
+        self._ck(self.lib.nemo_gpu_ssh_swp(self.h, kt), "ssh_swp")
+
+    def stp_model(self, kt):
+        """One model step: the hot path closed by wzv, the dyn_zdf time step, tra_nxt,
+        dyn_nxt and ssh_swp (see nemo_gpu.h)."""
+        self._ck(self.lib.nemo_gpu_stp_model(self.h, kt), "stp_model")
+
     # ------------------------------------------------------------------ adjoints
     # The adjoint twins of the tracer routines (FP64 contexts): the tracer arrays of
     # the forward's argument list are replaced by their adjoints; see nemo_gpu.h.

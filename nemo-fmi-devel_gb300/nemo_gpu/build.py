@@ -1,6 +1,6 @@
 """Build recipe of the CUDA library (sm_103a only).
 
-Five translation units are compiled in parallel and linked into
+Six translation units are compiled in parallel and linked into
 ``nemo_gpu/_lib/libnemo_gpu.so``:
 
 * ``inst_fp64.cu`` -- FP64 kernels, ``--fmad=false`` so that every double operation
@@ -12,7 +12,9 @@ Five translation units are compiled in parallel and linked into
 * ``capi.cu``      -- the C ABI (host code);
 * ``noalloc.cu``   -- the allocation-free global sum (static device scratch);
 * ``adj_fp64.cu``  -- the adjoint kernels of the tracer routines and tra_nxt
-  (``--fmad=false``).
+  (``--fmad=false``);
+* ``inst_step.cu`` -- wzv, the dyn_zdf time step, dyn_nxt and ssh_swp, both
+  precisions (``--fmad=false``).
 """
 import concurrent.futures as cf
 import os
@@ -32,6 +34,7 @@ UNITS = {
     "capi.cu": [],
     "noalloc.cu": ["--fmad=false"],
     "adj_fp64.cu": ["--fmad=false"],
+    "inst_step.cu": ["--fmad=false"],
 }
 
 

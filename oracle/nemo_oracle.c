@@ -1583,13 +1583,12 @@ int ora_glob_sum(ora_ctx *c, const double *ptab, int nk, double *out) {
 /* ---------------------------------------------------------- one hot-path step */
 /* step.F90:194-257 on the bound fields: dyn_spg_ts, tsa = 0, tra_adv (transports
  * + FCT), tra_ldf (iso or lap), tra_zdf. FCT orders from nn_fct_h/v (0 = 2). */
-int ora_stp_hotpath(ora_ctx *c, int kt) {
+/* The tracer part of the step: tsa = 0, tra_adv (transports + FCT), tra_ldf, tra_zdf. */
+static int stp_tracers(ora_ctx *c, int kt) {
   const nemo_namelist *nm = &c->nam;
   const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk;
   double *tsb = c->f[NEMO_F_TSB], *tsn = c->f[NEMO_F_TSN], *tsa = c->f[NEMO_F_TSA];
-  if (!tsb || !tsn || !tsa || !c->f[NEMO_F_UN] || !c->f[NEMO_F_VN] || !c->f[NEMO_F_WN]) return NEMO_ERR_UNBOUND;
-  int st = ora_dyn_spg_ts(c, kt);
-  if (st) return st;
+  int st;
   memset(tsa, 0, 2 * n3 * sizeof(double));
   double r2dt = (nm->neuler == 0 && kt == nm->nit000) ? nm->rn_rdt : 2.0 * nm->rn_rdt;
   double *zun = zalloc(n3), *zvn = zalloc(n3), *zwn = zalloc(n3);
@@ -1607,6 +1606,14 @@ int ora_stp_hotpath(ora_ctx *c, int kt) {
                          c->f[NEMO_F_GTUI], c->f[NEMO_F_GTVI], tsb, tsa, 2, 1);
   if (st) return st;
   return ora_tra_zdf(c, kt);
+}
+
+int ora_stp_hotpath(ora_ctx *c, int kt) {
+  double *tsb = c->f[NEMO_F_TSB], *tsn = c->f[NEMO_F_TSN], *tsa = c->f[NEMO_F_TSA];
+  if (!tsb || !tsn || !tsa || !c->f[NEMO_F_UN] || !c->f[NEMO_F_VN] || !c->f[NEMO_F_WN]) return NEMO_ERR_UNBOUND;
+  int st = ora_dyn_spg_ts(c, kt);
+  if (st) return st;
+  return stp_tracers(c, kt);
 }
 
 /* =================================================================== adjoint */
@@ -2034,4 +2041,174 @@ int ora_tra_nxt_adj(ora_ctx *c, int kt, double *tsb_ad, double *tsn_ad, double *
   }
   lbc_closed(jpi, jpj, tsa_ad, 2 * jpk, 'T', 0.0);
   return NEMO_OK;
+}
+
+/* ======================================================= the rest of the step */
+/* The parts of stp (step.F90:96-305) that close the path into a time step with the
+ * linear free surface: the vertical velocity, the time step and the swaps of the
+ * momentum and the sea surface height. The momentum trends outside the path
+ * (dyn_adv, dyn_vor, dyn_ldf, dyn_hpg) and the vertical viscosity are held at 0. */
+
+/* div_hor (divhor.F90:62-110) and wzv (sshwzv.F90:129-213) on the bound un, vn, wn. */
+int ora_wzv(ora_ctx *c, int kt) {
+  const nemo_namelist *nm = &c->nam;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  const double *un = c->f[NEMO_F_UN], *vn = c->f[NEMO_F_VN];
+  double *wn = c->f[NEMO_F_WN];
+  if (!un || !vn || !wn) return NEMO_ERR_UNBOUND;
+  const double *e3u = fld(c, NEMO_F_E3U_N), *e3v = fld(c, NEMO_F_E3V_N), *e3t_n = fld(c, NEMO_F_E3T_N);
+  const double *e3t_a = fld(c, NEMO_F_E3T_A), *e3t_b = fld(c, NEMO_F_E3T_B);
+  double *hdivn = zalloc(n3);
+  for (int jk = 1; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t q = I3(ji, jj, jk);
+        hdivn[q] = (c->e2u[I2(ji, jj)] * e3u[q] * un[q] - c->e2u[I2(ji - 1, jj)] * e3u[I3(ji - 1, jj, jk)] * un[I3(ji - 1, jj, jk)]
+                    + c->e1v[I2(ji, jj)] * e3v[q] * vn[q] - c->e1v[I2(ji, jj - 1)] * e3v[I3(ji, jj - 1, jk)] * vn[I3(ji, jj - 1, jk)])
+                   * c->r1_e1e2t[I2(ji, jj)] / e3t_n[q];
+      }
+  lbc_closed(jpi, jpj, hdivn, jpk, 'T', 0.0);
+  double z1_2dt = 1. / (2. * nm->rn_rdt);
+  if (nm->neuler == 0 && kt == nm->nit000) z1_2dt = 1. / nm->rn_rdt;
+  for (size_t p = 0; p < n2; ++p) wn[p + n2 * (jpk - 1)] = 0.0;
+  for (int jk = jpk - 1; jk >= 1; --jk)
+    for (size_t p = 0; p < n2; ++p) {
+      size_t q = p + n2 * (jk - 1);
+      wn[q] = wn[q + n2] - (e3t_n[q] * hdivn[q] + z1_2dt * (e3t_a[q] - e3t_b[q])) * c->tmask[q];
+    }
+  free(hdivn);
+  return NEMO_OK;
+}
+
+/* The time step of dyn_zdf (dynzdf.F90:112) without vertical viscosity or drag:
+ * ua = (ub + r2dt ua) umask; the implicit viscosity solve is not on the path. */
+int ora_dyn_zdf_step(ora_ctx *c, int kt) {
+  const nemo_namelist *nm = &c->nam;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n3 = (size_t)jpi * jpj * jpk, n2 = (size_t)jpi * jpj;
+  double *ua = c->f[NEMO_F_UA], *va = c->f[NEMO_F_VA];
+  const double *ub = c->f[NEMO_F_UB], *vb = c->f[NEMO_F_VB];
+  if (!ua || !va || !ub || !vb) return NEMO_ERR_UNBOUND;
+  const double r2dt = (nm->neuler == 0 && kt == nm->nit000) ? nm->rn_rdt : 2. * nm->rn_rdt;
+  for (size_t q = 0; q < n3 - n2; ++q) {
+    ua[q] = (ub[q] + r2dt * ua[q]) * c->umask[q];
+    va[q] = (vb[q] + r2dt * va[q]) * c->vmask[q];
+  }
+  return NEMO_OK;
+}
+
+/* dyn_nxt (dynnxt.F90:66-377): linear free surface, ln_dynspg_ts with ln_bt_fw. */
+int ora_dyn_nxt(ora_ctx *c, int kt) {
+  const nemo_namelist *nm = &c->nam;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj;
+  double **F = c->f;
+  double *ua = F[NEMO_F_UA], *va = F[NEMO_F_VA], *un = F[NEMO_F_UN], *vn = F[NEMO_F_VN];
+  double *ub = F[NEMO_F_UB], *vb = F[NEMO_F_VB];
+  double *un_b = F[NEMO_F_UN_B], *vn_b = F[NEMO_F_VN_B], *ub_b = F[NEMO_F_UB_B], *vb_b = F[NEMO_F_VB_B];
+  const double *ua_b = F[NEMO_F_UA_B], *va_b = F[NEMO_F_VA_B];
+  if (!ua || !va || !un || !vn || !ub || !vb || !un_b || !vn_b || !ub_b || !vb_b || !ua_b || !va_b)
+    return NEMO_ERR_UNBOUND;
+  if (!nm->ln_linssh || !nm->ln_bt_fw) return NEMO_ERR_ARG;
+  const double *e3u = c->e3u_0, *e3v = c->e3v_0, *umask = c->umask, *vmask = c->vmask;
+  const double atfp = nm->rn_atfp;
+  double *zue = zalloc(n2), *zve = zalloc(n2);
+  /* (:114-126) the barotropic part of the after velocity from the sub-steps */
+  for (size_t p = 0; p < n2; ++p) { zue[p] = e3u[p] * ua[p] * umask[p]; zve[p] = e3v[p] * va[p] * vmask[p]; }
+  for (int jk = 2; jk <= jpk - 1; ++jk)
+    for (size_t p = 0; p < n2; ++p) {
+      size_t q = p + n2 * (jk - 1);
+      zue[p] = zue[p] + e3u[q] * ua[q] * umask[q];
+      zve[p] = zve[p] + e3v[q] * va[q] * vmask[q];
+    }
+  for (int jk = 1; jk <= jpk - 1; ++jk)
+    for (size_t p = 0; p < n2; ++p) {
+      size_t q = p + n2 * (jk - 1);
+      ua[q] = (ua[q] - zue[p] * c->r1_hu_0[p] + ua_b[p]) * umask[q];
+      va[q] = (va[q] - zve[p] * c->r1_hv_0[p] + va_b[p]) * vmask[q];
+    }
+  lbc_closed(jpi, jpj, ua, jpk, 'U', 0.0);                    /* :146 */
+  lbc_closed(jpi, jpj, va, jpk, 'V', 0.0);
+  if (nm->neuler == 0 && kt == nm->nit000) {                 /* :168-188 Euler: swap only */
+    memcpy(un, ua, (size_t)(jpk - 1) * n2 * sizeof(double));
+    memcpy(vn, va, (size_t)(jpk - 1) * n2 * sizeof(double));
+  } else {                                                    /* :195-211 Asselin filter and swap */
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (size_t p = 0; p < n2; ++p) {
+        size_t q = p + n2 * (jk - 1);
+        double zuf = un[q] + atfp * (ub[q] - 2.0 * un[q] + ua[q]);
+        double zvf = vn[q] + atfp * (vb[q] - 2.0 * vn[q] + va[q]);
+        ub[q] = zuf; vb[q] = zvf;
+        un[q] = ua[q]; vn[q] = va[q];
+      }
+    /* (:312-324) the before velocity back to the time-split barotropic estimate */
+    for (size_t p = 0; p < n2; ++p) { zue[p] = e3u[p] * ub[p] * umask[p]; zve[p] = e3v[p] * vb[p] * vmask[p]; }
+    for (int jk = 2; jk <= jpk - 1; ++jk)
+      for (size_t p = 0; p < n2; ++p) {
+        size_t q = p + n2 * (jk - 1);
+        zue[p] = zue[p] + e3u[q] * ub[q] * umask[q];
+        zve[p] = zve[p] + e3v[q] * vb[q] * vmask[q];
+      }
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (size_t p = 0; p < n2; ++p) {
+        size_t q = p + n2 * (jk - 1);
+        ub[q] = ub[q] - (zue[p] * c->r1_hu_0[p] - un_b[p]) * umask[q];
+        vb[q] = vb[q] - (zve[p] * c->r1_hv_0[p] - vn_b[p]) * vmask[q];
+      }
+  }
+  /* (:345-358) now and before barotropic velocities for the next step */
+  for (size_t p = 0; p < n2; ++p) {
+    un_b[p] = e3u[p] * un[p] * umask[p]; ub_b[p] = e3u[p] * ub[p] * umask[p];
+    vn_b[p] = e3v[p] * vn[p] * vmask[p]; vb_b[p] = e3v[p] * vb[p] * vmask[p];
+  }
+  for (int jk = 2; jk <= jpk - 1; ++jk)
+    for (size_t p = 0; p < n2; ++p) {
+      size_t q = p + n2 * (jk - 1);
+      un_b[p] = un_b[p] + e3u[q] * un[q] * umask[q]; ub_b[p] = ub_b[p] + e3u[q] * ub[q] * umask[q];
+      vn_b[p] = vn_b[p] + e3v[q] * vn[q] * vmask[q]; vb_b[p] = vb_b[p] + e3v[q] * vb[q] * vmask[q];
+    }
+  for (size_t p = 0; p < n2; ++p) {
+    un_b[p] = un_b[p] * c->r1_hu_0[p]; vn_b[p] = vn_b[p] * c->r1_hv_0[p];
+    ub_b[p] = ub_b[p] * c->r1_hu_0[p]; vb_b[p] = vb_b[p] * c->r1_hv_0[p];
+  }
+  free(zue); free(zve);
+  return NEMO_OK;
+}
+
+/* ssh_swp (sshwzv.F90:216-267), linear free surface. */
+int ora_ssh_swp(ora_ctx *c, int kt) {
+  const nemo_namelist *nm = &c->nam;
+  const size_t n2 = (size_t)c->jpi * c->jpj;
+  double *sshb = c->f[NEMO_F_SSHB], *sshn = c->f[NEMO_F_SSHN];
+  const double *ssha = c->f[NEMO_F_SSHA];
+  if (!sshb || !sshn || !ssha) return NEMO_ERR_UNBOUND;
+  if (!nm->ln_linssh) return NEMO_ERR_ARG;
+  if (nm->neuler == 0 && kt == nm->nit000) {
+    memcpy(sshn, ssha, n2 * sizeof(double));
+  } else {
+    for (size_t p = 0; p < n2; ++p) {
+      sshb[p] = sshn[p] + nm->rn_atfp * (sshb[p] - 2 * sshn[p] + ssha[p]);
+      sshn[p] = ssha[p];
+    }
+  }
+  return NEMO_OK;
+}
+
+/* One model step (step.F90:96-305) with the path and the routines above: ua = va = 0,
+ * dyn_spg_ts, div_hor + wzv, the dyn_zdf time step, tsa = 0, tra_adv, tra_ldf,
+ * tra_zdf, tra_nxt, dyn_nxt, ssh_swp. */
+int ora_stp_model(ora_ctx *c, int kt) {
+  const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk;
+  if (!c->f[NEMO_F_UA] || !c->f[NEMO_F_VA]) return NEMO_ERR_UNBOUND;
+  memset(c->f[NEMO_F_UA], 0, n3 * sizeof(double));
+  memset(c->f[NEMO_F_VA], 0, n3 * sizeof(double));
+  int st = ora_dyn_spg_ts(c, kt);
+  if (!st) st = ora_wzv(c, kt);
+  if (!st) st = ora_dyn_zdf_step(c, kt);
+  if (!st) st = stp_tracers(c, kt);
+  if (!st) st = ora_tra_nxt(c, kt);
+  if (!st) st = ora_dyn_nxt(c, kt);
+  if (!st) st = ora_ssh_swp(c, kt);
+  return st;
 }

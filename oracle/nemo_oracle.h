@@ -79,6 +79,13 @@ int ora_tra_zdf_imp_adj(ora_ctx *c, int kt, int kit000, const char *cdtype, doub
                         double *ptb_ad, double *pta_ad, int kjpt);
 int ora_tra_nxt(ora_ctx *c, int kt);
 int ora_tra_nxt_adj(ora_ctx *c, int kt, double *tsb_ad, double *tsn_ad, double *tsa_ad);
+/* The rest of a linear-free-surface step, and one model step built from them and
+ * the path (momentum trends outside the path and vertical viscosity held at 0). */
+int ora_wzv(ora_ctx *c, int kt);
+int ora_dyn_zdf_step(ora_ctx *c, int kt);
+int ora_dyn_nxt(ora_ctx *c, int kt);
+int ora_ssh_swp(ora_ctx *c, int kt);
+int ora_stp_model(ora_ctx *c, int kt);
 /* 1: start the work arrays standing for Fortran automatic arrays as NaN */
 void ora_set_poison(int on);
 

@@ -50,6 +50,8 @@ def lib():
         P("ora_tra_zdf_imp_adj", [vp, i, i, cp, d, vp, vp, i])
         P("ora_tra_nxt", [vp, i])
         P("ora_tra_nxt_adj", [vp, i, vp, vp, vp])
+        for name in ("ora_wzv", "ora_dyn_zdf_step", "ora_dyn_nxt", "ora_ssh_swp", "ora_stp_model"):
+            P(name, [vp, i])
         _lib = L
     return _lib
 
@@ -195,3 +197,19 @@ class Oracle:
 
     def tra_nxt_adj(self, kt, tsb_ad, tsn_ad, tsa_ad):
         self._ck(lib().ora_tra_nxt_adj(self.h, kt, _p(tsb_ad), _p(tsn_ad), _p(tsa_ad)), "tra_nxt_adj")
+
+    # ------------------------------------------------------- rest of the step
+    def wzv(self, kt):
+        self._ck(lib().ora_wzv(self.h, kt), "wzv")
+
+    def dyn_zdf_step(self, kt):
+        self._ck(lib().ora_dyn_zdf_step(self.h, kt), "dyn_zdf_step")
+
+    def dyn_nxt(self, kt):
+        self._ck(lib().ora_dyn_nxt(self.h, kt), "dyn_nxt")
+
+    def ssh_swp(self, kt):
+        self._ck(lib().ora_ssh_swp(self.h, kt), "ssh_swp")
+
+    def stp_model(self, kt):
+        self._ck(lib().ora_stp_model(self.h, kt), "stp_model")
