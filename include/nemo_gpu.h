@@ -402,6 +402,16 @@ enum nemo_kernel_id {
   NEMO_K_COUNT
 };
 
+/* Autotuner of the hot path's launch shapes (no counterpart in the reference):
+ * runs nrep timed steps of nemo_gpu_stp_hotpath at step kt (> nit000 + 1) for each
+ * candidate block height (32 x 4, 32 x 2, 32 x 1) of the 32-wide kernels and keeps,
+ * per kernel, the fastest; every bound field the step writes is put back before
+ * each trial and at the end, so the state is as before the call. The TMA-staged
+ * kernels and the persistent sub-step kernel keep their fixed tiles. */
+int nemo_gpu_autotune(nemo_ctx *ctx, int kt, int nrep);
+/* The block heights in use, ty[id] per nemo_kernel_id (n entries). */
+int nemo_gpu_get_launch_shape(const nemo_ctx *ctx, int *ty, int n);
+
 /* Per-kernel device timing of nemo_gpu_stp_hotpath while timing is on (no
  * counterpart in the reference, whose timing stops at routines): a CUDA event is
  * recorded on the context's stream after every kernel launch, so

@@ -104,6 +104,7 @@ struct nemo_ctx {
   int tcalls = 0;
   // per-kernel timing (events after every launch while timing is on)
   KernelClock kc;
+  LaunchShape shape;  // block heights chosen by nemo_gpu_autotune (0: the default)
   // host copies: uploads and downloads run on their own streams, each in call order
   // (one stream already saturates the host link each way), so the downloads of one
   // step overlap the uploads of the next; every field has the events of its last
@@ -131,6 +132,7 @@ struct nemo_ctx {
 
 namespace nemo {
 thread_local KernelClock* t_kclock = nullptr;
+thread_local const LaunchShape* t_shape = nullptr;
 }
 
 namespace {
@@ -914,9 +916,9 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
   auto mark = [&](int i) { if (c->timing) cudaEventRecord(c->tev[i], c->stream); };
   // the kernel clock is installed for this thread until the function returns
   struct ClockGuard {
-    explicit ClockGuard(KernelClock* k) { t_kclock = k; }
-    ~ClockGuard() { t_kclock = nullptr; }
-  } guard(c->timing ? &c->kc : nullptr);
+    explicit ClockGuard(KernelClock* k, const LaunchShape* sh) { t_kclock = k; t_shape = sh; }
+    ~ClockGuard() { t_kclock = nullptr; t_shape = nullptr; }
+  } guard(c->timing ? &c->kc : nullptr, &c->shape);
   if (c->timing) {
     c->kc.n = 0;
     cudaEventRecord(c->kc.ev[0], c->stream);
@@ -1621,6 +1623,84 @@ static int stp_common(nemo_ctx* c, int kt, bool model) {
 int nemo_gpu_stp_hotpath(nemo_ctx* c, int kt) { return stp_common(c, kt, false); }
 
 int nemo_gpu_stp_model(nemo_ctx* c, int kt) { return stp_common(c, kt, true); }
+
+// ------------------------------------------------------------------ autotuner
+// The kernels of the hot path whose 32-wide block height the autotuner chooses
+// (the TMA-staged and the persistent sub-step kernels have fixed tiles).
+static const int kTunable[] = {NEMO_K_FCT_A, NEMO_K_FCT_B, NEMO_K_FCT_C, NEMO_K_ISO_FLUX, NEMO_K_ZDF_IMP,
+                               NEMO_K_SPG_COR, NEMO_K_SPG_P1A, NEMO_K_SPG_P1B, NEMO_K_SPG_P3};
+
+int nemo_gpu_autotune(nemo_ctx* c, int kt, int nrep) {
+  if (!c) return NEMO_ERR_ARG;
+  const nemo_namelist& nm = c->nam;
+  if (nrep < 1) nrep = 3;
+  if (kt <= nm.nit000 + 1) return fail(c, NEMO_ERR_ARG, "autotune: kt must be a steady-state step (> nit000 + 1)");
+  if (!nm.ln_bt_av)
+    return fail(c, NEMO_ERR_UNSUPPORTED, "autotune: the sub-step state carries across steps without ln_bt_av");
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  // every bound field the hot path writes, saved and put back before each trial step
+  std::vector<std::pair<int, void*>> saved;
+  auto bytes_of = [&](int id) {
+    return field_numel(c, id) * c->nmem * (nemo_gpu_field_is_fp64(c, id) ? 8 : 4);
+  };
+  auto cleanup = [&]() {
+    for (auto& p : saved) cudaFree(p.second);
+  };
+  for (int id = 0; id < NEMO_F_COUNT; ++id) {
+    if (!c->f[id] || !(spg_writes(id) || id == NEMO_F_TSA || id == NEMO_F_AH_WSLP2 || id == NEMO_F_AKZ)) continue;
+    void* p = nullptr;
+    if (cudaMalloc(&p, bytes_of(id)) != cudaSuccess) {
+      cleanup();
+      return fail(c, NEMO_ERR_NOMEM, "autotune: copies of the written fields");
+    }
+    saved.push_back({id, p});
+    CK(cudaMemcpyAsync(p, c->f[id], bytes_of(id), cudaMemcpyDeviceToDevice, c->stream), "autotune save");
+  }
+  auto restore = [&]() -> cudaError_t {
+    for (auto& p : saved) {
+      cudaError_t e = cudaMemcpyAsync(c->f[p.first], p.second, bytes_of(p.first), cudaMemcpyDeviceToDevice, c->stream);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  };
+  const bool was_timing = c->timing;
+  if (int s = nemo_gpu_set_timing(c, 1)) { cleanup(); return s; }
+  double best[NEMO_K_COUNT];
+  unsigned char pick[NEMO_K_COUNT] = {};
+  for (double& b : best) b = 1e300;
+  int st = NEMO_OK;
+  for (int ty : {4, 2, 1}) {
+    for (int id : kTunable) c->shape.ty[id] = (unsigned char)ty;
+    for (int r = 0; r <= nrep && st == NEMO_OK; ++r) {
+      if (r == 1) {  // the first step of each shape warms up
+        for (double& t : c->kms) t = 0.0;
+        for (int& n : c->kcnt) n = 0;
+      }
+      if (restore() != cudaSuccess) st = fail(c, NEMO_ERR_CUDA, "autotune restore");
+      else st = c->prec == NEMO_PREC_FP64 ? run_hotpath<double>(c, kt, false) : run_hotpath<float>(c, kt, false);
+    }
+    if (st) break;
+    for (int id : kTunable)
+      if (c->kcnt[id] > 0 && c->kms[id] / c->kcnt[id] < best[id]) {
+        best[id] = c->kms[id] / c->kcnt[id];
+        pick[id] = (unsigned char)ty;
+      }
+  }
+  for (int id : kTunable) c->shape.ty[id] = pick[id];
+  if (restore() != cudaSuccess && st == NEMO_OK) st = fail(c, NEMO_ERR_CUDA, "autotune restore");
+  cudaStreamSynchronize(c->stream);
+  cleanup();
+  nemo_gpu_set_timing(c, was_timing);
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);  // recaptured with the chosen shapes
+  c->graphs.clear();
+  return st;
+}
+
+int nemo_gpu_get_launch_shape(const nemo_ctx* c, int* ty, int n) {
+  if (!c || n < 0 || (n > 0 && !ty)) return NEMO_ERR_ARG;
+  for (int i = 0; i < n; ++i) ty[i] = i < NEMO_K_COUNT && c->shape.ty[i] ? c->shape.ty[i] : 4;
+  return NEMO_OK;
+}
 
 int nemo_gpu_set_timing(nemo_ctx* c, int on) {
   if (!c) return NEMO_ERR_ARG;

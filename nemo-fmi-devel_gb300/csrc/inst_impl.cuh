@@ -13,16 +13,16 @@ namespace nemo {
 
 constexpr int BX = 32, BY = 4;
 
-// one thread per water column (recurrences along k)
+// one thread per water column (recurrences along k); ty: block height
 template <class T>
-static dim3 col_grid(const Dom<T>& d) {
-  return dim3((d.jpi + BX - 1) / BX, (d.jpj + BY - 1) / BY, d.nmem);
+static dim3 col_grid(const Dom<T>& d, int ty = BY) {
+  return dim3((d.jpi + BX - 1) / BX, (d.jpj + ty - 1) / ty, d.nmem);
 }
 
 // one thread per KCH-level chunk of a column: z = member * nchunk + chunk
 template <class T>
-static dim3 kc_grid(const Dom<T>& d) {
-  return dim3((d.jpi + BX - 1) / BX, (d.jpj + BY - 1) / BY, d.nmem * ((d.jpk + KCH - 1) / KCH));
+static dim3 kc_grid(const Dom<T>& d, int ty = BY) {
+  return dim3((d.jpi + BX - 1) / BX, (d.jpj + ty - 1) / ty, d.nmem * ((d.jpk + KCH - 1) / KCH));
 }
 
 // one thread per (i,j,k) point: z = member * jpk + (k - 1)
@@ -116,18 +116,20 @@ cudaError_t launch_fct(const Dom<T>& d, const FctArgs<T>& a, cudaStream_t s) {
             ktick(NEMO_K_FCT_A_TMA, s);
             k_fct_b_tma<T><<<grid, dim3(TM_X, TM_Y), FB_SMEM, s>>>(d, a, mb, a.err, 1 << 16);
             ktick(NEMO_K_FCT_B_TMA, s);
-            k_fct_c_hot<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+            const int tc = kty(NEMO_K_FCT_C);
+            k_fct_c_hot<T><<<kc_grid(d, tc), dim3(BX, tc), 0, s>>>(d, a);
             ktick(NEMO_K_FCT_C, s);
             return cudaGetLastError();
           }
         }
       }
     }
-    k_fct_a_hot<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+    const int ta = kty(NEMO_K_FCT_A), tb = kty(NEMO_K_FCT_B), tc = kty(NEMO_K_FCT_C);
+    k_fct_a_hot<T><<<kc_grid(d, ta), dim3(BX, ta), 0, s>>>(d, a);
     ktick(NEMO_K_FCT_A, s);
-    k_fct_b_hot<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+    k_fct_b_hot<T><<<kc_grid(d, tb), dim3(BX, tb), 0, s>>>(d, a);
     ktick(NEMO_K_FCT_B, s);
-    k_fct_c_hot<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+    k_fct_c_hot<T><<<kc_grid(d, tc), dim3(BX, tc), 0, s>>>(d, a);
     ktick(NEMO_K_FCT_C, s);
     return cudaGetLastError();
   }
@@ -175,7 +177,8 @@ cudaError_t launch_iso_flux(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s
         return cudaGetLastError();
       }
     }
-    k_iso_flux_hot<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+    const int ti = kty(NEMO_K_ISO_FLUX);
+    k_iso_flux_hot<T><<<kc_grid(d, ti), dim3(BX, ti), 0, s>>>(d, a);
   } else {
     k_iso_flux<T><<<kc_grid(d), dim3(BX, BY), 0, s>>>(d, a);
   }
@@ -203,17 +206,20 @@ cudaError_t launch_zdf(const Dom<T>& d, const ZdfArgs<T>& a, cudaStream_t s) {
   if constexpr (sizeof(T) == 4) {
     if (d.jpk == 31) {  // the GYRE levels: columns staged in shared memory
       static bool attr = false;  // dynamic shared memory beyond 48 KB needs the opt-in
-      constexpr int smem = 4 * 31 * BX * BY * sizeof(float);
+      constexpr int smem_max = 4 * 31 * BX * BY * sizeof(float);
       if (!attr) {
-        cudaFuncSetAttribute(k_zdf_imp_async<31>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaFuncSetAttribute(k_zdf_imp_async<31>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
         attr = true;
       }
-      k_zdf_imp_async<31><<<col_grid(d), dim3(BX, BY), smem, s>>>(d, a);
+      const int tz = kty(NEMO_K_ZDF_IMP);
+      const int smem = 4 * 31 * BX * tz * sizeof(float);
+      k_zdf_imp_async<31><<<col_grid(d, tz), dim3(BX, tz), smem, s>>>(d, a);
       ktick(NEMO_K_ZDF_IMP, s);
       return cudaGetLastError();
     }
   }
-  k_zdf_imp<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  const int tz = kty(NEMO_K_ZDF_IMP);
+  k_zdf_imp<T><<<col_grid(d, tz), dim3(BX, tz), 0, s>>>(d, a);
   ktick(NEMO_K_ZDF_IMP, s);
   return cudaGetLastError();
 }
@@ -250,13 +256,18 @@ cudaError_t launch_spg(const Dom<T>& d, const SpgArgs<T>& a, const GridBar& bar,
   bool p1a_reg = false;
   if constexpr (sizeof(T) == 4) {
     if (d.jpk == 31) {  // the GYRE levels: columns in registers
-      k_spg_p1a_reg<31><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+      const int t1 = kty(NEMO_K_SPG_P1A);
+      k_spg_p1a_reg<31><<<col_grid(d, t1), dim3(BX, t1), 0, s>>>(d, a);
       p1a_reg = true;
     }
   }
-  if (!p1a_reg) k_spg_p1a<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  if (!p1a_reg) {
+    const int t1 = kty(NEMO_K_SPG_P1A);
+    k_spg_p1a<T><<<col_grid(d, t1), dim3(BX, t1), 0, s>>>(d, a);
+  }
   ktick(NEMO_K_SPG_P1A, s);
-  k_spg_p1b<T><<<col_grid(d), dim3(BX, BY), 0, s>>>(d, a);
+  const int t1b = kty(NEMO_K_SPG_P1B);
+  k_spg_p1b<T><<<col_grid(d, t1b), dim3(BX, t1b), 0, s>>>(d, a);
   ktick(NEMO_K_SPG_P1B, s);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(p2_blocks);
@@ -272,8 +283,9 @@ cudaError_t launch_spg(const Dom<T>& d, const SpgArgs<T>& a, const GridBar& bar,
                         : cudaLaunchKernelEx(&cfg, k_spg_p2<T, false>, d, a, bar);
   if (e != cudaSuccess) return e;
   ktick(NEMO_K_SPG_P2, s);
-  k_spg_p3<T><<<dim3((d.jpi + BX - 1) / BX, (d.jpj + BY - 1) / BY, d.nmem * ((d.jpk + KCH3 - 1) / KCH3)),
-                 dim3(BX, BY), 0, s>>>(d, a);
+  const int t3 = kty(NEMO_K_SPG_P3);
+  k_spg_p3<T><<<dim3((d.jpi + BX - 1) / BX, (d.jpj + t3 - 1) / t3, d.nmem * ((d.jpk + KCH3 - 1) / KCH3)),
+                 dim3(BX, t3), 0, s>>>(d, a);
   ktick(NEMO_K_SPG_P3, s);
   return cudaGetLastError();
 }

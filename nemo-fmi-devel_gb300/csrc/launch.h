@@ -17,6 +17,18 @@ struct KernelClock {
   int n = 0;
 };
 extern thread_local KernelClock* t_kclock;
+
+// Block heights of the 32-wide (i, j) launches, per kernel id, chosen by the
+// context's autotuner (nemo_gpu_autotune): a context installs its table for the
+// calling thread while it runs the hot path; elsewhere the default 4 (32 x 4).
+struct LaunchShape {
+  unsigned char ty[NEMO_K_COUNT] = {};
+};
+extern thread_local const LaunchShape* t_shape;
+inline int kty(int id) {
+  const LaunchShape* s = t_shape;
+  return (s && s->ty[id]) ? s->ty[id] : 4;
+}
 inline void ktick(int id, cudaStream_t s) {
   KernelClock* k = t_kclock;
   if (k && k->n < KernelClock::CAP) {

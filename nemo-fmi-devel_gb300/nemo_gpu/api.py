@@ -130,6 +130,19 @@ class Context:
     def set_fct_fused(self, on):
         self._ck(self.lib.nemo_gpu_set_fct_fused(self.h, int(on)), "set_fct_fused")
 
+    def autotune(self, kt, nrep=3):
+        """Choose the block height of each tunable hot-path kernel by timing nrep steps
+        per candidate at step kt; the bound state is left as it was."""
+        self._ck(self.lib.nemo_gpu_autotune(self.h, kt, nrep), "autotune")
+
+    def launch_shape(self):
+        """{kernel name: block height} of the 32-wide hot-path launches."""
+        nk = _ffi.K["COUNT"]
+        ty = (C.c_int * nk)()
+        self._ck(self.lib.nemo_gpu_get_launch_shape(self.h, ty, nk), "get_launch_shape")
+        names = {v: k.lower() for k, v in _ffi.K.items() if k != "COUNT"}
+        return {names[i]: ty[i] for i in range(nk)}
+
     def set_timing(self, on):
         self._ck(self.lib.nemo_gpu_set_timing(self.h, int(on)), "set_timing")
 
