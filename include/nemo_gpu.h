@@ -112,6 +112,7 @@ typedef struct nemo_namelist {
   int nn_fct_h;           /* &namtra_adv: FCT order in the horizontal (2 or 4; 0 = 2)  */
   int nn_fct_v;           /*              and the vertical (2 or 4; 0 = 2), used by
                              nemo_gpu_stp_hotpath                                       */
+  double rn_slpmax;       /* &namtra_ldf: maximum iso-neutral slope (0 = 0.01)         */
 } nemo_namelist;
 
 /* ------------------------------------------------------- module-global fields
@@ -165,6 +166,12 @@ enum nemo_field_id {
    * member, ordered (member, tracer, face x/y/z, k, j, i); 0 where the forward
    * zeroed the antidiffusive flux. */
   NEMO_F_FCT_TAPE,
+  /* ldf_slp (ldfslp.F90) module inputs: depths of the now T- and W-points
+   * (dom_oce gdept_n, gdepw_n), and the mixed layer of zdf_mxl (zdfmxl.F90): its
+   * level nmln (int32 in both precisions), depth hmlp and the depth of its last
+   * T-point hmlpt. */
+  NEMO_F_GDEPT_N, NEMO_F_GDEPW_N,      /* [T]                                         */
+  NEMO_F_NMLN, NEMO_F_HMLP, NEMO_F_HMLPT, /* [S]                                      */
   NEMO_F_COUNT
 };
 
@@ -194,7 +201,8 @@ int nemo_gpu_synchronize(nemo_ctx *ctx);
  * the e3 fields = NULL select the rest-state e3*_0 of the domain). */
 int nemo_gpu_bind(nemo_ctx *ctx, int field_id, void *dev_ptr);
 
-/* Number of elements (per member) and precision of a field (1 = FP64, 0 = FP32). */
+/* Number of elements (per member) and precision of a field (1 = FP64, 0 = 4-byte
+ * elements: FP32, or int32 for NEMO_F_NMLN). */
 size_t nemo_gpu_field_numel(const nemo_ctx *ctx, int field_id);
 int nemo_gpu_field_is_fp64(const nemo_ctx *ctx, int field_id);
 
@@ -272,6 +280,15 @@ int nemo_gpu_tra_nxt(nemo_ctx *ctx, int kt);
  * the horizontal divergence (0 on the closed edges), then wn integrated up from
  * wn(jpk) = 0, with the e3t_a - e3t_b term of z*. */
 int nemo_gpu_wzv(nemo_ctx *ctx, int kt);
+/* ldf_slp (ldfslp.F90:83-374, with ldf_slp_mxl :620-729): the iso-neutral slopes
+ * uslp, vslp, wslpi, wslpj (the bound NEMO_F_USLP, ... fields, levels 2..jpk-1;
+ * levels 1 and jpk are left as they are except on the closed edges) from the in
+ * situ density anomaly prd and N^2 pn2 (3-D device arrays), the bound depths and
+ * mixed layer. z-coordinate without ice-shelf cavities and without partial steps
+ * (the zps bottom density gradients are not an input here): NEMO_ERR_UNSUPPORTED
+ * otherwise. */
+int nemo_gpu_ldf_slp(nemo_ctx *ctx, int kt, const void *prd, const void *pn2);
+
 /* The time step of dyn_zdf (dynzdf.F90:112) without vertical viscosity or drag:
  * ua = (ub + r2dt ua) umask, va likewise. The implicit viscosity solve of
  * dynzdf.F90:160-330 is not implemented. */
@@ -399,6 +416,7 @@ enum nemo_kernel_id {
   NEMO_K_FCT_ADJ, NEMO_K_LAP_ADJ, NEMO_K_ISO_ADJ, NEMO_K_ZDF_ADJ, /* adjoints */
   NEMO_K_TRA_NXT, NEMO_K_TRA_NXT_ADJ,
   NEMO_K_WZV, NEMO_K_DYN_ZDF_STEP, NEMO_K_DYN_NXT, NEMO_K_SSH_SWP, /* rest of the model step */
+  NEMO_K_LDF_SLP,      /* the three iso-neutral slope kernels */
   NEMO_K_COUNT
 };
 

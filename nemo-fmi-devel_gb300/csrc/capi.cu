@@ -75,6 +75,7 @@ struct nemo_ctx {
   void* iso_w[3] = {};         // iso-neutral fluxes zftu, zftv, ztfw
   void* adj_w[4] = {};         // iso-neutral adjoint: G and the gradient adjoints
   int adj_kjpt = 0;
+  void* slp_w = nullptr;       // ldf_slp work: 4 3-D and 6 2-D arrays per member
   int iso_kjpt = 0;
   int fct_kjpt = 0;
   void* spg_w[5] = {};
@@ -218,7 +219,7 @@ bool spg_writes(int id) {
 // scale factors at u- and v-points, every 2-D field (and e3f_n)
 bool spg_reads(int id) {
   if (spg_writes(id) || id == NEMO_F_UB || id == NEMO_F_VB || id == NEMO_F_E3U_N || id == NEMO_F_E3V_N) return true;
-  return id >= NEMO_F_SSHB && id != NEMO_F_FCT_TAPE;
+  return id >= NEMO_F_SSHB && id < NEMO_F_FCT_TAPE;
 }
 
 inline size_t I2(const nemo_ctx* c, int i, int j) { return (size_t)(i - 1) + (size_t)c->jpi * (j - 1); }
@@ -240,6 +241,7 @@ size_t field_numel(const nemo_ctx* c, int id) {
     case NEMO_F_GTSU: case NEMO_F_GTSV: case NEMO_F_GTUI: case NEMO_F_GTVI: return 2 * (size_t)c->n2;
     case NEMO_F_E3F_N: return (size_t)c->n3;
     case NEMO_F_FCT_TAPE: return 6 * (size_t)c->n3;  // 3 faces x 2 tracers
+    case NEMO_F_GDEPT_N: case NEMO_F_GDEPW_N: return (size_t)c->n3;
     default: break;
   }
   if (id >= NEMO_F_SSHB) return (size_t)c->n2;
@@ -840,6 +842,30 @@ int run_spg(nemo_ctx* c, int kt) {
   return NEMO_OK;
 }
 
+template <class T>
+int run_ldf_slp(nemo_ctx* c, const void* prd, const void* pn2) {
+  const nemo_namelist& nm = c->nam;
+  const size_t n3 = (size_t)c->n3 * c->nmem, n2 = (size_t)c->n2 * c->nmem;
+  if (!c->slp_w && cudaMalloc(&c->slp_w, (4 * n3 + 6 * n2) * sizeof(T)) != cudaSuccess)
+    return fail(c, NEMO_ERR_NOMEM, "ldf_slp work arrays");
+  T* w = (T*)c->slp_w;
+  SlpArgs<T> a{};
+  a.prd = (const T*)prd; a.pn2 = (const T*)pn2;
+  a.gdept = (const T*)c->f[NEMO_F_GDEPT_N]; a.gdepw = (const T*)c->f[NEMO_F_GDEPW_N];
+  a.nmln = (const int*)c->f[NEMO_F_NMLN];
+  a.hmlp = (const T*)c->f[NEMO_F_HMLP]; a.hmlpt = (const T*)c->f[NEMO_F_HMLPT];
+  a.uslp = (T*)c->f[NEMO_F_USLP]; a.vslp = (T*)c->f[NEMO_F_VSLP];
+  a.wslpi = (T*)c->f[NEMO_F_WSLPI]; a.wslpj = (T*)c->f[NEMO_F_WSLPJ];
+  a.zu = w; a.zv = w + n3; a.zwi = w + 2 * n3; a.zwj = w + 3 * n3;
+  T* w2 = w + 4 * n3;
+  a.uml = w2; a.vml = w2 + n2; a.wiml = w2 + 2 * n2; a.wjml = w2 + 3 * n2; a.hu = w2 + 4 * n2; a.hv = w2 + 5 * n2;
+  a.zeps = (T)1.e-20; a.zm1_g = (T)(-1.0 / nm.grav); a.zm1_2g = (T)(-0.5 / nm.grav);
+  a.z1_slpmax = (T)(1.0 / (nm.rn_slpmax > 0 ? nm.rn_slpmax : 0.01));
+  cudaError_t e = launch_ldf_slp<T>(dom_now<T>(c), a, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "ldf_slp launch");
+  return NEMO_OK;
+}
+
 // ------------------------------------------------- the rest of a model step
 int model_fields(nemo_ctx* c, const char* what) {
   const nemo_namelist& nm = c->nam;
@@ -1154,6 +1180,7 @@ int nemo_gpu_destroy(nemo_ctx* c) {
   cudaFree(c->fct_ztw);
   for (auto p : c->iso_w) cudaFree(p);
   for (auto p : c->adj_w) cudaFree(p);
+  cudaFree(c->slp_w);
   for (auto p : c->spg_w) cudaFree(p);
   for (auto p : c->spg_cor) cudaFree(p);
   for (auto p : c->ring) cudaFree(p);
@@ -1218,7 +1245,7 @@ size_t nemo_gpu_field_numel(const nemo_ctx* c, int id) {
 }
 
 int nemo_gpu_field_is_fp64(const nemo_ctx* c, int id) {
-  if (!c) return 0;
+  if (!c || id == NEMO_F_NMLN) return 0;  // the mixed-layer level is int32
   return c->prec == NEMO_PREC_FP64 || is_fp64_field(id);
 }
 
@@ -1372,6 +1399,20 @@ int nemo_gpu_tra_nxt(nemo_ctx* c, int kt) {
     return fail(c, NEMO_ERR_UNBOUND, "tra_nxt: tsb, tsn and tsa must be bound");
   if (!nm.ln_linssh) return fail(c, NEMO_ERR_ARG, "tra_nxt: linear free surface only (ln_linssh)");
   return c->prec == NEMO_PREC_FP64 ? run_tra_nxt<double>(c, kt) : run_tra_nxt<float>(c, kt);
+}
+
+int nemo_gpu_ldf_slp(nemo_ctx* c, int kt, const void* prd, const void* pn2) {
+  (void)kt;
+  if (!c) return NEMO_ERR_ARG;
+  if (!prd || !pn2) return fail(c, NEMO_ERR_ARG, "ldf_slp: null prd or pn2");
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  for (int id : {NEMO_F_USLP, NEMO_F_VSLP, NEMO_F_WSLPI, NEMO_F_WSLPJ, NEMO_F_GDEPT_N, NEMO_F_GDEPW_N, NEMO_F_NMLN,
+                 NEMO_F_HMLP, NEMO_F_HMLPT})
+    if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "ldf_slp: field %d must be bound", id);
+  const nemo_namelist& nm = c->nam;
+  if (nm.ln_zps || nm.ln_isfcav || nm.ln_sco)
+    return fail(c, NEMO_ERR_UNSUPPORTED, "ldf_slp: z-coordinate without partial steps or cavities only");
+  return c->prec == NEMO_PREC_FP64 ? run_ldf_slp<double>(c, prd, pn2) : run_ldf_slp<float>(c, prd, pn2);
 }
 
 int nemo_gpu_wzv(nemo_ctx* c, int kt) {

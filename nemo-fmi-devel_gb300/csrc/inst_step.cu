@@ -38,11 +38,21 @@ cudaError_t launch_ssh_swp(const Dom<T>& d, T* sshb, T* sshn, const double* ssha
   return cudaGetLastError();
 }
 
+template <class T>
+cudaError_t launch_ldf_slp(const Dom<T>& d, const SlpArgs<T>& a, cudaStream_t s) {
+  k_slp_mxl<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a);
+  k_slp_pre<T><<<s_pt(d), dim3(SX, SY), 0, s>>>(d, a);
+  k_slp_filter<T><<<s_pt(d), dim3(SX, SY), 0, s>>>(d, a);
+  ktick(NEMO_K_LDF_SLP, s);
+  return cudaGetLastError();
+}
+
 #define NEMO_STEP_INST(T)                                                                                      \
   template cudaError_t launch_wzv<T>(const Dom<T>&, const T*, const T*, T*, T, cudaStream_t);                  \
   template cudaError_t launch_dyn_zdf_step<T>(const Dom<T>&, const T*, const T*, T*, T*, T, cudaStream_t);     \
   template cudaError_t launch_dyn_nxt<T>(const Dom<T>&, const NxtArgs<T, double>&, cudaStream_t);              \
-  template cudaError_t launch_ssh_swp<T>(const Dom<T>&, T*, T*, const double*, T, int, cudaStream_t);
+  template cudaError_t launch_ssh_swp<T>(const Dom<T>&, T*, T*, const double*, T, int, cudaStream_t);      \
+  template cudaError_t launch_ldf_slp<T>(const Dom<T>&, const SlpArgs<T>&, cudaStream_t);
 NEMO_STEP_INST(double)
 NEMO_STEP_INST(float)
 

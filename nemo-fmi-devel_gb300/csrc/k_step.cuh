@@ -138,4 +138,174 @@ __global__ void k_ssh_swp(Dom<T> d, T* sshb, T* sshn, const A* __restrict__ ssha
   sshn[p] = sa;
 }
 
+
+// ----------------------------------------------------------------------- ldf_slp
+// ldf_slp (ldfslp.F90:83-374) with ldf_slp_mxl (:620-729), z-coordinate without
+// cavities or partial steps, in three kernels: the slopes just below the mixed
+// layer (one column per thread), the slopes before the Shapiro filter at u-, v- and
+// w-points (one point per thread), the filter with the coastal decrease and lbc.
+// The density gradients zgru, zgrv and zdzr of the reference's work arrays are
+// formed where they are read, from the same operands in the same order.
+template <class T>
+struct SlpPt {
+  const Dom<T>& d;
+  const SlpArgs<T>& a;
+  long m3;
+  int m;
+  __device__ __forceinline__ long Q(int i, int j, int k) const {
+    return (long)(i - 1) + (long)(j - 1) * d.jpi + (long)(k - 1) * d.n2;
+  }
+  __device__ __forceinline__ T um(int i, int j, int k) const { return umsk<T>(d.ci[Q(i, j, 1)], k); }
+  __device__ __forceinline__ T vm(int i, int j, int k) const { return vmsk<T>(d.ci[Q(i, j, 1)], k); }
+  __device__ __forceinline__ T tm(int i, int j, int k) const { return tmsk<T>(d.ci[Q(i, j, 1)], k); }
+  __device__ __forceinline__ T wm(int i, int j, int k) const { return wmsk<T>(d.ci[Q(i, j, 1)], k); }
+  __device__ __forceinline__ T prd(int i, int j, int k) const { return a.prd[m3 + Q(i, j, k)]; }
+  __device__ __forceinline__ T gru(int i, int j, int k) const { return um(i, j, k) * (prd(i + 1, j, k) - prd(i, j, k)); }
+  __device__ __forceinline__ T grv(int i, int j, int k) const { return vm(i, j, k) * (prd(i, j + 1, k) - prd(i, j, k)); }
+  __device__ __forceinline__ T dzr(int i, int j, int k) const {
+    if (k == 1) return T(0);
+    const long q = m3 + Q(i, j, k);
+    return a.zm1_g * (a.prd[q] + T(1)) * (a.pn2[q] + a.pn2[q + d.n2]) * (T(1) - T(0.5) * tm(i, j, k + 1));
+  }
+  __device__ __forceinline__ T oml(int i, int j, int k) const {
+    return k <= a.nmln[(long)m * d.n2 + Q(i, j, 1)] - 1 ? T(1) : T(0);
+  }
+};
+
+template <class T>
+__global__ void k_slp_mxl(Dom<T> d, SlpArgs<T> a) {
+  ColIdx<T> c = col_index(d);
+  if (!c.valid) return;
+  const long p = (long)c.m * d.n2 + c.ij;
+  if (!c.interior) {  // lbc_lnk of the four mixed-layer slopes: the closed edges 0
+    a.uml[p] = T(0); a.vml[p] = T(0); a.wiml[p] = T(0); a.wjml[p] = T(0);
+    a.hu[p] = T(0); a.hv[p] = T(0);
+    return;
+  }
+  const SlpPt<T> P{d, a, (long)c.m * d.n3, c.m};
+  const int i = c.i, j = c.j, jpk = d.jpk, jpi = d.jpi;
+  const long ij = c.ij, m2 = (long)c.m * d.n2;
+  const int n0 = a.nmln[m2 + ij], ne = a.nmln[m2 + ij + 1], nn = a.nmln[m2 + ij + jpi];
+  int iku = n0 > ne ? n0 : ne;
+  iku = iku < 1 ? 1 : (iku > jpk - 1 ? jpk - 1 : iku);
+  int ikv = n0 > nn ? n0 : nn;
+  ikv = ikv < 1 ? 1 : (ikv > jpk - 1 ? jpk - 1 : ikv);
+  T zbu = T(0.5) * (P.dzr(i, j, iku) + P.dzr(i + 1, j, iku));
+  T zbv = T(0.5) * (P.dzr(i, j, ikv) + P.dzr(i, j + 1, ikv));
+  const T zau = P.gru(i, j, iku) * d.r1_e1u[ij];
+  const T zav = P.grv(i, j, ikv) * d.r1_e2v[ij];
+  zbu = fmn(fmn(zbu, -a.z1_slpmax * fabs(zau)), T(-7.e+3) / d.e3u_n(ij, iku, c.m) * fabs(zau));
+  zbv = fmn(fmn(zbv, -a.z1_slpmax * fabs(zav)), T(-7.e+3) / d.e3v_n(ij, ikv, c.m) * fabs(zav));
+  const T uml = zau / (zbu - a.zeps) * P.um(i, j, iku);
+  const T vml = zav / (zbv - a.zeps) * P.vm(i, j, ikv);
+  const int ik = n0 + 1 < jpk ? n0 + 1 : jpk;
+  const int ikm1 = ik - 1 > 1 ? ik - 1 : 1;
+  const T zbw = a.zm1_2g * a.pn2[P.m3 + P.Q(i, j, ik)] * (P.prd(i, j, ik) + P.prd(i, j, ikm1) + T(2));
+  const T zci = fmx(P.um(i - 1, j, ik) + P.um(i, j, ik) + P.um(i - 1, j, ikm1) + P.um(i, j, ikm1), a.zeps) * d.e1t[ij];
+  const T zcj = fmx(P.vm(i, j - 1, ik) + P.vm(i, j, ik) + P.vm(i, j - 1, ikm1) + P.vm(i, j, ikm1), a.zeps) * d.e2t[ij];
+  const T tmk = P.tm(i, j, ik);
+  const T zai = (P.gru(i - 1, j, ik) + P.gru(i, j, ik) + P.gru(i - 1, j, ikm1) + P.gru(i, j, ikm1)) / zci * tmk;
+  const T zaj = (P.grv(i, j - 1, ik) + P.grv(i, j, ik) + P.grv(i, j - 1, ikm1) + P.grv(i, j, ikm1)) / zcj * tmk;
+  const T e3w = d.e3w_n(ij, ik, c.m);
+  const T zbi = fmn(fmn(zbw, T(-100) * fabs(zai)), T(-7.e+3) / e3w * fabs(zai));
+  const T zbj = fmn(fmn(zbw, T(-100) * fabs(zaj)), T(-7.e+3) / e3w * fabs(zaj));
+  a.uml[p] = uml;
+  a.vml[p] = vml;
+  a.wiml[p] = zai / (zbi - a.zeps) * tmk;
+  a.wjml[p] = zaj / (zbj - a.zeps) * tmk;
+  // (:188-194) the mixed-layer slope over the depth of the last T-point in it
+  const T h0 = a.hmlpt[p], he = a.hmlpt[p + 1], hn = a.hmlpt[p + jpi];
+  a.hu[p] = uml / fmx(fmx(h0, he), T(5));
+  a.hv[p] = vml / fmx(fmx(h0, hn), T(5));
+}
+
+// The slopes before the filter: u, v (:197-233) and w (:281-315) at levels 2..jpkm1;
+// 0 on the closed edges (the lbc_lnk of :234 and :316).
+template <class T>
+__global__ void k_slp_pre(Dom<T> d, SlpArgs<T> a) {
+  const PtIdx c = pt_index(d);
+  if (!c.valid || c.k < 2 || c.k > d.jpk - 1) return;
+  const long o = (long)c.m * d.n3 + c.q;
+  if (!c.interior) {
+    a.zu[o] = T(0); a.zv[o] = T(0); a.zwi[o] = T(0); a.zwj[o] = T(0);
+    return;
+  }
+  const SlpPt<T> P{d, a, (long)c.m * d.n3, c.m};
+  const int i = c.i, j = c.j, k = c.k, jpi = d.jpi;
+  const long ij = c.ij, p = (long)c.m * d.n2 + ij;
+  // u- and v-points
+  {
+    const T zau = P.gru(i, j, k) * d.r1_e1u[ij];
+    const T zav = P.grv(i, j, k) * d.r1_e2v[ij];
+    const T dz0 = P.dzr(i, j, k);
+    T zbu = T(0.5) * (dz0 + P.dzr(i + 1, j, k));
+    T zbv = T(0.5) * (dz0 + P.dzr(i, j + 1, k));
+    zbu = fmn(fmn(zbu, -a.z1_slpmax * fabs(zau)), T(-7.e+3) / d.e3u_n(ij, k, c.m) * fabs(zau));
+    zbv = fmn(fmn(zbv, -a.z1_slpmax * fabs(zav)), T(-7.e+3) / d.e3v_n(ij, k, c.m) * fabs(zav));
+    const T o0 = P.oml(i, j, k);
+    const T zfi = fmx(o0, P.oml(i + 1, j, k));
+    const T zfj = fmx(o0, P.oml(i, j + 1, k));
+    const long m3 = P.m3;
+    const T g0 = a.gdept[m3 + c.q];
+    const T zdepu = T(0.5) * ((g0 + a.gdept[m3 + c.q + 1]) - T(2) * T(0) - d.e3u_n(ij, 1, c.m));
+    const T zdepv = T(0.5) * ((g0 + a.gdept[m3 + c.q + jpi]) - T(2) * T(0) - d.e3v_n(ij, 1, c.m));
+    a.zu[o] = ((T(1) - zfi) * zau / (zbu - a.zeps) + zfi * zdepu * a.hu[p]) * P.um(i, j, k);
+    a.zv[o] = ((T(1) - zfj) * zav / (zbv - a.zeps) + zfj * zdepv * a.hv[p]) * P.vm(i, j, k);
+  }
+  // w-points
+  {
+    const long q = P.m3 + c.q;
+    const T zbw = a.zm1_2g * a.pn2[q] * (a.prd[q] + a.prd[q - d.n2] + T(2));
+    const T zci = fmx(P.um(i - 1, j, k) + P.um(i, j, k) + P.um(i - 1, j, k - 1) + P.um(i, j, k - 1), a.zeps) * d.e1t[ij];
+    const T zcj = fmx(P.vm(i, j - 1, k) + P.vm(i, j, k - 1) + P.vm(i, j - 1, k - 1) + P.vm(i, j, k), a.zeps) * d.e2t[ij];
+    const T wmk = P.wm(i, j, k);
+    const T zai = (P.gru(i - 1, j, k) + P.gru(i, j, k - 1) + P.gru(i - 1, j, k - 1) + P.gru(i, j, k)) / zci * wmk;
+    const T zaj = (P.grv(i, j - 1, k) + P.grv(i, j, k - 1) + P.grv(i, j - 1, k - 1) + P.grv(i, j, k)) / zcj * wmk;
+    const T e3w = d.e3w_n(ij, k, c.m);
+    const T zbi = fmn(fmn(zbw, T(-100) * fabs(zai)), T(-7.e+3) / e3w * fabs(zai));
+    const T zbj = fmn(fmn(zbw, T(-100) * fabs(zaj)), T(-7.e+3) / e3w * fabs(zaj));
+    const T zfk = fmx(P.oml(i, j, k), P.oml(i, j, k - 1));
+    const T gw1 = a.gdepw[P.m3 + ij];
+    const T zck = (a.gdepw[q] - gw1) / fmx(a.hmlp[p] - gw1, T(10));
+    a.zwi[o] = (zai / (zbi - a.zeps) * (T(1) - zfk) + zck * a.wiml[p] * zfk) * wmk;
+    a.zwj[o] = (zaj / (zbj - a.zeps) * (T(1) - zfk) + zck * a.wjml[p] * zfk) * wmk;
+  }
+}
+
+// 1-2-1 Shapiro filter of the nine neighbours at level k (:237-275, :319-353)
+template <class T>
+__device__ __forceinline__ T shapiro(const T* __restrict__ z, long q, int jpi) {
+  return z[q - 1 - jpi] + z[q + 1 - jpi] + z[q - 1 + jpi] + z[q + 1 + jpi] +
+         T(2) * (z[q - jpi] + z[q - 1] + z[q + 1] + z[q + jpi]) + T(4) * z[q];
+}
+
+// The filtered slopes with the decrease near coasts and topography (:237-361) on
+// the interior of levels 2..jpkm1; lbc_lnk (:365): 0 on the closed edges, every level.
+template <class T>
+__global__ void k_slp_filter(Dom<T> d, SlpArgs<T> a) {
+  const PtIdx c = pt_index(d);
+  if (!c.valid) return;
+  const long o = (long)c.m * d.n3 + c.q;
+  if (!c.interior) {
+    a.uslp[o] = T(0); a.vslp[o] = T(0); a.wslpi[o] = T(0); a.wslpj[o] = T(0);
+    return;
+  }
+  if (c.k < 2 || c.k > d.jpk - 1) return;
+  const SlpPt<T> P{d, a, (long)c.m * d.n3, c.m};
+  const int i = c.i, j = c.j, k = c.k, jpi = d.jpi;
+  const T z1_16 = T(1) / T(16);
+  T u = z1_16 * shapiro(a.zu, o, jpi);
+  T v = z1_16 * shapiro(a.zv, o, jpi);
+  u = u * (P.um(i, j + 1, k) + P.um(i, j - 1, k)) * T(0.5) * (P.um(i, j, k) + P.um(i, j, k + 1)) * T(0.5);
+  v = v * (P.vm(i + 1, j, k) + P.vm(i - 1, j, k)) * T(0.5) * (P.vm(i, j, k) + P.vm(i, j, k + 1)) * T(0.5);
+  const T zcofw = P.wm(i, j, k) * z1_16;
+  T wi = shapiro(a.zwi, o, jpi) * zcofw;
+  T wj = shapiro(a.zwj, o, jpi) * zcofw;
+  const T zck = (P.um(i, j, k) + P.um(i - 1, j, k)) * (P.vm(i, j, k) + P.vm(i, j - 1, k)) * T(0.25);
+  a.uslp[o] = u;
+  a.vslp[o] = v;
+  a.wslpi[o] = wi * zck;
+  a.wslpj[o] = wj * zck;
+}
+
 }  // namespace nemo

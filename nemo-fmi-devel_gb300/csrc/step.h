@@ -15,6 +15,21 @@ struct NxtArgs {
 };
 
 template <class T>
+struct SlpArgs {
+  const T *prd, *pn2;                  // in situ density anomaly, N^2 (3-D per member)
+  const T *gdept, *gdepw;              // depths of the now T-, W-points (3-D)
+  const int* nmln;                     // mixed-layer level (2-D, int)
+  const T *hmlp, *hmlpt;               // mixed-layer depth, depth of its last T-point
+  T *uslp, *vslp, *wslpi, *wslpj;      // out
+  T *uml, *vml, *wiml, *wjml, *hu, *hv;  // work (2-D): slopes below the mixed layer
+  T *zu, *zv, *zwi, *zwj;              // work (3-D): slopes before the filter
+  T zeps, zm1_g, zm1_2g, z1_slpmax;
+};
+
+template <class T>
+cudaError_t launch_ldf_slp(const Dom<T>& d, const SlpArgs<T>& a, cudaStream_t s);
+
+template <class T>
 cudaError_t launch_wzv(const Dom<T>& d, const T* un, const T* vn, T* wn, T z1_2dt, cudaStream_t s);
 template <class T>
 cudaError_t launch_dyn_zdf_step(const Dom<T>& d, const T* ub, const T* vb, T* ua, T* va, T r2dt, cudaStream_t s);

@@ -51,7 +51,7 @@ class Namelist(C.Structure):
                 ("rn_bt_alpha", C.c_double), ("nvor_scheme", C.c_int), ("nn_een_e3f", C.c_int),
                 ("ln_dynadv_vec", C.c_int), ("ln_sco", C.c_int), ("ln_apr_dyn", C.c_int),
                 ("rn_scal_load", C.c_double), ("grav", C.c_double), ("rau0", C.c_double),
-                ("nn_fct_h", C.c_int), ("nn_fct_v", C.c_int)]
+                ("nn_fct_h", C.c_int), ("nn_fct_v", C.c_int), ("rn_slpmax", C.c_double)]
 
 
 def make_desc(dom):
@@ -110,6 +110,7 @@ def load(path):
     _proto(lib, "nemo_gpu_tra_zdf_imp", i, [vp, i, i, cp, d, vp, vp, i])
     _proto(lib, "nemo_gpu_tra_nxt", i, [vp, i])
     _proto(lib, "nemo_gpu_autotune", i, [vp, i, i])
+    _proto(lib, "nemo_gpu_ldf_slp", i, [vp, i, vp, vp])
     _proto(lib, "nemo_gpu_get_launch_shape", i, [vp, _ip, i])
     for name in ("nemo_gpu_wzv", "nemo_gpu_dyn_zdf_step", "nemo_gpu_dyn_nxt", "nemo_gpu_ssh_swp",
                  "nemo_gpu_stp_model"):

@@ -89,6 +89,8 @@ class Context:
 
     # ------------------------------------------------------------------ fields
     def field_dtype(self, name):
+        if name == "NMLN":  # the mixed-layer level is an integer field
+            return self.torch.int32
         return self.torch.float64 if self.lib.nemo_gpu_field_is_fp64(self.h, _ffi.F[name]) else self.torch.float32
 
     def field_numel(self, name):
@@ -194,6 +196,11 @@ class Context:
 
     def tra_nxt(self, kt):
         self._ck(self.lib.nemo_gpu_tra_nxt(self.h, kt), "tra_nxt")
+
+    def ldf_slp(self, kt, prd, pn2):
+        """ldf_slp (ldfslp.F90): the bound slope fields from the density anomaly and
+        N^2 (device tensors) and the bound depths and mixed layer."""
+        self._ck(self.lib.nemo_gpu_ldf_slp(self.h, kt, _ptr(prd), _ptr(pn2)), "ldf_slp")
 
     def wzv(self, kt):
         self._ck(self.lib.nemo_gpu_wzv(self.h, kt), "wzv")

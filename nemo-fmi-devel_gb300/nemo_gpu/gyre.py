@@ -32,7 +32,7 @@ def namelist(**over):
         rn_aht_0=(0.5 * 0.02) * 100.0e3, ln_zdfddm=0, ln_zad_Aimp=0,
         ln_bt_fw=1, ln_bt_av=1, nn_bt_flt=1, ln_bt_auto=1, nn_baro=30, rn_bt_cmax=0.8, rn_bt_alpha=0.0,
         nvor_scheme=1, nn_een_e3f=0, ln_dynadv_vec=1, ln_sco=0, ln_apr_dyn=0, rn_scal_load=0.0,
-        grav=GRAV, rau0=RAU0, nn_fct_h=2, nn_fct_v=2)
+        grav=GRAV, rau0=RAU0, nn_fct_h=2, nn_fct_v=2, rn_slpmax=0.01)
     nam.update(over)
     return nam
 
@@ -290,3 +290,35 @@ def zstar(dom, st, ssha=None):
                 e3f_n=to_f(e3u_n), ht_n=f((e3t_n * tm)[:, :, :-1].sum(axis=2)),
                 hu_n=hu_n, hv_n=hv_n, r1_hu_n=inv(hu_n, ssumask), r1_hv_n=inv(hv_n, ssvmask),
                 hu_b=hu_b, hv_b=hv_b, r1_hu_b=inv(hu_b, ssumask), r1_hv_b=inv(hv_b, ssvmask))
+
+
+def slope_inputs(dom, nam, st, rho_c=0.01):
+    """Inputs of ldf_slp from a state: the in situ density anomaly of a linear
+    equation of state (rn_a0 = 1.655e-1, rn_b0 = 7.6554e-1 of eosbn2's linear case),
+    N^2 from it, the mixed layer of zdf_mxl (zdfmxl.F90:92-122, rho_c = 0.01) and the
+    rest-state depths of the T- and W-points."""
+    jpi, jpj, jpk = dom["jpi"], dom["jpj"], dom["jpk"]
+    tm, _, _, wm = masks(dom)
+    ts = st["tsn"]
+    rhd = (-1.655e-1 * (ts[..., 0] - 10.0) + 7.6554e-1 * (ts[..., 1] - 35.0)) / nam["rau0"] * tm
+    e3t, e3w = dom["e3t_0"], dom["e3w_0"]
+    rn2 = np.zeros_like(rhd)
+    rn2[:, :, 1:-1] = nam["grav"] * (rhd[:, :, 1:-1] - rhd[:, :, :-2]) / e3w[:, :, 1:-1] * wm[:, :, 1:-1]
+    gdepw = np.zeros_like(e3t)
+    gdepw[:, :, 1:] = np.cumsum(e3t[:, :, :-1], axis=2)
+    gdept = gdepw + 0.5 * e3t if "gdept_1d" not in dom else np.broadcast_to(dom["gdept_1d"], e3t.shape).copy()
+    n2c = nam["grav"] * rho_c / nam["rau0"]
+    nlb10 = 1 + int((gdepw[1, 1, :] < 10.0).sum())          # 1-based level below 10 m
+    mbkt = dom["k_bot"]
+    nmln = np.full((jpi, jpj), nlb10, dtype=np.int32)
+    h = np.zeros((jpi, jpj))
+    for jk in range(nlb10, jpk):                            # 1-based jk = nlb10 .. jpk-1
+        h += np.maximum(rn2[:, :, jk - 1], 0.0) * e3w[:, :, jk - 1]
+        nmln = np.where(h < n2c, np.minimum(jk, mbkt) + 1, nmln).astype(np.int32)
+    ssm = tm.max(axis=2)
+    ii, jj = np.meshgrid(np.arange(jpi), np.arange(jpj), indexing="ij")
+    hmlp = gdepw[ii, jj, nmln - 1] * ssm
+    hmlpt = gdept[ii, jj, np.maximum(nmln - 2, 0)] * ssm
+    f = np.asfortranarray
+    return dict(rhd=f(rhd), rn2b=f(rn2), nmln=f(nmln.astype(np.int32)), hmlp=f(hmlp), hmlpt=f(hmlpt),
+                gdept_n=f(gdept), gdepw_n=f(gdepw))

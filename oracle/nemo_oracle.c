@@ -2212,3 +2212,187 @@ int ora_stp_model(ora_ctx *c, int kt) {
   if (!st) st = ora_ssh_swp(c, kt);
   return st;
 }
+
+/* ---------------------------------------------------------------- ldf_slp */
+/* ldf_slp (ldfslp.F90:83-374) with ldf_slp_mxl (:620-729): z-coordinate without
+ * ice-shelf cavities (risfdep = 0, mikt = miku = mikv = 1), without partial steps
+ * and without the s-coordinate level slope. prd, pn2: in situ density anomaly and
+ * N^2; bound: GDEPT_N, GDEPW_N, NMLN (int), HMLP, HMLPT; out: USLP, VSLP, WSLPI,
+ * WSLPJ on levels 2..jpk-1 of the interior, then lbc_lnk on every level. */
+int ora_ldf_slp(ora_ctx *c, int kt, const double *prd, const double *pn2) {
+  (void)kt;
+  const nemo_namelist *nm = &c->nam;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  double *uslp = c->f[NEMO_F_USLP], *vslp = c->f[NEMO_F_VSLP], *wslpi = c->f[NEMO_F_WSLPI], *wslpj = c->f[NEMO_F_WSLPJ];
+  const double *gdept = c->f[NEMO_F_GDEPT_N], *gdepw = c->f[NEMO_F_GDEPW_N];
+  const double *hmlp = c->f[NEMO_F_HMLP], *hmlpt = c->f[NEMO_F_HMLPT];
+  const int *nmln = (const int *)c->f[NEMO_F_NMLN];
+  if (!prd || !pn2) return NEMO_ERR_ARG;
+  if (!uslp || !vslp || !wslpi || !wslpj || !gdept || !gdepw || !hmlp || !hmlpt || !nmln) return NEMO_ERR_UNBOUND;
+  if (nm->ln_zps || nm->ln_isfcav || nm->ln_sco) return NEMO_ERR_UNSUPPORTED;
+  const double *tmask = c->tmask, *umask = c->umask, *vmask = c->vmask, *wmask = c->wmask;
+  const double *e3u = fld(c, NEMO_F_E3U_N), *e3v = fld(c, NEMO_F_E3V_N), *e3w = fld(c, NEMO_F_E3W_N);
+  const double zeps = 1.e-20, z1_16 = 1.0 / 16., zm1_g = -1.0 / nm->grav, zm1_2g = -0.5 / nm->grav;
+  const double z1_slpmax = 1. / (nm->rn_slpmax > 0 ? nm->rn_slpmax : 0.01);
+  double *zgru = walloc(n3), *zgrv = walloc(n3), *zdzr = walloc(n3);
+  double *zwz = zalloc(n3), *zww = zalloc(n3);
+  double *uml = zalloc(n2), *vml = zalloc(n2), *wiml = zalloc(n2), *wjml = zalloc(n2);
+  double *hu = zalloc(n2), *hv = zalloc(n2);
+#define OML(ji, jj, jk) ((jk) <= nmln[I2(ji, jj)] - 1 ? 1.0 : 0.0)
+  /* (:136-143) */
+  for (int jk = 1; jk <= jpk; ++jk)
+    for (int jj = 1; jj <= jpj - 1; ++jj)
+      for (int ji = 1; ji <= jpi - 1; ++ji) {
+        size_t q = I3(ji, jj, jk);
+        zgru[q] = umask[q] * (prd[I3(ji + 1, jj, jk)] - prd[q]);
+        zgrv[q] = vmask[q] * (prd[I3(ji, jj + 1, jk)] - prd[q]);
+      }
+  /* (:161-171) */
+  for (size_t p = 0; p < n2; ++p) zdzr[p] = 0.0;
+  for (int jk = 2; jk <= jpk - 1; ++jk)
+    for (size_t p = 0; p < n2; ++p) {
+      size_t q = p + n2 * (jk - 1);
+      zdzr[q] = zm1_g * (prd[q] + 1.0) * (pn2[q] + pn2[q + n2]) * (1.0 - 0.5 * tmask[q + n2]);
+    }
+  /* ldf_slp_mxl (:660-726) */
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      size_t p = I2(ji, jj);
+      int n0 = nmln[p], ne = nmln[I2(ji + 1, jj)], nn_ = nmln[I2(ji, jj + 1)];
+      int iku = n0 > ne ? n0 : ne; if (iku < 1) iku = 1; if (iku > jpk - 1) iku = jpk - 1;
+      int ikv = n0 > nn_ ? n0 : nn_; if (ikv < 1) ikv = 1; if (ikv > jpk - 1) ikv = jpk - 1;
+      double zbu = 0.5 * (zdzr[I3(ji, jj, iku)] + zdzr[I3(ji + 1, jj, iku)]);
+      double zbv = 0.5 * (zdzr[I3(ji, jj, ikv)] + zdzr[I3(ji, jj + 1, ikv)]);
+      double zau = zgru[I3(ji, jj, iku)] * c->r1_e1u[p];
+      double zav = zgrv[I3(ji, jj, ikv)] * c->r1_e2v[p];
+      zbu = dmin(dmin(zbu, -z1_slpmax * fabs(zau)), -7.e+3 / e3u[I3(ji, jj, iku)] * fabs(zau));
+      zbv = dmin(dmin(zbv, -z1_slpmax * fabs(zav)), -7.e+3 / e3v[I3(ji, jj, ikv)] * fabs(zav));
+      uml[p] = zau / (zbu - zeps) * umask[I3(ji, jj, iku)];
+      vml[p] = zav / (zbv - zeps) * vmask[I3(ji, jj, ikv)];
+      int ik = n0 + 1 < jpk ? n0 + 1 : jpk;
+      int ikm1 = ik - 1 > 1 ? ik - 1 : 1;
+      double zbw = zm1_2g * pn2[I3(ji, jj, ik)] * (prd[I3(ji, jj, ik)] + prd[I3(ji, jj, ikm1)] + 2.);
+      double zci = dmax(umask[I3(ji - 1, jj, ik)] + umask[I3(ji, jj, ik)] + umask[I3(ji - 1, jj, ikm1)]
+                        + umask[I3(ji, jj, ikm1)], zeps) * c->e1t[p];
+      double zcj = dmax(vmask[I3(ji, jj - 1, ik)] + vmask[I3(ji, jj, ik)] + vmask[I3(ji, jj - 1, ikm1)]
+                        + vmask[I3(ji, jj, ikm1)], zeps) * c->e2t[p];
+      double zai = (zgru[I3(ji - 1, jj, ik)] + zgru[I3(ji, jj, ik)] + zgru[I3(ji - 1, jj, ikm1)]
+                    + zgru[I3(ji, jj, ikm1)]) / zci * tmask[I3(ji, jj, ik)];
+      double zaj = (zgrv[I3(ji, jj - 1, ik)] + zgrv[I3(ji, jj, ik)] + zgrv[I3(ji, jj - 1, ikm1)]
+                    + zgrv[I3(ji, jj, ikm1)]) / zcj * tmask[I3(ji, jj, ik)];
+      double zbi = dmin(dmin(zbw, -100. * fabs(zai)), -7.e+3 / e3w[I3(ji, jj, ik)] * fabs(zai));
+      double zbj = dmin(dmin(zbw, -100. * fabs(zaj)), -7.e+3 / e3w[I3(ji, jj, ik)] * fabs(zaj));
+      wiml[p] = zai / (zbi - zeps) * tmask[I3(ji, jj, ik)];
+      wjml[p] = zaj / (zbj - zeps) * tmask[I3(ji, jj, ik)];
+    }
+  lbc_closed(jpi, jpj, uml, 1, 'U', 0.0); lbc_closed(jpi, jpj, vml, 1, 'V', 0.0);
+  lbc_closed(jpi, jpj, wiml, 1, 'W', 0.0); lbc_closed(jpi, jpj, wjml, 1, 'W', 0.0);
+  /* (:188-194) */
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      size_t p = I2(ji, jj);
+      hu[p] = uml[p] / dmax(dmax(hmlpt[p], hmlpt[I2(ji + 1, jj)]), 5.0);
+      hv[p] = vml[p] / dmax(dmax(hmlpt[p], hmlpt[I2(ji, jj + 1)]), 5.0);
+    }
+  /* (:197-233) slopes at u- and v-points */
+  for (int jk = 2; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t p = I2(ji, jj), q = I3(ji, jj, jk);
+        double zau = zgru[q] * c->r1_e1u[p];
+        double zav = zgrv[q] * c->r1_e2v[p];
+        double zbu = 0.5 * (zdzr[q] + zdzr[I3(ji + 1, jj, jk)]);
+        double zbv = 0.5 * (zdzr[q] + zdzr[I3(ji, jj + 1, jk)]);
+        zbu = dmin(dmin(zbu, -z1_slpmax * fabs(zau)), -7.e+3 / e3u[q] * fabs(zau));
+        zbv = dmin(dmin(zbv, -z1_slpmax * fabs(zav)), -7.e+3 / e3v[q] * fabs(zav));
+        double zfi = dmax(OML(ji, jj, jk), OML(ji + 1, jj, jk));
+        double zfj = dmax(OML(ji, jj, jk), OML(ji, jj + 1, jk));
+        double zdepu = 0.5 * ((gdept[q] + gdept[I3(ji + 1, jj, jk)]) - 2 * 0.0 - e3u[I3(ji, jj, 1)]);
+        double zdepv = 0.5 * ((gdept[q] + gdept[I3(ji, jj + 1, jk)]) - 2 * 0.0 - e3v[I3(ji, jj, 1)]);
+        zwz[q] = ((1. - zfi) * zau / (zbu - zeps) + zfi * zdepu * hu[p]) * umask[q];
+        zww[q] = ((1. - zfj) * zav / (zbv - zeps) + zfj * zdepv * hv[p]) * vmask[q];
+      }
+  lbc_closed(jpi, jpj, zwz, jpk, 'U', 0.0);
+  lbc_closed(jpi, jpj, zww, jpk, 'V', 0.0);
+  /* (:236-275) Shapiro filter, decrease along coastal boundaries */
+  for (int jk = 2; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t q = I3(ji, jj, jk);
+        uslp[q] = z1_16 * (zwz[I3(ji - 1, jj - 1, jk)] + zwz[I3(ji + 1, jj - 1, jk)]
+                           + zwz[I3(ji - 1, jj + 1, jk)] + zwz[I3(ji + 1, jj + 1, jk)]
+                           + 2. * (zwz[I3(ji, jj - 1, jk)] + zwz[I3(ji - 1, jj, jk)]
+                                   + zwz[I3(ji + 1, jj, jk)] + zwz[I3(ji, jj + 1, jk)])
+                           + 4. * zwz[q]);
+        vslp[q] = z1_16 * (zww[I3(ji - 1, jj - 1, jk)] + zww[I3(ji + 1, jj - 1, jk)]
+                           + zww[I3(ji - 1, jj + 1, jk)] + zww[I3(ji + 1, jj + 1, jk)]
+                           + 2. * (zww[I3(ji, jj - 1, jk)] + zww[I3(ji - 1, jj, jk)]
+                                   + zww[I3(ji + 1, jj, jk)] + zww[I3(ji, jj + 1, jk)])
+                           + 4. * zww[q]);
+      }
+  for (int jk = 2; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t q = I3(ji, jj, jk);
+        uslp[q] = uslp[q] * (umask[I3(ji, jj + 1, jk)] + umask[I3(ji, jj - 1, jk)]) * 0.5
+                          * (umask[q] + umask[I3(ji, jj, jk + 1)]) * 0.5;
+        vslp[q] = vslp[q] * (vmask[I3(ji + 1, jj, jk)] + vmask[I3(ji - 1, jj, jk)]) * 0.5
+                          * (vmask[q] + vmask[I3(ji, jj, jk + 1)]) * 0.5;
+      }
+  /* (:281-315) slopes at w-points */
+  for (int jk = 2; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t p = I2(ji, jj), q = I3(ji, jj, jk);
+        double zbw = zm1_2g * pn2[q] * (prd[q] + prd[I3(ji, jj, jk - 1)] + 2.);
+        double zci = dmax(umask[I3(ji - 1, jj, jk)] + umask[q] + umask[I3(ji - 1, jj, jk - 1)]
+                          + umask[I3(ji, jj, jk - 1)], zeps) * c->e1t[p];
+        double zcj = dmax(vmask[I3(ji, jj - 1, jk)] + vmask[I3(ji, jj, jk - 1)] + vmask[I3(ji, jj - 1, jk - 1)]
+                          + vmask[q], zeps) * c->e2t[p];
+        double zai = (zgru[I3(ji - 1, jj, jk)] + zgru[I3(ji, jj, jk - 1)] + zgru[I3(ji - 1, jj, jk - 1)]
+                      + zgru[q]) / zci * wmask[q];
+        double zaj = (zgrv[I3(ji, jj - 1, jk)] + zgrv[I3(ji, jj, jk - 1)] + zgrv[I3(ji, jj - 1, jk - 1)]
+                      + zgrv[q]) / zcj * wmask[q];
+        double zbi = dmin(dmin(zbw, -100. * fabs(zai)), -7.e+3 / e3w[q] * fabs(zai));
+        double zbj = dmin(dmin(zbw, -100. * fabs(zaj)), -7.e+3 / e3w[q] * fabs(zaj));
+        double zfk = dmax(OML(ji, jj, jk), OML(ji, jj, jk - 1));
+        double zck = (gdepw[q] - gdepw[I3(ji, jj, 1)]) / dmax(hmlp[p] - gdepw[I3(ji, jj, 1)], 10.);
+        zwz[q] = (zai / (zbi - zeps) * (1. - zfk) + zck * wiml[p] * zfk) * wmask[q];
+        zww[q] = (zaj / (zbj - zeps) * (1. - zfk) + zck * wjml[p] * zfk) * wmask[q];
+      }
+  lbc_closed(jpi, jpj, zwz, jpk, 'T', 0.0);
+  lbc_closed(jpi, jpj, zww, jpk, 'T', 0.0);
+  /* (:318-361) */
+  for (int jk = 2; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t q = I3(ji, jj, jk);
+        double zcofw = wmask[q] * z1_16;
+        wslpi[q] = (zwz[I3(ji - 1, jj - 1, jk)] + zwz[I3(ji + 1, jj - 1, jk)]
+                    + zwz[I3(ji - 1, jj + 1, jk)] + zwz[I3(ji + 1, jj + 1, jk)]
+                    + 2. * (zwz[I3(ji, jj - 1, jk)] + zwz[I3(ji - 1, jj, jk)]
+                            + zwz[I3(ji + 1, jj, jk)] + zwz[I3(ji, jj + 1, jk)])
+                    + 4. * zwz[q]) * zcofw;
+        wslpj[q] = (zww[I3(ji - 1, jj - 1, jk)] + zww[I3(ji + 1, jj - 1, jk)]
+                    + zww[I3(ji - 1, jj + 1, jk)] + zww[I3(ji + 1, jj + 1, jk)]
+                    + 2. * (zww[I3(ji, jj - 1, jk)] + zww[I3(ji - 1, jj, jk)]
+                            + zww[I3(ji + 1, jj, jk)] + zww[I3(ji, jj + 1, jk)])
+                    + 4. * zww[q]) * zcofw;
+      }
+  for (int jk = 2; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        size_t q = I3(ji, jj, jk);
+        double zck = (umask[q] + umask[I3(ji - 1, jj, jk)]) * (vmask[q] + vmask[I3(ji, jj - 1, jk)]) * 0.25;
+        wslpi[q] = wslpi[q] * zck;
+        wslpj[q] = wslpj[q] * zck;
+      }
+  /* (:365) */
+  lbc_closed(jpi, jpj, uslp, jpk, 'U', 0.0); lbc_closed(jpi, jpj, vslp, jpk, 'V', 0.0);
+  lbc_closed(jpi, jpj, wslpi, jpk, 'W', 0.0); lbc_closed(jpi, jpj, wslpj, jpk, 'W', 0.0);
+#undef OML
+  free(zgru); free(zgrv); free(zdzr); free(zwz); free(zww);
+  free(uml); free(vml); free(wiml); free(wjml); free(hu); free(hv);
+  return NEMO_OK;
+}

@@ -86,6 +86,9 @@ int ora_dyn_zdf_step(ora_ctx *c, int kt);
 int ora_dyn_nxt(ora_ctx *c, int kt);
 int ora_ssh_swp(ora_ctx *c, int kt);
 int ora_stp_model(ora_ctx *c, int kt);
+/* ldf_slp with ldf_slp_mxl (z-coordinate, no cavities, no partial steps); NMLN is
+ * bound as an int array. */
+int ora_ldf_slp(ora_ctx *c, int kt, const double *prd, const double *pn2);
 /* 1: start the work arrays standing for Fortran automatic arrays as NaN */
 void ora_set_poison(int on);
 

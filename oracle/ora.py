@@ -52,6 +52,7 @@ def lib():
         P("ora_tra_nxt_adj", [vp, i, vp, vp, vp])
         for name in ("ora_wzv", "ora_dyn_zdf_step", "ora_dyn_nxt", "ora_ssh_swp", "ora_stp_model"):
             P(name, [vp, i])
+        P("ora_ldf_slp", [vp, i, vp, vp])
         _lib = L
     return _lib
 
@@ -92,9 +93,14 @@ class Oracle:
         self.close()
 
     def bind(self, name, arr):
-        """Bind a float64 Fortran-order array to a module-global field (kept alive here)."""
+        """Bind a float64 Fortran-order array to a module-global field (kept alive here);
+        NMLN, the mixed-layer level, is an int32 array."""
         self.bound[name] = arr
-        st = lib().ora_bind(self.h, _ffi.F[name], _p(arr))
+        if name == "NMLN":
+            assert arr.dtype == np.int32 and arr.flags.f_contiguous
+            st = lib().ora_bind(self.h, _ffi.F[name], arr.ctypes.data)
+        else:
+            st = lib().ora_bind(self.h, _ffi.F[name], _p(arr))
         assert st == 0
 
     def spg_info(self):
@@ -213,3 +219,6 @@ class Oracle:
 
     def stp_model(self, kt):
         self._ck(lib().ora_stp_model(self.h, kt), "stp_model")
+
+    def ldf_slp(self, kt, prd, pn2):
+        self._ck(lib().ora_ldf_slp(self.h, kt, _p(prd), _p(pn2)), "ldf_slp")
