@@ -256,6 +256,16 @@ int nemo_gpu_tra_ldf_iso(nemo_ctx *ctx, int kt, int kit000, const char *cdtype,
                          const void *pgu, const void *pgv, const void *pgui, const void *pgvi,
                          const void *ptb, const void *ptbb, void *pta, int kjpt, int kpass);
 
+/* tra_ldf_blp (traldf_lap_blp.F90:161-231): the bilaplacian as two passes of the
+ * laplacian, kldf = 20 (np_blp: iso-level, tra_ldf_lap) or 21 (np_blp_i: rotated,
+ * tra_ldf_iso), with lbc_lnk of the first laplacian in between. Without partial
+ * steps (the zps_hde of the first laplacian is not implemented: NEMO_ERR_UNSUPPORTED
+ * with ln_zps), and without the triad operator (kldf = 22). nemo_gpu_stp_hotpath
+ * calls it when ln_traldf_blp is set (traldf.F90:75-76). */
+int nemo_gpu_tra_ldf_blp(nemo_ctx *ctx, int kt, int kit000, const char *cdtype, const void *pahu,
+                         const void *pahv, const void *pgu, const void *pgv, const void *pgui,
+                         const void *pgvi, const void *ptb, void *pta, int kjpt, int kldf);
+
 /* tra_zdf_imp (trazdf.F90:109-268): pta becomes the after tracer. Reads the bound
  * avt (avs), and ah_wslp2/akz when ln_traldf_iso. */
 int nemo_gpu_tra_zdf_imp(nemo_ctx *ctx, int kt, int kit000, const char *cdtype, double p2dt,

@@ -76,6 +76,8 @@ struct nemo_ctx {
   void* adj_w[4] = {};         // iso-neutral adjoint: G and the gradient adjoints
   int adj_kjpt = 0;
   void* slp_w = nullptr;       // ldf_slp work: 4 3-D and 6 2-D arrays per member
+  void* blp_w = nullptr;       // tra_ldf_blp: the first laplacian (jpi,jpj,jpk,kjpt) per member
+  int blp_kjpt = 0;
   int iso_kjpt = 0;
   int fct_kjpt = 0;
   void* spg_w[5] = {};
@@ -717,6 +719,29 @@ int run_ldf_iso(nemo_ctx* c, int kt, int kit000, const void* pahu, const void* p
   return NEMO_OK;
 }
 
+// tra_ldf_blp (traldf_lap_blp.F90:161-231) without partial steps: the first
+// laplacian (kldf 20 iso-level, 21 rotated) of ptb into zlap, lbc_lnk, the second of
+// zlap into pta
+template <class T>
+int run_ldf_blp(nemo_ctx* c, int kt, int kit000, const void* pahu, const void* pahv, const void* ptb, void* pta,
+                int kjpt, int kldf) {
+  const size_t bytes = (size_t)kjpt * c->n3 * c->nmem * sizeof(T);
+  if (kjpt > c->blp_kjpt) {
+    cudaFree(c->blp_w);
+    c->blp_w = nullptr;
+    if (cudaMalloc(&c->blp_w, bytes) != cudaSuccess) return fail(c, NEMO_ERR_NOMEM, "tra_ldf_blp work array");
+    c->blp_kjpt = kjpt;
+  }
+  CK(cudaMemsetAsync(c->blp_w, 0, bytes, c->stream), "zlap = 0");
+  int s = kldf == 20 ? run_ldf_lap<T>(c, pahu, pahv, nullptr, nullptr, ptb, c->blp_w, kjpt, 1)
+                     : run_ldf_iso<T>(c, kt, kit000, pahu, pahv, nullptr, nullptr, ptb, ptb, c->blp_w, kjpt, 1);
+  if (s) return s;
+  cudaError_t e = launch_lbc<T>((T*)c->blp_w, c->jpi, c->jpj, (long)c->jpk * kjpt * c->nmem, 0, T(0), c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "tra_ldf_blp lbc");
+  return kldf == 20 ? run_ldf_lap<T>(c, pahu, pahv, nullptr, nullptr, c->blp_w, pta, kjpt, 2)
+                    : run_ldf_iso<T>(c, kt, kit000, pahu, pahv, nullptr, nullptr, c->blp_w, ptb, pta, kjpt, 2);
+}
+
 template <class T>
 int run_zdf(nemo_ctx* c, double p2dt, const void* ptb, void* pta, int kjpt, int is_trc, int clamp) {
   const nemo_namelist& nm = c->nam;
@@ -962,7 +987,7 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
   if (staged)  // the iso-neutral coefficients the first pass may zero on this stream
     if (wait_field(c, c->stream, NEMO_F_AH_WSLP2, true) || wait_field(c, c->stream, NEMO_F_AKZ, true))
       return NEMO_ERR_CUDA;
-  const bool fused = nm.ln_traldf_iso && !c->no_fusion;
+  const bool fused = nm.ln_traldf_iso && !nm.ln_traldf_blp && !c->no_fusion;
   LdfArgs<T> la{};
   // The iso-neutral fluxes read tsb and the slopes only, and dyn_spg_ts touches
   // neither them nor their outputs: outside per-kernel timing they run on the side
@@ -1018,7 +1043,10 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
                  F[NEMO_F_TSA], 2, fct_h, fct_v);
   if (s) return s;
   mark(2);
-  if (nm.ln_traldf_iso)
+  if (nm.ln_traldf_blp)  // traldf.F90:75-76
+    s = run_ldf_blp<T>(c, kt, nm.nit000, F[NEMO_F_AHTU], F[NEMO_F_AHTV], F[NEMO_F_TSB], F[NEMO_F_TSA], 2,
+                       nm.ln_traldf_iso ? 21 : 20);
+  else if (nm.ln_traldf_iso)
     s = run_ldf_iso<T>(c, kt, nm.nit000, F[NEMO_F_AHTU], F[NEMO_F_AHTV], F[NEMO_F_GTSU], F[NEMO_F_GTSV], F[NEMO_F_TSB],
                        F[NEMO_F_TSB], F[NEMO_F_TSA], 2, 1);
   else
@@ -1181,6 +1209,7 @@ int nemo_gpu_destroy(nemo_ctx* c) {
   for (auto p : c->iso_w) cudaFree(p);
   for (auto p : c->adj_w) cudaFree(p);
   cudaFree(c->slp_w);
+  cudaFree(c->blp_w);
   for (auto p : c->spg_w) cudaFree(p);
   for (auto p : c->spg_cor) cudaFree(p);
   for (auto p : c->ring) cudaFree(p);
@@ -1356,6 +1385,22 @@ int nemo_gpu_tra_ldf_iso(nemo_ctx* c, int kt, int kit000, const char* cdtype, co
   return c->prec == NEMO_PREC_FP64
              ? run_ldf_iso<double>(c, kt, kit000, pahu, pahv, pgu, pgv, ptb, ptbb, pta, kjpt, kpass)
              : run_ldf_iso<float>(c, kt, kit000, pahu, pahv, pgu, pgv, ptb, ptbb, pta, kjpt, kpass);
+}
+
+int nemo_gpu_tra_ldf_blp(nemo_ctx* c, int kt, int kit000, const char* cdtype, const void* pahu, const void* pahv,
+                         const void* pgu, const void* pgv, const void* pgui, const void* pgvi, const void* ptb,
+                         void* pta, int kjpt, int kldf) {
+  (void)pgu; (void)pgv; (void)pgui; (void)pgvi;
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  int is_trc = 0;
+  if (int s = check_cdtype(c, cdtype, &is_trc)) return s;
+  if (!ptb || !pta || kjpt < 1) return fail(c, NEMO_ERR_ARG, "tra_ldf_blp: bad argument");
+  if (kldf != 20 && kldf != 21)
+    return fail(c, NEMO_ERR_UNSUPPORTED, "tra_ldf_blp: kldf 20 (iso-level) or 21 (rotated) only");
+  if (c->nam.ln_zps) return fail(c, NEMO_ERR_UNSUPPORTED, "tra_ldf_blp: partial steps need zps_hde of the laplacian");
+  return c->prec == NEMO_PREC_FP64 ? run_ldf_blp<double>(c, kt, kit000, pahu, pahv, ptb, pta, kjpt, kldf)
+                                   : run_ldf_blp<float>(c, kt, kit000, pahu, pahv, ptb, pta, kjpt, kldf);
 }
 
 int nemo_gpu_tra_zdf_imp(nemo_ctx* c, int kt, int kit000, const char* cdtype, double p2dt, const void* ptb, void* pta,

@@ -187,6 +187,10 @@ class Context:
         self._ck(self.lib.nemo_gpu_tra_ldf_iso(self.h, kt, kit000, cdtype.encode(), *map(_ptr, (
             pahu, pahv, pgu, pgv, pgui, pgvi, ptb, ptbb, pta)), kjpt, kpass), "tra_ldf_iso")
 
+    def tra_ldf_blp(self, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb, pta, kjpt, kldf):
+        self._ck(self.lib.nemo_gpu_tra_ldf_blp(self.h, kt, kit000, cdtype.encode(), *map(_ptr, (
+            pahu, pahv, pgu, pgv, pgui, pgvi, ptb, pta)), kjpt, kldf), "tra_ldf_blp")
+
     def tra_zdf_imp(self, kt, kit000, cdtype, p2dt, ptb, pta, kjpt):
         self._ck(self.lib.nemo_gpu_tra_zdf_imp(self.h, kt, kit000, cdtype.encode(), p2dt, _ptr(ptb), _ptr(pta), kjpt),
                  "tra_zdf_imp")

@@ -1583,6 +1583,29 @@ int ora_glob_sum(ora_ctx *c, const double *ptab, int nk, double *out) {
 /* ---------------------------------------------------------- one hot-path step */
 /* step.F90:194-257 on the bound fields: dyn_spg_ts, tsa = 0, tra_adv (transports
  * + FCT), tra_ldf (iso or lap), tra_zdf. FCT orders from nn_fct_h/v (0 = 2). */
+/* tra_ldf_blp (traldf_lap_blp.F90:161-231) without partial steps: the first
+ * laplacian (kldf 20 iso-level, 21 rotated) of ptb into zlap, lbc_lnk, the second of
+ * zlap into pta. */
+int ora_tra_ldf_blp(ora_ctx *c, int kt, int kit000, const char *cdtype,
+                    const double *pahu, const double *pahv,
+                    const double *pgu, const double *pgv, const double *pgui, const double *pgvi,
+                    const double *ptb, double *pta, int kjpt, int kldf) {
+  (void)pgu; (void)pgv;
+  if (kldf != 20 && kldf != 21) return NEMO_ERR_UNSUPPORTED;
+  if (c->nam.ln_zps) return NEMO_ERR_UNSUPPORTED;
+  const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk;
+  double *zlap = zalloc(n3 * (size_t)kjpt);
+  int st = kldf == 20 ? ora_tra_ldf_lap(c, kt, kit000, cdtype, pahu, pahv, NULL, NULL, pgui, pgvi, ptb, zlap, kjpt, 1)
+                      : ora_tra_ldf_iso(c, kt, kit000, cdtype, pahu, pahv, NULL, NULL, pgui, pgvi, ptb, ptb, zlap, kjpt, 1);
+  if (!st) {
+    lbc_closed(c->jpi, c->jpj, zlap, c->jpk * kjpt, 'T', 0.0);
+    st = kldf == 20 ? ora_tra_ldf_lap(c, kt, kit000, cdtype, pahu, pahv, NULL, NULL, NULL, NULL, zlap, pta, kjpt, 2)
+                    : ora_tra_ldf_iso(c, kt, kit000, cdtype, pahu, pahv, NULL, NULL, NULL, NULL, zlap, ptb, pta, kjpt, 2);
+  }
+  free(zlap);
+  return st;
+}
+
 /* The tracer part of the step: tsa = 0, tra_adv (transports + FCT), tra_ldf, tra_zdf. */
 static int stp_tracers(ora_ctx *c, int kt) {
   const nemo_namelist *nm = &c->nam;
@@ -1598,7 +1621,10 @@ static int stp_tracers(ora_ctx *c, int kt) {
   free(zun); free(zvn); free(zwn);
   if (st) return st;
   const double *ahtu = c->f[NEMO_F_AHTU], *ahtv = c->f[NEMO_F_AHTV];
-  if (nm->ln_traldf_iso)
+  if (nm->ln_traldf_blp)   /* traldf.F90:75-76 */
+    st = ora_tra_ldf_blp(c, kt, nm->nit000, "TRA", ahtu, ahtv, c->f[NEMO_F_GTSU], c->f[NEMO_F_GTSV],
+                         c->f[NEMO_F_GTUI], c->f[NEMO_F_GTVI], tsb, tsa, 2, nm->ln_traldf_iso ? 21 : 20);
+  else if (nm->ln_traldf_iso)
     st = ora_tra_ldf_iso(c, kt, nm->nit000, "TRA", ahtu, ahtv, c->f[NEMO_F_GTSU], c->f[NEMO_F_GTSV],
                          c->f[NEMO_F_GTUI], c->f[NEMO_F_GTVI], tsb, tsb, tsa, 2, 1);
   else

@@ -52,6 +52,10 @@ int ora_tra_ldf_iso(ora_ctx *c, int kt, int kit000, const char *cdtype,
                     const double *pahu, const double *pahv,
                     const double *pgu, const double *pgv, const double *pgui, const double *pgvi,
                     const double *ptb, const double *ptbb, double *pta, int kjpt, int kpass);
+int ora_tra_ldf_blp(ora_ctx *c, int kt, int kit000, const char *cdtype,
+                    const double *pahu, const double *pahv,
+                    const double *pgu, const double *pgv, const double *pgui, const double *pgvi,
+                    const double *ptb, double *pta, int kjpt, int kldf);
 int ora_tra_zdf_imp(ora_ctx *c, int kt, int kit000, const char *cdtype, double p2dt,
                     const double *ptb, double *pta, int kjpt);
 int ora_tra_zdf(ora_ctx *c, int kt);

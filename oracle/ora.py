@@ -53,6 +53,7 @@ def lib():
         for name in ("ora_wzv", "ora_dyn_zdf_step", "ora_dyn_nxt", "ora_ssh_swp", "ora_stp_model"):
             P(name, [vp, i])
         P("ora_ldf_slp", [vp, i, vp, vp])
+        P("ora_tra_ldf_blp", [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
         _lib = L
     return _lib
 
@@ -222,3 +223,7 @@ class Oracle:
 
     def ldf_slp(self, kt, prd, pn2):
         self._ck(lib().ora_ldf_slp(self.h, kt, _p(prd), _p(pn2)), "ldf_slp")
+
+    def tra_ldf_blp(self, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb, pta, kjpt, kldf):
+        self._ck(lib().ora_tra_ldf_blp(self.h, kt, kit000, cdtype.encode(), _p(pahu), _p(pahv), _p(pgu), _p(pgv),
+                                       _p(pgui), _p(pgvi), _p(ptb), _p(pta), kjpt, kldf), "tra_ldf_blp")
