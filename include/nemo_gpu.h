@@ -256,12 +256,18 @@ int nemo_gpu_tra_ldf_iso(nemo_ctx *ctx, int kt, int kit000, const char *cdtype,
                          const void *pgu, const void *pgv, const void *pgui, const void *pgvi,
                          const void *ptb, const void *ptbb, void *pta, int kjpt, int kpass);
 
+/* zps_hde (zpshde.F90:41-148): pgtu, pgtv (jpi,jpj,kjpt) = the horizontal
+ * gradients of pta (jpi,jpj,jpk,kjpt) at the partial-step bottom level of the u-
+ * and v-points, with lbc_lnk. The optional density part (prd, pgru, pgrv) needs
+ * eos and is not implemented. */
+int nemo_gpu_zps_hde(nemo_ctx *ctx, int kt, int kjpt, const void *pta, void *pgtu, void *pgtv);
+
 /* tra_ldf_blp (traldf_lap_blp.F90:161-231): the bilaplacian as two passes of the
  * laplacian, kldf = 20 (np_blp: iso-level, tra_ldf_lap) or 21 (np_blp_i: rotated,
- * tra_ldf_iso), with lbc_lnk of the first laplacian in between. Without partial
- * steps (the zps_hde of the first laplacian is not implemented: NEMO_ERR_UNSUPPORTED
- * with ln_zps), and without the triad operator (kldf = 22). nemo_gpu_stp_hotpath
- * calls it when ln_traldf_blp is set (traldf.F90:75-76). */
+ * tra_ldf_iso), with lbc_lnk of the first laplacian and, with ln_zps, its zps_hde
+ * gradients in between (pgu/pgv, the gradients of ptb, are then required). Not the
+ * triad operator (kldf = 22). nemo_gpu_stp_hotpath calls it when ln_traldf_blp is
+ * set (traldf.F90:75-76). */
 int nemo_gpu_tra_ldf_blp(nemo_ctx *ctx, int kt, int kit000, const char *cdtype, const void *pahu,
                          const void *pahv, const void *pgu, const void *pgv, const void *pgui,
                          const void *pgvi, const void *ptb, void *pta, int kjpt, int kldf);
@@ -427,6 +433,7 @@ enum nemo_kernel_id {
   NEMO_K_TRA_NXT, NEMO_K_TRA_NXT_ADJ,
   NEMO_K_WZV, NEMO_K_DYN_ZDF_STEP, NEMO_K_DYN_NXT, NEMO_K_SSH_SWP, /* rest of the model step */
   NEMO_K_LDF_SLP,      /* the three iso-neutral slope kernels */
+  NEMO_K_ZPS_HDE,      /* partial-step bottom gradients */
   NEMO_K_COUNT
 };
 

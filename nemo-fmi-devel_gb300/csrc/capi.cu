@@ -723,23 +723,32 @@ int run_ldf_iso(nemo_ctx* c, int kt, int kit000, const void* pahu, const void* p
 // laplacian (kldf 20 iso-level, 21 rotated) of ptb into zlap, lbc_lnk, the second of
 // zlap into pta
 template <class T>
-int run_ldf_blp(nemo_ctx* c, int kt, int kit000, const void* pahu, const void* pahv, const void* ptb, void* pta,
-                int kjpt, int kldf) {
-  const size_t bytes = (size_t)kjpt * c->n3 * c->nmem * sizeof(T);
+int run_ldf_blp(nemo_ctx* c, int kt, int kit000, const void* pahu, const void* pahv, const void* pgu,
+                const void* pgv, const void* ptb, void* pta, int kjpt, int kldf) {
+  const size_t n3b = (size_t)kjpt * c->n3 * c->nmem * sizeof(T), n2b = (size_t)kjpt * c->n2 * c->nmem * sizeof(T);
   if (kjpt > c->blp_kjpt) {
     cudaFree(c->blp_w);
     c->blp_w = nullptr;
-    if (cudaMalloc(&c->blp_w, bytes) != cudaSuccess) return fail(c, NEMO_ERR_NOMEM, "tra_ldf_blp work array");
+    if (cudaMalloc(&c->blp_w, n3b + 2 * n2b) != cudaSuccess) return fail(c, NEMO_ERR_NOMEM, "tra_ldf_blp work array");
     c->blp_kjpt = kjpt;
   }
-  CK(cudaMemsetAsync(c->blp_w, 0, bytes, c->stream), "zlap = 0");
-  int s = kldf == 20 ? run_ldf_lap<T>(c, pahu, pahv, nullptr, nullptr, ptb, c->blp_w, kjpt, 1)
-                     : run_ldf_iso<T>(c, kt, kit000, pahu, pahv, nullptr, nullptr, ptb, ptb, c->blp_w, kjpt, 1);
+  T* zlap = (T*)c->blp_w;
+  T* zglu = (T*)((char*)c->blp_w + n3b);
+  T* zglv = (T*)((char*)c->blp_w + n3b + n2b);
+  CK(cudaMemsetAsync(zlap, 0, n3b, c->stream), "zlap = 0");
+  int s = kldf == 20 ? run_ldf_lap<T>(c, pahu, pahv, pgu, pgv, ptb, zlap, kjpt, 1)
+                     : run_ldf_iso<T>(c, kt, kit000, pahu, pahv, pgu, pgv, ptb, ptb, zlap, kjpt, 1);
   if (s) return s;
-  cudaError_t e = launch_lbc<T>((T*)c->blp_w, c->jpi, c->jpj, (long)c->jpk * kjpt * c->nmem, 0, T(0), c->stream);
+  cudaError_t e = launch_lbc<T>(zlap, c->jpi, c->jpj, (long)c->jpk * kjpt * c->nmem, 0, T(0), c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "tra_ldf_blp lbc");
-  return kldf == 20 ? run_ldf_lap<T>(c, pahu, pahv, nullptr, nullptr, c->blp_w, pta, kjpt, 2)
-                    : run_ldf_iso<T>(c, kt, kit000, pahu, pahv, nullptr, nullptr, c->blp_w, ptb, pta, kjpt, 2);
+  const bool zps = c->nam.ln_zps;
+  if (zps) {  // GRADh of the first laplacian at the partial steps
+    e = launch_zps_hde<T>(dom_now<T>(c), zlap, zglu, zglv, kjpt, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "tra_ldf_blp zps_hde");
+  }
+  return kldf == 20 ? run_ldf_lap<T>(c, pahu, pahv, zps ? zglu : nullptr, zps ? zglv : nullptr, zlap, pta, kjpt, 2)
+                    : run_ldf_iso<T>(c, kt, kit000, pahu, pahv, zps ? zglu : nullptr, zps ? zglv : nullptr, zlap, ptb,
+                                     pta, kjpt, 2);
 }
 
 template <class T>
@@ -1044,8 +1053,8 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
   if (s) return s;
   mark(2);
   if (nm.ln_traldf_blp)  // traldf.F90:75-76
-    s = run_ldf_blp<T>(c, kt, nm.nit000, F[NEMO_F_AHTU], F[NEMO_F_AHTV], F[NEMO_F_TSB], F[NEMO_F_TSA], 2,
-                       nm.ln_traldf_iso ? 21 : 20);
+    s = run_ldf_blp<T>(c, kt, nm.nit000, F[NEMO_F_AHTU], F[NEMO_F_AHTV], F[NEMO_F_GTSU], F[NEMO_F_GTSV],
+                       F[NEMO_F_TSB], F[NEMO_F_TSA], 2, nm.ln_traldf_iso ? 21 : 20);
   else if (nm.ln_traldf_iso)
     s = run_ldf_iso<T>(c, kt, nm.nit000, F[NEMO_F_AHTU], F[NEMO_F_AHTV], F[NEMO_F_GTSU], F[NEMO_F_GTSV], F[NEMO_F_TSB],
                        F[NEMO_F_TSB], F[NEMO_F_TSA], 2, 1);
@@ -1390,7 +1399,7 @@ int nemo_gpu_tra_ldf_iso(nemo_ctx* c, int kt, int kit000, const char* cdtype, co
 int nemo_gpu_tra_ldf_blp(nemo_ctx* c, int kt, int kit000, const char* cdtype, const void* pahu, const void* pahv,
                          const void* pgu, const void* pgv, const void* pgui, const void* pgvi, const void* ptb,
                          void* pta, int kjpt, int kldf) {
-  (void)pgu; (void)pgv; (void)pgui; (void)pgvi;
+  (void)pgui; (void)pgvi;
   if (!c) return NEMO_ERR_ARG;
   if (join_copies(c)) return NEMO_ERR_CUDA;
   int is_trc = 0;
@@ -1398,9 +1407,23 @@ int nemo_gpu_tra_ldf_blp(nemo_ctx* c, int kt, int kit000, const char* cdtype, co
   if (!ptb || !pta || kjpt < 1) return fail(c, NEMO_ERR_ARG, "tra_ldf_blp: bad argument");
   if (kldf != 20 && kldf != 21)
     return fail(c, NEMO_ERR_UNSUPPORTED, "tra_ldf_blp: kldf 20 (iso-level) or 21 (rotated) only");
-  if (c->nam.ln_zps) return fail(c, NEMO_ERR_UNSUPPORTED, "tra_ldf_blp: partial steps need zps_hde of the laplacian");
-  return c->prec == NEMO_PREC_FP64 ? run_ldf_blp<double>(c, kt, kit000, pahu, pahv, ptb, pta, kjpt, kldf)
-                                   : run_ldf_blp<float>(c, kt, kit000, pahu, pahv, ptb, pta, kjpt, kldf);
+  if (c->nam.ln_zps && (!pgu || !pgv)) return fail(c, NEMO_ERR_ARG, "tra_ldf_blp: pgu/pgv required with ln_zps");
+  return c->prec == NEMO_PREC_FP64 ? run_ldf_blp<double>(c, kt, kit000, pahu, pahv, pgu, pgv, ptb, pta, kjpt, kldf)
+                                   : run_ldf_blp<float>(c, kt, kit000, pahu, pahv, pgu, pgv, ptb, pta, kjpt, kldf);
+}
+
+int nemo_gpu_zps_hde(nemo_ctx* c, int kt, int kjpt, const void* pta, void* pgtu, void* pgtv) {
+  (void)kt;
+  if (!c) return NEMO_ERR_ARG;
+  if (!pta || !pgtu || !pgtv || kjpt < 1) return fail(c, NEMO_ERR_ARG, "zps_hde: bad argument");
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  cudaError_t e = c->prec == NEMO_PREC_FP64
+                      ? launch_zps_hde<double>(dom_now<double>(c), (const double*)pta, (double*)pgtu, (double*)pgtv,
+                                               kjpt, c->stream)
+                      : launch_zps_hde<float>(dom_now<float>(c), (const float*)pta, (float*)pgtu, (float*)pgtv, kjpt,
+                                              c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "zps_hde launch");
+  return NEMO_OK;
 }
 
 int nemo_gpu_tra_zdf_imp(nemo_ctx* c, int kt, int kit000, const char* cdtype, double p2dt, const void* ptb, void* pta,

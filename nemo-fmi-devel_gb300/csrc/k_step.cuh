@@ -308,4 +308,53 @@ __global__ void k_slp_filter(Dom<T> d, SlpArgs<T> a) {
   a.wslpj[o] = wj * zck;
 }
 
+// zps_hde (zpshde.F90:41-148): the horizontal gradients of the tracers at the last
+// ocean level of the u- and v-points (the partial step), each tracer interpolated
+// to the shallower bottom; the loop of the reference covers i <= jpim1, j <= jpjm1
+// and lbc_lnk then zeroes the closed edges, so only the interior is nonzero.
+template <class T>
+__global__ void k_zps_hde(Dom<T> d, RO<T> pta, T* __restrict__ pgtu, T* __restrict__ pgtv, int kjpt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i > d.jpi || j > d.jpj) return;
+  const int m = blockIdx.z, jpi = d.jpi;
+  const long ij = (long)(i - 1) + (long)(j - 1) * jpi, n2 = d.n2, n3 = d.n3;
+  const bool inner = i >= 2 && i <= jpi - 1 && j >= 2 && j <= d.jpj - 1;
+  const ColInfo ci = d.ci[ij];
+  const int iku = ci.mbku, ikum1 = iku - 1 > 1 ? iku - 1 : 1;
+  const int ikv = ci.mbkv, ikvm1 = ikv - 1 > 1 ? ikv - 1 : 1;
+  for (int n = 0; n < kjpt; ++n) {
+    const long g = ((long)m * kjpt + n) * n2 + ij;
+    if (!inner) {
+      pgtu[g] = T(0);
+      pgtv[g] = T(0);
+      continue;
+    }
+    const RO<T> t = pta + ((long)m * kjpt + n) * n3;
+    auto Q = [&](long o, int k) { return o + (long)(k - 1) * d.n2; };
+    const T ze3wu = d.e3w_n(ij + 1, iku, m) - d.e3w_n(ij, iku, m);
+    const T ze3wv = d.e3w_n(ij + jpi, ikv, m) - d.e3w_n(ij, ikv, m);
+    T gu, gv;
+    if (ze3wu >= T(0)) {
+      const T zmaxu = ze3wu / d.e3w_n(ij + 1, iku, m);
+      const T zti = t[Q(ij + 1, iku)] + zmaxu * (t[Q(ij + 1, ikum1)] - t[Q(ij + 1, iku)]);
+      gu = umsk<T>(ci, 1) * (zti - t[Q(ij, iku)]);
+    } else {
+      const T zmaxu = -ze3wu / d.e3w_n(ij, iku, m);
+      const T zti = t[Q(ij, iku)] + zmaxu * (t[Q(ij, ikum1)] - t[Q(ij, iku)]);
+      gu = umsk<T>(ci, 1) * (t[Q(ij + 1, iku)] - zti);
+    }
+    if (ze3wv >= T(0)) {
+      const T zmaxv = ze3wv / d.e3w_n(ij + jpi, ikv, m);
+      const T ztj = t[Q(ij + jpi, ikv)] + zmaxv * (t[Q(ij + jpi, ikvm1)] - t[Q(ij + jpi, ikv)]);
+      gv = vmsk<T>(ci, 1) * (ztj - t[Q(ij, ikv)]);
+    } else {
+      const T zmaxv = -ze3wv / d.e3w_n(ij, ikv, m);
+      const T ztj = t[Q(ij, ikv)] + zmaxv * (t[Q(ij, ikvm1)] - t[Q(ij, ikv)]);
+      gv = vmsk<T>(ci, 1) * (t[Q(ij + jpi, ikv)] - ztj);
+    }
+    pgtu[g] = gu;
+    pgtv[g] = gv;
+  }
+}
+
 }  // namespace nemo

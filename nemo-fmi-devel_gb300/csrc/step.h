@@ -27,6 +27,8 @@ struct SlpArgs {
 };
 
 template <class T>
+cudaError_t launch_zps_hde(const Dom<T>& d, const T* pta, T* pgtu, T* pgtv, int kjpt, cudaStream_t s);
+template <class T>
 cudaError_t launch_ldf_slp(const Dom<T>& d, const SlpArgs<T>& a, cudaStream_t s);
 
 template <class T>

@@ -112,6 +112,7 @@ def load(path):
     _proto(lib, "nemo_gpu_autotune", i, [vp, i, i])
     _proto(lib, "nemo_gpu_ldf_slp", i, [vp, i, vp, vp])
     _proto(lib, "nemo_gpu_tra_ldf_blp", i, [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
+    _proto(lib, "nemo_gpu_zps_hde", i, [vp, i, i, vp, vp, vp])
     _proto(lib, "nemo_gpu_get_launch_shape", i, [vp, _ip, i])
     for name in ("nemo_gpu_wzv", "nemo_gpu_dyn_zdf_step", "nemo_gpu_dyn_nxt", "nemo_gpu_ssh_swp",
                  "nemo_gpu_stp_model"):

@@ -191,6 +191,9 @@ class Context:
         self._ck(self.lib.nemo_gpu_tra_ldf_blp(self.h, kt, kit000, cdtype.encode(), *map(_ptr, (
             pahu, pahv, pgu, pgv, pgui, pgvi, ptb, pta)), kjpt, kldf), "tra_ldf_blp")
 
+    def zps_hde(self, kt, kjpt, pta, pgtu, pgtv):
+        self._ck(self.lib.nemo_gpu_zps_hde(self.h, kt, kjpt, _ptr(pta), _ptr(pgtu), _ptr(pgtv)), "zps_hde")
+
     def tra_zdf_imp(self, kt, kit000, cdtype, p2dt, ptb, pta, kjpt):
         self._ck(self.lib.nemo_gpu_tra_zdf_imp(self.h, kt, kit000, cdtype.encode(), p2dt, _ptr(ptb), _ptr(pta), kjpt),
                  "tra_zdf_imp")

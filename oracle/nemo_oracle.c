@@ -1583,26 +1583,72 @@ int ora_glob_sum(ora_ctx *c, const double *ptab, int nk, double *out) {
 /* ---------------------------------------------------------- one hot-path step */
 /* step.F90:194-257 on the bound fields: dyn_spg_ts, tsa = 0, tra_adv (transports
  * + FCT), tra_ldf (iso or lap), tra_zdf. FCT orders from nn_fct_h/v (0 = 2). */
-/* tra_ldf_blp (traldf_lap_blp.F90:161-231) without partial steps: the first
- * laplacian (kldf 20 iso-level, 21 rotated) of ptb into zlap, lbc_lnk, the second of
- * zlap into pta. */
+/* zps_hde (zpshde.F90:41-148): the horizontal gradients of the tracers at the last
+ * (partial-step) ocean level of u- and v-points, each tracer interpolated to the
+ * shallower of the two bottom depths; lbc_lnk. The density part needs eos and is not
+ * restated. */
+int ora_zps_hde(ora_ctx *c, int kt, int kjpt, const double *pta, double *pgtu, double *pgtv) {
+  (void)kt;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  const double *e3w = fld(c, NEMO_F_E3W_N), *umask = c->umask, *vmask = c->vmask;
+  memset(pgtu, 0, n2 * kjpt * sizeof(double));
+  memset(pgtv, 0, n2 * kjpt * sizeof(double));
+  for (int jn = 1; jn <= kjpt; ++jn) {
+    const double *t = pta + n3 * (jn - 1);
+    double *gu = pgtu + n2 * (jn - 1), *gv = pgtv + n2 * (jn - 1);
+    for (int jj = 1; jj <= jpj - 1; ++jj)
+      for (int ji = 1; ji <= jpi - 1; ++ji) {
+        size_t p = I2(ji, jj);
+        int iku = c->mbku[p], ikum1 = iku - 1 > 1 ? iku - 1 : 1;
+        int ikv = c->mbkv[p], ikvm1 = ikv - 1 > 1 ? ikv - 1 : 1;
+        double ze3wu = e3w[I3(ji + 1, jj, iku)] - e3w[I3(ji, jj, iku)];
+        double ze3wv = e3w[I3(ji, jj + 1, ikv)] - e3w[I3(ji, jj, ikv)];
+        if (ze3wu >= 0.0) {
+          double zmaxu = ze3wu / e3w[I3(ji + 1, jj, iku)];
+          double zti = t[I3(ji + 1, jj, iku)] + zmaxu * (t[I3(ji + 1, jj, ikum1)] - t[I3(ji + 1, jj, iku)]);
+          gu[p] = umask[p] * (zti - t[I3(ji, jj, iku)]);
+        } else {
+          double zmaxu = -ze3wu / e3w[I3(ji, jj, iku)];
+          double zti = t[I3(ji, jj, iku)] + zmaxu * (t[I3(ji, jj, ikum1)] - t[I3(ji, jj, iku)]);
+          gu[p] = umask[p] * (t[I3(ji + 1, jj, iku)] - zti);
+        }
+        if (ze3wv >= 0.0) {
+          double zmaxv = ze3wv / e3w[I3(ji, jj + 1, ikv)];
+          double ztj = t[I3(ji, jj + 1, ikv)] + zmaxv * (t[I3(ji, jj + 1, ikvm1)] - t[I3(ji, jj + 1, ikv)]);
+          gv[p] = vmask[p] * (ztj - t[I3(ji, jj, ikv)]);
+        } else {
+          double zmaxv = -ze3wv / e3w[I3(ji, jj, ikv)];
+          double ztj = t[I3(ji, jj, ikv)] + zmaxv * (t[I3(ji, jj, ikvm1)] - t[I3(ji, jj, ikv)]);
+          gv[p] = vmask[p] * (t[I3(ji, jj + 1, ikv)] - ztj);
+        }
+      }
+  }
+  lbc_closed(jpi, jpj, pgtu, kjpt, 'U', 0.0);
+  lbc_closed(jpi, jpj, pgtv, kjpt, 'V', 0.0);
+  return NEMO_OK;
+}
+
+/* tra_ldf_blp (traldf_lap_blp.F90:161-231): the first laplacian (kldf 20
+ * iso-level, 21 rotated) of ptb into zlap, lbc_lnk, with partial steps zps_hde of
+ * zlap, the second laplacian of zlap into pta. */
 int ora_tra_ldf_blp(ora_ctx *c, int kt, int kit000, const char *cdtype,
                     const double *pahu, const double *pahv,
                     const double *pgu, const double *pgv, const double *pgui, const double *pgvi,
                     const double *ptb, double *pta, int kjpt, int kldf) {
-  (void)pgu; (void)pgv;
   if (kldf != 20 && kldf != 21) return NEMO_ERR_UNSUPPORTED;
-  if (c->nam.ln_zps) return NEMO_ERR_UNSUPPORTED;
-  const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk;
-  double *zlap = zalloc(n3 * (size_t)kjpt);
-  int st = kldf == 20 ? ora_tra_ldf_lap(c, kt, kit000, cdtype, pahu, pahv, NULL, NULL, pgui, pgvi, ptb, zlap, kjpt, 1)
-                      : ora_tra_ldf_iso(c, kt, kit000, cdtype, pahu, pahv, NULL, NULL, pgui, pgvi, ptb, ptb, zlap, kjpt, 1);
+  if (c->nam.ln_zps && (!pgu || !pgv)) return NEMO_ERR_ARG;
+  const size_t n2 = (size_t)c->jpi * c->jpj, n3 = n2 * c->jpk;
+  double *zlap = zalloc(n3 * (size_t)kjpt), *zglu = zalloc(n2 * kjpt), *zglv = zalloc(n2 * kjpt);
+  int st = kldf == 20 ? ora_tra_ldf_lap(c, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb, zlap, kjpt, 1)
+                      : ora_tra_ldf_iso(c, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb, ptb, zlap, kjpt, 1);
   if (!st) {
     lbc_closed(c->jpi, c->jpj, zlap, c->jpk * kjpt, 'T', 0.0);
-    st = kldf == 20 ? ora_tra_ldf_lap(c, kt, kit000, cdtype, pahu, pahv, NULL, NULL, NULL, NULL, zlap, pta, kjpt, 2)
-                    : ora_tra_ldf_iso(c, kt, kit000, cdtype, pahu, pahv, NULL, NULL, NULL, NULL, zlap, ptb, pta, kjpt, 2);
+    if (c->nam.ln_zps) ora_zps_hde(c, kt, kjpt, zlap, zglu, zglv);   /* GRADh(zlap) at the partial steps */
+    st = kldf == 20 ? ora_tra_ldf_lap(c, kt, kit000, cdtype, pahu, pahv, zglu, zglv, NULL, NULL, zlap, pta, kjpt, 2)
+                    : ora_tra_ldf_iso(c, kt, kit000, cdtype, pahu, pahv, zglu, zglv, NULL, NULL, zlap, ptb, pta, kjpt, 2);
   }
-  free(zlap);
+  free(zlap); free(zglu); free(zglv);
   return st;
 }
 

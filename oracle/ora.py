@@ -54,6 +54,7 @@ def lib():
             P(name, [vp, i])
         P("ora_ldf_slp", [vp, i, vp, vp])
         P("ora_tra_ldf_blp", [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
+        P("ora_zps_hde", [vp, i, i, vp, vp, vp])
         _lib = L
     return _lib
 
@@ -227,3 +228,9 @@ class Oracle:
     def tra_ldf_blp(self, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb, pta, kjpt, kldf):
         self._ck(lib().ora_tra_ldf_blp(self.h, kt, kit000, cdtype.encode(), _p(pahu), _p(pahv), _p(pgu), _p(pgv),
                                        _p(pgui), _p(pgvi), _p(ptb), _p(pta), kjpt, kldf), "tra_ldf_blp")
+
+    def zps_hde(self, kt, kjpt, pta):
+        gu = np.zeros((self.jpi, self.jpj, kjpt), order="F")
+        gv = np.zeros((self.jpi, self.jpj, kjpt), order="F")
+        self._ck(lib().ora_zps_hde(self.h, kt, kjpt, _p(pta), _p(gu), _p(gv)), "zps_hde")
+        return gu, gv
