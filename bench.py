@@ -511,6 +511,51 @@ def run_reference(args):
     print(json.dumps(res))
 
 
+def run_model(args):
+    """The model step (nemo_gpu_stp_model: the hot path closed by wzv, the dyn_zdf
+    time step, tra_nxt, dyn_nxt, ssh_swp) on GYRE nn_GYRE=--nn, in --prec, device-resident."""
+    import torch
+    from nemo_gpu import dist
+    rank, world = dist.init("nccl")
+    _, _, local = dist.env_rank()
+    torch.cuda.set_device(local)
+    dom, nam, states = build_case(args.nn, args.members, seed=100 + rank)
+    nam = dict(nam, neuler=0)
+    jpi, jpj, jpk = dom["jpi"], dom["jpj"], dom["jpk"]
+    cells = jpi * jpj * jpk * args.members
+    stream = torch.cuda.Stream()
+    ctx, dev = make_ctx(dom, nam, states, args.prec, stream)
+    for w in range(args.warmup):
+        ctx.stp_model(1 + w)
+    ctx.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist.barrier(local)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for s in range(args.steps):
+            ctx.stp_model(1 + args.warmup + s)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms = dist.max_over_ranks(e0.elapsed_time(e1), device=f"cuda:{local}")
+    ctx.set_timing(True)
+    for s in range(3):
+        ctx.stp_model(5000 + s)
+    ctx.synchronize()
+    kt = {k: {"us": 1e3 * v[0] / v[1], "launches": v[1] / 3} for k, v in ctx.get_kernel_timing().items()}
+    ctx.set_timing(False)
+    if rank == 0:
+        print(json.dumps({
+            "metric": "cell-steps/s of the model step (hot path + wzv, dyn_zdf time step, tra_nxt, dyn_nxt, ssh_swp)",
+            "value": cells * world * args.steps / (ms / 1e3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 bulk + f64 accumulators" if args.prec == "mixed" else "f64",
+            "data": "synthetic: seeded GYRE analytic state",
+            "config": {"workload": f"GYRE nn_GYRE={args.nn} model step", "grid": [jpi, jpj, jpk],
+                       "members": args.members, "cells": cells},
+            "gpu_launches": int(round(sum(v["launches"] for v in kt.values()) * args.steps)), "kernels": kt}))
+
+
 def run_window(args):
     """C4: gradient of the SST cost of a 48-step FP64 tracer window on GYRE
     nn_GYRE=10 (forward sweep + checkpointed reverse sweep, checkpoints every 8)."""
@@ -584,9 +629,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--prec", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--nn", type=int, default=25)
-    ap.add_argument("--workload", default="gyre", choices=["gyre", "shelf", "window"],
+    ap.add_argument("--workload", default="gyre", choices=["gyre", "shelf", "window", "model"],
                     help="gyre: GYRE nn_GYRE=--nn (the headline); shelf: the 1000x1200x56 z* shelf; "
-                         "window: the gradient of a 48-step FP64 tracer window (nn_GYRE=10)")
+                         "window: the gradient of a 48-step FP64 tracer window (nn_GYRE=10); "
+                         "model: the model step (the hot path closed into a time step)")
     ap.add_argument("--members", type=int, default=1)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -601,6 +647,8 @@ def main():
         run_reference(args)
     elif args.workload == "window":
         run_window(args)
+    elif args.workload == "model":
+        run_model(args)
     else:
         run_gpu(args)
 

@@ -12,7 +12,9 @@ namespace nemo {
 
 // div_hor (divhor.F90:76-106: the horizontal divergence of the interior, 0 on the
 // closed edges) and wzv (sshwzv.F90:172-189: w integrated up from w(jpk) = 0), one
-// column per thread.
+// column per thread. The loads of a level do not depend on the running sum, so the
+// unrolled k-loops keep several levels' loads in flight (the column kernels of this
+// file are otherwise bound by one memory round trip per level).
 template <class T>
 __global__ void k_wzv(Dom<T> d, RO<T> un, RO<T> vn, T* wn, T z1_2dt) {
   ColIdx<T> c = col_index(d);
@@ -22,6 +24,7 @@ __global__ void k_wzv(Dom<T> d, RO<T> un, RO<T> vn, T* wn, T z1_2dt) {
   const ColInfo ci = d.ci[ij];
   wn[m3 + ij + (long)(jpk - 1) * n2] = T(0);
   T w = T(0);
+  #pragma unroll 4
   for (int k = jpk - 1; k >= 1; --k) {
     const long q = m3 + ij + (long)(k - 1) * n2;
     const T e3n = d.e3t_n(ij, k, c.m);
@@ -60,20 +63,23 @@ __global__ void k_dyn_nxt(Dom<T> d, NxtArgs<T, A> a) {
   const ColInfo ci = d.ci[ij];
   const T r1u = d.r1_hu_0[ij], r1v = d.r1_hv_0[ij];
   const T uab = T(a.ua_b[m2 + ij]), vab = T(a.va_b[m2 + ij]);
-  T* ua = a.ua + m3;
-  T* va = a.va + m3;
-  T* un = a.un + m3;
-  T* vn = a.vn + m3;
-  T* ub = a.ub + m3;
-  T* vb = a.vb + m3;
+  // six distinct arrays: restrict lets the unrolled loops load ahead of the stores
+  T* __restrict__ ua = a.ua + m3;
+  T* __restrict__ va = a.va + m3;
+  T* __restrict__ un = a.un + m3;
+  T* __restrict__ vn = a.vn + m3;
+  T* __restrict__ ub = a.ub + m3;
+  T* __restrict__ vb = a.vb + m3;
   auto Q = [&](int k) { return ij + (long)(k - 1) * n2; };
   // (:114-126)
   T zue = T(0), zve = T(0);
+  #pragma unroll 4
   for (int k = 1; k <= jpk - 1; ++k) {
     const long q = Q(k);
     zue = zue + d.e3u_n(ij, k, c.m) * ua[q] * umsk<T>(ci, k);
     zve = zve + d.e3v_n(ij, k, c.m) * va[q] * vmsk<T>(ci, k);
   }
+  #pragma unroll 4
   for (int k = 1; k <= jpk - 1; ++k) {
     const long q = Q(k);
     ua[q] = (ua[q] - zue * r1u + uab) * umsk<T>(ci, k);
@@ -84,41 +90,53 @@ __global__ void k_dyn_nxt(Dom<T> d, NxtArgs<T, A> a) {
       ua[Q(k)] = T(0);
       va[Q(k)] = T(0);
     }
+  // the now and before barotropic velocities (:345-358) are summed where un and ub
+  // take their final values, level by level in the same order
+  T sun = T(0), sub = T(0), svn = T(0), svb = T(0);
   if (a.euler) {  // (:168-171)
+    #pragma unroll 4
     for (int k = 1; k <= jpk - 1; ++k) {
-      un[Q(k)] = ua[Q(k)];
-      vn[Q(k)] = va[Q(k)];
+      const long q = Q(k);
+      const T eu = d.e3u_n(ij, k, c.m), ev = d.e3v_n(ij, k, c.m), um = umsk<T>(ci, k), vm = vmsk<T>(ci, k);
+      const T u = ua[q], v = va[q];
+      un[q] = u;
+      vn[q] = v;
+      sun = sun + eu * u * um;
+      sub = sub + eu * ub[q] * um;
+      svn = svn + ev * v * vm;
+      svb = svb + ev * vb[q] * vm;
     }
   } else {  // (:197-211), then (:312-324)
     T sb = T(0), tb = T(0);
+    #pragma unroll 4
     for (int k = 1; k <= jpk - 1; ++k) {
       const long q = Q(k);
+      const T eu = d.e3u_n(ij, k, c.m), ev = d.e3v_n(ij, k, c.m), um = umsk<T>(ci, k), vm = vmsk<T>(ci, k);
+      const T u = ua[q], v = va[q];
       // FP32: the time laplacian from differences (see k_tra_nxt)
-      const T zuf = un[q] + a.atfp * (sizeof(T) == 4 ? (ua[q] - un[q]) - (un[q] - ub[q]) : ub[q] - T(2) * un[q] + ua[q]);
-      const T zvf = vn[q] + a.atfp * (sizeof(T) == 4 ? (va[q] - vn[q]) - (vn[q] - vb[q]) : vb[q] - T(2) * vn[q] + va[q]);
+      const T zuf = un[q] + a.atfp * (sizeof(T) == 4 ? (u - un[q]) - (un[q] - ub[q]) : ub[q] - T(2) * un[q] + u);
+      const T zvf = vn[q] + a.atfp * (sizeof(T) == 4 ? (v - vn[q]) - (vn[q] - vb[q]) : vb[q] - T(2) * vn[q] + v);
       ub[q] = zuf;
       vb[q] = zvf;
-      un[q] = ua[q];
-      vn[q] = va[q];
-      sb = sb + d.e3u_n(ij, k, c.m) * zuf * umsk<T>(ci, k);
-      tb = tb + d.e3v_n(ij, k, c.m) * zvf * vmsk<T>(ci, k);
+      un[q] = u;
+      vn[q] = v;
+      sb = sb + eu * zuf * um;
+      tb = tb + ev * zvf * vm;
+      sun = sun + eu * u * um;
+      svn = svn + ev * v * vm;
     }
     const T unb = a.un_b[m2 + ij], vnb = a.vn_b[m2 + ij];
+    #pragma unroll 4
     for (int k = 1; k <= jpk - 1; ++k) {
       const long q = Q(k);
-      ub[q] = ub[q] - (sb * r1u - unb) * umsk<T>(ci, k);
-      vb[q] = vb[q] - (tb * r1v - vnb) * vmsk<T>(ci, k);
+      const T eu = d.e3u_n(ij, k, c.m), ev = d.e3v_n(ij, k, c.m), um = umsk<T>(ci, k), vm = vmsk<T>(ci, k);
+      const T ubk = ub[q] - (sb * r1u - unb) * um;
+      const T vbk = vb[q] - (tb * r1v - vnb) * vm;
+      ub[q] = ubk;
+      vb[q] = vbk;
+      sub = sub + eu * ubk * um;
+      svb = svb + ev * vbk * vm;
     }
-  }
-  // (:345-358)
-  T sun = T(0), sub = T(0), svn = T(0), svb = T(0);
-  for (int k = 1; k <= jpk - 1; ++k) {
-    const long q = Q(k);
-    const T eu = d.e3u_n(ij, k, c.m), ev = d.e3v_n(ij, k, c.m), um = umsk<T>(ci, k), vm = vmsk<T>(ci, k);
-    sun = sun + eu * un[q] * um;
-    sub = sub + eu * ub[q] * um;
-    svn = svn + ev * vn[q] * vm;
-    svb = svb + ev * vb[q] * vm;
   }
   a.un_b[m2 + ij] = sun * r1u;
   a.ub_b[m2 + ij] = sub * r1u;
