@@ -113,6 +113,9 @@ typedef struct nemo_namelist {
   int nn_fct_v;           /*              and the vertical (2 or 4; 0 = 2), used by
                              nemo_gpu_stp_hotpath                                       */
   double rn_slpmax;       /* &namtra_ldf: maximum iso-neutral slope (0 = 0.01)         */
+  int    ln_traqsr;       /* &namsbc: solar radiation penetrates (tra_qsr, 2 bands)     */
+  double rn_abs, rn_si0, rn_si1; /* &namtra_qsr: near-surface fraction, extinction depths */
+  double rcp;             /* specific heat (eosbn2.F90:1245: 3991.86795711963; 0 = that) */
 } nemo_namelist;
 
 /* ------------------------------------------------------- module-global fields
@@ -172,6 +175,16 @@ enum nemo_field_id {
    * T-point hmlpt. */
   NEMO_F_GDEPT_N, NEMO_F_GDEPW_N,      /* [T]                                         */
   NEMO_F_NMLN, NEMO_F_HMLP, NEMO_F_HMLPT, /* [S]                                      */
+  /* Surface boundary condition of the tracers (sbc_oce.F90): the non-solar and solar
+   * heat fluxes qns, qsr [W/m2] and the salt flux sfx (with emp above); sbc_tsc and
+   * sbc_tsc_b, the now and before tracer-content trends of the forcing,
+   * (jpi,jpj,jpts) restart fields; qsr_hc and qsr_hc_b (jpi,jpj,jpk), the now and
+   * before heat-content trends of the penetrating solar flux (restart fields);
+   * fraqsr_1lev, the fraction of qsr absorbed in the first level. */
+  NEMO_F_QNS, NEMO_F_QSR, NEMO_F_SFX,  /* [S]                                         */
+  NEMO_F_SBC_TSC, NEMO_F_SBC_TSC_B,    /* [S] x jpts                                  */
+  NEMO_F_QSR_HC, NEMO_F_QSR_HC_B,      /* [T]                                         */
+  NEMO_F_FRAQSR_1LEV,                  /* [S]                                         */
   NEMO_F_COUNT
 };
 
@@ -256,6 +269,23 @@ int nemo_gpu_tra_ldf_iso(nemo_ctx *ctx, int kt, int kit000, const char *cdtype,
                          const void *pgu, const void *pgv, const void *pgui, const void *pgvi,
                          const void *ptb, const void *ptbb, void *pta, int kjpt, int kpass);
 
+/* tra_sbc (trasbc.F90:53-206): the surface forcing trend of the tracers. Reads the
+ * bound qns, qsr, emp, sfx, tsn and e3t_n; swaps and fills the bound sbc_tsc_b,
+ * sbc_tsc; adds zfact * (sbc_tsc_b + sbc_tsc) / e3t_n to the first level of the bound
+ * tsa (zfact = 1 on an Euler first step, else 1/2). Without ln_traqsr, qsr is first
+ * moved into qns (:76-79). Runoff (ln_rnf) and ice-shelf melt (ln_isf) are not
+ * included; a restart start (neuler = 1 at nit000) keeps the bound sbc_tsc_b as the
+ * restart's sbc_hc_b / sbc_sc_b. */
+int nemo_gpu_tra_sbc(nemo_ctx *ctx, int kt);
+
+/* tra_qsr (traqsr.F90:77-302), two-band light penetration (ln_qsr_2bd): swaps and
+ * fills the bound qsr_hc_b, qsr_hc from the bound qsr and gdepw_n on levels 1..nksr
+ * (nksr from trc_oce_ext_lev, trc_oce.F90:215-256, at context creation), adds
+ * z1_2 * (qsr_hc_b + qsr_hc) / e3t_n to the temperature of the bound tsa, and sets
+ * the bound fraqsr_1lev with its lbc_lnk. The RGB and bio-model bands are not
+ * included. Needs ln_traqsr. */
+int nemo_gpu_tra_qsr(nemo_ctx *ctx, int kt);
+
 /* zps_hde (zpshde.F90:41-148): pgtu, pgtv (jpi,jpj,kjpt) = the horizontal
  * gradients of pta (jpi,jpj,jpk,kjpt) at the partial-step bottom level of the u-
  * and v-points, with lbc_lnk. The optional density part (prd, pgru, pgrv) needs
@@ -317,7 +347,8 @@ int nemo_gpu_dyn_nxt(nemo_ctx *ctx, int kt);
 /* ssh_swp (sshwzv.F90:216-267), linear free surface. */
 int nemo_gpu_ssh_swp(nemo_ctx *ctx, int kt);
 /* One model step on the bound fields, in step.F90's order: ua = va = 0, dyn_spg_ts,
- * div_hor + wzv, the dyn_zdf time step, tsa = 0, tra_adv, tra_ldf, tra_zdf (with
+ * div_hor + wzv, the dyn_zdf time step, tsa = 0, tra_sbc and tra_qsr (when their
+ * fields are bound; tra_qsr with ln_traqsr), tra_adv, tra_ldf, tra_zdf (with
  * the salinity clamp), tra_nxt, dyn_nxt, ssh_swp -- the hot path closed by the
  * routines above, with the momentum trends of dyn_adv, dyn_vor, dyn_ldf, dyn_hpg and
  * the vertical viscosity held at 0 (they are not on the path). Captured into a CUDA
@@ -434,6 +465,7 @@ enum nemo_kernel_id {
   NEMO_K_WZV, NEMO_K_DYN_ZDF_STEP, NEMO_K_DYN_NXT, NEMO_K_SSH_SWP, /* rest of the model step */
   NEMO_K_LDF_SLP,      /* the three iso-neutral slope kernels */
   NEMO_K_ZPS_HDE,      /* partial-step bottom gradients */
+  NEMO_K_TRA_SBC, NEMO_K_TRA_QSR, /* surface forcing of the tracers */
   NEMO_K_COUNT
 };
 

@@ -57,6 +57,7 @@ struct nemo_ctx {
   bool e3_uniform[5] = {false, false, false, false, false};
   // spg
   int nn_baro = 0, icycle = 0;
+  int nksr = 0;  // tra_qsr: level of light extinction of the two bands
   double rdtbt = 0;
   std::vector<double> wgt1, wgt2;
   double* d_wgt1 = nullptr;
@@ -244,6 +245,8 @@ size_t field_numel(const nemo_ctx* c, int id) {
     case NEMO_F_E3F_N: return (size_t)c->n3;
     case NEMO_F_FCT_TAPE: return 6 * (size_t)c->n3;  // 3 faces x 2 tracers
     case NEMO_F_GDEPT_N: case NEMO_F_GDEPW_N: return (size_t)c->n3;
+    case NEMO_F_SBC_TSC: case NEMO_F_SBC_TSC_B: return 2 * (size_t)c->n2;
+    case NEMO_F_QSR_HC: case NEMO_F_QSR_HC_B: return (size_t)c->n3;
     default: break;
   }
   if (id >= NEMO_F_SSHB) return (size_t)c->n2;
@@ -438,6 +441,31 @@ void float_weights(nemo_ctx* c) {
   }
 }
 
+// trc_oce_ext_lev (trc_oce.F90:215-256): the last T-level reached by a fraction
+// pqsr_frc of the light of longest extinction depth prldex, or the sea bed; the
+// rest-state W-depths are the sums of e3t_0 of e3_to_depth (DOM/depth_e3.F90).
+int ext_lev(const nemo_ctx* c, double prldex, double pqsr_frc) {
+  const int jpk = c->jpk;
+  const size_t n2 = c->n2;
+  const double zhext = prldex * (std::log(10.0) * 15.0 + std::log(pqsr_frc));
+  std::vector<double> gdepw((size_t)jpk * n2, 0.0);
+  for (int jk = 2; jk <= jpk; ++jk)
+    for (size_t p = 0; p < n2; ++p)
+      gdepw[p + n2 * (jk - 1)] = gdepw[p + n2 * (jk - 2)] + c->e3_0[0][p + n2 * (jk - 2)];
+  int pjl = jpk - 1;
+  for (int jk = jpk - 1; jk >= 1; --jk) {
+    bool wet = false;
+    double zem = -1e300;
+    for (size_t p = 0; p < n2; ++p) {
+      const double tm = (jk >= c->ci[p].tlo && jk <= c->ci[p].thi) ? 1.0 : 0.0;
+      wet = wet || tm > 0;
+      zem = std::max(zem, gdepw[p + n2 * jk] * tm);
+    }
+    if (!wet || zem >= zhext) pjl = jk;
+  }
+  return pjl;
+}
+
 // Domain derivation (dommsk.F90:133-238, domzgr.F90:292-314, domhgr.F90:133-151,
 // domain.F90:149-183) and spg set-up (dynspg_ts.F90:1479-1493).
 int derive_domain(nemo_ctx* c, const nemo_dom_desc* dm) {
@@ -563,6 +591,7 @@ int derive_domain(nemo_ctx* c, const nemo_dom_desc* dm) {
   int jpit = 0;
   ts_wgt(c, c->nam.ln_bt_av, c->nam.ln_bt_fw, &jpit);
   c->icycle = jpit;
+  c->nksr = ext_lev(c, c->nam.rn_si1 > 0 ? c->nam.rn_si1 : 23.0, 100.0);
   coriolis_factors(c, tmask, umask);
   return NEMO_OK;
 }
@@ -967,6 +996,62 @@ int run_ssh_swp(nemo_ctx* c, int kt) {
   return NEMO_OK;
 }
 
+// first-step mode of the forcing swaps: 0 swap, 1 Euler start (before = 0), 2 restart
+int sbc_mode(const nemo_ctx* c, int kt) {
+  if (kt != c->nam.nit000) return 0;
+  return c->nam.neuler == 0 ? 1 : 2;
+}
+double rcp_of(const nemo_namelist& nm) { return nm.rcp > 0 ? nm.rcp : 3991.86795711963; }
+
+template <class T>
+int run_tra_sbc(nemo_ctx* c, int kt) {
+  const nemo_namelist& nm = c->nam;
+  void* const* F = c->f;
+  SbcArgs<T> a{};
+  a.qns = (T*)F[NEMO_F_QNS]; a.qsr = (T*)F[NEMO_F_QSR];
+  a.emp = (const T*)F[NEMO_F_EMP]; a.sfx = (const T*)F[NEMO_F_SFX]; a.tsn = (const T*)F[NEMO_F_TSN];
+  a.tsc = (T*)F[NEMO_F_SBC_TSC]; a.tsc_b = (T*)F[NEMO_F_SBC_TSC_B]; a.tsa = (T*)F[NEMO_F_TSA];
+  const double rau0_rcp = nm.rau0 * rcp_of(nm);
+  a.r1_rau0 = (T)(1.0 / nm.rau0); a.r1_rau0_rcp = (T)(1.0 / rau0_rcp);
+  a.mode = sbc_mode(c, kt);
+  a.zfact = (T)(a.mode == 1 ? 1.0 : 0.5);
+  a.traqsr = nm.ln_traqsr; a.linssh = nm.ln_linssh;
+  cudaError_t e = launch_tra_sbc<T>(dom_now<T>(c), a, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "tra_sbc launch");
+  return NEMO_OK;
+}
+
+template <class T>
+int run_tra_qsr(nemo_ctx* c, int kt) {
+  const nemo_namelist& nm = c->nam;
+  void* const* F = c->f;
+  QsrArgs<T> a{};
+  a.qsr = (const T*)F[NEMO_F_QSR]; a.gdepw = (const T*)F[NEMO_F_GDEPW_N];
+  a.hc = (T*)F[NEMO_F_QSR_HC]; a.hc_b = (T*)F[NEMO_F_QSR_HC_B]; a.fraq = (T*)F[NEMO_F_FRAQSR_1LEV];
+  a.tsa = (T*)F[NEMO_F_TSA];
+  const double r1_rau0_rcp = 1.0 / (nm.rau0 * rcp_of(nm));
+  a.zz0 = (T)(nm.rn_abs * r1_rau0_rcp); a.zz1 = (T)((1. - nm.rn_abs) * r1_rau0_rcp);
+  a.xsi0r = (T)(1.0 / nm.rn_si0); a.xsi1r = (T)(1.0 / nm.rn_si1);
+  a.r1_rau0_rcp = (T)r1_rau0_rcp;
+  a.mode = sbc_mode(c, kt);
+  a.z1_2 = (T)(a.mode == 1 ? 1.0 : 0.5);
+  a.nksr = c->nksr;
+  cudaError_t e = launch_tra_qsr<T>(dom_now<T>(c), a, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "tra_qsr launch");
+  return NEMO_OK;
+}
+
+bool sbc_bound(const nemo_ctx* c) {
+  for (int id : {NEMO_F_QNS, NEMO_F_QSR, NEMO_F_EMP, NEMO_F_SFX, NEMO_F_SBC_TSC, NEMO_F_SBC_TSC_B})
+    if (!c->f[id]) return false;
+  return true;
+}
+bool qsr_bound(const nemo_ctx* c) {
+  for (int id : {NEMO_F_QSR, NEMO_F_GDEPW_N, NEMO_F_QSR_HC, NEMO_F_QSR_HC_B, NEMO_F_FRAQSR_1LEV})
+    if (!c->f[id]) return false;
+  return true;
+}
+
 template <class T>
 int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
   const nemo_namelist& nm = c->nam;
@@ -996,7 +1081,8 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
   if (staged)  // the iso-neutral coefficients the first pass may zero on this stream
     if (wait_field(c, c->stream, NEMO_F_AH_WSLP2, true) || wait_field(c, c->stream, NEMO_F_AKZ, true))
       return NEMO_ERR_CUDA;
-  const bool fused = nm.ln_traldf_iso && !nm.ln_traldf_blp && !c->no_fusion;
+  const bool forced = model && sbc_bound(c);  // tra_sbc (and tra_qsr) before tra_adv
+  const bool fused = nm.ln_traldf_iso && !nm.ln_traldf_blp && !c->no_fusion && !forced;
   LdfArgs<T> la{};
   // The iso-neutral fluxes read tsb and the slopes only, and dyn_spg_ts touches
   // neither them nor their outputs: outside per-kernel timing they run on the side
@@ -1031,6 +1117,11 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
     if (join_copies(c)) return NEMO_ERR_CUDA;  // the tracer part: every remaining copy
   }
   mark(1);
+  if (forced) {  // step.F90:230-233
+    CK(cudaMemsetAsync(F[NEMO_F_TSA], 0, 2 * (size_t)c->n3 * c->nmem * sizeof(T), c->stream), "tsa = 0");
+    if ((s = run_tra_sbc<T>(c, kt))) return s;
+    if (nm.ln_traqsr && (s = run_tra_qsr<T>(c, kt))) return s;
+  }
   const double r2dt = (nm.neuler == 0 && kt == nm.nit000) ? nm.rn_rdt : 2.0 * nm.rn_rdt;
   const int fct_h = nm.nn_fct_h ? nm.nn_fct_h : 2, fct_v = nm.nn_fct_v ? nm.nn_fct_v : 2;  // &namtra_adv
   if (fused) {
@@ -1047,8 +1138,9 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
     if (e != cudaSuccess) return cuda_fail(c, e, "iso edges");
     mark(2);
   } else {
-  // tsa = 0 (step.F90:234) folded into the first trend (pta_in = NULL)
-  s = run_fct<T>(c, r2dt, F[NEMO_F_UN], F[NEMO_F_VN], F[NEMO_F_WN], 1, F[NEMO_F_TSB], F[NEMO_F_TSN], nullptr,
+  // tsa = 0 (step.F90:234) folded into the first trend (pta_in = NULL), or, with the
+  // surface forcing of the model step, tsa = 0, tra_sbc, tra_qsr and FCT adding on
+  s = run_fct<T>(c, r2dt, F[NEMO_F_UN], F[NEMO_F_VN], F[NEMO_F_WN], 1, F[NEMO_F_TSB], F[NEMO_F_TSN], forced ? F[NEMO_F_TSA] : nullptr,
                  F[NEMO_F_TSA], 2, fct_h, fct_v);
   if (s) return s;
   mark(2);
@@ -1481,6 +1573,23 @@ int nemo_gpu_ldf_slp(nemo_ctx* c, int kt, const void* prd, const void* pn2) {
   if (nm.ln_zps || nm.ln_isfcav || nm.ln_sco)
     return fail(c, NEMO_ERR_UNSUPPORTED, "ldf_slp: z-coordinate without partial steps or cavities only");
   return c->prec == NEMO_PREC_FP64 ? run_ldf_slp<double>(c, prd, pn2) : run_ldf_slp<float>(c, prd, pn2);
+}
+
+int nemo_gpu_tra_sbc(nemo_ctx* c, int kt) {
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (!sbc_bound(c) || !c->f[NEMO_F_TSN] || !c->f[NEMO_F_TSA])
+    return fail(c, NEMO_ERR_UNBOUND, "tra_sbc: qns, qsr, emp, sfx, sbc_tsc, sbc_tsc_b, tsn and tsa must be bound");
+  return c->prec == NEMO_PREC_FP64 ? run_tra_sbc<double>(c, kt) : run_tra_sbc<float>(c, kt);
+}
+
+int nemo_gpu_tra_qsr(nemo_ctx* c, int kt) {
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (!c->nam.ln_traqsr) return fail(c, NEMO_ERR_ARG, "tra_qsr: ln_traqsr is off");
+  if (!qsr_bound(c) || !c->f[NEMO_F_TSA])
+    return fail(c, NEMO_ERR_UNBOUND, "tra_qsr: qsr, gdepw_n, qsr_hc, qsr_hc_b, fraqsr_1lev and tsa must be bound");
+  return c->prec == NEMO_PREC_FP64 ? run_tra_qsr<double>(c, kt) : run_tra_qsr<float>(c, kt);
 }
 
 int nemo_gpu_wzv(nemo_ctx* c, int kt) {

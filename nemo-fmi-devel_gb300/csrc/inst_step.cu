@@ -54,13 +54,29 @@ cudaError_t launch_zps_hde(const Dom<T>& d, const T* pta, T* pgtu, T* pgtv, int 
   return cudaGetLastError();
 }
 
+template <class T>
+cudaError_t launch_tra_sbc(const Dom<T>& d, const SbcArgs<T>& a, cudaStream_t s) {
+  k_tra_sbc<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a);
+  ktick(NEMO_K_TRA_SBC, s);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_tra_qsr(const Dom<T>& d, const QsrArgs<T>& a, cudaStream_t s) {
+  k_tra_qsr<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a);
+  ktick(NEMO_K_TRA_QSR, s);
+  return cudaGetLastError();
+}
+
 #define NEMO_STEP_INST(T)                                                                                      \
   template cudaError_t launch_wzv<T>(const Dom<T>&, const T*, const T*, T*, T, cudaStream_t);                  \
   template cudaError_t launch_dyn_zdf_step<T>(const Dom<T>&, const T*, const T*, T*, T*, T, cudaStream_t);     \
   template cudaError_t launch_dyn_nxt<T>(const Dom<T>&, const NxtArgs<T, double>&, cudaStream_t);              \
   template cudaError_t launch_ssh_swp<T>(const Dom<T>&, T*, T*, const double*, T, int, cudaStream_t);      \
   template cudaError_t launch_ldf_slp<T>(const Dom<T>&, const SlpArgs<T>&, cudaStream_t);                  \
-  template cudaError_t launch_zps_hde<T>(const Dom<T>&, const T*, T*, T*, int, cudaStream_t);
+  template cudaError_t launch_zps_hde<T>(const Dom<T>&, const T*, T*, T*, int, cudaStream_t);             \
+  template cudaError_t launch_tra_sbc<T>(const Dom<T>&, const SbcArgs<T>&, cudaStream_t);                  \
+  template cudaError_t launch_tra_qsr<T>(const Dom<T>&, const QsrArgs<T>&, cudaStream_t);
 NEMO_STEP_INST(double)
 NEMO_STEP_INST(float)
 

@@ -375,4 +375,108 @@ __global__ void k_zps_hde(Dom<T> d, RO<T> pta, T* __restrict__ pgtu, T* __restri
   }
 }
 
+// ------------------------------------------------------------ surface forcing
+// tra_sbc (trasbc.F90:53-206) without runoff and ice-shelf melt, one (i,j) point per
+// thread: the move of qsr into qns without penetration (:76-79), the swap of the
+// forcing trends (:81-100), the trends of the heat and salt fluxes with the
+// concentration/dilution of the linear free surface (:104-118) and their addition to
+// the first level of tsa (:123-129), on the reference's index ranges.
+template <class T>
+__global__ void k_tra_sbc(Dom<T> d, SbcArgs<T> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i > d.jpi || j > d.jpj) return;
+  const int m = blockIdx.z;
+  const long ij = (long)(i - 1) + (long)(j - 1) * d.jpi;
+  const long p = (long)m * d.n2 + ij, pt = 2 * (long)m * d.n2 + ij, ps = pt + d.n2;
+  T qns = a.qns[p];
+  if (!a.traqsr) {
+    qns = qns + a.qsr[p];
+    a.qns[p] = qns;
+    a.qsr[p] = T(0);
+  }
+  T bt, bs;
+  if (a.mode == 0) {
+    bt = a.tsc[pt];
+    bs = a.tsc[ps];
+  } else if (a.mode == 1) {
+    bt = T(0);
+    bs = T(0);
+  } else {
+    bt = a.tsc_b[pt];
+    bs = a.tsc_b[ps];
+  }
+  if (a.mode != 2) {
+    a.tsc_b[pt] = bt;
+    a.tsc_b[ps] = bs;
+  }
+  if (i < 2 || i > d.jpi - 1 || j < 2) {
+    if (a.mode != 0) {  // first step: sbc_tsc = 0 everywhere
+      a.tsc[pt] = T(0);
+      a.tsc[ps] = T(0);
+    }
+    return;
+  }
+  T tt = a.r1_rau0_rcp * qns;
+  T ts = a.r1_rau0 * a.sfx[p];
+  if (a.linssh) {
+    const long q = 2 * (long)m * d.n3 + ij;
+    const T e = a.emp[p];
+    tt = tt + a.r1_rau0 * e * a.tsn[q];
+    ts = ts + a.r1_rau0 * e * a.tsn[q + d.n3];
+  }
+  a.tsc[pt] = tt;
+  a.tsc[ps] = ts;
+  const long q = 2 * (long)m * d.n3 + ij;
+  const T e3 = d.e3t_n(ij, 1, m);
+  a.tsa[q] = a.tsa[q] + a.zfact * (bt + tt) / e3;
+  a.tsa[q + d.n3] = a.tsa[q + d.n3] + a.zfact * (bs + ts) / e3;
+}
+
+// tra_qsr (traqsr.F90:77-302) with two bands (np_2BD, :243-256), one column per
+// thread: the swap of the heat-content trend over the whole column (:134-147), the
+// absorbed flux of levels 1..nksr, whose lower-interface attenuation is the next
+// level's upper one (the same expression of the same depth, so computed once), the
+// temperature trend (:260-267) and the first-level fraction with the closed lbc_lnk
+// (:270-277: 0 on the domain edge).
+template <class T>
+__global__ void k_tra_qsr(Dom<T> d, QsrArgs<T> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i > d.jpi || j > d.jpj) return;
+  const int m = blockIdx.z;
+  const long ij = (long)(i - 1) + (long)(j - 1) * d.jpi;
+  const long c3 = (long)m * d.n3 + ij;
+  const bool inner = i >= 2 && i <= d.jpi - 1 && j >= 2 && j <= d.jpj - 1;
+  if (a.mode != 2) {
+    const int k1 = inner ? a.nksr + 1 : 1;  // levels the solve below does not read
+    for (int k = k1; k <= d.jpk; ++k) {
+      const long q = c3 + (long)(k - 1) * d.n2;
+      a.hc_b[q] = a.mode == 0 ? a.hc[q] : T(0);
+    }
+  }
+  if (!inner) {
+    a.fraq[(long)m * d.n2 + ij] = T(0);
+    return;
+  }
+  const ColInfo ci = d.ci[ij];
+  const T qsr = a.qsr[(long)m * d.n2 + ij];
+  T* ta = a.tsa + 2 * (long)m * d.n3 + ij;  // temperature
+  T g = a.gdepw[c3];
+  T zc0 = a.zz0 * exp(-g * a.xsi0r) + a.zz1 * exp(-g * a.xsi1r);
+  T h1 = T(0);
+  for (int k = 1; k <= a.nksr; ++k) {
+    const long q = c3 + (long)(k - 1) * d.n2;
+    g = a.gdepw[q + d.n2];
+    const T zc1 = a.zz0 * exp(-g * a.xsi0r) + a.zz1 * exp(-g * a.xsi1r);
+    const T hb = a.mode == 0 ? a.hc[q] : (a.mode == 1 ? T(0) : a.hc_b[q]);
+    if (a.mode != 2) a.hc_b[q] = hb;
+    const T h = qsr * (zc0 * wmsk<T>(ci, k) - zc1 * wmsk<T>(ci, k + 1));
+    a.hc[q] = h;
+    const long qt = (long)(k - 1) * d.n2;
+    ta[qt] = ta[qt] + a.z1_2 * (hb + h) / d.e3t_n(ij, k, m);
+    if (k == 1) h1 = h;
+    zc0 = zc1;
+  }
+  a.fraq[(long)m * d.n2 + ij] = qsr != T(0) ? h1 / (a.r1_rau0_rcp * qsr) : T(1);
+}
+
 }  // namespace nemo

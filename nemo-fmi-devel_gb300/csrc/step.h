@@ -26,6 +26,31 @@ struct SlpArgs {
   T zeps, zm1_g, zm1_2g, z1_slpmax;
 };
 
+// tra_sbc: mode 0 swaps sbc_tsc into sbc_tsc_b, 1 zeroes both (Euler first step),
+// 2 zeroes sbc_tsc and keeps sbc_tsc_b (restart first step)
+template <class T>
+struct SbcArgs {
+  T *qns, *qsr;                       // (jpi,jpj) per member; qsr moved into qns without ln_traqsr
+  const T *emp, *sfx, *tsn;
+  T *tsc, *tsc_b;                     // (jpi,jpj,2) per member
+  T* tsa;
+  T r1_rau0, r1_rau0_rcp, zfact;
+  int traqsr, linssh, mode;
+};
+
+// tra_qsr, two bands: mode as for tra_sbc (qsr_hc into qsr_hc_b)
+template <class T>
+struct QsrArgs {
+  const T *qsr, *gdepw;
+  T *hc, *hc_b, *fraq, *tsa;
+  T zz0, zz1, xsi0r, xsi1r, z1_2, r1_rau0_rcp;
+  int nksr, mode;
+};
+
+template <class T>
+cudaError_t launch_tra_sbc(const Dom<T>& d, const SbcArgs<T>& a, cudaStream_t s);
+template <class T>
+cudaError_t launch_tra_qsr(const Dom<T>& d, const QsrArgs<T>& a, cudaStream_t s);
 template <class T>
 cudaError_t launch_zps_hde(const Dom<T>& d, const T* pta, T* pgtu, T* pgtv, int kjpt, cudaStream_t s);
 template <class T>

@@ -51,7 +51,13 @@ class Namelist(C.Structure):
                 ("rn_bt_alpha", C.c_double), ("nvor_scheme", C.c_int), ("nn_een_e3f", C.c_int),
                 ("ln_dynadv_vec", C.c_int), ("ln_sco", C.c_int), ("ln_apr_dyn", C.c_int),
                 ("rn_scal_load", C.c_double), ("grav", C.c_double), ("rau0", C.c_double),
-                ("nn_fct_h", C.c_int), ("nn_fct_v", C.c_int), ("rn_slpmax", C.c_double)]
+                ("nn_fct_h", C.c_int), ("nn_fct_v", C.c_int), ("rn_slpmax", C.c_double),
+                ("ln_traqsr", C.c_int), ("rn_abs", C.c_double), ("rn_si0", C.c_double), ("rn_si1", C.c_double),
+                ("rcp", C.c_double)]
+
+
+# members a namelist may leave out (&namtra_qsr of namelist_ref; rcp 0 selects 3991.86795711963)
+NAMELIST_DEFAULTS = {"ln_traqsr": 0, "rn_abs": 0.58, "rn_si0": 0.35, "rn_si1": 23.0, "rcp": 0.0}
 
 
 def make_desc(dom):
@@ -78,7 +84,7 @@ def make_desc(dom):
 def make_namelist(nam):
     n = Namelist()
     for k, _ in Namelist._fields_:
-        setattr(n, k, nam[k])
+        setattr(n, k, nam[k] if k in nam else NAMELIST_DEFAULTS[k])
     return n
 
 
@@ -114,7 +120,8 @@ def load(path):
     _proto(lib, "nemo_gpu_tra_ldf_blp", i, [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
     _proto(lib, "nemo_gpu_zps_hde", i, [vp, i, i, vp, vp, vp])
     _proto(lib, "nemo_gpu_get_launch_shape", i, [vp, _ip, i])
-    for name in ("nemo_gpu_wzv", "nemo_gpu_dyn_zdf_step", "nemo_gpu_dyn_nxt", "nemo_gpu_ssh_swp",
+    for name in ("nemo_gpu_tra_sbc", "nemo_gpu_tra_qsr",
+                 "nemo_gpu_wzv", "nemo_gpu_dyn_zdf_step", "nemo_gpu_dyn_nxt", "nemo_gpu_ssh_swp",
                  "nemo_gpu_stp_model"):
         _proto(lib, name, i, [vp, i])
     _proto(lib, "nemo_gpu_tra_adv_fct_adj", i, [vp, i, i, cp, d, vp, vp, vp, vp, vp, vp, i, i, i])

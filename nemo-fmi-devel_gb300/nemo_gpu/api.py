@@ -221,6 +221,12 @@ class Context:
     def ssh_swp(self, kt):
         self._ck(self.lib.nemo_gpu_ssh_swp(self.h, kt), "ssh_swp")
 
+    def tra_sbc(self, kt):
+        self._ck(self.lib.nemo_gpu_tra_sbc(self.h, kt), "tra_sbc")
+
+    def tra_qsr(self, kt):
+        self._ck(self.lib.nemo_gpu_tra_qsr(self.h, kt), "tra_qsr")
+
     def stp_model(self, kt):
         """One model step: the hot path closed by wzv, the dyn_zdf time step, tra_nxt,
         dyn_nxt and ssh_swp (see nemo_gpu.h)."""

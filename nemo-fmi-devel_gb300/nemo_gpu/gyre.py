@@ -22,6 +22,7 @@ import math
 import numpy as np
 
 RA, RAD, OMEGA, GRAV, RAU0 = 6371229.0, math.pi / 180.0, 7.292116e-05, 9.80665, 1026.0
+RCP = 3991.86795711963   # specific heat of sea water (eosbn2.F90:1245)
 
 
 def namelist(**over):
@@ -32,7 +33,8 @@ def namelist(**over):
         rn_aht_0=(0.5 * 0.02) * 100.0e3, ln_zdfddm=0, ln_zad_Aimp=0,
         ln_bt_fw=1, ln_bt_av=1, nn_bt_flt=1, ln_bt_auto=1, nn_baro=30, rn_bt_cmax=0.8, rn_bt_alpha=0.0,
         nvor_scheme=1, nn_een_e3f=0, ln_dynadv_vec=1, ln_sco=0, ln_apr_dyn=0, rn_scal_load=0.0,
-        grav=GRAV, rau0=RAU0, nn_fct_h=2, nn_fct_v=2, rn_slpmax=0.01)
+        grav=GRAV, rau0=RAU0, nn_fct_h=2, nn_fct_v=2, rn_slpmax=0.01,
+        ln_traqsr=1, rn_abs=0.58, rn_si0=0.35, rn_si1=23.0, rcp=RCP)
     nam.update(over)
     return nam
 
@@ -322,3 +324,33 @@ def slope_inputs(dom, nam, st, rho_c=0.01):
     f = np.asfortranarray
     return dict(rhd=f(rhd), rn2b=f(rn2), nmln=f(nmln.astype(np.int32)), hmlp=f(hmlp), hmlpt=f(hmlpt),
                 gdept_n=f(gdept), gdepw_n=f(gdepw))
+
+
+def sbc_inputs(dom, nam, st, kt=1):
+    """Surface heat and salt forcing of tra_sbc / tra_qsr at time step kt, from the
+    GYRE analytic fluxes (usrdef_sbc.F90:90-151, year 1 starting on January 1st, 360-day
+    year): qsr, and qns with the -40 W/m2/K restoring to the seasonal T* computed from
+    the before SST and the sensible heat of E-P at the SST (sst_m = the now SST); sfx
+    = 0. Also the rest-state depths of the W-points (gdepw_n) that tra_qsr reads, and
+    zeroed restart fields sbc_tsc, sbc_tsc_b (jpi,jpj,2), qsr_hc, qsr_hc_b."""
+    jpi, jpj, jpk = dom["jpi"], dom["jpj"], dom["jpk"]
+    g = dom["gphit"]
+    ztime = kt * nam["rn_rdt"] / 3600.0                       # hours since January 1st
+    tmax1 = (5 * 30 + 21) * 24.0
+    tmin1 = tmax1 + 24.0 * 360 / 2
+    tmax2 = (6 * 30 + 21) * 24.0
+    tmin2 = tmax2 - 24.0 * 360 / 2
+    c1 = math.cos((ztime - tmax1) / (tmin1 - tmax1) * math.pi)
+    c2 = math.cos((ztime - tmax2) / (tmax2 - tmin2) * math.pi)
+    t_star = 28.3 * (1.0 + c2 / 50.0) * np.cos(math.pi * (g - 5.0) / (53.5 * (1 + 11 / 53.5 * c2) * 2.0))
+    qsr = 230.0 * np.cos(3.1415 * (g - 23.5 * c1) / (0.9 * 180))
+    qns = -40.0 * (st["tsb"][:, :, 0, 0] - t_star) - qsr
+    qns = qns - st["emp"] * st["tsn"][:, :, 0, 0] * RCP
+    e3t = dom["e3t_0"]
+    gdepw = np.zeros_like(e3t)
+    gdepw[:, :, 1:] = np.cumsum(e3t[:, :, :-1], axis=2)         # e3_to_depth (depth_e3.F90)
+    f = np.asfortranarray
+    return dict(qsr=f(qsr * 1.0), qns=f(qns), sfx=f(np.zeros((jpi, jpj))), gdepw_n=f(gdepw),
+                sbc_tsc=f(np.zeros((jpi, jpj, 2))), sbc_tsc_b=f(np.zeros((jpi, jpj, 2))),
+                qsr_hc=f(np.zeros((jpi, jpj, jpk))), qsr_hc_b=f(np.zeros((jpi, jpj, jpk))),
+                fraqsr_1lev=f(np.ones((jpi, jpj))))

@@ -46,6 +46,7 @@ struct ora_ctx {
   double *ahtu_c, *ahtv_c; /* constant masked diffusivity (ldftra.F90:292-372) */
   /* dyn_spg_ts module state */
   int nn_baro, icycle;
+  int nksr;  /* level of light extinction of tra_qsr's two bands */
   double rdtbt;
   double *wgtbtp1, *wgtbtp2, *zwz, *ftne, *ftnw, *ftse, *ftsw;
   double *sshn_e, *sshb_e, *sshbb_e, *un_e, *ub_e, *ubb_e, *vn_e, *vb_e, *vbb_e;
@@ -139,6 +140,32 @@ static void ts_wgt(ora_ctx *c, int ll_av, int ll_fw, int *jpit, double *zwgt1, d
 }
 
 /* ------------------------------------------------------------------ create */
+/* trc_oce_ext_lev (trc_oce.F90:215-256): the last T-level reached by a fraction
+ * pqsr_frc of the light with longest extinction depth prldex, or the sea bed. The
+ * rest-state W-depths come from e3t_0 as e3_to_depth forms them (DOM/depth_e3.F90):
+ * gdepw_0(1) = 0, gdepw_0(k) = gdepw_0(k-1) + e3t_0(k-1). */
+static int ext_lev(const ora_ctx *c, const double *e3t_0, double prldex, double pqsr_frc) {
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj;
+  const double zhext = prldex * (log(10.0) * 15.0 + log(pqsr_frc));
+  double *gdepw = zalloc(n2 * jpk);
+  for (int jk = 2; jk <= jpk; ++jk)
+    for (size_t p = 0; p < n2; ++p) gdepw[p + n2 * (jk - 1)] = gdepw[p + n2 * (jk - 2)] + e3t_0[p + n2 * (jk - 2)];
+  int pjl = jpk - 1;
+  for (int jk = jpk - 1; jk >= 1; --jk) {
+    double sum = 0.0, zem = -1e300;
+    for (size_t p = 0; p < n2; ++p) sum += c->tmask[p + n2 * (jk - 1)];
+    if (sum > 0) {
+      for (size_t p = 0; p < n2; ++p) zem = dmax(zem, gdepw[p + n2 * jk] * c->tmask[p + n2 * (jk - 1)]);
+      if (zem >= zhext) pjl = jk;
+    } else {
+      pjl = jk;
+    }
+  }
+  free(gdepw);
+  return pjl;
+}
+
 int ora_create(const nemo_dom_desc *d, const nemo_namelist *nam, ora_ctx **out) {
   if (!d || !nam || !out) return NEMO_ERR_ARG;
   if (d->jpi < 4 || d->jpj < 4 || d->jpk < 3 || d->jperio != 0) return NEMO_ERR_UNSUPPORTED;
@@ -189,6 +216,7 @@ int ora_create(const nemo_dom_desc *d, const nemo_namelist *nam, ora_ctx **out) 
   for (size_t p = 0; p < n2; ++p) c->wmask[p] = c->tmask[p];
   for (int jk = 2; jk <= jpk; ++jk)
     for (size_t p = 0; p < n2; ++p) c->wmask[p + n2 * (jk - 1)] = c->tmask[p + n2 * (jk - 1)] * c->tmask[p + n2 * (jk - 2)];
+  c->nksr = ext_lev(c, d->e3t_0, c->nam.rn_si1 > 0 ? c->nam.rn_si1 : 23.0, 100.0);
   /* dommsk.F90:201-238 */
   c->ssmask = zalloc(n2); c->ssumask = zalloc(n2); c->ssvmask = zalloc(n2);
   c->tmask_h = zalloc(n2); c->tmask_i = zalloc(n2);
@@ -1653,12 +1681,23 @@ int ora_tra_ldf_blp(ora_ctx *c, int kt, int kit000, const char *cdtype,
 }
 
 /* The tracer part of the step: tsa = 0, tra_adv (transports + FCT), tra_ldf, tra_zdf. */
+int ora_tra_sbc(ora_ctx *c, int kt);
+int ora_tra_qsr(ora_ctx *c, int kt);
+/* The model step runs tra_sbc (and tra_qsr) when the surface forcing is bound. */
+static int sbc_bound(const ora_ctx *c) {
+  return c->f[NEMO_F_QNS] && c->f[NEMO_F_QSR] && c->f[NEMO_F_SFX] && c->f[NEMO_F_SBC_TSC] && c->f[NEMO_F_SBC_TSC_B];
+}
+
 static int stp_tracers(ora_ctx *c, int kt) {
   const nemo_namelist *nm = &c->nam;
   const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk;
   double *tsb = c->f[NEMO_F_TSB], *tsn = c->f[NEMO_F_TSN], *tsa = c->f[NEMO_F_TSA];
   int st;
   memset(tsa, 0, 2 * n3 * sizeof(double));
+  if (sbc_bound(c)) {                                        /* step.F90:232-233 */
+    if ((st = ora_tra_sbc(c, kt))) return st;
+    if (nm->ln_traqsr && (st = ora_tra_qsr(c, kt))) return st;
+  }
   double r2dt = (nm->neuler == 0 && kt == nm->nit000) ? nm->rn_rdt : 2.0 * nm->rn_rdt;
   double *zun = zalloc(n3), *zvn = zalloc(n3), *zwn = zalloc(n3);
   ora_tra_adv_trp(c, c->f[NEMO_F_UN], c->f[NEMO_F_VN], c->f[NEMO_F_WN], zun, zvn, zwn);
@@ -2266,6 +2305,107 @@ int ora_ssh_swp(ora_ctx *c, int kt) {
   }
   return NEMO_OK;
 }
+
+/* ------------------------------------------------------- surface forcing */
+static double rcp_of(const nemo_namelist *nm) { return nm->rcp > 0 ? nm->rcp : 3991.86795711963; }
+
+/* tra_sbc (trasbc.F90:53-206) without runoff and ice-shelf melt: bound QNS, QSR, EMP,
+ * SFX, SBC_TSC, SBC_TSC_B (jpi,jpj,2), TSN, TSA. */
+int ora_tra_sbc(ora_ctx *c, int kt) {
+  const nemo_namelist *nm = &c->nam;
+  const int jpi = c->jpi, jpj = c->jpj;
+  const size_t n2 = (size_t)jpi * jpj;
+  double *qns = c->f[NEMO_F_QNS], *qsr = c->f[NEMO_F_QSR];
+  const double *emp = c->f[NEMO_F_EMP], *sfx = c->f[NEMO_F_SFX], *tsn = c->f[NEMO_F_TSN];
+  double *tsc = c->f[NEMO_F_SBC_TSC], *tsc_b = c->f[NEMO_F_SBC_TSC_B], *tsa = c->f[NEMO_F_TSA];
+  if (!qns || !qsr || !emp || !sfx || !tsn || !tsc || !tsc_b || !tsa) return NEMO_ERR_UNBOUND;
+  const double *e3t_n = fld(c, NEMO_F_E3T_N);
+  const size_t n3 = n2 * c->jpk;
+  const double rau0 = nm->rau0, r1_rau0 = 1.0 / rau0, rau0_rcp = rau0 * rcp_of(nm), r1_rau0_rcp = 1.0 / rau0_rcp;
+  if (!nm->ln_traqsr)                                        /* :76-79 */
+    for (size_t p = 0; p < n2; ++p) { qns[p] = qns[p] + qsr[p]; qsr[p] = 0.0; }
+  double zfact;
+  if (kt == nm->nit000) {                                    /* :81-96 */
+    if (nm->neuler != 0) {              /* restart: sbc_tsc_b holds the restart's sbc_hc_b, sbc_sc_b */
+      zfact = 0.5;
+      memset(tsc, 0, 2 * n2 * sizeof(double));
+    } else {
+      zfact = 1.0;
+      memset(tsc, 0, 2 * n2 * sizeof(double));
+      memset(tsc_b, 0, 2 * n2 * sizeof(double));
+    }
+  } else {                                                   /* :97-100 */
+    zfact = 0.5;
+    memcpy(tsc_b, tsc, 2 * n2 * sizeof(double));
+  }
+  for (int jj = 2; jj <= jpj; ++jj)                          /* :104-109 */
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      tsc[I2(ji, jj)] = r1_rau0_rcp * qns[I2(ji, jj)];
+      tsc[n2 + I2(ji, jj)] = r1_rau0 * sfx[I2(ji, jj)];
+    }
+  if (nm->ln_linssh)                                         /* :111-118 */
+    for (int jj = 2; jj <= jpj; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        tsc[I2(ji, jj)] = tsc[I2(ji, jj)] + r1_rau0 * emp[I2(ji, jj)] * tsn[I2(ji, jj)];
+        tsc[n2 + I2(ji, jj)] = tsc[n2 + I2(ji, jj)] + r1_rau0 * emp[I2(ji, jj)] * tsn[n3 + I2(ji, jj)];
+      }
+  for (int jn = 0; jn < 2; ++jn)                             /* :123-129 */
+    for (int jj = 2; jj <= jpj; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t p = I2(ji, jj);
+        tsa[n3 * jn + p] = tsa[n3 * jn + p] + zfact * (tsc_b[n2 * jn + p] + tsc[n2 * jn + p]) / e3t_n[p];
+      }
+  return NEMO_OK;
+}
+
+/* tra_qsr (traqsr.F90:77-302), two bands (np_2BD): bound QSR, QSR_HC, QSR_HC_B,
+ * FRAQSR_1LEV, GDEPW_N, TSA. */
+int ora_tra_qsr(ora_ctx *c, int kt) {
+  const nemo_namelist *nm = &c->nam;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  const double *qsr = c->f[NEMO_F_QSR], *gdepw = c->f[NEMO_F_GDEPW_N];
+  double *hc = c->f[NEMO_F_QSR_HC], *hc_b = c->f[NEMO_F_QSR_HC_B], *fraq = c->f[NEMO_F_FRAQSR_1LEV];
+  double *tsa = c->f[NEMO_F_TSA];
+  if (!qsr || !gdepw || !hc || !hc_b || !fraq || !tsa) return NEMO_ERR_UNBOUND;
+  if (!nm->ln_traqsr) return NEMO_ERR_ARG;
+  const double *e3t_n = fld(c, NEMO_F_E3T_N), *wmask = c->wmask;
+  const double r1_rau0_rcp = 1.0 / (nm->rau0 * rcp_of(nm));
+  const double rn_abs = nm->rn_abs, xsi0r = 1.0 / nm->rn_si0, xsi1r = 1.0 / nm->rn_si1;
+  const int nksr = c->nksr;
+  double z1_2;
+  if (kt == nm->nit000) {                                    /* :134-143 */
+    if (nm->neuler != 0) z1_2 = 0.5;    /* restart: qsr_hc_b holds the restart's qsr_hc_b */
+    else { z1_2 = 1.0; memset(hc_b, 0, n3 * sizeof(double)); }
+  } else {                                                   /* :144-147 */
+    z1_2 = 0.5;
+    memcpy(hc_b, hc, n3 * sizeof(double));
+  }
+  const double zz0 = rn_abs * r1_rau0_rcp, zz1 = (1. - rn_abs) * r1_rau0_rcp;   /* :245-255 */
+  for (int jk = 1; jk <= nksr; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const double g0 = gdepw[I3(ji, jj, jk)], g1 = gdepw[I3(ji, jj, jk + 1)];
+        const double zc0 = zz0 * exp(-g0 * xsi0r) + zz1 * exp(-g0 * xsi1r);
+        const double zc1 = zz0 * exp(-g1 * xsi0r) + zz1 * exp(-g1 * xsi1r);
+        hc[I3(ji, jj, jk)] = qsr[I2(ji, jj)] * (zc0 * wmask[I3(ji, jj, jk)] - zc1 * wmask[I3(ji, jj, jk + 1)]);
+      }
+  for (int jk = 1; jk <= nksr; ++jk)                         /* :260-267 */
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t q = I3(ji, jj, jk);
+        tsa[q] = tsa[q] + z1_2 * (hc_b[q] + hc[q]) / e3t_n[q];
+      }
+  for (int jj = 2; jj <= jpj - 1; ++jj)                      /* :270-277 */
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      const size_t p = I2(ji, jj);
+      fraq[p] = qsr[p] != 0.0 ? hc[p] / (r1_rau0_rcp * qsr[p]) : 1.0;
+    }
+  lbc_closed(jpi, jpj, fraq, 1, 'T', 0.0);
+  return NEMO_OK;
+}
+
+int ora_nksr(const ora_ctx *c) { return c->nksr; }
 
 /* One model step (step.F90:96-305) with the path and the routines above: ua = va = 0,
  * dyn_spg_ts, div_hor + wzv, the dyn_zdf time step, tsa = 0, tra_adv, tra_ldf,

@@ -94,6 +94,11 @@ int ora_stp_model(ora_ctx *c, int kt);
 /* ldf_slp with ldf_slp_mxl (z-coordinate, no cavities, no partial steps); NMLN is
  * bound as an int array. */
 int ora_ldf_slp(ora_ctx *c, int kt, const double *prd, const double *pn2);
+/* tra_sbc and tra_qsr (two bands) on the bound surface forcing; nksr: the level of
+ * light extinction found at creation. */
+int ora_tra_sbc(ora_ctx *c, int kt);
+int ora_tra_qsr(ora_ctx *c, int kt);
+int ora_nksr(const ora_ctx *c);
 /* 1: start the work arrays standing for Fortran automatic arrays as NaN */
 void ora_set_poison(int on);
 

@@ -50,9 +50,11 @@ def lib():
         P("ora_tra_zdf_imp_adj", [vp, i, i, cp, d, vp, vp, i])
         P("ora_tra_nxt", [vp, i])
         P("ora_tra_nxt_adj", [vp, i, vp, vp, vp])
-        for name in ("ora_wzv", "ora_dyn_zdf_step", "ora_dyn_nxt", "ora_ssh_swp", "ora_stp_model"):
+        for name in ("ora_wzv", "ora_dyn_zdf_step", "ora_dyn_nxt", "ora_ssh_swp", "ora_stp_model", "ora_tra_sbc",
+                     "ora_tra_qsr"):
             P(name, [vp, i])
         P("ora_ldf_slp", [vp, i, vp, vp])
+        P("ora_nksr", [vp], C.c_int)
         P("ora_tra_ldf_blp", [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
         P("ora_zps_hde", [vp, i, i, vp, vp, vp])
         _lib = L
@@ -221,6 +223,15 @@ class Oracle:
 
     def stp_model(self, kt):
         self._ck(lib().ora_stp_model(self.h, kt), "stp_model")
+
+    def tra_sbc(self, kt):
+        self._ck(lib().ora_tra_sbc(self.h, kt), "tra_sbc")
+
+    def tra_qsr(self, kt):
+        self._ck(lib().ora_tra_qsr(self.h, kt), "tra_qsr")
+
+    def nksr(self):
+        return lib().ora_nksr(self.h)
 
     def ldf_slp(self, kt, prd, pn2):
         self._ck(lib().ora_ldf_slp(self.h, kt, _p(prd), _p(pn2)), "ldf_slp")
