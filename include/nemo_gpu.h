@@ -116,6 +116,8 @@ typedef struct nemo_namelist {
   int    ln_traqsr;       /* &namsbc: solar radiation penetrates (tra_qsr, 2 bands)     */
   double rn_abs, rn_si0, rn_si1; /* &namtra_qsr: near-surface fraction, extinction depths */
   double rcp;             /* specific heat (eosbn2.F90:1245: 3991.86795711963; 0 = that) */
+  int    ln_seos;         /* &nameos: the simplified equation of state (the only one here) */
+  double rn_a0, rn_b0, rn_lambda1, rn_lambda2, rn_mu1, rn_mu2, rn_nu; /* &nameos S-EOS  */
 } nemo_namelist;
 
 /* ------------------------------------------------------- module-global fields
@@ -185,6 +187,9 @@ enum nemo_field_id {
   NEMO_F_SBC_TSC, NEMO_F_SBC_TSC_B,    /* [S] x jpts                                  */
   NEMO_F_QSR_HC, NEMO_F_QSR_HC_B,      /* [T]                                         */
   NEMO_F_FRAQSR_1LEV,                  /* [S]                                         */
+  /* in situ density anomaly rhd (the input of dyn_hpg) and potential density rhop of
+   * the model step's eos (oce.F90) */
+  NEMO_F_RHD, NEMO_F_RHOP,             /* [T]                                         */
   NEMO_F_COUNT
 };
 
@@ -286,6 +291,24 @@ int nemo_gpu_tra_sbc(nemo_ctx *ctx, int kt);
  * included. Needs ln_traqsr. */
 int nemo_gpu_tra_qsr(nemo_ctx *ctx, int kt);
 
+/* The simplified equation of state (ln_seos, eosbn2.F90 np_seos; Vallis 2006) on
+ * levels 1..jpk-1 of every point; pts (jpi,jpj,jpk,2), pdep (jpi,jpj,jpk) depths:
+ * eos_insitu (:188-301): prd = in situ density anomaly (rho - rau0) / rau0;
+ * eos_insitu_pot (:304-470): prd and prhop, the potential density at the surface;
+ * rab_3d (:566-676): pab (jpi,jpj,jpk,2) the thermal / haline expansion ratios at
+ * the bound gdept_n; bn2 (:889-933): pn2 (jpi,jpj,jpk), the Brunt-Vaisala frequency
+ * squared on levels 2..jpk-1 from the bound gdept_n, gdepw_n and e3w_n.
+ * NEMO_ERR_UNSUPPORTED without ln_seos (the EOS-80 and TEOS-10 polynomials are not
+ * included). */
+int nemo_gpu_eos_insitu(nemo_ctx *ctx, const void *pts, void *prd, const void *pdep);
+int nemo_gpu_eos_insitu_pot(nemo_ctx *ctx, const void *pts, void *prd, void *prhop, const void *pdep);
+int nemo_gpu_rab_3d(nemo_ctx *ctx, const void *pts, void *pab);
+int nemo_gpu_bn2(nemo_ctx *ctx, const void *pts, const void *pab, void *pn2);
+
+/* dyn_hpg with hpg_zco (dynhpg.F90:258-323, z-coordinate with full steps): adds the
+ * hydrostatic pressure gradient of the bound rhd to the bound ua, va. */
+int nemo_gpu_dyn_hpg(nemo_ctx *ctx, int kt);
+
 /* zps_hde (zpshde.F90:41-148): pgtu, pgtv (jpi,jpj,kjpt) = the horizontal
  * gradients of pta (jpi,jpj,jpk,kjpt) at the partial-step bottom level of the u-
  * and v-points, with lbc_lnk. The optional density part (prd, pgru, pgrv) needs
@@ -347,7 +370,9 @@ int nemo_gpu_dyn_nxt(nemo_ctx *ctx, int kt);
 /* ssh_swp (sshwzv.F90:216-267), linear free surface. */
 int nemo_gpu_ssh_swp(nemo_ctx *ctx, int kt);
 /* One model step on the bound fields, in step.F90's order: ua = va = 0, dyn_spg_ts,
- * div_hor + wzv, the dyn_zdf time step, tsa = 0, tra_sbc and tra_qsr (when their
+ * (with the bound rhd and rhop and ln_seos: eos_insitu_pot of tsn at gdept_n and
+ * dyn_hpg after ua = va = 0), div_hor + wzv, the dyn_zdf time step, tsa = 0,
+ * tra_sbc and tra_qsr (when their
  * fields are bound; tra_qsr with ln_traqsr), tra_adv, tra_ldf, tra_zdf (with
  * the salinity clamp), tra_nxt, dyn_nxt, ssh_swp -- the hot path closed by the
  * routines above, with the momentum trends of dyn_adv, dyn_vor, dyn_ldf, dyn_hpg and
@@ -466,6 +491,7 @@ enum nemo_kernel_id {
   NEMO_K_LDF_SLP,      /* the three iso-neutral slope kernels */
   NEMO_K_ZPS_HDE,      /* partial-step bottom gradients */
   NEMO_K_TRA_SBC, NEMO_K_TRA_QSR, /* surface forcing of the tracers */
+  NEMO_K_EOS, NEMO_K_BN2, NEMO_K_DYN_HPG, /* equation of state, N^2, pressure gradient */
   NEMO_K_COUNT
 };
 

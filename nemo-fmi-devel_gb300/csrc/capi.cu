@@ -1041,6 +1041,45 @@ int run_tra_qsr(nemo_ctx* c, int kt) {
   return NEMO_OK;
 }
 
+template <class T>
+EosArgs<T> eos_args(const nemo_ctx* c, int what) {
+  const nemo_namelist& nm = c->nam;
+  EosArgs<T> a{};
+  a.a0 = (T)nm.rn_a0; a.b0 = (T)nm.rn_b0; a.lambda1 = (T)nm.rn_lambda1; a.lambda2 = (T)nm.rn_lambda2;
+  a.mu1 = (T)nm.rn_mu1; a.mu2 = (T)nm.rn_mu2; a.nu = (T)nm.rn_nu;
+  a.rau0 = (T)nm.rau0; a.r1_rau0 = (T)(1.0 / nm.rau0); a.grav = (T)nm.grav;
+  a.gdept = (const T*)c->f[NEMO_F_GDEPT_N]; a.gdepw = (const T*)c->f[NEMO_F_GDEPW_N];
+  a.what = what;
+  return a;
+}
+
+template <class T>
+int run_eos(nemo_ctx* c, int what, const void* pts, void* prd, void* prhop, const void* pdep, void* pab,
+            const void* pab_in, void* pn2) {
+  EosArgs<T> a = eos_args<T>(c, what);
+  a.pts = (const T*)pts; a.prd = (T*)prd; a.prhop = (T*)prhop; a.pdep = (const T*)pdep;
+  a.pab = (T*)pab; a.pab_in = (const T*)pab_in; a.pn2 = (T*)pn2;
+  cudaError_t e = launch_eos<T>(dom_now<T>(c), a, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "eos launch");
+  return NEMO_OK;
+}
+
+template <class T>
+int run_dyn_hpg(nemo_ctx* c) {
+  cudaError_t e = launch_dyn_hpg<T>(dom_now<T>(c), (const T*)c->f[NEMO_F_RHD], (T*)c->f[NEMO_F_UA],
+                                    (T*)c->f[NEMO_F_VA], (T)(-c->nam.grav * 0.5), c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "dyn_hpg launch");
+  return NEMO_OK;
+}
+
+// the model step's eos + dyn_hpg: rhd, rhop and gdept_n bound, the simplified eos,
+// z-coordinate with full steps
+bool hpg_on(const nemo_ctx* c) {
+  const nemo_namelist& nm = c->nam;
+  return c->f[NEMO_F_RHD] && c->f[NEMO_F_RHOP] && c->f[NEMO_F_GDEPT_N] && nm.ln_seos && !nm.ln_zps && !nm.ln_sco &&
+         !nm.ln_isfcav;
+}
+
 bool sbc_bound(const nemo_ctx* c) {
   for (int id : {NEMO_F_QNS, NEMO_F_QSR, NEMO_F_EMP, NEMO_F_SFX, NEMO_F_SBC_TSC, NEMO_F_SBC_TSC_B})
     if (!c->f[id]) return false;
@@ -1069,10 +1108,16 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
     cudaEventRecord(c->kc.ev[0], c->stream);
   }
   mark(0);
-  if (model) {  // ua = va = 0 (step.F90:183-184): no momentum trend outside the path
+  if (model) {  // ua = va = 0 (step.F90:183-184)
     const size_t bytes = (size_t)c->n3 * c->nmem * sizeof(T);
     CK(cudaMemsetAsync(F[NEMO_F_UA], 0, bytes, c->stream), "ua = 0");
     CK(cudaMemsetAsync(F[NEMO_F_VA], 0, bytes, c->stream), "va = 0");
+    if (hpg_on(c)) {  // eos of tsn at gdept_n (step.F90:165) and dyn_hpg (:193)
+      int s = run_eos<T>(c, 1, F[NEMO_F_TSN], F[NEMO_F_RHD], F[NEMO_F_RHOP], F[NEMO_F_GDEPT_N], nullptr, nullptr,
+                         nullptr);
+      if (!s) s = run_dyn_hpg<T>(c);
+      if (s) return s;
+    }
   }
   // Staged (host copies pending): each part waits only for the copies of the fields it
   // reads or writes -- dyn_spg_ts starts while the tracers and slopes still upload,
@@ -1573,6 +1618,57 @@ int nemo_gpu_ldf_slp(nemo_ctx* c, int kt, const void* prd, const void* pn2) {
   if (nm.ln_zps || nm.ln_isfcav || nm.ln_sco)
     return fail(c, NEMO_ERR_UNSUPPORTED, "ldf_slp: z-coordinate without partial steps or cavities only");
   return c->prec == NEMO_PREC_FP64 ? run_ldf_slp<double>(c, prd, pn2) : run_ldf_slp<float>(c, prd, pn2);
+}
+
+static int eos_check(nemo_ctx* c, const char* what) {
+  if (!c) return NEMO_ERR_ARG;
+  if (!c->nam.ln_seos)
+    return fail(c, NEMO_ERR_UNSUPPORTED, "%s: only the simplified equation of state (ln_seos) is included", what);
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  return NEMO_OK;
+}
+
+int nemo_gpu_eos_insitu(nemo_ctx* c, const void* pts, void* prd, const void* pdep) {
+  if (int s = eos_check(c, "eos_insitu")) return s;
+  if (!pts || !prd || !pdep) return fail(c, NEMO_ERR_ARG, "eos_insitu: null array");
+  return c->prec == NEMO_PREC_FP64 ? run_eos<double>(c, 0, pts, prd, nullptr, pdep, nullptr, nullptr, nullptr)
+                                   : run_eos<float>(c, 0, pts, prd, nullptr, pdep, nullptr, nullptr, nullptr);
+}
+
+int nemo_gpu_eos_insitu_pot(nemo_ctx* c, const void* pts, void* prd, void* prhop, const void* pdep) {
+  if (int s = eos_check(c, "eos_insitu_pot")) return s;
+  if (!pts || !prd || !prhop || !pdep) return fail(c, NEMO_ERR_ARG, "eos_insitu_pot: null array");
+  return c->prec == NEMO_PREC_FP64 ? run_eos<double>(c, 1, pts, prd, prhop, pdep, nullptr, nullptr, nullptr)
+                                   : run_eos<float>(c, 1, pts, prd, prhop, pdep, nullptr, nullptr, nullptr);
+}
+
+int nemo_gpu_rab_3d(nemo_ctx* c, const void* pts, void* pab) {
+  if (int s = eos_check(c, "rab_3d")) return s;
+  if (!pts || !pab) return fail(c, NEMO_ERR_ARG, "rab_3d: null array");
+  if (!c->f[NEMO_F_GDEPT_N]) return fail(c, NEMO_ERR_UNBOUND, "rab_3d: gdept_n must be bound");
+  return c->prec == NEMO_PREC_FP64 ? run_eos<double>(c, 2, pts, nullptr, nullptr, nullptr, pab, nullptr, nullptr)
+                                   : run_eos<float>(c, 2, pts, nullptr, nullptr, nullptr, pab, nullptr, nullptr);
+}
+
+int nemo_gpu_bn2(nemo_ctx* c, const void* pts, const void* pab, void* pn2) {
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (!pts || !pab || !pn2) return fail(c, NEMO_ERR_ARG, "bn2: null array");
+  if (!c->f[NEMO_F_GDEPT_N] || !c->f[NEMO_F_GDEPW_N])
+    return fail(c, NEMO_ERR_UNBOUND, "bn2: gdept_n and gdepw_n must be bound");
+  return c->prec == NEMO_PREC_FP64 ? run_eos<double>(c, 3, pts, nullptr, nullptr, nullptr, nullptr, pab, pn2)
+                                   : run_eos<float>(c, 3, pts, nullptr, nullptr, nullptr, nullptr, pab, pn2);
+}
+
+int nemo_gpu_dyn_hpg(nemo_ctx* c, int kt) {
+  (void)kt;
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (!c->f[NEMO_F_RHD] || !c->f[NEMO_F_UA] || !c->f[NEMO_F_VA])
+    return fail(c, NEMO_ERR_UNBOUND, "dyn_hpg: rhd, ua and va must be bound");
+  if (c->nam.ln_zps || c->nam.ln_sco || c->nam.ln_isfcav)
+    return fail(c, NEMO_ERR_UNSUPPORTED, "dyn_hpg: z-coordinate with full steps only (hpg_zco)");
+  return c->prec == NEMO_PREC_FP64 ? run_dyn_hpg<double>(c) : run_dyn_hpg<float>(c);
 }
 
 int nemo_gpu_tra_sbc(nemo_ctx* c, int kt) {

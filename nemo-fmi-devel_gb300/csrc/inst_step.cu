@@ -68,6 +68,20 @@ cudaError_t launch_tra_qsr(const Dom<T>& d, const QsrArgs<T>& a, cudaStream_t s)
   return cudaGetLastError();
 }
 
+template <class T>
+cudaError_t launch_eos(const Dom<T>& d, const EosArgs<T>& a, cudaStream_t s) {
+  k_eos<T><<<s_pt(d), dim3(SX, SY), 0, s>>>(d, a);
+  ktick(a.what == 3 ? NEMO_K_BN2 : NEMO_K_EOS, s);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_dyn_hpg(const Dom<T>& d, const T* rhd, T* ua, T* va, T zcoef0, cudaStream_t s) {
+  k_hpg_zco<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, rhd, ua, va, zcoef0);
+  ktick(NEMO_K_DYN_HPG, s);
+  return cudaGetLastError();
+}
+
 #define NEMO_STEP_INST(T)                                                                                      \
   template cudaError_t launch_wzv<T>(const Dom<T>&, const T*, const T*, T*, T, cudaStream_t);                  \
   template cudaError_t launch_dyn_zdf_step<T>(const Dom<T>&, const T*, const T*, T*, T*, T, cudaStream_t);     \
@@ -76,7 +90,9 @@ cudaError_t launch_tra_qsr(const Dom<T>& d, const QsrArgs<T>& a, cudaStream_t s)
   template cudaError_t launch_ldf_slp<T>(const Dom<T>&, const SlpArgs<T>&, cudaStream_t);                  \
   template cudaError_t launch_zps_hde<T>(const Dom<T>&, const T*, T*, T*, int, cudaStream_t);             \
   template cudaError_t launch_tra_sbc<T>(const Dom<T>&, const SbcArgs<T>&, cudaStream_t);                  \
-  template cudaError_t launch_tra_qsr<T>(const Dom<T>&, const QsrArgs<T>&, cudaStream_t);
+  template cudaError_t launch_tra_qsr<T>(const Dom<T>&, const QsrArgs<T>&, cudaStream_t);                  \
+  template cudaError_t launch_eos<T>(const Dom<T>&, const EosArgs<T>&, cudaStream_t);                      \
+  template cudaError_t launch_dyn_hpg<T>(const Dom<T>&, const T*, T*, T*, T, cudaStream_t);
 NEMO_STEP_INST(double)
 NEMO_STEP_INST(float)
 

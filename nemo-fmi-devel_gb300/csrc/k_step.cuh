@@ -479,4 +479,73 @@ __global__ void k_tra_qsr(Dom<T> d, QsrArgs<T> a) {
   a.fraq[(long)m * d.n2 + ij] = qsr != T(0) ? h1 / (a.r1_rau0_rcp * qsr) : T(1);
 }
 
+// ------------------------------------------- the simplified equation of state
+// eos_insitu (eosbn2.F90:276-292), eos_insitu_pot (:440-462), rab_3d (:645-661)
+// with np_seos, and bn2 (:889-933), one point per thread, each expression in the
+// reference's association.
+template <class T>
+__global__ void k_eos(Dom<T> d, EosArgs<T> a) {
+  const PtIdx c = pt_index(d);
+  if (!c.valid || c.k > d.jpk - 1) return;
+  const long q = (long)c.m * d.n3 + c.q;          // one 3-D field
+  const long qt = 2 * (long)c.m * d.n3 + c.q;     // temperature of (jpi,jpj,jpk,2)
+  const long qs = qt + d.n3;
+  const ColInfo ci = d.ci[c.ij];
+  if (a.what == 3) {
+    if (c.k < 2) return;
+    const T zrw = (a.gdepw[q] - a.gdept[q]) / (a.gdept[q - d.n2] - a.gdept[q]);
+    const T zaw = a.pab_in[qt] * (T(1) - zrw) + a.pab_in[qt - d.n2] * zrw;
+    const T zbw = a.pab_in[qs] * (T(1) - zrw) + a.pab_in[qs - d.n2] * zrw;
+    a.pn2[q] = a.grav * (zaw * (a.pts[qt - d.n2] - a.pts[qt]) - zbw * (a.pts[qs - d.n2] - a.pts[qs])) /
+               d.e3w_n(c.ij, c.k, c.m) * wmsk<T>(ci, c.k);
+    return;
+  }
+  const T zt = a.pts[qt] - T(10), zs = a.pts[qs] - T(35), ztm = tmsk<T>(ci, c.k);
+  if (a.what == 2) {
+    const T zh = a.gdept[q];
+    T zn = a.a0 * (T(1) + a.lambda1 * zt + a.mu1 * zh) + a.nu * zs;
+    a.pab[qt] = zn * a.r1_rau0 * ztm;
+    zn = a.b0 * (T(1) - a.lambda2 * zs - a.mu2 * zh) - a.nu * zt;
+    a.pab[qs] = zn * a.r1_rau0 * ztm;
+    return;
+  }
+  const T zh = a.pdep[q];
+  if (a.what == 0) {
+    const T zn = -a.a0 * (T(1) + T(0.5) * a.lambda1 * zt + a.mu1 * zh) * zt +
+                 a.b0 * (T(1) - T(0.5) * a.lambda2 * zs - a.mu2 * zh) * zs - a.nu * zt * zs;
+    a.prd[q] = zn * a.r1_rau0 * ztm;
+  } else {
+    T zn = -a.a0 * (T(1) + T(0.5) * a.lambda1 * zt) * zt + a.b0 * (T(1) - T(0.5) * a.lambda2 * zs) * zs -
+           a.nu * zt * zs;
+    a.prhop[q] = (a.rau0 + zn) * ztm;
+    zn = zn - (a.a0 * a.mu1 * zt + a.b0 * a.mu2 * zs) * zh;
+    a.prd[q] = zn * a.r1_rau0 * ztm;
+  }
+}
+
+// hpg_zco (dynhpg.F90:258-323), one interior column per thread: the pressure
+// gradient integrated downwards from the surface in registers.
+template <class T>
+__global__ void k_hpg_zco(Dom<T> d, const T* __restrict__ rhd, T* ua, T* va, T zcoef0) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i < 2 || i > d.jpi - 1 || j < 2 || j > d.jpj - 1) return;
+  const int m = blockIdx.z;
+  const long ij = (long)(i - 1) + (long)(j - 1) * d.jpi;
+  const long c3 = (long)m * d.n3 + ij;
+  const T r1u = d.r1_e1u[ij], r1v = d.r1_e2v[ij];
+  T zcoef1 = zcoef0 * d.e3w_n(ij, 1, m);
+  T zhpi = zcoef1 * (rhd[c3 + 1] - rhd[c3]) * r1u;
+  T zhpj = zcoef1 * (rhd[c3 + d.jpi] - rhd[c3]) * r1v;
+  ua[c3] = ua[c3] + zhpi;
+  va[c3] = va[c3] + zhpj;
+  for (int k = 2; k <= d.jpk - 1; ++k) {
+    const long q = c3 + (long)(k - 1) * d.n2, qu = q - d.n2;
+    zcoef1 = zcoef0 * d.e3w_n(ij, k, m);
+    zhpi = zhpi + zcoef1 * ((rhd[q + 1] + rhd[qu + 1]) - (rhd[q] + rhd[qu])) * r1u;
+    zhpj = zhpj + zcoef1 * ((rhd[q + d.jpi] + rhd[qu + d.jpi]) - (rhd[q] + rhd[qu])) * r1v;
+    ua[q] = ua[q] + zhpi;
+    va[q] = va[q] + zhpj;
+  }
+}
+
 }  // namespace nemo

@@ -47,6 +47,20 @@ struct QsrArgs {
   int nksr, mode;
 };
 
+// The simplified equation of state (np_seos), rab_3d and bn2; member strides are
+// those of the bound fields (2 x n3 for pts and pab, n3 for the others).
+template <class T>
+struct EosArgs {
+  const T *pts, *pdep, *gdept, *gdepw, *pab_in;
+  T *prd, *prhop, *pab, *pn2;
+  T a0, b0, lambda1, lambda2, mu1, mu2, nu, rau0, r1_rau0, grav;
+  int what;  // 0 eos_insitu, 1 eos_insitu_pot, 2 rab_3d, 3 bn2
+};
+
+template <class T>
+cudaError_t launch_eos(const Dom<T>& d, const EosArgs<T>& a, cudaStream_t s);
+template <class T>
+cudaError_t launch_dyn_hpg(const Dom<T>& d, const T* rhd, T* ua, T* va, T zcoef0, cudaStream_t s);
 template <class T>
 cudaError_t launch_tra_sbc(const Dom<T>& d, const SbcArgs<T>& a, cudaStream_t s);
 template <class T>

@@ -53,11 +53,15 @@ class Namelist(C.Structure):
                 ("rn_scal_load", C.c_double), ("grav", C.c_double), ("rau0", C.c_double),
                 ("nn_fct_h", C.c_int), ("nn_fct_v", C.c_int), ("rn_slpmax", C.c_double),
                 ("ln_traqsr", C.c_int), ("rn_abs", C.c_double), ("rn_si0", C.c_double), ("rn_si1", C.c_double),
-                ("rcp", C.c_double)]
+                ("rcp", C.c_double), ("ln_seos", C.c_int), ("rn_a0", C.c_double), ("rn_b0", C.c_double),
+                ("rn_lambda1", C.c_double), ("rn_lambda2", C.c_double), ("rn_mu1", C.c_double),
+                ("rn_mu2", C.c_double), ("rn_nu", C.c_double)]
 
 
 # members a namelist may leave out (&namtra_qsr of namelist_ref; rcp 0 selects 3991.86795711963)
-NAMELIST_DEFAULTS = {"ln_traqsr": 0, "rn_abs": 0.58, "rn_si0": 0.35, "rn_si1": 23.0, "rcp": 0.0}
+NAMELIST_DEFAULTS = {"ln_traqsr": 0, "rn_abs": 0.58, "rn_si0": 0.35, "rn_si1": 23.0, "rcp": 0.0,
+                     "ln_seos": 0, "rn_a0": 1.6550e-1, "rn_b0": 7.6554e-1, "rn_lambda1": 5.9520e-2,
+                     "rn_lambda2": 7.4914e-4, "rn_mu1": 1.4970e-4, "rn_mu2": 1.1090e-5, "rn_nu": 2.4341e-3}
 
 
 def make_desc(dom):
@@ -120,7 +124,11 @@ def load(path):
     _proto(lib, "nemo_gpu_tra_ldf_blp", i, [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
     _proto(lib, "nemo_gpu_zps_hde", i, [vp, i, i, vp, vp, vp])
     _proto(lib, "nemo_gpu_get_launch_shape", i, [vp, _ip, i])
-    for name in ("nemo_gpu_tra_sbc", "nemo_gpu_tra_qsr",
+    _proto(lib, "nemo_gpu_eos_insitu", i, [vp, vp, vp, vp])
+    _proto(lib, "nemo_gpu_eos_insitu_pot", i, [vp, vp, vp, vp, vp])
+    _proto(lib, "nemo_gpu_rab_3d", i, [vp, vp, vp])
+    _proto(lib, "nemo_gpu_bn2", i, [vp, vp, vp, vp])
+    for name in ("nemo_gpu_tra_sbc", "nemo_gpu_tra_qsr", "nemo_gpu_dyn_hpg",
                  "nemo_gpu_wzv", "nemo_gpu_dyn_zdf_step", "nemo_gpu_dyn_nxt", "nemo_gpu_ssh_swp",
                  "nemo_gpu_stp_model"):
         _proto(lib, name, i, [vp, i])

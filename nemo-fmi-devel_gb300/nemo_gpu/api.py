@@ -227,6 +227,22 @@ class Context:
     def tra_qsr(self, kt):
         self._ck(self.lib.nemo_gpu_tra_qsr(self.h, kt), "tra_qsr")
 
+    def eos_insitu(self, pts, prd, pdep):
+        self._ck(self.lib.nemo_gpu_eos_insitu(self.h, _ptr(pts), _ptr(prd), _ptr(pdep)), "eos_insitu")
+
+    def eos_insitu_pot(self, pts, prd, prhop, pdep):
+        self._ck(self.lib.nemo_gpu_eos_insitu_pot(self.h, _ptr(pts), _ptr(prd), _ptr(prhop), _ptr(pdep)),
+                 "eos_insitu_pot")
+
+    def rab_3d(self, pts, pab):
+        self._ck(self.lib.nemo_gpu_rab_3d(self.h, _ptr(pts), _ptr(pab)), "rab_3d")
+
+    def bn2(self, pts, pab, pn2):
+        self._ck(self.lib.nemo_gpu_bn2(self.h, _ptr(pts), _ptr(pab), _ptr(pn2)), "bn2")
+
+    def dyn_hpg(self, kt):
+        self._ck(self.lib.nemo_gpu_dyn_hpg(self.h, kt), "dyn_hpg")
+
     def stp_model(self, kt):
         """One model step: the hot path closed by wzv, the dyn_zdf time step, tra_nxt,
         dyn_nxt and ssh_swp (see nemo_gpu.h)."""

@@ -34,7 +34,10 @@ def namelist(**over):
         ln_bt_fw=1, ln_bt_av=1, nn_bt_flt=1, ln_bt_auto=1, nn_baro=30, rn_bt_cmax=0.8, rn_bt_alpha=0.0,
         nvor_scheme=1, nn_een_e3f=0, ln_dynadv_vec=1, ln_sco=0, ln_apr_dyn=0, rn_scal_load=0.0,
         grav=GRAV, rau0=RAU0, nn_fct_h=2, nn_fct_v=2, rn_slpmax=0.01,
-        ln_traqsr=1, rn_abs=0.58, rn_si0=0.35, rn_si1=23.0, rcp=RCP)
+        ln_traqsr=1, rn_abs=0.58, rn_si0=0.35, rn_si1=23.0, rcp=RCP,
+        # GYRE selects EOS-80 (not included); the simplified eos of namelist_ref &nameos
+        ln_seos=0, rn_a0=1.6550e-1, rn_b0=7.6554e-1, rn_lambda1=5.9520e-2, rn_lambda2=7.4914e-4,
+        rn_mu1=1.4970e-4, rn_mu2=1.1090e-5, rn_nu=2.4341e-3)
     nam.update(over)
     return nam
 

@@ -2407,6 +2407,113 @@ int ora_tra_qsr(ora_ctx *c, int kt) {
 
 int ora_nksr(const ora_ctx *c) { return c->nksr; }
 
+/* ------------------------------------------- simplified equation of state */
+/* eos_insitu (eosbn2.F90:276-292), np_seos: levels 1..jpk-1 of every point. */
+int ora_eos_insitu(ora_ctx *c, const double *pts, double *prd, const double *pdep) {
+  const nemo_namelist *nm = &c->nam;
+  if (!nm->ln_seos) return NEMO_ERR_UNSUPPORTED;
+  const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk, nl = (size_t)c->jpi * c->jpj * (c->jpk - 1);
+  const double r1_rau0 = 1.0 / nm->rau0;
+  for (size_t q = 0; q < nl; ++q) {
+    const double zt = pts[q] - 10., zs = pts[n3 + q] - 35., zh = pdep[q], ztm = c->tmask[q];
+    const double zn = -nm->rn_a0 * (1. + 0.5 * nm->rn_lambda1 * zt + nm->rn_mu1 * zh) * zt
+                      + nm->rn_b0 * (1. - 0.5 * nm->rn_lambda2 * zs - nm->rn_mu2 * zh) * zs
+                      - nm->rn_nu * zt * zs;
+    prd[q] = zn * r1_rau0 * ztm;
+  }
+  return NEMO_OK;
+}
+
+/* eos_insitu_pot (eosbn2.F90:440-462), np_seos. */
+int ora_eos_insitu_pot(ora_ctx *c, const double *pts, double *prd, double *prhop, const double *pdep) {
+  const nemo_namelist *nm = &c->nam;
+  if (!nm->ln_seos) return NEMO_ERR_UNSUPPORTED;
+  const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk, nl = (size_t)c->jpi * c->jpj * (c->jpk - 1);
+  const double r1_rau0 = 1.0 / nm->rau0;
+  for (size_t q = 0; q < nl; ++q) {
+    const double zt = pts[q] - 10., zs = pts[n3 + q] - 35., zh = pdep[q], ztm = c->tmask[q];
+    double zn = -nm->rn_a0 * (1. + 0.5 * nm->rn_lambda1 * zt) * zt
+                + nm->rn_b0 * (1. - 0.5 * nm->rn_lambda2 * zs) * zs
+                - nm->rn_nu * zt * zs;
+    prhop[q] = (nm->rau0 + zn) * ztm;
+    zn = zn - (nm->rn_a0 * nm->rn_mu1 * zt + nm->rn_b0 * nm->rn_mu2 * zs) * zh;
+    prd[q] = zn * r1_rau0 * ztm;
+  }
+  return NEMO_OK;
+}
+
+/* rab_3d (eosbn2.F90:645-661), np_seos, at the bound GDEPT_N. */
+int ora_rab_3d(ora_ctx *c, const double *pts, double *pab) {
+  const nemo_namelist *nm = &c->nam;
+  if (!nm->ln_seos) return NEMO_ERR_UNSUPPORTED;
+  const double *gdept = c->f[NEMO_F_GDEPT_N];
+  if (!gdept) return NEMO_ERR_UNBOUND;
+  const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk, nl = (size_t)c->jpi * c->jpj * (c->jpk - 1);
+  const double r1_rau0 = 1.0 / nm->rau0;
+  for (size_t q = 0; q < nl; ++q) {
+    const double zt = pts[q] - 10., zs = pts[n3 + q] - 35., zh = gdept[q], ztm = c->tmask[q];
+    double zn = nm->rn_a0 * (1. + nm->rn_lambda1 * zt + nm->rn_mu1 * zh) + nm->rn_nu * zs;
+    pab[q] = zn * r1_rau0 * ztm;
+    zn = nm->rn_b0 * (1. - nm->rn_lambda2 * zs - nm->rn_mu2 * zh) - nm->rn_nu * zt;
+    pab[n3 + q] = zn * r1_rau0 * ztm;
+  }
+  return NEMO_OK;
+}
+
+/* bn2 (eosbn2.F90:889-933): levels 2..jpk-1 of every point. */
+int ora_bn2(ora_ctx *c, const double *pts, const double *pab, double *pn2) {
+  const nemo_namelist *nm = &c->nam;
+  const double *gdept = c->f[NEMO_F_GDEPT_N], *gdepw = c->f[NEMO_F_GDEPW_N];
+  if (!gdept || !gdepw) return NEMO_ERR_UNBOUND;
+  const double *e3w = fld(c, NEMO_F_E3W_N);
+  const size_t n2 = (size_t)c->jpi * c->jpj, n3 = n2 * c->jpk;
+  for (int jk = 2; jk <= c->jpk - 1; ++jk)
+    for (size_t p = 0; p < n2; ++p) {
+      const size_t q = p + n2 * (jk - 1), qu = q - n2;
+      const double zrw = (gdepw[q] - gdept[q]) / (gdept[qu] - gdept[q]);
+      const double zaw = pab[q] * (1. - zrw) + pab[qu] * zrw;
+      const double zbw = pab[n3 + q] * (1. - zrw) + pab[n3 + qu] * zrw;
+      pn2[q] = nm->grav * (zaw * (pts[qu] - pts[q]) - zbw * (pts[n3 + qu] - pts[n3 + q])) / e3w[q] * c->wmask[q];
+    }
+  return NEMO_OK;
+}
+
+/* dyn_hpg with hpg_zco (dynhpg.F90:258-323): bound RHD, UA, VA. */
+int ora_dyn_hpg(ora_ctx *c, int kt) {
+  (void)kt;
+  const nemo_namelist *nm = &c->nam;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const double *rhd = c->f[NEMO_F_RHD];
+  double *ua = c->f[NEMO_F_UA], *va = c->f[NEMO_F_VA];
+  if (!rhd || !ua || !va) return NEMO_ERR_UNBOUND;
+  if (nm->ln_zps || nm->ln_sco || nm->ln_isfcav) return NEMO_ERR_UNSUPPORTED;
+  const double *e3w = fld(c, NEMO_F_E3W_N);
+  const double zcoef0 = -nm->grav * 0.5;
+  const size_t n2 = (size_t)jpi * jpj;
+  double *zhpi = zalloc(n2), *zhpj = zalloc(n2);
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      const size_t p = I2(ji, jj);
+      const double zcoef1 = zcoef0 * e3w[p];
+      zhpi[p] = zcoef1 * (rhd[I2(ji + 1, jj)] - rhd[p]) * c->r1_e1u[p];
+      zhpj[p] = zcoef1 * (rhd[I2(ji, jj + 1)] - rhd[p]) * c->r1_e2v[p];
+      ua[p] = ua[p] + zhpi[p];
+      va[p] = va[p] + zhpj[p];
+    }
+  for (int jk = 2; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t p = I2(ji, jj), q = I3(ji, jj, jk), qu = q - n2;
+        const double zcoef1 = zcoef0 * e3w[q];
+        zhpi[p] = zhpi[p] + zcoef1 * ((rhd[q + 1] + rhd[qu + 1]) - (rhd[q] + rhd[qu])) * c->r1_e1u[p];
+        zhpj[p] = zhpj[p] + zcoef1 * ((rhd[q + jpi] + rhd[qu + jpi]) - (rhd[q] + rhd[qu])) * c->r1_e2v[p];
+        ua[q] = ua[q] + zhpi[p];
+        va[q] = va[q] + zhpj[p];
+      }
+  free(zhpi); free(zhpj);
+  return NEMO_OK;
+}
+
 /* One model step (step.F90:96-305) with the path and the routines above: ua = va = 0,
  * dyn_spg_ts, div_hor + wzv, the dyn_zdf time step, tsa = 0, tra_adv, tra_ldf,
  * tra_zdf, tra_nxt, dyn_nxt, ssh_swp. */
@@ -2415,7 +2522,13 @@ int ora_stp_model(ora_ctx *c, int kt) {
   if (!c->f[NEMO_F_UA] || !c->f[NEMO_F_VA]) return NEMO_ERR_UNBOUND;
   memset(c->f[NEMO_F_UA], 0, n3 * sizeof(double));
   memset(c->f[NEMO_F_VA], 0, n3 * sizeof(double));
-  int st = ora_dyn_spg_ts(c, kt);
+  int st = 0;
+  if (c->f[NEMO_F_RHD] && c->f[NEMO_F_RHOP] && c->nam.ln_seos) {   /* step.F90:165, :193 */
+    if (!c->f[NEMO_F_GDEPT_N]) return NEMO_ERR_UNBOUND;
+    st = ora_eos_insitu_pot(c, c->f[NEMO_F_TSN], c->f[NEMO_F_RHD], c->f[NEMO_F_RHOP], c->f[NEMO_F_GDEPT_N]);
+    if (!st) st = ora_dyn_hpg(c, kt);
+  }
+  if (!st) st = ora_dyn_spg_ts(c, kt);
   if (!st) st = ora_wzv(c, kt);
   if (!st) st = ora_dyn_zdf_step(c, kt);
   if (!st) st = stp_tracers(c, kt);

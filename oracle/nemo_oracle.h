@@ -99,6 +99,12 @@ int ora_ldf_slp(ora_ctx *c, int kt, const double *prd, const double *pn2);
 int ora_tra_sbc(ora_ctx *c, int kt);
 int ora_tra_qsr(ora_ctx *c, int kt);
 int ora_nksr(const ora_ctx *c);
+/* the simplified equation of state, N^2 and hpg_zco */
+int ora_eos_insitu(ora_ctx *c, const double *pts, double *prd, const double *pdep);
+int ora_eos_insitu_pot(ora_ctx *c, const double *pts, double *prd, double *prhop, const double *pdep);
+int ora_rab_3d(ora_ctx *c, const double *pts, double *pab);
+int ora_bn2(ora_ctx *c, const double *pts, const double *pab, double *pn2);
+int ora_dyn_hpg(ora_ctx *c, int kt);
 /* 1: start the work arrays standing for Fortran automatic arrays as NaN */
 void ora_set_poison(int on);
 

@@ -55,6 +55,11 @@ def lib():
             P(name, [vp, i])
         P("ora_ldf_slp", [vp, i, vp, vp])
         P("ora_nksr", [vp], C.c_int)
+        P("ora_eos_insitu", [vp, vp, vp, vp])
+        P("ora_eos_insitu_pot", [vp, vp, vp, vp, vp])
+        P("ora_rab_3d", [vp, vp, vp])
+        P("ora_bn2", [vp, vp, vp, vp])
+        P("ora_dyn_hpg", [vp, i])
         P("ora_tra_ldf_blp", [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
         P("ora_zps_hde", [vp, i, i, vp, vp, vp])
         _lib = L
@@ -229,6 +234,21 @@ class Oracle:
 
     def tra_qsr(self, kt):
         self._ck(lib().ora_tra_qsr(self.h, kt), "tra_qsr")
+
+    def eos_insitu(self, pts, prd, pdep):
+        self._ck(lib().ora_eos_insitu(self.h, _p(pts), _p(prd), _p(pdep)), "eos_insitu")
+
+    def eos_insitu_pot(self, pts, prd, prhop, pdep):
+        self._ck(lib().ora_eos_insitu_pot(self.h, _p(pts), _p(prd), _p(prhop), _p(pdep)), "eos_insitu_pot")
+
+    def rab_3d(self, pts, pab):
+        self._ck(lib().ora_rab_3d(self.h, _p(pts), _p(pab)), "rab_3d")
+
+    def bn2(self, pts, pab, pn2):
+        self._ck(lib().ora_bn2(self.h, _p(pts), _p(pab), _p(pn2)), "bn2")
+
+    def dyn_hpg(self, kt):
+        self._ck(lib().ora_dyn_hpg(self.h, kt), "dyn_hpg")
 
     def nksr(self):
         return lib().ora_nksr(self.h)
