@@ -190,6 +190,10 @@ enum nemo_field_id {
   /* in situ density anomaly rhd (the input of dyn_hpg) and potential density rhop of
    * the model step's eos (oce.F90) */
   NEMO_F_RHD, NEMO_F_RHOP,             /* [T]                                         */
+  /* zdf_mxl (zdfmxl.F90): its input, the before Brunt-Vaisala frequency rn2b
+   * (zdf_oce), and its turbocline depth hmld (written when bound) */
+  NEMO_F_RN2B,                         /* [T]                                         */
+  NEMO_F_HMLD,                         /* [S]                                         */
   NEMO_F_COUNT
 };
 
@@ -308,6 +312,12 @@ int nemo_gpu_bn2(nemo_ctx *ctx, const void *pts, const void *pab, void *pn2);
 /* dyn_hpg with hpg_zco (dynhpg.F90:258-323, z-coordinate with full steps): adds the
  * hydrostatic pressure gradient of the bound rhd to the bound ua, va. */
 int nemo_gpu_dyn_hpg(nemo_ctx *ctx, int kt);
+
+/* zdf_mxl (zdfmxl.F90:59-141): the mixed layer of the bound rn2b (density criterion
+ * rho_c = 0.01 integrated from the first W-level below 10 m, nlb10 of domzgr.F90:144-
+ * 146) into the bound nmln (int32), hmlp and hmlpt, and the turbocline of the bound
+ * avt (avt_c = 5e-4) into hmld when bound; reads the bound gdept_n and gdepw_n. */
+int nemo_gpu_zdf_mxl(nemo_ctx *ctx, int kt);
 
 /* zps_hde (zpshde.F90:41-148): pgtu, pgtv (jpi,jpj,kjpt) = the horizontal
  * gradients of pta (jpi,jpj,jpk,kjpt) at the partial-step bottom level of the u-
@@ -492,6 +502,7 @@ enum nemo_kernel_id {
   NEMO_K_ZPS_HDE,      /* partial-step bottom gradients */
   NEMO_K_TRA_SBC, NEMO_K_TRA_QSR, /* surface forcing of the tracers */
   NEMO_K_EOS, NEMO_K_BN2, NEMO_K_DYN_HPG, /* equation of state, N^2, pressure gradient */
+  NEMO_K_ZDF_MXL,      /* mixed-layer depth */
   NEMO_K_COUNT
 };
 

@@ -58,6 +58,7 @@ struct nemo_ctx {
   // spg
   int nn_baro = 0, icycle = 0;
   int nksr = 0;  // tra_qsr: level of light extinction of the two bands
+  int nlb10 = 0;  // zdf_mxl: the first W-level below 10 m
   double rdtbt = 0;
   std::vector<double> wgt1, wgt2;
   double* d_wgt1 = nullptr;
@@ -466,6 +467,24 @@ int ext_lev(const nemo_ctx* c, double prldex, double pqsr_frc) {
   return pjl;
 }
 
+// nlb10 (domzgr.F90:144-146): the shallowest W-level deeper than 10 m less a tenth
+// of the thinnest W-layer, on the 1-D reference profile (the rest-state column with
+// the most wet levels; gdepw_1d from its e3t_0 as e3_to_depth sums them).
+int nlb10_of(const nemo_ctx* c) {
+  const size_t n2 = c->n2;
+  size_t best = 0;
+  for (size_t p = 0; p < n2; ++p)
+    if (c->mbkt[p] > c->mbkt[best]) best = p;
+  double e3wmin = 1e300, gdepw = 0.0;
+  for (int jk = 1; jk <= c->jpk; ++jk) e3wmin = std::min(e3wmin, c->e3_0[3][best + n2 * (jk - 1)]);
+  const double zrefdep = 10.0 - 0.1 * e3wmin;
+  for (int jk = 1; jk <= c->jpk; ++jk) {
+    if (gdepw > zrefdep) return jk;
+    gdepw = gdepw + c->e3_0[0][best + n2 * (jk - 1)];
+  }
+  return c->jpk;
+}
+
 // Domain derivation (dommsk.F90:133-238, domzgr.F90:292-314, domhgr.F90:133-151,
 // domain.F90:149-183) and spg set-up (dynspg_ts.F90:1479-1493).
 int derive_domain(nemo_ctx* c, const nemo_dom_desc* dm) {
@@ -592,6 +611,7 @@ int derive_domain(nemo_ctx* c, const nemo_dom_desc* dm) {
   ts_wgt(c, c->nam.ln_bt_av, c->nam.ln_bt_fw, &jpit);
   c->icycle = jpit;
   c->nksr = ext_lev(c, c->nam.rn_si1 > 0 ? c->nam.rn_si1 : 23.0, 100.0);
+  c->nlb10 = nlb10_of(c);
   coriolis_factors(c, tmask, umask);
   return NEMO_OK;
 }
@@ -1038,6 +1058,22 @@ int run_tra_qsr(nemo_ctx* c, int kt) {
   a.nksr = c->nksr;
   cudaError_t e = launch_tra_qsr<T>(dom_now<T>(c), a, c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "tra_qsr launch");
+  return NEMO_OK;
+}
+
+template <class T>
+int run_zdf_mxl(nemo_ctx* c) {
+  void* const* F = c->f;
+  MxlArgs<T> a{};
+  a.rn2b = (const T*)F[NEMO_F_RN2B]; a.avt = (const T*)F[NEMO_F_AVT];
+  a.gdept = (const T*)F[NEMO_F_GDEPT_N]; a.gdepw = (const T*)F[NEMO_F_GDEPW_N];
+  a.nmln = (int*)F[NEMO_F_NMLN]; a.hmlp = (T*)F[NEMO_F_HMLP]; a.hmlpt = (T*)F[NEMO_F_HMLPT];
+  a.hmld = (T*)F[NEMO_F_HMLD];
+  a.zn2_c = (T)(c->nam.grav * 0.01 * (1.0 / c->nam.rau0));
+  a.avt_c = (T)5.e-4;
+  a.nlb10 = c->nlb10;
+  cudaError_t e = launch_zdf_mxl<T>(dom_now<T>(c), a, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "zdf_mxl launch");
   return NEMO_OK;
 }
 
@@ -1618,6 +1654,15 @@ int nemo_gpu_ldf_slp(nemo_ctx* c, int kt, const void* prd, const void* pn2) {
   if (nm.ln_zps || nm.ln_isfcav || nm.ln_sco)
     return fail(c, NEMO_ERR_UNSUPPORTED, "ldf_slp: z-coordinate without partial steps or cavities only");
   return c->prec == NEMO_PREC_FP64 ? run_ldf_slp<double>(c, prd, pn2) : run_ldf_slp<float>(c, prd, pn2);
+}
+
+int nemo_gpu_zdf_mxl(nemo_ctx* c, int kt) {
+  (void)kt;
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  for (int id : {NEMO_F_RN2B, NEMO_F_AVT, NEMO_F_GDEPT_N, NEMO_F_GDEPW_N, NEMO_F_NMLN, NEMO_F_HMLP, NEMO_F_HMLPT})
+    if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "zdf_mxl: field %d must be bound", id);
+  return c->prec == NEMO_PREC_FP64 ? run_zdf_mxl<double>(c) : run_zdf_mxl<float>(c);
 }
 
 static int eos_check(nemo_ctx* c, const char* what) {

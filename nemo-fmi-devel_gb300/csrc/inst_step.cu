@@ -82,6 +82,13 @@ cudaError_t launch_dyn_hpg(const Dom<T>& d, const T* rhd, T* ua, T* va, T zcoef0
   return cudaGetLastError();
 }
 
+template <class T>
+cudaError_t launch_zdf_mxl(const Dom<T>& d, const MxlArgs<T>& a, cudaStream_t s) {
+  k_zdf_mxl<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a);
+  ktick(NEMO_K_ZDF_MXL, s);
+  return cudaGetLastError();
+}
+
 #define NEMO_STEP_INST(T)                                                                                      \
   template cudaError_t launch_wzv<T>(const Dom<T>&, const T*, const T*, T*, T, cudaStream_t);                  \
   template cudaError_t launch_dyn_zdf_step<T>(const Dom<T>&, const T*, const T*, T*, T*, T, cudaStream_t);     \
@@ -92,7 +99,8 @@ cudaError_t launch_dyn_hpg(const Dom<T>& d, const T* rhd, T* ua, T* va, T zcoef0
   template cudaError_t launch_tra_sbc<T>(const Dom<T>&, const SbcArgs<T>&, cudaStream_t);                  \
   template cudaError_t launch_tra_qsr<T>(const Dom<T>&, const QsrArgs<T>&, cudaStream_t);                  \
   template cudaError_t launch_eos<T>(const Dom<T>&, const EosArgs<T>&, cudaStream_t);                      \
-  template cudaError_t launch_dyn_hpg<T>(const Dom<T>&, const T*, T*, T*, T, cudaStream_t);
+  template cudaError_t launch_dyn_hpg<T>(const Dom<T>&, const T*, T*, T*, T, cudaStream_t);              \
+  template cudaError_t launch_zdf_mxl<T>(const Dom<T>&, const MxlArgs<T>&, cudaStream_t);
 NEMO_STEP_INST(double)
 NEMO_STEP_INST(float)
 

@@ -548,4 +548,35 @@ __global__ void k_hpg_zco(Dom<T> d, const T* __restrict__ rhd, T* ua, T* va, T z
   }
 }
 
+// zdf_mxl (zdfmxl.F90:59-141), one (i,j) column per thread: N^2 integrated
+// downwards from nlb10 against the density criterion, the turbocline searched upwards
+// from the bottom, then the depths of the two levels.
+template <class T>
+__global__ void k_zdf_mxl(Dom<T> d, MxlArgs<T> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i > d.jpi || j > d.jpj) return;
+  const int m = blockIdx.z;
+  const long ij = (long)(i - 1) + (long)(j - 1) * d.jpi;
+  const long c3 = (long)m * d.n3 + ij, c2 = (long)m * d.n2 + ij;
+  const int ikt = d.mbkt[ij];
+  const ColInfo ci = d.ci[ij];
+  int nmln = a.nlb10;
+  T h = T(0);
+  for (int k = a.nlb10; k <= d.jpk - 1; ++k) {
+    const T n2 = a.rn2b[c3 + (long)(k - 1) * d.n2];
+    h = h + (n2 > T(0) ? n2 : T(0)) * d.e3w_n(ij, k, m);
+    if (h < a.zn2_c) nmln = (k < ikt ? k : ikt) + 1;
+  }
+  const T ssm = d.ssmask[ij];
+  if (a.hmld) {
+    int imld = ikt + 1;
+    for (int k = d.jpk - 1; k >= a.nlb10; --k)
+      if (a.avt[c3 + (long)(k - 1) * d.n2] < a.avt_c * wmsk<T>(ci, k)) imld = k;
+    a.hmld[c2] = a.gdepw[c3 + (long)(imld - 1) * d.n2] * ssm;
+  }
+  a.nmln[c2] = nmln;
+  a.hmlp[c2] = a.gdepw[c3 + (long)(nmln - 1) * d.n2] * ssm;
+  a.hmlpt[c2] = a.gdept[c3 + (long)(nmln - 2) * d.n2] * ssm;
+}
+
 }  // namespace nemo

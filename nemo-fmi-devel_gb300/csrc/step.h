@@ -58,6 +58,17 @@ struct EosArgs {
 };
 
 template <class T>
+struct MxlArgs {
+  const T *rn2b, *avt, *gdept, *gdepw;
+  int* nmln;
+  T *hmlp, *hmlpt, *hmld;  // hmld may be null
+  T zn2_c, avt_c;
+  int nlb10;
+};
+
+template <class T>
+cudaError_t launch_zdf_mxl(const Dom<T>& d, const MxlArgs<T>& a, cudaStream_t s);
+template <class T>
 cudaError_t launch_eos(const Dom<T>& d, const EosArgs<T>& a, cudaStream_t s);
 template <class T>
 cudaError_t launch_dyn_hpg(const Dom<T>& d, const T* rhd, T* ua, T* va, T zcoef0, cudaStream_t s);

@@ -240,6 +240,9 @@ class Context:
     def bn2(self, pts, pab, pn2):
         self._ck(self.lib.nemo_gpu_bn2(self.h, _ptr(pts), _ptr(pab), _ptr(pn2)), "bn2")
 
+    def zdf_mxl(self, kt):
+        self._ck(self.lib.nemo_gpu_zdf_mxl(self.h, kt), "zdf_mxl")
+
     def dyn_hpg(self, kt):
         self._ck(self.lib.nemo_gpu_dyn_hpg(self.h, kt), "dyn_hpg")
 

@@ -2407,6 +2407,61 @@ int ora_tra_qsr(ora_ctx *c, int kt) {
 
 int ora_nksr(const ora_ctx *c) { return c->nksr; }
 
+/* nlb10 (domzgr.F90:144-146): the shallowest W-level deeper than 10 m less a tenth of
+ * the thinnest W-layer, on the 1-D reference profile (the rest-state column with
+ * the most wet levels: gdepw_1d from its e3t_0 as e3_to_depth sums them). */
+static int nlb10_of(const ora_ctx *c) {
+  const size_t n2 = (size_t)c->jpi * c->jpj;
+  size_t best = 0;
+  for (size_t p = 0; p < n2; ++p)
+    if (c->mbkt[p] > c->mbkt[best]) best = p;
+  double e3wmin = 1e300, gdepw = 0.0;
+  for (int jk = 1; jk <= c->jpk; ++jk) e3wmin = dmin(e3wmin, c->e3w_0[best + n2 * (jk - 1)]);
+  const double zrefdep = 10.0 - 0.1 * e3wmin;
+  for (int jk = 1; jk <= c->jpk; ++jk) {
+    if (gdepw > zrefdep) return jk;
+    gdepw = gdepw + c->e3t_0[best + n2 * (jk - 1)];
+  }
+  return c->jpk;
+}
+
+/* zdf_mxl (zdfmxl.F90:59-141): bound RN2B, AVT, GDEPT_N, GDEPW_N -> NMLN (int),
+ * HMLP, HMLPT, HMLD (when bound). */
+int ora_zdf_mxl(ora_ctx *c, int kt) {
+  (void)kt;
+  const nemo_namelist *nm = &c->nam;
+  const int jpk = c->jpk;
+  const size_t n2 = (size_t)c->jpi * c->jpj;
+  const double *rn2b = c->f[NEMO_F_RN2B], *avt = c->f[NEMO_F_AVT];
+  const double *gdept = c->f[NEMO_F_GDEPT_N], *gdepw = c->f[NEMO_F_GDEPW_N];
+  int *nmln = (int *)c->f[NEMO_F_NMLN];
+  double *hmlp = c->f[NEMO_F_HMLP], *hmlpt = c->f[NEMO_F_HMLPT], *hmld = c->f[NEMO_F_HMLD];
+  if (!rn2b || !avt || !gdept || !gdepw || !nmln || !hmlp || !hmlpt) return NEMO_ERR_UNBOUND;
+  const double *e3w = fld(c, NEMO_F_E3W_N);
+  const int nlb10 = nlb10_of(c);
+  const double rho_c = 0.01, avt_c = 5.e-4;
+  const double zN2_c = nm->grav * rho_c * (1.0 / nm->rau0);
+  for (size_t p = 0; p < n2; ++p) { nmln[p] = nlb10; hmlp[p] = 0.0; }
+  for (int jk = nlb10; jk <= jpk - 1; ++jk)
+    for (size_t p = 0; p < n2; ++p) {
+      const int ikt = c->mbkt[p];
+      hmlp[p] = hmlp[p] + dmax(rn2b[p + n2 * (jk - 1)], 0.0) * e3w[p + n2 * (jk - 1)];
+      if (hmlp[p] < zN2_c) nmln[p] = (jk < ikt ? jk : ikt) + 1;
+    }
+  for (size_t p = 0; p < n2; ++p) {
+    int imld = c->mbkt[p] + 1;
+    for (int jk = jpk - 1; jk >= nlb10; --jk)
+      if (avt[p + n2 * (jk - 1)] < avt_c * c->wmask[p + n2 * (jk - 1)]) imld = jk;
+    const int iikn = nmln[p];
+    if (hmld) hmld[p] = gdepw[p + n2 * (imld - 1)] * c->ssmask[p];
+    hmlp[p] = gdepw[p + n2 * (iikn - 1)] * c->ssmask[p];
+    hmlpt[p] = gdept[p + n2 * (iikn - 2)] * c->ssmask[p];
+  }
+  return NEMO_OK;
+}
+
+int ora_nlb10(const ora_ctx *c) { return nlb10_of(c); }
+
 /* ------------------------------------------- simplified equation of state */
 /* eos_insitu (eosbn2.F90:276-292), np_seos: levels 1..jpk-1 of every point. */
 int ora_eos_insitu(ora_ctx *c, const double *pts, double *prd, const double *pdep) {

@@ -105,6 +105,9 @@ int ora_eos_insitu_pot(ora_ctx *c, const double *pts, double *prd, double *prhop
 int ora_rab_3d(ora_ctx *c, const double *pts, double *pab);
 int ora_bn2(ora_ctx *c, const double *pts, const double *pab, double *pn2);
 int ora_dyn_hpg(ora_ctx *c, int kt);
+/* zdf_mxl; nlb10, the first W-level below 10 m */
+int ora_zdf_mxl(ora_ctx *c, int kt);
+int ora_nlb10(const ora_ctx *c);
 /* 1: start the work arrays standing for Fortran automatic arrays as NaN */
 void ora_set_poison(int on);
 

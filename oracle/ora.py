@@ -60,6 +60,8 @@ def lib():
         P("ora_rab_3d", [vp, vp, vp])
         P("ora_bn2", [vp, vp, vp, vp])
         P("ora_dyn_hpg", [vp, i])
+        P("ora_zdf_mxl", [vp, i])
+        P("ora_nlb10", [vp], C.c_int)
         P("ora_tra_ldf_blp", [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
         P("ora_zps_hde", [vp, i, i, vp, vp, vp])
         _lib = L
@@ -249,6 +251,12 @@ class Oracle:
 
     def dyn_hpg(self, kt):
         self._ck(lib().ora_dyn_hpg(self.h, kt), "dyn_hpg")
+
+    def zdf_mxl(self, kt):
+        self._ck(lib().ora_zdf_mxl(self.h, kt), "zdf_mxl")
+
+    def nlb10(self):
+        return lib().ora_nlb10(self.h)
 
     def nksr(self):
         return lib().ora_nksr(self.h)
