@@ -379,7 +379,9 @@ int nemo_gpu_dyn_zdf_step(nemo_ctx *ctx, int kt);
 int nemo_gpu_dyn_nxt(nemo_ctx *ctx, int kt);
 /* ssh_swp (sshwzv.F90:216-267), linear free surface. */
 int nemo_gpu_ssh_swp(nemo_ctx *ctx, int kt);
-/* One model step on the bound fields, in step.F90's order: ua = va = 0, dyn_spg_ts,
+/* One model step on the bound fields, in step.F90's order: (with rn2b, rhd, the
+ * depths, the mixed-layer fields and the slopes bound, ln_seos and ln_traldf_iso:
+ * rab_3d of tsb, bn2, zdf_mxl, eos_insitu of tsb and ldf_slp), ua = va = 0, dyn_spg_ts,
  * (with the bound rhd and rhop and ln_seos: eos_insitu_pot of tsn at gdept_n and
  * dyn_hpg after ua = va = 0), div_hor + wzv, the dyn_zdf time step, tsa = 0,
  * tra_sbc and tra_qsr (when their

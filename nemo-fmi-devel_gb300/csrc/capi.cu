@@ -78,6 +78,7 @@ struct nemo_ctx {
   void* adj_w[4] = {};         // iso-neutral adjoint: G and the gradient adjoints
   int adj_kjpt = 0;
   void* slp_w = nullptr;       // ldf_slp work: 4 3-D and 6 2-D arrays per member
+  void* rab_w = nullptr;       // the model step's before expansion ratios rab_b (jpi,jpj,jpk,2)
   void* blp_w = nullptr;       // tra_ldf_blp: the first laplacian (jpi,jpj,jpk,kjpt) per member
   int blp_kjpt = 0;
   int iso_kjpt = 0;
@@ -1116,6 +1117,35 @@ bool hpg_on(const nemo_ctx* c) {
          !nm.ln_isfcav;
 }
 
+// the model step's iso-neutral slopes from the before tracers (step.F90:127-150):
+// the simplified eos, rotated diffusion, z-coordinate with full steps, and every
+// field of the chain bound
+bool slopes_on(const nemo_ctx* c) {
+  const nemo_namelist& nm = c->nam;
+  if (!nm.ln_seos || !nm.ln_traldf_iso || nm.ln_zps || nm.ln_sco || nm.ln_isfcav) return false;
+  for (int id : {NEMO_F_RN2B, NEMO_F_RHD, NEMO_F_GDEPT_N, NEMO_F_GDEPW_N, NEMO_F_NMLN, NEMO_F_HMLP, NEMO_F_HMLPT,
+                 NEMO_F_USLP, NEMO_F_VSLP, NEMO_F_WSLPI, NEMO_F_WSLPJ, NEMO_F_AVT})
+    if (!c->f[id]) return false;
+  return true;
+}
+
+// eos_rab(tsb, rab_b), bn2(tsb, rab_b, rn2b), zdf_mxl, eos(tsb, rhd, gdept_0) and
+// ldf_slp(rhd, rn2b) (step.F90:127-150; the now-tracer rab_n and rn2 feed only the
+// vertical physics, which is not on the device). gdept_0 is the bound gdept_n: the
+// linear free surface keeps the rest-state depths.
+template <class T>
+int run_slopes(nemo_ctx* c) {
+  void* const* F = c->f;
+  if (!c->rab_w && cudaMalloc(&c->rab_w, 2 * (size_t)c->n3 * c->nmem * sizeof(T)) != cudaSuccess)
+    return fail(c, NEMO_ERR_NOMEM, "rab_b work array");
+  int s = run_eos<T>(c, 2, F[NEMO_F_TSB], nullptr, nullptr, nullptr, c->rab_w, nullptr, nullptr);
+  if (!s) s = run_eos<T>(c, 3, F[NEMO_F_TSB], nullptr, nullptr, nullptr, nullptr, c->rab_w, F[NEMO_F_RN2B]);
+  if (!s) s = run_zdf_mxl<T>(c);
+  if (!s) s = run_eos<T>(c, 0, F[NEMO_F_TSB], F[NEMO_F_RHD], nullptr, F[NEMO_F_GDEPT_N], nullptr, nullptr, nullptr);
+  if (!s) s = run_ldf_slp<T>(c, F[NEMO_F_RHD], F[NEMO_F_RN2B]);
+  return s;
+}
+
 bool sbc_bound(const nemo_ctx* c) {
   for (int id : {NEMO_F_QNS, NEMO_F_QSR, NEMO_F_EMP, NEMO_F_SFX, NEMO_F_SBC_TSC, NEMO_F_SBC_TSC_B})
     if (!c->f[id]) return false;
@@ -1145,6 +1175,10 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
   }
   mark(0);
   if (model) {  // ua = va = 0 (step.F90:183-184)
+    if (slopes_on(c)) {
+      int s = run_slopes<T>(c);
+      if (s) return s;
+    }
     const size_t bytes = (size_t)c->n3 * c->nmem * sizeof(T);
     CK(cudaMemsetAsync(F[NEMO_F_UA], 0, bytes, c->stream), "ua = 0");
     CK(cudaMemsetAsync(F[NEMO_F_VA], 0, bytes, c->stream), "va = 0");
@@ -1391,6 +1425,7 @@ int nemo_gpu_destroy(nemo_ctx* c) {
   for (auto p : c->iso_w) cudaFree(p);
   for (auto p : c->adj_w) cudaFree(p);
   cudaFree(c->slp_w);
+  cudaFree(c->rab_w);
   cudaFree(c->blp_w);
   for (auto p : c->spg_w) cudaFree(p);
   for (auto p : c->spg_cor) cudaFree(p);

@@ -2575,9 +2575,23 @@ int ora_dyn_hpg(ora_ctx *c, int kt) {
 int ora_stp_model(ora_ctx *c, int kt) {
   const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk;
   if (!c->f[NEMO_F_UA] || !c->f[NEMO_F_VA]) return NEMO_ERR_UNBOUND;
+  int st = 0;
+  const nemo_namelist *nm = &c->nam;
+  if (nm->ln_seos && nm->ln_traldf_iso && !nm->ln_zps && !nm->ln_sco && !nm->ln_isfcav && c->f[NEMO_F_RN2B] &&
+      c->f[NEMO_F_RHD] && c->f[NEMO_F_GDEPT_N] && c->f[NEMO_F_GDEPW_N] && c->f[NEMO_F_NMLN] && c->f[NEMO_F_HMLP] &&
+      c->f[NEMO_F_HMLPT] && c->f[NEMO_F_USLP] && c->f[NEMO_F_VSLP] && c->f[NEMO_F_WSLPI] && c->f[NEMO_F_WSLPJ] &&
+      c->f[NEMO_F_AVT]) {                                          /* step.F90:127-150 */
+    double *rab = zalloc(2 * n3);
+    st = ora_rab_3d(c, c->f[NEMO_F_TSB], rab);
+    if (!st) st = ora_bn2(c, c->f[NEMO_F_TSB], rab, c->f[NEMO_F_RN2B]);
+    free(rab);
+    if (!st) st = ora_zdf_mxl(c, kt);
+    if (!st) st = ora_eos_insitu(c, c->f[NEMO_F_TSB], c->f[NEMO_F_RHD], c->f[NEMO_F_GDEPT_N]);
+    if (!st) st = ora_ldf_slp(c, kt, c->f[NEMO_F_RHD], c->f[NEMO_F_RN2B]);
+    if (st) return st;
+  }
   memset(c->f[NEMO_F_UA], 0, n3 * sizeof(double));
   memset(c->f[NEMO_F_VA], 0, n3 * sizeof(double));
-  int st = 0;
   if (c->f[NEMO_F_RHD] && c->f[NEMO_F_RHOP] && c->nam.ln_seos) {   /* step.F90:165, :193 */
     if (!c->f[NEMO_F_GDEPT_N]) return NEMO_ERR_UNBOUND;
     st = ora_eos_insitu_pot(c, c->f[NEMO_F_TSN], c->f[NEMO_F_RHD], c->f[NEMO_F_RHOP], c->f[NEMO_F_GDEPT_N]);

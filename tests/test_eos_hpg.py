@@ -167,3 +167,44 @@ def test_gpu_stp_model_with_hpg(prec):
     for name in ("UN", "VN", "UB", "VB"):
         p.compare(name, p.s3, tu)
     p.compare("RHD", p.s3, 1e-12 if prec == "fp64" else 2e-5)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_gpu_stp_model_with_slopes_from_the_tracers(prec):
+    """The model step forming its iso-neutral slopes from the before tracers
+    (rab_3d, bn2, zdf_mxl, eos_insitu, ldf_slp) before the path, with eos and dyn_hpg
+    of the now tracers: steps 1 (Euler), 2, 3 (graph capture) and 4 (replay)."""
+    torch = pytest.importorskip("torch")
+    p = eos_pair(prec, neuler=0)
+    for st in p.states:
+        st.update(rn2b=np.zeros(p.s3), hmlp=np.zeros(p.s2), hmlpt=np.zeros(p.s2))
+    for name in ("RHD", "RHOP", "RN2B", "HMLP", "HMLPT"):
+        p.bind(name)
+    nm = [np.zeros(p.s2, dtype=np.int32, order="F") for _ in range(p.nmem)]
+    for m, o in enumerate(p.ora):
+        o.bind("NMLN", nm[m])
+    p.ctx.bind("NMLN", torch.zeros(p.nmem * nm[0].size, dtype=torch.int32, device="cuda"))
+    for kt in (1, 2, 3, 4):
+        for o in p.ora:
+            o.stp_model(kt)
+        p.ctx.stp_model(kt)
+    p.ctx.synchronize()
+    if prec == "fp64":
+        got = p.ctx.bound["NMLN"].cpu().numpy()
+        assert np.array_equal(got, np.concatenate([a.ravel(order="F") for a in nm]))
+        for name in ("USLP", "VSLP", "WSLPI", "WSLPJ", "RN2B"):
+            p.compare(name, p.s3, 1e-12)
+        p.compare("TSN", p.s4, 1e-12)
+    else:
+        # The slopes divide the horizontal density gradient by N^2 from FP32 tracer
+        # differences: where the water is nearly unstratified they are ill-conditioned
+        # (the FP64 form above matches the oracle to 1e-12), so the mixed form is held
+        # to the tracers it produces and to agreement of the slopes at almost all points.
+        p.compare("TSN", p.s4, 1e-4)
+        for name in ("USLP", "VSLP", "WSLPI", "WSLPJ"):
+            got = p.per_member(p.dev[name], p.s3)
+            for m in range(p.nmem):
+                ref = p.host[m][name]
+                off = np.abs(got[m] - ref) > 1e-3 * np.abs(ref).max()
+                assert off.mean() < 0.01, (name, m, off.mean())
