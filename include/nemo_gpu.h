@@ -194,6 +194,8 @@ enum nemo_field_id {
    * (zdf_oce), and its turbocline depth hmld (written when bound) */
   NEMO_F_RN2B,                         /* [T]                                         */
   NEMO_F_HMLD,                         /* [S]                                         */
+  /* lateral eddy viscosity at T- and F-points (ldfdyn.F90 ahmt, ahmf, masked) */
+  NEMO_F_AHMT, NEMO_F_AHMF,            /* [T]                                         */
   NEMO_F_COUNT
 };
 
@@ -312,6 +314,13 @@ int nemo_gpu_bn2(nemo_ctx *ctx, const void *pts, const void *pab, void *pn2);
 /* dyn_hpg with hpg_zco (dynhpg.F90:258-323, z-coordinate with full steps): adds the
  * hydrostatic pressure gradient of the bound rhd to the bound ua, va. */
 int nemo_gpu_dyn_hpg(nemo_ctx *ctx, int kt);
+
+/* dyn_ldf_lap (dynldf_lap_blp.F90:37-104): adds the iso-level laplacian viscous
+ * trend -curl(ahmf curl u) + grad(ahmt div u) of pub, pvb (jpi,jpj,jpk) to pua, pva,
+ * with the bound ahmt and ahmf (kpass 2: the second pass of the bilaplacian, minus
+ * sign). Linear free surface (e3*_b = e3*_n); e3f from the bound e3f_n or the rest
+ * state. */
+int nemo_gpu_dyn_ldf_lap(nemo_ctx *ctx, int kt, const void *pub, const void *pvb, void *pua, void *pva, int kpass);
 
 /* zdf_mxl (zdfmxl.F90:59-141): the mixed layer of the bound rn2b (density criterion
  * rho_c = 0.01 integrated from the first W-level below 10 m, nlb10 of domzgr.F90:144-
@@ -505,6 +514,7 @@ enum nemo_kernel_id {
   NEMO_K_TRA_SBC, NEMO_K_TRA_QSR, /* surface forcing of the tracers */
   NEMO_K_EOS, NEMO_K_BN2, NEMO_K_DYN_HPG, /* equation of state, N^2, pressure gradient */
   NEMO_K_ZDF_MXL,      /* mixed-layer depth */
+  NEMO_K_DYN_LDF,      /* lateral viscosity */
   NEMO_K_COUNT
 };
 

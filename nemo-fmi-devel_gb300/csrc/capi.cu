@@ -48,7 +48,7 @@ struct nemo_ctx {
   // derived host domain (FP64)
   std::vector<double> e1t, e2t, e1u, e2u, e1v, e2v, e1f, e2f, ff_f, ff_t;
   std::vector<double> r1_e1t, r1_e2t, r1_e1u, r1_e2u, r1_e1v, r1_e2v, e1e2t, r1_e1e2t, e1e2u, e1e2v;
-  std::vector<double> r1_e1e2u, r1_e1e2v, e2_e1u, e1_e2v;
+  std::vector<double> r1_e1e2u, r1_e1e2v, e2_e1u, e1_e2v, r1_e1e2f;
   std::vector<double> ssmask, ssumask, ssvmask, tmask_i, ht_0, hu_0, hv_0, r1_hu_0, r1_hv_0;
   std::vector<double> zwz, ftne, ftnw, ftse, ftsw;
   std::vector<ColInfo> ci;
@@ -395,7 +395,7 @@ int build_dom(nemo_ctx* c, DomStore<T>& st) {
 #define UP(name) if ((s = upload(c, st, c->name, &d.name))) return s
   UP(e1t); UP(e2t); UP(e1u); UP(e2u); UP(e1v); UP(e2v);
   UP(r1_e1u); UP(r1_e2u); UP(r1_e1v); UP(r1_e2v);
-  UP(e1e2t); UP(r1_e1e2t); UP(e2_e1u); UP(e1_e2v); UP(r1_e1e2u); UP(r1_e1e2v);
+  UP(e1e2t); UP(r1_e1e2t); UP(e2_e1u); UP(e1_e2v); UP(r1_e1e2u); UP(r1_e1e2v); UP(r1_e1e2f);
   UP(ht_0); UP(hu_0); UP(hv_0); UP(r1_hu_0); UP(r1_hv_0);
   UP(ssmask); UP(ssumask); UP(ssvmask);
   UP(ff_t); UP(ff_f); UP(zwz); UP(ftne); UP(ftnw); UP(ftse); UP(ftsw);
@@ -420,6 +420,7 @@ int build_dom(nemo_ctx* c, DomStore<T>& st) {
   if ((s = upload_e3(c, st, 1, &d.e3u_n))) return s;
   if ((s = upload_e3(c, st, 2, &d.e3v_n))) return s;
   if ((s = upload_e3(c, st, 3, &d.e3w_n))) return s;
+  if ((s = upload_e3(c, st, 4, &d.e3f_n))) return s;
   return NEMO_OK;
 }
 
@@ -508,7 +509,7 @@ int derive_domain(nemo_ctx* c, const nemo_dom_desc* dm) {
   }
   auto mk = [&](std::vector<double>& v) { v.assign(n2, 0.0); };
   mk(c->r1_e1t); mk(c->r1_e2t); mk(c->r1_e1u); mk(c->r1_e2u); mk(c->r1_e1v); mk(c->r1_e2v); mk(c->e1e2t);
-  mk(c->r1_e1e2t); mk(c->e1e2u); mk(c->e1e2v); mk(c->r1_e1e2u); mk(c->r1_e1e2v); mk(c->e2_e1u); mk(c->e1_e2v);
+  mk(c->r1_e1e2t); mk(c->e1e2u); mk(c->e1e2v); mk(c->r1_e1e2u); mk(c->r1_e1e2v); mk(c->e2_e1u); mk(c->e1_e2v); mk(c->r1_e1e2f);
   for (size_t p = 0; p < n2; ++p) {
     c->r1_e1t[p] = 1.0 / c->e1t[p]; c->r1_e2t[p] = 1.0 / c->e2t[p];
     c->r1_e1u[p] = 1.0 / c->e1u[p]; c->r1_e2u[p] = 1.0 / c->e2u[p];
@@ -516,6 +517,7 @@ int derive_domain(nemo_ctx* c, const nemo_dom_desc* dm) {
     c->e1e2t[p] = c->e1t[p] * c->e2t[p]; c->r1_e1e2t[p] = 1.0 / c->e1e2t[p];
     c->e1e2u[p] = c->e1u[p] * c->e2u[p]; c->e1e2v[p] = c->e1v[p] * c->e2v[p];
     c->r1_e1e2u[p] = 1.0 / c->e1e2u[p]; c->r1_e1e2v[p] = 1.0 / c->e1e2v[p];
+    c->r1_e1e2f[p] = 1.0 / (c->e1f[p] * c->e2f[p]);
     c->e2_e1u[p] = c->e2u[p] / c->e1u[p]; c->e1_e2v[p] = c->e1v[p] / c->e2v[p];
   }
   // masks
@@ -633,6 +635,7 @@ Dom<T> dom_now(nemo_ctx* c) {
   };
   sub(NEMO_F_E3T_B, d.e3t_b); sub(NEMO_F_E3T_N, d.e3t_n); sub(NEMO_F_E3T_A, d.e3t_a);
   sub(NEMO_F_E3U_N, d.e3u_n); sub(NEMO_F_E3V_N, d.e3v_n); sub(NEMO_F_E3W_N, d.e3w_n);
+  sub(NEMO_F_E3F_N, d.e3f_n);
   return d;
 }
 
@@ -1698,6 +1701,26 @@ int nemo_gpu_zdf_mxl(nemo_ctx* c, int kt) {
   for (int id : {NEMO_F_RN2B, NEMO_F_AVT, NEMO_F_GDEPT_N, NEMO_F_GDEPW_N, NEMO_F_NMLN, NEMO_F_HMLP, NEMO_F_HMLPT})
     if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "zdf_mxl: field %d must be bound", id);
   return c->prec == NEMO_PREC_FP64 ? run_zdf_mxl<double>(c) : run_zdf_mxl<float>(c);
+}
+
+int nemo_gpu_dyn_ldf_lap(nemo_ctx* c, int kt, const void* pub, const void* pvb, void* pua, void* pva, int kpass) {
+  (void)kt;
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (!pub || !pvb || !pua || !pva || (kpass != 1 && kpass != 2)) return fail(c, NEMO_ERR_ARG, "dyn_ldf_lap: bad argument");
+  if (!c->f[NEMO_F_AHMT] || !c->f[NEMO_F_AHMF]) return fail(c, NEMO_ERR_UNBOUND, "dyn_ldf_lap: ahmt and ahmf must be bound");
+  if (!c->nam.ln_linssh) return fail(c, NEMO_ERR_UNSUPPORTED, "dyn_ldf_lap: linear free surface only");
+  cudaError_t e;
+  if (c->prec == NEMO_PREC_FP64)
+    e = launch_dyn_ldf_lap<double>(dom_now<double>(c), (const double*)c->f[NEMO_F_AHMT], (const double*)c->f[NEMO_F_AHMF],
+                                   (const double*)pub, (const double*)pvb, (double*)pua, (double*)pva,
+                                   kpass == 1 ? 1.0 : -1.0, c->stream);
+  else
+    e = launch_dyn_ldf_lap<float>(dom_now<float>(c), (const float*)c->f[NEMO_F_AHMT], (const float*)c->f[NEMO_F_AHMF],
+                                  (const float*)pub, (const float*)pvb, (float*)pua, (float*)pva,
+                                  kpass == 1 ? 1.f : -1.f, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "dyn_ldf_lap launch");
+  return NEMO_OK;
 }
 
 static int eos_check(nemo_ctx* c, const char* what) {

@@ -89,6 +89,14 @@ cudaError_t launch_zdf_mxl(const Dom<T>& d, const MxlArgs<T>& a, cudaStream_t s)
   return cudaGetLastError();
 }
 
+template <class T>
+cudaError_t launch_dyn_ldf_lap(const Dom<T>& d, const T* ahmt, const T* ahmf, const T* pub, const T* pvb, T* pua, T* pva,
+                               T zsign, cudaStream_t s) {
+  k_dyn_ldf_lap<T><<<s_pt(d), dim3(SX, SY), 0, s>>>(d, ahmt, ahmf, pub, pvb, pua, pva, zsign);
+  ktick(NEMO_K_DYN_LDF, s);
+  return cudaGetLastError();
+}
+
 #define NEMO_STEP_INST(T)                                                                                      \
   template cudaError_t launch_wzv<T>(const Dom<T>&, const T*, const T*, T*, T, cudaStream_t);                  \
   template cudaError_t launch_dyn_zdf_step<T>(const Dom<T>&, const T*, const T*, T*, T*, T, cudaStream_t);     \
@@ -100,7 +108,9 @@ cudaError_t launch_zdf_mxl(const Dom<T>& d, const MxlArgs<T>& a, cudaStream_t s)
   template cudaError_t launch_tra_qsr<T>(const Dom<T>&, const QsrArgs<T>&, cudaStream_t);                  \
   template cudaError_t launch_eos<T>(const Dom<T>&, const EosArgs<T>&, cudaStream_t);                      \
   template cudaError_t launch_dyn_hpg<T>(const Dom<T>&, const T*, T*, T*, T, cudaStream_t);              \
-  template cudaError_t launch_zdf_mxl<T>(const Dom<T>&, const MxlArgs<T>&, cudaStream_t);
+  template cudaError_t launch_zdf_mxl<T>(const Dom<T>&, const MxlArgs<T>&, cudaStream_t);                  \
+  template cudaError_t launch_dyn_ldf_lap<T>(const Dom<T>&, const T*, const T*, const T*, const T*, T*, T*, T,   \
+                                             cudaStream_t);
 NEMO_STEP_INST(double)
 NEMO_STEP_INST(float)
 

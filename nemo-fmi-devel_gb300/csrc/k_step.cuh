@@ -579,4 +579,45 @@ __global__ void k_zdf_mxl(Dom<T> d, MxlArgs<T> a) {
   a.hmlpt[c2] = a.gdept[c3 + (long)(nmln - 2) * d.n2] * ssm;
 }
 
+// dyn_ldf_lap (dynldf_lap_blp.F90:37-104), linear free surface (e3*_b = e3*_n),
+// one (i,j,k) point per thread: -curl(curl) + grad(div) of the before velocity.
+// The relative vorticity zcur and divergence zdiv a point needs (three of each) are
+// formed where read, each with the reference's expression.
+template <class T>
+struct LdfDyn {
+  const Dom<T>& d;
+  const T *ahmt, *ahmf, *pub, *pvb;
+  long m3;
+  int k, m;
+  __device__ __forceinline__ long P(int i, int j) const { return (long)(i - 1) + (long)(j - 1) * d.jpi; }
+  __device__ __forceinline__ T cur(int a, int b) const {
+    const long p = P(a, b), q = m3 + p + (long)(k - 1) * d.n2;
+    return a_(ahmf, q) * d.e3f_n(p, k, m) * d.r1_e1e2f[p] *
+           (d.e2v[p + 1] * a_(pvb, q + 1) - d.e2v[p] * a_(pvb, q) - d.e1u[p + d.jpi] * a_(pub, q + d.jpi) +
+            d.e1u[p] * a_(pub, q));
+  }
+  __device__ __forceinline__ T div(int a, int b) const {
+    const long p = P(a, b), q = m3 + p + (long)(k - 1) * d.n2;
+    return a_(ahmt, q) * d.r1_e1e2t[p] / d.e3t_b(p, k, m) *
+           (d.e2u[p] * d.e3u_n(p, k, m) * a_(pub, q) - d.e2u[p - 1] * d.e3u_n(p - 1, k, m) * a_(pub, q - 1) +
+            d.e1v[p] * d.e3v_n(p, k, m) * a_(pvb, q) - d.e1v[p - d.jpi] * d.e3v_n(p - d.jpi, k, m) * a_(pvb, q - d.jpi));
+  }
+  __device__ __forceinline__ static T a_(const T* x, long q) { return __ldg(x + q); }
+};
+
+template <class T>
+__global__ void k_dyn_ldf_lap(Dom<T> d, const T* __restrict__ ahmt, const T* __restrict__ ahmf,
+                              const T* __restrict__ pub, const T* __restrict__ pvb, T* pua, T* pva, T zsign) {
+  const PtIdx c = pt_index(d);
+  if (!c.valid || c.k > d.jpk - 1 || c.i < 2 || c.i > d.jpi - 1 || c.j < 2 || c.j > d.jpj - 1) return;
+  const LdfDyn<T> L{d, ahmt, ahmf, pub, pvb, (long)c.m * d.n3, c.k, c.m};
+  const int i = c.i, j = c.j;
+  const long q = (long)c.m * d.n3 + c.q;
+  const T zc = L.cur(i, j), zd = L.div(i, j);
+  pua[q] = pua[q] + zsign * (-((zc - L.cur(i, j - 1)) * d.r1_e2u[c.ij] / d.e3u_n(c.ij, c.k, c.m)) +
+                             (L.div(i + 1, j) - zd) * d.r1_e1u[c.ij]);
+  pva[q] = pva[q] + zsign * ((zc - L.cur(i - 1, j)) * d.r1_e1v[c.ij] / d.e3v_n(c.ij, c.k, c.m) +
+                             (L.div(i, j + 1) - zd) * d.r1_e2v[c.ij]);
+}
+
 }  // namespace nemo

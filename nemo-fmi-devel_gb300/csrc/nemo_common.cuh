@@ -72,6 +72,8 @@ struct Dom {
   RO<ColInfo> ci;
   RO<uint8_t> mbkt;
   E3<T> e3t_b, e3t_n, e3t_a, e3u_n, e3v_n, e3w_n;
+  E3<T> e3f_n;       // now e3 at f-points (the rest state unless NEMO_F_E3F_N is bound)
+  RO<T> r1_e1e2f;    // 1 / (e1f e2f)
 };
 
 __device__ __forceinline__ bool in_range(int k, int lo, int hi) { return k >= lo && k <= hi; }

@@ -240,6 +240,10 @@ class Context:
     def bn2(self, pts, pab, pn2):
         self._ck(self.lib.nemo_gpu_bn2(self.h, _ptr(pts), _ptr(pab), _ptr(pn2)), "bn2")
 
+    def dyn_ldf_lap(self, kt, pub, pvb, pua, pva, kpass=1):
+        self._ck(self.lib.nemo_gpu_dyn_ldf_lap(self.h, kt, _ptr(pub), _ptr(pvb), _ptr(pua), _ptr(pva), kpass),
+                 "dyn_ldf_lap")
+
     def zdf_mxl(self, kt):
         self._ck(self.lib.nemo_gpu_zdf_mxl(self.h, kt), "zdf_mxl")
 

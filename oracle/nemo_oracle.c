@@ -2462,6 +2462,44 @@ int ora_zdf_mxl(ora_ctx *c, int kt) {
 
 int ora_nlb10(const ora_ctx *c) { return nlb10_of(c); }
 
+/* dyn_ldf_lap (dynldf_lap_blp.F90:37-104), linear free surface (e3*_b = e3*_0):
+ * bound AHMT, AHMF. */
+int ora_dyn_ldf_lap(ora_ctx *c, int kt, const double *pub, const double *pvb, double *pua, double *pva, int kpass) {
+  (void)kt;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj;
+  const double *ahmt = c->f[NEMO_F_AHMT], *ahmf = c->f[NEMO_F_AHMF];
+  if (!ahmt || !ahmf) return NEMO_ERR_UNBOUND;
+  if (!c->nam.ln_linssh) return NEMO_ERR_UNSUPPORTED;
+  const double *e3f = fld(c, NEMO_F_E3F_N), *e3t_b = fld(c, NEMO_F_E3T_B);
+  const double *e3u = fld(c, NEMO_F_E3U_N), *e3v = fld(c, NEMO_F_E3V_N);
+  const double zsign = kpass == 1 ? 1.0 : -1.0;
+  double *zcur = zalloc(n2), *zdiv = zalloc(n2);
+  for (int jk = 1; jk <= jpk - 1; ++jk) {
+    for (int jj = 2; jj <= jpj; ++jj)
+      for (int ji = 2; ji <= jpi; ++ji) {
+        const size_t pm = I2(ji - 1, jj - 1), qm = I3(ji - 1, jj - 1, jk);
+        zcur[pm] = ahmf[qm] * e3f[qm] * (1.0 / (c->e1f[pm] * c->e2f[pm]))
+                 * (c->e2v[I2(ji, jj - 1)] * pvb[I3(ji, jj - 1, jk)] - c->e2v[pm] * pvb[qm]
+                    - c->e1u[I2(ji - 1, jj)] * pub[I3(ji - 1, jj, jk)] + c->e1u[pm] * pub[qm]);
+        const size_t p = I2(ji, jj), q = I3(ji, jj, jk);
+        zdiv[p] = ahmt[q] * c->r1_e1e2t[p] / e3t_b[q]
+                * (c->e2u[p] * e3u[q] * pub[q] - c->e2u[I2(ji - 1, jj)] * e3u[I3(ji - 1, jj, jk)] * pub[I3(ji - 1, jj, jk)]
+                   + c->e1v[p] * e3v[q] * pvb[q] - c->e1v[I2(ji, jj - 1)] * e3v[I3(ji, jj - 1, jk)] * pvb[I3(ji, jj - 1, jk)]);
+      }
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t p = I2(ji, jj), q = I3(ji, jj, jk);
+        pua[q] = pua[q] + zsign * (-(zcur[p] - zcur[I2(ji, jj - 1)]) * c->r1_e2u[p] / e3u[q]
+                                   + (zdiv[I2(ji + 1, jj)] - zdiv[p]) * c->r1_e1u[p]);
+        pva[q] = pva[q] + zsign * ((zcur[p] - zcur[I2(ji - 1, jj)]) * c->r1_e1v[p] / e3v[q]
+                                   + (zdiv[I2(ji, jj + 1)] - zdiv[p]) * c->r1_e2v[p]);
+      }
+  }
+  free(zcur); free(zdiv);
+  return NEMO_OK;
+}
+
 /* ------------------------------------------- simplified equation of state */
 /* eos_insitu (eosbn2.F90:276-292), np_seos: levels 1..jpk-1 of every point. */
 int ora_eos_insitu(ora_ctx *c, const double *pts, double *prd, const double *pdep) {

@@ -1,0 +1,76 @@
+"""dyn_ldf_lap (the iso-level laplacian viscosity of the momentum): known answers of
+the oracle on the CPU and the GPU through the C ABI against the oracle."""
+import numpy as np
+import pytest
+
+from nemo_gpu import gyre
+from harness import Pair
+
+
+def viscosity(dom, ahm0=1.0e5):
+    """ahmt = ahm0 tmask, ahmf = ahm0 fmask (free slip: fmask from the four
+    surrounding T-points, ldfdyn.F90:258-259 with :328-329)."""
+    tm = gyre.masks(dom)[0]
+    fm = np.zeros_like(tm)
+    fm[:-1, :-1] = tm[:-1, :-1] * tm[1:, :-1] * tm[:-1, 1:] * tm[1:, 1:]
+    ahmt, ahmf = ahm0 * tm, ahm0 * fm
+    ahmt[:, :, -1] = 0.0
+    ahmf[:, :, -1] = 0.0
+    return np.asfortranarray(ahmt), np.asfortranarray(ahmf)
+
+
+def oracle_case(nn=2):
+    from oracle import ora
+    dom = gyre.domain(nn)
+    nam = gyre.namelist()
+    o = ora.Oracle(dom, nam)
+    ahmt, ahmf = viscosity(dom)
+    o.bind("AHMT", ahmt)
+    o.bind("AHMF", ahmf)
+    return dom, o, (ahmt, ahmf)
+
+
+def test_uniform_flow_has_no_interior_trend_and_passes_flip_sign():
+    dom, o, keep = oracle_case()
+    s3 = (dom["jpi"], dom["jpj"], dom["jpk"])
+    _, um, vm, _ = gyre.masks(dom)
+    ub = np.asfortranarray(0.3 * um)
+    vb = np.asfortranarray(-0.2 * vm)
+    ua, va = np.zeros(s3, order="F"), np.zeros(s3, order="F")
+    o.dyn_ldf_lap(1, ub, vb, ua, va, 1)
+    inner = (slice(3, -3), slice(3, -3), slice(0, -1))
+    scale = 1e5 * 0.3 / dom["e1u"].min() ** 2
+    assert np.abs(ua[inner]).max() < 1e-12 * scale and np.abs(va[inner]).max() < 1e-12 * scale
+    assert np.abs(ua).max() > 1e-6 * scale            # the walls do act
+    rng = np.random.default_rng(3)
+    ub = np.asfortranarray(rng.standard_normal(s3) * um)
+    vb = np.asfortranarray(rng.standard_normal(s3) * vm)
+    a1, b1 = np.zeros(s3, order="F"), np.zeros(s3, order="F")
+    a2, b2 = np.zeros(s3, order="F"), np.zeros(s3, order="F")
+    o.dyn_ldf_lap(1, ub, vb, a1, b1, 1)
+    o.dyn_ldf_lap(1, ub, vb, a2, b2, 2)
+    assert np.array_equal(a1, -a2) and np.array_equal(b1, -b2)
+    a3, b3 = np.zeros(s3, order="F"), np.zeros(s3, order="F")
+    o.dyn_ldf_lap(1, np.asfortranarray(2 * ub), np.asfortranarray(2 * vb), a3, b3, 1)
+    assert np.array_equal(a3, 2 * a1) and np.array_equal(b3, 2 * b1)   # exact: scaling by 2
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_gpu_dyn_ldf_lap(prec):
+    pytest.importorskip("torch")
+    p = Pair(nn=2, prec=prec, seed=47, nmem=2)
+    for st in p.states:
+        st["ahmt"], st["ahmf"] = viscosity(p.dom)
+    p.bind_spg()
+    p.bind("AHMT")
+    p.bind("AHMF")
+    for kpass, (u, v) in ((1, ("UB", "VB")), (2, ("UN", "VN"))):   # the second pass on other velocities
+        for m, o in enumerate(p.ora):
+            h = p.host[m]
+            o.dyn_ldf_lap(3, h[u], h[v], h["UA"], h["VA"], kpass)
+        p.ctx.dyn_ldf_lap(3, p.dev[u], p.dev[v], p.dev["UA"], p.dev["VA"], kpass)
+    p.ctx.synchronize()
+    t = 1e-12 if prec == "fp64" else 5e-5
+    p.compare("UA", p.s3, t)
+    p.compare("VA", p.s3, t)
