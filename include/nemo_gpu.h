@@ -322,6 +322,13 @@ int nemo_gpu_dyn_hpg(nemo_ctx *ctx, int kt);
  * state. */
 int nemo_gpu_dyn_ldf_lap(nemo_ctx *ctx, int kt, const void *pub, const void *pvb, void *pua, void *pva, int kpass);
 
+/* vor_ene (dynvor.F90:324-429), the energy-conserving vorticity trend added to pua,
+ * pva from the now velocities pun, pvn (jpi,jpj,jpk), z-coordinate without
+ * ln_dynvor_msk: kvor 1 (np_COR, planetary), 2 (np_RVO, relative) or 4 (np_CRV,
+ * both: dyn_vor's ntot with the vector-form momentum); the metric terms of the flux
+ * form (3, 5) are NEMO_ERR_UNSUPPORTED. */
+int nemo_gpu_vor_ene(nemo_ctx *ctx, int kt, int kvor, const void *pun, const void *pvn, void *pua, void *pva);
+
 /* zdf_mxl (zdfmxl.F90:59-141): the mixed layer of the bound rn2b (density criterion
  * rho_c = 0.01 integrated from the first W-level below 10 m, nlb10 of domzgr.F90:144-
  * 146) into the bound nmln (int32), hmlp and hmlpt, and the turbocline of the bound
@@ -515,6 +522,7 @@ enum nemo_kernel_id {
   NEMO_K_EOS, NEMO_K_BN2, NEMO_K_DYN_HPG, /* equation of state, N^2, pressure gradient */
   NEMO_K_ZDF_MXL,      /* mixed-layer depth */
   NEMO_K_DYN_LDF,      /* lateral viscosity */
+  NEMO_K_DYN_VOR,      /* vorticity trend */
   NEMO_K_COUNT
 };
 

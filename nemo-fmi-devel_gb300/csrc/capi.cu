@@ -1703,6 +1703,23 @@ int nemo_gpu_zdf_mxl(nemo_ctx* c, int kt) {
   return c->prec == NEMO_PREC_FP64 ? run_zdf_mxl<double>(c) : run_zdf_mxl<float>(c);
 }
 
+int nemo_gpu_vor_ene(nemo_ctx* c, int kt, int kvor, const void* pun, const void* pvn, void* pua, void* pva) {
+  (void)kt;
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (!pun || !pvn || !pua || !pva) return fail(c, NEMO_ERR_ARG, "vor_ene: null array");
+  if (kvor != 1 && kvor != 2 && kvor != 4)
+    return fail(c, NEMO_ERR_UNSUPPORTED, "vor_ene: kvor %d (the flux-form metric terms are not included)", kvor);
+  if (c->nam.ln_sco) return fail(c, NEMO_ERR_UNSUPPORTED, "vor_ene: z-coordinate only");
+  cudaError_t e = c->prec == NEMO_PREC_FP64
+                      ? launch_vor_ene<double>(dom_now<double>(c), kvor, (const double*)pun, (const double*)pvn,
+                                               (double*)pua, (double*)pva, c->stream)
+                      : launch_vor_ene<float>(dom_now<float>(c), kvor, (const float*)pun, (const float*)pvn,
+                                              (float*)pua, (float*)pva, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "vor_ene launch");
+  return NEMO_OK;
+}
+
 int nemo_gpu_dyn_ldf_lap(nemo_ctx* c, int kt, const void* pub, const void* pvb, void* pua, void* pva, int kpass) {
   (void)kt;
   if (!c) return NEMO_ERR_ARG;

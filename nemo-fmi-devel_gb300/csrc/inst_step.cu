@@ -97,6 +97,13 @@ cudaError_t launch_dyn_ldf_lap(const Dom<T>& d, const T* ahmt, const T* ahmf, co
   return cudaGetLastError();
 }
 
+template <class T>
+cudaError_t launch_vor_ene(const Dom<T>& d, int kvor, const T* pun, const T* pvn, T* pua, T* pva, cudaStream_t s) {
+  k_vor_ene<T><<<s_pt(d), dim3(SX, SY), 0, s>>>(d, kvor, pun, pvn, pua, pva);
+  ktick(NEMO_K_DYN_VOR, s);
+  return cudaGetLastError();
+}
+
 #define NEMO_STEP_INST(T)                                                                                      \
   template cudaError_t launch_wzv<T>(const Dom<T>&, const T*, const T*, T*, T, cudaStream_t);                  \
   template cudaError_t launch_dyn_zdf_step<T>(const Dom<T>&, const T*, const T*, T*, T*, T, cudaStream_t);     \
@@ -110,7 +117,8 @@ cudaError_t launch_dyn_ldf_lap(const Dom<T>& d, const T* ahmt, const T* ahmf, co
   template cudaError_t launch_dyn_hpg<T>(const Dom<T>&, const T*, T*, T*, T, cudaStream_t);              \
   template cudaError_t launch_zdf_mxl<T>(const Dom<T>&, const MxlArgs<T>&, cudaStream_t);                  \
   template cudaError_t launch_dyn_ldf_lap<T>(const Dom<T>&, const T*, const T*, const T*, const T*, T*, T*, T,   \
-                                             cudaStream_t);
+                                             cudaStream_t);                                             \
+  template cudaError_t launch_vor_ene<T>(const Dom<T>&, int, const T*, const T*, T*, T*, cudaStream_t);
 NEMO_STEP_INST(double)
 NEMO_STEP_INST(float)
 

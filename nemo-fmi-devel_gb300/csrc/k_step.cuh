@@ -620,4 +620,36 @@ __global__ void k_dyn_ldf_lap(Dom<T> d, const T* __restrict__ ahmt, const T* __r
                              (L.div(i, j + 1) - zd) * d.r1_e2v[c.ij]);
 }
 
+// vor_ene (dynvor.F90:324-429), z-coordinate without ln_dynvor_msk, one (i,j,k)
+// point per thread; the vorticities zwz and transports zwx, zwy of the four
+// surrounding points are formed where read, each with the reference's expression.
+template <class T>
+__global__ void k_vor_ene(Dom<T> d, int kvor, const T* __restrict__ pun, const T* __restrict__ pvn, T* pua,
+                          T* pva) {
+  const PtIdx c = pt_index(d);
+  if (!c.valid || c.k > d.jpk - 1 || c.i < 2 || c.i > d.jpi - 1 || c.j < 2 || c.j > d.jpj - 1) return;
+  const long o = (long)c.m * d.n3 + (long)(c.k - 1) * d.n2;  // this level of this member
+  const long J = d.jpi;
+  auto zwz = [&](long p) -> T {
+    if (kvor == 1) return d.ff_f[p];
+    const T rv = (d.e2v[p + 1] * __ldg(pvn + o + p + 1) - d.e2v[p] * __ldg(pvn + o + p) -
+                  d.e1u[p + J] * __ldg(pun + o + p + J) + d.e1u[p] * __ldg(pun + o + p)) *
+                 d.r1_e1e2f[p];
+    if (kvor == 2) return rv;
+    return d.ff_f[p] + (d.e2v[p + 1] * __ldg(pvn + o + p + 1) - d.e2v[p] * __ldg(pvn + o + p) -
+                        d.e1u[p + J] * __ldg(pun + o + p + J) + d.e1u[p] * __ldg(pun + o + p)) *
+                           d.r1_e1e2f[p];
+  };
+  auto zwx = [&](long p) -> T { return d.e2u[p] * __ldg(pun + o + p); };
+  auto zwy = [&](long p) -> T { return d.e1v[p] * __ldg(pvn + o + p); };
+  const long p = c.ij, q = o + p;
+  const T zy1 = zwy(p - J) + zwy(p + 1 - J);
+  const T zy2 = zwy(p) + zwy(p + 1);
+  const T zx1 = zwx(p - 1) + zwx(p - 1 + J);
+  const T zx2 = zwx(p) + zwx(p + J);
+  const T zc = zwz(p);
+  pua[q] = pua[q] + T(0.25) * d.r1_e1u[p] * (zwz(p - J) * zy1 + zc * zy2);
+  pva[q] = pva[q] - T(0.25) * d.r1_e2v[p] * (zwz(p - 1) * zx1 + zc * zx2);
+}
+
 }  // namespace nemo

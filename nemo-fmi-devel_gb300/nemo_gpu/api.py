@@ -244,6 +244,9 @@ class Context:
         self._ck(self.lib.nemo_gpu_dyn_ldf_lap(self.h, kt, _ptr(pub), _ptr(pvb), _ptr(pua), _ptr(pva), kpass),
                  "dyn_ldf_lap")
 
+    def vor_ene(self, kt, kvor, pun, pvn, pua, pva):
+        self._ck(self.lib.nemo_gpu_vor_ene(self.h, kt, kvor, _ptr(pun), _ptr(pvn), _ptr(pua), _ptr(pva)), "vor_ene")
+
     def zdf_mxl(self, kt):
         self._ck(self.lib.nemo_gpu_zdf_mxl(self.h, kt), "zdf_mxl")
 

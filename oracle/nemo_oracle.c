@@ -2462,6 +2462,47 @@ int ora_zdf_mxl(ora_ctx *c, int kt) {
 
 int ora_nlb10(const ora_ctx *c) { return nlb10_of(c); }
 
+/* vor_ene (dynvor.F90:324-429), z-coordinate, no ln_dynvor_msk; kvor 1, 2 or 4. */
+int ora_vor_ene(ora_ctx *c, int kt, int kvor, const double *pun, const double *pvn, double *pua, double *pva) {
+  (void)kt;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj;
+  if (kvor != 1 && kvor != 2 && kvor != 4) return NEMO_ERR_UNSUPPORTED;
+  if (c->nam.ln_sco) return NEMO_ERR_UNSUPPORTED;
+  double *zwz = zalloc(n2), *zwx = zalloc(n2), *zwy = zalloc(n2);
+  const double r1_4 = 0.250;
+  for (int jk = 1; jk <= jpk - 1; ++jk) {
+    const double *un = pun + n2 * (jk - 1), *vn = pvn + n2 * (jk - 1);
+    if (kvor == 1) {
+      memcpy(zwz, c->ff_f, n2 * sizeof(double));
+    } else {
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          const size_t p = I2(ji, jj);
+          const double rv = (c->e2v[I2(ji + 1, jj)] * vn[I2(ji + 1, jj)] - c->e2v[p] * vn[p]
+                             - c->e1u[I2(ji, jj + 1)] * un[I2(ji, jj + 1)] + c->e1u[p] * un[p])
+                            * (1.0 / (c->e1f[p] * c->e2f[p]));
+          zwz[p] = kvor == 2 ? rv : c->ff_f[p] + (c->e2v[I2(ji + 1, jj)] * vn[I2(ji + 1, jj)] - c->e2v[p] * vn[p]
+                                                  - c->e1u[I2(ji, jj + 1)] * un[I2(ji, jj + 1)] + c->e1u[p] * un[p])
+                                                     * (1.0 / (c->e1f[p] * c->e2f[p]));
+        }
+    }
+    for (size_t p = 0; p < n2; ++p) { zwx[p] = c->e2u[p] * un[p]; zwy[p] = c->e1v[p] * vn[p]; }
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t p = I2(ji, jj), q = p + n2 * (jk - 1);
+        const double zy1 = zwy[I2(ji, jj - 1)] + zwy[I2(ji + 1, jj - 1)];
+        const double zy2 = zwy[p] + zwy[I2(ji + 1, jj)];
+        const double zx1 = zwx[I2(ji - 1, jj)] + zwx[I2(ji - 1, jj + 1)];
+        const double zx2 = zwx[p] + zwx[I2(ji, jj + 1)];
+        pua[q] = pua[q] + r1_4 * c->r1_e1u[p] * (zwz[I2(ji, jj - 1)] * zy1 + zwz[p] * zy2);
+        pva[q] = pva[q] - r1_4 * c->r1_e2v[p] * (zwz[I2(ji - 1, jj)] * zx1 + zwz[p] * zx2);
+      }
+  }
+  free(zwz); free(zwx); free(zwy);
+  return NEMO_OK;
+}
+
 /* dyn_ldf_lap (dynldf_lap_blp.F90:37-104), linear free surface (e3*_b = e3*_0):
  * bound AHMT, AHMF. */
 int ora_dyn_ldf_lap(ora_ctx *c, int kt, const double *pub, const double *pvb, double *pua, double *pva, int kpass) {

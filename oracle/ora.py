@@ -63,6 +63,7 @@ def lib():
         P("ora_zdf_mxl", [vp, i])
         P("ora_nlb10", [vp], C.c_int)
         P("ora_dyn_ldf_lap", [vp, i, vp, vp, vp, vp, i])
+        P("ora_vor_ene", [vp, i, i, vp, vp, vp, vp])
         P("ora_tra_ldf_blp", [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
         P("ora_zps_hde", [vp, i, i, vp, vp, vp])
         _lib = L
@@ -258,6 +259,9 @@ class Oracle:
 
     def dyn_ldf_lap(self, kt, pub, pvb, pua, pva, kpass=1):
         self._ck(lib().ora_dyn_ldf_lap(self.h, kt, _p(pub), _p(pvb), _p(pua), _p(pva), kpass), "dyn_ldf_lap")
+
+    def vor_ene(self, kt, kvor, pun, pvn, pua, pva):
+        self._ck(lib().ora_vor_ene(self.h, kt, kvor, _p(pun), _p(pvn), _p(pua), _p(pva)), "vor_ene")
 
     def nlb10(self):
         return lib().ora_nlb10(self.h)

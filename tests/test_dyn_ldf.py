@@ -74,3 +74,42 @@ def test_gpu_dyn_ldf_lap(prec):
     t = 1e-12 if prec == "fp64" else 5e-5
     p.compare("UA", p.s3, t)
     p.compare("VA", p.s3, t)
+
+
+@pytest.mark.parametrize("kvor", [1, 2, 4])
+def test_vor_ene_does_no_work(kvor):
+    """The energy-conserving scheme: for any vorticity the trend is normal to the
+    flow, sum(e1e2u u ua) + sum(e1e2v v va) = 0 on each level of a closed basin."""
+    from oracle import ora
+    dom = gyre.domain(2)
+    o = ora.Oracle(dom, gyre.namelist())
+    s3 = (dom["jpi"], dom["jpj"], dom["jpk"])
+    _, um, vm, _ = gyre.masks(dom)
+    rng = np.random.default_rng(kvor)
+    un = np.asfortranarray(rng.standard_normal(s3) * um)
+    vn = np.asfortranarray(rng.standard_normal(s3) * vm)
+    ua, va = np.zeros(s3, order="F"), np.zeros(s3, order="F")
+    o.vor_ene(1, kvor, un, vn, ua, va)
+    wu = (dom["e1u"] * dom["e2u"])[:, :, None] * un * ua
+    wv = (dom["e1v"] * dom["e2v"])[:, :, None] * vn * va
+    work = (wu + wv).sum(axis=(0, 1))
+    size = (np.abs(wu) + np.abs(wv)).sum(axis=(0, 1))
+    assert np.all(np.abs(work[:-1]) <= 1e-12 * size[:-1])
+    assert np.all(size[:-1] > 0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_gpu_vor_ene(prec):
+    pytest.importorskip("torch")
+    p = Pair(nn=2, prec=prec, seed=49, nmem=2)
+    p.bind_spg()
+    for kvor, (u, v) in ((4, ("UN", "VN")), (1, ("UB", "VB")), (2, ("UN", "VN"))):
+        for m, o in enumerate(p.ora):
+            h = p.host[m]
+            o.vor_ene(3, kvor, h[u], h[v], h["UA"], h["VA"])
+        p.ctx.vor_ene(3, kvor, p.dev[u], p.dev[v], p.dev["UA"], p.dev["VA"])
+    p.ctx.synchronize()
+    t = 1e-12 if prec == "fp64" else 5e-5
+    p.compare("UA", p.s3, t)
+    p.compare("VA", p.s3, t)
