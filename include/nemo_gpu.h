@@ -329,6 +329,13 @@ int nemo_gpu_dyn_ldf_lap(nemo_ctx *ctx, int kt, const void *pub, const void *pvb
  * form (3, 5) are NEMO_ERR_UNSUPPORTED. */
 int nemo_gpu_vor_ene(nemo_ctx *ctx, int kt, int kvor, const void *pun, const void *pvn, void *pua, void *pva);
 
+/* dyn_keg (dynkeg.F90, nkeg_C2 = 0): subtracts the gradient of the horizontal
+ * kinetic energy of the bound un, vn from the bound ua, va; the Hollingsworth form
+ * (kscheme 1) is NEMO_ERR_UNSUPPORTED. dyn_zad (dynzad.F90): subtracts the vertical
+ * advection of the bound un, vn by the bound wn. */
+int nemo_gpu_dyn_keg(nemo_ctx *ctx, int kt, int kscheme);
+int nemo_gpu_dyn_zad(nemo_ctx *ctx, int kt);
+
 /* zdf_mxl (zdfmxl.F90:59-141): the mixed layer of the bound rn2b (density criterion
  * rho_c = 0.01 integrated from the first W-level below 10 m, nlb10 of domzgr.F90:144-
  * 146) into the bound nmln (int32), hmlp and hmlpt, and the turbocline of the bound
@@ -523,6 +530,7 @@ enum nemo_kernel_id {
   NEMO_K_ZDF_MXL,      /* mixed-layer depth */
   NEMO_K_DYN_LDF,      /* lateral viscosity */
   NEMO_K_DYN_VOR,      /* vorticity trend */
+  NEMO_K_DYN_KEG, NEMO_K_DYN_ZAD, /* momentum advection, vector form */
   NEMO_K_COUNT
 };
 

@@ -1703,6 +1703,41 @@ int nemo_gpu_zdf_mxl(nemo_ctx* c, int kt) {
   return c->prec == NEMO_PREC_FP64 ? run_zdf_mxl<double>(c) : run_zdf_mxl<float>(c);
 }
 
+int nemo_gpu_dyn_keg(nemo_ctx* c, int kt, int kscheme) {
+  (void)kt;
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  for (int id : {NEMO_F_UN, NEMO_F_VN, NEMO_F_UA, NEMO_F_VA})
+    if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "dyn_keg: un, vn, ua and va must be bound");
+  if (kscheme != 0) return fail(c, NEMO_ERR_UNSUPPORTED, "dyn_keg: the centred scheme (nkeg_C2) only");
+  void* const* F = c->f;
+  cudaError_t e = c->prec == NEMO_PREC_FP64
+                      ? launch_dyn_keg<double>(dom_now<double>(c), (const double*)F[NEMO_F_UN], (const double*)F[NEMO_F_VN],
+                                               (double*)F[NEMO_F_UA], (double*)F[NEMO_F_VA], c->stream)
+                      : launch_dyn_keg<float>(dom_now<float>(c), (const float*)F[NEMO_F_UN], (const float*)F[NEMO_F_VN],
+                                              (float*)F[NEMO_F_UA], (float*)F[NEMO_F_VA], c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "dyn_keg launch");
+  return NEMO_OK;
+}
+
+int nemo_gpu_dyn_zad(nemo_ctx* c, int kt) {
+  (void)kt;
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  for (int id : {NEMO_F_UN, NEMO_F_VN, NEMO_F_WN, NEMO_F_UA, NEMO_F_VA})
+    if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "dyn_zad: un, vn, wn, ua and va must be bound");
+  void* const* F = c->f;
+  cudaError_t e = c->prec == NEMO_PREC_FP64
+                      ? launch_dyn_zad<double>(dom_now<double>(c), (const double*)F[NEMO_F_UN], (const double*)F[NEMO_F_VN],
+                                               (const double*)F[NEMO_F_WN], (double*)F[NEMO_F_UA],
+                                               (double*)F[NEMO_F_VA], c->stream)
+                      : launch_dyn_zad<float>(dom_now<float>(c), (const float*)F[NEMO_F_UN], (const float*)F[NEMO_F_VN],
+                                              (const float*)F[NEMO_F_WN], (float*)F[NEMO_F_UA], (float*)F[NEMO_F_VA],
+                                              c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "dyn_zad launch");
+  return NEMO_OK;
+}
+
 int nemo_gpu_vor_ene(nemo_ctx* c, int kt, int kvor, const void* pun, const void* pvn, void* pua, void* pva) {
   (void)kt;
   if (!c) return NEMO_ERR_ARG;

@@ -104,6 +104,20 @@ cudaError_t launch_vor_ene(const Dom<T>& d, int kvor, const T* pun, const T* pvn
   return cudaGetLastError();
 }
 
+template <class T>
+cudaError_t launch_dyn_keg(const Dom<T>& d, const T* un, const T* vn, T* ua, T* va, cudaStream_t s) {
+  k_dyn_keg<T><<<s_pt(d), dim3(SX, SY), 0, s>>>(d, un, vn, ua, va);
+  ktick(NEMO_K_DYN_KEG, s);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_dyn_zad(const Dom<T>& d, const T* un, const T* vn, const T* wn, T* ua, T* va, cudaStream_t s) {
+  k_dyn_zad<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, un, vn, wn, ua, va);
+  ktick(NEMO_K_DYN_ZAD, s);
+  return cudaGetLastError();
+}
+
 #define NEMO_STEP_INST(T)                                                                                      \
   template cudaError_t launch_wzv<T>(const Dom<T>&, const T*, const T*, T*, T, cudaStream_t);                  \
   template cudaError_t launch_dyn_zdf_step<T>(const Dom<T>&, const T*, const T*, T*, T*, T, cudaStream_t);     \
@@ -118,7 +132,9 @@ cudaError_t launch_vor_ene(const Dom<T>& d, int kvor, const T* pun, const T* pvn
   template cudaError_t launch_zdf_mxl<T>(const Dom<T>&, const MxlArgs<T>&, cudaStream_t);                  \
   template cudaError_t launch_dyn_ldf_lap<T>(const Dom<T>&, const T*, const T*, const T*, const T*, T*, T*, T,   \
                                              cudaStream_t);                                             \
-  template cudaError_t launch_vor_ene<T>(const Dom<T>&, int, const T*, const T*, T*, T*, cudaStream_t);
+  template cudaError_t launch_vor_ene<T>(const Dom<T>&, int, const T*, const T*, T*, T*, cudaStream_t);       \
+  template cudaError_t launch_dyn_keg<T>(const Dom<T>&, const T*, const T*, T*, T*, cudaStream_t);             \
+  template cudaError_t launch_dyn_zad<T>(const Dom<T>&, const T*, const T*, const T*, T*, T*, cudaStream_t);
 NEMO_STEP_INST(double)
 NEMO_STEP_INST(float)
 

@@ -652,4 +652,52 @@ __global__ void k_vor_ene(Dom<T> d, int kvor, const T* __restrict__ pun, const T
   pva[q] = pva[q] - T(0.25) * d.r1_e2v[p] * (zwz(p - 1) * zx1 + zc * zx2);
 }
 
+// dyn_keg (dynkeg.F90, nkeg_C2), one (i,j,k) interior point per thread: the kinetic
+// energy of the point and of its east / north neighbours formed where read.
+template <class T>
+__global__ void k_dyn_keg(Dom<T> d, const T* __restrict__ un, const T* __restrict__ vn, T* ua, T* va) {
+  const PtIdx c = pt_index(d);
+  if (!c.valid || c.k > d.jpk - 1 || c.i < 2 || c.i > d.jpi - 1 || c.j < 2 || c.j > d.jpj - 1) return;
+  const long q = (long)c.m * d.n3 + c.q, J = d.jpi;
+  auto hke = [&](long r) -> T {
+    const T u0 = __ldg(un + r - 1), u1 = __ldg(un + r), v0 = __ldg(vn + r - J), v1 = __ldg(vn + r);
+    const T zu = u0 * u0 + u1 * u1;
+    const T zv = v0 * v0 + v1 * v1;
+    return T(0.25) * (zv + zu);
+  };
+  const T h = hke(q);
+  ua[q] = ua[q] - (hke(q + 1) - h) / d.e1u[c.ij];
+  va[q] = va[q] - (hke(q + J) - h) / d.e2v[c.ij];
+}
+
+// dyn_zad (dynzad.F90), one interior column per thread: the w-level momentum fluxes
+// of the column carried down, each formed once.
+template <class T>
+__global__ void k_dyn_zad(Dom<T> d, const T* __restrict__ un, const T* __restrict__ vn, const T* __restrict__ wn,
+                          T* ua, T* va) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i < 2 || i > d.jpi - 1 || j < 2 || j > d.jpj - 1) return;
+  const int m = blockIdx.z;
+  const long ij = (long)(i - 1) + (long)(j - 1) * d.jpi, J = d.jpi;
+  const long c3 = (long)m * d.n3 + ij;
+  const T e0 = d.e1e2t[ij], e1 = d.e1e2t[ij + 1], e2 = d.e1e2t[ij + J];
+  const T r1u = d.r1_e1e2u[ij], r1v = d.r1_e1e2v[ij];
+  T wu = T(0), wv = T(0);  // zwuw, zwvw at the top of level k
+  for (int k = 1; k <= d.jpk - 1; ++k) {
+    const long q = c3 + (long)(k - 1) * d.n2;
+    T wu1 = T(0), wv1 = T(0);  // at its bottom (w-level k+1), 0 at jpk
+    if (k + 1 <= d.jpk - 1) {
+      const long qb = q + d.n2;
+      const T z0 = T(0.25) * e0 * __ldg(wn + qb), zi = T(0.25) * e1 * __ldg(wn + qb + 1),
+              zj = T(0.25) * e2 * __ldg(wn + qb + J);
+      wu1 = (zi + z0) * (__ldg(un + q) - __ldg(un + qb));
+      wv1 = (zj + z0) * (__ldg(vn + q) - __ldg(vn + qb));
+    }
+    ua[q] = ua[q] - (wu + wu1) * r1u / d.e3u_n(ij, k, m);
+    va[q] = va[q] - (wv + wv1) * r1v / d.e3v_n(ij, k, m);
+    wu = wu1;
+    wv = wv1;
+  }
+}
+
 }  // namespace nemo

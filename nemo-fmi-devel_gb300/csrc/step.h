@@ -72,6 +72,10 @@ cudaError_t launch_dyn_ldf_lap(const Dom<T>& d, const T* ahmt, const T* ahmf, co
 template <class T>
 cudaError_t launch_vor_ene(const Dom<T>& d, int kvor, const T* pun, const T* pvn, T* pua, T* pva, cudaStream_t s);
 template <class T>
+cudaError_t launch_dyn_keg(const Dom<T>& d, const T* un, const T* vn, T* ua, T* va, cudaStream_t s);
+template <class T>
+cudaError_t launch_dyn_zad(const Dom<T>& d, const T* un, const T* vn, const T* wn, T* ua, T* va, cudaStream_t s);
+template <class T>
 cudaError_t launch_zdf_mxl(const Dom<T>& d, const MxlArgs<T>& a, cudaStream_t s);
 template <class T>
 cudaError_t launch_eos(const Dom<T>& d, const EosArgs<T>& a, cudaStream_t s);

@@ -130,6 +130,8 @@ def load(path):
     _proto(lib, "nemo_gpu_bn2", i, [vp, vp, vp, vp])
     _proto(lib, "nemo_gpu_dyn_ldf_lap", i, [vp, i, vp, vp, vp, vp, i])
     _proto(lib, "nemo_gpu_vor_ene", i, [vp, i, i, vp, vp, vp, vp])
+    _proto(lib, "nemo_gpu_dyn_keg", i, [vp, i, i])
+    _proto(lib, "nemo_gpu_dyn_zad", i, [vp, i])
     for name in ("nemo_gpu_tra_sbc", "nemo_gpu_tra_qsr", "nemo_gpu_dyn_hpg", "nemo_gpu_zdf_mxl",
                  "nemo_gpu_wzv", "nemo_gpu_dyn_zdf_step", "nemo_gpu_dyn_nxt", "nemo_gpu_ssh_swp",
                  "nemo_gpu_stp_model"):

@@ -247,6 +247,12 @@ class Context:
     def vor_ene(self, kt, kvor, pun, pvn, pua, pva):
         self._ck(self.lib.nemo_gpu_vor_ene(self.h, kt, kvor, _ptr(pun), _ptr(pvn), _ptr(pua), _ptr(pva)), "vor_ene")
 
+    def dyn_keg(self, kt, kscheme=0):
+        self._ck(self.lib.nemo_gpu_dyn_keg(self.h, kt, kscheme), "dyn_keg")
+
+    def dyn_zad(self, kt):
+        self._ck(self.lib.nemo_gpu_dyn_zad(self.h, kt), "dyn_zad")
+
     def zdf_mxl(self, kt):
         self._ck(self.lib.nemo_gpu_zdf_mxl(self.h, kt), "zdf_mxl")
 

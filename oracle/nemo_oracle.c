@@ -2462,6 +2462,66 @@ int ora_zdf_mxl(ora_ctx *c, int kt) {
 
 int ora_nlb10(const ora_ctx *c) { return nlb10_of(c); }
 
+/* dyn_keg (dynkeg.F90), nkeg_C2: bound UN, VN, UA, VA. */
+int ora_dyn_keg(ora_ctx *c, int kt, int kscheme) {
+  (void)kt;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj;
+  const double *un = c->f[NEMO_F_UN], *vn = c->f[NEMO_F_VN];
+  double *ua = c->f[NEMO_F_UA], *va = c->f[NEMO_F_VA];
+  if (!un || !vn || !ua || !va) return NEMO_ERR_UNBOUND;
+  if (kscheme != 0) return NEMO_ERR_UNSUPPORTED;
+  double *zhke = zalloc(n2);
+  for (int jk = 1; jk <= jpk - 1; ++jk) {
+    for (int jj = 2; jj <= jpj; ++jj)
+      for (int ji = 2; ji <= jpi; ++ji) {
+        const size_t q = I3(ji, jj, jk);
+        const double zu = un[q - 1] * un[q - 1] + un[q] * un[q];
+        const double zv = vn[q - jpi] * vn[q - jpi] + vn[q] * vn[q];
+        zhke[I2(ji, jj)] = 0.25 * (zv + zu);
+      }
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t p = I2(ji, jj), q = I3(ji, jj, jk);
+        ua[q] = ua[q] - (zhke[p + 1] - zhke[p]) / c->e1u[p];
+        va[q] = va[q] - (zhke[p + jpi] - zhke[p]) / c->e2v[p];
+      }
+  }
+  free(zhke);
+  return NEMO_OK;
+}
+
+/* dyn_zad (dynzad.F90): bound UN, VN, WN, UA, VA. */
+int ora_dyn_zad(ora_ctx *c, int kt) {
+  (void)kt;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  const double *un = c->f[NEMO_F_UN], *vn = c->f[NEMO_F_VN], *wn = c->f[NEMO_F_WN];
+  double *ua = c->f[NEMO_F_UA], *va = c->f[NEMO_F_VA];
+  if (!un || !vn || !wn || !ua || !va) return NEMO_ERR_UNBOUND;
+  const double *e3u = fld(c, NEMO_F_E3U_N), *e3v = fld(c, NEMO_F_E3V_N);
+  double *zww = zalloc(n2), *zwuw = zalloc(n3), *zwvw = zalloc(n3);
+  for (int jk = 2; jk <= jpk - 1; ++jk) {
+    for (int jj = 2; jj <= jpj; ++jj)
+      for (int ji = 2; ji <= jpi; ++ji) zww[I2(ji, jj)] = 0.25 * c->e1e2t[I2(ji, jj)] * wn[I3(ji, jj, jk)];
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t p = I2(ji, jj), q = I3(ji, jj, jk);
+        zwuw[q] = (zww[p + 1] + zww[p]) * (un[q - n2] - un[q]);
+        zwvw[q] = (zww[p + jpi] + zww[p]) * (vn[q - n2] - vn[q]);
+      }
+  }
+  for (int jk = 1; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t p = I2(ji, jj), q = I3(ji, jj, jk);
+        ua[q] = ua[q] - (zwuw[q] + zwuw[q + n2]) * c->r1_e1e2u[p] / e3u[q];
+        va[q] = va[q] - (zwvw[q] + zwvw[q + n2]) * c->r1_e1e2v[p] / e3v[q];
+      }
+  free(zww); free(zwuw); free(zwvw);
+  return NEMO_OK;
+}
+
 /* vor_ene (dynvor.F90:324-429), z-coordinate, no ln_dynvor_msk; kvor 1, 2 or 4. */
 int ora_vor_ene(ora_ctx *c, int kt, int kvor, const double *pun, const double *pvn, double *pua, double *pva) {
   (void)kt;

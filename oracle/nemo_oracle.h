@@ -108,6 +108,8 @@ int ora_dyn_hpg(ora_ctx *c, int kt);
 /* zdf_mxl; nlb10, the first W-level below 10 m */
 int ora_zdf_mxl(ora_ctx *c, int kt);
 int ora_nlb10(const ora_ctx *c);
+int ora_dyn_keg(ora_ctx *c, int kt, int kscheme);
+int ora_dyn_zad(ora_ctx *c, int kt);
 int ora_vor_ene(ora_ctx *c, int kt, int kvor, const double *pun, const double *pvn, double *pua, double *pva);
 int ora_dyn_ldf_lap(ora_ctx *c, int kt, const double *pub, const double *pvb, double *pua, double *pva, int kpass);
 /* 1: start the work arrays standing for Fortran automatic arrays as NaN */

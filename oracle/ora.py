@@ -64,6 +64,8 @@ def lib():
         P("ora_nlb10", [vp], C.c_int)
         P("ora_dyn_ldf_lap", [vp, i, vp, vp, vp, vp, i])
         P("ora_vor_ene", [vp, i, i, vp, vp, vp, vp])
+        P("ora_dyn_keg", [vp, i, i])
+        P("ora_dyn_zad", [vp, i])
         P("ora_tra_ldf_blp", [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
         P("ora_zps_hde", [vp, i, i, vp, vp, vp])
         _lib = L
@@ -262,6 +264,12 @@ class Oracle:
 
     def vor_ene(self, kt, kvor, pun, pvn, pua, pva):
         self._ck(lib().ora_vor_ene(self.h, kt, kvor, _p(pun), _p(pvn), _p(pua), _p(pva)), "vor_ene")
+
+    def dyn_keg(self, kt, kscheme=0):
+        self._ck(lib().ora_dyn_keg(self.h, kt, kscheme), "dyn_keg")
+
+    def dyn_zad(self, kt):
+        self._ck(lib().ora_dyn_zad(self.h, kt), "dyn_zad")
 
     def nlb10(self):
         return lib().ora_nlb10(self.h)

@@ -113,3 +113,62 @@ def test_gpu_vor_ene(prec):
     t = 1e-12 if prec == "fp64" else 5e-5
     p.compare("UA", p.s3, t)
     p.compare("VA", p.s3, t)
+
+
+def test_keg_and_zad_known_answers():
+    """Uniform horizontal flow: no kinetic-energy gradient in the interior; a trend
+    quadratic in the velocity (x2 -> x4, exactly); no vertical advection without w or
+    with a depth-independent flow."""
+    from oracle import ora
+    dom = gyre.domain(2)
+    o = ora.Oracle(dom, gyre.namelist())
+    s3 = (dom["jpi"], dom["jpj"], dom["jpk"])
+    _, um, vm, wm = gyre.masks(dom)
+    a = {k: np.zeros(s3, order="F") for k in ("UN", "VN", "WN", "UA", "VA")}
+    for k, v in a.items():
+        o.bind(k, v)
+    a["UN"][...] = 0.2 * um
+    a["VN"][...] = -0.1 * vm
+    o.dyn_keg(1)
+    inner = (slice(3, -3), slice(3, -3), slice(0, -1))
+    assert np.all(a["UA"][inner] == 0) and np.all(a["VA"][inner] == 0)
+    rng = np.random.default_rng(5)
+    a["UN"][...] = rng.standard_normal(s3) * um
+    a["VN"][...] = rng.standard_normal(s3) * vm
+    a["UA"][...] = 0.0
+    a["VA"][...] = 0.0
+    o.dyn_keg(1)
+    t1 = a["UA"].copy(), a["VA"].copy()
+    a["UN"][...] *= 2
+    a["VN"][...] *= 2
+    a["UA"][...] = 0.0
+    a["VA"][...] = 0.0
+    o.dyn_keg(1)
+    assert np.array_equal(a["UA"], 4 * t1[0]) and np.array_equal(a["VA"], 4 * t1[1])
+    a["UA"][...] = 0.0
+    a["VA"][...] = 0.0
+    o.dyn_zad(1)                                            # w = 0
+    assert np.all(a["UA"] == 0) and np.all(a["VA"] == 0)
+    a["WN"][...] = rng.standard_normal(s3) * wm
+    a["UN"][...] = np.broadcast_to(a["UN"][:, :, :1], s3)   # depth-independent
+    a["VN"][...] = np.broadcast_to(a["VN"][:, :, :1], s3)
+    o.dyn_zad(1)
+    assert np.all(a["UA"] == 0) and np.all(a["VA"] == 0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_gpu_keg_zad(prec):
+    pytest.importorskip("torch")
+    p = Pair(nn=2, prec=prec, seed=51, nmem=2)
+    p.bind_spg()
+    p.bind("WN")
+    for o in p.ora:
+        o.dyn_keg(3)
+        o.dyn_zad(3)
+    p.ctx.dyn_keg(3)
+    p.ctx.dyn_zad(3)
+    p.ctx.synchronize()
+    t = 1e-12 if prec == "fp64" else 5e-5
+    p.compare("UA", p.s3, t)
+    p.compare("VA", p.s3, t)
