@@ -30,6 +30,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "nemo-fmi-devel_gb300"))
 
+# the mixed form: FP32 storage and arithmetic; inside the sub-step kernel the five
+# barotropic time-filter sums are compensated FP32 pairs (error ~2^-46 of the sum),
+# written to FP64 fields once per step
+DTYPE_MIXED = "f32 bulk; barotropic time-filter sums as compensated f32 pairs, f64 results"
 METRIC = "cell-steps/s, mixed-precision vs FP64 GPU at ≤1e-3 K SST error; % HBM peak"
 UNIT = "cell-steps/s"
 # algorithmic bytes per 3-D cell of each routine (FP64, FP32-bulk): every 3-D field
@@ -85,6 +89,40 @@ TRAFFIC = {(k, "mixed", 25): v * 1e6 for k, v in {
     "spg_p2": 59.1, "iso_flux_tma": 548.6, "fct_c": 901.6, "fct_a_tma": 680.1, "fct_b_tma": 592.6, "zdf_imp": 277.5,
     "spg_p3": 219.6, "spg_p1a": 96.7, "spg_p1b": 36.2}.items()}
 TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, nn_GYRE=15 capture scaled by cells"
+
+
+# FP64 operations (DADD + DMUL + 2 x DFMA thread instructions) and FP64 divisions per
+# launch of the FP64 kernels, from one ncu capture at nn_GYRE=15, scaled to the
+# workload by cells: (kernel, nn_GYRE) -> (flops, divisions)
+FP64_OPS = {}
+FP64_OPS_SOURCE = None
+
+
+def fp64_kernels(kt, nsteps, cells, n2, icycle, nn, shelf):
+    """Per-kernel event time of the FP64 step, its algorithmic GB/s against the copy
+    bandwidth, and (where the ncu count exists) its FP64 FLOP/s."""
+    hbm, _ = peaks()
+    out = {}
+    for name, (kms, nl) in kt.items():
+        us = 1e3 * kms / max(nl, 1)
+        if name == "spg_p2":
+            kb = ALG_BYTES["dyn_spg_ts_substep_2d"][0] * icycle * n2
+        elif name in KERNEL_BYTES_2D:
+            kb = KERNEL_BYTES_2D[name][0] * n2
+        elif shelf:
+            kb = 0
+        else:
+            kb = KERNEL_FIELDS.get(name, 0) * 8 * cells
+        e = {"us": us, "launches_per_step": nl / nsteps, "alg_bytes": kb,
+             "alg_GBps": kb / (us / 1e6) / 1e9 if kb and us > 0 else None,
+             "frac": kb / (us / 1e6) / 1e9 / hbm if kb and us > 0 else None}
+        ops = FP64_OPS.get((name, nn))
+        if ops:
+            e["fp64_tflops"] = ops[0] / (us / 1e6) / 1e12
+            e["fp64_divisions_per_s"] = ops[1] / (us / 1e6)
+            e["fp64_ops_source"] = FP64_OPS_SOURCE
+        out[name] = e
+    return out
 
 
 def peaks():
@@ -154,6 +192,29 @@ def build_case(nn, nmem, seed, workload="gyre"):
     nam = gyre.namelist()
     states = [gyre.state(dom, nam, seed=seed, member=m) for m in range(nmem)]
     return dom, nam, states
+
+
+def config_dict(args, dom, nam, icycle, nn_baro, world):
+    """The workload's configuration, the same dict in both arms of the benchmark."""
+    cells = dom["jpi"] * dom["jpj"] * dom["jpk"] * args.members
+    return {"workload": workload_name(args), "grid": [dom["jpi"], dom["jpj"], dom["jpk"]],
+            "members": args.members, "cells": cells, "icycle": icycle, "nn_baro": nn_baro,
+            "rdt": nam["rn_rdt"], "ln_bench": args.workload == "gyre",
+            "l2": ("inputs larger than L2 (129 MB), no flush" if cells * 4 * 20 > 129e6
+                   else "inputs smaller than L2 (129 MB), no flush"),
+            "parallelism": f"replicas x{world}"}
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu), for the CPU figures."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
 
 
 def workload_name(args):
@@ -319,6 +380,7 @@ def run_gpu(args):
             ctx64.stp_hotpath(kt0 + 1000 + s)
         ctx64.synchronize()
         rt64, n64 = ctx64.get_timing()
+        kt64 = ctx64.get_kernel_timing()
         ctx64.set_timing(False)
         # the same step on the same inputs in both forms: SST (T at level 1) difference
         for c_, d_ in ((ctx, dev), (ctx64, dev64)):
@@ -340,6 +402,8 @@ def run_gpu(args):
         sss_err = float(np.abs(a32[:, :, 0, 1] - a64[:, :, 0, 1])[tm].max())
         fp64 = {"value": cells * world * k64 / (ms64 / 1e3), "ms_per_step": ms64 / k64,
                 "routine_ms": {k: v / max(n64, 1) for k, v in rt64.items()},
+                "kernels": fp64_kernels(kt64, 3, cells, n2=jpi * jpj * args.members, icycle=icycle, nn=args.nn,
+                                        shelf=args.workload == "shelf"),
                 "sst_abs_err_1step_K": sst_err, "sss_abs_err_1step_psu": sss_err}
         ctx64.close()
         del dev64
@@ -421,16 +485,12 @@ def run_gpu(args):
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 bulk + f64 accumulators" if args.prec == "mixed" else "f64",
+        "vs_baseline": None, "dtype": DTYPE_MIXED if args.prec == "mixed" else "f64",
         "data": "synthetic: seeded GYRE analytic state (no reference data files exist)" if args.workload == "gyre"
         else "synthetic: seeded shelf (lognormal bathymetry, z*, partial steps); no reference data files exist",
-        "config": {"workload": workload_name(args),
-                   "grid": [jpi, jpj, jpk], "members": args.members, "cells": cells, "icycle": icycle,
-                   "nn_baro": nn_baro, "rdt": nam["rn_rdt"], "ln_bench": args.workload == "gyre",
-                   "l2": "inputs larger than L2 (%.2f GB resident), no flush" % (
-                       sum(t.numel() * t.element_size() for t in dev.values()) / 1e9),
-                   "parallelism": f"replicas x{world}",
-                   "launch_shape": ({k: f"32x{v}" for k, v in shape.items()} if shape else "32x4 (not tuned)")},
+        "config": config_dict(args, dom, nam, icycle, nn_baro, world),
+        "resident_GB": sum(t.numel() * t.element_size() for t in dev.values()) / 1e9,
+        "launch_shape": ({k: f"32x{v}" for k, v in shape.items()} if shape else "32x4 (not tuned)"),
         "clocks": ck, "gpu_launches": int(round(launches_per_step * args.steps)),
         "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm if achieved else None, "traffic": TRAFFIC.get((top, args.prec, args.nn)),
@@ -451,61 +511,111 @@ def run_gpu(args):
         print(json.dumps(res))
 
 
-def cpu_baseline(dom, nam, st, budget_s=20.0, threads=None, what="GYRE nn_GYRE=25 workload"):
-    """The oracle (C FP64 restatement of the reference routines) on the host cores."""
-    import numpy as np
-    from oracle import ora
-    if threads:
-        os.environ["OMP_NUM_THREADS"] = str(threads)
-    o = ora.Oracle(dom, nam)
-    keep = {}
-    for n in ("tsb", "tsn") + HOT_3D + ("ub", "vb", "sshb") + HOT_2D:
-        keep[n] = np.array(st[n], order="F", copy=True)
-        o.bind(n.upper(), keep[n])
-    keep["rc"] = np.array(st["rcdu_bot"], order="F", copy=True)
-    o.bind("RCDU_BOT", keep["rc"])
-    for n in SHELF_FIELDS:
-        if n in st:
+class OracleStep:
+    """The oracle (C FP64 restatement of the reference routines) bound to one
+    member's state of the workload, stepping the hot path on the host cores."""
+
+    def __init__(self, dom, nam, st):
+        import numpy as np
+        from oracle import ora
+        self.o = o = ora.Oracle(dom, nam)
+        self.keep = keep = {}
+        for n in ("tsb", "tsn") + HOT_3D + ("ub", "vb", "sshb") + HOT_2D:
             keep[n] = np.array(st[n], order="F", copy=True)
             o.bind(n.upper(), keep[n])
-    keep["tsa"] = np.zeros_like(st["tsb"], order="F")
-    o.bind("TSA", keep["tsa"])
-    for n in ("AH_WSLP2", "AKZ"):
-        keep[n] = np.zeros_like(st["avt"], order="F")
-        o.bind(n, keep[n])
-    for n in ACC_2D:
-        keep[n] = np.array(st[n.lower()], order="F", copy=True) if n.lower() in st else np.zeros(st["sshn"].shape, order="F")
-        o.bind(n, keep[n])
+        keep["rc"] = np.array(st["rcdu_bot"], order="F", copy=True)
+        o.bind("RCDU_BOT", keep["rc"])
+        for n in SHELF_FIELDS:
+            if n in st:
+                keep[n] = np.array(st[n], order="F", copy=True)
+                o.bind(n.upper(), keep[n])
+        keep["tsa"] = np.zeros_like(st["tsb"], order="F")
+        o.bind("TSA", keep["tsa"])
+        for n in ("AH_WSLP2", "AKZ"):
+            keep[n] = np.zeros_like(st["avt"], order="F")
+            o.bind(n, keep[n])
+        for n in ACC_2D:
+            keep[n] = (np.array(st[n.lower()], order="F", copy=True) if n.lower() in st
+                       else np.zeros(st["sshn"].shape, order="F"))
+            o.bind(n, keep[n])
+        self.kt = 5
+
+    def step(self):
+        self.o.stp_hotpath(self.kt)
+        self.kt += 1
+
+    def close(self):
+        self.o.close()
+
+
+def cpu_baseline(dom, nam, st, budget_s=20.0, what="GYRE nn_GYRE=25 workload"):
+    """The oracle on the host cores: all cores (OpenMP) on a bounded sample of full
+    steps, and one core on one step. The oracle's work arrays are allocated on the
+    first (untimed) step and reused after it."""
+    from oracle import ora
+    ncores = os.cpu_count()
     cells = dom["jpi"] * dom["jpj"] * dom["jpk"]
+    s = OracleStep(dom, nam, st)
+    ora.set_threads(ncores)
+    s.step()  # untimed: first touch of the work arrays
     t0 = time.perf_counter()
     n = 0
     while True:
-        o.stp_hotpath(5 + n)
+        s.step()
         n += 1
-        if time.perf_counter() - t0 > budget_s or n >= 50:
+        if time.perf_counter() - t0 > 0.7 * budget_s or n >= 50:
             break
     dt = time.perf_counter() - t0
-    nthr = int(os.environ.get("OMP_NUM_THREADS", "0") or 0) or os.cpu_count()
-    o.close()
-    return {"value": cells * n / dt, "unit": UNIT, "cores": nthr, "kind": "port",
-            "sample": f"{n} full hot-path steps of the same {what} (FP64 oracle, OpenMP)"}
+    ora.set_threads(1)
+    t1 = time.perf_counter()
+    s.step()
+    dt1 = time.perf_counter() - t1
+    ora.set_threads(ncores)
+    s.close()
+    return {"value": cells * n / dt, "unit": UNIT, "cores": ncores, "kind": "port",
+            "sample": f"{n} full hot-path steps of the same {what} (FP64 oracle, OpenMP, {ncores} threads) "
+                      f"after one untimed step",
+            "single_thread": {"value": cells / dt1, "unit": UNIT, "cores": 1, "sample": "one full step"},
+            "cpu_model": cpu_model(), "build": "gcc -O3 -ffp-contract=off -fno-fast-math -fopenmp"}
 
 
 def run_reference(args):
+    """The reference arm: the oracle on the host cores, --warmup untimed full steps
+    then exactly --steps timed full steps of the same workload (rank 0 only)."""
     from nemo_gpu import dist
+    from oracle import ora
     rank, world = dist.init("gloo")
     if rank != 0:
         return
-    dom, nam, states = build_case(args.nn, 1, seed=100, workload=args.workload)
-    cb = cpu_baseline(dom, nam, states[0], budget_s=max(5.0, min(60.0, 2.0 * args.steps)), what=workload_name(args))
-    res = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": world,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dom["jpi"] * dom["jpj"] * dom["jpk"] / cb["value"],
+    dom, nam, states = build_case(args.nn, args.members, seed=100, workload=args.workload)
+    ncores = os.cpu_count()
+    ora.set_threads(ncores)
+    members = [OracleStep(dom, nam, st) for st in states]  # one oracle per member, stepped in turn
+    icycle, nn_baro, _ = members[0].o.spg_info()
+    for _ in range(args.warmup):
+        for s in members:
+            s.step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for s in members:
+            s.step()
+    dt = time.perf_counter() - t0
+    for s in members:
+        s.close()
+    cells = dom["jpi"] * dom["jpj"] * dom["jpk"] * args.members
+    value = cells * args.steps / dt
+    cb = {"value": value, "unit": UNIT, "cores": ncores, "kind": "port",
+          "sample": f"{args.steps} full hot-path steps after {args.warmup} untimed ones (FP64 oracle, OpenMP, "
+                    f"{ncores} threads)", "cpu_model": cpu_model(),
+          "build": "gcc -O3 -ffp-contract=off -fno-fast-math -fopenmp"}
+    res = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-           "data": "synthetic: seeded GYRE analytic state" if args.workload == "gyre" else "synthetic: seeded shelf",
-           "config": {"workload": workload_name(args),
-                      "grid": [dom["jpi"], dom["jpj"], dom["jpk"]], "members": 1},
+           "data": "synthetic: seeded GYRE analytic state (no reference data files exist)" if args.workload == "gyre"
+           else "synthetic: seeded shelf (lognormal bathymetry, z*, partial steps); no reference data files exist",
+           "config": config_dict(args, dom, nam, icycle, nn_baro, world),
            "cpu_baseline": cb,
-           "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "note": "NEMO (Fortran) cannot be built in this environment; the reference arm runs the C FP64 "
                    "restatement of the same routines (oracle/) on the host cores"}
     print(json.dumps(res))
@@ -549,7 +659,7 @@ def run_model(args):
             "metric": "cell-steps/s of the model step (hot path + wzv, dyn_zdf time step, tra_nxt, dyn_nxt, ssh_swp)",
             "value": cells * world * args.steps / (ms / 1e3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 bulk + f64 accumulators" if args.prec == "mixed" else "f64",
+            "vs_baseline": None, "dtype": DTYPE_MIXED if args.prec == "mixed" else "f64",
             "data": "synthetic: seeded GYRE analytic state",
             "config": {"workload": f"GYRE nn_GYRE={args.nn} model step", "grid": [jpi, jpj, jpk],
                        "members": args.members, "cells": cells},

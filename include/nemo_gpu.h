@@ -476,9 +476,9 @@ int nemo_gpu_glob_sum(nemo_ctx *ctx, const char *cdname, const void *ptab, int n
                       int is_fp64, double *out);
 
 /* glob_sum without any device allocation, for callers that cannot allocate at
- * the point of the call: code running inside an open CUDA stream capture, hosts
- * whose device memory belongs to another runtime (OpenACC / CUDA Fortran data
- * regions, a coupler's caching allocator), or set-ups that fix their device
+ * the point of the call: hosts whose device memory belongs to another runtime
+ * (OpenACC / CUDA Fortran data regions, a coupler's caching allocator), which must
+ * not see allocations made behind its back, and set-ups that fix their device
  * footprint at start-up. This entry point has no counterpart in the reference
  * (whose glob_sum is lib_fortran_generic.h90:32-65); it computes the same masked
  * double-double sum as nemo_gpu_glob_sum but needs no context: ptab holds nmembers
@@ -578,6 +578,14 @@ int nemo_gpu_set_fct_fused(nemo_ctx *ctx, int on);
  * NEMO_ERR_TIMEOUT. extra_arrivals > 0 makes every barrier wait for blocks that do
  * not exist, so that the timeout path can be exercised without faulting the GPU. */
 int nemo_gpu_set_barrier_limit(nemo_ctx *ctx, long long max_spins, int extra_arrivals);
+
+/* Bound of each wait of the TMA-staged tracer kernels on their tensor copies:
+ * max_polls polls of at most ~1 us each (default 65536). When a wait gives up, the
+ * kernel records the failure, still waits (with its own fixed bound) for every copy
+ * it has issued, and returns; the next nemo_gpu_synchronize() returns
+ * NEMO_ERR_TIMEOUT. max_polls = 0 makes the first wait give up at once, so that the
+ * timeout path can be exercised without faulting the GPU. */
+int nemo_gpu_set_tma_poll_limit(nemo_ctx *ctx, int max_polls);
 
 #ifdef __cplusplus
 }

@@ -91,6 +91,7 @@ struct nemo_ctx {
   unsigned int* bar_mem = nullptr;  // count, gen
   int* err_flag = nullptr;
   long long bar_spins = 4000000;
+  int tma_polls = 1 << 16;  // bound of each wait of a TMA kernel on its tensor copies
   int bar_extra = 0;
   int p2_blocks = 0;
   int p2_cache = 0;  // the sub-step kernel keeps its constants in shared memory
@@ -698,7 +699,7 @@ int run_fct(nemo_ctx* c, double p2dt, const void* pun, const void* pvn, const vo
   a.betup = (T*)c->fct_w[4]; a.betdo = (T*)c->fct_w[5];
   a.ztw = (const T*)c->fct_ztw;
   a.kjpt = kjpt; a.kn_fct_h = kh; a.kn_fct_v = kv; a.linssh = c->nam.ln_linssh;
-  a.tma = !c->no_tma; a.fused = c->fct_fused; a.err = c->err_flag;
+  a.tma = !c->no_tma; a.fused = c->fct_fused; a.err = c->err_flag; a.polls = c->tma_polls;
   if (iso) {
     a.with_iso = 1;
     a.iso = *iso;
@@ -747,7 +748,7 @@ int iso_args(nemo_ctx* c, int kt, int kit000, const void* pahu, const void* pahv
   a.ah_wslp2 = (T*)c->f[NEMO_F_AH_WSLP2]; a.akz = (T*)c->f[NEMO_F_AKZ];
   a.lap = nm.ln_traldf_lap; a.blp = nm.ln_traldf_blp; a.msc = nm.ln_traldf_msc;
   a.zftu = (T*)c->iso_w[0]; a.zftv = (T*)c->iso_w[1]; a.ztfw = (T*)c->iso_w[2];
-  a.tma = !c->no_tma; a.err = c->err_flag;
+  a.tma = !c->no_tma; a.err = c->err_flag; a.polls = c->tma_polls;
   const double z2dt = (nm.neuler == 0 && kt == nm.nit000) ? nm.rn_rdt : 2.0 * nm.rn_rdt;
   a.z2dt = (T)z2dt; a.z1_2dt = (T)(1.0 / z2dt);
   if (kpass == 1 && kt == kit000) {
@@ -2220,6 +2221,14 @@ int nemo_gpu_set_fct_fused(nemo_ctx* c, int on) {
 int nemo_gpu_set_tma(nemo_ctx* c, int on) {
   if (!c) return NEMO_ERR_ARG;
   c->no_tma = !on;
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);
+  c->graphs.clear();
+  return NEMO_OK;
+}
+
+int nemo_gpu_set_tma_poll_limit(nemo_ctx* c, int max_polls) {
+  if (!c || max_polls < 0) return fail(c, NEMO_ERR_ARG, "set_tma_poll_limit: bad argument");
+  c->tma_polls = max_polls;
   for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);
   c->graphs.clear();
   return NEMO_OK;

@@ -85,7 +85,7 @@ cudaError_t launch_fct(const Dom<T>& d, const FctArgs<T>& a, cudaStream_t s) {
                 cudaFuncSetAttribute(k_fct_fused_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, FF_SMEM);
             if (attr != cudaSuccess) return attr;
             const dim3 grid((d.jpi + TM_X - 1) / TM_X, (d.jpj + TM_Y - 1) / TM_Y, d.nmem);
-            k_fct_fused_tma<T><<<grid, dim3(TM_X, TM_Y), FF_SMEM, s>>>(d, a, maps, a.err, 1 << 16);
+            k_fct_fused_tma<T><<<grid, dim3(TM_X, TM_Y), FF_SMEM, s>>>(d, a, maps, a.err, a.polls);
             ktick(NEMO_K_FCT_FUSED, s);
             return cudaGetLastError();
           }
@@ -112,9 +112,9 @@ cudaError_t launch_fct(const Dom<T>& d, const FctArgs<T>& a, cudaStream_t s) {
             if (attr_a != cudaSuccess) return attr_a;
             if (attr_b != cudaSuccess) return attr_b;
             const dim3 grid((d.jpi + TM_X - 1) / TM_X, (d.jpj + TM_Y - 1) / TM_Y, d.nmem * ((d.jpk + KCH - 1) / KCH));
-            k_fct_a_tma<T><<<grid, dim3(TM_X, TM_Y), FA_SMEM, s>>>(d, a, ma, a.err, 1 << 16);
+            k_fct_a_tma<T><<<grid, dim3(TM_X, TM_Y), FA_SMEM, s>>>(d, a, ma, a.err, a.polls);
             ktick(NEMO_K_FCT_A_TMA, s);
-            k_fct_b_tma<T><<<grid, dim3(TM_X, TM_Y), FB_SMEM, s>>>(d, a, mb, a.err, 1 << 16);
+            k_fct_b_tma<T><<<grid, dim3(TM_X, TM_Y), FB_SMEM, s>>>(d, a, mb, a.err, a.polls);
             ktick(NEMO_K_FCT_B_TMA, s);
             const int tc = kty(NEMO_K_FCT_C);
             k_fct_c_hot<T><<<kc_grid(d, tc), dim3(BX, tc), 0, s>>>(d, a);
@@ -172,7 +172,7 @@ cudaError_t launch_iso_flux(const Dom<T>& d, const LdfArgs<T>& a, cudaStream_t s
           field_tensor_map(d, a.wslpi.p, 1, TM_X, TM_Y, &maps.wslpi) &&
           field_tensor_map(d, a.wslpj.p, 1, TM_X, TM_Y, &maps.wslpj)) {
         const dim3 grid((d.jpi + TM_X - 1) / TM_X, (d.jpj + TM_Y - 1) / TM_Y, d.nmem * ((d.jpk + KCH - 1) / KCH));
-        k_iso_flux_tma<T><<<grid, dim3(TM_X, TM_Y), 0, s>>>(d, a, maps, a.err, 1 << 16);
+        k_iso_flux_tma<T><<<grid, dim3(TM_X, TM_Y), 0, s>>>(d, a, maps, a.err, a.polls);
         ktick(NEMO_K_ISO_FLUX_TMA, s);
         return cudaGetLastError();
       }

@@ -54,6 +54,10 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
       "l"((unsigned long long)map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
       : "memory");
 }
+// After a failed wait a kernel still waits for every copy it has issued, with this
+// bound (independent of the caller's max_polls), before it returns.
+constexpr int TM_DRAIN_POLLS = 1 << 16;
+
 // wait for the completion of phase `parity`; false after max_polls polls of at most
 // ~1 us each (suspend-time hint), so a wait never lasts longer than ~max_polls us
 __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, int max_polls) {
@@ -322,7 +326,7 @@ __global__ void __launch_bounds__(TM_X * TM_Y, 2)
       for (unsigned s = 0; s < TM_NS; ++s) {
         if (issued <= s) continue;
         const unsigned last = s + TM_NS * ((issued - 1 - s) / TM_NS);  // last plane issued into slot s
-        mbar_wait(&bar[s], (last / TM_NS) & 1, max_polls);
+        mbar_wait(&bar[s], (last / TM_NS) & 1, TM_DRAIN_POLLS);
       }
     }
     __syncthreads();
@@ -627,7 +631,7 @@ __global__ void __launch_bounds__(TM_X * TM_Y, 2)
       for (unsigned s = 0; s < FF_NS; ++s) {
         if (issued <= s) continue;
         const unsigned last = s + FF_NS * ((issued - 1 - s) / FF_NS);
-        mbar_wait(&bar[s], (last / FF_NS) & 1, max_polls);
+        mbar_wait(&bar[s], (last / FF_NS) & 1, TM_DRAIN_POLLS);
       }
     }
     __syncthreads();
@@ -793,7 +797,7 @@ __global__ void __launch_bounds__(TM_X * TM_Y, 3)
   if (!ok) {
     if (c.tid == 0) {
       atomicExch(err, TM_ERR);
-      ring.drain(issued, max_polls);
+      ring.drain(issued, TM_DRAIN_POLLS);
     }
     __syncthreads();
   }
@@ -920,7 +924,7 @@ __global__ void __launch_bounds__(TM_X * TM_Y, 3)
   if (!ok) {
     if (c.tid == 0) {
       atomicExch(err, TM_ERR);
-      ring.drain(issued, max_polls);
+      ring.drain(issued, TM_DRAIN_POLLS);
     }
     __syncthreads();
   }

@@ -126,6 +126,7 @@ struct LdfArgs {
   T *zftu, *zftv, *ztfw;     // work: iso-neutral fluxes (jpi,jpj,jpk,kjpt)
   int tma;                   // FP32 hot configuration: stage the tracer planes by TMA
   int* err;                  // device error flag (a timed-out wait of the TMA kernel)
+  int polls;                 // bound of each wait on a tensor copy (polls of <= ~1 us)
 };
 
 // Arguments shared by the three FCT kernels.
@@ -146,6 +147,7 @@ struct FctArgs {
   int tma;                   // FP32 hot configuration: stage the planes by TMA
   int fused;                 // with tma: the three stages as one kernel (k_fct_fused_tma)
   int* err;                  // device error flag (a timed-out wait of a TMA kernel)
+  int polls;                 // bound of each wait on a tensor copy (polls of <= ~1 us)
   T* lim;                    // NULL, or where k_fct_c records the limiter multipliers
                              // ((member*kjpt + n)*3 + face)*n3, for the adjoint
 };

@@ -2,9 +2,6 @@
 //
 // Some callers of this library cannot allocate device memory at the point where
 // they need a global sum:
-//  * code that runs while a CUDA stream capture is open: cudaMalloc / cudaFree are
-//    not permitted inside a capture in the default (global) mode, and an
-//    allocation made there would not be replayed by the graph anyway;
 //  * host models whose device memory is owned by another runtime -- an OpenACC or
 //    CUDA Fortran data region, or the caching allocator of a coupling framework --
 //    which must not see allocations made behind its back;
@@ -13,7 +10,8 @@
 // They can call nemo_gpu_glob_sum_noalloc: it needs no context, takes the field, the
 // mask and the output as device pointers, and keeps its block partial sums in the
 // file-scope array g_globsum_scratch below (about 1 MB that every GPU which loads
-// the library holds until the process exits).
+// the library holds until the process exits). It calls no cudaMalloc, cudaFree or
+// other allocating routine.
 #include <cstdio>
 #include <mutex>
 

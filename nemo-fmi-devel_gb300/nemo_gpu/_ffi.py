@@ -152,6 +152,7 @@ def load(path):
     _proto(lib, "nemo_gpu_set_timing", i, [vp, i])
     _proto(lib, "nemo_gpu_set_fusion", i, [vp, i])
     _proto(lib, "nemo_gpu_set_tma", i, [vp, i])
+    _proto(lib, "nemo_gpu_set_tma_poll_limit", i, [vp, i])
     _proto(lib, "nemo_gpu_set_fct_fused", i, [vp, i])
     _proto(lib, "nemo_gpu_get_timing", i, [vp, C.POINTER(d), C.POINTER(i)])
     _proto(lib, "nemo_gpu_get_kernel_timing", i, [vp, C.POINTER(d), C.POINTER(i), i])

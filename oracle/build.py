@@ -1,7 +1,10 @@
 """Build recipe of the oracle (test infrastructure; see nemo_oracle.h).
 
-gcc -O2 -ffp-contract=off: no multiply-add fusion, so each FP64 operation rounds
-like the reference's gfortran build without FMA contraction.
+gcc -O3 -ffp-contract=off -fno-fast-math: no multiply-add fusion and no
+reassociation, so each FP64 operation rounds like the reference's gfortran build
+without FMA contraction (-O3's vectorisation keeps every operation and its order).
+No -march/-mcpu=native: the same source builds on the x86 container and on the
+Arm host of the GPU and must give the same results on both.
 """
 import os
 import subprocess
@@ -16,7 +19,7 @@ def build(force=False):
     os.makedirs(os.path.dirname(OUT), exist_ok=True)
     if not force and os.path.exists(OUT) and all(os.path.getmtime(p) < os.path.getmtime(OUT) for p in [src] + hdrs):
         return OUT
-    cmd = ["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-fPIC", "-shared",
+    cmd = ["gcc", "-std=c11", "-O3", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-fPIC", "-shared",
            "-fopenmp", "-o", OUT, src, "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -10,7 +10,7 @@
  * with 1-based index helpers I2/I3/I4. Automatic Fortran work arrays that the
  * reference leaves undefined outside the loop ranges are zero-filled here; the
  * routines never read those points (this is checked by the NaN-poisoning test).
- * Compile with -O2 -ffp-contract=off so that no multiply-add is fused.
+ * Compile with -ffp-contract=off so that no multiply-add is fused.
  */
 #include "nemo_oracle.h"
 
@@ -59,18 +59,85 @@ struct ora_ctx {
 };
 
 static void spg_coriolis_factors(ora_ctx *c, const double *ht_n, const double *e3f_n);
-static double *zalloc(size_t n) { return (double *)calloc(n ? n : 1, sizeof(double)); }
+
+/* Work arrays of the routines come from a small per-thread pool of freed blocks
+ * (a block of the same length is reused), so that a time loop over the routines
+ * allocates only on its first step, as the reference's automatic arrays live on
+ * the stack. The pool keeps at most WP_SLOTS blocks and WP_BYTES bytes. */
+#define WP_SLOTS 96
+#define WP_BYTES ((size_t)6 << 30)
+static _Thread_local struct { double *p[WP_SLOTS]; size_t n[WP_SLOTS]; int cnt; size_t bytes; } g_wpool;
+
+static double *pool_take(size_t n) {
+  for (int s = g_wpool.cnt - 1; s >= 0; --s)
+    if (g_wpool.n[s] == n) {
+      double *p = g_wpool.p[s];
+      g_wpool.bytes -= n * sizeof(double);
+      g_wpool.p[s] = g_wpool.p[g_wpool.cnt - 1];
+      g_wpool.n[s] = g_wpool.n[g_wpool.cnt - 1];
+      g_wpool.cnt--;
+      return p;
+    }
+  return (double *)malloc(n * sizeof(double));
+}
+/* return a block of n doubles from zalloc / walloc to the pool */
+static void wfree_n(double *p, size_t n) {
+  if (!p) return;
+  if (g_wpool.cnt < WP_SLOTS && g_wpool.bytes + n * sizeof(double) <= WP_BYTES) {
+    g_wpool.p[g_wpool.cnt] = p;
+    g_wpool.n[g_wpool.cnt] = n;
+    g_wpool.cnt++;
+    g_wpool.bytes += n * sizeof(double);
+  } else {
+    free(p);
+  }
+}
+/* the length of each block handed out, kept in a header in front of it */
+static double *blk_new(size_t n) {
+  double *b = pool_take(n + 2);
+  if (!b) return NULL;
+  b[0] = (double)n;
+  return b + 2;
+}
+static void wfree(double *p) {
+  if (p) wfree_n(p - 2, (size_t)p[-2] + 2);
+}
+/* zero-filled: arrays the reference sets to 0 itself (or reads as 0) */
+static double *zalloc(size_t n) {
+  n = n ? n : 1;
+  double *p = blk_new(n);
+  if (!p) return NULL;
+  OMP_FOR
+  for (size_t i = 0; i < n; ++i) p[i] = 0.0;
+  return p;
+}
 
 /* Work arrays that stand for the reference's automatic arrays (undefined until
- * written). With ora_set_poison(1) they start as NaN instead of 0, so a test can
+ * written): not cleared. With ora_set_poison(1) they start as NaN, so a test can
  * show that no routine reads a point the reference leaves undefined. */
 static int g_poison = 0;
 void ora_set_poison(int on) { g_poison = on; }
 static double *walloc(size_t n) {
-  double *p = zalloc(n);
-  if (g_poison)
+  n = n ? n : 1;
+  double *p = blk_new(n);
+  if (p && g_poison)
     for (size_t i = 0; i < n; ++i) p[i] = NAN;
   return p;
+}
+
+/* OpenMP threads of the routines' parallel loops (the CPU baseline's 1-thread and
+ * all-core figures); n < 1 keeps the current setting. */
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+int ora_set_threads(int n) {
+#ifdef _OPENMP
+  if (n >= 1) omp_set_num_threads(n);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
 }
 
 /* SIGN(a,b) of lib_fortran.F90:339-351 (key_nosignedzero): b >= 0 gives |a|. */
@@ -162,7 +229,7 @@ static int ext_lev(const ora_ctx *c, const double *e3t_0, double prldex, double 
       pjl = jk;
     }
   }
-  free(gdepw);
+  wfree(gdepw);
   return pjl;
 }
 
@@ -317,7 +384,7 @@ int ora_destroy(ora_ctx *c) {
                    &c->wgtbtp1, &c->wgtbtp2, &c->zwz, &c->ftne, &c->ftnw, &c->ftse, &c->ftsw,
                    &c->sshn_e, &c->sshb_e, &c->sshbb_e, &c->un_e, &c->ub_e, &c->ubb_e, &c->vn_e, &c->vb_e,
                    &c->vbb_e, &c->ssha_e, &c->ua_e, &c->va_e, &c->hu_e, &c->hv_e, &c->hur_e, &c->hvr_e};
-  for (size_t i = 0; i < sizeof(dp) / sizeof(dp[0]); ++i) free(*dp[i]);
+  for (size_t i = 0; i < sizeof(dp) / sizeof(dp[0]); ++i) wfree(*dp[i]);
   free(c->mikt); free(c->mbkt); free(c->mbku); free(c->mbkv);
   free(c);
   return NEMO_OK;
@@ -443,7 +510,7 @@ int ora_interp_4th_cpt(ora_ctx *c, const double *pt_in, double *pt_out) {
     for (int jj = 2; jj <= jpj - 1; ++jj)
       for (int ji = 2; ji <= jpi - 1; ++ji)
         pt_out[I3(ji, jj, jk)] = (pt_out[I3(ji, jj, jk)] - zws[I3(ji, jj, jk)] * pt_out[I3(ji, jj, jk + 1)]) / zwt[I3(ji, jj, jk)];
-  free(zwd); free(zwi); free(zws); free(zwrm); free(zwt);
+  wfree(zwd); wfree(zwi); wfree(zws); wfree(zwrm); wfree(zwt);
   return NEMO_OK;
 }
 
@@ -509,7 +576,7 @@ static void nonosc(ora_ctx *c, const double *pbef, double *paa, double *pbb, dou
       }
   lbc_closed(jpi, jpj, paa, jpk, 'U', 0.0);
   lbc_closed(jpi, jpj, pbb, jpk, 'V', 0.0);
-  free(zbetup); free(zbetdo); free(zbup); free(zbdo);
+  wfree(zbetup); wfree(zbetdo); wfree(zbup); wfree(zbdo);
 }
 
 /* --------------------------------------------------------------- tra_adv_fct */
@@ -660,7 +727,7 @@ int ora_tra_adv_fct(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
                            + zwz[q] - zwz[I3(ji, jj, jk + 1)]) * c->r1_e1e2t[I2(ji, jj)] / e3t_n[q];
         }
   }
-  free(zwi); free(zwx); free(zwy); free(zwz); free(ztu); free(ztv); free(zltu); free(zltv); free(ztw);
+  wfree(zwi); wfree(zwx); wfree(zwy); wfree(zwz); wfree(ztu); wfree(ztv); wfree(zltu); wfree(zltv); wfree(ztw);
   return NEMO_OK;
 }
 
@@ -713,7 +780,7 @@ int ora_tra_ldf_lap(ora_ctx *c, int kt, int kit000, const char *cdtype,
                               / (c->e1e2t[I2(ji, jj)] * e3t_n[q]);
         }
   }
-  free(ztu); free(ztv); free(zaheeu); free(zaheev);
+  wfree(ztu); wfree(ztv); wfree(zaheeu); wfree(zaheev);
   return NEMO_OK;
 }
 
@@ -911,7 +978,7 @@ int ora_tra_ldf_iso(ora_ctx *c, int kt, int kit000, const char *cdtype,
           ta[q] = ta[q] + zsign * (ztfw[q] - ztfw[I3(ji, jj, jk + 1)]) * c->r1_e1e2t[I2(ji, jj)] / e3t_n[q];
         }
   }
-  free(zdit); free(zdjt); free(zftu); free(zftv); free(ztfw); free(zdkt); free(zdk1t);
+  wfree(zdit); wfree(zdjt); wfree(zftu); wfree(zftv); wfree(ztfw); wfree(zdkt); wfree(zdk1t);
   return NEMO_OK;
 }
 
@@ -974,7 +1041,7 @@ int ora_tra_zdf_imp(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
     double *ta = pta + n3 * (jn - 1);
     if ((!is_trc && (jn == 1 || (jn == 2 && nm->ln_zdfddm))) || (is_trc && jn == 1)) {
       const double *coef = (!is_trc && jn == 1) ? avt : avs;
-      if (!coef) { free(zwi); free(zwt); free(zwd); free(zws); return NEMO_ERR_UNBOUND; }
+      if (!coef) { wfree(zwi); wfree(zwt); wfree(zwd); wfree(zws); return NEMO_ERR_UNBOUND; }
       zdf_lu(c, coef, p2dt, zwi, zwt, zwd, zws);
     }
     for (int jj = 2; jj <= jpj - 1; ++jj)
@@ -1003,7 +1070,7 @@ int ora_tra_zdf_imp(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
           ta[q] = (ta[q] - zws[q] * ta[I3(ji, jj, jk + 1)]) / zwt[q] * tmask[q];
         }
   }
-  free(zwi); free(zwt); free(zwd); free(zws);
+  wfree(zwi); wfree(zwt); wfree(zwd); wfree(zws);
   return NEMO_OK;
 }
 
@@ -1093,7 +1160,7 @@ static void spg_coriolis_factors(ora_ctx *c, const double *ht_n, const double *e
       if (zhf[p] != 0.0) c->zwz[p] = 1.0 / zhf[p];
     for (size_t p = 0; p < n2; ++p) c->zwz[p] = c->ff_f[p] * c->zwz[p];
   }
-  free(zhf);
+  wfree(zhf);
 }
 
 /* ---------------------------------------------------------------- dyn_spg_ts */
@@ -1577,9 +1644,9 @@ int ora_dyn_spg_ts(ora_ctx *c, int kt) {
       un[q] = (un[q] + un_adv[p] * r1_hu_n[p] - un_b[p]) * umask[q];
       vn[q] = (vn[q] + vn_adv[p] * r1_hv_n[p] - vn_b[p]) * vmask[q];
     }
-  free(zu_frc); free(zv_frc); free(zu_trd); free(zv_trd); free(zwx); free(zwy); free(zssh_frc); free(zhdiv);
-  free(zsshp2_e); free(zCdU_u); free(zCdU_v);
-  free(zhup2_e); free(zhvp2_e); free(zhtp2_e); free(zsshu_a); free(zsshv_a); free(zhust_e); free(zhvst_e);
+  wfree(zu_frc); wfree(zv_frc); wfree(zu_trd); wfree(zv_trd); wfree(zwx); wfree(zwy); wfree(zssh_frc); wfree(zhdiv);
+  wfree(zsshp2_e); wfree(zCdU_u); wfree(zCdU_v);
+  wfree(zhup2_e); wfree(zhvp2_e); wfree(zhtp2_e); wfree(zsshu_a); wfree(zsshv_a); wfree(zhust_e); wfree(zhvst_e);
   return NEMO_OK;
 }
 
@@ -1676,7 +1743,7 @@ int ora_tra_ldf_blp(ora_ctx *c, int kt, int kit000, const char *cdtype,
     st = kldf == 20 ? ora_tra_ldf_lap(c, kt, kit000, cdtype, pahu, pahv, zglu, zglv, NULL, NULL, zlap, pta, kjpt, 2)
                     : ora_tra_ldf_iso(c, kt, kit000, cdtype, pahu, pahv, zglu, zglv, NULL, NULL, zlap, ptb, pta, kjpt, 2);
   }
-  free(zlap); free(zglu); free(zglv);
+  wfree(zlap); wfree(zglu); wfree(zglv);
   return st;
 }
 
@@ -1703,7 +1770,7 @@ static int stp_tracers(ora_ctx *c, int kt) {
   ora_tra_adv_trp(c, c->f[NEMO_F_UN], c->f[NEMO_F_VN], c->f[NEMO_F_WN], zun, zvn, zwn);
   st = ora_tra_adv_fct(c, kt, nm->nit000, "TRA", r2dt, zun, zvn, zwn, tsb, tsn, tsa, 2, nm->nn_fct_h ? nm->nn_fct_h : 2,
                        nm->nn_fct_v ? nm->nn_fct_v : 2);
-  free(zun); free(zvn); free(zwn);
+  wfree(zun); wfree(zvn); wfree(zwn);
   if (st) return st;
   const double *ahtu = c->f[NEMO_F_AHTU], *ahtv = c->f[NEMO_F_AHTV];
   if (nm->ln_traldf_blp)   /* traldf.F90:75-76 */
@@ -1839,7 +1906,7 @@ int ora_tra_adv_fct_adj(ora_ctx *c, int kt, int kit000, const char *cdtype, doub
           tb_ad[I3(ji, jj + 1, jk)] += 0.5 * (pvn[q] - fabs(pvn[q])) * fy[q];
         }
   }
-  free(ax); free(ay); free(az); free(fx); free(fy); free(fz);
+  wfree(ax); wfree(ay); wfree(az); wfree(fx); wfree(fy); wfree(fz);
   return NEMO_OK;
 }
 
@@ -1885,7 +1952,7 @@ int ora_tra_ldf_lap_adj(ora_ctx *c, int kt, int kit000, const char *cdtype,
           tb_ad[I3(ji, jj + 1, jk)] += av; tb_ad[q] -= av;
         }
   }
-  free(ztu); free(ztv);
+  wfree(ztu); wfree(ztv);
   return NEMO_OK;
 }
 
@@ -2030,7 +2097,7 @@ int ora_tra_ldf_iso_adj(ora_ctx *c, int kt, int kit000, const char *cdtype,
           tb_ad[I3(ji, jj + 1, jk)] += b; tb_ad[q] -= b;
         }
   }
-  free(dit); free(djt); free(tfw); free(dkt); free(dk1t); free(ftu); free(ftv);
+  wfree(dit); wfree(djt); wfree(tfw); wfree(dkt); wfree(dk1t); wfree(ftu); wfree(ftv);
   return NEMO_OK;
 }
 
@@ -2053,7 +2120,7 @@ int ora_tra_zdf_imp_adj(ora_ctx *c, int kt, int kit000, const char *cdtype, doub
     double *tb_ad = ptb_ad + n3 * (jn - 1), *lam = pta_ad + n3 * (jn - 1);
     if ((!is_trc && (jn == 1 || (jn == 2 && nm->ln_zdfddm))) || (is_trc && jn == 1)) {
       const double *coef = (!is_trc && jn == 1) ? avt : avs;
-      if (!coef) { free(zwi); free(zwt); free(zwd); free(zws); return NEMO_ERR_UNBOUND; }
+      if (!coef) { wfree(zwi); wfree(zwt); wfree(zwd); wfree(zws); return NEMO_ERR_UNBOUND; }
       zdf_lu(c, coef, p2dt, zwi, zwt, zwd, zws);
     }
     for (int jj = 2; jj <= jpj - 1; ++jj)
@@ -2079,7 +2146,7 @@ int ora_tra_zdf_imp_adj(ora_ctx *c, int kt, int kit000, const char *cdtype, doub
         lam[q1] = p2dt * e3t_n[q1] * lam[q1];
       }
   }
-  free(zwi); free(zwt); free(zwd); free(zws);
+  wfree(zwi); wfree(zwt); wfree(zwd); wfree(zws);
   return NEMO_OK;
 }
 
@@ -2188,7 +2255,7 @@ int ora_wzv(ora_ctx *c, int kt) {
       size_t q = p + n2 * (jk - 1);
       wn[q] = wn[q + n2] - (e3t_n[q] * hdivn[q] + z1_2dt * (e3t_a[q] - e3t_b[q])) * c->tmask[q];
     }
-  free(hdivn);
+  wfree(hdivn);
   return NEMO_OK;
 }
 
@@ -2283,7 +2350,7 @@ int ora_dyn_nxt(ora_ctx *c, int kt) {
     un_b[p] = un_b[p] * c->r1_hu_0[p]; vn_b[p] = vn_b[p] * c->r1_hv_0[p];
     ub_b[p] = ub_b[p] * c->r1_hu_0[p]; vb_b[p] = vb_b[p] * c->r1_hv_0[p];
   }
-  free(zue); free(zve);
+  wfree(zue); wfree(zve);
   return NEMO_OK;
 }
 
@@ -2487,7 +2554,7 @@ int ora_dyn_keg(ora_ctx *c, int kt, int kscheme) {
         va[q] = va[q] - (zhke[p + jpi] - zhke[p]) / c->e2v[p];
       }
   }
-  free(zhke);
+  wfree(zhke);
   return NEMO_OK;
 }
 
@@ -2518,7 +2585,7 @@ int ora_dyn_zad(ora_ctx *c, int kt) {
         ua[q] = ua[q] - (zwuw[q] + zwuw[q + n2]) * c->r1_e1e2u[p] / e3u[q];
         va[q] = va[q] - (zwvw[q] + zwvw[q + n2]) * c->r1_e1e2v[p] / e3v[q];
       }
-  free(zww); free(zwuw); free(zwvw);
+  wfree(zww); wfree(zwuw); wfree(zwvw);
   return NEMO_OK;
 }
 
@@ -2559,7 +2626,7 @@ int ora_vor_ene(ora_ctx *c, int kt, int kvor, const double *pun, const double *p
         pva[q] = pva[q] - r1_4 * c->r1_e2v[p] * (zwz[I2(ji - 1, jj)] * zx1 + zwz[p] * zx2);
       }
   }
-  free(zwz); free(zwx); free(zwy);
+  wfree(zwz); wfree(zwx); wfree(zwy);
   return NEMO_OK;
 }
 
@@ -2597,7 +2664,7 @@ int ora_dyn_ldf_lap(ora_ctx *c, int kt, const double *pub, const double *pvb, do
                                    + (zdiv[I2(ji, jj + 1)] - zdiv[p]) * c->r1_e2v[p]);
       }
   }
-  free(zcur); free(zdiv);
+  wfree(zcur); wfree(zdiv);
   return NEMO_OK;
 }
 
@@ -2704,7 +2771,7 @@ int ora_dyn_hpg(ora_ctx *c, int kt) {
         ua[q] = ua[q] + zhpi[p];
         va[q] = va[q] + zhpj[p];
       }
-  free(zhpi); free(zhpj);
+  wfree(zhpi); wfree(zhpj);
   return NEMO_OK;
 }
 
@@ -2723,7 +2790,7 @@ int ora_stp_model(ora_ctx *c, int kt) {
     double *rab = zalloc(2 * n3);
     st = ora_rab_3d(c, c->f[NEMO_F_TSB], rab);
     if (!st) st = ora_bn2(c, c->f[NEMO_F_TSB], rab, c->f[NEMO_F_RN2B]);
-    free(rab);
+    wfree(rab);
     if (!st) st = ora_zdf_mxl(c, kt);
     if (!st) st = ora_eos_insitu(c, c->f[NEMO_F_TSB], c->f[NEMO_F_RHD], c->f[NEMO_F_GDEPT_N]);
     if (!st) st = ora_ldf_slp(c, kt, c->f[NEMO_F_RHD], c->f[NEMO_F_RN2B]);
@@ -2768,7 +2835,7 @@ int ora_ldf_slp(ora_ctx *c, int kt, const double *prd, const double *pn2) {
   const double *e3u = fld(c, NEMO_F_E3U_N), *e3v = fld(c, NEMO_F_E3V_N), *e3w = fld(c, NEMO_F_E3W_N);
   const double zeps = 1.e-20, z1_16 = 1.0 / 16., zm1_g = -1.0 / nm->grav, zm1_2g = -0.5 / nm->grav;
   const double z1_slpmax = 1. / (nm->rn_slpmax > 0 ? nm->rn_slpmax : 0.01);
-  double *zgru = walloc(n3), *zgrv = walloc(n3), *zdzr = walloc(n3);
+  double *zgru = zalloc(n3), *zgrv = zalloc(n3), *zdzr = zalloc(n3);
   double *zwz = zalloc(n3), *zww = zalloc(n3);
   double *uml = zalloc(n2), *vml = zalloc(n2), *wiml = zalloc(n2), *wjml = zalloc(n2);
   double *hu = zalloc(n2), *hv = zalloc(n2);
@@ -2925,7 +2992,7 @@ int ora_ldf_slp(ora_ctx *c, int kt, const double *prd, const double *pn2) {
   lbc_closed(jpi, jpj, uslp, jpk, 'U', 0.0); lbc_closed(jpi, jpj, vslp, jpk, 'V', 0.0);
   lbc_closed(jpi, jpj, wslpi, jpk, 'W', 0.0); lbc_closed(jpi, jpj, wslpj, jpk, 'W', 0.0);
 #undef OML
-  free(zgru); free(zgrv); free(zdzr); free(zwz); free(zww);
-  free(uml); free(vml); free(wiml); free(wjml); free(hu); free(hv);
+  wfree(zgru); wfree(zgrv); wfree(zdzr); wfree(zwz); wfree(zww);
+  wfree(uml); wfree(vml); wfree(wiml); wfree(wjml); wfree(hu); wfree(hv);
   return NEMO_OK;
 }

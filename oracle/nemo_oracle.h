@@ -31,6 +31,8 @@ int ora_create(const nemo_dom_desc *dom, const nemo_namelist *nam, ora_ctx **out
 int ora_destroy(ora_ctx *c);
 int ora_bind(ora_ctx *c, int field_id, double *host_ptr);
 int ora_spg_info(const ora_ctx *c, int *icycle, int *nn_baro, double *rdtbt);
+/* OpenMP threads of the parallel loops (n < 1: unchanged); returns the setting. */
+int ora_set_threads(int n);
 /* Derived domain arrays for inspection: name in tmask, umask, vmask, wmask (3-D),
  * ssmask, ssumask, ssvmask, tmask_i, ht_0, hu_0, hv_0, r1_hu_0, r1_hv_0, e1e2t,
  * r1_e1e2t (2-D), wgtbtp1, wgtbtp2 (3*nn_baro). Returns NULL for an unknown name. */

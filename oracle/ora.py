@@ -43,6 +43,7 @@ def lib():
         P("ora_glob_sum", [vp, vp, i, C.POINTER(d)])
         P("ora_stp_hotpath", [vp, i])
         P("ora_set_poison", [i], None)
+        P("ora_set_threads", [i])
         P("ora_set_fct_tape", [vp, vp, i])
         P("ora_tra_adv_fct_adj", [vp, i, i, cp, d, vp, vp, vp, vp, vp, vp, i, i, i])
         P("ora_tra_ldf_lap_adj", [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
@@ -75,6 +76,11 @@ def lib():
 def set_poison(on):
     """Start the oracle's automatic-array work buffers as NaN (1) or 0 (0)."""
     lib().ora_set_poison(int(on))
+
+
+def set_threads(n):
+    """OpenMP threads of the oracle's parallel loops (n < 1: unchanged); returns the setting."""
+    return lib().ora_set_threads(int(n))
 
 
 def _p(a):

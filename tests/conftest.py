@@ -19,3 +19,20 @@ def gyre1():
     dom = gyre.domain(1)
     nam = gyre.namelist()
     return dom, nam
+
+
+def pytest_sessionfinish(session, exitstatus):
+    """Write the pointwise parity statistics (tests/harness.py REPORT) to the JSON
+    file named by $NEMO_PARITY_REPORT, when that is set."""
+    path = os.environ.get("NEMO_PARITY_REPORT")
+    if not path:
+        return
+    try:
+        import json
+
+        from harness import REPORT
+    except Exception:
+        return
+    os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+    with open(path, "w") as f:
+        json.dump(REPORT, f, indent=1, sort_keys=True)

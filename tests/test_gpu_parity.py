@@ -424,6 +424,29 @@ def test_barrier_timeout_is_reported():
     p.ctx.synchronize()
 
 
+def test_tma_wait_timeout_is_reported():
+    """A TMA-staged tracer kernel whose waits on its tensor copies give up at once
+    (poll limit 0) records the failure, drains its copies and returns:
+    NEMO_ERR_TIMEOUT at the next synchronize, and the context stays usable."""
+    from nemo_gpu.api import NemoError
+    p = Pair(nn=3, prec="mixed", seed=23)
+    p.bind_hotpath()
+    p.ctx.set_tma_poll_limit(0)
+    p.ctx.stp_hotpath(5)
+    with pytest.raises(NemoError, match="tensor copy"):
+        p.ctx.synchronize()
+    p.ctx.set_tma_poll_limit(1 << 16)
+    p.ctx.stp_hotpath(6)  # the context steps again without error
+    p.ctx.synchronize()
+    # and a clean step in this process still matches the oracle
+    q = Pair(nn=3, prec="mixed", seed=23)
+    q.bind_hotpath()
+    q.ora[0].stp_hotpath(5)
+    q.ctx.stp_hotpath(5)
+    q.ctx.synchronize()
+    q.compare("TSA", q.s4, TOL32_FIELD)
+
+
 def test_gyre25_one_step_fp64():
     """One full hot-path step at the benchmark size (752 x 502 x 31) against the oracle."""
     p = Pair(nn=25, prec="fp64", seed=14)
