@@ -571,6 +571,12 @@ int nemo_gpu_set_tma(nemo_ctx *ctx, int on);
  * halos instead of storing them; on = 0 (default): three kernels. Same results. */
 int nemo_gpu_set_fct_fused(nemo_ctx *ctx, int on);
 
+/* The sub-step kernel of dyn_spg_ts in the mixed form with a linear free surface
+ * and the ENE/MIX vorticity scheme: on (default) the specialised kernel where the
+ * grid allows it, off the general one (both compute the same sub-steps; tests
+ * compare them). No counterpart in the reference. */
+int nemo_gpu_set_spg_specialised(nemo_ctx *ctx, int on);
+
 /* ------------------------------------------------------------ test hook */
 
 /* Bound of the grid barriers of the persistent sub-step kernel: each wait gives up

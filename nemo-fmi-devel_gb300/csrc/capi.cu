@@ -95,6 +95,8 @@ struct nemo_ctx {
   int bar_extra = 0;
   int p2_blocks = 0;
   int p2_cache = 0;  // the sub-step kernel keeps its constants in shared memory
+  int p2_hot = 0;    // the sub-step kernel is k_spg_p2_ene (mixed, linear free surface, ENE/MIX)
+  bool no_p2_hot = false;  // keep the general sub-step kernel (tests compare both)
   double* gs_part = nullptr;
   double* gs_out = nullptr;
   int gs_nblk = 0;
@@ -893,6 +895,7 @@ int run_spg(nemo_ctx* c, int kt) {
   a.du = (T*)c->spg_x[2]; a.dv = (T*)c->spg_x[3]; a.cu = (T*)c->spg_x[4]; a.cv = (T*)c->spg_x[5];
   a.zmu = (T*)c->spg_x[6]; a.zmv = (T*)c->spg_x[7];
   a.cache = c->p2_cache;
+  a.hot = c->p2_hot;
   a.ff = c->spg_ff;
   a.wgt1 = c->d_wgt1; a.wgt2 = c->d_wgt2; a.wgtf = c->d_wgtf; a.nwgt = (int)c->wgt1.size();
   a.ln_bt_fw = nm.ln_bt_fw; a.ln_apr_dyn = nm.ln_apr_dyn; a.nvor = nm.nvor_scheme; a.ll_init = ll_init;
@@ -1311,6 +1314,39 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
 // ================================================================== C ABI
 extern "C" {
 
+// The sub-step kernel and its grid: one block per 32 x 8 tile, at most all
+// co-resident. The mixed form with a linear free surface and the ENE/MIX scheme runs
+// k_spg_p2_ene when no block then owns more than P2H_MAXT tiles; otherwise
+// k_spg_p2, which keeps its constants in shared memory (ENE/MIX, mixed form) when no
+// block owns more than P2_MAXT tiles.
+void select_p2(nemo_ctx* c) {
+  const long need = (long)((c->jpi + 31) / 32) * ((c->jpj + 7) / 8) * c->nmem;
+  const int vvl = !c->nam.ln_linssh;
+  const int prec = c->prec;
+  auto p2_grid = [&](int cache) {
+    const int bps =
+        prec == NEMO_PREC_FP64 ? spg_p2_blocks_per_sm<double>(0, vvl) : spg_p2_blocks_per_sm<float>(cache, vvl);
+    const long maxb = (long)bps * c->nsm;
+    c->p2_blocks = (int)(need < maxb ? need : maxb);
+    c->p2_cache = cache;
+  };
+  const int nv = c->nam.nvor_scheme;
+  const bool ene = prec != NEMO_PREC_FP64 && !vvl && (nv == 1 || nv == 5);
+  c->p2_hot = 0;
+  if (ene && !c->no_p2_hot) {
+    const long maxb = (long)spg_p2_ene_blocks_per_sm<float>() * c->nsm;
+    if (maxb > 0 && need <= maxb * P2H_MAXT) {
+      c->p2_blocks = (int)(need < maxb ? need : maxb);
+      c->p2_cache = 1;
+      c->p2_hot = 1;
+    }
+  }
+  if (!c->p2_hot) {
+    p2_grid(ene ? 1 : 0);
+    if (c->p2_cache && (c->p2_blocks < 1 || need > (long)c->p2_blocks * P2_MAXT)) p2_grid(0);
+  }
+}
+
 int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmembers, int prec, void* stream,
                     nemo_ctx** out) {
   if (!out) return NEMO_ERR_ARG;
@@ -1376,7 +1412,8 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
     cudaMemset(c->spg_x[w], 0, bytes);
   }
   if (prec != NEMO_PREC_FP64) {
-    const size_t bytes = 10 * (size_t)c->nmem * c->n2 * sizeof(float);
+    // ten floats a point (k_spg_p2), or three float4 a point (k_spg_p2_ene)
+    const size_t bytes = 12 * (size_t)c->nmem * c->n2 * sizeof(float);
     if (cudaMalloc(&c->spg_ff, bytes) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
     cudaMemset(c->spg_ff, 0, bytes);
   }
@@ -1391,21 +1428,7 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
   if (cudaMalloc(&c->err_flag, sizeof(int)) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
   cudaMemset(c->bar_mem, 0, 2 * sizeof(unsigned int));
   cudaMemset(c->err_flag, 0, sizeof(int));
-  // one block per 32 x 8 tile of the sub-step kernel, at most all co-resident; the
-  // mixed form with the ENE/MIX scheme keeps its constants in shared memory when no
-  // block owns more than P2_MAXT tiles
-  const long need = (long)((c->jpi + 31) / 32) * ((c->jpj + 7) / 8) * c->nmem;
-  const int vvl = !nam->ln_linssh;
-  auto p2_grid = [&](int cache) {
-    const int bps =
-        prec == NEMO_PREC_FP64 ? spg_p2_blocks_per_sm<double>(0, vvl) : spg_p2_blocks_per_sm<float>(cache, vvl);
-    const long maxb = (long)bps * c->nsm;
-    c->p2_blocks = (int)(need < maxb ? need : maxb);
-    c->p2_cache = cache;
-  };
-  const int nv = c->nam.nvor_scheme;
-  p2_grid(prec != NEMO_PREC_FP64 && !vvl && (nv == 1 || nv == 5) ? 1 : 0);
-  if (c->p2_cache && (c->p2_blocks < 1 || need > (long)c->p2_blocks * P2_MAXT)) p2_grid(0);
+  select_p2(c);
   if (c->p2_blocks < 1) return bad(NEMO_ERR_CUDA);
   c->gs_nblk = c->nsm * 4;
   if (cudaMalloc(&c->gs_part, 2 * (size_t)c->gs_nblk * c->nmem * 8) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
@@ -2224,6 +2247,15 @@ int nemo_gpu_set_tma(nemo_ctx* c, int on) {
   for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);
   c->graphs.clear();
   return NEMO_OK;
+}
+
+int nemo_gpu_set_spg_specialised(nemo_ctx* c, int on) {
+  if (!c) return NEMO_ERR_ARG;
+  c->no_p2_hot = !on;
+  select_p2(c);
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);
+  c->graphs.clear();
+  return c->p2_blocks < 1 ? fail(c, NEMO_ERR_CUDA, "set_spg_specialised: no launch shape") : NEMO_OK;
 }
 
 int nemo_gpu_set_tma_poll_limit(nemo_ctx* c, int max_polls) {

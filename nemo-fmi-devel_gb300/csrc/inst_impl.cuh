@@ -247,6 +247,23 @@ int spg_p2_blocks_per_sm(int cache, int vvl) {
   return nb;
 }
 
+// co-resident blocks per SM of the specialised sub-step kernel (mixed form, linear
+// free surface, ENE/MIX), with its constant cache
+template <class T>
+int spg_p2_ene_blocks_per_sm() {
+  if constexpr (sizeof(T) != 4) {
+    return 0;
+  } else {
+    if (cudaFuncSetAttribute(k_spg_p2_ene<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)P2H_CACHE_BYTES) != cudaSuccess)
+      return 0;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_spg_p2_ene<T>, 256, P2H_CACHE_BYTES) != cudaSuccess)
+      return 0;
+    return nb;
+  }
+}
+
 template <class T>
 cudaError_t launch_spg(const Dom<T>& d, const SpgArgs<T>& a, const GridBar& bar, int p2_blocks, cudaStream_t s) {
   if (a.vvl) {  // Coriolis factors from the now depths (:241-343)
@@ -279,8 +296,19 @@ cudaError_t launch_spg(const Dom<T>& d, const SpgArgs<T>& a, const GridBar& bar,
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaError_t e = a.vvl ? cudaLaunchKernelEx(&cfg, k_spg_p2<T, true>, d, a, bar)
-                        : cudaLaunchKernelEx(&cfg, k_spg_p2<T, false>, d, a, bar);
+  cudaError_t e;
+  if constexpr (sizeof(T) == 4) {
+    if (a.hot) {
+      cfg.dynamicSmemBytes = P2H_CACHE_BYTES;
+      e = cudaLaunchKernelEx(&cfg, k_spg_p2_ene<T>, d, a, bar);
+    } else {
+      e = a.vvl ? cudaLaunchKernelEx(&cfg, k_spg_p2<T, true>, d, a, bar)
+                : cudaLaunchKernelEx(&cfg, k_spg_p2<T, false>, d, a, bar);
+    }
+  } else {
+    e = a.vvl ? cudaLaunchKernelEx(&cfg, k_spg_p2<T, true>, d, a, bar)
+              : cudaLaunchKernelEx(&cfg, k_spg_p2<T, false>, d, a, bar);
+  }
   if (e != cudaSuccess) return e;
   ktick(NEMO_K_SPG_P2, s);
   const int t3 = kty(NEMO_K_SPG_P3);
@@ -318,6 +346,7 @@ cudaError_t launch_globsum(const T* x, const double* tmask_i, long n2, int nk, i
   template cudaError_t launch_clamp<T>(T*, long, cudaStream_t);                                              \
   template cudaError_t launch_spg<T>(const Dom<T>&, const SpgArgs<T>&, const GridBar&, int, cudaStream_t);   \
   template int spg_p2_blocks_per_sm<T>(int, int);                                                                 \
+  template int spg_p2_ene_blocks_per_sm<T>();                                                                 \
   template cudaError_t launch_lbc<T>(T*, int, int, long, int, T, cudaStream_t);                              \
   template cudaError_t launch_globsum<T>(const T*, const double*, long, int, int, double*, int, double*, cudaStream_t);
 

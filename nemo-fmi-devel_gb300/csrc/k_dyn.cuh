@@ -41,6 +41,7 @@ struct SpgArgs {
   int nwgt;
   int ln_bt_fw, ln_apr_dyn, nvor, ll_init, icycle, ring0, phase3_filter;
   int cache;  // mixed form, ENE/MIX: the sub-step constants cached in shared memory
+  int hot;    // mixed form, linear free surface, ENE/MIX: k_spg_p2_ene instead of k_spg_p2
   // Column depths (2-D): for a linear free surface the rest-state ht_0, hu_0, ...
   // shared by all members (member stride hs = 0); with a variable volume the bound
   // now / before depths of each member (hs = points per member). The Coriolis
@@ -887,6 +888,259 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (VVL ? 3 : 4) : 2) k_spg
     }
     a.cu[g] = (T)(uadv * r1hu);
     a.cv[g] = (T)(vadv * r1hv);
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// The sub-steps of the mixed form for a linear free surface with the ENE or MIX
+// vorticity scheme (GYRE's configuration), specialised for a short critical path:
+// the sub-step time is set by the slowest block, i.e. by the tiles a block owns, so
+// this kernel keeps to <= 48 registers for 5 co-resident blocks per SM and owns at
+// most P2H_MAXT = 2 tiles a block (GYRE nn_GYRE=25: 1512 tiles on 760 blocks),
+// where the general kernel runs 4 blocks per SM with up to 3 tiles. Per point it
+// keeps in shared memory the constants of both stages (those of k_spg_p2's cache,
+// plus rdtbt * zssh_frc and rdtbt / e1e2t of the new ssh), and it packs the five
+// compensated sums of a point into three float4 (one 16-byte access each instead
+// of ten 4-byte ones). Same steps as k_spg_p2 (:712-1207): the east/north halo of
+// the new ssh recomputed by each block, one grid barrier per sub-step.
+constexpr int P2H_MAXT = 2;
+constexpr int P2H_NC = 18;
+constexpr size_t P2H_CACHE_BYTES = (size_t)P2H_NC * P2H_MAXT * 256 * sizeof(float);
+
+// the packed sums: plane 0 = {ssha hi, lo, ua_b hi, lo}, 1 = {va_b hi, lo, un_adv hi,
+// lo}, 2 = {vn_adv hi, lo, 0, 0}; plane q of point g at ff4[q * nmem2 + g]
+__device__ __forceinline__ void ff4_add_w(float& h, float& l, float wh, float wl, float x) {
+  FF s{h, l};
+  ff_add_w(s, wh, wl, x);
+  h = s.h;
+  l = s.l;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256, 5) k_spg_p2_ene(Dom<T> d, SpgArgs<T> a, GridBar bar) {
+  static_assert(sizeof(T) == 4, "the mixed form's kernel");
+  __shared__ float zs_s[P2_TY + 1][P2_TX + 1];
+  extern __shared__ float p2h[];
+  const int n2 = (int)d.n2, nmem2 = d.nmem * n2, jpi = d.jpi, jpj = d.jpj;
+  const int ntx = (jpi + P2_TX - 1) / P2_TX, nty = (jpj + P2_TY - 1) / P2_TY;
+  const int ntile = ntx * nty * d.nmem;
+  const int tx = threadIdx.x % P2_TX, ty = threadIdx.x / P2_TX;
+  const float rdtbt = a.rdtbt;
+  float4* const ff4 = reinterpret_cast<float4*>(a.ff);
+  constexpr int CS = P2H_MAXT * 256;  // stride of one constant in the cache
+  auto interior = [&](int i, int j) -> bool { return i >= 2 && i <= jpi - 1 && j >= 2 && j <= jpj - 1; };
+  auto tile = [&](int t, int& m2, int& i0, int& j0) {
+    const int m = t / (ntx * nty), tt = t - m * (ntx * nty);
+    m2 = m * n2;
+    i0 = (tt % ntx) * P2_TX + 1;
+    j0 = (tt / ntx) * P2_TY + 1;
+  };
+  int r = a.ring0;
+  // ---- the constants of the owned points, the predictor of sub-step 1 (:724-800)
+  // and the sums started with its un_adv / vn_adv terms (:860-862)
+  {
+    float za1, za2, za3;
+    ab3(1, a.ll_init, za1, za2, za3);
+    const int sn = r & 3, sb = (r + 1) & 3, sbb = (r + 2) & 3;
+    const float w2 = a.wgtf[2 * a.nwgt];
+    int slot = 0;
+    for (int t = blockIdx.x; t < ntile && slot < P2H_MAXT; t += gridDim.x, ++slot) {
+      int m2, i0, j0;
+      tile(t, m2, i0, j0);
+      const int i = i0 + tx, j = j0 + ty;
+      float cv[P2H_NC] = {};
+      if (i <= jpi && j <= jpj) {
+        const int p = (i - 1) + (j - 1) * jpi, g = m2 + p;
+        if (interior(i, j)) {
+          const float su = (1.0f - a.scal_load) * (-a.grav);
+          cv[0] = 0.25f * d.zwz[p - jpi] * d.r1_e1u[p];
+          cv[1] = 0.25f * d.zwz[p] * d.r1_e1u[p];
+          cv[2] = -0.25f * d.zwz[p - 1] * d.r1_e2v[p];
+          cv[3] = -0.25f * d.zwz[p] * d.r1_e2v[p];
+          cv[4] = a.zCdU_u[g] * d.r1_hu_0[p];
+          cv[5] = a.zCdU_v[g] * d.r1_hv_0[p];
+          cv[6] = su * d.r1_e1u[p];
+          cv[7] = su * d.r1_e2v[p];
+          cv[8] = a.zu_frc[g];
+          cv[9] = a.zv_frc[g];
+          cv[10] = d.ssumask[p];
+          cv[11] = d.ssvmask[p];
+          cv[16] = __fmul_rn(rdtbt, a.zssh_frc[g]);
+          cv[17] = __fmul_rn(rdtbt, d.r1_e1e2t[p]);
+        }
+        cv[12] = d.e2u[p] * d.hu_0[p];
+        cv[13] = d.e1v[p] * d.hv_0[p];
+        cv[14] = d.r1_e2u[p];
+        cv[15] = d.r1_e1v[p];
+        const float ua_e = za1 * a.ring_u[sn * nmem2 + g] + za2 * a.ring_u[sb * nmem2 + g] +
+                           za3 * a.ring_u[sbb * nmem2 + g];
+        const float va_e = za1 * a.ring_v[sn * nmem2 + g] + za2 * a.ring_v[sb * nmem2 + g] +
+                           za3 * a.ring_v[sbb * nmem2 + g];
+        const float zwx = d.e2u[p] * ua_e * d.hu_0[p];
+        const float zwy = d.e1v[p] * va_e * d.hv_0[p];
+        a.fx[nmem2 + g] = zwx;  // slot (1 & 1)
+        a.fy[nmem2 + g] = zwy;
+        ff4[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+        ff4[nmem2 + g] = make_float4(0.f, 0.f, w2 * zwx * d.r1_e2u[p], 0.f);
+        ff4[2 * nmem2 + g] = make_float4(w2 * zwy * d.r1_e1v[p], 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int cc = 0; cc < P2H_NC; ++cc) p2h[cc * CS + slot * 256 + threadIdx.x] = cv[cc];
+    }
+  }
+  // the halo position of this thread, if any: the east column (9) and the north row
+  // (32) of the tile
+  int hti = -1, htj = -1;
+  if (threadIdx.x < P2_TY + 1) { hti = P2_TX; htj = threadIdx.x; }
+  else if (threadIdx.x < P2_TY + 1 + P2_TX) { hti = threadIdx.x - (P2_TY + 1); htj = P2_TY; }
+  if (!grid_barrier(bar)) return;
+  for (int jn = 1; jn <= a.icycle; ++jn) {
+    const int sn = r & 3, sb = (r + 1) & 3, sbb = (r + 2) & 3, sa = (r + 3) & 3;
+    const float* fx = a.fx + (jn & 1) * nmem2;
+    const float* fy = a.fy + (jn & 1) * nmem2;
+    const float w1h = a.wgtf[jn - 1], w1l = a.wgtf[a.nwgt + jn - 1];
+    float zb0, zb1, zb2, zb3;
+    am4(jn, a.ll_init, a.rn_bt_alpha, zb0, zb1, zb2, zb3);
+    int slot = 0;
+    for (int t = blockIdx.x; t < ntile; t += gridDim.x, ++slot) {
+      int m2, i0, j0;
+      tile(t, m2, i0, j0);
+      const int i = i0 + tx, j = j0 + ty;
+      const bool own = i <= jpi && j <= jpj;
+      const bool inner = own && interior(i, j);
+      const int p = own ? (i - 1) + (j - 1) * jpi : 0, g = m2 + p;
+      const float* C = p2h + slot * 256 + threadIdx.x;
+      // the values of both stages first, so that their loads are in flight together;
+      // those of the sums and the predictor's before levels at the start of stage B
+      // (fewer registers live across the block barrier)
+      float x[4] = {}, y[4] = {};
+      float sn0 = 0.f, sb0 = 0.f, sbb0 = 0.f, un_e = 0.f, vn_e = 0.f;
+      float4 f0 = {};
+      if (own) {
+        sn0 = a.ring_ssh[sn * nmem2 + g];
+        sb0 = a.ring_ssh[sb * nmem2 + g];
+        sbb0 = a.ring_ssh[sbb * nmem2 + g];
+        un_e = a.ring_u[sn * nmem2 + g];
+        vn_e = a.ring_v[sn * nmem2 + g];
+        f0 = ff4[g];
+        if (inner) {
+          nbx([&](long q) { return fx[m2 + q]; }, (long)p, jpi, x);
+          nby([&](long q) { return fy[m2 + q]; }, (long)p, jpi, y);
+        }
+      }
+      const int hi_ = i0 + hti, hj_ = j0 + htj;
+      const bool halo = hti >= 0 && hi_ <= jpi && hj_ <= jpj;
+      // ---- ssha_e (:871-879) and zsshp2_e (:930-931) of the owned point and the halo
+      // the owner of a point and the blocks whose halo it is form its values with the
+      // same rounded operations (explicit intrinsics: no contraction choices)
+      auto ssha_of = [&](float s0, float frc, float div, float dv, float msk) {
+        return __fmul_rn(__fsub_rn(s0, __fmaf_rn(div, dv, frc)), msk);
+      };
+      auto zs_of = [&](float e, float s0, float s1, float s2) {
+        return __fmaf_rn(zb3, s2, __fmaf_rn(zb2, s1, __fmaf_rn(zb1, s0, __fmul_rn(zb0, e))));
+      };
+      if (own) {
+        float ssha_e = 0.f;
+        if (inner) {
+          const float dv = __fsub_rn(__fadd_rn(__fsub_rn(x[1], x[0]), y[2]), y[0]);
+          ssha_e = ssha_of(sn0, C[16 * CS], C[17 * CS], dv, d.ssmask[p]);
+        }
+        zs_s[ty][tx] = zs_of(ssha_e, sn0, sb0, sbb0);
+        a.ring_ssh[sa * nmem2 + g] = ssha_e;
+        ff4_add_w(f0.x, f0.y, w1h, w1l, ssha_e);
+      }
+      if (halo) {
+        const int hp = (hi_ - 1) + (hj_ - 1) * jpi, hg = m2 + hp;
+        const float h_sn = a.ring_ssh[sn * nmem2 + hg];
+        float ssha_e = 0.f;
+        if (interior(hi_, hj_)) {
+          const float dv = __fsub_rn(__fadd_rn(__fsub_rn(fx[hg], fx[hg - 1]), fy[hg]), fy[hg - jpi]);
+          ssha_e = ssha_of(h_sn, __fmul_rn(rdtbt, a.zssh_frc[hg]), __fmul_rn(rdtbt, d.r1_e1e2t[hp]), dv,
+                           d.ssmask[hp]);
+        }
+        zs_s[htj][hti] = zs_of(ssha_e, h_sn, a.ring_ssh[sb * nmem2 + hg], a.ring_ssh[sbb * nmem2 + hg]);
+      }
+      __syncthreads();
+      // ---- Coriolis, drag, pressure gradient, ua_e / va_e and their sums
+      // (:1000-1204), the predictor of sub-step jn+1 (:724-800) and its sums (:860-862)
+      if (own) {
+        float4 f1 = ff4[nmem2 + g];
+        const float ub_e = a.ring_u[sb * nmem2 + g], vb_e = a.ring_v[sb * nmem2 + g];
+        float ua_e = 0.f, va_e = 0.f;
+        if (inner) {
+          const float s0 = zs_s[ty][tx];
+          const float zu_trd = C[0] * (y[0] + y[1]) + C[CS] * (y[2] + y[3]) + C[4 * CS] * un_e;
+          const float zv_trd = C[2 * CS] * (x[0] + x[2]) + C[3 * CS] * (x[1] + x[3]) + C[5 * CS] * vn_e;
+          const float wxs = C[6 * CS] * (zs_s[ty][tx + 1] - s0);
+          const float wys = C[7 * CS] * (zs_s[ty + 1][tx] - s0);
+          ua_e = (un_e + rdtbt * (wxs + zu_trd + C[8 * CS])) * C[10 * CS];
+          va_e = (vn_e + rdtbt * (wys + zv_trd + C[9 * CS])) * C[11 * CS];
+        }
+        a.ring_u[sa * nmem2 + g] = ua_e;
+        a.ring_v[sa * nmem2 + g] = va_e;
+        ff4_add_w(f0.z, f0.w, w1h, w1l, ua_e);
+        ff4_add_w(f1.x, f1.y, w1h, w1l, va_e);
+        ff4[g] = f0;
+        if (jn < a.icycle) {
+          float2 f2 = reinterpret_cast<float2*>(ff4 + 2 * nmem2)[2 * g];
+          float za1, za2, za3;
+          ab3(jn + 1, a.ll_init, za1, za2, za3);
+          const float uex = za1 * ua_e + za2 * un_e + za3 * ub_e;
+          const float vex = za1 * va_e + za2 * vn_e + za3 * vb_e;
+          const float zwx = C[12 * CS] * uex;
+          const float zwy = C[13 * CS] * vex;
+          a.fx[((jn + 1) & 1) * nmem2 + g] = zwx;
+          a.fy[((jn + 1) & 1) * nmem2 + g] = zwy;
+          const float w2 = a.wgtf[2 * a.nwgt + jn];
+          FF s{f1.z, f1.w};
+          ff_add(s, w2 * zwx * C[14 * CS], 0.0f);
+          f1.z = s.h;
+          f1.w = s.l;
+          s = FF{f2.x, f2.y};
+          ff_add(s, w2 * zwy * C[15 * CS], 0.0f);
+          f2.x = s.h;
+          f2.y = s.l;
+          reinterpret_cast<float2*>(ff4 + 2 * nmem2)[2 * g] = f2;
+        }
+        ff4[nmem2 + g] = f1;
+      }
+      __syncthreads();  // zs_s is rewritten by the next tile
+    }
+    r = (r + 3) & 3;
+    if (!grid_barrier(bar)) return;
+  }
+  // ---- phase 3, per column (:1214-1240, :1266-1269): the sums into the FP64 fields,
+  // the time-filtered transports and the two depth-independent terms of each level
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nth = gridDim.x * blockDim.x;
+  for (int g = tid; g < nmem2; g += nth) {
+    const int p = g % n2;
+    const float4 f0 = ff4[g], f1 = ff4[nmem2 + g], f2 = ff4[2 * nmem2 + g];
+    a.ssha[g] = (double)f0.x + (double)f0.y;
+    const double uab = (double)f0.z + (double)f0.w, vab = (double)f1.x + (double)f1.y;
+    a.ua_b[g] = uab;
+    a.va_b[g] = vab;
+    double uadv = (double)f1.z + (double)f1.w, vadv = (double)f2.x + (double)f2.y;
+    if (a.ln_bt_fw) {
+      const double zwx = uadv, zwy = vadv;
+      if (a.phase3_filter) {
+        uadv = 0.5 * (a.ub2_b[g] + zwx - a.rn_atfp * a.un_bf[g]);
+        vadv = 0.5 * (a.vb2_b[g] + zwy - a.rn_atfp * a.vn_bf[g]);
+        a.un_bf[g] = a.rn_atfp * a.un_bf[g] + (zwx - a.ub2_b[g]);
+        a.vn_bf[g] = a.rn_atfp * a.vn_bf[g] + (zwy - a.vb2_b[g]);
+      } else {
+        a.un_bf[g] = 0.0;
+        a.vn_bf[g] = 0.0;
+      }
+      a.ub2_b[g] = zwx;
+      a.vb2_b[g] = zwy;
+    }
+    a.un_adv[g] = uadv;
+    a.vn_adv[g] = vadv;
+    a.du[g] = (float)((uab - (double)a.ub_b[g]) * a.r1_2dt_b);
+    a.dv[g] = (float)((vab - (double)a.vb_b[g]) * a.r1_2dt_b);
+    a.cu[g] = (float)(uadv * (double)d.r1_hu_0[p]);
+    a.cv[g] = (float)(vadv * (double)d.r1_hv_0[p]);
   }
 }
 

@@ -59,6 +59,8 @@ cudaError_t launch_spg(const Dom<T>& d, const SpgArgs<T>& a, const GridBar& bar,
 template <class T>
 int spg_p2_blocks_per_sm(int cache, int vvl);
 template <class T>
+int spg_p2_ene_blocks_per_sm();
+template <class T>
 cudaError_t launch_lbc(T* p, int jpi, int jpj, long nslab, int is_f, T pval, cudaStream_t s);
 template <class T>
 cudaError_t launch_globsum(const T* x, const double* tmask_i, long n2, int nk, int nmem, double* part, int nblk,

@@ -153,6 +153,7 @@ def load(path):
     _proto(lib, "nemo_gpu_set_fusion", i, [vp, i])
     _proto(lib, "nemo_gpu_set_tma", i, [vp, i])
     _proto(lib, "nemo_gpu_set_tma_poll_limit", i, [vp, i])
+    _proto(lib, "nemo_gpu_set_spg_specialised", i, [vp, i])
     _proto(lib, "nemo_gpu_set_fct_fused", i, [vp, i])
     _proto(lib, "nemo_gpu_get_timing", i, [vp, C.POINTER(d), C.POINTER(i)])
     _proto(lib, "nemo_gpu_get_kernel_timing", i, [vp, C.POINTER(d), C.POINTER(i), i])

@@ -129,6 +129,9 @@ class Context:
     def set_tma(self, on):
         self._ck(self.lib.nemo_gpu_set_tma(self.h, int(on)), "set_tma")
 
+    def set_spg_specialised(self, on):
+        self._ck(self.lib.nemo_gpu_set_spg_specialised(self.h, int(on)), "set_spg_specialised")
+
     def set_tma_poll_limit(self, max_polls):
         self._ck(self.lib.nemo_gpu_set_tma_poll_limit(self.h, int(max_polls)), "set_tma_poll_limit")
 

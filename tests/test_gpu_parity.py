@@ -424,6 +424,29 @@ def test_barrier_timeout_is_reported():
     p.ctx.synchronize()
 
 
+@pytest.mark.parametrize("case", [dict(), dict(nvor_scheme=5), dict(ln_bt_fw=0), dict(nn_bt_flt=2)])
+def test_spg_specialised_kernel(case):
+    """The mixed form's specialised sub-step kernel (linear free surface, ENE/MIX)
+    against the oracle and against the general kernel on the same inputs: both
+    within the mixed tolerance of the oracle, and within FP32 rounding of each
+    other (the constants are combined in another order, so they are not identical)."""
+    res = {}
+    for spec in (1, 0):
+        p = _spg_pair("mixed", case, nn=5)
+        p.ctx.set_spg_specialised(spec)
+        for kt in (5, 6):
+            for o in p.ora:
+                o.dyn_spg_ts(kt)
+            p.ctx.dyn_spg_ts(kt)
+            p.ctx.synchronize()
+        _spg_compare(p, "mixed")
+        res[spec] = {n: np.asarray(p.ctx.to_host(p.dev[n], p.s2)) for n in ACC_2D}
+        res[spec].update({n: np.asarray(p.ctx.to_host(p.dev[n], p.s3)) for n in ("UA", "VA", "UN", "VN")})
+    for n in res[1]:
+        assert relerr(res[0][n], res[1][n]) <= 2e-5, n
+    assert any(not np.array_equal(res[0][n], res[1][n]) for n in res[1])  # two different kernels ran
+
+
 def test_tma_wait_timeout_is_reported():
     """A TMA-staged tracer kernel whose waits on its tensor copies give up at once
     (poll limit 0) records the failure, drains its copies and returns:
