@@ -424,6 +424,12 @@ int build_dom(nemo_ctx* c, DomStore<T>& st) {
   if ((s = upload_e3(c, st, 2, &d.e3v_n))) return s;
   if ((s = upload_e3(c, st, 3, &d.e3w_n))) return s;
   if ((s = upload_e3(c, st, 4, &d.e3f_n))) return s;
+  for (int w : {0, 3}) {  // reciprocal profiles of e3t_0 and e3w_0
+    if (!c->e3_uniform[w]) continue;
+    std::vector<double> r(c->jpk);
+    for (int k = 0; k < c->jpk; ++k) r[k] = 1.0 / c->e3_0[w][(size_t)k * c->n2];
+    if ((s = upload(c, st, r, w == 0 ? &d.r1_e3t : &d.r1_e3w))) return s;
+  }
   return NEMO_OK;
 }
 
@@ -695,6 +701,7 @@ int run_fct(nemo_ctx* c, double p2dt, const void* pun, const void* pvn, const vo
     CK(cudaMemsetAsync(lim, 0, 3 * (size_t)kjpt * c->n3 * c->nmem * sizeof(T), c->stream), "FCT tape = 0");
   }
   a.p2dt = (T)p2dt;
+  a.r1_p2dt = (T)(1.0 / p2dt);
   a.pun = (const T*)pun; a.pvn = (const T*)pvn; a.pwn = (const T*)pwn; a.trp = trp;
   a.ptb = (const T*)ptb; a.ptn = (const T*)ptn; a.pta_in = (const T*)pta_in; a.pta = (T*)pta;
   a.zwi = (T*)c->fct_w[0]; a.ax = (T*)c->fct_w[1]; a.ay = (T*)c->fct_w[2]; a.az = (T*)c->fct_w[3];

@@ -63,11 +63,10 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 3) k_iso_flux_hot(Do
   }
   // per-column metrics
   const T e2_e1u = d.e2_e1u[ij], e1_e2v = d.e1_e2v[ij], e2u = d.e2u[ij], e1v = d.e1v[ij];
-  const T e2t = icol ? d.e2t[ij] : T(0), e1t = icol ? d.e1t[ij] : T(0), e1e2t = icol ? d.e1e2t[ij] : T(0);
+  const T e2t = icol ? d.e2t[ij] : T(0), e1t = icol ? d.e1t[ij] : T(0);
   const T aht = a.aht_c;
   const T* e3u = d.e3u_n.p.p;
   const T* e3v = d.e3v_n.p.p;
-  const T* e3w = d.e3w_n.p.p;
   const long m3 = (long)c.m * d.n3;
   const T* uslp = a.uslp.p + m3 + ij;
   const T* vslp = a.vslp.p + m3 + ij;
@@ -107,33 +106,34 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 3) k_iso_flux_hot(Do
         break;
       }
       // wmask of the three columns at k and k+1
-      const T wk = k == 1 ? t0 : t0m * t0, wk1 = t0 * t0p;
-      const T wke = k == 1 ? te_ : tem * te_, wk1e = te_ * tep;
-      const T wkn = k == 1 ? tn_ : tnm * tn_, wk1n = tn_ * tnp;
+      const T wk = k == 1 ? t0 : msel(t0, t0m), wk1 = msel(t0p, t0);
+      const T wke = k == 1 ? te_ : msel(te_, tem), wk1e = msel(tep, te_);
+      const T wkn = k == 1 ? tn_ : msel(tn_, tnm), wk1n = msel(tnp, tn_);
       // horizontal fluxes' coefficients (:255-276)
-      T pah = aht * u0;
+      T pah = msel(aht, u0);
       const T zabe1 = pah * e2_e1u * __ldg(e3u + k - 1);
-      const T zmsku_h = rcount(wke + wk1 + wk1e + wk);
+      const T zmsku_h = rcount4(wke, wk1, wk1e, wk);
       const T zcof1 = -pah * e2u * __ldg(uslp + q) * zmsku_h;
-      pah = aht * v0;
+      pah = msel(aht, v0);
       const T zabe2 = pah * e1_e2v * __ldg(e3v + k - 1);
-      const T zmskv_h = rcount(wkn + wk1 + wk1n + wk);
+      const T zmskv_h = rcount4(wkn, wk1, wk1n, wk);
       const T zcof2 = -pah * e1v * __ldg(vslp + q) * zmskv_h;
-      // vertical flux coefficients and ah_wslp2 = akz (:146-164, :200-201, :291-321)
+      // vertical flux coefficients and ah_wslp2 = akz (:146-164, :200-201, :291-321).
+      // The term (ah_wslp2 - akz) * dk(tb) of :323-332 is an exact 0 here (akz =
+      // ah_wslp2) and adding it changes no value, so it is left out.
       const bool vface = icol && k >= 2;
-      T zcoef3 = T(0), zcoef4 = T(0), zvert = T(0);
+      T zcoef3 = T(0), zcoef4 = T(0);
       if (vface) {
-        const T zmsku = wk * rcount(u0m + uw + uwm + u0);
-        const T zmskv = wk * rcount(v0m + vs + vsm + v0);
-        const T zahu_w = (aht * u0m + aht * uw + aht * uwm + aht * u0) * zmsku;
-        const T zahv_w = (aht * v0m + aht * vs + aht * vsm + aht * v0) * zmskv;
+        const T zmsku = msel(rcount4(u0m, uw, uwm, u0), wk);
+        const T zmskv = msel(rcount4(v0m, vs, vsm, v0), wk);
+        const T zahu_w = (msel(aht, u0m) + msel(aht, uw) + msel(aht, uwm) + msel(aht, u0)) * zmsku;
+        const T zahv_w = (msel(aht, v0m) + msel(aht, vs) + msel(aht, vsm) + msel(aht, v0)) * zmskv;
         const T wi = __ldg(wslpi + q), wj = __ldg(wslpj + q);
         const T ahw = zahu_w * wi * wi + zahv_w * wj * wj;
         ahw_out[q] = ahw;
         akz_out[q] = ahw;
         zcoef3 = -zahu_w * e2t * zmsku * wi;
         zcoef4 = -zahv_w * e1t * zmskv * wj;
-        zvert = e1e2t / __ldg(e3w + k - 1) * wk * (ahw - ahw);
       }
 #pragma unroll
       for (int nn = 0; nn < NT; ++nn) {
@@ -144,40 +144,39 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 3) k_iso_flux_hot(Do
           if (k > 1) {
             const int qm = q - n2;
             const T a0 = __ldg(t + qm), ae = __ldg(t + qm + 1), an = __ldg(t + qm + jpi);
-            k10[nn] = (a0 - t0c[nn]) * wk;
-            k1e[nn] = (ae - tec[nn]) * wke;
-            k1n[nn] = (an - tnc[nn]) * wkn;
+            k10[nn] = msel(a0 - t0c[nn], wk);
+            k1e[nn] = msel(ae - tec[nn], wke);
+            k1n[nn] = msel(an - tnc[nn], wkn);
             tup[nn] = a0;
             if (icol) {
               const T aw = __ldg(t + qm - 1), as = __ldg(t + qm - jpi);
-              di0[nn] = (ae - a0) * u0m;
-              diw[nn] = (a0 - aw) * uwm;
-              dj0[nn] = (an - a0) * v0m;
-              djs[nn] = (a0 - as) * vsm;
+              di0[nn] = msel(ae - a0, u0m);
+              diw[nn] = msel(a0 - aw, uwm);
+              dj0[nn] = msel(an - a0, v0m);
+              djs[nn] = msel(a0 - as, vsm);
             }
           }
         }
         const T tc = t0c[nn], te = tec[nn], tn = tnc[nn];
         const T t1 = __ldg(t + q + n2), te1 = __ldg(t + q + 1 + n2), tn1 = __ldg(t + q + jpi + n2);
         // vertical gradients (:250-254)
-        const T dk1_0 = (tc - t1) * wk1, dk1_e = (te - te1) * wk1e, dk1_n = (tn - tn1) * wk1n;
+        const T dk1_0 = msel(tc - t1, wk1), dk1_e = msel(te - te1, wk1e), dk1_n = msel(tn - tn1, wk1n);
         const T dk0_0 = k == 1 ? dk1_0 : k10[nn];
         const T dk0_e = k == 1 ? dk1_e : k1e[nn];
         const T dk0_n = k == 1 ? dk1_n : k1n[nn];
-        const T zdi = (te - tc) * u0;
-        const T zdj = (tn - tc) * v0;
-        fu[nn][q] = (zabe1 * zdi + zcof1 * (dk0_e + dk1_0 + dk1_e + dk0_0)) * u0;
-        fv[nn][q] = (zabe2 * zdj + zcof2 * (dk0_n + dk1_0 + dk1_n + dk0_0)) * v0;
+        const T zdi = msel(te - tc, u0);
+        const T zdj = msel(tn - tc, v0);
+        fu[nn][q] = msel(zabe1 * zdi + zcof1 * (dk0_e + dk1_0 + dk1_e + dk0_0), u0);
+        fv[nn][q] = msel(zabe2 * zdj + zcof2 * (dk0_n + dk1_0 + dk1_n + dk0_0), v0);
         if (icol) {
           const T tw = __ldg(t + q - 1), ts = __ldg(t + q - jpi);
-          const T zdiw = (tc - tw) * uw;
-          const T zdjs = (tc - ts) * vs;
+          const T zdiw = msel(tc - tw, uw);
+          const T zdjs = msel(tc - ts, vs);
           T z = T(0);
           if (vface) {
             const T sdi = di0[nn] + zdiw + diw[nn] + zdi;
             const T sdj = dj0[nn] + zdjs + djs[nn] + zdj;
             z = zcoef3 * sdi + zcoef4 * sdj;
-            z = z + zvert * (tup[nn] - tc);
           }
           fw[nn][q] = z;
           di0[nn] = zdi; diw[nn] = zdiw; dj0[nn] = zdj; djs[nn] = zdjs;
@@ -267,7 +266,8 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 3) k_fct_a_hot(Dom<T
       if (first) wt = e1e2t * __ldg(wn + q);
       const T wb = (k + 1 <= jpk - 1) ? e1e2t * __ldg(wn + q + n2) : T(0);
       const T e3n = __ldg(e3tn + k - 1), e3b = __ldg(e3tb + k - 1), e3a = __ldg(e3ta + k - 1);
-      const T tm = tk, wk = k == 1 ? tk : tkm * tk, wk1 = tk * tkp;
+      const T r1n = d.r1_e3t[k - 1];  // e3t_n, e3t_b and e3t_a are the one rest-state profile here
+      const T tm = tk, wk = k == 1 ? tk : msel(tk, tkm), wk1 = msel(tkp, tk);
 #pragma unroll
       for (int nn = 0; nn < NT; ++nn) {
         if (nn >= nt) break;
@@ -278,21 +278,21 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 3) k_fct_a_hot(Dom<T
         if (first && k > 1) {  // the carried values of level k-1
           tbc[nn] = __ldg(tb + q - n2);
           tnc[nn] = __ldg(tn + q - n2);
-          zwzb[nn] = ups(wt, tb0, tbc[nn]) * wk;
+          zwzb[nn] = msel(ups(wt, tb0, tbc[nn]), wk);
         }
         const T zwx_e = ups(ue, tb0, __ldg(tb + q + 1)), zwx_w = ups(uw, __ldg(tb + q - 1), tb0);
         const T zwy_n = ups(vn_, tb0, __ldg(tb + q + jpi)), zwy_s = ups(vs, __ldg(tb + q - jpi), tb0);
         // upstream vertical fluxes at the top (k) and bottom (k+1) faces (:137-156)
         const T zwz_t = (k == 1) ? (a.linssh ? wt * tb0 : T(0)) : zwzb[nn];
-        const T zwz_b = (k + 1 <= jpk - 1) ? ups(wb, __ldg(tb + q + n2), tb0) * wk1 : T(0);
+        const T zwz_b = (k + 1 <= jpk - 1) ? msel(ups(wb, __ldg(tb + q + n2), tb0), wk1) : T(0);
         const T ztra = -(zwx_e - zwx_w + zwy_n - zwy_s + zwz_t - zwz_b) * r1_e1e2t;
-        ta[o + q] = T(0) + ztra / e3n * tm;
-        zwi[o + q] = (e3b * tb0 + p2dt * ztra) / e3a * tm;
+        ta[o + q] = T(0) + msel(divq(ztra, e3n, r1n), tm);
+        zwi[o + q] = msel(divq(e3b * tb0 + p2dt * ztra, e3a, r1n), tm);
         // 2nd-order antidiffusive fluxes (:180-190, :255-263)
         const T tn0 = __ldg(tn + q), tne = __ldg(tn + q + 1), tnn = __ldg(tn + q + jpi);
         ax[o + q] = T(0.5) * ue * (tn0 + tne) - zwx_e;
         ay[o + q] = T(0.5) * vn_ * (tn0 + tnn) - zwy_n;
-        az[o + q] = k >= 2 ? (wt * T(0.5) * (tn0 + tnc[nn]) - zwz_t) * wk : T(0);
+        az[o + q] = k >= 2 ? msel(wt * T(0.5) * (tn0 + tnc[nn]) - zwz_t, wk) : T(0);
         tbc[nn] = tb0;
         tnc[nn] = tn0;
         zwzb[nn] = zwz_b;
@@ -349,7 +349,7 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 4) k_fct_b_hot(Dom<T
       }
       const bool first = k == k0;
       const int qp = q + n2;
-      const T zbt = e1e2t * __ldg(e3tn + k - 1) / a.p2dt;
+      const T zbt = divq(e1e2t * __ldg(e3tn + k - 1), a.p2dt, a.r1_p2dt);
       const T tw = t_in<T>(ciw, k), te = t_in<T>(cie, k), ts = t_in<T>(cis, k), tn = t_in<T>(cin, k);
 #pragma unroll
       for (int nn = 0; nn < NT; ++nn) {
@@ -372,16 +372,16 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 4) k_fct_b_hot(Dom<T
         bupdo(__ldg(tb + qp), zwp, tkp, upp, dnp);
         // the reference's order: centre, west, east, south, north, above, below
         T up = up0[nn], dn = dn0[nn], u2, d2;
-        bupdo(__ldg(tb + q - 1), __ldg(zwi + q - 1), tw, u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-        bupdo(__ldg(tb + q + 1), __ldg(zwi + q + 1), te, u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-        bupdo(__ldg(tb + q - jpi), __ldg(zwi + q - jpi), ts, u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-        bupdo(__ldg(tb + q + jpi), __ldg(zwi + q + jpi), tn, u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-        up = fmx(up, upm[nn]); dn = fmn(dn, dnm[nn]);
-        up = fmx(up, upp); dn = fmn(dn, dnp);
+        bupdo(__ldg(tb + q - 1), __ldg(zwi + q - 1), tw, u2, d2); up = vmax(up, u2); dn = vmin(dn, d2);
+        bupdo(__ldg(tb + q + 1), __ldg(zwi + q + 1), te, u2, d2); up = vmax(up, u2); dn = vmin(dn, d2);
+        bupdo(__ldg(tb + q - jpi), __ldg(zwi + q - jpi), ts, u2, d2); up = vmax(up, u2); dn = vmin(dn, d2);
+        bupdo(__ldg(tb + q + jpi), __ldg(zwi + q + jpi), tn, u2, d2); up = vmax(up, u2); dn = vmin(dn, d2);
+        up = vmax(up, upm[nn]); dn = vmin(dn, dnm[nn]);
+        up = vmax(up, upp); dn = vmin(dn, dnp);
         const T axw = __ldg(ax + q - 1), ax0 = __ldg(ax + q), ays = __ldg(ay + q - jpi), ay0 = __ldg(ay + q);
         const T az0 = azk[nn], azb = __ldg(az + qp);
-        const T zpos = fmx(T(0), axw) - fmn(T(0), ax0) + fmx(T(0), ays) - fmn(T(0), ay0) + fmx(T(0), azb) - fmn(T(0), az0);
-        const T zneg = fmx(T(0), ax0) - fmn(T(0), axw) + fmx(T(0), ay0) - fmn(T(0), ays) + fmx(T(0), az0) - fmn(T(0), azb);
+        const T zpos = pos_part(axw) - neg_part(ax0) + pos_part(ays) - neg_part(ay0) + pos_part(azb) - neg_part(az0);
+        const T zneg = pos_part(ax0) - neg_part(axw) + pos_part(ay0) - neg_part(ays) + pos_part(az0) - neg_part(azb);
         const T zw = zwik[nn];
         bu[o + q] = (up - zw) / (zpos + zrtrn) * zbt;
         bd[o + q] = (zw - dn) / (zneg + zrtrn) * zbt;
@@ -450,10 +450,11 @@ __global__ void __launch_bounds__(128) k_fct_c_hot(Dom<T> d, FctArgs<T> a) {
       const T ayl = limit(ay0, bd0, bun, bu0, bdn);
       const T ayls = s_lim ? limit(ays, bds, bu0, bus, bd0) : T(0);
       const T azl_b = limit(azp, bdp, bu0, bup, bd0);
-      T tav = ta0 - (axl - axlw + ayl - ayls + azt - azl_b) * r1_e1e2t / e3n;
+      const T r1n = d.r1_e3t[k - 1];
+      T tav = ta0 - divq((axl - axlw + ayl - ayls + azt - azl_b) * r1_e1e2t, e3n, r1n);
       if (iso) {
-        tav = tav + zsign * (fu0 - fuw + fv0 - fvs) * r1_e1e2t / e3n;
-        tav = tav + zsign * (fwt - fwb) * r1_e1e2t / e3n;
+        tav = tav + divq(zsign * (fu0 - fuw + fv0 - fvs) * r1_e1e2t, e3n, r1n);
+        tav = tav + divq(zsign * (fwt - fwb) * r1_e1e2t, e3n, r1n);
         fwt = fwb;
       }
       ta[q] = tav;

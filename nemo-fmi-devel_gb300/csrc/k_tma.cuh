@@ -568,16 +568,16 @@ __global__ void __launch_bounds__(TM_X * TM_Y, 2)
             bupdo(Qp[b], zp[r2], mp[r2], upp, dnp);
             // the reference's order: centre, west, east, south, north, above, below
             T up = up0, dn = dn0;
-            bupdo(Q0[b - 1], z0[r2 - 1], m0[r2 - 1], u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-            bupdo(Q0[b + 1], z0[r2 + 1], m0[r2 + 1], u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-            bupdo(Q0[b - FF_BW], z0[r2 - R2W], m0[r2 - R2W], u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-            bupdo(Q0[b + FF_BW], z0[r2 + R2W], m0[r2 + R2W], u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-            up = fmx(up, upm); dn = fmn(dn, dnm);
-            up = fmx(up, upp); dn = fmn(dn, dnp);
+            bupdo(Q0[b - 1], z0[r2 - 1], m0[r2 - 1], u2, d2); up = vmax(up, u2); dn = vmin(dn, d2);
+            bupdo(Q0[b + 1], z0[r2 + 1], m0[r2 + 1], u2, d2); up = vmax(up, u2); dn = vmin(dn, d2);
+            bupdo(Q0[b - FF_BW], z0[r2 - R2W], m0[r2 - R2W], u2, d2); up = vmax(up, u2); dn = vmin(dn, d2);
+            bupdo(Q0[b + FF_BW], z0[r2 + R2W], m0[r2 + R2W], u2, d2); up = vmax(up, u2); dn = vmin(dn, d2);
+            up = vmax(up, upm); dn = vmin(dn, dnm);
+            up = vmax(up, upp); dn = vmin(dn, dnp);
             const T axw = x0[r2 - 1], ax0 = x0[r2], ays_ = y0[r2 - R2W], ay0 = y0[r2];
             const T az0 = a0[r2], azb = ap[r2];
-            const T zpos = fmx(T(0), axw) - fmn(T(0), ax0) + fmx(T(0), ays_) - fmn(T(0), ay0) + fmx(T(0), azb) - fmn(T(0), az0);
-            const T zneg = fmx(T(0), ax0) - fmn(T(0), axw) + fmx(T(0), ay0) - fmn(T(0), ays_) + fmx(T(0), az0) - fmn(T(0), azb);
+            const T zpos = pos_part(axw) - neg_part(ax0) + pos_part(ays_) - neg_part(ay0) + pos_part(azb) - neg_part(az0);
+            const T zneg = pos_part(ax0) - neg_part(axw) + pos_part(ay0) - neg_part(ays_) + pos_part(az0) - neg_part(azb);
             const T zw = z0[r2];
             bu = (up - zw) / (zpos + zrtrn) * zbt;
             bd = (zw - dn) / (zneg + zrtrn) * zbt;
@@ -891,16 +891,16 @@ __global__ void __launch_bounds__(TM_X * TM_Y, 3)
         bupdo(L1(nn)[o], zwp, tkp, upp, dnp);
         // the reference's order: centre, west, east, south, north, above, below
         T up = up0[nn], dn = dn0[nn], u2, d2;
-        bupdo(TB[o - 1], ZW[o - 1], tw, u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-        bupdo(TB[o + 1], ZW[o + 1], te, u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-        bupdo(TB[o - TM_W], ZW[o - TM_W], ts, u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-        bupdo(TB[o + TM_W], ZW[o + TM_W], tn, u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-        up = fmx(up, upm[nn]); dn = fmn(dn, dnm[nn]);
-        up = fmx(up, upp); dn = fmn(dn, dnp);
+        bupdo(TB[o - 1], ZW[o - 1], tw, u2, d2); up = vmax(up, u2); dn = vmin(dn, d2);
+        bupdo(TB[o + 1], ZW[o + 1], te, u2, d2); up = vmax(up, u2); dn = vmin(dn, d2);
+        bupdo(TB[o - TM_W], ZW[o - TM_W], ts, u2, d2); up = vmax(up, u2); dn = vmin(dn, d2);
+        bupdo(TB[o + TM_W], ZW[o + TM_W], tn, u2, d2); up = vmax(up, u2); dn = vmin(dn, d2);
+        up = vmax(up, upm[nn]); dn = vmin(dn, dnm[nn]);
+        up = vmax(up, upp); dn = vmin(dn, dnp);
         const T axw = AX[o - 1], ax0 = AX[o], ays = AY[o - TM_W], ay0 = AY[o];
         const T az0 = azk[nn], azb = L1(8 + nn)[o];
-        const T zpos = fmx(T(0), axw) - fmn(T(0), ax0) + fmx(T(0), ays) - fmn(T(0), ay0) + fmx(T(0), azb) - fmn(T(0), az0);
-        const T zneg = fmx(T(0), ax0) - fmn(T(0), axw) + fmx(T(0), ay0) - fmn(T(0), ays) + fmx(T(0), az0) - fmn(T(0), azb);
+        const T zpos = pos_part(axw) - neg_part(ax0) + pos_part(ays) - neg_part(ay0) + pos_part(azb) - neg_part(az0);
+        const T zneg = pos_part(ax0) - neg_part(axw) + pos_part(ay0) - neg_part(ays) + pos_part(az0) - neg_part(azb);
         const T zw = zwik[nn];
         bu[on + q] = (up - zw) / (zpos + zrtrn) * zbt;
         bd[on + q] = (zw - dn) / (zneg + zrtrn) * zbt;

@@ -133,6 +133,7 @@ struct LdfArgs {
 template <class T>
 struct FctArgs {
   T p2dt;
+  T r1_p2dt;                 // 1 / p2dt, correctly rounded
   RO<T> pun, pvn, pwn;       // transports, or velocities when trp != 0
   int trp;                   // 1: scale velocities to transports on the fly (traadv.F90:110-114)
   RO<T> ptb, ptn;            // (jpi,jpj,jpk,kjpt)
@@ -168,11 +169,76 @@ __device__ __forceinline__ T trp_w(const Dom<T>& d, const FctArgs<T>& a, long ij
   T w = a.pwn[q];
   return a.trp ? d.e1e2t[ij] * w : w;
 }
+// ---- value-exact helpers of the FCT and iso-neutral kernels. FP64 runs at 1/64 of
+// the FP32 rate on this GPU, and compares, min/max and products by 0/1 masks all
+// occupy that pipe; these forms move them to the integer pipe or drop them while
+// giving the reference's values (at most the sign of a zero differs, which no later
+// operation of these routines can see: zeros are added, multiplied or compared
+// with SIGN of key_nosignedzero).
+
+// the sign bit of x is clear (x > 0 or x = +0; -0 counts as negative)
+template <class T>
+__device__ __forceinline__ bool sgn_pos(T x) {
+  if constexpr (sizeof(T) == 8) return __double2hiint(x) >= 0;
+  else return __float_as_int(x) >= 0;
+}
+// integer with the order of the FP64 values (-0 just below +0)
+__device__ __forceinline__ long long ord_key(double x) {
+  const long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+// MAX / MIN of two values: FP64 through the integer order of the values, FP32 by
+// the min/max instruction
+template <class T>
+__device__ __forceinline__ T vmax(T a, T b) {
+  if constexpr (sizeof(T) == 8) return ord_key(a) > ord_key(b) ? a : b;
+  else return fmaxf(a, b);
+}
+template <class T>
+__device__ __forceinline__ T vmin(T a, T b) {
+  if constexpr (sizeof(T) == 8) return ord_key(a) < ord_key(b) ? a : b;
+  else return fminf(a, b);
+}
+// MAX(0, x) and MIN(0, x)
+template <class T>
+__device__ __forceinline__ T pos_part(T x) { return sgn_pos(x) ? x : T(0); }
+template <class T>
+__device__ __forceinline__ T neg_part(T x) { return sgn_pos(x) ? T(0) : x; }
+// x * m for a 0/1 mask m: FP64 selects (no product), FP32 keeps the product
+template <class T>
+__device__ __forceinline__ T msel(T x, T m) {
+  if constexpr (sizeof(T) == 8) return __double2hiint(m) != 0 ? x : T(0);
+  else return x * m;
+}
+// x / y given ry = 1 / y correctly rounded. FP64: Markstein's final correction
+// (P. Markstein, IBM J. Res. Dev. 34, 1990): with q0 = x * ry the remainder
+// e = x - q0 * y is exact as one fused multiply-add and q0 + e * ry rounds to the
+// correctly rounded quotient, i.e. the reference's x / y, in three FP64 operations
+// instead of a division. FP32: the division itself.
+template <class T>
+__device__ __forceinline__ T divq(T x, T y, T ry) {
+  if constexpr (sizeof(T) == 8) {
+    const double q0 = __dmul_rn(x, ry);
+    return __fma_rn(__fma_rn(-q0, y, x), ry, q0);
+  } else {
+    (void)ry;
+    return x / y;
+  }
+}
+
+// Upstream flux 0.5 * ((u + |u|) * tl + (u - |u|) * tr) (traadv_fct.F90:126-136):
+// exactly u * tl for u > 0 and u * tr for u < 0 (the doubled product scales exactly
+// and the other term is an exact 0), formed as one product of the selected value.
+// The product is rounded on its own (no contraction into the sum that follows), so
+// every kernel that forms this flux gets the same value.
+template <class T>
+__device__ __forceinline__ T rmul(T a, T b) {
+  if constexpr (sizeof(T) == 8) return __dmul_rn(a, b);
+  else return __fmul_rn(a, b);
+}
 template <class T>
 __device__ __forceinline__ T ups(T u, T tl, T tr) {
-  T zfp = u + fabs(u);
-  T zfm = u - fabs(u);
-  return T(0.5) * (zfp * tl + zfm * tr);
+  return rmul(u, sgn_pos(u) ? tl : tr);
 }
 
 // FCT stage a: upstream trend into pta, monotone guess zwi, antidiffusive fluxes
@@ -302,8 +368,11 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 3) k_fct_a(Dom<T> d,
 template <class T>
 __device__ __forceinline__ void bupdo(T pbef, T paft, T tm, T& up, T& dn) {
   const T zbig = Big<T>::v;
-  up = tm != T(0) ? fmx(pbef, paft) : -zbig;
-  dn = tm != T(0) ? fmn(pbef, paft) : zbig;
+  bool wet;
+  if constexpr (sizeof(T) == 8) wet = __double2hiint(tm) != 0;  // tm is 0 or 1
+  else wet = tm != T(0);
+  up = wet ? vmax(pbef, paft) : -zbig;
+  dn = wet ? vmin(pbef, paft) : zbig;
 }
 // FCT stage b: nonosc extrema and limiter coefficients zbetup / zbetdo
 // (traadv_fct.F90:366-400), edge values 0 (lbc_lnk of :400). k-march: tb, zwi and
@@ -367,15 +436,15 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 4) k_fct_b(Dom<T> d,
         bupdo(tb[qp], zwi[qp], tmsk<T>(ci, k + 1), upp, dnp);
         // the reference's order: centre, west, east, south, north, above, below
         T up = up0[nn], dn = dn0[nn], u2, d2;
-        bupdo(tb[q - 1], zwi[q - 1], tmsk<T>(ciw, k), u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-        bupdo(tb[q + 1], zwi[q + 1], tmsk<T>(cie, k), u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-        bupdo(tb[q - jpi], zwi[q - jpi], tmsk<T>(cis, k), u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-        bupdo(tb[q + jpi], zwi[q + jpi], tmsk<T>(cin, k), u2, d2); up = fmx(up, u2); dn = fmn(dn, d2);
-        up = fmx(up, upm[nn]); dn = fmn(dn, dnm[nn]);
-        up = fmx(up, upp); dn = fmn(dn, dnp);
+        bupdo(tb[q - 1], zwi[q - 1], tmsk<T>(ciw, k), u2, d2); up = vmax(up, u2); dn = vmin(dn, d2);
+        bupdo(tb[q + 1], zwi[q + 1], tmsk<T>(cie, k), u2, d2); up = vmax(up, u2); dn = vmin(dn, d2);
+        bupdo(tb[q - jpi], zwi[q - jpi], tmsk<T>(cis, k), u2, d2); up = vmax(up, u2); dn = vmin(dn, d2);
+        bupdo(tb[q + jpi], zwi[q + jpi], tmsk<T>(cin, k), u2, d2); up = vmax(up, u2); dn = vmin(dn, d2);
+        up = vmax(up, upm[nn]); dn = vmin(dn, dnm[nn]);
+        up = vmax(up, upp); dn = vmin(dn, dnp);
         const T axw = ax[q - 1], ax0 = ax[q], ays = ay[q - jpi], ay0 = ay[q], az0 = azk[nn], azb = az[qp];
-        const T zpos = fmx(T(0), axw) - fmn(T(0), ax0) + fmx(T(0), ays) - fmn(T(0), ay0) + fmx(T(0), azb) - fmn(T(0), az0);
-        const T zneg = fmx(T(0), ax0) - fmn(T(0), axw) + fmx(T(0), ay0) - fmn(T(0), ays) + fmx(T(0), az0) - fmn(T(0), azb);
+        const T zpos = pos_part(axw) - neg_part(ax0) + pos_part(ays) - neg_part(ay0) + pos_part(azb) - neg_part(az0);
+        const T zneg = pos_part(ax0) - neg_part(axw) + pos_part(ay0) - neg_part(ays) + pos_part(az0) - neg_part(azb);
         const T zw = zwik[nn];
         a.betup[mo + q] = (up - zw) / (zpos + zrtrn) * zbt;
         a.betdo[mo + q] = (zw - dn) / (zneg + zrtrn) * zbt;
@@ -389,17 +458,17 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 4) k_fct_b(Dom<T> d,
 }
 
 // Limiter multiplier of an antidiffusive flux f (traadv_fct.F90:407-422): c*a + (1-c)*b.
+// With zc = 0.5 + SIGN(0.5, f) in {0, 1} the sum is exactly a where f >= 0 and b
+// where f < 0 (products by 1 and 0 are exact), so the operands are selected first.
 template <class T>
 __device__ __forceinline__ T limit_mult(T f, T bdo0, T bup1, T bup0, T bdo1) {
-  const T za = fmn(T(1), fmn(bdo0, bup1));
-  const T zb = fmn(T(1), fmn(bup0, bdo1));
-  const T zc = (T(0.5) + sign_nsz(T(0.5), f));
-  return zc * za + (T(1) - zc) * zb;
+  const bool p = sgn_pos(f);
+  return vmin(T(1), vmin(p ? bdo0 : bup0, p ? bup1 : bdo1));
 }
 // Limited antidiffusive flux: f * ( c*a + (1-c)*b ).
 template <class T>
 __device__ __forceinline__ T limit(T f, T bdo0, T bup1, T bup0, T bdo1) {
-  return f * limit_mult(f, bdo0, bup1, bup0, bdo1);
+  return rmul(f, limit_mult(f, bdo0, bup1, bup0, bdo1));
 }
 
 // interp_4th_cpt (traadv_fct.F90:517-616): compact 4th-order tn at w-points for the

@@ -74,6 +74,9 @@ struct Dom {
   E3<T> e3t_b, e3t_n, e3t_a, e3u_n, e3v_n, e3w_n;
   E3<T> e3f_n;       // now e3 at f-points (the rest state unless NEMO_F_E3F_N is bound)
   RO<T> r1_e1e2f;    // 1 / (e1f e2f)
+  // 1 / e3t_0 and 1 / e3w_0 per level (correctly rounded) where the rest-state scale
+  // factor is a 1-D profile, else NULL: the divisors of the hot-path tracer kernels
+  RO<T> r1_e3t, r1_e3w;
 };
 
 __device__ __forceinline__ bool in_range(int k, int lo, int hi) { return k >= lo && k <= hi; }
@@ -131,6 +134,17 @@ template <> struct Third<float> { static constexpr float v = 0x1.555556p-2f; };
 template <class T>
 __device__ __forceinline__ T rcount(T n) {
   return n <= T(1) ? T(1) : (n == T(2) ? T(0.5) : (n == T(3) ? Third<T>::v : T(0.25)));
+}
+// rcount of the sum of four 0/1 masks; FP64 counts them on the integer pipe
+template <class T>
+__device__ __forceinline__ T rcount4(T a, T b, T c, T d) {
+  if constexpr (sizeof(T) == 8) {
+    const int n = (__double2hiint(a) != 0) + (__double2hiint(b) != 0) + (__double2hiint(c) != 0) +
+                  (__double2hiint(d) != 0);
+    return n <= 1 ? T(1) : (n == 2 ? T(0.5) : (n == 3 ? Third<T>::v : T(0.25)));
+  } else {
+    return rcount(a + b + c + d);
+  }
 }
 
 // Land sentinel of nonosc (traadv_fct.F90:354). 1e40 overflows FP32; 1e30 keeps the
