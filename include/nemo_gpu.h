@@ -40,7 +40,10 @@ enum nemo_status {
   NEMO_ERR_CUDA = 4,         /* CUDA runtime error                                    */
   NEMO_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up (barrier)          */
   NEMO_ERR_NOMEM = 6,        /* device allocation failed at context creation          */
-  NEMO_ERR_STATE = 7         /* call order violated (e.g. iso before its first pass)  */
+  NEMO_ERR_STATE = 7,        /* call order violated (e.g. iso before its first pass)  */
+  NEMO_ERR_BLOWUP = 8        /* stp_ctl: |ssh| > 20 m, |U| > 10 m/s, S <= 0, S >= 100
+                                or NaN (stpctl.F90:149-157); reported by the next
+                                nemo_gpu_synchronize after the check ran             */
 };
 
 /* ------------------------------------------------------------ precision modes */
@@ -494,6 +497,48 @@ int nemo_gpu_glob_sum(nemo_ctx *ctx, const char *cdname, const void *ptab, int n
 int nemo_gpu_glob_sum_noalloc(const void *ptab, const double *tmask_i, int jpi, int jpj, int nk,
                               int nmembers, int is_fp64, void *stream, double *out);
 
+/* ------------------------------------------------ run control and budgets */
+
+/* Sizes of the per-member results of stp_ctl and dia_hsb below. */
+#define NEMO_CTL_N 6
+#define NEMO_CTL_NLOC 11
+#define NEMO_HSB_N 16
+
+/* stp_ctl (stpctl.F90:44-194): the test of extrema of every member on the device
+ * (:112-127): |ssh| max, |U| max (zonal velocity, every point), and the maxima of
+ * -S, S, -T, T over tmask = 1 (a NaN makes its extremum NaN); then the blow-up test
+ * (:149-157) when the domain has ocean points. Enqueued on the context's stream; no
+ * host synchronisation. If it fires for a member, the next nemo_gpu_synchronize
+ * returns NEMO_ERR_BLOWUP (the reference's ctl_stop / kindic = -3), and
+ * nemo_gpu_stp_ctl_result gives the values and positions. nemo_gpu_stp_model runs
+ * it at the end of every step (step.F90:305). */
+int nemo_gpu_stp_ctl(nemo_ctx *ctx, int kt);
+/* The last stp_ctl's results (synchronises): per member m, zmax[NEMO_CTL_N*m ..] =
+ * |ssh| max, |U| max, -S min, S max, -T min, T max (the reference's zmax(1:6));
+ * loc[NEMO_CTL_NLOC*m ..] = the 1-based positions of :158-170 (i j of |ssh| max,
+ * i j k of |U| max, S min, S max; 0 when the test did not fire); kindic[m] = -3 when
+ * it fired, else 0. Each pointer may be NULL. */
+int nemo_gpu_stp_ctl_result(nemo_ctx *ctx, double *zmax, int *loc, int *kindic);
+
+/* dia_hsb (diahsb.F90): heat, salt and volume budgets with FP64 compensated
+ * (double-double) global sums, in both precisions. nemo_gpu_dia_hsb_init is
+ * dia_hsb_rst( nit000, 'READ' ) of a run without restart (:283-311): it records the
+ * initial ssh, scale factors and contents of the bound fields and zeroes the
+ * forcing sums; after it nemo_gpu_stp_model runs dia_hsb after ssh_swp
+ * (step.F90:282). nemo_gpu_dia_hsb is one call of :60-239 (without runoff, ice-shelf
+ * and geothermal inputs; rnf enters the volume flux where bound); it reads SSHN,
+ * TSN, TSB, E3T_N (or the rest state), EMP, SBC_TSC, WN (ln_linssh) and QSR
+ * (ln_traqsr), and masks tsn and tsb in place as the reference does (:88-89). */
+int nemo_gpu_dia_hsb_init(nemo_ctx *ctx);
+int nemo_gpu_dia_hsb(nemo_ctx *ctx, int kt);
+/* The last dia_hsb's terms (synchronises): per member m, out[NEMO_HSB_N*m ..] =
+ * frc_v, frc_t, frc_s, frc_wn_t, frc_wn_s (the accumulated forcing), zdiff_v1,
+ * zdiff_v2, zdiff_hc, zdiff_sc (drifts after the forcing, :174-178), zdiff_hc1,
+ * zdiff_sc1, zerr_hc1, zerr_sc1 (linear free surface, :179-185, else 0), zvol_tot,
+ * surf_tot, 0. The reference's diagnostics follow from them, e.g. the temperature
+ * drift bgtemper = zdiff_hc1 / zvol_tot (linear free surface). */
+int nemo_gpu_dia_hsb_result(nemo_ctx *ctx, double *out);
+
 /* The path of one timestep stp (step.F90:194-257) on the bound fields, in the
  * reference's order: dyn_spg_ts, tsa = 0 (:234), tra_adv (transports + FCT),
  * tra_ldf (lap or iso, per the namelist), tra_zdf (implicit + salinity clamp).
@@ -531,6 +576,7 @@ enum nemo_kernel_id {
   NEMO_K_DYN_LDF,      /* lateral viscosity */
   NEMO_K_DYN_VOR,      /* vorticity trend */
   NEMO_K_DYN_KEG, NEMO_K_DYN_ZAD, /* momentum advection, vector form */
+  NEMO_K_STP_CTL, NEMO_K_DIA_HSB, /* run control extrema, conservation budgets */
   NEMO_K_COUNT
 };
 

@@ -90,6 +90,17 @@ struct nemo_ctx {
   float* spg_ff = nullptr;  // mixed form: compensated sub-step sums, 10 x nmem x n2
   unsigned int* bar_mem = nullptr;  // count, gen
   int* err_flag = nullptr;
+  // stp_ctl (block partials, per-member results, the blow-up flag) and dia_hsb
+  double* ctl_part = nullptr;
+  double* ctl_out = nullptr;
+  int* ctl_flag = nullptr;
+  int ctl_nblk = 0;
+  int someoce = 0;  // the domain has ocean points (stpctl.F90:111)
+  bool hsb_on = false;
+  double* hsb_mem = nullptr;  // surf, tmask_h; ssh, ssh heat, ssh salt (x nmem); e3t, heat, salt (x nmem)
+  double* hsb_part = nullptr;
+  double* hsb_state = nullptr;  // 8 a member: frc_v, frc_t, frc_s, frc_wn_t, frc_wn_s, surf_tot
+  double* hsb_out = nullptr;    // NEMO_HSB_N a member
   long long bar_spins = 4000000;
   int tma_polls = 1 << 16;  // bound of each wait of a TMA kernel on its tensor copies
   int bar_extra = 0;
@@ -1171,6 +1182,50 @@ bool qsr_bound(const nemo_ctx* c) {
   return true;
 }
 
+// stp_ctl and dia_hsb (k_diag.cuh)
+template <class T>
+int run_stp_ctl(nemo_ctx* c) {
+  cudaError_t e = launch_stp_ctl<T>(dom<T>(c), (const T*)c->f[NEMO_F_SSHN], (const T*)c->f[NEMO_F_UN],
+                                    (const T*)c->f[NEMO_F_TSN], c->ctl_part, c->ctl_nblk, c->someoce, c->ctl_out,
+                                    c->ctl_flag, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "stp_ctl launch");
+  return NEMO_OK;
+}
+
+template <class T>
+HsbArgs<T> hsb_args(nemo_ctx* c) {
+  HsbArgs<T> a{};
+  const size_t n2 = c->n2, n3 = c->n3, nm = c->nmem;
+  a.tsn = (T*)c->f[NEMO_F_TSN]; a.tsb = (T*)c->f[NEMO_F_TSB];
+  a.sshn = (const T*)c->f[NEMO_F_SSHN]; a.emp = (const T*)c->f[NEMO_F_EMP]; a.rnf = (const T*)c->f[NEMO_F_RNF];
+  a.tsc = (const T*)c->f[NEMO_F_SBC_TSC]; a.qsr = (const T*)c->f[NEMO_F_QSR]; a.wn = (const T*)c->f[NEMO_F_WN];
+  a.e3t = dom_now<T>(c).e3t_n;
+  double* m = c->hsb_mem;
+  a.surf = m; a.tmask_h = m + n2;
+  a.ssh_ini = m + 2 * n2; a.ssh_hc_ini = a.ssh_ini + nm * n2; a.ssh_sc_ini = a.ssh_hc_ini + nm * n2;
+  a.e3t_ini = a.ssh_sc_ini + nm * n2; a.hc_ini = a.e3t_ini + nm * n3; a.sc_ini = a.hc_ini + nm * n3;
+  a.state = c->hsb_state; a.out = c->hsb_out;
+  const double rcp = c->nam.rcp > 0 ? c->nam.rcp : 3991.86795711963;
+  a.rdt = c->nam.rn_rdt; a.r1_rau0 = 1.0 / c->nam.rau0; a.r1_rau0_rcp = 1.0 / (c->nam.rau0 * rcp);
+  a.linssh = c->nam.ln_linssh; a.traqsr = c->nam.ln_traqsr;
+  return a;
+}
+
+int hsb_check(nemo_ctx* c) {
+  if (!c->hsb_on) return fail(c, NEMO_ERR_STATE, "dia_hsb: call nemo_gpu_dia_hsb_init first");
+  if (!c->f[NEMO_F_TSN] || !c->f[NEMO_F_TSB] || !c->f[NEMO_F_SSHN] || !c->f[NEMO_F_EMP] || !c->f[NEMO_F_SBC_TSC] ||
+      !c->f[NEMO_F_WN] || (c->nam.ln_traqsr && !c->f[NEMO_F_QSR]))
+    return fail(c, NEMO_ERR_UNBOUND, "dia_hsb: tsn, tsb, sshn, emp, sbc_tsc, wn (and qsr) must be bound");
+  return NEMO_OK;
+}
+
+template <class T>
+int run_dia_hsb(nemo_ctx* c) {
+  cudaError_t e = launch_dia_hsb<T>(dom<T>(c), hsb_args<T>(c), c->hsb_part, c->ctl_nblk, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "dia_hsb launch");
+  return NEMO_OK;
+}
+
 template <class T>
 int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
   const nemo_namelist& nm = c->nam;
@@ -1290,10 +1345,15 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
   }
   s = run_zdf<T>(c, r2dt, F[NEMO_F_TSB], F[NEMO_F_TSA], 2, 0, 1);
   if (s) return s;
-  if (model) {  // tra_nxt, dyn_nxt, ssh_swp (step.F90:280-282)
+  if (model) {  // tra_nxt, dyn_nxt, ssh_swp (step.F90:277-279), dia_hsb (:282), stp_ctl (:305)
     if ((s = run_tra_nxt<T>(c, kt))) return s;
     if ((s = run_dyn_nxt<T>(c, kt))) return s;
     if ((s = run_ssh_swp<T>(c, kt))) return s;
+    if (c->hsb_on) {
+      if ((s = hsb_check(c))) return s;
+      if ((s = run_dia_hsb<T>(c))) return s;
+    }
+    if ((s = run_stp_ctl<T>(c))) return s;
   }
   if (staged) CK(cudaEventRecord(c->ev_step_done, c->stream), "end of the step");
   if (c->timing) {
@@ -1436,6 +1496,14 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
   cudaMemset(c->bar_mem, 0, 2 * sizeof(unsigned int));
   cudaMemset(c->err_flag, 0, sizeof(int));
   select_p2(c);
+  c->ctl_nblk = 2 * c->nsm;
+  if (cudaMalloc(&c->ctl_part, (size_t)c->ctl_nblk * c->nmem * CTL_REC * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&c->ctl_out, (size_t)c->nmem * 32 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&c->ctl_flag, sizeof(int)) != cudaSuccess)
+    return bad(NEMO_ERR_NOMEM);
+  cudaMemset(c->ctl_out, 0, (size_t)c->nmem * 32 * sizeof(double));
+  cudaMemset(c->ctl_flag, 0, sizeof(int));
+  for (size_t p = 0; p < (size_t)c->n2; ++p) c->someoce |= c->ssmask[p] == 1.0;
   if (c->p2_blocks < 1) return bad(NEMO_ERR_CUDA);
   c->gs_nblk = c->nsm * 4;
   if (cudaMalloc(&c->gs_part, 2 * (size_t)c->gs_nblk * c->nmem * 8) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
@@ -1468,6 +1536,8 @@ int nemo_gpu_destroy(nemo_ctx* c) {
   cudaFree(c->spg_ff);
   cudaFree(c->d_wgt1); cudaFree(c->d_wgt2); cudaFree(c->d_wgtf);
   cudaFree(c->bar_mem); cudaFree(c->err_flag);
+  cudaFree(c->ctl_part); cudaFree(c->ctl_out); cudaFree(c->ctl_flag);
+  cudaFree(c->hsb_mem); cudaFree(c->hsb_part); cudaFree(c->hsb_state); cudaFree(c->hsb_out);
   cudaFree(c->gs_part); cudaFree(c->gs_out);
   for (auto e : c->tev)
     if (e) cudaEventDestroy(e);
@@ -1500,7 +1570,22 @@ int nemo_gpu_synchronize(nemo_ctx* c) {
   for (bool& b : c->upf_pending) b = false;
   for (bool& b : c->field_pending) b = false;
   CK(cudaStreamSynchronize(c->stream), "synchronize");
-  int flag = 0;
+  int flag = 0, blow = 0;
+  CK(cudaMemcpy(&blow, c->ctl_flag, sizeof(int), cudaMemcpyDeviceToHost), "read status");
+  if (blow) {  // stp_ctl's blow-up test fired (stpctl.F90:149-184)
+    cudaMemset(c->ctl_flag, 0, sizeof(int));
+    std::vector<double> o((size_t)c->nmem * 32);
+    CK(cudaMemcpy(o.data(), c->ctl_out, o.size() * sizeof(double), cudaMemcpyDeviceToHost), "read stp_ctl");
+    for (int m = 0; m < c->nmem; ++m) {
+      const double* z = &o[(size_t)m * 32];
+      if (z[6] != 0.0)
+        return fail(c, NEMO_ERR_BLOWUP,
+                    "stp_ctl: |ssh| > 20 m or |U| > 10 m/s or S <= 0 or S >= 100 or NaN (member %d: |ssh| max %g at "
+                    "%d %d, |U| max %g at %d %d %d, S min %g at %d %d %d, S max %g at %d %d %d)",
+                    m, z[0], (int)z[7], (int)z[8], z[1], (int)z[9], (int)z[10], (int)z[11], -z[2], (int)z[12],
+                    (int)z[13], (int)z[14], z[3], (int)z[15], (int)z[16], (int)z[17]);
+    }
+  }
   CK(cudaMemcpy(&flag, c->err_flag, sizeof(int), cudaMemcpyDeviceToHost), "read status");
   if (flag) {
     cudaMemset(c->err_flag, 0, sizeof(int));
@@ -1895,6 +1980,95 @@ int nemo_gpu_dyn_nxt(nemo_ctx* c, int kt) {
   if (join_copies(c)) return NEMO_ERR_CUDA;
   if (int s = model_fields(c, "dyn_nxt")) return s;
   return c->prec == NEMO_PREC_FP64 ? run_dyn_nxt<double>(c, kt) : run_dyn_nxt<float>(c, kt);
+}
+
+// ---------------------------------------------------------------- stp_ctl, dia_hsb
+int nemo_gpu_stp_ctl(nemo_ctx* c, int kt) {
+  (void)kt;
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (!c->f[NEMO_F_SSHN] || !c->f[NEMO_F_UN] || !c->f[NEMO_F_TSN])
+    return fail(c, NEMO_ERR_UNBOUND, "stp_ctl: sshn, un and tsn must be bound");
+  return c->prec == NEMO_PREC_FP64 ? run_stp_ctl<double>(c) : run_stp_ctl<float>(c);
+}
+
+int nemo_gpu_stp_ctl_result(nemo_ctx* c, double* zmax, int* loc, int* kindic) {
+  if (!c) return NEMO_ERR_ARG;
+  CK(cudaStreamSynchronize(c->stream), "stp_ctl result");
+  std::vector<double> o((size_t)c->nmem * 32);
+  CK(cudaMemcpy(o.data(), c->ctl_out, o.size() * sizeof(double), cudaMemcpyDeviceToHost), "stp_ctl result");
+  for (int m = 0; m < c->nmem; ++m) {
+    const double* z = &o[(size_t)m * 32];
+    if (zmax)
+      for (int t = 0; t < NEMO_CTL_N; ++t) zmax[(size_t)m * NEMO_CTL_N + t] = z[t];
+    if (kindic) kindic[m] = (int)z[6];
+    if (loc)
+      for (int t = 0; t < NEMO_CTL_NLOC; ++t) loc[(size_t)m * NEMO_CTL_NLOC + t] = (int)z[7 + t];
+  }
+  return NEMO_OK;
+}
+
+int nemo_gpu_dia_hsb_init(nemo_ctx* c) {
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (!c->f[NEMO_F_SSHN] || !c->f[NEMO_F_TSN])
+    return fail(c, NEMO_ERR_UNBOUND, "dia_hsb_init: sshn and tsn must be bound");
+  const size_t n2 = c->n2, n3 = c->n3, nm = c->nmem;
+  if (!c->hsb_mem) {
+    const size_t words = 2 * n2 + 3 * nm * n2 + 3 * nm * n3;
+    if (cudaMalloc(&c->hsb_mem, words * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&c->hsb_part, (size_t)c->ctl_nblk * nm * HSB_NS * 2 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&c->hsb_state, nm * 8 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&c->hsb_out, nm * NEMO_HSB_N * sizeof(double)) != cudaSuccess)
+      return fail(c, NEMO_ERR_NOMEM, "dia_hsb work arrays");
+    CK(cudaMemset(c->hsb_mem, 0, words * sizeof(double)), "dia_hsb = 0");
+  }
+  // surf = e1e2t * tmask_i (diahsb.F90:411), tmask_h (dommsk.F90:213-217, closed
+  // domain), surf_tot = glob_sum(surf) with DDPDD (:412)
+  std::vector<double> h(2 * n2);
+  double re = 0.0, im = 0.0;
+  for (size_t p = 0; p < n2; ++p) {
+    h[p] = c->e1e2t[p] * c->tmask_i[p];
+    const int ji = (int)(p % c->jpi) + 1, jj = (int)(p / c->jpi) + 1;
+    h[n2 + p] = (ji == 1 || ji == c->jpi || jj == 1 || jj == c->jpj) ? 0.0 : 1.0;
+    const double a = h[p] * c->tmask_i[p];  // DDPDD (lib_fortran.F90:300-332)
+    const double zt1 = a + re, zerr = zt1 - a;
+    const double zt2 = ((re - zerr) + (a - (zt1 - zerr))) + 0.0 + im;
+    const double sum = zt1 + zt2;
+    im = zt2 - ((zt1 + zt2) - zt1);
+    re = sum;
+  }
+  CK(cudaMemcpy(c->hsb_mem, h.data(), 2 * n2 * sizeof(double), cudaMemcpyHostToDevice), "dia_hsb surf");
+  std::vector<double> st(nm * 8, 0.0);
+  for (size_t m = 0; m < nm; ++m) st[m * 8 + 5] = re;
+  CK(cudaMemcpy(c->hsb_state, st.data(), st.size() * sizeof(double), cudaMemcpyHostToDevice), "dia_hsb state");
+  CK(cudaMemset(c->hsb_out, 0, nm * NEMO_HSB_N * sizeof(double)), "dia_hsb out");
+  cudaError_t e = c->prec == NEMO_PREC_FP64
+                      ? launch_hsb_init<double>(dom<double>(c), hsb_args<double>(c), 4 * c->nsm, c->stream)
+                      : launch_hsb_init<float>(dom<float>(c), hsb_args<float>(c), 4 * c->nsm, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "dia_hsb_init launch");
+  c->hsb_on = true;
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);  // the model step now runs dia_hsb
+  c->graphs.clear();
+  return NEMO_OK;
+}
+
+int nemo_gpu_dia_hsb(nemo_ctx* c, int kt) {
+  (void)kt;
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  int s = hsb_check(c);
+  if (s) return s;
+  return c->prec == NEMO_PREC_FP64 ? run_dia_hsb<double>(c) : run_dia_hsb<float>(c);
+}
+
+int nemo_gpu_dia_hsb_result(nemo_ctx* c, double* out) {
+  if (!c || !out) return NEMO_ERR_ARG;
+  if (!c->hsb_on) return fail(c, NEMO_ERR_STATE, "dia_hsb_result: no dia_hsb yet");
+  CK(cudaStreamSynchronize(c->stream), "dia_hsb result");
+  CK(cudaMemcpy(out, c->hsb_out, (size_t)c->nmem * NEMO_HSB_N * sizeof(double), cudaMemcpyDeviceToHost),
+     "dia_hsb result");
+  return NEMO_OK;
 }
 
 int nemo_gpu_ssh_swp(nemo_ctx* c, int kt) {

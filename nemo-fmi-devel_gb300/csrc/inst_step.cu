@@ -1,5 +1,6 @@
 // inst_step.cu -- launchers of the rest-of-step kernels, both precisions; compiled
 // with --fmad=false so the FP64 form rounds as the reference's FP64 CPU build.
+#include "k_diag.cuh"
 #include "k_step.cuh"
 #include "launch.h"
 
@@ -118,7 +119,32 @@ cudaError_t launch_dyn_zad(const Dom<T>& d, const T* un, const T* vn, const T* w
   return cudaGetLastError();
 }
 
+template <class T>
+cudaError_t launch_stp_ctl(const Dom<T>& d, const T* sshn, const T* un, const T* ts, double* part, int nblk,
+                           int someoce, double* out, int* flag, cudaStream_t s) {
+  k_ctl_partial<T><<<dim3(nblk, d.nmem), DG_THREADS, 0, s>>>(d, sshn, un, ts, part);
+  k_ctl_final<T><<<(d.nmem + 31) / 32, 32, 0, s>>>(d, part, nblk, someoce, out, flag);
+  ktick(NEMO_K_STP_CTL, s);
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_hsb_init(const Dom<T>& d, const HsbArgs<T>& a, int nblk, cudaStream_t s) {
+  k_hsb_init<T><<<nblk, DG_THREADS, 0, s>>>(d, a);
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_dia_hsb(const Dom<T>& d, const HsbArgs<T>& a, double* part, int nblk, cudaStream_t s) {
+  k_hsb_partial<T><<<dim3(nblk, d.nmem), DG_THREADS, 0, s>>>(d, a, part);
+  k_hsb_final<T><<<d.nmem, 32, 0, s>>>(d, a, part, nblk);
+  ktick(NEMO_K_DIA_HSB, s);
+  return cudaGetLastError();
+}
+
 #define NEMO_STEP_INST(T)                                                                                      \
+  template cudaError_t launch_stp_ctl<T>(const Dom<T>&, const T*, const T*, const T*, double*, int, int,       \
+                                         double*, int*, cudaStream_t);                                         \
+  template cudaError_t launch_hsb_init<T>(const Dom<T>&, const HsbArgs<T>&, int, cudaStream_t);                \
+  template cudaError_t launch_dia_hsb<T>(const Dom<T>&, const HsbArgs<T>&, double*, int, cudaStream_t);         \
   template cudaError_t launch_wzv<T>(const Dom<T>&, const T*, const T*, T*, T, cudaStream_t);                  \
   template cudaError_t launch_dyn_zdf_step<T>(const Dom<T>&, const T*, const T*, T*, T*, T, cudaStream_t);     \
   template cudaError_t launch_dyn_nxt<T>(const Dom<T>&, const NxtArgs<T, double>&, cudaStream_t);              \

@@ -1,6 +1,7 @@
 // step.h -- host launchers of the rest-of-step kernels (k_step.cuh), defined in
 // inst_step.cu for both precisions.
 #pragma once
+#include "k_diag.cuh"
 #include "k_tra.cuh"
 
 namespace nemo {
@@ -98,5 +99,14 @@ template <class T>
 cudaError_t launch_dyn_nxt(const Dom<T>& d, const NxtArgs<T, double>& a, cudaStream_t s);
 template <class T>
 cudaError_t launch_ssh_swp(const Dom<T>& d, T* sshb, T* sshn, const double* ssha, T atfp, int euler, cudaStream_t s);
+// stp_ctl: block partials part (nblk x nmem records), results out (32 doubles a member)
+template <class T>
+cudaError_t launch_stp_ctl(const Dom<T>& d, const T* sshn, const T* un, const T* ts, double* part, int nblk,
+                           int someoce, double* out, int* flag, cudaStream_t s);
+// dia_hsb: the initial fields, and one call (block partials part: nblk x nmem x 13 pairs)
+template <class T>
+cudaError_t launch_hsb_init(const Dom<T>& d, const HsbArgs<T>& a, int nblk, cudaStream_t s);
+template <class T>
+cudaError_t launch_dia_hsb(const Dom<T>& d, const HsbArgs<T>& a, double* part, int nblk, cudaStream_t s);
 
 }  // namespace nemo

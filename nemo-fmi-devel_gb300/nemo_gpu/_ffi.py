@@ -12,7 +12,8 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.ab
                       "include", "nemo_gpu.h")
 
 NEMO_OK, NEMO_ERR_ARG, NEMO_ERR_UNSUPPORTED, NEMO_ERR_UNBOUND = 0, 1, 2, 3
-NEMO_ERR_CUDA, NEMO_ERR_TIMEOUT, NEMO_ERR_NOMEM, NEMO_ERR_STATE = 4, 5, 6, 7
+NEMO_ERR_CUDA, NEMO_ERR_TIMEOUT, NEMO_ERR_NOMEM, NEMO_ERR_STATE, NEMO_ERR_BLOWUP = 4, 5, 6, 7, 8
+NEMO_CTL_N, NEMO_CTL_NLOC, NEMO_HSB_N = 6, 11, 16  # result sizes of stp_ctl and dia_hsb
 PREC_FP64, PREC_MIXED = 0, 1
 VOR = {"ENS": 0, "ENE": 1, "ENT": 2, "EET": 3, "EEN": 4, "MIX": 5}
 
@@ -153,6 +154,11 @@ def load(path):
     _proto(lib, "nemo_gpu_set_fusion", i, [vp, i])
     _proto(lib, "nemo_gpu_set_tma", i, [vp, i])
     _proto(lib, "nemo_gpu_set_tma_poll_limit", i, [vp, i])
+    _proto(lib, "nemo_gpu_stp_ctl", i, [vp, i])
+    _proto(lib, "nemo_gpu_stp_ctl_result", i, [vp, vp, vp, vp])
+    _proto(lib, "nemo_gpu_dia_hsb_init", i, [vp])
+    _proto(lib, "nemo_gpu_dia_hsb", i, [vp, i])
+    _proto(lib, "nemo_gpu_dia_hsb_result", i, [vp, vp])
     _proto(lib, "nemo_gpu_set_spg_specialised", i, [vp, i])
     _proto(lib, "nemo_gpu_set_fct_fused", i, [vp, i])
     _proto(lib, "nemo_gpu_get_timing", i, [vp, C.POINTER(d), C.POINTER(i)])

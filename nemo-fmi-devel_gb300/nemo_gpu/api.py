@@ -129,6 +129,33 @@ class Context:
     def set_tma(self, on):
         self._ck(self.lib.nemo_gpu_set_tma(self.h, int(on)), "set_tma")
 
+    # ---------------------------------------------------------------- stp_ctl, dia_hsb
+    def stp_ctl(self, kt):
+        self._ck(self.lib.nemo_gpu_stp_ctl(self.h, kt), "stp_ctl")
+
+    def stp_ctl_result(self):
+        """(zmax[nmem, 6], loc[nmem, 11], kindic[nmem]) of the last stp_ctl"""
+        import numpy as np
+        z = np.zeros((self.nmem, _ffi.NEMO_CTL_N))
+        loc = np.zeros((self.nmem, _ffi.NEMO_CTL_NLOC), dtype=np.int32)
+        k = np.zeros(self.nmem, dtype=np.int32)
+        self._ck(self.lib.nemo_gpu_stp_ctl_result(self.h, z.ctypes.data, loc.ctypes.data, k.ctypes.data),
+                 "stp_ctl_result")
+        return z, loc, k
+
+    def dia_hsb_init(self):
+        self._ck(self.lib.nemo_gpu_dia_hsb_init(self.h), "dia_hsb_init")
+
+    def dia_hsb(self, kt):
+        self._ck(self.lib.nemo_gpu_dia_hsb(self.h, kt), "dia_hsb")
+
+    def dia_hsb_result(self):
+        """the terms of the last dia_hsb, [nmem, NEMO_HSB_N]"""
+        import numpy as np
+        out = np.zeros((self.nmem, _ffi.NEMO_HSB_N))
+        self._ck(self.lib.nemo_gpu_dia_hsb_result(self.h, out.ctypes.data), "dia_hsb_result")
+        return out
+
     def set_spg_specialised(self, on):
         self._ck(self.lib.nemo_gpu_set_spg_specialised(self.h, int(on)), "set_spg_specialised")
 

@@ -56,6 +56,14 @@ struct ora_ctx {
   /* FCT limiter multipliers (3 faces x kjpt fields): 1 = record, 2 = replay */
   double *fct_tape;
   int fct_tape_mode;
+  /* dia_hsb module state (diahsb.F90:40-52): set by ora_dia_hsb_init */
+  int hsb_on;
+  double surf_tot, frc_v, frc_t, frc_s, frc_wn_t, frc_wn_s;
+  double *surf, *surf_ini, *ssh_ini, *ssh_hc_loc_ini, *ssh_sc_loc_ini, *e3t_ini, *hc_loc_ini, *sc_loc_ini;
+  double hsb_out[NEMO_HSB_N];
+  /* the last stp_ctl of the model step */
+  double ctl_zmax[NEMO_CTL_N];
+  int ctl_loc[NEMO_CTL_NLOC], ctl_kindic;
 };
 
 static void spg_coriolis_factors(ora_ctx *c, const double *ht_n, const double *e3f_n);
@@ -383,7 +391,9 @@ int ora_destroy(ora_ctx *c) {
                    &c->ht_0, &c->hu_0, &c->hv_0, &c->r1_hu_0, &c->r1_hv_0, &c->ahtu_c, &c->ahtv_c,
                    &c->wgtbtp1, &c->wgtbtp2, &c->zwz, &c->ftne, &c->ftnw, &c->ftse, &c->ftsw,
                    &c->sshn_e, &c->sshb_e, &c->sshbb_e, &c->un_e, &c->ub_e, &c->ubb_e, &c->vn_e, &c->vb_e,
-                   &c->vbb_e, &c->ssha_e, &c->ua_e, &c->va_e, &c->hu_e, &c->hv_e, &c->hur_e, &c->hvr_e};
+                   &c->vbb_e, &c->ssha_e, &c->ua_e, &c->va_e, &c->hu_e, &c->hv_e, &c->hur_e, &c->hvr_e,
+                   &c->surf, &c->surf_ini, &c->ssh_ini, &c->ssh_hc_loc_ini, &c->ssh_sc_loc_ini, &c->e3t_ini,
+                   &c->hc_loc_ini, &c->sc_loc_ini};
   for (size_t i = 0; i < sizeof(dp) / sizeof(dp[0]); ++i) wfree(*dp[i]);
   free(c->mikt); free(c->mbkt); free(c->mbku); free(c->mbkv);
   free(c);
@@ -1675,6 +1685,243 @@ int ora_glob_sum(ora_ctx *c, const double *ptab, int nk, double *out) {
   return NEMO_OK;
 }
 
+/* ---------------------------------------------------------------- stp_ctl */
+/* stp_ctl (stpctl.F90:44-194), the test of extrema (:112-127) and the blow-up
+ * conditions (:149-157): zmax = |ssh| max, |U| max (zonal, every point), then the
+ * maxima of -S, S, -T, T over tmask = 1. MAXVAL of values that include a NaN is
+ * taken as NaN here (the NaN test of :155 then fires). On a blow-up the positions
+ * (:158-170) are MAXLOC(|ssh|), MAXLOC(|un|), MINLOC(S), MAXLOC(S) (1-based, first
+ * in Fortran order; a NaN counts as the extreme) and kindic = -3 (:184). */
+int ora_stp_ctl(ora_ctx *c, int kt, double *zmax, int *loc, int *kindic) {
+  (void)kt;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  const double *sshn = c->f[NEMO_F_SSHN], *un = c->f[NEMO_F_UN], *ts = c->f[NEMO_F_TSN];
+  if (!sshn || !un || !ts || !zmax) return NEMO_ERR_UNBOUND;
+  const double huge = 1.7976931348623157e308;
+  int lsomeoce = 0;
+  for (size_t p = 0; p < n2; ++p) lsomeoce |= c->ssmask[p] == 1.0;
+  double z[6] = {-huge, -huge, -huge, -huge, -huge, -huge};
+  int nan1 = 0, nan2 = 0, nan3 = 0;
+  for (size_t p = 0; p < n2; ++p) {
+    const double v = fabs(sshn[p]);
+    if (isnan(v)) nan1 = 1; else if (v > z[0]) z[0] = v;
+  }
+  for (size_t q = 0; q < n3; ++q) {
+    const double v = fabs(un[q]);
+    if (isnan(v)) nan2 = 1; else if (v > z[1]) z[1] = v;
+    if (c->tmask[q] == 1.0) {
+      const double sv = ts[q + n3], tv = ts[q];
+      if (isnan(sv)) nan3 = 1;
+      else { if (-sv > z[2]) z[2] = -sv; if (sv > z[3]) z[3] = sv; }
+      if (!isnan(tv)) { if (-tv > z[4]) z[4] = -tv; if (tv > z[5]) z[5] = tv; }
+    }
+  }
+  if (nan1) z[0] = NAN;
+  if (nan2) z[1] = NAN;
+  if (nan3) { z[2] = NAN; z[3] = NAN; }
+  for (int i = 0; i < 6; ++i) zmax[i] = z[i];
+  const int trip = lsomeoce && (z[0] > 20.0 || z[1] > 10.0 || z[2] >= 0.0 || z[3] >= 100.0 || z[3] < 0.0 ||
+                                isnan(z[0] + z[1] + z[2]));
+  if (kindic) *kindic = trip ? -3 : 0;
+  if (loc) {
+    for (int i = 0; i < NEMO_CTL_NLOC; ++i) loc[i] = 0;
+    if (trip) {
+      size_t best = 0;
+      double bv = -INFINITY;
+      for (size_t p = 0; p < n2; ++p) {  /* MAXLOC(ABS(sshn)) */
+        const double v = isnan(sshn[p]) ? INFINITY : fabs(sshn[p]);
+        if (v > bv) { bv = v; best = p; }
+      }
+      loc[0] = (int)(best % jpi) + 1; loc[1] = (int)(best / jpi) + 1;
+      best = 0; bv = -INFINITY;
+      for (size_t q = 0; q < n3; ++q) {  /* MAXLOC(ABS(un)) */
+        const double v = isnan(un[q]) ? INFINITY : fabs(un[q]);
+        if (v > bv) { bv = v; best = q; }
+      }
+      loc[2] = (int)(best % jpi) + 1; loc[3] = (int)((best / jpi) % jpj) + 1; loc[4] = (int)(best / n2) + 1;
+      size_t bmin = 0, bmax = 0;
+      double vmin = INFINITY, vmax = -INFINITY;
+      int any = 0;
+      for (size_t q = 0; q < n3; ++q) {  /* MINLOC / MAXLOC(S, mask = tmask == 1) */
+        if (c->tmask[q] != 1.0) continue;
+        const double sv = ts[q + n3];
+        const double lo = isnan(sv) ? -INFINITY : sv, hi = isnan(sv) ? INFINITY : sv;
+        if (!any || lo < vmin) { vmin = lo; bmin = q; }
+        if (!any || hi > vmax) { vmax = hi; bmax = q; }
+        any = 1;
+      }
+      if (any) {
+        loc[5] = (int)(bmin % jpi) + 1; loc[6] = (int)((bmin / jpi) % jpj) + 1; loc[7] = (int)(bmin / n2) + 1;
+        loc[8] = (int)(bmax % jpi) + 1; loc[9] = (int)((bmax / jpi) % jpj) + 1; loc[10] = (int)(bmax / n2) + 1;
+      }
+    }
+  }
+  return NEMO_OK;
+}
+
+/* ---------------------------------------------------------------- dia_hsb */
+static double gsum(const ora_ctx *c, const double *x, int nk, const double *mask) {
+  const size_t n2 = (size_t)c->jpi * c->jpj;
+  double re = 0.0, im = 0.0;
+  for (int jk = 0; jk < nk; ++jk)
+    for (size_t p = 0; p < n2; ++p) ddpdd(x[p + n2 * jk] * mask[p], &re, &im);
+  return re;
+}
+
+/* dia_hsb_init (diahsb.F90:411-412) and dia_hsb_rst( nit000, 'READ' ) without a
+ * restart (:283-311): the masked cell area, the initial ssh, scale factors, heat and
+ * salt contents, and zero forcing sums. */
+int ora_dia_hsb_init(ora_ctx *c) {
+  const int jpk = c->jpk;
+  const size_t n2 = (size_t)c->jpi * c->jpj, n3 = n2 * jpk;
+  const double *sshn = c->f[NEMO_F_SSHN], *ts = c->f[NEMO_F_TSN];
+  if (!sshn || !ts) return NEMO_ERR_UNBOUND;
+  const double *e3t = fld(c, NEMO_F_E3T_N);
+  if (!c->surf) {
+    c->surf = zalloc(n2); c->surf_ini = zalloc(n2); c->ssh_ini = zalloc(n2);
+    c->ssh_hc_loc_ini = zalloc(n2); c->ssh_sc_loc_ini = zalloc(n2);
+    c->e3t_ini = zalloc(n3); c->hc_loc_ini = zalloc(n3); c->sc_loc_ini = zalloc(n3);
+  }
+  for (size_t p = 0; p < n2; ++p) c->surf[p] = c->e1e2t[p] * c->tmask_i[p];
+  c->surf_tot = gsum(c, c->surf, 1, c->tmask_i);
+  for (size_t p = 0; p < n2; ++p) {
+    c->surf_ini[p] = c->e1e2t[p] * c->tmask_i[p];
+    c->ssh_ini[p] = sshn[p];
+  }
+  for (size_t q = 0; q < n3; ++q) {
+    c->e3t_ini[q] = e3t[q] * c->tmask[q];
+    c->hc_loc_ini[q] = ts[q] * e3t[q] * c->tmask[q];
+    c->sc_loc_ini[q] = ts[q + n3] * e3t[q] * c->tmask[q];
+  }
+  c->frc_v = c->frc_t = c->frc_s = 0.0;
+  if (c->nam.ln_linssh) {
+    for (size_t p = 0; p < n2; ++p) {
+      c->ssh_hc_loc_ini[p] = ts[p] * sshn[p];
+      c->ssh_sc_loc_ini[p] = ts[p + n3] * sshn[p];
+    }
+    c->frc_wn_t = c->frc_wn_s = 0.0;
+  }
+  c->hsb_on = 1;
+  return NEMO_OK;
+}
+
+/* dia_hsb (diahsb.F90:60-239) without runoff, ice-shelf and geothermal inputs
+ * (ln_rnf, ln_isf, ln_trabbc off; rnf enters the volume flux where bound): the
+ * forcing sums (:93-123), the content variations (:130-169), the drifts (:174-185)
+ * and the total volume (:190-193). out[NEMO_HSB_N] = frc_v, frc_t, frc_s, frc_wn_t,
+ * frc_wn_s, zdiff_v1, zdiff_v2, zdiff_hc, zdiff_sc, zdiff_hc1, zdiff_sc1, zerr_hc1,
+ * zerr_sc1, zvol_tot, surf_tot (the last four of the first group of the linear free
+ * surface only, else 0). tsn and tsb are masked in place (:88-89). */
+int ora_dia_hsb(ora_ctx *c, int kt, double *out) {
+  (void)kt;
+  const int jpk = c->jpk;
+  const size_t n2 = (size_t)c->jpi * c->jpj, n3 = n2 * jpk;
+  double *tsn = c->f[NEMO_F_TSN], *tsb = c->f[NEMO_F_TSB];
+  const double *sshn = c->f[NEMO_F_SSHN], *emp = c->f[NEMO_F_EMP], *rnf = c->f[NEMO_F_RNF];
+  const double *tsc = c->f[NEMO_F_SBC_TSC], *qsr = c->f[NEMO_F_QSR], *wn = c->f[NEMO_F_WN];
+  if (!c->hsb_on) return NEMO_ERR_STATE;
+  if (!tsn || !tsb || !sshn || !emp || !tsc || !wn || (c->nam.ln_traqsr && !qsr)) return NEMO_ERR_UNBOUND;
+  const double *e3t = fld(c, NEMO_F_E3T_N);
+  const double rdt = c->nam.rn_rdt, rau0 = c->nam.rau0;
+  const double rcp = c->nam.rcp > 0 ? c->nam.rcp : 3991.86795711963;
+  const double r1_rau0 = 1.0 / rau0, r1_rau0_rcp = 1.0 / (rau0 * rcp);
+  for (size_t q = 0; q < n3; ++q) {
+    tsn[q] = tsn[q] * c->tmask[q]; tsb[q] = tsb[q] * c->tmask[q];
+    tsn[q + n3] = tsn[q + n3] * c->tmask[q]; tsb[q + n3] = tsb[q + n3] * c->tmask[q];
+  }
+  double *z2d0 = walloc(n2), *z2d1 = walloc(n2), *zwrk = walloc(n2 * (jpk - 1));
+  /* 1 - trends due to forcing */
+  for (size_t p = 0; p < n2; ++p) z2d0[p] = -(emp[p] - (rnf ? rnf[p] : 0.0) + 0.0) * c->surf[p];
+  const double z_frc_trd_v = r1_rau0 * gsum(c, z2d0, 1, c->tmask_i);
+  for (size_t p = 0; p < n2; ++p) z2d0[p] = tsc[p] * c->surf[p];
+  double z_frc_trd_t = gsum(c, z2d0, 1, c->tmask_i);
+  for (size_t p = 0; p < n2; ++p) z2d0[p] = tsc[p + n2] * c->surf[p];
+  const double z_frc_trd_s = gsum(c, z2d0, 1, c->tmask_i);
+  if (c->nam.ln_traqsr) {
+    for (size_t p = 0; p < n2; ++p) z2d0[p] = qsr[p] * c->surf[p];
+    z_frc_trd_t = z_frc_trd_t + r1_rau0_rcp * gsum(c, z2d0, 1, c->tmask_i);
+  }
+  double z_wn_trd_t = 0.0, z_wn_trd_s = 0.0;
+  if (c->nam.ln_linssh) {
+    for (size_t p = 0; p < n2; ++p) {
+      z2d0[p] = c->surf[p] * wn[p] * tsb[p];
+      z2d1[p] = c->surf[p] * wn[p] * tsb[p + n3];
+    }
+    z_wn_trd_t = -gsum(c, z2d0, 1, c->tmask_i);
+    z_wn_trd_s = -gsum(c, z2d1, 1, c->tmask_i);
+  }
+  c->frc_v = c->frc_v + z_frc_trd_v * rdt;
+  c->frc_t = c->frc_t + z_frc_trd_t * rdt;
+  c->frc_s = c->frc_s + z_frc_trd_s * rdt;
+  if (c->nam.ln_linssh) {
+    c->frc_wn_t = c->frc_wn_t + z_wn_trd_t * rdt;
+    c->frc_wn_s = c->frc_wn_s + z_wn_trd_s * rdt;
+  }
+  /* 2 - content variations (glob_sum_full: mask tmask_h) */
+  for (size_t p = 0; p < n2; ++p) z2d0[p] = c->surf[p] * sshn[p] - c->surf_ini[p] * c->ssh_ini[p];
+  double zdiff_v1 = gsum(c, z2d0, 1, c->tmask_h);
+  double z_ssh_hc = 0.0, z_ssh_sc = 0.0;
+  if (c->nam.ln_linssh) {
+    for (size_t p = 0; p < n2; ++p) {
+      z2d0[p] = c->surf[p] * (tsn[p] * sshn[p] - c->ssh_hc_loc_ini[p]);
+      z2d1[p] = c->surf[p] * (tsn[p + n3] * sshn[p] - c->ssh_sc_loc_ini[p]);
+    }
+    z_ssh_hc = gsum(c, z2d0, 1, c->tmask_h);
+    z_ssh_sc = gsum(c, z2d1, 1, c->tmask_h);
+  }
+  for (size_t q = 0; q < n2 * (jpk - 1); ++q) {
+    const size_t p = q % n2;
+    zwrk[q] = (c->surf[p] * e3t[q] - c->surf_ini[p] * c->e3t_ini[q]) * c->tmask[q];
+  }
+  double zdiff_v2 = gsum(c, zwrk, jpk - 1, c->tmask_h);
+  for (size_t q = 0; q < n2 * (jpk - 1); ++q) {
+    const size_t p = q % n2;
+    zwrk[q] = (c->surf[p] * e3t[q] * tsn[q] - c->surf_ini[p] * c->hc_loc_ini[q]) * c->tmask[q];
+  }
+  double zdiff_hc = gsum(c, zwrk, jpk - 1, c->tmask_h);
+  for (size_t q = 0; q < n2 * (jpk - 1); ++q) {
+    const size_t p = q % n2;
+    zwrk[q] = (c->surf[p] * e3t[q] * tsn[q + n3] - c->surf_ini[p] * c->sc_loc_ini[q]) * c->tmask[q];
+  }
+  double zdiff_sc = gsum(c, zwrk, jpk - 1, c->tmask_h);
+  /* 3 - drifts */
+  zdiff_v1 = zdiff_v1 - c->frc_v;
+  if (!c->nam.ln_linssh) zdiff_v2 = zdiff_v2 - c->frc_v;
+  zdiff_hc = zdiff_hc - c->frc_t;
+  zdiff_sc = zdiff_sc - c->frc_s;
+  double zdiff_hc1 = 0.0, zdiff_sc1 = 0.0, zerr_hc1 = 0.0, zerr_sc1 = 0.0;
+  if (c->nam.ln_linssh) {
+    zdiff_hc1 = zdiff_hc + z_ssh_hc;
+    zdiff_sc1 = zdiff_sc + z_ssh_sc;
+    zerr_hc1 = z_ssh_hc - c->frc_wn_t;
+    zerr_sc1 = z_ssh_sc - c->frc_wn_s;
+  }
+  /* 4 - total volume */
+  for (size_t q = 0; q < n2 * (jpk - 1); ++q) zwrk[q] = c->surf[q % n2] * e3t[q] * c->tmask[q];
+  const double zvol_tot = gsum(c, zwrk, jpk - 1, c->tmask_h);
+  wfree(z2d0); wfree(z2d1); wfree(zwrk);
+  double *o = c->hsb_out;
+  o[0] = c->frc_v; o[1] = c->frc_t; o[2] = c->frc_s; o[3] = c->frc_wn_t; o[4] = c->frc_wn_s;
+  o[5] = zdiff_v1; o[6] = zdiff_v2; o[7] = zdiff_hc; o[8] = zdiff_sc; o[9] = zdiff_hc1; o[10] = zdiff_sc1;
+  o[11] = zerr_hc1; o[12] = zerr_sc1; o[13] = zvol_tot; o[14] = c->surf_tot; o[15] = 0.0;
+  if (out) memcpy(out, o, NEMO_HSB_N * sizeof(double));
+  return NEMO_OK;
+}
+
+/* the last model step's stp_ctl and dia_hsb */
+int ora_stp_ctl_last(const ora_ctx *c, double *zmax, int *loc, int *kindic) {
+  if (zmax) memcpy(zmax, c->ctl_zmax, sizeof(c->ctl_zmax));
+  if (loc) memcpy(loc, c->ctl_loc, sizeof(c->ctl_loc));
+  if (kindic) *kindic = c->ctl_kindic;
+  return NEMO_OK;
+}
+int ora_dia_hsb_last(const ora_ctx *c, double *out) {
+  if (!c->hsb_on) return NEMO_ERR_STATE;
+  memcpy(out, c->hsb_out, sizeof(c->hsb_out));
+  return NEMO_OK;
+}
+
 /* ---------------------------------------------------------- one hot-path step */
 /* step.F90:194-257 on the bound fields: dyn_spg_ts, tsa = 0, tra_adv (transports
  * + FCT), tra_ldf (iso or lap), tra_zdf. FCT orders from nn_fct_h/v (0 = 2). */
@@ -2810,6 +3057,9 @@ int ora_stp_model(ora_ctx *c, int kt) {
   if (!st) st = ora_tra_nxt(c, kt);
   if (!st) st = ora_dyn_nxt(c, kt);
   if (!st) st = ora_ssh_swp(c, kt);
+  if (!st && c->hsb_on) st = ora_dia_hsb(c, kt, NULL);                  /* step.F90:282 */
+  if (!st && c->f[NEMO_F_SSHN] && c->f[NEMO_F_UN] && c->f[NEMO_F_TSN])  /* :305 */
+    st = ora_stp_ctl(c, kt, c->ctl_zmax, c->ctl_loc, &c->ctl_kindic);
   return st;
 }
 

@@ -64,6 +64,15 @@ int ora_tra_zdf_imp(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
 int ora_tra_zdf(ora_ctx *c, int kt);
 int ora_dyn_spg_ts(ora_ctx *c, int kt);
 int ora_lbc_lnk(ora_ctx *c, double *ptab, int nk, int nl, char cd_nat, double psgn, double pval);
+/* stp_ctl (stpctl.F90:44-194): zmax[NEMO_CTL_N], loc[NEMO_CTL_NLOC], kindic */
+int ora_stp_ctl(ora_ctx *c, int kt, double *zmax, int *loc, int *kindic);
+/* dia_hsb (diahsb.F90): the initial state of the budgets, then one step's budget
+ * terms out[NEMO_HSB_N] (see nemo_gpu_dia_hsb_result) */
+int ora_dia_hsb_init(ora_ctx *c);
+int ora_dia_hsb(ora_ctx *c, int kt, double *out);
+/* stp_ctl and dia_hsb of the last ora_stp_model */
+int ora_stp_ctl_last(const ora_ctx *c, double *zmax, int *loc, int *kindic);
+int ora_dia_hsb_last(const ora_ctx *c, double *out);
 int ora_glob_sum(ora_ctx *c, const double *ptab, int nk, double *out);
 int ora_stp_hotpath(ora_ctx *c, int kt);
 /* Adjoints with respect to the tracer arguments (the coefficients held fixed).

@@ -44,6 +44,11 @@ def lib():
         P("ora_stp_hotpath", [vp, i])
         P("ora_set_poison", [i], None)
         P("ora_set_threads", [i])
+        P("ora_stp_ctl", [vp, i, vp, vp, C.POINTER(i)])
+        P("ora_dia_hsb_init", [vp])
+        P("ora_dia_hsb", [vp, i, vp])
+        P("ora_stp_ctl_last", [vp, vp, vp, C.POINTER(i)])
+        P("ora_dia_hsb_last", [vp, vp])
         P("ora_set_fct_tape", [vp, vp, i])
         P("ora_tra_adv_fct_adj", [vp, i, i, cp, d, vp, vp, vp, vp, vp, vp, i, i, i])
         P("ora_tra_ldf_lap_adj", [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
@@ -192,6 +197,35 @@ class Oracle:
 
     def stp_hotpath(self, kt):
         self._ck(lib().ora_stp_hotpath(self.h, kt), "stp_hotpath")
+
+    # ---------------------------------------------------------------- stp_ctl, dia_hsb
+    def stp_ctl(self, kt):
+        """(zmax[6], loc[11], kindic) of stpctl.F90:112-184 on the bound fields"""
+        z = np.zeros(_ffi.NEMO_CTL_N)
+        loc = np.zeros(_ffi.NEMO_CTL_NLOC, dtype=np.int32)
+        k = C.c_int(0)
+        self._ck(lib().ora_stp_ctl(self.h, kt, _p(z), loc.ctypes.data, C.byref(k)), "stp_ctl")
+        return z, loc, k.value
+
+    def stp_ctl_last(self):
+        z = np.zeros(_ffi.NEMO_CTL_N)
+        loc = np.zeros(_ffi.NEMO_CTL_NLOC, dtype=np.int32)
+        k = C.c_int(0)
+        self._ck(lib().ora_stp_ctl_last(self.h, _p(z), loc.ctypes.data, C.byref(k)), "stp_ctl_last")
+        return z, loc, k.value
+
+    def dia_hsb_init(self):
+        self._ck(lib().ora_dia_hsb_init(self.h), "dia_hsb_init")
+
+    def dia_hsb(self, kt):
+        out = np.zeros(_ffi.NEMO_HSB_N)
+        self._ck(lib().ora_dia_hsb(self.h, kt, _p(out)), "dia_hsb")
+        return out
+
+    def dia_hsb_last(self):
+        out = np.zeros(_ffi.NEMO_HSB_N)
+        self._ck(lib().ora_dia_hsb_last(self.h, _p(out)), "dia_hsb_last")
+        return out
 
     # ---------------------------------------------------------------- adjoint
     def set_fct_tape(self, tape, mode):
