@@ -121,6 +121,23 @@ typedef struct nemo_namelist {
   double rcp;             /* specific heat (eosbn2.F90:1245: 3991.86795711963; 0 = that) */
   int    ln_seos;         /* &nameos: the simplified equation of state (the only one here) */
   double rn_a0, rn_b0, rn_lambda1, rn_lambda2, rn_mu1, rn_mu2, rn_nu; /* &nameos S-EOS  */
+  int    ln_eos80;        /* &nameos: the polynomial EOS-80 equation of state (GYRE's;
+                             exclusive with ln_seos)                                   */
+  /* &namzdf / &namzdf_tke (zdf_phy with the TKE closure and zdf_evd) */
+  int    ln_zdftke;       /* TKE closure for avt, avm (zdftke.F90)                     */
+  int    ln_zdfevd;       /* enhanced vertical diffusion where unstable (zdfevd.F90)   */
+  int    nn_evdm;         /*   on tracers (0) or tracers and momentum (1)              */
+  double rn_evd;          /*   mixing coefficient [m2/s]                               */
+  double rn_avm0, rn_avt0;/* background viscosity and diffusivity [m2/s] (nn_avb = 0)  */
+  double rn_ediff, rn_ediss, rn_ebb, rn_emin, rn_emin0, rn_bshear; /* TKE coefficients */
+  int    nn_pdl;          /* Prandtl number a function of Ri (1) or not (0)           */
+  int    nn_mxl;          /* mixing length: 0..3                                       */
+  int    ln_mxl0;         /* surface mixing length from the wind stress               */
+  double rn_mxl0;         /* surface mixing length minimum (ln_mxl0 = 0)              */
+  int    ln_lc;           /* Langmuir cells (Axell 2002)                               */
+  double rn_lc;
+  int    nn_etau;         /* tke penetration below the mixed layer: 0 only here        */
+  int    ln_drg_tke;      /* friction as TKE boundary condition (ln_drg): 0 only here */
 } nemo_namelist;
 
 /* ------------------------------------------------------- module-global fields
@@ -199,6 +216,14 @@ enum nemo_field_id {
   NEMO_F_HMLD,                         /* [S]                                         */
   /* lateral eddy viscosity at T- and F-points (ldfdyn.F90 ahmt, ahmf, masked) */
   NEMO_F_AHMT, NEMO_F_AHMF,            /* [T]                                         */
+  /* vertical physics (zdf_oce.F90, zdftke.F90): the vertical eddy viscosity avm, the
+   * turbulent closure's coefficients avm_k, avt_k, the turbulent kinetic energy en
+   * and its dissipation dissl (restart fields), the now Brunt-Vaisala frequency rn2
+   * (the before one is NEMO_F_RN2B), the wind-stress module taum (sbc_oce.F90) and
+   * the sea-ice fraction fr_i (unbound = 0) */
+  NEMO_F_AVM, NEMO_F_AVM_K, NEMO_F_AVT_K, NEMO_F_EN, NEMO_F_DISSL, /* [T]            */
+  NEMO_F_RN2,                          /* [T]                                         */
+  NEMO_F_TAUM, NEMO_F_FR_I,            /* [S]                                         */
   NEMO_F_COUNT
 };
 

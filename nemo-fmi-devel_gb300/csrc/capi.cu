@@ -17,6 +17,7 @@
 #include "../../include/nemo_gpu.h"
 #include "adj.h"
 #include "step.h"
+#include "eos80.h"
 #include "launch.h"
 
 using namespace nemo;
@@ -90,6 +91,11 @@ struct nemo_ctx {
   float* spg_ff = nullptr;  // mixed form: compensated sub-step sums, 10 x nmem x n2
   unsigned int* bar_mem = nullptr;  // count, gen
   int* err_flag = nullptr;
+  // EOS-80 tables (eos80.h): raw FP64 [3][4][7][7]; FP32 re-expanded about s0 =
+  // sqrt((35 + 20) / 40), and the density at (35 psu, 0 degC, 0 m)
+  double* e80_raw = nullptr;
+  float* e80_tay = nullptr;
+  double e80_s0 = 0.0, e80_rho0 = 0.0;
   // stp_ctl (block partials, per-member results, the blow-up flag) and dia_hsb
   double* ctl_part = nullptr;
   double* ctl_out = nullptr;
@@ -263,6 +269,9 @@ size_t field_numel(const nemo_ctx* c, int id) {
     case NEMO_F_GDEPT_N: case NEMO_F_GDEPW_N: return (size_t)c->n3;
     case NEMO_F_SBC_TSC: case NEMO_F_SBC_TSC_B: return 2 * (size_t)c->n2;
     case NEMO_F_QSR_HC: case NEMO_F_QSR_HC_B: return (size_t)c->n3;
+    case NEMO_F_RHD: case NEMO_F_RHOP: case NEMO_F_RN2B: case NEMO_F_AHMT: case NEMO_F_AHMF: return (size_t)c->n3;
+    case NEMO_F_AVM: case NEMO_F_AVM_K: case NEMO_F_AVT_K: case NEMO_F_EN: case NEMO_F_DISSL: case NEMO_F_RN2:
+      return (size_t)c->n3;
     default: break;
   }
   if (id >= NEMO_F_SSHB) return (size_t)c->n2;
@@ -1112,6 +1121,9 @@ EosArgs<T> eos_args(const nemo_ctx* c, int what) {
   a.rau0 = (T)nm.rau0; a.r1_rau0 = (T)(1.0 / nm.rau0); a.grav = (T)nm.grav;
   a.gdept = (const T*)c->f[NEMO_F_GDEPT_N]; a.gdepw = (const T*)c->f[NEMO_F_GDEPW_N];
   a.what = what;
+  a.eos80 = nm.ln_eos80;
+  a.e80_raw = c->e80_raw; a.e80_tay = c->e80_tay;
+  a.e80_s0 = (float)c->e80_s0; a.e80_rho0 = (float)c->e80_rho0; a.e80_anom = (float)(c->e80_rho0 - nm.rau0);
   return a;
 }
 
@@ -1138,8 +1150,8 @@ int run_dyn_hpg(nemo_ctx* c) {
 // z-coordinate with full steps
 bool hpg_on(const nemo_ctx* c) {
   const nemo_namelist& nm = c->nam;
-  return c->f[NEMO_F_RHD] && c->f[NEMO_F_RHOP] && c->f[NEMO_F_GDEPT_N] && nm.ln_seos && !nm.ln_zps && !nm.ln_sco &&
-         !nm.ln_isfcav;
+  return c->f[NEMO_F_RHD] && c->f[NEMO_F_RHOP] && c->f[NEMO_F_GDEPT_N] && (nm.ln_seos || nm.ln_eos80) &&
+         !nm.ln_zps && !nm.ln_sco && !nm.ln_isfcav;
 }
 
 // the model step's iso-neutral slopes from the before tracers (step.F90:127-150):
@@ -1147,7 +1159,7 @@ bool hpg_on(const nemo_ctx* c) {
 // field of the chain bound
 bool slopes_on(const nemo_ctx* c) {
   const nemo_namelist& nm = c->nam;
-  if (!nm.ln_seos || !nm.ln_traldf_iso || nm.ln_zps || nm.ln_sco || nm.ln_isfcav) return false;
+  if (!(nm.ln_seos || nm.ln_eos80) || !nm.ln_traldf_iso || nm.ln_zps || nm.ln_sco || nm.ln_isfcav) return false;
   for (int id : {NEMO_F_RN2B, NEMO_F_RHD, NEMO_F_GDEPT_N, NEMO_F_GDEPW_N, NEMO_F_NMLN, NEMO_F_HMLP, NEMO_F_HMLPT,
                  NEMO_F_USLP, NEMO_F_VSLP, NEMO_F_WSLPI, NEMO_F_WSLPJ, NEMO_F_AVT})
     if (!c->f[id]) return false;
@@ -1381,6 +1393,42 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
 // ================================================================== C ABI
 extern "C" {
 
+// The EOS-80 tables on the device. FP32 evaluates each polynomial re-expanded in
+// s' = zs - s0 about the reference salinity's s0 = sqrt((35 + 20) / 40), with the
+// density's constant term (its value at 35 psu, 0 degC, 0 m) kept apart: in the
+// monomial basis about zs = 0 the terms reach ~900 kg/m3 and cancel to the density,
+// so FP32 would lose the density anomaly (~1e-4 kg/m3 against neighbour differences
+// of 1e-3..1e-1); about s0 the terms are of the size of the anomaly itself. The
+// re-expansion is exact in FP64 (binomial sums) and then rounded to FP32.
+int upload_eos80(nemo_ctx* c) {
+  static const double raw[3][4][7][7] = NEMO_EOS80_TABLE;
+  const double s0 = std::sqrt((35.0 + NEMO_EOS80_RDELTAS) * NEMO_EOS80_R1_S0);
+  std::vector<float> tay(3 * 4 * 49, 0.0f);
+  double binom[7][7] = {};
+  for (int n = 0; n < 7; ++n) {
+    binom[n][0] = 1.0;
+    for (int r = 1; r <= n; ++r) binom[n][r] = binom[n - 1][r - 1] + (r <= n - 1 ? binom[n - 1][r] : 0.0);
+  }
+  for (int t = 0; t < 3; ++t)
+    for (int k = 0; k < 4; ++k)
+      for (int j = 0; j < 7; ++j)
+        for (int ip = 0; ip < 7; ++ip) {
+          double v = 0.0;
+          for (int i = ip; i < 7; ++i) v += raw[t][k][i][j] * binom[i][ip] * std::pow(s0, i - ip);
+          tay[((t * 4 + k) * 7 + ip) * 7 + j] = (float)v;
+        }
+  // the density at (s' = 0, zt = 0, zh = 0): the constant term of the surface table
+  double rho0 = 0.0;
+  for (int i = 0; i < 7; ++i) rho0 += raw[0][0][i][0] * std::pow(s0, i);
+  c->e80_s0 = s0;
+  c->e80_rho0 = rho0;
+  if (cudaMalloc(&c->e80_raw, sizeof(raw)) != cudaSuccess) return NEMO_ERR_NOMEM;
+  if (cudaMalloc(&c->e80_tay, tay.size() * sizeof(float)) != cudaSuccess) return NEMO_ERR_NOMEM;
+  cudaMemcpy(c->e80_raw, raw, sizeof(raw), cudaMemcpyHostToDevice);
+  cudaMemcpy(c->e80_tay, tay.data(), tay.size() * sizeof(float), cudaMemcpyHostToDevice);
+  return NEMO_OK;
+}
+
 // The sub-step kernel and its grid: one block per 32 x 8 tile, at most all
 // co-resident. The mixed form with a linear free surface and the ENE/MIX scheme runs
 // k_spg_p2_ene when no block then owns more than P2H_MAXT tiles; otherwise
@@ -1496,6 +1544,8 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
   cudaMemset(c->bar_mem, 0, 2 * sizeof(unsigned int));
   cudaMemset(c->err_flag, 0, sizeof(int));
   select_p2(c);
+  if (nam->ln_eos80 && nam->ln_seos) return bad(NEMO_ERR_ARG);  // eos_init: exactly one equation of state
+  if (nam->ln_eos80 && upload_eos80(c)) return bad(NEMO_ERR_NOMEM);
   c->ctl_nblk = 2 * c->nsm;
   if (cudaMalloc(&c->ctl_part, (size_t)c->ctl_nblk * c->nmem * CTL_REC * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&c->ctl_out, (size_t)c->nmem * 32 * sizeof(double)) != cudaSuccess ||
@@ -1537,6 +1587,7 @@ int nemo_gpu_destroy(nemo_ctx* c) {
   cudaFree(c->d_wgt1); cudaFree(c->d_wgt2); cudaFree(c->d_wgtf);
   cudaFree(c->bar_mem); cudaFree(c->err_flag);
   cudaFree(c->ctl_part); cudaFree(c->ctl_out); cudaFree(c->ctl_flag);
+  cudaFree(c->e80_raw); cudaFree(c->e80_tay);
   cudaFree(c->hsb_mem); cudaFree(c->hsb_part); cudaFree(c->hsb_state); cudaFree(c->hsb_out);
   cudaFree(c->gs_part); cudaFree(c->gs_out);
   for (auto e : c->tev)
@@ -1893,8 +1944,8 @@ int nemo_gpu_dyn_ldf_lap(nemo_ctx* c, int kt, const void* pub, const void* pvb, 
 
 static int eos_check(nemo_ctx* c, const char* what) {
   if (!c) return NEMO_ERR_ARG;
-  if (!c->nam.ln_seos)
-    return fail(c, NEMO_ERR_UNSUPPORTED, "%s: only the simplified equation of state (ln_seos) is included", what);
+  if (!c->nam.ln_seos && !c->nam.ln_eos80)
+    return fail(c, NEMO_ERR_UNSUPPORTED, "%s: the simplified (ln_seos) or EOS-80 (ln_eos80) equation of state", what);
   if (join_copies(c)) return NEMO_ERR_CUDA;
   return NEMO_OK;
 }

@@ -483,6 +483,95 @@ __global__ void k_tra_qsr(Dom<T> d, QsrArgs<T> a) {
 // eos_insitu (eosbn2.F90:276-292), eos_insitu_pot (:440-462), rab_3d (:645-661)
 // with np_seos, and bn2 (:889-933), one point per thread, each expression in the
 // reference's association.
+// ---- EOS-80. FP64: one power k of the depth of a table in the reference's
+// association (eosbn2.F90:242-265): acc = C(0,D); for j = D-1 .. 0,
+// acc = (acc*zt + H_j*zs) + C(0,j), H_j = (..(C(n,j)*zs + C(n-1,j))*zs .. + C(1,j)),
+// n = D - j. C points at [i][j] (7 x 7) of that k.
+template <int D>
+__device__ __forceinline__ double e80_zn(const double* __restrict__ C, double zt, double zs) {
+  double acc = __ldg(C + D);
+#pragma unroll
+  for (int j = D - 1; j >= 0; --j) {
+    const int n = D - j;
+    double h = __ldg(C + n * 7 + j);
+#pragma unroll
+    for (int i = n - 1; i >= 1; --i) h = h * zs + __ldg(C + i * 7 + j);
+    acc = (acc * zt + h * zs) + __ldg(C + j);
+  }
+  return acc;
+}
+// table t (0 EOS: degrees 6 4 2 1 in zt; 1 ALP, 2 BET: 5 3 1 0), all depth powers
+template <int D0, int D1, int D2, int D3>
+__device__ __forceinline__ double e80_poly(const double* __restrict__ tab, double zt, double zs, double zh,
+                                           double& zn0) {
+  const double z3 = e80_zn<D3>(tab + 3 * 49, zt, zs), z2 = e80_zn<D2>(tab + 2 * 49, zt, zs);
+  const double z1 = e80_zn<D1>(tab + 49, zt, zs);
+  zn0 = e80_zn<D0>(tab, zt, zs);
+  return ((z3 * zh + z2) * zh + z1) * zh + zn0;
+}
+// FP32: the re-expanded table (in s' = zs - s0), Horner in s', zt, zh; skip00 leaves
+// out the constant term of the surface part (the density's, added apart)
+template <int D>
+__device__ __forceinline__ float e80_q32(const float* __restrict__ C, float zt, float sp, bool skip00) {
+  float acc = 0.f;
+#pragma unroll
+  for (int j = D; j >= 0; --j) {
+    float h = 0.f;
+#pragma unroll
+    for (int i = D - j; i >= 0; --i) h = h * sp + ((skip00 && i == 0 && j == 0) ? 0.f : __ldg(C + i * 7 + j));
+    acc = acc * zt + h;
+  }
+  return acc;
+}
+template <int D0, int D1, int D2, int D3>
+__device__ __forceinline__ float e80_poly32(const float* __restrict__ tab, float zt, float sp, float zh,
+                                            bool skip00, float& zn0) {
+  const float z3 = e80_q32<D3>(tab + 3 * 49, zt, sp, false), z2 = e80_q32<D2>(tab + 2 * 49, zt, sp, false);
+  const float z1 = e80_q32<D1>(tab + 49, zt, sp, false);
+  zn0 = e80_q32<D0>(tab, zt, sp, skip00);
+  return ((z3 * zh + z2) * zh + z1) * zh + zn0;
+}
+
+// eos_insitu, eos_insitu_pot and rab_3d with EOS-80 (eosbn2.F90:236-270, :400-436,
+// :588-642) at point q (temperature qt, salinity qs)
+template <class T>
+__device__ __forceinline__ void eos80_point(const EosArgs<T>& a, long q, long qt, long qs, T ztm) {
+  constexpr double r1_Z0 = 1.e-4, r1_T0 = 1.0 / 40.0, r1_S0 = 1.0 / 40.0, rdeltaS = 20.0;
+  const T dep = a.what == 2 ? a.gdept[q] : a.pdep[q];
+  if constexpr (sizeof(T) == 8) {
+    const double zh = dep * r1_Z0, zt = a.pts[qt] * r1_T0;
+    const double zs = sqrt(fabs(a.pts[qs] + rdeltaS) * r1_S0);
+    double zn0;
+    if (a.what == 2) {
+      double zn = e80_poly<5, 3, 1, 0>(a.e80_raw + 196, zt, zs, zh, zn0);
+      a.pab[qt] = zn * a.r1_rau0 * ztm;
+      zn = e80_poly<5, 3, 1, 0>(a.e80_raw + 392, zt, zs, zh, zn0);
+      a.pab[qs] = zn / zs * a.r1_rau0 * ztm;
+    } else {
+      const double zn = e80_poly<6, 4, 2, 1>(a.e80_raw, zt, zs, zh, zn0);
+      if (a.what == 1) a.prhop[q] = zn0 * ztm;
+      a.prd[q] = (zn * a.r1_rau0 - 1.0) * ztm;
+    }
+  } else {
+    const float zh = dep * (float)r1_Z0, zt = a.pts[qt] * (float)r1_T0;
+    const float x = fabsf(a.pts[qs] + (float)rdeltaS) * (float)r1_S0;
+    const float zs = sqrtf(x);
+    const float sp = (x - a.e80_s0 * a.e80_s0) / (zs + a.e80_s0);  // zs - s0 without cancellation
+    float zn0;
+    if (a.what == 2) {
+      float zn = e80_poly32<5, 3, 1, 0>(a.e80_tay + 196, zt, sp, zh, false, zn0);
+      a.pab[qt] = zn * a.r1_rau0 * ztm;
+      zn = e80_poly32<5, 3, 1, 0>(a.e80_tay + 392, zt, sp, zh, false, zn0);
+      a.pab[qs] = zn / zs * a.r1_rau0 * ztm;
+    } else {
+      // the anomaly of the density about its value at (35 psu, 0 degC, 0 m) first
+      const float zn = e80_poly32<6, 4, 2, 1>(a.e80_tay, zt, sp, zh, true, zn0);
+      if (a.what == 1) a.prhop[q] = (zn0 + a.e80_rho0) * ztm;
+      a.prd[q] = ((zn + a.e80_anom) * a.r1_rau0) * ztm;
+    }
+  }
+}
+
 template <class T>
 __global__ void k_eos(Dom<T> d, EosArgs<T> a) {
   const PtIdx c = pt_index(d);
@@ -491,6 +580,10 @@ __global__ void k_eos(Dom<T> d, EosArgs<T> a) {
   const long qt = 2 * (long)c.m * d.n3 + c.q;     // temperature of (jpi,jpj,jpk,2)
   const long qs = qt + d.n3;
   const ColInfo ci = d.ci[c.ij];
+  if (a.eos80 && a.what != 3) {
+    eos80_point(a, q, qt, qs, tmsk<T>(ci, c.k));
+    return;
+  }
   if (a.what == 3) {
     if (c.k < 2) return;
     const T zrw = (a.gdepw[q] - a.gdept[q]) / (a.gdept[q - d.n2] - a.gdept[q]);

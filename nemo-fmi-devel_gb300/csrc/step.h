@@ -56,6 +56,14 @@ struct EosArgs {
   T *prd, *prhop, *pab, *pn2;
   T a0, b0, lambda1, lambda2, mu1, mu2, nu, rau0, r1_rau0, grav;
   int what;  // 0 eos_insitu, 1 eos_insitu_pot, 2 rab_3d, 3 bn2
+  // EOS-80 (ln_eos80): FP64 evaluates the reference's table in its association
+  // (e80_raw: [table][k][i][j], eos80.h); FP32 the same polynomials re-expanded about
+  // the salinity 35 (e80_tay, same layout, in s' = zs - e80_s0), the density's
+  // constant term kept apart (e80_rho0, and e80_anom = e80_rho0 - rau0)
+  int eos80;
+  const double* e80_raw;
+  const float* e80_tay;
+  float e80_s0, e80_rho0, e80_anom;
 };
 
 template <class T>

@@ -56,13 +56,26 @@ class Namelist(C.Structure):
                 ("ln_traqsr", C.c_int), ("rn_abs", C.c_double), ("rn_si0", C.c_double), ("rn_si1", C.c_double),
                 ("rcp", C.c_double), ("ln_seos", C.c_int), ("rn_a0", C.c_double), ("rn_b0", C.c_double),
                 ("rn_lambda1", C.c_double), ("rn_lambda2", C.c_double), ("rn_mu1", C.c_double),
-                ("rn_mu2", C.c_double), ("rn_nu", C.c_double)]
+                ("rn_mu2", C.c_double), ("rn_nu", C.c_double), ("ln_eos80", C.c_int),
+                ("ln_zdftke", C.c_int), ("ln_zdfevd", C.c_int), ("nn_evdm", C.c_int), ("rn_evd", C.c_double),
+                ("rn_avm0", C.c_double), ("rn_avt0", C.c_double), ("rn_ediff", C.c_double),
+                ("rn_ediss", C.c_double), ("rn_ebb", C.c_double), ("rn_emin", C.c_double),
+                ("rn_emin0", C.c_double), ("rn_bshear", C.c_double), ("nn_pdl", C.c_int), ("nn_mxl", C.c_int),
+                ("ln_mxl0", C.c_int), ("rn_mxl0", C.c_double), ("ln_lc", C.c_int), ("rn_lc", C.c_double),
+                ("nn_etau", C.c_int), ("ln_drg_tke", C.c_int)]
 
 
 # members a namelist may leave out (&namtra_qsr of namelist_ref; rcp 0 selects 3991.86795711963)
 NAMELIST_DEFAULTS = {"ln_traqsr": 0, "rn_abs": 0.58, "rn_si0": 0.35, "rn_si1": 23.0, "rcp": 0.0,
                      "ln_seos": 0, "rn_a0": 1.6550e-1, "rn_b0": 7.6554e-1, "rn_lambda1": 5.9520e-2,
-                     "rn_lambda2": 7.4914e-4, "rn_mu1": 1.4970e-4, "rn_mu2": 1.1090e-5, "rn_nu": 2.4341e-3}
+                     "rn_lambda2": 7.4914e-4, "rn_mu1": 1.4970e-4, "rn_mu2": 1.1090e-5, "rn_nu": 2.4341e-3,
+                     "ln_eos80": 0,
+                     # &namzdf and &namzdf_tke of namelist_ref, with GYRE's namelist_cfg
+                     # (TKE, EVD on tracers and momentum, rn_evd = 100, nn_etau = 0)
+                     "ln_zdftke": 0, "ln_zdfevd": 0, "nn_evdm": 1, "rn_evd": 100.0, "rn_avm0": 1.2e-4,
+                     "rn_avt0": 1.2e-5, "rn_ediff": 0.1, "rn_ediss": 0.7, "rn_ebb": 67.83, "rn_emin": 1.e-6,
+                     "rn_emin0": 1.e-4, "rn_bshear": 1.e-20, "nn_pdl": 1, "nn_mxl": 2, "ln_mxl0": 1,
+                     "rn_mxl0": 0.04, "ln_lc": 1, "rn_lc": 0.15, "nn_etau": 0, "ln_drg_tke": 0}
 
 
 def make_desc(dom):

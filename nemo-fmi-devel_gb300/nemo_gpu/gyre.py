@@ -35,9 +35,10 @@ def namelist(**over):
         nvor_scheme=1, nn_een_e3f=0, ln_dynadv_vec=1, ln_sco=0, ln_apr_dyn=0, rn_scal_load=0.0,
         grav=GRAV, rau0=RAU0, nn_fct_h=2, nn_fct_v=2, rn_slpmax=0.01,
         ln_traqsr=1, rn_abs=0.58, rn_si0=0.35, rn_si1=23.0, rcp=RCP,
-        # GYRE selects EOS-80 (not included); the simplified eos of namelist_ref &nameos
+        # GYRE's namelist_cfg selects EOS-80 (ln_eos80 = 1 below for a GYRE run); the
+        # simplified eos of namelist_ref &nameos is the alternative
         ln_seos=0, rn_a0=1.6550e-1, rn_b0=7.6554e-1, rn_lambda1=5.9520e-2, rn_lambda2=7.4914e-4,
-        rn_mu1=1.4970e-4, rn_mu2=1.1090e-5, rn_nu=2.4341e-3)
+        rn_mu1=1.4970e-4, rn_mu2=1.1090e-5, rn_nu=2.4341e-3, ln_eos80=0)
     nam.update(over)
     return nam
 

@@ -13,6 +13,7 @@
  * Compile with -ffp-contract=off so that no multiply-add is fused.
  */
 #include "nemo_oracle.h"
+#include "../nemo-fmi-devel_gb300/csrc/eos80.h"
 
 #include <math.h>
 #include <stdint.h>
@@ -1685,6 +1686,281 @@ int ora_glob_sum(ora_ctx *c, const double *ptab, int nk, double *out) {
   return NEMO_OK;
 }
 
+/* ---------------------------------------------------------------- zdf_phy */
+/* zdf_phy (zdfphy.F90:243-291) for the TKE closure: zdf_sh2 (zdfsh2.F90:30-76)
+ * with the closure's avm_k, zdf_tke = tke_tke + tke_avn (zdftke.F90:168-630) for
+ * ln_drg = .false., no ice-shelf cavities and nn_etau = 0 (GYRE), then avt, avm
+ * from the closure on levels 2..jpk-1, zdf_evd (zdfevd.F90:40-121) and avs = avt.
+ * Bound: UB VB UN VN, AVM_K AVT_K AVM AVT (and AVS), EN DISSL (restart fields; a
+ * cold start sets en = rn_emin wmask, dissl = 1e-12), RN2 RN2B, TAUM, GDEPW_N; FR_I
+ * optional (0). The rest-state e3uw/e3vw are the minima of the neighbouring e3w_0
+ * (equal to e3w_0 on full steps, usrdef_zgr.F90:241-242). */
+int ora_zdf_phy(ora_ctx *c, int kt) {
+  (void)kt;
+  const nemo_namelist *nm = &c->nam;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  double *ub = c->f[NEMO_F_UB], *vb = c->f[NEMO_F_VB], *un = c->f[NEMO_F_UN], *vn = c->f[NEMO_F_VN];
+  double *avm_k = c->f[NEMO_F_AVM_K], *avt_k = c->f[NEMO_F_AVT_K], *avm = c->f[NEMO_F_AVM], *avt = c->f[NEMO_F_AVT];
+  double *avs = c->f[NEMO_F_AVS], *en = c->f[NEMO_F_EN], *dissl = c->f[NEMO_F_DISSL];
+  const double *rn2 = c->f[NEMO_F_RN2], *rn2b = c->f[NEMO_F_RN2B], *taum = c->f[NEMO_F_TAUM];
+  const double *pdepw = c->f[NEMO_F_GDEPW_N], *fr_i = c->f[NEMO_F_FR_I];
+  if (!ub || !vb || !un || !vn || !avm_k || !avt_k || !avm || !avt || !en || !dissl || !rn2 || !rn2b || !taum || !pdepw)
+    return NEMO_ERR_UNBOUND;
+  if (!nm->ln_zdftke || nm->nn_etau != 0 || nm->ln_drg_tke || nm->ln_isfcav || !nm->ln_linssh)
+    return NEMO_ERR_UNSUPPORTED;
+  const double *e3t = fld(c, NEMO_F_E3T_N), *e3w = fld(c, NEMO_F_E3W_N);
+  const double *tmask = c->tmask, *wmask = c->wmask, *umask = c->umask, *vmask = c->vmask;
+  const double rdt = nm->rn_rdt, rau0 = nm->rau0, grav = nm->grav;
+  const double rpi = 3.141592653589793, vkarmn = 0.4, rsmall = 0.5 * 2.220446049250313e-16;
+  const double ri_cri = 2.0 / (2.0 + nm->rn_ediss / nm->rn_ediff);
+  const double rmxl_min = 1.e-6 / (nm->rn_ediff * sqrt(nm->rn_emin));
+  const double rn_mxl0 = nm->ln_mxl0 ? rmxl_min : nm->rn_mxl0;
+  double *sh2 = zalloc(n3), *apdlr = zalloc(n3), *zdiag = zalloc(n3), *zd_up = zalloc(n3), *zd_lw = zalloc(n3);
+  double *zpelc = zalloc(n3), *zmxlm = zalloc(n3), *zmxld = zalloc(n3), *zhlc = zalloc(n2), *zfr_i = zalloc(n2);
+  double *zsh2u = zalloc(n2), *zsh2v = zalloc(n2);
+#define E3UW(ji, jj, jk) dmin(e3w[I3(ji, jj, jk)], e3w[I3((ji) + 1, jj, jk)])
+#define E3VW(ji, jj, jk) dmin(e3w[I3(ji, jj, jk)], e3w[I3(ji, (jj) + 1, jk)])
+#define WUM(ji, jj, jk) (umask[I3(ji, jj, jk)] * umask[I3(ji, jj, (jk) - 1)])
+#define WVM(ji, jj, jk) (vmask[I3(ji, jj, jk)] * vmask[I3(ji, jj, (jk) - 1)])
+  /* zdf_sh2 (zdfsh2.F90:57-74), p_avm = avm_k */
+  for (int jk = 2; jk <= jpk - 1; ++jk) {
+    for (int jj = 1; jj <= jpj - 1; ++jj)
+      for (int ji = 1; ji <= jpi - 1; ++ji) {
+        zsh2u[I2(ji, jj)] = (avm_k[I3(ji + 1, jj, jk)] + avm_k[I3(ji, jj, jk)]) *
+                            (un[I3(ji, jj, jk - 1)] - un[I3(ji, jj, jk)]) *
+                            (ub[I3(ji, jj, jk - 1)] - ub[I3(ji, jj, jk)]) / (E3UW(ji, jj, jk) * E3UW(ji, jj, jk)) *
+                            WUM(ji, jj, jk);
+        zsh2v[I2(ji, jj)] = (avm_k[I3(ji, jj + 1, jk)] + avm_k[I3(ji, jj, jk)]) *
+                            (vn[I3(ji, jj, jk - 1)] - vn[I3(ji, jj, jk)]) *
+                            (vb[I3(ji, jj, jk - 1)] - vb[I3(ji, jj, jk)]) / (E3VW(ji, jj, jk) * E3VW(ji, jj, jk)) *
+                            WVM(ji, jj, jk);
+      }
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji)
+        sh2[I3(ji, jj, jk)] =
+            0.25 * ((zsh2u[I2(ji - 1, jj)] + zsh2u[I2(ji, jj)]) * (2. - umask[I3(ji - 1, jj, jk)] * umask[I3(ji, jj, jk)]) +
+                    (zsh2v[I2(ji, jj - 1)] + zsh2v[I2(ji, jj)]) * (2. - vmask[I3(ji, jj - 1, jk)] * vmask[I3(ji, jj, jk)]));
+  }
+  /* ---- tke_tke (zdftke.F90:168-440), p_avm = avm_k, p_avt = avt_k */
+  const double zbbrau = nm->rn_ebb / rau0, zfact1 = -.5 * rdt, zfact2 = 1.5 * rdt * nm->rn_ediss;
+  const double zfact3 = 0.5 * nm->rn_ediss;
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji)
+      en[I3(ji, jj, 1)] = dmax(nm->rn_emin0, zbbrau * taum[I2(ji, jj)]) * tmask[I3(ji, jj, 1)];
+  if (nm->ln_lc) {  /* Langmuir circulation (:243-311) */
+    const double zrhoa = 1.22, zcdrag = 1.5e-3;
+    for (size_t p = 0; p < n2; ++p) zpelc[p] = dmax(rn2b[p], 0.) * pdepw[p] * e3w[p];
+    for (int jk = 2; jk <= jpk; ++jk)
+      for (size_t p = 0; p < n2; ++p) {
+        const size_t q = p + n2 * (jk - 1);
+        zpelc[q] = zpelc[q - n2] + dmax(rn2b[q], 0.) * pdepw[q] * e3w[q];
+      }
+    double zcof = 0.5 * 0.016 * 0.016 / (zrhoa * zcdrag);
+    for (size_t p = 0; p < n2; ++p) {
+      int imlc = c->mbkt[p] + 1;
+      for (int jk = jpk - 1; jk >= 2; --jk) {
+        const double zus = zcof * taum[p];
+        if (zpelc[p + n2 * (jk - 1)] > zus) imlc = jk;
+      }
+      zhlc[p] = pdepw[p + n2 * (imlc - 1)];
+    }
+    zcof = 0.016 / sqrt(zrhoa * zcdrag);
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t p = I2(ji, jj);
+        const double zus = zcof * sqrt(taum[p]);
+        zfr_i[p] = (1. - 4. * (fr_i ? fr_i[p] : 0.)) * zus * zus * zus * tmask[p];
+        if (zfr_i[p] < 0.) zfr_i[p] = 0.;
+      }
+    for (int jk = 2; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          const size_t p = I2(ji, jj), q = I3(ji, jj, jk);
+          if (zfr_i[p] != 0.) {
+            if (pdepw[q] - zhlc[p] < 0 && wmask[q] != 0.) {
+              const double zwlc = nm->rn_lc * sin(rpi * pdepw[q] / zhlc[p]);
+              en[q] = en[q] + rdt * zfr_i[p] * (zwlc * zwlc * zwlc) / zhlc[p];
+            }
+          }
+        }
+  }
+  if (nm->nn_pdl == 1)  /* (:323-334) */
+    for (int jk = 2; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          const size_t q = I3(ji, jj, jk);
+          const double zri = dmax(rn2b[q], 0.) * avm_k[q] / (sh2[q] + nm->rn_bshear);
+          apdlr[q] = dmax(0.1, ri_cri / dmax(ri_cri, zri));
+        }
+  for (int jk = 2; jk <= jpk - 1; ++jk)  /* matrix and right-hand side (:336-356) */
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t q = I3(ji, jj, jk);
+        const double zcof = zfact1 * tmask[q];
+        const double zzd_up = zcof * dmax(avm_k[q + n2] + avm_k[q], 2.e-5) / (e3t[q] * e3w[q]);
+        const double zzd_lw = zcof * dmax(avm_k[q] + avm_k[q - n2], 2.e-5) / (e3t[q - n2] * e3w[q]);
+        zd_up[q] = zzd_up;
+        zd_lw[q] = zzd_lw;
+        zdiag[q] = 1. - zzd_lw - zzd_up + zfact2 * dissl[q] * wmask[q];
+        en[q] = en[q] + rdt * (sh2[q] - avt_k[q] * rn2[q] + zfact3 * dissl[q] * en[q]) * wmask[q];
+      }
+  for (int jk = 3; jk <= jpk - 1; ++jk)  /* recurrences (:358-390) */
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t q = I3(ji, jj, jk);
+        zdiag[q] = zdiag[q] - zd_lw[q] * zd_up[q - n2] / zdiag[q - n2];
+      }
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji)
+      zd_lw[I3(ji, jj, 2)] = en[I3(ji, jj, 2)] - zd_lw[I3(ji, jj, 2)] * en[I3(ji, jj, 1)];
+  for (int jk = 3; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t q = I3(ji, jj, jk);
+        zd_lw[q] = en[q] - zd_lw[q] / zdiag[q - n2] * zd_lw[q - n2];
+      }
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji)
+      en[I3(ji, jj, jpk - 1)] = zd_lw[I3(ji, jj, jpk - 1)] / zdiag[I3(ji, jj, jpk - 1)];
+  for (int jk = jpk - 2; jk >= 2; --jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t q = I3(ji, jj, jk);
+        en[q] = (zd_lw[q] - zd_up[q] * en[q + n2]) / zdiag[q];
+      }
+  for (int jk = 2; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t q = I3(ji, jj, jk);
+        en[q] = dmax(en[q], nm->rn_emin) * wmask[q];
+      }
+  /* ---- tke_avn (zdftke.F90:443-630) */
+  for (size_t q = 0; q < n3; ++q) { zmxlm[q] = rmxl_min; zmxld[q] = rmxl_min; }
+  if (nm->ln_mxl0) {
+    const double zraug = vkarmn * 2.e5 / (rau0 * grav);
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji)
+        zmxlm[I2(ji, jj)] = dmax(rn_mxl0, zraug * taum[I2(ji, jj)] * tmask[I2(ji, jj)]);
+  } else {
+    for (size_t p = 0; p < n2; ++p) zmxlm[p] = rn_mxl0;
+  }
+  for (int jk = 2; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t q = I3(ji, jj, jk);
+        const double zrn2 = dmax(rn2[q], rsmall);
+        zmxlm[q] = dmax(rmxl_min, sqrt(2. * en[q] / zrn2));
+      }
+  for (size_t p = 0; p < n2; ++p) { zmxld[p] = zmxlm[p]; zmxld[p + n2 * (jpk - 1)] = rmxl_min; }
+  switch (nm->nn_mxl) {
+    case 0:
+      for (int jk = 2; jk <= jpk - 1; ++jk)
+        for (int jj = 2; jj <= jpj - 1; ++jj)
+          for (int ji = 2; ji <= jpi - 1; ++ji) {
+            const size_t p = I2(ji, jj), q = I3(ji, jj, jk);
+            const double a = pdepw[q] - pdepw[p + n2 * (c->mikt[p] - 1)], b = pdepw[p + n2 * c->mbkt[p]] - pdepw[q];
+            const double zemxl = dmin(dmin(a, zmxlm[q]), b);
+            zmxlm[q] = zemxl * wmask[q] + dmin(zmxlm[q], e3w[q]) * (1 - wmask[q]);
+            zmxld[q] = zemxl * wmask[q] + dmin(zmxlm[q], e3w[q]) * (1 - wmask[q]);
+          }
+      break;
+    case 1:
+      for (int jk = 2; jk <= jpk - 1; ++jk)
+        for (int jj = 2; jj <= jpj - 1; ++jj)
+          for (int ji = 2; ji <= jpi - 1; ++ji) {
+            const size_t q = I3(ji, jj, jk);
+            const double zemxl = dmin(e3w[q], zmxlm[q]);
+            zmxlm[q] = zemxl;
+            zmxld[q] = zemxl;
+          }
+      break;
+    case 2:
+      for (int jk = 2; jk <= jpk - 1; ++jk)
+        for (int jj = 2; jj <= jpj - 1; ++jj)
+          for (int ji = 2; ji <= jpi - 1; ++ji) {
+            const size_t q = I3(ji, jj, jk);
+            zmxlm[q] = dmin(zmxlm[q - n2] + e3t[q - n2], zmxlm[q]);
+          }
+      for (int jk = jpk - 1; jk >= 2; --jk)
+        for (int jj = 2; jj <= jpj - 1; ++jj)
+          for (int ji = 2; ji <= jpi - 1; ++ji) {
+            const size_t q = I3(ji, jj, jk);
+            const double zemxl = dmin(zmxlm[q + n2] + e3t[q + n2], zmxlm[q]);
+            zmxlm[q] = zemxl;
+            zmxld[q] = zemxl;
+          }
+      break;
+    default:  /* 3 */
+      for (int jk = 2; jk <= jpk - 1; ++jk)
+        for (int jj = 2; jj <= jpj - 1; ++jj)
+          for (int ji = 2; ji <= jpi - 1; ++ji) {
+            const size_t q = I3(ji, jj, jk);
+            zmxld[q] = dmin(zmxld[q - n2] + e3t[q - n2], zmxlm[q]);
+          }
+      for (int jk = jpk - 1; jk >= 2; --jk)
+        for (int jj = 2; jj <= jpj - 1; ++jj)
+          for (int ji = 2; ji <= jpi - 1; ++ji) {
+            const size_t q = I3(ji, jj, jk);
+            zmxlm[q] = dmin(zmxlm[q + n2] + e3t[q + n2], zmxlm[q]);
+          }
+      for (int jk = 2; jk <= jpk - 1; ++jk)
+        for (int jj = 2; jj <= jpj - 1; ++jj)
+          for (int ji = 2; ji <= jpi - 1; ++ji) {
+            const size_t q = I3(ji, jj, jk);
+            const double zemlm = dmin(zmxld[q], zmxlm[q]), zemlp = sqrt(zmxld[q] * zmxlm[q]);
+            zmxlm[q] = zemlm;
+            zmxld[q] = zemlp;
+          }
+      break;
+  }
+  for (int jk = 1; jk <= jpk - 1; ++jk)  /* avm_k, avt_k, dissl (:610-620), nn_avb = nn_havtb = 0 */
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t q = I3(ji, jj, jk);
+        const double zsqen = sqrt(en[q]);
+        const double zav = nm->rn_ediff * zmxlm[q] * zsqen;
+        avm_k[q] = dmax(zav, nm->rn_avm0) * wmask[q];
+        avt_k[q] = dmax(zav, 1.0 * nm->rn_avt0) * wmask[q];
+        dissl[q] = zsqen / zmxld[q];
+      }
+  if (nm->nn_pdl == 1)
+    for (int jk = 2; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          const size_t q = I3(ji, jj, jk);
+          avt_k[q] = dmax(apdlr[q] * avt_k[q], 1.0 * nm->rn_avt0) * tmask[q];
+        }
+  /* ---- zdf_phy: ocean Kz from the closure (zdfphy.F90:269-291) */
+  for (int jk = 2; jk <= jpk - 1; ++jk)
+    for (size_t p = 0; p < n2; ++p) {
+      const size_t q = p + n2 * (jk - 1);
+      avt[q] = avt_k[q];
+      avm[q] = avm_k[q];
+    }
+  if (nm->ln_zdfevd)  /* zdfevd.F90:76-109 */
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          const size_t q = I3(ji, jj, jk);
+          if (dmin(rn2[q], rn2b[q]) <= -1.e-12) {
+            avt[q] = nm->rn_evd * wmask[q];
+            if (nm->nn_evdm == 1) avm[q] = nm->rn_evd * wmask[q];
+          }
+        }
+  if (avs)
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) avs[I3(ji, jj, jk)] = avt[I3(ji, jj, jk)];
+#undef E3UW
+#undef E3VW
+#undef WUM
+#undef WVM
+  wfree(sh2); wfree(apdlr); wfree(zdiag); wfree(zd_up); wfree(zd_lw); wfree(zpelc); wfree(zmxlm); wfree(zmxld);
+  wfree(zhlc); wfree(zfr_i); wfree(zsh2u); wfree(zsh2v);
+  return NEMO_OK;
+}
+
 /* ---------------------------------------------------------------- stp_ctl */
 /* stp_ctl (stpctl.F90:44-194), the test of extrema (:112-127) and the blow-up
  * conditions (:149-157): zmax = |ssh| max, |U| max (zonal, every point), then the
@@ -2917,8 +3193,51 @@ int ora_dyn_ldf_lap(ora_ctx *c, int kt, const double *pub, const double *pvb, do
 
 /* ------------------------------------------- simplified equation of state */
 /* eos_insitu (eosbn2.F90:276-292), np_seos: levels 1..jpk-1 of every point. */
+/* ---- EOS-80 (np_eos80): the polynomial of eosbn2.F90:236-270 (density), :588-642
+ * (expansion coefficients), written in the reference's association: for one power
+ * k of the depth, acc = C(0,D); then for j = D-1 .. 0, acc = (acc*zt + H_j*zs) +
+ * C(0,j) with H_j = (..(C(n,j)*zs + C(n-1,j))*zs .. + C(1,j)), n = D - j. */
+static const double eos80_c[3][4][7][7] = NEMO_EOS80_TABLE;
+
+static double eos80_zn(int t, int k, int deg, double zt, double zs) {
+  const double (*C)[7] = eos80_c[t][k];
+  double acc = C[0][deg];
+  for (int j = deg - 1; j >= 0; --j) {
+    const int n = deg - j;
+    double h = C[n][j];
+    for (int i = n - 1; i >= 1; --i) h = h * zs + C[i][j];
+    acc = (acc * zt + h * zs) + C[0][j];
+  }
+  return acc;
+}
+/* zn = ((zn3*zh + zn2)*zh + zn1)*zh + zn0 of table t (0 EOS: degrees 6 4 2 1 in zt;
+ * 1 ALP, 2 BET: 5 3 1 0); *zn0 = the surface part */
+static double eos80_poly(int t, double zt, double zs, double zh, double *zn0) {
+  const int d0 = t == 0 ? 6 : 5, d1 = t == 0 ? 4 : 3, d2 = t == 0 ? 2 : 1, d3 = t == 0 ? 1 : 0;
+  const double z3 = eos80_zn(t, 3, d3, zt, zs), z2 = eos80_zn(t, 2, d2, zt, zs);
+  const double z1 = eos80_zn(t, 1, d1, zt, zs), z0 = eos80_zn(t, 0, d0, zt, zs);
+  if (zn0) *zn0 = z0;
+  return ((z3 * zh + z2) * zh + z1) * zh + z0;
+}
+static void eos80_vars(double t, double s, double dep, double *zt, double *zs, double *zh) {
+  *zh = dep * NEMO_EOS80_R1_Z0;
+  *zt = t * NEMO_EOS80_R1_T0;
+  *zs = sqrt(fabs(s + NEMO_EOS80_RDELTAS) * NEMO_EOS80_R1_S0);
+}
+
 int ora_eos_insitu(ora_ctx *c, const double *pts, double *prd, const double *pdep) {
   const nemo_namelist *nm = &c->nam;
+  if (nm->ln_eos80) {  /* eosbn2.F90:236-270 */
+    const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk, nl = (size_t)c->jpi * c->jpj * (c->jpk - 1);
+    const double r1_rau0 = 1.0 / nm->rau0;
+    for (size_t q = 0; q < nl; ++q) {
+      double zt, zs, zh;
+      eos80_vars(pts[q], pts[n3 + q], pdep[q], &zt, &zs, &zh);
+      const double zn = eos80_poly(0, zt, zs, zh, NULL);
+      prd[q] = (zn * r1_rau0 - 1.0) * c->tmask[q];
+    }
+    return NEMO_OK;
+  }
   if (!nm->ln_seos) return NEMO_ERR_UNSUPPORTED;
   const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk, nl = (size_t)c->jpi * c->jpj * (c->jpk - 1);
   const double r1_rau0 = 1.0 / nm->rau0;
@@ -2935,6 +3254,18 @@ int ora_eos_insitu(ora_ctx *c, const double *pts, double *prd, const double *pde
 /* eos_insitu_pot (eosbn2.F90:440-462), np_seos. */
 int ora_eos_insitu_pot(ora_ctx *c, const double *pts, double *prd, double *prhop, const double *pdep) {
   const nemo_namelist *nm = &c->nam;
+  if (nm->ln_eos80) {  /* eosbn2.F90:400-436 (ln_sto_eos off) */
+    const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk, nl = (size_t)c->jpi * c->jpj * (c->jpk - 1);
+    const double r1_rau0 = 1.0 / nm->rau0;
+    for (size_t q = 0; q < nl; ++q) {
+      double zt, zs, zh, zn0;
+      eos80_vars(pts[q], pts[n3 + q], pdep[q], &zt, &zs, &zh);
+      const double zn = eos80_poly(0, zt, zs, zh, &zn0);
+      prhop[q] = zn0 * c->tmask[q];
+      prd[q] = (zn * r1_rau0 - 1.0) * c->tmask[q];
+    }
+    return NEMO_OK;
+  }
   if (!nm->ln_seos) return NEMO_ERR_UNSUPPORTED;
   const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk, nl = (size_t)c->jpi * c->jpj * (c->jpk - 1);
   const double r1_rau0 = 1.0 / nm->rau0;
@@ -2953,8 +3284,23 @@ int ora_eos_insitu_pot(ora_ctx *c, const double *pts, double *prd, double *prhop
 /* rab_3d (eosbn2.F90:645-661), np_seos, at the bound GDEPT_N. */
 int ora_rab_3d(ora_ctx *c, const double *pts, double *pab) {
   const nemo_namelist *nm = &c->nam;
-  if (!nm->ln_seos) return NEMO_ERR_UNSUPPORTED;
   const double *gdept = c->f[NEMO_F_GDEPT_N];
+  if (nm->ln_eos80) {  /* eosbn2.F90:588-642 */
+    if (!gdept) return NEMO_ERR_UNBOUND;
+    const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk, nl = (size_t)c->jpi * c->jpj * (c->jpk - 1);
+    const double r1_rau0 = 1.0 / nm->rau0;
+    for (size_t q = 0; q < nl; ++q) {
+      double zt, zs, zh;
+      eos80_vars(pts[q], pts[n3 + q], gdept[q], &zt, &zs, &zh);
+      const double ztm = c->tmask[q];
+      double zn = eos80_poly(1, zt, zs, zh, NULL);
+      pab[q] = zn * r1_rau0 * ztm;
+      zn = eos80_poly(2, zt, zs, zh, NULL);
+      pab[n3 + q] = zn / zs * r1_rau0 * ztm;
+    }
+    return NEMO_OK;
+  }
+  if (!nm->ln_seos) return NEMO_ERR_UNSUPPORTED;
   if (!gdept) return NEMO_ERR_UNBOUND;
   const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk, nl = (size_t)c->jpi * c->jpj * (c->jpk - 1);
   const double r1_rau0 = 1.0 / nm->rau0;
@@ -3030,7 +3376,7 @@ int ora_stp_model(ora_ctx *c, int kt) {
   if (!c->f[NEMO_F_UA] || !c->f[NEMO_F_VA]) return NEMO_ERR_UNBOUND;
   int st = 0;
   const nemo_namelist *nm = &c->nam;
-  if (nm->ln_seos && nm->ln_traldf_iso && !nm->ln_zps && !nm->ln_sco && !nm->ln_isfcav && c->f[NEMO_F_RN2B] &&
+  if ((nm->ln_seos || nm->ln_eos80) && nm->ln_traldf_iso && !nm->ln_zps && !nm->ln_sco && !nm->ln_isfcav && c->f[NEMO_F_RN2B] &&
       c->f[NEMO_F_RHD] && c->f[NEMO_F_GDEPT_N] && c->f[NEMO_F_GDEPW_N] && c->f[NEMO_F_NMLN] && c->f[NEMO_F_HMLP] &&
       c->f[NEMO_F_HMLPT] && c->f[NEMO_F_USLP] && c->f[NEMO_F_VSLP] && c->f[NEMO_F_WSLPI] && c->f[NEMO_F_WSLPJ] &&
       c->f[NEMO_F_AVT]) {                                          /* step.F90:127-150 */
@@ -3045,7 +3391,7 @@ int ora_stp_model(ora_ctx *c, int kt) {
   }
   memset(c->f[NEMO_F_UA], 0, n3 * sizeof(double));
   memset(c->f[NEMO_F_VA], 0, n3 * sizeof(double));
-  if (c->f[NEMO_F_RHD] && c->f[NEMO_F_RHOP] && c->nam.ln_seos) {   /* step.F90:165, :193 */
+  if (c->f[NEMO_F_RHD] && c->f[NEMO_F_RHOP] && (c->nam.ln_seos || c->nam.ln_eos80)) {  /* step.F90:165, :193 */
     if (!c->f[NEMO_F_GDEPT_N]) return NEMO_ERR_UNBOUND;
     st = ora_eos_insitu_pot(c, c->f[NEMO_F_TSN], c->f[NEMO_F_RHD], c->f[NEMO_F_RHOP], c->f[NEMO_F_GDEPT_N]);
     if (!st) st = ora_dyn_hpg(c, kt);

@@ -64,6 +64,8 @@ int ora_tra_zdf_imp(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
 int ora_tra_zdf(ora_ctx *c, int kt);
 int ora_dyn_spg_ts(ora_ctx *c, int kt);
 int ora_lbc_lnk(ora_ctx *c, double *ptab, int nk, int nl, char cd_nat, double psgn, double pval);
+/* zdf_phy with zdf_sh2, the TKE closure and zdf_evd (see nemo_gpu_zdf_phy) */
+int ora_zdf_phy(ora_ctx *c, int kt);
 /* stp_ctl (stpctl.F90:44-194): zmax[NEMO_CTL_N], loc[NEMO_CTL_NLOC], kindic */
 int ora_stp_ctl(ora_ctx *c, int kt, double *zmax, int *loc, int *kindic);
 /* dia_hsb (diahsb.F90): the initial state of the budgets, then one step's budget

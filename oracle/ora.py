@@ -45,6 +45,7 @@ def lib():
         P("ora_set_poison", [i], None)
         P("ora_set_threads", [i])
         P("ora_stp_ctl", [vp, i, vp, vp, C.POINTER(i)])
+        P("ora_zdf_phy", [vp, i])
         P("ora_dia_hsb_init", [vp])
         P("ora_dia_hsb", [vp, i, vp])
         P("ora_stp_ctl_last", [vp, vp, vp, C.POINTER(i)])
@@ -197,6 +198,9 @@ class Oracle:
 
     def stp_hotpath(self, kt):
         self._ck(lib().ora_stp_hotpath(self.h, kt), "stp_hotpath")
+
+    def zdf_phy(self, kt):
+        self._ck(lib().ora_zdf_phy(self.h, kt), "zdf_phy")
 
     # ---------------------------------------------------------------- stp_ctl, dia_hsb
     def stp_ctl(self, kt):

@@ -1,6 +1,7 @@
-"""The simplified equation of state (eos_insitu, eos_insitu_pot, rab_3d), bn2 and
-hpg_zco: known answers of the oracle on the CPU, and the GPU through the C ABI
-against the oracle, routine by routine and inside the model step."""
+"""The equations of state (eos_insitu, eos_insitu_pot, rab_3d: the simplified one
+and the polynomial EOS-80), bn2 and hpg_zco: known answers of the oracle on the CPU
+(including the reference's EOS-80 check value, eosbn2.F90:208), and the GPU through
+the C ABI against the oracle, routine by routine and inside the model step."""
 import numpy as np
 import pytest
 
@@ -90,6 +91,57 @@ def test_hpg_zco_known_answers():
     assert np.all(va == 0) and np.all(ua[:, :, -1] == 0)
 
 
+def eos80_case(nn=1):
+    from oracle import ora
+    dom = gyre.domain(nn)
+    nam = gyre.namelist(ln_eos80=1)
+    return dom, nam, ora.Oracle(dom, nam)
+
+
+def test_eos80_check_value():
+    """eosbn2.F90:208: rho = 1028.35011066567 kg/m3 at 3000 m, pt = 3 degC, sp = 35.5 psu."""
+    dom, nam, o = eos80_case()
+    s3 = (dom["jpi"], dom["jpj"], dom["jpk"])
+    ts = np.zeros(s3 + (2,), order="F")
+    ts[..., 0], ts[..., 1] = 3.0, 35.5
+    dep = np.full(s3, 3000.0, order="F")
+    prd, rhop = np.zeros(s3, order="F"), np.zeros(s3, order="F")
+    o.eos_insitu(ts, prd, dep)
+    tm = gyre.masks(dom)[0]
+    rho = (prd[:, :, :-1][tm[:, :, :-1] > 0] + 1.0) * nam["rau0"]
+    assert np.allclose(rho, 1028.35011066567, rtol=0, atol=1e-10)
+    o.eos_insitu_pot(ts, prd, rhop, dep)
+    assert np.allclose((prd[:, :, :-1][tm[:, :, :-1] > 0] + 1.0) * nam["rau0"], 1028.35011066567, rtol=0, atol=1e-10)
+
+
+def test_eos80_expansion_coefficients_are_the_derivatives():
+    """rab_3d's alpha and beta tables against central differences of the density
+    polynomial: alpha = -1/rau0 drho/dT, beta = 1/rau0 drho/dS (eosbn2.F90:588-642)."""
+    dom, nam, o = eos80_case()
+    s3 = (dom["jpi"], dom["jpj"], dom["jpk"])
+    rng = np.random.default_rng(3)
+    ts = np.zeros(s3 + (2,), order="F")
+    ts[..., 0] = rng.uniform(-1.5, 28.0, s3)
+    ts[..., 1] = rng.uniform(33.0, 37.5, s3)
+    dep = np.asfortranarray(rng.uniform(0.0, 4000.0, s3))
+    o.bind("GDEPT_N", dep)
+    pab = np.zeros(s3 + (2,), order="F")
+    o.rab_3d(ts, pab)
+    h = 1e-3
+    rho = {}
+    for key, (n, d) in {"t+": (0, h), "t-": (0, -h), "s+": (1, h), "s-": (1, -h)}.items():
+        t2 = ts.copy(order="F")
+        t2[..., n] += d
+        prd = np.zeros(s3, order="F")
+        o.eos_insitu(t2, prd, dep)
+        rho[key] = prd
+    tm = gyre.masks(dom)[0][:, :, :-1] > 0
+    alpha = -(rho["t+"] - rho["t-"]) / (2 * h)
+    beta = (rho["s+"] - rho["s-"]) / (2 * h)
+    assert np.allclose(pab[:, :, :-1, 0][tm], alpha[:, :, :-1][tm], rtol=2e-6, atol=0)
+    assert np.allclose(pab[:, :, :-1, 1][tm], beta[:, :, :-1][tm], rtol=2e-6, atol=0)
+
+
 def test_eos_needs_the_simplified_eos():
     from oracle import ora
     dom = gyre.domain(1)
@@ -100,9 +152,12 @@ def test_eos_needs_the_simplified_eos():
 
 
 # ------------------------------------------------------------------------- GPU
-def eos_pair(prec, nmem=2, **over):
+EOS = {"seos": dict(ln_seos=1), "eos80": dict(ln_eos80=1)}
+
+
+def eos_pair(prec, nmem=2, eos="seos", **over):
     pytest.importorskip("torch")
-    p = Pair(nn=2, prec=prec, seed=43, nmem=nmem, ln_seos=1, **over)
+    p = Pair(nn=2, prec=prec, seed=43, nmem=nmem, **EOS[eos], **over)
     for st in p.states:
         sl = gyre.slope_inputs(p.dom, p.nam, st)
         st.update(gdept_n=sl["gdept_n"], gdepw_n=sl["gdepw_n"], rhd=np.zeros(p.s3), rhop=np.zeros(p.s3))
@@ -113,9 +168,10 @@ def eos_pair(prec, nmem=2, **over):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("eos", ["seos", "eos80"])
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
-def test_gpu_eos_bn2_hpg(prec):
-    p = eos_pair(prec)
+def test_gpu_eos_bn2_hpg(prec, eos):
+    p = eos_pair(prec, eos=eos)
     nm = p.nmem
     z3 = [np.zeros(p.s3, order="F") for _ in range(nm)]
     z4 = [np.zeros(p.s4, order="F") for _ in range(nm)]
@@ -149,11 +205,12 @@ def test_gpu_eos_bn2_hpg(prec):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("eos", ["seos", "eos80"])
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
-def test_gpu_stp_model_with_hpg(prec):
+def test_gpu_stp_model_with_hpg(prec, eos):
     """The model step with eos and dyn_hpg: steps 1 (Euler), 2, 3 (graph capture) and
     4 (replay)."""
-    p = eos_pair(prec, neuler=0)
+    p = eos_pair(prec, eos=eos, neuler=0)
     for name in ("RHD", "RHOP"):
         p.bind(name)
     for kt in (1, 2, 3, 4):
@@ -170,13 +227,14 @@ def test_gpu_stp_model_with_hpg(prec):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("eos", ["seos", "eos80"])
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
-def test_gpu_stp_model_with_slopes_from_the_tracers(prec):
+def test_gpu_stp_model_with_slopes_from_the_tracers(prec, eos):
     """The model step forming its iso-neutral slopes from the before tracers
     (rab_3d, bn2, zdf_mxl, eos_insitu, ldf_slp) before the path, with eos and dyn_hpg
     of the now tracers: steps 1 (Euler), 2, 3 (graph capture) and 4 (replay)."""
     torch = pytest.importorskip("torch")
-    p = eos_pair(prec, neuler=0)
+    p = eos_pair(prec, eos=eos, neuler=0)
     for st in p.states:
         st.update(rn2b=np.zeros(p.s3), hmlp=np.zeros(p.s2), hmlpt=np.zeros(p.s2))
     for name in ("RHD", "RHOP", "RN2B", "HMLP", "HMLPT"):
