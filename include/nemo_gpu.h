@@ -370,6 +370,22 @@ int nemo_gpu_dyn_zad(nemo_ctx *ctx, int kt);
  * avt (avt_c = 5e-4) into hmld when bound; reads the bound gdept_n and gdepw_n. */
 int nemo_gpu_zdf_mxl(nemo_ctx *ctx, int kt);
 
+/* zdf_phy (zdfphy.F90:243-316) with the TKE closure (ln_zdftke: tke_tke and tke_avn,
+ * zdftke.F90:168-630, with Langmuir cells (ln_lc), the Prandtl number of nn_pdl and
+ * the mixing lengths of nn_mxl; nn_etau = 0 and ln_drg off as in GYRE) and zdf_evd
+ * (ln_zdfevd, nn_evdm, zdfevd.F90:40-121): the shear production zdf_sh2
+ * (zdfsh2.F90:30-76) from the closure's avm_k of the last call, then en and dissl,
+ * avm_k and avt_k, the ocean avm and avt on levels 2..jpk-1 with evd where N^2 or the
+ * before N^2 is <= -1e-12, avs = avt, and the closed lbc_lnk of the five
+ * coefficients. Linear free surface, z-levels. Bound: UB VB UN VN, AVM_K AVT_K AVM AVT
+ * (AVS optional), EN DISSL, RN2 RN2B, TAUM, GDEPW_N (FR_I optional, else 0). A cold
+ * start binds en = rn_emin wmask, dissl = 1e-12, avm_k = rn_avm0 wmask, avt_k =
+ * rn_avt0 wmask (tke_rst, zdftke.F90:778-783, zdf_phy_init). nemo_gpu_stp_model runs it
+ * at the head of the step, after rab_3d and bn2 of the before and now tracers (into
+ * rn2b and rn2, step.F90:127-133), when an equation of state is selected and these
+ * fields and GDEPT_N are bound. */
+int nemo_gpu_zdf_phy(nemo_ctx *ctx, int kt);
+
 /* zps_hde (zpshde.F90:41-148): pgtu, pgtv (jpi,jpj,kjpt) = the horizontal
  * gradients of pta (jpi,jpj,jpk,kjpt) at the partial-step bottom level of the u-
  * and v-points, with lbc_lnk. The optional density part (prd, pgru, pgrv) needs
@@ -602,6 +618,7 @@ enum nemo_kernel_id {
   NEMO_K_DYN_VOR,      /* vorticity trend */
   NEMO_K_DYN_KEG, NEMO_K_DYN_ZAD, /* momentum advection, vector form */
   NEMO_K_STP_CTL, NEMO_K_DIA_HSB, /* run control extrema, conservation budgets */
+  NEMO_K_ZDF_PHY,      /* shear production, TKE closure, enhanced vertical diffusion */
   NEMO_K_COUNT
 };
 

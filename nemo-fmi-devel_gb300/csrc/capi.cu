@@ -80,6 +80,8 @@ struct nemo_ctx {
   int adj_kjpt = 0;
   void* slp_w = nullptr;       // ldf_slp work: 4 3-D and 6 2-D arrays per member
   void* rab_w = nullptr;       // the model step's before expansion ratios rab_b (jpi,jpj,jpk,2)
+  void* rab_n = nullptr;       // and the now ones rab_n, with the vertical physics
+  void* zphy_w = nullptr;      // zdf_phy work: sh2, apdlr and the TKE system, 5 x n3 per member
   void* blp_w = nullptr;       // tra_ldf_blp: the first laplacian (jpi,jpj,jpk,kjpt) per member
   int blp_kjpt = 0;
   int iso_kjpt = 0;
@@ -1167,19 +1169,102 @@ bool slopes_on(const nemo_ctx* c) {
 }
 
 // eos_rab(tsb, rab_b), bn2(tsb, rab_b, rn2b), zdf_mxl, eos(tsb, rhd, gdept_0) and
-// ldf_slp(rhd, rn2b) (step.F90:127-150; the now-tracer rab_n and rn2 feed only the
-// vertical physics, which is not on the device). gdept_0 is the bound gdept_n: the
-// linear free surface keeps the rest-state depths.
+// ldf_slp(rhd, rn2b) (step.F90:127-150). With the vertical physics on, rn2b is
+// already formed (run_vphys) and only zdf_mxl onwards runs. gdept_0 is the bound
+// gdept_n: the linear free surface keeps the rest-state depths.
 template <class T>
-int run_slopes(nemo_ctx* c) {
+int run_slopes(nemo_ctx* c, bool rn2b_done) {
   void* const* F = c->f;
-  if (!c->rab_w && cudaMalloc(&c->rab_w, 2 * (size_t)c->n3 * c->nmem * sizeof(T)) != cudaSuccess)
-    return fail(c, NEMO_ERR_NOMEM, "rab_b work array");
-  int s = run_eos<T>(c, 2, F[NEMO_F_TSB], nullptr, nullptr, nullptr, c->rab_w, nullptr, nullptr);
-  if (!s) s = run_eos<T>(c, 3, F[NEMO_F_TSB], nullptr, nullptr, nullptr, nullptr, c->rab_w, F[NEMO_F_RN2B]);
+  int s = NEMO_OK;
+  if (!rn2b_done) {
+    if (!c->rab_w && cudaMalloc(&c->rab_w, 2 * (size_t)c->n3 * c->nmem * sizeof(T)) != cudaSuccess)
+      return fail(c, NEMO_ERR_NOMEM, "rab_b work array");
+    s = run_eos<T>(c, 2, F[NEMO_F_TSB], nullptr, nullptr, nullptr, c->rab_w, nullptr, nullptr);
+    if (!s) s = run_eos<T>(c, 3, F[NEMO_F_TSB], nullptr, nullptr, nullptr, nullptr, c->rab_w, F[NEMO_F_RN2B]);
+  }
   if (!s) s = run_zdf_mxl<T>(c);
   if (!s) s = run_eos<T>(c, 0, F[NEMO_F_TSB], F[NEMO_F_RHD], nullptr, F[NEMO_F_GDEPT_N], nullptr, nullptr, nullptr);
   if (!s) s = run_ldf_slp<T>(c, F[NEMO_F_RHD], F[NEMO_F_RN2B]);
+  return s;
+}
+
+// zdf_phy (zdfphy.F90:243-316) with the TKE closure: zdf_sh2, then the column
+// kernel (tke_tke, tke_avn, the ocean Kz, zdf_evd, avs, the closed lbc_lnk)
+bool zphy_bound(const nemo_ctx* c) {
+  for (int id : {NEMO_F_UB, NEMO_F_VB, NEMO_F_UN, NEMO_F_VN, NEMO_F_AVM_K, NEMO_F_AVT_K, NEMO_F_AVM, NEMO_F_AVT,
+                 NEMO_F_EN, NEMO_F_DISSL, NEMO_F_RN2, NEMO_F_RN2B, NEMO_F_TAUM, NEMO_F_GDEPW_N})
+    if (!c->f[id]) return false;
+  return true;
+}
+bool zphy_covered(const nemo_namelist& nm) {
+  return nm.ln_zdftke && nm.nn_etau == 0 && !nm.ln_drg_tke && !nm.ln_isfcav && nm.ln_linssh && !nm.ln_sco;
+}
+int zphy_check(nemo_ctx* c) {
+  if (!zphy_covered(c->nam))
+    return fail(c, NEMO_ERR_UNSUPPORTED,
+                "zdf_phy: the TKE closure with nn_etau = 0, ln_drg off, a linear free surface and z-levels");
+  if (!zphy_bound(c))
+    return fail(c, NEMO_ERR_UNBOUND,
+                "zdf_phy: ub vb un vn avm_k avt_k avm avt en dissl rn2 rn2b taum gdepw_n must be bound");
+  return NEMO_OK;
+}
+
+template <class T>
+int run_zdf_phy(nemo_ctx* c) {
+  const nemo_namelist& nm = c->nam;
+  const size_t n = (size_t)c->n3 * c->nmem;
+  if (!c->zphy_w && cudaMalloc(&c->zphy_w, 5 * n * sizeof(T)) != cudaSuccess)
+    return fail(c, NEMO_ERR_NOMEM, "zdf_phy work arrays");
+  void* const* F = c->f;
+  ZphyArgs<T> a{};
+  a.ub = (const T*)F[NEMO_F_UB]; a.vb = (const T*)F[NEMO_F_VB];
+  a.un = (const T*)F[NEMO_F_UN]; a.vn = (const T*)F[NEMO_F_VN];
+  a.rn2 = (const T*)F[NEMO_F_RN2]; a.rn2b = (const T*)F[NEMO_F_RN2B]; a.taum = (const T*)F[NEMO_F_TAUM];
+  a.gdepw = (const T*)F[NEMO_F_GDEPW_N]; a.fr_i = (const T*)F[NEMO_F_FR_I];
+  a.avm_k = (T*)F[NEMO_F_AVM_K]; a.avt_k = (T*)F[NEMO_F_AVT_K]; a.avm = (T*)F[NEMO_F_AVM];
+  a.avt = (T*)F[NEMO_F_AVT]; a.avs = (T*)F[NEMO_F_AVS]; a.en = (T*)F[NEMO_F_EN]; a.dissl = (T*)F[NEMO_F_DISSL];
+  T* w = (T*)c->zphy_w;
+  a.sh2 = w; a.apdlr = w + n; a.zdiag = w + 2 * n; a.zd_up = w + 3 * n; a.zd_lw = w + 4 * n;
+  // the constants of zdf_tke_init (zdftke.F90:663-690), tke_tke and tke_avn
+  const double rdt = nm.rn_rdt, zrhoa = 1.22, zcdrag = 1.5e-3;
+  const double rmxl_min = 1.e-6 / (nm.rn_ediff * std::sqrt(nm.rn_emin));
+  a.rdt = (T)rdt; a.zbbrau = (T)(nm.rn_ebb / nm.rau0); a.zfact1 = (T)(-.5 * rdt);
+  a.zfact2 = (T)(1.5 * rdt * nm.rn_ediss); a.zfact3 = (T)(0.5 * nm.rn_ediss);
+  a.rn_emin = (T)nm.rn_emin; a.rn_emin0 = (T)nm.rn_emin0; a.rn_bshear = (T)nm.rn_bshear;
+  a.rn_ediff = (T)nm.rn_ediff; a.rn_lc = (T)nm.rn_lc; a.rn_evd = (T)nm.rn_evd;
+  a.rn_avm0 = (T)nm.rn_avm0; a.rn_avt0 = (T)nm.rn_avt0;
+  a.ri_cri = (T)(2.0 / (2.0 + nm.rn_ediss / nm.rn_ediff)); a.rmxl_min = (T)rmxl_min;
+  a.rn_mxl0 = (T)(nm.ln_mxl0 ? rmxl_min : nm.rn_mxl0);
+  a.zraug = (T)(0.4 * 2.e5 / (nm.rau0 * nm.grav));
+  a.rsmall = (T)(0.5 * 2.220446049250313e-16);
+  a.lc_cof1 = (T)(0.5 * 0.016 * 0.016 / (zrhoa * zcdrag));
+  a.lc_cof2 = (T)(0.016 / std::sqrt(zrhoa * zcdrag));
+  a.rpi = (T)3.141592653589793;
+  a.nn_pdl = nm.nn_pdl; a.nn_mxl = nm.nn_mxl; a.ln_mxl0 = nm.ln_mxl0; a.ln_lc = nm.ln_lc;
+  a.ln_zdfevd = nm.ln_zdfevd; a.nn_evdm = nm.nn_evdm;
+  cudaError_t e = launch_zdf_phy<T>(dom_now<T>(c), a, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "zdf_phy launch");
+  return NEMO_OK;
+}
+
+// the model step's vertical physics (step.F90:127-133): an equation of state, the
+// TKE closure as zdf_phy covers it, z-levels with full steps, every field bound
+bool zphy_on(const nemo_ctx* c) {
+  const nemo_namelist& nm = c->nam;
+  return zphy_covered(nm) && (nm.ln_seos || nm.ln_eos80) && !nm.ln_zps && zphy_bound(c) && c->f[NEMO_F_GDEPT_N];
+}
+// rab_3d and bn2 of the before and now tracers, then zdf_phy
+template <class T>
+int run_vphys(nemo_ctx* c) {
+  void* const* F = c->f;
+  const size_t b2 = 2 * (size_t)c->n3 * c->nmem * sizeof(T);
+  if (!c->rab_w && cudaMalloc(&c->rab_w, b2) != cudaSuccess) return fail(c, NEMO_ERR_NOMEM, "rab_b work array");
+  if (!c->rab_n && cudaMalloc(&c->rab_n, b2) != cudaSuccess) return fail(c, NEMO_ERR_NOMEM, "rab_n work array");
+  int s = run_eos<T>(c, 2, F[NEMO_F_TSB], nullptr, nullptr, nullptr, c->rab_w, nullptr, nullptr);
+  if (!s) s = run_eos<T>(c, 2, F[NEMO_F_TSN], nullptr, nullptr, nullptr, c->rab_n, nullptr, nullptr);
+  if (!s) s = run_eos<T>(c, 3, F[NEMO_F_TSB], nullptr, nullptr, nullptr, nullptr, c->rab_w, F[NEMO_F_RN2B]);
+  if (!s) s = run_eos<T>(c, 3, F[NEMO_F_TSN], nullptr, nullptr, nullptr, nullptr, c->rab_n, F[NEMO_F_RN2]);
+  if (!s) s = run_zdf_phy<T>(c);
   return s;
 }
 
@@ -1256,8 +1341,13 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
   }
   mark(0);
   if (model) {  // ua = va = 0 (step.F90:183-184)
+    const bool vphys = zphy_on(c);
+    if (vphys) {
+      int s = run_vphys<T>(c);
+      if (s) return s;
+    }
     if (slopes_on(c)) {
-      int s = run_slopes<T>(c);
+      int s = run_slopes<T>(c, vphys);
       if (s) return s;
     }
     const size_t bytes = (size_t)c->n3 * c->nmem * sizeof(T);
@@ -1577,7 +1667,7 @@ int nemo_gpu_destroy(nemo_ctx* c) {
   for (auto p : c->iso_w) cudaFree(p);
   for (auto p : c->adj_w) cudaFree(p);
   cudaFree(c->slp_w);
-  cudaFree(c->rab_w);
+  cudaFree(c->rab_w); cudaFree(c->rab_n); cudaFree(c->zphy_w);
   cudaFree(c->blp_w);
   for (auto p : c->spg_w) cudaFree(p);
   for (auto p : c->spg_cor) cudaFree(p);
@@ -1868,6 +1958,14 @@ int nemo_gpu_zdf_mxl(nemo_ctx* c, int kt) {
   for (int id : {NEMO_F_RN2B, NEMO_F_AVT, NEMO_F_GDEPT_N, NEMO_F_GDEPW_N, NEMO_F_NMLN, NEMO_F_HMLP, NEMO_F_HMLPT})
     if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "zdf_mxl: field %d must be bound", id);
   return c->prec == NEMO_PREC_FP64 ? run_zdf_mxl<double>(c) : run_zdf_mxl<float>(c);
+}
+
+int nemo_gpu_zdf_phy(nemo_ctx* c, int kt) {
+  (void)kt;
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (int s = zphy_check(c)) return s;
+  return c->prec == NEMO_PREC_FP64 ? run_zdf_phy<double>(c) : run_zdf_phy<float>(c);
 }
 
 int nemo_gpu_dyn_keg(nemo_ctx* c, int kt, int kscheme) {

@@ -793,4 +793,219 @@ __global__ void k_dyn_zad(Dom<T> d, const T* __restrict__ un, const T* __restric
   }
 }
 
+// ---------------------------------------------------------------- zdf_phy (TKE)
+// 2 x the shear production at the uw-point (i+1/2, j, k) and the vw-point
+// (i, j+1/2, k) of column ij (zdfsh2.F90:57-66) with the closure's avm_k. With a
+// linear free surface e3uw_n = e3uw_b = the rest-state MIN of the neighbouring e3w.
+template <class T>
+__device__ __forceinline__ T zsh2_u(const Dom<T>& d, const ZphyArgs<T>& a, long m3, long ij, int k, int m) {
+  const ColInfo c = d.ci[ij];
+  const long q = m3 + ij + (long)(k - 1) * d.n2;
+  const T e = fmn(d.e3w_n(ij, k, m), d.e3w_n(ij + 1, k, m));
+  return (a.avm_k[q + 1] + a.avm_k[q]) * (a.un[q - d.n2] - a.un[q]) * (a.ub[q - d.n2] - a.ub[q]) / (e * e) *
+         (umsk<T>(c, k) * umsk<T>(c, k - 1));
+}
+template <class T>
+__device__ __forceinline__ T zsh2_v(const Dom<T>& d, const ZphyArgs<T>& a, long m3, long ij, int k, int m) {
+  const ColInfo c = d.ci[ij];
+  const long q = m3 + ij + (long)(k - 1) * d.n2;
+  const T e = fmn(d.e3w_n(ij, k, m), d.e3w_n(ij + d.jpi, k, m));
+  return (a.avm_k[q + d.jpi] + a.avm_k[q]) * (a.vn[q - d.n2] - a.vn[q]) * (a.vb[q - d.n2] - a.vb[q]) / (e * e) *
+         (vmsk<T>(c, k) * vmsk<T>(c, k - 1));
+}
+
+// zdf_sh2 (zdfsh2.F90:67-74): the shear production at the interior w-points of
+// levels 2..jpk-1, one point per thread; each of the four uw/vw terms it averages is
+// formed where read (two threads form each).
+template <class T>
+__global__ void k_zdf_sh2(Dom<T> d, ZphyArgs<T> a) {
+  const PtIdx c = pt_index(d);
+  if (!c.valid || !c.interior || c.k < 2 || c.k > d.jpk - 1) return;
+  const long m3 = (long)c.m * d.n3;
+  const int k = c.k;
+  const T u0 = zsh2_u(d, a, m3, c.ij - 1, k, c.m), u1 = zsh2_u(d, a, m3, c.ij, k, c.m);
+  const T v0 = zsh2_v(d, a, m3, c.ij - d.jpi, k, c.m), v1 = zsh2_v(d, a, m3, c.ij, k, c.m);
+  const ColInfo cw = d.ci[c.ij - 1], ch = d.ci[c.ij], cs = d.ci[c.ij - d.jpi];
+  a.sh2[m3 + c.q] = T(0.25) * ((u0 + u1) * (T(2) - umsk<T>(cw, k) * umsk<T>(ch, k)) +
+                               (v0 + v1) * (T(2) - vmsk<T>(cs, k) * vmsk<T>(ch, k)));
+}
+
+// The column part of zdf_phy, one water column per thread (its levels are coupled
+// by the implicit TKE equation and the mixing-length limits):
+//  tke_tke (zdftke.F90:168-440): surface value of en, Langmuir cells, the inverse
+//    Prandtl number apdlr, the implicit system assembled and forward-eliminated in
+//    one downward sweep, back-substituted upwards, the floor rn_emin;
+//  tke_avn (:443-630): the buoyancy length sqrt(2 en / N^2), limited by nn_mxl in a
+//    downward and an upward sweep, and on that upward sweep avm_k, avt_k, dissl, the
+//    Prandtl correction of avt_k, then zdf_phy's avt, avm (zdfphy.F90:269-270),
+//    zdf_evd (zdfevd.F90:76-109) and avs = avt (:284).
+// Edge columns get the closed lbc_lnk of the five coefficients (zdfphy.F90:301-303).
+// Each expression keeps the reference's association.
+template <class T>
+__global__ void k_zdf_tke(Dom<T> d, ZphyArgs<T> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i > d.jpi || j > d.jpj) return;
+  const int m = blockIdx.z, jpk = d.jpk;
+  const long n2 = d.n2;
+  const long ij = (long)(i - 1) + (long)(j - 1) * d.jpi;
+  const long c3 = (long)m * d.n3 + ij, c2 = (long)m * d.n2 + ij;
+  if (i == 1 || i == d.jpi || j == 1 || j == d.jpj) {
+    for (int k = 1; k <= jpk; ++k) {
+      const long q = c3 + (long)(k - 1) * n2;
+      a.avm_k[q] = T(0); a.avt_k[q] = T(0); a.avm[q] = T(0); a.avt[q] = T(0);
+      if (a.avs) a.avs[q] = T(0);
+    }
+    return;
+  }
+  const ColInfo ci = d.ci[ij];
+  const T tm1 = tmsk<T>(ci, 1);
+  const T taum = a.taum[c2];
+  const T en1 = fmx(a.rn_emin0, a.zbbrau * taum) * tm1;  // surface boundary condition
+  a.en[c3] = en1;
+  // Langmuir cells: the depth zhlc of the first w-level whose cumulated potential
+  // energy exceeds the Stokes-drift scale, and the source amplitude zfr
+  T zhlc = T(1), zfr = T(0);
+  if (a.ln_lc) {
+    const T zus = a.lc_cof1 * taum;
+    T zpelc = fmx(a.rn2b[c3], T(0)) * a.gdepw[c3] * d.e3w_n(ij, 1, m);
+    int imlc = d.mbkt[ij] + 1;
+    for (int k = 2; k <= jpk - 1; ++k) {
+      const long q = c3 + (long)(k - 1) * n2;
+      zpelc = zpelc + fmx(a.rn2b[q], T(0)) * a.gdepw[q] * d.e3w_n(ij, k, m);
+      if (zpelc > zus) { imlc = k; break; }
+    }
+    zhlc = a.gdepw[c3 + (long)(imlc - 1) * n2];
+    const T zs = a.lc_cof2 * sqrt(taum);
+    zfr = (T(1) - T(4) * (a.fr_i ? a.fr_i[c2] : T(0))) * zs * zs * zs * tm1;
+    if (zfr < T(0)) zfr = T(0);
+  }
+  // downward sweep: right-hand side, matrix, forward elimination
+  T dg_p = T(1), up_p = T(0), lw_p = T(0);
+  T avm_km1 = a.avm_k[c3];
+  for (int k = 2; k <= jpk - 1; ++k) {
+    const long q = c3 + (long)(k - 1) * n2;
+    const T wm = wmsk<T>(ci, k), tm = tmsk<T>(ci, k);
+    T en = a.en[q];
+    if (zfr != T(0)) {
+      const T dep = a.gdepw[q];
+      if (dep - zhlc < T(0) && wm != T(0)) {
+        const T zwlc = a.rn_lc * sin(a.rpi * dep / zhlc);
+        en = en + a.rdt * zfr * (zwlc * zwlc * zwlc) / zhlc;
+      }
+    }
+    const T avm_k = a.avm_k[q], avm_kp1 = a.avm_k[q + n2];
+    const T sh2 = a.sh2[q], dissl = a.dissl[q], rn2 = a.rn2[q];
+    if (a.nn_pdl == 1) {
+      const T zri = fmx(a.rn2b[q], T(0)) * avm_k / (sh2 + a.rn_bshear);
+      a.apdlr[q] = fmx(T(0.1), a.ri_cri / fmx(a.ri_cri, zri));
+    }
+    const T zcof = a.zfact1 * tm;
+    const T e3w = d.e3w_n(ij, k, m);
+    const T up = zcof * fmx(avm_kp1 + avm_k, T(2.e-5)) / (d.e3t_n(ij, k, m) * e3w);
+    const T lw = zcof * fmx(avm_k + avm_km1, T(2.e-5)) / (d.e3t_n(ij, k - 1, m) * e3w);
+    T dg = T(1) - lw - up + a.zfact2 * dissl * wm;
+    const T rhs = en + a.rdt * (sh2 - a.avt_k[q] * rn2 + a.zfact3 * dissl * en) * wm;
+    T lf;
+    if (k == 2) {
+      lf = rhs - lw * en1;
+    } else {
+      dg = dg - lw * up_p / dg_p;
+      lf = rhs - lw / dg_p * lw_p;
+    }
+    a.zdiag[q] = dg; a.zd_up[q] = up; a.zd_lw[q] = lf;
+    dg_p = dg; up_p = up; lw_p = lf;
+    avm_km1 = avm_k;
+  }
+  // upward sweep: back substitution, the floor, and the buoyancy length (into zdiag)
+  T en_p = T(0);
+  for (int k = jpk - 1; k >= 2; --k) {
+    const long q = c3 + (long)(k - 1) * n2;
+    const T en = (k == jpk - 1) ? a.zd_lw[q] / a.zdiag[q] : (a.zd_lw[q] - a.zd_up[q] * en_p) / a.zdiag[q];
+    en_p = en;
+    const T e = fmx(en, a.rn_emin) * wmsk<T>(ci, k);
+    a.en[q] = e;
+    a.zdiag[q] = fmx(a.rmxl_min, sqrt(T(2) * e / fmx(a.rn2[q], a.rsmall)));
+  }
+  T* zmxlm = a.zdiag;
+  T* zmxld = a.zd_up;
+  const T mxl1 = a.ln_mxl0 ? fmx(a.rn_mxl0, a.zraug * taum * tm1) : a.rn_mxl0;
+  // downward limits of nn_mxl = 2 (zmxlm) and 3 (zmxld, from the unlimited zmxlm)
+  if (a.nn_mxl == 2) {
+    T p = mxl1;
+    for (int k = 2; k <= jpk - 1; ++k) {
+      const long q = c3 + (long)(k - 1) * n2;
+      p = fmn(p + d.e3t_n(ij, k - 1, m), zmxlm[q]);
+      zmxlm[q] = p;
+    }
+  } else if (a.nn_mxl == 3) {
+    T p = mxl1;
+    for (int k = 2; k <= jpk - 1; ++k) {
+      const long q = c3 + (long)(k - 1) * n2;
+      p = fmn(p + d.e3t_n(ij, k - 1, m), zmxlm[q]);
+      zmxld[q] = p;
+    }
+  }
+  // upward sweep: the limited lengths, the coefficients, the ocean Kz
+  const T evd = a.rn_evd;
+  T nxt = a.rmxl_min;  // zmxlm(jpk)
+  for (int k = jpk - 1; k >= 2; --k) {
+    const long q = c3 + (long)(k - 1) * n2;
+    const T wm = wmsk<T>(ci, k), tm = tmsk<T>(ci, k);
+    const T raw = zmxlm[q];
+    T lm, ld;
+    if (a.nn_mxl == 2) {
+      lm = fmn(nxt + d.e3t_n(ij, k + 1, m), raw);
+      ld = lm;
+      nxt = lm;
+    } else if (a.nn_mxl == 3) {
+      const T dn = fmn(nxt + d.e3t_n(ij, k + 1, m), raw);
+      nxt = dn;
+      const T lu = zmxld[q];
+      lm = fmn(lu, dn);
+      ld = sqrt(lu * dn);
+    } else if (a.nn_mxl == 1) {
+      lm = fmn(d.e3w_n(ij, k, m), raw);
+      ld = lm;
+    } else {  // 0: bounded by the distances to the surface (mikt = 1) and the bottom
+      const T dep = a.gdepw[q], e3w = d.e3w_n(ij, k, m);
+      const T z = fmn(fmn(dep - a.gdepw[c3], raw), a.gdepw[c3 + (long)d.mbkt[ij] * n2] - dep);
+      lm = z * wm + fmn(raw, e3w) * (T(1) - wm);
+      ld = z * wm + fmn(lm, e3w) * (T(1) - wm);
+    }
+    const T zsqen = sqrt(a.en[q]);
+    const T zav = a.rn_ediff * lm * zsqen;
+    const T avmk = fmx(zav, a.rn_avm0) * wm;
+    T avtk = fmx(zav, a.rn_avt0) * wm;
+    a.dissl[q] = zsqen / ld;
+    if (a.nn_pdl == 1) avtk = fmx(a.apdlr[q] * avtk, a.rn_avt0) * tm;
+    a.avm_k[q] = avmk;
+    a.avt_k[q] = avtk;
+    T avt = avtk, avm = avmk;
+    if (a.ln_zdfevd && fmn(a.rn2[q], a.rn2b[q]) <= T(-1.e-12)) {
+      avt = evd * wm;
+      if (a.nn_evdm == 1) avm = evd * wm;
+    }
+    a.avt[q] = avt;
+    a.avm[q] = avm;
+    if (a.avs) a.avs[q] = avt;
+  }
+  // the surface level: coefficients from en(1) and the surface length; avt, avm
+  // keep their values there unless zdf_evd acts
+  {
+    const T wm = tm1;
+    const T zsqen = sqrt(en1);
+    const T zav = a.rn_ediff * mxl1 * zsqen;
+    a.avm_k[c3] = fmx(zav, a.rn_avm0) * wm;
+    a.avt_k[c3] = fmx(zav, a.rn_avt0) * wm;
+    a.dissl[c3] = zsqen / mxl1;
+    T avt = a.avt[c3];
+    if (a.ln_zdfevd && fmn(a.rn2[c3], a.rn2b[c3]) <= T(-1.e-12)) {
+      avt = evd * wm;
+      a.avt[c3] = avt;
+      if (a.nn_evdm == 1) a.avm[c3] = evd * wm;
+    }
+    if (a.avs) a.avs[c3] = avt;
+  }
+}
+
 }  // namespace nemo

@@ -75,6 +75,20 @@ struct MxlArgs {
   int nlb10;
 };
 
+// zdf_phy with the TKE closure and zdf_evd. Member strides n3 (3-D) and n2 (taum,
+// fr_i). Work arrays (n3 per member): sh2, apdlr (the inverse Prandtl number), and
+// the three diagonals of the TKE system, whose storage the mixing lengths zmxlm
+// (zdiag) and zmxld (zd_up) take over once the system is solved.
+template <class T>
+struct ZphyArgs {
+  const T *ub, *vb, *un, *vn, *rn2, *rn2b, *taum, *gdepw, *fr_i;  // fr_i may be null
+  T *avm_k, *avt_k, *avm, *avt, *avs, *en, *dissl;                 // avs may be null
+  T *sh2, *apdlr, *zdiag, *zd_up, *zd_lw;
+  T rdt, zbbrau, zfact1, zfact2, zfact3, rn_emin, rn_emin0, rn_bshear, rn_ediff, rn_lc, rn_evd;
+  T rn_avm0, rn_avt0, ri_cri, rmxl_min, rn_mxl0, zraug, rsmall, lc_cof1, lc_cof2, rpi;
+  int nn_pdl, nn_mxl, ln_mxl0, ln_lc, ln_zdfevd, nn_evdm;
+};
+
 template <class T>
 cudaError_t launch_dyn_ldf_lap(const Dom<T>& d, const T* ahmt, const T* ahmf, const T* pub, const T* pvb, T* pua, T* pva,
                                T zsign, cudaStream_t s);
@@ -86,6 +100,8 @@ template <class T>
 cudaError_t launch_dyn_zad(const Dom<T>& d, const T* un, const T* vn, const T* wn, T* ua, T* va, cudaStream_t s);
 template <class T>
 cudaError_t launch_zdf_mxl(const Dom<T>& d, const MxlArgs<T>& a, cudaStream_t s);
+template <class T>
+cudaError_t launch_zdf_phy(const Dom<T>& d, const ZphyArgs<T>& a, cudaStream_t s);
 template <class T>
 cudaError_t launch_eos(const Dom<T>& d, const EosArgs<T>& a, cudaStream_t s);
 template <class T>

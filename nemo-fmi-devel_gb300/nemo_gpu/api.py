@@ -289,6 +289,10 @@ class Context:
     def zdf_mxl(self, kt):
         self._ck(self.lib.nemo_gpu_zdf_mxl(self.h, kt), "zdf_mxl")
 
+    def zdf_phy(self, kt):
+        """zdf_sh2, the TKE closure and zdf_evd on the bound fields (zdfphy.F90:243-316)"""
+        self._ck(self.lib.nemo_gpu_zdf_phy(self.h, kt), "zdf_phy")
+
     def dyn_hpg(self, kt):
         self._ck(self.lib.nemo_gpu_dyn_hpg(self.h, kt), "dyn_hpg")
 

@@ -358,3 +358,24 @@ def sbc_inputs(dom, nam, st, kt=1):
                 sbc_tsc=f(np.zeros((jpi, jpj, 2))), sbc_tsc_b=f(np.zeros((jpi, jpj, 2))),
                 qsr_hc=f(np.zeros((jpi, jpj, jpk))), qsr_hc_b=f(np.zeros((jpi, jpj, jpk))),
                 fraqsr_1lev=f(np.ones((jpi, jpj))))
+
+
+def vphys_inputs(dom, nam, st):
+    """Inputs of zdf_phy with the TKE closure for a state: the wind-stress modulus at
+    T-points from the state's utau, vtau (usrdef_sbc.F90:176-186, interior points,
+    zero on the closed edges) and the cold start of the closure (zdf_phy_init and
+    tke_rst, zdftke.F90:778-783): en = rn_emin wmask, dissl = 1e-12, avm_k = rn_avm0
+    wmask, avt_k = rn_avt0 wmask, avm = avs = 0; rn2 is formed by the step (zeros)."""
+    from ._ffi import NAMELIST_DEFAULTS
+    nam = {**NAMELIST_DEFAULTS, **nam}
+    jpi, jpj, jpk = dom["jpi"], dom["jpj"], dom["jpk"]
+    wm = masks(dom)[3]
+    ut, vt = st["utau"], st["vtau"]
+    taum = np.zeros((jpi, jpj))
+    ztx = ut[:-2, 1:-1] + ut[1:-1, 1:-1]
+    zty = vt[1:-1, :-2] + vt[1:-1, 1:-1]
+    taum[1:-1, 1:-1] = 0.5 * np.sqrt(ztx * ztx + zty * zty)
+    f = np.asfortranarray
+    z3 = lambda: f(np.zeros((jpi, jpj, jpk)))
+    return dict(taum=f(taum), en=f(nam["rn_emin"] * wm), dissl=f(np.full((jpi, jpj, jpk), 1.e-12)),
+                avm_k=f(nam["rn_avm0"] * wm), avt_k=f(nam["rn_avt0"] * wm), avm=z3(), avs=z3(), rn2=z3())

@@ -1694,7 +1694,8 @@ int ora_glob_sum(ora_ctx *c, const double *ptab, int nk, double *out) {
  * Bound: UB VB UN VN, AVM_K AVT_K AVM AVT (and AVS), EN DISSL (restart fields; a
  * cold start sets en = rn_emin wmask, dissl = 1e-12), RN2 RN2B, TAUM, GDEPW_N; FR_I
  * optional (0). The rest-state e3uw/e3vw are the minima of the neighbouring e3w_0
- * (equal to e3w_0 on full steps, usrdef_zgr.F90:241-242). */
+ * (equal to e3w_0 on full steps, usrdef_zgr.F90:241-242). The five coefficients get
+ * the closed lbc_lnk of a W-point field at the end. */
 int ora_zdf_phy(ora_ctx *c, int kt) {
   (void)kt;
   const nemo_namelist *nm = &c->nam;
@@ -1952,6 +1953,12 @@ int ora_zdf_phy(ora_ctx *c, int kt) {
     for (int jk = 1; jk <= jpk - 1; ++jk)
       for (int jj = 2; jj <= jpj - 1; ++jj)
         for (int ji = 2; ji <= jpi - 1; ++ji) avs[I3(ji, jj, jk)] = avt[I3(ji, jj, jk)];
+  /* closed lateral boundaries of the five coefficients (zdfphy.F90:301-303) */
+  lbc_closed(jpi, jpj, avm_k, jpk, 'W', 0.0);
+  lbc_closed(jpi, jpj, avt_k, jpk, 'W', 0.0);
+  lbc_closed(jpi, jpj, avm, jpk, 'W', 0.0);
+  lbc_closed(jpi, jpj, avt, jpk, 'W', 0.0);
+  if (avs) lbc_closed(jpi, jpj, avs, jpk, 'W', 0.0);
 #undef E3UW
 #undef E3VW
 #undef WUM
@@ -3368,22 +3375,52 @@ int ora_dyn_hpg(ora_ctx *c, int kt) {
   return NEMO_OK;
 }
 
-/* One model step (step.F90:96-305) with the path and the routines above: ua = va = 0,
- * dyn_spg_ts, div_hor + wzv, the dyn_zdf time step, tsa = 0, tra_adv, tra_ldf,
- * tra_zdf, tra_nxt, dyn_nxt, ssh_swp. */
+/* the model step's vertical physics is on: the TKE closure selected as zdf_phy
+ * covers it, an equation of state and every field of zdf_phy bound */
+static int vphys_on(const ora_ctx *c) {
+  const nemo_namelist *nm = &c->nam;
+  static const int ids[] = {NEMO_F_UB, NEMO_F_VB, NEMO_F_UN, NEMO_F_VN, NEMO_F_AVM_K, NEMO_F_AVT_K, NEMO_F_AVM,
+                            NEMO_F_AVT, NEMO_F_EN, NEMO_F_DISSL, NEMO_F_RN2, NEMO_F_RN2B, NEMO_F_TAUM,
+                            NEMO_F_GDEPW_N, NEMO_F_GDEPT_N};
+  if (!nm->ln_zdftke || !(nm->ln_seos || nm->ln_eos80) || nm->nn_etau != 0 || nm->ln_drg_tke || !nm->ln_linssh ||
+      nm->ln_isfcav || nm->ln_sco || nm->ln_zps)
+    return 0;
+  for (size_t i = 0; i < sizeof(ids) / sizeof(ids[0]); ++i)
+    if (!c->f[ids[i]]) return 0;
+  return 1;
+}
+
+/* One model step (step.F90:96-305) with the path and the routines above: the
+ * vertical physics (rab_3d and bn2 of the before and now tracers, zdf_phy), the
+ * iso-neutral slopes, ua = va = 0, eos + dyn_hpg, dyn_spg_ts, div_hor + wzv, the
+ * dyn_zdf time step, tsa = 0, tra_adv, tra_ldf, tra_zdf, tra_nxt, dyn_nxt, ssh_swp,
+ * dia_hsb, stp_ctl; each where its fields are bound. */
 int ora_stp_model(ora_ctx *c, int kt) {
   const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk;
   if (!c->f[NEMO_F_UA] || !c->f[NEMO_F_VA]) return NEMO_ERR_UNBOUND;
   int st = 0;
   const nemo_namelist *nm = &c->nam;
+  const int vphys = vphys_on(c);
+  if (vphys) {                                                    /* step.F90:127-133 */
+    double *rab = zalloc(2 * n3);
+    st = ora_rab_3d(c, c->f[NEMO_F_TSB], rab);
+    if (!st) st = ora_bn2(c, c->f[NEMO_F_TSB], rab, c->f[NEMO_F_RN2B]);
+    if (!st) st = ora_rab_3d(c, c->f[NEMO_F_TSN], rab);
+    if (!st) st = ora_bn2(c, c->f[NEMO_F_TSN], rab, c->f[NEMO_F_RN2]);
+    wfree(rab);
+    if (!st) st = ora_zdf_phy(c, kt);
+    if (st) return st;
+  }
   if ((nm->ln_seos || nm->ln_eos80) && nm->ln_traldf_iso && !nm->ln_zps && !nm->ln_sco && !nm->ln_isfcav && c->f[NEMO_F_RN2B] &&
       c->f[NEMO_F_RHD] && c->f[NEMO_F_GDEPT_N] && c->f[NEMO_F_GDEPW_N] && c->f[NEMO_F_NMLN] && c->f[NEMO_F_HMLP] &&
       c->f[NEMO_F_HMLPT] && c->f[NEMO_F_USLP] && c->f[NEMO_F_VSLP] && c->f[NEMO_F_WSLPI] && c->f[NEMO_F_WSLPJ] &&
       c->f[NEMO_F_AVT]) {                                          /* step.F90:127-150 */
-    double *rab = zalloc(2 * n3);
-    st = ora_rab_3d(c, c->f[NEMO_F_TSB], rab);
-    if (!st) st = ora_bn2(c, c->f[NEMO_F_TSB], rab, c->f[NEMO_F_RN2B]);
-    wfree(rab);
+    if (!vphys) {  /* (rn2b comes from the vertical physics otherwise) */
+      double *rab = zalloc(2 * n3);
+      st = ora_rab_3d(c, c->f[NEMO_F_TSB], rab);
+      if (!st) st = ora_bn2(c, c->f[NEMO_F_TSB], rab, c->f[NEMO_F_RN2B]);
+      wfree(rab);
+    }
     if (!st) st = ora_zdf_mxl(c, kt);
     if (!st) st = ora_eos_insitu(c, c->f[NEMO_F_TSB], c->f[NEMO_F_RHD], c->f[NEMO_F_GDEPT_N]);
     if (!st) st = ora_ldf_slp(c, kt, c->f[NEMO_F_RHD], c->f[NEMO_F_RN2B]);

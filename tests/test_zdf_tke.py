@@ -1,0 +1,189 @@
+"""The vertical physics of the model step: zdf_phy (zdfphy.F90:243-316) with the TKE
+closure (zdftke.F90:168-630) and enhanced vertical diffusion (zdfevd.F90:40-121).
+
+On the CPU, properties of the oracle that the reference's equations fix: the surface
+boundary value of the turbulent kinetic energy, the floors rn_emin, rn_avm0 and
+rn_avt0, the enhanced diffusion where N^2 of either time level is negative, avs = avt,
+the closed boundary, and the response to the wind. On the GPU, zdf_phy through the C
+ABI against the oracle over three calls from a cold start, for each mixing-length
+option, and the model step forming N^2 from the tracers (rab_3d, bn2) before zdf_phy."""
+import numpy as np
+import pytest
+
+from harness import Pair
+from nemo_gpu import gyre
+
+TKE = dict(ln_zdftke=1, ln_zdfevd=1, ln_seos=1)
+VFIELDS = ("TAUM", "EN", "DISSL", "AVM_K", "AVT_K", "AVM", "AVS", "RN2", "RN2B", "GDEPW_N")
+OUT = ("EN", "DISSL", "AVM_K", "AVT_K", "AVM", "AVT", "AVS")
+UNSTABLE = ((6, 8, 4), (10, 12, 9), (20, 5, 2))   # (i, j, k) 0-based, wet interior w-points
+
+
+def full_namelist(nam):
+    from nemo_gpu._ffi import NAMELIST_DEFAULTS
+    return {**NAMELIST_DEFAULTS, **nam}
+
+
+def vphys_state(dom, nam, st):
+    """a state with the closure's cold start and the N^2 of a linear equation of state
+    (before = now), negative at the points of UNSTABLE"""
+    st = dict(st)
+    st.update(gyre.vphys_inputs(dom, nam, st))
+    sl = gyre.slope_inputs(dom, nam, st)
+    rn2 = np.array(sl["rn2b"], order="F")
+    for i, j, k in UNSTABLE:
+        rn2[i, j, k] = -1e-6
+    st.update(rn2=rn2, rn2b=np.array(rn2, order="F"), gdepw_n=sl["gdepw_n"], gdept_n=sl["gdept_n"])
+    return st
+
+
+def oracle_case(seed=5, wind=1.0, **over):
+    from oracle import ora
+    dom = gyre.domain(1)
+    nam = gyre.namelist(**{**TKE, **over})
+    st = gyre.state(dom, nam, seed=seed)
+    st["utau"] = st["utau"] * wind
+    st["vtau"] = st["vtau"] * wind
+    st = vphys_state(dom, nam, st)
+    o = ora.Oracle(dom, nam)
+    f = {}
+    for n in ("UB", "VB", "UN", "VN", "AVT") + VFIELDS:
+        f[n] = np.array(st[n.lower()], order="F", copy=True)
+        o.bind(n, f[n])
+    return dom, nam, o, f
+
+
+def interior(dom):
+    m = np.zeros((dom["jpi"], dom["jpj"]), bool)
+    m[1:-1, 1:-1] = True
+    return m
+
+
+def test_tke_floors_surface_value_and_closed_edges():
+    dom, nam, o, f = oracle_case()
+    d = full_namelist(nam)
+    for kt in (1, 2, 3):
+        o.zdf_phy(kt)
+    tm, _, _, wm = gyre.masks(dom)
+    inner = interior(dom)
+    wet = (wm > 0) & inner[:, :, None]
+    wet[:, :, 0] = False
+    wet[:, :, -1] = False
+    assert (f["EN"][wet] >= d["rn_emin"]).all()
+    surf = np.maximum(d["rn_emin0"], d["rn_ebb"] / nam["rau0"] * f["TAUM"]) * tm[:, :, 0]
+    np.testing.assert_array_equal(f["EN"][:, :, 0][inner], surf[inner])
+    assert (f["AVM_K"][wet] >= d["rn_avm0"]).all() and (f["AVT_K"][wet] >= d["rn_avt0"]).all()
+    assert (f["DISSL"][wet] > 0).all()
+    np.testing.assert_array_equal(f["AVS"][:, :, :-1], f["AVT"][:, :, :-1])
+    for n in ("AVM_K", "AVT_K", "AVM", "AVT", "AVS"):
+        a = f[n]
+        assert not a[0].any() and not a[-1].any() and not a[:, 0].any() and not a[:, -1].any(), n
+        assert not a[wm == 0].any(), n
+
+
+def test_evd_where_either_n2_is_negative():
+    """avt = avm = rn_evd at the unstable points with nn_evdm = 1, avt only with
+    nn_evdm = 0, neither without ln_zdfevd; a negative before N^2 alone triggers too
+    (MIN of rn2 and rn2b)."""
+    for evdm in (1, 0):
+        dom, nam, o, f = oracle_case(nn_evdm=evdm)
+        evd = full_namelist(nam)["rn_evd"]
+        o.zdf_phy(1)
+        for i, j, k in UNSTABLE:
+            assert f["AVT"][i, j, k] == evd and f["AVS"][i, j, k] == evd
+            assert (f["AVM"][i, j, k] == evd) == (evdm == 1)
+            assert f["AVT_K"][i, j, k] < 1.0                        # the closure's own value
+    dom, nam, o, f = oracle_case(ln_zdfevd=0)
+    o.zdf_phy(1)
+    for i, j, k in UNSTABLE:
+        assert f["AVT"][i, j, k] < 1.0
+    dom, nam, o, f = oracle_case()
+    i, j, k = 12, 7, 6
+    f["RN2"][i, j, k] = abs(f["RN2"][i, j, k]) + 1e-8
+    f["RN2B"][i, j, k] = -1e-9
+    o.zdf_phy(1)
+    assert f["AVT"][i, j, k] == full_namelist(nam)["rn_evd"]
+
+
+def test_wind_deepens_the_turbulence():
+    """Stronger wind stress raises the surface energy and the energy below it."""
+    ens = []
+    for wind in (0.0, 1.0, 3.0):
+        dom, nam, o, f = oracle_case(wind=wind)
+        for kt in (1, 2, 3, 4):
+            o.zdf_phy(kt)
+        inner = interior(dom)
+        wet = dom["k_bot"][inner] > 3
+        ens.append([f["EN"][:, :, k][inner][wet].mean() for k in (0, 1, 2)])
+    ens = np.array(ens)
+    assert (np.diff(ens, axis=0) > 0).all(), ens
+
+
+def test_zdf_phy_refuses_what_it_does_not_cover():
+    dom, nam, o, f = oracle_case(ln_zdftke=0)
+    with pytest.raises(RuntimeError):
+        o.zdf_phy(1)
+
+
+# ------------------------------------------------------------------------- GPU
+def tke_pair(prec, nmem=2, eos="seos", **over):
+    pytest.importorskip("torch")
+    eos_nam = dict(ln_seos=1) if eos == "seos" else dict(ln_eos80=1, ln_seos=0)
+    p = Pair(nn=2, prec=prec, seed=47, nmem=nmem, **{**TKE, **eos_nam, **over})
+    p.states = [vphys_state(p.dom, p.nam, st) for st in p.states]
+    p.bind_hotpath()
+    for n in VFIELDS:
+        p.bind(n)
+    return p
+
+
+# FP32: en and the coefficients pass through the shear of FP32 velocity differences,
+# square roots and MAX floors
+TOL_TKE = {"fp64": 1e-12, "mixed": 1e-4}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nn_mxl,ln_lc,nn_pdl", [(2, 1, 1), (0, 1, 1), (1, 0, 0), (3, 1, 1)])
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_gpu_zdf_phy(prec, nn_mxl, ln_lc, nn_pdl):
+    """Three zdf_phy calls from the cold start, two members, compared after each."""
+    p = tke_pair(prec, nn_mxl=nn_mxl, ln_lc=ln_lc, nn_pdl=nn_pdl)
+    for kt in (1, 2, 3):
+        for o in p.ora:
+            o.zdf_phy(kt)
+        p.ctx.zdf_phy(kt)
+        p.ctx.synchronize()
+        for n in OUT:
+            p.compare(n, p.s3, TOL_TKE[prec])
+    avt = p.per_member(p.dev["AVT"], p.s3)
+    for i, j, k in UNSTABLE:
+        assert avt[0][i, j, k] == 100.0 and avt[1][i, j, k] == 100.0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("eos", ["seos", "eos80"])
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_gpu_stp_model_with_tke(prec, eos):
+    """The model step with its vertical physics (rab_3d and bn2 of the before and now
+    tracers, zdf_phy) ahead of the tracer and momentum path, eos and dyn_hpg of the
+    now tracers: steps 1 (Euler), 2, 3 (graph capture) and 4 (replay)."""
+    p = tke_pair(prec, eos=eos, neuler=0)
+    for st in p.states:
+        st.update(rhd=np.zeros(p.s3), rhop=np.zeros(p.s3))
+    for n in ("GDEPT_N", "RHD", "RHOP"):
+        p.bind(n)
+    for kt in (1, 2, 3, 4):
+        for o in p.ora:
+            o.stp_model(kt)
+        p.ctx.stp_model(kt)
+    p.ctx.synchronize()
+    fp64 = prec == "fp64"
+    p.compare("TSN", p.s4, 1e-12 if fp64 else 1e-4)
+    for n in ("UN", "VN"):
+        p.compare(n, p.s3, 1e-12 if fp64 else 2e-3)
+    for n in ("RN2", "RN2B") if fp64 else ():
+        p.compare(n, p.s3, 1e-12)
+    # the mixed form's N^2 comes from FP32 tracer differences: the closure follows
+    # it to a looser tolerance than a call on identical inputs
+    for n in OUT:
+        p.compare(n, p.s3, 1e-12 if fp64 else 5e-2)
