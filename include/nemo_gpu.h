@@ -435,9 +435,16 @@ int nemo_gpu_wzv(nemo_ctx *ctx, int kt);
  * otherwise. */
 int nemo_gpu_ldf_slp(nemo_ctx *ctx, int kt, const void *prd, const void *pn2);
 
-/* The time step of dyn_zdf (dynzdf.F90:112) without vertical viscosity or drag:
- * ua = (ub + r2dt ua) umask, va likewise. The implicit viscosity solve of
- * dynzdf.F90:160-330 is not implemented. */
+/* dyn_zdf (dynzdf.F90:47-499). Its leap-frog time step ua = (ub + r2dt ua) umask, va
+ * likewise (:112); and, while the ocean viscosity NEMO_F_AVM is bound, the implicit
+ * vertical viscosity of a linear free surface with the split-explicit free surface
+ * and implicit bottom drag (ln_drgimp, the reference's default), iso-level lateral
+ * mixing and ln_zad_Aimp off: the barotropic after velocity UA_B / VA_B of
+ * dyn_spg_ts removed and its bottom stress (RCDU_BOT) added (:122-141), the
+ * tridiagonal system of avm with the implicit drag on the bottom diagonal and the
+ * wind stress (utau_b + utau) / 2 in the surface right-hand side (UTAU_B, VTAU_B when
+ * bound, else UTAU, VTAU), solved per column (:205-302). nemo_gpu_stp_model runs it
+ * after dyn_spg_ts. */
 int nemo_gpu_dyn_zdf_step(nemo_ctx *ctx, int kt);
 /* dyn_nxt (dynnxt.F90:66-377) for ln_linssh with ln_dynspg_ts and ln_bt_fw: the
  * barotropic part of ua replaced by ua_b, lbc_lnk, the Euler swap or the Asselin

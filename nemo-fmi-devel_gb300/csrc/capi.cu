@@ -82,6 +82,7 @@ struct nemo_ctx {
   void* rab_w = nullptr;       // the model step's before expansion ratios rab_b (jpi,jpj,jpk,2)
   void* rab_n = nullptr;       // and the now ones rab_n, with the vertical physics
   void* zphy_w = nullptr;      // zdf_phy work: sh2, apdlr and the TKE system, 5 x n3 per member
+  void* zdyn_w = nullptr;      // dyn_zdf work: the implicit viscosity system, 2 x n3 per member
   void* blp_w = nullptr;       // tra_ldf_blp: the first laplacian (jpi,jpj,jpk,kjpt) per member
   int blp_kjpt = 0;
   int iso_kjpt = 0;
@@ -1008,13 +1009,46 @@ int run_wzv(nemo_ctx* c, int kt) {
   return NEMO_OK;
 }
 
+// dyn_zdf: the time step alone, or with the implicit vertical viscosity where the
+// ocean avm is bound
+int dyn_zdf_check(nemo_ctx* c) {
+  void* const* F = c->f;
+  for (int id : {NEMO_F_UA, NEMO_F_VA, NEMO_F_UB, NEMO_F_VB})
+    if (!F[id]) return fail(c, NEMO_ERR_UNBOUND, "dyn_zdf: ua, va, ub and vb must be bound");
+  if (!F[NEMO_F_AVM]) return NEMO_OK;
+  for (int id : {NEMO_F_UA_B, NEMO_F_VA_B, NEMO_F_RCDU_BOT, NEMO_F_UTAU, NEMO_F_VTAU})
+    if (!F[id]) return fail(c, NEMO_ERR_UNBOUND, "dyn_zdf with avm: ua_b, va_b, rcdu_bot, utau, vtau must be bound");
+  const nemo_namelist& nm = c->nam;
+  if (!nm.ln_linssh || nm.ln_isfcav || nm.ln_zad_Aimp)
+    return fail(c, NEMO_ERR_UNSUPPORTED, "dyn_zdf with avm: a linear free surface without cavities or ln_zad_Aimp");
+  return NEMO_OK;
+}
+
 template <class T>
 int run_dyn_zdf_step(nemo_ctx* c, int kt) {
   const nemo_namelist& nm = c->nam;
+  void* const* F = c->f;
   const double r2dt = (nm.neuler == 0 && kt == nm.nit000) ? nm.rn_rdt : 2.0 * nm.rn_rdt;
-  cudaError_t e = launch_dyn_zdf_step<T>(dom_now<T>(c), (const T*)c->f[NEMO_F_UB], (const T*)c->f[NEMO_F_VB],
-                                         (T*)c->f[NEMO_F_UA], (T*)c->f[NEMO_F_VA], (T)r2dt, c->stream);
-  if (e != cudaSuccess) return cuda_fail(c, e, "dyn_zdf step launch");
+  cudaError_t e;
+  if (!F[NEMO_F_AVM]) {
+    e = launch_dyn_zdf_step<T>(dom_now<T>(c), (const T*)F[NEMO_F_UB], (const T*)F[NEMO_F_VB], (T*)F[NEMO_F_UA],
+                               (T*)F[NEMO_F_VA], (T)r2dt, c->stream);
+  } else {
+    const size_t n = (size_t)c->n3 * c->nmem;
+    if (!c->zdyn_w && cudaMalloc(&c->zdyn_w, 2 * n * sizeof(T)) != cudaSuccess)
+      return fail(c, NEMO_ERR_NOMEM, "dyn_zdf work arrays");
+    DynZdfArgs<T> a{};
+    a.ub = (const T*)F[NEMO_F_UB]; a.vb = (const T*)F[NEMO_F_VB]; a.avm = (const T*)F[NEMO_F_AVM];
+    a.rcdu = (const T*)F[NEMO_F_RCDU_BOT]; a.utau = (const T*)F[NEMO_F_UTAU]; a.vtau = (const T*)F[NEMO_F_VTAU];
+    a.utau_b = F[NEMO_F_UTAU_B] ? (const T*)F[NEMO_F_UTAU_B] : a.utau;
+    a.vtau_b = F[NEMO_F_VTAU_B] ? (const T*)F[NEMO_F_VTAU_B] : a.vtau;
+    a.ua_b = (const double*)F[NEMO_F_UA_B]; a.va_b = (const double*)F[NEMO_F_VA_B];
+    a.ua = (T*)F[NEMO_F_UA]; a.va = (T*)F[NEMO_F_VA];
+    a.zwd = (T*)c->zdyn_w; a.zws = a.zwd + n;
+    a.r2dt = (T)r2dt; a.zdt = (T)(r2dt * 0.5); a.rau0 = (T)nm.rau0;
+    e = launch_dyn_zdf_imp<T>(dom_now<T>(c), a, c->stream);
+  }
+  if (e != cudaSuccess) return cuda_fail(c, e, "dyn_zdf launch");
   return NEMO_OK;
 }
 
@@ -1341,6 +1375,7 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
   }
   mark(0);
   if (model) {  // ua = va = 0 (step.F90:183-184)
+    if (int s = dyn_zdf_check(c)) return s;
     const bool vphys = zphy_on(c);
     if (vphys) {
       int s = run_vphys<T>(c);
@@ -1667,7 +1702,7 @@ int nemo_gpu_destroy(nemo_ctx* c) {
   for (auto p : c->iso_w) cudaFree(p);
   for (auto p : c->adj_w) cudaFree(p);
   cudaFree(c->slp_w);
-  cudaFree(c->rab_w); cudaFree(c->rab_n); cudaFree(c->zphy_w);
+  cudaFree(c->rab_w); cudaFree(c->rab_n); cudaFree(c->zphy_w); cudaFree(c->zdyn_w);
   cudaFree(c->blp_w);
   for (auto p : c->spg_w) cudaFree(p);
   for (auto p : c->spg_cor) cudaFree(p);
@@ -2119,8 +2154,7 @@ int nemo_gpu_wzv(nemo_ctx* c, int kt) {
 int nemo_gpu_dyn_zdf_step(nemo_ctx* c, int kt) {
   if (!c) return NEMO_ERR_ARG;
   if (join_copies(c)) return NEMO_ERR_CUDA;
-  for (int id : {NEMO_F_UA, NEMO_F_VA, NEMO_F_UB, NEMO_F_VB})
-    if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "dyn_zdf_step: ua, va, ub and vb must be bound");
+  if (int s = dyn_zdf_check(c)) return s;
   return c->prec == NEMO_PREC_FP64 ? run_dyn_zdf_step<double>(c, kt) : run_dyn_zdf_step<float>(c, kt);
 }
 

@@ -91,6 +91,13 @@ cudaError_t launch_zdf_mxl(const Dom<T>& d, const MxlArgs<T>& a, cudaStream_t s)
 }
 
 template <class T>
+cudaError_t launch_dyn_zdf_imp(const Dom<T>& d, const DynZdfArgs<T>& a, cudaStream_t s) {
+  k_dyn_zdf_imp<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a);
+  ktick(NEMO_K_DYN_ZDF_STEP, s);
+  return cudaGetLastError();
+}
+
+template <class T>
 cudaError_t launch_zdf_phy(const Dom<T>& d, const ZphyArgs<T>& a, cudaStream_t s) {
   k_zdf_sh2<T><<<s_pt(d), dim3(SX, SY), 0, s>>>(d, a);
   ktick(NEMO_K_ZDF_PHY, s);
@@ -165,6 +172,7 @@ cudaError_t launch_dia_hsb(const Dom<T>& d, const HsbArgs<T>& a, double* part, i
   template cudaError_t launch_eos<T>(const Dom<T>&, const EosArgs<T>&, cudaStream_t);                      \
   template cudaError_t launch_dyn_hpg<T>(const Dom<T>&, const T*, T*, T*, T, cudaStream_t);              \
   template cudaError_t launch_zdf_mxl<T>(const Dom<T>&, const MxlArgs<T>&, cudaStream_t);                  \
+  template cudaError_t launch_dyn_zdf_imp<T>(const Dom<T>&, const DynZdfArgs<T>&, cudaStream_t);           \
   template cudaError_t launch_zdf_phy<T>(const Dom<T>&, const ZphyArgs<T>&, cudaStream_t);                 \
   template cudaError_t launch_dyn_ldf_lap<T>(const Dom<T>&, const T*, const T*, const T*, const T*, T*, T*, T,   \
                                              cudaStream_t);                                             \

@@ -6,6 +6,7 @@
 // 0 by the caller. T is the bulk type, A the type of the barotropic accumulators
 // (ua_b, va_b, ssha: double in both forms).
 #pragma once
+#include "nemo_sin.h"
 #include "step.h"
 
 namespace nemo {
@@ -47,6 +48,82 @@ __global__ void k_dyn_zdf_step(Dom<T> d, RO<T> ub, RO<T> vb, T* ua, T* va, T r2d
   const ColInfo ci = d.ci[c.ij];
   ua[q] = (ub[q] + r2dt * ua[q]) * umsk<T>(ci, c.k);
   va[q] = (vb[q] + r2dt * va[q]) * vmsk<T>(ci, c.k);
+}
+
+// The implicit vertical viscosity of one U- (V-) column of dyn_zdf
+// (dynzdf.F90:127-141, :205-302) after its time step: the bottom stress of the
+// barotropic after velocity ab, then the system of avm (iso-level lateral mixing,
+// no adaptive-implicit advection) with the surface condition, the implicit drag on
+// the bottom diagonal and the wind stress in the surface right-hand side, assembled
+// and forward-eliminated in one downward sweep (its diagonals kept in zwd, zws) and
+// back-substituted upwards. The W-point scale factor across the U- (V-) point is the
+// MIN of the neighbouring e3w (the rest state of a linear free surface).
+template <bool U, class T>
+__device__ __forceinline__ void dyn_zdf_column(const Dom<T>& d, const DynZdfArgs<T>& a, long ij, int m,
+                                               const ColInfo& ci, T* pa, const double* ab, const T* tau,
+                                               const T* tau_b) {
+  const long n2 = d.n2, m3 = (long)m * d.n3 + ij, p2 = (long)m * d.n2 + ij;
+  const long nb = U ? 1 : d.jpi;
+  const int jpk = d.jpk, kb = U ? ci.mbku : ci.mbkv;
+  auto mk = [&](int k) { return U ? umsk<T>(ci, k) : vmsk<T>(ci, k); };
+  auto e3 = [&](int k) { return U ? d.e3u_n(ij, k, m) : d.e3v_n(ij, k, m); };
+  auto e3xw = [&](int k) { return fmn(d.e3w_n(ij, k, m), d.e3w_n(ij + nb, k, m)); };
+  auto wxm = [&](int k) { return k == 1 ? mk(1) : mk(k) * mk(k - 1); };
+  const T rc = a.rcdu[p2 + nb] + a.rcdu[p2];
+  {
+    const long q = m3 + (long)(kb - 1) * n2;
+    pa[q] = pa[q] + a.r2dt * T(0.5) * rc * (T)ab[p2] / e3(kb);
+  }
+  T wd_p = T(1), ws_p = T(0), x_p = T(0);
+  for (int k = 1; k <= jpk - 1; ++k) {
+    const long q = m3 + (long)(k - 1) * n2;
+    const T ze3a = e3(k);
+    const T zzws = -a.zdt * (a.avm[q + n2 + nb] + a.avm[q + n2]) / (ze3a * e3xw(k + 1)) * wxm(k + 1);
+    T wd, x = pa[q];
+    if (k == 1) {
+      wd = T(1) - zzws;
+      if (k == kb) wd = wd - a.r2dt * T(0.5) * rc / e3(kb);
+      x = x + a.r2dt * T(0.5) * (tau_b[p2] + tau[p2]) / (ze3a * a.rau0) * mk(1);
+    } else {
+      const T zzwi = -a.zdt * (a.avm[q + nb] + a.avm[q]) / (ze3a * e3xw(k)) * wxm(k);
+      wd = T(1) - zzwi - zzws;
+      if (k == kb) wd = wd - a.r2dt * T(0.5) * rc / e3(kb);
+      wd = wd - zzwi * ws_p / wd_p;
+      x = x - zzwi / wd_p * x_p;
+    }
+    a.zwd[q] = wd;
+    a.zws[q] = zzws;
+    pa[q] = x;
+    wd_p = wd; ws_p = zzws; x_p = x;
+  }
+  T nxt = T(0);
+  for (int k = jpk - 1; k >= 1; --k) {
+    const long q = m3 + (long)(k - 1) * n2;
+    const T x = (k == jpk - 1) ? pa[q] / a.zwd[q] : (pa[q] - a.zws[q] * nxt) / a.zwd[q];
+    pa[q] = x;
+    nxt = x;
+  }
+}
+
+// dyn_zdf (dynzdf.F90:47-499) with the implicit vertical viscosity, one column per
+// thread: the time step and the removal of the barotropic after velocity on every
+// column (:112, :122-126), then the u and v systems of the interior columns.
+template <class T>
+__global__ void k_dyn_zdf_imp(Dom<T> d, DynZdfArgs<T> a) {
+  const ColIdx<T> c = col_index(d);
+  if (!c.valid) return;
+  const long n2 = d.n2, m3 = (long)c.m * d.n3 + c.ij, p2 = (long)c.m * d.n2 + c.ij;
+  const ColInfo ci = d.ci[c.ij];
+  const T uab = (T)a.ua_b[p2], vab = (T)a.va_b[p2];
+  for (int k = 1; k <= d.jpk - 1; ++k) {
+    const long q = m3 + (long)(k - 1) * n2;
+    const T um = umsk<T>(ci, k), vm = vmsk<T>(ci, k);
+    a.ua[q] = ((a.ub[q] + a.r2dt * a.ua[q]) * um - uab) * um;
+    a.va[q] = ((a.vb[q] + a.r2dt * a.va[q]) * vm - vab) * vm;
+  }
+  if (!c.interior) return;
+  dyn_zdf_column<true>(d, a, c.ij, c.m, ci, a.ua, a.ua_b, a.utau, a.utau_b);
+  dyn_zdf_column<false>(d, a, c.ij, c.m, ci, a.va, a.va_b, a.vtau, a.vtau_b);
 }
 
 // dyn_nxt (dynnxt.F90:114-358; linear free surface, ln_dynspg_ts with ln_bt_fw),
@@ -794,6 +871,11 @@ __global__ void k_dyn_zad(Dom<T> d, const T* __restrict__ un, const T* __restric
 }
 
 // ---------------------------------------------------------------- zdf_phy (TKE)
+// SIN of the Langmuir-cell source: FP64 by the evaluation the test oracle shares
+// (nemo_sin.h), FP32 by the library
+__device__ __forceinline__ double lc_sin(double x) { return nemo_sin_0pi(x); }
+__device__ __forceinline__ float lc_sin(float x) { return sinf(x); }
+
 // 2 x the shear production at the uw-point (i+1/2, j, k) and the vw-point
 // (i, j+1/2, k) of column ij (zdfsh2.F90:57-66) with the closure's avm_k. With a
 // linear free surface e3uw_n = e3uw_b = the rest-state MIN of the neighbouring e3w.
@@ -889,7 +971,7 @@ __global__ void k_zdf_tke(Dom<T> d, ZphyArgs<T> a) {
     if (zfr != T(0)) {
       const T dep = a.gdepw[q];
       if (dep - zhlc < T(0) && wm != T(0)) {
-        const T zwlc = a.rn_lc * sin(a.rpi * dep / zhlc);
+        const T zwlc = a.rn_lc * lc_sin(a.rpi * dep / zhlc);
         en = en + a.rdt * zfr * (zwlc * zwlc * zwlc) / zhlc;
       }
     }

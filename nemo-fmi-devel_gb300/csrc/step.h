@@ -75,6 +75,18 @@ struct MxlArgs {
   int nlb10;
 };
 
+// dyn_zdf with the implicit vertical viscosity: the ocean avm, the bottom drag
+// rcdu (2-D), the wind stress (utau_b may be utau), the barotropic after velocity of
+// dyn_spg_ts (FP64 in both precisions); work: the diagonal and upper diagonal of the
+// system, n3 per member each (u and v in turn)
+template <class T>
+struct DynZdfArgs {
+  const T *ub, *vb, *avm, *rcdu, *utau, *vtau, *utau_b, *vtau_b;
+  const double *ua_b, *va_b;
+  T *ua, *va, *zwd, *zws;
+  T r2dt, zdt, rau0;
+};
+
 // zdf_phy with the TKE closure and zdf_evd. Member strides n3 (3-D) and n2 (taum,
 // fr_i). Work arrays (n3 per member): sh2, apdlr (the inverse Prandtl number), and
 // the three diagonals of the TKE system, whose storage the mixing lengths zmxlm
@@ -100,6 +112,8 @@ template <class T>
 cudaError_t launch_dyn_zad(const Dom<T>& d, const T* un, const T* vn, const T* wn, T* ua, T* va, cudaStream_t s);
 template <class T>
 cudaError_t launch_zdf_mxl(const Dom<T>& d, const MxlArgs<T>& a, cudaStream_t s);
+template <class T>
+cudaError_t launch_dyn_zdf_imp(const Dom<T>& d, const DynZdfArgs<T>& a, cudaStream_t s);
 template <class T>
 cudaError_t launch_zdf_phy(const Dom<T>& d, const ZphyArgs<T>& a, cudaStream_t s);
 template <class T>

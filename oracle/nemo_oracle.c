@@ -14,6 +14,7 @@
  */
 #include "nemo_oracle.h"
 #include "../nemo-fmi-devel_gb300/csrc/eos80.h"
+#include "../nemo-fmi-devel_gb300/csrc/nemo_sin.h"
 
 #include <math.h>
 #include <stdint.h>
@@ -1686,6 +1687,9 @@ int ora_glob_sum(ora_ctx *c, const double *ptab, int nk, double *out) {
   return NEMO_OK;
 }
 
+/* the shared sine of the Langmuir-cell source, exported for its accuracy test */
+double ora_sin_0pi(double x) { return nemo_sin_0pi(x); }
+
 /* ---------------------------------------------------------------- zdf_phy */
 /* zdf_phy (zdfphy.F90:243-291) for the TKE closure: zdf_sh2 (zdfsh2.F90:30-76)
  * with the closure's avm_k, zdf_tke = tke_tke + tke_avn (zdftke.F90:168-630) for
@@ -1780,7 +1784,8 @@ int ora_zdf_phy(ora_ctx *c, int kt) {
           const size_t p = I2(ji, jj), q = I3(ji, jj, jk);
           if (zfr_i[p] != 0.) {
             if (pdepw[q] - zhlc[p] < 0 && wmask[q] != 0.) {
-              const double zwlc = nm->rn_lc * sin(rpi * pdepw[q] / zhlc[p]);
+              /* SIN by the evaluation the CUDA kernels share (nemo_sin.h) */
+              const double zwlc = nm->rn_lc * nemo_sin_0pi(rpi * pdepw[q] / zhlc[p]);
               en[q] = en[q] + rdt * zfr_i[p] * (zwlc * zwlc * zwlc) / zhlc[p];
             }
           }
@@ -2789,8 +2794,16 @@ int ora_wzv(ora_ctx *c, int kt) {
   return NEMO_OK;
 }
 
-/* The time step of dyn_zdf (dynzdf.F90:112) without vertical viscosity or drag:
- * ua = (ub + r2dt ua) umask; the implicit viscosity solve is not on the path. */
+/* dyn_zdf (dynzdf.F90:47-499). The leap-frog time step ua = (ub + r2dt ua) umask
+ * (:112); then, where the ocean viscosity AVM is bound, the implicit vertical
+ * viscosity of a linear free surface with the split-explicit free surface and
+ * implicit bottom drag (ln_drgimp, the reference's default), iso-level lateral
+ * mixing and no adaptive-implicit advection: the barotropic after velocity ua_b
+ * removed (:122-126) and its bottom stress added (:127-141), the matrix of avm
+ * (:205-232) with the implicit drag on the bottom diagonal (:243-250), and the
+ * Thomas solve with the wind stress (utau_b + utau) / 2 in the surface right-hand
+ * side (:266-302); u then v. utau_b, vtau_b: the bound ones, else utau, vtau. The
+ * U- and V-W scale factors are the MIN of the neighbouring e3w_0 (domzgr). */
 int ora_dyn_zdf_step(ora_ctx *c, int kt) {
   const nemo_namelist *nm = &c->nam;
   const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
@@ -2803,6 +2816,91 @@ int ora_dyn_zdf_step(ora_ctx *c, int kt) {
     ua[q] = (ub[q] + r2dt * ua[q]) * c->umask[q];
     va[q] = (vb[q] + r2dt * va[q]) * c->vmask[q];
   }
+  const double *avm = c->f[NEMO_F_AVM];
+  if (!avm) return NEMO_OK;
+  const double *ua_b = c->f[NEMO_F_UA_B], *va_b = c->f[NEMO_F_VA_B], *rcdu = c->f[NEMO_F_RCDU_BOT];
+  const double *utau = c->f[NEMO_F_UTAU], *vtau = c->f[NEMO_F_VTAU];
+  const double *utau_b = c->f[NEMO_F_UTAU_B] ? c->f[NEMO_F_UTAU_B] : utau;
+  const double *vtau_b = c->f[NEMO_F_VTAU_B] ? c->f[NEMO_F_VTAU_B] : vtau;
+  if (!ua_b || !va_b || !rcdu || !utau || !vtau) return NEMO_ERR_UNBOUND;
+  if (!nm->ln_linssh || nm->ln_isfcav || nm->ln_zad_Aimp) return NEMO_ERR_UNSUPPORTED;
+  const double *umask = c->umask, *vmask = c->vmask;
+  const double *e3u = fld(c, NEMO_F_E3U_N), *e3v = fld(c, NEMO_F_E3V_N), *e3w = fld(c, NEMO_F_E3W_N);
+  const double zdt = r2dt * 0.5, rau0 = nm->rau0;
+  for (int jk = 1; jk <= jpk - 1; ++jk)  /* (:122-126) */
+    for (size_t p = 0; p < n2; ++p) {
+      const size_t q = p + n2 * (jk - 1);
+      ua[q] = (ua[q] - ua_b[p]) * umask[q];
+      va[q] = (va[q] - va_b[p]) * vmask[q];
+    }
+  for (int jj = 2; jj <= jpj - 1; ++jj)  /* (:127-141) */
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      const size_t p = I2(ji, jj);
+      const int iku = c->mbku[p], ikv = c->mbkv[p];
+      ua[I3(ji, jj, iku)] = ua[I3(ji, jj, iku)] +
+                            r2dt * 0.5 * (rcdu[I2(ji + 1, jj)] + rcdu[p]) * ua_b[p] / e3u[I3(ji, jj, iku)];
+      va[I3(ji, jj, ikv)] = va[I3(ji, jj, ikv)] +
+                            r2dt * 0.5 * (rcdu[I2(ji, jj + 1)] + rcdu[p]) * va_b[p] / e3v[I3(ji, jj, ikv)];
+    }
+  double *zwi = zalloc(n3), *zwd = zalloc(n3), *zws = zalloc(n3);
+  for (int comp = 0; comp < 2; ++comp) {
+    const int u = comp == 0;
+    double *pa = u ? ua : va;
+    const double *mask = u ? umask : vmask, *e3 = u ? e3u : e3v, *tau = u ? utau : vtau, *tau_b = u ? utau_b : vtau_b;
+    const int *mbk = u ? c->mbku : c->mbkv;
+    const size_t nb = u ? 1 : (size_t)jpi;  /* the neighbour across the U- (V-) point */
+#define WXM(q, jk) ((jk) == 1 ? mask[q] : mask[q] * mask[(q) - n2])
+#define E3XW(q) dmin(e3w[q], e3w[(q) + nb])
+    for (int jk = 1; jk <= jpk - 1; ++jk)  /* matrix (:222-232) */
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          const size_t q = I3(ji, jj, jk);
+          const double ze3a = e3[q];
+          const double zzwi = -zdt * (avm[q + nb] + avm[q]) / (ze3a * E3XW(q)) * WXM(q, jk);
+          const double zzws = -zdt * (avm[q + n2 + nb] + avm[q + n2]) / (ze3a * E3XW(q + n2)) * WXM(q + n2, jk + 1);
+          zwi[q] = zzwi;
+          zws[q] = zzws;
+          zwd[q] = 1. - zzwi - zzws;
+        }
+    for (int jj = 2; jj <= jpj - 1; ++jj)  /* surface (:234-239), implicit bottom drag (:243-250) */
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t p = I2(ji, jj), qb = I3(ji, jj, mbk[p]);
+        zwi[p] = 0.;
+        zwd[p] = 1. - zws[p];
+        zwd[qb] = zwd[qb] - r2dt * 0.5 * (rcdu[p + nb] + rcdu[p]) / e3[qb];
+      }
+    for (int jk = 2; jk <= jpk - 1; ++jk)  /* first recurrence (:266-272) */
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          const size_t q = I3(ji, jj, jk);
+          zwd[q] = zwd[q] - zwi[q] * zws[q - n2] / zwd[q - n2];
+        }
+    for (int jj = 2; jj <= jpj - 1; ++jj)  /* wind stress (:274-279) */
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t p = I2(ji, jj);
+        pa[p] = pa[p] + r2dt * 0.5 * (tau_b[p] + tau[p]) / (e3[p] * rau0) * mask[p];
+      }
+    for (int jk = 2; jk <= jpk - 1; ++jk)  /* second recurrence (:280-286) */
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          const size_t q = I3(ji, jj, jk);
+          pa[q] = pa[q] - zwi[q] / zwd[q - n2] * pa[q - n2];
+        }
+    for (int jj = 2; jj <= jpj - 1; ++jj)  /* third recurrence (:288-299) */
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t q = I3(ji, jj, jpk - 1);
+        pa[q] = pa[q] / zwd[q];
+      }
+    for (int jk = jpk - 2; jk >= 1; --jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          const size_t q = I3(ji, jj, jk);
+          pa[q] = (pa[q] - zws[q] * pa[q + n2]) / zwd[q];
+        }
+#undef WXM
+#undef E3XW
+  }
+  wfree(zwi); wfree(zwd); wfree(zws);
   return NEMO_OK;
 }
 

@@ -46,6 +46,7 @@ def lib():
         P("ora_set_threads", [i])
         P("ora_stp_ctl", [vp, i, vp, vp, C.POINTER(i)])
         P("ora_zdf_phy", [vp, i])
+        P("ora_sin_0pi", [d], d)
         P("ora_dia_hsb_init", [vp])
         P("ora_dia_hsb", [vp, i, vp])
         P("ora_stp_ctl_last", [vp, vp, vp, C.POINTER(i)])

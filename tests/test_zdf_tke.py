@@ -140,6 +140,8 @@ def tke_pair(prec, nmem=2, eos="seos", **over):
 # FP32: en and the coefficients pass through the shear of FP32 velocity differences,
 # square roots and MAX floors
 TOL_TKE = {"fp64": 1e-12, "mixed": 1e-4}
+# and after four model steps, where the FP32 tracers' N^2 feeds the closure
+TOL_TKE_STEP = dict(EN=1e-2, DISSL=1e-4, AVM_K=2e-2, AVT_K=2e-2, AVM=2e-2, AVT=2e-2, AVS=2e-2)
 
 
 @pytest.mark.gpu
@@ -160,14 +162,8 @@ def test_gpu_zdf_phy(prec, nn_mxl, ln_lc, nn_pdl):
         assert avt[0][i, j, k] == 100.0 and avt[1][i, j, k] == 100.0
 
 
-@pytest.mark.gpu
-@pytest.mark.parametrize("eos", ["seos", "eos80"])
-@pytest.mark.parametrize("prec", ["fp64", "mixed"])
-def test_gpu_stp_model_with_tke(prec, eos):
-    """The model step with its vertical physics (rab_3d and bn2 of the before and now
-    tracers, zdf_phy) ahead of the tracer and momentum path, eos and dyn_hpg of the
-    now tracers: steps 1 (Euler), 2, 3 (graph capture) and 4 (replay)."""
-    p = tke_pair(prec, eos=eos, neuler=0)
+def run_model_with_tke(prec, eos, **over):
+    p = tke_pair(prec, eos=eos, neuler=0, **over)
     for st in p.states:
         st.update(rhd=np.zeros(p.s3), rhop=np.zeros(p.s3))
     for n in ("GDEPT_N", "RHD", "RHOP"):
@@ -177,13 +173,50 @@ def test_gpu_stp_model_with_tke(prec, eos):
             o.stp_model(kt)
         p.ctx.stp_model(kt)
     p.ctx.synchronize()
-    fp64 = prec == "fp64"
-    p.compare("TSN", p.s4, 1e-12 if fp64 else 1e-4)
-    for n in ("UN", "VN"):
-        p.compare(n, p.s3, 1e-12 if fp64 else 2e-3)
-    for n in ("RN2", "RN2B") if fp64 else ():
+    return p
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("eos", ["seos", "eos80"])
+def test_gpu_stp_model_with_tke_fp64(eos):
+    """The model step with its vertical physics (rab_3d and bn2 of the before and now
+    tracers, zdf_phy, the implicit viscosity of dyn_zdf) in FP64: steps 1 (Euler), 2,
+    3 (graph capture) and 4 (replay) against the oracle."""
+    p = run_model_with_tke("fp64", eos)
+    p.compare("TSN", p.s4, 1e-12)
+    for n in ("UN", "VN", "RN2", "RN2B") + OUT:
         p.compare(n, p.s3, 1e-12)
-    # the mixed form's N^2 comes from FP32 tracer differences: the closure follows
-    # it to a looser tolerance than a call on identical inputs
-    for n in OUT:
-        p.compare(n, p.s3, 1e-12 if fp64 else 5e-2)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("eos", ["seos", "eos80"])
+def test_gpu_stp_model_with_tke_mixed(eos):
+    """The same model steps in the mixed form. Enhanced vertical diffusion is a
+    threshold on N^2 (<= -1e-12, avt jumps to 100 m2/s), and the FP32 tracer
+    differences that form N^2 decide it differently where the water is neutral; so
+    without it the form is held to the field tolerances, and with it to the share of
+    w-points where the decision differs and to the tracers of the columns whose
+    decisions agree."""
+    p = run_model_with_tke("mixed", eos, ln_zdfevd=0)
+    p.compare("TSN", p.s4, 1e-4)
+    for n in ("UN", "VN"):
+        p.compare(n, p.s3, 2e-3)
+    for n in OUT:  # measured after four steps: en 3e-3, dissl 3e-6, the coefficients 6e-3
+        p.compare(n, p.s3, TOL_TKE_STEP[n])
+    p = run_model_with_tke("mixed", eos)
+    avt = p.per_member(p.dev["AVT"], p.s3)
+    tsn = p.per_member(p.dev["TSN"], p.s4)
+    wm = gyre.masks(p.dom)[3] > 0
+    for m in range(p.nmem):
+        flip = (avt[m] >= 1.0) != (p.host[m]["AVT"] >= 1.0)
+        share = flip[wm].mean()
+        cols = flip.any(axis=2)
+        keep = ~cols
+        for _ in range(8):  # four steps of advection and diffusion reach 2 points each
+            keep[1:-1, 1:-1] &= keep[:-2, 1:-1] & keep[2:, 1:-1] & keep[1:-1, :-2] & keep[1:-1, 2:]
+        ref, got = p.host[m]["TSN"][keep], tsn[m][keep]
+        err = np.abs(got - ref).max() / np.abs(ref).max()
+        # measured: decisions differ at 4e-5 .. 2e-4 of the w-points; the tracers of
+        # the other columns still feel those through the pressure gradient and the
+        # barotropic mode of the same steps: 2e-5 .. 5e-4
+        assert share < 1e-3 and keep.mean() > 0.5 and err <= 1e-3, (share, keep.mean(), err)
