@@ -264,16 +264,41 @@ def make_ctx(dom, nam, states, prec, stream):
     return ctx, dev
 
 
+def full_gyre(dom, nam, states):
+    """The namelist and the states of the full GYRE step (gyre.full_physics)."""
+    from nemo_gpu import gyre
+    out = [gyre.full_physics(dom, nam, st) for st in states]
+    return out[0][0], [st for _, st in out]
+
+
+def bind_full(ctx, dev, states):
+    """Bind the fields of the full GYRE step (besides make_ctx's)."""
+    import numpy as np
+    import torch
+    from nemo_gpu import gyre
+    for n in gyre.FULL_3D + gyre.FULL_2D:
+        t = ctx.to_device([s[n] for s in states])
+        dev[n.upper()] = t
+        ctx.bind(n.upper(), t)
+    t = torch.from_numpy(np.concatenate([np.asarray(s["nmln"], dtype=np.int32).ravel(order="F")
+                                         for s in states])).cuda()
+    dev["NMLN"] = t
+    ctx.bind("NMLN", t)
+
+
 def ten_days(dom, nam, states, stream, nsteps=120):
     """The mixed form against FP64 after ten model days (120 steps of rdt = 7200 s) of
-    nemo_gpu_stp_model from an Euler start on the same state: RMS over wet points
-    and max of |mixed - FP64| for T, S, SST, SSS, SSH, U, V."""
+    the full GYRE step (nemo_gpu_stp_model with GYRE's physics) from an Euler start on
+    the same state: RMS over wet points and max of |mixed - FP64| for T, S, SST, SSS,
+    SSH, U, V."""
     import numpy as np
     nam = dict(nam, neuler=0)
+    nam, states = full_gyre(dom, nam, states)
     jpi, jpj, jpk = dom["jpi"], dom["jpj"], dom["jpk"]
     out = {}
     for prec in ("fp64", "mixed"):
         ctx, dev = make_ctx(dom, nam, states, prec, stream)
+        bind_full(ctx, dev, states)
         for kt in range(1, nsteps + 1):
             ctx.stp_model(kt)
         ctx.synchronize()
@@ -284,8 +309,11 @@ def ten_days(dom, nam, states, stream, nsteps=120):
         del dev
     tm = np.arange(1, jpk + 1)[None, None, :] <= dom["k_bot"][:, :, None]
     res = {"steps": nsteps, "model_days": nsteps * nam["rn_rdt"] / 86400.0,
-           "step": "nemo_gpu_stp_model: the hot path + wzv, dyn_zdf time step, tra_nxt, dyn_nxt, ssh_swp; "
-                   "momentum trends outside the path held at 0"}
+           "step": "nemo_gpu_stp_model with GYRE's physics: rab_3d + bn2, zdf_phy (TKE, evd), zdf_mxl, "
+                   "eos_insitu + ldf_slp, dyn_keg + dyn_zad + vor_ene + dyn_ldf_lap, EOS-80 + dyn_hpg, "
+                   "dyn_spg_ts, wzv, dyn_zdf (implicit viscosity), tra_sbc + tra_qsr, the hot path, "
+                   "tra_nxt, dyn_nxt, ssh_swp, stp_ctl",
+           "forcing": "GYRE analytic fluxes of the first time step, held for the run"}
     for n, sel in (("T", None), ("S", None), ("SST", "T"), ("SSS", "S"), ("U", None), ("V", None), ("SSH", None)):
         a, b = out["mixed"][sel or n], out["fp64"][sel or n]
         if n in ("SST", "SSS"):
@@ -446,6 +474,18 @@ def run_gpu(args):
                "d2h_bytes_per_step": bo, "ms_per_step": wms / ke,
                "timer": "host wall clock from the first upload to the synchronize after the last download",
                "host_buffers": "pinned; nemo_gpu_field_upload/download through the C ABI"}
+    # ---------------------------------------------------------------- the full GYRE step
+    model = None
+    if not args.no_model and args.workload == "gyre":
+        km = max(3, args.steps // 5)
+        ms_m, kt_m = model_step(dom, nam, states, args.prec, stream, km, 3, local)
+        model = {"value": cells * world / (ms_m / 1e3), "unit": UNIT, "ms_per_step": ms_m, "steps": km,
+                 "step": "nemo_gpu_stp_model with GYRE's physics (EOS-80, TKE + evd, slopes from the tracers, "
+                         "momentum trends, implicit vertical viscosity, surface forcing, stp_ctl), "
+                         "device-resident, CUDA events",
+                 "launches_per_step": sum(v["launches"] for v in kt_m.values()),
+                 "kernels_us_per_step": {k: v["us"] * v["launches"] for k, v in
+                                         sorted(kt_m.items(), key=lambda kv: -kv[1]["us"] * kv[1]["launches"])}}
     # ---------------------------------------------------------------- roofline
     hbm, src = peaks()
     b = 1 if args.prec == "mixed" else 0
@@ -500,7 +540,7 @@ def run_gpu(args):
         "kernels": kernels,
         "routines": routines,
         "step_alg_GBps": step_bytes / (ms_step / 1e3) / 1e9,
-        "e2e": e2e, "fp64": fp64,
+        "e2e": e2e, "fp64": fp64, "model_step": model,
     }
     if fp64:
         res["speedup_vs_fp64"] = value / fp64["value"]
@@ -621,21 +661,15 @@ def run_reference(args):
     print(json.dumps(res))
 
 
-def run_model(args):
-    """The model step (nemo_gpu_stp_model: the hot path closed by wzv, the dyn_zdf
-    time step, tra_nxt, dyn_nxt, ssh_swp) on GYRE nn_GYRE=--nn, in --prec, device-resident."""
+def model_step(dom, nam, states, prec, stream, steps, warmup, local):
+    """Device time of the full GYRE step (nemo_gpu_stp_model with GYRE's physics) on
+    resident fields: ms per step, the kernels of one step and their launches."""
     import torch
     from nemo_gpu import dist
-    rank, world = dist.init("nccl")
-    _, _, local = dist.env_rank()
-    torch.cuda.set_device(local)
-    dom, nam, states = build_case(args.nn, args.members, seed=100 + rank)
-    nam = dict(nam, neuler=0)
-    jpi, jpj, jpk = dom["jpi"], dom["jpj"], dom["jpk"]
-    cells = jpi * jpj * jpk * args.members
-    stream = torch.cuda.Stream()
-    ctx, dev = make_ctx(dom, nam, states, args.prec, stream)
-    for w in range(args.warmup):
+    nam, states = full_gyre(dom, dict(nam, neuler=0), states)
+    ctx, dev = make_ctx(dom, nam, states, prec, stream)
+    bind_full(ctx, dev, states)
+    for w in range(warmup):
         ctx.stp_model(1 + w)
     ctx.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -643,8 +677,8 @@ def run_model(args):
     torch.cuda.synchronize()
     with torch.cuda.stream(stream):
         e0.record(stream)
-        for s in range(args.steps):
-            ctx.stp_model(1 + args.warmup + s)
+        for s in range(steps):
+            ctx.stp_model(1 + warmup + s)
         e1.record(stream)
     torch.cuda.synchronize()
     ms = dist.max_over_ranks(e0.elapsed_time(e1), device=f"cuda:{local}")
@@ -654,14 +688,32 @@ def run_model(args):
     ctx.synchronize()
     kt = {k: {"us": 1e3 * v[0] / v[1], "launches": v[1] / 3} for k, v in ctx.get_kernel_timing().items()}
     ctx.set_timing(False)
+    ctx.close()
+    return ms / steps, kt
+
+
+def run_model(args):
+    """The full GYRE step (nemo_gpu_stp_model with GYRE's physics) on GYRE
+    nn_GYRE=--nn, in --prec, device-resident."""
+    import torch
+    from nemo_gpu import dist
+    rank, world = dist.init("nccl")
+    _, _, local = dist.env_rank()
+    torch.cuda.set_device(local)
+    dom, nam, states = build_case(args.nn, args.members, seed=100 + rank)
+    jpi, jpj, jpk = dom["jpi"], dom["jpj"], dom["jpk"]
+    cells = jpi * jpj * jpk * args.members
+    stream = torch.cuda.Stream()
+    ms_step, kt = model_step(dom, nam, states, args.prec, stream, args.steps, args.warmup, local)
+    ms = ms_step * args.steps
     if rank == 0:
         print(json.dumps({
-            "metric": "cell-steps/s of the model step (hot path + wzv, dyn_zdf time step, tra_nxt, dyn_nxt, ssh_swp)",
+            "metric": "cell-steps/s of the full GYRE step (nemo_gpu_stp_model with GYRE's physics)",
             "value": cells * world * args.steps / (ms / 1e3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": DTYPE_MIXED if args.prec == "mixed" else "f64",
             "data": "synthetic: seeded GYRE analytic state",
-            "config": {"workload": f"GYRE nn_GYRE={args.nn} model step", "grid": [jpi, jpj, jpk],
+            "config": {"workload": f"GYRE nn_GYRE={args.nn} full model step", "grid": [jpi, jpj, jpk],
                        "members": args.members, "cells": cells},
             "gpu_launches": int(round(sum(v["launches"] for v in kt.values()) * args.steps)), "kernels": kt}))
 
@@ -748,6 +800,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default 32 x 4 launch shapes")
     ap.add_argument("--no-ten-days", action="store_true", help="skip the ten-day mixed-vs-FP64 divergence")
+    ap.add_argument("--no-model", action="store_true", help="skip the timing of the full GYRE step")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     args = ap.parse_args()

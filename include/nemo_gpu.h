@@ -138,6 +138,9 @@ typedef struct nemo_namelist {
   double rn_lc;
   int    nn_etau;         /* tke penetration below the mixed layer: 0 only here        */
   int    ln_drg_tke;      /* friction as TKE boundary condition (ln_drg): 0 only here */
+  /* &namdyn_adv: the momentum advection of nemo_gpu_stp_model */
+  int    ln_dynadv_OFF;   /* linear dynamics (no momentum advection; Coriolis only)    */
+  int    nn_dynkeg;       /* grad(KE) scheme: 0 C2 (1, Hollingsworth: not supported)   */
 } nemo_namelist;
 
 /* ------------------------------------------------------- module-global fields
@@ -453,17 +456,24 @@ int nemo_gpu_dyn_zdf_step(nemo_ctx *ctx, int kt);
 int nemo_gpu_dyn_nxt(nemo_ctx *ctx, int kt);
 /* ssh_swp (sshwzv.F90:216-267), linear free surface. */
 int nemo_gpu_ssh_swp(nemo_ctx *ctx, int kt);
-/* One model step on the bound fields, in step.F90's order: (with rn2b, rhd, the
- * depths, the mixed-layer fields and the slopes bound, ln_seos and ln_traldf_iso:
- * rab_3d of tsb, bn2, zdf_mxl, eos_insitu of tsb and ldf_slp), ua = va = 0, dyn_spg_ts,
- * (with the bound rhd and rhop and ln_seos: eos_insitu_pot of tsn at gdept_n and
- * dyn_hpg after ua = va = 0), div_hor + wzv, the dyn_zdf time step, tsa = 0,
- * tra_sbc and tra_qsr (when their
- * fields are bound; tra_qsr with ln_traqsr), tra_adv, tra_ldf, tra_zdf (with
- * the salinity clamp), tra_nxt, dyn_nxt, ssh_swp -- the hot path closed by the
- * routines above, with the momentum trends of dyn_adv, dyn_vor, dyn_ldf, dyn_hpg and
- * the vertical viscosity held at 0 (they are not on the path). Captured into a CUDA
- * graph like nemo_gpu_stp_hotpath. Linear free surface with ln_bt_fw. */
+/* One model step on the bound fields, in step.F90's order (:96-305):
+ *  - the vertical physics (:127-133), with ln_zdftke, an equation of state and the
+ *    fields of nemo_gpu_zdf_phy and gdept_n bound: rab_3d and bn2 of tsb and tsn into
+ *    rn2b and rn2, then zdf_phy;
+ *  - the iso-neutral slopes (:137-150), with rn2b, rhd, the depths, the mixed-layer
+ *    fields and the slopes bound and ln_traldf_iso: (rab_3d and bn2 of tsb unless done
+ *    above,) zdf_mxl, eos_insitu of tsb and ldf_slp;
+ *  - ua = va = 0; dyn_adv in the vector form (dyn_keg C2 + dyn_zad; none with
+ *    ln_dynadv_OFF), dyn_vor (vor_ene of the total vorticity; the Coriolis term alone
+ *    with ln_dynadv_OFF; the ENE scheme only), dyn_ldf (the iso-level laplacian of ub,
+ *    vb, while ahmt and ahmf are bound) (:188-192);
+ *  - with rhd and rhop bound: eos_insitu_pot of tsn at gdept_n and dyn_hpg (:165, :193);
+ *  - dyn_spg_ts, div_hor + wzv, dyn_zdf (the implicit vertical viscosity while avm is
+ *    bound), tsa = 0, tra_sbc and tra_qsr (when their fields are bound; tra_qsr with
+ *    ln_traqsr), tra_adv, tra_ldf, tra_zdf (with the salinity clamp), tra_nxt,
+ *    dyn_nxt, ssh_swp, dia_hsb (after nemo_gpu_dia_hsb_init), stp_ctl (:305).
+ * Captured into a CUDA graph like nemo_gpu_stp_hotpath. Linear free surface with
+ * ln_bt_fw. */
 int nemo_gpu_stp_model(nemo_ctx *ctx, int kt);
 
 /* ------------------------------------------------------------ adjoint

@@ -1281,6 +1281,40 @@ int run_zdf_phy(nemo_ctx* c) {
   return NEMO_OK;
 }
 
+// the momentum trends of the model step (step.F90:190-192): dyn_adv in the vector
+// form (keg C2 + zad), dyn_vor with vor_ene of the total vorticity (the Coriolis
+// term alone for linear dynamics, dynvor.F90:904-913), dyn_ldf where the viscosity
+// ahmt, ahmf is bound
+int mom_check(nemo_ctx* c) {
+  const nemo_namelist& nm = c->nam;
+  if (!nm.ln_dynadv_OFF && (!nm.ln_dynadv_vec || nm.nn_dynkeg != 0))
+    return fail(c, NEMO_ERR_UNSUPPORTED, "stp_model: momentum advection in the vector form with nn_dynkeg = 0 only");
+  if (nm.nvor_scheme != NEMO_VOR_ENE)
+    return fail(c, NEMO_ERR_UNSUPPORTED, "stp_model: the energy-conserving vorticity scheme (ENE) only");
+  if (nm.ln_sco) return fail(c, NEMO_ERR_UNSUPPORTED, "stp_model: z-coordinate only");
+  if (c->f[NEMO_F_AHMT] && c->f[NEMO_F_AHMF] && !nm.ln_linssh)
+    return fail(c, NEMO_ERR_UNSUPPORTED, "stp_model: the lateral viscosity of a linear free surface only");
+  return NEMO_OK;
+}
+template <class T>
+int run_mom_trends(nemo_ctx* c) {
+  const nemo_namelist& nm = c->nam;
+  void* const* F = c->f;
+  const Dom<T> d = dom_now<T>(c);
+  const T *un = (const T*)F[NEMO_F_UN], *vn = (const T*)F[NEMO_F_VN];
+  T *ua = (T*)F[NEMO_F_UA], *va = (T*)F[NEMO_F_VA];
+  if (!nm.ln_dynadv_OFF) {
+    CK(launch_dyn_keg<T>(d, un, vn, ua, va, c->stream), "dyn_keg launch");
+    CK(launch_dyn_zad<T>(d, un, vn, (const T*)F[NEMO_F_WN], ua, va, c->stream), "dyn_zad launch");
+  }
+  CK(launch_vor_ene<T>(d, nm.ln_dynadv_OFF ? 1 : 4, un, vn, ua, va, c->stream), "vor_ene launch");
+  if (F[NEMO_F_AHMT] && F[NEMO_F_AHMF])
+    CK(launch_dyn_ldf_lap<T>(d, (const T*)F[NEMO_F_AHMT], (const T*)F[NEMO_F_AHMF], (const T*)F[NEMO_F_UB],
+                             (const T*)F[NEMO_F_VB], ua, va, T(1), c->stream),
+       "dyn_ldf_lap launch");
+  return NEMO_OK;
+}
+
 // the model step's vertical physics (step.F90:127-133): an equation of state, the
 // TKE closure as zdf_phy covers it, z-levels with full steps, every field bound
 bool zphy_on(const nemo_ctx* c) {
@@ -1376,6 +1410,7 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
   mark(0);
   if (model) {  // ua = va = 0 (step.F90:183-184)
     if (int s = dyn_zdf_check(c)) return s;
+    if (int s = mom_check(c)) return s;
     const bool vphys = zphy_on(c);
     if (vphys) {
       int s = run_vphys<T>(c);
@@ -1388,6 +1423,7 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
     const size_t bytes = (size_t)c->n3 * c->nmem * sizeof(T);
     CK(cudaMemsetAsync(F[NEMO_F_UA], 0, bytes, c->stream), "ua = 0");
     CK(cudaMemsetAsync(F[NEMO_F_VA], 0, bytes, c->stream), "va = 0");
+    if (int s = run_mom_trends<T>(c)) return s;
     if (hpg_on(c)) {  // eos of tsn at gdept_n (step.F90:165) and dyn_hpg (:193)
       int s = run_eos<T>(c, 1, F[NEMO_F_TSN], F[NEMO_F_RHD], F[NEMO_F_RHOP], F[NEMO_F_GDEPT_N], nullptr, nullptr,
                          nullptr);

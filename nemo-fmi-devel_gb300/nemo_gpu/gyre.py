@@ -379,3 +379,43 @@ def vphys_inputs(dom, nam, st):
     z3 = lambda: f(np.zeros((jpi, jpj, jpk)))
     return dict(taum=f(taum), en=f(nam["rn_emin"] * wm), dissl=f(np.full((jpi, jpj, jpk), 1.e-12)),
                 avm_k=f(nam["rn_avm0"] * wm), avt_k=f(nam["rn_avt0"] * wm), avm=z3(), avs=z3(), rn2=z3())
+
+
+def viscosity(dom, ahm0=1.0e5):
+    """The lateral eddy viscosity of GYRE's &namdyn_ldf (laplacian, iso-level,
+    nn_ahm_ijk_t = 0: 1/2 rn_Uv rn_Lv = 1/2 x 2 m/s x 100 km = 1e5 m2/s, ldfdyn.F90:
+    248-259): ahmt = ahm0 tmask, ahmf = ahm0 fmask, fmask of the free-slip coast
+    (rn_shlat = 0) from the four surrounding T-points; level jpk is 0."""
+    tm = masks(dom)[0]
+    fm = np.zeros_like(tm)
+    fm[:-1, :-1] = tm[:-1, :-1] * tm[1:, :-1] * tm[:-1, 1:] * tm[1:, 1:]
+    ahmt, ahmf = ahm0 * tm, ahm0 * fm
+    ahmt[:, :, -1] = 0.0
+    ahmf[:, :, -1] = 0.0
+    return np.asfortranarray(ahmt), np.asfortranarray(ahmf)
+
+
+# GYRE's physics (cfgs/GYRE_PISCES/EXPREF/namelist_cfg): EOS-80, the TKE closure with
+# enhanced vertical diffusion, the penetrating solar flux
+FULL_NAMELIST = dict(ln_eos80=1, ln_seos=0, ln_zdftke=1, ln_zdfevd=1, ln_traqsr=1)
+# the fields of the full step besides the hot path's (3-D, then 2-D; nmln is int32)
+FULL_3D = ("en", "dissl", "avm_k", "avt_k", "avm", "avs", "rn2", "rn2b", "rhd", "rhop", "gdept_n", "gdepw_n",
+           "qsr_hc", "qsr_hc_b", "ahmt", "ahmf")
+FULL_2D = ("taum", "qsr", "qns", "sfx", "fraqsr_1lev", "hmlp", "hmlpt", "sbc_tsc", "sbc_tsc_b")
+
+
+def full_physics(dom, nam, st):
+    """The namelist and the state of the full GYRE step from a state of state(): the
+    analytic surface forcing of the first time step (sbc_inputs), the cold start of
+    the TKE closure (vphys_inputs), the rest-state depths, the lateral viscosity, and
+    zeroed rn2b, rhd, rhop, mixed-layer fields (the step forms them)."""
+    nam = dict(nam, **FULL_NAMELIST)
+    ahmt, ahmf = viscosity(dom)
+    st = dict(st)
+    st.update(sbc_inputs(dom, nam, st, kt=1))
+    st.update(vphys_inputs(dom, nam, st))
+    sl = slope_inputs(dom, nam, st)
+    z3, z2 = np.zeros_like(st["avt"]), np.zeros_like(st["sshn"])
+    st.update(gdept_n=sl["gdept_n"], rn2b=z3, rhd=z3.copy(), rhop=z3.copy(), ahmt=ahmt, ahmf=ahmf, hmlp=z2,
+              hmlpt=z2.copy(), nmln=np.zeros(z2.shape, dtype=np.int32, order="F"))
+    return nam, st

@@ -3490,9 +3490,10 @@ static int vphys_on(const ora_ctx *c) {
 
 /* One model step (step.F90:96-305) with the path and the routines above: the
  * vertical physics (rab_3d and bn2 of the before and now tracers, zdf_phy), the
- * iso-neutral slopes, ua = va = 0, eos + dyn_hpg, dyn_spg_ts, div_hor + wzv, the
- * dyn_zdf time step, tsa = 0, tra_adv, tra_ldf, tra_zdf, tra_nxt, dyn_nxt, ssh_swp,
- * dia_hsb, stp_ctl; each where its fields are bound. */
+ * iso-neutral slopes, ua = va = 0, dyn_adv (keg + zad), dyn_vor (vor_ene), dyn_ldf,
+ * eos + dyn_hpg, dyn_spg_ts, div_hor + wzv, dyn_zdf, tsa = 0, tra_sbc, tra_qsr,
+ * tra_adv, tra_ldf, tra_zdf, tra_nxt, dyn_nxt, ssh_swp, dia_hsb, stp_ctl; the
+ * optional ones where their fields are bound. */
 int ora_stp_model(ora_ctx *c, int kt) {
   const size_t n3 = (size_t)c->jpi * c->jpj * c->jpk;
   if (!c->f[NEMO_F_UA] || !c->f[NEMO_F_VA]) return NEMO_ERR_UNBOUND;
@@ -3526,6 +3527,20 @@ int ora_stp_model(ora_ctx *c, int kt) {
   }
   memset(c->f[NEMO_F_UA], 0, n3 * sizeof(double));
   memset(c->f[NEMO_F_VA], 0, n3 * sizeof(double));
+  /* dyn_adv, dyn_vor (step.F90:190-191): the vector form, keg (C2) + zad, and vor_ene
+   * of the total vorticity (dynvor.F90:904-913: Coriolis alone for linear dynamics) */
+  if (!nm->ln_dynadv_OFF) {
+    if (!nm->ln_dynadv_vec || nm->nn_dynkeg != 0) return NEMO_ERR_UNSUPPORTED;
+    st = ora_dyn_keg(c, kt, 0);
+    if (!st) st = ora_dyn_zad(c, kt);
+  }
+  if (nm->nvor_scheme != NEMO_VOR_ENE) return NEMO_ERR_UNSUPPORTED;
+  if (!st) st = ora_vor_ene(c, kt, nm->ln_dynadv_OFF ? 1 : 4, c->f[NEMO_F_UN], c->f[NEMO_F_VN], c->f[NEMO_F_UA],
+                            c->f[NEMO_F_VA]);
+  /* dyn_ldf (:192): the iso-level laplacian where the viscosity AHMT, AHMF is bound */
+  if (!st && c->f[NEMO_F_AHMT] && c->f[NEMO_F_AHMF])
+    st = ora_dyn_ldf_lap(c, kt, c->f[NEMO_F_UB], c->f[NEMO_F_VB], c->f[NEMO_F_UA], c->f[NEMO_F_VA], 1);
+  if (st) return st;
   if (c->f[NEMO_F_RHD] && c->f[NEMO_F_RHOP] && (c->nam.ln_seos || c->nam.ln_eos80)) {  /* step.F90:165, :193 */
     if (!c->f[NEMO_F_GDEPT_N]) return NEMO_ERR_UNBOUND;
     st = ora_eos_insitu_pot(c, c->f[NEMO_F_TSN], c->f[NEMO_F_RHD], c->f[NEMO_F_RHOP], c->f[NEMO_F_GDEPT_N]);

@@ -8,15 +8,7 @@ from harness import Pair
 
 
 def viscosity(dom, ahm0=1.0e5):
-    """ahmt = ahm0 tmask, ahmf = ahm0 fmask (free slip: fmask from the four
-    surrounding T-points, ldfdyn.F90:258-259 with :328-329)."""
-    tm = gyre.masks(dom)[0]
-    fm = np.zeros_like(tm)
-    fm[:-1, :-1] = tm[:-1, :-1] * tm[1:, :-1] * tm[:-1, 1:] * tm[1:, 1:]
-    ahmt, ahmf = ahm0 * tm, ahm0 * fm
-    ahmt[:, :, -1] = 0.0
-    ahmf[:, :, -1] = 0.0
-    return np.asfortranarray(ahmt), np.asfortranarray(ahmf)
+    return gyre.viscosity(dom, ahm0)
 
 
 def oracle_case(nn=2):

@@ -163,10 +163,13 @@ def test_gpu_zdf_phy(prec, nn_mxl, ln_lc, nn_pdl):
 
 
 def run_model_with_tke(prec, eos, **over):
+    """four steps of the full GYRE step: the vertical physics, the momentum trends with
+    the lateral viscosity, eos + hpg, the implicit vertical viscosity"""
     p = tke_pair(prec, eos=eos, neuler=0, **over)
+    ahmt, ahmf = gyre.viscosity(p.dom)
     for st in p.states:
-        st.update(rhd=np.zeros(p.s3), rhop=np.zeros(p.s3))
-    for n in ("GDEPT_N", "RHD", "RHOP"):
+        st.update(rhd=np.zeros(p.s3), rhop=np.zeros(p.s3), ahmt=ahmt, ahmf=ahmf)
+    for n in ("GDEPT_N", "RHD", "RHOP", "AHMT", "AHMF"):
         p.bind(n)
     for kt in (1, 2, 3, 4):
         for o in p.ora:
