@@ -141,6 +141,8 @@ typedef struct nemo_namelist {
   /* &namdyn_adv: the momentum advection of nemo_gpu_stp_model */
   int    ln_dynadv_OFF;   /* linear dynamics (no momentum advection; Coriolis only)    */
   int    nn_dynkeg;       /* grad(KE) scheme: 0 C2 (1, Hollingsworth: not supported)   */
+  /* &namsbc: the user-defined (GYRE analytic) surface forcing, formed each model step */
+  int    ln_usr;
 } nemo_namelist;
 
 /* ------------------------------------------------------- module-global fields
@@ -227,6 +229,9 @@ enum nemo_field_id {
   NEMO_F_AVM, NEMO_F_AVM_K, NEMO_F_AVT_K, NEMO_F_EN, NEMO_F_DISSL, /* [T]            */
   NEMO_F_RN2,                          /* [T]                                         */
   NEMO_F_TAUM, NEMO_F_FR_I,            /* [S]                                         */
+  /* latitudes of the T-, U- and V-points (dom_oce gphit, gphiu, gphiv) [degrees], read
+   * by GYRE's analytic surface forcing (nemo_gpu_usrdef_sbc) */
+  NEMO_F_GPHIT, NEMO_F_GPHIU, NEMO_F_GPHIV, /* [S]                                    */
   NEMO_F_COUNT
 };
 
@@ -389,6 +394,15 @@ int nemo_gpu_zdf_mxl(nemo_ctx *ctx, int kt);
  * fields and GDEPT_N are bound. */
 int nemo_gpu_zdf_phy(nemo_ctx *ctx, int kt);
 
+/* usrdef_sbc_oce (usrdef_sbc.F90:62-190), GYRE's analytic surface forcing at time step
+ * kt (year 1 of a 360-day calendar), preceded by sbc's swap of the before fields
+ * UTAU_B, VTAU_B, EMP_B when bound and kt /= nit000 (sbcmod.F90:389-394): qsr, the
+ * restoring qns from the before SST, E-P less its domain mean (GLOB_SUM) with its heat
+ * content at the now SST in qns, sfx = 0, the wind stress utau, vtau and its modulus
+ * taum. Bound: GPHIT GPHIU GPHIV TSB TSN QSR QNS EMP SFX UTAU VTAU TAUM. With ln_usr,
+ * nemo_gpu_stp_model runs it first (step.F90:116). */
+int nemo_gpu_usrdef_sbc(nemo_ctx *ctx, int kt);
+
 /* zps_hde (zpshde.F90:41-148): pgtu, pgtv (jpi,jpj,kjpt) = the horizontal
  * gradients of pta (jpi,jpj,jpk,kjpt) at the partial-step bottom level of the u-
  * and v-points, with lbc_lnk. The optional density part (prd, pgru, pgrv) needs
@@ -463,6 +477,7 @@ int nemo_gpu_ssh_swp(nemo_ctx *ctx, int kt);
  *  - the iso-neutral slopes (:137-150), with rn2b, rhd, the depths, the mixed-layer
  *    fields and the slopes bound and ln_traldf_iso: (rab_3d and bn2 of tsb unless done
  *    above,) zdf_mxl, eos_insitu of tsb and ldf_slp;
+ *  - div_hor + wzv of the now velocities (:156-160; ssha comes from dyn_spg_ts);
  *  - ua = va = 0; dyn_adv in the vector form (dyn_keg C2 + dyn_zad; none with
  *    ln_dynadv_OFF), dyn_vor (vor_ene of the total vorticity; the Coriolis term alone
  *    with ln_dynadv_OFF; the ENE scheme only), dyn_ldf (the iso-level laplacian of ub,
@@ -472,8 +487,10 @@ int nemo_gpu_ssh_swp(nemo_ctx *ctx, int kt);
  *    bound), tsa = 0, tra_sbc and tra_qsr (when their fields are bound; tra_qsr with
  *    ln_traqsr), tra_adv, tra_ldf, tra_zdf (with the salinity clamp), tra_nxt,
  *    dyn_nxt, ssh_swp, dia_hsb (after nemo_gpu_dia_hsb_init), stp_ctl (:305).
- * Captured into a CUDA graph like nemo_gpu_stp_hotpath. Linear free surface with
- * ln_bt_fw. */
+ * With ln_usr the step opens with GYRE's analytic forcing (nemo_gpu_usrdef_sbc; its
+ * time-dependent scalars are written to the device ahead of each step, so the
+ * captured graph replays with the step's own). Captured into a CUDA graph like
+ * nemo_gpu_stp_hotpath. Linear free surface with ln_bt_fw. */
 int nemo_gpu_stp_model(nemo_ctx *ctx, int kt);
 
 /* ------------------------------------------------------------ adjoint
@@ -636,6 +653,7 @@ enum nemo_kernel_id {
   NEMO_K_DYN_KEG, NEMO_K_DYN_ZAD, /* momentum advection, vector form */
   NEMO_K_STP_CTL, NEMO_K_DIA_HSB, /* run control extrema, conservation budgets */
   NEMO_K_ZDF_PHY,      /* shear production, TKE closure, enhanced vertical diffusion */
+  NEMO_K_USR_SBC,      /* GYRE's analytic surface forcing */
   NEMO_K_COUNT
 };
 

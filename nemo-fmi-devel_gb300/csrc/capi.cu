@@ -18,6 +18,7 @@
 #include "adj.h"
 #include "step.h"
 #include "eos80.h"
+#include "nemo_sin.h"
 #include "launch.h"
 
 using namespace nemo;
@@ -83,6 +84,8 @@ struct nemo_ctx {
   void* rab_n = nullptr;       // and the now ones rab_n, with the vertical physics
   void* zphy_w = nullptr;      // zdf_phy work: sh2, apdlr and the TKE system, 5 x n3 per member
   void* zdyn_w = nullptr;      // dyn_zdf work: the implicit viscosity system, 2 x n3 per member
+  double* usr_s = nullptr;     // usrdef_sbc: the step's scalars (7), written before each step
+  double usr_zsurf = 0.0;      // usrdef_sbc: GLOB_SUM(tmask(:,:,1))
   void* blp_w = nullptr;       // tra_ldf_blp: the first laplacian (jpi,jpj,jpk,kjpt) per member
   int blp_kjpt = 0;
   int iso_kjpt = 0;
@@ -102,6 +105,7 @@ struct nemo_ctx {
   // stp_ctl (block partials, per-member results, the blow-up flag) and dia_hsb
   double* ctl_part = nullptr;
   double* ctl_out = nullptr;
+  unsigned long long* ctl_idx = nullptr;  // first indices of the extremes (4 per member)
   int* ctl_flag = nullptr;
   int ctl_nblk = 0;
   int someoce = 0;  // the domain has ocean points (stpctl.F90:111)
@@ -988,8 +992,69 @@ int run_ldf_slp(nemo_ctx* c, const void* prd, const void* pn2) {
 }
 
 // ------------------------------------------------- the rest of a model step
+// usrdef_sbc (usrdef_sbc.F90:62-190): GYRE's analytic surface forcing
+int usr_check(nemo_ctx* c) {
+  for (int id : {NEMO_F_GPHIT, NEMO_F_GPHIU, NEMO_F_GPHIV, NEMO_F_TSB, NEMO_F_TSN, NEMO_F_QSR, NEMO_F_QNS,
+                 NEMO_F_EMP, NEMO_F_SFX, NEMO_F_UTAU, NEMO_F_VTAU, NEMO_F_TAUM})
+    if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "usrdef_sbc: field %d must be bound", id);
+  return NEMO_OK;
+}
+// the scalars of step kt (year 1 of a 360-day calendar): the amplitude and the
+// denominator of T*, 23.5 zcos_sais1, the seasonal factors of E-P south and north,
+// ztaun, and whether sbc swaps the before fields (kt /= nit000)
+void usr_scalars(const nemo_namelist& nm, int kt, double v[7]) {
+  const double rpi = 3.141592653589793, zyydd = 360.0, rjjhh = 24.0;
+  const double ztime = (double)kt * nm.rn_rdt / (60.0 * 60.0);
+  const double ztimemax1 = ((5. * 30.) + 21.) * 24., ztimemin1 = ztimemax1 + rjjhh * zyydd / 2;
+  const double ztimemax2 = ((6. * 30.) + 21.) * 24., ztimemin2 = ztimemax2 - rjjhh * zyydd / 2;
+  const double zemp_S = 0.7, zemp_N = 0.8, zemp_sais = 0.1, zTstar = 28.3;
+  const double zcos_sais1 = nemo_cos((ztime - ztimemax1) / (ztimemin1 - ztimemax1) * rpi);
+  const double zcos_sais2 = nemo_cos((ztime - ztimemax2) / (ztimemax2 - ztimemin2) * rpi);
+  v[0] = zTstar * (1. + 1. / 50. * zcos_sais2);
+  v[1] = 53.5 * (1 + 11 / 53.5 * zcos_sais2) * 2.;
+  v[2] = 23.5 * zcos_sais1;
+  v[3] = 1 - zemp_sais / zemp_S * zcos_sais1;
+  v[4] = 1 - zemp_sais / zemp_N * zcos_sais1;
+  const double ztimemax = ((5. * 30.) + 21.) * 24., ztimemin = ztimemax + rjjhh * zyydd / 2;
+  const double ztau = 0.105 / std::sqrt(2.), ztau_sais = 0.015;
+  v[5] = ztau - ztau_sais * nemo_cos((ztime - ztimemax) / (ztimemin - ztimemax) * rpi);
+  v[6] = kt != nm.nit000 ? 1.0 : 0.0;
+}
+// the step's scalars into device memory, ahead of the step (and of its graph)
+int usr_put(nemo_ctx* c, int kt) {
+  if (!c->usr_s && cudaMalloc(&c->usr_s, 8 * sizeof(double)) != cudaSuccess)
+    return fail(c, NEMO_ERR_NOMEM, "usrdef_sbc scalars");
+  double v[7];
+  usr_scalars(c->nam, kt, v);
+  cudaError_t e = launch_usr_put(c->usr_s, v, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "usrdef_sbc scalars launch");
+  return NEMO_OK;
+}
+template <class T>
+int run_usrdef_sbc(nemo_ctx* c) {
+  void* const* F = c->f;
+  UsrSbcArgs<T> a{};
+  a.gphit = (const T*)F[NEMO_F_GPHIT]; a.gphiu = (const T*)F[NEMO_F_GPHIU]; a.gphiv = (const T*)F[NEMO_F_GPHIV];
+  a.tsb = (const T*)F[NEMO_F_TSB]; a.tsn = (const T*)F[NEMO_F_TSN];
+  a.qsr = (T*)F[NEMO_F_QSR]; a.qns = (T*)F[NEMO_F_QNS]; a.emp = (T*)F[NEMO_F_EMP]; a.sfx = (T*)F[NEMO_F_SFX];
+  a.utau = (T*)F[NEMO_F_UTAU]; a.vtau = (T*)F[NEMO_F_VTAU]; a.taum = (T*)F[NEMO_F_TAUM];
+  a.utau_b = (T*)F[NEMO_F_UTAU_B]; a.vtau_b = (T*)F[NEMO_F_VTAU_B]; a.emp_b = (T*)F[NEMO_F_EMP_B];
+  a.s = c->usr_s; a.gsum = c->gs_out;
+  a.zsurf = c->usr_zsurf;
+  a.rcp = c->nam.rcp > 0 ? c->nam.rcp : 3991.86795711963;
+  const Dom<T> d = dom<T>(c);
+  CK(launch_usr_sbc_a<T>(d, a, c->stream), "usrdef_sbc launch");
+  CK(launch_globsum<T>((const T*)F[NEMO_F_EMP], d.tmask_i.p, c->n2, 1, c->nmem, c->gs_part, c->gs_nblk,
+                       c->gs_out, c->stream),
+     "usrdef_sbc glob_sum");
+  CK(launch_usr_sbc_b<T>(d, a, c->stream), "usrdef_sbc launch");
+  return NEMO_OK;
+}
+
 int model_fields(nemo_ctx* c, const char* what) {
   const nemo_namelist& nm = c->nam;
+  if (nm.ln_usr)
+    if (int s = usr_check(c)) return s;
   for (int id : {NEMO_F_UN, NEMO_F_VN, NEMO_F_WN, NEMO_F_UA, NEMO_F_VA, NEMO_F_UB, NEMO_F_VB, NEMO_F_UN_B,
                  NEMO_F_VN_B, NEMO_F_UB_B, NEMO_F_VB_B, NEMO_F_UA_B, NEMO_F_VA_B, NEMO_F_SSHB, NEMO_F_SSHN,
                  NEMO_F_SSHA, NEMO_F_TSB, NEMO_F_TSN, NEMO_F_TSA})
@@ -1352,7 +1417,7 @@ template <class T>
 int run_stp_ctl(nemo_ctx* c) {
   cudaError_t e = launch_stp_ctl<T>(dom<T>(c), (const T*)c->f[NEMO_F_SSHN], (const T*)c->f[NEMO_F_UN],
                                     (const T*)c->f[NEMO_F_TSN], c->ctl_part, c->ctl_nblk, c->someoce, c->ctl_out,
-                                    c->ctl_flag, c->stream);
+                                    c->ctl_idx, c->ctl_flag, c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "stp_ctl launch");
   return NEMO_OK;
 }
@@ -1410,6 +1475,8 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
   mark(0);
   if (model) {  // ua = va = 0 (step.F90:183-184)
     if (int s = dyn_zdf_check(c)) return s;
+    if (nm.ln_usr)  // sbc (step.F90:116), its scalars put by stp_common
+      if (int s = run_usrdef_sbc<T>(c)) return s;
     if (int s = mom_check(c)) return s;
     const bool vphys = zphy_on(c);
     if (vphys) {
@@ -1420,6 +1487,9 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
       int s = run_slopes<T>(c, vphys);
       if (s) return s;
     }
+    // ssh_nxt's div_hor and wzv (step.F90:156-160): the now vertical velocity of
+    // dyn_adv (ssha comes from dyn_spg_ts with the split-explicit free surface)
+    if (int s = run_wzv<T>(c, kt)) return s;
     const size_t bytes = (size_t)c->n3 * c->nmem * sizeof(T);
     CK(cudaMemsetAsync(F[NEMO_F_UA], 0, bytes, c->stream), "ua = 0");
     CK(cudaMemsetAsync(F[NEMO_F_VA], 0, bytes, c->stream), "va = 0");
@@ -1709,12 +1779,15 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
   if (nam->ln_eos80 && upload_eos80(c)) return bad(NEMO_ERR_NOMEM);
   c->ctl_nblk = 2 * c->nsm;
   if (cudaMalloc(&c->ctl_part, (size_t)c->ctl_nblk * c->nmem * CTL_REC * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&c->ctl_out, (size_t)c->nmem * 32 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&c->ctl_out, (size_t)c->nmem * CTL_OUT * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&c->ctl_idx, (size_t)c->nmem * 4 * sizeof(unsigned long long)) != cudaSuccess ||
       cudaMalloc(&c->ctl_flag, sizeof(int)) != cudaSuccess)
     return bad(NEMO_ERR_NOMEM);
-  cudaMemset(c->ctl_out, 0, (size_t)c->nmem * 32 * sizeof(double));
+  cudaMemset(c->ctl_out, 0, (size_t)c->nmem * CTL_OUT * sizeof(double));
   cudaMemset(c->ctl_flag, 0, sizeof(int));
   for (size_t p = 0; p < (size_t)c->n2; ++p) c->someoce |= c->ssmask[p] == 1.0;
+  for (size_t p = 0; p < (size_t)c->n2; ++p)  // a count: exact in any order
+    c->usr_zsurf += (1 >= c->ci[p].tlo && 1 <= c->ci[p].thi ? 1.0 : 0.0) * c->tmask_i[p];
   if (c->p2_blocks < 1) return bad(NEMO_ERR_CUDA);
   c->gs_nblk = c->nsm * 4;
   if (cudaMalloc(&c->gs_part, 2 * (size_t)c->gs_nblk * c->nmem * 8) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
@@ -1738,7 +1811,7 @@ int nemo_gpu_destroy(nemo_ctx* c) {
   for (auto p : c->iso_w) cudaFree(p);
   for (auto p : c->adj_w) cudaFree(p);
   cudaFree(c->slp_w);
-  cudaFree(c->rab_w); cudaFree(c->rab_n); cudaFree(c->zphy_w); cudaFree(c->zdyn_w);
+  cudaFree(c->rab_w); cudaFree(c->rab_n); cudaFree(c->zphy_w); cudaFree(c->zdyn_w); cudaFree(c->usr_s);
   cudaFree(c->blp_w);
   for (auto p : c->spg_w) cudaFree(p);
   for (auto p : c->spg_cor) cudaFree(p);
@@ -1747,7 +1820,7 @@ int nemo_gpu_destroy(nemo_ctx* c) {
   cudaFree(c->spg_ff);
   cudaFree(c->d_wgt1); cudaFree(c->d_wgt2); cudaFree(c->d_wgtf);
   cudaFree(c->bar_mem); cudaFree(c->err_flag);
-  cudaFree(c->ctl_part); cudaFree(c->ctl_out); cudaFree(c->ctl_flag);
+  cudaFree(c->ctl_part); cudaFree(c->ctl_out); cudaFree(c->ctl_idx); cudaFree(c->ctl_flag);
   cudaFree(c->e80_raw); cudaFree(c->e80_tay);
   cudaFree(c->hsb_mem); cudaFree(c->hsb_part); cudaFree(c->hsb_state); cudaFree(c->hsb_out);
   cudaFree(c->gs_part); cudaFree(c->gs_out);
@@ -1786,10 +1859,10 @@ int nemo_gpu_synchronize(nemo_ctx* c) {
   CK(cudaMemcpy(&blow, c->ctl_flag, sizeof(int), cudaMemcpyDeviceToHost), "read status");
   if (blow) {  // stp_ctl's blow-up test fired (stpctl.F90:149-184)
     cudaMemset(c->ctl_flag, 0, sizeof(int));
-    std::vector<double> o((size_t)c->nmem * 32);
+    std::vector<double> o((size_t)c->nmem * CTL_OUT);
     CK(cudaMemcpy(o.data(), c->ctl_out, o.size() * sizeof(double), cudaMemcpyDeviceToHost), "read stp_ctl");
     for (int m = 0; m < c->nmem; ++m) {
-      const double* z = &o[(size_t)m * 32];
+      const double* z = &o[(size_t)m * CTL_OUT];
       if (z[6] != 0.0)
         return fail(c, NEMO_ERR_BLOWUP,
                     "stp_ctl: |ssh| > 20 m or |U| > 10 m/s or S <= 0 or S >= 100 or NaN (member %d: |ssh| max %g at "
@@ -2031,6 +2104,14 @@ int nemo_gpu_zdf_mxl(nemo_ctx* c, int kt) {
   return c->prec == NEMO_PREC_FP64 ? run_zdf_mxl<double>(c) : run_zdf_mxl<float>(c);
 }
 
+int nemo_gpu_usrdef_sbc(nemo_ctx* c, int kt) {
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (int s = usr_check(c)) return s;
+  if (int s = usr_put(c, kt)) return s;
+  return c->prec == NEMO_PREC_FP64 ? run_usrdef_sbc<double>(c) : run_usrdef_sbc<float>(c);
+}
+
 int nemo_gpu_zdf_phy(nemo_ctx* c, int kt) {
   (void)kt;
   if (!c) return NEMO_ERR_ARG;
@@ -2214,10 +2295,10 @@ int nemo_gpu_stp_ctl(nemo_ctx* c, int kt) {
 int nemo_gpu_stp_ctl_result(nemo_ctx* c, double* zmax, int* loc, int* kindic) {
   if (!c) return NEMO_ERR_ARG;
   CK(cudaStreamSynchronize(c->stream), "stp_ctl result");
-  std::vector<double> o((size_t)c->nmem * 32);
+  std::vector<double> o((size_t)c->nmem * CTL_OUT);
   CK(cudaMemcpy(o.data(), c->ctl_out, o.size() * sizeof(double), cudaMemcpyDeviceToHost), "stp_ctl result");
   for (int m = 0; m < c->nmem; ++m) {
-    const double* z = &o[(size_t)m * 32];
+    const double* z = &o[(size_t)m * CTL_OUT];
     if (zmax)
       for (int t = 0; t < NEMO_CTL_N; ++t) zmax[(size_t)m * NEMO_CTL_N + t] = z[t];
     if (kindic) kindic[m] = (int)z[6];
@@ -2480,6 +2561,8 @@ static int stp_common(nemo_ctx* c, int kt, bool model) {
     return c->prec == NEMO_PREC_FP64 ? run_hotpath<double>(c, kt, true) : run_hotpath<float>(c, kt, true);
   if (join_copies(c)) return NEMO_ERR_CUDA;
   const nemo_namelist& nm = c->nam;
+  if (model && nm.ln_usr)  // the forcing's scalars of this step, outside the graph
+    if (int s = usr_put(c, kt)) return s;
   // class of kt: the Euler/leapfrog start steps differ in scalars and weights
   const int cls = kt == nm.nit000 ? 0 : (kt == nm.nit000 + 1 ? 1 : 2);
   const bool carry = !nm.ln_bt_av;  // ring rotation carries across calls: no replay

@@ -98,6 +98,23 @@ cudaError_t launch_dyn_zdf_imp(const Dom<T>& d, const DynZdfArgs<T>& a, cudaStre
 }
 
 template <class T>
+cudaError_t launch_usr_sbc_a(const Dom<T>& d, const UsrSbcArgs<T>& a, cudaStream_t s) {
+  k_usr_sbc_a<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a);
+  ktick(NEMO_K_USR_SBC, s);
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_usr_sbc_b(const Dom<T>& d, const UsrSbcArgs<T>& a, cudaStream_t s) {
+  k_usr_sbc_b<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a);
+  ktick(NEMO_K_USR_SBC, s);
+  return cudaGetLastError();
+}
+cudaError_t launch_usr_put(double* dst, const double* v, cudaStream_t s) {
+  k_usr_put<<<1, 1, 0, s>>>(dst, v[0], v[1], v[2], v[3], v[4], v[5], v[6]);
+  return cudaGetLastError();
+}
+
+template <class T>
 cudaError_t launch_zdf_phy(const Dom<T>& d, const ZphyArgs<T>& a, cudaStream_t s) {
   k_zdf_sh2<T><<<s_pt(d), dim3(SX, SY), 0, s>>>(d, a);
   ktick(NEMO_K_ZDF_PHY, s);
@@ -137,9 +154,14 @@ cudaError_t launch_dyn_zad(const Dom<T>& d, const T* un, const T* vn, const T* w
 
 template <class T>
 cudaError_t launch_stp_ctl(const Dom<T>& d, const T* sshn, const T* un, const T* ts, double* part, int nblk,
-                           int someoce, double* out, int* flag, cudaStream_t s) {
+                           int someoce, double* out, unsigned long long* idx, int* flag, cudaStream_t s) {
   k_ctl_partial<T><<<dim3(nblk, d.nmem), DG_THREADS, 0, s>>>(d, sshn, un, ts, part);
-  k_ctl_final<T><<<(d.nmem + 31) / 32, 32, 0, s>>>(d, part, nblk, someoce, out, flag);
+  ktick(NEMO_K_STP_CTL, s);
+  k_ctl_final<T><<<(d.nmem + 31) / 32, 32, 0, s>>>(d, part, nblk, someoce, out, idx, flag);
+  ktick(NEMO_K_STP_CTL, s);
+  k_ctl_locate<T><<<dim3(nblk, d.nmem), DG_THREADS, 0, s>>>(d, sshn, un, ts, out, idx);
+  ktick(NEMO_K_STP_CTL, s);
+  k_ctl_pos<T><<<(d.nmem + 31) / 32, 32, 0, s>>>(d, out, idx);
   ktick(NEMO_K_STP_CTL, s);
   return cudaGetLastError();
 }
@@ -158,7 +180,7 @@ cudaError_t launch_dia_hsb(const Dom<T>& d, const HsbArgs<T>& a, double* part, i
 
 #define NEMO_STEP_INST(T)                                                                                      \
   template cudaError_t launch_stp_ctl<T>(const Dom<T>&, const T*, const T*, const T*, double*, int, int,       \
-                                         double*, int*, cudaStream_t);                                         \
+                                         double*, unsigned long long*, int*, cudaStream_t);                    \
   template cudaError_t launch_hsb_init<T>(const Dom<T>&, const HsbArgs<T>&, int, cudaStream_t);                \
   template cudaError_t launch_dia_hsb<T>(const Dom<T>&, const HsbArgs<T>&, double*, int, cudaStream_t);         \
   template cudaError_t launch_wzv<T>(const Dom<T>&, const T*, const T*, T*, T, cudaStream_t);                  \
@@ -173,6 +195,8 @@ cudaError_t launch_dia_hsb(const Dom<T>& d, const HsbArgs<T>& a, double* part, i
   template cudaError_t launch_dyn_hpg<T>(const Dom<T>&, const T*, T*, T*, T, cudaStream_t);              \
   template cudaError_t launch_zdf_mxl<T>(const Dom<T>&, const MxlArgs<T>&, cudaStream_t);                  \
   template cudaError_t launch_dyn_zdf_imp<T>(const Dom<T>&, const DynZdfArgs<T>&, cudaStream_t);           \
+  template cudaError_t launch_usr_sbc_a<T>(const Dom<T>&, const UsrSbcArgs<T>&, cudaStream_t);              \
+  template cudaError_t launch_usr_sbc_b<T>(const Dom<T>&, const UsrSbcArgs<T>&, cudaStream_t);              \
   template cudaError_t launch_zdf_phy<T>(const Dom<T>&, const ZphyArgs<T>&, cudaStream_t);                 \
   template cudaError_t launch_dyn_ldf_lap<T>(const Dom<T>&, const T*, const T*, const T*, const T*, T*, T*, T,   \
                                              cudaStream_t);                                             \

@@ -15,38 +15,26 @@ namespace nemo {
 constexpr int DG_THREADS = 256;
 
 // ------------------------------------------------------------------ stp_ctl
-// A partial record: the six maxima (|ssh|, |U|, -S, S, -T, T; NaN-free values), the
-// NaN flags of ssh, U and S, and for the positions of a blow-up the (key, index)
-// pairs of MAXLOC(|ssh|), MAXLOC(|U|), MINLOC(S), MAXLOC(S) with a NaN as the extreme
-// and ties to the first index in Fortran order.
-constexpr int CTL_REC = 18;
+// Pass 1 (k_ctl_partial) reduces the six maxima (|ssh|, |U|, -S, S, -T, T; NaN-free
+// values, in the field's precision: a maximum is exact) and the NaN flags of ssh, U
+// and S into one record per block, marching down each water column (S and T over
+// its wet levels only). Pass 2 (k_ctl_final, one thread per member) merges the
+// records and applies the blow-up test. Only when the test fires does pass 3
+// (k_ctl_locate) find the positions the reference prints, MAXLOC(|ssh|),
+// MAXLOC(|U|), MINLOC(S), MAXLOC(S), as the first index in Fortran order holding the
+// extreme value (a NaN counts as the extreme), and pass 4 (k_ctl_pos) turns them
+// into (i, j, k); both return at once otherwise.
+constexpr int CTL_REC = 9;
+// out[m * 32 + ...]: zmax(1:6) at 0..5, kindic at 6, positions at 7..17, the locate
+// request at 18 and the four keys of the extreme values at 19..22
+constexpr int CTL_OUT = 32;
 
-struct CtlAcc {
-  double v[6];
-  int nan[3];
-  double k[4];
-  long long i[4];
-};
-
-__device__ __forceinline__ void ctl_init(CtlAcc& a) {
-  for (int t = 0; t < 6; ++t) a.v[t] = -1.7976931348623157e308;
-  for (int t = 0; t < 3; ++t) a.nan[t] = 0;
-  a.k[0] = a.k[1] = a.k[3] = -INFINITY;
-  a.k[2] = INFINITY;
-  for (int t = 0; t < 4; ++t) a.i[t] = 0x7fffffffffffffffLL;
-}
-// larger key (smaller for the S minimum, t = 2), ties to the smaller index
-__device__ __forceinline__ void loc_merge(CtlAcc& a, int t, double k, long long i) {
-  const bool better = t == 2 ? (k < a.k[t] || (k == a.k[t] && i < a.i[t])) : (k > a.k[t] || (k == a.k[t] && i < a.i[t]));
-  if (better) { a.k[t] = k; a.i[t] = i; }
-}
-__device__ __forceinline__ void ctl_merge(CtlAcc& a, const CtlAcc& b) {
-  for (int t = 0; t < 6; ++t) a.v[t] = fmax(a.v[t], b.v[t]);
-  for (int t = 0; t < 3; ++t) a.nan[t] |= b.nan[t];
-  for (int t = 0; t < 4; ++t) loc_merge(a, t, b.k[t], b.i[t]);
+template <class T>
+__device__ __forceinline__ double ctl_rec_value(T v) {
+  return v == -INFINITY ? -1.7976931348623157e308 : (double)v;
 }
 
-// grid (nblk, nmem): block partials of member blockIdx.y into part[(m * nblk + b) * CTL_REC]
+// grid (nblk, nmem): block records of member blockIdx.y into part[(m * nblk + b) * CTL_REC]
 template <class T>
 __global__ void __launch_bounds__(DG_THREADS) k_ctl_partial(Dom<T> d, const T* __restrict__ sshn,
                                                             const T* __restrict__ un, const T* __restrict__ ts,
@@ -54,109 +42,148 @@ __global__ void __launch_bounds__(DG_THREADS) k_ctl_partial(Dom<T> d, const T* _
   const int m = blockIdx.y, nblk = gridDim.x;
   const long n2 = d.n2, n3 = d.n3;
   const long stride = (long)nblk * DG_THREADS;
-  CtlAcc a;
-  ctl_init(a);
+  T v[6];
+  for (int t = 0; t < 6; ++t) v[t] = T(-INFINITY);
+  int nan = 0;
   const T* s2 = sshn + m * n2;
-  for (long p = blockIdx.x * (long)DG_THREADS + threadIdx.x; p < n2; p += stride) {
-    const double v = fabs((double)s2[p]);
-    if (isnan(v)) { a.nan[0] = 1; loc_merge(a, 0, INFINITY, p); }
-    else { a.v[0] = fmax(a.v[0], v); loc_merge(a, 0, v, p); }
-  }
   const T* u3 = un + m * n3;
   const T* t3 = ts + m * 2 * n3;
-  for (long q = blockIdx.x * (long)DG_THREADS + threadIdx.x; q < n3; q += stride) {
-    const double v = fabs((double)u3[q]);
-    if (isnan(v)) { a.nan[1] = 1; loc_merge(a, 1, INFINITY, q); }
-    else { a.v[1] = fmax(a.v[1], v); loc_merge(a, 1, v, q); }
-    const long p = q % n2;
-    const int k = (int)(q / n2) + 1;
+  for (long p = blockIdx.x * (long)DG_THREADS + threadIdx.x; p < n2; p += stride) {
+    const T s = fabs(s2[p]);
+    v[0] = fmax(v[0], s);
+    nan |= s != s ? 1 : 0;
+    for (int k = 1; k <= d.jpk; ++k) {
+      const T x = fabs(u3[p + (long)(k - 1) * n2]);
+      v[1] = fmax(v[1], x);
+      nan |= x != x ? 2 : 0;
+    }
     const ColInfo c = d.ci[p];
-    if (k >= c.tlo && k <= c.thi) {
-      const double sv = (double)t3[q + n3], tv = (double)t3[q];
-      if (isnan(sv)) {
-        a.nan[2] = 1;
-        loc_merge(a, 2, -INFINITY, q);
-        loc_merge(a, 3, INFINITY, q);
-      } else {
-        a.v[2] = fmax(a.v[2], -sv);
-        a.v[3] = fmax(a.v[3], sv);
-        loc_merge(a, 2, sv, q);
-        loc_merge(a, 3, sv, q);
-      }
-      if (!isnan(tv)) {
-        a.v[4] = fmax(a.v[4], -tv);
-        a.v[5] = fmax(a.v[5], tv);
-      }
+    for (int k = c.tlo; k <= c.thi; ++k) {
+      const long q = p + (long)(k - 1) * n2;
+      const T tv = t3[q], sv = t3[q + n3];
+      v[2] = fmax(v[2], -sv);
+      v[3] = fmax(v[3], sv);
+      nan |= sv != sv ? 4 : 0;
+      v[4] = fmax(v[4], -tv);
+      v[5] = fmax(v[5], tv);
     }
   }
-  // block reduction through shared memory, one record per warp then one per block
-  __shared__ CtlAcc s_acc[DG_THREADS / 32];
   for (int off = 16; off > 0; off >>= 1) {
-    CtlAcc o;
-    for (int t = 0; t < 6; ++t) o.v[t] = __shfl_down_sync(0xffffffffu, a.v[t], off);
-    for (int t = 0; t < 3; ++t) o.nan[t] = __shfl_down_sync(0xffffffffu, a.nan[t], off);
-    for (int t = 0; t < 4; ++t) {
-      o.k[t] = __shfl_down_sync(0xffffffffu, a.k[t], off);
-      o.i[t] = __shfl_down_sync(0xffffffffu, a.i[t], off);
-    }
-    ctl_merge(a, o);
+    for (int t = 0; t < 6; ++t) v[t] = fmax(v[t], __shfl_down_sync(0xffffffffu, v[t], off));
+    nan |= __shfl_down_sync(0xffffffffu, nan, off);
   }
-  if ((threadIdx.x & 31) == 0) s_acc[threadIdx.x >> 5] = a;
+  __shared__ T s_v[DG_THREADS / 32][6];
+  __shared__ int s_nan[DG_THREADS / 32];
+  if ((threadIdx.x & 31) == 0) {
+    for (int t = 0; t < 6; ++t) s_v[threadIdx.x >> 5][t] = v[t];
+    s_nan[threadIdx.x >> 5] = nan;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int w = 1; w < DG_THREADS / 32; ++w) ctl_merge(a, s_acc[w]);
-    double* r = part + ((long)m * nblk + blockIdx.x) * CTL_REC;
-    for (int t = 0; t < 6; ++t) r[t] = a.v[t];
-    for (int t = 0; t < 3; ++t) r[6 + t] = (double)a.nan[t];
-    for (int t = 0; t < 4; ++t) {
-      r[9 + 2 * t] = a.k[t];
-      r[10 + 2 * t] = (double)a.i[t];
+    for (int w = 1; w < DG_THREADS / 32; ++w) {
+      for (int t = 0; t < 6; ++t) v[t] = fmax(v[t], s_v[w][t]);
+      nan |= s_nan[w];
     }
-    r[17] = 0.0;
+    double* r = part + ((long)m * nblk + blockIdx.x) * CTL_REC;
+    for (int t = 0; t < 6; ++t) r[t] = ctl_rec_value(v[t]);
+    for (int t = 0; t < 3; ++t) r[6 + t] = (nan >> t) & 1 ? 1.0 : 0.0;
   }
 }
 
 // One thread per member: the member's record, the blow-up test (:149-157), its
-// results out[m * 32 ..] = zmax(1:6), kindic, positions (11); flag = 1 when it fires.
+// results out[m * CTL_OUT ..] = zmax(1:6), kindic; when it fires the locate request,
+// the keys of the extremes, idx = the largest index (to be lowered by k_ctl_locate),
+// and flag = 1.
 template <class T>
-__global__ void k_ctl_final(Dom<T> d, const double* part, int nblk, int someoce, double* out, int* flag) {
+__global__ void k_ctl_final(Dom<T> d, const double* part, int nblk, int someoce, double* out,
+                            unsigned long long* idx, int* flag) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= d.nmem) return;
-  CtlAcc a;
-  ctl_init(a);
+  double z[6];
+  for (int t = 0; t < 6; ++t) z[t] = -1.7976931348623157e308;
+  int nan[3] = {0, 0, 0};
   for (int b = 0; b < nblk; ++b) {
     const double* r = part + ((long)m * nblk + b) * CTL_REC;
-    CtlAcc o;
-    for (int t = 0; t < 6; ++t) o.v[t] = r[t];
-    for (int t = 0; t < 3; ++t) o.nan[t] = r[6 + t] != 0.0;
-    for (int t = 0; t < 4; ++t) {
-      o.k[t] = r[9 + 2 * t];
-      o.i[t] = (long long)r[10 + 2 * t];
-    }
-    ctl_merge(a, o);
+    for (int t = 0; t < 6; ++t) z[t] = fmax(z[t], r[t]);
+    for (int t = 0; t < 3; ++t) nan[t] |= r[6 + t] != 0.0;
   }
-  double z[6];
-  for (int t = 0; t < 6; ++t) z[t] = a.v[t];
-  if (a.nan[0]) z[0] = NAN;
-  if (a.nan[1]) z[1] = NAN;
-  if (a.nan[2]) { z[2] = NAN; z[3] = NAN; }
+  double key[4] = {nan[0] ? INFINITY : z[0], nan[1] ? INFINITY : z[1], nan[2] ? -INFINITY : -z[2],
+                   nan[2] ? INFINITY : z[3]};
+  if (nan[0]) z[0] = NAN;
+  if (nan[1]) z[1] = NAN;
+  if (nan[2]) { z[2] = NAN; z[3] = NAN; }
   const bool trip = someoce && (z[0] > 20.0 || z[1] > 10.0 || z[2] >= 0.0 || z[3] >= 100.0 || z[3] < 0.0 ||
                                 isnan(z[0] + z[1] + z[2]));
-  double* o = out + (long)m * 32;
+  double* o = out + (long)m * CTL_OUT;
   for (int t = 0; t < 6; ++t) o[t] = z[t];
   o[6] = trip ? -3.0 : 0.0;
-  const long n2 = d.n2;
-  const int jpi = d.jpi, jpj = d.jpj;
   for (int t = 0; t < 11; ++t) o[7 + t] = 0.0;
-  if (trip) {
-    const long ih = a.i[0], iu = a.i[1], i1 = a.i[2], i2 = a.i[3];
-    o[7] = (double)(ih % jpi + 1); o[8] = (double)(ih / jpi + 1);
-    o[9] = (double)(iu % jpi + 1); o[10] = (double)((iu / jpi) % jpj + 1); o[11] = (double)(iu / n2 + 1);
-    if (i1 != 0x7fffffffffffffffLL) {
-      o[12] = (double)(i1 % jpi + 1); o[13] = (double)((i1 / jpi) % jpj + 1); o[14] = (double)(i1 / n2 + 1);
-      o[15] = (double)(i2 % jpi + 1); o[16] = (double)((i2 / jpi) % jpj + 1); o[17] = (double)(i2 / n2 + 1);
+  o[18] = trip ? 1.0 : 0.0;
+  for (int t = 0; t < 4; ++t) {
+    o[19 + t] = key[t];
+    idx[m * 4 + t] = 0xffffffffffffffffULL;
+  }
+  if (trip) atomicExch(flag, 1);
+}
+
+// grid (nblk, nmem): the first index in Fortran order of each extreme of a member
+// whose test fired (atomicMin into idx); returns at once for the others
+template <class T>
+__global__ void __launch_bounds__(DG_THREADS) k_ctl_locate(Dom<T> d, const T* __restrict__ sshn,
+                                                           const T* __restrict__ un, const T* __restrict__ ts,
+                                                           const double* out, unsigned long long* idx) {
+  const int m = blockIdx.y;
+  const double* o = out + (long)m * CTL_OUT;
+  if (o[18] == 0.0) return;
+  const double k0 = o[19], k1 = o[20], k2 = o[21], k3 = o[22];
+  const long n2 = d.n2, n3 = d.n3;
+  const long stride = (long)gridDim.x * DG_THREADS;
+  unsigned long long best[4] = {~0ULL, ~0ULL, ~0ULL, ~0ULL};
+  const T* s2 = sshn + m * n2;
+  const T* u3 = un + m * n3;
+  const T* t3 = ts + m * 2 * n3;
+  for (long p = blockIdx.x * (long)DG_THREADS + threadIdx.x; p < n2; p += stride) {
+    const T s = fabs(s2[p]);
+    if ((s != s ? INFINITY : (double)s) == k0 && (unsigned long long)p < best[0]) best[0] = p;
+    for (int k = 1; k <= d.jpk; ++k) {
+      const long q = p + (long)(k - 1) * n2;
+      const T x = fabs(u3[q]);
+      if ((x != x ? INFINITY : (double)x) == k1 && (unsigned long long)q < best[1]) best[1] = q;
     }
-    atomicExch(flag, 1);
+    const ColInfo c = d.ci[p];
+    for (int k = c.tlo; k <= c.thi; ++k) {
+      const long q = p + (long)(k - 1) * n2;
+      const T sv = t3[q + n3];
+      if ((sv != sv ? -INFINITY : (double)sv) == k2 && (unsigned long long)q < best[2]) best[2] = q;
+      if ((sv != sv ? INFINITY : (double)sv) == k3 && (unsigned long long)q < best[3]) best[3] = q;
+    }
+  }
+  for (int t = 0; t < 4; ++t) {
+    unsigned long long b = best[t];
+    for (int off = 16; off > 0; off >>= 1) {
+      const unsigned long long o2 = __shfl_down_sync(0xffffffffu, b, off);
+      b = o2 < b ? o2 : b;
+    }
+    if ((threadIdx.x & 31) == 0 && b != ~0ULL) atomicMin(idx + m * 4 + t, b);
+  }
+}
+
+// One thread per member: the positions (i, j[, k], 1-based) of the located extremes
+template <class T>
+__global__ void k_ctl_pos(Dom<T> d, double* out, const unsigned long long* idx) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= d.nmem) return;
+  double* o = out + (long)m * CTL_OUT;
+  if (o[18] == 0.0) return;
+  const long long n2 = d.n2, jpi = d.jpi, jpj = d.jpj;
+  const unsigned long long* x = idx + m * 4;
+  if (x[0] != ~0ULL) { o[7] = (double)(x[0] % jpi + 1); o[8] = (double)(x[0] / jpi + 1); }
+  if (x[1] != ~0ULL) {
+    o[9] = (double)(x[1] % jpi + 1); o[10] = (double)((x[1] / jpi) % jpj + 1); o[11] = (double)(x[1] / n2 + 1);
+  }
+  if (x[2] != ~0ULL && x[3] != ~0ULL) {
+    o[12] = (double)(x[2] % jpi + 1); o[13] = (double)((x[2] / jpi) % jpj + 1); o[14] = (double)(x[2] / n2 + 1);
+    o[15] = (double)(x[3] % jpi + 1); o[16] = (double)((x[3] / jpi) % jpj + 1); o[17] = (double)(x[3] / n2 + 1);
   }
 }
 

@@ -870,6 +870,80 @@ __global__ void k_dyn_zad(Dom<T> d, const T* __restrict__ un, const T* __restric
   }
 }
 
+// ---------------------------------------------------------------- usrdef_sbc (GYRE)
+// SIN and COS of the analytic forcing: FP64 by the evaluations the test oracle shares
+// (nemo_sin.h), FP32 by the library
+template <class T> __device__ __forceinline__ T usr_sin(T x);
+template <class T> __device__ __forceinline__ T usr_cos(T x);
+template <> __device__ __forceinline__ double usr_sin<double>(double x) { return nemo_sin(x); }
+template <> __device__ __forceinline__ double usr_cos<double>(double x) { return nemo_cos(x); }
+template <> __device__ __forceinline__ float usr_sin<float>(float x) { return sinf(x); }
+template <> __device__ __forceinline__ float usr_cos<float>(float x) { return cosf(x); }
+
+// The point part of usrdef_sbc_oce (usrdef_sbc.F90:113-135, :160-172), one (i,j) a
+// thread: sbc's swap of the before fields, qsr, the restoring qns from the before SST,
+// the raw E-P, the wind stress
+template <class T>
+__global__ void k_usr_sbc_a(Dom<T> d, UsrSbcArgs<T> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i > d.jpi || j > d.jpj) return;
+  const int m = blockIdx.z;
+  const long ij = (long)(i - 1) + (long)(j - 1) * d.jpi, p = (long)m * d.n2 + ij;
+  const long q = (long)m * 2 * d.n3 + ij;  // surface temperature of the member
+  if (a.s[6] != 0.0) {
+    if (a.utau_b) a.utau_b[p] = a.utau[p];
+    if (a.vtau_b) a.vtau_b[p] = a.vtau[p];
+    if (a.emp_b) a.emp_b[p] = a.emp[p];
+  }
+  const T rpi = T(3.141592653589793);
+  const T g = a.gphit[p];
+  const T t_star = T(a.s[0]) * usr_cos<T>(rpi * (g - T(5.)) / T(a.s[1]));
+  const T qsr = T(230) * usr_cos<T>(T(3.1415) * (g - T(a.s[2])) / T(0.9 * 180));
+  a.qsr[p] = qsr;
+  a.qns[p] = T(-40.e0) * (a.tsb[q] - t_star) - qsr;
+  T emp;
+  if (g >= T(14.845) && T(37.2) >= g)
+    emp = T(0.7) * T(3.16e-5) * usr_sin<T>(rpi / T(2) * (g - T(37.2)) / T(24.6 - 37.2)) * T(a.s[3]);
+  else
+    emp = -T(0.8) * T(3.16e-5) * usr_sin<T>(rpi / T(2) * (g - T(37.2)) / T(46.8 - 37.2)) * T(a.s[4]);
+  a.emp[p] = emp;
+  const T ztaun = T(a.s[5]);
+  a.utau[p] = -ztaun * usr_sin<T>(rpi * (a.gphiu[p] - T(15.)) / T(29. - 15.));
+  a.vtau[p] = ztaun * usr_sin<T>(rpi * (a.gphiv[p] - T(15.)) / T(29. - 15.));
+}
+
+// The rest (usrdef_sbc.F90:137-144, :176-186): E-P less its domain mean, sfx = 0, the
+// heat content of E-P at the now SST in qns, the wind-stress modulus (interior; the
+// closed lbc_lnk zeroes the edges)
+template <class T>
+__global__ void k_usr_sbc_b(Dom<T> d, UsrSbcArgs<T> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i > d.jpi || j > d.jpj) return;
+  const int m = blockIdx.z;
+  const long ij = (long)(i - 1) + (long)(j - 1) * d.jpi, p = (long)m * d.n2 + ij;
+  const long q = (long)m * 2 * d.n3 + ij;
+  const double zsumemp = a.gsum[m] / a.zsurf;
+  const T tm = tmsk<T>(d.ci[ij], 1);
+  const T emp = (T)((double)a.emp[p] - zsumemp * (double)tm);
+  a.emp[p] = emp;
+  a.sfx[p] = T(0);
+  a.qns[p] = a.qns[p] - emp * a.tsn[q] * T(a.rcp);
+  T tau = T(0);
+  if (i >= 2 && i <= d.jpi - 1 && j >= 2 && j <= d.jpj - 1) {
+    const T ztx = a.utau[p - 1] + a.utau[p];
+    const T zty = a.vtau[p - d.jpi] + a.vtau[p];
+    tau = T(0.5) * sqrt(ztx * ztx + zty * zty);
+  }
+  a.taum[p] = tau;
+}
+
+// the step's scalars of the forcing into device memory (a launch outside any
+// captured graph, so a replay reads the values of its own step)
+__global__ void k_usr_put(double* dst, double s0, double s1, double s2, double s3, double s4, double s5,
+                          double s6) {
+  dst[0] = s0; dst[1] = s1; dst[2] = s2; dst[3] = s3; dst[4] = s4; dst[5] = s5; dst[6] = s6;
+}
+
 // ---------------------------------------------------------------- zdf_phy (TKE)
 // SIN of the Langmuir-cell source: FP64 by the evaluation the test oracle shares
 // (nemo_sin.h), FP32 by the library

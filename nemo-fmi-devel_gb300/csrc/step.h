@@ -87,6 +87,18 @@ struct DynZdfArgs {
   T r2dt, zdt, rau0;
 };
 
+// GYRE's analytic surface forcing (usrdef_sbc.F90). s: the step's scalars formed on
+// the host (usr_scalars): the amplitude and the denominator of T*, 23.5 zcos_sais1,
+// the two seasonal factors of E-P, ztaun, and the swap flag (kt /= nit000); gsum:
+// glob_sum of the raw E-P per member; the before fields may be null.
+template <class T>
+struct UsrSbcArgs {
+  const T *gphit, *gphiu, *gphiv, *tsb, *tsn;
+  T *qsr, *qns, *emp, *sfx, *utau, *vtau, *taum, *utau_b, *vtau_b, *emp_b;
+  const double *s, *gsum;
+  double zsurf, rcp;
+};
+
 // zdf_phy with the TKE closure and zdf_evd. Member strides n3 (3-D) and n2 (taum,
 // fr_i). Work arrays (n3 per member): sh2, apdlr (the inverse Prandtl number), and
 // the three diagonals of the TKE system, whose storage the mixing lengths zmxlm
@@ -115,6 +127,11 @@ cudaError_t launch_zdf_mxl(const Dom<T>& d, const MxlArgs<T>& a, cudaStream_t s)
 template <class T>
 cudaError_t launch_dyn_zdf_imp(const Dom<T>& d, const DynZdfArgs<T>& a, cudaStream_t s);
 template <class T>
+cudaError_t launch_usr_sbc_a(const Dom<T>& d, const UsrSbcArgs<T>& a, cudaStream_t s);
+template <class T>
+cudaError_t launch_usr_sbc_b(const Dom<T>& d, const UsrSbcArgs<T>& a, cudaStream_t s);
+cudaError_t launch_usr_put(double* dst, const double* v, cudaStream_t s);
+template <class T>
 cudaError_t launch_zdf_phy(const Dom<T>& d, const ZphyArgs<T>& a, cudaStream_t s);
 template <class T>
 cudaError_t launch_eos(const Dom<T>& d, const EosArgs<T>& a, cudaStream_t s);
@@ -140,7 +157,7 @@ cudaError_t launch_ssh_swp(const Dom<T>& d, T* sshb, T* sshn, const double* ssha
 // stp_ctl: block partials part (nblk x nmem records), results out (32 doubles a member)
 template <class T>
 cudaError_t launch_stp_ctl(const Dom<T>& d, const T* sshn, const T* un, const T* ts, double* part, int nblk,
-                           int someoce, double* out, int* flag, cudaStream_t s);
+                           int someoce, double* out, unsigned long long* idx, int* flag, cudaStream_t s);
 // dia_hsb: the initial fields, and one call (block partials part: nblk x nmem x 13 pairs)
 template <class T>
 cudaError_t launch_hsb_init(const Dom<T>& d, const HsbArgs<T>& a, int nblk, cudaStream_t s);

@@ -289,6 +289,10 @@ class Context:
     def zdf_mxl(self, kt):
         self._ck(self.lib.nemo_gpu_zdf_mxl(self.h, kt), "zdf_mxl")
 
+    def usrdef_sbc(self, kt):
+        """GYRE's analytic surface forcing of step kt on the bound fields (usrdef_sbc.F90)"""
+        self._ck(self.lib.nemo_gpu_usrdef_sbc(self.h, kt), "usrdef_sbc")
+
     def zdf_phy(self, kt):
         """zdf_sh2, the TKE closure and zdf_evd on the bound fields (zdfphy.F90:243-316)"""
         self._ck(self.lib.nemo_gpu_zdf_phy(self.h, kt), "zdf_phy")

@@ -9,11 +9,15 @@ Six translation units are compiled in parallel and linked into
   ``--prec-div=false`` (single-precision quotients within 2 ulp instead of
   correctly rounded: the mixed form's tolerance is set by FP32 storage, and the
   correctly rounded quotient costs a multi-instruction sequence per division);
-* ``capi.cu``      -- the C ABI (host code);
+* ``capi.cu``      -- the C ABI (host code; the host compiler without contraction,
+  ``-ffp-contract=off``, so that the scalars it forms -- barotropic weights, the
+  EOS-80 re-expansion, the forcing's seasonal factors -- round like the oracle's on
+  any host, FMA-capable Arm included);
 * ``noalloc.cu``   -- the allocation-free global sum (static device scratch);
 * ``adj_fp64.cu``  -- the adjoint kernels of the tracer routines and tra_nxt
   (``--fmad=false``);
-* ``inst_step.cu`` -- wzv, the dyn_zdf time step, dyn_nxt and ssh_swp, both
+* ``inst_step.cu`` -- the rest of the model step (wzv, dyn_zdf, dyn_nxt, ssh_swp,
+  the momentum trends, eos, zdf_phy, the forcing, stp_ctl, dia_hsb, ...), both
   precisions (``--fmad=false``).
 """
 import concurrent.futures as cf
@@ -31,7 +35,7 @@ COMMON = ["-O3", "-std=c++17", "--extended-lambda", "-lineinfo", "-Xcompiler", "
 UNITS = {
     "inst_fp64.cu": ["--fmad=false"],
     "inst_fp32.cu": ["--prec-div=false"],
-    "capi.cu": [],
+    "capi.cu": ["-Xcompiler", "-ffp-contract=off"],
     "noalloc.cu": ["--fmad=false"],
     "adj_fp64.cu": ["--fmad=false"],
     "inst_step.cu": ["--fmad=false"],

@@ -395,20 +395,24 @@ def viscosity(dom, ahm0=1.0e5):
     return np.asfortranarray(ahmt), np.asfortranarray(ahmf)
 
 
-# GYRE's physics (cfgs/GYRE_PISCES/EXPREF/namelist_cfg): EOS-80, the TKE closure with
-# enhanced vertical diffusion, the penetrating solar flux
-FULL_NAMELIST = dict(ln_eos80=1, ln_seos=0, ln_zdftke=1, ln_zdfevd=1, ln_traqsr=1)
+# GYRE's physics (cfgs/GYRE_PISCES/EXPREF/namelist_cfg): the analytic surface forcing
+# formed every step, EOS-80, the TKE closure with enhanced vertical diffusion, the
+# penetrating solar flux
+FULL_NAMELIST = dict(ln_usr=1, ln_eos80=1, ln_seos=0, ln_zdftke=1, ln_zdfevd=1, ln_traqsr=1)
 # the fields of the full step besides the hot path's (3-D, then 2-D; nmln is int32)
 FULL_3D = ("en", "dissl", "avm_k", "avt_k", "avm", "avs", "rn2", "rn2b", "rhd", "rhop", "gdept_n", "gdepw_n",
            "qsr_hc", "qsr_hc_b", "ahmt", "ahmf")
-FULL_2D = ("taum", "qsr", "qns", "sfx", "fraqsr_1lev", "hmlp", "hmlpt", "sbc_tsc", "sbc_tsc_b")
+FULL_2D = ("taum", "qsr", "qns", "sfx", "fraqsr_1lev", "hmlp", "hmlpt", "sbc_tsc", "sbc_tsc_b", "gphit", "gphiu",
+           "gphiv", "utau_b", "vtau_b")
 
 
 def full_physics(dom, nam, st):
     """The namelist and the state of the full GYRE step from a state of state(): the
-    analytic surface forcing of the first time step (sbc_inputs), the cold start of
-    the TKE closure (vphys_inputs), the rest-state depths, the lateral viscosity, and
-    zeroed rn2b, rhd, rhop, mixed-layer fields (the step forms them)."""
+    latitudes the analytic forcing reads (the step forms the forcing itself;
+    sbc_inputs gives the first values and the restart fields of tra_sbc / tra_qsr),
+    the cold start of the TKE closure (vphys_inputs), the rest-state depths, the
+    lateral viscosity, and zeroed rn2b, rhd, rhop, mixed-layer fields (the step forms
+    them)."""
     nam = dict(nam, **FULL_NAMELIST)
     ahmt, ahmf = viscosity(dom)
     st = dict(st)
@@ -417,5 +421,8 @@ def full_physics(dom, nam, st):
     sl = slope_inputs(dom, nam, st)
     z3, z2 = np.zeros_like(st["avt"]), np.zeros_like(st["sshn"])
     st.update(gdept_n=sl["gdept_n"], rn2b=z3, rhd=z3.copy(), rhop=z3.copy(), ahmt=ahmt, ahmf=ahmf, hmlp=z2,
-              hmlpt=z2.copy(), nmln=np.zeros(z2.shape, dtype=np.int32, order="F"))
+              hmlpt=z2.copy(), nmln=np.zeros(z2.shape, dtype=np.int32, order="F"),
+              gphit=np.asfortranarray(dom["gphit"]), gphiu=np.asfortranarray(dom["gphiu"]),
+              gphiv=np.asfortranarray(dom["gphiv"]), utau_b=np.array(st["utau"], order="F"),
+              vtau_b=np.array(st["vtau"], order="F"))
     return nam, st

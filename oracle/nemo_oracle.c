@@ -1687,8 +1687,81 @@ int ora_glob_sum(ora_ctx *c, const double *ptab, int nk, double *out) {
   return NEMO_OK;
 }
 
-/* the shared sine of the Langmuir-cell source, exported for its accuracy test */
+/* the shared sines and cosine (nemo_sin.h), exported for their accuracy tests */
 double ora_sin_0pi(double x) { return nemo_sin_0pi(x); }
+double ora_sin(double x) { return nemo_sin(x); }
+double ora_cos(double x) { return nemo_cos(x); }
+
+/* ---------------------------------------------------------------- usrdef_sbc */
+/* GYRE's analytic surface forcing, usrdef_sbc_oce (usrdef_sbc.F90:62-190) at time
+ * step kt, year 1 of a 360-day calendar, preceded by sbc's swap of the before fields
+ * (sbcmod.F90:389-394) when kt /= nit000 and they are bound: qsr and the restoring
+ * qns from the before SST, E-P (its domain mean removed, GLOB_SUM) and its heat
+ * content at the now SST (sst_m of sbc_ssm with nn_fsbc = 1), sfx = 0, the wind
+ * stress and its modulus taum (interior, closed lbc_lnk). SIN and COS are the shared
+ * evaluations of nemo_sin.h. Bound: GPHIT GPHIU GPHIV TSB TSN, QSR QNS EMP SFX UTAU
+ * VTAU TAUM; UTAU_B VTAU_B EMP_B optional. */
+int ora_usrdef_sbc(ora_ctx *c, int kt) {
+  const nemo_namelist *nm = &c->nam;
+  const int jpi = c->jpi, jpj = c->jpj;
+  const size_t n2 = (size_t)jpi * jpj;
+  double **F = c->f;
+  const double *gphit = F[NEMO_F_GPHIT], *gphiu = F[NEMO_F_GPHIU], *gphiv = F[NEMO_F_GPHIV];
+  const double *tsb = F[NEMO_F_TSB], *tsn = F[NEMO_F_TSN];
+  double *qsr = F[NEMO_F_QSR], *qns = F[NEMO_F_QNS], *emp = F[NEMO_F_EMP], *sfx = F[NEMO_F_SFX];
+  double *utau = F[NEMO_F_UTAU], *vtau = F[NEMO_F_VTAU], *taum = F[NEMO_F_TAUM];
+  if (!gphit || !gphiu || !gphiv || !tsb || !tsn || !qsr || !qns || !emp || !sfx || !utau || !vtau || !taum)
+    return NEMO_ERR_UNBOUND;
+  if (kt != nm->nit000) {  /* sbcmod.F90:389-394 */
+    if (F[NEMO_F_UTAU_B]) memcpy(F[NEMO_F_UTAU_B], utau, n2 * sizeof(double));
+    if (F[NEMO_F_VTAU_B]) memcpy(F[NEMO_F_VTAU_B], vtau, n2 * sizeof(double));
+    if (F[NEMO_F_EMP_B]) memcpy(F[NEMO_F_EMP_B], emp, n2 * sizeof(double));
+  }
+  const double rpi = 3.141592653589793, rcp = nm->rcp > 0 ? nm->rcp : 3991.86795711963;
+  const double zyydd = 360.0, rjjhh = 24.0;
+  const double ztime = (double)kt * nm->rn_rdt / (60.0 * 60.0);  /* hours; year 1: no years to subtract */
+  const double ztimemax1 = ((5. * 30.) + 21.) * 24., ztimemin1 = ztimemax1 + rjjhh * zyydd / 2;
+  const double ztimemax2 = ((6. * 30.) + 21.) * 24., ztimemin2 = ztimemax2 - rjjhh * zyydd / 2;
+  const double zemp_S = 0.7, zemp_N = 0.8, zemp_sais = 0.1, zTstar = 28.3;
+  const double zcos_sais1 = nemo_cos((ztime - ztimemax1) / (ztimemin1 - ztimemax1) * rpi);
+  const double zcos_sais2 = nemo_cos((ztime - ztimemax2) / (ztimemax2 - ztimemin2) * rpi);
+  const double ztrp = -40.e0, zconv = 3.16e-5;
+  for (size_t p = 0; p < n2; ++p) {  /* (:113-135) */
+    const double g = gphit[p];
+    const double t_star = zTstar * (1. + 1. / 50. * zcos_sais2) * nemo_cos(rpi * (g - 5.) / (53.5 * (1 + 11 / 53.5 * zcos_sais2) * 2.));
+    qsr[p] = 230 * nemo_cos(3.1415 * (g - 23.5 * zcos_sais1) / (0.9 * 180));
+    qns[p] = ztrp * (tsb[p] - t_star) - qsr[p];
+    if (g >= 14.845 && 37.2 >= g)
+      emp[p] = zemp_S * zconv * nemo_sin(rpi / 2 * (g - 37.2) / (24.6 - 37.2)) * (1 - zemp_sais / zemp_S * zcos_sais1);
+    else
+      emp[p] = -zemp_N * zconv * nemo_sin(rpi / 2 * (g - 37.2) / (46.8 - 37.2)) * (1 - zemp_sais / zemp_N * zcos_sais1);
+  }
+  double zsumemp, zsurf;  /* (:137-139) */
+  ora_glob_sum(c, emp, 1, &zsumemp);
+  ora_glob_sum(c, c->tmask, 1, &zsurf);
+  zsumemp = zsumemp / zsurf;
+  for (size_t p = 0; p < n2; ++p) {  /* (:142-144) */
+    emp[p] = emp[p] - zsumemp * c->tmask[p];
+    sfx[p] = 0.0;
+    qns[p] = qns[p] - emp[p] * tsn[p] * rcp;
+  }
+  /* the wind stress (:160-172) and its modulus (:176-186) */
+  const double ztimemax = ((5. * 30.) + 21.) * 24., ztimemin = ztimemax + rjjhh * zyydd / 2;
+  const double ztau = 0.105 / sqrt(2.), ztau_sais = 0.015;
+  const double ztaun = ztau - ztau_sais * nemo_cos((ztime - ztimemax) / (ztimemin - ztimemax) * rpi);
+  for (size_t p = 0; p < n2; ++p) {
+    utau[p] = -ztaun * nemo_sin(rpi * (gphiu[p] - 15.) / (29. - 15.));
+    vtau[p] = ztaun * nemo_sin(rpi * (gphiv[p] - 15.) / (29. - 15.));
+  }
+  for (size_t p = 0; p < n2; ++p) taum[p] = 0.0;
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      const double ztx = utau[I2(ji - 1, jj)] + utau[I2(ji, jj)];
+      const double zty = vtau[I2(ji, jj - 1)] + vtau[I2(ji, jj)];
+      taum[I2(ji, jj)] = 0.5 * sqrt(ztx * ztx + zty * zty);
+    }
+  return NEMO_OK;
+}
 
 /* ---------------------------------------------------------------- zdf_phy */
 /* zdf_phy (zdfphy.F90:243-291) for the TKE closure: zdf_sh2 (zdfsh2.F90:30-76)
@@ -2759,8 +2832,7 @@ int ora_tra_nxt_adj(ora_ctx *c, int kt, double *tsb_ad, double *tsn_ad, double *
 /* ======================================================= the rest of the step */
 /* The parts of stp (step.F90:96-305) that close the path into a time step with the
  * linear free surface: the vertical velocity, the time step and the swaps of the
- * momentum and the sea surface height. The momentum trends outside the path
- * (dyn_adv, dyn_vor, dyn_ldf, dyn_hpg) and the vertical viscosity are held at 0. */
+ * momentum and the sea surface height. */
 
 /* div_hor (divhor.F90:62-110) and wzv (sshwzv.F90:129-213) on the bound un, vn, wn. */
 int ora_wzv(ora_ctx *c, int kt) {
@@ -3489,8 +3561,9 @@ static int vphys_on(const ora_ctx *c) {
 }
 
 /* One model step (step.F90:96-305) with the path and the routines above: the
- * vertical physics (rab_3d and bn2 of the before and now tracers, zdf_phy), the
- * iso-neutral slopes, ua = va = 0, dyn_adv (keg + zad), dyn_vor (vor_ene), dyn_ldf,
+ * GYRE analytic forcing (ln_usr), the vertical physics (rab_3d and bn2 of the
+ * before and now tracers, zdf_phy), the
+ * iso-neutral slopes, div_hor + wzv, ua = va = 0, dyn_adv (keg + zad), dyn_vor (vor_ene), dyn_ldf,
  * eos + dyn_hpg, dyn_spg_ts, div_hor + wzv, dyn_zdf, tsa = 0, tra_sbc, tra_qsr,
  * tra_adv, tra_ldf, tra_zdf, tra_nxt, dyn_nxt, ssh_swp, dia_hsb, stp_ctl; the
  * optional ones where their fields are bound. */
@@ -3499,6 +3572,10 @@ int ora_stp_model(ora_ctx *c, int kt) {
   if (!c->f[NEMO_F_UA] || !c->f[NEMO_F_VA]) return NEMO_ERR_UNBOUND;
   int st = 0;
   const nemo_namelist *nm = &c->nam;
+  if (nm->ln_usr) {                                               /* step.F90:116: sbc */
+    st = ora_usrdef_sbc(c, kt);
+    if (st) return st;
+  }
   const int vphys = vphys_on(c);
   if (vphys) {                                                    /* step.F90:127-133 */
     double *rab = zalloc(2 * n3);
@@ -3525,6 +3602,10 @@ int ora_stp_model(ora_ctx *c, int kt) {
     if (!st) st = ora_ldf_slp(c, kt, c->f[NEMO_F_RHD], c->f[NEMO_F_RN2B]);
     if (st) return st;
   }
+  /* ssh_nxt's div_hor and wzv (step.F90:156-160): the now vertical velocity of dyn_adv
+   * (ssha is dyn_spg_ts's with the split-explicit free surface) */
+  st = ora_wzv(c, kt);
+  if (st) return st;
   memset(c->f[NEMO_F_UA], 0, n3 * sizeof(double));
   memset(c->f[NEMO_F_VA], 0, n3 * sizeof(double));
   /* dyn_adv, dyn_vor (step.F90:190-191): the vector form, keg (C2) + zad, and vor_ene

@@ -65,6 +65,9 @@ int ora_tra_zdf(ora_ctx *c, int kt);
 int ora_dyn_spg_ts(ora_ctx *c, int kt);
 int ora_lbc_lnk(ora_ctx *c, double *ptab, int nk, int nl, char cd_nat, double psgn, double pval);
 /* zdf_phy with zdf_sh2, the TKE closure and zdf_evd (see nemo_gpu_zdf_phy) */
+double ora_sin(double x);
+double ora_cos(double x);
+int ora_usrdef_sbc(ora_ctx *c, int kt);
 double ora_sin_0pi(double x);
 int ora_zdf_phy(ora_ctx *c, int kt);
 /* stp_ctl (stpctl.F90:44-194): zmax[NEMO_CTL_N], loc[NEMO_CTL_NLOC], kindic */

@@ -47,6 +47,9 @@ def lib():
         P("ora_stp_ctl", [vp, i, vp, vp, C.POINTER(i)])
         P("ora_zdf_phy", [vp, i])
         P("ora_sin_0pi", [d], d)
+        P("ora_sin", [d], d)
+        P("ora_cos", [d], d)
+        P("ora_usrdef_sbc", [vp, i])
         P("ora_dia_hsb_init", [vp])
         P("ora_dia_hsb", [vp, i, vp])
         P("ora_stp_ctl_last", [vp, vp, vp, C.POINTER(i)])
@@ -199,6 +202,9 @@ class Oracle:
 
     def stp_hotpath(self, kt):
         self._ck(lib().ora_stp_hotpath(self.h, kt), "stp_hotpath")
+
+    def usrdef_sbc(self, kt):
+        self._ck(lib().ora_usrdef_sbc(self.h, kt), "usrdef_sbc")
 
     def zdf_phy(self, kt):
         self._ck(lib().ora_zdf_phy(self.h, kt), "zdf_phy")
