@@ -225,8 +225,10 @@ def state(dom, nam, seed=0, noise_t=0.05, noise_s=0.01, u0=0.5, member=0, noise_
         a = 0.004 * rng.standard_normal((jpi, jpj, jpk))
         return np.asfortranarray(np.clip(a, -0.01, 0.01) * m)
     uslp, vslp, wslpi, wslpj = slope(um), slope(vm), slope(wm), slope(wm)
-    wslpi[:, :, 0] = 0.0
-    wslpj[:, :, 0] = 0.0
+    # ldf_slp writes levels 2..jpk-1 only: the surface slopes stay at their initial 0
+    # (ldf_slp_init), and a model step that forms the slopes keeps them there
+    for a in (uslp, vslp, wslpi, wslpj):
+        a[:, :, 0] = 0.0
     # restart fields of a run in progress (dynspg_ts.F90:1214-1227): the half-step
     # transports of the previous step, close to the now barotropic transports
     ub2_b, vb2_b = np.asfortranarray(un_b * hu), np.asfortranarray(vn_b * hv)
