@@ -294,11 +294,16 @@ def ten_days(dom, nam, states, stream, nsteps=120):
     import numpy as np
     nam = dict(nam, neuler=0)
     nam, states = full_gyre(dom, nam, states)
+    # the FP64 step from the same state rounded to FP32: how far the model's own
+    # sensitivity (convective and closure thresholds) carries a 6e-8 perturbation
+    rounded = [{k: (np.asfortranarray(v.astype(np.float32).astype(np.float64))
+                    if isinstance(v, np.ndarray) and v.dtype == np.float64 else v) for k, v in st.items()}
+               for st in states]
     jpi, jpj, jpk = dom["jpi"], dom["jpj"], dom["jpk"]
     out = {}
-    for prec in ("fp64", "mixed"):
-        ctx, dev = make_ctx(dom, nam, states, prec, stream)
-        bind_full(ctx, dev, states)
+    for prec, sts in (("fp64", states), ("mixed", states), ("fp64_rounded", rounded)):
+        ctx, dev = make_ctx(dom, nam, sts, prec.split("_")[0], stream)
+        bind_full(ctx, dev, sts)
         for kt in range(1, nsteps + 1):
             ctx.stp_model(kt)
         ctx.synchronize()
@@ -313,18 +318,26 @@ def ten_days(dom, nam, states, stream, nsteps=120):
                    "eos_insitu + ldf_slp, dyn_keg + dyn_zad + vor_ene + dyn_ldf_lap, EOS-80 + dyn_hpg, "
                    "dyn_spg_ts, wzv, dyn_zdf (implicit viscosity), tra_sbc + tra_qsr, the hot path, "
                    "tra_nxt, dyn_nxt, ssh_swp, stp_ctl",
-           "forcing": "GYRE analytic fluxes of the first time step, held for the run"}
+           "forcing": "GYRE's analytic fluxes formed on the device every step (usrdef_sbc)",
+           "fp64_rounded": "the FP64 step started from the same state rounded to FP32, against the FP64 step: "
+                           "the model's own sensitivity, a floor for any FP32-storage form"}
     for n, sel in (("T", None), ("S", None), ("SST", "T"), ("SSS", "S"), ("U", None), ("V", None), ("SSH", None)):
-        a, b = out["mixed"][sel or n], out["fp64"][sel or n]
+        b = out["fp64"][sel or n]
         if n in ("SST", "SSS"):
-            a, b, m = a[:, :, 0], b[:, :, 0], tm[:, :, 0]
+            b, m = b[:, :, 0], tm[:, :, 0]
         elif n == "SSH":
             m = tm[:, :, 0]
         else:
             m = tm
-        d = (a - b)[m]
-        res[n] = {"rms": float(np.sqrt(np.mean(d * d))), "max": float(np.abs(d).max()),
-                  "range": float(np.abs(b[m]).max())}
+        res[n] = {"range": float(np.abs(b[m]).max())}
+        for arm in ("mixed", "fp64_rounded"):
+            a = out[arm][sel or n]
+            if n in ("SST", "SSS"):
+                a = a[:, :, 0]
+            d = (a - b)[m]
+            key = "" if arm == "mixed" else "_fp64_rounded"
+            res[n]["rms" + key] = float(np.sqrt(np.mean(d * d)))
+            res[n]["max" + key] = float(np.abs(d).max())
     return res
 
 
