@@ -108,6 +108,7 @@ struct nemo_ctx {
   unsigned long long* ctl_idx = nullptr;  // first indices of the extremes (4 per member)
   int* ctl_flag = nullptr;
   int ctl_nblk = 0;
+  int hsb_nblk = 0;  // dia_hsb's block partials (2 per SM)
   int someoce = 0;  // the domain has ocean points (stpctl.F90:111)
   bool hsb_on = false;
   double* hsb_mem = nullptr;  // surf, tmask_h; ssh, ssh heat, ssh salt (x nmem); e3t, heat, salt (x nmem)
@@ -1451,7 +1452,7 @@ int hsb_check(nemo_ctx* c) {
 
 template <class T>
 int run_dia_hsb(nemo_ctx* c) {
-  cudaError_t e = launch_dia_hsb<T>(dom<T>(c), hsb_args<T>(c), c->hsb_part, c->ctl_nblk, c->stream);
+  cudaError_t e = launch_dia_hsb<T>(dom<T>(c), hsb_args<T>(c), c->hsb_part, c->hsb_nblk, c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "dia_hsb launch");
   return NEMO_OK;
 }
@@ -1777,7 +1778,9 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
   select_p2(c);
   if (nam->ln_eos80 && nam->ln_seos) return bad(NEMO_ERR_ARG);  // eos_init: exactly one equation of state
   if (nam->ln_eos80 && upload_eos80(c)) return bad(NEMO_ERR_NOMEM);
-  c->ctl_nblk = 2 * c->nsm;
+  // stp_ctl: one column a thread (at most 2048 blocks of DG_THREADS, then a grid stride)
+  c->ctl_nblk = (int)std::min<long>(2048, (c->n2 + DG_THREADS - 1) / DG_THREADS);
+  c->hsb_nblk = 2 * c->nsm;
   if (cudaMalloc(&c->ctl_part, (size_t)c->ctl_nblk * c->nmem * CTL_REC * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&c->ctl_out, (size_t)c->nmem * CTL_OUT * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&c->ctl_idx, (size_t)c->nmem * 4 * sizeof(unsigned long long)) != cudaSuccess ||
@@ -2317,7 +2320,7 @@ int nemo_gpu_dia_hsb_init(nemo_ctx* c) {
   if (!c->hsb_mem) {
     const size_t words = 2 * n2 + 3 * nm * n2 + 3 * nm * n3;
     if (cudaMalloc(&c->hsb_mem, words * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&c->hsb_part, (size_t)c->ctl_nblk * nm * HSB_NS * 2 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&c->hsb_part, (size_t)c->hsb_nblk * nm * HSB_NS * 2 * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&c->hsb_state, nm * 8 * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&c->hsb_out, nm * NEMO_HSB_N * sizeof(double)) != cudaSuccess)
       return fail(c, NEMO_ERR_NOMEM, "dia_hsb work arrays");

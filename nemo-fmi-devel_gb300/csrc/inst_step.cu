@@ -157,7 +157,7 @@ cudaError_t launch_stp_ctl(const Dom<T>& d, const T* sshn, const T* un, const T*
                            int someoce, double* out, unsigned long long* idx, int* flag, cudaStream_t s) {
   k_ctl_partial<T><<<dim3(nblk, d.nmem), DG_THREADS, 0, s>>>(d, sshn, un, ts, part);
   ktick(NEMO_K_STP_CTL, s);
-  k_ctl_final<T><<<(d.nmem + 31) / 32, 32, 0, s>>>(d, part, nblk, someoce, out, idx, flag);
+  k_ctl_final<T><<<d.nmem, DG_THREADS, 0, s>>>(d, part, nblk, someoce, out, idx, flag);
   ktick(NEMO_K_STP_CTL, s);
   k_ctl_locate<T><<<dim3(nblk, d.nmem), DG_THREADS, 0, s>>>(d, sshn, un, ts, out, idx);
   ktick(NEMO_K_STP_CTL, s);

@@ -52,12 +52,14 @@ __global__ void __launch_bounds__(DG_THREADS) k_ctl_partial(Dom<T> d, const T* _
     const T s = fabs(s2[p]);
     v[0] = fmax(v[0], s);
     nan |= s != s ? 1 : 0;
+#pragma unroll 4
     for (int k = 1; k <= d.jpk; ++k) {
       const T x = fabs(u3[p + (long)(k - 1) * n2]);
       v[1] = fmax(v[1], x);
       nan |= x != x ? 2 : 0;
     }
     const ColInfo c = d.ci[p];
+#pragma unroll 4
     for (int k = c.tlo; k <= c.thi; ++k) {
       const long q = p + (long)(k - 1) * n2;
       const T tv = t3[q], sv = t3[q + n3];
@@ -90,28 +92,43 @@ __global__ void __launch_bounds__(DG_THREADS) k_ctl_partial(Dom<T> d, const T* _
   }
 }
 
-// One thread per member: the member's record, the blow-up test (:149-157), its
-// results out[m * CTL_OUT ..] = zmax(1:6), kindic; when it fires the locate request,
-// the keys of the extremes, idx = the largest index (to be lowered by k_ctl_locate),
-// and flag = 1.
+// One block (DG_THREADS) per member: the member's records merged, the blow-up test
+// (:149-157), its results out[m * CTL_OUT ..] = zmax(1:6), kindic; when it fires the
+// locate request, the keys of the extremes, idx = the largest index (to be lowered
+// by k_ctl_locate), and flag = 1.
 template <class T>
-__global__ void k_ctl_final(Dom<T> d, const double* part, int nblk, int someoce, double* out,
-                            unsigned long long* idx, int* flag) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= d.nmem) return;
+__global__ void __launch_bounds__(DG_THREADS) k_ctl_final(Dom<T> d, const double* part, int nblk, int someoce,
+                                                          double* out, unsigned long long* idx, int* flag) {
+  const int m = blockIdx.x;
   double z[6];
   for (int t = 0; t < 6; ++t) z[t] = -1.7976931348623157e308;
-  int nan[3] = {0, 0, 0};
-  for (int b = 0; b < nblk; ++b) {
+  int nan = 0;
+  for (int b = threadIdx.x; b < nblk; b += DG_THREADS) {
     const double* r = part + ((long)m * nblk + b) * CTL_REC;
     for (int t = 0; t < 6; ++t) z[t] = fmax(z[t], r[t]);
-    for (int t = 0; t < 3; ++t) nan[t] |= r[6 + t] != 0.0;
+    for (int t = 0; t < 3; ++t) nan |= r[6 + t] != 0.0 ? 1 << t : 0;
   }
-  double key[4] = {nan[0] ? INFINITY : z[0], nan[1] ? INFINITY : z[1], nan[2] ? -INFINITY : -z[2],
-                   nan[2] ? INFINITY : z[3]};
-  if (nan[0]) z[0] = NAN;
-  if (nan[1]) z[1] = NAN;
-  if (nan[2]) { z[2] = NAN; z[3] = NAN; }
+  for (int off = 16; off > 0; off >>= 1) {
+    for (int t = 0; t < 6; ++t) z[t] = fmax(z[t], __shfl_down_sync(0xffffffffu, z[t], off));
+    nan |= __shfl_down_sync(0xffffffffu, nan, off);
+  }
+  __shared__ double s_z[DG_THREADS / 32][6];
+  __shared__ int s_nan[DG_THREADS / 32];
+  if ((threadIdx.x & 31) == 0) {
+    for (int t = 0; t < 6; ++t) s_z[threadIdx.x >> 5][t] = z[t];
+    s_nan[threadIdx.x >> 5] = nan;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  for (int w = 1; w < DG_THREADS / 32; ++w) {
+    for (int t = 0; t < 6; ++t) z[t] = fmax(z[t], s_z[w][t]);
+    nan |= s_nan[w];
+  }
+  const bool n0 = nan & 1, n1 = (nan >> 1) & 1, n2s = (nan >> 2) & 1;
+  double key[4] = {n0 ? INFINITY : z[0], n1 ? INFINITY : z[1], n2s ? -INFINITY : -z[2], n2s ? INFINITY : z[3]};
+  if (n0) z[0] = NAN;
+  if (n1) z[1] = NAN;
+  if (n2s) { z[2] = NAN; z[3] = NAN; }
   const bool trip = someoce && (z[0] > 20.0 || z[1] > 10.0 || z[2] >= 0.0 || z[3] >= 100.0 || z[3] < 0.0 ||
                                 isnan(z[0] + z[1] + z[2]));
   double* o = out + (long)m * CTL_OUT;

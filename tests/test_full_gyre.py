@@ -110,3 +110,32 @@ def test_gpu_full_step_mixed():
     for n in ("UN", "VN"):
         p.compare(n, p.s3, 5e-3)
     p.compare("SSHN", p.s2, 5e-3)
+
+
+@pytest.mark.gpu
+def test_gpu_full_step_ten_days_fp64():
+    """Ten model days (120 steps) of the full GYRE step on GYRE nn_GYRE=1 in FP64
+    against the oracle: every field within 1e-12 (bit-identical when the arithmetic
+    matches), run control quiet."""
+    pytest.importorskip("torch")
+    import torch
+    dom = gyre.domain(1)
+    base = gyre.namelist(neuler=0)
+    nam, st = gyre.full_physics(dom, base, gyre.state(dom, base, seed=61))
+    p = Pair(dom=dom, nam=nam, prec="fp64", states=[st])
+    p.bind_hotpath()
+    for n in gyre.FULL_3D + gyre.FULL_2D:
+        p.bind(n.upper())
+    nm = np.zeros(p.s2, dtype=np.int32, order="F")
+    p.ora[0].bind("NMLN", nm)
+    p.ctx.bind("NMLN", torch.zeros(nm.size, dtype=torch.int32, device="cuda"))
+    for kt in range(1, 121):
+        p.ora[0].stp_model(kt)
+        p.ctx.stp_model(kt)
+    p.ctx.synchronize()
+    p.compare("TSN", p.s4, 1e-12)
+    for n in ("UN", "VN", "WN", "AVT", "EN"):
+        p.compare(n, p.s3, 1e-12)
+    for n in ("SSHN", "QNS", "EMP", "TAUM"):
+        p.compare(n, p.s2, 1e-12)
+    assert p.ctx.stp_ctl_result()[2][0] == 0
