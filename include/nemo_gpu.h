@@ -232,6 +232,9 @@ enum nemo_field_id {
   /* latitudes of the T-, U- and V-points (dom_oce gphit, gphiu, gphiv) [degrees], read
    * by GYRE's analytic surface forcing (nemo_gpu_usrdef_sbc) */
   NEMO_F_GPHIT, NEMO_F_GPHIU, NEMO_F_GPHIV, /* [S]                                    */
+  /* the horizontal gradients of the in situ density at the last ocean level of u- and
+   * v-points (oce.F90 gru, grv; zps_hde with partial steps), read by ldf_slp */
+  NEMO_F_GRU, NEMO_F_GRV,              /* [S]                                         */
   NEMO_F_COUNT
 };
 
@@ -409,6 +412,15 @@ int nemo_gpu_usrdef_sbc(nemo_ctx *ctx, int kt);
  * eos and is not implemented. */
 int nemo_gpu_zps_hde(nemo_ctx *ctx, int kt, int kjpt, const void *pta, void *pgtu, void *pgtv);
 
+/* zps_hde's density part (zpshde.F90:150-184, the reference's optional arguments prd,
+ * pgru, pgrv): pts (jpi,jpj,jpk,2) are T and S; each is interpolated to the shallower
+ * bottom depth of the u- (v-) point as the tracer part does, its in situ density there
+ * formed by eos_insitu_2d (eosbn2.F90:295-398, EOS-80 or the simplified eos) at
+ * gdept_n of the shallower bottom cell, and pgru, pgrv (jpi,jpj) = its difference with
+ * prd (jpi,jpj,jpk) on the deeper side, masked, edges 0. Bound: GDEPT_N. Bind the
+ * results as NEMO_F_GRU, NEMO_F_GRV for nemo_gpu_ldf_slp with partial steps. */
+int nemo_gpu_zps_hde_rd(nemo_ctx *ctx, int kt, const void *pts, const void *prd, void *pgru, void *pgrv);
+
 /* tra_ldf_blp (traldf_lap_blp.F90:161-231): the bilaplacian as two passes of the
  * laplacian, kldf = 20 (np_blp: iso-level, tra_ldf_lap) or 21 (np_blp_i: rotated,
  * tra_ldf_iso), with lbc_lnk of the first laplacian and, with ln_zps, its zps_hde
@@ -447,9 +459,9 @@ int nemo_gpu_wzv(nemo_ctx *ctx, int kt);
  * uslp, vslp, wslpi, wslpj (the bound NEMO_F_USLP, ... fields, levels 2..jpk-1;
  * levels 1 and jpk are left as they are except on the closed edges) from the in
  * situ density anomaly prd and N^2 pn2 (3-D device arrays), the bound depths and
- * mixed layer. z-coordinate without ice-shelf cavities and without partial steps
- * (the zps bottom density gradients are not an input here): NEMO_ERR_UNSUPPORTED
- * otherwise. */
+ * mixed layer. z-coordinate (z* with the now e3 and depths bound) without ice-shelf
+ * cavities; with partial steps (ln_zps) the bottom level's density gradients are the
+ * bound NEMO_F_GRU, NEMO_F_GRV of zps_hde (ldfslp.F90:144-151). */
 int nemo_gpu_ldf_slp(nemo_ctx *ctx, int kt, const void *prd, const void *pn2);
 
 /* dyn_zdf (dynzdf.F90:47-499). Its leap-frog time step ua = (ub + r2dt ua) umask, va

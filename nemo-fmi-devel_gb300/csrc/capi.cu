@@ -982,6 +982,7 @@ int run_ldf_slp(nemo_ctx* c, const void* prd, const void* pn2) {
   a.hmlp = (const T*)c->f[NEMO_F_HMLP]; a.hmlpt = (const T*)c->f[NEMO_F_HMLPT];
   a.uslp = (T*)c->f[NEMO_F_USLP]; a.vslp = (T*)c->f[NEMO_F_VSLP];
   a.wslpi = (T*)c->f[NEMO_F_WSLPI]; a.wslpj = (T*)c->f[NEMO_F_WSLPJ];
+  if (nm.ln_zps) { a.gru_b = (const T*)c->f[NEMO_F_GRU]; a.grv_b = (const T*)c->f[NEMO_F_GRV]; }
   a.zu = w; a.zv = w + n3; a.zwi = w + 2 * n3; a.zwj = w + 3 * n3;
   T* w2 = w + 4 * n3;
   a.uml = w2; a.vml = w2 + n2; a.wiml = w2 + 2 * n2; a.wjml = w2 + 3 * n2; a.hu = w2 + 4 * n2; a.hv = w2 + 5 * n2;
@@ -2041,6 +2042,28 @@ int nemo_gpu_zps_hde(nemo_ctx* c, int kt, int kjpt, const void* pta, void* pgtu,
   return NEMO_OK;
 }
 
+int nemo_gpu_zps_hde_rd(nemo_ctx* c, int kt, const void* pts, const void* prd, void* pgru, void* pgrv) {
+  (void)kt;
+  if (!c) return NEMO_ERR_ARG;
+  if (!pts || !prd || !pgru || !pgrv) return fail(c, NEMO_ERR_ARG, "zps_hde_rd: null array");
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (!c->nam.ln_seos && !c->nam.ln_eos80)
+    return fail(c, NEMO_ERR_UNSUPPORTED, "zps_hde_rd: needs an equation of state (ln_seos or ln_eos80)");
+  if (!c->f[NEMO_F_GDEPT_N]) return fail(c, NEMO_ERR_UNBOUND, "zps_hde_rd: gdept_n must be bound");
+  cudaError_t e;
+  if (c->prec == NEMO_PREC_FP64) {
+    EosArgs<double> a = eos_args<double>(c, 0);
+    a.pts = (const double*)pts;
+    e = launch_zps_hde_rd<double>(dom_now<double>(c), a, (const double*)prd, (double*)pgru, (double*)pgrv, c->stream);
+  } else {
+    EosArgs<float> a = eos_args<float>(c, 0);
+    a.pts = (const float*)pts;
+    e = launch_zps_hde_rd<float>(dom_now<float>(c), a, (const float*)prd, (float*)pgru, (float*)pgrv, c->stream);
+  }
+  if (e != cudaSuccess) return cuda_fail(c, e, "zps_hde_rd launch");
+  return NEMO_OK;
+}
+
 int nemo_gpu_tra_zdf_imp(nemo_ctx* c, int kt, int kit000, const char* cdtype, double p2dt, const void* ptb, void* pta,
                          int kjpt) {
   (void)kt; (void)kit000;
@@ -2093,8 +2116,10 @@ int nemo_gpu_ldf_slp(nemo_ctx* c, int kt, const void* prd, const void* pn2) {
                  NEMO_F_HMLP, NEMO_F_HMLPT})
     if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "ldf_slp: field %d must be bound", id);
   const nemo_namelist& nm = c->nam;
-  if (nm.ln_zps || nm.ln_isfcav || nm.ln_sco)
-    return fail(c, NEMO_ERR_UNSUPPORTED, "ldf_slp: z-coordinate without partial steps or cavities only");
+  if (nm.ln_isfcav || nm.ln_sco)
+    return fail(c, NEMO_ERR_UNSUPPORTED, "ldf_slp: z-coordinate without cavities only");
+  if (nm.ln_zps && (!c->f[NEMO_F_GRU] || !c->f[NEMO_F_GRV]))
+    return fail(c, NEMO_ERR_UNBOUND, "ldf_slp with partial steps: gru and grv (zps_hde) must be bound");
   return c->prec == NEMO_PREC_FP64 ? run_ldf_slp<double>(c, prd, pn2) : run_ldf_slp<float>(c, prd, pn2);
 }
 

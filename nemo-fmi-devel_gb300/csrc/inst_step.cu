@@ -49,6 +49,13 @@ cudaError_t launch_ldf_slp(const Dom<T>& d, const SlpArgs<T>& a, cudaStream_t s)
 }
 
 template <class T>
+cudaError_t launch_zps_hde_rd(const Dom<T>& d, const EosArgs<T>& a, const T* prd, T* pgru, T* pgrv, cudaStream_t s) {
+  k_zps_hde_rd<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a, prd, pgru, pgrv);
+  ktick(NEMO_K_ZPS_HDE, s);
+  return cudaGetLastError();
+}
+
+template <class T>
 cudaError_t launch_zps_hde(const Dom<T>& d, const T* pta, T* pgtu, T* pgtv, int kjpt, cudaStream_t s) {
   k_zps_hde<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, pta, pgtu, pgtv, kjpt);
   ktick(NEMO_K_ZPS_HDE, s);
@@ -188,6 +195,7 @@ cudaError_t launch_dia_hsb(const Dom<T>& d, const HsbArgs<T>& a, double* part, i
   template cudaError_t launch_dyn_nxt<T>(const Dom<T>&, const NxtArgs<T, double>&, cudaStream_t);              \
   template cudaError_t launch_ssh_swp<T>(const Dom<T>&, T*, T*, const double*, T, int, cudaStream_t);      \
   template cudaError_t launch_ldf_slp<T>(const Dom<T>&, const SlpArgs<T>&, cudaStream_t);                  \
+  template cudaError_t launch_zps_hde_rd<T>(const Dom<T>&, const EosArgs<T>&, const T*, T*, T*, cudaStream_t);  \
   template cudaError_t launch_zps_hde<T>(const Dom<T>&, const T*, T*, T*, int, cudaStream_t);             \
   template cudaError_t launch_tra_sbc<T>(const Dom<T>&, const SbcArgs<T>&, cudaStream_t);                  \
   template cudaError_t launch_tra_qsr<T>(const Dom<T>&, const QsrArgs<T>&, cudaStream_t);                  \

@@ -255,8 +255,15 @@ struct SlpPt {
   __device__ __forceinline__ T tm(int i, int j, int k) const { return tmsk<T>(d.ci[Q(i, j, 1)], k); }
   __device__ __forceinline__ T wm(int i, int j, int k) const { return wmsk<T>(d.ci[Q(i, j, 1)], k); }
   __device__ __forceinline__ T prd(int i, int j, int k) const { return a.prd[m3 + Q(i, j, k)]; }
-  __device__ __forceinline__ T gru(int i, int j, int k) const { return um(i, j, k) * (prd(i + 1, j, k) - prd(i, j, k)); }
-  __device__ __forceinline__ T grv(int i, int j, int k) const { return vm(i, j, k) * (prd(i, j + 1, k) - prd(i, j, k)); }
+  // with partial steps the bottom level's gradients are zps_hde's (ldfslp.F90:144-151)
+  __device__ __forceinline__ T gru(int i, int j, int k) const {
+    if (a.gru_b && k == d.ci[Q(i, j, 1)].mbku) return a.gru_b[(long)m * d.n2 + Q(i, j, 1)];
+    return um(i, j, k) * (prd(i + 1, j, k) - prd(i, j, k));
+  }
+  __device__ __forceinline__ T grv(int i, int j, int k) const {
+    if (a.grv_b && k == d.ci[Q(i, j, 1)].mbkv) return a.grv_b[(long)m * d.n2 + Q(i, j, 1)];
+    return vm(i, j, k) * (prd(i, j + 1, k) - prd(i, j, k));
+  }
   __device__ __forceinline__ T dzr(int i, int j, int k) const {
     if (k == 1) return T(0);
     const long q = m3 + Q(i, j, k);
@@ -450,6 +457,60 @@ __global__ void k_zps_hde(Dom<T> d, RO<T> pta, T* __restrict__ pgtu, T* __restri
     pgtu[g] = gu;
     pgtv[g] = gv;
   }
+}
+
+// The unmasked in situ density anomaly of one (T, S, depth), eos_insitu_2d
+// (eosbn2.F90:295-398): EOS-80 or the simplified equation of state
+template <class T>
+__device__ __forceinline__ T eos_rd_2d(const EosArgs<T>& a, T t, T sal, T dep);
+
+// zps_hde's density part (zpshde.F90:150-184), one (i,j) a thread: T and S
+// interpolated to the shallower bottom depth of the u- (v-) point as k_zps_hde does,
+// their density there (eos_insitu_2d at gdept_n of the shallower bottom cell), its
+// difference with prd on the deeper side; the closed edges 0 (lbc_lnk)
+template <class T>
+__global__ void k_zps_hde_rd(Dom<T> d, EosArgs<T> a, RO<T> prd, T* __restrict__ pgru, T* __restrict__ pgrv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i > d.jpi || j > d.jpj) return;
+  const int m = blockIdx.z, jpi = d.jpi;
+  const long ij = (long)(i - 1) + (long)(j - 1) * jpi, n2 = d.n2, n3 = d.n3;
+  const long g = (long)m * n2 + ij;
+  if (!(i >= 2 && i <= jpi - 1 && j >= 2 && j <= d.jpj - 1)) {
+    pgru[g] = T(0);
+    pgrv[g] = T(0);
+    return;
+  }
+  const ColInfo ci = d.ci[ij];
+  const int iku = ci.mbku, ikum1 = iku - 1 > 1 ? iku - 1 : 1;
+  const int ikv = ci.mbkv, ikvm1 = ikv - 1 > 1 ? ikv - 1 : 1;
+  auto Q = [&](long o, int k) { return o + (long)(k - 1) * n2; };
+  const T ze3wu = d.e3w_n(ij + 1, iku, m) - d.e3w_n(ij, iku, m);
+  const T ze3wv = d.e3w_n(ij + jpi, ikv, m) - d.e3w_n(ij, ikv, m);
+  T zti[2], ztj[2];
+  for (int n = 0; n < 2; ++n) {
+    const RO<T> t = a.pts + ((long)m * 2 + n) * n3;
+    if (ze3wu >= T(0)) {
+      const T zmaxu = ze3wu / d.e3w_n(ij + 1, iku, m);
+      zti[n] = t[Q(ij + 1, iku)] + zmaxu * (t[Q(ij + 1, ikum1)] - t[Q(ij + 1, iku)]);
+    } else {
+      const T zmaxu = -ze3wu / d.e3w_n(ij, iku, m);
+      zti[n] = t[Q(ij, iku)] + zmaxu * (t[Q(ij, ikum1)] - t[Q(ij, iku)]);
+    }
+    if (ze3wv >= T(0)) {
+      const T zmaxv = ze3wv / d.e3w_n(ij + jpi, ikv, m);
+      ztj[n] = t[Q(ij + jpi, ikv)] + zmaxv * (t[Q(ij + jpi, ikvm1)] - t[Q(ij + jpi, ikv)]);
+    } else {
+      const T zmaxv = -ze3wv / d.e3w_n(ij, ikv, m);
+      ztj[n] = t[Q(ij, ikv)] + zmaxv * (t[Q(ij, ikvm1)] - t[Q(ij, ikv)]);
+    }
+  }
+  const long m3 = (long)m * n3;
+  const T zhi = ze3wu >= T(0) ? a.gdept[m3 + Q(ij, iku)] : a.gdept[m3 + Q(ij + 1, iku)];
+  const T zhj = ze3wv >= T(0) ? a.gdept[m3 + Q(ij, ikv)] : a.gdept[m3 + Q(ij + jpi, ikv)];
+  const T zri = eos_rd_2d(a, zti[0], zti[1], zhi), zrj = eos_rd_2d(a, ztj[0], ztj[1], zhj);
+  const T um1 = umsk<T>(ci, 1), vm1 = vmsk<T>(ci, 1);
+  pgru[g] = ze3wu >= T(0) ? um1 * (zri - prd[m3 + Q(ij, iku)]) : um1 * (prd[m3 + Q(ij + 1, iku)] - zri);
+  pgrv[g] = ze3wv >= T(0) ? vm1 * (zrj - prd[m3 + Q(ij, ikv)]) : vm1 * (prd[m3 + Q(ij + jpi, ikv)] - zrj);
 }
 
 // ------------------------------------------------------------ surface forcing
@@ -647,6 +708,29 @@ __device__ __forceinline__ void eos80_point(const EosArgs<T>& a, long q, long qt
       a.prd[q] = ((zn + a.e80_anom) * a.r1_rau0) * ztm;
     }
   }
+}
+
+template <class T>
+__device__ __forceinline__ T eos_rd_2d(const EosArgs<T>& a, T t, T sal, T dep) {
+  if (a.eos80) {
+    constexpr double r1_Z0 = 1.e-4, r1_T0 = 1.0 / 40.0, r1_S0 = 1.0 / 40.0, rdeltaS = 20.0;
+    if constexpr (sizeof(T) == 8) {
+      const double zh = dep * r1_Z0, zt = t * r1_T0, zs = sqrt(fabs(sal + rdeltaS) * r1_S0);
+      double zn0;
+      return e80_poly<6, 4, 2, 1>(a.e80_raw, zt, zs, zh, zn0) * a.r1_rau0 - 1.0;
+    } else {
+      const float zh = dep * (float)r1_Z0, zt = t * (float)r1_T0;
+      const float x = fabsf(sal + (float)rdeltaS) * (float)r1_S0;
+      const float zs = sqrtf(x);
+      const float sp = (x - a.e80_s0 * a.e80_s0) / (zs + a.e80_s0);
+      float zn0;
+      return (e80_poly32<6, 4, 2, 1>(a.e80_tay, zt, sp, zh, true, zn0) + a.e80_anom) * a.r1_rau0;
+    }
+  }
+  const T zt = t - T(10), zs = sal - T(35);
+  const T zn = -a.a0 * (T(1) + T(0.5) * a.lambda1 * zt + a.mu1 * dep) * zt +
+               a.b0 * (T(1) - T(0.5) * a.lambda2 * zs - a.mu2 * dep) * zs - a.nu * zt * zs;
+  return zn * a.r1_rau0;
 }
 
 template <class T>

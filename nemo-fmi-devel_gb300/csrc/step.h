@@ -21,6 +21,7 @@ struct SlpArgs {
   const T *gdept, *gdepw;              // depths of the now T-, W-points (3-D)
   const int* nmln;                     // mixed-layer level (2-D, int)
   const T *hmlp, *hmlpt;               // mixed-layer depth, depth of its last T-point
+  const T *gru_b, *grv_b;              // partial steps: zps_hde's bottom gradients (2-D), else null
   T *uslp, *vslp, *wslpi, *wslpj;      // out
   T *uml, *vml, *wiml, *wjml, *hu, *hv;  // work (2-D): slopes below the mixed layer
   T *zu, *zv, *zwi, *zwj;              // work (3-D): slopes before the filter
@@ -141,6 +142,8 @@ template <class T>
 cudaError_t launch_tra_sbc(const Dom<T>& d, const SbcArgs<T>& a, cudaStream_t s);
 template <class T>
 cudaError_t launch_tra_qsr(const Dom<T>& d, const QsrArgs<T>& a, cudaStream_t s);
+template <class T>
+cudaError_t launch_zps_hde_rd(const Dom<T>& d, const EosArgs<T>& a, const T* prd, T* pgru, T* pgrv, cudaStream_t s);
 template <class T>
 cudaError_t launch_zps_hde(const Dom<T>& d, const T* pta, T* pgtu, T* pgtv, int kjpt, cudaStream_t s);
 template <class T>

@@ -144,6 +144,7 @@ def load(path):
     _proto(lib, "nemo_gpu_eos_insitu_pot", i, [vp, vp, vp, vp, vp])
     _proto(lib, "nemo_gpu_rab_3d", i, [vp, vp, vp])
     _proto(lib, "nemo_gpu_bn2", i, [vp, vp, vp, vp])
+    _proto(lib, "nemo_gpu_zps_hde_rd", i, [vp, i, vp, vp, vp, vp])
     _proto(lib, "nemo_gpu_dyn_ldf_lap", i, [vp, i, vp, vp, vp, vp, i])
     _proto(lib, "nemo_gpu_vor_ene", i, [vp, i, i, vp, vp, vp, vp])
     _proto(lib, "nemo_gpu_dyn_keg", i, [vp, i, i])

@@ -227,6 +227,11 @@ class Context:
     def zps_hde(self, kt, kjpt, pta, pgtu, pgtv):
         self._ck(self.lib.nemo_gpu_zps_hde(self.h, kt, kjpt, _ptr(pta), _ptr(pgtu), _ptr(pgtv)), "zps_hde")
 
+    def zps_hde_rd(self, kt, pts, prd, pgru, pgrv):
+        """zps_hde's density part: the bottom density gradients pgru, pgrv"""
+        self._ck(self.lib.nemo_gpu_zps_hde_rd(self.h, kt, _ptr(pts), _ptr(prd), _ptr(pgru), _ptr(pgrv)),
+                 "zps_hde_rd")
+
     def tra_zdf_imp(self, kt, kit000, cdtype, p2dt, ptb, pta, kjpt):
         self._ck(self.lib.nemo_gpu_tra_zdf_imp(self.h, kt, kit000, cdtype.encode(), p2dt, _ptr(ptb), _ptr(pta), kjpt),
                  "tra_zdf_imp")

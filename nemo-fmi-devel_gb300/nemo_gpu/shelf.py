@@ -146,3 +146,17 @@ def state(dom, nam, seed=0, member=0):
     st["ssh_ib"] = np.asfortranarray(0.02 * np.sin(2 * math.pi * (x + 0.3 * np.arange(jpj)[None, :] / jpj)))
     st["ssh_ibb"] = np.asfortranarray(0.9 * st["ssh_ib"])
     return st
+
+
+def depths(st):
+    """The now depths of a state's z* levels (domvvl.F90:641-652, no cavities): gdepw_n = 0 at the
+    surface and the running sum of e3t_n below; gdept_n = e3w_n / 2 at the surface and
+    the running sum of e3w_n below."""
+    e3t, e3w = st["e3t_n"], st["e3w_n"]
+    gdepw = np.zeros_like(e3t)
+    gdept = np.zeros_like(e3t)
+    gdept[:, :, 0] = 0.5 * e3w[:, :, 0]
+    for k in range(1, e3t.shape[2]):
+        gdepw[:, :, k] = gdepw[:, :, k - 1] + e3t[:, :, k - 1]
+        gdept[:, :, k] = gdept[:, :, k - 1] + e3w[:, :, k]
+    return dict(gdept_n=np.asfortranarray(gdept), gdepw_n=np.asfortranarray(gdepw))

@@ -2288,8 +2288,7 @@ int ora_dia_hsb_last(const ora_ctx *c, double *out) {
  * + FCT), tra_ldf (iso or lap), tra_zdf. FCT orders from nn_fct_h/v (0 = 2). */
 /* zps_hde (zpshde.F90:41-148): the horizontal gradients of the tracers at the last
  * (partial-step) ocean level of u- and v-points, each tracer interpolated to the
- * shallower of the two bottom depths; lbc_lnk. The density part needs eos and is not
- * restated. */
+ * shallower of the two bottom depths; lbc_lnk. The density part is ora_zps_hde_rd. */
 int ora_zps_hde(ora_ctx *c, int kt, int kjpt, const double *pta, double *pgtu, double *pgtv) {
   (void)kt;
   const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
@@ -2329,6 +2328,64 @@ int ora_zps_hde(ora_ctx *c, int kt, int kjpt, const double *pta, double *pgtu, d
   }
   lbc_closed(jpi, jpj, pgtu, kjpt, 'U', 0.0);
   lbc_closed(jpi, jpj, pgtv, kjpt, 'V', 0.0);
+  return NEMO_OK;
+}
+
+/* eos_insitu_2d (eosbn2.F90:295-398): the unmasked in situ density anomaly of one
+ * (T, S, depth) with EOS-80 or the simplified equation of state */
+static double eos_rd_2d(const ora_ctx *c, double t, double sal, double dep);
+
+/* zps_hde's density part (zpshde.F90:150-184): T and S interpolated to the shallower
+ * bottom depth of each u- (v-) point as the tracer part does, their density at that
+ * depth (gdept_n of the shallower bottom cell) by eos_insitu_2d, its difference with
+ * the bound prd of the deeper side; the closed lbc_lnk. pts: T and S (jpi,jpj,jpk,2),
+ * out: pgru, pgrv (jpi,jpj). Bound: GDEPT_N. */
+int ora_zps_hde_rd(ora_ctx *c, int kt, const double *pts, const double *prd, double *pgru, double *pgrv) {
+  (void)kt;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  const double *e3w = fld(c, NEMO_F_E3W_N), *gdept = c->f[NEMO_F_GDEPT_N], *umask = c->umask, *vmask = c->vmask;
+  if (!pts || !prd || !pgru || !pgrv) return NEMO_ERR_ARG;
+  if (!gdept) return NEMO_ERR_UNBOUND;
+  if (!c->nam.ln_seos && !c->nam.ln_eos80) return NEMO_ERR_UNSUPPORTED;
+  memset(pgru, 0, n2 * sizeof(double));
+  memset(pgrv, 0, n2 * sizeof(double));
+  for (int jj = 1; jj <= jpj - 1; ++jj)
+    for (int ji = 1; ji <= jpi - 1; ++ji) {
+      const size_t p = I2(ji, jj);
+      const int iku = c->mbku[p], ikum1 = iku - 1 > 1 ? iku - 1 : 1;
+      const int ikv = c->mbkv[p], ikvm1 = ikv - 1 > 1 ? ikv - 1 : 1;
+      const double ze3wu = e3w[I3(ji + 1, jj, iku)] - e3w[I3(ji, jj, iku)];
+      const double ze3wv = e3w[I3(ji, jj + 1, ikv)] - e3w[I3(ji, jj, ikv)];
+      double zti[2], ztj[2];
+      for (int jn = 0; jn < 2; ++jn) {  /* the tracer part's interpolation (:108-140) */
+        const double *t = pts + n3 * jn;
+        if (ze3wu >= 0.0) {
+          const double zmaxu = ze3wu / e3w[I3(ji + 1, jj, iku)];
+          zti[jn] = t[I3(ji + 1, jj, iku)] + zmaxu * (t[I3(ji + 1, jj, ikum1)] - t[I3(ji + 1, jj, iku)]);
+        } else {
+          const double zmaxu = -ze3wu / e3w[I3(ji, jj, iku)];
+          zti[jn] = t[I3(ji, jj, iku)] + zmaxu * (t[I3(ji, jj, ikum1)] - t[I3(ji, jj, iku)]);
+        }
+        if (ze3wv >= 0.0) {
+          const double zmaxv = ze3wv / e3w[I3(ji, jj + 1, ikv)];
+          ztj[jn] = t[I3(ji, jj + 1, ikv)] + zmaxv * (t[I3(ji, jj + 1, ikvm1)] - t[I3(ji, jj + 1, ikv)]);
+        } else {
+          const double zmaxv = -ze3wv / e3w[I3(ji, jj, ikv)];
+          ztj[jn] = t[I3(ji, jj, ikv)] + zmaxv * (t[I3(ji, jj, ikvm1)] - t[I3(ji, jj, ikv)]);
+        }
+      }
+      const double zhi = ze3wu >= 0.0 ? gdept[I3(ji, jj, iku)] : gdept[I3(ji + 1, jj, iku)];
+      const double zhj = ze3wv >= 0.0 ? gdept[I3(ji, jj, ikv)] : gdept[I3(ji, jj + 1, ikv)];
+      /* eos of the interpolated tracers; its lbc_lnk zeroes the edge values, which
+         only the edge gradients read and the final lbc_lnk zeroes too */
+      const double zri = (ji == 1 || jj == 1) ? 0.0 : eos_rd_2d(c, zti[0], zti[1], zhi);
+      const double zrj = (ji == 1 || jj == 1) ? 0.0 : eos_rd_2d(c, ztj[0], ztj[1], zhj);
+      pgru[p] = ze3wu >= 0.0 ? umask[p] * (zri - prd[I3(ji, jj, iku)]) : umask[p] * (prd[I3(ji + 1, jj, iku)] - zri);
+      pgrv[p] = ze3wv >= 0.0 ? vmask[p] * (zrj - prd[I3(ji, jj, ikv)]) : vmask[p] * (prd[I3(ji, jj + 1, ikv)] - zrj);
+    }
+  lbc_closed(jpi, jpj, pgru, 1, 'U', 0.0);
+  lbc_closed(jpi, jpj, pgrv, 1, 'V', 0.0);
   return NEMO_OK;
 }
 
@@ -3402,6 +3459,21 @@ static void eos80_vars(double t, double s, double dep, double *zt, double *zs, d
   *zs = sqrt(fabs(s + NEMO_EOS80_RDELTAS) * NEMO_EOS80_R1_S0);
 }
 
+static double eos_rd_2d(const ora_ctx *c, double t, double sal, double dep) {
+  const nemo_namelist *nm = &c->nam;
+  const double r1_rau0 = 1.0 / nm->rau0;
+  if (nm->ln_eos80) {  /* eosbn2.F90:318-347 */
+    double zt, zs, zh;
+    eos80_vars(t, sal, dep, &zt, &zs, &zh);
+    return eos80_poly(0, zt, zs, zh, NULL) * r1_rau0 - 1.0;
+  }
+  const double zt = t - 10., zs = sal - 35., zh = dep;  /* :366-376 */
+  const double zn = -nm->rn_a0 * (1. + 0.5 * nm->rn_lambda1 * zt + nm->rn_mu1 * zh) * zt
+                    + nm->rn_b0 * (1. - 0.5 * nm->rn_lambda2 * zs - nm->rn_mu2 * zh) * zs
+                    - nm->rn_nu * zt * zs;
+  return zn * r1_rau0;
+}
+
 int ora_eos_insitu(ora_ctx *c, const double *pts, double *prd, const double *pdep) {
   const nemo_namelist *nm = &c->nam;
   if (nm->ln_eos80) {  /* eosbn2.F90:236-270 */
@@ -3642,10 +3714,11 @@ int ora_stp_model(ora_ctx *c, int kt) {
 
 /* ---------------------------------------------------------------- ldf_slp */
 /* ldf_slp (ldfslp.F90:83-374) with ldf_slp_mxl (:620-729): z-coordinate without
- * ice-shelf cavities (risfdep = 0, mikt = miku = mikv = 1), without partial steps
- * and without the s-coordinate level slope. prd, pn2: in situ density anomaly and
- * N^2; bound: GDEPT_N, GDEPW_N, NMLN (int), HMLP, HMLPT; out: USLP, VSLP, WSLPI,
- * WSLPJ on levels 2..jpk-1 of the interior, then lbc_lnk on every level. */
+ * ice-shelf cavities (risfdep = 0, mikt = miku = mikv = 1) and without the
+ * s-coordinate level slope; with partial steps (ln_zps) the density gradients of the
+ * bottom level are the bound GRU, GRV of zps_hde (:144-151). prd, pn2: in situ density
+ * anomaly and N^2; bound: GDEPT_N, GDEPW_N, NMLN (int), HMLP, HMLPT; out: USLP, VSLP,
+ * WSLPI, WSLPJ on levels 2..jpk-1 of the interior, then lbc_lnk on every level. */
 int ora_ldf_slp(ora_ctx *c, int kt, const double *prd, const double *pn2) {
   (void)kt;
   const nemo_namelist *nm = &c->nam;
@@ -3657,7 +3730,9 @@ int ora_ldf_slp(ora_ctx *c, int kt, const double *prd, const double *pn2) {
   const int *nmln = (const int *)c->f[NEMO_F_NMLN];
   if (!prd || !pn2) return NEMO_ERR_ARG;
   if (!uslp || !vslp || !wslpi || !wslpj || !gdept || !gdepw || !hmlp || !hmlpt || !nmln) return NEMO_ERR_UNBOUND;
-  if (nm->ln_zps || nm->ln_isfcav || nm->ln_sco) return NEMO_ERR_UNSUPPORTED;
+  const double *gru = c->f[NEMO_F_GRU], *grv = c->f[NEMO_F_GRV];
+  if (nm->ln_isfcav || nm->ln_sco) return NEMO_ERR_UNSUPPORTED;
+  if (nm->ln_zps && (!gru || !grv)) return NEMO_ERR_UNBOUND;
   const double *tmask = c->tmask, *umask = c->umask, *vmask = c->vmask, *wmask = c->wmask;
   const double *e3u = fld(c, NEMO_F_E3U_N), *e3v = fld(c, NEMO_F_E3V_N), *e3w = fld(c, NEMO_F_E3W_N);
   const double zeps = 1.e-20, z1_16 = 1.0 / 16., zm1_g = -1.0 / nm->grav, zm1_2g = -0.5 / nm->grav;
@@ -3674,6 +3749,13 @@ int ora_ldf_slp(ora_ctx *c, int kt, const double *prd, const double *pn2) {
         size_t q = I3(ji, jj, jk);
         zgru[q] = umask[q] * (prd[I3(ji + 1, jj, jk)] - prd[q]);
         zgrv[q] = vmask[q] * (prd[I3(ji, jj + 1, jk)] - prd[q]);
+      }
+  if (nm->ln_zps)  /* the partial-step gradients at the bottom level (:144-151) */
+    for (int jj = 1; jj <= jpj - 1; ++jj)
+      for (int ji = 1; ji <= jpi - 1; ++ji) {
+        const size_t p = I2(ji, jj);
+        zgru[I3(ji, jj, c->mbku[p])] = gru[p];
+        zgrv[I3(ji, jj, c->mbkv[p])] = grv[p];
       }
   /* (:161-171) */
   for (size_t p = 0; p < n2; ++p) zdzr[p] = 0.0;

@@ -54,6 +54,7 @@ int ora_tra_ldf_iso(ora_ctx *c, int kt, int kit000, const char *cdtype,
                     const double *pahu, const double *pahv,
                     const double *pgu, const double *pgv, const double *pgui, const double *pgvi,
                     const double *ptb, const double *ptbb, double *pta, int kjpt, int kpass);
+int ora_zps_hde_rd(ora_ctx *c, int kt, const double *pts, const double *prd, double *pgru, double *pgrv);
 int ora_zps_hde(ora_ctx *c, int kt, int kjpt, const double *pta, double *pgtu, double *pgtv);
 int ora_tra_ldf_blp(ora_ctx *c, int kt, int kit000, const char *cdtype,
                     const double *pahu, const double *pahv,

@@ -79,6 +79,7 @@ def lib():
         P("ora_dyn_zad", [vp, i])
         P("ora_tra_ldf_blp", [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
         P("ora_zps_hde", [vp, i, i, vp, vp, vp])
+        P("ora_zps_hde_rd", [vp, i, vp, vp, vp, vp])
         _lib = L
     return _lib
 
@@ -339,4 +340,11 @@ class Oracle:
         gu = np.zeros((self.jpi, self.jpj, kjpt), order="F")
         gv = np.zeros((self.jpi, self.jpj, kjpt), order="F")
         self._ck(lib().ora_zps_hde(self.h, kt, kjpt, _p(pta), _p(gu), _p(gv)), "zps_hde")
+        return gu, gv
+
+    def zps_hde_rd(self, kt, pts, prd):
+        """zps_hde's density part: (gru, grv) of the density of the interpolated T, S"""
+        gu = np.zeros((self.jpi, self.jpj), order="F")
+        gv = np.zeros((self.jpi, self.jpj), order="F")
+        self._ck(lib().ora_zps_hde_rd(self.h, kt, _p(pts), _p(prd), _p(gu), _p(gv)), "zps_hde_rd")
         return gu, gv
