@@ -517,9 +517,11 @@ int nemo_gpu_stp_model(nemo_ctx *ctx, int kt);
  * (ptb_ad += ...); the adjoint of a trend array that the forward only adds to
  * (pta_ad of tra_adv_fct and tra_ldf_*) is read and left unchanged. */
 
-/* FCT (kn_fct_h = kn_fct_v = 2) with the limiter multipliers the forward call
- * recorded in NEMO_F_FCT_TAPE held fixed: ptb_ad += A_b^T pta_ad,
- * ptn_ad += A_n^T pta_ad. pun, pvn, pwn are the forward call's transports. */
+/* FCT with the limiter multipliers the forward call recorded in NEMO_F_FCT_TAPE held
+ * fixed: ptb_ad += A_b^T pta_ad, ptn_ad += A_n^T pta_ad. pun, pvn, pwn are the forward
+ * call's transports; kn_fct_h = 2 or 4 (the 4th-order centred horizontal fluxes,
+ * traadv_fct.F90:191-227), kn_fct_v = 2 or 4 (the compact 4th-order vertical
+ * interpolation interp_4th_cpt, :517-616, transposed column by column). */
 int nemo_gpu_tra_adv_fct_adj(nemo_ctx *ctx, int kt, int kit000, const char *cdtype, double p2dt,
                              const void *pun, const void *pvn, const void *pwn, void *ptb_ad,
                              void *ptn_ad, const void *pta_ad, int kjpt, int kn_fct_h, int kn_fct_v);

@@ -11,6 +11,8 @@ struct FctAdj {
   RO<double> tape;           // limiter multipliers, ((m*kjpt + n)*3 + face)*n3, face x,y,z
   double *tb_ad, *tn_ad;
   int kjpt, linssh;
+  int kh, kv;              // orders of the forward's antidiffusive fluxes (2 or 4)
+  double *zwt, *za;        // kv = 4: work of the transposed vertical interpolation (n3 per member)
 };
 
 struct LdfAdj {

@@ -20,6 +20,10 @@ dim3 acol_grid(const Dom<T>& d) {
 cudaError_t launch_fct_adj(const Dom<double>& d, const FctAdj& a, cudaStream_t s) {
   k_fct_adj<<<apt_grid(d), dim3(AX, AY), 0, s>>>(d, a);
   ktick(NEMO_K_FCT_ADJ, s);
+  if (a.kv == 4) {
+    k_fct_adj_v4<<<acol_grid(d), dim3(AX, AY), 0, s>>>(d, a);
+    ktick(NEMO_K_FCT_ADJ, s);
+  }
   return cudaGetLastError();
 }
 

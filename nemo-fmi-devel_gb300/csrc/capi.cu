@@ -84,6 +84,7 @@ struct nemo_ctx {
   void* rab_n = nullptr;       // and the now ones rab_n, with the vertical physics
   void* zphy_w = nullptr;      // zdf_phy work: sh2, apdlr and the TKE system, 5 x n3 per member
   void* zdyn_w = nullptr;      // dyn_zdf work: the implicit viscosity system, 2 x n3 per member
+  double* fadj_w = nullptr;    // FCT adjoint with kn_fct_v = 4: 2 x n3 per member
   double* usr_s = nullptr;     // usrdef_sbc: the step's scalars (7), written before each step
   double usr_zsurf = 0.0;      // usrdef_sbc: GLOB_SUM(tmask(:,:,1))
   void* blp_w = nullptr;       // tra_ldf_blp: the first laplacian (jpi,jpj,jpk,kjpt) per member
@@ -1815,7 +1816,7 @@ int nemo_gpu_destroy(nemo_ctx* c) {
   for (auto p : c->iso_w) cudaFree(p);
   for (auto p : c->adj_w) cudaFree(p);
   cudaFree(c->slp_w);
-  cudaFree(c->rab_w); cudaFree(c->rab_n); cudaFree(c->zphy_w); cudaFree(c->zdyn_w); cudaFree(c->usr_s);
+  cudaFree(c->rab_w); cudaFree(c->rab_n); cudaFree(c->zphy_w); cudaFree(c->zdyn_w); cudaFree(c->usr_s); cudaFree(c->fadj_w);
   cudaFree(c->blp_w);
   for (auto p : c->spg_w) cudaFree(p);
   for (auto p : c->spg_cor) cudaFree(p);
@@ -2438,7 +2439,13 @@ int nemo_gpu_tra_adv_fct_adj(nemo_ctx* c, int kt, int kit000, const char* cdtype
   if (int s = adj_check(c, cdtype, &is_trc, "tra_adv_fct_adj")) return s;
   if (!pun || !pvn || !pwn || !ptb_ad || !ptn_ad || !pta_ad || kjpt < 1)
     return fail(c, NEMO_ERR_ARG, "tra_adv_fct_adj: bad argument");
-  if (kn_fct_h != 2 || kn_fct_v != 2) return fail(c, NEMO_ERR_ARG, "tra_adv_fct_adj: kn_fct_h = kn_fct_v = 2 only");
+  if ((kn_fct_h != 2 && kn_fct_h != 4) || (kn_fct_v != 2 && kn_fct_v != 4))
+    return fail(c, NEMO_ERR_ARG, "tra_adv_fct_adj: kn_fct_h and kn_fct_v must be 2 or 4");
+  if (kn_fct_v == 4 && c->nam.ln_isfcav)
+    return fail(c, NEMO_ERR_UNSUPPORTED, "tra_adv_fct_adj: the compact vertical scheme without cavities");
+  if (kn_fct_v == 4 && !c->fadj_w &&
+      cudaMalloc(&c->fadj_w, 2 * (size_t)c->n3 * c->nmem * sizeof(double)) != cudaSuccess)
+    return fail(c, NEMO_ERR_NOMEM, "tra_adv_fct_adj work arrays");
   if (!c->f[NEMO_F_FCT_TAPE])
     return fail(c, NEMO_ERR_UNBOUND, "tra_adv_fct_adj: the limiter tape NEMO_F_FCT_TAPE must be bound");
   FctAdj a{};
@@ -2446,6 +2453,8 @@ int nemo_gpu_tra_adv_fct_adj(nemo_ctx* c, int kt, int kit000, const char* cdtype
   a.lam = (const double*)pta_ad; a.tape = (const double*)c->f[NEMO_F_FCT_TAPE];
   a.tb_ad = (double*)ptb_ad; a.tn_ad = (double*)ptn_ad;
   a.kjpt = kjpt; a.linssh = c->nam.ln_linssh;
+  a.kh = kn_fct_h; a.kv = kn_fct_v;
+  a.zwt = c->fadj_w; a.za = c->fadj_w ? c->fadj_w + (size_t)c->n3 * c->nmem : nullptr;
   cudaError_t e = launch_fct_adj(dom_now<double>(c), a, c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "tra_adv_fct_adj launch");
   return NEMO_OK;

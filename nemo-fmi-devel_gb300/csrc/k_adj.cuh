@@ -38,8 +38,9 @@ template <class T>
 __device__ __forceinline__ Pt3 pt3(const Dom<T>& d) { return Pt3{d.jpi, d.jpj, d.jpk, d.n2}; }
 
 // ------------------------------------------------------------------ tra_adv_fct
-// Adjoint of tra_adv_fct (traadv_fct.F90:54-327, kn_fct_h = kn_fct_v = 2) at one
-// point. With g = lam r1_e1e2t / e3t_n and h = g tmask on the interior cells (0
+// Adjoint of tra_adv_fct (traadv_fct.F90:54-327) at one point; with kn_fct_h = 4 the
+// 4th-order centred horizontal fluxes (:191-227), with kn_fct_v = 4 the compact
+// vertical interpolation's part is k_fct_adj_v4's (below). With g = lam r1_e1e2t / e3t_n and h = g tmask on the interior cells (0
 // elsewhere), the limited antidiffusive flux of face f has the adjoint
 // -(g(f) - g(f+1)); times the recorded multiplier (0 where the forward zeroed the
 // flux) it is the adjoint of the flux before limiting, the centred flux of tn minus
@@ -97,8 +98,35 @@ __global__ void __launch_bounds__(128) k_fct_adj(Dom<double> d, FctAdj a) {
     if (fw) tnv += 0.5 * un[q - 1] * axw;
     if (fn) tnv += 0.5 * vn[q] * ayn;
     if (fs) tnv += 0.5 * vn[q - jpi] * ays;
-    if (zt) tnv += wn[q] * 0.5 * azt;
-    if (zb) tnv += wn[q + n2] * 0.5 * azb;
+    if (a.kv == 2) {
+      if (zt) tnv += wn[q] * 0.5 * azt;
+      if (zb) tnv += wn[q + n2] * 0.5 * azb;
+    }
+    if (a.kh == 4) {
+      // zltu(m) = (ztu(m) + ztu(m-1)) / 6 enters the flux of u-face m with + and that
+      // of face m-1 with -; ztu(m) = (tn(m+1) - tn(m)) umask(m). S: the adjoint of a
+      // face's centred bracket; Z: of zltu (interior points only, lbc_lnk zeroes the
+      // edges). Likewise in j.
+      auto Su = [&](int fi) -> double {
+        if (!P.uface(fi, j, k)) return 0.0;
+        const long qf = P.q(fi, j, k);
+        return 0.5 * un[qf] * (tx[qf] * (g(fi + 1, j, k) - g(fi, j, k)));
+      };
+      auto Sv = [&](int fj) -> double {
+        if (!P.uface(i, fj, k)) return 0.0;
+        const long qf = P.q(i, fj, k);
+        return 0.5 * vn[qf] * (ty[qf] * (g(i, fj + 1, k) - g(i, fj, k)));
+      };
+      auto Zu = [&](int mi) -> double { return P.cell(mi, j, k) ? Su(mi) - Su(mi - 1) : 0.0; };
+      auto Zv = [&](int mj) -> double { return P.cell(i, mj, k) ? Sv(mj) - Sv(mj - 1) : 0.0; };
+      const double zu0 = Zu(i - 1), zu1 = Zu(i), zu2 = Zu(i + 1);
+      const double zv0 = Zv(j - 1), zv1 = Zv(j), zv2 = Zv(j + 1);
+      const double r1_6 = 1. / 6.;
+      if (i >= 2) tnv += r1_6 * (zu0 + zu1) * umsk<double>(d.ci[c.ij - 1], k);
+      tnv -= r1_6 * (zu1 + zu2) * umsk<double>(ci, k);
+      if (j >= 2) tnv += r1_6 * (zv0 + zv1) * vmsk<double>(d.ci[c.ij - jpi], k);
+      tnv -= r1_6 * (zv1 + zv2) * vmsk<double>(ci, k);
+    }
     // upstream fluxes: minus the antidiffusive adjoint plus their own trend's
     const double fxe = -axe + (he - hc), fxw = -axw + (hc - hw);
     const double fyn = -ayn + (hn - hc), fys = -ays + (hc - hs);
@@ -113,6 +141,85 @@ __global__ void __launch_bounds__(128) k_fct_adj(Dom<double> d, FctAdj a) {
     if (k == 1 && a.linssh) tbv += wn[q] * fzt;  // surface flux w tb (:146-156)
     a.tb_ad[mo + q] += tbv;
     a.tn_ad[mo + q] += tnv;
+  }
+}
+
+// With kn_fct_v = 4 (traadv_fct.F90:253-275): the vertical antidiffusive flux reads
+// ztw = M^-1 R tn of interp_4th_cpt (:517-616). One interior column a thread: the
+// adjoint V(k) = wn(k) az(k) of ztw(k), k = 2..jpk-1, then tn_ad += R^T M^-T V with
+// the forward's rows (special top and bottom rows), pivots zwt, the back
+// substitution undone forwards and the elimination backwards (as the oracle's
+// ora_interp_4th_cpt_adj). Runs after k_fct_adj, which leaves this part out.
+__global__ void k_fct_adj_v4(Dom<double> d, FctAdj a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i < 2 || i > d.jpi - 1 || j < 2 || j > d.jpj - 1) return;
+  const int m = blockIdx.z, jpk = d.jpk;
+  const Pt3 P = pt3(d);
+  const long ij = P.ij(i, j), n2 = d.n2, n3 = d.n3, c3 = (long)m * n3 + ij;
+  const ColInfo ci = d.ci[ij];
+  const int ikt = 2, ikb = d.mbkt[ij];
+  const RO<double> wn = a.pwn + (long)m * n3;
+  const double r1 = d.r1_e1e2t[ij];
+  auto row = [&](int k, double& dd, double& wi, double& ws, double& w) {
+    const double wm = wmsk<double>(ci, k);
+    if (k == ikt || k == ikb) { dd = 1.0; wi = 0.0; ws = 0.0; w = 0.5; }
+    else { dd = 3.0 * wm + 1.0; wi = wm; ws = wm; w = 3.0 * wm; }
+  };
+  // the pivots (the same for every tracer)
+  {
+    double dd, wi, ws, w, wsp;
+    row(2, dd, wi, wsp, w);
+    a.zwt[c3 + n2] = dd;
+    double tp = dd;
+    for (int k = 3; k <= jpk - 1; ++k) {
+      row(k, dd, wi, ws, w);
+      tp = dd - wi * wsp / tp;
+      a.zwt[c3 + (long)(k - 1) * n2] = tp;
+      wsp = ws;
+    }
+  }
+  for (int n = 0; n < a.kjpt; ++n) {
+    const long mo = ((long)m * a.kjpt + n) * n3;
+    const RO<double> lam = a.lam + mo;
+    const RO<double> tz = a.tape + ((long)m * a.kjpt + n) * 3 * n3 + 2 * n3;
+    auto g = [&](int k) -> double {
+      return (k >= 1 && k <= jpk - 1) ? lam[ij + (long)(k - 1) * n2] * r1 / d.e3t_n(ij, k, m) : 0.0;
+    };
+    // V into za, then the back substitution undone (za: the adjoint of z)
+    for (int k = 2; k <= jpk - 1; ++k) {
+      const long q = ij + (long)(k - 1) * n2;
+      const double az = tz[q] * (g(k - 1) - g(k)) * wmsk<double>(ci, k);
+      a.za[c3 + (long)(k - 1) * n2] = wn[q] * az;
+    }
+    double carry = 0.0;
+    for (int k = 2; k <= jpk - 2; ++k) {
+      const long o = c3 + (long)(k - 1) * n2;
+      double dd, wi, ws, w;
+      row(k, dd, wi, ws, w);
+      const double x = a.za[o] + carry;
+      const double z = x / a.zwt[o];
+      a.za[o] = z;
+      carry = -ws * z;
+    }
+    {
+      const long o = c3 + (long)(jpk - 2) * n2;
+      a.za[o] = (a.za[o] + carry) / a.zwt[o];
+    }
+    // the elimination undone, then the right-hand side transposed
+    double zk = a.za[c3 + (long)(jpk - 2) * n2];
+    for (int k = jpk - 1; k >= 2; --k) {
+      double dd, wi, ws, w;
+      row(k, dd, wi, ws, w);
+      const long o = c3 + (long)(k - 1) * n2;
+      if (k >= 3) {
+        const long om = o - n2;
+        const double zm = a.za[om] - wi / a.zwt[om] * zk;
+        a.za[om] = zm;
+      }
+      a.tn_ad[mo + ij + (long)(k - 1) * n2] += w * zk;
+      a.tn_ad[mo + ij + (long)(k - 2) * n2] += w * zk;
+      if (k >= 3) zk = a.za[o - n2];
+    }
   }
 }
 

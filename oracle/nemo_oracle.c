@@ -526,6 +526,46 @@ int ora_interp_4th_cpt(ora_ctx *c, const double *pt_in, double *pt_out) {
   return NEMO_OK;
 }
 
+/* The adjoint of ora_interp_4th_cpt with respect to pt_in: pv holds the adjoint of
+ * pt_out on the interior columns, levels 2..jpkm1; pt_ad accumulates R^T M^-T pv, M
+ * the tridiagonal matrix and R the right-hand-side operator the forward builds (the
+ * same rows, pivots zwt and special top and bottom rows), the back substitution
+ * undone forwards and the elimination backwards. */
+int ora_interp_4th_cpt_adj(ora_ctx *c, const double *pv, double *pt_ad) {
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const double *wmask = c->wmask;
+  double *d = malloc(sizeof(double) * jpk), *wi = malloc(sizeof(double) * jpk), *ws = malloc(sizeof(double) * jpk);
+  double *w = malloc(sizeof(double) * jpk), *zwt = malloc(sizeof(double) * jpk), *xa = malloc(sizeof(double) * jpk);
+  double *za = malloc(sizeof(double) * jpk);
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      const size_t p = I2(ji, jj);
+      const int ikt = c->mikt[p] + 1, ikb = c->mbkt[p];
+      for (int jk = 2; jk <= jpk - 1; ++jk) {  /* the forward's rows (:535-565) */
+        const double wm = wmask[I3(ji, jj, jk)];
+        if (jk == ikt || jk == ikb) { d[jk] = 1.0; wi[jk] = 0.0; ws[jk] = 0.0; w[jk] = 0.5; }
+        else if (jk >= 3) { d[jk] = 3.0 * wm + 1.0; wi[jk] = wm; ws[jk] = wm; w[jk] = 3.0 * wm; }
+        else { d[jk] = 0.0; wi[jk] = 0.0; ws[jk] = 0.0; w[jk] = 0.0; }
+      }
+      zwt[2] = d[2];
+      for (int jk = 3; jk <= jpk - 1; ++jk) zwt[jk] = d[jk] - wi[jk] * ws[jk - 1] / zwt[jk - 1];
+      for (int jk = 2; jk <= jpk - 1; ++jk) xa[jk] = pv[I3(ji, jj, jk)];
+      for (int jk = 2; jk <= jpk - 2; ++jk) {  /* back substitution, undone (:596-607) */
+        za[jk] = xa[jk] / zwt[jk];
+        xa[jk + 1] = xa[jk + 1] - ws[jk] * za[jk];
+      }
+      za[jpk - 1] = xa[jpk - 1] / zwt[jpk - 1];
+      for (int jk = jpk - 1; jk >= 3; --jk)  /* elimination, undone (:584-593) */
+        za[jk - 1] = za[jk - 1] - wi[jk] / zwt[jk - 1] * za[jk];
+      for (int jk = 2; jk <= jpk - 1; ++jk) {  /* the right-hand side, transposed */
+        pt_ad[I3(ji, jj, jk)] += w[jk] * za[jk];
+        pt_ad[I3(ji, jj, jk - 1)] += w[jk] * za[jk];
+      }
+    }
+  free(d); free(wi); free(ws); free(w); free(zwt); free(xa); free(za);
+  return NEMO_OK;
+}
+
 /* -------------------------------------------------------------------- nonosc */
 /* traadv_fct.F90:330-428 */
 static void nonosc(ora_ctx *c, const double *pbef, double *paa, double *pbb, double *pcc,
@@ -2487,13 +2527,15 @@ int ora_tra_adv_fct_adj(ora_ctx *c, int kt, int kit000, const char *cdtype, doub
                         double *ptb_ad, double *ptn_ad, const double *pta_ad,
                         int kjpt, int kn_fct_h, int kn_fct_v) {
   (void)kt; (void)kit000; (void)cdtype; (void)p2dt;
-  if (kn_fct_h != 2 || kn_fct_v != 2 || kjpt < 1) return NEMO_ERR_ARG;
+  if ((kn_fct_h != 2 && kn_fct_h != 4) || (kn_fct_v != 2 && kn_fct_v != 4) || kjpt < 1) return NEMO_ERR_ARG;
   if (!c->fct_tape) return NEMO_ERR_UNBOUND;
   const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
   const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
   const double *tmask = c->tmask, *wmask = c->wmask, *e3t_n = fld(c, NEMO_F_E3T_N);
+  const double *umask = c->umask, *vmask = c->vmask, r1_6 = 1. / 6.;
   double *ax = zalloc(n3), *ay = zalloc(n3), *az = zalloc(n3);
   double *fx = zalloc(n3), *fy = zalloc(n3), *fz = zalloc(n3);
+  double *zlu = zalloc(n3), *zlv = zalloc(n3), *zv = zalloc(n3);
   for (int jn = 1; jn <= kjpt; ++jn) {
     const double *lam = pta_ad + n3 * (jn - 1), *tp = c->fct_tape + 3 * n3 * (size_t)(jn - 1);
     double *tb_ad = ptb_ad + n3 * (jn - 1), *tn_ad = ptn_ad + n3 * (jn - 1);
@@ -2513,31 +2555,63 @@ int ora_tra_adv_fct_adj(ora_ctx *c, int kt, int kit000, const char *cdtype, doub
     /* (:276-278) linear free surface: no antidiffusive flux through the surface */
     if (c->nam.ln_linssh)
       for (size_t p = 0; p < n2; ++p) az[p] = 0.0;
-    /* (:255-263) vertical antidiffusive flux = centred - upstream, interior columns */
+    /* (:253-275) vertical antidiffusive flux = centred (C2, or the compact 4th-order
+     * interpolation ztw) - upstream, interior columns */
     memcpy(fz, az, n3 * sizeof(double));
+    if (kn_fct_v == 4) memset(zv, 0, n3 * sizeof(double));
     for (int jk = 2; jk <= jpk - 1; ++jk)
       for (int jj = 2; jj <= jpj - 1; ++jj)
         for (int ji = 2; ji <= jpi - 1; ++ji) {
           size_t q = I3(ji, jj, jk);
           double a = az[q] * wmask[q];
-          tn_ad[q] += pwn[q] * 0.5 * a;
-          tn_ad[I3(ji, jj, jk - 1)] += pwn[q] * 0.5 * a;
+          if (kn_fct_v == 2) {
+            tn_ad[q] += pwn[q] * 0.5 * a;
+            tn_ad[I3(ji, jj, jk - 1)] += pwn[q] * 0.5 * a;
+          } else {
+            zv[q] = pwn[q] * a;  /* the adjoint of ztw */
+          }
           fz[q] = -a;
         }
-    /* (:182-190) horizontal antidiffusive fluxes */
+    if (kn_fct_v == 4) ora_interp_4th_cpt_adj(c, zv, tn_ad);
+    /* (:182-190, :191-227) horizontal antidiffusive fluxes, C2 or C4 */
     memcpy(fx, ax, n3 * sizeof(double));
     memcpy(fy, ay, n3 * sizeof(double));
+    if (kn_fct_h == 4) { memset(zlu, 0, n3 * sizeof(double)); memset(zlv, 0, n3 * sizeof(double)); }
     for (int jk = 1; jk <= jpk - 1; ++jk)
       for (int jj = 1; jj <= jpj - 1; ++jj)
         for (int ji = 1; ji <= jpi - 1; ++ji) {
           size_t q = I3(ji, jj, jk);
-          tn_ad[q] += 0.5 * pun[q] * ax[q];
-          tn_ad[I3(ji + 1, jj, jk)] += 0.5 * pun[q] * ax[q];
-          tn_ad[q] += 0.5 * pvn[q] * ay[q];
-          tn_ad[I3(ji, jj + 1, jk)] += 0.5 * pvn[q] * ay[q];
+          const double su = 0.5 * pun[q] * ax[q], sv = 0.5 * pvn[q] * ay[q];
+          tn_ad[q] += su;
+          tn_ad[I3(ji + 1, jj, jk)] += su;
+          tn_ad[q] += sv;
+          tn_ad[I3(ji, jj + 1, jk)] += sv;
+          if (kn_fct_h == 4) {  /* + zltu(ji) - zltu(ji+1) */
+            zlu[q] += su; zlu[I3(ji + 1, jj, jk)] -= su;
+            zlv[q] += sv; zlv[I3(ji, jj + 1, jk)] -= sv;
+          }
           fx[q] = -ax[q];
           fy[q] = -ay[q];
         }
+    if (kn_fct_h == 4) {
+      /* zltu, zltv: only the interior values enter the fluxes (their lbc_lnk zeroes
+       * the edges); zltu = (ztu(ji) + ztu(ji-1)) / 6, ztu = (tn(ji+1) - tn(ji)) umask */
+      for (int jk = 1; jk <= jpk - 1; ++jk)
+        for (int jj = 2; jj <= jpj - 1; ++jj)
+          for (int ji = 2; ji <= jpi - 1; ++ji) {
+            size_t q = I3(ji, jj, jk);
+            const double zu = zlu[q] * r1_6, zw = zlv[q] * r1_6;
+            const size_t qw = I3(ji - 1, jj, jk), qs = I3(ji, jj - 1, jk);
+            tn_ad[I3(ji + 1, jj, jk)] += zu * umask[q];
+            tn_ad[q] -= zu * umask[q];
+            tn_ad[q] += zu * umask[qw];
+            tn_ad[qw] -= zu * umask[qw];
+            tn_ad[I3(ji, jj + 1, jk)] += zw * vmask[q];
+            tn_ad[q] -= zw * vmask[q];
+            tn_ad[q] += zw * vmask[qs];
+            tn_ad[qs] -= zw * vmask[qs];
+          }
+    }
     /* (:158-170) upstream trend (zwi, used only by the frozen limiter, drops out) */
     for (int jk = 1; jk <= jpk - 1; ++jk)
       for (int jj = 2; jj <= jpj - 1; ++jj)
@@ -2571,7 +2645,7 @@ int ora_tra_adv_fct_adj(ora_ctx *c, int kt, int kit000, const char *cdtype, doub
           tb_ad[I3(ji, jj + 1, jk)] += 0.5 * (pvn[q] - fabs(pvn[q])) * fy[q];
         }
   }
-  wfree(ax); wfree(ay); wfree(az); wfree(fx); wfree(fy); wfree(fz);
+  wfree(ax); wfree(ay); wfree(az); wfree(fx); wfree(fy); wfree(fz); wfree(zlu); wfree(zlv); wfree(zv);
   return NEMO_OK;
 }
 

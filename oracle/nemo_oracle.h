@@ -46,6 +46,7 @@ int ora_tra_adv_fct(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
                     const double *ptb, const double *ptn, double *pta,
                     int kjpt, int kn_fct_h, int kn_fct_v);
 int ora_interp_4th_cpt(ora_ctx *c, const double *pt_in, double *pt_out);
+int ora_interp_4th_cpt_adj(ora_ctx *c, const double *pv, double *pt_ad);
 int ora_tra_ldf_lap(ora_ctx *c, int kt, int kit000, const char *cdtype,
                     const double *pahu, const double *pahv,
                     const double *pgu, const double *pgv, const double *pgui, const double *pgvi,

@@ -34,6 +34,7 @@ def lib():
         P("ora_tra_adv_trp", [vp, vp, vp, vp, vp, vp, vp])
         P("ora_tra_adv_fct", [vp, i, i, cp, d, vp, vp, vp, vp, vp, vp, i, i, i])
         P("ora_interp_4th_cpt", [vp, vp, vp])
+        P("ora_interp_4th_cpt_adj", [vp, vp, vp])
         P("ora_tra_ldf_lap", [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
         P("ora_tra_ldf_iso", [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
         P("ora_tra_zdf_imp", [vp, i, i, cp, d, vp, vp, i])
@@ -173,6 +174,9 @@ class Oracle:
         self._ck(lib().ora_interp_4th_cpt(self.h, _p(pt_in), _p(out)), "interp_4th_cpt")
         return out
 
+    def interp_4th_cpt_adj(self, pv, pt_ad):
+        """pt_ad += the adjoint of interp_4th_cpt applied to pv"""
+        self._ck(lib().ora_interp_4th_cpt_adj(self.h, _p(pv), _p(pt_ad)), "interp_4th_cpt_adj")
     def tra_ldf_lap(self, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb, pta, kjpt, kpass):
         self._ck(lib().ora_tra_ldf_lap(self.h, kt, kit000, cdtype.encode(), _p(pahu), _p(pahv), _p(pgu), _p(pgv),
                                        _p(pgui), _p(pgvi), _p(ptb), _p(pta), kjpt, kpass), "tra_ldf_lap")

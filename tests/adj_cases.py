@@ -73,29 +73,30 @@ class Case:
         return np.array(self.st["tsn"], dtype=np.float64, order="F")
 
     # ---------------------------------------------------------- forward / TL
-    def fct_record(self, tb=None, tn=None):
+    def fct_record(self, tb=None, tn=None, kh=2, kv=2):
         """Forward FCT on the state, recording the limiter; returns (tape, ta)."""
         tape = np.zeros(3 * 2 * self.n3)
         self.o.set_fct_tape(tape, 1)
         ta = np.zeros(self.s4, order="F")
         self.o.tra_adv_fct(self.kit + 2, self.kit, "TRA", self.p2dt, self.zun, self.zvn, self.zwn,
-                           self.tsb() if tb is None else tb, self.tsn() if tn is None else tn, ta, 2, 2, 2)
+                           self.tsb() if tb is None else tb, self.tsn() if tn is None else tn, ta, 2, kh, kv)
         self.o.set_fct_tape(None, 0)
         return tape, ta
 
-    def fct_tl(self, tape, dtb, dtn):
+    def fct_tl(self, tape, dtb, dtn, kh=2, kv=2):
         self.o.set_fct_tape(tape, 2)
         ta = np.zeros(self.s4, order="F")
-        self.o.tra_adv_fct(self.kit + 2, self.kit, "TRA", self.p2dt, self.zun, self.zvn, self.zwn, dtb, dtn, ta, 2, 2, 2)
+        self.o.tra_adv_fct(self.kit + 2, self.kit, "TRA", self.p2dt, self.zun, self.zvn, self.zwn, dtb, dtn, ta, 2,
+                           kh, kv)
         self.o.set_fct_tape(None, 0)
         return ta
 
-    def fct_adj(self, tape, lam):
+    def fct_adj(self, tape, lam, kh=2, kv=2):
         tb_ad = np.zeros(self.s4, order="F")
         tn_ad = np.zeros(self.s4, order="F")
         self.o.set_fct_tape(tape, 2)
         self.o.tra_adv_fct_adj(self.kit + 2, self.kit, "TRA", self.p2dt, self.zun, self.zvn, self.zwn,
-                               tb_ad, tn_ad, lam, 2, 2, 2)
+                               tb_ad, tn_ad, lam, 2, kh, kv)
         self.o.set_fct_tape(None, 0)
         return tb_ad, tn_ad
 

@@ -23,14 +23,17 @@ def cases(request):
     return c, GpuCase(c)
 
 
-def test_fct_tape_matches_oracle_and_adjoint(cases):
+@pytest.mark.parametrize("kh,kv", [(2, 2), (4, 4), (4, 2), (2, 4)])
+def test_fct_tape_matches_oracle_and_adjoint(cases, kh, kv):
+    """FCT 2/2 and, with the 4th-order centred horizontal fluxes and the compact
+    vertical interpolation, FCT 4/4 (the shelf's configuration) and the mixed orders."""
     c, g = cases
-    tape_o, ta_o = c.fct_record()
+    tape_o, ta_o = c.fct_record(kh=kh, kv=kv)
     tape_d = g.dev(np.zeros(3 * 2 * c.n3))
     g.ctx.bind("FCT_TAPE", tape_d)
     ta_d = g.dev(np.zeros(c.s4, order="F"))
     kt = c.kit + 2
-    g.ctx.tra_adv_fct(kt, c.kit, "TRA", c.p2dt, g.zun, g.zvn, g.zwn, g.dev(c.tsb()), g.dev(c.tsn()), ta_d, 2, 2, 2)
+    g.ctx.tra_adv_fct(kt, c.kit, "TRA", c.p2dt, g.zun, g.zvn, g.zwn, g.dev(c.tsb()), g.dev(c.tsn()), ta_d, 2, kh, kv)
     assert relerr(ta_o, g.host(ta_d, c.s4)[0]) <= TOL
     g.ctx.synchronize()
     tape_g = tape_d.cpu().numpy()
@@ -41,14 +44,14 @@ def test_fct_tape_matches_oracle_and_adjoint(cases):
     dtb, dtn = c.rand4(), c.rand4()
     tb_ad, tn_ad = g.dev(np.zeros(c.s4, order="F")), g.dev(np.zeros(c.s4, order="F"))
     lam_d = g.dev(lam)
-    g.ctx.tra_adv_fct_adj(kt, c.kit, "TRA", c.p2dt, g.zun, g.zvn, g.zwn, tb_ad, tn_ad, lam_d, 2, 2, 2)
+    g.ctx.tra_adv_fct_adj(kt, c.kit, "TRA", c.p2dt, g.zun, g.zvn, g.zwn, tb_ad, tn_ad, lam_d, 2, kh, kv)
     g.ctx.synchronize()
     assert np.array_equal(g.host(lam_d, c.s4)[0], lam)   # pta_ad is left unchanged
-    rtb, rtn = c.fct_adj(tape_g.copy(), lam)
+    rtb, rtn = c.fct_adj(tape_g.copy(), lam, kh=kh, kv=kv)
     gtb, gtn = g.host(tb_ad, c.s4)[0], g.host(tn_ad, c.s4)[0]
-    assert relerr(rtb, gtb) <= TOL and relerr(rtn, gtn) <= TOL
+    assert relerr(rtb, gtb) <= TOL and relerr(rtn, gtn) <= TOL, (relerr(rtb, gtb), relerr(rtn, gtn))
     # dot-product test: oracle tangent-linear with the same tape, GPU adjoint
-    y = c.fct_tl(tape_g.copy(), dtb, dtn)
+    y = c.fct_tl(tape_g.copy(), dtb, dtn, kh=kh, kv=kv)
     err, lhs, _ = dot_test([(y, lam)], [(dtb, gtb), (dtn, gtn)])
     assert lhs != 0 and err <= TOL, err
     g.ctx.bind("FCT_TAPE", None)

@@ -42,6 +42,37 @@ def test_fct_dot_product(kind, gyre_case, shelf_case):
     assert err < DOT_TOL, err
 
 
+@pytest.mark.parametrize("kh,kv", [(4, 4), (4, 2), (2, 4)])
+@pytest.mark.parametrize("kind", ["gyre", "shelf"])
+def test_fct_fourth_order_dot_product(kind, kh, kv, gyre_case, shelf_case):
+    """FCT with the 4th-order centred horizontal fluxes (traadv_fct.F90:191-227)
+    and/or the compact 4th-order vertical interpolation (:517-616)."""
+    c = gyre_case if kind == "gyre" else shelf_case
+    tape, _ = c.fct_record(kh=kh, kv=kv)
+    dtb, dtn, lam = c.rand4(), c.rand4(), c.rand4(masked=False)
+    y = c.fct_tl(tape, dtb, dtn, kh=kh, kv=kv)
+    tb_ad, tn_ad = c.fct_adj(tape, lam, kh=kh, kv=kv)
+    err, lhs, _ = dot_test([(y, lam)], [(dtb, tb_ad), (dtn, tn_ad)])
+    assert abs(lhs) > 0
+    assert err < DOT_TOL, err
+
+
+def test_interp_4th_cpt_dot_product(shelf_case):
+    """<interp(dt), v> = <dt, interp^T v> on the interior columns, levels 2..jpk-1."""
+    c = shelf_case
+    rng = np.random.default_rng(7)
+    jpi, jpj, jpk = c.s4[:3]
+    dt = np.asfortranarray(rng.standard_normal((jpi, jpj, jpk)))
+    v = np.zeros((jpi, jpj, jpk), order="F")
+    v[1:-1, 1:-1, 1:-1] = rng.standard_normal((jpi - 2, jpj - 2, jpk - 2))
+    y = c.o.interp_4th_cpt(dt)
+    ad = np.zeros((jpi, jpj, jpk), order="F")
+    c.o.interp_4th_cpt_adj(v, ad)
+    lhs = (y[1:-1, 1:-1, 1:-1] * v[1:-1, 1:-1, 1:-1]).sum()
+    rhs = (dt * ad).sum()
+    assert abs(lhs - rhs) <= 1e-12 * (np.abs(y[1:-1, 1:-1, 1:-1] * v[1:-1, 1:-1, 1:-1]).sum()), (lhs, rhs)
+
+
 def test_fct_tangent_linear_matches_finite_differences_away_from_limiter(gyre_case):
     """Perturb one wet point whose neighbourhood (3 points each way) has every
     limiter multiplier at 1: the forward is linear there, so the central
