@@ -235,6 +235,17 @@ enum nemo_field_id {
   /* the horizontal gradients of the in situ density at the last ocean level of u- and
    * v-points (oce.F90 gru, grv; zps_hde with partial steps), read by ldf_slp */
   NEMO_F_GRU, NEMO_F_GRV,              /* [S]                                         */
+  /* z* time stepping (domvvl.F90, dynnxt.F90; dom_oce.F90 names): the after scale
+   * factors at u- and v-points and the after column depths of dom_vvl_sf_nxt, the
+   * before (time-filtered) scale factors of dyn_nxt, the remaining now and before
+   * scale factors, depths and gde3w of dom_vvl_sf_swp, and the rest-state e3uw_0,
+   * e3vw_0 (domain-file inputs, read only when E3UW_N/E3VW_N are bound). */
+  NEMO_F_E3U_A, NEMO_F_E3V_A,          /* [T]                                         */
+  NEMO_F_HU_A, NEMO_F_HV_A, NEMO_F_R1_HU_A, NEMO_F_R1_HV_A, /* [S]                    */
+  NEMO_F_E3U_B, NEMO_F_E3V_B, NEMO_F_E3W_B, /* [T]                                    */
+  NEMO_F_E3UW_N, NEMO_F_E3VW_N, NEMO_F_E3UW_B, NEMO_F_E3VW_B, /* [T]                  */
+  NEMO_F_GDEPT_B, NEMO_F_GDEPW_B, NEMO_F_GDE3W_N, /* [T]                              */
+  NEMO_F_E3UW_0, NEMO_F_E3VW_0,        /* [T]                                         */
   NEMO_F_COUNT
 };
 
@@ -440,11 +451,15 @@ int nemo_gpu_tra_zdf_imp(nemo_ctx *ctx, int kt, int kit000, const char *cdtype, 
  * implicit solve, then WHERE( tsa(:,:,:,jp_sal) < 0 ) tsa = 0.1 (:83). */
 int nemo_gpu_tra_zdf(nemo_ctx *ctx, int kt);
 
-/* tra_nxt (tranxt.F90:66-188 with tra_nxt_fix :191-237) on the bound tsb, tsn,
- * tsa: lbc_lnk of tsa, then at the first step of an Euler start (neuler = 0,
- * kt = nit000) tsn = tsa, otherwise the leapfrog swap with the Asselin filter
- * tsb = tsn + rn_atfp (tsa - 2 tsn + tsb), tsn = tsa on the interior, and lbc_lnk
- * of tsb and tsn. Linear free surface only (tra_nxt_vvl is not on the path). */
+/* tra_nxt (tranxt.F90:66-188) on the bound tsb, tsn, tsa: lbc_lnk of tsa, then at
+ * the first step of an Euler start (neuler = 0, kt = nit000) tsn = tsa, otherwise
+ * the leapfrog swap with the Asselin filter on the interior and lbc_lnk of tsb and
+ * tsn. Linear free surface: tra_nxt_fix (:191-237), tsb = tsn + rn_atfp (tsa - 2 tsn
+ * + tsb). Variable volume (ln_linssh = 0): tra_nxt_vvl (:240-380), the
+ * thickness-weighted filter of E3T_B, E3T_N, E3T_A with the forcing removed at the
+ * first level (EMP_B / EMP, RNF_B / RNF when bound, SBC_TSC / SBC_TSC_B) and, with
+ * ln_traqsr, in the penetrating-light levels (QSR_HC / QSR_HC_B); no runoff depth,
+ * ice-shelf melt or tracer runoff (ln_rnf). */
 int nemo_gpu_tra_nxt(nemo_ctx *ctx, int kt);
 
 /* ------------------------------------------------- the rest of a model step
@@ -475,13 +490,32 @@ int nemo_gpu_ldf_slp(nemo_ctx *ctx, int kt, const void *prd, const void *pn2);
  * bound, else UTAU, VTAU), solved per column (:205-302). nemo_gpu_stp_model runs it
  * after dyn_spg_ts. */
 int nemo_gpu_dyn_zdf_step(nemo_ctx *ctx, int kt);
-/* dyn_nxt (dynnxt.F90:66-377) for ln_linssh with ln_dynspg_ts and ln_bt_fw: the
- * barotropic part of ua replaced by ua_b, lbc_lnk, the Euler swap or the Asselin
- * filter and swap with ub returned to the time-split estimate, then un_b, ub_b.
- * NEMO_ERR_UNSUPPORTED for other settings. */
+/* dyn_nxt (dynnxt.F90:66-377) with ln_dynspg_ts and ln_bt_fw: the barotropic part
+ * of ua replaced by ua_b, lbc_lnk, the Euler swap or the Asselin filter and swap
+ * with ub returned to the time-split estimate, then un_b, ub_b. Variable volume
+ * (ln_linssh = 0) adds the time filter of E3T_B with the forcing removed at the
+ * first level (:217-226), E3U_B / E3V_B interpolated from it, the filter on the
+ * velocity (ln_dynadv_vec) or on the thickness-weighted velocity (flux form,
+ * :277-307), HU_B, HV_B and their inverses, and at the Euler step the copy of
+ * E3T_A, E3U_A, E3V_A into the now fields (:172-186); it reads E3U_A, E3V_A,
+ * R1_HU_A, R1_HV_A of dom_vvl_sf_nxt and R1_HU_N, R1_HV_N. */
 int nemo_gpu_dyn_nxt(nemo_ctx *ctx, int kt);
-/* ssh_swp (sshwzv.F90:216-267), linear free surface. */
+/* ssh_swp (sshwzv.F90:216-267); with variable volume the forcing (EMP_B - EMP,
+ * RNF_B - RNF when bound) removed from the filtered before ssh (:254-258). */
 int nemo_gpu_ssh_swp(nemo_ctx *ctx, int kt);
+/* dom_vvl_sf_nxt (domvvl.F90:268-562) for z* (ln_vvl_zstar; z-tilde and layer
+ * coordinates are not on this path): E3T_A = E3T_B + E3T_N z_scale on the wet
+ * levels, z_scale = (ssha - sshb) ssmask / (ht_0 + sshn + 1 - ssmask); E3U_A, E3V_A
+ * by dom_vvl_interpol (:678-782: surface-weighted means of the e3t_a change, lbc,
+ * plus the rest state); HU_A, HV_A and R1_HU_A, R1_HV_A. Reads SSHA, SSHB, SSHN. */
+int nemo_gpu_dom_vvl_sf_nxt(nemo_ctx *ctx, int kt);
+/* dom_vvl_sf_swp (domvvl.F90:565-675, z*): GDEPT_B / GDEPW_B = the now depths (when
+ * bound), E3T_N, E3U_N, E3V_N = the after fields, E3F_N from E3U_N, E3W_N from
+ * E3T_N and E3W_B from E3T_B (and E3UW_N/E3VW_N, E3UW_B/E3VW_B from the u-/v-scale
+ * factors when bound, with the rest-state E3UW_0/E3VW_0), the now depths GDEPT_N,
+ * GDEPW_N and GDE3W_N (when bound), HU_N, HV_N, R1_HU_N, R1_HV_N = the after ones,
+ * HT_N. No restart write (that is nemo_gpu/restart.py's). */
+int nemo_gpu_dom_vvl_sf_swp(nemo_ctx *ctx, int kt);
 /* One model step on the bound fields, in step.F90's order (:96-305):
  *  - the vertical physics (:127-133), with ln_zdftke, an equation of state and the
  *    fields of nemo_gpu_zdf_phy and gdept_n bound: rab_3d and bn2 of tsb and tsn into
@@ -668,6 +702,8 @@ enum nemo_kernel_id {
   NEMO_K_STP_CTL, NEMO_K_DIA_HSB, /* run control extrema, conservation budgets */
   NEMO_K_ZDF_PHY,      /* shear production, TKE closure, enhanced vertical diffusion */
   NEMO_K_USR_SBC,      /* GYRE's analytic surface forcing */
+  NEMO_K_VVL_SF,       /* z*: the after scale factors and the swap (dom_vvl_sf_nxt/_swp) */
+  NEMO_K_VVL_NXT,      /* z*: tra_nxt_vvl, dyn_nxt's filter of e3 and velocities, ssh_swp */
   NEMO_K_COUNT
 };
 

@@ -10,6 +10,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <map>
 #include <string>
 #include <vector>
@@ -281,6 +282,10 @@ size_t field_numel(const nemo_ctx* c, int id) {
     case NEMO_F_RHD: case NEMO_F_RHOP: case NEMO_F_RN2B: case NEMO_F_AHMT: case NEMO_F_AHMF: return (size_t)c->n3;
     case NEMO_F_AVM: case NEMO_F_AVM_K: case NEMO_F_AVT_K: case NEMO_F_EN: case NEMO_F_DISSL: case NEMO_F_RN2:
       return (size_t)c->n3;
+    case NEMO_F_E3U_A: case NEMO_F_E3V_A: case NEMO_F_E3U_B: case NEMO_F_E3V_B: case NEMO_F_E3W_B:
+    case NEMO_F_E3UW_N: case NEMO_F_E3VW_N: case NEMO_F_E3UW_B: case NEMO_F_E3VW_B:
+    case NEMO_F_GDEPT_B: case NEMO_F_GDEPW_B: case NEMO_F_GDE3W_N: case NEMO_F_E3UW_0: case NEMO_F_E3VW_0:
+      return (size_t)c->n3;
     default: break;
   }
   if (id >= NEMO_F_SSHB) return (size_t)c->n2;
@@ -427,7 +432,7 @@ int build_dom(nemo_ctx* c, DomStore<T>& st) {
 #define UP(name) if ((s = upload(c, st, c->name, &d.name))) return s
   UP(e1t); UP(e2t); UP(e1u); UP(e2u); UP(e1v); UP(e2v);
   UP(r1_e1u); UP(r1_e2u); UP(r1_e1v); UP(r1_e2v);
-  UP(e1e2t); UP(r1_e1e2t); UP(e2_e1u); UP(e1_e2v); UP(r1_e1e2u); UP(r1_e1e2v); UP(r1_e1e2f);
+  UP(e1e2t); UP(r1_e1e2t); UP(e2_e1u); UP(e1_e2v); UP(r1_e1e2u); UP(r1_e1e2v); UP(r1_e1e2f); UP(e1e2u);
   UP(ht_0); UP(hu_0); UP(hv_0); UP(r1_hu_0); UP(r1_hv_0);
   UP(ssmask); UP(ssumask); UP(ssvmask);
   UP(ff_t); UP(ff_f); UP(zwz); UP(ftne); UP(ftnw); UP(ftse); UP(ftsw);
@@ -1152,6 +1157,72 @@ int run_ssh_swp(nemo_ctx* c, int kt) {
                                     (const double*)c->f[NEMO_F_SSHA], (T)nm.rn_atfp,
                                     nm.neuler == 0 && kt == nm.nit000, c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "ssh_swp launch");
+  return NEMO_OK;
+}
+
+// ------------------------------------------------------------ z* time stepping
+// The arguments of the k_vvl.cuh kernels from the bound fields (null where unbound).
+template <class T>
+VvlArgs<T> vvl_args(nemo_ctx* c, int kt) {
+  const nemo_namelist& nm = c->nam;
+  void* const* F = c->f;
+  auto t = [&](int id) { return (T*)F[id]; };
+  VvlArgs<T> a{};
+  a.ssha = (const double*)F[NEMO_F_SSHA]; a.sshb = t(NEMO_F_SSHB); a.sshn = t(NEMO_F_SSHN);
+  a.emp = t(NEMO_F_EMP); a.emp_b = t(NEMO_F_EMP_B); a.rnf = t(NEMO_F_RNF); a.rnf_b = t(NEMO_F_RNF_B);
+  a.e3t_b = t(NEMO_F_E3T_B); a.e3t_n = t(NEMO_F_E3T_N); a.e3t_a = t(NEMO_F_E3T_A);
+  a.e3u_n = t(NEMO_F_E3U_N); a.e3v_n = t(NEMO_F_E3V_N); a.e3u_a = t(NEMO_F_E3U_A); a.e3v_a = t(NEMO_F_E3V_A);
+  a.e3u_b = t(NEMO_F_E3U_B); a.e3v_b = t(NEMO_F_E3V_B);
+  a.e3w_n = t(NEMO_F_E3W_N); a.e3f_n = t(NEMO_F_E3F_N); a.e3w_b = t(NEMO_F_E3W_B);
+  a.e3uw_n = t(NEMO_F_E3UW_N); a.e3vw_n = t(NEMO_F_E3VW_N); a.e3uw_b = t(NEMO_F_E3UW_B); a.e3vw_b = t(NEMO_F_E3VW_B);
+  a.e3uw_0 = t(NEMO_F_E3UW_0); a.e3vw_0 = t(NEMO_F_E3VW_0);
+  a.hu_a = t(NEMO_F_HU_A); a.hv_a = t(NEMO_F_HV_A); a.r1_hu_a = t(NEMO_F_R1_HU_A); a.r1_hv_a = t(NEMO_F_R1_HV_A);
+  a.hu_n = t(NEMO_F_HU_N); a.hv_n = t(NEMO_F_HV_N); a.r1_hu_n = t(NEMO_F_R1_HU_N); a.r1_hv_n = t(NEMO_F_R1_HV_N);
+  a.ht_n = t(NEMO_F_HT_N);
+  a.hu_b = t(NEMO_F_HU_B); a.hv_b = t(NEMO_F_HV_B); a.r1_hu_b = t(NEMO_F_R1_HU_B); a.r1_hv_b = t(NEMO_F_R1_HV_B);
+  a.gdept_n = t(NEMO_F_GDEPT_N); a.gdepw_n = t(NEMO_F_GDEPW_N); a.gde3w_n = t(NEMO_F_GDE3W_N);
+  a.gdept_b = t(NEMO_F_GDEPT_B); a.gdepw_b = t(NEMO_F_GDEPW_B);
+  a.ua = t(NEMO_F_UA); a.va = t(NEMO_F_VA); a.un = t(NEMO_F_UN); a.vn = t(NEMO_F_VN);
+  a.ub = t(NEMO_F_UB); a.vb = t(NEMO_F_VB);
+  a.un_b = t(NEMO_F_UN_B); a.vn_b = t(NEMO_F_VN_B); a.ub_b = t(NEMO_F_UB_B); a.vb_b = t(NEMO_F_VB_B);
+  a.ua_b = (const double*)F[NEMO_F_UA_B]; a.va_b = (const double*)F[NEMO_F_VA_B];
+  a.tsb = t(NEMO_F_TSB); a.tsn = t(NEMO_F_TSN); a.tsa = t(NEMO_F_TSA);
+  a.tsc = t(NEMO_F_SBC_TSC); a.tsc_b = t(NEMO_F_SBC_TSC_B); a.qsr_hc = t(NEMO_F_QSR_HC); a.qsr_hc_b = t(NEMO_F_QSR_HC_B);
+  a.atfp = (T)nm.rn_atfp;
+  const double zfact1 = nm.rn_atfp * nm.rn_rdt;   // tranxt.F90:294-295, dynnxt.F90:223, sshwzv.F90:255
+  a.zfact1 = (T)zfact1;
+  a.zfact2 = (T)(zfact1 * (1.0 / nm.rau0));
+  a.euler = nm.neuler == 0 && kt == nm.nit000;
+  a.vec = nm.ln_dynadv_vec;
+  a.traqsr = nm.ln_traqsr;
+  a.nksr = c->nksr;
+  return a;
+}
+
+enum { VVL_SF_NXT, VVL_SF_SWP, VVL_TRA_NXT, VVL_DYN_NXT, VVL_SSH_SWP };
+
+template <class T>
+int run_vvl(nemo_ctx* c, int kt, int what) {
+  const VvlArgs<T> a = vvl_args<T>(c, kt);
+  const Dom<T>& d0 = dom<T>(c);  // the rest-state scale factors
+  cudaError_t e = cudaSuccess;
+  switch (what) {
+    case VVL_SF_NXT: e = launch_vvl_sf_nxt<T>(d0, a, c->stream); break;
+    case VVL_SF_SWP: e = launch_vvl_sf_swp<T>(d0, a, c->stream); break;
+    case VVL_TRA_NXT: e = launch_tra_nxt_vvl<T>(d0, a, c->stream); break;
+    case VVL_DYN_NXT: e = launch_dyn_nxt_vvl<T>(d0, a, c->stream); break;
+    default: e = launch_ssh_swp_vvl<T>(d0, a, (T*)c->f[NEMO_F_SSHB], (T*)c->f[NEMO_F_SSHN], c->stream); break;
+  }
+  if (e != cudaSuccess) return cuda_fail(c, e, "z* time-stepping launch");
+  return NEMO_OK;
+}
+
+// the fields a z* routine reads or writes, and the pairs bound together
+int vvl_check(nemo_ctx* c, const char* what, std::initializer_list<int> ids) {
+  if (c->nam.ln_linssh) return fail(c, NEMO_ERR_ARG, "%s: variable volume only (ln_linssh = 0)", what);
+  for (int id : ids)
+    if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "%s: field %d must be bound", what, id);
+  if (!c->f[NEMO_F_RNF] != !c->f[NEMO_F_RNF_B]) return fail(c, NEMO_ERR_UNBOUND, "%s: bind both rnf and rnf_b", what);
   return NEMO_OK;
 }
 
@@ -2104,7 +2175,14 @@ int nemo_gpu_tra_nxt(nemo_ctx* c, int kt) {
   void* const* F = c->f;
   if (!F[NEMO_F_TSB] || !F[NEMO_F_TSN] || !F[NEMO_F_TSA])
     return fail(c, NEMO_ERR_UNBOUND, "tra_nxt: tsb, tsn and tsa must be bound");
-  if (!nm.ln_linssh) return fail(c, NEMO_ERR_ARG, "tra_nxt: linear free surface only (ln_linssh)");
+  if (!nm.ln_linssh) {  // tra_nxt_vvl
+    if (int s = vvl_check(c, "tra_nxt", {NEMO_F_E3T_B, NEMO_F_E3T_N, NEMO_F_E3T_A, NEMO_F_EMP, NEMO_F_EMP_B,
+                                         NEMO_F_SBC_TSC, NEMO_F_SBC_TSC_B}))
+      return s;
+    if (nm.ln_traqsr && (!F[NEMO_F_QSR_HC] || !F[NEMO_F_QSR_HC_B]))
+      return fail(c, NEMO_ERR_UNBOUND, "tra_nxt: qsr_hc and qsr_hc_b must be bound with ln_traqsr");
+    return c->prec == NEMO_PREC_FP64 ? run_vvl<double>(c, kt, VVL_TRA_NXT) : run_vvl<float>(c, kt, VVL_TRA_NXT);
+  }
   return c->prec == NEMO_PREC_FP64 ? run_tra_nxt<double>(c, kt) : run_tra_nxt<float>(c, kt);
 }
 
@@ -2307,6 +2385,17 @@ int nemo_gpu_dyn_zdf_step(nemo_ctx* c, int kt) {
 int nemo_gpu_dyn_nxt(nemo_ctx* c, int kt) {
   if (!c) return NEMO_ERR_ARG;
   if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (!c->nam.ln_linssh) {
+    if (!c->nam.ln_bt_fw) return fail(c, NEMO_ERR_UNSUPPORTED, "dyn_nxt: ln_bt_fw only");
+    if (int s = vvl_check(c, "dyn_nxt",
+                          {NEMO_F_UN, NEMO_F_VN, NEMO_F_UA, NEMO_F_VA, NEMO_F_UB, NEMO_F_VB, NEMO_F_UN_B, NEMO_F_VN_B,
+                           NEMO_F_UB_B, NEMO_F_VB_B, NEMO_F_UA_B, NEMO_F_VA_B, NEMO_F_E3T_B, NEMO_F_E3T_N,
+                           NEMO_F_E3T_A, NEMO_F_E3U_N, NEMO_F_E3V_N, NEMO_F_E3U_A, NEMO_F_E3V_A, NEMO_F_E3U_B,
+                           NEMO_F_E3V_B, NEMO_F_R1_HU_A, NEMO_F_R1_HV_A, NEMO_F_R1_HU_N, NEMO_F_R1_HV_N, NEMO_F_HU_B,
+                           NEMO_F_HV_B, NEMO_F_R1_HU_B, NEMO_F_R1_HV_B, NEMO_F_EMP, NEMO_F_EMP_B}))
+      return s;
+    return c->prec == NEMO_PREC_FP64 ? run_vvl<double>(c, kt, VVL_DYN_NXT) : run_vvl<float>(c, kt, VVL_DYN_NXT);
+  }
   if (int s = model_fields(c, "dyn_nxt")) return s;
   return c->prec == NEMO_PREC_FP64 ? run_dyn_nxt<double>(c, kt) : run_dyn_nxt<float>(c, kt);
 }
@@ -2405,8 +2494,39 @@ int nemo_gpu_ssh_swp(nemo_ctx* c, int kt) {
   if (join_copies(c)) return NEMO_ERR_CUDA;
   if (!c->f[NEMO_F_SSHB] || !c->f[NEMO_F_SSHN] || !c->f[NEMO_F_SSHA])
     return fail(c, NEMO_ERR_UNBOUND, "ssh_swp: sshb, sshn and ssha must be bound");
-  if (!c->nam.ln_linssh) return fail(c, NEMO_ERR_UNSUPPORTED, "ssh_swp: linear free surface only");
+  if (!c->nam.ln_linssh) {
+    if (int s = vvl_check(c, "ssh_swp", {NEMO_F_EMP, NEMO_F_EMP_B})) return s;
+    return c->prec == NEMO_PREC_FP64 ? run_vvl<double>(c, kt, VVL_SSH_SWP) : run_vvl<float>(c, kt, VVL_SSH_SWP);
+  }
   return c->prec == NEMO_PREC_FP64 ? run_ssh_swp<double>(c, kt) : run_ssh_swp<float>(c, kt);
+}
+
+int nemo_gpu_dom_vvl_sf_nxt(nemo_ctx* c, int kt) {
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (int s = vvl_check(c, "dom_vvl_sf_nxt",
+                        {NEMO_F_SSHA, NEMO_F_SSHB, NEMO_F_SSHN, NEMO_F_E3T_B, NEMO_F_E3T_N, NEMO_F_E3T_A, NEMO_F_E3U_A,
+                         NEMO_F_E3V_A, NEMO_F_HU_A, NEMO_F_HV_A, NEMO_F_R1_HU_A, NEMO_F_R1_HV_A}))
+    return s;
+  return c->prec == NEMO_PREC_FP64 ? run_vvl<double>(c, kt, VVL_SF_NXT) : run_vvl<float>(c, kt, VVL_SF_NXT);
+}
+
+int nemo_gpu_dom_vvl_sf_swp(nemo_ctx* c, int kt) {
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (int s = vvl_check(c, "dom_vvl_sf_swp",
+                        {NEMO_F_E3T_B, NEMO_F_E3T_N, NEMO_F_E3T_A, NEMO_F_E3U_N, NEMO_F_E3V_N, NEMO_F_E3W_N,
+                         NEMO_F_E3U_A, NEMO_F_E3V_A, NEMO_F_SSHN, NEMO_F_HU_A, NEMO_F_HV_A, NEMO_F_R1_HU_A,
+                         NEMO_F_R1_HV_A, NEMO_F_HU_N, NEMO_F_HV_N, NEMO_F_R1_HU_N, NEMO_F_R1_HV_N, NEMO_F_HT_N}))
+    return s;
+  void* const* F = c->f;
+  if ((F[NEMO_F_E3UW_N] || F[NEMO_F_E3UW_B]) && !F[NEMO_F_E3UW_0])
+    return fail(c, NEMO_ERR_UNBOUND, "dom_vvl_sf_swp: e3uw_0 must be bound with e3uw_n or e3uw_b");
+  if ((F[NEMO_F_E3VW_N] || F[NEMO_F_E3VW_B]) && !F[NEMO_F_E3VW_0])
+    return fail(c, NEMO_ERR_UNBOUND, "dom_vvl_sf_swp: e3vw_0 must be bound with e3vw_n or e3vw_b");
+  if ((F[NEMO_F_E3UW_B] && !F[NEMO_F_E3U_B]) || (F[NEMO_F_E3VW_B] && !F[NEMO_F_E3V_B]))
+    return fail(c, NEMO_ERR_UNBOUND, "dom_vvl_sf_swp: e3u_b, e3v_b must be bound with e3uw_b, e3vw_b");
+  return c->prec == NEMO_PREC_FP64 ? run_vvl<double>(c, kt, VVL_SF_SWP) : run_vvl<float>(c, kt, VVL_SF_SWP);
 }
 
 // ---------------------------------------------------------------------- adjoint

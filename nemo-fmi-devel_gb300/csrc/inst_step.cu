@@ -40,6 +40,39 @@ cudaError_t launch_ssh_swp(const Dom<T>& d, T* sshb, T* sshn, const double* ssha
 }
 
 template <class T>
+cudaError_t launch_vvl_sf_nxt(const Dom<T>& d, const VvlArgs<T>& a, cudaStream_t s) {
+  k_vvl_sf_nxt_t<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a);
+  k_vvl_sf_nxt_uv<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a);
+  ktick(NEMO_K_VVL_SF, s);
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_vvl_sf_swp(const Dom<T>& d, const VvlArgs<T>& a, cudaStream_t s) {
+  k_vvl_sf_swp<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a);
+  ktick(NEMO_K_VVL_SF, s);
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_tra_nxt_vvl(const Dom<T>& d, const VvlArgs<T>& a, cudaStream_t s) {
+  k_tra_nxt_vvl<T><<<s_pt(d), dim3(SX, SY), 0, s>>>(d, a);
+  ktick(NEMO_K_VVL_NXT, s);
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_dyn_nxt_vvl(const Dom<T>& d, const VvlArgs<T>& a, cudaStream_t s) {
+  k_dyn_nxt_vvl_a<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a);
+  k_dyn_nxt_vvl_b<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a);
+  ktick(NEMO_K_VVL_NXT, s);
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_ssh_swp_vvl(const Dom<T>& d, const VvlArgs<T>& a, T* sshb, T* sshn, cudaStream_t s) {
+  k_ssh_swp_vvl<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a, sshb, sshn);
+  ktick(NEMO_K_VVL_NXT, s);
+  return cudaGetLastError();
+}
+
+template <class T>
 cudaError_t launch_ldf_slp(const Dom<T>& d, const SlpArgs<T>& a, cudaStream_t s) {
   k_slp_mxl<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a);
   k_slp_pre<T><<<s_pt(d), dim3(SX, SY), 0, s>>>(d, a);
@@ -194,6 +227,11 @@ cudaError_t launch_dia_hsb(const Dom<T>& d, const HsbArgs<T>& a, double* part, i
   template cudaError_t launch_dyn_zdf_step<T>(const Dom<T>&, const T*, const T*, T*, T*, T, cudaStream_t);     \
   template cudaError_t launch_dyn_nxt<T>(const Dom<T>&, const NxtArgs<T, double>&, cudaStream_t);              \
   template cudaError_t launch_ssh_swp<T>(const Dom<T>&, T*, T*, const double*, T, int, cudaStream_t);      \
+  template cudaError_t launch_vvl_sf_nxt<T>(const Dom<T>&, const VvlArgs<T>&, cudaStream_t);                \
+  template cudaError_t launch_vvl_sf_swp<T>(const Dom<T>&, const VvlArgs<T>&, cudaStream_t);                \
+  template cudaError_t launch_tra_nxt_vvl<T>(const Dom<T>&, const VvlArgs<T>&, cudaStream_t);               \
+  template cudaError_t launch_dyn_nxt_vvl<T>(const Dom<T>&, const VvlArgs<T>&, cudaStream_t);               \
+  template cudaError_t launch_ssh_swp_vvl<T>(const Dom<T>&, const VvlArgs<T>&, T*, T*, cudaStream_t);       \
   template cudaError_t launch_ldf_slp<T>(const Dom<T>&, const SlpArgs<T>&, cudaStream_t);                  \
   template cudaError_t launch_zps_hde_rd<T>(const Dom<T>&, const EosArgs<T>&, const T*, T*, T*, cudaStream_t);  \
   template cudaError_t launch_zps_hde<T>(const Dom<T>&, const T*, T*, T*, int, cudaStream_t);             \

@@ -3,6 +3,7 @@
 #pragma once
 #include "k_diag.cuh"
 #include "k_tra.cuh"
+#include "k_vvl.cuh"
 
 namespace nemo {
 
@@ -157,6 +158,17 @@ template <class T>
 cudaError_t launch_dyn_nxt(const Dom<T>& d, const NxtArgs<T, double>& a, cudaStream_t s);
 template <class T>
 cudaError_t launch_ssh_swp(const Dom<T>& d, T* sshb, T* sshn, const double* ssha, T atfp, int euler, cudaStream_t s);
+// z* time stepping (k_vvl.cuh); d0: the domain with the rest-state scale factors
+template <class T>
+cudaError_t launch_vvl_sf_nxt(const Dom<T>& d0, const VvlArgs<T>& a, cudaStream_t s);
+template <class T>
+cudaError_t launch_vvl_sf_swp(const Dom<T>& d0, const VvlArgs<T>& a, cudaStream_t s);
+template <class T>
+cudaError_t launch_tra_nxt_vvl(const Dom<T>& d0, const VvlArgs<T>& a, cudaStream_t s);
+template <class T>
+cudaError_t launch_dyn_nxt_vvl(const Dom<T>& d0, const VvlArgs<T>& a, cudaStream_t s);
+template <class T>
+cudaError_t launch_ssh_swp_vvl(const Dom<T>& d0, const VvlArgs<T>& a, T* sshb, T* sshn, cudaStream_t s);
 // stp_ctl: block partials part (nblk x nmem records), results out (32 doubles a member)
 template <class T>
 cudaError_t launch_stp_ctl(const Dom<T>& d, const T* sshn, const T* un, const T* ts, double* part, int nblk,

@@ -151,6 +151,7 @@ def load(path):
     _proto(lib, "nemo_gpu_dyn_zad", i, [vp, i])
     for name in ("nemo_gpu_tra_sbc", "nemo_gpu_tra_qsr", "nemo_gpu_dyn_hpg", "nemo_gpu_zdf_mxl",
                  "nemo_gpu_wzv", "nemo_gpu_dyn_zdf_step", "nemo_gpu_dyn_nxt", "nemo_gpu_ssh_swp",
+                 "nemo_gpu_dom_vvl_sf_nxt", "nemo_gpu_dom_vvl_sf_swp",
                  "nemo_gpu_stp_model", "nemo_gpu_zdf_phy", "nemo_gpu_usrdef_sbc"):
         _proto(lib, name, i, [vp, i])
     _proto(lib, "nemo_gpu_tra_adv_fct_adj", i, [vp, i, i, cp, d, vp, vp, vp, vp, vp, vp, i, i, i])

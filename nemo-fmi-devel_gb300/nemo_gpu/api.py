@@ -259,6 +259,12 @@ class Context:
     def ssh_swp(self, kt):
         self._ck(self.lib.nemo_gpu_ssh_swp(self.h, kt), "ssh_swp")
 
+    def dom_vvl_sf_nxt(self, kt):
+        self._ck(self.lib.nemo_gpu_dom_vvl_sf_nxt(self.h, kt), "dom_vvl_sf_nxt")
+
+    def dom_vvl_sf_swp(self, kt):
+        self._ck(self.lib.nemo_gpu_dom_vvl_sf_swp(self.h, kt), "dom_vvl_sf_swp")
+
     def tra_sbc(self, kt):
         self._ck(self.lib.nemo_gpu_tra_sbc(self.h, kt), "tra_sbc")
 

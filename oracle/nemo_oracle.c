@@ -2890,19 +2890,68 @@ int ora_tra_zdf_imp_adj(ora_ctx *c, int kt, int kit000, const char *cdtype, doub
 }
 
 /* ---------------------------------------------------------------- tra_nxt */
-/* tranxt.F90:66-188 with tra_nxt_fix (:191-237) on the bound tsb, tsn, tsa
- * (linear free surface; no trend diagnostics, bdy or agrif). */
+/* tra_nxt_vvl (tranxt.F90:240-380) for the active tracers, p2dt = rdt as tra_nxt
+ * passes it (:161): the thickness-weighted Asselin filter with the forcing removed at
+ * the first level (emp, rnf without ln_rnf_depth, sbc_tsc) and in the levels of
+ * penetrating light (qsr_hc, ln_traqsr); no ice-shelf melt, no tracer runoff. */
+static int tra_nxt_vvl(ora_ctx *c, double *tsb, double *tsn, const double *tsa) {
+  const nemo_namelist *nm = &c->nam;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  const double *e3t_b = c->f[NEMO_F_E3T_B], *e3t_n = c->f[NEMO_F_E3T_N], *e3t_a = c->f[NEMO_F_E3T_A];
+  const double *emp = c->f[NEMO_F_EMP], *emp_b = c->f[NEMO_F_EMP_B];
+  const double *rnf = c->f[NEMO_F_RNF], *rnf_b = c->f[NEMO_F_RNF_B];
+  const double *tsc = c->f[NEMO_F_SBC_TSC], *tsc_b = c->f[NEMO_F_SBC_TSC_B];
+  const double *hc = c->f[NEMO_F_QSR_HC], *hc_b = c->f[NEMO_F_QSR_HC_B];
+  if (!e3t_b || !e3t_n || !e3t_a || !emp || !emp_b || !tsc || !tsc_b) return NEMO_ERR_UNBOUND;
+  if ((rnf == NULL) != (rnf_b == NULL)) return NEMO_ERR_UNBOUND;
+  if (nm->ln_traqsr && (!hc || !hc_b)) return NEMO_ERR_UNBOUND;
+  const double atfp = nm->rn_atfp, r1_rau0 = 1.0 / nm->rau0;
+  const double zfact1 = atfp * nm->rn_rdt, zfact2 = zfact1 * r1_rau0;   /* :293-295 */
+  for (int jn = 1; jn <= 2; ++jn)
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          const size_t p = I2(ji, jj), q = I3(ji, jj, jk), o = q + n3 * (jn - 1);
+          const double ze3t_b = e3t_b[q], ze3t_n = e3t_n[q], ze3t_a = e3t_a[q];
+          const double ztc_b = tsb[o] * ze3t_b, ztc_n = tsn[o] * ze3t_n, ztc_a = tsa[o] * ze3t_a;
+          const double ze3t_d = ze3t_a - 2. * ze3t_n + ze3t_b;
+          const double ztc_d = ztc_a - 2. * ztc_n + ztc_b;
+          double ze3t_f = ze3t_n + atfp * ze3t_d;
+          double ztc_f = ztc_n + atfp * ztc_d;
+          if (jk == c->mikt[p]) {                               /* :314-319 */
+            ze3t_f = ze3t_f - zfact2 * (emp_b[p] - emp[p]);
+            ztc_f = ztc_f - zfact1 * (tsc[p + n2 * (jn - 1)] - tsc_b[p + n2 * (jn - 1)]);
+            if (rnf) ze3t_f = ze3t_f - zfact2 * (-(rnf_b[p] - rnf[p]));   /* :325-329 */
+          }
+          if (nm->ln_traqsr && jn == 1 && jk <= c->nksr)        /* :333-334 */
+            ztc_f = ztc_f - zfact1 * (hc[q] - hc_b[q]);
+          ze3t_f = 1.e0 / ze3t_f;
+          tsb[o] = ztc_f * ze3t_f;
+          tsn[o] = tsa[o];
+        }
+  return NEMO_OK;
+}
+
+/* tranxt.F90:66-188 with tra_nxt_fix (:191-237) or, with a variable volume,
+ * tra_nxt_vvl on the bound tsb, tsn, tsa (no trend diagnostics, bdy or agrif). */
 int ora_tra_nxt(ora_ctx *c, int kt) {
   const nemo_namelist *nm = &c->nam;
   const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
   const size_t n3 = (size_t)jpi * jpj * jpk;
   double *tsb = c->f[NEMO_F_TSB], *tsn = c->f[NEMO_F_TSN], *tsa = c->f[NEMO_F_TSA];
   if (!tsb || !tsn || !tsa) return NEMO_ERR_UNBOUND;
-  if (!nm->ln_linssh) return NEMO_ERR_ARG;
   lbc_closed(jpi, jpj, tsa, 2 * jpk, 'T', 0.0);          /* :109 */
   if (nm->neuler == 0 && kt == nm->nit000) {               /* :144-149 Euler: swap only */
     for (int jn = 0; jn < 2; ++jn)
       memcpy(tsn + n3 * jn, tsa + n3 * jn, (n3 - (size_t)jpi * jpj) * sizeof(double));
+    return NEMO_OK;
+  }
+  if (!nm->ln_linssh) {                                     /* :160-162 */
+    const int st = tra_nxt_vvl(c, tsb, tsn, tsa);
+    if (st) return st;
+    lbc_closed(jpi, jpj, tsb, 2 * jpk, 'T', 0.0);
+    lbc_closed(jpi, jpj, tsn, 2 * jpk, 'T', 0.0);
     return NEMO_OK;
   }
   const double atfp = nm->rn_atfp;
@@ -3107,11 +3156,160 @@ int ora_dyn_zdf_step(ora_ctx *c, int kt) {
   return NEMO_OK;
 }
 
-/* dyn_nxt (dynnxt.F90:66-377): linear free surface, ln_dynspg_ts with ln_bt_fw. */
+/* ----------------------------------------------------- z* scale factors */
+/* dom_vvl_interpol (domvvl.F90:678-782) without wetting and drying (zlnwd = 0): the
+ * scale factor at the out point is its rest state plus the change of pe3_in,
+ * surface-weighted between two neighbours ('U', 'V', 'F', then lbc_lnk) or averaged
+ * between two levels ('W', 'UW', 'VW'). */
+static int vvl_interpol(const ora_ctx *c, const double *in, double *out, char pout, int w) {
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj;
+  if (!w) {                                               /* U, V, F: :705-742 */
+    const double *in0 = pout == 'F' ? c->e3u_0 : c->e3t_0;
+    const double *out0 = pout == 'U' ? c->e3u_0 : pout == 'V' ? c->e3v_0 : c->e3f_0;
+    for (int jk = 1; jk <= jpk; ++jk)
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          const size_t p = I2(ji, jj), q = I3(ji, jj, jk);
+          if (pout == 'U') {
+            const size_t p1 = I2(ji + 1, jj), q1 = I3(ji + 1, jj, jk);
+            out[q] = 0.5 * (c->umask[q] * (1.0 - 0.0) + 0.0) * c->r1_e1e2u[p] *
+                     (c->e1e2t[p] * (in[q] - in0[q]) + c->e1e2t[p1] * (in[q1] - in0[q1]));
+          } else if (pout == 'V') {
+            const size_t p1 = I2(ji, jj + 1), q1 = I3(ji, jj + 1, jk);
+            out[q] = 0.5 * (c->vmask[q] * (1.0 - 0.0) + 0.0) * c->r1_e1e2v[p] *
+                     (c->e1e2t[p] * (in[q] - in0[q]) + c->e1e2t[p1] * (in[q1] - in0[q1]));
+          } else {
+            const size_t p1 = I2(ji, jj + 1), q1 = I3(ji, jj + 1, jk);
+            const double r1_e1e2f = 1.0 / (c->e1f[p] * c->e2f[p]);
+            out[q] = 0.5 * (c->umask[q] * c->umask[q1] * (1.0 - 0.0) + 0.0) * r1_e1e2f *
+                     (c->e1e2u[p] * (in[q] - in0[q]) + c->e1e2u[p1] * (in[q1] - in0[q1]));
+          }
+        }
+    lbc_closed(jpi, jpj, out, jpk, pout, 0.0);
+    for (size_t q = 0; q < n2 * jpk; ++q) out[q] = out[q] + out0[q];
+    return NEMO_OK;
+  }
+  /* W, UW, VW: :744-779 */
+  const double *out0 = pout == 'W' ? c->e3w_0 : pout == 'U' ? c->f[NEMO_F_E3UW_0] : c->f[NEMO_F_E3VW_0];
+  const double *in0 = pout == 'W' ? c->e3t_0 : pout == 'U' ? c->e3u_0 : c->e3v_0;
+  const double *msk = pout == 'W' ? c->tmask : pout == 'U' ? c->umask : c->vmask;
+  if (!out0) return NEMO_ERR_UNBOUND;
+  for (size_t p = 0; p < n2; ++p) out[p] = out0[p] + in[p] - in0[p];
+  for (int jk = 2; jk <= jpk; ++jk)
+    for (size_t p = 0; p < n2; ++p) {
+      const size_t q = p + n2 * (jk - 1), qm = q - n2;
+      const double m = msk[q] * (1.0 - 0.0) + 0.0;
+      out[q] = out0[q] + (1.0 - 0.5 * m) * (in[qm] - in0[qm]) + 0.5 * m * (in[q] - in0[q]);
+    }
+  return NEMO_OK;
+}
+
+/* a column depth and its masked inverse: h = sum of e3 mask over the levels 1..jpkm1,
+ * r1_h = ssmask / (h + 1 - ssmask) (domvvl.F90:549-558) */
+static void vvl_depth(const ora_ctx *c, const double *e3, const double *msk, const double *ssm, double *h,
+                      double *r1_h) {
+  const size_t n2 = (size_t)c->jpi * c->jpj;
+  for (size_t p = 0; p < n2; ++p) h[p] = e3[p] * msk[p];
+  for (int jk = 2; jk <= c->jpk - 1; ++jk)
+    for (size_t p = 0; p < n2; ++p) h[p] = h[p] + e3[p + n2 * (jk - 1)] * msk[p + n2 * (jk - 1)];
+  if (r1_h)
+    for (size_t p = 0; p < n2; ++p) r1_h[p] = ssm[p] / (h[p] + 1.0 - ssm[p]);
+}
+
+/* dom_vvl_sf_nxt (domvvl.F90:268-562), z*: the after scale factors from the ssh
+ * increment (:323-327), at u- and v-points (:542-543), the after column depths. */
+int ora_dom_vvl_sf_nxt(ora_ctx *c, int kt) {
+  (void)kt;
+  double **F = c->f;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj;
+  if (c->nam.ln_linssh) return NEMO_ERR_ARG;
+  const double *ssha = F[NEMO_F_SSHA], *sshb = F[NEMO_F_SSHB], *sshn = F[NEMO_F_SSHN];
+  const double *e3t_b = F[NEMO_F_E3T_B], *e3t_n = F[NEMO_F_E3T_N];
+  double *e3t_a = F[NEMO_F_E3T_A], *e3u_a = F[NEMO_F_E3U_A], *e3v_a = F[NEMO_F_E3V_A];
+  double *hu_a = F[NEMO_F_HU_A], *hv_a = F[NEMO_F_HV_A], *r1_hu_a = F[NEMO_F_R1_HU_A], *r1_hv_a = F[NEMO_F_R1_HV_A];
+  if (!ssha || !sshb || !sshn || !e3t_b || !e3t_n || !e3t_a || !e3u_a || !e3v_a || !hu_a || !hv_a || !r1_hu_a ||
+      !r1_hv_a)
+    return NEMO_ERR_UNBOUND;
+  (void)jpi; (void)jpj;
+  for (size_t p = 0; p < n2; ++p) {
+    const double z_scale = (ssha[p] - sshb[p]) * c->ssmask[p] / (c->ht_0[p] + sshn[p] + 1. - c->ssmask[p]);
+    for (int jk = 1; jk <= jpk - 1; ++jk) {
+      const size_t q = p + n2 * (jk - 1);
+      e3t_a[q] = e3t_b[q] + e3t_n[q] * z_scale * c->tmask[q];
+    }
+  }
+  vvl_interpol(c, e3t_a, e3u_a, 'U', 0);
+  vvl_interpol(c, e3t_a, e3v_a, 'V', 0);
+  vvl_depth(c, e3u_a, c->umask, c->ssumask, hu_a, r1_hu_a);
+  vvl_depth(c, e3v_a, c->vmask, c->ssvmask, hv_a, r1_hv_a);
+  return NEMO_OK;
+}
+
+/* dom_vvl_sf_swp (domvvl.F90:565-675), z*: the swap of the scale factors, the now
+ * and before e3 at w-, f-, uw- and vw-points, the now depths and column depths. The
+ * optional outputs are formed when bound. */
+int ora_dom_vvl_sf_swp(ora_ctx *c, int kt) {
+  (void)kt;
+  double **F = c->f;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  if (c->nam.ln_linssh) return NEMO_ERR_ARG;
+  double *e3t_n = F[NEMO_F_E3T_N], *e3u_n = F[NEMO_F_E3U_N], *e3v_n = F[NEMO_F_E3V_N], *e3w_n = F[NEMO_F_E3W_N];
+  const double *e3t_a = F[NEMO_F_E3T_A], *e3u_a = F[NEMO_F_E3U_A], *e3v_a = F[NEMO_F_E3V_A], *e3t_b = F[NEMO_F_E3T_B];
+  const double *sshn = F[NEMO_F_SSHN];
+  if (!e3t_n || !e3u_n || !e3v_n || !e3w_n || !e3t_a || !e3u_a || !e3v_a || !e3t_b || !sshn || !F[NEMO_F_HU_A] ||
+      !F[NEMO_F_HV_A] || !F[NEMO_F_R1_HU_A] || !F[NEMO_F_R1_HV_A] || !F[NEMO_F_HU_N] || !F[NEMO_F_HV_N] ||
+      !F[NEMO_F_R1_HU_N] || !F[NEMO_F_R1_HV_N] || !F[NEMO_F_HT_N])
+    return NEMO_ERR_UNBOUND;
+  if ((F[NEMO_F_E3UW_N] || F[NEMO_F_E3UW_B]) && !F[NEMO_F_E3UW_0]) return NEMO_ERR_UNBOUND;
+  if ((F[NEMO_F_E3VW_N] || F[NEMO_F_E3VW_B]) && !F[NEMO_F_E3VW_0]) return NEMO_ERR_UNBOUND;
+  if ((F[NEMO_F_E3UW_B] && !F[NEMO_F_E3U_B]) || (F[NEMO_F_E3VW_B] && !F[NEMO_F_E3V_B])) return NEMO_ERR_UNBOUND;
+  double *gdept = F[NEMO_F_GDEPT_N], *gdepw = F[NEMO_F_GDEPW_N], *gde3w = F[NEMO_F_GDE3W_N];
+  if (F[NEMO_F_GDEPT_B] && gdept) memcpy(F[NEMO_F_GDEPT_B], gdept, n3 * sizeof(double));   /* :617-618 */
+  if (F[NEMO_F_GDEPW_B] && gdepw) memcpy(F[NEMO_F_GDEPW_B], gdepw, n3 * sizeof(double));
+  memcpy(e3t_n, e3t_a, n3 * sizeof(double));                                               /* :620-622 */
+  memcpy(e3u_n, e3u_a, n3 * sizeof(double));
+  memcpy(e3v_n, e3v_a, n3 * sizeof(double));
+  if (F[NEMO_F_E3F_N]) vvl_interpol(c, e3u_n, F[NEMO_F_E3F_N], 'F', 0);                     /* :631 */
+  vvl_interpol(c, e3t_n, e3w_n, 'W', 1);                                                    /* :634-640 */
+  if (F[NEMO_F_E3UW_N]) vvl_interpol(c, e3u_n, F[NEMO_F_E3UW_N], 'U', 1);
+  if (F[NEMO_F_E3VW_N]) vvl_interpol(c, e3v_n, F[NEMO_F_E3VW_N], 'V', 1);
+  if (F[NEMO_F_E3W_B]) vvl_interpol(c, e3t_b, F[NEMO_F_E3W_B], 'W', 1);
+  if (F[NEMO_F_E3UW_B]) vvl_interpol(c, F[NEMO_F_E3U_B], F[NEMO_F_E3UW_B], 'U', 1);
+  if (F[NEMO_F_E3VW_B]) vvl_interpol(c, F[NEMO_F_E3V_B], F[NEMO_F_E3VW_B], 'V', 1);
+  if (gdept && gdepw) {                                                                     /* :642-657 */
+    for (size_t p = 0; p < n2; ++p) {
+      gdept[p] = 0.5 * e3w_n[p];
+      gdepw[p] = 0.0;
+      if (gde3w) gde3w[p] = gdept[p] - sshn[p];
+    }
+    for (int jk = 2; jk <= jpk; ++jk)
+      for (size_t p = 0; p < n2; ++p) {
+        const size_t q = p + n2 * (jk - 1), qm = q - n2;
+        const double zcoef = c->tmask[q] - c->wmask[q];
+        gdepw[q] = gdepw[qm] + e3t_n[qm];
+        gdept[q] = zcoef * (gdepw[q] + 0.5 * e3w_n[q]) + (1 - zcoef) * (gdept[qm] + e3w_n[q]);
+        if (gde3w) gde3w[q] = gdept[q] - sshn[p];
+      }
+  }
+  memcpy(F[NEMO_F_HU_N], F[NEMO_F_HU_A], n2 * sizeof(double));                              /* :661-662 */
+  memcpy(F[NEMO_F_R1_HU_N], F[NEMO_F_R1_HU_A], n2 * sizeof(double));
+  memcpy(F[NEMO_F_HV_N], F[NEMO_F_HV_A], n2 * sizeof(double));
+  memcpy(F[NEMO_F_R1_HV_N], F[NEMO_F_R1_HV_A], n2 * sizeof(double));
+  vvl_depth(c, e3t_n, c->tmask, NULL, F[NEMO_F_HT_N], NULL);                                /* :664-667 */
+  return NEMO_OK;
+}
+
+/* dyn_nxt (dynnxt.F90:66-377) with ln_dynspg_ts and ln_bt_fw; with a variable
+ * volume the after e3 and column depths of dom_vvl_sf_nxt, the time filter of e3t_b
+ * (:217-226, runoff only with ln_rnf: not on this path), e3u_b / e3v_b from it, and
+ * the filter on the velocity (ln_dynadv_vec) or on the thickness-weighted velocity. */
 int ora_dyn_nxt(ora_ctx *c, int kt) {
   const nemo_namelist *nm = &c->nam;
   const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
-  const size_t n2 = (size_t)jpi * jpj;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
   double **F = c->f;
   double *ua = F[NEMO_F_UA], *va = F[NEMO_F_VA], *un = F[NEMO_F_UN], *vn = F[NEMO_F_VN];
   double *ub = F[NEMO_F_UB], *vb = F[NEMO_F_VB];
@@ -3119,85 +3317,151 @@ int ora_dyn_nxt(ora_ctx *c, int kt) {
   const double *ua_b = F[NEMO_F_UA_B], *va_b = F[NEMO_F_VA_B];
   if (!ua || !va || !un || !vn || !ub || !vb || !un_b || !vn_b || !ub_b || !vb_b || !ua_b || !va_b)
     return NEMO_ERR_UNBOUND;
-  if (!nm->ln_linssh || !nm->ln_bt_fw) return NEMO_ERR_ARG;
-  const double *e3u = c->e3u_0, *e3v = c->e3v_0, *umask = c->umask, *vmask = c->vmask;
+  if (!nm->ln_bt_fw) return NEMO_ERR_ARG;
+  const int vvl = !nm->ln_linssh;
+  const double *umask = c->umask, *vmask = c->vmask;
+  const double *e3u_a = c->e3u_0, *e3v_a = c->e3v_0, *r1_hu_a = c->r1_hu_0, *r1_hv_a = c->r1_hv_0;
+  const double *r1_hu_n = c->r1_hu_0, *r1_hv_n = c->r1_hv_0;
+  double *e3u_b = c->e3u_0, *e3v_b = c->e3v_0, *r1_hu_b = c->r1_hu_0, *r1_hv_b = c->r1_hv_0;
+  if (vvl) {
+    const int need[] = {NEMO_F_E3T_B, NEMO_F_E3T_N, NEMO_F_E3T_A, NEMO_F_E3U_N, NEMO_F_E3V_N, NEMO_F_E3U_A,
+                        NEMO_F_E3V_A, NEMO_F_E3U_B, NEMO_F_E3V_B, NEMO_F_R1_HU_A, NEMO_F_R1_HV_A, NEMO_F_R1_HU_N,
+                        NEMO_F_R1_HV_N, NEMO_F_HU_B, NEMO_F_HV_B, NEMO_F_R1_HU_B, NEMO_F_R1_HV_B, NEMO_F_EMP,
+                        NEMO_F_EMP_B};
+    for (size_t i = 0; i < sizeof need / sizeof need[0]; ++i)
+      if (!F[need[i]]) return NEMO_ERR_UNBOUND;
+    e3u_a = F[NEMO_F_E3U_A]; e3v_a = F[NEMO_F_E3V_A]; r1_hu_a = F[NEMO_F_R1_HU_A]; r1_hv_a = F[NEMO_F_R1_HV_A];
+    r1_hu_n = F[NEMO_F_R1_HU_N]; r1_hv_n = F[NEMO_F_R1_HV_N];
+    e3u_b = F[NEMO_F_E3U_B]; e3v_b = F[NEMO_F_E3V_B]; r1_hu_b = F[NEMO_F_R1_HU_B]; r1_hv_b = F[NEMO_F_R1_HV_B];
+  }
   const double atfp = nm->rn_atfp;
   double *zue = zalloc(n2), *zve = zalloc(n2);
   /* (:114-126) the barotropic part of the after velocity from the sub-steps */
-  for (size_t p = 0; p < n2; ++p) { zue[p] = e3u[p] * ua[p] * umask[p]; zve[p] = e3v[p] * va[p] * vmask[p]; }
+  for (size_t p = 0; p < n2; ++p) { zue[p] = e3u_a[p] * ua[p] * umask[p]; zve[p] = e3v_a[p] * va[p] * vmask[p]; }
   for (int jk = 2; jk <= jpk - 1; ++jk)
     for (size_t p = 0; p < n2; ++p) {
       size_t q = p + n2 * (jk - 1);
-      zue[p] = zue[p] + e3u[q] * ua[q] * umask[q];
-      zve[p] = zve[p] + e3v[q] * va[q] * vmask[q];
+      zue[p] = zue[p] + e3u_a[q] * ua[q] * umask[q];
+      zve[p] = zve[p] + e3v_a[q] * va[q] * vmask[q];
     }
   for (int jk = 1; jk <= jpk - 1; ++jk)
     for (size_t p = 0; p < n2; ++p) {
       size_t q = p + n2 * (jk - 1);
-      ua[q] = (ua[q] - zue[p] * c->r1_hu_0[p] + ua_b[p]) * umask[q];
-      va[q] = (va[q] - zve[p] * c->r1_hv_0[p] + va_b[p]) * vmask[q];
+      ua[q] = (ua[q] - zue[p] * r1_hu_a[p] + ua_b[p]) * umask[q];
+      va[q] = (va[q] - zve[p] * r1_hv_a[p] + va_b[p]) * vmask[q];
     }
   lbc_closed(jpi, jpj, ua, jpk, 'U', 0.0);                    /* :146 */
   lbc_closed(jpi, jpj, va, jpk, 'V', 0.0);
   if (nm->neuler == 0 && kt == nm->nit000) {                 /* :168-188 Euler: swap only */
     memcpy(un, ua, (size_t)(jpk - 1) * n2 * sizeof(double));
     memcpy(vn, va, (size_t)(jpk - 1) * n2 * sizeof(double));
-  } else {                                                    /* :195-211 Asselin filter and swap */
-    for (int jk = 1; jk <= jpk - 1; ++jk)
-      for (size_t p = 0; p < n2; ++p) {
-        size_t q = p + n2 * (jk - 1);
-        double zuf = un[q] + atfp * (ub[q] - 2.0 * un[q] + ua[q]);
-        double zvf = vn[q] + atfp * (vb[q] - 2.0 * vn[q] + va[q]);
+    if (vvl) {                                                /* :172-186 */
+      memcpy(F[NEMO_F_E3T_N], F[NEMO_F_E3T_A], (size_t)(jpk - 1) * n2 * sizeof(double));
+      memcpy(F[NEMO_F_E3U_N], F[NEMO_F_E3U_A], (size_t)(jpk - 1) * n2 * sizeof(double));
+      memcpy(F[NEMO_F_E3V_N], F[NEMO_F_E3V_A], (size_t)(jpk - 1) * n2 * sizeof(double));
+    }
+  } else {
+    double *ze3u_f = NULL, *ze3v_f = NULL;
+    if (vvl) {                                                /* :217-226 e3t_b filtered */
+      double *e3t_b = F[NEMO_F_E3T_B];
+      const double *e3t_n = F[NEMO_F_E3T_N], *e3t_a = F[NEMO_F_E3T_A];
+      for (size_t q = 0; q < n3 - n2; ++q) e3t_b[q] = e3t_n[q] + atfp * (e3t_b[q] - 2. * e3t_n[q] + e3t_a[q]);
+      const double zcoef = atfp * nm->rn_rdt * (1.0 / nm->rau0);
+      const double *emp = F[NEMO_F_EMP], *emp_b = F[NEMO_F_EMP_B];
+      for (size_t p = 0; p < n2; ++p) e3t_b[p] = e3t_b[p] - zcoef * (emp_b[p] - emp[p]) * c->tmask[p];
+      if (nm->ln_dynadv_vec) {                                /* :262-263 */
+        vvl_interpol(c, e3t_b, e3u_b, 'U', 0);
+        vvl_interpol(c, e3t_b, e3v_b, 'V', 0);
+      } else {                                                /* :282-283 */
+        ze3u_f = walloc(n3); ze3v_f = walloc(n3);
+        vvl_interpol(c, e3t_b, ze3u_f, 'U', 0);
+        vvl_interpol(c, e3t_b, ze3v_f, 'V', 0);
+      }
+    }
+    if (!ze3u_f) {                                            /* :195-211, :264-276 */
+      for (int jk = 1; jk <= jpk - 1; ++jk)
+        for (size_t p = 0; p < n2; ++p) {
+          size_t q = p + n2 * (jk - 1);
+          double zuf = un[q] + atfp * (ub[q] - 2.0 * un[q] + ua[q]);
+          double zvf = vn[q] + atfp * (vb[q] - 2.0 * vn[q] + va[q]);
+          ub[q] = zuf; vb[q] = zvf;
+          un[q] = ua[q]; vn[q] = va[q];
+        }
+    } else {                                                  /* :284-305 thickness-weighted */
+      const double *e3u_n = F[NEMO_F_E3U_N], *e3v_n = F[NEMO_F_E3V_N];
+      for (size_t q = 0; q < n3 - n2; ++q) {
+        const double zue3a = e3u_a[q] * ua[q], zve3a = e3v_a[q] * va[q];
+        const double zue3n = e3u_n[q] * un[q], zve3n = e3v_n[q] * vn[q];
+        const double zue3b = e3u_b[q] * ub[q], zve3b = e3v_b[q] * vb[q];
+        const double zuf = (zue3n + atfp * (zue3b - 2. * zue3n + zue3a)) / ze3u_f[q];
+        const double zvf = (zve3n + atfp * (zve3b - 2. * zve3n + zve3a)) / ze3v_f[q];
         ub[q] = zuf; vb[q] = zvf;
         un[q] = ua[q]; vn[q] = va[q];
       }
+      memcpy(e3u_b, ze3u_f, (n3 - n2) * sizeof(double));      /* :304-305 */
+      memcpy(e3v_b, ze3v_f, (n3 - n2) * sizeof(double));
+      wfree(ze3u_f); wfree(ze3v_f);
+    }
     /* (:312-324) the before velocity back to the time-split barotropic estimate */
-    for (size_t p = 0; p < n2; ++p) { zue[p] = e3u[p] * ub[p] * umask[p]; zve[p] = e3v[p] * vb[p] * vmask[p]; }
+    for (size_t p = 0; p < n2; ++p) { zue[p] = e3u_b[p] * ub[p] * umask[p]; zve[p] = e3v_b[p] * vb[p] * vmask[p]; }
     for (int jk = 2; jk <= jpk - 1; ++jk)
       for (size_t p = 0; p < n2; ++p) {
         size_t q = p + n2 * (jk - 1);
-        zue[p] = zue[p] + e3u[q] * ub[q] * umask[q];
-        zve[p] = zve[p] + e3v[q] * vb[q] * vmask[q];
+        zue[p] = zue[p] + e3u_b[q] * ub[q] * umask[q];
+        zve[p] = zve[p] + e3v_b[q] * vb[q] * vmask[q];
       }
     for (int jk = 1; jk <= jpk - 1; ++jk)
       for (size_t p = 0; p < n2; ++p) {
         size_t q = p + n2 * (jk - 1);
-        ub[q] = ub[q] - (zue[p] * c->r1_hu_0[p] - un_b[p]) * umask[q];
-        vb[q] = vb[q] - (zve[p] * c->r1_hv_0[p] - vn_b[p]) * vmask[q];
+        ub[q] = ub[q] - (zue[p] * r1_hu_n[p] - un_b[p]) * umask[q];
+        vb[q] = vb[q] - (zve[p] * r1_hv_n[p] - vn_b[p]) * vmask[q];
       }
+  }
+  if (vvl) {                                                  /* :334-343 */
+    vvl_depth(c, e3u_b, umask, c->ssumask, F[NEMO_F_HU_B], r1_hu_b);
+    vvl_depth(c, e3v_b, vmask, c->ssvmask, F[NEMO_F_HV_B], r1_hv_b);
   }
   /* (:345-358) now and before barotropic velocities for the next step */
   for (size_t p = 0; p < n2; ++p) {
-    un_b[p] = e3u[p] * un[p] * umask[p]; ub_b[p] = e3u[p] * ub[p] * umask[p];
-    vn_b[p] = e3v[p] * vn[p] * vmask[p]; vb_b[p] = e3v[p] * vb[p] * vmask[p];
+    un_b[p] = e3u_a[p] * un[p] * umask[p]; ub_b[p] = e3u_b[p] * ub[p] * umask[p];
+    vn_b[p] = e3v_a[p] * vn[p] * vmask[p]; vb_b[p] = e3v_b[p] * vb[p] * vmask[p];
   }
   for (int jk = 2; jk <= jpk - 1; ++jk)
     for (size_t p = 0; p < n2; ++p) {
       size_t q = p + n2 * (jk - 1);
-      un_b[p] = un_b[p] + e3u[q] * un[q] * umask[q]; ub_b[p] = ub_b[p] + e3u[q] * ub[q] * umask[q];
-      vn_b[p] = vn_b[p] + e3v[q] * vn[q] * vmask[q]; vb_b[p] = vb_b[p] + e3v[q] * vb[q] * vmask[q];
+      un_b[p] = un_b[p] + e3u_a[q] * un[q] * umask[q]; ub_b[p] = ub_b[p] + e3u_b[q] * ub[q] * umask[q];
+      vn_b[p] = vn_b[p] + e3v_a[q] * vn[q] * vmask[q]; vb_b[p] = vb_b[p] + e3v_b[q] * vb[q] * vmask[q];
     }
   for (size_t p = 0; p < n2; ++p) {
-    un_b[p] = un_b[p] * c->r1_hu_0[p]; vn_b[p] = vn_b[p] * c->r1_hv_0[p];
-    ub_b[p] = ub_b[p] * c->r1_hu_0[p]; vb_b[p] = vb_b[p] * c->r1_hv_0[p];
+    un_b[p] = un_b[p] * r1_hu_a[p]; vn_b[p] = vn_b[p] * r1_hv_a[p];
+    ub_b[p] = ub_b[p] * r1_hu_b[p]; vb_b[p] = vb_b[p] * r1_hv_b[p];
   }
   wfree(zue); wfree(zve);
   return NEMO_OK;
 }
 
-/* ssh_swp (sshwzv.F90:216-267), linear free surface. */
+/* ssh_swp (sshwzv.F90:216-267); with a variable volume the forcing is removed from
+ * the filtered before ssh (:254-258; rnf when bound, no ice-shelf melt). */
 int ora_ssh_swp(ora_ctx *c, int kt) {
   const nemo_namelist *nm = &c->nam;
   const size_t n2 = (size_t)c->jpi * c->jpj;
   double *sshb = c->f[NEMO_F_SSHB], *sshn = c->f[NEMO_F_SSHN];
   const double *ssha = c->f[NEMO_F_SSHA];
+  const double *emp = c->f[NEMO_F_EMP], *emp_b = c->f[NEMO_F_EMP_B];
+  const double *rnf = c->f[NEMO_F_RNF], *rnf_b = c->f[NEMO_F_RNF_B];
   if (!sshb || !sshn || !ssha) return NEMO_ERR_UNBOUND;
-  if (!nm->ln_linssh) return NEMO_ERR_ARG;
+  if (!nm->ln_linssh && (!emp || !emp_b || (rnf == NULL) != (rnf_b == NULL))) return NEMO_ERR_UNBOUND;
   if (nm->neuler == 0 && kt == nm->nit000) {
     memcpy(sshn, ssha, n2 * sizeof(double));
   } else {
+    const double zcoef = nm->rn_atfp * nm->rn_rdt * (1.0 / nm->rau0);
     for (size_t p = 0; p < n2; ++p) {
       sshb[p] = sshn[p] + nm->rn_atfp * (sshb[p] - 2 * sshn[p] + ssha[p]);
+      if (!nm->ln_linssh) {
+        double zf = emp_b[p] - emp[p];
+        if (rnf) zf = zf - rnf_b[p] + rnf[p];
+        sshb[p] = sshb[p] - zcoef * zf * c->ssmask[p];
+      }
       sshn[p] = ssha[p];
     }
   }

@@ -109,6 +109,9 @@ int ora_wzv(ora_ctx *c, int kt);
 int ora_dyn_zdf_step(ora_ctx *c, int kt);
 int ora_dyn_nxt(ora_ctx *c, int kt);
 int ora_ssh_swp(ora_ctx *c, int kt);
+/* z* time stepping: dom_vvl_sf_nxt (domvvl.F90:268-562) and dom_vvl_sf_swp (:565-675) */
+int ora_dom_vvl_sf_nxt(ora_ctx *c, int kt);
+int ora_dom_vvl_sf_swp(ora_ctx *c, int kt);
 int ora_stp_model(ora_ctx *c, int kt);
 /* ldf_slp with ldf_slp_mxl (z-coordinate, no cavities, no partial steps); NMLN is
  * bound as an int array. */

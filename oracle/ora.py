@@ -62,8 +62,8 @@ def lib():
         P("ora_tra_zdf_imp_adj", [vp, i, i, cp, d, vp, vp, i])
         P("ora_tra_nxt", [vp, i])
         P("ora_tra_nxt_adj", [vp, i, vp, vp, vp])
-        for name in ("ora_wzv", "ora_dyn_zdf_step", "ora_dyn_nxt", "ora_ssh_swp", "ora_stp_model", "ora_tra_sbc",
-                     "ora_tra_qsr"):
+        for name in ("ora_wzv", "ora_dyn_zdf_step", "ora_dyn_nxt", "ora_ssh_swp", "ora_dom_vvl_sf_nxt",
+                     "ora_dom_vvl_sf_swp", "ora_stp_model", "ora_tra_sbc", "ora_tra_qsr"):
             P(name, [vp, i])
         P("ora_ldf_slp", [vp, i, vp, vp])
         P("ora_nksr", [vp], C.c_int)
@@ -287,6 +287,12 @@ class Oracle:
 
     def ssh_swp(self, kt):
         self._ck(lib().ora_ssh_swp(self.h, kt), "ssh_swp")
+
+    def dom_vvl_sf_nxt(self, kt):
+        self._ck(lib().ora_dom_vvl_sf_nxt(self.h, kt), "dom_vvl_sf_nxt")
+
+    def dom_vvl_sf_swp(self, kt):
+        self._ck(lib().ora_dom_vvl_sf_swp(self.h, kt), "dom_vvl_sf_swp")
 
     def stp_model(self, kt):
         self._ck(lib().ora_stp_model(self.h, kt), "stp_model")
