@@ -143,6 +143,11 @@ typedef struct nemo_namelist {
   int    nn_dynkeg;       /* grad(KE) scheme: 0 C2 (1, Hollingsworth: not supported)   */
   /* &namsbc: the user-defined (GYRE analytic) surface forcing, formed each model step */
   int    ln_usr;
+  /* &namtra_ldf: the triad direction (exclusive with ln_traldf_iso) and its options */
+  int    ln_traldf_triad;
+  int    ln_triad_iso;    /* pure horizontal mixing in the mixed layer                 */
+  int    ln_botmix_triad; /* lateral mixing on the bottom half cells                   */
+  double rn_sw_triad;     /* 1 switching triads, 0 all four triads used                */
 } nemo_namelist;
 
 /* ------------------------------------------------------- module-global fields
@@ -246,6 +251,12 @@ enum nemo_field_id {
   NEMO_F_E3UW_N, NEMO_F_E3VW_N, NEMO_F_E3UW_B, NEMO_F_E3VW_B, /* [T]                  */
   NEMO_F_GDEPT_B, NEMO_F_GDEPW_B, NEMO_F_GDE3W_N, /* [T]                              */
   NEMO_F_E3UW_0, NEMO_F_E3VW_0,        /* [T]                                         */
+  /* the triad operator (ldfslp.F90 module arrays of ldf_slp_triad): the slopes of the
+   * four i-k (j-k) triads of each T-point relative to geopotentials (triadi_g,
+   * triadj_g) and to the model levels (triadi, triadj), each (jpi,jpj,jpk,0:1,0:1)
+   * in Fortran order, i.e. 4 x jpi*jpj*jpk per member; wslp2 [T] */
+  NEMO_F_TRIADI_G, NEMO_F_TRIADJ_G, NEMO_F_TRIADI, NEMO_F_TRIADJ,
+  NEMO_F_WSLP2,
   NEMO_F_COUNT
 };
 
@@ -441,6 +452,24 @@ int nemo_gpu_zps_hde_rd(nemo_ctx *ctx, int kt, const void *pts, const void *prd,
 int nemo_gpu_tra_ldf_blp(nemo_ctx *ctx, int kt, int kit000, const char *cdtype, const void *pahu,
                          const void *pahv, const void *pgu, const void *pgv, const void *pgui,
                          const void *pgvi, const void *ptb, void *pta, int kjpt, int kldf);
+
+/* ldf_slp_triad (ldfslp.F90:377-617): the triad slopes from the before tracers and
+ * their expansion ratios prab_b (jpi,jpj,jpk,2), eos_rab of tsb (step.F90:127), into
+ * the bound TRIADI_G, TRIADJ_G, TRIADI, TRIADJ and, when bound, WSLP2. Reads the
+ * bound TSB, GDEPT_N, GDEPW_N, NMLN (mixed-layer level) and the now scale factors.
+ * No eddy-induced velocity; the partial-step bottom correction of the reference is
+ * off (l_grad_zps = .FALSE.). Faces outside the reference's loops keep their values
+ * except at levels 1 and jpk, which are zeroed. */
+int nemo_gpu_ldf_slp_triad(nemo_ctx *ctx, int kt, const void *prab_b);
+/* tra_ldf_triad (traldf_triad.F90:50-429), the same argument list as tra_ldf_iso
+ * (pgu, pgv, pgui, pgvi are unread: l_grad_zps = .FALSE.): pass 1 writes the bound
+ * AH_WSLP2 and AKZ from the triads (ln_traldf_msc: the stabilising akz), then per
+ * tracer the triad fluxes, the 33 flux (laplacian: ah_wslp2 - akz; bilaplacian pass 1
+ * ah_wslp2, pass 2 ah_wslp2 on ptb and akz on ptbb) and their divergence added to
+ * pta (sign -1 in pass 2). Reads the bound triad arrays and GDEPT_N. */
+int nemo_gpu_tra_ldf_triad(nemo_ctx *ctx, int kt, int kit000, const char *cdtype, const void *pahu,
+                           const void *pahv, const void *pgu, const void *pgv, const void *pgui,
+                           const void *pgvi, const void *ptb, const void *ptbb, void *pta, int kjpt, int kpass);
 
 /* tra_zdf_imp (trazdf.F90:109-268): pta becomes the after tracer. Reads the bound
  * avt (avs), and ah_wslp2/akz when ln_traldf_iso. */
@@ -704,6 +733,7 @@ enum nemo_kernel_id {
   NEMO_K_USR_SBC,      /* GYRE's analytic surface forcing */
   NEMO_K_VVL_SF,       /* z*: the after scale factors and the swap (dom_vvl_sf_nxt/_swp) */
   NEMO_K_VVL_NXT,      /* z*: tra_nxt_vvl, dyn_nxt's filter of e3 and velocities, ssh_swp */
+  NEMO_K_TRIAD,        /* the triad operator: slopes, coefficients, fluxes, divergence */
   NEMO_K_COUNT
 };
 

@@ -18,6 +18,7 @@
 #include "../../include/nemo_gpu.h"
 #include "adj.h"
 #include "step.h"
+#include "triad.h"
 #include "eos80.h"
 #include "nemo_sin.h"
 #include "launch.h"
@@ -285,7 +286,10 @@ size_t field_numel(const nemo_ctx* c, int id) {
     case NEMO_F_E3U_A: case NEMO_F_E3V_A: case NEMO_F_E3U_B: case NEMO_F_E3V_B: case NEMO_F_E3W_B:
     case NEMO_F_E3UW_N: case NEMO_F_E3VW_N: case NEMO_F_E3UW_B: case NEMO_F_E3VW_B:
     case NEMO_F_GDEPT_B: case NEMO_F_GDEPW_B: case NEMO_F_GDE3W_N: case NEMO_F_E3UW_0: case NEMO_F_E3VW_0:
+    case NEMO_F_WSLP2:
       return (size_t)c->n3;
+    case NEMO_F_TRIADI_G: case NEMO_F_TRIADJ_G: case NEMO_F_TRIADI: case NEMO_F_TRIADJ:
+      return 4 * (size_t)c->n3;
     default: break;
   }
   if (id >= NEMO_F_SSHB) return (size_t)c->n2;
@@ -432,7 +436,7 @@ int build_dom(nemo_ctx* c, DomStore<T>& st) {
 #define UP(name) if ((s = upload(c, st, c->name, &d.name))) return s
   UP(e1t); UP(e2t); UP(e1u); UP(e2u); UP(e1v); UP(e2v);
   UP(r1_e1u); UP(r1_e2u); UP(r1_e1v); UP(r1_e2v);
-  UP(e1e2t); UP(r1_e1e2t); UP(e2_e1u); UP(e1_e2v); UP(r1_e1e2u); UP(r1_e1e2v); UP(r1_e1e2f); UP(e1e2u);
+  UP(e1e2t); UP(r1_e1e2t); UP(e2_e1u); UP(e1_e2v); UP(r1_e1e2u); UP(r1_e1e2v); UP(r1_e1e2f); UP(e1e2u); UP(e1e2v);
   UP(ht_0); UP(hu_0); UP(hv_0); UP(r1_hu_0); UP(r1_hv_0);
   UP(ssmask); UP(ssumask); UP(ssvmask);
   UP(ff_t); UP(ff_f); UP(zwz); UP(ftne); UP(ftnw); UP(ftse); UP(ftsw);
@@ -819,6 +823,42 @@ int run_ldf_iso(nemo_ctx* c, int kt, int kit000, const void* pahu, const void* p
 // tra_ldf_blp (traldf_lap_blp.F90:161-231) without partial steps: the first
 // laplacian (kldf 20 iso-level, 21 rotated) of ptb into zlap, lbc_lnk, the second of
 // zlap into pta
+// ---------------------------------------------------------------- the triad operator
+template <class T>
+TriadArgs<T> triad_args(nemo_ctx* c) {
+  const nemo_namelist& nm = c->nam;
+  void* const* F = c->f;
+  TriadArgs<T> a{};
+  a.tsb = (const T*)F[NEMO_F_TSB];
+  a.gdept = (const T*)F[NEMO_F_GDEPT_N]; a.gdepw = (const T*)F[NEMO_F_GDEPW_N];
+  a.nmln = (const int*)F[NEMO_F_NMLN];
+  a.tig = (T*)F[NEMO_F_TRIADI_G]; a.tjg = (T*)F[NEMO_F_TRIADJ_G]; a.ti = (T*)F[NEMO_F_TRIADI]; a.tj = (T*)F[NEMO_F_TRIADJ];
+  a.wslp2 = (T*)F[NEMO_F_WSLP2];
+  a.slpmax = (T)(nm.rn_slpmax > 0 ? nm.rn_slpmax : 0.01);
+  a.sw = (T)nm.rn_sw_triad;
+  a.repsln = (T)1.e-25;   // ldfslp.F90:72
+  a.triad_iso = nm.ln_triad_iso;
+  a.botmix = nm.ln_botmix_triad;
+  return a;
+}
+
+template <class T>
+int run_ldf_triad(nemo_ctx* c, int kt, int kit000, const void* pahu, const void* pahv, const void* ptb,
+                  const void* ptbb, void* pta, int kjpt, int kpass) {
+  const nemo_namelist& nm = c->nam;
+  if (int s = ensure_iso_work(c, kjpt)) return s;
+  TriadArgs<T> a = triad_args<T>(c);
+  a.l = ldf_args<T>(c, pahu, pahv, nullptr, nullptr, ptb, ptbb, pta, kjpt, kpass);
+  a.l.ah_wslp2 = (T*)c->f[NEMO_F_AH_WSLP2]; a.l.akz = (T*)c->f[NEMO_F_AKZ];
+  a.l.lap = nm.ln_traldf_lap; a.l.blp = nm.ln_traldf_blp; a.l.msc = nm.ln_traldf_msc;
+  const double z2dt = (nm.neuler == 0 && kt == kit000) ? nm.rn_rdt : 2.0 * nm.rn_rdt;  // traldf_triad.F90:117-120
+  a.l.z2dt = (T)z2dt; a.l.z1_2dt = (T)(1.0 / z2dt);
+  a.l.zftu = (T*)c->iso_w[0]; a.l.zftv = (T*)c->iso_w[1]; a.l.ztfw = (T*)c->iso_w[2];
+  cudaError_t e = launch_tra_ldf_triad<T>(dom_now<T>(c), a, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "tra_ldf_triad launch");
+  return NEMO_OK;
+}
+
 template <class T>
 int run_ldf_blp(nemo_ctx* c, int kt, int kit000, const void* pahu, const void* pahv, const void* pgu,
                 const void* pgv, const void* ptb, void* pta, int kjpt, int kldf) {
@@ -834,7 +874,8 @@ int run_ldf_blp(nemo_ctx* c, int kt, int kit000, const void* pahu, const void* p
   T* zglv = (T*)((char*)c->blp_w + n3b + n2b);
   CK(cudaMemsetAsync(zlap, 0, n3b, c->stream), "zlap = 0");
   int s = kldf == 20 ? run_ldf_lap<T>(c, pahu, pahv, pgu, pgv, ptb, zlap, kjpt, 1)
-                     : run_ldf_iso<T>(c, kt, kit000, pahu, pahv, pgu, pgv, ptb, ptb, zlap, kjpt, 1);
+          : kldf == 21 ? run_ldf_iso<T>(c, kt, kit000, pahu, pahv, pgu, pgv, ptb, ptb, zlap, kjpt, 1)
+                       : run_ldf_triad<T>(c, kt, kit000, pahu, pahv, ptb, ptb, zlap, kjpt, 1);
   if (s) return s;
   cudaError_t e = launch_lbc<T>(zlap, c->jpi, c->jpj, (long)c->jpk * kjpt * c->nmem, 0, T(0), c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "tra_ldf_blp lbc");
@@ -843,6 +884,7 @@ int run_ldf_blp(nemo_ctx* c, int kt, int kit000, const void* pahu, const void* p
     e = launch_zps_hde<T>(dom_now<T>(c), zlap, zglu, zglv, kjpt, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "tra_ldf_blp zps_hde");
   }
+  if (kldf == 22) return run_ldf_triad<T>(c, kt, kit000, pahu, pahv, zlap, ptb, pta, kjpt, 2);
   return kldf == 20 ? run_ldf_lap<T>(c, pahu, pahv, zps ? zglu : nullptr, zps ? zglv : nullptr, zlap, pta, kjpt, 2)
                     : run_ldf_iso<T>(c, kt, kit000, pahu, pahv, zps ? zglu : nullptr, zps ? zglv : nullptr, zlap, ptb,
                                      pta, kjpt, 2);
@@ -857,7 +899,7 @@ int run_zdf(nemo_ctx* c, double p2dt, const void* ptb, void* pta, int kjpt, int 
   a.ddm = nm.ln_zdfddm; a.is_trc = is_trc; a.clamp_sal = clamp;
   if (!is_trc && !a.avt) return fail(c, NEMO_ERR_UNBOUND, "tra_zdf_imp: avt must be bound");
   if ((is_trc || nm.ln_zdfddm) && !a.avs) return fail(c, NEMO_ERR_UNBOUND, "tra_zdf_imp: avs must be bound");
-  if (nm.ln_traldf_iso) {
+  if (nm.ln_traldf_iso || nm.ln_traldf_triad) {  // l_ldfslp (ldftra.F90:253-255)
     a.add = (const T*)c->f[nm.ln_traldf_msc ? NEMO_F_AKZ : NEMO_F_AH_WSLP2];
     if (!a.add) return fail(c, NEMO_ERR_UNBOUND, "tra_zdf_imp: ah_wslp2/akz must be bound with iso-neutral mixing");
   }
@@ -1647,7 +1689,10 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
   mark(2);
   if (nm.ln_traldf_blp)  // traldf.F90:75-76
     s = run_ldf_blp<T>(c, kt, nm.nit000, F[NEMO_F_AHTU], F[NEMO_F_AHTV], F[NEMO_F_GTSU], F[NEMO_F_GTSV],
-                       F[NEMO_F_TSB], F[NEMO_F_TSA], 2, nm.ln_traldf_iso ? 21 : 20);
+                       F[NEMO_F_TSB], F[NEMO_F_TSA], 2, nm.ln_traldf_iso ? 21 : nm.ln_traldf_triad ? 22 : 20);
+  else if (nm.ln_traldf_triad)  // np_lap_it (traldf.F90:73-74)
+    s = run_ldf_triad<T>(c, kt, nm.nit000, F[NEMO_F_AHTU], F[NEMO_F_AHTV], F[NEMO_F_TSB], F[NEMO_F_TSB], F[NEMO_F_TSA],
+                         2, 1);
   else if (nm.ln_traldf_iso)
     s = run_ldf_iso<T>(c, kt, nm.nit000, F[NEMO_F_AHTU], F[NEMO_F_AHTV], F[NEMO_F_GTSU], F[NEMO_F_GTSV], F[NEMO_F_TSB],
                        F[NEMO_F_TSB], F[NEMO_F_TSA], 2, 1);
@@ -1784,6 +1829,7 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
   if (dm->jpi < 4 || dm->jpj < 4 || dm->jpk < 3 || dm->jpk > KMAX || dm->jpk > 255) return bad(NEMO_ERR_UNSUPPORTED);
   if (dm->jperio != 0 || nam->ln_isfcav || nam->ln_zad_Aimp) return bad(NEMO_ERR_UNSUPPORTED);
   if (nam->nvor_scheme < 0 || nam->nvor_scheme > 5) return bad(NEMO_ERR_ARG);
+  if (nam->ln_traldf_iso && nam->ln_traldf_triad) return bad(NEMO_ERR_ARG);  // one direction of diffusion
   for (int o : {nam->nn_fct_h, nam->nn_fct_v})
     if (o != 0 && o != 2 && o != 4) return bad(NEMO_ERR_ARG);
   int dev = 0;
@@ -1870,7 +1916,7 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
   if (cudaMalloc(&c->gs_out, (size_t)c->nmem * 8) != cudaSuccess) return bad(NEMO_ERR_NOMEM);
   // work arrays of the hot path allocated here, so graph capture never allocates
   if (ensure_fct_work(c, 2, c->nam.nn_fct_v == 4)) return bad(NEMO_ERR_NOMEM);
-  if (c->nam.ln_traldf_iso && ensure_iso_work(c, 2)) return bad(NEMO_ERR_NOMEM);
+  if ((c->nam.ln_traldf_iso || c->nam.ln_traldf_triad) && ensure_iso_work(c, 2)) return bad(NEMO_ERR_NOMEM);
   if (cudaDeviceSynchronize() != cudaSuccess) return bad(NEMO_ERR_CUDA);
   *out = c;
   return NEMO_OK;
@@ -2084,6 +2130,46 @@ int nemo_gpu_tra_ldf_iso(nemo_ctx* c, int kt, int kit000, const char* cdtype, co
              : run_ldf_iso<float>(c, kt, kit000, pahu, pahv, pgu, pgv, ptb, ptbb, pta, kjpt, kpass);
 }
 
+int nemo_gpu_ldf_slp_triad(nemo_ctx* c, int kt, const void* prab_b) {
+  (void)kt;
+  if (!c) return NEMO_ERR_ARG;
+  if (!prab_b) return fail(c, NEMO_ERR_ARG, "ldf_slp_triad: prab_b is NULL");
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  for (int id : {NEMO_F_TSB, NEMO_F_GDEPT_N, NEMO_F_GDEPW_N, NEMO_F_NMLN, NEMO_F_TRIADI_G, NEMO_F_TRIADJ_G,
+                 NEMO_F_TRIADI, NEMO_F_TRIADJ})
+    if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "ldf_slp_triad: field %d must be bound", id);
+  cudaError_t e;
+  if (c->prec == NEMO_PREC_FP64) {
+    TriadArgs<double> a = triad_args<double>(c);
+    a.rab = (const double*)prab_b;
+    e = launch_ldf_slp_triad<double>(dom_now<double>(c), a, c->stream);
+  } else {
+    TriadArgs<float> a = triad_args<float>(c);
+    a.rab = (const float*)prab_b;
+    e = launch_ldf_slp_triad<float>(dom_now<float>(c), a, c->stream);
+  }
+  if (e != cudaSuccess) return cuda_fail(c, e, "ldf_slp_triad launch");
+  return NEMO_OK;
+}
+
+
+int nemo_gpu_tra_ldf_triad(nemo_ctx* c, int kt, int kit000, const char* cdtype, const void* pahu, const void* pahv,
+                           const void* pgu, const void* pgv, const void* pgui, const void* pgvi, const void* ptb,
+                           const void* ptbb, void* pta, int kjpt, int kpass) {
+  (void)pgu; (void)pgv; (void)pgui; (void)pgvi;
+  if (!c) return NEMO_ERR_ARG;
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  int is_trc = 0;
+  if (int s = check_cdtype(c, cdtype, &is_trc)) return s;
+  if (!ptb || !pta || kjpt < 1 || (kpass != 1 && kpass != 2) || (kpass == 2 && !ptbb))
+    return fail(c, NEMO_ERR_ARG, "tra_ldf_triad: bad argument");
+  for (int id : {NEMO_F_AH_WSLP2, NEMO_F_AKZ, NEMO_F_TRIADI_G, NEMO_F_TRIADJ_G, NEMO_F_TRIADI, NEMO_F_TRIADJ,
+                 NEMO_F_GDEPT_N})
+    if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "tra_ldf_triad: field %d must be bound", id);
+  return c->prec == NEMO_PREC_FP64 ? run_ldf_triad<double>(c, kt, kit000, pahu, pahv, ptb, ptbb, pta, kjpt, kpass)
+                                   : run_ldf_triad<float>(c, kt, kit000, pahu, pahv, ptb, ptbb, pta, kjpt, kpass);
+}
+
 int nemo_gpu_tra_ldf_blp(nemo_ctx* c, int kt, int kit000, const char* cdtype, const void* pahu, const void* pahv,
                          const void* pgu, const void* pgv, const void* pgui, const void* pgvi, const void* ptb,
                          void* pta, int kjpt, int kldf) {
@@ -2093,8 +2179,12 @@ int nemo_gpu_tra_ldf_blp(nemo_ctx* c, int kt, int kit000, const char* cdtype, co
   int is_trc = 0;
   if (int s = check_cdtype(c, cdtype, &is_trc)) return s;
   if (!ptb || !pta || kjpt < 1) return fail(c, NEMO_ERR_ARG, "tra_ldf_blp: bad argument");
-  if (kldf != 20 && kldf != 21)
-    return fail(c, NEMO_ERR_UNSUPPORTED, "tra_ldf_blp: kldf 20 (iso-level) or 21 (rotated) only");
+  if (kldf != 20 && kldf != 21 && kldf != 22)
+    return fail(c, NEMO_ERR_UNSUPPORTED, "tra_ldf_blp: kldf 20 (iso-level), 21 (rotated) or 22 (triad) only");
+  if (kldf == 22)
+    for (int id : {NEMO_F_AH_WSLP2, NEMO_F_AKZ, NEMO_F_TRIADI_G, NEMO_F_TRIADJ_G, NEMO_F_TRIADI, NEMO_F_TRIADJ,
+                   NEMO_F_GDEPT_N})
+      if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "tra_ldf_blp: field %d must be bound (triad)", id);
   if (c->nam.ln_zps && (!pgu || !pgv)) return fail(c, NEMO_ERR_ARG, "tra_ldf_blp: pgu/pgv required with ln_zps");
   return c->prec == NEMO_PREC_FP64 ? run_ldf_blp<double>(c, kt, kit000, pahu, pahv, pgu, pgv, ptb, pta, kjpt, kldf)
                                    : run_ldf_blp<float>(c, kt, kit000, pahu, pahv, pgu, pgv, ptb, pta, kjpt, kldf);

@@ -64,7 +64,7 @@ struct Dom {
   long n2, n3;  // points per member of a 2-D / 3-D field
   RO<T> e1t, e2t, e1u, e2u, e1v, e2v;
   RO<T> r1_e1u, r1_e2u, r1_e1v, r1_e2v;
-  RO<T> e1e2t, r1_e1e2t, e2_e1u, e1_e2v, r1_e1e2u, r1_e1e2v, e1e2u;
+  RO<T> e1e2t, r1_e1e2t, e2_e1u, e1_e2v, r1_e1e2u, r1_e1e2v, e1e2u, e1e2v;
   RO<T> ht_0, hu_0, hv_0, r1_hu_0, r1_hv_0;
   RO<T> ssmask, ssumask, ssvmask;
   RO<T> ff_t, ff_f, zwz, ftne, ftnw, ftse, ftsw;

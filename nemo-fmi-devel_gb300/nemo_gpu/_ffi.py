@@ -63,7 +63,9 @@ class Namelist(C.Structure):
                 ("rn_emin0", C.c_double), ("rn_bshear", C.c_double), ("nn_pdl", C.c_int), ("nn_mxl", C.c_int),
                 ("ln_mxl0", C.c_int), ("rn_mxl0", C.c_double), ("ln_lc", C.c_int), ("rn_lc", C.c_double),
                 ("nn_etau", C.c_int), ("ln_drg_tke", C.c_int),
-                ("ln_dynadv_OFF", C.c_int), ("nn_dynkeg", C.c_int), ("ln_usr", C.c_int)]
+                ("ln_dynadv_OFF", C.c_int), ("nn_dynkeg", C.c_int), ("ln_usr", C.c_int),
+                ("ln_traldf_triad", C.c_int), ("ln_triad_iso", C.c_int), ("ln_botmix_triad", C.c_int),
+                ("rn_sw_triad", C.c_double)]
 
 
 # members a namelist may leave out (&namtra_qsr of namelist_ref; rcp 0 selects 3991.86795711963)
@@ -77,7 +79,8 @@ NAMELIST_DEFAULTS = {"ln_traqsr": 0, "rn_abs": 0.58, "rn_si0": 0.35, "rn_si1": 2
                      "rn_avt0": 1.2e-5, "rn_ediff": 0.1, "rn_ediss": 0.7, "rn_ebb": 67.83, "rn_emin": 1.e-6,
                      "rn_emin0": 1.e-4, "rn_bshear": 1.e-20, "nn_pdl": 1, "nn_mxl": 2, "ln_mxl0": 1,
                      "rn_mxl0": 0.04, "ln_lc": 1, "rn_lc": 0.15, "nn_etau": 0, "ln_drg_tke": 0,
-                     "ln_dynadv_OFF": 0, "nn_dynkeg": 0, "ln_usr": 0}
+                     "ln_dynadv_OFF": 0, "nn_dynkeg": 0, "ln_usr": 0,
+                     "ln_traldf_triad": 0, "ln_triad_iso": 0, "ln_botmix_triad": 0, "rn_sw_triad": 1.0}
 
 
 def make_desc(dom):
@@ -137,6 +140,8 @@ def load(path):
     _proto(lib, "nemo_gpu_tra_nxt", i, [vp, i])
     _proto(lib, "nemo_gpu_autotune", i, [vp, i, i])
     _proto(lib, "nemo_gpu_ldf_slp", i, [vp, i, vp, vp])
+    _proto(lib, "nemo_gpu_ldf_slp_triad", i, [vp, i, vp])
+    _proto(lib, "nemo_gpu_tra_ldf_triad", i, [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
     _proto(lib, "nemo_gpu_tra_ldf_blp", i, [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
     _proto(lib, "nemo_gpu_zps_hde", i, [vp, i, i, vp, vp, vp])
     _proto(lib, "nemo_gpu_get_launch_shape", i, [vp, _ip, i])

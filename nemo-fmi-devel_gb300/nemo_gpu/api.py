@@ -220,6 +220,13 @@ class Context:
         self._ck(self.lib.nemo_gpu_tra_ldf_iso(self.h, kt, kit000, cdtype.encode(), *map(_ptr, (
             pahu, pahv, pgu, pgv, pgui, pgvi, ptb, ptbb, pta)), kjpt, kpass), "tra_ldf_iso")
 
+    def tra_ldf_triad(self, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb, ptbb, pta, kjpt, kpass):
+        self._ck(self.lib.nemo_gpu_tra_ldf_triad(self.h, kt, kit000, cdtype.encode(), *map(_ptr, (
+            pahu, pahv, pgu, pgv, pgui, pgvi, ptb, ptbb, pta)), kjpt, kpass), "tra_ldf_triad")
+
+    def ldf_slp_triad(self, kt, prab_b):
+        self._ck(self.lib.nemo_gpu_ldf_slp_triad(self.h, kt, _ptr(prab_b)), "ldf_slp_triad")
+
     def tra_ldf_blp(self, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb, pta, kjpt, kldf):
         self._ck(self.lib.nemo_gpu_tra_ldf_blp(self.h, kt, kit000, cdtype.encode(), *map(_ptr, (
             pahu, pahv, pgu, pgv, pgui, pgvi, ptb, pta)), kjpt, kldf), "tra_ldf_blp")

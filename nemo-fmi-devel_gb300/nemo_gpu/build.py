@@ -1,6 +1,6 @@
 """Build recipe of the CUDA library (sm_103a only).
 
-Six translation units are compiled in parallel and linked into
+Seven translation units are compiled in parallel and linked into
 ``nemo_gpu/_lib/libnemo_gpu.so``:
 
 * ``inst_fp64.cu`` -- FP64 kernels, ``--fmad=false`` so that every double operation
@@ -17,7 +17,9 @@ Six translation units are compiled in parallel and linked into
 * ``adj_fp64.cu``  -- the adjoint kernels of the tracer routines and tra_nxt
   (``--fmad=false``);
 * ``inst_step.cu`` -- the rest of the model step (wzv, dyn_zdf, dyn_nxt, ssh_swp,
-  the momentum trends, eos, zdf_phy, the forcing, stp_ctl, dia_hsb, ...), both
+  the momentum trends, eos, zdf_phy, the forcing, stp_ctl, dia_hsb, the z* time
+  stepping, ...), both precisions (``--fmad=false``);
+* ``inst_triad.cu`` -- the triad operator (ldf_slp_triad, tra_ldf_triad), both
   precisions (``--fmad=false``).
 """
 import concurrent.futures as cf
@@ -39,6 +41,7 @@ UNITS = {
     "noalloc.cu": ["--fmad=false"],
     "adj_fp64.cu": ["--fmad=false"],
     "inst_step.cu": ["--fmad=false"],
+    "inst_triad.cu": ["--fmad=false"],
 }
 
 

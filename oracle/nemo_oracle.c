@@ -1042,7 +1042,7 @@ static void zdf_lu(ora_ctx *c, const double *coef, double p2dt, double *zwi, dou
   const nemo_namelist *nm = &c->nam;
   const double *akz = c->f[NEMO_F_AKZ], *ah_wslp2 = c->f[NEMO_F_AH_WSLP2];
   const double *e3t_a = fld(c, NEMO_F_E3T_A), *e3w = fld(c, NEMO_F_E3W_N);
-  const int l_ldfslp = nm->ln_traldf_iso;
+  const int l_ldfslp = nm->ln_traldf_iso || nm->ln_traldf_triad;   /* ldftra.F90:253-255 */
   for (int jk = 2; jk <= jpk; ++jk)
     for (int jj = 1; jj <= jpj; ++jj)
       for (int ji = 1; ji <= jpi; ++ji) zwt[I3(ji, jj, jk)] = coef[I3(ji, jj, jk)];
@@ -1084,7 +1084,7 @@ int ora_tra_zdf_imp(ora_ctx *c, int kt, int kit000, const char *cdtype, double p
   const double *avt = c->f[NEMO_F_AVT], *avs = c->f[NEMO_F_AVS];
   const double *akz = c->f[NEMO_F_AKZ], *ah_wslp2 = c->f[NEMO_F_AH_WSLP2];
   const double *e3t_b = fld(c, NEMO_F_E3T_B), *e3t_n = fld(c, NEMO_F_E3T_N), *tmask = c->tmask;
-  const int l_ldfslp = nm->ln_traldf_iso;
+  const int l_ldfslp = nm->ln_traldf_iso || nm->ln_traldf_triad;   /* ldftra.F90:253-255 */
   if (!avt && !is_trc) return NEMO_ERR_UNBOUND;
   if (l_ldfslp && ((nm->ln_traldf_msc && !akz) || (!nm->ln_traldf_msc && !ah_wslp2))) return NEMO_ERR_UNBOUND;
   double *zwi = walloc(n3), *zwt = walloc(n3), *zwd = walloc(n3), *zws = walloc(n3);
@@ -2436,17 +2436,19 @@ int ora_tra_ldf_blp(ora_ctx *c, int kt, int kit000, const char *cdtype,
                     const double *pahu, const double *pahv,
                     const double *pgu, const double *pgv, const double *pgui, const double *pgvi,
                     const double *ptb, double *pta, int kjpt, int kldf) {
-  if (kldf != 20 && kldf != 21) return NEMO_ERR_UNSUPPORTED;
+  if (kldf != 20 && kldf != 21 && kldf != 22) return NEMO_ERR_UNSUPPORTED;
   if (c->nam.ln_zps && (!pgu || !pgv)) return NEMO_ERR_ARG;
   const size_t n2 = (size_t)c->jpi * c->jpj, n3 = n2 * c->jpk;
   double *zlap = zalloc(n3 * (size_t)kjpt), *zglu = zalloc(n2 * kjpt), *zglv = zalloc(n2 * kjpt);
   int st = kldf == 20 ? ora_tra_ldf_lap(c, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb, zlap, kjpt, 1)
-                      : ora_tra_ldf_iso(c, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb, ptb, zlap, kjpt, 1);
+         : kldf == 21 ? ora_tra_ldf_iso(c, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb, ptb, zlap, kjpt, 1)
+                      : ora_tra_ldf_triad(c, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb, ptb, zlap, kjpt, 1);
   if (!st) {
     lbc_closed(c->jpi, c->jpj, zlap, c->jpk * kjpt, 'T', 0.0);
     if (c->nam.ln_zps) ora_zps_hde(c, kt, kjpt, zlap, zglu, zglv);   /* GRADh(zlap) at the partial steps */
     st = kldf == 20 ? ora_tra_ldf_lap(c, kt, kit000, cdtype, pahu, pahv, zglu, zglv, NULL, NULL, zlap, pta, kjpt, 2)
-                    : ora_tra_ldf_iso(c, kt, kit000, cdtype, pahu, pahv, zglu, zglv, NULL, NULL, zlap, ptb, pta, kjpt, 2);
+       : kldf == 21 ? ora_tra_ldf_iso(c, kt, kit000, cdtype, pahu, pahv, zglu, zglv, NULL, NULL, zlap, ptb, pta, kjpt, 2)
+                    : ora_tra_ldf_triad(c, kt, kit000, cdtype, pahu, pahv, zglu, zglv, NULL, NULL, zlap, ptb, pta, kjpt, 2);
   }
   wfree(zlap); wfree(zglu); wfree(zglv);
   return st;
@@ -2480,7 +2482,11 @@ static int stp_tracers(ora_ctx *c, int kt) {
   const double *ahtu = c->f[NEMO_F_AHTU], *ahtv = c->f[NEMO_F_AHTV];
   if (nm->ln_traldf_blp)   /* traldf.F90:75-76 */
     st = ora_tra_ldf_blp(c, kt, nm->nit000, "TRA", ahtu, ahtv, c->f[NEMO_F_GTSU], c->f[NEMO_F_GTSV],
-                         c->f[NEMO_F_GTUI], c->f[NEMO_F_GTVI], tsb, tsa, 2, nm->ln_traldf_iso ? 21 : 20);
+                         c->f[NEMO_F_GTUI], c->f[NEMO_F_GTVI], tsb, tsa, 2,
+                         nm->ln_traldf_iso ? 21 : nm->ln_traldf_triad ? 22 : 20);
+  else if (nm->ln_traldf_triad)   /* np_lap_it (traldf.F90:73-74) */
+    st = ora_tra_ldf_triad(c, kt, nm->nit000, "TRA", ahtu, ahtv, c->f[NEMO_F_GTSU], c->f[NEMO_F_GTSV],
+                           c->f[NEMO_F_GTUI], c->f[NEMO_F_GTVI], tsb, tsb, tsa, 2, 1);
   else if (nm->ln_traldf_iso)
     st = ora_tra_ldf_iso(c, kt, nm->nit000, "TRA", ahtu, ahtv, c->f[NEMO_F_GTSU], c->f[NEMO_F_GTSV],
                          c->f[NEMO_F_GTUI], c->f[NEMO_F_GTVI], tsb, tsb, tsa, 2, 1);
@@ -2852,7 +2858,8 @@ int ora_tra_zdf_imp_adj(ora_ctx *c, int kt, int kit000, const char *cdtype, doub
   const double *avt = c->f[NEMO_F_AVT], *avs = c->f[NEMO_F_AVS];
   const double *e3t_b = fld(c, NEMO_F_E3T_B), *e3t_n = fld(c, NEMO_F_E3T_N), *tmask = c->tmask;
   if (!avt && !is_trc) return NEMO_ERR_UNBOUND;
-  if (nm->ln_traldf_iso && ((nm->ln_traldf_msc && !c->f[NEMO_F_AKZ]) || (!nm->ln_traldf_msc && !c->f[NEMO_F_AH_WSLP2])))
+  if ((nm->ln_traldf_iso || nm->ln_traldf_triad) &&
+      ((nm->ln_traldf_msc && !c->f[NEMO_F_AKZ]) || (!nm->ln_traldf_msc && !c->f[NEMO_F_AH_WSLP2])))
     return NEMO_ERR_UNBOUND;
   double *zwi = zalloc(n3), *zwt = zalloc(n3), *zwd = zalloc(n3), *zws = zalloc(n3);
   for (int jn = 1; jn <= kjpt; ++jn) {
@@ -4049,6 +4056,331 @@ int ora_stp_model(ora_ctx *c, int kt) {
     st = ora_stp_ctl(c, kt, c->ctl_zmax, c->ctl_loc, &c->ctl_kindic);
   return st;
 }
+
+/* -------------------------------------------------------- the triad operator */
+/* offset of (ji,jj,jk,a,b) in a (jpi,jpj,jpk,0:1,0:1) triad array */
+#define TRI(ji, jj, jk, a, b) (I3(ji, jj, jk) + n3 * (size_t)((a) + 2 * (b)))
+static inline double dmin3(double a, double b, double c) { double m = a < b ? a : b; return m < c ? m : c; }
+
+/* ldf_slp_triad (ldfslp.F90:377-617): the slopes of the four i-k and four j-k
+ * Griffies triads of each T-point relative to geopotentials (triadi_g, triadj_g) and
+ * to the model levels (triadi, triadj), and wslp2. The density gradients use the
+ * before expansion ratios prab_b (jpi,jpj,jpk,2: eos_rab of tsb) at the triad's
+ * T-point; inside the mixed layer the slope tapers linearly from its value just
+ * below the mixed-layer base. No eddy-induced velocity; l_grad_zps is .FALSE. (the
+ * reference never sets it, ldfslp.F90:54). Bound: TSB, GDEPT_N, GDEPW_N, NMLN and
+ * the outputs TRIADI_G, TRIADJ_G, TRIADI, TRIADJ (jpi,jpj,jpk,2,2), WSLP2 when
+ * bound. Entries of faces outside the reference's loops keep their values, except
+ * levels 1 and jpk, which are zeroed (:480-483; triadi's jpk level too). */
+int ora_ldf_slp_triad(ora_ctx *c, int kt, const double *prab_b) {
+  (void)kt;
+  const nemo_namelist *nm = &c->nam;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  double **F = c->f;
+  const double *tsb = F[NEMO_F_TSB], *gdept = F[NEMO_F_GDEPT_N], *gdepw = F[NEMO_F_GDEPW_N];
+  const int *nmln = (const int *)F[NEMO_F_NMLN];
+  double *tig = F[NEMO_F_TRIADI_G], *tjg = F[NEMO_F_TRIADJ_G], *ti = F[NEMO_F_TRIADI], *tj = F[NEMO_F_TRIADJ];
+  double *wslp2 = F[NEMO_F_WSLP2];
+  if (!prab_b) return NEMO_ERR_ARG;
+  if (!tsb || !gdept || !gdepw || !nmln || !tig || !tjg || !ti || !tj) return NEMO_ERR_UNBOUND;
+  if (nm->ln_isfcav) return NEMO_ERR_UNSUPPORTED;
+  const double repsln = 1.e-25, slpmax = nm->rn_slpmax > 0 ? nm->rn_slpmax : 0.01, sw = nm->rn_sw_triad;
+  const double *e3w = fld(c, NEMO_F_E3W_N), *e3u = fld(c, NEMO_F_E3U_N), *e3v = fld(c, NEMO_F_E3V_N);
+  const double *tt = tsb, *ts = tsb + n3, *ra = prab_b, *rb = prab_b + n3;
+  const double *umask = c->umask, *vmask = c->vmask;
+  double *zdxrho = zalloc(2 * n3), *zdyrho = zalloc(2 * n3), *zdzrho = zalloc(2 * n3);
+  double *zti_mlb = zalloc(4 * n2), *ztj_mlb = zalloc(4 * n2), *z1_mlbw = zalloc(n2);
+  for (int jl = 0; jl <= 1; ++jl) {                                      /* :415-429 */
+    const int ip = jl, jp = jl;
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          const double zdit = tt[I3(ji + 1, jj, jk)] - tt[I3(ji, jj, jk)];
+          const double zdis = ts[I3(ji + 1, jj, jk)] - ts[I3(ji, jj, jk)];
+          const double zdjt = tt[I3(ji, jj + 1, jk)] - tt[I3(ji, jj, jk)];
+          const double zdjs = ts[I3(ji, jj + 1, jk)] - ts[I3(ji, jj, jk)];
+          const double xr = (-ra[I3(ji + ip, jj, jk)] * zdit + rb[I3(ji + ip, jj, jk)] * zdis) * c->r1_e1u[I2(ji, jj)];
+          const double yr = (-ra[I3(ji, jj + jp, jk)] * zdjt + rb[I3(ji, jj + jp, jk)] * zdjs) * c->r1_e2v[I2(ji, jj)];
+          zdxrho[I3(ji + ip, jj, jk) + n3 * (1 - ip)] = sign_nsz(repsln > fabs(xr) ? repsln : fabs(xr), xr);
+          zdyrho[I3(ji, jj + jp, jk) + n3 * (1 - jp)] = sign_nsz(repsln > fabs(yr) ? repsln : fabs(yr), yr);
+        }
+  }
+  for (int kp = 0; kp <= 1; ++kp)                                        /* :446-463 */
+    for (int jk = 1; jk <= jpk - 1; ++jk)
+      for (size_t p = 0; p < n2; ++p) {
+        const int k = jk + kp;
+        const size_t q = p + n2 * (k - 1);
+        double zdkt = 0.0, zdks = 0.0;
+        if (k > 1) { zdkt = tt[q - n2] - tt[q]; zdks = ts[q - n2] - ts[q]; }
+        const double zr = (-ra[q] * zdkt + rb[q] * zdks) / e3w[q];
+        zdzrho[p + n2 * (jk - 1) + n3 * kp] = -(-repsln < zr ? -repsln : zr);
+      }
+  for (int jj = 1; jj <= jpj; ++jj)                                      /* :465-470 */
+    for (int ji = 1; ji <= jpi; ++ji) {
+      const size_t p = I2(ji, jj);
+      int jk = (nmln[p] < c->mbkt[p] ? nmln[p] : c->mbkt[p]) + 1;
+      jk = jk < 1 ? 1 : jk;   /* kept in the column whatever nmln holds */
+      z1_mlbw[p] = 1.0 / gdepw[I3(ji, jj, jk)];
+    }
+  if (wslp2) memset(wslp2, 0, n3 * sizeof(double));                     /* :478-483 */
+  for (int a = 0; a < 4; ++a)
+    for (size_t p = 0; p < n2; ++p) {
+      tig[p + n3 * a] = 0.0; tig[p + n2 * (jpk - 1) + n3 * a] = 0.0;
+      tjg[p + n3 * a] = 0.0; tjg[p + n2 * (jpk - 1) + n3 * a] = 0.0;
+      ti[p + n3 * a] = 0.0; ti[p + n2 * (jpk - 1) + n3 * a] = 0.0;
+      tj[p + n3 * a] = 0.0; tj[p + n2 * (jpk - 1) + n3 * a] = 0.0;
+    }
+  for (int jl = 0; jl <= 1; ++jl)                                        /* :489-521 */
+    for (int kp = 0; kp <= 1; ++kp)
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          const int ip = jl, jp = jl;
+          int jk = nmln[I2(ji + ip, jj)] + 1;
+          double *mi = &zti_mlb[I2(ji + ip, jj) + n2 * ((1 - ip) + 2 * kp)];
+          if (jk > c->mbkt[I2(ji + ip, jj)] || jk - kp < 1) {   /* (jk - kp >= 1 for nmln >= 1) */
+            *mi = 0.0;
+          } else {
+            const double g = (zdxrho[I3(ji + ip, jj, jk - kp) + n3 * (1 - ip)] / zdzrho[I3(ji + ip, jj, jk - kp) + n3 * kp]
+                              - (gdept[I3(ji + 1, jj, jk - kp)] - gdept[I3(ji, jj, jk - kp)]) * c->r1_e1u[I2(ji, jj)])
+                             * umask[I3(ji, jj, jk)];
+            const double ze3_e1 = e3w[I3(ji + ip, jj, jk - kp)] * c->r1_e1u[I2(ji, jj)];
+            *mi = sign_nsz(dmin3(slpmax, 5.0 * ze3_e1, fabs(g)), g);
+          }
+          jk = nmln[I2(ji, jj + jp)] + 1;
+          double *mj = &ztj_mlb[I2(ji, jj + jp) + n2 * ((1 - jp) + 2 * kp)];
+          if (jk > c->mbkt[I2(ji, jj + jp)] || jk - kp < 1) {
+            *mj = 0.0;
+          } else {
+            const double g = (zdyrho[I3(ji, jj + jp, jk - kp) + n3 * (1 - jp)] / zdzrho[I3(ji, jj + jp, jk - kp) + n3 * kp]
+                              - (gdept[I3(ji, jj + 1, jk - kp)] - gdept[I3(ji, jj, jk - kp)]) / c->e2v[I2(ji, jj)])
+                             * vmask[I3(ji, jj, jk)];
+            const double ze3_e2 = e3w[I3(ji, jj + jp, jk - kp)] / c->e2v[I2(ji, jj)];
+            *mj = sign_nsz(dmin3(slpmax, 5.0 * ze3_e2, fabs(g)), g);
+          }
+        }
+  for (int kp = 0; kp <= 1; ++kp)                                        /* :527-609 */
+    for (int jl = 0; jl <= 1; ++jl) {
+      const int ip = jl, jp = jl;
+      for (int jk = 1; jk <= jpk - 1; ++jk) {
+        const double znot = (jk + kp == 1) ? 0.0 : 1.0;
+        for (int jj = 1; jj <= jpj - 1; ++jj)
+          for (int ji = 1; ji <= jpi - 1; ++ji) {
+            const size_t pi = I2(ji + ip, jj), pj = I2(ji, jj + jp), pu = I2(ji, jj);
+            const double dxr = zdxrho[I3(ji + ip, jj, jk) + n3 * (1 - ip)];
+            const double dyr = zdyrho[I3(ji, jj + jp, jk) + n3 * (1 - jp)];
+            double zti_raw = dxr / zdzrho[I3(ji + ip, jj, jk) + n3 * kp];
+            double ztj_raw = dyr / zdzrho[I3(ji, jj + jp, jk) + n3 * kp];
+            const double zti_coord = znot * (gdept[I3(ji + 1, jj, jk)] - gdept[I3(ji, jj, jk)]) * c->r1_e1u[pu];
+            const double ztj_coord = znot * (gdept[I3(ji, jj + 1, jk)] - gdept[I3(ji, jj, jk)]) * c->r1_e2v[pu];
+            const double zti_g_raw = zti_raw - zti_coord, ztj_g_raw = ztj_raw - ztj_coord;
+            const double ze3_e1 = e3w[I3(ji + ip, jj, jk + kp)] * c->r1_e1u[pu];
+            const double ze3_e2 = e3w[I3(ji, jj + jp, jk + kp)] * c->r1_e2v[pu];
+            double zti_g_lim = sign_nsz(dmin3(slpmax, 5.0 * ze3_e1, fabs(zti_g_raw)), zti_g_raw);
+            double ztj_g_lim = sign_nsz(dmin3(slpmax, 5.0 * ze3_e2, fabs(ztj_g_raw)), ztj_g_raw);
+            const double zfacti = (jk + kp - 1 >= nmln[pi]) ? 1.0 : 0.0;
+            const double zfactj = (jk + kp - 1 >= nmln[pj]) ? 1.0 : 0.0;
+            zti_g_lim = (zfacti * zti_g_lim + (1.0 - zfacti) * zti_mlb[pi + n2 * ((1 - ip) + 2 * kp)] *
+                         gdepw[I3(ji + ip, jj, jk + kp)] * z1_mlbw[pi]) * umask[I3(ji, jj, jk + kp)];
+            ztj_g_lim = (zfactj * ztj_g_lim + (1.0 - zfactj) * ztj_mlb[pj + n2 * ((1 - jp) + 2 * kp)] *
+                         gdepw[I3(ji, jj + jp, jk + kp)] * z1_mlbw[pj]) * vmask[I3(ji, jj, jk + kp)];
+            tig[TRI(ji + ip, jj, jk, 1 - ip, kp)] = zti_g_lim;
+            tjg[TRI(ji, jj + jp, jk, 1 - jp, kp)] = ztj_g_lim;
+            double zti_lim = (zti_g_lim + zti_coord) * umask[I3(ji, jj, jk + kp)];
+            double ztj_lim = (ztj_g_lim + ztj_coord) * vmask[I3(ji, jj, jk + kp)];
+            if (nm->ln_triad_iso) {                                      /* :581-588 */
+              zti_raw = zti_lim * zti_lim / zti_raw;
+              ztj_raw = ztj_lim * ztj_lim / ztj_raw;
+              zti_raw = sign_nsz(fabs(zti_lim) < fabs(zti_raw) ? fabs(zti_lim) : fabs(zti_raw), zti_raw);
+              ztj_raw = sign_nsz(fabs(ztj_lim) < fabs(ztj_raw) ? fabs(ztj_lim) : fabs(ztj_raw), ztj_raw);
+              zti_lim = zfacti * zti_lim + (1.0 - zfacti) * zti_raw;
+              ztj_lim = zfactj * ztj_lim + (1.0 - zfactj) * ztj_raw;
+            }
+            const double zisw = (1.0 - sw) + sw * 2.0 * fabs(0.5 - kp - (0.5 - ip) * sign_nsz(1.0, dxr));
+            const double zjsw = (1.0 - sw) + sw * 2.0 * fabs(0.5 - kp - (0.5 - jp) * sign_nsz(1.0, dyr));
+            ti[TRI(ji + ip, jj, jk, 1 - ip, kp)] = zti_lim * zisw;
+            tj[TRI(ji, jj + jp, jk, 1 - jp, kp)] = ztj_lim * zjsw;
+            if (wslp2) {
+              const double zbu = c->e1e2u[pu] * e3u[I3(ji, jj, jk)], zbv = c->e1e2v[pu] * e3v[I3(ji, jj, jk)];
+              const double zbti = c->e1e2t[pi] * e3w[I3(ji + ip, jj, jk + kp)];
+              const double zbtj = c->e1e2t[pj] * e3w[I3(ji, jj + jp, jk + kp)];
+              wslp2[I3(ji + ip, jj, jk + kp)] += 0.25 * zbu / zbti * zti_g_lim * zti_g_lim;
+              wslp2[I3(ji, jj + jp, jk + kp)] += 0.25 * zbv / zbtj * ztj_g_lim * ztj_g_lim;
+            }
+          }
+      }
+    }
+  if (wslp2) {                                                           /* :611-613 */
+    memset(wslp2, 0, n2 * sizeof(double));
+    lbc_closed(jpi, jpj, wslp2, jpk, 'W', 0.0);
+  }
+  wfree(zdxrho); wfree(zdyrho); wfree(zdzrho); wfree(zti_mlb); wfree(ztj_mlb); wfree(z1_mlbw);
+  return NEMO_OK;
+}
+
+/* tra_ldf_triad (traldf_triad.F90:50-429), no eddy-induced velocity, l_grad_zps =
+ * .FALSE. (pgu, pgv, pgui, pgvi unread): in the first pass ah_wslp2 and akz from the
+ * triads (:135-222); per tracer the horizontal fluxes of the four triads of each
+ * u- (v-) face and their vertical counterparts at the triads' w-points, masked by
+ * the face's mask at the w-level unless ln_botmix_triad (:260-358), the horizontal
+ * divergence added level by level, then the 33 flux and the vertical divergence
+ * (:370-410). Reads the bound triad arrays and writes the bound AH_WSLP2, AKZ. */
+int ora_tra_ldf_triad(ora_ctx *c, int kt, int kit000, const char *cdtype, const double *pahu,
+                      const double *pahv, const double *pgu, const double *pgv, const double *pgui,
+                      const double *pgvi, const double *ptb, const double *ptbb, double *pta, int kjpt, int kpass) {
+  (void)cdtype; (void)pgu; (void)pgv; (void)pgui; (void)pgvi;
+  const nemo_namelist *nm = &c->nam;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  double **F = c->f;
+  double *ah_wslp2 = F[NEMO_F_AH_WSLP2], *akz = F[NEMO_F_AKZ];
+  const double *tig = F[NEMO_F_TRIADI_G], *tjg = F[NEMO_F_TRIADJ_G], *ti = F[NEMO_F_TRIADI], *tj = F[NEMO_F_TRIADJ];
+  if (!ptb || !pta || kjpt < 1 || (kpass != 1 && kpass != 2) || (kpass == 2 && !ptbb)) return NEMO_ERR_ARG;
+  if (!ah_wslp2 || !akz || !tig || !tjg || !ti || !tj) return NEMO_ERR_UNBOUND;
+  if (!pahu) pahu = c->ahtu_c;
+  if (!pahv) pahv = c->ahtv_c;
+  const double *tmask = c->tmask, *umask = c->umask, *vmask = c->vmask;
+  const double *e3u = fld(c, NEMO_F_E3U_N), *e3v = fld(c, NEMO_F_E3V_N), *e3t = fld(c, NEMO_F_E3T_N);
+  const double *e3w = fld(c, NEMO_F_E3W_N), *gdept = fld(c, NEMO_F_GDEPT_N);
+  if (!gdept) return NEMO_ERR_UNBOUND;
+  const double z2dt = (nm->neuler == 0 && kt == kit000) ? nm->rn_rdt : 2. * nm->rn_rdt;   /* :117-120 */
+  const double z1_2dt = 1.0 / z2dt;
+  const double zsign = kpass == 1 ? 1.0 : -1.0;
+  if (kpass == 1) {                                                      /* :131-222 */
+    memset(akz, 0, n3 * sizeof(double));
+    memset(ah_wslp2, 0, n3 * sizeof(double));
+    for (int ip = 0; ip <= 1; ++ip)
+      for (int kp = 0; kp <= 1; ++kp)
+        for (int jk = 1; jk <= jpk - 1; ++jk)
+          for (int jj = 1; jj <= jpj - 1; ++jj)
+            for (int ji = 1; ji <= jpi - 1; ++ji) {
+              const size_t pu = I2(ji, jj), w = I3(ji + ip, jj, jk + kp);
+              const double ze3wr = 1.0 / e3w[w];
+              const double zbu = c->e1e2u[pu] * e3u[I3(ji, jj, jk)];
+              const double zah = 0.25 * pahu[I3(ji, jj, jk)];
+              const double skew = tig[TRI(ji + ip, jj, jk, 1 - ip, kp)];
+              double s2 = skew + (gdept[I3(ji + 1, jj, jk)] - gdept[I3(ji, jj, jk)]) * c->r1_e1u[pu] * umask[I3(ji, jj, jk + kp)];
+              s2 = s2 * s2;
+              ah_wslp2[w] = ah_wslp2[w] + zah * zbu * ze3wr * c->r1_e1e2t[I2(ji + ip, jj)] * s2;
+              akz[w] = akz[w] + zah * c->r1_e1u[pu] * c->r1_e1u[pu] * umask[I3(ji, jj, jk + kp)];
+            }
+    for (int jp = 0; jp <= 1; ++jp)
+      for (int kp = 0; kp <= 1; ++kp)
+        for (int jk = 1; jk <= jpk - 1; ++jk)
+          for (int jj = 1; jj <= jpj - 1; ++jj)
+            for (int ji = 1; ji <= jpi - 1; ++ji) {
+              const size_t pv = I2(ji, jj), w = I3(ji, jj + jp, jk + kp);
+              const double ze3wr = 1.0 / e3w[w];
+              const double zbv = c->e1e2v[pv] * e3v[I3(ji, jj, jk)];
+              const double zah = 0.25 * pahv[I3(ji, jj, jk)];
+              const double skew = tjg[TRI(ji, jj + jp, jk, 1 - jp, kp)];
+              double s2 = skew + (gdept[I3(ji, jj + 1, jk)] - gdept[I3(ji, jj, jk)]) * c->r1_e2v[pv] * vmask[I3(ji, jj, jk + kp)];
+              s2 = s2 * s2;
+              ah_wslp2[w] = ah_wslp2[w] + zah * zbv * ze3wr * c->r1_e1e2t[I2(ji, jj + jp)] * s2;
+              akz[w] = akz[w] + zah * c->r1_e2v[pv] * c->r1_e2v[pv] * vmask[I3(ji, jj, jk + kp)];
+            }
+    if (nm->ln_traldf_msc) {                                             /* :190-212 */
+      for (int jk = 2; jk <= jpk - 1; ++jk)
+        for (int jj = 1; jj <= jpj - 1; ++jj)
+          for (int ji = 1; ji <= jpi - 1; ++ji) {
+            const size_t q = I3(ji, jj, jk);
+            if (nm->ln_traldf_blp) {
+              akz[q] = 16.0 * ah_wslp2[q] * (akz[q] + ah_wslp2[q] / (e3w[q] * e3w[q]));
+            } else {
+              const double ze3w_2 = e3w[q] * e3w[q];
+              const double zcoef0 = z2dt * (akz[q] + ah_wslp2[q] / ze3w_2);
+              akz[q] = (zcoef0 - 0.5 > 0.0 ? zcoef0 - 0.5 : 0.0) * ze3w_2 * z1_2dt;
+            }
+          }
+    } else {                                                             /* :214-215 */
+      memcpy(akz, ah_wslp2, n3 * sizeof(double));
+    }
+  }
+  double *zdit = zalloc(n3), *zdjt = zalloc(n3), *zftu = walloc(n3), *zftv = walloc(n3), *ztfw = walloc(n3);
+  double *zdk0 = walloc(n2), *zdk1 = walloc(n2);
+  for (int jn = 0; jn < kjpt; ++jn) {
+    const double *tb = ptb + n3 * jn, *tbb = kpass == 2 ? ptbb + n3 * jn : NULL;
+    double *ta = pta + n3 * jn;
+    memset(ztfw, 0, n3 * sizeof(double));
+    memset(zftu, 0, n3 * sizeof(double));
+    memset(zftv, 0, n3 * sizeof(double));
+    for (int jk = 1; jk <= jpk - 1; ++jk)                                /* :234-241 */
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 1; ji <= jpi - 1; ++ji) {
+          const size_t q = I3(ji, jj, jk);
+          zdit[q] = (tb[I3(ji + 1, jj, jk)] - tb[q]) * umask[q];
+          zdjt[q] = (tb[I3(ji, jj + 1, jk)] - tb[q]) * vmask[q];
+        }
+    for (int jk = 1; jk <= jpk - 1; ++jk) {                              /* :263-364 */
+      for (size_t p = 0; p < n2; ++p) {
+        const size_t q = p + n2 * (jk - 1);
+        zdk1[p] = (tb[q] - tb[q + n2]) * tmask[q + n2];
+        zdk0[p] = jk == 1 ? zdk1[p] : (tb[q - n2] - tb[q]) * tmask[q];
+      }
+      for (int ip = 0; ip <= 1; ++ip)
+        for (int kp = 0; kp <= 1; ++kp)
+          for (int jj = 1; jj <= jpj - 1; ++jj)
+            for (int ji = 1; ji <= jpi - 1; ++ji) {
+              const size_t pu = I2(ji, jj), q = I3(ji, jj, jk), w = I3(ji + ip, jj, jk + kp);
+              const double ze1ur = c->r1_e1u[pu];
+              const double zdxt = zdit[q] * ze1ur;
+              const double ze3wr = 1.0 / e3w[w];
+              const double zdzt = (kp ? zdk1 : zdk0)[I2(ji + ip, jj)] * ze3wr;
+              const double zslope_iso = ti[TRI(ji + ip, jj, jk, 1 - ip, kp)];
+              const double zbu = 0.25 * c->e1e2u[pu] * e3u[q];
+              const double zah = nm->ln_botmix_triad ? pahu[q] : pahu[q] * umask[I3(ji, jj, jk + kp)];
+              const double zah_slp = zah * zslope_iso;
+              const double zaei_slp = 0.0;
+              zftu[q] = zftu[q] - (zah * zdxt + (zah_slp - zaei_slp) * zdzt) * zbu * ze1ur;
+              ztfw[w] = ztfw[w] - (zah_slp + zaei_slp) * zdxt * zbu * ze3wr;
+            }
+      for (int jp = 0; jp <= 1; ++jp)
+        for (int kp = 0; kp <= 1; ++kp)
+          for (int jj = 1; jj <= jpj - 1; ++jj)
+            for (int ji = 1; ji <= jpi - 1; ++ji) {
+              const size_t pv = I2(ji, jj), q = I3(ji, jj, jk), w = I3(ji, jj + jp, jk + kp);
+              const double ze2vr = c->r1_e2v[pv];
+              const double zdyt = zdjt[q] * ze2vr;
+              const double ze3wr = 1.0 / e3w[w];
+              const double zdzt = (kp ? zdk1 : zdk0)[I2(ji, jj + jp)] * ze3wr;
+              const double zslope_iso = tj[TRI(ji, jj + jp, jk, 1 - jp, kp)];
+              const double zbv = 0.25 * c->e1e2v[pv] * e3v[q];
+              const double zah = nm->ln_botmix_triad ? pahv[q] : pahv[q] * vmask[I3(ji, jj, jk + kp)];
+              const double zah_slp = zah * zslope_iso;
+              const double zaei_slp = 0.0;
+              zftv[q] = zftv[q] - (zah * zdyt + (zah_slp - zaei_slp) * zdzt) * zbv * ze2vr;
+              ztfw[w] = ztfw[w] - (zah_slp + zaei_slp) * zdyt * zbv * ze3wr;
+            }
+      for (int jj = 2; jj <= jpj - 1; ++jj)                              /* :356-363 */
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          const size_t q = I3(ji, jj, jk);
+          ta[q] = ta[q] + zsign * (zftu[I3(ji - 1, jj, jk)] - zftu[q] + zftv[I3(ji, jj - 1, jk)] - zftv[q]) /
+                              (c->e1e2t[I2(ji, jj)] * e3t[q]);
+        }
+    }
+    for (int jk = 2; jk <= jpk - 1; ++jk)                                /* :368-402 */
+      for (int jj = 1; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          const size_t q = I3(ji, jj, jk), p = I2(ji, jj);
+          if (nm->ln_traldf_lap)
+            ztfw[q] = ztfw[q] - c->e1e2t[p] / e3w[q] * tmask[q] * (ah_wslp2[q] - akz[q]) * (tb[q - n2] - tb[q]);
+          else if (kpass == 1)
+            ztfw[q] = ztfw[q] - c->e1e2t[p] / e3w[q] * tmask[q] * ah_wslp2[q] * (tb[q - n2] - tb[q]);
+          else
+            ztfw[q] = ztfw[q] - c->e1e2t[p] / e3w[q] * tmask[q] *
+                                    (ah_wslp2[q] * (tb[q - n2] - tb[q]) + akz[q] * (tbb[q - n2] - tbb[q]));
+        }
+    for (int jk = 1; jk <= jpk - 1; ++jk)                                /* :404-410 */
+      for (int jj = 2; jj <= jpj - 1; ++jj)
+        for (int ji = 2; ji <= jpi - 1; ++ji) {
+          const size_t q = I3(ji, jj, jk);
+          ta[q] = ta[q] + zsign * (ztfw[q + n2] - ztfw[q]) / (c->e1e2t[I2(ji, jj)] * e3t[q]);
+        }
+  }
+  wfree(zdit); wfree(zdjt); wfree(zftu); wfree(zftv); wfree(ztfw); wfree(zdk0); wfree(zdk1);
+  return NEMO_OK;
+}
+#undef TRI
 
 /* ---------------------------------------------------------------- ldf_slp */
 /* ldf_slp (ldfslp.F90:83-374) with ldf_slp_mxl (:620-729): z-coordinate without

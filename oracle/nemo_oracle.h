@@ -115,6 +115,11 @@ int ora_dom_vvl_sf_swp(ora_ctx *c, int kt);
 int ora_stp_model(ora_ctx *c, int kt);
 /* ldf_slp with ldf_slp_mxl (z-coordinate, no cavities, no partial steps); NMLN is
  * bound as an int array. */
+/* the triad operator: ldf_slp_triad (ldfslp.F90:377-617), tra_ldf_triad (traldf_triad.F90:50-429) */
+int ora_ldf_slp_triad(ora_ctx *c, int kt, const double *prab_b);
+int ora_tra_ldf_triad(ora_ctx *c, int kt, int kit000, const char *cdtype, const double *pahu,
+                      const double *pahv, const double *pgu, const double *pgv, const double *pgui,
+                      const double *pgvi, const double *ptb, const double *ptbb, double *pta, int kjpt, int kpass);
 int ora_ldf_slp(ora_ctx *c, int kt, const double *prd, const double *pn2);
 /* tra_sbc and tra_qsr (two bands) on the bound surface forcing; nksr: the level of
  * light extinction found at creation. */

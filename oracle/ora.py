@@ -66,6 +66,8 @@ def lib():
                      "ora_dom_vvl_sf_swp", "ora_stp_model", "ora_tra_sbc", "ora_tra_qsr"):
             P(name, [vp, i])
         P("ora_ldf_slp", [vp, i, vp, vp])
+        P("ora_ldf_slp_triad", [vp, i, vp])
+        P("ora_tra_ldf_triad", [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
         P("ora_nksr", [vp], C.c_int)
         P("ora_eos_insitu", [vp, vp, vp, vp])
         P("ora_eos_insitu_pot", [vp, vp, vp, vp, vp])
@@ -341,6 +343,14 @@ class Oracle:
 
     def ldf_slp(self, kt, prd, pn2):
         self._ck(lib().ora_ldf_slp(self.h, kt, _p(prd), _p(pn2)), "ldf_slp")
+
+    def ldf_slp_triad(self, kt, prab_b):
+        self._ck(lib().ora_ldf_slp_triad(self.h, kt, _p(prab_b)), "ldf_slp_triad")
+
+    def tra_ldf_triad(self, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb, ptbb, pta, kjpt, kpass):
+        self._ck(lib().ora_tra_ldf_triad(self.h, kt, kit000, cdtype.encode(), _p(pahu), _p(pahv), _p(pgu), _p(pgv),
+                                         _p(pgui), _p(pgvi), _p(ptb), _p(ptbb), _p(pta), kjpt, kpass),
+                 "tra_ldf_triad")
 
     def tra_ldf_blp(self, kt, kit000, cdtype, pahu, pahv, pgu, pgv, pgui, pgvi, ptb, pta, kjpt, kldf):
         self._ck(lib().ora_tra_ldf_blp(self.h, kt, kit000, cdtype.encode(), _p(pahu), _p(pahv), _p(pgu), _p(pgv),
