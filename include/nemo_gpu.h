@@ -607,6 +607,27 @@ int nemo_gpu_tra_zdf_imp_adj(nemo_ctx *ctx, int kt, int kit000, const char *cdty
  * swapped tsb, tsn, tsa, on exit those of the fields before the swap. */
 int nemo_gpu_tra_nxt_adj(nemo_ctx *ctx, int kt, void *tsb_ad, void *tsn_ad, void *tsa_ad);
 
+/* Adjoint arrays of dyn_spg_ts (FP64, laid out like the fields they shadow, per
+ * member): of the outputs only -- ssha, ua_b, va_b, un_adv, vn_adv: read, then
+ * zeroed (the forward overwrites them); in and out -- ua, va, un, vn (3-D) and ub2_b,
+ * vb2_b, un_bf, vn_bf: on entry the adjoint of the value after the call, on exit
+ * that of the value before; of the inputs only -- sshn, un_b, vn_b, ub_b, vb_b:
+ * accumulated. */
+typedef struct nemo_spg_adj {
+  void *ua, *va, *un, *vn;
+  void *ssha, *ua_b, *va_b, *un_adv, *vn_adv;
+  void *ub2_b, *vb2_b, *un_bf, *vn_bf;
+  void *sshn, *un_b, *vn_b, *ub_b, *vb_b;
+} nemo_spg_adj;
+/* dyn_spg_ts_adj: the adjoint of nemo_gpu_dyn_spg_ts (dynspg_ts.F90:121-1310) with
+ * respect to the state, with the forcing (wind stress, E-P, runoff, atmospheric
+ * pressure), the bottom drag coefficient and the Coriolis factors held fixed: phase
+ * 3, the sub-steps in reverse order, phase 1. Linear free surface, ln_bt_fw and
+ * ln_bt_av (every step starts the sub-steps from sshn, un_b, vn_b), the vorticity
+ * schemes ENE, ENS, EEN and MIX (not ENT: NEMO_ERR_UNSUPPORTED). Uses the sub-step
+ * count and weights of the forward's last call: run nemo_gpu_dyn_spg_ts(kt) first. */
+int nemo_gpu_dyn_spg_ts_adj(nemo_ctx *ctx, int kt, const nemo_spg_adj *adj);
+
 /* dyn_spg_ts (dynspg_ts.F90:121-1310) on the bound fields: phase 1 forcing,
  * icycle barotropic sub-steps in one persistent kernel, phase 3 correction. */
 int nemo_gpu_dyn_spg_ts(nemo_ctx *ctx, int kt);
@@ -734,6 +755,7 @@ enum nemo_kernel_id {
   NEMO_K_VVL_SF,       /* z*: the after scale factors and the swap (dom_vvl_sf_nxt/_swp) */
   NEMO_K_VVL_NXT,      /* z*: tra_nxt_vvl, dyn_nxt's filter of e3 and velocities, ssh_swp */
   NEMO_K_TRIAD,        /* the triad operator: slopes, coefficients, fluxes, divergence */
+  NEMO_K_SPG_ADJ,      /* the adjoint of dyn_spg_ts (phase 3, reverse sub-steps, phase 1) */
   NEMO_K_COUNT
 };
 

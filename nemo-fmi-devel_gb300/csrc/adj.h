@@ -22,6 +22,30 @@ struct LdfAdj {
   double *dit, *djt, *dk;   // work: adjoints of the gradients (jpi,jpj,jpk,kjpt)
 };
 
+// the adjoint of dyn_spg_ts (k_spg_adj.cuh)
+struct SpgAdjArgs {
+  double *ua, *va, *un, *vn;                    // 3-D adjoints (in/out)
+  double *ssha, *ua_b, *va_b, *un_adv, *vn_adv; // adjoints of outputs only (read, then zeroed)
+  double *ub2_b, *vb2_b, *un_bf, *vn_bf;        // in/out
+  double *sshn, *un_b, *vn_b, *ub_b, *vb_b;     // adjoints of inputs only (accumulated)
+  const double* rcdu;                           // the forward's bottom drag coefficient
+  // work, (jpi,jpj) per member
+  double *X, *Y, *uab, *vab;                    // adjoints of the sub-step sums un_adv, vn_adv, ua_b, va_b
+  double *Au, *Aub, *Aubb, *Av, *Avb, *Avbb;    // carried adjoints of un_e, ub_e, ubb_e (vn_e ...)
+  double *Sn, *Sb, *Sbb;                        // of sshn_e, sshb_e, sshbb_e
+  double *Fu, *Fv;                              // of the barotropic forcing zu_frc, zv_frc
+  double *gu, *gv, *zhd;                        // per sub-step
+  double r1_2dt_b, atfp, rdtbt, grav, sl;
+  int euler, sc;
+};
+
+// per sub-step constants
+struct SpgAdjStep {
+  double w1, w2;              // wgtbtp1, wgtbtp2 of the sub-step
+  double zb1, zb2, zb3;       // AB3 extrapolation (:724-736)
+  double za0, za1, za2, za3;  // AM4 ssh (:904-931)
+};
+
 struct ZdfAdj {
   double* lam;     // pta_ad: in, the after tracer's adjoint; out, the trend's
   double* tb_ad;
@@ -36,5 +60,8 @@ template <class T>
 cudaError_t launch_tra_nxt(const Dom<T>& d, T* tsb, T* tsn, T* tsa, T atfp, int euler, cudaStream_t s);
 cudaError_t launch_tra_nxt_adj(const Dom<double>& d, double* tsb_ad, double* tsn_ad, double* tsa_ad, double atfp,
                                int euler, cudaStream_t s);
+// the adjoint of dyn_spg_ts: steps[jn - 1] holds the constants of sub-step jn
+cudaError_t launch_spg_adj(const Dom<double>& d, const SpgAdjArgs& a, const SpgAdjStep* steps, int icycle,
+                           cudaStream_t s);
 
 }  // namespace nemo

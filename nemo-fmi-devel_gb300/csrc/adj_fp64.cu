@@ -1,6 +1,7 @@
 // adj_fp64.cu -- launchers of the adjoint kernels and of tra_nxt. Compiled with
 // --fmad=false like the FP64 forward kernels.
 #include "k_adj.cuh"
+#include "k_spg_adj.cuh"
 #include "launch.h"
 
 namespace nemo {
@@ -60,6 +61,19 @@ cudaError_t launch_tra_nxt_adj(const Dom<double>& d, double* tsb_ad, double* tsn
                                int euler, cudaStream_t s) {
   k_tra_nxt_adj<<<apt_grid(d), dim3(AX, AY), 0, s>>>(d, tsb_ad, tsn_ad, tsa_ad, atfp, euler);
   ktick(NEMO_K_TRA_NXT_ADJ, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spg_adj(const Dom<double>& d, const SpgAdjArgs& a, const SpgAdjStep* steps, int icycle,
+                           cudaStream_t s) {
+  k_spg_adj_p3<<<acol_grid(d), dim3(AX, AY), 0, s>>>(d, a);
+  for (int jn = icycle; jn >= 1; --jn) {
+    k_spg_adj_s1<<<acol_grid(d), dim3(AX, AY), 0, s>>>(d, a, steps[jn - 1]);
+    k_spg_adj_s2<<<acol_grid(d), dim3(AX, AY), 0, s>>>(d, a, steps[jn - 1]);
+    k_spg_adj_s3<<<acol_grid(d), dim3(AX, AY), 0, s>>>(d, a, steps[jn - 1]);
+  }
+  k_spg_adj_p1<<<acol_grid(d), dim3(AX, AY), 0, s>>>(d, a);
+  ktick(NEMO_K_SPG_ADJ, s);
   return cudaGetLastError();
 }
 

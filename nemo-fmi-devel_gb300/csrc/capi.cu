@@ -80,6 +80,7 @@ struct nemo_ctx {
   void* fct_ztw = nullptr;
   void* iso_w[3] = {};         // iso-neutral fluxes zftu, zftv, ztfw
   void* adj_w[4] = {};         // iso-neutral adjoint: G and the gradient adjoints
+  double* spgadj_w = nullptr;  // dyn_spg_ts adjoint: 18 (jpi,jpj) arrays per member
   int adj_kjpt = 0;
   void* slp_w = nullptr;       // ldf_slp work: 4 3-D and 6 2-D arrays per member
   void* rab_w = nullptr;       // the model step's before expansion ratios rab_b (jpi,jpj,jpk,2)
@@ -2735,6 +2736,68 @@ int nemo_gpu_tra_zdf_imp_adj(nemo_ctx* c, int kt, int kit000, const char* cdtype
   ZdfAdj b{(double*)pta_ad, (double*)ptb_ad};
   cudaError_t e = launch_zdf_adj(dom_now<double>(c), a, b, c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "tra_zdf_imp_adj launch");
+  return NEMO_OK;
+}
+
+int nemo_gpu_dyn_spg_ts_adj(nemo_ctx* c, int kt, const nemo_spg_adj* adj) {
+  if (!c) return NEMO_ERR_ARG;
+  if (c->prec != NEMO_PREC_FP64) return fail(c, NEMO_ERR_ARG, "dyn_spg_ts_adj: FP64 contexts only");
+  if (!adj) return fail(c, NEMO_ERR_ARG, "dyn_spg_ts_adj: adj is NULL");
+  void* const ptrs[] = {adj->ua, adj->va, adj->un, adj->vn, adj->ssha, adj->ua_b, adj->va_b, adj->un_adv, adj->vn_adv,
+                        adj->ub2_b, adj->vb2_b, adj->un_bf, adj->vn_bf, adj->sshn, adj->un_b, adj->vn_b, adj->ub_b,
+                        adj->vb_b};
+  for (void* q : ptrs)
+    if (!q) return fail(c, NEMO_ERR_ARG, "dyn_spg_ts_adj: null adjoint array");
+  const nemo_namelist& nm = c->nam;
+  if (!nm.ln_linssh || !nm.ln_bt_fw || !nm.ln_bt_av || nm.nvor_scheme == NEMO_VOR_ENT)
+    return fail(c, NEMO_ERR_UNSUPPORTED,
+                "dyn_spg_ts_adj: linear free surface with ln_bt_fw and ln_bt_av, vorticity ENE, ENS, EEN or MIX");
+  if (!c->f[NEMO_F_RCDU_BOT]) return fail(c, NEMO_ERR_UNBOUND, "dyn_spg_ts_adj: rcdu_bot must be bound");
+  if (c->icycle < 1 || (int)c->wgt1.size() < c->icycle)
+    return fail(c, NEMO_ERR_STATE, "dyn_spg_ts_adj: run the forward dyn_spg_ts first (sub-step weights)");
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  const size_t n2m = (size_t)c->n2 * c->nmem;
+  if (!c->spgadj_w && cudaMalloc(&c->spgadj_w, 18 * n2m * sizeof(double)) != cudaSuccess)
+    return fail(c, NEMO_ERR_NOMEM, "dyn_spg_ts_adj work arrays");
+  SpgAdjArgs a{};
+  a.ua = (double*)adj->ua; a.va = (double*)adj->va; a.un = (double*)adj->un; a.vn = (double*)adj->vn;
+  a.ssha = (double*)adj->ssha; a.ua_b = (double*)adj->ua_b; a.va_b = (double*)adj->va_b;
+  a.un_adv = (double*)adj->un_adv; a.vn_adv = (double*)adj->vn_adv;
+  a.ub2_b = (double*)adj->ub2_b; a.vb2_b = (double*)adj->vb2_b; a.un_bf = (double*)adj->un_bf;
+  a.vn_bf = (double*)adj->vn_bf;
+  a.sshn = (double*)adj->sshn; a.un_b = (double*)adj->un_b; a.vn_b = (double*)adj->vn_b;
+  a.ub_b = (double*)adj->ub_b; a.vb_b = (double*)adj->vb_b;
+  a.rcdu = (const double*)c->f[NEMO_F_RCDU_BOT];
+  double* w = c->spgadj_w;
+  double** work[] = {&a.X, &a.Y, &a.uab, &a.vab, &a.Au, &a.Aub, &a.Aubb, &a.Av, &a.Avb, &a.Avbb,
+                     &a.Sn, &a.Sb, &a.Sbb, &a.Fu, &a.Fv, &a.gu, &a.gv, &a.zhd};
+  for (int i = 0; i < 18; ++i) *work[i] = w + (size_t)i * n2m;
+  const int euler = kt == nm.nit000 && nm.neuler == 0;
+  a.euler = euler;
+  a.r1_2dt_b = 1.0 / (euler ? nm.rn_rdt : 2.0 * nm.rn_rdt);
+  a.atfp = nm.rn_atfp; a.rdtbt = c->rdtbt; a.grav = nm.grav; a.sl = nm.rn_scal_load;
+  a.sc = nm.nvor_scheme;
+  // the per-sub-step constants of the forward (dynspg_ts.F90:724-736, :904-931), ll_init
+  std::vector<SpgAdjStep> steps(c->icycle);
+  for (int jn = 1; jn <= c->icycle; ++jn) {
+    SpgAdjStep& s = steps[jn - 1];
+    s.w1 = c->wgt1[jn - 1]; s.w2 = c->wgt2[jn - 1];
+    if (jn < 3) { s.zb1 = 1.0; s.zb2 = 0.0; s.zb3 = 0.0; }
+    else { s.zb1 = 1.781105; s.zb2 = -1.06221; s.zb3 = 0.281105; }
+    if (jn == 1) { s.za0 = 1.0; s.za1 = 0.0; s.za2 = 0.0; s.za3 = 0.0; }
+    else if (jn == 2) { s.za0 = 1.0833333333333; s.za1 = -0.1666666666666; s.za2 = 0.0833333333333; s.za3 = 0.0; }
+    else if (nm.rn_bt_alpha == 0.0) { s.za0 = 0.614; s.za1 = 0.285; s.za2 = 0.088; s.za3 = 0.013; }
+    else {
+      const double zepsilon = 0.00976186 - 0.13451357 * nm.rn_bt_alpha;
+      const double zgamma = 0.08344500 - 0.51358400 * nm.rn_bt_alpha;
+      s.za0 = 0.5 + zgamma + 2.0 * nm.rn_bt_alpha + 2.0 * zepsilon;
+      s.za1 = 1.0 - s.za0 - zgamma - zepsilon;
+      s.za2 = zgamma;
+      s.za3 = zepsilon;
+    }
+  }
+  cudaError_t e = launch_spg_adj(dom<double>(c), a, steps.data(), c->icycle, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "dyn_spg_ts_adj launch");
   return NEMO_OK;
 }
 

@@ -42,6 +42,15 @@ class DomDesc(C.Structure):
                 ("e3t_0", _dp), ("e3u_0", _dp), ("e3v_0", _dp), ("e3w_0", _dp), ("e3f_0", _dp)]
 
 
+# members of nemo_spg_adj (the adjoint arrays of dyn_spg_ts), in order
+SPG_ADJ = ("ua", "va", "un", "vn", "ssha", "ua_b", "va_b", "un_adv", "vn_adv", "ub2_b", "vb2_b", "un_bf", "vn_bf",
+           "sshn", "un_b", "vn_b", "ub_b", "vb_b")
+
+
+class SpgAdj(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in SPG_ADJ]
+
+
 class Namelist(C.Structure):
     _fields_ = [("rn_rdt", C.c_double), ("rn_atfp", C.c_double), ("nit000", C.c_int), ("neuler", C.c_int),
                 ("ln_linssh", C.c_int), ("ln_zps", C.c_int), ("ln_isfcav", C.c_int),
@@ -160,6 +169,7 @@ def load(path):
                  "nemo_gpu_stp_model", "nemo_gpu_zdf_phy", "nemo_gpu_usrdef_sbc"):
         _proto(lib, name, i, [vp, i])
     _proto(lib, "nemo_gpu_tra_adv_fct_adj", i, [vp, i, i, cp, d, vp, vp, vp, vp, vp, vp, i, i, i])
+    _proto(lib, "nemo_gpu_dyn_spg_ts_adj", i, [vp, i, C.POINTER(SpgAdj)])
     _proto(lib, "nemo_gpu_tra_ldf_lap_adj", i, [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
     _proto(lib, "nemo_gpu_tra_ldf_iso_adj", i, [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
     _proto(lib, "nemo_gpu_tra_zdf_imp_adj", i, [vp, i, i, cp, d, vp, vp, i])

@@ -348,6 +348,11 @@ class Context:
     def tra_nxt_adj(self, kt, tsb_ad, tsn_ad, tsa_ad):
         self._ck(self.lib.nemo_gpu_tra_nxt_adj(self.h, kt, _ptr(tsb_ad), _ptr(tsn_ad), _ptr(tsa_ad)), "tra_nxt_adj")
 
+    def dyn_spg_ts_adj(self, kt, adj):
+        """adj: dict of device FP64 tensors keyed by the members of nemo_spg_adj."""
+        s = _ffi.SpgAdj(*[_ptr(adj[n]) for n in _ffi.SPG_ADJ])
+        self._ck(self.lib.nemo_gpu_dyn_spg_ts_adj(self.h, kt, C.byref(s)), "dyn_spg_ts_adj")
+
     def dyn_spg_ts(self, kt):
         self._ck(self.lib.nemo_gpu_dyn_spg_ts(self.h, kt), "dyn_spg_ts")
 

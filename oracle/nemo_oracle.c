@@ -2896,6 +2896,224 @@ int ora_tra_zdf_imp_adj(ora_ctx *c, int kt, int kit000, const char *cdtype, doub
   return NEMO_OK;
 }
 
+/* ------------------------------------------------------ dyn_spg_ts adjoint */
+/* The barotropic Coriolis trend of dyn_spg_ts (dynspg_ts.F90:387-443, :1000-1056)
+ * as weights of four neighbouring fluxes: zu_trd(p) = sum_t cu(t,p) zwy(p + du_t)
+ * with du = (0,-1), (1,-1), (0,0), (1,0), and zv_trd(p) = sum_t cv(t,p) zwx(p + dv_t)
+ * with dv = (-1,0), (-1,1), (0,0), (0,1); ENE (and MIX), ENS, EEN. */
+static const int SPG_DUI[4] = {0, 1, 0, 1}, SPG_DUJ[4] = {-1, -1, 0, 0};
+static const int SPG_DVI[4] = {-1, -1, 0, 0}, SPG_DVJ[4] = {0, 1, 0, 1};
+static double spg_cu(const ora_ctx *c, int sc, int t, int ji, int jj) {
+  const int jpi = c->jpi;
+  const size_t p = I2(ji, jj);
+  if (sc == NEMO_VOR_ENS) return 0.125 * c->r1_e1u[p] * (c->zwz[I2(ji, jj - 1)] + c->zwz[p]);
+  if (sc == NEMO_VOR_EEN) {
+    const double f = t == 0 ? c->ftse[p] : t == 1 ? c->ftsw[I2(ji + 1, jj)] : t == 2 ? c->ftne[p] : c->ftnw[I2(ji + 1, jj)];
+    return (1.0 / 12.0) * c->r1_e1u[p] * f;
+  }
+  return 0.25 * (t < 2 ? c->zwz[I2(ji, jj - 1)] : c->zwz[p]) * c->r1_e1u[p];
+}
+static double spg_cv(const ora_ctx *c, int sc, int t, int ji, int jj) {
+  const int jpi = c->jpi;
+  const size_t p = I2(ji, jj);
+  if (sc == NEMO_VOR_ENS) return -0.125 * c->r1_e2v[p] * (c->zwz[I2(ji - 1, jj)] + c->zwz[p]);
+  if (sc == NEMO_VOR_EEN) {
+    const double f = t == 0 ? c->ftnw[p] : t == 1 ? c->ftsw[I2(ji, jj + 1)] : t == 2 ? c->ftne[p] : c->ftse[I2(ji, jj + 1)];
+    return -(1.0 / 12.0) * c->r1_e2v[p] * f;
+  }
+  return -0.25 * (t < 2 ? c->zwz[I2(ji - 1, jj)] : c->zwz[p]) * c->r1_e2v[p];
+}
+/* the transpose: the flux adjoints zwxa, zwya += C^T (gu, gv) for trend adjoints gu,
+ * gv on the interior */
+static void spg_cor_adj(const ora_ctx *c, int sc, const double *gu, const double *gv, double *zwxa, double *zwya) {
+  const int jpi = c->jpi, jpj = c->jpj;
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      const size_t p = I2(ji, jj);
+      for (int t = 0; t < 4; ++t) {
+        zwya[I2(ji + SPG_DUI[t], jj + SPG_DUJ[t])] += spg_cu(c, sc, t, ji, jj) * gu[p];
+        zwxa[I2(ji + SPG_DVI[t], jj + SPG_DVJ[t])] += spg_cv(c, sc, t, ji, jj) * gv[p];
+      }
+    }
+}
+
+/* Adjoint of ora_dyn_spg_ts (the argument roles of nemo_spg_adj in nemo_gpu.h) for a
+ * linear free surface with ln_bt_fw and ln_bt_av: the forward's operations in
+ * reverse order -- phase 3 (:1214-1269), the sub-steps from the last (:712-1207:
+ * sums, swap, lbc, next velocities, bottom stress, pressure gradient, Coriolis, AM4
+ * ssh, ssh update, divergence, flux sums, fluxes, AB3 extrapolation), the start of
+ * the sub-steps from sshn, un_b, vn_b (:665-702), phase 1 (:358-557). The forcing
+ * terms are constants of the map. The weights are those of the last forward call. */
+int ora_dyn_spg_ts_adj(ora_ctx *c, int kt, const nemo_spg_adj *A) {
+  const nemo_namelist *nm = &c->nam;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj;
+  if (!A) return NEMO_ERR_ARG;
+  double *ua_ad = A->ua, *va_ad = A->va, *un_ad = A->un, *vn_ad = A->vn;
+  double *ssha_ad = A->ssha, *uab_ad = A->ua_b, *vab_ad = A->va_b, *unadv_ad = A->un_adv, *vnadv_ad = A->vn_adv;
+  double *ub2_ad = A->ub2_b, *vb2_ad = A->vb2_b, *unbf_ad = A->un_bf, *vnbf_ad = A->vn_bf;
+  double *sshn_ad = A->sshn, *unb_ad = A->un_b, *vnb_ad = A->vn_b, *ubb_ad = A->ub_b, *vbb_ad = A->vb_b;
+  if (!ua_ad || !va_ad || !un_ad || !vn_ad || !ssha_ad || !uab_ad || !vab_ad || !unadv_ad || !vnadv_ad || !ub2_ad ||
+      !vb2_ad || !unbf_ad || !vnbf_ad || !sshn_ad || !unb_ad || !vnb_ad || !ubb_ad || !vbb_ad)
+    return NEMO_ERR_ARG;
+  const int sc = nm->nvor_scheme;
+  if (!nm->ln_linssh || !nm->ln_bt_fw || !nm->ln_bt_av || sc == NEMO_VOR_ENT) return NEMO_ERR_UNSUPPORTED;
+  const double *rCdU_bot = c->f[NEMO_F_RCDU_BOT];
+  if (!rCdU_bot) return NEMO_ERR_UNBOUND;
+  const int euler = kt == nm->nit000 && nm->neuler == 0;
+  const double r1_2dt_b = 1.0 / (euler ? nm->rn_rdt : 2.0 * nm->rn_rdt), atfp = nm->rn_atfp;
+  const double rdtbt = c->rdtbt, grav = nm->grav, sl = nm->rn_scal_load, r1_2 = 0.5;
+  const double *umask = c->umask, *vmask = c->vmask, *e3u = c->e3u_0, *e3v = c->e3v_0;
+  const double *hu = c->hu_0, *hv = c->hv_0, *r1_hu = c->r1_hu_0, *r1_hv = c->r1_hv_0;
+  const double *ssumask = c->ssumask, *ssvmask = c->ssvmask, *ssmask = c->ssmask;
+  double *X = zalloc(n2), *Y = zalloc(n2), *uab = zalloc(n2), *vab = zalloc(n2);
+  double *Au = zalloc(n2), *Aub = zalloc(n2), *Aubb = zalloc(n2), *Av = zalloc(n2), *Avb = zalloc(n2), *Avbb = zalloc(n2);
+  double *Sn = zalloc(n2), *Sb = zalloc(n2), *Sbb = zalloc(n2);
+  double *Nu = zalloc(n2), *Nub = zalloc(n2), *Nubb = zalloc(n2), *Nv = zalloc(n2), *Nvb = zalloc(n2), *Nvbb = zalloc(n2);
+  double *Nsn = zalloc(n2), *Nsb = zalloc(n2), *Nsbb = zalloc(n2);
+  double *Fu = zalloc(n2), *Fv = zalloc(n2), *gu = zalloc(n2), *gv = zalloc(n2);
+  double *uae = zalloc(n2), *vae = zalloc(n2), *sae = zalloc(n2), *zsp = zalloc(n2), *zhd = zalloc(n2);
+  double *zwxa = zalloc(n2), *zwya = zalloc(n2);
+  /* phase 3 */
+  for (size_t p = 0; p < n2; ++p) {
+    double su = 0.0, sv = 0.0, ta = 0.0, tb = 0.0;
+    for (int jk = 1; jk <= jpk - 1; ++jk) {
+      const size_t q = p + n2 * (jk - 1);
+      su += un_ad[q] * umask[q]; sv += vn_ad[q] * vmask[q];
+      ta += ua_ad[q]; tb += va_ad[q];
+      un_ad[q] = un_ad[q] * umask[q]; vn_ad[q] = vn_ad[q] * vmask[q];
+    }
+    const double adu = unadv_ad[p] + su * r1_hu[p], adv = vnadv_ad[p] + sv * r1_hv[p];
+    unb_ad[p] -= su; vnb_ad[p] -= sv;
+    uab[p] = uab_ad[p] + ta * r1_2dt_b; vab[p] = vab_ad[p] + tb * r1_2dt_b;
+    ubb_ad[p] -= ta * r1_2dt_b; vbb_ad[p] -= tb * r1_2dt_b;
+    if (!euler) {
+      X[p] = 0.5 * adu + unbf_ad[p] + ub2_ad[p];
+      Y[p] = 0.5 * adv + vnbf_ad[p] + vb2_ad[p];
+      const double u2 = 0.5 * adu - unbf_ad[p], v2 = 0.5 * adv - vnbf_ad[p];
+      unbf_ad[p] = -0.5 * atfp * adu + atfp * unbf_ad[p];
+      vnbf_ad[p] = -0.5 * atfp * adv + atfp * vnbf_ad[p];
+      ub2_ad[p] = u2; vb2_ad[p] = v2;
+    } else {
+      X[p] = adu + ub2_ad[p]; Y[p] = adv + vb2_ad[p];
+      ub2_ad[p] = 0.0; vb2_ad[p] = 0.0; unbf_ad[p] = 0.0; vnbf_ad[p] = 0.0;
+    }
+  }
+  /* the sub-steps, last first */
+  for (int jn = c->icycle; jn >= 1; --jn) {
+    const double w1 = c->wgtbtp1[jn - 1], w2 = c->wgtbtp2[jn - 1];
+    double zb1, zb2, zb3, za0, za1, za2, za3;
+    if (jn < 3) { zb1 = 1.0; zb2 = 0.0; zb3 = 0.0; }
+    else { zb1 = 1.781105; zb2 = -1.06221; zb3 = 0.281105; }
+    if (jn == 1) { za0 = 1.0; za1 = 0.0; za2 = 0.0; za3 = 0.0; }
+    else if (jn == 2) { za0 = 1.0833333333333; za1 = -0.1666666666666; za2 = 0.0833333333333; za3 = 0.0; }
+    else if (nm->rn_bt_alpha == 0.0) { za0 = 0.614; za1 = 0.285; za2 = 0.088; za3 = 0.013; }
+    else {
+      const double zepsilon = 0.00976186 - 0.13451357 * nm->rn_bt_alpha;
+      const double zgamma = 0.08344500 - 0.51358400 * nm->rn_bt_alpha;
+      za0 = 0.5 + zgamma + 2.0 * nm->rn_bt_alpha + 2.0 * zepsilon;
+      za1 = 1.0 - za0 - zgamma - zepsilon;
+      za2 = zgamma;
+      za3 = zepsilon;
+    }
+    for (size_t p = 0; p < n2; ++p) {       /* sums and swap (:1176-1204) */
+      uae[p] = Au[p] + w1 * uab[p]; vae[p] = Av[p] + w1 * vab[p];
+      sae[p] = Sn[p] + w1 * ssha_ad[p];
+      Nu[p] = Aub[p]; Nub[p] = Aubb[p]; Nubb[p] = 0.0;
+      Nv[p] = Avb[p]; Nvb[p] = Avbb[p]; Nvbb[p] = 0.0;
+      Nsn[p] = Sb[p]; Nsb[p] = Sbb[p]; Nsbb[p] = 0.0;
+      gu[p] = 0.0; gv[p] = 0.0; zsp[p] = 0.0; zwxa[p] = 0.0; zwya[p] = 0.0;
+    }
+    lbc_closed(jpi, jpj, uae, 1, 'U', 0.0);   /* (:1167) */
+    lbc_closed(jpi, jpj, vae, 1, 'V', 0.0);
+    for (int jj = 2; jj <= jpj - 1; ++jj)    /* next velocities (:1106-1122), bottom stress (:1072-1079) */
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t p = I2(ji, jj);
+        const double tu = uae[p] * ssumask[p], tv = vae[p] * ssvmask[p];
+        gu[p] = rdtbt * tu; gv[p] = rdtbt * tv;
+        Fu[p] += gu[p]; Fv[p] += gv[p];
+        Nu[p] += tu + r1_2 * (rCdU_bot[I2(ji + 1, jj)] + rCdU_bot[p]) * r1_hu[p] * gu[p];
+        Nv[p] += tv + r1_2 * (rCdU_bot[I2(ji, jj + 1)] + rCdU_bot[p]) * r1_hv[p] * gv[p];
+        /* surface pressure gradient (:1093-1101) */
+        const double ku = (1.0 - sl) * (-grav) * c->r1_e1u[p] * gu[p];
+        const double kv = (1.0 - sl) * (-grav) * c->r1_e2v[p] * gv[p];
+        zsp[I2(ji + 1, jj)] += ku; zsp[p] -= ku;
+        zsp[I2(ji, jj + 1)] += kv; zsp[p] -= kv;
+      }
+    spg_cor_adj(c, sc, gu, gv, zwxa, zwya);  /* Coriolis of the fluxes (:1000-1056) */
+    for (size_t p = 0; p < n2; ++p) {        /* AM4 ssh (:904-931) */
+      sae[p] += za0 * zsp[p]; Nsn[p] += za1 * zsp[p]; Nsb[p] += za2 * zsp[p]; Nsbb[p] += za3 * zsp[p];
+    }
+    lbc_closed(jpi, jpj, sae, 1, 'T', 0.0);  /* (:879) */
+    for (size_t p = 0; p < n2; ++p) {        /* ssh update (:871-877) */
+      const double t = sae[p] * ssmask[p];
+      Nsn[p] += t;
+      zhd[p] = -rdtbt * t;
+    }
+    for (int jj = 2; jj <= jpj - 1; ++jj)    /* divergence (:866-869) */
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t p = I2(ji, jj);
+        const double t = zhd[p] * c->r1_e1e2t[p];
+        zwxa[p] += t; zwxa[I2(ji - 1, jj)] -= t;
+        zwya[p] += t; zwya[I2(ji, jj - 1)] -= t;
+      }
+    for (size_t p = 0; p < n2; ++p) {        /* flux sums (:860-862), fluxes (:799-800), AB3 (:724-736) */
+      zwxa[p] += w2 * X[p] * c->r1_e2u[p];
+      zwya[p] += w2 * Y[p] * c->r1_e1v[p];
+      const double eu = zwxa[p] * c->e2u[p] * hu[p], ev = zwya[p] * c->e1v[p] * hv[p];
+      Nu[p] += zb1 * eu; Nub[p] += zb2 * eu; Nubb[p] += zb3 * eu;
+      Nv[p] += zb1 * ev; Nvb[p] += zb2 * ev; Nvbb[p] += zb3 * ev;
+    }
+    double *t;
+    t = Au; Au = Nu; Nu = t;  t = Aub; Aub = Nub; Nub = t;  t = Aubb; Aubb = Nubb; Nubb = t;
+    t = Av; Av = Nv; Nv = t;  t = Avb; Avb = Nvb; Nvb = t;  t = Avbb; Avbb = Nvbb; Nvbb = t;
+    t = Sn; Sn = Nsn; Nsn = t;  t = Sb; Sb = Nsb; Nsb = t;  t = Sbb; Sbb = Nsbb; Nsbb = t;
+  }
+  for (size_t p = 0; p < n2; ++p) {          /* the start from sshn, un_b, vn_b (:688-693) */
+    unb_ad[p] += Au[p]; vnb_ad[p] += Av[p]; sshn_ad[p] += Sn[p];
+  }
+  /* phase 1: bottom stress of the baroclinic velocities (:519-557) */
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      const size_t p = I2(ji, jj);
+      const double tu = r1_hu[p] * r1_2 * (rCdU_bot[I2(ji + 1, jj)] + rCdU_bot[p]) * Fu[p];
+      const double tv = r1_hv[p] * r1_2 * (rCdU_bot[I2(ji, jj + 1)] + rCdU_bot[p]) * Fv[p];
+      un_ad[I3(ji, jj, c->mbku[p])] += tu; unb_ad[p] -= tu;
+      vn_ad[I3(ji, jj, c->mbkv[p])] += tv; vnb_ad[p] -= tv;
+    }
+  /* Coriolis of un_b, vn_b (:387-443) removed from the forcing (:511-516) */
+  for (size_t p = 0; p < n2; ++p) { gu[p] = 0.0; gv[p] = 0.0; zwxa[p] = 0.0; zwya[p] = 0.0; }
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      const size_t p = I2(ji, jj);
+      gu[p] = -Fu[p] * ssumask[p]; gv[p] = -Fv[p] * ssvmask[p];
+    }
+  spg_cor_adj(c, sc, gu, gv, zwxa, zwya);
+  for (size_t p = 0; p < n2; ++p) { unb_ad[p] += zwxa[p] * hu[p] * c->e2u[p]; vnb_ad[p] += zwya[p] * hv[p] * c->e1v[p]; }
+  /* the baroclinic trend's vertical mean (:358-378) */
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      const size_t p = I2(ji, jj);
+      double su = Fu[p], sv = Fv[p];
+      for (int jk = 1; jk <= jpk - 1; ++jk) {
+        const size_t q = p + n2 * (jk - 1);
+        su -= ua_ad[q] * umask[q]; sv -= va_ad[q] * vmask[q];
+      }
+      for (int jk = 1; jk <= jpk - 1; ++jk) {
+        const size_t q = p + n2 * (jk - 1);
+        ua_ad[q] += e3u[q] * umask[q] * r1_hu[p] * su;
+        va_ad[q] += e3v[q] * vmask[q] * r1_hv[p] * sv;
+      }
+    }
+  for (size_t p = 0; p < n2; ++p) {          /* the outputs the forward overwrites */
+    ssha_ad[p] = 0.0; uab_ad[p] = 0.0; vab_ad[p] = 0.0; unadv_ad[p] = 0.0; vnadv_ad[p] = 0.0;
+  }
+  double *w[] = {X, Y, uab, vab, Au, Aub, Aubb, Av, Avb, Avbb, Sn, Sb, Sbb, Nu, Nub, Nubb, Nv, Nvb, Nvbb, Nsn, Nsb, Nsbb,
+                 Fu, Fv, gu, gv, uae, vae, sae, zsp, zhd, zwxa, zwya};
+  for (size_t i = 0; i < sizeof w / sizeof w[0]; ++i) wfree(w[i]);
+  return NEMO_OK;
+}
+
 /* ---------------------------------------------------------------- tra_nxt */
 /* tra_nxt_vvl (tranxt.F90:240-380) for the active tracers, p2dt = rdt as tra_nxt
  * passes it (:161): the thickness-weighted Asselin filter with the forcing removed at

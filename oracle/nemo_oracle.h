@@ -103,6 +103,8 @@ int ora_tra_zdf_imp_adj(ora_ctx *c, int kt, int kit000, const char *cdtype, doub
                         double *ptb_ad, double *pta_ad, int kjpt);
 int ora_tra_nxt(ora_ctx *c, int kt);
 int ora_tra_nxt_adj(ora_ctx *c, int kt, double *tsb_ad, double *tsn_ad, double *tsa_ad);
+/* adjoint of ora_dyn_spg_ts; the arrays of nemo_spg_adj are double * */
+int ora_dyn_spg_ts_adj(ora_ctx *c, int kt, const nemo_spg_adj *adj);
 /* The rest of a linear-free-surface step, and one model step built from them and
  * the path (momentum trends outside the path and vertical viscosity held at 0). */
 int ora_wzv(ora_ctx *c, int kt);

@@ -62,6 +62,7 @@ def lib():
         P("ora_tra_zdf_imp_adj", [vp, i, i, cp, d, vp, vp, i])
         P("ora_tra_nxt", [vp, i])
         P("ora_tra_nxt_adj", [vp, i, vp, vp, vp])
+        P("ora_dyn_spg_ts_adj", [vp, i, C.POINTER(_ffi.SpgAdj)])
         for name in ("ora_wzv", "ora_dyn_zdf_step", "ora_dyn_nxt", "ora_ssh_swp", "ora_dom_vvl_sf_nxt",
                      "ora_dom_vvl_sf_swp", "ora_stp_model", "ora_tra_sbc", "ora_tra_qsr"):
             P(name, [vp, i])
@@ -273,6 +274,11 @@ class Oracle:
 
     def tra_nxt(self, kt):
         self._ck(lib().ora_tra_nxt(self.h, kt), "tra_nxt")
+
+    def dyn_spg_ts_adj(self, kt, adj):
+        """adj: dict of FP64 Fortran-order arrays keyed by the members of nemo_spg_adj."""
+        s = _ffi.SpgAdj(*[_p(adj[n]) for n in _ffi.SPG_ADJ])
+        self._ck(lib().ora_dyn_spg_ts_adj(self.h, kt, C.byref(s)), "dyn_spg_ts_adj")
 
     def tra_nxt_adj(self, kt, tsb_ad, tsn_ad, tsa_ad):
         self._ck(lib().ora_tra_nxt_adj(self.h, kt, _p(tsb_ad), _p(tsn_ad), _p(tsa_ad)), "tra_nxt_adj")
