@@ -628,6 +628,26 @@ typedef struct nemo_spg_adj {
  * count and weights of the forward's last call: run nemo_gpu_dyn_spg_ts(kt) first. */
 int nemo_gpu_dyn_spg_ts_adj(nemo_ctx *ctx, int kt, const nemo_spg_adj *adj);
 
+/* The adjoints of the time stepping of the model step, linear free surface, FP64.
+ * wzv_adj (sshwzv.F90:129-213 with divhor.F90:62-110): un_ad, vn_ad += the transpose
+ * of the map (un, vn) -> wn applied to wn_ad; wn_ad (of the output only) is zeroed.
+ * The thickness-change term is a constant of the map. */
+int nemo_gpu_wzv_adj(nemo_ctx *ctx, int kt, void *un_ad, void *vn_ad, void *wn_ad);
+/* Adjoint arrays of dyn_nxt: in and out -- ua, va, un, vn, ub, vb (3-D) and un_b,
+ * vn_b; of the outputs only -- ub_b, vb_b (read, then zeroed); of the inputs only --
+ * ua_b, va_b (FP64 like the forward's, accumulated). */
+typedef struct nemo_nxt_adj {
+  void *ua, *va, *un, *vn, *ub, *vb;
+  void *un_b, *vn_b, *ub_b, *vb_b;
+  void *ua_b, *va_b;
+} nemo_nxt_adj;
+/* dyn_nxt_adj: the adjoint of nemo_gpu_dyn_nxt (dynnxt.F90:66-377) for ln_linssh with
+ * ln_dynspg_ts and ln_bt_fw, one column per thread. */
+int nemo_gpu_dyn_nxt_adj(nemo_ctx *ctx, int kt, const nemo_nxt_adj *adj);
+/* ssh_swp_adj (sshwzv.F90:216-267, linear free surface): on entry the adjoints of the
+ * swapped sshb, sshn and of ssha, on exit those of the values before the swap. */
+int nemo_gpu_ssh_swp_adj(nemo_ctx *ctx, int kt, void *sshb_ad, void *sshn_ad, void *ssha_ad);
+
 /* dyn_spg_ts (dynspg_ts.F90:121-1310) on the bound fields: phase 1 forcing,
  * icycle barotropic sub-steps in one persistent kernel, phase 3 correction. */
 int nemo_gpu_dyn_spg_ts(nemo_ctx *ctx, int kt);
@@ -756,6 +776,7 @@ enum nemo_kernel_id {
   NEMO_K_VVL_NXT,      /* z*: tra_nxt_vvl, dyn_nxt's filter of e3 and velocities, ssh_swp */
   NEMO_K_TRIAD,        /* the triad operator: slopes, coefficients, fluxes, divergence */
   NEMO_K_SPG_ADJ,      /* the adjoint of dyn_spg_ts (phase 3, reverse sub-steps, phase 1) */
+  NEMO_K_STEP_ADJ,     /* the adjoints of wzv, dyn_nxt, ssh_swp */
   NEMO_K_COUNT
 };
 

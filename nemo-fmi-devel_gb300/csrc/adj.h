@@ -46,6 +46,15 @@ struct SpgAdjStep {
   double za0, za1, za2, za3;  // AM4 ssh (:904-931)
 };
 
+// the adjoint of dyn_nxt (k_step_adj.cuh)
+struct NxtAdjArgs {
+  double *ua, *va, *un, *vn, *ub, *vb;
+  double *un_b, *vn_b, *ub_b, *vb_b;
+  double *ua_b, *va_b;
+  double atfp;
+  int euler;
+};
+
 struct ZdfAdj {
   double* lam;     // pta_ad: in, the after tracer's adjoint; out, the trend's
   double* tb_ad;
@@ -60,6 +69,11 @@ template <class T>
 cudaError_t launch_tra_nxt(const Dom<T>& d, T* tsb, T* tsn, T* tsa, T atfp, int euler, cudaStream_t s);
 cudaError_t launch_tra_nxt_adj(const Dom<double>& d, double* tsb_ad, double* tsn_ad, double* tsa_ad, double atfp,
                                int euler, cudaStream_t s);
+// the adjoints of wzv (G: a (jpi,jpj,jpk) work array per member), dyn_nxt, ssh_swp
+cudaError_t launch_wzv_adj(const Dom<double>& d, double* un_ad, double* vn_ad, double* wn_ad, double* G, cudaStream_t s);
+cudaError_t launch_dyn_nxt_adj(const Dom<double>& d, const NxtAdjArgs& a, cudaStream_t s);
+cudaError_t launch_ssh_swp_adj(const Dom<double>& d, double* sb, double* sn, double* sa, double atfp, int euler,
+                               cudaStream_t s);
 // the adjoint of dyn_spg_ts: steps[jn - 1] holds the constants of sub-step jn
 cudaError_t launch_spg_adj(const Dom<double>& d, const SpgAdjArgs& a, const SpgAdjStep* steps, int icycle,
                            cudaStream_t s);

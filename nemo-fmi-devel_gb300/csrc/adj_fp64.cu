@@ -2,6 +2,7 @@
 // --fmad=false like the FP64 forward kernels.
 #include "k_adj.cuh"
 #include "k_spg_adj.cuh"
+#include "k_step_adj.cuh"
 #include "launch.h"
 
 namespace nemo {
@@ -74,6 +75,26 @@ cudaError_t launch_spg_adj(const Dom<double>& d, const SpgAdjArgs& a, const SpgA
   }
   k_spg_adj_p1<<<acol_grid(d), dim3(AX, AY), 0, s>>>(d, a);
   ktick(NEMO_K_SPG_ADJ, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wzv_adj(const Dom<double>& d, double* un_ad, double* vn_ad, double* wn_ad, double* G, cudaStream_t s) {
+  k_wzv_adj_g<<<acol_grid(d), dim3(AX, AY), 0, s>>>(d, wn_ad, G);
+  k_wzv_adj_uv<<<apt_grid(d), dim3(AX, AY), 0, s>>>(d, un_ad, vn_ad, G);
+  ktick(NEMO_K_STEP_ADJ, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dyn_nxt_adj(const Dom<double>& d, const NxtAdjArgs& a, cudaStream_t s) {
+  k_dyn_nxt_adj<<<acol_grid(d), dim3(AX, AY), 0, s>>>(d, a);
+  ktick(NEMO_K_STEP_ADJ, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ssh_swp_adj(const Dom<double>& d, double* sb, double* sn, double* sa, double atfp, int euler,
+                               cudaStream_t s) {
+  k_ssh_swp_adj<<<acol_grid(d), dim3(AX, AY), 0, s>>>(d, sb, sn, sa, atfp, euler);
+  ktick(NEMO_K_STEP_ADJ, s);
   return cudaGetLastError();
 }
 

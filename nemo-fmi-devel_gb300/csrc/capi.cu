@@ -81,6 +81,7 @@ struct nemo_ctx {
   void* iso_w[3] = {};         // iso-neutral fluxes zftu, zftv, ztfw
   void* adj_w[4] = {};         // iso-neutral adjoint: G and the gradient adjoints
   double* spgadj_w = nullptr;  // dyn_spg_ts adjoint: 18 (jpi,jpj) arrays per member
+  double* wzvadj_w = nullptr;  // wzv adjoint: one (jpi,jpj,jpk) array per member
   int adj_kjpt = 0;
   void* slp_w = nullptr;       // ldf_slp work: 4 3-D and 6 2-D arrays per member
   void* rab_w = nullptr;       // the model step's before expansion ratios rab_b (jpi,jpj,jpk,2)
@@ -2798,6 +2799,55 @@ int nemo_gpu_dyn_spg_ts_adj(nemo_ctx* c, int kt, const nemo_spg_adj* adj) {
   }
   cudaError_t e = launch_spg_adj(dom<double>(c), a, steps.data(), c->icycle, c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "dyn_spg_ts_adj launch");
+  return NEMO_OK;
+}
+
+int nemo_gpu_wzv_adj(nemo_ctx* c, int kt, void* un_ad, void* vn_ad, void* wn_ad) {
+  (void)kt;
+  if (!c) return NEMO_ERR_ARG;
+  if (c->prec != NEMO_PREC_FP64) return fail(c, NEMO_ERR_ARG, "wzv_adj: FP64 contexts only");
+  if (!un_ad || !vn_ad || !wn_ad) return fail(c, NEMO_ERR_ARG, "wzv_adj: null adjoint array");
+  if (!c->nam.ln_linssh) return fail(c, NEMO_ERR_UNSUPPORTED, "wzv_adj: linear free surface only");
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  if (!c->wzvadj_w && cudaMalloc(&c->wzvadj_w, (size_t)c->n3 * c->nmem * sizeof(double)) != cudaSuccess)
+    return fail(c, NEMO_ERR_NOMEM, "wzv_adj work array");
+  cudaError_t e = launch_wzv_adj(dom<double>(c), (double*)un_ad, (double*)vn_ad, (double*)wn_ad, c->wzvadj_w,
+                                 c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "wzv_adj launch");
+  return NEMO_OK;
+}
+
+int nemo_gpu_dyn_nxt_adj(nemo_ctx* c, int kt, const nemo_nxt_adj* adj) {
+  if (!c) return NEMO_ERR_ARG;
+  if (c->prec != NEMO_PREC_FP64) return fail(c, NEMO_ERR_ARG, "dyn_nxt_adj: FP64 contexts only");
+  if (!adj || !adj->ua || !adj->va || !adj->un || !adj->vn || !adj->ub || !adj->vb || !adj->un_b || !adj->vn_b ||
+      !adj->ub_b || !adj->vb_b || !adj->ua_b || !adj->va_b)
+    return fail(c, NEMO_ERR_ARG, "dyn_nxt_adj: null adjoint array");
+  const nemo_namelist& nm = c->nam;
+  if (!nm.ln_linssh || !nm.ln_bt_fw) return fail(c, NEMO_ERR_UNSUPPORTED, "dyn_nxt_adj: ln_linssh with ln_bt_fw only");
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  NxtAdjArgs a{};
+  a.ua = (double*)adj->ua; a.va = (double*)adj->va; a.un = (double*)adj->un; a.vn = (double*)adj->vn;
+  a.ub = (double*)adj->ub; a.vb = (double*)adj->vb;
+  a.un_b = (double*)adj->un_b; a.vn_b = (double*)adj->vn_b; a.ub_b = (double*)adj->ub_b; a.vb_b = (double*)adj->vb_b;
+  a.ua_b = (double*)adj->ua_b; a.va_b = (double*)adj->va_b;
+  a.atfp = nm.rn_atfp;
+  a.euler = nm.neuler == 0 && kt == nm.nit000;
+  cudaError_t e = launch_dyn_nxt_adj(dom<double>(c), a, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "dyn_nxt_adj launch");
+  return NEMO_OK;
+}
+
+int nemo_gpu_ssh_swp_adj(nemo_ctx* c, int kt, void* sshb_ad, void* sshn_ad, void* ssha_ad) {
+  if (!c) return NEMO_ERR_ARG;
+  if (c->prec != NEMO_PREC_FP64) return fail(c, NEMO_ERR_ARG, "ssh_swp_adj: FP64 contexts only");
+  if (!sshb_ad || !sshn_ad || !ssha_ad) return fail(c, NEMO_ERR_ARG, "ssh_swp_adj: null adjoint array");
+  const nemo_namelist& nm = c->nam;
+  if (!nm.ln_linssh) return fail(c, NEMO_ERR_UNSUPPORTED, "ssh_swp_adj: linear free surface only");
+  if (join_copies(c)) return NEMO_ERR_CUDA;
+  cudaError_t e = launch_ssh_swp_adj(dom<double>(c), (double*)sshb_ad, (double*)sshn_ad, (double*)ssha_ad,
+                                     nm.rn_atfp, nm.neuler == 0 && kt == nm.nit000, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "ssh_swp_adj launch");
   return NEMO_OK;
 }
 

@@ -51,6 +51,14 @@ class SpgAdj(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in SPG_ADJ]
 
 
+# members of nemo_nxt_adj (the adjoint arrays of dyn_nxt), in order
+NXT_ADJ = ("ua", "va", "un", "vn", "ub", "vb", "un_b", "vn_b", "ub_b", "vb_b", "ua_b", "va_b")
+
+
+class NxtAdj(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in NXT_ADJ]
+
+
 class Namelist(C.Structure):
     _fields_ = [("rn_rdt", C.c_double), ("rn_atfp", C.c_double), ("nit000", C.c_int), ("neuler", C.c_int),
                 ("ln_linssh", C.c_int), ("ln_zps", C.c_int), ("ln_isfcav", C.c_int),
@@ -170,6 +178,9 @@ def load(path):
         _proto(lib, name, i, [vp, i])
     _proto(lib, "nemo_gpu_tra_adv_fct_adj", i, [vp, i, i, cp, d, vp, vp, vp, vp, vp, vp, i, i, i])
     _proto(lib, "nemo_gpu_dyn_spg_ts_adj", i, [vp, i, C.POINTER(SpgAdj)])
+    _proto(lib, "nemo_gpu_dyn_nxt_adj", i, [vp, i, C.POINTER(NxtAdj)])
+    _proto(lib, "nemo_gpu_wzv_adj", i, [vp, i, vp, vp, vp])
+    _proto(lib, "nemo_gpu_ssh_swp_adj", i, [vp, i, vp, vp, vp])
     _proto(lib, "nemo_gpu_tra_ldf_lap_adj", i, [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
     _proto(lib, "nemo_gpu_tra_ldf_iso_adj", i, [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
     _proto(lib, "nemo_gpu_tra_zdf_imp_adj", i, [vp, i, i, cp, d, vp, vp, i])

@@ -348,6 +348,18 @@ class Context:
     def tra_nxt_adj(self, kt, tsb_ad, tsn_ad, tsa_ad):
         self._ck(self.lib.nemo_gpu_tra_nxt_adj(self.h, kt, _ptr(tsb_ad), _ptr(tsn_ad), _ptr(tsa_ad)), "tra_nxt_adj")
 
+    def wzv_adj(self, kt, un_ad, vn_ad, wn_ad):
+        self._ck(self.lib.nemo_gpu_wzv_adj(self.h, kt, _ptr(un_ad), _ptr(vn_ad), _ptr(wn_ad)), "wzv_adj")
+
+    def dyn_nxt_adj(self, kt, adj):
+        """adj: dict of device FP64 tensors keyed by the members of nemo_nxt_adj."""
+        s = _ffi.NxtAdj(*[_ptr(adj[n]) for n in _ffi.NXT_ADJ])
+        self._ck(self.lib.nemo_gpu_dyn_nxt_adj(self.h, kt, C.byref(s)), "dyn_nxt_adj")
+
+    def ssh_swp_adj(self, kt, sshb_ad, sshn_ad, ssha_ad):
+        self._ck(self.lib.nemo_gpu_ssh_swp_adj(self.h, kt, _ptr(sshb_ad), _ptr(sshn_ad), _ptr(ssha_ad)),
+                 "ssh_swp_adj")
+
     def dyn_spg_ts_adj(self, kt, adj):
         """adj: dict of device FP64 tensors keyed by the members of nemo_spg_adj."""
         s = _ffi.SpgAdj(*[_ptr(adj[n]) for n in _ffi.SPG_ADJ])

@@ -3234,6 +3234,132 @@ int ora_tra_nxt_adj(ora_ctx *c, int kt, double *tsb_ad, double *tsn_ad, double *
   return NEMO_OK;
 }
 
+/* ------------------------------------- adjoints of the step's time stepping */
+/* Adjoint of ora_wzv for the linear free surface: the transpose of (un, vn) -> wn
+ * (sshwzv.F90:129-213 with divhor.F90:62-110): hdivn_ad(l) = -e3t_n tmask times the
+ * sum of wn_ad over levels 1..l, then the transposed divergence. wn_ad is zeroed. */
+int ora_wzv_adj(ora_ctx *c, int kt, double *un_ad, double *vn_ad, double *wn_ad) {
+  (void)kt;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj, n3 = n2 * jpk;
+  if (!un_ad || !vn_ad || !wn_ad) return NEMO_ERR_ARG;
+  if (!c->nam.ln_linssh) return NEMO_ERR_UNSUPPORTED;
+  const double *e3u = c->e3u_0, *e3v = c->e3v_0, *e3t = c->e3t_0;
+  double *G = zalloc(n3);
+  for (int jj = 2; jj <= jpj - 1; ++jj)
+    for (int ji = 2; ji <= jpi - 1; ++ji) {
+      double C = 0.0;
+      for (int jk = 1; jk <= jpk - 1; ++jk) {
+        const size_t q = I3(ji, jj, jk);
+        C += wn_ad[q];
+        const double hd = -(e3t[q] * c->tmask[q]) * C;
+        G[q] = hd * c->r1_e1e2t[I2(ji, jj)] / e3t[q];
+      }
+    }
+  for (int jk = 1; jk <= jpk - 1; ++jk)
+    for (int jj = 2; jj <= jpj - 1; ++jj)
+      for (int ji = 2; ji <= jpi - 1; ++ji) {
+        const size_t q = I3(ji, jj, jk), p = I2(ji, jj);
+        un_ad[q] += c->e2u[p] * e3u[q] * G[q];
+        un_ad[I3(ji - 1, jj, jk)] -= c->e2u[I2(ji - 1, jj)] * e3u[I3(ji - 1, jj, jk)] * G[q];
+        vn_ad[q] += c->e1v[p] * e3v[q] * G[q];
+        vn_ad[I3(ji, jj - 1, jk)] -= c->e1v[I2(ji, jj - 1)] * e3v[I3(ji, jj - 1, jk)] * G[q];
+      }
+  memset(wn_ad, 0, n3 * sizeof(double));
+  wfree(G);
+  return NEMO_OK;
+}
+
+/* Adjoint of ora_dyn_nxt (dynnxt.F90:66-377, linear free surface, ln_bt_fw), the
+ * roles of nemo_nxt_adj. Reverse order: the barotropic velocities, the return of ub
+ * to the time-split estimate, the Asselin filter and swap (or the Euler swap), the
+ * lbc and the replacement of the barotropic part of ua by ua_b. */
+int ora_dyn_nxt_adj(ora_ctx *c, int kt, const nemo_nxt_adj *A) {
+  const nemo_namelist *nm = &c->nam;
+  const int jpi = c->jpi, jpj = c->jpj, jpk = c->jpk;
+  const size_t n2 = (size_t)jpi * jpj;
+  if (!A || !A->ua || !A->va || !A->un || !A->vn || !A->ub || !A->vb || !A->un_b || !A->vn_b || !A->ub_b ||
+      !A->vb_b || !A->ua_b || !A->va_b)
+    return NEMO_ERR_ARG;
+  if (!nm->ln_linssh || !nm->ln_bt_fw) return NEMO_ERR_UNSUPPORTED;
+  const int euler = nm->neuler == 0 && kt == nm->nit000;
+  const double atfp = nm->rn_atfp;
+  for (int dir = 0; dir < 2; ++dir) {
+    double *ua = dir ? A->va : A->ua, *un = dir ? A->vn : A->un, *ub = dir ? A->vb : A->ub;
+    double *unb = dir ? A->vn_b : A->un_b, *ubb = dir ? A->vb_b : A->ub_b, *uab = dir ? A->va_b : A->ua_b;
+    const double *e3 = dir ? c->e3v_0 : c->e3u_0, *msk = dir ? c->vmask : c->umask, *r1h = dir ? c->r1_hv_0 : c->r1_hu_0;
+    const char nat = dir ? 'V' : 'U';
+    for (size_t p = 0; p < n2; ++p) {
+      /* (:345-358) the barotropic velocities of the next step */
+      double su = 0.0;
+      for (int jk = 1; jk <= jpk - 1; ++jk) {
+        const size_t q = p + n2 * (jk - 1);
+        un[q] += e3[q] * msk[q] * r1h[p] * unb[p];
+        ub[q] += e3[q] * msk[q] * r1h[p] * ubb[p];
+      }
+      unb[p] = 0.0; ubb[p] = 0.0;
+      if (!euler) {
+        /* (:312-324) ub returned to the time-split estimate */
+        for (int jk = 1; jk <= jpk - 1; ++jk) su += ub[p + n2 * (jk - 1)] * msk[p + n2 * (jk - 1)];
+        unb[p] += su;
+        const double zad = -su * r1h[p];
+        for (int jk = 1; jk <= jpk - 1; ++jk) {
+          const size_t q = p + n2 * (jk - 1);
+          ub[q] += e3[q] * msk[q] * zad;
+          /* (:197-211) the Asselin filter and swap */
+          const double b = ub[q];
+          ua[q] += un[q] + atfp * b;
+          un[q] = (1.0 - 2.0 * atfp) * b;
+          ub[q] = atfp * b;
+        }
+      } else {
+        for (int jk = 1; jk <= jpk - 1; ++jk) {   /* (:168-171) */
+          const size_t q = p + n2 * (jk - 1);
+          ua[q] += un[q];
+          un[q] = 0.0;
+        }
+      }
+    }
+    lbc_closed(jpi, jpj, ua, jpk, nat, 0.0);   /* (:146) */
+    for (size_t p = 0; p < n2; ++p) {           /* (:114-126) */
+      double s = 0.0;
+      for (int jk = 1; jk <= jpk - 1; ++jk) {
+        const size_t q = p + n2 * (jk - 1);
+        ua[q] = ua[q] * msk[q];
+        s += ua[q];
+      }
+      uab[p] += s;
+      const double zad = -s * r1h[p];
+      for (int jk = 1; jk <= jpk - 1; ++jk) {
+        const size_t q = p + n2 * (jk - 1);
+        ua[q] += e3[q] * msk[q] * zad;
+      }
+    }
+  }
+  return NEMO_OK;
+}
+
+/* Adjoint of ora_ssh_swp (sshwzv.F90:216-267), linear free surface. */
+int ora_ssh_swp_adj(ora_ctx *c, int kt, double *sshb_ad, double *sshn_ad, double *ssha_ad) {
+  const nemo_namelist *nm = &c->nam;
+  const size_t n2 = (size_t)c->jpi * c->jpj;
+  if (!sshb_ad || !sshn_ad || !ssha_ad) return NEMO_ERR_ARG;
+  if (!nm->ln_linssh) return NEMO_ERR_UNSUPPORTED;
+  const double atfp = nm->rn_atfp;
+  for (size_t p = 0; p < n2; ++p) {
+    if (nm->neuler == 0 && kt == nm->nit000) {
+      ssha_ad[p] += sshn_ad[p];
+      sshn_ad[p] = 0.0;
+    } else {
+      const double b = sshb_ad[p];
+      ssha_ad[p] += sshn_ad[p] + atfp * b;
+      sshn_ad[p] = (1.0 - 2.0 * atfp) * b;
+      sshb_ad[p] = atfp * b;
+    }
+  }
+  return NEMO_OK;
+}
+
 /* ======================================================= the rest of the step */
 /* The parts of stp (step.F90:96-305) that close the path into a time step with the
  * linear free surface: the vertical velocity, the time step and the swaps of the

@@ -105,6 +105,10 @@ int ora_tra_nxt(ora_ctx *c, int kt);
 int ora_tra_nxt_adj(ora_ctx *c, int kt, double *tsb_ad, double *tsn_ad, double *tsa_ad);
 /* adjoint of ora_dyn_spg_ts; the arrays of nemo_spg_adj are double * */
 int ora_dyn_spg_ts_adj(ora_ctx *c, int kt, const nemo_spg_adj *adj);
+/* adjoints of the step's time stepping (linear free surface) */
+int ora_wzv_adj(ora_ctx *c, int kt, double *un_ad, double *vn_ad, double *wn_ad);
+int ora_dyn_nxt_adj(ora_ctx *c, int kt, const nemo_nxt_adj *adj);
+int ora_ssh_swp_adj(ora_ctx *c, int kt, double *sshb_ad, double *sshn_ad, double *ssha_ad);
 /* The rest of a linear-free-surface step, and one model step built from them and
  * the path (momentum trends outside the path and vertical viscosity held at 0). */
 int ora_wzv(ora_ctx *c, int kt);

@@ -63,6 +63,9 @@ def lib():
         P("ora_tra_nxt", [vp, i])
         P("ora_tra_nxt_adj", [vp, i, vp, vp, vp])
         P("ora_dyn_spg_ts_adj", [vp, i, C.POINTER(_ffi.SpgAdj)])
+        P("ora_dyn_nxt_adj", [vp, i, C.POINTER(_ffi.NxtAdj)])
+        P("ora_wzv_adj", [vp, i, vp, vp, vp])
+        P("ora_ssh_swp_adj", [vp, i, vp, vp, vp])
         for name in ("ora_wzv", "ora_dyn_zdf_step", "ora_dyn_nxt", "ora_ssh_swp", "ora_dom_vvl_sf_nxt",
                      "ora_dom_vvl_sf_swp", "ora_stp_model", "ora_tra_sbc", "ora_tra_qsr"):
             P(name, [vp, i])
@@ -274,6 +277,16 @@ class Oracle:
 
     def tra_nxt(self, kt):
         self._ck(lib().ora_tra_nxt(self.h, kt), "tra_nxt")
+
+    def wzv_adj(self, kt, un_ad, vn_ad, wn_ad):
+        self._ck(lib().ora_wzv_adj(self.h, kt, _p(un_ad), _p(vn_ad), _p(wn_ad)), "wzv_adj")
+
+    def dyn_nxt_adj(self, kt, adj):
+        s = _ffi.NxtAdj(*[_p(adj[n]) for n in _ffi.NXT_ADJ])
+        self._ck(lib().ora_dyn_nxt_adj(self.h, kt, C.byref(s)), "dyn_nxt_adj")
+
+    def ssh_swp_adj(self, kt, sshb_ad, sshn_ad, ssha_ad):
+        self._ck(lib().ora_ssh_swp_adj(self.h, kt, _p(sshb_ad), _p(sshn_ad), _p(ssha_ad)), "ssh_swp_adj")
 
     def dyn_spg_ts_adj(self, kt, adj):
         """adj: dict of FP64 Fortran-order arrays keyed by the members of nemo_spg_adj."""
