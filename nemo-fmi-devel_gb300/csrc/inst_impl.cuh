@@ -286,6 +286,10 @@ cudaError_t launch_spg(const Dom<T>& d, const SpgArgs<T>& a, const GridBar& bar,
   const int t1b = kty(NEMO_K_SPG_P1B);
   k_spg_p1b<T><<<col_grid(d, t1b), dim3(BX, t1b), 0, s>>>(d, a);
   ktick(NEMO_K_SPG_P1B, s);
+  {  // the barrier's arrival counter starts at 0 in every launch
+    cudaError_t ez = cudaMemsetAsync(bar.count, 0, sizeof(unsigned int), s);
+    if (ez != cudaSuccess) return ez;
+  }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(p2_blocks);
   cfg.blockDim = dim3(256);

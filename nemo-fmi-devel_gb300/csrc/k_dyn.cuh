@@ -434,6 +434,7 @@ __device__ __forceinline__ int p2_tiles(const Dom<T>& d) {
 
 template <class T, bool VVL>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (VVL ? 3 : 4) : 2) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar bar) {
+  unsigned int bar_epoch = 0;  // barriers passed by this block
   __shared__ T zs_s[P2_TY + 1][P2_TX + 1];
   // Variable volume: the new ssh ssha_e [0], the predictor ssh of the next sub-step
   // [1] and the now ssh [2] of the tile and its halo, for the depths at u- and
@@ -555,7 +556,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (VVL ? 3 : 4) : 2) k_spg
       for (int cc = 0; cc < P2_NC; ++cc) p2c[(cc * P2_MAXT + slot) * 256 + threadIdx.x] = cv[cc];
     }
   }
-  if (!grid_barrier(bar)) return;
+  if (!grid_barrier(bar, bar_epoch)) return;
   for (int jn = 1; jn <= a.icycle; ++jn) {
     const int sn = r & 3, sb = (r + 1) & 3, sbb = (r + 2) & 3, sa = (r + 3) & 3;
     const T* fx = a.fx + (jn & 1) * nmem2;
@@ -822,7 +823,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (VVL ? 3 : 4) : 2) k_spg
       __syncthreads();  // zs_s is rewritten by the next tile
     }
     r = (r + 3) & 3;
-    if (!grid_barrier(bar)) return;
+    if (!grid_barrier(bar, bar_epoch)) return;
   }
   // ---- phase 3, per column (:1214-1262, :1266-1269): time-filtered transports
   // and the two depth-independent terms each level adds
@@ -918,6 +919,7 @@ __device__ __forceinline__ void ff4_add_w(float& h, float& l, float wh, float wl
 
 template <class T>
 __global__ void __launch_bounds__(256, 5) k_spg_p2_ene(Dom<T> d, SpgArgs<T> a, GridBar bar) {
+  unsigned int bar_epoch = 0;  // barriers passed by this block
   static_assert(sizeof(T) == 4, "the mixed form's kernel");
   __shared__ float zs_s[P2_TY + 1][P2_TX + 1];
   extern __shared__ float p2h[];
@@ -993,7 +995,7 @@ __global__ void __launch_bounds__(256, 5) k_spg_p2_ene(Dom<T> d, SpgArgs<T> a, G
   int hti = -1, htj = -1;
   if (threadIdx.x < P2_TY + 1) { hti = P2_TX; htj = threadIdx.x; }
   else if (threadIdx.x < P2_TY + 1 + P2_TX) { hti = threadIdx.x - (P2_TY + 1); htj = P2_TY; }
-  if (!grid_barrier(bar)) return;
+  if (!grid_barrier(bar, bar_epoch)) return;
   for (int jn = 1; jn <= a.icycle; ++jn) {
     const int sn = r & 3, sb = (r + 1) & 3, sbb = (r + 2) & 3, sa = (r + 3) & 3;
     const float* fx = a.fx + (jn & 1) * nmem2;
@@ -1107,7 +1109,7 @@ __global__ void __launch_bounds__(256, 5) k_spg_p2_ene(Dom<T> d, SpgArgs<T> a, G
       __syncthreads();  // zs_s is rewritten by the next tile
     }
     r = (r + 3) & 3;
-    if (!grid_barrier(bar)) return;
+    if (!grid_barrier(bar, bar_epoch)) return;
   }
   // ---- phase 3, per column (:1214-1240, :1266-1269): the sums into the FP64 fields,
   // the time-filtered transports and the two depth-independent terms of each level

@@ -163,16 +163,18 @@ template <> struct Big<double> { static constexpr double v = 1.e+40; };
 template <> struct Big<float> { static constexpr float v = 1.e+10f; };
 
 // Grid barrier for persistent kernels launched cooperatively (all blocks resident).
-// Thread 0 of each block reads the generation (acquire), arrives on the counter
-// with an acquire-release atomic, and the last block to arrive resets the counter
-// and publishes the next generation with a release store; the others poll the
-// generation with acquire loads, which makes every write before the barrier
-// visible after it. Each wait is bounded: after max_spins polls the block records
-// NEMO_ERR_TIMEOUT in *err and returns false; every block checks the flag after
-// each barrier and leaves its loop, so the kernel always ends.
+// The arrival counter only grows within a launch (the launcher zeroes it before
+// each launch): at its e-th barrier, thread 0 of each block adds 1 with a release
+// reduction -- posted, no value returned, so it does not wait for the L2 round trip
+// of an atomic -- and polls the counter with acquire loads until it reaches e times
+// the block count; the release/acquire pair makes every write before the barrier
+// visible after it. No block resets or publishes anything, so the last block to
+// arrive is not on the critical path twice. Each wait is bounded: after max_spins
+// polls the block records NEMO_ERR_TIMEOUT in *err and returns false; every block
+// checks the flag after each barrier and leaves its loop, so the kernel always ends.
 struct GridBar {
-  unsigned int* count;
-  unsigned int* gen;
+  unsigned int* count;   // zeroed before each launch
+  unsigned int* gen;     // unused
   int* err;
   unsigned int nblocks;
   long long max_spins;
@@ -192,24 +194,25 @@ __device__ __forceinline__ void st_release_gpu(unsigned int* p, unsigned int v) 
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-__device__ __forceinline__ bool grid_barrier(const GridBar& b) {
+__device__ __forceinline__ void red_add_release_gpu(unsigned int* p, unsigned int v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// epoch: the block's count of barriers passed in this launch (a register, 0 at start)
+__device__ __forceinline__ bool grid_barrier(const GridBar& b, unsigned int& epoch) {
   __shared__ int s_err;  // the error flag as thread 0 saw it, for the whole block
   __syncthreads();
+  ++epoch;
   if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) {
     volatile int* verr = b.err;
-    const unsigned int g = ld_acquire_gpu(b.gen);
-    const unsigned int arrived = atom_add_acq_rel_gpu(b.count, 1u);
-    if (arrived == b.nblocks - 1) {
-      *b.count = 0u;  // ordered before the release below
-      st_release_gpu(b.gen, g + 1u);
-    } else {
-      long long s = 0;
-      while (ld_acquire_gpu(b.gen) == g) {
-        if ((++s & 63) == 0 && *verr != 0) break;
-        if (s > b.max_spins) {
-          atomicExch(b.err, 5);
-          break;
-        }
+    const unsigned int target = epoch * b.nblocks;
+    red_add_release_gpu(b.count, 1u);
+    long long s = 0;
+    while ((int)(ld_acquire_gpu(b.count) - target) < 0) {
+      if ((++s & 63) == 0 && *verr != 0) break;
+      if (s > b.max_spins) {
+        atomicExch(b.err, 5);
+        break;
       }
     }
     s_err = *verr;
