@@ -509,7 +509,9 @@ int nemo_gpu_wzv(nemo_ctx *ctx, int kt);
 int nemo_gpu_ldf_slp(nemo_ctx *ctx, int kt, const void *prd, const void *pn2);
 
 /* dyn_zdf (dynzdf.F90:47-499). Its leap-frog time step ua = (ub + r2dt ua) umask, va
- * likewise (:112); and, while the ocean viscosity NEMO_F_AVM is bound, the implicit
+ * likewise (:109-114), or with a variable volume and flux-form momentum on the
+ * thickness-weighted velocity, ua = (e3u_b ub + r2dt e3u_n ua) / e3u_a umask
+ * (:115-120; E3U_B, E3U_N, E3U_A and the v ones bound); and, while the ocean viscosity NEMO_F_AVM is bound, the implicit
  * vertical viscosity of a linear free surface with the split-explicit free surface
  * and implicit bottom drag (ln_drgimp, the reference's default), iso-level lateral
  * mixing and ln_zad_Aimp off: the barotropic after velocity UA_B / VA_B of

@@ -1132,6 +1132,9 @@ int dyn_zdf_check(nemo_ctx* c) {
   void* const* F = c->f;
   for (int id : {NEMO_F_UA, NEMO_F_VA, NEMO_F_UB, NEMO_F_VB})
     if (!F[id]) return fail(c, NEMO_ERR_UNBOUND, "dyn_zdf: ua, va, ub and vb must be bound");
+  if (!c->nam.ln_linssh && !c->nam.ln_dynadv_vec)
+    for (int id : {NEMO_F_E3U_B, NEMO_F_E3V_B, NEMO_F_E3U_N, NEMO_F_E3V_N, NEMO_F_E3U_A, NEMO_F_E3V_A})
+      if (!F[id]) return fail(c, NEMO_ERR_UNBOUND, "dyn_zdf (flux form, variable volume): e3u/e3v _b, _n, _a must be bound");
   if (!F[NEMO_F_AVM]) return NEMO_OK;
   for (int id : {NEMO_F_UA_B, NEMO_F_VA_B, NEMO_F_RCDU_BOT, NEMO_F_UTAU, NEMO_F_VTAU})
     if (!F[id]) return fail(c, NEMO_ERR_UNBOUND, "dyn_zdf with avm: ua_b, va_b, rcdu_bot, utau, vtau must be bound");
@@ -1148,8 +1151,11 @@ int run_dyn_zdf_step(nemo_ctx* c, int kt) {
   const double r2dt = (nm.neuler == 0 && kt == nm.nit000) ? nm.rn_rdt : 2.0 * nm.rn_rdt;
   cudaError_t e;
   if (!F[NEMO_F_AVM]) {
+    const bool flux = !nm.ln_linssh && !nm.ln_dynadv_vec;
     e = launch_dyn_zdf_step<T>(dom_now<T>(c), (const T*)F[NEMO_F_UB], (const T*)F[NEMO_F_VB], (T*)F[NEMO_F_UA],
-                               (T*)F[NEMO_F_VA], (T)r2dt, c->stream);
+                               (T*)F[NEMO_F_VA], (T)r2dt, flux ? (const T*)F[NEMO_F_E3U_B] : nullptr,
+                               flux ? (const T*)F[NEMO_F_E3V_B] : nullptr, flux ? (const T*)F[NEMO_F_E3U_A] : nullptr,
+                               flux ? (const T*)F[NEMO_F_E3V_A] : nullptr, c->stream);
   } else {
     const size_t n = (size_t)c->n3 * c->nmem;
     if (!c->zdyn_w && cudaMalloc(&c->zdyn_w, 2 * n * sizeof(T)) != cudaSuccess)

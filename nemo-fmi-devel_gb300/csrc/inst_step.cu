@@ -21,8 +21,9 @@ cudaError_t launch_wzv(const Dom<T>& d, const T* un, const T* vn, T* wn, T z1_2d
   return cudaGetLastError();
 }
 template <class T>
-cudaError_t launch_dyn_zdf_step(const Dom<T>& d, const T* ub, const T* vb, T* ua, T* va, T r2dt, cudaStream_t s) {
-  k_dyn_zdf_step<T><<<s_pt(d), dim3(SX, SY), 0, s>>>(d, ub, vb, ua, va, r2dt);
+cudaError_t launch_dyn_zdf_step(const Dom<T>& d, const T* ub, const T* vb, T* ua, T* va, T r2dt, const T* e3u_b,
+                                const T* e3v_b, const T* e3u_a, const T* e3v_a, cudaStream_t s) {
+  k_dyn_zdf_step<T><<<s_pt(d), dim3(SX, SY), 0, s>>>(d, ub, vb, ua, va, r2dt, e3u_b, e3v_b, e3u_a, e3v_a);
   ktick(NEMO_K_DYN_ZDF_STEP, s);
   return cudaGetLastError();
 }
@@ -224,7 +225,8 @@ cudaError_t launch_dia_hsb(const Dom<T>& d, const HsbArgs<T>& a, double* part, i
   template cudaError_t launch_hsb_init<T>(const Dom<T>&, const HsbArgs<T>&, int, cudaStream_t);                \
   template cudaError_t launch_dia_hsb<T>(const Dom<T>&, const HsbArgs<T>&, double*, int, cudaStream_t);         \
   template cudaError_t launch_wzv<T>(const Dom<T>&, const T*, const T*, T*, T, cudaStream_t);                  \
-  template cudaError_t launch_dyn_zdf_step<T>(const Dom<T>&, const T*, const T*, T*, T*, T, cudaStream_t);     \
+  template cudaError_t launch_dyn_zdf_step<T>(const Dom<T>&, const T*, const T*, T*, T*, T, const T*, const T*, \
+                                              const T*, const T*, cudaStream_t);                            \
   template cudaError_t launch_dyn_nxt<T>(const Dom<T>&, const NxtArgs<T, double>&, cudaStream_t);              \
   template cudaError_t launch_ssh_swp<T>(const Dom<T>&, T*, T*, const double*, T, int, cudaStream_t);      \
   template cudaError_t launch_vvl_sf_nxt<T>(const Dom<T>&, const VvlArgs<T>&, cudaStream_t);                \

@@ -41,13 +41,19 @@ __global__ void k_wzv(Dom<T> d, RO<T> un, RO<T> vn, T* wn, T z1_2dt) {
 
 // The time step of dyn_zdf (dynzdf.F90:112) with no vertical viscosity or drag.
 template <class T>
-__global__ void k_dyn_zdf_step(Dom<T> d, RO<T> ub, RO<T> vb, T* ua, T* va, T r2dt) {
+__global__ void k_dyn_zdf_step(Dom<T> d, RO<T> ub, RO<T> vb, T* ua, T* va, T r2dt, RO<T> e3u_b, RO<T> e3v_b,
+                               RO<T> e3u_a, RO<T> e3v_a) {
   const PtIdx c = pt_index(d);
   if (!c.valid || c.k > d.jpk - 1) return;
   const long q = (long)c.m * d.n3 + c.q;
   const ColInfo ci = d.ci[c.ij];
-  ua[q] = (ub[q] + r2dt * ua[q]) * umsk<T>(ci, c.k);
-  va[q] = (vb[q] + r2dt * va[q]) * vmsk<T>(ci, c.k);
+  if (e3u_b) {  // flux form with a variable volume: on the thickness-weighted velocity (:115-120)
+    ua[q] = (e3u_b[q] * ub[q] + r2dt * d.e3u_n(c.ij, c.k, c.m) * ua[q]) / e3u_a[q] * umsk<T>(ci, c.k);
+    va[q] = (e3v_b[q] * vb[q] + r2dt * d.e3v_n(c.ij, c.k, c.m) * va[q]) / e3v_a[q] * vmsk<T>(ci, c.k);
+  } else {      // on the velocity (:109-114)
+    ua[q] = (ub[q] + r2dt * ua[q]) * umsk<T>(ci, c.k);
+    va[q] = (vb[q] + r2dt * va[q]) * vmsk<T>(ci, c.k);
+  }
 }
 
 // The implicit vertical viscosity of one U- (V-) column of dyn_zdf

@@ -153,7 +153,10 @@ cudaError_t launch_ldf_slp(const Dom<T>& d, const SlpArgs<T>& a, cudaStream_t s)
 template <class T>
 cudaError_t launch_wzv(const Dom<T>& d, const T* un, const T* vn, T* wn, T z1_2dt, cudaStream_t s);
 template <class T>
-cudaError_t launch_dyn_zdf_step(const Dom<T>& d, const T* ub, const T* vb, T* ua, T* va, T r2dt, cudaStream_t s);
+// e3u_b ... e3v_a null: the time step on the velocity; else on the thickness-weighted
+// velocity (variable volume, flux-form momentum)
+cudaError_t launch_dyn_zdf_step(const Dom<T>& d, const T* ub, const T* vb, T* ua, T* va, T r2dt, const T* e3u_b,
+                                const T* e3v_b, const T* e3u_a, const T* e3v_a, cudaStream_t s);
 template <class T>
 cudaError_t launch_dyn_nxt(const Dom<T>& d, const NxtArgs<T, double>& a, cudaStream_t s);
 template <class T>

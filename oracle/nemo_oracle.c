@@ -3415,9 +3415,19 @@ int ora_dyn_zdf_step(ora_ctx *c, int kt) {
   const double *ub = c->f[NEMO_F_UB], *vb = c->f[NEMO_F_VB];
   if (!ua || !va || !ub || !vb) return NEMO_ERR_UNBOUND;
   const double r2dt = (nm->neuler == 0 && kt == nm->nit000) ? nm->rn_rdt : 2. * nm->rn_rdt;
-  for (size_t q = 0; q < n3 - n2; ++q) {
-    ua[q] = (ub[q] + r2dt * ua[q]) * c->umask[q];
-    va[q] = (vb[q] + r2dt * va[q]) * c->vmask[q];
+  if (!nm->ln_linssh && !nm->ln_dynadv_vec) {   /* (:115-120) on the thickness-weighted velocity */
+    const double *e3u_b = c->f[NEMO_F_E3U_B], *e3v_b = c->f[NEMO_F_E3V_B], *e3u_a = c->f[NEMO_F_E3U_A];
+    const double *e3v_a = c->f[NEMO_F_E3V_A], *e3u_n = c->f[NEMO_F_E3U_N], *e3v_n = c->f[NEMO_F_E3V_N];
+    if (!e3u_b || !e3v_b || !e3u_a || !e3v_a || !e3u_n || !e3v_n) return NEMO_ERR_UNBOUND;
+    for (size_t q = 0; q < n3 - n2; ++q) {
+      ua[q] = (e3u_b[q] * ub[q] + r2dt * e3u_n[q] * ua[q]) / e3u_a[q] * c->umask[q];
+      va[q] = (e3v_b[q] * vb[q] + r2dt * e3v_n[q] * va[q]) / e3v_a[q] * c->vmask[q];
+    }
+  } else {                                        /* (:109-114) */
+    for (size_t q = 0; q < n3 - n2; ++q) {
+      ua[q] = (ub[q] + r2dt * ua[q]) * c->umask[q];
+      va[q] = (vb[q] + r2dt * va[q]) * c->vmask[q];
+    }
   }
   const double *avm = c->f[NEMO_F_AVM];
   if (!avm) return NEMO_OK;

@@ -298,3 +298,91 @@ def test_gpu_vvl_cycle_mixed():
     the filtered velocities and tracers to the rounding of the differences."""
     p = gpu_pair("mixed", neuler=0, ln_dynadv_vec=0, ln_traqsr=1)
     cycle(p, 3, 2e-5, 2e-5)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_gpu_zstar_hotpath_and_time_stepping_cycle(prec):
+    """The variable-volume hot path (FCT 4/4, iso-neutral diffusion with partial-step
+    gradients, zdf, dyn_spg_ts with EEN and flux-form momentum) chained with the z*
+    time stepping for four steps from an Euler start, on both sides: wzv, stp_hotpath,
+    the flux-form time step of dyn_zdf, dom_vvl_sf_nxt of the time-split ssha,
+    tra_nxt_vvl, dyn_nxt, ssh_swp, dom_vvl_sf_swp -- each step reads the scale factors,
+    depths and velocities the previous one formed; the other momentum trends are held
+    fixed. (Chain parity; NEMO forms e3t_a before the tracer trends, here the hot path
+    reads the previous step's.)"""
+    pytest.importorskip("torch")
+    dom = shelf.domain(seed=6, **SMALL)
+    nam = shelf.namelist(neuler=0, ln_traqsr=0)
+    states = []
+    for m in range(2):
+        st = vvl_state(dom, nam, seed=6, member=m)
+        base = shelf.state(dom, nam, seed=6, member=m)
+        st["ua"], st["va"] = base["ua"], base["va"]   # the hot path's ua, va are trends
+        states.append(st)
+    p = Pair(dom=dom, nam=nam, prec=prec, states=states)
+    p.bind_hotpath()
+    for n in OUT3 + OUT2 + IN3 + IN2 + ("SBC_TSC", "SBC_TSC_B", "GTSU", "GTSV", "SSH_IB"):
+        if n not in ("UN", "VN", "UB", "VB", "UA", "VA", "SSHB", "SSHN", "UN_B", "VN_B", "UB_B", "VB_B"):
+            p.bind(n)
+    tol3 = 1e-12 if prec == "fp64" else 2e-4
+    trend = [(F(st["ua"]), F(st["va"])) for st in states]
+    for kt in range(1, 5):
+        if kt > 1:  # the momentum trend of the other routines, held fixed
+            for n, i in (("UA", 0), ("VA", 1)):
+                for m in range(2):
+                    p.host[m][n][...] = trend[m][i]
+                p.dev[n].copy_(p.to_dev([trend[m][i] for m in range(2)]))
+        for o in p.ora:
+            o.wzv(kt)
+            o.stp_hotpath(kt)
+            o.dyn_zdf_step(kt)
+            o.dom_vvl_sf_nxt(kt)
+            o.tra_nxt(kt)
+            o.dyn_nxt(kt)
+            o.ssh_swp(kt)
+            o.dom_vvl_sf_swp(kt)
+        p.ctx.wzv(kt)
+        p.ctx.stp_hotpath(kt)
+        p.ctx.dyn_zdf_step(kt)
+        p.ctx.dom_vvl_sf_nxt(kt)
+        p.ctx.tra_nxt(kt)
+        p.ctx.dyn_nxt(kt)
+        p.ctx.ssh_swp(kt)
+        p.ctx.dom_vvl_sf_swp(kt)
+    p.ctx.synchronize()
+    p.compare("TSN", p.s4, tol3)
+    p.compare("TSB", p.s4, tol3)
+    for n in ("UN", "VN", "UB", "E3T_N", "E3T_B", "E3U_N", "E3W_N", "GDEPT_N"):
+        p.compare(n, p.s3, tol3)
+    for n in ("SSHN", "SSHB", "HT_N", "UN_B"):
+        p.compare(n, p.s2, tol3)
+
+
+def test_oracle_dyn_zdf_flux_form_time_step():
+    """dyn_zdf's flux-form time step with a variable volume (dynzdf.F90:115-120):
+    (e3u_b ub + r2dt e3u_n ua) / e3u_a, which is the vector form when the three
+    scale factors are equal."""
+    from oracle import ora
+    dom = shelf.domain(seed=4, **SMALL)
+    nam = shelf.namelist(neuler=1, ln_dynadv_vec=0)
+    st = vvl_state(dom, nam, seed=4)
+    um = gyre.masks(dom)[1]
+    r2dt = 2.0 * nam["rn_rdt"]
+    for equal in (False, True):
+        o = ora.Oracle(dom, nam)
+        f = {n: np.array(st[n.lower()], order="F", copy=True) for n in ("UA", "VA", "UB", "VB", "E3U_B", "E3V_B",
+                                                                         "E3U_N", "E3V_N", "E3U_A", "E3V_A")}
+        if equal:
+            for n in ("E3U_B", "E3U_A"):
+                f[n][...] = f["E3U_N"]
+        for n, a in f.items():
+            o.bind(n, a)
+        ua0, ub = f["UA"].copy(), f["UB"]
+        o.dyn_zdf_step(3)
+        k = slice(0, dom["jpk"] - 1)
+        if equal:
+            want = (ub + r2dt * ua0) * um
+        else:
+            want = (st["e3u_b"] * ub + r2dt * st["e3u_n"] * ua0) / st["e3u_a"] * um
+        np.testing.assert_allclose(f["UA"][:, :, k], want[:, :, k], rtol=1e-14, atol=1e-14 * np.abs(want).max())
