@@ -104,7 +104,9 @@ class Context:
         return torch.from_numpy(flat).to(device="cuda", dtype=dtype or self.dtype).contiguous()
 
     def to_host(self, t, shape):
-        """Fortran-order numpy array(s) (one per member) from a device tensor."""
+        """Fortran-order numpy array(s) (one per member) from a device tensor, after
+        the device's work (the context's stream does not order with torch's)."""
+        self.torch.cuda.synchronize()
         a = t.detach().to("cpu", self.torch.float64).numpy()
         n = int(np.prod(shape))
         if a.size == n:

@@ -79,6 +79,8 @@ class Pair:
         from oracle import ora
         self.dom = dom or gyre.domain(nn, jpk=jpk)
         self.nam = nam or gyre.namelist(**nam_over)
+        if states is not None and nmem == 1:
+            nmem = len(states)  # one member per given state
         self.nmem = nmem
         self.states = states or [gyre.state(self.dom, self.nam, seed=seed, member=m) for m in range(nmem)]
         self.vvl = not self.nam["ln_linssh"]
@@ -125,6 +127,16 @@ class Pair:
         self.dev[name] = t
         self.ctx.bind(name, t)
         return t
+
+    def set(self, name, arrays):
+        """New values of the bound field NAME on every member: the oracles' arrays in
+        place, the device tensor by a copy ordered after the context's work and
+        finished before its next call (the context's stream is not torch's)."""
+        for i, m in enumerate(self.sample):
+            self.host[i][name][...] = arrays[m]
+        self.torch.cuda.synchronize()
+        self.dev[name].copy_(self.to_dev(list(arrays), fp64=self.dev[name].dtype == self.torch.float64))
+        self.torch.cuda.synchronize()
 
     def bind_iso(self):
         for n in ("USLP", "VSLP", "WSLPI", "WSLPJ"):

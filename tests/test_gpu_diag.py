@@ -33,6 +33,7 @@ def forced_pair(prec, nn=2, nmem=2, seed=41):
 
 def put(p, name, shape):
     """upload the oracles' (host) copies of field NAME to the GPU"""
+    torch.cuda.synchronize()   # after the context's work (its own stream)
     p.dev[name].copy_(p.to_dev([p.host[m][name] for m in range(p.nmem)], fp64=p.dev[name].dtype == torch.float64))
     torch.cuda.synchronize()
 

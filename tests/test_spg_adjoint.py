@@ -160,7 +160,7 @@ def test_gpu_spg_adjoint(sc, nmem, euler):
     if kt != 1:
         p.ctx.dyn_spg_ts(kt)
     o, f = tl_oracle(dom, nam)
-    p.dev["RCDU_BOT"].copy_(p.to_dev([f["RCDU_BOT"]] * nmem))   # one drag coefficient for both
+    p.set("RCDU_BOT", [f["RCDU_BOT"]] * nmem)   # one drag coefficient for both
     rng = np.random.default_rng([sc, nmem])
     if not euler:
         tangent_linear(o, f, perturbation(dom, rng), 1)

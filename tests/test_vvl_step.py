@@ -241,10 +241,7 @@ def refresh(p, kt):
         new["UA_B"].append(F(h["UN_B"] + 5e-4 * rng.standard_normal((jpi, jpj)) * um.max(axis=2)))
         new["VA_B"].append(F(h["VN_B"] + 5e-4 * rng.standard_normal((jpi, jpj)) * vm.max(axis=2)))
     for n, arrs in new.items():
-        for m in range(p.nmem):
-            p.host[m][n][...] = arrs[m]
-        from nemo_gpu import _ffi
-        p.dev[n].copy_(p.to_dev(arrs, fp64=n in _ffi.FP64_FIELDS))
+        p.set(n, arrs)
 
 
 def cycle(p, steps, tol3, tol2):
@@ -330,9 +327,7 @@ def test_gpu_zstar_hotpath_and_time_stepping_cycle(prec):
     for kt in range(1, 5):
         if kt > 1:  # the momentum trend of the other routines, held fixed
             for n, i in (("UA", 0), ("VA", 1)):
-                for m in range(2):
-                    p.host[m][n][...] = trend[m][i]
-                p.dev[n].copy_(p.to_dev([trend[m][i] for m in range(2)]))
+                p.set(n, [trend[m][i] for m in range(2)])
         for o in p.ora:
             o.wzv(kt)
             o.stp_hotpath(kt)
