@@ -433,7 +433,7 @@ __device__ __forceinline__ int p2_tiles(const Dom<T>& d) {
 }
 
 template <class T, bool VVL>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? (VVL ? 3 : 4) : 2) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar bar) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar bar) {
   unsigned int bar_epoch = 0;  // barriers passed by this block
   __shared__ T zs_s[P2_TY + 1][P2_TX + 1];
   // Variable volume: the new ssh ssha_e [0], the predictor ssh of the next sub-step
