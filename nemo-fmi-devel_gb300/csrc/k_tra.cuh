@@ -640,7 +640,7 @@ __device__ __forceinline__ void iso_coefs_at(const Dom<T>& d, const LdfArgs<T>& 
 // whose differences the fluxes take, the vertical gradients zdk1t(k) (= zdkt(k+1))
 // and the four horizontal gradients zdit / zdjt that the w-face flux averages.
 template <class T>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 3) k_iso_flux(Dom<T> d, LdfArgs<T> a) {
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 3) k_iso_flux(Dom<T> d, LdfArgs<T> a) {
   const KIdx c = k_index(d);
   if (!c.valid) return;
   const int jpi = d.jpi, jpj = d.jpj, jpk = d.jpk;
