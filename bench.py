@@ -180,10 +180,10 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def build_case(nn, nmem, seed, workload="gyre"):
-    if workload == "shelf":  # 1000 x 1200 x 56 synthetic shelf, z* levels
+def build_case(nn, nmem, seed, workload="gyre", shelf_grid=(1000, 1200)):
+    if workload == "shelf":  # synthetic shelf, 56 z* levels (1000 x 1200 by default)
         from nemo_gpu import shelf
-        dom = shelf.domain(1000, 1200, 56, seed=seed)
+        dom = shelf.domain(shelf_grid[0], shelf_grid[1], 56, seed=seed)
         nam = shelf.namelist()
         states = [shelf.state(dom, nam, seed=seed, member=m) for m in range(nmem)]
         return dom, nam, states
@@ -219,7 +219,8 @@ def cpu_model():
 
 def workload_name(args):
     if args.workload == "shelf":
-        return ("synthetic shelf 1000x1200x56 hot path step (dyn_spg_ts z* flux form + FCT 4/4 + iso ldf "
+        nx, ny = args.shelf_grid
+        return (f"synthetic shelf {nx}x{ny}x56 hot path step (dyn_spg_ts z* flux form + FCT 4/4 + iso ldf "
                 "with partial steps + zdf)")
     return f"GYRE nn_GYRE={args.nn} hot path step (dyn_spg_ts + FCT + iso ldf + zdf)"
 
@@ -365,7 +366,8 @@ def run_gpu(args):
     rank, world = dist.init("nccl")
     _, _, local = dist.env_rank()
     torch.cuda.set_device(local)
-    dom, nam, states = build_case(args.nn, args.members, seed=100 + rank, workload=args.workload)
+    dom, nam, states = build_case(args.nn, args.members, seed=100 + rank, workload=args.workload,
+                                   shelf_grid=args.shelf_grid)
     jpi, jpj, jpk = dom["jpi"], dom["jpj"], dom["jpk"]
     cells = jpi * jpj * jpk * args.members
     stream = torch.cuda.Stream()
@@ -640,7 +642,8 @@ def run_reference(args):
     rank, world = dist.init("gloo")
     if rank != 0:
         return
-    dom, nam, states = build_case(args.nn, args.members, seed=100, workload=args.workload)
+    dom, nam, states = build_case(args.nn, args.members, seed=100, workload=args.workload,
+                                   shelf_grid=args.shelf_grid)
     ncores = os.cpu_count()
     ora.set_threads(ncores)
     members = [OracleStep(dom, nam, st) for st in states]  # one oracle per member, stepped in turn
@@ -808,6 +811,8 @@ def main():
                     help="gyre: GYRE nn_GYRE=--nn (the headline); shelf: the 1000x1200x56 z* shelf; "
                          "window: the gradient of a 48-step FP64 tracer window (nn_GYRE=10); "
                          "model: the model step (the hot path closed into a time step)")
+    ap.add_argument("--shelf-grid", type=int, nargs=2, default=[1000, 1200], metavar=("NX", "NY"),
+                    help="horizontal size of the shelf workload (a smaller one for profiler captures)")
     ap.add_argument("--members", type=int, default=1)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

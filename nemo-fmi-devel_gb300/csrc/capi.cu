@@ -1032,7 +1032,11 @@ int run_ldf_slp(nemo_ctx* c, const void* prd, const void* pn2) {
   a.hmlp = (const T*)c->f[NEMO_F_HMLP]; a.hmlpt = (const T*)c->f[NEMO_F_HMLPT];
   a.uslp = (T*)c->f[NEMO_F_USLP]; a.vslp = (T*)c->f[NEMO_F_VSLP];
   a.wslpi = (T*)c->f[NEMO_F_WSLPI]; a.wslpj = (T*)c->f[NEMO_F_WSLPJ];
-  if (nm.ln_zps) { a.gru_b = (const T*)c->f[NEMO_F_GRU]; a.grv_b = (const T*)c->f[NEMO_F_GRV]; }
+  if (nm.ln_zps) {
+    if (!c->f[NEMO_F_GRU] || !c->f[NEMO_F_GRV])
+      return fail(c, NEMO_ERR_UNBOUND, "ldf_slp with partial steps: gru and grv (zps_hde) must be bound");
+    a.gru_b = (const T*)c->f[NEMO_F_GRU]; a.grv_b = (const T*)c->f[NEMO_F_GRV];
+  }
   a.zu = w; a.zv = w + n3; a.zwi = w + 2 * n3; a.zwj = w + 3 * n3;
   T* w2 = w + 4 * n3;
   a.uml = w2; a.vml = w2 + n2; a.wiml = w2 + 2 * n2; a.wjml = w2 + 3 * n2; a.hu = w2 + 4 * n2; a.hv = w2 + 5 * n2;
@@ -2295,8 +2299,6 @@ int nemo_gpu_ldf_slp(nemo_ctx* c, int kt, const void* prd, const void* pn2) {
   const nemo_namelist& nm = c->nam;
   if (nm.ln_isfcav || nm.ln_sco)
     return fail(c, NEMO_ERR_UNSUPPORTED, "ldf_slp: z-coordinate without cavities only");
-  if (nm.ln_zps && (!c->f[NEMO_F_GRU] || !c->f[NEMO_F_GRV]))
-    return fail(c, NEMO_ERR_UNBOUND, "ldf_slp with partial steps: gru and grv (zps_hde) must be bound");
   return c->prec == NEMO_PREC_FP64 ? run_ldf_slp<double>(c, prd, pn2) : run_ldf_slp<float>(c, prd, pn2);
 }
 

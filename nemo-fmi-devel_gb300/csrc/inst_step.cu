@@ -75,8 +75,13 @@ cudaError_t launch_ssh_swp_vvl(const Dom<T>& d, const VvlArgs<T>& a, T* sshb, T*
 
 template <class T>
 cudaError_t launch_ldf_slp(const Dom<T>& d, const SlpArgs<T>& a, cudaStream_t s) {
-  k_slp_mxl<T><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a);
-  k_slp_pre<T><<<s_pt(d), dim3(SX, SY), 0, s>>>(d, a);
+  if (a.gru_b) {  // partial steps: the bottom level's gradients from zps_hde
+    k_slp_mxl<T, true><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a);
+    k_slp_pre<T, true><<<s_pt(d), dim3(SX, SY), 0, s>>>(d, a);
+  } else {
+    k_slp_mxl<T, false><<<s_col(d), dim3(SX, SY), 0, s>>>(d, a);
+    k_slp_pre<T, false><<<s_pt(d), dim3(SX, SY), 0, s>>>(d, a);
+  }
   k_slp_filter<T><<<s_pt(d), dim3(SX, SY), 0, s>>>(d, a);
   ktick(NEMO_K_LDF_SLP, s);
   return cudaGetLastError();

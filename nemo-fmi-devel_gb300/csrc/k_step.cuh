@@ -241,13 +241,13 @@ __global__ void k_ssh_swp(Dom<T> d, T* sshb, T* sshn, const A* __restrict__ ssha
 
 
 // ----------------------------------------------------------------------- ldf_slp
-// ldf_slp (ldfslp.F90:83-374) with ldf_slp_mxl (:620-729), z-coordinate without
-// cavities or partial steps, in three kernels: the slopes just below the mixed
+// ldf_slp (ldfslp.F90:83-374) with ldf_slp_mxl (:620-729), z-coordinate with or
+// without partial steps, without cavities, in three kernels: the slopes just below the mixed
 // layer (one column per thread), the slopes before the Shapiro filter at u-, v- and
 // w-points (one point per thread), the filter with the coastal decrease and lbc.
 // The density gradients zgru, zgrv and zdzr of the reference's work arrays are
 // formed where they are read, from the same operands in the same order.
-template <class T>
+template <class T, bool ZPS = false>
 struct SlpPt {
   const Dom<T>& d;
   const SlpArgs<T>& a;
@@ -261,13 +261,18 @@ struct SlpPt {
   __device__ __forceinline__ T tm(int i, int j, int k) const { return tmsk<T>(d.ci[Q(i, j, 1)], k); }
   __device__ __forceinline__ T wm(int i, int j, int k) const { return wmsk<T>(d.ci[Q(i, j, 1)], k); }
   __device__ __forceinline__ T prd(int i, int j, int k) const { return a.prd[m3 + Q(i, j, k)]; }
-  // with partial steps the bottom level's gradients are zps_hde's (ldfslp.F90:144-151)
+  // with partial steps (ZPS) the bottom level's gradients are zps_hde's
+  // (ldfslp.F90:144-151); the z-coordinate form compiles without the test
   __device__ __forceinline__ T gru(int i, int j, int k) const {
-    if (a.gru_b && k == d.ci[Q(i, j, 1)].mbku) return a.gru_b[(long)m * d.n2 + Q(i, j, 1)];
+    if constexpr (ZPS) {
+      if (k == d.ci[Q(i, j, 1)].mbku) return a.gru_b[(long)m * d.n2 + Q(i, j, 1)];
+    }
     return um(i, j, k) * (prd(i + 1, j, k) - prd(i, j, k));
   }
   __device__ __forceinline__ T grv(int i, int j, int k) const {
-    if (a.grv_b && k == d.ci[Q(i, j, 1)].mbkv) return a.grv_b[(long)m * d.n2 + Q(i, j, 1)];
+    if constexpr (ZPS) {
+      if (k == d.ci[Q(i, j, 1)].mbkv) return a.grv_b[(long)m * d.n2 + Q(i, j, 1)];
+    }
     return vm(i, j, k) * (prd(i, j + 1, k) - prd(i, j, k));
   }
   __device__ __forceinline__ T dzr(int i, int j, int k) const {
@@ -280,7 +285,7 @@ struct SlpPt {
   }
 };
 
-template <class T>
+template <class T, bool ZPS>
 __global__ void k_slp_mxl(Dom<T> d, SlpArgs<T> a) {
   ColIdx<T> c = col_index(d);
   if (!c.valid) return;
@@ -290,7 +295,7 @@ __global__ void k_slp_mxl(Dom<T> d, SlpArgs<T> a) {
     a.hu[p] = T(0); a.hv[p] = T(0);
     return;
   }
-  const SlpPt<T> P{d, a, (long)c.m * d.n3, c.m};
+  const SlpPt<T, ZPS> P{d, a, (long)c.m * d.n3, c.m};
   const int i = c.i, j = c.j, jpk = d.jpk, jpi = d.jpi;
   const long ij = c.ij, m2 = (long)c.m * d.n2;
   const int n0 = a.nmln[m2 + ij], ne = a.nmln[m2 + ij + 1], nn = a.nmln[m2 + ij + jpi];
@@ -329,7 +334,7 @@ __global__ void k_slp_mxl(Dom<T> d, SlpArgs<T> a) {
 
 // The slopes before the filter: u, v (:197-233) and w (:281-315) at levels 2..jpkm1;
 // 0 on the closed edges (the lbc_lnk of :234 and :316).
-template <class T>
+template <class T, bool ZPS>
 __global__ void k_slp_pre(Dom<T> d, SlpArgs<T> a) {
   const PtIdx c = pt_index(d);
   if (!c.valid || c.k < 2 || c.k > d.jpk - 1) return;
@@ -338,7 +343,7 @@ __global__ void k_slp_pre(Dom<T> d, SlpArgs<T> a) {
     a.zu[o] = T(0); a.zv[o] = T(0); a.zwi[o] = T(0); a.zwj[o] = T(0);
     return;
   }
-  const SlpPt<T> P{d, a, (long)c.m * d.n3, c.m};
+  const SlpPt<T, ZPS> P{d, a, (long)c.m * d.n3, c.m};
   const int i = c.i, j = c.j, k = c.k, jpi = d.jpi;
   const long ij = c.ij, p = (long)c.m * d.n2 + ij;
   // u- and v-points
