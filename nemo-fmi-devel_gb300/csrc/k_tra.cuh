@@ -933,7 +933,12 @@ struct ZdfArgs {
 };
 
 // Any jpk <= KMAX, the reference's recurrences with the pivots in local memory; in
-// double precision the operations are those of trazdf.F90:218-264 in order.
+// double precision the operations are those of trazdf.F90:218-264 in order, with
+// every quotient correctly rounded as the reference's division gives it, but formed
+// from a reciprocal (divq): one division per level (1 / zwt(k)) where the reference
+// divides six times (zwi, zws, the two pivot quotients of the 1st recurrence and the
+// 3rd recurrence of each of T and S); zwi(k+1) is zws(k), the same expression, formed
+// once; the divisions by e3w use the rest-state reciprocal profile where e3w is it.
 template <class T>
 __global__ void k_zdf_imp(Dom<T> d, ZdfArgs<T> a) {
   ColIdx<T> c = col_index(d);
@@ -944,7 +949,7 @@ __global__ void k_zdf_imp(Dom<T> d, ZdfArgs<T> a) {
   const long m3 = (long)c.m * n3;
   // rat(k) = zwi(k) / zwt(k-1): the tracer-independent factor of the 2nd recurrence
   T rat[KMAX], zws[KMAX], zwt[KMAX];
-  T zwi_k[sizeof(T) == 4 ? KMAX : 1];  // FP32: the sub-diagonal, for the increment form
+  T aux[KMAX];  // FP32: the sub-diagonal zwi, for the increment form; FP64: 1 / zwt
   for (int n = 0; n < a.kjpt; ++n) {
     const bool build = (!a.is_trc && (n == 0 || (n == 1 && a.ddm))) || (a.is_trc && n == 0);
     if (build) {
@@ -957,6 +962,27 @@ __global__ void k_zdf_imp(Dom<T> d, ZdfArgs<T> a) {
         if (a.add && k <= jpk - 1) v = v + a.add[q];
         return v;
       };
+      if constexpr (sizeof(T) == 8) {
+        // 1st recurrence as written in the reference (trazdf.F90:218-234)
+        const bool r3w = d.r1_e3w && d.e3w_n.s == 0;  // e3w is the rest-state profile
+        auto over_e3w = [&](T x, int k) {
+          const T e = d.e3w_n(c.ij, k, c.m);
+          return r3w ? divq(x, e, d.r1_e3w[k - 1]) : x / e;
+        };
+        T zwi = over_e3w(-a.p2dt * wt(1), 1);
+        for (int k = 1; k <= jpk - 1; ++k) {
+          zws[k] = over_e3w(-a.p2dt * wt(k + 1), k + 1);
+          const T zwd = d.e3t_a(c.ij, k, c.m) - zwi - zws[k];
+          if (k == 1) {
+            zwt[k] = zwd;
+          } else {
+            rat[k] = divq(zwi, zwt[k - 1], aux[k - 1]);
+            zwt[k] = zwd - divq(zwi * zws[k - 1], zwt[k - 1], aux[k - 1]);
+          }
+          aux[k] = T(1) / zwt[k];
+          zwi = zws[k];
+        }
+      } else {
       T wtk = wt(1);
       T g = T(0);
       for (int k = 1; k <= jpk - 1; ++k) {
@@ -965,12 +991,8 @@ __global__ void k_zdf_imp(Dom<T> d, ZdfArgs<T> a) {
         zws[k] = -a.p2dt * wtk1 / d.e3w_n(c.ij, k + 1, c.m);
         const T e3a = d.e3t_a(c.ij, k, c.m);
         if (k >= 2) rat[k] = zwi / zwt[k - 1];
-        if constexpr (sizeof(T) == 4) zwi_k[k] = zwi;
-        if constexpr (sizeof(T) == 8) {
-          // 1st recurrence as written in the reference (trazdf.F90:223-234)
-          const T zwd = e3a - zwi - zws[k];
-          zwt[k] = (k == 1) ? zwd : zwd - zwi * zws[k - 1] / zwt[k - 1];
-        } else {
+        aux[k] = zwi;
+        {
           // FP32: the same pivots without cancellation. With g(k) = zwt(k) + zws(k),
           // zwt(k) = zwd(k) - zwi(k) zws(k-1)/zwt(k-1) is g(k) - zws(k) where
           // g(k) = e3t_a(k) - zwi(k) g(k-1)/zwt(k-1): a sum of non-negative terms
@@ -980,6 +1002,7 @@ __global__ void k_zdf_imp(Dom<T> d, ZdfArgs<T> a) {
           zwt[k] = g - zws[k];
         }
         wtk = wtk1;
+      }
       }
     }
     const long mo = ((long)c.m * a.kjpt + n) * n3;
@@ -995,7 +1018,7 @@ __global__ void k_zdf_imp(Dom<T> d, ZdfArgs<T> a) {
         const long q = c.ij + (long)(k - 1) * n2;
         const T tbk = tb[q];
         T r = a.p2dt * d.e3t_n(c.ij, k, c.m) * ta[q] + (d.e3t_b(c.ij, k, c.m) - d.e3t_a(c.ij, k, c.m)) * tbk;
-        if (k > 1) r = r - zwi_k[k] * (tb[q - n2] - tbk);
+        if (k > 1) r = r - aux[k] * (tb[q - n2] - tbk);
         if (k < K1) r = r - zws[k] * (tb[q + n2] - tbk);
         else r = r + zws[k] * tbk;
         prev = (k == 1) ? r : r - rat[k] * prev;
@@ -1024,12 +1047,12 @@ __global__ void k_zdf_imp(Dom<T> d, ZdfArgs<T> a) {
     {
       const int k = jpk - 1;
       const long q = c.ij + (long)(k - 1) * n2;
-      nxt = ta[q] / zwt[k] * tmsk<T>(ci, k);
+      nxt = divq(ta[q], zwt[k], aux[k]) * tmsk<T>(ci, k);
       ta[q] = (clamp && nxt < T(0)) ? T(0.1) : nxt;
     }
     for (int k = jpk - 2; k >= 1; --k) {
       const long q = c.ij + (long)(k - 1) * n2;
-      nxt = (ta[q] - zws[k] * nxt) / zwt[k] * tmsk<T>(ci, k);
+      nxt = divq(ta[q] - zws[k] * nxt, zwt[k], aux[k]) * tmsk<T>(ci, k);
       ta[q] = (clamp && nxt < T(0)) ? T(0.1) : nxt;
     }
     }
