@@ -747,7 +747,10 @@ int nemo_gpu_stp_hotpath(nemo_ctx *ctx, int kt);
  * reference's ln_timing (timing.F90:89-212, timing_start/stop around tra_adv,
  * tra_ldf, tra_zdf, dyn_spg). While on, the hot path runs without graph replay and
  * records CUDA events between routines. ms[0..3] = cumulative milliseconds in
- * dyn_spg_ts, tra_adv, tra_ldf, tra_zdf since timing was switched on. */
+ * dyn_spg_ts, tra_adv, tra_ldf, tra_zdf since timing was switched on. Where the
+ * iso-neutral operator is fused into FCT (ln_traldf_iso without blp), tra_ldf is
+ * the iso-neutral flux kernel and tra_adv the three FCT stages, the last of which
+ * also adds the iso-neutral divergence. */
 int nemo_gpu_set_timing(nemo_ctx *ctx, int on);
 int nemo_gpu_get_timing(nemo_ctx *ctx, double *ms, int *ncalls);
 
