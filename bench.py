@@ -474,6 +474,11 @@ def run_gpu(args):
         bi = sum(host[n].numel() * host[n].element_size() for n in ins)
         bo = sum(host[n].numel() * host[n].element_size() for n in outs)
         ke = max(2, args.steps // 2)
+        for n in ins:  # one untimed round (the context makes its staging buffers here)
+            ctx.upload(n, host[n])
+        ctx.stp_hotpath(kt0 + 8999)
+        for n in outs:
+            ctx.download(n, host[n])
         ctx.synchronize()
         t0 = time.perf_counter()
         for s in range(ke):

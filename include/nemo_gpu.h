@@ -295,21 +295,24 @@ int nemo_gpu_field_is_fp64(const nemo_ctx *ctx, int field_id);
 int nemo_gpu_spg_info(const nemo_ctx *ctx, int *icycle, int *nn_baro, double *rdtbt);
 
 /* Copy between a host buffer and a bound field (all members). Both are
- * asynchronous and ordered with the context's work per field. An upload runs after
- * the work already queued that reads the field and after a pending download of the
- * field; a download runs after the work already queued that writes the field and
+ * asynchronous and ordered with the context's work per field. An upload copies the
+ * host buffer into a device staging buffer of the field (made at its first upload)
+ * on a copy stream, as soon as the staging buffer's previous contents are in the
+ * field; the work that next reads or writes the field, or a download of it, first
+ * copies the staged data into the field on its own stream (after the field's pending
+ * download). So the next step's uploads run while this step still reads the
+ * fields, and of two uploads of a field with no work between them the later one
+ * wins. A download runs after the work already queued that writes the field (after
+ * nemo_gpu_stp_hotpath: the fields dyn_spg_ts writes as soon as dyn_spg_ts ends) and
  * after a pending upload of it. Uploads run in call order on one copy stream and
  * downloads on another, so one step's downloads overlap the next step's uploads.
- * After nemo_gpu_stp_hotpath "the work that reads / writes the field" is the part of
- * the step that last reads / writes it: the upload of a field the next step needs
- * early (dyn_spg_ts's) starts while this step's tracer kernels run, and a download of
- * what dyn_spg_ts writes starts when dyn_spg_ts ends. A routine waits only for the
- * copies of the fields it reads or writes when nemo_gpu_stp_hotpath is called with
- * copies in flight (dyn_spg_ts starts while the tracers still upload), for all
- * pending copies otherwise. Upload fields in the order the step releases them:
- * dyn_spg_ts's (ua, va, the 2-D fields), the slopes, un vn wn tsn, then the rest.
- * Host memory should be pinned; read a downloaded buffer, or upload it into another
- * field, only after nemo_gpu_synchronize. */
+ * When nemo_gpu_stp_hotpath is called with copies in flight, each of its parts
+ * waits only for the copies of the fields it reads or writes (dyn_spg_ts starts
+ * while the tracers still upload); other routines wait for all pending copies.
+ * Upload fields in the order the step reads them: dyn_spg_ts's (ua, va, the 2-D
+ * fields), the slopes, un vn wn tsn, then the rest. Host memory should be pinned;
+ * read a downloaded buffer, or reuse an uploaded one, only after
+ * nemo_gpu_synchronize. */
 int nemo_gpu_field_upload(nemo_ctx *ctx, int field_id, const void *host);
 int nemo_gpu_field_download(nemo_ctx *ctx, int field_id, void *host);
 

@@ -156,11 +156,18 @@ struct nemo_ctx {
   cudaEvent_t ev_field[NEMO_F_COUNT] = {};  // the last download of each field
   bool upf_pending[NEMO_F_COUNT] = {};
   bool field_pending[NEMO_F_COUNT] = {};
-  // the ends of dyn_spg_ts, the iso-neutral fluxes, FCT and the whole step in the
-  // last (staged) hot-path step: downloads of what dyn_spg_ts writes wait only for
-  // it, and the upload of a field waits only for the last part that reads it
-  cudaEvent_t ev_spg_done = nullptr, ev_fct_done = nullptr, ev_step_done = nullptr;
-  cudaEvent_t ev_iso_done = nullptr;  // ev_join when the iso-neutral fluxes ran on the side stream, else ev_fct_done
+  // the staging buffer of each uploaded field: an upload copies the host buffer into
+  // it on the copy stream as soon as the buffer's previous contents have been copied
+  // into the field, and the work that next reads the field (or a download of it)
+  // makes that device copy on its own stream; so the next step's uploads do not wait
+  // for this step's readers of the fields
+  void* stage[NEMO_F_COUNT] = {};
+  size_t stage_bytes[NEMO_F_COUNT] = {};
+  cudaEvent_t ev_h2d[NEMO_F_COUNT] = {};  // the last host copy into the staging buffer
+  bool stage_dirty[NEMO_F_COUNT] = {};    // staged data not yet copied into the field
+  // the end of dyn_spg_ts in the last (staged) hot-path step: downloads of what
+  // dyn_spg_ts writes wait only for it
+  cudaEvent_t ev_spg_done = nullptr;
   bool spg_done_valid = false;
   // hot path: the iso-neutral fluxes run on a side stream beside dyn_spg_ts
   cudaStream_t side = nullptr;
@@ -198,9 +205,24 @@ int cuda_fail(nemo_ctx* c, cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
   } while (0)
 
+// The device copy of field id's staged upload into the field, on stream st: after
+// the host copy into the staging buffer and the field's pending download (the copy
+// overwrites the field); ev_upf marks its end.
+int flush_stage(nemo_ctx* c, cudaStream_t st, int id) {
+  if (!c->stage_dirty[id]) return NEMO_OK;
+  CK(cudaStreamWaitEvent(st, c->ev_h2d[id], 0), "staged upload");
+  if (c->field_pending[id]) CK(cudaStreamWaitEvent(st, c->ev_field[id], 0), "staged upload");
+  CK(cudaMemcpyAsync(c->f[id], c->stage[id], c->stage_bytes[id], cudaMemcpyDeviceToDevice, st), "staged upload");
+  CK(cudaEventRecord(c->ev_upf[id], st), "staged upload");
+  c->stage_dirty[id] = false;
+  c->upf_pending[id] = true;
+  return NEMO_OK;
+}
+
 // Make stream st wait for the pending upload of field id (its device data) and, when
 // `writes`, for its pending download (the work overwrites it).
 int wait_field(nemo_ctx* c, cudaStream_t st, int id, bool writes) {
+  if (flush_stage(c, st, id)) return NEMO_ERR_CUDA;
   if (c->upf_pending[id]) CK(cudaStreamWaitEvent(st, c->ev_upf[id], 0), "wait for an upload");
   if (writes && c->field_pending[id]) CK(cudaStreamWaitEvent(st, c->ev_field[id], 0), "wait for a download");
   return NEMO_OK;
@@ -218,26 +240,9 @@ int join_copies(nemo_ctx* c) {
   return NEMO_OK;
 }
 
-// the event after the last part of the last staged hot-path step that reads field id
-cudaEvent_t last_reader(const nemo_ctx* c, int id) {
-  switch (id) {
-    case NEMO_F_UA: case NEMO_F_VA: case NEMO_F_UB: case NEMO_F_VB:
-      return c->ev_spg_done;
-    case NEMO_F_USLP: case NEMO_F_VSLP: case NEMO_F_WSLPI: case NEMO_F_WSLPJ:
-    case NEMO_F_AHTU: case NEMO_F_AHTV: case NEMO_F_GTSU: case NEMO_F_GTSV:
-      return c->ev_iso_done;
-    case NEMO_F_UN: case NEMO_F_VN: case NEMO_F_WN: case NEMO_F_TSN:
-      return c->ev_fct_done;
-    default:
-      break;
-  }
-  if (id >= NEMO_F_SSHB && id != NEMO_F_E3F_N) return c->ev_spg_done;  // the 2-D fields: dyn_spg_ts only
-  return c->ev_step_done;
-}
-
 bool copies_pending(const nemo_ctx* c) {
   for (int id = 0; id < NEMO_F_COUNT; ++id)
-    if (c->upf_pending[id] || c->field_pending[id]) return true;
+    if (c->upf_pending[id] || c->field_pending[id] || c->stage_dirty[id]) return true;
   return false;
 }
 
@@ -1714,10 +1719,6 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
   if (s) return s;
   }
   mark(3);
-  if (staged) {
-    CK(cudaEventRecord(c->ev_fct_done, c->stream), "end of tra_adv / tra_ldf");
-    c->ev_iso_done = overlap ? c->ev_join : c->ev_fct_done;
-  }
   s = run_zdf<T>(c, r2dt, F[NEMO_F_TSB], F[NEMO_F_TSA], 2, 0, 1);
   if (s) return s;
   if (model) {  // tra_nxt, dyn_nxt, ssh_swp (step.F90:277-279), dia_hsb (:282), stp_ctl (:305)
@@ -1730,7 +1731,6 @@ int run_hotpath(nemo_ctx* c, int kt, bool staged, bool model = false) {
     }
     if ((s = run_stp_ctl<T>(c))) return s;
   }
-  if (staged) CK(cudaEventRecord(c->ev_step_done, c->stream), "end of the step");
   if (c->timing) {
     mark(4);
     CK(cudaEventSynchronize(c->tev[4]), "timing");
@@ -1866,8 +1866,9 @@ int nemo_gpu_create(const nemo_dom_desc* dm, const nemo_namelist* nam, int nmemb
     if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return bad(NEMO_ERR_CUDA);
   for (auto& e : c->ev_upf)
     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return bad(NEMO_ERR_CUDA);
-  for (cudaEvent_t* e : {&c->ev_spg_done, &c->ev_fct_done, &c->ev_step_done})
-    if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return bad(NEMO_ERR_CUDA);
+  for (auto& e : c->ev_h2d)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return bad(NEMO_ERR_CUDA);
+  if (cudaEventCreateWithFlags(&c->ev_spg_done, cudaEventDisableTiming) != cudaSuccess) return bad(NEMO_ERR_CUDA);
   for (auto& e : c->ev_field)
     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return bad(NEMO_ERR_CUDA);
   int s = derive_domain(c, dm);
@@ -1971,8 +1972,10 @@ int nemo_gpu_destroy(nemo_ctx* c) {
     if (e) cudaEventDestroy(e);
   for (auto e : c->ev_upf)
     if (e) cudaEventDestroy(e);
-  for (cudaEvent_t e : {c->ev_spg_done, c->ev_fct_done, c->ev_step_done})
+  for (auto e : c->ev_h2d)
     if (e) cudaEventDestroy(e);
+  for (auto p : c->stage) cudaFree(p);
+  if (c->ev_spg_done) cudaEventDestroy(c->ev_spg_done);
   if (c->side) cudaStreamDestroy(c->side);
   for (auto e : c->ev_field)
     if (e) cudaEventDestroy(e);
@@ -2050,19 +2053,27 @@ int nemo_gpu_field_upload(nemo_ctx* c, int id, const void* host) {
   if (!c || id < 0 || id >= NEMO_F_COUNT || !host) return fail(c, NEMO_ERR_ARG, "field_upload: bad argument");
   if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "field_upload: field %d is not bound", id);
   size_t bytes = field_numel(c, id) * c->nmem * (nemo_gpu_field_is_fp64(c, id) ? 8 : 4);
-  // after the work that reads the field (its last reader in the last staged hot-path
-  // step, else all the work already queued) and the field's download
   cudaStream_t st = c->h2d[0];
-  if (c->spg_done_valid) {
-    CK(cudaStreamWaitEvent(st, last_reader(c, id), 0), "field_upload");
-  } else {
-    CK(cudaEventRecord(c->ev_main, c->stream), "field_upload");
-    CK(cudaStreamWaitEvent(st, c->ev_main, 0), "field_upload");
+  if (c->stage_bytes[id] != bytes) {  // the field's staging buffer, made at its first upload
+    if (c->stage[id]) {
+      CK(cudaStreamSynchronize(c->stream), "field_upload");
+      CK(cudaStreamSynchronize(c->side), "field_upload");
+      CK(cudaStreamSynchronize(st), "field_upload");
+      cudaFree(c->stage[id]);
+      c->stage[id] = nullptr;
+      c->stage_bytes[id] = 0;
+      c->stage_dirty[id] = false;
+    }
+    if (cudaMalloc(&c->stage[id], bytes) != cudaSuccess)
+      return fail(c, NEMO_ERR_NOMEM, "field_upload: staging buffer of %zu bytes", bytes);
+    c->stage_bytes[id] = bytes;
+  } else if (!c->stage_dirty[id]) {
+    // the buffer's previous contents are in the field once its device copy has run
+    CK(cudaStreamWaitEvent(st, c->ev_upf[id], 0), "field_upload");
   }
-  if (c->field_pending[id]) CK(cudaStreamWaitEvent(st, c->ev_field[id], 0), "field_upload");
-  CK(cudaMemcpyAsync(c->f[id], host, bytes, cudaMemcpyHostToDevice, st), "field_upload");
-  CK(cudaEventRecord(c->ev_upf[id], st), "field_upload");
-  c->upf_pending[id] = true;
+  CK(cudaMemcpyAsync(c->stage[id], host, bytes, cudaMemcpyHostToDevice, st), "field_upload");
+  CK(cudaEventRecord(c->ev_h2d[id], st), "field_upload");
+  c->stage_dirty[id] = true;
   return NEMO_OK;
 }
 
@@ -2073,6 +2084,7 @@ int nemo_gpu_field_download(nemo_ctx* c, int id, void* host) {
   // after the work that writes the field (dyn_spg_ts of the last hot-path step for
   // the fields it writes, else all the work already queued) and the field's upload
   cudaStream_t st = c->d2h[0];
+  if (flush_stage(c, c->stream, id)) return NEMO_ERR_CUDA;  // an upload not yet in the field
   if (c->spg_done_valid && spg_writes(id)) {
     CK(cudaStreamWaitEvent(st, c->ev_spg_done, 0), "field_download");
   } else {

@@ -57,3 +57,27 @@ def test_overlapped_copies_match_serialised(prec):
     for n in OUTS:
         for s, (x, y) in enumerate(zip(a[n], b[n])):
             assert torch.equal(x, y), f"{n} step {s}: overlapped copies differ from serialised ones"
+
+
+def test_upload_then_download_without_a_step():
+    """An upload is staged on the device and copied into the field by the next work
+    that reads it; a download before any such work still returns the uploaded
+    values, and of two uploads of a field without work between them the later one
+    wins."""
+    p = Pair(nn=1, prec="mixed", seed=3)
+    p.bind_hotpath()
+    n = p.dev["TSB"].numel()
+    first = torch.arange(n, dtype=torch.float32).pin_memory()
+    second = (torch.arange(n, dtype=torch.float32) * 0.5 + 1.0).pin_memory()
+    got = torch.empty(n, dtype=torch.float32).pin_memory()
+    p.ctx.upload("TSB", first)
+    p.ctx.download("TSB", got)
+    p.ctx.synchronize()
+    assert torch.equal(got, first)
+    p.ctx.upload("TSB", first)
+    p.ctx.upload("TSB", second)
+    p.ctx.download("TSB", got)
+    p.ctx.synchronize()
+    assert torch.equal(got, second)
+    # and the field itself (read through torch after a synchronize) holds it too
+    assert torch.equal(p.dev["TSB"].detach().reshape(-1).cpu(), second)
