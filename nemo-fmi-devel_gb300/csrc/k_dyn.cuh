@@ -435,11 +435,14 @@ __device__ __forceinline__ int p2_tiles(const Dom<T>& d) {
 template <class T, bool VVL>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d, SpgArgs<T> a, GridBar bar) {
   unsigned int bar_epoch = 0;  // barriers passed by this block
-  __shared__ T zs_s[P2_TY + 1][P2_TX + 1];
+  // two buffers, alternating between a block's tiles: a warp may start the next
+  // tile while others still read this one's (the block barrier between the two
+  // stages of the next tile orders the reuse)
+  __shared__ T zs_b[2][P2_TY + 1][P2_TX + 1];
   // Variable volume: the new ssh ssha_e [0], the predictor ssh of the next sub-step
   // [1] and the now ssh [2] of the tile and its halo, for the depths at u- and
   // v-points that average two neighbouring T-points.
-  __shared__ T vv_s[VVL ? 3 : 1][P2_TY + 1][P2_TX + 1];
+  __shared__ T vv_b[2][VVL ? 3 : 1][P2_TY + 1][P2_TX + 1];
   const int n2 = (int)d.n2;
   const int nmem2 = d.nmem * n2;
   const int jpi = d.jpi, jpj = d.jpj;
@@ -577,6 +580,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
     for (int t = blockIdx.x; t < ntile; t += gridDim.x, ++slot) {
       int m2, i0, j0;
       tile(t, m2, i0, j0);
+      auto& zs_s = zs_b[slot & 1];
+      auto& vv_s = vv_b[slot & 1];
       const long hm = VVL ? m2 : 0;  // member offset of the depths and Coriolis factors
       // Every value this tile reads that the sub-step does not produce is loaded
       // first, so the loads of both stages are in flight together.
@@ -820,7 +825,6 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_spg_p2(Dom<T> d
           }
         }
       }
-      __syncthreads();  // zs_s is rewritten by the next tile
     }
     r = (r + 3) & 3;
     if (!grid_barrier(bar, bar_epoch)) return;
