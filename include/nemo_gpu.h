@@ -295,14 +295,15 @@ int nemo_gpu_field_is_fp64(const nemo_ctx *ctx, int field_id);
 int nemo_gpu_spg_info(const nemo_ctx *ctx, int *icycle, int *nn_baro, double *rdtbt);
 
 /* Copy between a host buffer and a bound field (all members). Both are
- * asynchronous and ordered with the context's work per field. An upload copies the
- * host buffer into a device staging buffer of the field (made at its first upload)
- * on a copy stream, as soon as the staging buffer's previous contents are in the
- * field; the work that next reads or writes the field, or a download of it, first
- * copies the staged data into the field on its own stream (after the field's pending
- * download). So the next step's uploads run while this step still reads the
- * fields, and of two uploads of a field with no work between them the later one
- * wins. A download runs after the work already queued that writes the field (after
+ * asynchronous and ordered with the context's work per field. An upload of a field
+ * of 1 MB or more copies the host buffer into a device staging buffer of the field
+ * (made at its first upload) on a copy stream, as soon as the staging buffer's
+ * previous contents are in the field; the work that next reads or writes the field,
+ * or a download of it, first copies the staged data into the field on its own stream
+ * (after the field's pending download). So the next step's uploads run while this
+ * step still reads the fields, and of two uploads of a field with no work between
+ * them the later one wins. A smaller field is copied straight into place after the
+ * work already queued and its pending download. A download runs after the work already queued that writes the field (after
  * nemo_gpu_stp_hotpath: the fields dyn_spg_ts writes as soon as dyn_spg_ts ends) and
  * after a pending upload of it. Uploads run in call order on one copy stream and
  * downloads on another, so one step's downloads overlap the next step's uploads.

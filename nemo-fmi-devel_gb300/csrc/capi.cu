@@ -2054,6 +2054,19 @@ int nemo_gpu_field_upload(nemo_ctx* c, int id, const void* host) {
   if (!c->f[id]) return fail(c, NEMO_ERR_UNBOUND, "field_upload: field %d is not bound", id);
   size_t bytes = field_numel(c, id) * c->nmem * (nemo_gpu_field_is_fp64(c, id) ? 8 : 4);
   cudaStream_t st = c->h2d[0];
+  // A field under 1 MB goes straight into place, after the work already queued and
+  // its pending download: for it the device copy out of a staging buffer would cost
+  // more than the overlap gains.
+  constexpr size_t stage_min_bytes = (size_t)1 << 20;
+  if (bytes < stage_min_bytes) {
+    CK(cudaEventRecord(c->ev_main, c->stream), "field_upload");
+    CK(cudaStreamWaitEvent(st, c->ev_main, 0), "field_upload");
+    if (c->field_pending[id]) CK(cudaStreamWaitEvent(st, c->ev_field[id], 0), "field_upload");
+    CK(cudaMemcpyAsync(c->f[id], host, bytes, cudaMemcpyHostToDevice, st), "field_upload");
+    CK(cudaEventRecord(c->ev_upf[id], st), "field_upload");
+    c->upf_pending[id] = true;
+    return NEMO_OK;
+  }
   if (c->stage_bytes[id] != bytes) {  // the field's staging buffer, made at its first upload
     if (c->stage[id]) {
       CK(cudaStreamSynchronize(c->stream), "field_upload");

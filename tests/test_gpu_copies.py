@@ -59,12 +59,14 @@ def test_overlapped_copies_match_serialised(prec):
             assert torch.equal(x, y), f"{n} step {s}: overlapped copies differ from serialised ones"
 
 
-def test_upload_then_download_without_a_step():
-    """An upload is staged on the device and copied into the field by the next work
-    that reads it; a download before any such work still returns the uploaded
-    values, and of two uploads of a field without work between them the later one
-    wins."""
-    p = Pair(nn=1, prec="mixed", seed=3)
+@pytest.mark.parametrize("nn", [1, 3])
+def test_upload_then_download_without_a_step(nn):
+    """A field of 1 MB or more (tsb at nn_GYRE=3) is staged on the device and copied
+    into the field by the next work that reads it, a smaller one (nn_GYRE=1) goes
+    straight into place; either way a download before any such work returns the
+    uploaded values, and of two uploads of a field without work between them the
+    later one wins."""
+    p = Pair(nn=nn, prec="mixed", seed=3)
     p.bind_hotpath()
     n = p.dev["TSB"].numel()
     first = torch.arange(n, dtype=torch.float32).pin_memory()
