@@ -798,6 +798,10 @@ enum nemo_kernel_id {
 int nemo_gpu_autotune(nemo_ctx *ctx, int kt, int nrep);
 /* The block heights in use, ty[id] per nemo_kernel_id (n entries). */
 int nemo_gpu_get_launch_shape(const nemo_ctx *ctx, int *ty, int n);
+/* Set them (n entries from kernel id 0): 0 or 4 = 32 x 4; 2 or 1 only for the
+ * kernels the autotuner tunes (NEMO_ERR_ARG otherwise). The results do not depend
+ * on the shape: a test runs the step under each and requires the same bits. */
+int nemo_gpu_set_launch_shape(nemo_ctx *ctx, const int *ty, int n);
 
 /* Per-kernel device timing of nemo_gpu_stp_hotpath while timing is on (no
  * counterpart in the reference, whose timing stops at routines): a CUDA event is

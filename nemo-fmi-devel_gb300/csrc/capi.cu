@@ -3070,6 +3070,19 @@ int nemo_gpu_autotune(nemo_ctx* c, int kt, int nrep) {
   return st;
 }
 
+int nemo_gpu_set_launch_shape(nemo_ctx* c, const int* ty, int n) {
+  if (!c || n < 0 || n > NEMO_K_COUNT || (n > 0 && !ty)) return fail(c, NEMO_ERR_ARG, "set_launch_shape: bad argument");
+  bool tunable[NEMO_K_COUNT] = {};
+  for (int id : kTunable) tunable[id] = true;
+  for (int i = 0; i < n; ++i)
+    if (!(ty[i] == 0 || ty[i] == 4 || (tunable[i] && (ty[i] == 1 || ty[i] == 2))))
+      return fail(c, NEMO_ERR_ARG, "set_launch_shape: kernel %d cannot take block height %d", i, ty[i]);
+  for (int i = 0; i < n; ++i) c->shape.ty[i] = (unsigned char)(ty[i] == 4 ? 0 : ty[i]);
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);  // recaptured with the new shapes
+  c->graphs.clear();
+  return NEMO_OK;
+}
+
 int nemo_gpu_get_launch_shape(const nemo_ctx* c, int* ty, int n) {
   if (!c || n < 0 || (n > 0 && !ty)) return NEMO_ERR_ARG;
   for (int i = 0; i < n; ++i) ty[i] = i < NEMO_K_COUNT && c->shape.ty[i] ? c->shape.ty[i] : 4;

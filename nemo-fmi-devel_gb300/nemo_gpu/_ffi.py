@@ -162,6 +162,7 @@ def load(path):
     _proto(lib, "nemo_gpu_tra_ldf_blp", i, [vp, i, i, cp, vp, vp, vp, vp, vp, vp, vp, vp, i, i])
     _proto(lib, "nemo_gpu_zps_hde", i, [vp, i, i, vp, vp, vp])
     _proto(lib, "nemo_gpu_get_launch_shape", i, [vp, _ip, i])
+    _proto(lib, "nemo_gpu_set_launch_shape", i, [vp, _ip, i])
     _proto(lib, "nemo_gpu_eos_insitu", i, [vp, vp, vp, vp])
     _proto(lib, "nemo_gpu_eos_insitu_pot", i, [vp, vp, vp, vp, vp])
     _proto(lib, "nemo_gpu_rab_3d", i, [vp, vp, vp])

@@ -180,6 +180,14 @@ class Context:
         names = {v: k.lower() for k, v in _ffi.K.items() if k != "COUNT"}
         return {names[i]: ty[i] for i in range(nk)}
 
+    def set_launch_shape(self, shape):
+        """{kernel name: block height (4, 2 or 1)}; kernels not named keep 32 x 4."""
+        nk = _ffi.K["COUNT"]
+        ty = (C.c_int * nk)()
+        for name, h in shape.items():
+            ty[_ffi.K[name.upper()]] = int(h)
+        self._ck(self.lib.nemo_gpu_set_launch_shape(self.h, ty, nk), "set_launch_shape")
+
     def set_timing(self, on):
         self._ck(self.lib.nemo_gpu_set_timing(self.h, int(on)), "set_timing")
 
