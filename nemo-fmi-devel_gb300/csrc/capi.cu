@@ -15,6 +15,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/nemo_gpu.h"
 #include "adj.h"
 #include "step.h"
@@ -2123,9 +2125,18 @@ int nemo_gpu_tra_adv_trp(nemo_ctx* c, const void* un, const void* vn, const void
   return NEMO_OK;
 }
 
+// An NVTX range named after the reference routine for the duration of a call, the
+// counterpart of timing_start / timing_stop (timing.F90:89-212); free when no tool
+// is attached (header-only NVTX v3).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
+
 int nemo_gpu_tra_adv_fct(nemo_ctx* c, int kt, int kit000, const char* cdtype, double p2dt, const void* pun,
                          const void* pvn, const void* pwn, const void* ptb, const void* ptn, void* pta, int kjpt,
                          int kn_fct_h, int kn_fct_v) {
+  NvtxRange nvtx_range("tra_adv_fct");
   (void)kt; (void)kit000;
   if (!c) return NEMO_ERR_ARG;
   if (join_copies(c)) return NEMO_ERR_CUDA;
@@ -2145,6 +2156,7 @@ int nemo_gpu_tra_adv_fct(nemo_ctx* c, int kt, int kit000, const char* cdtype, do
 int nemo_gpu_tra_ldf_lap(nemo_ctx* c, int kt, int kit000, const char* cdtype, const void* pahu, const void* pahv,
                          const void* pgu, const void* pgv, const void* pgui, const void* pgvi, const void* ptb,
                          void* pta, int kjpt, int kpass) {
+  NvtxRange nvtx_range("tra_ldf_lap");
   (void)kt; (void)kit000; (void)pgui; (void)pgvi;
   if (!c) return NEMO_ERR_ARG;
   if (join_copies(c)) return NEMO_ERR_CUDA;
@@ -2159,6 +2171,7 @@ int nemo_gpu_tra_ldf_lap(nemo_ctx* c, int kt, int kit000, const char* cdtype, co
 int nemo_gpu_tra_ldf_iso(nemo_ctx* c, int kt, int kit000, const char* cdtype, const void* pahu, const void* pahv,
                          const void* pgu, const void* pgv, const void* pgui, const void* pgvi, const void* ptb,
                          const void* ptbb, void* pta, int kjpt, int kpass) {
+  NvtxRange nvtx_range("tra_ldf_iso");
   (void)pgui; (void)pgvi;
   if (!c) return NEMO_ERR_ARG;
   if (join_copies(c)) return NEMO_ERR_CUDA;
@@ -2198,6 +2211,7 @@ int nemo_gpu_ldf_slp_triad(nemo_ctx* c, int kt, const void* prab_b) {
 int nemo_gpu_tra_ldf_triad(nemo_ctx* c, int kt, int kit000, const char* cdtype, const void* pahu, const void* pahv,
                            const void* pgu, const void* pgv, const void* pgui, const void* pgvi, const void* ptb,
                            const void* ptbb, void* pta, int kjpt, int kpass) {
+  NvtxRange nvtx_range("tra_ldf_triad");
   (void)pgu; (void)pgv; (void)pgui; (void)pgvi;
   if (!c) return NEMO_ERR_ARG;
   if (join_copies(c)) return NEMO_ERR_CUDA;
@@ -2215,6 +2229,7 @@ int nemo_gpu_tra_ldf_triad(nemo_ctx* c, int kt, int kit000, const char* cdtype, 
 int nemo_gpu_tra_ldf_blp(nemo_ctx* c, int kt, int kit000, const char* cdtype, const void* pahu, const void* pahv,
                          const void* pgu, const void* pgv, const void* pgui, const void* pgvi, const void* ptb,
                          void* pta, int kjpt, int kldf) {
+  NvtxRange nvtx_range("tra_ldf_blp");
   (void)pgui; (void)pgvi;
   if (!c) return NEMO_ERR_ARG;
   if (join_copies(c)) return NEMO_ERR_CUDA;
@@ -2270,6 +2285,7 @@ int nemo_gpu_zps_hde_rd(nemo_ctx* c, int kt, const void* pts, const void* prd, v
 
 int nemo_gpu_tra_zdf_imp(nemo_ctx* c, int kt, int kit000, const char* cdtype, double p2dt, const void* ptb, void* pta,
                          int kjpt) {
+  NvtxRange nvtx_range("tra_zdf_imp");
   (void)kt; (void)kit000;
   if (!c) return NEMO_ERR_ARG;
   if (join_copies(c)) return NEMO_ERR_CUDA;
@@ -2319,6 +2335,7 @@ int nemo_gpu_tra_nxt(nemo_ctx* c, int kt) {
 }
 
 int nemo_gpu_ldf_slp(nemo_ctx* c, int kt, const void* prd, const void* pn2) {
+  NvtxRange nvtx_range("ldf_slp");
   (void)kt;
   if (!c) return NEMO_ERR_ARG;
   if (!prd || !pn2) return fail(c, NEMO_ERR_ARG, "ldf_slp: null prd or pn2");
@@ -2903,6 +2920,7 @@ int nemo_gpu_tra_nxt_adj(nemo_ctx* c, int kt, void* tsb_ad, void* tsn_ad, void* 
 }
 
 int nemo_gpu_dyn_spg_ts(nemo_ctx* c, int kt) {
+  NvtxRange nvtx_range("dyn_spg_ts");
   if (!c) return NEMO_ERR_ARG;
   if (join_copies(c)) return NEMO_ERR_CUDA;
   return c->prec == NEMO_PREC_FP64 ? run_spg<double>(c, kt) : run_spg<float>(c, kt);
@@ -2910,6 +2928,7 @@ int nemo_gpu_dyn_spg_ts(nemo_ctx* c, int kt) {
 
 int nemo_gpu_lbc_lnk(nemo_ctx* c, const char* cdname, void* ptab, int nk, int nl, const char* cd_nat, double psgn,
                      double pval, int is_fp64) {
+  NvtxRange nvtx_range("lbc_lnk");
   (void)cdname; (void)psgn;
   if (!c || !ptab || nk < 1 || nl < 1 || !cd_nat) return fail(c, NEMO_ERR_ARG, "lbc_lnk: bad argument");
   if (join_copies(c)) return NEMO_ERR_CUDA;
@@ -2935,6 +2954,7 @@ int nemo_gpu_lbc_lnk_multi(nemo_ctx* c, const char* cdname, int kfld, void* cons
 }
 
 int nemo_gpu_glob_sum(nemo_ctx* c, const char* cdname, const void* ptab, int nk, int is_fp64, double* out) {
+  NvtxRange nvtx_range("glob_sum");
   (void)cdname;
   if (!c || !ptab || nk < 1 || !out) return fail(c, NEMO_ERR_ARG, "glob_sum: bad argument");
   if (join_copies(c)) return NEMO_ERR_CUDA;
@@ -2951,6 +2971,7 @@ int nemo_gpu_glob_sum(nemo_ctx* c, const char* cdname, const void* ptab, int nk,
 
 static int stp_common(nemo_ctx* c, int kt, bool model) {
   if (!c) return NEMO_ERR_ARG;
+  NvtxRange nvtx_range(model ? "stp" : "stp_hotpath");
   if (model)
     if (int s = model_fields(c, "stp_model")) return s;
   // host copies in flight: direct launches that wait per field (see run_hotpath);
