@@ -329,20 +329,21 @@ __global__ void k_spg_p1b(Dom<T> d, SpgArgs<T> a) {
 // loaded whole into registers and summed in the reference's order, so all loads are
 // in flight together.
 template <int NK>
-__global__ void __launch_bounds__(128) k_spg_p1a_reg(Dom<float> d, SpgArgs<float> a) {
+__global__ void __launch_bounds__(128, 8) k_spg_p1a_reg(Dom<float> d, SpgArgs<float> a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int m = blockIdx.z;
   if (i > d.jpi || j > d.jpj) return;
   const long ij = pt_ij(d, i, j), n2 = d.n2, m2 = (long)m * n2;
   const ColInfo ci = d.ci[ij];
-  float* ua = a.ua + (long)m * d.n3 + ij;
-  float* va = a.va + (long)m * d.n3 + ij;
+  // read-only loads (this kernel writes neither ua nor va)
+  const float* ua = a.ua + (long)m * d.n3 + ij;
+  const float* va = a.va + (long)m * d.n3 + ij;
   float u[NK - 1], v[NK - 1];
 #pragma unroll
   for (int k = 1; k <= NK - 1; ++k) {
-    u[k - 1] = ua[(k - 1) * n2];
-    v[k - 1] = va[(k - 1) * n2];
+    u[k - 1] = __ldg(ua + (k - 1) * n2);
+    v[k - 1] = __ldg(va + (k - 1) * n2);
   }
   float su = 0.f, sv = 0.f;
 #pragma unroll
@@ -1171,10 +1172,25 @@ __global__ void __launch_bounds__(128) k_spg_p3(Dom<T> d, SpgArgs<T> a) {
   const bool interior = i >= 2 && i <= d.jpi - 1 && j >= 2 && j <= d.jpj - 1;
   const T zm_u = interior ? a.zmu[m2 + p] : T(0), zm_v = interior ? a.zmv[m2 + p] : T(0);
   const long base = (long)m * d.n3 + p;
-  for (int k = k0; k <= k1; ++k) {
+  // all levels of the chunk loaded before the first store (the stores may alias the
+  // loads for the compiler, which would otherwise keep one level in flight)
+  T lua[KCH3], lva[KCH3], lun[KCH3], lvn[KCH3];
+#pragma unroll
+  for (int kk = 0; kk < KCH3; ++kk) {
+    if (k0 + kk > k1) break;
+    const long q = base + (long)(k0 + kk - 1) * d.n2;
+    lua[kk] = a.ua[q];
+    lva[kk] = a.va[q];
+    lun[kk] = a.un[q];
+    lvn[kk] = a.vn[q];
+  }
+#pragma unroll
+  for (int kk = 0; kk < KCH3; ++kk) {
+    const int k = k0 + kk;
+    if (k > k1) break;
     const long q = base + (long)(k - 1) * d.n2;
-    T ua = a.ua[q], va = a.va[q];
-    const T un = a.un[q], vn = a.vn[q];
+    T ua = lua[kk], va = lva[kk];
+    const T un = lun[kk], vn = lvn[kk];
     if (interior) {
       ua = ua - zm_u * umsk<T>(ci, k);
       va = va - zm_v * vmsk<T>(ci, k);
